@@ -1,0 +1,106 @@
+/*
+ * sl3dgpu — the C ABI of the GB300-native 3D viscoelastic hot path of sl3dpp.
+ *
+ * Plain C: opaque handles, pointers and sizes, int status codes, a CUDA stream
+ * passed as void*. Every entry point names the reference interface it replaces
+ * (file:line within the sl3dpp source tree). Status codes: SL3DGPU_OK (0);
+ * a positive LAPACK-style info for a failed factorisation; negative codes for
+ * errors, whose text sl3dgpu_last_error() returns (per thread).
+ *
+ * Layouts. "Reference layout" is the reference's own: band storage as
+ * LAPACK's (include/sl3dpp/detail/BandSolvers.hpp:24-49), right-hand sides
+ * column-major; spin-N coefficients at l^2 - N^2 + (m + l), real spin-0 ones
+ * at l(l+1)/2 + m (include/sl3dpp/SurfaceGrid.hpp:110-118, 191-200); grid
+ * values colatitude-major. Batched device calls keep right-hand sides
+ * row-major (dof-major, columns fastest), the layout the kernels coalesce on.
+ */
+#ifndef SL3DGPU_H
+#define SL3DGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  SL3DGPU_OK = 0,
+  SL3DGPU_ERR_ARGUMENT = -1,   /* std::invalid_argument in the reference */
+  SL3DGPU_ERR_CUDA = -2,       /* a CUDA call failed */
+  SL3DGPU_ERR_RUNTIME = -3,    /* std::runtime_error in the reference */
+  SL3DGPU_ERR_UNCONVERGED = -4, /* an iteration ended without converging */
+  SL3DGPU_ERR_WAIT = -5        /* a device-side wait ran out of its budget */
+};
+
+/* The last error's text on this thread. */
+const char* sl3dgpu_last_error(void);
+/* Library version string. */
+const char* sl3dgpu_version(void);
+
+/* ---- band solvers (include/sl3dpp/detail/BandSolvers.hpp:24-49) -----------
+ * Host-pointer drop-ins of detail::BandCholeskyFactor / BandCholeskySolve /
+ * BandLuFactor / BandLuSolve (src/BandSolvers.cpp:23-139): the same storage,
+ * pivots (zero-based) and info returns, computed on the GPU. */
+int sl3dgpu_band_cholesky_factor(double* ab, int n, int kd);
+int sl3dgpu_band_cholesky_solve(const double* ab, int n, int kd, double* b, int nrhs);
+int sl3dgpu_band_lu_factor(double* ab, int n, int kl, int ku, int* pivots);
+int sl3dgpu_band_lu_solve(const double* ab, int n, int kl, int ku, const int* pivots,
+                          double* b, int nrhs);
+
+/* One system of a device batch: every degree's system solved in one launch
+ * (DegreeOperator::BeginSolve/FinishSolve, src/DegreeOperator.cpp:861-901;
+ * ToroidalOperator::BeginSolve/FinishSolve, src/ToroidalOperator.cpp). */
+typedef struct sl3dgpu_band_system {
+  int n;            /* order */
+  int kl, ku;       /* sub- and superdiagonals; Cholesky reads ku as kd */
+  int nrhs;         /* right-hand sides of a solve */
+  long long band;   /* offset (doubles) of the band in the batch's band array */
+  long long pivots; /* offset (ints) of the LU pivots */
+  long long rhs;    /* offset (doubles) of the n x nrhs right-hand sides, row-major */
+  long long scale;  /* offset (doubles) of the symmetric diagonal scaling, -1 none */
+  int pinned0, pinned1; /* dofs pinned to zero (identity rows), -1 none */
+} sl3dgpu_band_system;
+
+/* Factorise a batch in place (device pointers), Cholesky (lu = 0) or LU with
+ * partial pivoting (lu = 1); info[i] receives system i's LAPACK-style info. */
+int sl3dgpu_band_factor_batch(const sl3dgpu_band_system* dev_systems,
+                              const sl3dgpu_band_system* host_systems, int count,
+                              double* bands, int* pivots, int* info, int lu, void* stream);
+/* The work items of a batch solve: (system, first column) pairs, one per 32
+ * right-hand sides; returns their count (items may be NULL to ask). */
+int sl3dgpu_band_work_items(const sl3dgpu_band_system* host_systems, int count, int* items,
+                            int capacity);
+/* Solve a factorised batch in place on row-major right-hand sides. */
+int sl3dgpu_band_solve_batch(const sl3dgpu_band_system* dev_systems,
+                             const sl3dgpu_band_system* host_systems, int count,
+                             const int* dev_items, int item_count, const double* bands,
+                             const int* pivots, double* rhs, const double* scales, int lu,
+                             void* stream);
+
+/* ---- the surface grid (include/sl3dpp/SurfaceGrid.hpp:58-287) ---------------
+ * A Gauss-Legendre grid for degrees to lmax and spins to nmax, oversampled
+ * by `oversampling` (band L' = ceil(oversampling lmax): L' + 1 colatitudes,
+ * the smallest 2^a 3^b 5^c >= 2 L' + 1 longitudes from zero). */
+typedef struct sl3dgpu_grid sl3dgpu_grid;
+int sl3dgpu_grid_create(int lmax, int nmax, double oversampling, sl3dgpu_grid** out);
+void sl3dgpu_grid_destroy(sl3dgpu_grid* grid);
+int sl3dgpu_grid_shape(const sl3dgpu_grid* grid, int* ntheta, int* nphi);
+/* Host copies of the colatitudes and their Gauss-Legendre weights. */
+int sl3dgpu_grid_colatitudes(const sl3dgpu_grid* grid, double* theta, double* weights);
+/* SurfaceGrid::SynthesiseSpinBatch / ExpandSpinBatch (SurfaceGrid.hpp:217-253):
+ * `count` spin-N fields end to end, device pointers, complex values as
+ * (re, im) pairs, reference layouts. */
+int sl3dgpu_synthesise_spin_batch(sl3dgpu_grid* grid, int N, const double* coeffs, int count,
+                                  double* fields, void* stream);
+int sl3dgpu_expand_spin_batch(sl3dgpu_grid* grid, int N, const double* fields, int count,
+                              double* coeffs, void* stream);
+/* SurfaceGrid::SynthesiseBatch / ExpandBatch (SurfaceGrid.hpp:164-185): real
+ * spin-0 fields from and to m >= 0 coefficients. */
+int sl3dgpu_synthesise_batch(sl3dgpu_grid* grid, const double* coeffs, int count,
+                             double* fields, void* stream);
+int sl3dgpu_expand_batch(sl3dgpu_grid* grid, const double* fields, int count, double* coeffs,
+                         void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SL3DGPU_H */

@@ -1,0 +1,38 @@
+// Shared helpers of the sl3dgpu CUDA library: status codes, the thread-local
+// error text behind sl3dgpu_last_error(), and checked CUDA calls.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <string>
+
+#include "../../include/sl3dgpu.h"
+
+namespace sl3dgpu {
+
+void SetError(const std::string& text);
+
+#define SL3D_CUDA(call)                                                        \
+  do {                                                                         \
+    const cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess) {                                                   \
+      ::sl3dgpu::SetError(std::string(#call) + ": " + cudaGetErrorString(_e)); \
+      return SL3DGPU_ERR_CUDA;                                                 \
+    }                                                                          \
+  } while (0)
+
+#define SL3D_CHECK_LAUNCH()                                                          \
+  do {                                                                               \
+    const cudaError_t _e = cudaGetLastError();                                       \
+    if (_e != cudaSuccess) {                                                         \
+      ::sl3dgpu::SetError(std::string("kernel launch: ") + cudaGetErrorString(_e)); \
+      return SL3DGPU_ERR_CUDA;                                                       \
+    }                                                                                \
+  } while (0)
+
+inline cudaStream_t AsStream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+constexpr int kWarp = 32;
+
+}  // namespace sl3dgpu

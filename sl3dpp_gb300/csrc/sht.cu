@@ -1,0 +1,733 @@
+// Spin-weighted spherical-harmonic transforms on the device (the GSHTrans
+// transforms behind SurfaceGrid's batched calls, include/sl3dpp/SurfaceGrid.hpp:164-253).
+//
+// A transform factors into the Legendre contraction over degrees at every
+// (order, colatitude) and a longitude FFT per colatitude ring:
+//  - synthesis: H_m(theta_j) = sum_l Lambda^N_lm(theta_j) c_lm, then
+//    f(theta_j, phi_k) = sum_m H_m(theta_j) e^{i m phi_k};
+//  - analysis: G_m(theta_j) = (2 pi / nphi) w_j sum_k f e^{-i m phi_k}, then
+//    c_lm = sum_j Lambda^N_lm(theta_j) G_m(theta_j).
+// The contraction is one dense matrix product per (spin, order) with the
+// batch's fields as columns, run here as a batched FP64 register-tiled GEMM;
+// the FFT is a mixed-radix (2, 3, 4, 5) Stockham transform in shared memory,
+// several rings per CTA.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "sht.cuh"
+
+namespace sl3dgpu {
+
+int FftFriendly(int n) {
+  for (int m = std::max(n, 1);; ++m) {
+    int r = m;
+    for (int p : {2, 3, 5})
+      while (r % p == 0) r /= p;
+    if (r == 1) return m;
+  }
+}
+
+namespace {
+
+// -- Wigner table --------------------------------------------------------------------
+
+// The closed form at l0 = max(|m|, |N|) for N <= 0 (see the host oracle's
+// restatement of the same algorithm): a product recursion in |m|.
+__device__ double WignerStart(int N, int m, double c, double s) {
+  const int M = abs(m), A = -N;
+  if (M >= A) {
+    double v = 1.0;
+    for (int k = 0; k < 2 * A; ++k) v *= (m >= 0 ? s : c);
+    for (int k = A; k < M; ++k)
+      v *= sqrt((2.0 * k + 2.0) * (2.0 * k + 1.0) / ((k + 1.0 + N) * (k + 1.0 - N))) * c * s;
+    if (m >= 0 && ((M - N) % 2 != 0)) v = -v;
+    return v;
+  }
+  const int l = A;
+  const double fact[5] = {1.0, 1.0, 2.0, 6.0, 24.0};
+  double v = sqrt(fact[2 * l] / (fact[l + m] * fact[l - m]));
+  for (int k = 0; k < l - m; ++k) v *= c;
+  for (int k = 0; k < l + m; ++k) v *= s;
+  if ((l + m) % 2 != 0) v = -v;
+  return v;
+}
+
+// One thread per (order, colatitude): the three-term recurrence in l.
+__global__ void WignerTableKernel(int lmax, int N, int ntheta, const double* theta,
+                                  const int* rowOffset, double* table) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = static_cast<int>(blockIdx.y) - lmax;
+  if (j >= ntheta) return;
+  const double pi = 3.14159265358979323846;
+  const int l0 = max(abs(m), abs(N));
+  if (l0 > lmax) return;
+  const bool mirrored = N > 0;
+  const int Nr = mirrored ? -N : N;
+  const double t = mirrored ? pi - theta[j] : theta[j];
+  const double c = cos(0.5 * t), s = sin(0.5 * t);
+  double* out = table + static_cast<long long>(rowOffset[m + lmax]) * ntheta + j;
+  double dprev = 0.0, d = WignerStart(Nr, m, c, s);
+  const double ct = cos(t);
+  for (int l = l0; l <= lmax; ++l) {
+    const double sign = mirrored && ((l + m) % 2 != 0) ? -1.0 : 1.0;
+    out[static_cast<long long>(l - l0) * ntheta] = sign * sqrt((2.0 * l + 1.0) / (4.0 * pi)) * d;
+    if (l == lmax) break;
+    double next;
+    if (l == 0) {
+      next = ct;
+    } else {
+      const double a = (l + 1.0) * (2.0 * l + 1.0) /
+                       sqrt(((l + 1.0) * (l + 1.0) - 1.0 * m * m) * ((l + 1.0) * (l + 1.0) - 1.0 * Nr * Nr));
+      const double b = 1.0 * m * Nr / (l * (l + 1.0));
+      const double e = sqrt((1.0 * l * l - 1.0 * m * m) * (1.0 * l * l - 1.0 * Nr * Nr)) / (l * (2.0 * l + 1.0));
+      next = a * ((ct - b) * d - e * dprev);
+    }
+    dprev = d;
+    d = next;
+  }
+}
+
+// -- batched FP64 GEMM: C(i, n) = sum_k A(i, k) B(k, n) --------------------------------
+
+constexpr int kBM = 64, kBN = 64, kBK = 16;
+
+__global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, const double* A,
+                                                     const double* B, double* C) {
+  const GemmItem it = items[blockIdx.z];
+  const int i0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+  if (i0 >= it.M || n0 >= it.N) return;
+  __shared__ double As[kBK][kBM + 1];
+  __shared__ double Bs[kBK][kBN];
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  const double* a = A + it.a;
+  const double* b = B + it.b;
+  double acc[4][4] = {};
+  for (int k0 = 0; k0 < it.K; k0 += kBK) {
+    if (it.sAk == 1) {
+      for (int e = tid; e < kBM * kBK; e += 256) {
+        const int kk = e % kBK, ii = e / kBK;
+        const int i = i0 + ii, k = k0 + kk;
+        As[kk][ii] = (i < it.M && k < it.K) ? a[static_cast<long long>(i) * it.sAi + k] : 0.0;
+      }
+    } else {
+      for (int e = tid; e < kBM * kBK; e += 256) {
+        const int ii = e % kBM, kk = e / kBM;
+        const int i = i0 + ii, k = k0 + kk;
+        As[kk][ii] = (i < it.M && k < it.K)
+                         ? a[static_cast<long long>(i) * it.sAi + static_cast<long long>(k) * it.sAk]
+                         : 0.0;
+      }
+    }
+    for (int e = tid; e < kBK * kBN; e += 256) {
+      const int nn = e % kBN, kk = e / kBN;
+      const int n = n0 + nn, k = k0 + kk;
+      Bs[kk][nn] = (n < it.N && k < it.K) ? b[static_cast<long long>(k) * it.ldb + n] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kBK; ++kk) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) av[r] = As[kk][ty + 16 * r];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) bv[q] = Bs[kk][tx + 16 * q];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] = fma(av[r], bv[q], acc[r][q]);
+    }
+    __syncthreads();
+  }
+  double* c = C + it.c;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int i = i0 + ty + 16 * r;
+    if (i >= it.M) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int n = n0 + tx + 16 * q;
+      if (n < it.N) c[static_cast<long long>(i) * it.ldc + n] = acc[r][q];
+    }
+  }
+}
+
+// -- FFT ---------------------------------------------------------------------------------
+
+__device__ inline double2 Mul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ inline double2 Add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ inline double2 Sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+// e^{sign 2 pi i e / n} from the table of e^{2 pi i x / n}.
+__device__ inline double2 Twiddle(const double2* tw, int e, int n, int sign) {
+  double2 w = tw[e % n];
+  if (sign < 0) w.y = -w.y;
+  return w;
+}
+
+// Stockham autosort over `groups` transforms of length n held at
+// buf0 + g * n (ping-pong with buf1 + g * n); `sign` +1 synthesis, -1
+// analysis. Returns 0 when the result is in buf0, 1 in buf1.
+__device__ int StockhamFft(double2* buf0, double2* buf1, int groups, const FftPlan& plan,
+                           const double2* tw, int sign) {
+  const int n = plan.n;
+  double2* src = buf0;
+  double2* dst = buf1;
+  int Ns = 1;
+  for (int s = 0; s < plan.stages; ++s) {
+    const int r = plan.radix[s];
+    const int m = n / r;
+    const int stride = n / (Ns * r);
+    for (int t = threadIdx.x; t < groups * m; t += blockDim.x) {
+      const int g = t / m, idx = t % m;
+      const double2* in = src + g * n;
+      double2* out = dst + g * n;
+      const int k = idx % Ns;
+      double2 v[5];
+      for (int q = 0; q < r; ++q) {
+        v[q] = in[idx + q * m];
+        if (q > 0 && k > 0) v[q] = Mul(v[q], Twiddle(tw, q * k * stride, n, sign));
+      }
+      const int base = (idx / Ns) * Ns * r + k;
+      if (r == 2) {
+        out[base] = Add(v[0], v[1]);
+        out[base + Ns] = Sub(v[0], v[1]);
+      } else if (r == 4) {
+        const double2 a0 = Add(v[0], v[2]), a1 = Sub(v[0], v[2]);
+        const double2 b0 = Add(v[1], v[3]), b1 = Sub(v[1], v[3]);
+        // i^sign * b1
+        const double2 ib1 = sign > 0 ? make_double2(-b1.y, b1.x) : make_double2(b1.y, -b1.x);
+        out[base] = Add(a0, b0);
+        out[base + Ns] = Add(a1, ib1);
+        out[base + 2 * Ns] = Sub(a0, b0);
+        out[base + 3 * Ns] = Sub(a1, ib1);
+      } else {
+        for (int u = 0; u < r; ++u) {
+          double2 y = v[0];
+          for (int q = 1; q < r; ++q) y = Add(y, Mul(v[q], Twiddle(tw, ((q * u) % r) * (n / r), n, sign)));
+          out[base + u * Ns] = y;
+        }
+      }
+    }
+    __syncthreads();
+    double2* swap = src;
+    src = dst;
+    dst = swap;
+    Ns *= r;
+  }
+  return src == buf0 ? 0 : 1;
+}
+
+constexpr int kRingGroup = 4;  // rings (fields at one colatitude) per CTA
+
+// Spectra [mIndex][j][count] -> fields [count][j][k]: rings (p0..p0+G, j).
+__global__ void RingSynthesisKernel(int lmax, int ntheta, int count, bool real, FftPlan plan,
+                                    const double2* tw, const double2* spectra, void* fields) {
+  extern __shared__ double2 smem[];
+  const int n = plan.n;
+  double2* buf0 = smem;
+  double2* buf1 = smem + kRingGroup * n;
+  const int j = blockIdx.y;
+  const int p0 = blockIdx.x * kRingGroup;
+  const int groups = min(kRingGroup, count - p0);
+  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) buf0[e] = make_double2(0.0, 0.0);
+  __syncthreads();
+  const int mcount = real ? lmax + 1 : 2 * lmax + 1;
+  for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
+    const int g = e % groups, mi = e / groups;
+    const int m = real ? mi : mi - lmax;
+    double2 v = spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
+    if (real) {
+      if (m == 0) {
+        buf0[g * n] = make_double2(v.x, 0.0);
+      } else {
+        buf0[g * n + m] = v;
+        buf0[g * n + n - m] = make_double2(v.x, -v.y);
+      }
+    } else {
+      buf0[g * n + ((m % n) + n) % n] = v;
+    }
+  }
+  __syncthreads();
+  const int where = StockhamFft(buf0, buf1, groups, plan, tw, +1);
+  const double2* res = where == 0 ? buf0 : buf1;
+  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
+    const int g = e / n, k = e % n;
+    const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
+    if (real)
+      static_cast<double*>(fields)[at] = res[e].x;
+    else
+      static_cast<double2*>(fields)[at] = res[e];
+  }
+}
+
+// Fields [count][j][k] -> spectra [mIndex][j][count], scaled by (2 pi / n) w_j.
+__global__ void RingAnalysisKernel(int lmax, int ntheta, int count, bool real, FftPlan plan,
+                                   const double2* tw, const double* weights, const void* fields,
+                                   double2* spectra) {
+  extern __shared__ double2 smem[];
+  const int n = plan.n;
+  double2* buf0 = smem;
+  double2* buf1 = smem + kRingGroup * n;
+  const int j = blockIdx.y;
+  const int p0 = blockIdx.x * kRingGroup;
+  const int groups = min(kRingGroup, count - p0);
+  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
+    const int g = e / n, k = e % n;
+    const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
+    buf0[e] = real ? make_double2(static_cast<const double*>(fields)[at], 0.0)
+                   : static_cast<const double2*>(fields)[at];
+  }
+  __syncthreads();
+  const int where = StockhamFft(buf0, buf1, groups, plan, tw, -1);
+  const double2* res = where == 0 ? buf0 : buf1;
+  const double scale = 2.0 * 3.14159265358979323846 / n * weights[j];
+  const int mcount = real ? lmax + 1 : 2 * lmax + 1;
+  for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
+    const int g = e % groups, mi = e / groups;
+    const int m = real ? mi : mi - lmax;
+    const double2 v = res[g * n + ((m % n) + n) % n];
+    spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] =
+        make_double2(v.x * scale, v.y * scale);
+  }
+}
+
+// -- layout permutations -------------------------------------------------------------------
+
+__global__ void ToDeviceKernel(int lmax, int N, bool real, int count, const int* rowOffset,
+                               const double2* ref, double2* dev) {
+  const long long rows = real ? static_cast<long long>(lmax + 1) * (lmax + 2) / 2
+                              : static_cast<long long>(lmax + 1) * (lmax + 1) - N * N;
+  const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (t >= rows * count) return;
+  const int p = static_cast<int>(t / rows);
+  const long long i = t % rows;
+  int l, m;
+  if (real) {
+    l = static_cast<int>((sqrt(8.0 * i + 1.0) - 1.0) * 0.5);
+    while (static_cast<long long>(l) * (l + 1) / 2 > i) --l;
+    while (static_cast<long long>(l + 1) * (l + 2) / 2 <= i) ++l;
+    m = static_cast<int>(i - static_cast<long long>(l) * (l + 1) / 2);
+  } else {
+    const long long q = i + N * N;
+    l = static_cast<int>(sqrt(static_cast<double>(q)));
+    while (static_cast<long long>(l) * l > q) --l;
+    while (static_cast<long long>(l + 1) * (l + 1) <= q) ++l;
+    m = static_cast<int>(q - static_cast<long long>(l) * l) - l;
+  }
+  const int l0 = max(abs(m), abs(N));
+  const long long row = rowOffset[m + lmax] - (real ? rowOffset[lmax] : 0) + (l - l0);
+  dev[row * count + p] = ref[t];
+}
+
+__global__ void FromDeviceKernel(int lmax, int N, bool real, int count, const int* rowOffset,
+                                 const double2* dev, double2* ref) {
+  const long long rows = real ? static_cast<long long>(lmax + 1) * (lmax + 2) / 2
+                              : static_cast<long long>(lmax + 1) * (lmax + 1) - N * N;
+  const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (t >= rows * count) return;
+  const int p = static_cast<int>(t / rows);
+  const long long i = t % rows;
+  int l, m;
+  if (real) {
+    l = static_cast<int>((sqrt(8.0 * i + 1.0) - 1.0) * 0.5);
+    while (static_cast<long long>(l) * (l + 1) / 2 > i) --l;
+    while (static_cast<long long>(l + 1) * (l + 2) / 2 <= i) ++l;
+    m = static_cast<int>(i - static_cast<long long>(l) * (l + 1) / 2);
+  } else {
+    const long long q = i + N * N;
+    l = static_cast<int>(sqrt(static_cast<double>(q)));
+    while (static_cast<long long>(l) * l > q) --l;
+    while (static_cast<long long>(l + 1) * (l + 1) <= q) ++l;
+    m = static_cast<int>(q - static_cast<long long>(l) * l) - l;
+  }
+  const int l0 = max(abs(m), abs(N));
+  const long long row = rowOffset[m + lmax] - (real ? rowOffset[lmax] : 0) + (l - l0);
+  ref[t] = dev[row * count + p];
+}
+
+void GaussLegendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  const double pi = 3.14159265358979323846;
+  x.resize(n);
+  w.resize(n);
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(pi * (i + 0.75) / (n + 0.5));
+    auto legendre = [n](double zz, double& p1, double& p0) {
+      p0 = 1.0;
+      p1 = zz;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * zz * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (n == 1) {
+        p1 = zz;
+        p0 = 1.0;
+      }
+    };
+    double p1, p0, dp;
+    for (int it = 0; it < 100; ++it) {
+      legendre(z, p1, p0);
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::abs(dz) < 1e-16) break;
+    }
+    legendre(z, p1, p0);
+    dp = n * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = z;
+    w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+}  // namespace
+
+int Grid::Create(int lmax, int nmax, double oversampling, std::unique_ptr<Grid>& out) {
+  if (lmax < 0 || nmax < 0 || nmax > lmax + 1 || !(oversampling >= 1.0)) {
+    SetError("grid: lmax >= 0, 0 <= nmax, oversampling >= 1");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto g = std::make_unique<Grid>();
+  g->lmax = lmax;
+  g->nmax = nmax;
+  g->band = static_cast<int>(std::ceil(oversampling * lmax - 1e-12));
+  g->ntheta = g->band + 1;
+  g->nphi = FftFriendly(2 * g->band + 1);
+  std::vector<double> x;
+  GaussLegendre(g->ntheta, x, g->weights);
+  g->theta.resize(g->ntheta);
+  for (int j = 0; j < g->ntheta; ++j) g->theta[j] = std::acos(x[j]);
+  // FFT plan: fours first, then twos, threes and fives.
+  int r = g->nphi;
+  auto& plan = g->plan;
+  plan.n = g->nphi;
+  while (r % 4 == 0) {
+    plan.radix[plan.stages++] = 4;
+    r /= 4;
+  }
+  for (int p : {2, 3, 5})
+    while (r % p == 0) {
+      plan.radix[plan.stages++] = p;
+      r /= p;
+    }
+  std::vector<double2> tw(g->nphi);
+  for (int k = 0; k < g->nphi; ++k) {
+    const double a = 2.0 * 3.14159265358979323846 * k / g->nphi;
+    tw[k] = make_double2(std::cos(a), std::sin(a));
+  }
+  SL3D_CUDA(cudaMalloc(&g->dTheta, g->ntheta * sizeof(double)));
+  SL3D_CUDA(cudaMalloc(&g->dWeights, g->ntheta * sizeof(double)));
+  SL3D_CUDA(cudaMalloc(&g->dTwiddle, g->nphi * sizeof(double2)));
+  SL3D_CUDA(cudaMemcpy(g->dTheta, g->theta.data(), g->ntheta * sizeof(double), cudaMemcpyHostToDevice));
+  SL3D_CUDA(cudaMemcpy(g->dWeights, g->weights.data(), g->ntheta * sizeof(double), cudaMemcpyHostToDevice));
+  SL3D_CUDA(cudaMemcpy(g->dTwiddle, tw.data(), g->nphi * sizeof(double2), cudaMemcpyHostToDevice));
+  out = std::move(g);
+  return SL3DGPU_OK;
+}
+
+Grid::~Grid() {
+  cudaFree(dTheta);
+  cudaFree(dWeights);
+  cudaFree(dTwiddle);
+  cudaFree(dItems_);
+  cudaFree(scratchSpectra_);
+  cudaFree(scratchCoeffs_);
+  for (auto& [N, t] : tables_) {
+    cudaFree(t.values);
+    cudaFree(t.dRowOffset);
+  }
+}
+
+int Grid::Table(int N, const SpinTable** out) {
+  if (std::abs(N) > nmax) {
+    SetError("grid: spin " + std::to_string(N) + " beyond the grid's nmax " + std::to_string(nmax));
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto found = tables_.find(N);
+  if (found == tables_.end()) {
+    SpinTable t;
+    t.N = N;
+    t.rowOffset.assign(2 * lmax + 2, 0);
+    for (int m = -lmax; m <= lmax; ++m) {
+      const int l0 = std::max(std::abs(m), std::abs(N));
+      t.rowOffset[m + lmax + 1] = t.rowOffset[m + lmax] + std::max(0, lmax - l0 + 1);
+    }
+    const size_t size = static_cast<size_t>(t.rowOffset.back()) * ntheta;
+    SL3D_CUDA(cudaMalloc(&t.values, std::max<size_t>(size, 1) * sizeof(double)));
+    SL3D_CUDA(cudaMalloc(&t.dRowOffset, t.rowOffset.size() * sizeof(int)));
+    SL3D_CUDA(cudaMemcpy(t.dRowOffset, t.rowOffset.data(), t.rowOffset.size() * sizeof(int),
+                         cudaMemcpyHostToDevice));
+    dim3 grid((ntheta + 127) / 128, 2 * lmax + 1);
+    WignerTableKernel<<<grid, 128>>>(lmax, N, ntheta, dTheta, t.dRowOffset, t.values);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaDeviceSynchronize());
+    found = tables_.emplace(N, std::move(t)).first;
+  }
+  *out = &found->second;
+  return SL3DGPU_OK;
+}
+
+int Grid::RunGemm(const double* A, const double* B, double* C, cudaStream_t stream) {
+  if (items_.empty()) return SL3DGPU_OK;
+  if (items_.size() > dItemsCapacity_) {
+    cudaFree(dItems_);
+    dItems_ = nullptr;
+    dItemsCapacity_ = 0;
+    SL3D_CUDA(cudaMalloc(&dItems_, items_.size() * sizeof(GemmItem)));
+    dItemsCapacity_ = items_.size();
+  }
+  SL3D_CUDA(cudaMemcpyAsync(dItems_, items_.data(), items_.size() * sizeof(GemmItem),
+                            cudaMemcpyHostToDevice, stream));
+  int maxM = 0, maxN = 0;
+  for (const auto& it : items_) {
+    maxM = std::max(maxM, it.M);
+    maxN = std::max(maxN, it.N);
+  }
+  dim3 grid((maxM + kBM - 1) / kBM, (maxN + kBN - 1) / kBN, static_cast<unsigned>(items_.size()));
+  GemmF64Kernel<<<grid, 256, 0, stream>>>(dItems_, A, B, C);
+  SL3D_CHECK_LAUNCH();
+  // The item list is host memory the copy reads: finish before it changes.
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Grid::LegendreSynthesis(int N, bool real, const double* coeffs, int count, double* spectra,
+                            cudaStream_t stream) {
+  const SpinTable* t = nullptr;
+  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+  items_.clear();
+  const int mlo = real ? 0 : -lmax;
+  const long long base = real ? t->rowOffset[lmax] : 0;
+  for (int m = mlo; m <= lmax; ++m) {
+    const int rows = t->Rows(m, lmax);
+    const int mi = m - mlo;
+    GemmItem it{};
+    it.M = ntheta;
+    it.N = 2 * count;
+    it.K = rows;
+    it.a = static_cast<long long>(t->rowOffset[m + lmax]) * ntheta;
+    it.b = (t->rowOffset[m + lmax] - base) * 2LL * count;
+    it.c = static_cast<long long>(mi) * ntheta * 2LL * count;
+    it.sAi = 1;
+    it.sAk = ntheta;
+    it.ldb = 2 * count;
+    it.ldc = 2 * count;
+    if (rows == 0) {
+      SL3D_CUDA(cudaMemsetAsync(spectra + it.c, 0, sizeof(double) * ntheta * 2 * count, stream));
+      continue;
+    }
+    items_.push_back(it);
+  }
+  return RunGemm(t->values, coeffs, spectra, stream);
+}
+
+int Grid::LegendreAnalysis(int N, bool real, const double* spectra, int count, double* coeffs,
+                           cudaStream_t stream) {
+  const SpinTable* t = nullptr;
+  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+  items_.clear();
+  const int mlo = real ? 0 : -lmax;
+  const long long base = real ? t->rowOffset[lmax] : 0;
+  for (int m = mlo; m <= lmax; ++m) {
+    const int rows = t->Rows(m, lmax);
+    if (rows == 0) continue;
+    const int mi = m - mlo;
+    GemmItem it{};
+    it.M = rows;
+    it.N = 2 * count;
+    it.K = ntheta;
+    it.a = static_cast<long long>(t->rowOffset[m + lmax]) * ntheta;
+    it.b = static_cast<long long>(mi) * ntheta * 2LL * count;
+    it.c = (t->rowOffset[m + lmax] - base) * 2LL * count;
+    it.sAi = ntheta;
+    it.sAk = 1;
+    it.ldb = 2 * count;
+    it.ldc = 2 * count;
+    items_.push_back(it);
+  }
+  return RunGemm(t->values, spectra, coeffs, stream);
+}
+
+int Grid::RingSynthesis(bool real, const double* spectra, int count, double* fields,
+                        cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const size_t smem = 2 * kRingGroup * static_cast<size_t>(nphi) * sizeof(double2);
+  SL3D_CUDA(cudaFuncSetAttribute(RingSynthesisKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)));
+  dim3 grid((count + kRingGroup - 1) / kRingGroup, ntheta);
+  RingSynthesisKernel<<<grid, 256, smem, stream>>>(lmax, ntheta, count, real, plan, dTwiddle,
+                                                   reinterpret_cast<const double2*>(spectra), fields);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Grid::RingAnalysis(bool real, const double* fields, int count, double* spectra,
+                       cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const size_t smem = 2 * kRingGroup * static_cast<size_t>(nphi) * sizeof(double2);
+  SL3D_CUDA(cudaFuncSetAttribute(RingAnalysisKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)));
+  dim3 grid((count + kRingGroup - 1) / kRingGroup, ntheta);
+  RingAnalysisKernel<<<grid, 256, smem, stream>>>(lmax, ntheta, count, real, plan, dTwiddle,
+                                                  dWeights, fields,
+                                                  reinterpret_cast<double2*>(spectra));
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Grid::ToDevice(int N, bool real, const double* ref, int count, double* dev,
+                   cudaStream_t stream) {
+  const SpinTable* t = nullptr;
+  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+  const long long total = (real ? RealRows() : SpinRows(N)) * count;
+  if (total == 0) return SL3DGPU_OK;
+  ToDeviceKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(
+      lmax, N, real, count, t->dRowOffset, reinterpret_cast<const double2*>(ref),
+      reinterpret_cast<double2*>(dev));
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Grid::FromDevice(int N, bool real, const double* dev, int count, double* ref,
+                     cudaStream_t stream) {
+  const SpinTable* t = nullptr;
+  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+  const long long total = (real ? RealRows() : SpinRows(N)) * count;
+  if (total == 0) return SL3DGPU_OK;
+  FromDeviceKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(
+      lmax, N, real, count, t->dRowOffset, reinterpret_cast<const double2*>(dev),
+      reinterpret_cast<double2*>(ref));
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Grid::Scratch(size_t spectraDoubles, size_t coeffDoubles, double** spectra, double** coeffs) {
+  if (spectraDoubles > scratchSpectraSize_) {
+    cudaFree(scratchSpectra_);
+    scratchSpectra_ = nullptr;
+    scratchSpectraSize_ = 0;
+    SL3D_CUDA(cudaMalloc(&scratchSpectra_, spectraDoubles * sizeof(double)));
+    scratchSpectraSize_ = spectraDoubles;
+  }
+  if (coeffDoubles > scratchCoeffsSize_) {
+    cudaFree(scratchCoeffs_);
+    scratchCoeffs_ = nullptr;
+    scratchCoeffsSize_ = 0;
+    SL3D_CUDA(cudaMalloc(&scratchCoeffs_, coeffDoubles * sizeof(double)));
+    scratchCoeffsSize_ = coeffDoubles;
+  }
+  *spectra = scratchSpectra_;
+  *coeffs = scratchCoeffs_;
+  return SL3DGPU_OK;
+}
+
+}  // namespace sl3dgpu
+
+// -- the C ABI: SurfaceGrid's batched calls on device buffers in the reference layouts -----
+
+using namespace sl3dgpu;
+
+struct sl3dgpu_grid {
+  std::unique_ptr<Grid> grid;
+};
+
+extern "C" int sl3dgpu_grid_create(int lmax, int nmax, double oversampling, sl3dgpu_grid** out) {
+  if (out == nullptr) {
+    SetError("null output handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto handle = std::make_unique<sl3dgpu_grid>();
+  if (int st = Grid::Create(lmax, nmax, oversampling, handle->grid); st != SL3DGPU_OK) return st;
+  *out = handle.release();
+  return SL3DGPU_OK;
+}
+
+extern "C" void sl3dgpu_grid_destroy(sl3dgpu_grid* grid) { delete grid; }
+
+extern "C" int sl3dgpu_grid_shape(const sl3dgpu_grid* grid, int* ntheta, int* nphi) {
+  if (grid == nullptr) {
+    SetError("null grid");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (ntheta) *ntheta = grid->grid->ntheta;
+  if (nphi) *nphi = grid->grid->nphi;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_grid_colatitudes(const sl3dgpu_grid* grid, double* theta, double* weights) {
+  if (grid == nullptr) {
+    SetError("null grid");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& g = *grid->grid;
+  if (theta) std::memcpy(theta, g.theta.data(), g.theta.size() * sizeof(double));
+  if (weights) std::memcpy(weights, g.weights.data(), g.weights.size() * sizeof(double));
+  return SL3DGPU_OK;
+}
+
+namespace {
+
+int Synthesise(sl3dgpu_grid* handle, int N, bool real, const double* coeffs, int count,
+               double* fields, void* stream) {
+  if (handle == nullptr || count < 0) {
+    SetError("null grid or negative count");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto& g = *handle->grid;
+  const cudaStream_t s = AsStream(stream);
+  const size_t mcount = real ? g.lmax + 1 : 2 * g.lmax + 1;
+  const size_t rows = real ? g.RealRows() : g.SpinRows(N);
+  double *spectra = nullptr, *dev = nullptr;
+  if (int st = g.Scratch(mcount * g.ntheta * 2 * std::max(count, 1), rows * 2 * std::max(count, 1),
+                         &spectra, &dev);
+      st != SL3DGPU_OK)
+    return st;
+  if (int st = g.ToDevice(N, real, coeffs, count, dev, s); st != SL3DGPU_OK) return st;
+  if (int st = g.LegendreSynthesis(N, real, dev, count, spectra, s); st != SL3DGPU_OK) return st;
+  return g.RingSynthesis(real, spectra, count, fields, s);
+}
+
+int Expand(sl3dgpu_grid* handle, int N, bool real, const double* fields, int count, double* coeffs,
+           void* stream) {
+  if (handle == nullptr || count < 0) {
+    SetError("null grid or negative count");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto& g = *handle->grid;
+  const cudaStream_t s = AsStream(stream);
+  const size_t mcount = real ? g.lmax + 1 : 2 * g.lmax + 1;
+  const size_t rows = real ? g.RealRows() : g.SpinRows(N);
+  double *spectra = nullptr, *dev = nullptr;
+  if (int st = g.Scratch(mcount * g.ntheta * 2 * std::max(count, 1), rows * 2 * std::max(count, 1),
+                         &spectra, &dev);
+      st != SL3DGPU_OK)
+    return st;
+  if (int st = g.RingAnalysis(real, fields, count, spectra, s); st != SL3DGPU_OK) return st;
+  if (int st = g.LegendreAnalysis(N, real, spectra, count, dev, s); st != SL3DGPU_OK) return st;
+  return g.FromDevice(N, real, dev, count, coeffs, s);
+}
+
+}  // namespace
+
+extern "C" int sl3dgpu_synthesise_spin_batch(sl3dgpu_grid* grid, int N, const double* coeffs,
+                                             int count, double* fields, void* stream) {
+  return Synthesise(grid, N, false, coeffs, count, fields, stream);
+}
+
+extern "C" int sl3dgpu_expand_spin_batch(sl3dgpu_grid* grid, int N, const double* fields,
+                                         int count, double* coeffs, void* stream) {
+  return Expand(grid, N, false, fields, count, coeffs, stream);
+}
+
+extern "C" int sl3dgpu_synthesise_batch(sl3dgpu_grid* grid, const double* coeffs, int count,
+                                        double* fields, void* stream) {
+  return Synthesise(grid, 0, true, coeffs, count, fields, stream);
+}
+
+extern "C" int sl3dgpu_expand_batch(sl3dgpu_grid* grid, const double* fields, int count,
+                                    double* coeffs, void* stream) {
+  return Expand(grid, 0, true, fields, count, coeffs, stream);
+}

@@ -1,0 +1,101 @@
+// The device spherical-harmonic grid: Gauss-Legendre colatitudes, uniform
+// longitudes, the stored spin-N Legendre (Wigner-d) tables and the FFT plan,
+// with the batched transforms between coefficients and grid values.
+//
+// Basis (docs/design.md:245-250 of the reference): Y^N_lm =
+// sqrt((2l+1)/4pi) d^l_{Nm}(theta) e^{i m phi}, d^l_{0m} the Condon-Shortley
+// associated Legendre function; forward transform the integral of conj(Y) f.
+// Reference index layouts (include/sl3dpp/SurfaceGrid.hpp:110-118, 191-200):
+// spin N complex, l^2 - N^2 + (m + l) over l = |N|..lmax and every m; real
+// spin 0, l(l+1)/2 + m over m >= 0. Grid values colatitude-major, longitude
+// k at 2 pi k / nphi.
+//
+// Device ("m-major") layouts, what the kernels read and write: a batch of
+// `count` fields keeps, per spin, the coefficients of order m and degree l at
+// row RowOffset(m) + (l - l0(m)) of a [row][count] complex array (the node
+// fastest), so that one order's degrees over the batch are one dense matrix;
+// ring spectra are [m][j][count] complex.
+#pragma once
+
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sl3dgpu {
+
+struct FftPlan {
+  int n = 0;
+  int stages = 0;
+  int radix[16] = {};
+};
+
+// One spin's table: for each order m in [-lmax, lmax] (index m + lmax) a
+// block of (lmax - l0 + 1) rows of ntheta values, rows = degrees.
+struct SpinTable {
+  int N = 0;
+  std::vector<int> rowOffset;  // 2 lmax + 2 entries, cumulative rows by m index
+  double* values = nullptr;    // device
+  int* dRowOffset = nullptr;   // device copy of rowOffset
+  int Rows(int m, int lmax) const { return rowOffset[m + lmax + 1] - rowOffset[m + lmax]; }
+};
+
+struct GemmItem {
+  int M, N, K, pad;
+  long long a, b, c;
+  int sAi, sAk, ldb, ldc;
+};
+
+class Grid {
+ public:
+  static int Create(int lmax, int nmax, double oversampling, std::unique_ptr<Grid>& out);
+  ~Grid();
+
+  int lmax = 0, nmax = 0, band = 0, ntheta = 0, nphi = 0;
+  std::vector<double> theta, weights;  // host copies
+  double* dTheta = nullptr;
+  double* dWeights = nullptr;
+  double2* dTwiddle = nullptr;
+  FftPlan plan;
+
+  // The table of spin N, built on first use (device kernel).
+  int Table(int N, const SpinTable** out);
+  // Rows of one spin's coefficients per field (its (l, m) count).
+  long long SpinRows(int N) const { return static_cast<long long>(lmax + 1) * (lmax + 1) - N * N; }
+  // Rows of a real spin-0 field (m >= 0).
+  long long RealRows() const { return static_cast<long long>(lmax + 1) * (lmax + 2) / 2; }
+
+  // -- transforms in the device layouts -------------------------------------------
+  // Spin N: coefficients [row][count] complex -> spectra [m][j][count] -> fields
+  // [count][j][k] complex; and back. Real spin 0 likewise with m >= 0 rows.
+  int LegendreSynthesis(int N, bool real, const double* coeffs, int count, double* spectra,
+                        cudaStream_t stream);
+  int LegendreAnalysis(int N, bool real, const double* spectra, int count, double* coeffs,
+                       cudaStream_t stream);
+  int RingSynthesis(bool real, const double* spectra, int count, double* fields, cudaStream_t stream);
+  int RingAnalysis(bool real, const double* fields, int count, double* spectra, cudaStream_t stream);
+
+  // Reference layout <-> device layout permutations.
+  int ToDevice(int N, bool real, const double* ref, int count, double* dev, cudaStream_t stream);
+  int FromDevice(int N, bool real, const double* dev, int count, double* ref, cudaStream_t stream);
+
+  // Scratch owned by the grid for the reference-layout batch calls.
+  int Scratch(size_t spectraDoubles, size_t coeffDoubles, double** spectra, double** coeffs);
+
+ private:
+  std::map<int, SpinTable> tables_;
+  std::vector<GemmItem> items_;
+  GemmItem* dItems_ = nullptr;
+  size_t dItemsCapacity_ = 0;
+  double* scratchSpectra_ = nullptr;
+  size_t scratchSpectraSize_ = 0;
+  double* scratchCoeffs_ = nullptr;
+  size_t scratchCoeffsSize_ = 0;
+  int RunGemm(const double* A, const double* B, double* C, cudaStream_t stream);
+};
+
+// Smallest 2^a 3^b 5^c at or above n.
+int FftFriendly(int n);
+
+}  // namespace sl3dgpu
