@@ -99,6 +99,93 @@ int sl3dgpu_synthesise_batch(sl3dgpu_grid* grid, const double* coeffs, int count
 int sl3dgpu_expand_batch(sl3dgpu_grid* grid, const double* fields, int count, double* coeffs,
                          void* stream);
 
+/* ---- the 3D viscoelastic step (include/sl3dpp/Viscoelastic3D.hpp:79-837) -----
+ * A layered Earth (SI), each field linear in radius within its layer: the
+ * host-side counterpart of the reference's EarthModel + RadialMesh + Material
+ * + Rheology (Maxwell, or Burgers where kelvin_fraction > 0). */
+typedef struct sl3dgpu_layer {
+  double r0, r1;           /* metres */
+  int fluid;               /* 1: a fluid layer (mu = 0) */
+  int elements;            /* radial spectral elements in the layer */
+  double rho0, rho1;       /* density at r0, r1 (kg m^-3) */
+  double kappa0, kappa1;   /* bulk modulus (Pa) */
+  double mu0, mu1;         /* shear modulus (Pa) */
+  double viscosity;        /* Pa s; 0: elastic */
+  double kelvin_fraction;  /* Burgers: Kelvin modulus over mu; 0: Maxwell */
+  double kelvin_viscosity; /* Burgers: Kelvin viscosity (Pa s) */
+} sl3dgpu_layer;
+
+/* Viscoelastic3D::Options (Viscoelastic3D.hpp:89-187) for the fixed-point step. */
+typedef struct sl3dgpu_v3d_options {
+  int lmax;
+  int ngll;              /* GLL nodes per element (order + 1) */
+  double eps;            /* truncation level, 1e-8 */
+  double oversampling;   /* 1.5 */
+  int max_iterations;    /* 40 */
+  double rtol;           /* 1e-11 */
+  double damping;        /* 1.0 */
+  int anderson_memory;   /* 5 */
+  double anderson_rate;  /* 0.5 */
+  int precision;         /* 0: FP64 throughout; 1: mixed (see sl3dgpu_v3d_create) */
+} sl3dgpu_v3d_options;
+
+/* Viscoelastic3D::StepInfo (Viscoelastic3D.hpp:357-375). */
+typedef struct sl3dgpu_step_info {
+  int iterations;
+  double residual;
+  int converged;
+  int mixed_passes;
+} sl3dgpu_step_info;
+
+/* The configurations' Earth (radius 6371 km, fluid core to 3480 km, linear
+ * mantle, 100 km elastic lid, 5e21 / 5e20 Pa s below / above 670 km), the
+ * given element count spread over its four layers in proportion to
+ * thickness; kelvin_fraction > 0 makes the viscous layers Burgers bodies
+ * (Kelvin viscosity = viscosity / kelvin_div). Fills layers[0..3]. */
+int sl3dgpu_standard_earth(int elements, double kelvin_fraction, double kelvin_div,
+                           sl3dgpu_layer* layers);
+
+/* The 3D operator: Viscoelastic3D's constructor (src/Viscoelastic3D.cpp:169-356)
+ * over the layered Earth, at the Gauss memory points. The unrelaxed degree
+ * systems are assembled on the host and factorised on the GPU; delta is zero
+ * until sl3dgpu_v3d_set_delta. */
+typedef struct sl3dgpu_v3d sl3dgpu_v3d;
+typedef struct sl3dgpu_v3d_state sl3dgpu_v3d_state;
+int sl3dgpu_v3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options* options,
+                       sl3dgpu_v3d** out);
+void sl3dgpu_v3d_destroy(sl3dgpu_v3d* op);
+/* Memory nodes, and the grid every node's values sit on (GridCoupling's one
+ * block: NodeCount, Grid().NumberOfCoLatitudes/NumberOfLongitudes). */
+int sl3dgpu_v3d_shape(const sl3dgpu_v3d* op, int* nodes, int* ntheta, int* nphi);
+/* GridCoupling::RadiusOfNode / ElementOfNode, non-dimensional radii. */
+int sl3dgpu_v3d_nodes(const sl3dgpu_v3d* op, double* radius, int* element);
+int sl3dgpu_v3d_colatitudes(const sl3dgpu_v3d* op, double* theta, double* weights);
+/* The model's scales (SI per unit): length, time, surface density. */
+int sl3dgpu_v3d_scales(const sl3dgpu_v3d* op, double* length, double* time, double* surface_density);
+/* The log-viscosity perturbation delta(r, theta, phi) sampled over every
+ * memory node's grid (node-major, colatitude, longitude): the samples the
+ * reference's delta callback gives (Viscoelastic3D.cpp:250-287); host or
+ * device pointer. */
+int sl3dgpu_v3d_set_delta(sl3dgpu_v3d* op, const double* samples, int on_device);
+/* Viscoelastic3D::ZeroState (Viscoelastic3D.hpp, State). */
+int sl3dgpu_v3d_zero_state(sl3dgpu_v3d* op, sl3dgpu_v3d_state** out);
+void sl3dgpu_v3d_free_state(sl3dgpu_v3d_state* state);
+/* Viscoelastic3D::Step (Viscoelastic3D.cpp:1982-2030): scheme 0
+ * ExponentialTrapezoid, 1 BackwardEuler, 2 Sdirk2; the load channel's
+ * coefficients (host, complex pairs, real spin-0 layout l(l+1)/2 + m,
+ * non-dimensional surface density) at the step's start and end, the stages
+ * taking the linear interpolation between them; NULL for none. The state
+ * advances in place. */
+int sl3dgpu_v3d_step(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme,
+                     const double* load0, const double* load1, sl3dgpu_step_info* info);
+/* Viscoelastic3D::Surface (Viscoelastic3D.cpp:2032-2051) of the last step's
+ * solutions: component 0 U, 1 V, 2 phi; complex m >= 0 columns per degree in
+ * the l(l+1)/2 + m layout, into host memory. */
+int sl3dgpu_v3d_surface(sl3dgpu_v3d* op, int component, double* out);
+/* A state's strain coefficients in the reference layouts, node-major blocks:
+ * spin -2, spin -1, real spin 0 (GridCoupling::SpectralTensor). Host out. */
+int sl3dgpu_v3d_state_strain(sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, double* out);
+
 #ifdef __cplusplus
 }
 #endif

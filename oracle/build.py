@@ -19,7 +19,9 @@ PRODUCT_HOST = HERE.parent / "sl3dpp_gb300" / "csrc" / "host"
 
 
 def _sources() -> list[pathlib.Path]:
-    return sorted(HERE.glob("*.cpp"))
+    # the oracle's own restatement, plus the library's host-side radial setup
+    # (mesh, material, rheology, degree systems), which it shares
+    return sorted(HERE.glob("*.cpp")) + sorted(PRODUCT_HOST.glob("radial.cpp"))
 
 
 def _stale(sources: list[pathlib.Path]) -> bool:

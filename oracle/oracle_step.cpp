@@ -1,0 +1,1068 @@
+// ORACLE — test infrastructure only (see oracle_core.cpp's header).
+//
+// A CPU FP64 restatement of the reference's 3D quasi-static step: the grid
+// coupling and the within-step fixed point of Viscoelastic3D, on the Gauss
+// memory points, one node block, the fixed-point solver (Picard, adaptive
+// Anderson). It follows:
+//  - include/sl3dpp/SpinComponents.hpp:53-145 (DeviatoricComponents,
+//    ForceRowsFromComponents);
+//  - src/GridCoupling.cpp:56-161 (memory nodes), 263-314 (Synthesise,
+//    Analyse), 497-509 (Multiply), 595-689 (Scatter, Gather,
+//    AddStrainOfSolution), 691-809 (SpheroidalForce, ToroidalForce);
+//  - src/Viscoelastic3D.cpp:169-356 (itau sampling), 433-492 (StageState),
+//    876-1073 (SolveForces, SolveElastic, AddUnitChannels), 1223-1424
+//    (StartStep, Respond), 1758-1786 (StrainOf), 1636-1669 (RelativeChange),
+//    1885-1974 (Finish, Converge), 1982-2030 (Step, Sdirk2 by recipe),
+//    2032-2079 (Surface);
+//  - include/sl3dpp/detail/AndersonMixer.hpp:65-219 (the mixer, its Gram
+//    least squares by the symmetric minimum-norm solve of lstsq.hpp in place
+//    of LAPACK's dgelss);
+//  - include/sl3dpp/StepRecipe.hpp, src/StepRecipe.cpp (Sdirk2's stages).
+// The radial setup (mesh, material, rheology, degree systems) is the
+// library's host code (sl3dpp_gb300/csrc/host/radial.cpp), shared; the
+// factorisations, solves, transforms and every per-pass operation are
+// restated here on the CPU.
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <optional>
+#include <vector>
+
+#include "../include/sl3dgpu.h"
+#include "lstsq.hpp"
+#include "oracle.h"
+#include "radial.hpp"
+
+namespace oracle {
+
+using C = std::complex<double>;
+using namespace sl3dgpu::host;
+
+// -- FFT (recursive mixed radix 2, 3, 5) --------------------------------------------------------
+
+void FftRec(const C* in, int stride, C* out, int n, int sign) {
+  if (n == 1) {
+    out[0] = in[0];
+    return;
+  }
+  int p = 2;
+  for (int f : {2, 3, 5})
+    if (n % f == 0) {
+      p = f;
+      break;
+    }
+  const int m = n / p;
+  for (int s = 0; s < p; ++s) FftRec(in + s * stride, stride * p, out + s * m, m, sign);
+  std::vector<C> tmp(n);
+  for (int k = 0; k < m; ++k)
+    for (int q = 0; q < p; ++q) {
+      C sum{};
+      const int idx = k + q * m;
+      for (int s = 0; s < p; ++s) {
+        const double ang = sign * 2.0 * kPi * static_cast<double>((static_cast<long long>(s) * idx) % n) / n;
+        sum += C(std::cos(ang), std::sin(ang)) * out[s * m + k];
+      }
+      tmp[idx] = sum;
+    }
+  std::copy(tmp.begin(), tmp.end(), out);
+}
+
+// -- the grid --------------------------------------------------------------------------------------
+
+struct OGrid {
+  int lmax = 0, ntheta = 0, nphi = 0;
+  std::vector<double> theta, w;
+  std::map<int, std::vector<std::vector<double>>> tables;
+
+  OGrid(int lmax_, double oversampling) : lmax(lmax_) {
+    const int band = static_cast<int>(std::ceil(oversampling * lmax - 1e-12));
+    ntheta = band + 1;
+    int n = 2 * band + 1;
+    for (;; ++n) {
+      int r = n;
+      for (int p : {2, 3, 5})
+        while (r % p == 0) r /= p;
+      if (r == 1) break;
+    }
+    nphi = n;
+    std::vector<double> x(ntheta);
+    w.resize(ntheta);
+    oracle_gauss_legendre(ntheta, x.data(), w.data());
+    theta.resize(ntheta);
+    for (int j = 0; j < ntheta; ++j) theta[j] = std::acos(x[j]);
+    for (int N : {-2, -1, 0}) {
+      auto& t = tables[N];
+      t.resize(2 * lmax + 1);
+      for (int m = -lmax; m <= lmax; ++m) {
+        const int l0 = std::max(std::abs(m), std::abs(N));
+        if (l0 > lmax) continue;
+        t[m + lmax].resize(static_cast<std::size_t>(lmax - l0 + 1) * ntheta);
+        oracle_wigner_column(lmax, N, m, ntheta, theta.data(), t[m + lmax].data());
+      }
+    }
+  }
+  std::size_t FieldSize() const { return static_cast<std::size_t>(ntheta) * nphi; }
+  std::size_t SpinSize(int N) const { return static_cast<std::size_t>(lmax + 1) * (lmax + 1) - N * N; }
+  std::size_t RealSize() const { return static_cast<std::size_t>(lmax + 1) * (lmax + 2) / 2; }
+  static std::size_t SpinIndex(int N, int l, int m) { return static_cast<std::size_t>(l) * l - N * N + (m + l); }
+  static std::size_t Index(int l, int m) { return static_cast<std::size_t>(l) * (l + 1) / 2 + m; }
+
+  void SynthSpin(int N, const C* c, C* f) const {
+    const auto& t = tables.at(N);
+    std::vector<C> ring(nphi), out(nphi);
+    for (int j = 0; j < ntheta; ++j) {
+      std::fill(ring.begin(), ring.end(), C{});
+      for (int m = -lmax; m <= lmax; ++m) {
+        const int l0 = std::max(std::abs(m), std::abs(N));
+        if (l0 > lmax) continue;
+        const auto& col = t[m + lmax];
+        C sum{};
+        for (int l = l0; l <= lmax; ++l) sum += col[static_cast<std::size_t>(l - l0) * ntheta + j] * c[SpinIndex(N, l, m)];
+        ring[((m % nphi) + nphi) % nphi] = sum;
+      }
+      FftRec(ring.data(), 1, out.data(), nphi, +1);
+      std::copy(out.begin(), out.end(), f + static_cast<std::size_t>(j) * nphi);
+    }
+  }
+  void ExpandSpin(int N, const C* f, C* c) const {
+    const auto& t = tables.at(N);
+    std::vector<C> G(static_cast<std::size_t>(2 * lmax + 1) * ntheta), out(nphi);
+    for (int j = 0; j < ntheta; ++j) {
+      FftRec(f + static_cast<std::size_t>(j) * nphi, 1, out.data(), nphi, -1);
+      const double s = 2.0 * kPi / nphi * w[j];
+      for (int m = -lmax; m <= lmax; ++m) G[static_cast<std::size_t>(m + lmax) * ntheta + j] = out[((m % nphi) + nphi) % nphi] * s;
+    }
+    for (int m = -lmax; m <= lmax; ++m) {
+      const int l0 = std::max(std::abs(m), std::abs(N));
+      if (l0 > lmax) continue;
+      const auto& col = t[m + lmax];
+      for (int l = l0; l <= lmax; ++l) {
+        C sum{};
+        for (int j = 0; j < ntheta; ++j) sum += col[static_cast<std::size_t>(l - l0) * ntheta + j] * G[static_cast<std::size_t>(m + lmax) * ntheta + j];
+        c[SpinIndex(N, l, m)] = sum;
+      }
+    }
+  }
+  void SynthReal(const C* c, double* f) const {
+    const auto& t = tables.at(0);
+    std::vector<C> ring(nphi), out(nphi);
+    for (int j = 0; j < ntheta; ++j) {
+      std::fill(ring.begin(), ring.end(), C{});
+      for (int m = 0; m <= lmax; ++m) {
+        const auto& col = t[m + lmax];
+        C sum{};
+        for (int l = m; l <= lmax; ++l) sum += col[static_cast<std::size_t>(l - m) * ntheta + j] * c[Index(l, m)];
+        if (m == 0) {
+          ring[0] = C(sum.real(), 0.0);
+        } else {
+          ring[m] = sum;
+          ring[nphi - m] = std::conj(sum);
+        }
+      }
+      FftRec(ring.data(), 1, out.data(), nphi, +1);
+      for (int k = 0; k < nphi; ++k) f[static_cast<std::size_t>(j) * nphi + k] = out[k].real();
+    }
+  }
+  void ExpandReal(const double* f, C* c) const {
+    const auto& t = tables.at(0);
+    std::vector<C> G(static_cast<std::size_t>(lmax + 1) * ntheta), ring(nphi), out(nphi);
+    for (int j = 0; j < ntheta; ++j) {
+      for (int k = 0; k < nphi; ++k) ring[k] = C(f[static_cast<std::size_t>(j) * nphi + k], 0.0);
+      FftRec(ring.data(), 1, out.data(), nphi, -1);
+      const double s = 2.0 * kPi / nphi * w[j];
+      for (int m = 0; m <= lmax; ++m) G[static_cast<std::size_t>(m) * ntheta + j] = out[m] * s;
+    }
+    for (int m = 0; m <= lmax; ++m) {
+      const auto& col = t[m + lmax];
+      for (int l = m; l <= lmax; ++l) {
+        C sum{};
+        for (int j = 0; j < ntheta; ++j) sum += col[static_cast<std::size_t>(l - m) * ntheta + j] * G[static_cast<std::size_t>(m) * ntheta + j];
+        c[Index(l, m)] = sum;
+      }
+    }
+  }
+};
+
+// -- spin components (SpinComponents.hpp:53-145) ------------------------------------------------
+
+struct NodeValues {
+  C U, V, W, rdU, rdV, rdW;
+};
+
+std::array<C, 5> DeviatoricComponents(int l, const NodeValues& v, double r) {
+  const C i(0.0, 1.0);
+  const double zeta2 = l * (l + 1.0), zeta = std::sqrt(zeta2);
+  std::array<C, 5> A{};
+  A[2] = (v.rdU - v.U + 0.5 * zeta2 * v.V) / (3.0 * r);
+  if (l >= 1) {
+    const C tangential = v.rdV - v.V + v.U;
+    const C twist = v.W - v.rdW;
+    A[1] = zeta * (tangential + i * twist) / (2.0 * std::sqrt(2.0) * r);
+    A[3] = zeta * (tangential - i * twist) / (2.0 * std::sqrt(2.0) * r);
+  }
+  if (l >= 2) {
+    const double factor = 0.5 * zeta * std::sqrt(zeta2 - 2.0) / r;
+    A[0] = factor * (v.V - i * v.W);
+    A[4] = factor * (v.V + i * v.W);
+  }
+  return A;
+}
+
+struct Rows {
+  C u, v, w, du, dv, dw;
+};
+
+Rows ForceRows(int l, const std::array<C, 5>& A, double r) {
+  const C i(0.0, 1.0);
+  const double zeta2 = l * (l + 1.0), zeta = std::sqrt(zeta2);
+  const double root = std::sqrt(std::max(zeta2 - 2.0, 0.0));
+  const double s2 = std::sqrt(2.0);
+  Rows rows;
+  rows.u = s2 * zeta * (A[1] + A[3]) - 4.0 * A[2];
+  rows.v = zeta * root * (A[0] + A[4]) + 2.0 * zeta2 * A[2] - s2 * zeta * (A[1] + A[3]);
+  rows.w = i * (zeta * root * (A[0] - A[4]) - s2 * zeta * (A[1] - A[3]));
+  rows.du = 4.0 * r * A[2];
+  rows.dv = s2 * zeta * r * (A[1] + A[3]);
+  rows.dw = i * s2 * zeta * r * (A[1] - A[3]);
+  return rows;
+}
+
+// -- tensors ----------------------------------------------------------------------------------------
+
+struct Spectral {
+  std::vector<C> c0, c1, r;  // spin -2, spin -1 (full m), spin 0 (m >= 0); node-major
+};
+struct Tensor {
+  std::vector<C> c0, c1;
+  std::vector<double> r;
+};
+
+struct Factor {
+  bool cholesky = true;
+  int n = 0, kd = 0;
+  std::vector<double> band;
+  std::vector<int> pivots, pinned;
+  std::vector<double> scale;
+};
+
+Factor FactorSpheroidal(const DegreeOperator& op) {
+  Factor f;
+  f.n = op.DofCount();
+  f.kd = op.Bandwidth();
+  f.scale = op.Scale();
+  if (op.PositiveDiagonal()) {
+    f.band = op.ScaledCholeskyBand();
+    if (oracle_band_cholesky_factor(f.band.data(), f.n, f.kd) == 0) return f;
+  }
+  f.cholesky = false;
+  f.band = op.ScaledLuBand();
+  f.pivots.resize(f.n);
+  if (oracle_band_lu_factor(f.band.data(), f.n, f.kd, f.kd, f.pivots.data()) != 0)
+    throw std::runtime_error("the banded LU factorisation failed");
+  return f;
+}
+
+Factor FactorToroidal(const ToroidalOperator& op) {
+  Factor f;
+  f.n = op.DofCount();
+  f.kd = op.Bandwidth();
+  f.scale = op.Scale();
+  f.pinned = op.Pinned();
+  f.band = op.ScaledCholeskyBand();
+  if (oracle_band_cholesky_factor(f.band.data(), f.n, f.kd) != 0)
+    throw std::runtime_error("toroidal Cholesky failed");
+  return f;
+}
+
+// x with A x = b for complex columns (ndof x cols, column-major), as
+// SolveForces' begin/finish: real and imaginary parts as real columns.
+std::vector<C> SolveComplex(const Factor& f, const std::vector<C>& b, int cols) {
+  const int n = f.n;
+  std::vector<double> x(static_cast<std::size_t>(n) * 2 * cols);
+  for (int c = 0; c < cols; ++c)
+    for (int d = 0; d < n; ++d) {
+      x[static_cast<std::size_t>(c) * n + d] = b[static_cast<std::size_t>(c) * n + d].real();
+      x[static_cast<std::size_t>(cols + c) * n + d] = b[static_cast<std::size_t>(c) * n + d].imag();
+    }
+  for (int k = 0; k < 2 * cols; ++k) {
+    for (int j = 0; j < n; ++j) x[static_cast<std::size_t>(k) * n + j] *= f.scale[j];
+    for (int p : f.pinned) x[static_cast<std::size_t>(k) * n + p] = 0.0;
+  }
+  if (f.cholesky)
+    oracle_band_cholesky_solve(f.band.data(), n, f.kd, x.data(), 2 * cols);
+  else
+    oracle_band_lu_solve(f.band.data(), n, f.kd, f.kd, f.pivots.data(), x.data(), 2 * cols);
+  for (int k = 0; k < 2 * cols; ++k)
+    for (int j = 0; j < n; ++j) x[static_cast<std::size_t>(k) * n + j] *= f.scale[j];
+  std::vector<C> out(static_cast<std::size_t>(n) * cols);
+  for (int c = 0; c < cols; ++c)
+    for (int d = 0; d < n; ++d)
+      out[static_cast<std::size_t>(c) * n + d] = C(x[static_cast<std::size_t>(c) * n + d], x[static_cast<std::size_t>(cols + c) * n + d]);
+  return out;
+}
+
+struct Flavour {
+  std::vector<std::unique_ptr<DegreeOperator>> sph;
+  std::vector<std::unique_ptr<ToroidalOperator>> tor;
+  std::vector<Factor> sphF, torF;
+  std::vector<std::vector<double>> units;  // K^-1 Load per degree
+  PointShear shear;
+};
+
+struct Solutions {
+  std::vector<std::vector<C>> sph, tor;  // per degree, (ndof x (l + 1)) column-major
+};
+
+struct State {
+  double t = 0.0;
+  std::vector<Tensor> m;
+  std::optional<Tensor> strain;
+  std::optional<Spectral> strainCoefficients;
+};
+
+struct Info {
+  int iterations = 0;
+  double residual = 0.0;
+  bool converged = false;
+  int mixedPasses = 0;
+};
+
+// -- the Anderson mixer (AndersonMixer.hpp:65-219) ----------------------------------------------
+
+class Mixer {
+ public:
+  explicit Mixer(int memory) : memory_(memory) {}
+  // x (in/out) and gx as flat real vectors.
+  void Update(std::vector<double*> xs, std::vector<const double*> gs, std::vector<std::size_t> sizes) {
+    std::size_t n = 0;
+    for (auto s : sizes) n += s;
+    auto sweep = [&](auto&& body) {
+      std::size_t at = 0;
+      for (std::size_t s = 0; s < xs.size(); ++s)
+        for (std::size_t j = 0; j < sizes[s]; ++j, ++at) body(s, j, at);
+    };
+    if (xPrev_.empty()) {
+      dG_.assign(memory_, std::vector<double>(n));
+      dF_.assign(memory_, std::vector<double>(n));
+      gram_.assign(static_cast<std::size_t>(memory_) * memory_, 0.0);
+      xPrev_.resize(n);
+      fPrev_.resize(n);
+      sweep([&](std::size_t s, std::size_t j, std::size_t at) {
+        xPrev_[at] = xs[s][j];
+        fPrev_[at] = gs[s][j] - xs[s][j];
+        xs[s][j] = gs[s][j];
+      });
+      return;
+    }
+    const int slot = slot_;
+    const int m = std::min(count_ + 1, memory_);
+    std::vector<double> column(m, 0.0), gamma(m, 0.0);
+    sweep([&](std::size_t s, std::size_t j, std::size_t at) {
+      const double f = gs[s][j] - xs[s][j];
+      const double dx = xs[s][j] - xPrev_[at];
+      dF_[slot][at] = f - fPrev_[at];
+      dG_[slot][at] = dx + dF_[slot][at];
+      xPrev_[at] = xs[s][j];
+      fPrev_[at] = f;
+      for (int i = 0; i < m; ++i) {
+        column[i] += dF_[i][at] * dF_[slot][at];
+        gamma[i] += dF_[i][at] * f;
+      }
+    });
+    count_ = m;
+    slot_ = (slot + 1) % memory_;
+    for (int i = 0; i < m; ++i) {
+      gram_[static_cast<std::size_t>(slot) * memory_ + i] = column[i];
+      gram_[static_cast<std::size_t>(i) * memory_ + slot] = column[i];
+    }
+    std::vector<double> a(static_cast<std::size_t>(m) * m), g(m);
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) a[static_cast<std::size_t>(i) * m + j] = gram_[static_cast<std::size_t>(i) * memory_ + j];
+    if (!sl3dgpu::SymmetricLstsq(m, a.data(), gamma.data(), g.data())) {
+      sweep([&](std::size_t s, std::size_t j, std::size_t) { xs[s][j] = gs[s][j]; });
+      return;
+    }
+    sweep([&](std::size_t s, std::size_t j, std::size_t at) {
+      double value = gs[s][j];
+      for (int i = 0; i < m; ++i) value -= g[i] * dG_[i][at];
+      xs[s][j] = value;
+    });
+  }
+
+ private:
+  int memory_, count_ = 0, slot_ = 0;
+  std::vector<double> xPrev_, fPrev_, gram_;
+  std::vector<std::vector<double>> dG_, dF_;
+};
+
+// -- the 3D operator --------------------------------------------------------------------------------
+
+struct Node {
+  int element, q;
+  double r;
+};
+
+class Viscoelastic3D {
+ public:
+  Viscoelastic3D(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& options)
+      : options_(options),
+        earth_(ToLayers(layers, nlayers), Scales::Geophysical(layers[nlayers - 1].r1)),
+        mesh_(RadialMesh::Create(earth_, options.ngll)),
+        material_(Material::Create(earth_, mesh_)),
+        rheology_(Rheology::FromEarth(earth_, material_)),
+        reference_(rheology_, true),
+        grid_(options.lmax, options.oversampling) {
+    const auto& mesh = reference_.nodal.mesh;
+    const int n = mesh.NGll();
+    const auto& pts = reference_.points;
+    for (int e = 0; e < mesh.ElementCount(); ++e) {
+      bool carries = false;
+      for (int i = 0; i < n; ++i) carries = carries || rheology_.IsActive(static_cast<std::size_t>(e) * n + i);
+      if (!carries) continue;
+      for (int p = 0; p < pts.count; ++p) nodes_.push_back({e, p, pts.RadiusAt(mesh, e, p)});
+    }
+    const int L = options.lmax;
+    firstNode_.resize(L + 1);
+    for (int l = 0; l <= L; ++l) {
+      const int fe = l > 0 ? mesh.StartElement(l, options.eps) : 0;
+      int first = static_cast<int>(nodes_.size());
+      for (std::size_t p = 0; p < nodes_.size(); ++p)
+        if (nodes_[p].element >= fe) {
+          first = static_cast<int>(p);
+          break;
+        }
+      firstNode_[l] = first;
+    }
+    factor_.assign(static_cast<std::size_t>(NodeCount()) * grid_.FieldSize(), 1.0);
+    // the elastic (unrelaxed) operators
+    elastic_ = BuildFlavour(reference_.elastic);
+  }
+
+  static std::vector<Layer> ToLayers(const sl3dgpu_layer* layers, int n) {
+    std::vector<Layer> out(n);
+    for (int i = 0; i < n; ++i) {
+      const auto& s = layers[i];
+      out[i] = Layer{s.r0, s.r1, s.fluid != 0, s.rho0, s.rho1, s.kappa0, s.kappa1, s.mu0, s.mu1,
+                     s.viscosity, s.kelvin_fraction, s.kelvin_viscosity, s.elements};
+    }
+    return out;
+  }
+
+  int NodeCount() const { return static_cast<int>(nodes_.size()); }
+  const OGrid& Grid() const { return grid_; }
+  const std::vector<Node>& Nodes() const { return nodes_; }
+  const Scales& ModelScales() const { return earth_.scales(); }
+  int Lmax() const { return options_.lmax; }
+
+  void SetDelta(const double* samples) {
+    for (std::size_t i = 0; i < factor_.size(); ++i) factor_[i] = std::exp(-samples[i]);
+  }
+
+  State ZeroState() const {
+    State s;
+    for (std::size_t k = 0; k < rheology_.branches.size(); ++k) s.m.push_back(ZeroTensor());
+    return s;
+  }
+
+  Tensor ZeroTensor() const {
+    const auto size = static_cast<std::size_t>(NodeCount()) * grid_.FieldSize();
+    return Tensor{std::vector<C>(size), std::vector<C>(size), std::vector<double>(size)};
+  }
+  Spectral ZeroSpectral() const {
+    const auto P = static_cast<std::size_t>(NodeCount());
+    return Spectral{std::vector<C>(P * grid_.SpinSize(-2)), std::vector<C>(P * grid_.SpinSize(-1)),
+                    std::vector<C>(P * grid_.RealSize())};
+  }
+
+  // GridCoupling::Synthesise / Analyse
+  void Synthesise(const Spectral& s, Tensor& t) const {
+    const int P = NodeCount();
+    const auto fs = grid_.FieldSize();
+#pragma omp parallel for schedule(dynamic)
+    for (int p = 0; p < P; ++p) {
+      grid_.SynthSpin(-2, s.c0.data() + p * grid_.SpinSize(-2), t.c0.data() + p * fs);
+      grid_.SynthSpin(-1, s.c1.data() + p * grid_.SpinSize(-1), t.c1.data() + p * fs);
+      grid_.SynthReal(s.r.data() + p * grid_.RealSize(), t.r.data() + p * fs);
+    }
+  }
+  void Analyse(const Tensor& t, Spectral& s) const {
+    const int P = NodeCount();
+    const auto fs = grid_.FieldSize();
+#pragma omp parallel for schedule(dynamic)
+    for (int p = 0; p < P; ++p) {
+      grid_.ExpandSpin(-2, t.c0.data() + p * fs, s.c0.data() + p * grid_.SpinSize(-2));
+      grid_.ExpandSpin(-1, t.c1.data() + p * fs, s.c1.data() + p * grid_.SpinSize(-1));
+      grid_.ExpandReal(t.r.data() + p * fs, s.r.data() + p * grid_.RealSize());
+    }
+  }
+
+  void Scatter(Spectral& s, int node, int l, int m, const std::array<C, 5>& A) const {
+    const double sign = (m % 2 == 0) ? 1.0 : -1.0;
+    const int spins[2] = {-2, -1};
+    for (int c = 0; c < 2; ++c) {
+      if (l < std::abs(spins[c])) continue;
+      auto& block = c == 0 ? s.c0 : s.c1;
+      C* b = block.data() + static_cast<std::size_t>(node) * grid_.SpinSize(spins[c]);
+      b[OGrid::SpinIndex(spins[c], l, m)] += A[c];
+      if (m > 0) b[OGrid::SpinIndex(spins[c], l, -m)] += sign * std::conj(A[4 - c]);
+    }
+    s.r[static_cast<std::size_t>(node) * grid_.RealSize() + OGrid::Index(l, m)] += A[2];
+  }
+
+  std::array<C, 5> Gather(const Spectral& s, int node, int l, int m) const {
+    const double sign = (m % 2 == 0) ? 1.0 : -1.0;
+    std::array<C, 5> A{};
+    A[2] = s.r[static_cast<std::size_t>(node) * grid_.RealSize() + OGrid::Index(l, m)];
+    if (l >= 1) {
+      const C* b = s.c1.data() + static_cast<std::size_t>(node) * grid_.SpinSize(-1);
+      A[1] = b[OGrid::SpinIndex(-1, l, m)];
+      A[3] = sign * std::conj(b[OGrid::SpinIndex(-1, l, -m)]);
+    }
+    if (l >= 2) {
+      const C* b = s.c0.data() + static_cast<std::size_t>(node) * grid_.SpinSize(-2);
+      A[0] = b[OGrid::SpinIndex(-2, l, m)];
+      A[4] = sign * std::conj(b[OGrid::SpinIndex(-2, l, -m)]);
+    }
+    return A;
+  }
+
+  // StrainOf: every degree's solution into a fresh spectral tensor.
+  Spectral StrainOf(const Solutions& x, const Flavour& f) const {
+    Spectral s = ZeroSpectral();
+    const auto& mesh = reference_.nodal.mesh;
+    const auto& pts = reference_.points;
+    const int n = mesh.NGll();
+    const int L = options_.lmax;
+#pragma omp parallel for schedule(dynamic)
+    for (int l = L; l >= 0; --l) {
+      const auto& sph = *f.sph[l];
+      const ToroidalOperator* tor = l >= 1 ? f.tor[l].get() : nullptr;
+      const int ndof = sph.DofCount();
+      const auto& xs = x.sph[l];
+      for (int node = firstNode_[l]; node < NodeCount(); ++node) {
+        const int e = nodes_[node].element, q = nodes_[node].q;
+        const double r = nodes_[node].r, jac = mesh.Jacobian(e);
+        for (int m = 0; m <= l; ++m) {
+          NodeValues v{};
+          for (int i = 0; i < n; ++i) {
+            const int g = mesh.GlobalIndex(e, i);
+            const int dU = sph.Dof(g, kU), dV = sph.Dof(g, kV);
+            const C U = dU >= 0 ? xs[static_cast<std::size_t>(m) * ndof + dU] : C{};
+            const C V = dV >= 0 ? xs[static_cast<std::size_t>(m) * ndof + dV] : C{};
+            C W{};
+            if (tor != nullptr) {
+              const int dW = tor->Dof(g);
+              if (dW >= 0) W = x.tor[l][static_cast<std::size_t>(m) * tor->DofCount() + dW];
+            }
+            const double val = pts.Value(q, i);
+            v.U += val * U;
+            v.V += val * V;
+            v.W += val * W;
+            const double b = r * pts.Derivative(q, i) / jac;
+            v.rdU += b * U;
+            v.rdV += b * V;
+            v.rdW += b * W;
+          }
+          Scatter(s, node, l, m, DeviatoricComponents(l, v, r));
+        }
+      }
+    }
+    return s;
+  }
+
+  // SpheroidalForce + ToroidalForce.
+  void Forces(const Spectral& w, const Flavour& f, std::vector<std::vector<C>>& sph,
+              std::vector<std::vector<C>>& tor) const {
+    const auto& mesh = reference_.nodal.mesh;
+    const auto& pts = reference_.points;
+    const int n = mesh.NGll();
+    const int L = options_.lmax;
+    sph.assign(L + 1, {});
+    tor.assign(L + 1, {});
+#pragma omp parallel for schedule(dynamic)
+    for (int l = L; l >= 0; --l) {
+      const auto& op = *f.sph[l];
+      const ToroidalOperator* top = l >= 1 ? f.tor[l].get() : nullptr;
+      const int cols = l + 1;
+      std::vector<C> b(static_cast<std::size_t>(op.DofCount()) * cols);
+      std::vector<C> bt(top ? static_cast<std::size_t>(top->DofCount()) * cols : 0);
+      for (int node = firstNode_[l]; node < NodeCount(); ++node) {
+        const int e = nodes_[node].element, q = nodes_[node].q;
+        const double r = nodes_[node].r, jac = mesh.Jacobian(e);
+        for (int m = 0; m < cols; ++m) {
+          const auto rows = ForceRows(l, Gather(w, node, l, m), r);
+          const double point = jac * pts.weight[q] * r;
+          for (int i = 0; i < n; ++i) {
+            const int g = mesh.GlobalIndex(e, i);
+            const double v = point * pts.Value(q, i);
+            const double deriv = pts.weight[q] * pts.Derivative(q, i) * r;
+            const int iU = op.Dof(g, kU), iV = op.Dof(g, kV);
+            if (iU >= 0) b[static_cast<std::size_t>(m) * op.DofCount() + iU] += v * rows.u;
+            if (iV >= 0) b[static_cast<std::size_t>(m) * op.DofCount() + iV] += v * rows.v;
+            if (iU >= 0) b[static_cast<std::size_t>(m) * op.DofCount() + iU] += deriv * rows.du;
+            if (iV >= 0) b[static_cast<std::size_t>(m) * op.DofCount() + iV] += deriv * rows.dv;
+            if (top != nullptr) {
+              const int iW = top->Dof(g);
+              if (iW >= 0) {
+                bt[static_cast<std::size_t>(m) * top->DofCount() + iW] += v * rows.w;
+                bt[static_cast<std::size_t>(m) * top->DofCount() + iW] += deriv * rows.dw;
+              }
+            }
+          }
+        }
+      }
+      sph[l] = std::move(b);
+      tor[l] = std::move(bt);
+    }
+  }
+
+  Solutions SolveForces(const std::vector<std::vector<C>>& sphF, const std::vector<std::vector<C>>& torF,
+                        const Flavour& f) const {
+    const int L = options_.lmax;
+    Solutions x;
+    x.sph.assign(L + 1, {});
+    x.tor.assign(L + 1, {});
+#pragma omp parallel for schedule(dynamic)
+    for (int t = 0; t < 2 * L + 1; ++t) {
+      if (t <= L) {
+        const int l = L - t;
+        x.sph[l] = SolveComplex(f.sphF[l], sphF[l], l + 1);
+      } else {
+        const int l = 2 * L + 1 - t;
+        x.tor[l] = SolveComplex(f.torF[l], torF[l], l + 1);
+      }
+    }
+    return x;
+  }
+
+  Solutions SolveAll(const Spectral& analysed, const Flavour& f) const {
+    std::vector<std::vector<C>> sph, tor;
+    Forces(analysed, f, sph, tor);
+    return SolveForces(sph, tor, f);
+  }
+
+  // x += sigma_lm K^-1 Load (AddUnitChannels, the load channel alone).
+  void AddLoad(Solutions& x, const Flavour& f, const C* load) const {
+    if (load == nullptr) return;
+    for (int l = 0; l <= options_.lmax; ++l) {
+      const int ndof = f.sph[l]->DofCount();
+      for (int m = 0; m <= l; ++m) {
+        const C a = load[OGrid::Index(l, m)];
+        if (a == C{}) continue;
+        for (int d = 0; d < ndof; ++d) x.sph[l][static_cast<std::size_t>(m) * ndof + d] += a * f.units[l][d];
+      }
+    }
+  }
+
+  std::unique_ptr<Flavour> BuildFlavour(const PointShear& shear) const {
+    auto f = std::make_unique<Flavour>();
+    f->shear = shear;
+    const int L = options_.lmax;
+    f->sph.resize(L + 1);
+    f->tor.resize(L + 1);
+    f->sphF.resize(L + 1);
+    f->torF.resize(L + 1);
+    f->units.resize(L + 1);
+#pragma omp parallel for schedule(dynamic)
+    for (int l = 0; l <= L; ++l) {
+      f->sph[l] = std::make_unique<DegreeOperator>(reference_.nodal, l, options_.eps, &f->shear);
+      f->sphF[l] = FactorSpheroidal(*f->sph[l]);
+      const auto load = f->sph[l]->Load();
+      std::vector<C> b(load.begin(), load.end());
+      const auto x = SolveComplex(f->sphF[l], b, 1);
+      f->units[l].resize(x.size());
+      for (std::size_t i = 0; i < x.size(); ++i) f->units[l][i] = x[i].real();
+      if (l >= 1) {
+        f->tor[l] = std::make_unique<ToroidalOperator>(reference_.nodal, l, options_.eps, &f->shear);
+        f->torF[l] = FactorToroidal(*f->tor[l]);
+      }
+    }
+    return f;
+  }
+
+  const Flavour& FlavourOf(Scheme scheme, double dt) {
+    for (auto& [key, f] : flavours_)
+      if (key.first == static_cast<int>(scheme) && key.second == dt) return *f;
+    flavours_.emplace_back(std::make_pair(static_cast<int>(scheme), dt), BuildFlavour(reference_.StepShear(scheme, dt)));
+    return *flavours_.back().second;
+  }
+
+  static double RelativeChange(const Spectral& next, const Spectral& now) {
+    double scale = 0.0, diff = 0.0;
+    bool finite = true;
+    for (int b = 0; b < 3; ++b) {
+      const auto& nv = b == 0 ? next.c0 : b == 1 ? next.c1 : next.r;
+      const auto& ov = b == 0 ? now.c0 : b == 1 ? now.c1 : now.r;
+      for (std::size_t i = 0; i < nv.size(); ++i) {
+        finite = finite && std::isfinite(nv[i].real()) && std::isfinite(nv[i].imag());
+        scale = std::max(scale, std::norm(nv[i]));
+        diff = std::max(diff, std::norm(nv[i] - ov[i]));
+      }
+    }
+    if (!finite) return std::numeric_limits<double>::quiet_NaN();
+    return scale > 0.0 ? std::sqrt(diff) / std::sqrt(scale) : 0.0;
+  }
+
+  // SolveElastic + StrainCoefficients: the start strain under the memory and
+  // the load channel at the state's time, through the unrelaxed operators.
+  Spectral ElasticStrainCoefficients(const State& state, const C* load) const {
+    Tensor combined = ZeroTensor();
+    const auto fs = grid_.FieldSize();
+    for (std::size_t k = 0; k < state.m.size(); ++k) {
+      for (int node = 0; node < NodeCount(); ++node) {
+        const double mu = MuBranch(k, node);
+        if (mu == 0.0) continue;
+        for (std::size_t i = node * fs; i < (node + 1) * fs; ++i) {
+          combined.c0[i] += mu * state.m[k].c0[i];
+          combined.c1[i] += mu * state.m[k].c1[i];
+          combined.r[i] += mu * state.m[k].r[i];
+        }
+      }
+    }
+    Spectral weighted = ZeroSpectral();
+    Analyse(combined, weighted);
+    auto solutions = SolveAll(weighted, *elastic_);
+    AddLoad(solutions, *elastic_, load);
+    return StrainOf(solutions, *elastic_);
+  }
+
+  double MuBranch(std::size_t k, int node) const {
+    const auto& nd = nodes_[node];
+    return reference_.pointMu[k][static_cast<std::size_t>(nd.element) * reference_.points.count + nd.q];
+  }
+  double ItauRef(std::size_t k, int node) const {
+    const auto& nd = nodes_[node];
+    return reference_.pointItau[k][static_cast<std::size_t>(nd.element) * reference_.points.count + nd.q];
+  }
+
+  // One stage: StartStep, Converge(Respond + AddChannels + StrainOf), Finish.
+  State StepOnce(const State& state, double dt, Scheme scheme, const C* loadStart, const C* loadEnd,
+                 Info& info, Solutions& solutionsOut) {
+    const auto& flavour = FlavourOf(scheme, dt);
+    const auto fs = grid_.FieldSize();
+    const std::size_t K = state.m.size();
+    // The start strain.
+    Spectral s0;
+    if (state.strainCoefficients.has_value()) {
+      s0 = *state.strainCoefficients;
+    } else if (state.strain.has_value()) {
+      s0 = ZeroSpectral();
+      Analyse(*state.strain, s0);
+    } else {
+      s0 = ElasticStrainCoefficients(state, loadStart);
+    }
+    Tensor made;
+    if (!state.strain.has_value()) {
+      made = ZeroTensor();
+      Synthesise(s0, made);
+    }
+    const Tensor& d0 = state.strain.has_value() ? *state.strain : made;
+    // Weights, decayed memory, lateral weight and the fixed memory force.
+    std::vector<Tensor> memory(K, ZeroTensor());
+    std::vector<std::vector<double>> beta(K, std::vector<double>(d0.r.size()));
+    std::vector<double> weight(d0.r.size(), 0.0);
+    Tensor fixed = ZeroTensor();
+    for (std::size_t k = 0; k < K; ++k) {
+      for (int node = 0; node < NodeCount(); ++node) {
+        const double itauRef = ItauRef(k, node);
+        const double refBeta = scheme == Scheme::BackwardEuler ? 1.0 - BackwardEulerWeight(dt * itauRef)
+                                                               : ExponentialTrapezoidWeights(dt * itauRef).beta;
+        const double mu = MuBranch(k, node);
+        for (std::size_t at = node * fs; at < (node + 1) * fs; ++at) {
+          const double h = dt * (itauRef * factor_[at]);
+          double e_w, a_w, b_w;
+          if (scheme == Scheme::BackwardEuler) {
+            const double wbe = BackwardEulerWeight(h);
+            e_w = wbe;
+            a_w = 0.0;
+            b_w = 1.0 - wbe;
+          } else {
+            const auto tw = ExponentialTrapezoidWeights(h);
+            e_w = tw.e;
+            a_w = tw.alpha;
+            b_w = tw.beta;
+          }
+          beta[k][at] = b_w;
+          memory[k].c0[at] = e_w * state.m[k].c0[at] + a_w * d0.c0[at];
+          memory[k].c1[at] = e_w * state.m[k].c1[at] + a_w * d0.c1[at];
+          memory[k].r[at] = e_w * state.m[k].r[at] + a_w * d0.r[at];
+          if (k == 0) {
+            weight[at] = 0.0 + mu * (b_w - refBeta);
+            fixed.c0[at] = C{} + mu * memory[k].c0[at];
+            fixed.c1[at] = C{} + mu * memory[k].c1[at];
+            fixed.r[at] = 0.0 + mu * memory[k].r[at];
+            continue;
+          }
+          if (mu == 0.0) continue;
+          weight[at] += mu * (b_w - refBeta);
+          fixed.c0[at] += mu * memory[k].c0[at];
+          fixed.c1[at] += mu * memory[k].c1[at];
+          fixed.r[at] += mu * memory[k].r[at];
+        }
+      }
+    }
+    Spectral fixedS = ZeroSpectral();
+    Analyse(fixed, fixedS);
+    // Respond: synthesise, weight, analyse, add the fixed force, solve.
+    Tensor grid = ZeroTensor();
+    Spectral analysed = ZeroSpectral();
+    auto respond = [&](const Spectral& strain) {
+      Synthesise(strain, grid);
+      for (std::size_t i = 0; i < weight.size(); ++i) {
+        grid.c0[i] *= weight[i];
+        grid.c1[i] *= weight[i];
+        grid.r[i] *= weight[i];
+      }
+      Analyse(grid, analysed);
+      for (std::size_t i = 0; i < analysed.c0.size(); ++i) analysed.c0[i] += fixedS.c0[i];
+      for (std::size_t i = 0; i < analysed.c1.size(); ++i) analysed.c1[i] += fixedS.c1[i];
+      for (std::size_t i = 0; i < analysed.r.size(); ++i) analysed.r[i] += fixedS.r[i];
+      return SolveAll(analysed, flavour);
+    };
+    // The load channel at the stage's end time.
+    Solutions solutions;
+    auto pass = [&](const Spectral& s) {
+      solutions = respond(s);
+      AddLoad(solutions, flavour, loadEnd);
+      return StrainOf(solutions, flavour);
+    };
+    // Converge (Viscoelastic3D.cpp:1916-1974).
+    Spectral s = s0;
+    info = Info{};
+    const bool adaptive = options_.anderson_rate > 0.0;
+    std::optional<Mixer> mixer;
+    if (options_.anderson_memory > 0 && !adaptive) mixer.emplace(options_.anderson_memory);
+    double previous = 0.0;
+    for (int iteration = 0; iteration < options_.max_iterations; ++iteration) {
+      Spectral next = pass(s);
+      info.iterations = iteration + 1;
+      info.residual = RelativeChange(next, s);
+      if (!std::isfinite(info.residual)) break;
+      if (info.residual <= options_.rtol) {
+        info.converged = true;
+        s = std::move(next);
+        break;
+      }
+      if (options_.damping != 1.0) {
+        auto damp = [&](std::vector<C>& nv, const std::vector<C>& ov) {
+          for (std::size_t i = 0; i < nv.size(); ++i) nv[i] = ov[i] + options_.damping * (nv[i] - ov[i]);
+        };
+        damp(next.c0, s.c0);
+        damp(next.c1, s.c1);
+        damp(next.r, s.r);
+      }
+      if (adaptive && !mixer && options_.anderson_memory > 0 && iteration > 0 &&
+          info.residual > options_.anderson_rate * previous)
+        mixer.emplace(options_.anderson_memory);
+      previous = info.residual;
+      if (mixer) {
+        mixer->Update({reinterpret_cast<double*>(s.c0.data()), reinterpret_cast<double*>(s.c1.data()),
+                       reinterpret_cast<double*>(s.r.data())},
+                      {reinterpret_cast<const double*>(next.c0.data()), reinterpret_cast<const double*>(next.c1.data()),
+                       reinterpret_cast<const double*>(next.r.data())},
+                      {2 * s.c0.size(), 2 * s.c1.size(), 2 * s.r.size()});
+        ++info.mixedPasses;
+      } else {
+        s = std::move(next);
+      }
+    }
+    // Finish: synthesise the strain and advance the memory.
+    State out;
+    out.t = state.t + dt;
+    Tensor d = ZeroTensor();
+    Synthesise(s, d);
+    for (std::size_t k = 0; k < K; ++k) {
+      auto& mk = memory[k];
+      for (std::size_t i = 0; i < mk.r.size(); ++i) {
+        mk.c0[i] += beta[k][i] * d.c0[i];
+        mk.c1[i] += beta[k][i] * d.c1[i];
+        mk.r[i] += beta[k][i] * d.r[i];
+      }
+      out.m.push_back(std::move(mk));
+    }
+    out.strain = std::move(d);
+    out.strainCoefficients = std::move(s);
+    solutionsOut = std::move(solutions);
+    return out;
+  }
+
+  // Step (Viscoelastic3D.cpp:1982-2030): one stage, or Sdirk2's two backward
+  // Euler stages of gamma dt, the second from (1 - r) m_n + r Y_1.
+  State Step(const State& state, double dt, Scheme scheme, const C* load0, const C* load1, Info& info) {
+    if (scheme != Scheme::Sdirk2 || dt == 0.0) {
+      const Scheme one = scheme == Scheme::Sdirk2 ? Scheme::BackwardEuler : scheme;
+      return StepOnce(state, dt, one, load0, load1, info, last_);
+    }
+    const double gamma = kSdirk2Gamma;
+    const double h = gamma * dt;
+    const auto size = grid_.RealSize();
+    std::vector<C> loadMid;
+    const C* mid = nullptr;
+    if (load0 != nullptr || load1 != nullptr) {
+      loadMid.assign(size, C{});
+      for (std::size_t i = 0; i < size; ++i)
+        loadMid[i] = (1.0 - gamma) * (load0 ? load0[i] : C{}) + gamma * (load1 ? load1[i] : C{});
+      mid = loadMid.data();
+    }
+    Info i1, i2;
+    State y1 = StepOnce(state, h, Scheme::BackwardEuler, load0, mid, i1, last_);
+    const double r = (1.0 - gamma) / gamma;
+    State from;
+    from.t = state.t + (1.0 - gamma) * dt;
+    for (std::size_t k = 0; k < state.m.size(); ++k) {
+      Tensor t = ZeroTensor();
+      for (std::size_t i = 0; i < t.r.size(); ++i) {
+        t.c0[i] = C{} + (1.0 - r) * state.m[k].c0[i];
+        t.c0[i] += r * y1.m[k].c0[i];
+        t.c1[i] = C{} + (1.0 - r) * state.m[k].c1[i];
+        t.c1[i] += r * y1.m[k].c1[i];
+        t.r[i] = 0.0 + (1.0 - r) * state.m[k].r[i];
+        t.r[i] += r * y1.m[k].r[i];
+      }
+      from.m.push_back(std::move(t));
+    }
+    from.strain = y1.strain;
+    from.strainCoefficients = y1.strainCoefficients;
+    State out = StepOnce(from, h, Scheme::BackwardEuler, mid, load1, i2, last_);
+    out.t = state.t + dt;
+    info.iterations = i1.iterations + i2.iterations;
+    info.mixedPasses = i1.mixedPasses + i2.mixedPasses;
+    info.residual = i2.residual;
+    info.converged = i1.converged && i2.converged;
+    return out;
+  }
+
+  // Surface (Viscoelastic3D.cpp:2032-2051): U, V or phi at the surface node.
+  void Surface(int component, C* out) const {
+    const int L = options_.lmax;
+    for (int l = 0; l <= L; ++l) {
+      const auto& op = *elastic_->sph[l];
+      const int dof = op.SurfaceDof(component);
+      for (int m = 0; m <= l; ++m)
+        out[OGrid::Index(l, m)] = dof >= 0 && !last_.sph.empty() ? last_.sph[l][static_cast<std::size_t>(m) * op.DofCount() + dof] : C{};
+    }
+  }
+
+  const Solutions& Last() const { return last_; }
+
+ private:
+  sl3dgpu_v3d_options options_;
+  LayeredEarth earth_;
+  RadialMesh mesh_;
+  Material material_;
+  Rheology rheology_;
+  ReferenceRheology reference_;
+  OGrid grid_;
+  std::vector<Node> nodes_;
+  std::vector<int> firstNode_;
+  std::vector<double> factor_;  // exp(-delta) per grid value
+  std::unique_ptr<Flavour> elastic_;
+  std::vector<std::pair<std::pair<int, double>, std::unique_ptr<Flavour>>> flavours_;
+  Solutions last_;
+};
+
+}  // namespace oracle
+
+// -- the C interface -----------------------------------------------------------------------------------
+
+using oracle::C;
+
+struct oracle_v3d {
+  std::unique_ptr<oracle::Viscoelastic3D> op;
+};
+struct oracle_state {
+  oracle::State s;
+};
+
+extern "C" {
+
+oracle_v3d* oracle_v3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options* options) {
+  auto h = new oracle_v3d;
+  h->op = std::make_unique<oracle::Viscoelastic3D>(layers, nlayers, *options);
+  return h;
+}
+
+void oracle_v3d_destroy(oracle_v3d* h) { delete h; }
+
+int oracle_v3d_node_count(const oracle_v3d* h) { return h->op->NodeCount(); }
+
+void oracle_v3d_nodes(const oracle_v3d* h, double* radius, int* element) {
+  const auto& nodes = h->op->Nodes();
+  for (std::size_t i = 0; i < nodes.size(); ++i) {
+    if (radius) radius[i] = nodes[i].r;
+    if (element) element[i] = nodes[i].element;
+  }
+}
+
+void oracle_v3d_grid(const oracle_v3d* h, int* ntheta, int* nphi, double* theta, double* weights) {
+  const auto& g = h->op->Grid();
+  if (ntheta) *ntheta = g.ntheta;
+  if (nphi) *nphi = g.nphi;
+  if (theta) std::memcpy(theta, g.theta.data(), g.theta.size() * sizeof(double));
+  if (weights) std::memcpy(weights, g.w.data(), g.w.size() * sizeof(double));
+}
+
+double oracle_v3d_time_scale(const oracle_v3d* h) { return h->op->ModelScales().time; }
+double oracle_v3d_surface_density_scale(const oracle_v3d* h) { return h->op->ModelScales().SurfaceDensity(); }
+
+void oracle_v3d_set_delta(oracle_v3d* h, const double* samples) { h->op->SetDelta(samples); }
+
+oracle_state* oracle_v3d_zero_state(const oracle_v3d* h) {
+  auto s = new oracle_state;
+  s->s = h->op->ZeroState();
+  return s;
+}
+
+void oracle_v3d_free_state(oracle_state* s) { delete s; }
+
+int oracle_v3d_step(oracle_v3d* h, oracle_state* state, double dt, int scheme, const double* load0,
+                    const double* load1, sl3dgpu_step_info* info) {
+  oracle::Info i;
+  try {
+    state->s = h->op->Step(state->s, dt, static_cast<sl3dgpu::host::Scheme>(scheme),
+                           reinterpret_cast<const C*>(load0), reinterpret_cast<const C*>(load1), i);
+  } catch (const std::exception&) {
+    return -3;
+  }
+  if (info) {
+    info->iterations = i.iterations;
+    info->residual = i.residual;
+    info->converged = i.converged ? 1 : 0;
+    info->mixed_passes = i.mixedPasses;
+  }
+  return 0;
+}
+
+void oracle_v3d_surface(const oracle_v3d* h, int component, double* out) {
+  h->op->Surface(component, reinterpret_cast<C*>(out));
+}
+
+// The state's strain coefficients (reference layouts, node-major): spin -2,
+// spin -1, real spin 0 blocks end to end.
+int oracle_v3d_state_strain(const oracle_state* s, double* out) {
+  if (!s->s.strainCoefficients) return -1;
+  const auto& sc = *s->s.strainCoefficients;
+  C* o = reinterpret_cast<C*>(out);
+  o = std::copy(sc.c0.begin(), sc.c0.end(), o);
+  o = std::copy(sc.c1.begin(), sc.c1.end(), o);
+  std::copy(sc.r.begin(), sc.r.end(), o);
+  return 0;
+}
+
+}  // extern "C"
+
+extern "C" int oracle_standard_earth(int elements, double kelvin_fraction, double kelvin_div,
+                                     sl3dgpu_layer* out) {
+  const auto layers = sl3dgpu::host::StandardEarthLayers(elements, kelvin_fraction, kelvin_div);
+  for (std::size_t i = 0; i < layers.size(); ++i) {
+    const auto& L = layers[i];
+    out[i] = sl3dgpu_layer{L.r0, L.r1, L.fluid ? 1 : 0, L.elements, L.rho0, L.rho1, L.kappa0, L.kappa1,
+                           L.mu0, L.mu1, L.viscosity, L.kelvin_fraction, L.kelvin_viscosity};
+  }
+  return static_cast<int>(layers.size());
+}

@@ -94,7 +94,7 @@ __global__ void WignerTableKernel(int lmax, int N, int ntheta, const double* the
 constexpr int kBM = 64, kBN = 64, kBK = 16;
 
 __global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, const double* A,
-                                                     const double* B, double* C) {
+                                                     const double* B, double* C, bool accumulate) {
   const GemmItem it = items[blockIdx.z];
   const int i0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
   if (i0 >= it.M || n0 >= it.N) return;
@@ -148,7 +148,9 @@ __global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, cons
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int n = n0 + tx + 16 * q;
-      if (n < it.N) c[static_cast<long long>(i) * it.ldc + n] = acc[r][q];
+      if (n >= it.N) continue;
+      double* out = c + static_cast<long long>(i) * it.ldc + n;
+      *out = accumulate ? acc[r][q] + *out : acc[r][q];
     }
   }
 }
@@ -223,76 +225,98 @@ __device__ int StockhamFft(double2* buf0, double2* buf1, int groups, const FftPl
 
 constexpr int kRingGroup = 4;  // rings (fields at one colatitude) per CTA
 
-// Spectra [mIndex][j][count] -> fields [count][j][k]: rings (p0..p0+G, j).
-__global__ void RingSynthesisKernel(int lmax, int ntheta, int count, bool real, FftPlan plan,
-                                    const double2* tw, const double2* spectra, void* fields) {
-  extern __shared__ double2 smem[];
-  const int n = plan.n;
-  double2* buf0 = smem;
-  double2* buf1 = smem + kRingGroup * n;
-  const int j = blockIdx.y;
-  const int p0 = blockIdx.x * kRingGroup;
-  const int groups = min(kRingGroup, count - p0);
-  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) buf0[e] = make_double2(0.0, 0.0);
+// Ring modes: spectra -> fields; fields (times an optional weight) ->
+// spectra; spectra -> fields -> weight -> spectra without leaving shared
+// memory.
+enum RingMode { kRingSynth = 0, kRingAnalyse = 1, kRingWeighted = 2 };
+
+__device__ void LoadSpectrum(double2* buf, int n, int groups, int lmax, int ntheta, int count, int j,
+                             int p0, bool real, const double2* spectra) {
+  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) buf[e] = make_double2(0.0, 0.0);
   __syncthreads();
   const int mcount = real ? lmax + 1 : 2 * lmax + 1;
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
-    double2 v = spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
+    const double2 v = spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
     if (real) {
       if (m == 0) {
-        buf0[g * n] = make_double2(v.x, 0.0);
+        buf[g * n] = make_double2(v.x, 0.0);
       } else {
-        buf0[g * n + m] = v;
-        buf0[g * n + n - m] = make_double2(v.x, -v.y);
+        buf[g * n + m] = v;
+        buf[g * n + n - m] = make_double2(v.x, -v.y);
       }
     } else {
-      buf0[g * n + ((m % n) + n) % n] = v;
+      buf[g * n + ((m % n) + n) % n] = v;
     }
   }
   __syncthreads();
-  const int where = StockhamFft(buf0, buf1, groups, plan, tw, +1);
-  const double2* res = where == 0 ? buf0 : buf1;
-  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
-    const int g = e / n, k = e % n;
-    const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
-    if (real)
-      static_cast<double*>(fields)[at] = res[e].x;
-    else
-      static_cast<double2*>(fields)[at] = res[e];
-  }
 }
 
-// Fields [count][j][k] -> spectra [mIndex][j][count], scaled by (2 pi / n) w_j.
-__global__ void RingAnalysisKernel(int lmax, int ntheta, int count, bool real, FftPlan plan,
-                                   const double2* tw, const double* weights, const void* fields,
-                                   double2* spectra) {
-  extern __shared__ double2 smem[];
-  const int n = plan.n;
-  double2* buf0 = smem;
-  double2* buf1 = smem + kRingGroup * n;
-  const int j = blockIdx.y;
-  const int p0 = blockIdx.x * kRingGroup;
-  const int groups = min(kRingGroup, count - p0);
-  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
-    const int g = e / n, k = e % n;
-    const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
-    buf0[e] = real ? make_double2(static_cast<const double*>(fields)[at], 0.0)
-                   : static_cast<const double2*>(fields)[at];
-  }
-  __syncthreads();
-  const int where = StockhamFft(buf0, buf1, groups, plan, tw, -1);
-  const double2* res = where == 0 ? buf0 : buf1;
-  const double scale = 2.0 * 3.14159265358979323846 / n * weights[j];
+__device__ void StoreSpectrum(const double2* res, int n, int groups, int lmax, int ntheta, int count,
+                              int j, int p0, bool real, double scale, double2* spectra) {
   const int mcount = real ? lmax + 1 : 2 * lmax + 1;
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
     const double2 v = res[g * n + ((m % n) + n) % n];
-    spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] =
-        make_double2(v.x * scale, v.y * scale);
+    spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = make_double2(v.x * scale, v.y * scale);
   }
+}
+
+__global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan,
+                           const double2* tw, const double* weights, const double2* spectraIn,
+                           const void* fieldsIn, const double* pointWeight, void* fieldsOut,
+                           double2* spectraOut) {
+  extern __shared__ double2 smem[];
+  const int n = plan.n;
+  double2* buf0 = smem;
+  double2* buf1 = smem + kRingGroup * n;
+  const int j = blockIdx.y;
+  const int p0 = blockIdx.x * kRingGroup;
+  const int groups = min(kRingGroup, count - p0);
+  double2* res = buf0;
+  if (mode == kRingSynth || mode == kRingWeighted) {
+    LoadSpectrum(buf0, n, groups, lmax, ntheta, count, j, p0, real, spectraIn);
+    res = StockhamFft(buf0, buf1, groups, plan, tw, +1) == 0 ? buf0 : buf1;
+    if (mode == kRingSynth) {
+      for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
+        const int g = e / n, k = e % n;
+        const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
+        if (real)
+          static_cast<double*>(fieldsOut)[at] = res[e].x;
+        else
+          static_cast<double2*>(fieldsOut)[at] = res[e];
+      }
+      return;
+    }
+    // the pointwise weight on the synthesised values (a real field's
+    // imaginary part is dropped, as its synthesis does)
+    for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
+      const int g = e / n, k = e % n;
+      const double w = pointWeight[(static_cast<long long>(p0 + g) * ntheta + j) * n + k];
+      const double2 v = res[e];
+      res[e] = real ? make_double2(v.x * w, 0.0) : make_double2(v.x * w, v.y * w);
+    }
+    __syncthreads();
+  } else {
+    for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
+      const int g = e / n, k = e % n;
+      const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
+      double2 v = real ? make_double2(static_cast<const double*>(fieldsIn)[at], 0.0)
+                       : static_cast<const double2*>(fieldsIn)[at];
+      if (pointWeight != nullptr) {
+        const double w = pointWeight[at];
+        v = make_double2(v.x * w, v.y * w);
+      }
+      buf0[e] = v;
+    }
+    __syncthreads();
+  }
+  double2* other = res == buf0 ? buf1 : buf0;
+  const double2* out = StockhamFft(res, other, groups, plan, tw, -1) == 0 ? res : other;
+  const double scale = 2.0 * 3.14159265358979323846 / n * weights[j];
+  StoreSpectrum(out, n, groups, lmax, ntheta, count, j, p0, real, scale, spectraOut);
 }
 
 // -- layout permutations -------------------------------------------------------------------
@@ -432,7 +456,7 @@ Grid::~Grid() {
   cudaFree(dTheta);
   cudaFree(dWeights);
   cudaFree(dTwiddle);
-  cudaFree(dItems_);
+  for (auto& [key, b] : batches_) cudaFree(b.items);
   cudaFree(scratchSpectra_);
   cudaFree(scratchCoeffs_);
   for (auto& [N, t] : tables_) {
@@ -470,112 +494,127 @@ int Grid::Table(int N, const SpinTable** out) {
   return SL3DGPU_OK;
 }
 
-int Grid::RunGemm(const double* A, const double* B, double* C, cudaStream_t stream) {
-  if (items_.empty()) return SL3DGPU_OK;
-  if (items_.size() > dItemsCapacity_) {
-    cudaFree(dItems_);
-    dItems_ = nullptr;
-    dItemsCapacity_ = 0;
-    SL3D_CUDA(cudaMalloc(&dItems_, items_.size() * sizeof(GemmItem)));
-    dItemsCapacity_ = items_.size();
+int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, const Batch** out) {
+  const std::array<long long, 6> key{N, real, analysis, P, p0, count};
+  auto found = batches_.find(key);
+  if (found != batches_.end()) {
+    *out = &found->second;
+    return SL3DGPU_OK;
   }
-  SL3D_CUDA(cudaMemcpyAsync(dItems_, items_.data(), items_.size() * sizeof(GemmItem),
-                            cudaMemcpyHostToDevice, stream));
-  int maxM = 0, maxN = 0;
-  for (const auto& it : items_) {
-    maxM = std::max(maxM, it.M);
-    maxN = std::max(maxN, it.N);
-  }
-  dim3 grid((maxM + kBM - 1) / kBM, (maxN + kBN - 1) / kBN, static_cast<unsigned>(items_.size()));
-  GemmF64Kernel<<<grid, 256, 0, stream>>>(dItems_, A, B, C);
-  SL3D_CHECK_LAUNCH();
-  // The item list is host memory the copy reads: finish before it changes.
-  SL3D_CUDA(cudaStreamSynchronize(stream));
-  return SL3DGPU_OK;
-}
-
-int Grid::LegendreSynthesis(int N, bool real, const double* coeffs, int count, double* spectra,
-                            cudaStream_t stream) {
   const SpinTable* t = nullptr;
   if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
-  items_.clear();
+  std::vector<GemmItem> items;
   const int mlo = real ? 0 : -lmax;
   const long long base = real ? t->rowOffset[lmax] : 0;
-  for (int m = mlo; m <= lmax; ++m) {
-    const int rows = t->Rows(m, lmax);
-    const int mi = m - mlo;
-    GemmItem it{};
-    it.M = ntheta;
-    it.N = 2 * count;
-    it.K = rows;
-    it.a = static_cast<long long>(t->rowOffset[m + lmax]) * ntheta;
-    it.b = (t->rowOffset[m + lmax] - base) * 2LL * count;
-    it.c = static_cast<long long>(mi) * ntheta * 2LL * count;
-    it.sAi = 1;
-    it.sAk = ntheta;
-    it.ldb = 2 * count;
-    it.ldc = 2 * count;
-    if (rows == 0) {
-      SL3D_CUDA(cudaMemsetAsync(spectra + it.c, 0, sizeof(double) * ntheta * 2 * count, stream));
-      continue;
-    }
-    items_.push_back(it);
-  }
-  return RunGemm(t->values, coeffs, spectra, stream);
-}
-
-int Grid::LegendreAnalysis(int N, bool real, const double* spectra, int count, double* coeffs,
-                           cudaStream_t stream) {
-  const SpinTable* t = nullptr;
-  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
-  items_.clear();
-  const int mlo = real ? 0 : -lmax;
-  const long long base = real ? t->rowOffset[lmax] : 0;
+  Batch b;
   for (int m = mlo; m <= lmax; ++m) {
     const int rows = t->Rows(m, lmax);
     if (rows == 0) continue;
     const int mi = m - mlo;
     GemmItem it{};
-    it.M = rows;
-    it.N = 2 * count;
-    it.K = ntheta;
-    it.a = static_cast<long long>(t->rowOffset[m + lmax]) * ntheta;
-    it.b = static_cast<long long>(mi) * ntheta * 2LL * count;
-    it.c = (t->rowOffset[m + lmax] - base) * 2LL * count;
-    it.sAi = ntheta;
-    it.sAk = 1;
-    it.ldb = 2 * count;
-    it.ldc = 2 * count;
-    items_.push_back(it);
+    if (!analysis) {
+      it.M = ntheta;
+      it.N = 2 * count;
+      it.K = rows;
+      it.a = static_cast<long long>(t->rowOffset[m + lmax]) * ntheta;
+      it.b = (t->rowOffset[m + lmax] - base) * 2LL * P + 2LL * p0;
+      it.c = static_cast<long long>(mi) * ntheta * 2LL * count;
+      it.sAi = 1;
+      it.sAk = ntheta;
+      it.ldb = 2 * P;
+      it.ldc = 2 * count;
+    } else {
+      it.M = rows;
+      it.N = 2 * count;
+      it.K = ntheta;
+      it.a = static_cast<long long>(t->rowOffset[m + lmax]) * ntheta;
+      it.b = static_cast<long long>(mi) * ntheta * 2LL * count;
+      it.c = (t->rowOffset[m + lmax] - base) * 2LL * P + 2LL * p0;
+      it.sAi = ntheta;
+      it.sAk = 1;
+      it.ldb = 2 * count;
+      it.ldc = 2 * P;
+    }
+    b.maxM = std::max(b.maxM, it.M);
+    b.maxN = std::max(b.maxN, it.N);
+    items.push_back(it);
   }
-  return RunGemm(t->values, spectra, coeffs, stream);
+  b.count = static_cast<int>(items.size());
+  if (b.count > 0) {
+    SL3D_CUDA(cudaMalloc(&b.items, items.size() * sizeof(GemmItem)));
+    SL3D_CUDA(cudaMemcpy(b.items, items.data(), items.size() * sizeof(GemmItem), cudaMemcpyHostToDevice));
+  }
+  *out = &batches_.emplace(key, b).first->second;
+  return SL3DGPU_OK;
 }
+
+int Grid::RunGemm(const Batch& b, const double* A, const double* B, double* C, bool accumulate,
+                  cudaStream_t stream) {
+  if (b.count == 0) return SL3DGPU_OK;
+  dim3 grid((b.maxM + kBM - 1) / kBM, (b.maxN + kBN - 1) / kBN, static_cast<unsigned>(b.count));
+  GemmF64Kernel<<<grid, 256, 0, stream>>>(b.items, A, B, C, accumulate);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Grid::LegendreSynthesis(int N, bool real, const double* coeffs, int P, int p0, int count,
+                            double* spectra, cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const SpinTable* t = nullptr;
+  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+  const Batch* b = nullptr;
+  if (int st = BatchFor(N, real, false, P, p0, count, &b); st != SL3DGPU_OK) return st;
+  // orders without degrees (|N| > lmax) leave their spectra zero
+  const int mlo = real ? 0 : -lmax;
+  for (int m = mlo; m <= lmax; ++m)
+    if (t->Rows(m, lmax) == 0)
+      SL3D_CUDA(cudaMemsetAsync(spectra + static_cast<long long>(m - mlo) * ntheta * 2LL * count, 0,
+                                sizeof(double) * ntheta * 2 * count, stream));
+  return RunGemm(*b, t->values, coeffs, spectra, false, stream);
+}
+
+int Grid::LegendreAnalysis(int N, bool real, const double* spectra, int P, int p0, int count,
+                           double* coeffs, bool accumulate, cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const SpinTable* t = nullptr;
+  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+  const Batch* b = nullptr;
+  if (int st = BatchFor(N, real, true, P, p0, count, &b); st != SL3DGPU_OK) return st;
+  return RunGemm(*b, t->values, spectra, coeffs, accumulate, stream);
+}
+
+namespace {
+int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spectraIn,
+               const void* fieldsIn, const double* weight, void* fieldsOut, double* spectraOut,
+               cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const size_t smem = 2 * kRingGroup * static_cast<size_t>(g.nphi) * sizeof(double2);
+  SL3D_CUDA(cudaFuncSetAttribute(RingKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)));
+  dim3 grid((count + kRingGroup - 1) / kRingGroup, g.ntheta);
+  RingKernel<<<grid, 256, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
+                                          g.dWeights, reinterpret_cast<const double2*>(spectraIn),
+                                          fieldsIn, weight, fieldsOut,
+                                          reinterpret_cast<double2*>(spectraOut));
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+}  // namespace
 
 int Grid::RingSynthesis(bool real, const double* spectra, int count, double* fields,
                         cudaStream_t stream) {
-  if (count == 0) return SL3DGPU_OK;
-  const size_t smem = 2 * kRingGroup * static_cast<size_t>(nphi) * sizeof(double2);
-  SL3D_CUDA(cudaFuncSetAttribute(RingSynthesisKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem)));
-  dim3 grid((count + kRingGroup - 1) / kRingGroup, ntheta);
-  RingSynthesisKernel<<<grid, 256, smem, stream>>>(lmax, ntheta, count, real, plan, dTwiddle,
-                                                   reinterpret_cast<const double2*>(spectra), fields);
-  SL3D_CHECK_LAUNCH();
-  return SL3DGPU_OK;
+  return LaunchRing(*this, kRingSynth, real, count, spectra, nullptr, nullptr, fields, nullptr, stream);
 }
 
 int Grid::RingAnalysis(bool real, const double* fields, int count, double* spectra,
-                       cudaStream_t stream) {
-  if (count == 0) return SL3DGPU_OK;
-  const size_t smem = 2 * kRingGroup * static_cast<size_t>(nphi) * sizeof(double2);
-  SL3D_CUDA(cudaFuncSetAttribute(RingAnalysisKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem)));
-  dim3 grid((count + kRingGroup - 1) / kRingGroup, ntheta);
-  RingAnalysisKernel<<<grid, 256, smem, stream>>>(lmax, ntheta, count, real, plan, dTwiddle,
-                                                  dWeights, fields,
-                                                  reinterpret_cast<double2*>(spectra));
-  SL3D_CHECK_LAUNCH();
-  return SL3DGPU_OK;
+                       cudaStream_t stream, const double* weight) {
+  return LaunchRing(*this, kRingAnalyse, real, count, nullptr, fields, weight, nullptr, spectra, stream);
+}
+
+int Grid::RingWeighted(bool real, const double* spectraIn, int count, const double* weight,
+                       double* spectraOut, cudaStream_t stream) {
+  return LaunchRing(*this, kRingWeighted, real, count, spectraIn, nullptr, weight, nullptr, spectraOut,
+                    stream);
 }
 
 int Grid::ToDevice(int N, bool real, const double* ref, int count, double* dev,

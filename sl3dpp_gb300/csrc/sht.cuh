@@ -17,6 +17,7 @@
 // ring spectra are [m][j][count] complex.
 #pragma once
 
+#include <array>
 #include <map>
 #include <memory>
 #include <vector>
@@ -67,14 +68,31 @@ class Grid {
   long long RealRows() const { return static_cast<long long>(lmax + 1) * (lmax + 2) / 2; }
 
   // -- transforms in the device layouts -------------------------------------------
-  // Spin N: coefficients [row][count] complex -> spectra [m][j][count] -> fields
-  // [count][j][k] complex; and back. Real spin 0 likewise with m >= 0 rows.
+  // Spin N: coefficients [row][P] complex (columns p0 .. p0 + count of them
+  // taking part) -> spectra [m][j][count] -> fields [count][j][k] complex;
+  // and back. Real spin 0 likewise with m >= 0 rows. The analysis may add its
+  // result to what the coefficients hold (the memory force's fixed part).
+  int LegendreSynthesis(int N, bool real, const double* coeffs, int P, int p0, int count,
+                        double* spectra, cudaStream_t stream);
+  int LegendreAnalysis(int N, bool real, const double* spectra, int P, int p0, int count,
+                       double* coeffs, bool accumulate, cudaStream_t stream);
   int LegendreSynthesis(int N, bool real, const double* coeffs, int count, double* spectra,
-                        cudaStream_t stream);
+                        cudaStream_t stream) {
+    return LegendreSynthesis(N, real, coeffs, count, 0, count, spectra, stream);
+  }
   int LegendreAnalysis(int N, bool real, const double* spectra, int count, double* coeffs,
-                       cudaStream_t stream);
+                       cudaStream_t stream) {
+    return LegendreAnalysis(N, real, spectra, count, 0, count, coeffs, false, stream);
+  }
   int RingSynthesis(bool real, const double* spectra, int count, double* fields, cudaStream_t stream);
-  int RingAnalysis(bool real, const double* fields, int count, double* spectra, cudaStream_t stream);
+  // Optional pointwise weight (a real field over the same values) applied
+  // before the analysis.
+  int RingAnalysis(bool real, const double* fields, int count, double* spectra, cudaStream_t stream,
+                   const double* weight = nullptr);
+  // Synthesis, the pointwise weight and the analysis of each ring in one
+  // pass through shared memory: the grid values never reach HBM.
+  int RingWeighted(bool real, const double* spectraIn, int count, const double* weight,
+                   double* spectraOut, cudaStream_t stream);
 
   // Reference layout <-> device layout permutations.
   int ToDevice(int N, bool real, const double* ref, int count, double* dev, cudaStream_t stream);
@@ -85,14 +103,18 @@ class Grid {
 
  private:
   std::map<int, SpinTable> tables_;
-  std::vector<GemmItem> items_;
-  GemmItem* dItems_ = nullptr;
-  size_t dItemsCapacity_ = 0;
+  struct Batch {
+    GemmItem* items = nullptr;
+    int count = 0, maxM = 0, maxN = 0;
+  };
+  std::map<std::array<long long, 6>, Batch> batches_;
+  int BatchFor(int N, bool real, bool analysis, int P, int p0, int count, const Batch** out);
   double* scratchSpectra_ = nullptr;
   size_t scratchSpectraSize_ = 0;
   double* scratchCoeffs_ = nullptr;
   size_t scratchCoeffsSize_ = 0;
-  int RunGemm(const double* A, const double* B, double* C, cudaStream_t stream);
+  int RunGemm(const Batch& b, const double* A, const double* B, double* C, bool accumulate,
+              cudaStream_t stream);
 };
 
 // Smallest 2^a 3^b 5^c at or above n.

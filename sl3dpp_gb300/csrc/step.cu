@@ -1,0 +1,1147 @@
+// The GB300 3D quasi-static step: Viscoelastic3D's fixed-point step
+// (src/Viscoelastic3D.cpp:1223-2030) with every per-pass operation on the
+// device and the host only steering the iteration.
+//
+// A pass (Respond + AddChannels + StrainOf): the lateral force W d of the
+// iterate strain, transformed only at the memory nodes where W is not
+// identically zero (elsewhere the reference's Analyse(0) is exactly zero) --
+// Legendre synthesis, the ring FFTs with the pointwise weight fused in shared
+// memory, Legendre analysis accumulated onto the stage's fixed memory force;
+// the force assembly onto every degree's spheroidal and toroidal right-hand
+// sides; one batched band solve over every system; the load channel; the
+// strain recovery into the next iterate. The convergence measure and the
+// Anderson mixer (Gram least squares in FP64 on the device) close the loop;
+// the host reads three numbers per pass.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "host/radial.hpp"
+#include "sht.cuh"
+#include "step_kernels.cuh"
+
+namespace sl3dgpu {
+
+int BandFactorBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                    double* bands, int* pivots, int* info, int lu, cudaStream_t stream);
+int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                   const int2* devItems, int itemCount, const double* bands, const int* pivots, double* rhs,
+                   const double* scales, int lu, cudaStream_t stream);
+std::vector<int2> BandWorkItems(const sl3dgpu_band_system* hostSystems, int count);
+
+namespace {
+
+using host::Scheme;
+
+// A device allocation owned by value.
+template <class T>
+struct Dev {
+  T* p = nullptr;
+  size_t n = 0;
+  Dev() = default;
+  Dev(const Dev&) = delete;
+  Dev& operator=(const Dev&) = delete;
+  Dev(Dev&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  Dev& operator=(Dev&& o) noexcept {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+    return *this;
+  }
+  ~Dev() { cudaFree(p); }
+  cudaError_t Alloc(size_t count) {
+    cudaFree(p);
+    p = nullptr;
+    n = count;
+    return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+  }
+  cudaError_t Upload(const std::vector<T>& v) {
+    if (cudaError_t e = Alloc(v.size()); e != cudaSuccess) return e;
+    return v.empty() ? cudaSuccess : cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+
+#define SL3D_TRY(expr)                            \
+  do {                                            \
+    if (int _st = (expr); _st != SL3DGPU_OK) return _st; \
+  } while (0)
+
+// A grid tensor: the spin -2 and -1 components complex, spin 0 real.
+struct GridTensor {
+  Dev<double2> c0, c1;
+  Dev<double> r;
+  cudaError_t Alloc(size_t values) {
+    if (auto e = c0.Alloc(values); e != cudaSuccess) return e;
+    if (auto e = c1.Alloc(values); e != cudaSuccess) return e;
+    return r.Alloc(values);
+  }
+};
+
+// One flavour (scheme, dt): the factorised systems and the load units.
+struct Flavour {
+  int scheme = 0;
+  double dt = 0.0;
+  Dev<double> bands, scales, units;
+  Dev<int> pivots;
+  Dev<long long> unitOffset;
+  std::vector<sl3dgpu_band_system> sphChol, sphLu, torChol;
+  Dev<sl3dgpu_band_system> dSphChol, dSphLu, dTorChol;
+  Dev<int2> iSphChol, iSphLu, iTorChol;
+  int nSphChol = 0, nSphLu = 0, nTorChol = 0;
+};
+
+}  // namespace
+
+struct V3dState {
+  std::vector<GridTensor> m;
+  GridTensor strain;
+  Dev<double2> coeffs;
+  bool hasStrain = false;
+  bool hasCoeffs = false;
+};
+
+class Viscoelastic3DGpu {
+ public:
+  sl3dgpu_v3d_options options{};
+  std::unique_ptr<host::LayeredEarth> earth;
+  std::unique_ptr<host::RadialMesh> mesh;
+  std::unique_ptr<host::Material> material;
+  std::unique_ptr<host::Rheology> rheology;
+  std::unique_ptr<host::ReferenceRheology> reference;
+  std::unique_ptr<Grid> grid;
+  cudaStream_t stream = nullptr;
+
+  // memory nodes
+  std::vector<int> nodeElement, nodeQ, elemFirstNode, firstNode;
+  std::vector<double> nodeR;
+  int P = 0, K = 0;
+  long long fieldSize = 0, values = 0;
+  long long rows0 = 0, rows1 = 0, rowsR = 0, spectralComplex = 0;
+  int lateralFirst = 0, lateralEnd = 0;  // nodes [first, end) where the lateral weight may be non-zero
+
+  // device geometry
+  Geometry geo{};
+  Dev<int> dNodeElement, dNodeQ, dElemFirstNode, dSphMap, dTorMap;
+  Dev<double> dNodeR, dElemJac, dValue, dDeriv, dWeight;
+  Dev<DegreeInfo> dDegrees;
+  std::vector<DegreeInfo> degrees;
+  long long rhsSphComplex = 0, rhsTorComplex = 0;
+
+  // per-operator device data
+  Dev<double> factor, muBranch, itauRef;
+  std::vector<std::unique_ptr<Flavour>> flavours;  // most recent first
+  std::unique_ptr<Flavour> elastic;
+
+  // workspaces
+  Dev<double2> rhsSph, rhsTor;
+  Dev<double2> s, sNext, fixedS, analysed, analysedStart;
+  Dev<double2> spectraA, spectraB;
+  GridTensor fixedGrid, dGrid;
+  Dev<double> weight;
+  std::vector<Dev<double>> beta;
+  Dev<double2> sigma0, sigmaMid, sigma1, surfaceOut;
+  Dev<double> changePartial, changeResult;
+  double* hostResult = nullptr;  // pinned
+  static constexpr int kChangeBlocks = 1024;
+
+  // mixer
+  int mixerMemory = 0;
+  Dev<double> xPrev, fPrev, gram, gammaOut, mixPartial;
+  std::vector<Dev<double>> dG, dF;
+  Dev<double*> dGPtr, dFPtr;
+  static constexpr int kMixBlocks = 1024;
+
+  V3dState scratch;  // the second buffer set a step writes into
+
+  ~Viscoelastic3DGpu() {
+    if (hostResult) cudaFreeHost(hostResult);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt);
+  int SetDelta(const double* samples, bool onDevice);
+  int ZeroState(V3dState& st);
+  int Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1, sl3dgpu_step_info* info);
+  int Surface(int component, double* out);
+  int StrainReference(const V3dState& st, double* out);
+
+ private:
+  int AllocState(V3dState& st);
+  int BuildFlavour(const host::PointShear& shear, Flavour& f);
+  int FlavourOf(int scheme, double dt, Flavour** out);
+  int Synthesise(const double2* spectral, GridTensor& out);
+  int Analyse(const GridTensor& in, double2* spectral);
+  int AnalyseWeighted(const GridTensor& in, const double* w, double2* spectral);  // accumulate, lateral nodes
+  int WeightedPass(const double2* strain, double2* out);                           // accumulate, lateral nodes
+  int Solve(const Flavour& f);
+  int Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma, double2* next);
+  int RelativeChange(const double2* next, const double2* now, double* residual);
+  int MixerReset();
+  int MixerUpdate(int& count, int& slot, bool& first);
+  int ElasticStrain(const V3dState& st, const double2* sigma);
+  int StepOnce(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
+               const double2* sigmaEnd, sl3dgpu_step_info& info);
+  double2* Block(double2* base, int spin) const {
+    return base + (spin == -2 ? 0 : spin == -1 ? rows0 * P : (rows0 + rows1) * P);
+  }
+};
+
+// -- construction ----------------------------------------------------------------------------------
+
+int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt) {
+  options = opt;
+  if (opt.lmax < 2 || opt.ngll < 2 || !(opt.oversampling >= 1.0) || opt.anderson_memory > 8 ||
+      opt.anderson_memory < 0 || nlayers < 1) {
+    SetError("v3d: lmax >= 2, ngll >= 2, oversampling >= 1, anderson_memory in [0, 8]");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (opt.precision != 0) {
+    SetError("v3d: only the FP64 form (precision 0) is built in this library version");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  try {
+    std::vector<host::Layer> ls(nlayers);
+    for (int i = 0; i < nlayers; ++i) {
+      const auto& s = layers[i];
+      ls[i] = host::Layer{s.r0, s.r1, s.fluid != 0, s.rho0, s.rho1, s.kappa0, s.kappa1, s.mu0, s.mu1,
+                          s.viscosity, s.kelvin_fraction, s.kelvin_viscosity, s.elements};
+    }
+    earth = std::make_unique<host::LayeredEarth>(ls, host::Scales::Geophysical(layers[nlayers - 1].r1));
+    mesh = std::make_unique<host::RadialMesh>(host::RadialMesh::Create(*earth, opt.ngll));
+    material = std::make_unique<host::Material>(host::Material::Create(*earth, *mesh));
+    rheology = std::make_unique<host::Rheology>(host::Rheology::FromEarth(*earth, *material));
+    reference = std::make_unique<host::ReferenceRheology>(*rheology, true);
+  } catch (const std::exception& e) {
+    SetError(std::string("v3d: ") + e.what());
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (rheology->branches.size() > 2) {
+    SetError("v3d: at most two Prony branches");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SL3D_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  SL3D_CUDA(cudaMallocHost(&hostResult, 8 * sizeof(double)));
+  SL3D_TRY(Grid::Create(opt.lmax, 2, opt.oversampling, grid));
+  const auto& nodal = reference->nodal;
+  const auto& msh = nodal.mesh;
+  const auto& pts = reference->points;
+  const int n = msh.NGll(), E = msh.ElementCount(), L = opt.lmax;
+  K = static_cast<int>(rheology->branches.size());
+  // The memory nodes: the Gauss points of every element where a branch relaxes.
+  elemFirstNode.assign(E, -1);
+  for (int e = 0; e < E; ++e) {
+    bool carries = false;
+    for (int i = 0; i < n; ++i) carries = carries || rheology->IsActive(static_cast<size_t>(e) * n + i);
+    if (!carries) continue;
+    elemFirstNode[e] = static_cast<int>(nodeElement.size());
+    for (int p = 0; p < pts.count; ++p) {
+      nodeElement.push_back(e);
+      nodeQ.push_back(p);
+      nodeR.push_back(pts.RadiusAt(msh, e, p));
+    }
+  }
+  P = static_cast<int>(nodeElement.size());
+  if (P == 0) {
+    SetError("v3d: the rheology has no active branch anywhere");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  firstNode.assign(L + 1, P);
+  for (int l = 0; l <= L; ++l) {
+    const int fe = l > 0 ? msh.StartElement(l, opt.eps) : 0;
+    for (int p = 0; p < P; ++p)
+      if (nodeElement[p] >= fe) {
+        firstNode[l] = p;
+        break;
+      }
+  }
+  fieldSize = static_cast<long long>(grid->ntheta) * grid->nphi;
+  values = fieldSize * P;
+  rows0 = grid->SpinRows(-2);
+  rows1 = grid->SpinRows(-1);
+  rowsR = grid->RealRows();
+  spectralComplex = (rows0 + rows1 + rowsR) * P;
+  lateralFirst = 0;
+  lateralEnd = P;
+
+  // The elastic operators: the dof maps and right-hand-side layout, shared by
+  // every flavour (they depend on the mesh and the degree alone).
+  elastic = std::make_unique<Flavour>();
+  const int nglob = msh.NodeCount();
+  std::vector<int> sphMap(static_cast<size_t>(L + 1) * nglob * 2, -1), torMap(static_cast<size_t>(L + 1) * nglob, -1);
+  degrees.resize(L + 1);
+  long long sphOff = 0, torOff = 0;
+  for (int l = 0; l <= L; ++l) {
+    host::DegreeOperator op(nodal, l, opt.eps, &reference->elastic);
+    auto& d = degrees[l];
+    d.firstNode = firstNode[l];
+    d.firstGlobal = d.firstNode < P ? msh.GlobalIndex(nodeElement[d.firstNode], 0) : 0;
+    d.lastGlobal = d.firstNode < P ? msh.GlobalIndex(nodeElement[P - 1], n - 1) : -1;
+    d.sphNdof = op.DofCount();
+    d.surfaceU = op.SurfaceDof(host::kU);
+    d.surfaceV = op.SurfaceDof(host::kV);
+    d.surfacePhi = op.SurfaceDof(host::kPhi);
+    d.sphMap = static_cast<long long>(l) * nglob * 2;
+    d.torMap = static_cast<long long>(l) * nglob;
+    d.sphRhs = sphOff;
+    sphOff += static_cast<long long>(d.sphNdof) * (l + 1);
+    for (int gn = 0; gn < nglob; ++gn) {
+      sphMap[d.sphMap + 2 * gn] = op.Dof(gn, host::kU);
+      sphMap[d.sphMap + 2 * gn + 1] = op.Dof(gn, host::kV);
+    }
+    d.torNdof = 0;
+    d.torRhs = torOff;
+    if (l >= 1) {
+      host::ToroidalOperator top(nodal, l, opt.eps, &reference->elastic);
+      d.torNdof = top.DofCount();
+      torOff += static_cast<long long>(d.torNdof) * (l + 1);
+      for (int gn = 0; gn < nglob; ++gn) torMap[d.torMap + gn] = top.Dof(gn);
+    }
+  }
+  rhsSphComplex = sphOff;
+  rhsTorComplex = torOff;
+
+  std::vector<double> elemJac(E);
+  for (int e = 0; e < E; ++e) elemJac[e] = msh.Jacobian(e);
+  SL3D_CUDA(dNodeElement.Upload(nodeElement));
+  SL3D_CUDA(dNodeQ.Upload(nodeQ));
+  SL3D_CUDA(dNodeR.Upload(nodeR));
+  SL3D_CUDA(dElemFirstNode.Upload(elemFirstNode));
+  SL3D_CUDA(dElemJac.Upload(elemJac));
+  SL3D_CUDA(dValue.Upload(pts.value));
+  SL3D_CUDA(dDeriv.Upload(pts.derivative));
+  SL3D_CUDA(dWeight.Upload(pts.weight));
+  SL3D_CUDA(dDegrees.Upload(degrees));
+  SL3D_CUDA(dSphMap.Upload(sphMap));
+  SL3D_CUDA(dTorMap.Upload(torMap));
+  const SpinTable *t0 = nullptr, *t1 = nullptr, *tr = nullptr;
+  SL3D_TRY(grid->Table(-2, &t0));
+  SL3D_TRY(grid->Table(-1, &t1));
+  SL3D_TRY(grid->Table(0, &tr));
+  geo = Geometry{L, P, n, pts.count, E, dNodeElement.p, dNodeQ.p, dNodeR.p, dElemFirstNode.p, dElemJac.p,
+                 dValue.p, dDeriv.p, dWeight.p, t0->dRowOffset, t1->dRowOffset, tr->dRowOffset,
+                 rows0, rows1, rowsR, dDegrees.p, dSphMap.p, dTorMap.p};
+
+  // Branch moduli and reference inverse times at the nodes; exp(-delta) = 1.
+  std::vector<double> mu(static_cast<size_t>(K) * P), itau(static_cast<size_t>(K) * P);
+  for (int k = 0; k < K; ++k)
+    for (int p = 0; p < P; ++p) {
+      const size_t at = static_cast<size_t>(nodeElement[p]) * pts.count + nodeQ[p];
+      mu[static_cast<size_t>(k) * P + p] = reference->pointMu[k][at];
+      itau[static_cast<size_t>(k) * P + p] = reference->pointItau[k][at];
+    }
+  SL3D_CUDA(muBranch.Upload(mu));
+  SL3D_CUDA(itauRef.Upload(itau));
+  std::vector<double> ones(values, 1.0);
+  SL3D_CUDA(factor.Upload(ones));
+  lateralFirst = lateralEnd = 0;  // no lateral variation until delta is set
+
+  // workspaces
+  SL3D_CUDA(rhsSph.Alloc(rhsSphComplex));
+  SL3D_CUDA(rhsTor.Alloc(std::max<long long>(rhsTorComplex, 1)));
+  for (auto* b : {&s, &sNext, &fixedS, &analysed, &analysedStart}) SL3D_CUDA(b->Alloc(spectralComplex));
+  const size_t spectra = static_cast<size_t>(2 * L + 1) * grid->ntheta * P;
+  SL3D_CUDA(spectraA.Alloc(spectra));
+  SL3D_CUDA(spectraB.Alloc(spectra));
+  SL3D_CUDA(fixedGrid.Alloc(values));
+  SL3D_CUDA(dGrid.Alloc(values));
+  SL3D_CUDA(weight.Alloc(values));
+  beta.resize(K);
+  for (auto& b : beta) SL3D_CUDA(b.Alloc(values));
+  const size_t lm = static_cast<size_t>(L + 1) * (L + 2) / 2;
+  for (auto* b : {&sigma0, &sigmaMid, &sigma1, &surfaceOut}) SL3D_CUDA(b->Alloc(lm));
+  SL3D_CUDA(changePartial.Alloc(3 * kChangeBlocks));
+  SL3D_CUDA(changeResult.Alloc(3));
+  SL3D_TRY(AllocState(scratch));
+  SL3D_TRY(BuildFlavour(reference->elastic, *elastic));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::AllocState(V3dState& st) {
+  st.m.resize(K);
+  for (auto& t : st.m) SL3D_CUDA(t.Alloc(values));
+  SL3D_CUDA(st.strain.Alloc(values));
+  SL3D_CUDA(st.coeffs.Alloc(spectralComplex));
+  st.hasStrain = st.hasCoeffs = false;
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::ZeroState(V3dState& st) {
+  SL3D_TRY(AllocState(st));
+  for (auto& t : st.m) {
+    SL3D_CUDA(cudaMemsetAsync(t.c0.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(t.c1.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(t.r.p, 0, values * sizeof(double), stream));
+  }
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
+  std::vector<double> host(values);
+  if (onDevice)
+    SL3D_CUDA(cudaMemcpy(host.data(), samples, values * sizeof(double), cudaMemcpyDeviceToHost));
+  else
+    std::memcpy(host.data(), samples, values * sizeof(double));
+  // exp(-delta) per value (as Viscoelastic3D's constructor samples it), and
+  // the nodes where it departs from one: only there can W be non-zero.
+  int first = P, last = -1;
+  for (int p = 0; p < P; ++p) {
+    bool lateral = false;
+    for (long long x = p * fieldSize; x < (p + 1) * fieldSize; ++x) {
+      host[x] = std::exp(-host[x]);
+      lateral = lateral || host[x] != 1.0;
+    }
+    if (lateral) {
+      first = std::min(first, p);
+      last = std::max(last, p);
+    }
+  }
+  lateralFirst = last >= 0 ? first : 0;
+  lateralEnd = last >= 0 ? last + 1 : 0;
+  SL3D_CUDA(cudaMemcpy(factor.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
+  return SL3DGPU_OK;
+}
+
+// -- flavours: assembly on the host (once), factorisation on the device ----------------------------
+
+int Viscoelastic3DGpu::BuildFlavour(const host::PointShear& shear, Flavour& f) {
+  const int L = options.lmax;
+  const auto& nodal = reference->nodal;
+  std::vector<std::unique_ptr<host::DegreeOperator>> sph(L + 1);
+  std::vector<std::unique_ptr<host::ToroidalOperator>> tor(L + 1);
+  std::string failure;
+  {
+    const int threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    std::mutex lock;
+    for (int t = 0; t < threads; ++t)
+      pool.emplace_back([&, t] {
+        for (int l = L - t; l >= 0; l -= threads) {
+          try {
+            sph[l] = std::make_unique<host::DegreeOperator>(nodal, l, options.eps, &shear);
+            if (l >= 1) tor[l] = std::make_unique<host::ToroidalOperator>(nodal, l, options.eps, &shear);
+          } catch (const std::exception& e) {
+            std::lock_guard<std::mutex> g(lock);
+            failure = e.what();
+          }
+        }
+      });
+    for (auto& th : pool) th.join();
+  }
+  if (!failure.empty()) {
+    SetError("v3d: " + failure);
+    return SL3DGPU_ERR_RUNTIME;
+  }
+  // Bands, scales, systems: spheroidal degrees 0..L, toroidal 1..L.
+  std::vector<double> bands, scales;
+  std::vector<sl3dgpu_band_system> chol;  // all Cholesky candidates, sph then tor
+  std::vector<int> cholDegree, cholKind;  // degree, 0 sph 1 tor
+  std::vector<sl3dgpu_band_system> lu;
+  std::vector<int> luDegree;
+  std::vector<long long> sphScale(L + 1), torScale(L + 1);
+  for (int l = 0; l <= L; ++l) {
+    sphScale[l] = static_cast<long long>(scales.size());
+    scales.insert(scales.end(), sph[l]->Scale().begin(), sph[l]->Scale().end());
+  }
+  for (int l = 1; l <= L; ++l) {
+    torScale[l] = static_cast<long long>(scales.size());
+    scales.insert(scales.end(), tor[l]->Scale().begin(), tor[l]->Scale().end());
+  }
+  auto system = [](int n, int kd, long long band, long long rhs, int nrhs, long long scale) {
+    sl3dgpu_band_system s{};
+    s.n = n;
+    s.kl = kd;
+    s.ku = kd;
+    s.nrhs = nrhs;
+    s.band = band;
+    s.pivots = 0;
+    s.rhs = rhs;
+    s.scale = scale;
+    s.pinned0 = s.pinned1 = -1;
+    return s;
+  };
+  for (int l = 0; l <= L; ++l) {
+    const auto& op = *sph[l];
+    if (op.PositiveDiagonal()) {
+      const auto b = op.ScaledCholeskyBand();
+      chol.push_back(system(op.DofCount(), op.Bandwidth(), static_cast<long long>(bands.size()),
+                            2 * degrees[l].sphRhs, 2 * (l + 1), sphScale[l]));
+      bands.insert(bands.end(), b.begin(), b.end());
+      cholDegree.push_back(l);
+      cholKind.push_back(0);
+    } else {
+      luDegree.push_back(l);
+    }
+  }
+  for (int l = 1; l <= L; ++l) {
+    const auto& op = *tor[l];
+    const auto b = op.ScaledCholeskyBand();
+    auto s = system(op.DofCount(), op.Bandwidth(), static_cast<long long>(bands.size()), 2 * degrees[l].torRhs,
+                    2 * (l + 1), torScale[l]);
+    if (!op.Pinned().empty()) s.pinned0 = op.Pinned()[0];
+    if (op.Pinned().size() > 1) s.pinned1 = op.Pinned()[1];
+    if (op.Pinned().size() > 2) {
+      SetError("v3d: more than two solid regions");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+    chol.push_back(s);
+    bands.insert(bands.end(), b.begin(), b.end());
+    cholDegree.push_back(l);
+    cholKind.push_back(1);
+  }
+  // Factor the Cholesky candidates; the spheroidal failures fall back to LU.
+  Dev<double> dBands;
+  SL3D_CUDA(dBands.Upload(bands));
+  Dev<sl3dgpu_band_system> dChol;
+  SL3D_CUDA(dChol.Upload(chol));
+  Dev<int> info;
+  SL3D_CUDA(info.Alloc(chol.size()));
+  SL3D_TRY(BandFactorBatch(dChol.p, chol.data(), static_cast<int>(chol.size()), dBands.p, nullptr, info.p, 0, stream));
+  std::vector<int> hInfo(chol.size());
+  SL3D_CUDA(cudaMemcpyAsync(hInfo.data(), info.p, hInfo.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  std::vector<double> hostBands(bands.size());
+  SL3D_CUDA(cudaMemcpy(hostBands.data(), dBands.p, bands.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  std::vector<double> finalBands;
+  f.sphChol.clear();
+  f.sphLu.clear();
+  f.torChol.clear();
+  for (size_t i = 0; i < chol.size(); ++i) {
+    if (hInfo[i] != 0) {
+      if (cholKind[i] == 1) {
+        SetError("v3d: toroidal degree " + std::to_string(cholDegree[i]) + ": Cholesky failed");
+        return SL3DGPU_ERR_RUNTIME;
+      }
+      luDegree.push_back(cholDegree[i]);
+      continue;
+    }
+    auto s = chol[i];
+    const size_t len = static_cast<size_t>(s.ku + 1) * s.n;
+    const long long at = static_cast<long long>(finalBands.size());
+    finalBands.insert(finalBands.end(), hostBands.begin() + s.band, hostBands.begin() + s.band + len);
+    s.band = at;
+    (cholKind[i] == 0 ? f.sphChol : f.torChol).push_back(s);
+  }
+  std::sort(luDegree.begin(), luDegree.end());
+  std::vector<int> pivots;
+  if (!luDegree.empty()) {
+    std::vector<double> luBands;
+    std::vector<sl3dgpu_band_system> luSys;
+    for (int l : luDegree) {
+      const auto& op = *sph[l];
+      auto s = system(op.DofCount(), op.Bandwidth(), static_cast<long long>(luBands.size()), 2 * degrees[l].sphRhs,
+                      2 * (l + 1), sphScale[l]);
+      s.pivots = static_cast<long long>(pivots.size());
+      pivots.resize(pivots.size() + op.DofCount());
+      const auto b = op.ScaledLuBand();
+      luBands.insert(luBands.end(), b.begin(), b.end());
+      luSys.push_back(s);
+    }
+    Dev<double> dLu;
+    SL3D_CUDA(dLu.Upload(luBands));
+    Dev<sl3dgpu_band_system> dLuSys;
+    SL3D_CUDA(dLuSys.Upload(luSys));
+    Dev<int> dPiv, luInfo;
+    SL3D_CUDA(dPiv.Alloc(pivots.size()));
+    SL3D_CUDA(luInfo.Alloc(luSys.size()));
+    SL3D_TRY(BandFactorBatch(dLuSys.p, luSys.data(), static_cast<int>(luSys.size()), dLu.p, dPiv.p, luInfo.p, 1, stream));
+    std::vector<int> hLuInfo(luSys.size());
+    SL3D_CUDA(cudaMemcpy(hLuInfo.data(), luInfo.p, hLuInfo.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < luSys.size(); ++i)
+      if (hLuInfo[i] != 0) {
+        SetError("v3d: degree " + std::to_string(luDegree[i]) + ": the banded LU factorisation failed (info = " +
+                 std::to_string(hLuInfo[i]) + ")");
+        return SL3DGPU_ERR_RUNTIME;
+      }
+    SL3D_CUDA(cudaMemcpy(luBands.data(), dLu.p, luBands.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    SL3D_CUDA(cudaMemcpy(pivots.data(), dPiv.p, pivots.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (auto s : luSys) {
+      const size_t len = static_cast<size_t>(3 * s.ku + 1) * s.n;
+      const long long at = static_cast<long long>(finalBands.size());
+      finalBands.insert(finalBands.end(), luBands.begin() + s.band, luBands.begin() + s.band + len);
+      s.band = at;
+      f.sphLu.push_back(s);
+    }
+  }
+  SL3D_CUDA(f.bands.Upload(finalBands));
+  SL3D_CUDA(f.scales.Upload(scales));
+  SL3D_CUDA(f.pivots.Upload(pivots.empty() ? std::vector<int>{0} : pivots));
+  auto upload = [&](const std::vector<sl3dgpu_band_system>& sys, Dev<sl3dgpu_band_system>& d, Dev<int2>& items,
+                    int& count) -> int {
+    SL3D_CUDA(d.Upload(sys));
+    const auto list = BandWorkItems(sys.data(), static_cast<int>(sys.size()));
+    SL3D_CUDA(items.Upload(list));
+    count = static_cast<int>(list.size());
+    return SL3DGPU_OK;
+  };
+  SL3D_TRY(upload(f.sphChol, f.dSphChol, f.iSphChol, f.nSphChol));
+  SL3D_TRY(upload(f.sphLu, f.dSphLu, f.iSphLu, f.nSphLu));
+  SL3D_TRY(upload(f.torChol, f.dTorChol, f.iTorChol, f.nTorChol));
+  // The load units K^-1 Load per degree (AddUnitChannels' cached responses).
+  std::vector<double> units;
+  std::vector<long long> unitOffset(L + 1);
+  for (int l = 0; l <= L; ++l) {
+    unitOffset[l] = static_cast<long long>(units.size());
+    const auto load = sph[l]->Load();
+    units.insert(units.end(), load.begin(), load.end());
+  }
+  SL3D_CUDA(f.units.Upload(units));
+  SL3D_CUDA(f.unitOffset.Upload(unitOffset));
+  auto unitSystems = [&](const std::vector<sl3dgpu_band_system>& src) {
+    std::vector<sl3dgpu_band_system> out;
+    for (auto s : src) {
+      // the system's degree from its right-hand-side offset
+      int l = 0;
+      while (l < L && 2 * degrees[l + 1].sphRhs <= s.rhs) ++l;
+      s.rhs = unitOffset[l];
+      s.nrhs = 1;
+      out.push_back(s);
+    }
+    return out;
+  };
+  for (int lu = 0; lu < 2; ++lu) {
+    const auto sys = unitSystems(lu ? f.sphLu : f.sphChol);
+    if (sys.empty()) continue;
+    Dev<sl3dgpu_band_system> d;
+    Dev<int2> items;
+    int count = 0;
+    SL3D_TRY(upload(sys, d, items, count));
+    SL3D_TRY(BandSolveBatch(d.p, sys.data(), static_cast<int>(sys.size()), items.p, count, f.bands.p, f.pivots.p,
+                            f.units.p, f.scales.p, lu, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+  }
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::FlavourOf(int scheme, double dt, Flavour** out) {
+  for (size_t i = 0; i < flavours.size(); ++i)
+    if (flavours[i]->scheme == scheme && flavours[i]->dt == dt) {
+      std::rotate(flavours.begin(), flavours.begin() + i, flavours.begin() + i + 1);
+      *out = flavours.front().get();
+      return SL3DGPU_OK;
+    }
+  constexpr size_t kFlavourCache = 4;  // the reference's LRU (Viscoelastic3D.cpp:535-558)
+  while (flavours.size() >= kFlavourCache) flavours.pop_back();
+  auto f = std::make_unique<Flavour>();
+  f->scheme = scheme;
+  f->dt = dt;
+  SL3D_TRY(BuildFlavour(reference->StepShear(static_cast<Scheme>(scheme), dt), *f));
+  flavours.insert(flavours.begin(), std::move(f));
+  *out = flavours.front().get();
+  return SL3DGPU_OK;
+}
+
+// -- transforms over the nodes ----------------------------------------------------------------------
+
+int Viscoelastic3DGpu::Synthesise(const double2* spectral, GridTensor& out) {
+  const auto* base = reinterpret_cast<const double*>(spectral);
+  auto* spectra = reinterpret_cast<double*>(spectraA.p);
+  SL3D_TRY(grid->LegendreSynthesis(-2, false, base, P, 0, P, spectra, stream));
+  SL3D_TRY(grid->RingSynthesis(false, spectra, P, reinterpret_cast<double*>(out.c0.p), stream));
+  SL3D_TRY(grid->LegendreSynthesis(-1, false, base + 2 * rows0 * P, P, 0, P, spectra, stream));
+  SL3D_TRY(grid->RingSynthesis(false, spectra, P, reinterpret_cast<double*>(out.c1.p), stream));
+  SL3D_TRY(grid->LegendreSynthesis(0, true, base + 2 * (rows0 + rows1) * P, P, 0, P, spectra, stream));
+  return grid->RingSynthesis(true, spectra, P, out.r.p, stream);
+}
+
+int Viscoelastic3DGpu::Analyse(const GridTensor& in, double2* spectral) {
+  auto* base = reinterpret_cast<double*>(spectral);
+  auto* spectra = reinterpret_cast<double*>(spectraA.p);
+  SL3D_TRY(grid->RingAnalysis(false, reinterpret_cast<const double*>(in.c0.p), P, spectra, stream));
+  SL3D_TRY(grid->LegendreAnalysis(-2, false, spectra, P, 0, P, base, false, stream));
+  SL3D_TRY(grid->RingAnalysis(false, reinterpret_cast<const double*>(in.c1.p), P, spectra, stream));
+  SL3D_TRY(grid->LegendreAnalysis(-1, false, spectra, P, 0, P, base + 2 * rows0 * P, false, stream));
+  SL3D_TRY(grid->RingAnalysis(true, in.r.p, P, spectra, stream));
+  return grid->LegendreAnalysis(0, true, spectra, P, 0, P, base + 2 * (rows0 + rows1) * P, false, stream);
+}
+
+// Analyse(w f) over the lateral nodes, added to what the spectral tensor holds.
+int Viscoelastic3DGpu::AnalyseWeighted(const GridTensor& in, const double* w, double2* spectral) {
+  const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+  if (count <= 0) return SL3DGPU_OK;
+  auto* base = reinterpret_cast<double*>(spectral);
+  auto* spectra = reinterpret_cast<double*>(spectraA.p);
+  const long long off = p0 * fieldSize;
+  SL3D_TRY(grid->RingAnalysis(false, reinterpret_cast<const double*>(in.c0.p + off), count, spectra, stream, w + off));
+  SL3D_TRY(grid->LegendreAnalysis(-2, false, spectra, P, p0, count, base, true, stream));
+  SL3D_TRY(grid->RingAnalysis(false, reinterpret_cast<const double*>(in.c1.p + off), count, spectra, stream, w + off));
+  SL3D_TRY(grid->LegendreAnalysis(-1, false, spectra, P, p0, count, base + 2 * rows0 * P, true, stream));
+  SL3D_TRY(grid->RingAnalysis(true, in.r.p + off, count, spectra, stream, w + off));
+  return grid->LegendreAnalysis(0, true, spectra, P, p0, count, base + 2 * (rows0 + rows1) * P, true, stream);
+}
+
+// Analyse(W Synthesise(strain)) over the lateral nodes, added onto out.
+int Viscoelastic3DGpu::WeightedPass(const double2* strain, double2* out) {
+  const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+  if (count <= 0) return SL3DGPU_OK;
+  const auto* in = reinterpret_cast<const double*>(strain);
+  auto* o = reinterpret_cast<double*>(out);
+  auto* a = reinterpret_cast<double*>(spectraA.p);
+  auto* b = reinterpret_cast<double*>(spectraB.p);
+  const double* w = weight.p + p0 * fieldSize;
+  const long long offs[3] = {0, 2 * rows0 * P, 2 * (rows0 + rows1) * P};
+  const int spins[3] = {-2, -1, 0};
+  for (int c = 0; c < 3; ++c) {
+    const bool real = c == 2;
+    SL3D_TRY(grid->LegendreSynthesis(spins[c], real, in + offs[c], P, p0, count, a, stream));
+    SL3D_TRY(grid->RingWeighted(real, a, count, w, b, stream));
+    SL3D_TRY(grid->LegendreAnalysis(spins[c], real, b, P, p0, count, o + offs[c], true, stream));
+  }
+  return SL3DGPU_OK;
+}
+
+// -- a pass --------------------------------------------------------------------------------------------
+
+int Viscoelastic3DGpu::Solve(const Flavour& f) {
+  auto* sphD = reinterpret_cast<double*>(rhsSph.p);
+  auto* torD = reinterpret_cast<double*>(rhsTor.p);
+  SL3D_TRY(BandSolveBatch(f.dSphChol.p, f.sphChol.data(), static_cast<int>(f.sphChol.size()), f.iSphChol.p,
+                          f.nSphChol, f.bands.p, f.pivots.p, sphD, f.scales.p, 0, stream));
+  SL3D_TRY(BandSolveBatch(f.dSphLu.p, f.sphLu.data(), static_cast<int>(f.sphLu.size()), f.iSphLu.p, f.nSphLu,
+                          f.bands.p, f.pivots.p, sphD, f.scales.p, 1, stream));
+  return BandSolveBatch(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
+                        f.nTorChol, f.bands.p, f.pivots.p, torD, f.scales.p, 0, stream);
+}
+
+int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma,
+                            double2* next) {
+  const double2* force = analysedStart.p;
+  if (!useStart) {
+    SL3D_CUDA(cudaMemcpyAsync(analysed.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                              stream));
+    SL3D_TRY(WeightedPass(strain, analysed.p));
+    force = analysed.p;
+  }
+  SL3D_CUDA(cudaMemsetAsync(rhsSph.p, 0, rhsSphComplex * sizeof(double2), stream));
+  SL3D_CUDA(cudaMemsetAsync(rhsTor.p, 0, std::max<long long>(rhsTorComplex, 1) * sizeof(double2), stream));
+  LaunchForces(geo, force, rhsSph.p, rhsTor.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(Solve(f));
+  if (sigma != nullptr) {
+    LaunchAddLoad(geo, sigma, f.units.p, f.unitOffset.p, rhsSph.p, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  LaunchStrain(geo, rhsSph.p, rhsTor.p, next, stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::RelativeChange(const double2* next, const double2* now, double* residual) {
+  LaunchRelativeChange(reinterpret_cast<const double*>(next), reinterpret_cast<const double*>(now),
+                       2 * spectralComplex, changePartial.p, kChangeBlocks, changeResult.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_CUDA(cudaMemcpyAsync(hostResult, changeResult.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  const double scale = hostResult[0], diff = hostResult[1];
+  if (hostResult[2] == 0.0) {
+    *residual = std::numeric_limits<double>::quiet_NaN();
+  } else {
+    *residual = scale > 0.0 ? std::sqrt(diff) / std::sqrt(scale) : 0.0;
+  }
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::MixerReset() {
+  const int memory = options.anderson_memory;
+  if (memory <= 0) return SL3DGPU_OK;
+  if (mixerMemory != memory) {
+    const size_t n = 2 * spectralComplex;
+    dG.resize(memory);
+    dF.resize(memory);
+    std::vector<double*> gp(memory), fp(memory);
+    for (int i = 0; i < memory; ++i) {
+      SL3D_CUDA(dG[i].Alloc(n));
+      SL3D_CUDA(dF[i].Alloc(n));
+      gp[i] = dG[i].p;
+      fp[i] = dF[i].p;
+    }
+    SL3D_CUDA(dGPtr.Upload(gp));
+    SL3D_CUDA(dFPtr.Upload(fp));
+    SL3D_CUDA(xPrev.Alloc(n));
+    SL3D_CUDA(fPrev.Alloc(n));
+    SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
+    SL3D_CUDA(gammaOut.Alloc(16));
+    SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks) * 16));
+    mixerMemory = memory;
+  }
+  SL3D_CUDA(cudaMemsetAsync(gram.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::MixerUpdate(int& count, int& slot, bool& first) {
+  MixerArgs a{};
+  a.n = 2 * spectralComplex;
+  a.memory = options.anderson_memory;
+  a.x = reinterpret_cast<double*>(s.p);
+  a.gx = reinterpret_cast<const double*>(sNext.p);
+  a.xPrev = xPrev.p;
+  a.fPrev = fPrev.p;
+  a.dG = dGPtr.p;
+  a.dF = dFPtr.p;
+  a.partial = mixPartial.p;
+  a.blocks = static_cast<int>(std::min<long long>(kMixBlocks, a.n));
+  a.gram = gram.p;
+  a.gamma = gammaOut.p;
+  if (first) {
+    LaunchMixerFirst(a, stream);
+    SL3D_CHECK_LAUNCH();
+    first = false;
+    return SL3DGPU_OK;
+  }
+  a.slot = slot;
+  a.m = std::min(count + 1, a.memory);
+  LaunchMixerUpdate(a, stream);
+  SL3D_CHECK_LAUNCH();
+  count = a.m;
+  slot = (slot + 1) % a.memory;
+  return SL3DGPU_OK;
+}
+
+// SolveElastic + StrainCoefficients into s: the memory force sum_k mu_k m_k,
+// the unrelaxed systems, the load channel at the state's time.
+int Viscoelastic3DGpu::ElasticStrain(const V3dState& st, const double2* sigma) {
+  for (int k = 0; k < K; ++k) {
+    LaunchCombine(values, fieldSize, muBranch.p + static_cast<long long>(k) * P, k == 0, st.m[k].c0.p,
+                  st.m[k].c1.p, st.m[k].r.p, fixedGrid.c0.p, fixedGrid.c1.p, fixedGrid.r.p, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  SL3D_TRY(Analyse(fixedGrid, analysedStart.p));
+  return Pass(*elastic, nullptr, true, sigma, s.p);
+}
+
+int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
+                                const double2* sigmaEnd, sl3dgpu_step_info& info) {
+  Flavour* f = nullptr;
+  SL3D_TRY(FlavourOf(scheme, dt, &f));
+  // The start strain: the cached coefficients, else the analysed cached grid
+  // strain, else a consistent unrelaxed solve.
+  if (in.hasCoeffs) {
+    SL3D_CUDA(cudaMemcpyAsync(s.p, in.coeffs.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  } else if (in.hasStrain) {
+    SL3D_TRY(Analyse(in.strain, s.p));
+  } else {
+    SL3D_TRY(ElasticStrain(in, sigmaStart));
+  }
+  const GridTensor* d0 = &in.strain;
+  if (!in.hasStrain) {
+    SL3D_TRY(Synthesise(s.p, dGrid));
+    d0 = &dGrid;
+  }
+  // Weights, decayed memory (into the output state's memory), lateral
+  // weight and fixed force; the fixed force analysed once.
+  WeightsArgs w{};
+  w.branches = K;
+  w.scheme = scheme == static_cast<int>(Scheme::BackwardEuler) ? 1 : 0;
+  w.dt = dt;
+  w.values = values;
+  w.fieldSize = fieldSize;
+  w.factor = factor.p;
+  w.muBranch = muBranch.p;
+  w.itauRef = itauRef.p;
+  for (int k = 0; k < K; ++k) {
+    w.m0[k] = in.m[k].c0.p;
+    w.m1[k] = in.m[k].c1.p;
+    w.mr[k] = in.m[k].r.p;
+    w.out0[k] = out.m[k].c0.p;
+    w.out1[k] = out.m[k].c1.p;
+    w.outr[k] = out.m[k].r.p;
+    w.beta[k] = beta[k].p;
+  }
+  w.d0c0 = d0->c0.p;
+  w.d0c1 = d0->c1.p;
+  w.d0r = d0->r.p;
+  w.weight = weight.p;
+  w.fixed0 = fixedGrid.c0.p;
+  w.fixed1 = fixedGrid.c1.p;
+  w.fixedr = fixedGrid.r.p;
+  LaunchWeights(w, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(Analyse(fixedGrid, fixedS.p));
+  // The first pass's force from the grid strain in hand: Analyse(W d0) + fixed.
+  SL3D_CUDA(cudaMemcpyAsync(analysedStart.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  SL3D_TRY(AnalyseWeighted(*d0, weight.p, analysedStart.p));
+
+  // Converge (Viscoelastic3D.cpp:1916-1974).
+  info = sl3dgpu_step_info{};
+  const bool adaptive = options.anderson_rate > 0.0;
+  bool mixing = options.anderson_memory > 0 && !adaptive;
+  bool firstMix = true;
+  int count = 0, slot = 0;
+  if (mixing) SL3D_TRY(MixerReset());
+  double previous = 0.0;
+  for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
+    SL3D_TRY(Pass(*f, s.p, iteration == 0, sigmaEnd, sNext.p));
+    double residual = 0.0;
+    SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
+    info.iterations = iteration + 1;
+    info.residual = residual;
+    if (!std::isfinite(residual)) break;
+    if (residual <= options.rtol) {
+      info.converged = 1;
+      std::swap(s, sNext);
+      break;
+    }
+    if (options.damping != 1.0) {
+      SetError("v3d: damping other than 1 is not built");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+    if (adaptive && !mixing && options.anderson_memory > 0 && iteration > 0 &&
+        residual > options.anderson_rate * previous) {
+      mixing = true;
+      firstMix = true;
+      count = slot = 0;
+      SL3D_TRY(MixerReset());
+    }
+    previous = residual;
+    if (mixing) {
+      SL3D_TRY(MixerUpdate(count, slot, firstMix));
+      ++info.mixed_passes;
+    } else {
+      std::swap(s, sNext);
+    }
+  }
+  // Finish: synthesise the strain, advance the memory.
+  SL3D_TRY(Synthesise(s.p, out.strain));
+  for (int k = 0; k < K; ++k) {
+    LaunchAdvance(values, beta[k].p, out.strain.c0.p, out.strain.c1.p, out.strain.r.p, out.m[k].c0.p,
+                  out.m[k].c1.p, out.m[k].r.p, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  SL3D_CUDA(cudaMemcpyAsync(out.coeffs.p, s.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  out.hasStrain = out.hasCoeffs = true;
+  return SL3DGPU_OK;
+}
+
+// Step (Viscoelastic3D.cpp:1982-2030): one stage, or Sdirk2's two backward
+// Euler stages of gamma dt, the second from (1 - r) m_n + r Y_1.
+int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1,
+                            sl3dgpu_step_info* infoOut) {
+  if (!(dt >= 0.0) || scheme < 0 || scheme > 2) {
+    SetError("v3d: dt >= 0 and a scheme of 0 (trapezoid), 1 (backward Euler) or 2 (Sdirk2)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  const double2* s0 = nullptr;
+  const double2* s1 = nullptr;
+  if (load0) {
+    SL3D_CUDA(cudaMemcpyAsync(sigma0.p, load0, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    s0 = sigma0.p;
+  }
+  if (load1) {
+    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, load1, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    s1 = sigma1.p;
+  }
+  sl3dgpu_step_info info{};
+  if (scheme != 2 || dt == 0.0) {
+    const int one = scheme == 2 ? 1 : scheme;
+    SL3D_TRY(StepOnce(st, scratch, dt, one, s0, s1, info));
+  } else {
+    const double gamma = host::kSdirk2Gamma;
+    const double h = gamma * dt;
+    const double2* mid = nullptr;
+    if (load0 || load1) {
+      std::vector<double2> v(lm);
+      for (size_t i = 0; i < lm; ++i) {
+        const double ax = load0 ? load0[2 * i] : 0.0, ay = load0 ? load0[2 * i + 1] : 0.0;
+        const double bx = load1 ? load1[2 * i] : 0.0, by = load1 ? load1[2 * i + 1] : 0.0;
+        v[i] = make_double2((1.0 - gamma) * ax + gamma * bx, (1.0 - gamma) * ay + gamma * by);
+      }
+      SL3D_CUDA(cudaMemcpyAsync(sigmaMid.p, v.data(), lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+      SL3D_CUDA(cudaStreamSynchronize(stream));
+      mid = sigmaMid.p;
+    }
+    sl3dgpu_step_info i1{}, i2{};
+    SL3D_TRY(StepOnce(st, scratch, h, 1, s0, mid, i1));
+    // the second stage's memory (1 - r) m_n + r Y_1, formed in place in Y_1
+    const double r = (1.0 - gamma) / gamma;
+    for (int k = 0; k < K; ++k) {
+      LaunchStageCombine(values, r, st.m[k].c0.p, st.m[k].c1.p, st.m[k].r.p, scratch.m[k].c0.p, scratch.m[k].c1.p,
+                         scratch.m[k].r.p, stream);
+      SL3D_CHECK_LAUNCH();
+    }
+    SL3D_TRY(StepOnce(scratch, scratch, h, 1, mid, s1, i2));
+    info.iterations = i1.iterations + i2.iterations;
+    info.mixed_passes = i1.mixed_passes + i2.mixed_passes;
+    info.residual = i2.residual;
+    info.converged = i1.converged && i2.converged;
+  }
+  std::swap(st.m, scratch.m);
+  std::swap(st.strain, scratch.strain);
+  std::swap(st.coeffs, scratch.coeffs);
+  st.hasStrain = st.hasCoeffs = true;
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  if (infoOut) *infoOut = info;
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::Surface(int component, double* out) {
+  if (component < 0 || component > 2) {
+    SetError("v3d: component 0 (U), 1 (V) or 2 (phi)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  LaunchSurface(geo, rhsSph.p, component, surfaceOut.p, stream);
+  SL3D_CHECK_LAUNCH();
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  SL3D_CUDA(cudaMemcpyAsync(out, surfaceOut.p, lm * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::StrainReference(const V3dState& st, double* out) {
+  if (!st.hasCoeffs) {
+    SetError("v3d: the state carries no strain coefficients");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  Dev<double> ref;
+  SL3D_CUDA(ref.Alloc(2 * spectralComplex));
+  const auto* base = reinterpret_cast<const double*>(st.coeffs.p);
+  SL3D_TRY(grid->FromDevice(-2, false, base, P, ref.p, stream));
+  SL3D_TRY(grid->FromDevice(-1, false, base + 2 * rows0 * P, P, ref.p + 2 * rows0 * P, stream));
+  SL3D_TRY(grid->FromDevice(0, true, base + 2 * (rows0 + rows1) * P, P, ref.p + 2 * (rows0 + rows1) * P, stream));
+  SL3D_CUDA(cudaMemcpyAsync(out, ref.p, 2 * spectralComplex * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+}  // namespace sl3dgpu
+
+// -- the C ABI -------------------------------------------------------------------------------------------
+
+using namespace sl3dgpu;
+
+struct sl3dgpu_v3d {
+  Viscoelastic3DGpu op;
+};
+struct sl3dgpu_v3d_state {
+  V3dState st;
+};
+
+extern "C" int sl3dgpu_v3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options* options,
+                                  sl3dgpu_v3d** out) {
+  if (layers == nullptr || options == nullptr || out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto h = std::make_unique<sl3dgpu_v3d>();
+  SL3D_TRY(h->op.Create(layers, nlayers, *options));
+  *out = h.release();
+  return SL3DGPU_OK;
+}
+
+extern "C" void sl3dgpu_v3d_destroy(sl3dgpu_v3d* h) { delete h; }
+
+extern "C" int sl3dgpu_v3d_shape(const sl3dgpu_v3d* h, int* nodes, int* ntheta, int* nphi) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (nodes) *nodes = h->op.P;
+  if (ntheta) *ntheta = h->op.grid->ntheta;
+  if (nphi) *nphi = h->op.grid->nphi;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_nodes(const sl3dgpu_v3d* h, double* radius, int* element) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (int p = 0; p < h->op.P; ++p) {
+    if (radius) radius[p] = h->op.nodeR[p];
+    if (element) element[p] = h->op.nodeElement[p];
+  }
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_colatitudes(const sl3dgpu_v3d* h, double* theta, double* weights) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& g = *h->op.grid;
+  if (theta) std::memcpy(theta, g.theta.data(), g.theta.size() * sizeof(double));
+  if (weights) std::memcpy(weights, g.weights.data(), g.weights.size() * sizeof(double));
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_scales(const sl3dgpu_v3d* h, double* length, double* time, double* surface_density) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& sc = h->op.earth->scales();
+  if (length) *length = sc.length;
+  if (time) *time = sc.time;
+  if (surface_density) *surface_density = sc.SurfaceDensity();
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_set_delta(sl3dgpu_v3d* h, const double* samples, int on_device) {
+  if (h == nullptr || samples == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SetDelta(samples, on_device != 0);
+}
+
+extern "C" int sl3dgpu_v3d_zero_state(sl3dgpu_v3d* h, sl3dgpu_v3d_state** out) {
+  if (h == nullptr || out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto s = std::make_unique<sl3dgpu_v3d_state>();
+  SL3D_TRY(h->op.ZeroState(s->st));
+  *out = s.release();
+  return SL3DGPU_OK;
+}
+
+extern "C" void sl3dgpu_v3d_free_state(sl3dgpu_v3d_state* s) { delete s; }
+
+extern "C" int sl3dgpu_v3d_step(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, double dt, int scheme, const double* load0,
+                                const double* load1, sl3dgpu_step_info* info) {
+  if (h == nullptr || state == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Step(state->st, dt, scheme, load0, load1, info);
+}
+
+extern "C" int sl3dgpu_v3d_surface(sl3dgpu_v3d* h, int component, double* out) {
+  if (h == nullptr || out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Surface(component, out);
+}
+
+extern "C" int sl3dgpu_v3d_state_strain(sl3dgpu_v3d* h, const sl3dgpu_v3d_state* state, double* out) {
+  if (h == nullptr || state == nullptr || out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StrainReference(state->st, out);
+}
+
+extern "C" int sl3dgpu_standard_earth(int elements, double kelvin_fraction, double kelvin_div, sl3dgpu_layer* out) {
+  if (out == nullptr || elements < 4) {
+    SetError("standard earth: at least four elements and an output of four layers");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto layers = host::StandardEarthLayers(elements, kelvin_fraction, kelvin_div);
+  for (size_t i = 0; i < layers.size(); ++i) {
+    const auto& L = layers[i];
+    out[i] = sl3dgpu_layer{L.r0, L.r1, L.fluid ? 1 : 0, L.elements, L.rho0, L.rho1, L.kappa0, L.kappa1,
+                           L.mu0, L.mu1, L.viscosity, L.kelvin_fraction, L.kelvin_viscosity};
+  }
+  return static_cast<int>(layers.size());
+}

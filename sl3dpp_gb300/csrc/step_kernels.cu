@@ -1,0 +1,572 @@
+// Device kernels of the 3D step (see step_kernels.cuh).
+//
+// The degree <-> spin maps restate include/sl3dpp/SpinComponents.hpp:53-145
+// and src/GridCoupling.cpp:595-809: one CTA per (degree l, order m >= 0), its
+// threads over the memory nodes (coalesced on the [row][node] spectral
+// layout) and then over the global mesh nodes of the degree's elements, with
+// the per-node values staged in shared memory so that every dof is written by
+// exactly one thread (no atomics, a fixed summation order).
+#include <cmath>
+
+#include "host/lstsq.hpp"
+#include "step_kernels.cuh"
+
+namespace sl3dgpu {
+namespace {
+
+__device__ inline double2 C(double x, double y) { return make_double2(x, y); }
+__device__ inline double2 CAdd(double2 a, double2 b) { return C(a.x + b.x, a.y + b.y); }
+__device__ inline double2 CSub(double2 a, double2 b) { return C(a.x - b.x, a.y - b.y); }
+__device__ inline double2 CScale(double s, double2 a) { return C(s * a.x, s * a.y); }
+__device__ inline double2 CConj(double2 a) { return C(a.x, -a.y); }
+__device__ inline double2 CI(double2 a) { return C(-a.y, a.x); }  // i a
+
+__device__ inline void DecodeLm(int lm, int& l, int& m) {
+  l = static_cast<int>((sqrt(8.0 * lm + 1.0) - 1.0) * 0.5);
+  while (l * (l + 1) / 2 > lm) --l;
+  while ((l + 1) * (l + 2) / 2 <= lm) ++l;
+  m = lm - l * (l + 1) / 2;
+}
+
+__device__ inline long long Row0(const Geometry& g, int l, int m) {
+  return g.rowOff0[m + g.lmax] + (l - max(abs(m), 2));
+}
+__device__ inline long long Row1(const Geometry& g, int l, int m) {
+  return g.rowOff1[m + g.lmax] + (l - max(abs(m), 1));
+}
+__device__ inline long long RowR(const Geometry& g, int l, int m) {
+  return g.rowOffR[m + g.lmax] - g.rowOffR[g.lmax] + (l - m);
+}
+
+struct Rows {
+  double2 u, v, w, du, dv, dw;
+};
+
+// ForceRowsFromComponents (SpinComponents.hpp:129-145).
+__device__ Rows ForceRows(int l, const double2 A[5], double r) {
+  const double zeta2 = l * (l + 1.0), zeta = sqrt(zeta2);
+  const double root = sqrt(fmax(zeta2 - 2.0, 0.0));
+  const double s2 = 1.41421356237309504880;
+  const double2 s13 = CAdd(A[1], A[3]), d13 = CSub(A[1], A[3]);
+  const double2 s04 = CAdd(A[0], A[4]), d04 = CSub(A[0], A[4]);
+  Rows rows;
+  rows.u = CSub(CScale(s2 * zeta, s13), CScale(4.0, A[2]));
+  rows.v = CSub(CAdd(CScale(zeta * root, s04), CScale(2.0 * zeta2, A[2])), CScale(s2 * zeta, s13));
+  rows.w = CI(CSub(CScale(zeta * root, d04), CScale(s2 * zeta, d13)));
+  rows.du = CScale(4.0 * r, A[2]);
+  rows.dv = CScale(s2 * zeta * r, s13);
+  rows.dw = CI(CScale(s2 * zeta * r, d13));
+  return rows;
+}
+
+__global__ void ForceKernel(Geometry g, const double2* spectral, double2* rhsSph, double2* rhsTor) {
+  int l, m;
+  DecodeLm(blockIdx.x, l, m);
+  const DegreeInfo d = g.degrees[l];
+  if (d.firstNode >= g.P) return;
+  extern __shared__ double2 rowsS[];  // (P - first) x 6
+  const double2* c0 = spectral;
+  const double2* c1 = spectral + g.rows0 * g.P;
+  const double2* cr = spectral + (g.rows0 + g.rows1) * g.P;
+  const double sign = (m % 2 == 0) ? 1.0 : -1.0;
+  for (int p = d.firstNode + threadIdx.x; p < g.P; p += blockDim.x) {
+    double2 A[5] = {C(0, 0), C(0, 0), C(0, 0), C(0, 0), C(0, 0)};
+    A[2] = cr[RowR(g, l, m) * g.P + p];
+    if (l >= 1) {
+      A[1] = c1[Row1(g, l, m) * g.P + p];
+      A[3] = CScale(sign, CConj(c1[Row1(g, l, -m) * g.P + p]));
+    }
+    if (l >= 2) {
+      A[0] = c0[Row0(g, l, m) * g.P + p];
+      A[4] = CScale(sign, CConj(c0[Row0(g, l, -m) * g.P + p]));
+    }
+    const Rows rows = ForceRows(l, A, g.nodeR[p]);
+    double2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
+    s[0] = rows.u;
+    s[1] = rows.v;
+    s[2] = rows.w;
+    s[3] = rows.du;
+    s[4] = rows.dv;
+    s[5] = rows.dw;
+  }
+  __syncthreads();
+  const int n = g.ngll, cols = l + 1;
+  for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
+    double2 bU = C(0, 0), bV = C(0, 0), bW = C(0, 0);
+    const int eHi = min(gn / (n - 1), g.elements - 1);
+    const int iHi = gn - eHi * (n - 1);
+    const int eLo = (iHi == 0 && eHi > 0) ? eHi - 1 : eHi;
+    for (int e = eLo; e <= eHi; ++e) {
+      const int fn = g.elemFirstNode[e];
+      if (fn < 0 || fn < d.firstNode) continue;
+      const int i = e == eHi ? iHi : n - 1;
+      const double jac = g.elemJac[e];
+      for (int q = 0; q < g.np; ++q) {
+        const int p = fn + q;
+        const double r = g.nodeR[p];
+        const double2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
+        const double point = jac * g.pWeight[q] * r;
+        const double v = point * g.pValue[q * n + i];
+        const double deriv = g.pWeight[q] * g.pDeriv[q * n + i] * r;
+        bU = CAdd(bU, CScale(v, s[0]));
+        bV = CAdd(bV, CScale(v, s[1]));
+        bU = CAdd(bU, CScale(deriv, s[3]));
+        bV = CAdd(bV, CScale(deriv, s[4]));
+        bW = CAdd(bW, CScale(v, s[2]));
+        bW = CAdd(bW, CScale(deriv, s[5]));
+      }
+    }
+    const int dU = g.sphMap[d.sphMap + 2LL * gn], dV = g.sphMap[d.sphMap + 2LL * gn + 1];
+    if (dU >= 0) rhsSph[d.sphRhs + static_cast<long long>(dU) * cols + m] = bU;
+    if (dV >= 0) rhsSph[d.sphRhs + static_cast<long long>(dV) * cols + m] = bV;
+    if (l >= 1) {
+      const int dW = g.torMap[d.torMap + gn];
+      if (dW >= 0) rhsTor[d.torRhs + static_cast<long long>(dW) * cols + m] = bW;
+    }
+  }
+}
+
+// DeviatoricComponents (SpinComponents.hpp:53-72) into the stored blocks
+// (GridCoupling::Scatter, the -m twins from the derived components).
+__global__ void StrainKernel(Geometry g, const double2* solSph, const double2* solTor, double2* spectral) {
+  int l, m;
+  DecodeLm(blockIdx.x, l, m);
+  const DegreeInfo d = g.degrees[l];
+  extern __shared__ double2 vals[];  // (lastGlobal - firstGlobal + 1) x 3
+  double2* c0 = spectral;
+  double2* c1 = spectral + g.rows0 * g.P;
+  double2* cr = spectral + (g.rows0 + g.rows1) * g.P;
+  const int cols = l + 1;
+  const bool any = d.firstNode < g.P;
+  if (any) {
+    for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
+      const int dU = g.sphMap[d.sphMap + 2LL * gn], dV = g.sphMap[d.sphMap + 2LL * gn + 1];
+      double2* v = vals + static_cast<long long>(gn - d.firstGlobal) * 3;
+      v[0] = dU >= 0 ? solSph[d.sphRhs + static_cast<long long>(dU) * cols + m] : C(0, 0);
+      v[1] = dV >= 0 ? solSph[d.sphRhs + static_cast<long long>(dV) * cols + m] : C(0, 0);
+      double2 W = C(0, 0);
+      if (l >= 1) {
+        const int dW = g.torMap[d.torMap + gn];
+        if (dW >= 0) W = solTor[d.torRhs + static_cast<long long>(dW) * cols + m];
+      }
+      v[2] = W;
+    }
+  }
+  __syncthreads();
+  const double sign = (m % 2 == 0) ? 1.0 : -1.0;
+  const int n = g.ngll;
+  const double zeta2 = l * (l + 1.0), zeta = sqrt(zeta2);
+  const double s2 = 1.41421356237309504880;
+  for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
+    double2 A[5] = {C(0, 0), C(0, 0), C(0, 0), C(0, 0), C(0, 0)};
+    if (any && p >= d.firstNode) {
+      const int e = g.nodeElement[p], q = g.nodeQ[p];
+      const double r = g.nodeR[p], jac = g.elemJac[e];
+      double2 U = C(0, 0), V = C(0, 0), W = C(0, 0), rdU = C(0, 0), rdV = C(0, 0), rdW = C(0, 0);
+      for (int i = 0; i < n; ++i) {
+        const double2* v = vals + static_cast<long long>(e * (n - 1) + i - d.firstGlobal) * 3;
+        const double val = g.pValue[q * n + i];
+        U = CAdd(U, CScale(val, v[0]));
+        V = CAdd(V, CScale(val, v[1]));
+        W = CAdd(W, CScale(val, v[2]));
+        const double b = r * g.pDeriv[q * n + i] / jac;
+        rdU = CAdd(rdU, CScale(b, v[0]));
+        rdV = CAdd(rdV, CScale(b, v[1]));
+        rdW = CAdd(rdW, CScale(b, v[2]));
+      }
+      const double2 t2 = CAdd(CSub(rdU, U), CScale(0.5 * zeta2, V));
+      A[2] = C(t2.x / (3.0 * r), t2.y / (3.0 * r));
+      if (l >= 1) {
+        const double2 tangential = CAdd(CSub(rdV, V), U);
+        const double2 twist = CSub(W, rdW);
+        const double den = 2.0 * s2 * r;
+        const double2 a1 = CScale(zeta, CAdd(tangential, CI(twist)));
+        const double2 a3 = CScale(zeta, CSub(tangential, CI(twist)));
+        A[1] = C(a1.x / den, a1.y / den);
+        A[3] = C(a3.x / den, a3.y / den);
+      }
+      if (l >= 2) {
+        const double factor = 0.5 * zeta * sqrt(zeta2 - 2.0) / r;
+        A[0] = CScale(factor, CSub(V, CI(W)));
+        A[4] = CScale(factor, CAdd(V, CI(W)));
+      }
+    }
+    if (l >= 2) {
+      c0[Row0(g, l, m) * g.P + p] = A[0];
+      if (m > 0) c0[Row0(g, l, -m) * g.P + p] = CScale(sign, CConj(A[4]));
+    }
+    if (l >= 1) {
+      c1[Row1(g, l, m) * g.P + p] = A[1];
+      if (m > 0) c1[Row1(g, l, -m) * g.P + p] = CScale(sign, CConj(A[3]));
+    }
+    cr[RowR(g, l, m) * g.P + p] = A[2];
+  }
+}
+
+__global__ void AddLoadKernel(Geometry g, const double2* sigma, const double* units,
+                              const long long* unitOffset, double2* sol) {
+  const int l = blockIdx.x;
+  const DegreeInfo d = g.degrees[l];
+  const int cols = l + 1;
+  const long long total = static_cast<long long>(d.sphNdof) * cols;
+  for (long long t = threadIdx.x; t < total; t += blockDim.x) {
+    const int dof = static_cast<int>(t / cols), m = static_cast<int>(t % cols);
+    const double2 a = sigma[l * (l + 1) / 2 + m];
+    if (a.x == 0.0 && a.y == 0.0) continue;
+    const double u = units[unitOffset[l] + dof];
+    double2& x = sol[d.sphRhs + t];
+    x = CAdd(x, CScale(u, a));
+  }
+}
+
+__global__ void SurfaceKernel(Geometry g, const double2* sol, int component, double2* out) {
+  const int lm = blockIdx.x * blockDim.x + threadIdx.x;
+  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  if (lm >= count) return;
+  int l, m;
+  DecodeLm(lm, l, m);
+  const DegreeInfo d = g.degrees[l];
+  const int dof = component == 0 ? d.surfaceU : component == 1 ? d.surfaceV : d.surfacePhi;
+  out[lm] = dof >= 0 ? sol[d.sphRhs + static_cast<long long>(dof) * (l + 1) + m] : C(0, 0);
+}
+
+// -- streaming kernels -----------------------------------------------------------------------
+
+__device__ inline double Phi1(double h, double e) {
+  if (fabs(h) < 1e-3) return 1.0 - h / 2.0 + h * h / 6.0 - h * h * h / 24.0 + h * h * h * h / 120.0;
+  return (1.0 - e) / h;
+}
+
+__global__ void WeightsKernel(WeightsArgs a) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const int P = static_cast<int>(a.values / a.fieldSize);
+  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < a.values; x += stride) {
+    const int node = static_cast<int>(x / a.fieldSize);
+    double w = 0.0;
+    double2 f0 = C(0, 0), f1 = C(0, 0);
+    double fr = 0.0;
+    for (int k = 0; k < a.branches; ++k) {
+      const double itauRef = a.itauRef[static_cast<long long>(k) * P + node];
+      const double mu = a.muBranch[static_cast<long long>(k) * P + node];
+      const double h0 = a.dt * itauRef;
+      double refBeta;
+      if (a.scheme == 1) {
+        refBeta = 1.0 - 1.0 / (1.0 + h0);
+      } else {
+        const double e0 = exp(-h0);
+        refBeta = 1.0 - Phi1(h0, e0);
+      }
+      const double h = a.dt * (itauRef * a.factor[x]);
+      double ew, aw, bw;
+      if (a.scheme == 1) {
+        const double wbe = 1.0 / (1.0 + h);
+        ew = wbe;
+        aw = 0.0;
+        bw = 1.0 - wbe;
+      } else {
+        const double e = exp(-h);
+        const double phi1 = Phi1(h, e);
+        ew = e;
+        aw = phi1 - e;
+        bw = 1.0 - phi1;
+      }
+      a.beta[k][x] = bw;
+      const double2 m0 = a.m0[k][x], m1 = a.m1[k][x];
+      const double mr = a.mr[k][x];
+      const double2 o0 = C(ew * m0.x + aw * a.d0c0[x].x, ew * m0.y + aw * a.d0c0[x].y);
+      const double2 o1 = C(ew * m1.x + aw * a.d0c1[x].x, ew * m1.y + aw * a.d0c1[x].y);
+      const double orr = ew * mr + aw * a.d0r[x];
+      a.out0[k][x] = o0;
+      a.out1[k][x] = o1;
+      a.outr[k][x] = orr;
+      if (k == 0) {
+        w = 0.0 + mu * (bw - refBeta);
+        f0 = C(0.0 + mu * o0.x, 0.0 + mu * o0.y);
+        f1 = C(0.0 + mu * o1.x, 0.0 + mu * o1.y);
+        fr = 0.0 + mu * orr;
+        continue;
+      }
+      if (mu == 0.0) continue;
+      w += mu * (bw - refBeta);
+      f0 = C(f0.x + mu * o0.x, f0.y + mu * o0.y);
+      f1 = C(f1.x + mu * o1.x, f1.y + mu * o1.y);
+      fr += mu * orr;
+    }
+    a.weight[x] = w;
+    a.fixed0[x] = f0;
+    a.fixed1[x] = f1;
+    a.fixedr[x] = fr;
+  }
+}
+
+__global__ void AdvanceKernel(long long values, const double* beta, const double2* d0, const double2* d1,
+                              const double* dr, double2* m0, double2* m1, double* mr) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < values; x += stride) {
+    const double b = beta[x];
+    m0[x] = C(m0[x].x + b * d0[x].x, m0[x].y + b * d0[x].y);
+    m1[x] = C(m1[x].x + b * d1[x].x, m1[x].y + b * d1[x].y);
+    mr[x] += b * dr[x];
+  }
+}
+
+__global__ void StageCombineKernel(long long values, double r, const double2* a0, const double2* a1,
+                                   const double* ar, double2* o0, double2* o1, double* orr) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const double s = 1.0 - r;
+  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < values; x += stride) {
+    o0[x] = C((0.0 + s * a0[x].x) + r * o0[x].x, (0.0 + s * a0[x].y) + r * o0[x].y);
+    o1[x] = C((0.0 + s * a1[x].x) + r * o1[x].x, (0.0 + s * a1[x].y) + r * o1[x].y);
+    orr[x] = (0.0 + s * ar[x]) + r * orr[x];
+  }
+}
+
+__global__ void CombineKernel(long long values, long long fieldSize, const double* mu, bool first,
+                              const double2* m0, const double2* m1, const double* mr, double2* o0,
+                              double2* o1, double* orr) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < values; x += stride) {
+    const double u = mu[x / fieldSize];
+    if (first) {
+      if (u == 0.0) {
+        o0[x] = C(0, 0);
+        o1[x] = C(0, 0);
+        orr[x] = 0.0;
+      } else {
+        o0[x] = C(0.0 + u * m0[x].x, 0.0 + u * m0[x].y);
+        o1[x] = C(0.0 + u * m1[x].x, 0.0 + u * m1[x].y);
+        orr[x] = 0.0 + u * mr[x];
+      }
+    } else if (u != 0.0) {
+      o0[x] = C(o0[x].x + u * m0[x].x, o0[x].y + u * m0[x].y);
+      o1[x] = C(o1[x].x + u * m1[x].x, o1[x].y + u * m1[x].y);
+      orr[x] += u * mr[x];
+    }
+  }
+}
+
+// -- the convergence measure ------------------------------------------------------------------
+
+__global__ void RelativeChangeKernel(const double2* next, const double2* now, long long n, double* partial) {
+  __shared__ double s0[256], s1[256], s2[256];
+  double scale = 0.0, diff = 0.0, finite = 1.0;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
+    const double2 a = next[i], b = now[i];
+    if (!(a.x - a.x == 0.0) || !(a.y - a.y == 0.0)) finite = 0.0;
+    scale = fmax(scale, a.x * a.x + a.y * a.y);
+    const double dx = a.x - b.x, dy = a.y - b.y;
+    diff = fmax(diff, dx * dx + dy * dy);
+  }
+  s0[threadIdx.x] = scale;
+  s1[threadIdx.x] = diff;
+  s2[threadIdx.x] = finite;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w /= 2) {
+    if (threadIdx.x < w) {
+      s0[threadIdx.x] = fmax(s0[threadIdx.x], s0[threadIdx.x + w]);
+      s1[threadIdx.x] = fmax(s1[threadIdx.x], s1[threadIdx.x + w]);
+      s2[threadIdx.x] = fmin(s2[threadIdx.x], s2[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x * 3 + 0] = s0[0];
+    partial[blockIdx.x * 3 + 1] = s1[0];
+    partial[blockIdx.x * 3 + 2] = s2[0];
+  }
+}
+
+__global__ void ReduceMaxKernel(const double* partial, int count, double* result) {
+  __shared__ double s0[256], s1[256], s2[256];
+  double a = 0.0, b = 0.0, c = 1.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) {
+    a = fmax(a, partial[3 * i]);
+    b = fmax(b, partial[3 * i + 1]);
+    c = fmin(c, partial[3 * i + 2]);
+  }
+  s0[threadIdx.x] = a;
+  s1[threadIdx.x] = b;
+  s2[threadIdx.x] = c;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w /= 2) {
+    if (threadIdx.x < w) {
+      s0[threadIdx.x] = fmax(s0[threadIdx.x], s0[threadIdx.x + w]);
+      s1[threadIdx.x] = fmax(s1[threadIdx.x], s1[threadIdx.x + w]);
+      s2[threadIdx.x] = fmin(s2[threadIdx.x], s2[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    result[0] = s0[0];
+    result[1] = s1[0];
+    result[2] = s2[0];
+  }
+}
+
+// -- the Anderson mixer ---------------------------------------------------------------------------
+
+__global__ void MixerFirstKernel(long long n, double* x, const double* gx, double* xPrev, double* fPrev) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
+    xPrev[i] = x[i];
+    fPrev[i] = gx[i] - x[i];
+    x[i] = gx[i];
+  }
+}
+
+constexpr int kMixThreads = 256;
+constexpr int kMaxMemory = 8;
+
+// One block per fixed chunk of the vector (fixed by n alone): the new
+// differences, the stored iterate and residual, and the block's partial Gram
+// column and right-hand side, summed in a fixed tree order.
+__global__ void MixerSweepKernel(MixerArgs a) {
+  __shared__ double red[kMixThreads][2 * kMaxMemory];
+  const long long begin = a.n * blockIdx.x / a.blocks, end = a.n * (blockIdx.x + 1) / a.blocks;
+  double col[kMaxMemory], gam[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) col[i] = gam[i] = 0.0;
+  double* dFs = a.dF[a.slot];
+  double* dGs = a.dG[a.slot];
+  for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
+    const double xs = a.x[at], gs = a.gx[at];
+    const double f = gs - xs;
+    const double dx = xs - a.xPrev[at];
+    const double df = f - a.fPrev[at];
+    dFs[at] = df;
+    dGs[at] = dx + df;
+    a.xPrev[at] = xs;
+    a.fPrev[at] = f;
+    for (int i = 0; i < a.m; ++i) {
+      const double di = i == a.slot ? df : a.dF[i][at];
+      col[i] += di * df;
+      gam[i] += di * f;
+    }
+  }
+  for (int i = 0; i < a.m; ++i) {
+    red[threadIdx.x][i] = col[i];
+    red[threadIdx.x][kMaxMemory + i] = gam[i];
+  }
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w /= 2) {
+    if (threadIdx.x < w)
+      for (int i = 0; i < a.m; ++i) {
+        red[threadIdx.x][i] += red[threadIdx.x + w][i];
+        red[threadIdx.x][kMaxMemory + i] += red[threadIdx.x + w][kMaxMemory + i];
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int i = 0; i < a.m; ++i) {
+      a.partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + i] = red[0][i];
+      a.partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + kMaxMemory + i] = red[0][kMaxMemory + i];
+    }
+}
+
+// The partials in block order, the Gram matrix's new row and column, and the
+// least-squares coefficients (FP64, one thread; gamma[m] = 1 when they hold).
+__global__ void MixerSolveKernel(MixerArgs a) {
+  if (threadIdx.x != 0) return;
+  double col[kMaxMemory], gam[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) col[i] = gam[i] = 0.0;
+  for (int b = 0; b < a.blocks; ++b)
+    for (int i = 0; i < a.m; ++i) {
+      col[i] += a.partial[static_cast<long long>(b) * 2 * kMaxMemory + i];
+      gam[i] += a.partial[static_cast<long long>(b) * 2 * kMaxMemory + kMaxMemory + i];
+    }
+  for (int i = 0; i < a.m; ++i) {
+    a.gram[a.slot * a.memory + i] = col[i];
+    a.gram[i * a.memory + a.slot] = col[i];
+  }
+  double A[kMaxMemory * kMaxMemory], x[kMaxMemory];
+  for (int i = 0; i < a.m; ++i)
+    for (int j = 0; j < a.m; ++j) A[i * a.m + j] = a.gram[i * a.memory + j];
+  const bool ok = SymmetricLstsq(a.m, A, gam, x);
+  for (int i = 0; i < a.m; ++i) a.gamma[i] = x[i];
+  a.gamma[a.m] = ok ? 1.0 : 0.0;
+}
+
+__global__ void MixerMixKernel(MixerArgs a) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const bool ok = a.gamma[a.m] != 0.0;
+  double g[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) g[i] = a.gamma[i];
+  for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < a.n; at += stride) {
+    double value = a.gx[at];
+    if (ok)
+      for (int i = 0; i < a.m; ++i) value -= g[i] * a.dG[i][at];
+    a.x[at] = value;
+  }
+}
+
+int StreamBlocks(long long values) {
+  const long long b = (values + 255) / 256;
+  return static_cast<int>(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
+}
+
+}  // namespace
+
+void LaunchForces(const Geometry& g, const double2* spectral, double2* rhsSph, double2* rhsTor,
+                  cudaStream_t stream) {
+  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  const size_t smem = static_cast<size_t>(g.P) * 6 * sizeof(double2);
+  cudaFuncSetAttribute(ForceKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  ForceKernel<<<count, 128, smem, stream>>>(g, spectral, rhsSph, rhsTor);
+}
+
+void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTor, double2* spectral,
+                  cudaStream_t stream) {
+  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 3 * sizeof(double2);
+  cudaFuncSetAttribute(StrainKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  StrainKernel<<<count, 128, smem, stream>>>(g, solSph, solTor, spectral);
+}
+
+void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units, const long long* unitOffset,
+                   double2* solSph, cudaStream_t stream) {
+  AddLoadKernel<<<g.lmax + 1, 256, 0, stream>>>(g, sigma, units, unitOffset, solSph);
+}
+
+void LaunchSurface(const Geometry& g, const double2* solSph, int component, double2* out, cudaStream_t stream) {
+  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  SurfaceKernel<<<(count + 127) / 128, 128, 0, stream>>>(g, solSph, component, out);
+}
+
+void LaunchWeights(const WeightsArgs& a, cudaStream_t stream) {
+  WeightsKernel<<<StreamBlocks(a.values), 256, 0, stream>>>(a);
+}
+
+void LaunchAdvance(long long values, const double* beta, const double2* d0, const double2* d1, const double* dr,
+                   double2* m0, double2* m1, double* mr, cudaStream_t stream) {
+  AdvanceKernel<<<StreamBlocks(values), 256, 0, stream>>>(values, beta, d0, d1, dr, m0, m1, mr);
+}
+
+void LaunchStageCombine(long long values, double r, const double2* a0, const double2* a1, const double* ar,
+                        double2* o0, double2* o1, double* orr, cudaStream_t stream) {
+  StageCombineKernel<<<StreamBlocks(values), 256, 0, stream>>>(values, r, a0, a1, ar, o0, o1, orr);
+}
+
+void LaunchCombine(long long values, long long fieldSize, const double* mu, bool first, const double2* m0,
+                   const double2* m1, const double* mr, double2* o0, double2* o1, double* orr,
+                   cudaStream_t stream) {
+  CombineKernel<<<StreamBlocks(values), 256, 0, stream>>>(values, fieldSize, mu, first, m0, m1, mr, o0, o1, orr);
+}
+
+void LaunchRelativeChange(const double* next, const double* now, long long n, double* partial, int partialCount,
+                          double* result, cudaStream_t stream) {
+  RelativeChangeKernel<<<partialCount, 256, 0, stream>>>(reinterpret_cast<const double2*>(next),
+                                                        reinterpret_cast<const double2*>(now), n / 2, partial);
+  ReduceMaxKernel<<<1, 256, 0, stream>>>(partial, partialCount, result);
+}
+
+void LaunchMixerFirst(const MixerArgs& a, cudaStream_t stream) {
+  MixerFirstKernel<<<StreamBlocks(a.n), 256, 0, stream>>>(a.n, a.x, a.gx, a.xPrev, a.fPrev);
+}
+
+void LaunchMixerUpdate(const MixerArgs& a, cudaStream_t stream) {
+  MixerSweepKernel<<<a.blocks, kMixThreads, 0, stream>>>(a);
+  MixerSolveKernel<<<1, 32, 0, stream>>>(a);
+  MixerMixKernel<<<StreamBlocks(a.n), 256, 0, stream>>>(a);
+}
+
+}  // namespace sl3dgpu

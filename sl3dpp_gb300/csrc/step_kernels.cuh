@@ -1,0 +1,120 @@
+// Device kernels of the 3D step: the degree <-> spin-component maps (strain
+// recovery and memory-force assembly), the streaming step-weight and memory
+// kernels, the load channel, the convergence measure and the Anderson mixer.
+#pragma once
+
+#include "common.cuh"
+
+namespace sl3dgpu {
+
+// Per degree l, what the maps need: its first memory node, the global node
+// range its memory nodes' elements span, and where its dof maps and its
+// right-hand sides / solutions start.
+struct DegreeInfo {
+  int firstNode;      // first memory node of the degree's element subset
+  int firstGlobal;    // global node range of the carrying elements from it
+  int lastGlobal;
+  int sphNdof, torNdof;
+  int surfaceU, surfaceV, surfacePhi;
+  long long sphMap, torMap;  // offsets into the dof maps
+  long long sphRhs, torRhs;  // complex offsets of the degree's [dof][l+1] blocks
+};
+
+// Constant geometry of the coupling.
+struct Geometry {
+  int lmax, P, ngll, np;     // degrees, memory nodes, GLL nodes, points per element
+  int elements;
+  const int* nodeElement;    // per memory node
+  const int* nodeQ;
+  const double* nodeR;
+  const int* elemFirstNode;  // per element, -1 when not carrying
+  const double* elemJac;
+  const double* pValue;      // (np, ngll) Lagrange values at the points
+  const double* pDeriv;      // (np, ngll) their xi-derivatives
+  const double* pWeight;     // (np)
+  const int* rowOff0;        // spin -2 row offsets (2 lmax + 2)
+  const int* rowOff1;        // spin -1
+  const int* rowOffR;        // spin 0 (full m range; real rows from m = 0)
+  long long rows0, rows1, rowsR;
+  const DegreeInfo* degrees;
+  const int* sphMap;         // (g, {U, V}) per degree
+  const int* torMap;         // g per degree
+};
+
+// The memory force of an analysed (mu-weighted) tensor into the degree
+// systems' right-hand sides (GridCoupling::SpheroidalForce/ToroidalForce).
+void LaunchForces(const Geometry& g, const double2* spectral, double2* rhsSph, double2* rhsTor,
+                  cudaStream_t stream);
+// The deviatoric strain of every degree's solutions into a spectral tensor
+// (StrainOf: AddStrainOfSolution + DeviatoricComponents + Scatter).
+void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTor, double2* spectral,
+                  cudaStream_t stream);
+// x += sigma_lm K^-1 Load for every degree (AddUnitChannels' load part).
+void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units,
+                   const long long* unitOffset, double2* solSph, cudaStream_t stream);
+// Surface values of a component (U, V or phi) for every (l, m >= 0).
+void LaunchSurface(const Geometry& g, const double2* solSph, int component, double2* out,
+                   cudaStream_t stream);
+
+// The step weights, decayed memory, lateral weight and fixed force
+// (StartStep's loop, src/Viscoelastic3D.cpp:1283-1354).
+struct WeightsArgs {
+  int branches;
+  int scheme;  // 0 trapezoid, 1 backward Euler
+  double dt;
+  long long values, fieldSize;
+  const double* factor;     // exp(-delta)
+  const double* muBranch;   // [k][P]
+  const double* itauRef;    // [k][P]
+  const double2* m0[2];     // state memory per branch: spin -2, spin -1, spin 0
+  const double2* m1[2];
+  const double* mr[2];
+  double2* out0[2];         // decayed memory per branch (may alias the state's)
+  double2* out1[2];
+  double* outr[2];
+  const double2* d0c0;      // start strain grid
+  const double2* d0c1;
+  const double* d0r;
+  double* beta[2];
+  double* weight;
+  double2* fixed0;
+  double2* fixed1;
+  double* fixedr;
+};
+void LaunchWeights(const WeightsArgs& a, cudaStream_t stream);
+
+// m += beta d (AdvanceMemory), per branch.
+void LaunchAdvance(long long values, const double* beta, const double2* d0, const double2* d1,
+                   const double* dr, double2* m0, double2* m1, double* mr, cudaStream_t stream);
+// out = (1 - r) a + r out, per grid value (Sdirk2's second-stage memory).
+void LaunchStageCombine(long long values, double r, const double2* a0, const double2* a1,
+                        const double* ar, double2* o0, double2* o1, double* orr, cudaStream_t stream);
+// out (+)= mu_k(node) m (SolveElastic's combined memory), first branch assigns.
+void LaunchCombine(long long values, long long fieldSize, const double* mu, bool first,
+                   const double2* m0, const double2* m1, const double* mr, double2* o0, double2* o1,
+                   double* orr, cudaStream_t stream);
+
+// RelativeChange: max |n|^2, max |n - o|^2 and finiteness over n doubles
+// (complex pairs), into result[3] on the device.
+void LaunchRelativeChange(const double* next, const double* now, long long n, double* partial,
+                          int partialCount, double* result, cudaStream_t stream);
+
+// The Anderson mixer's sweeps (AndersonMixer.hpp:65-219).
+struct MixerArgs {
+  long long n;
+  int m, slot, memory;
+  double* x;
+  const double* gx;
+  double* xPrev;
+  double* fPrev;
+  double** dG;  // device array of memory pointers
+  double** dF;
+  double* partial;  // blocks x 2m
+  int blocks;
+  double* gram;     // memory x memory
+  double* gamma;    // m (+1 status)
+};
+void LaunchMixerFirst(const MixerArgs& a, cudaStream_t stream);
+void LaunchMixerUpdate(const MixerArgs& a, cudaStream_t stream);
+
+}  // namespace sl3dgpu

@@ -1,0 +1,182 @@
+"""The 3D quasi-static step on the GPU, mirroring Viscoelastic3D.
+
+Mirrors include/sl3dpp/Viscoelastic3D.hpp:79-837 for the fixed-point step
+(Picard, then Anderson when a pass contracts too slowly): construction over a
+layered Earth with the log-viscosity perturbation delta sampled on every
+memory node's grid, ZeroState, Step (ExponentialTrapezoid, BackwardEuler or
+Sdirk2) under a surface-load channel, Surface. All compute runs in
+libsl3dgpu.so (the C ABI of include/sl3dgpu.h); this class holds the handles.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import P_double, P_int, c_void_p, check, lib
+
+SCHEMES = {"exponential_trapezoid": 0, "backward_euler": 1, "sdirk2": 2}
+COMPONENTS = {"U": 0, "V": 1, "phi": 2}
+
+
+class Layer(ctypes.Structure):
+    """sl3dgpu_layer."""
+
+    _fields_ = [("r0", ctypes.c_double), ("r1", ctypes.c_double), ("fluid", ctypes.c_int),
+                ("elements", ctypes.c_int), ("rho0", ctypes.c_double), ("rho1", ctypes.c_double),
+                ("kappa0", ctypes.c_double), ("kappa1", ctypes.c_double), ("mu0", ctypes.c_double),
+                ("mu1", ctypes.c_double), ("viscosity", ctypes.c_double),
+                ("kelvin_fraction", ctypes.c_double), ("kelvin_viscosity", ctypes.c_double)]
+
+
+class Options(ctypes.Structure):
+    """sl3dgpu_v3d_options (Viscoelastic3D::Options)."""
+
+    _fields_ = [("lmax", ctypes.c_int), ("ngll", ctypes.c_int), ("eps", ctypes.c_double),
+                ("oversampling", ctypes.c_double), ("max_iterations", ctypes.c_int),
+                ("rtol", ctypes.c_double), ("damping", ctypes.c_double), ("anderson_memory", ctypes.c_int),
+                ("anderson_rate", ctypes.c_double), ("precision", ctypes.c_int)]
+
+    @classmethod
+    def defaults(cls, lmax: int, ngll: int = 5, **kw) -> "Options":
+        o = cls(lmax=lmax, ngll=ngll, eps=1e-8, oversampling=1.5, max_iterations=40, rtol=1e-11,
+                damping=1.0, anderson_memory=5, anderson_rate=0.5, precision=0)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+
+class StepInfo(ctypes.Structure):
+    """sl3dgpu_step_info (Viscoelastic3D::StepInfo)."""
+
+    _fields_ = [("iterations", ctypes.c_int), ("residual", ctypes.c_double), ("converged", ctypes.c_int),
+                ("mixed_passes", ctypes.c_int)]
+
+
+_SIGNED = False
+
+
+def _signatures():
+    global _SIGNED
+    if _SIGNED:
+        return
+    L = lib()
+    v, i, d = c_void_p, ctypes.c_int, ctypes.c_double
+    sig = {
+        "sl3dgpu_standard_earth": (i, [i, d, d, ctypes.POINTER(Layer)]),
+        "sl3dgpu_v3d_create": (i, [ctypes.POINTER(Layer), i, ctypes.POINTER(Options), ctypes.POINTER(v)]),
+        "sl3dgpu_v3d_destroy": (None, [v]),
+        "sl3dgpu_v3d_shape": (i, [v, P_int, P_int, P_int]),
+        "sl3dgpu_v3d_nodes": (i, [v, P_double, P_int]),
+        "sl3dgpu_v3d_colatitudes": (i, [v, P_double, P_double]),
+        "sl3dgpu_v3d_scales": (i, [v, P_double, P_double, P_double]),
+        "sl3dgpu_v3d_set_delta": (i, [v, v, i]),
+        "sl3dgpu_v3d_zero_state": (i, [v, ctypes.POINTER(v)]),
+        "sl3dgpu_v3d_free_state": (None, [v]),
+        "sl3dgpu_v3d_step": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_surface": (i, [v, i, v]),
+        "sl3dgpu_v3d_state_strain": (i, [v, v, v]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _SIGNED = True
+
+
+def standard_earth(elements: int, kelvin_fraction: float = 0.0, kelvin_div: float = 10.0):
+    """The measured configurations' layered Earth (four layers)."""
+    _signatures()
+    layers = (Layer * 4)()
+    check(lib().sl3dgpu_standard_earth(elements, kelvin_fraction, kelvin_div, layers))
+    return layers
+
+
+class State:
+    """Viscoelastic3D::State: the memory tensors and the strain cache, on the GPU."""
+
+    def __init__(self, op: "Viscoelastic3D"):
+        self._op = op
+        h = c_void_p()
+        check(lib().sl3dgpu_v3d_zero_state(op._h, ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().sl3dgpu_v3d_free_state(h)
+            self._h = None
+
+    def strain_coefficients(self) -> np.ndarray:
+        """The strain coefficients, reference layouts (node-major spin -2, -1, 0 blocks)."""
+        out = np.zeros(self._op.spectral_size, dtype=np.complex128)
+        check(lib().sl3dgpu_v3d_state_strain(self._op._h, self._h, out.ctypes.data))
+        return out
+
+
+class Viscoelastic3D:
+    """The GPU 3D viscoelastic operator (Viscoelastic3D)."""
+
+    def __init__(self, layers, options: Options):
+        _signatures()
+        h = c_void_p()
+        check(lib().sl3dgpu_v3d_create(layers, len(layers), ctypes.byref(options), ctypes.byref(h)))
+        self._h = h
+        self.options = options
+        self.lmax = options.lmax
+        P, nt, nph = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().sl3dgpu_v3d_shape(h, ctypes.byref(P), ctypes.byref(nt), ctypes.byref(nph)))
+        self.node_count, self.ntheta, self.nphi = P.value, nt.value, nph.value
+        self.radius = np.empty(self.node_count)
+        self.element = np.empty(self.node_count, dtype=np.int32)
+        check(lib().sl3dgpu_v3d_nodes(h, self.radius.ctypes.data_as(P_double), self.element.ctypes.data_as(P_int)))
+        self.theta = np.empty(self.ntheta)
+        self.weights = np.empty(self.ntheta)
+        check(lib().sl3dgpu_v3d_colatitudes(h, self.theta.ctypes.data_as(P_double),
+                                            self.weights.ctypes.data_as(P_double)))
+        length, time, sigma = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().sl3dgpu_v3d_scales(h, ctypes.byref(length), ctypes.byref(time), ctypes.byref(sigma)))
+        self.length_scale, self.time_scale, self.surface_density_scale = length.value, time.value, sigma.value
+        L = self.lmax
+        self.spectral_size = ((L + 1) ** 2 - 4 + (L + 1) ** 2 - 1 + (L + 1) * (L + 2) // 2) * self.node_count
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().sl3dgpu_v3d_destroy(h)
+            self._h = None
+
+    @property
+    def values(self) -> int:
+        return self.node_count * self.ntheta * self.nphi
+
+    def set_delta(self, samples) -> None:
+        """delta over every node's grid: a host numpy array or a CUDA torch tensor."""
+        if isinstance(samples, np.ndarray):
+            a = np.ascontiguousarray(samples, dtype=np.float64).ravel()
+            assert a.size == self.values
+            check(lib().sl3dgpu_v3d_set_delta(self._h, a.ctypes.data, 0))
+        else:
+            assert samples.is_cuda and samples.numel() == self.values and samples.is_contiguous()
+            check(lib().sl3dgpu_v3d_set_delta(self._h, samples.data_ptr(), 1))
+
+    def ZeroState(self) -> State:
+        return State(self)
+
+    def Step(self, state: State, dt: float, scheme="sdirk2", load0=None, load1=None) -> StepInfo:
+        """One step of length dt (non-dimensional) under the load channel."""
+        code = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        info = StepInfo()
+        a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.complex128)
+        b = None if load1 is None else np.ascontiguousarray(load1, dtype=np.complex128)
+        check(lib().sl3dgpu_v3d_step(self._h, state._h, float(dt), code,
+                                     None if a is None else a.ctypes.data,
+                                     None if b is None else b.ctypes.data, ctypes.byref(info)))
+        return info
+
+    def Surface(self, component="U") -> np.ndarray:
+        code = COMPONENTS[component] if isinstance(component, str) else int(component)
+        out = np.zeros((self.lmax + 1) * (self.lmax + 2) // 2, dtype=np.complex128)
+        check(lib().sl3dgpu_v3d_surface(self._h, code, out.ctypes.data))
+        return out

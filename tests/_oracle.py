@@ -121,3 +121,119 @@ def expand_real(lmax, theta, weights, nphi, field):
     load().oracle_expand_real(lmax, theta.size, nphi, ptr(theta), ptr(weights), ptr(field),
                               coeffs.ctypes.data_as(P_double))
     return coeffs
+
+
+# -- the 3D step --------------------------------------------------------------------------
+
+import ctypes as _ct
+
+
+class Layer(_ct.Structure):
+    """sl3dgpu_layer (include/sl3dgpu.h)."""
+    _fields_ = [("r0", _ct.c_double), ("r1", _ct.c_double), ("fluid", _ct.c_int), ("elements", _ct.c_int),
+                ("rho0", _ct.c_double), ("rho1", _ct.c_double), ("kappa0", _ct.c_double), ("kappa1", _ct.c_double),
+                ("mu0", _ct.c_double), ("mu1", _ct.c_double), ("viscosity", _ct.c_double),
+                ("kelvin_fraction", _ct.c_double), ("kelvin_viscosity", _ct.c_double)]
+
+
+class Options(_ct.Structure):
+    """sl3dgpu_v3d_options (include/sl3dgpu.h)."""
+    _fields_ = [("lmax", _ct.c_int), ("ngll", _ct.c_int), ("eps", _ct.c_double), ("oversampling", _ct.c_double),
+                ("max_iterations", _ct.c_int), ("rtol", _ct.c_double), ("damping", _ct.c_double),
+                ("anderson_memory", _ct.c_int), ("anderson_rate", _ct.c_double), ("precision", _ct.c_int)]
+
+
+class StepInfo(_ct.Structure):
+    _fields_ = [("iterations", _ct.c_int), ("residual", _ct.c_double), ("converged", _ct.c_int),
+                ("mixed_passes", _ct.c_int)]
+
+
+def default_options(lmax, ngll=5, **kw):
+    o = Options(lmax=lmax, ngll=ngll, eps=1e-8, oversampling=1.5, max_iterations=40, rtol=1e-11, damping=1.0,
+                anderson_memory=5, anderson_rate=0.5, precision=0)
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def _v3d_sigs(L):
+    v, i, d = _ct.c_void_p, _ct.c_int, _ct.c_double
+    sig = {
+        "oracle_standard_earth": (i, [i, d, d, _ct.POINTER(Layer)]),
+        "oracle_v3d_create": (v, [_ct.POINTER(Layer), i, _ct.POINTER(Options)]),
+        "oracle_v3d_destroy": (None, [v]),
+        "oracle_v3d_node_count": (i, [v]),
+        "oracle_v3d_nodes": (None, [v, P_double, P_int]),
+        "oracle_v3d_grid": (None, [v, P_int, P_int, P_double, P_double]),
+        "oracle_v3d_time_scale": (d, [v]),
+        "oracle_v3d_surface_density_scale": (d, [v]),
+        "oracle_v3d_set_delta": (None, [v, P_double]),
+        "oracle_v3d_zero_state": (v, [v]),
+        "oracle_v3d_free_state": (None, [v]),
+        "oracle_v3d_step": (i, [v, v, d, i, v, v, _ct.POINTER(StepInfo)]),
+        "oracle_v3d_surface": (None, [v, i, v]),
+        "oracle_v3d_state_strain": (i, [v, v]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def standard_earth(elements, kelvin_fraction=0.0, kelvin_div=10.0):
+    L = load()
+    _v3d_sigs(L)
+    layers = (Layer * 4)()
+    L.oracle_standard_earth(elements, kelvin_fraction, kelvin_div, layers)
+    return layers
+
+
+class OracleStep:
+    """The oracle's Viscoelastic3D (CPU FP64), for parity checks."""
+
+    def __init__(self, layers, options):
+        self.L = load()
+        _v3d_sigs(self.L)
+        self.options = options
+        self.h = self.L.oracle_v3d_create(layers, len(layers), _ct.byref(options))
+        self.P = self.L.oracle_v3d_node_count(self.h)
+        nt, nph = _ct.c_int(), _ct.c_int()
+        self.L.oracle_v3d_grid(self.h, _ct.byref(nt), _ct.byref(nph), None, None)
+        self.ntheta, self.nphi = nt.value, nph.value
+        self.theta = np.empty(self.ntheta)
+        self.weights = np.empty(self.ntheta)
+        self.L.oracle_v3d_grid(self.h, None, None, ptr(self.theta), ptr(self.weights))
+        self.radius = np.empty(self.P)
+        self.element = np.empty(self.P, dtype=np.int32)
+        self.L.oracle_v3d_nodes(self.h, ptr(self.radius), ptr(self.element))
+        self.time_scale = self.L.oracle_v3d_time_scale(self.h)
+        self.sigma_scale = self.L.oracle_v3d_surface_density_scale(self.h)
+        self.state = self.L.oracle_v3d_zero_state(self.h)
+
+    def __del__(self):
+        try:
+            self.L.oracle_v3d_free_state(self.state)
+            self.L.oracle_v3d_destroy(self.h)
+        except Exception:
+            pass
+
+    def set_delta(self, samples):
+        samples = np.ascontiguousarray(samples, dtype=np.float64)
+        assert samples.size == self.P * self.ntheta * self.nphi
+        self.L.oracle_v3d_set_delta(self.h, ptr(samples))
+
+    def step(self, dt, scheme=2, load0=None, load1=None):
+        info = StepInfo()
+        a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.complex128)
+        b = None if load1 is None else np.ascontiguousarray(load1, dtype=np.complex128)
+        st = self.L.oracle_v3d_step(self.h, self.state, dt, scheme,
+                                    None if a is None else a.ctypes.data, None if b is None else b.ctypes.data,
+                                    _ct.byref(info))
+        assert st == 0
+        return info
+
+    def surface(self, component):
+        L = self.options.lmax
+        out = np.zeros((L + 1) * (L + 2) // 2, dtype=np.complex128)
+        self.L.oracle_v3d_surface(self.h, component, out.ctypes.data)
+        return out

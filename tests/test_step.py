@@ -1,0 +1,134 @@
+"""The 3D quasi-static step: the oracle's physics checks on the CPU, and the GPU
+step against the oracle on the same inputs (tolerance 1e-10 relative, the FP64
+form's bar).
+
+The reference's gates re-expressed here (tests/TestViscoelastic3D.cpp):
+zero-lateral steps decouple the degrees and converge in two passes a stage
+(:90-196); a lateral contrast couples orders and toroidal motion (:293-322);
+both Prony bodies (Maxwell, Burgers); every scheme."""
+
+import numpy as np
+import pytest
+
+from tests import _oracle as O
+from sl3dpp_gb300 import configs
+
+TOL = 1e-10
+
+
+def cap_load(op_lmax, sigma_scale, thickness, alpha=15.0):
+    theta, w, nphi = O.grid(op_lmax, 1.0)
+    field = configs.cap_field(theta, nphi, alpha, thickness)
+    return O.expand_real(op_lmax, theta, w, nphi, field) / sigma_scale
+
+
+def delta_for(oracle_step, lmax, ldelta, rms, seed):
+    c = configs.delta_coefficients(lmax, ldelta, rms, seed)
+    pattern = O.synthesise_real(lmax, oracle_step.theta, oracle_step.nphi, c)
+    return configs.delta_samples(pattern, oracle_step.radius)
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+# -- the oracle's physics ---------------------------------------------------------------------
+
+def test_zero_lateral_step_decouples_and_converges_in_two_passes():
+    lmax = 8
+    st = O.OracleStep(O.standard_earth(20), O.default_options(lmax))
+    load = cap_load(lmax, st.sigma_scale, 2000.0)
+    dt = 500 * configs.SECONDS_PER_YEAR / st.time_scale
+    for n in range(2):
+        info = st.step(dt, 2, load * n / 10, load * (n + 1) / 10)
+        assert info.converged and info.iterations == 4  # two passes in each Sdirk2 stage
+        U = st.surface(0)
+        zonal = np.array([configs.real_index(l, 0) for l in range(lmax + 1)])
+        rest = np.setdiff1d(np.arange(U.size), zonal)
+        assert np.max(np.abs(U[rest])) < 1e-12 * np.max(np.abs(U[zonal]))
+        assert U[configs.real_index(2, 0)].real < 0.0  # the load depresses the surface
+
+
+def test_lateral_viscosity_couples_orders():
+    lmax = 8
+    st = O.OracleStep(O.standard_earth(20), O.default_options(lmax))
+    st.set_delta(delta_for(st, lmax, 4, 0.5, seed=7))
+    load = cap_load(lmax, st.sigma_scale, 2000.0)
+    dt = 500 * configs.SECONDS_PER_YEAR / st.time_scale
+    for n in range(2):
+        info = st.step(dt, 2, load * n / 10, load * (n + 1) / 10)
+        assert info.converged and info.residual <= 1e-11
+    U = st.surface(0)
+    zonal = np.array([configs.real_index(l, 0) for l in range(lmax + 1)])
+    rest = np.setdiff1d(np.arange(U.size), zonal)
+    assert np.max(np.abs(U[rest])) > 1e-6 * np.max(np.abs(U[zonal]))
+
+
+# -- the GPU step against the oracle ------------------------------------------------------------
+
+def _pair(lmax, elements, ngll, kelvin=0.0, rms=0.5, ldelta=4, seed=11, **opt):
+    from sl3dpp_gb300.viscoelastic3d import Options, Viscoelastic3D, standard_earth
+
+    layers_o = O.standard_earth(elements, kelvin, 10.0)
+    o = O.OracleStep(layers_o, O.default_options(lmax, ngll, **opt))
+    g = Viscoelastic3D(standard_earth(elements, kelvin, 10.0), Options.defaults(lmax, ngll, **opt))
+    assert (g.node_count, g.ntheta, g.nphi) == (o.P, o.ntheta, o.nphi)
+    assert np.max(np.abs(g.radius - o.radius)) == 0.0
+    assert np.max(np.abs(g.theta - o.theta)) < 1e-15
+    if rms > 0:
+        d = delta_for(o, lmax, ldelta, rms, seed)
+        o.set_delta(d)
+        g.set_delta(d)
+    return o, g
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", [2, 0, 1])
+def test_gpu_step_matches_oracle(gpu, scheme):
+    lmax = 8
+    o, g = _pair(lmax, 20, 5)
+    state = g.ZeroState()
+    load = cap_load(lmax, o.sigma_scale, 2000.0)
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    for n in range(3):
+        l0, l1 = load * n / 10, load * (n + 1) / 10
+        io = o.step(dt, scheme, l0, l1)
+        ig = g.Step(state, dt, scheme, l0, l1)
+        assert ig.converged == io.converged == 1
+        assert abs(ig.iterations - io.iterations) <= 1
+        for comp in (0, 2):
+            assert rel(g.Surface(comp), o.surface(comp)) < TOL, (n, comp)
+    want = np.zeros(g.spectral_size, dtype=np.complex128)
+    o.L.oracle_v3d_state_strain(o.state, want.ctypes.data)
+    assert rel(state.strain_coefficients(), want) < TOL
+
+
+@pytest.mark.gpu
+def test_gpu_step_matches_oracle_burgers_ngll6_lmax16(gpu):
+    lmax = 16
+    o, g = _pair(lmax, 24, 6, kelvin=0.5, rms=1.0, ldelta=6, seed=3)
+    state = g.ZeroState()
+    load = cap_load(lmax, o.sigma_scale, 2000.0)
+    dt = 250 * configs.SECONDS_PER_YEAR / o.time_scale
+    for n in range(2):
+        l0, l1 = load * n / 10, load * (n + 1) / 10
+        io = o.step(dt, 2, l0, l1)
+        ig = g.Step(state, dt, 2, l0, l1)
+        assert ig.converged == io.converged == 1
+        for comp in (0, 2):
+            assert rel(g.Surface(comp), o.surface(comp)) < TOL, (n, comp)
+
+
+@pytest.mark.gpu
+def test_gpu_step_with_anderson_from_the_first_pass(gpu):
+    # anderson_rate 0: the mixer engages from the first pass (IterationControl)
+    lmax = 8
+    o, g = _pair(lmax, 20, 5, rms=1.5, anderson_rate=0.0)
+    state = g.ZeroState()
+    load = cap_load(lmax, o.sigma_scale, 2000.0)
+    dt = 2000 * configs.SECONDS_PER_YEAR / o.time_scale
+    io = o.step(dt, 2, 0 * load, load)
+    ig = g.Step(state, dt, 2, 0 * load, load)
+    assert ig.mixed_passes > 0 and ig.mixed_passes == io.mixed_passes
+    assert ig.converged == io.converged == 1
+    assert rel(g.Surface(0), o.surface(0)) < TOL
