@@ -1,0 +1,403 @@
+"""Benchmark: 3D viscoelastic steps per second on GB300.
+
+One step is one Sdirk2 step (two backward Euler stages, each closed by the
+within-step fixed point, Picard then Anderson, to the tolerance) of the 3D
+quasi-static operator at lmax 256: 120 radial elements of order 5, the
+configurations' layered Earth (Maxwell mantle, 100 km elastic lid), delta a
+seeded random spherical-harmonic field to degree 64 with RMS 1.0 between 100
+and 670 km depth, and a 15-degree polar ice cap growing to 2 km over 10 steps
+of 500 yr. All inputs are synthetic (numpy default_rng, seeds below).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). `value` is steps/s with the load coefficients
+resident in device memory, timed with CUDA events on the operator's stream;
+`e2e` is the same through the C ABI with the loads copied from pinned host
+memory and the surface U and phi read back every step. The arithmetic is FP64
+throughout (the plain FP64 form). `--impl reference` times the CPU
+restatement of the reference's path (oracle/, OpenMP on every host core) on a
+bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+LMAX = 256
+ELEMENTS = 120
+NGLL = 6
+LDELTA = 64
+DELTA_RMS = 1.0
+DELTA_SEED = 1
+CAP_DEGREES = 15.0
+CAP_THICKNESS = 2000.0
+RAMP_STEPS = 10
+DT_YEARS = 500.0
+RTOL = 1e-10
+MAX_ITERATIONS = 60
+# The FP64 fixed point's passes per step at this workload (both stages),
+# measured by the GPU arm (identical iterate sequences on both arms, pinned
+# pass for pass at small lmax); the CPU sample's steps/s is extrapolated with it.
+PASSES_PER_STEP = 120
+
+
+def _rescale(lmax):
+    """A smaller workload of the same shape (development runs only)."""
+    global LMAX, ELEMENTS, LDELTA
+    LMAX = lmax
+    ELEMENTS = max(20, int(round(120 * lmax / 256)))
+    LDELTA = max(2, lmax // 4)
+
+
+def workload_config():
+    return {"workload": f"3d_step_lmax{LMAX}_fp64_sdirk2", "lmax": LMAX, "elements": ELEMENTS,
+            "order": NGLL - 1, "delta_degree": LDELTA, "delta_rms": DELTA_RMS, "delta_seed": DELTA_SEED,
+            "rheology": "maxwell", "cap_degrees": CAP_DEGREES, "cap_thickness_m": CAP_THICKNESS,
+            "dt_years": DT_YEARS, "scheme": "sdirk2", "rtol": RTOL, "max_iterations": MAX_ITERATIONS,
+            "anderson_memory": 5, "oversampling": 1.5,
+            "l2": "working set far above L2 (memory tensors ~3.3 GB per array)",
+            "parallelism": "replicas (one independent operator per GPU)"}
+
+
+def load_ramp(full, step):
+    return full * min(step, RAMP_STEPS) / RAMP_STEPS
+
+
+# -- clocks ----------------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, f[5:9]):
+                if flag.lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# -- the GPU arm --------------------------------------------------------------------------------
+
+KIND_NAMES = ["legendre_synthesis", "legendre_analysis", "ring_fft", "force_assembly", "strain_recovery",
+              "band_solve", "streaming", "anderson", "other"]
+
+
+def profile_read():
+    import ctypes
+
+    from sl3dpp_gb300._lib import lib
+
+    out = {}
+    for k, name in enumerate(KIND_NAMES):
+        ms, n, fl, by = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+        lib().sl3dgpu_profile_read(k, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(fl), ctypes.byref(by))
+        out[name] = {"ms": ms.value, "launches": n.value, "flops": fl.value, "bytes": by.value}
+    return out
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        return json.loads(path.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch from the committed ncu summary of a kernel, if any."""
+    path = ROOT / "profiles" / f"{kernel}.md"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def build_operator(device):
+    import torch
+
+    from sl3dpp_gb300 import configs
+    from sl3dpp_gb300.grid import SurfaceGrid
+    from sl3dpp_gb300.viscoelastic3d import Options, Viscoelastic3D, standard_earth
+
+    op = Viscoelastic3D(standard_earth(ELEMENTS), Options.defaults(LMAX, NGLL, rtol=RTOL, max_iterations=MAX_ITERATIONS))
+    grid = SurfaceGrid(LMAX, 0, 1.5)
+    c = configs.delta_coefficients(LMAX, LDELTA, DELTA_RMS, DELTA_SEED)
+    pattern = grid.SynthesiseBatch(torch.tensor(c, device=device), 1)
+    ind = torch.tensor(configs.delta_indicator(op.radius), device=device)
+    op.set_delta((ind[:, None] * pattern[None, :]).contiguous().view(-1))
+    exact = SurfaceGrid(LMAX, 0, 1.0)
+    cap = configs.cap_field(exact.theta, exact.nphi, CAP_DEGREES, CAP_THICKNESS)
+    full = exact.ExpandBatch(torch.tensor(cap, device=device), 1) / op.surface_density_scale
+    dt = DT_YEARS * configs.SECONDS_PER_YEAR / op.time_scale
+    return op, full, dt
+
+
+def gpu_arm(args, rank, world, device):
+    import torch
+
+    from sl3dpp_gb300._lib import lib
+
+    t_setup = time.time()
+    op, full, dt = build_operator(device)
+    torch.cuda.synchronize()
+    setup_s = time.time() - t_setup
+    loads = [load_ramp(full, n).contiguous() for n in range(args.warmup + 2 * args.steps + 2)]
+    state = op.ZeroState()
+    n = 0
+    infos = []
+    for _ in range(args.warmup):
+        infos.append(op.StepDevice(state, dt, "sdirk2", loads[n], loads[n + 1]))
+        n += 1
+    stream = torch.cuda.ExternalStream(op.stream, device=device)
+    lib().sl3dgpu_profile_reset()
+    lib().sl3dgpu_profile_enable(1)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib().sl3dgpu_launch_count()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    passes = 0
+    with ClockSampler(torch.cuda.current_device()) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            info = op.StepDevice(state, dt, "sdirk2", loads[n], loads[n + 1])
+            passes += info.iterations
+            infos.append(info)
+            n += 1
+        stop.record(stream)
+        stop.synchronize()
+    torch.cuda.synchronize()
+    launches = lib().sl3dgpu_launch_count() - launches0
+    lib().sl3dgpu_profile_enable(0)
+    prof = profile_read()
+    ms = start.elapsed_time(stop)
+    # end to end: host loads from pinned memory, surface U and phi read back
+    host_loads = [l.cpu().pin_memory().numpy() for l in loads]
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.Step(state, dt, "sdirk2", host_loads[n], host_loads[n + 1])
+        U = op.Surface("U")
+        phi = op.Surface("phi")
+        n += 1
+    e2e_s = time.perf_counter() - t0
+    assert np.all(np.isfinite(U)) and np.all(np.isfinite(phi))
+    times = torch.tensor([ms / 1e3, e2e_s], device=device, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    return {"op": op, "seconds": times[0].item(), "e2e_seconds": times[1].item(), "passes": passes,
+            "infos": infos, "profile": prof, "launches": launches, "clocks": clocks.summary(),
+            "setup_s": setup_s, "load_bytes": int(full.numel() * 16)}
+
+
+def roofline(prof, fp64_gflops):
+    kind = max(prof, key=lambda k: prof[k]["ms"])
+    p = prof[kind]
+    peaks, source = measured_peaks()
+    per_launch_s = p["ms"] / 1e3 / max(p["launches"], 1)
+    if p["flops"] > 0 and kind in ("legendre_synthesis", "legendre_analysis", "band_solve"):
+        achieved = p["flops"] / max(p["launches"], 1) / per_launch_s / 1e12
+        peak = fp64_gflops / 1e3
+        return {"kernel": kind, "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": ncu_traffic(kind),
+                "peak_source": "FP64 FMA throughput measured live by sl3dgpu_fp64_fma_peak (FP64 arithmetic: no FP64 "
+                               "figure in MEASURED_PEAKS.json)",
+                "share_of_timed": p["ms"] / sum(v["ms"] for v in prof.values())}
+    achieved = p["bytes"] / max(p["launches"], 1) / per_launch_s / 1e9
+    return {"kernel": kind, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "traffic": ncu_traffic(kind), "peak_source": source,
+            "share_of_timed": p["ms"] / sum(v["ms"] for v in prof.values())}
+
+
+# -- the CPU restatement (oracle), a bounded sample --------------------------------------------
+
+class CpuSampler:
+    """The oracle (FP64 C++ + OpenMP, every host core) at the same workload:
+    steps/s from one backward Euler stage's start and a few passes timed,
+    extrapolated to two stages and passes_per_step passes."""
+
+    def __init__(self):
+        from sl3dpp_gb300 import configs
+        from tests import _oracle as O  # the checker, as the CPU baseline
+
+        t0 = time.time()
+        self.O = O
+        self.st = O.OracleStep(O.standard_earth(ELEMENTS),
+                               O.default_options(LMAX, NGLL, rtol=RTOL, max_iterations=MAX_ITERATIONS))
+        c = configs.delta_coefficients(LMAX, LDELTA, DELTA_RMS, DELTA_SEED)
+        pattern = O.synthesise_real(LMAX, self.st.theta, self.st.nphi, c)
+        self.st.set_delta(configs.delta_samples(pattern, self.st.radius))
+        theta, w, nphi = O.grid(LMAX, 1.0)
+        full = O.expand_real(LMAX, theta, w, nphi, configs.cap_field(theta, nphi, CAP_DEGREES, CAP_THICKNESS))
+        self.full = full / self.st.sigma_scale
+        self.dt = DT_YEARS * configs.SECONDS_PER_YEAR / self.st.time_scale
+        self.setup = time.time() - t0
+        self.threads = O.load().oracle_threads()
+
+    def sample(self, passes_per_step, sample_passes=1):
+        t_start, t_passes = self.st.sample(0.29289321881345247560 * self.dt, sample_passes, 0.5 * self.full,
+                                           0.6 * self.full)
+        per_pass = t_passes / sample_passes
+        step_s = 2 * t_start + passes_per_step * per_pass
+        return {"value": 1.0 / step_s, "unit": "steps/s", "cores": self.threads, "kind": "port",
+                "sample": (f"one backward Euler stage start ({t_start:.1f} s) and {sample_passes} pass(es) "
+                           f"({per_pass:.2f} s each) of the same lmax-{LMAX} workload, extrapolated to a step of two "
+                           f"stages and {passes_per_step:.0f} passes; construction {self.setup:.0f} s untimed"),
+                "seconds_per_step": step_s}
+
+
+# -- main ------------------------------------------------------------------------------------------
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lmax", type=int, default=LMAX, help="a smaller workload for development runs")
+    args = ap.parse_args()
+    if args.lmax != LMAX:
+        _rescale(args.lmax)
+    if args.warmup < 3:
+        raise SystemExit("at least three warm-up steps")
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import __graft_entry__
+
+        from oracle import build as oracle_build
+
+        oracle_build.build()
+        sampler = CpuSampler()
+        samples = []
+        for k in range(args.warmup + args.steps):
+            r = sampler.sample(PASSES_PER_STEP)
+            if k >= args.warmup:
+                samples.append(r)
+        value = float(np.median([s["value"] for s in samples]))
+        base = samples[-1]
+        line = {"metric": "3D steps/sec at lmax=256 (FP64)", "value": value, "unit": "steps/s", "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": workload_config(), "impl": "reference",
+                "cpu_baseline": {"value": value, "unit": "steps/s", "cores": base["cores"], "kind": "port",
+                                 "sample": base["sample"]},
+                "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+    device = torch.device("cuda", torch.cuda.current_device())
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from sl3dpp_gb300._lib import lib
+    import ctypes
+
+    fp64 = ctypes.c_double()
+    lib().sl3dgpu_fp64_fma_peak(ctypes.byref(fp64))
+    r = gpu_arm(args, rank, world, device)
+    steps_total = args.steps * world
+    value = steps_total / r["seconds"]
+    e2e = steps_total / r["e2e_seconds"]
+    passes_per_step = r["passes"] / args.steps
+    line = {"metric": "3D steps/sec at lmax=256 (FP64)", "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["seconds"] * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded delta field and ice-cap load; random-free radial Earth)",
+            "config": workload_config(),
+            "passes_per_step": passes_per_step,
+            "converged_steps": sum(int(i.converged) for i in r["infos"][args.warmup:]),
+            "final_residual": r["infos"][-1].residual,
+            "roofline": roofline(r["profile"], fp64.value),
+            "kernel_ms": {k: round(v["ms"], 3) for k, v in r["profile"].items()},
+            "gpu_launches": int(r["launches"]),
+            "clocks": r["clocks"],
+            "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 2 * r["load_bytes"],
+                    "d2h_bytes_per_step": 2 * r["load_bytes"]},
+            "setup_seconds": r["setup_s"]}
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            sampler = CpuSampler()
+            line["cpu_baseline"] = {k: v for k, v in sampler.sample(passes_per_step, 2).items()
+                                    if k != "seconds_per_step"}
+        except Exception as exc:  # the baseline is reported, not required
+            line["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

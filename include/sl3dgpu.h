@@ -178,13 +178,35 @@ void sl3dgpu_v3d_free_state(sl3dgpu_v3d_state* state);
  * advances in place. */
 int sl3dgpu_v3d_step(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme,
                      const double* load0, const double* load1, sl3dgpu_step_info* info);
+/* The same step with the load coefficients in device memory. */
+int sl3dgpu_v3d_step_device(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme,
+                            const double* load0, const double* load1, sl3dgpu_step_info* info);
 /* Viscoelastic3D::Surface (Viscoelastic3D.cpp:2032-2051) of the last step's
  * solutions: component 0 U, 1 V, 2 phi; complex m >= 0 columns per degree in
  * the l(l+1)/2 + m layout, into host memory. */
 int sl3dgpu_v3d_surface(sl3dgpu_v3d* op, int component, double* out);
+/* The CUDA stream the operator's kernels run on. */
+void* sl3dgpu_v3d_stream(const sl3dgpu_v3d* op);
+/* The last step's pass residuals (RelativeChange per pass, the stages in
+ * turn): returns their count, copying at most `capacity` into out. */
+int sl3dgpu_v3d_residual_history(const sl3dgpu_v3d* op, double* out, int capacity);
 /* A state's strain coefficients in the reference layouts, node-major blocks:
  * spin -2, spin -1, real spin 0 (GridCoupling::SpectralTensor). Host out. */
 int sl3dgpu_v3d_state_strain(sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, double* out);
+
+/* ---- measurement ------------------------------------------------------------
+ * Kernel launches the library has made since it was loaded. */
+long long sl3dgpu_launch_count(void);
+/* Per-kernel-kind CUDA-event timing of every launch (on its own stream) and
+ * its algorithmic work: kinds 0 Legendre synthesis, 1 Legendre analysis,
+ * 2 ring FFTs, 3 force assembly, 4 strain recovery, 5 band solves,
+ * 6 streaming weights/memory, 7 Anderson sweeps, 8 other. */
+int sl3dgpu_profile_enable(int on);
+int sl3dgpu_profile_reset(void);
+int sl3dgpu_profile_read(int kind, double* ms, long long* launches, double* flops, double* bytes);
+/* The FP64 FMA throughput of the device (GFLOP/s), measured by a short
+ * register-resident kernel: the FP64 path's compute roofline. */
+int sl3dgpu_fp64_fma_peak(double* gflops);
 
 #ifdef __cplusplus
 }

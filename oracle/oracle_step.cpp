@@ -33,6 +33,8 @@
 #include <optional>
 #include <vector>
 
+#include <omp.h>
+
 #include "../include/sl3dgpu.h"
 #include "lstsq.hpp"
 #include "oracle.h"
@@ -741,8 +743,13 @@ class Viscoelastic3D {
   }
 
   // One stage: StartStep, Converge(Respond + AddChannels + StrainOf), Finish.
+  // With `samplePasses` >= 0: the bounded timing sample of a stage -- the
+  // start (StartStep) and exactly that many passes, timed into tStart and
+  // tPasses (seconds), the state returned unchanged.
   State StepOnce(const State& state, double dt, Scheme scheme, const C* loadStart, const C* loadEnd,
-                 Info& info, Solutions& solutionsOut) {
+                 Info& info, Solutions& solutionsOut, int samplePasses = -1, double* tStart = nullptr,
+                 double* tPasses = nullptr) {
+    const double clock0 = omp_get_wtime();
     const auto& flavour = FlavourOf(scheme, dt);
     const auto fs = grid_.FieldSize();
     const std::size_t K = state.m.size();
@@ -831,6 +838,19 @@ class Viscoelastic3D {
       AddLoad(solutions, flavour, loadEnd);
       return StrainOf(solutions, flavour);
     };
+    if (samplePasses >= 0) {
+      if (tStart) *tStart = omp_get_wtime() - clock0;
+      const double clock1 = omp_get_wtime();
+      Spectral it = s0;
+      for (int k = 0; k < samplePasses; ++k) {
+        Spectral next = pass(it);
+        info.residual = RelativeChange(next, it);
+        it = std::move(next);
+      }
+      if (tPasses) *tPasses = omp_get_wtime() - clock1;
+      solutionsOut = std::move(solutions);
+      return state;
+    }
     // Converge (Viscoelastic3D.cpp:1916-1974).
     Spectral s = s0;
     info = Info{};
@@ -842,6 +862,7 @@ class Viscoelastic3D {
       Spectral next = pass(s);
       info.iterations = iteration + 1;
       info.residual = RelativeChange(next, s);
+      history_.push_back(info.residual);
       if (!std::isfinite(info.residual)) break;
       if (info.residual <= options_.rtol) {
         info.converged = true;
@@ -894,6 +915,7 @@ class Viscoelastic3D {
   // Step (Viscoelastic3D.cpp:1982-2030): one stage, or Sdirk2's two backward
   // Euler stages of gamma dt, the second from (1 - r) m_n + r Y_1.
   State Step(const State& state, double dt, Scheme scheme, const C* load0, const C* load1, Info& info) {
+    history_.clear();
     if (scheme != Scheme::Sdirk2 || dt == 0.0) {
       const Scheme one = scheme == Scheme::Sdirk2 ? Scheme::BackwardEuler : scheme;
       return StepOnce(state, dt, one, load0, load1, info, last_);
@@ -949,6 +971,13 @@ class Viscoelastic3D {
   }
 
   const Solutions& Last() const { return last_; }
+  // The bounded timing sample of one backward Euler stage (see StepOnce).
+  void Sample(const State& state, double dt, const C* load0, const C* load1, int passes, double* tStart,
+              double* tPasses) {
+    Info info;
+    StepOnce(state, dt, Scheme::BackwardEuler, load0, load1, info, last_, passes, tStart, tPasses);
+  }
+  const std::vector<double>& History() const { return history_; }
 
  private:
   sl3dgpu_v3d_options options_;
@@ -964,6 +993,7 @@ class Viscoelastic3D {
   std::unique_ptr<Flavour> elastic_;
   std::vector<std::pair<std::pair<int, double>, std::unique_ptr<Flavour>>> flavours_;
   Solutions last_;
+  std::vector<double> history_;
 };
 
 }  // namespace oracle
@@ -1037,6 +1067,26 @@ int oracle_v3d_step(oracle_v3d* h, oracle_state* state, double dt, int scheme, c
   }
   return 0;
 }
+
+int oracle_v3d_residual_history(const oracle_v3d* h, double* out, int capacity) {
+  const auto& v = h->op->History();
+  if (out != nullptr)
+    for (int i = 0; i < capacity && i < static_cast<int>(v.size()); ++i) out[i] = v[i];
+  return static_cast<int>(v.size());
+}
+
+int oracle_v3d_sample(oracle_v3d* h, oracle_state* state, double dt, const double* load0, const double* load1,
+                      int passes, double* start_seconds, double* pass_seconds) {
+  try {
+    h->op->Sample(state->s, dt, reinterpret_cast<const C*>(load0), reinterpret_cast<const C*>(load1), passes,
+                  start_seconds, pass_seconds);
+  } catch (const std::exception&) {
+    return -3;
+  }
+  return 0;
+}
+
+int oracle_threads(void) { return omp_get_max_threads(); }
 
 void oracle_v3d_surface(const oracle_v3d* h, int component, double* out) {
   h->op->Surface(component, reinterpret_cast<C*>(out));

@@ -86,6 +86,11 @@ def lib() -> ctypes.CDLL:
         "sl3dgpu_expand_spin_batch": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
         "sl3dgpu_synthesise_batch": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
         "sl3dgpu_expand_batch": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
+        "sl3dgpu_launch_count": (ctypes.c_longlong, []),
+        "sl3dgpu_profile_enable": (c_int, [c_int]),
+        "sl3dgpu_profile_reset": (c_int, []),
+        "sl3dgpu_profile_read": (c_int, [c_int, P_double, ctypes.POINTER(ctypes.c_longlong), P_double, P_double]),
+        "sl3dgpu_fp64_fma_peak": (c_int, [P_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "profile.cuh"
 
 namespace sl3dgpu {
 namespace {
@@ -295,6 +296,7 @@ int BandFactorBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sy
     SetError("band factor window exceeds shared memory");
     return SL3DGPU_ERR_ARGUMENT;
   }
+  prof::Scope scope(prof::kOther, stream);
   if (lu) {
     SL3D_CUDA(cudaFuncSetAttribute(LuFactorKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
@@ -327,6 +329,14 @@ int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sys
   const size_t smem = static_cast<size_t>(warpsPerBlock) * kRing * kWarp * sizeof(double);
   const int blocks = (itemCount + warpsPerBlock - 1) / warpsPerBlock;
   const auto* items = reinterpret_cast<const WorkItem*>(devItems);
+  double flops = 0.0, bytes = 0.0;
+  for (int i = 0; i < count; ++i) {
+    const auto& s = hostSystems[i];
+    const double n = s.n, r = s.nrhs;
+    flops += lu ? r * (2.0 * n * s.kl + 2.0 * n * (s.kl + s.ku) + n) : r * (4.0 * n * s.ku + 2.0 * n);
+    bytes += 4.0 * 8.0 * n * r + 8.0 * n * (lu ? 2 * s.kl + s.ku + 1 : s.ku + 1);
+  }
+  prof::Scope scope(prof::kBandSolve, stream, flops, bytes);
   if (lu) {
     SL3D_CUDA(cudaFuncSetAttribute(LuSolveKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <numeric>
 
+#include "profile.cuh"
 #include "sht.cuh"
 
 namespace sl3dgpu {
@@ -485,6 +486,7 @@ int Grid::Table(int N, const SpinTable** out) {
     SL3D_CUDA(cudaMemcpy(t.dRowOffset, t.rowOffset.data(), t.rowOffset.size() * sizeof(int),
                          cudaMemcpyHostToDevice));
     dim3 grid((ntheta + 127) / 128, 2 * lmax + 1);
+    prof::Scope scope(prof::kOther, nullptr);
     WignerTableKernel<<<grid, 128>>>(lmax, N, ntheta, dTheta, t.dRowOffset, t.values);
     SL3D_CHECK_LAUNCH();
     SL3D_CUDA(cudaDeviceSynchronize());
@@ -537,9 +539,11 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
     }
     b.maxM = std::max(b.maxM, it.M);
     b.maxN = std::max(b.maxN, it.N);
+    b.flops += 2.0 * it.M * it.N * it.K;
     items.push_back(it);
   }
   b.count = static_cast<int>(items.size());
+  b.analysis = analysis;
   if (b.count > 0) {
     SL3D_CUDA(cudaMalloc(&b.items, items.size() * sizeof(GemmItem)));
     SL3D_CUDA(cudaMemcpy(b.items, items.data(), items.size() * sizeof(GemmItem), cudaMemcpyHostToDevice));
@@ -552,6 +556,7 @@ int Grid::RunGemm(const Batch& b, const double* A, const double* B, double* C, b
                   cudaStream_t stream) {
   if (b.count == 0) return SL3DGPU_OK;
   dim3 grid((b.maxM + kBM - 1) / kBM, (b.maxN + kBN - 1) / kBN, static_cast<unsigned>(b.count));
+  prof::Scope scope(b.analysis ? prof::kLegendreAnalysis : prof::kLegendreSynthesis, stream, b.flops);
   GemmF64Kernel<<<grid, 256, 0, stream>>>(b.items, A, B, C, accumulate);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
@@ -592,6 +597,13 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   SL3D_CUDA(cudaFuncSetAttribute(RingKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
   dim3 grid((count + kRingGroup - 1) / kRingGroup, g.ntheta);
+  // algorithmic traffic: the spectra and the grid values the mode reads and writes
+  const double spec = static_cast<double>(real ? g.lmax + 1 : 2 * g.lmax + 1) * g.ntheta * count * 16.0;
+  const double field = static_cast<double>(g.ntheta) * g.nphi * count * (real ? 8.0 : 16.0);
+  const double wbytes = weight ? static_cast<double>(g.ntheta) * g.nphi * count * 8.0 : 0.0;
+  const double bytes = mode == kRingWeighted ? 2 * spec + wbytes : spec + field + wbytes;
+  const double ffts = static_cast<double>(g.ntheta) * count * (mode == kRingWeighted ? 2 : 1);
+  prof::Scope scope(prof::kRing, stream, ffts * 5.0 * g.nphi * std::log2(static_cast<double>(g.nphi)), bytes);
   RingKernel<<<grid, 256, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
                                           g.dWeights, reinterpret_cast<const double2*>(spectraIn),
                                           fieldsIn, weight, fieldsOut,
@@ -623,6 +635,7 @@ int Grid::ToDevice(int N, bool real, const double* ref, int count, double* dev,
   if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
   const long long total = (real ? RealRows() : SpinRows(N)) * count;
   if (total == 0) return SL3DGPU_OK;
+  prof::Scope scope(prof::kOther, stream);
   ToDeviceKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(
       lmax, N, real, count, t->dRowOffset, reinterpret_cast<const double2*>(ref),
       reinterpret_cast<double2*>(dev));
@@ -636,6 +649,7 @@ int Grid::FromDevice(int N, bool real, const double* dev, int count, double* ref
   if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
   const long long total = (real ? RealRows() : SpinRows(N)) * count;
   if (total == 0) return SL3DGPU_OK;
+  prof::Scope scope(prof::kOther, stream);
   FromDeviceKernel<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(
       lmax, N, real, count, t->dRowOffset, reinterpret_cast<const double2*>(dev),
       reinterpret_cast<double2*>(ref));

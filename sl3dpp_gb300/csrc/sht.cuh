@@ -106,6 +106,8 @@ class Grid {
   struct Batch {
     GemmItem* items = nullptr;
     int count = 0, maxM = 0, maxN = 0;
+    bool analysis = false;
+    double flops = 0.0;  // 2 M N K summed over the items
   };
   std::map<std::array<long long, 6>, Batch> batches_;
   int BatchFor(int N, bool real, bool analysis, int P, int p0, int count, const Batch** out);

@@ -160,6 +160,7 @@ class Viscoelastic3DGpu {
   static constexpr int kMixBlocks = 1024;
 
   V3dState scratch;  // the second buffer set a step writes into
+  std::vector<double> history;  // the last step's pass residuals, stages in turn
 
   ~Viscoelastic3DGpu() {
     if (hostResult) cudaFreeHost(hostResult);
@@ -169,7 +170,8 @@ class Viscoelastic3DGpu {
   int Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt);
   int SetDelta(const double* samples, bool onDevice);
   int ZeroState(V3dState& st);
-  int Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1, sl3dgpu_step_info* info);
+  int Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1, sl3dgpu_step_info* info,
+           bool onDevice = false);
   int Surface(int component, double* out);
   int StrainReference(const V3dState& st, double* out);
 
@@ -883,6 +885,7 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
     SL3D_TRY(Pass(*f, s.p, iteration == 0, sigmaEnd, sNext.p));
     double residual = 0.0;
     SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
+    history.push_back(residual);
     info.iterations = iteration + 1;
     info.residual = residual;
     if (!std::isfinite(residual)) break;
@@ -925,7 +928,7 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
 // Step (Viscoelastic3D.cpp:1982-2030): one stage, or Sdirk2's two backward
 // Euler stages of gamma dt, the second from (1 - r) m_n + r Y_1.
 int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1,
-                            sl3dgpu_step_info* infoOut) {
+                            sl3dgpu_step_info* infoOut, bool onDevice) {
   if (!(dt >= 0.0) || scheme < 0 || scheme > 2) {
     SetError("v3d: dt >= 0 and a scheme of 0 (trapezoid), 1 (backward Euler) or 2 (Sdirk2)");
     return SL3DGPU_ERR_ARGUMENT;
@@ -933,15 +936,17 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
   const double2* s0 = nullptr;
   const double2* s1 = nullptr;
+  const cudaMemcpyKind kind = onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if (load0) {
-    SL3D_CUDA(cudaMemcpyAsync(sigma0.p, load0, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(sigma0.p, load0, lm * sizeof(double2), kind, stream));
     s0 = sigma0.p;
   }
   if (load1) {
-    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, load1, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, load1, lm * sizeof(double2), kind, stream));
     s1 = sigma1.p;
   }
   sl3dgpu_step_info info{};
+  history.clear();
   if (scheme != 2 || dt == 0.0) {
     const int one = scheme == 2 ? 1 : scheme;
     SL3D_TRY(StepOnce(st, scratch, dt, one, s0, s1, info));
@@ -950,14 +955,9 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     const double h = gamma * dt;
     const double2* mid = nullptr;
     if (load0 || load1) {
-      std::vector<double2> v(lm);
-      for (size_t i = 0; i < lm; ++i) {
-        const double ax = load0 ? load0[2 * i] : 0.0, ay = load0 ? load0[2 * i + 1] : 0.0;
-        const double bx = load1 ? load1[2 * i] : 0.0, by = load1 ? load1[2 * i + 1] : 0.0;
-        v[i] = make_double2((1.0 - gamma) * ax + gamma * bx, (1.0 - gamma) * ay + gamma * by);
-      }
-      SL3D_CUDA(cudaMemcpyAsync(sigmaMid.p, v.data(), lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
-      SL3D_CUDA(cudaStreamSynchronize(stream));
+      // the first stage's end: (1 - gamma) of the start load and gamma of the end's
+      LaunchBlend(static_cast<long long>(lm), gamma, s0, s1, sigmaMid.p, stream);
+      SL3D_CHECK_LAUNCH();
       mid = sigmaMid.p;
     }
     sl3dgpu_step_info i1{}, i2{};
@@ -1116,6 +1116,15 @@ extern "C" int sl3dgpu_v3d_step(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, double
   return h->op.Step(state->st, dt, scheme, load0, load1, info);
 }
 
+extern "C" int sl3dgpu_v3d_step_device(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, double dt, int scheme,
+                                       const double* load0, const double* load1, sl3dgpu_step_info* info) {
+  if (h == nullptr || state == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Step(state->st, dt, scheme, load0, load1, info, true);
+}
+
 extern "C" int sl3dgpu_v3d_surface(sl3dgpu_v3d* h, int component, double* out) {
   if (h == nullptr || out == nullptr) {
     SetError("v3d: null argument");
@@ -1130,6 +1139,19 @@ extern "C" int sl3dgpu_v3d_state_strain(sl3dgpu_v3d* h, const sl3dgpu_v3d_state*
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.StrainReference(state->st, out);
+}
+
+extern "C" void* sl3dgpu_v3d_stream(const sl3dgpu_v3d* h) { return h ? h->op.stream : nullptr; }
+
+extern "C" int sl3dgpu_v3d_residual_history(const sl3dgpu_v3d* h, double* out, int capacity) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& v = h->op.history;
+  if (out != nullptr)
+    for (int i = 0; i < capacity && i < static_cast<int>(v.size()); ++i) out[i] = v[i];
+  return static_cast<int>(v.size());
 }
 
 extern "C" int sl3dgpu_standard_earth(int elements, double kelvin_fraction, double kelvin_div, sl3dgpu_layer* out) {

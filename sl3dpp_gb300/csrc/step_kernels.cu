@@ -9,6 +9,7 @@
 #include <cmath>
 
 #include "host/lstsq.hpp"
+#include "profile.cuh"
 #include "step_kernels.cuh"
 
 namespace sl3dgpu {
@@ -499,6 +500,13 @@ __global__ void MixerMixKernel(MixerArgs a) {
   }
 }
 
+__global__ void BlendKernel(long long n, double gamma, const double2* a, const double2* b, double2* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const double2 x = a ? a[i] : C(0, 0), y = b ? b[i] : C(0, 0);
+  out[i] = C((1.0 - gamma) * x.x + gamma * y.x, (1.0 - gamma) * x.y + gamma * y.y);
+}
+
 int StreamBlocks(long long values) {
   const long long b = (values + 255) / 256;
   return static_cast<int>(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
@@ -511,6 +519,7 @@ void LaunchForces(const Geometry& g, const double2* spectral, double2* rhsSph, d
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   const size_t smem = static_cast<size_t>(g.P) * 6 * sizeof(double2);
   cudaFuncSetAttribute(ForceKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  prof::Scope scope(prof::kForce, stream);
   ForceKernel<<<count, 128, smem, stream>>>(g, spectral, rhsSph, rhsTor);
 }
 
@@ -519,53 +528,77 @@ void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTo
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 3 * sizeof(double2);
   cudaFuncSetAttribute(StrainKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  prof::Scope scope(prof::kStrain, stream);
   StrainKernel<<<count, 128, smem, stream>>>(g, solSph, solTor, spectral);
 }
 
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units, const long long* unitOffset,
                    double2* solSph, cudaStream_t stream) {
+  prof::Scope scope(prof::kOther, stream);
   AddLoadKernel<<<g.lmax + 1, 256, 0, stream>>>(g, sigma, units, unitOffset, solSph);
 }
 
 void LaunchSurface(const Geometry& g, const double2* solSph, int component, double2* out, cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  prof::Scope scope(prof::kOther, stream);
   SurfaceKernel<<<(count + 127) / 128, 128, 0, stream>>>(g, solSph, component, out);
 }
 
 void LaunchWeights(const WeightsArgs& a, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, a.values * (8.0 + a.branches * 96.0 + 40.0 + 48.0));
   WeightsKernel<<<StreamBlocks(a.values), 256, 0, stream>>>(a);
 }
 
 void LaunchAdvance(long long values, const double* beta, const double2* d0, const double2* d1, const double* dr,
                    double2* m0, double2* m1, double* mr, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, values * 128.0);
   AdvanceKernel<<<StreamBlocks(values), 256, 0, stream>>>(values, beta, d0, d1, dr, m0, m1, mr);
 }
 
 void LaunchStageCombine(long long values, double r, const double2* a0, const double2* a1, const double* ar,
                         double2* o0, double2* o1, double* orr, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, values * 120.0);
   StageCombineKernel<<<StreamBlocks(values), 256, 0, stream>>>(values, r, a0, a1, ar, o0, o1, orr);
 }
 
 void LaunchCombine(long long values, long long fieldSize, const double* mu, bool first, const double2* m0,
                    const double2* m1, const double* mr, double2* o0, double2* o1, double* orr,
                    cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, values * 88.0);
   CombineKernel<<<StreamBlocks(values), 256, 0, stream>>>(values, fieldSize, mu, first, m0, m1, mr, o0, o1, orr);
+}
+
+void LaunchBlend(long long n, double gamma, const double2* a, const double2* b, double2* out, cudaStream_t stream) {
+  prof::Scope scope(prof::kOther, stream);
+  BlendKernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(n, gamma, a, b, out);
 }
 
 void LaunchRelativeChange(const double* next, const double* now, long long n, double* partial, int partialCount,
                           double* result, cudaStream_t stream) {
-  RelativeChangeKernel<<<partialCount, 256, 0, stream>>>(reinterpret_cast<const double2*>(next),
+  {
+    prof::Scope scope(prof::kOther, stream, 0.0, n * 16.0);
+    RelativeChangeKernel<<<partialCount, 256, 0, stream>>>(reinterpret_cast<const double2*>(next),
                                                         reinterpret_cast<const double2*>(now), n / 2, partial);
+  }
+  prof::Scope scope(prof::kOther, stream);
   ReduceMaxKernel<<<1, 256, 0, stream>>>(partial, partialCount, result);
 }
 
 void LaunchMixerFirst(const MixerArgs& a, cudaStream_t stream) {
+  prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 40.0);
   MixerFirstKernel<<<StreamBlocks(a.n), 256, 0, stream>>>(a.n, a.x, a.gx, a.xPrev, a.fPrev);
 }
 
 void LaunchMixerUpdate(const MixerArgs& a, cudaStream_t stream) {
-  MixerSweepKernel<<<a.blocks, kMixThreads, 0, stream>>>(a);
-  MixerSolveKernel<<<1, 32, 0, stream>>>(a);
+  {
+    prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 8.0 * (6 + a.m));
+    MixerSweepKernel<<<a.blocks, kMixThreads, 0, stream>>>(a);
+  }
+  {
+    prof::Scope scope(prof::kOther, stream);
+    MixerSolveKernel<<<1, 32, 0, stream>>>(a);
+  }
+  prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 8.0 * (2 + a.m));
   MixerMixKernel<<<StreamBlocks(a.n), 256, 0, stream>>>(a);
 }
 

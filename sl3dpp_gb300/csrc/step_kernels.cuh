@@ -94,6 +94,9 @@ void LaunchCombine(long long values, long long fieldSize, const double* mu, bool
                    const double2* m0, const double2* m1, const double* mr, double2* o0, double2* o1,
                    double* orr, cudaStream_t stream);
 
+// out = (1 - gamma) a + gamma b over complex values, a or b null for zero.
+void LaunchBlend(long long n, double gamma, const double2* a, const double2* b, double2* out, cudaStream_t stream);
+
 // RelativeChange: max |n|^2, max |n - o|^2 and finiteness over n doubles
 // (complex pairs), into result[3] on the device.
 void LaunchRelativeChange(const double* next, const double* now, long long n, double* partial,

@@ -77,6 +77,9 @@ def _signatures():
         "sl3dgpu_v3d_step": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_surface": (i, [v, i, v]),
         "sl3dgpu_v3d_state_strain": (i, [v, v, v]),
+        "sl3dgpu_v3d_residual_history": (i, [v, P_double, i]),
+        "sl3dgpu_v3d_step_device": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_stream": (v, [v]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -174,6 +177,28 @@ class Viscoelastic3D:
                                      None if a is None else a.ctypes.data,
                                      None if b is None else b.ctypes.data, ctypes.byref(info)))
         return info
+
+    def StepDevice(self, state: State, dt: float, scheme, load0, load1) -> StepInfo:
+        """Step with the load coefficients already in device memory (CUDA torch tensors)."""
+        code = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        info = StepInfo()
+        check(lib().sl3dgpu_v3d_step_device(self._h, state._h, float(dt), code,
+                                            None if load0 is None else load0.data_ptr(),
+                                            None if load1 is None else load1.data_ptr(), ctypes.byref(info)))
+        return info
+
+    @property
+    def stream(self) -> int:
+        """The CUDA stream (cudaStream_t) the operator's kernels run on."""
+        return lib().sl3dgpu_v3d_stream(self._h) or 0
+
+    def residual_history(self) -> np.ndarray:
+        """The last step's pass residuals, the stages in turn."""
+        n = lib().sl3dgpu_v3d_residual_history(self._h, None, 0)
+        out = np.zeros(max(n, 0))
+        if n > 0:
+            lib().sl3dgpu_v3d_residual_history(self._h, out.ctypes.data_as(P_double), n)
+        return out
 
     def Surface(self, component="U") -> np.ndarray:
         code = COMPONENTS[component] if isinstance(component, str) else int(component)

@@ -173,6 +173,9 @@ def _v3d_sigs(L):
         "oracle_v3d_step": (i, [v, v, d, i, v, v, _ct.POINTER(StepInfo)]),
         "oracle_v3d_surface": (None, [v, i, v]),
         "oracle_v3d_state_strain": (i, [v, v]),
+        "oracle_v3d_residual_history": (i, [v, P_double, i]),
+        "oracle_v3d_sample": (i, [v, v, d, v, v, i, P_double, P_double]),
+        "oracle_threads": (i, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -231,6 +234,23 @@ class OracleStep:
                                     _ct.byref(info))
         assert st == 0
         return info
+
+    def sample(self, dt, passes, load0=None, load1=None):
+        """Seconds of a backward Euler stage's start and of `passes` passes."""
+        a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.complex128)
+        b = None if load1 is None else np.ascontiguousarray(load1, dtype=np.complex128)
+        t0, t1 = _ct.c_double(), _ct.c_double()
+        st = self.L.oracle_v3d_sample(self.h, self.state, dt, None if a is None else a.ctypes.data,
+                                      None if b is None else b.ctypes.data, passes, _ct.byref(t0), _ct.byref(t1))
+        assert st == 0
+        return t0.value, t1.value
+
+    def residual_history(self):
+        n = self.L.oracle_v3d_residual_history(self.h, None, 0)
+        out = np.zeros(max(n, 0))
+        if n > 0:
+            self.L.oracle_v3d_residual_history(self.h, ptr(out), n)
+        return out
 
     def surface(self, component):
         L = self.options.lmax
