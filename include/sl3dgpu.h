@@ -75,6 +75,20 @@ int sl3dgpu_band_solve_batch(const sl3dgpu_band_system* dev_systems,
                              const int* pivots, double* rhs, const double* scales, int lu,
                              void* stream);
 
+/* A banded Cholesky solve (the factor from sl3dgpu_band_cholesky_factor,
+ * LAPACK upper storage, and n x nrhs column-major right-hand sides,
+ * overwritten by the solution) on DEVICE pointers that allocates no device
+ * memory: its scratch is a fixed 2^19-double (4 MiB) array in the library,
+ * held by every GPU that loads it. No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc (their device memory is owned by
+ * another allocator or a fixed arena, or a driver allocation is not
+ * acceptable on their loop). Larger n x nrhs is refused
+ * (SL3DGPU_ERR_ARGUMENT); the first call on a device looks the array's
+ * address up and should come before any stream capture; calls that overlap
+ * on the GPU race on the shared array. */
+int sl3dgpu_band_cholesky_solve_noalloc(const double* ab, int n, int kd, double* b, int nrhs,
+                                        void* stream);
+
 /* ---- the surface grid (include/sl3dpp/SurfaceGrid.hpp:58-287) ---------------
  * A Gauss-Legendre grid for degrees to lmax and spins to nmax, oversampled
  * by `oversampling` (band L' = ceil(oversampling lmax): L' + 1 colatitudes,
