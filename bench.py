@@ -10,13 +10,18 @@ of 500 yr. All inputs are synthetic (numpy default_rng, seeds below).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0). `value` is steps/s with the load coefficients
+Prints one JSON line (rank 0). `value` is steps/s of the mixed form (FP64
+passes and stopping rule, FP32 corrections between them; each step
+warm-started from the previous step's strain) with the load coefficients
 resident in device memory, timed with CUDA events on the operator's stream;
 `e2e` is the same through the C ABI with the loads copied from pinned host
-memory and the surface U and phi read back every step. The arithmetic is FP64
-throughout (the plain FP64 form). `--impl reference` times the CPU
-restatement of the reference's path (oracle/, OpenMP on every host core) on a
-bounded sample of the same workload.
+memory and the surface U and phi read back every step. The plain FP64 form
+then runs the same step sequence: its steps/s (`fp64_gpu`), and the mixed
+form's relative error against it on U and phi at every end-to-end step
+(`rel_err_vs_fp64`; the FP64 form matches the FP64 oracle to 1e-10 in the
+tests). `--precision fp64` makes the FP64 form the headline. `--impl
+reference` times the CPU restatement of the reference's path (oracle/,
+OpenMP on every host core) on a bounded sample of the same workload.
 """
 
 from __future__ import annotations
@@ -47,6 +52,8 @@ RAMP_STEPS = 10
 DT_YEARS = 500.0
 RTOL = 1e-10
 MAX_ITERATIONS = 60
+CORRECTION_RTOL = 1e-5
+METRIC = "3D steps/sec at lmax=256: mixed+warm-start vs plain FP64 GPU at rel err <=1e-8"
 # The FP64 fixed point's passes per step at this workload (both stages),
 # measured by the GPU arm (identical iterate sequences on both arms, pinned
 # pass for pass at small lmax); the CPU sample's steps/s is extrapolated with it.
@@ -61,12 +68,14 @@ def _rescale(lmax):
     LDELTA = max(2, lmax // 4)
 
 
-def workload_config():
-    return {"workload": f"3d_step_lmax{LMAX}_fp64_sdirk2", "lmax": LMAX, "elements": ELEMENTS,
+def workload_config(precision="mixed"):
+    return {"workload": f"3d_step_lmax{LMAX}_{precision}_sdirk2", "lmax": LMAX, "elements": ELEMENTS,
             "order": NGLL - 1, "delta_degree": LDELTA, "delta_rms": DELTA_RMS, "delta_seed": DELTA_SEED,
             "rheology": "maxwell", "cap_degrees": CAP_DEGREES, "cap_thickness_m": CAP_THICKNESS,
             "dt_years": DT_YEARS, "scheme": "sdirk2", "rtol": RTOL, "max_iterations": MAX_ITERATIONS,
-            "anderson_memory": 5, "oversampling": 1.5,
+            "anderson_memory": 5, "oversampling": 1.5, "precision": precision,
+            "correction_rtol": CORRECTION_RTOL if precision == "mixed" else None,
+            "warm_start": "previous step's strain coefficients (the reference's plain warm start)",
             "l2": "working set far above L2 (memory tensors ~3.3 GB per array)",
             "parallelism": "replicas (one independent operator per GPU)"}
 
@@ -134,7 +143,7 @@ class ClockSampler:
 # -- the GPU arm --------------------------------------------------------------------------------
 
 KIND_NAMES = ["legendre_synthesis", "legendre_analysis", "ring_fft", "force_assembly", "strain_recovery",
-              "band_solve", "streaming", "anderson", "other"]
+              "band_solve", "streaming", "anderson", "other", "legendre_f32", "ring_fft_f32", "band_solve_f32"]
 
 
 def profile_read():
@@ -171,14 +180,17 @@ def ncu_traffic(kernel: str):
     return None
 
 
-def build_operator(device):
+def build_operator(device, precision):
     import torch
 
     from sl3dpp_gb300 import configs
     from sl3dpp_gb300.grid import SurfaceGrid
     from sl3dpp_gb300.viscoelastic3d import Options, Viscoelastic3D, standard_earth
 
-    op = Viscoelastic3D(standard_earth(ELEMENTS), Options.defaults(LMAX, NGLL, rtol=RTOL, max_iterations=MAX_ITERATIONS))
+    op = Viscoelastic3D(standard_earth(ELEMENTS),
+                        Options.defaults(LMAX, NGLL, rtol=RTOL, max_iterations=MAX_ITERATIONS,
+                                         precision=1 if precision == "mixed" else 0,
+                                         correction_rtol=CORRECTION_RTOL))
     grid = SurfaceGrid(LMAX, 0, 1.5)
     c = configs.delta_coefficients(LMAX, LDELTA, DELTA_RMS, DELTA_SEED)
     pattern = grid.SynthesiseBatch(torch.tensor(c, device=device), 1)
@@ -191,13 +203,13 @@ def build_operator(device):
     return op, full, dt
 
 
-def gpu_arm(args, rank, world, device):
+def gpu_arm(args, rank, world, device, precision):
     import torch
 
     from sl3dpp_gb300._lib import lib
 
     t_setup = time.time()
-    op, full, dt = build_operator(device)
+    op, full, dt = build_operator(device, precision)
     torch.cuda.synchronize()
     setup_s = time.time() - t_setup
     loads = [load_ramp(full, n).contiguous() for n in range(args.warmup + 2 * args.steps + 2)]
@@ -215,12 +227,13 @@ def gpu_arm(args, rank, world, device):
     torch.cuda.synchronize()
     launches0 = lib().sl3dgpu_launch_count()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    passes = 0
+    passes = corrections = 0
     with ClockSampler(torch.cuda.current_device()) as clocks:
         start.record(stream)
         for _ in range(args.steps):
             info = op.StepDevice(state, dt, "sdirk2", loads[n], loads[n + 1])
             passes += info.iterations
+            corrections += info.correction_passes
             infos.append(info)
             n += 1
         stop.record(stream)
@@ -235,39 +248,53 @@ def gpu_arm(args, rank, world, device):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    surfaces = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
         op.Step(state, dt, "sdirk2", host_loads[n], host_loads[n + 1])
         U = op.Surface("U")
         phi = op.Surface("phi")
+        surfaces.append((U, phi))
         n += 1
     e2e_s = time.perf_counter() - t0
-    assert np.all(np.isfinite(U)) and np.all(np.isfinite(phi))
+    assert all(np.all(np.isfinite(U)) and np.all(np.isfinite(phi)) for U, phi in surfaces)
     times = torch.tensor([ms / 1e3, e2e_s], device=device, dtype=torch.float64)
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
     return {"op": op, "seconds": times[0].item(), "e2e_seconds": times[1].item(), "passes": passes,
+            "corrections": corrections, "surfaces": surfaces,
             "infos": infos, "profile": prof, "launches": launches, "clocks": clocks.summary(),
             "setup_s": setup_s, "load_bytes": int(full.numel() * 16)}
 
 
-def roofline(prof, fp64_gflops):
+def roofline(prof, fp64_gflops, fp32_gflops):
+    """The dominant kernel kind against its bound: the contractions against
+    the FMA throughput of their precision, measured live; the rest against the
+    measured HBM copy bandwidth."""
     kind = max(prof, key=lambda k: prof[k]["ms"])
     p = prof[kind]
     peaks, source = measured_peaks()
     per_launch_s = p["ms"] / 1e3 / max(p["launches"], 1)
-    if p["flops"] > 0 and kind in ("legendre_synthesis", "legendre_analysis", "band_solve"):
+    share = p["ms"] / sum(v["ms"] for v in prof.values())
+    compute = {"legendre_synthesis": ("fp64", fp64_gflops), "legendre_analysis": ("fp64", fp64_gflops),
+               "legendre_f32": ("fp32", fp32_gflops)}
+    if p["flops"] > 0 and kind in compute:
+        bound, gflops = compute[kind]
         achieved = p["flops"] / max(p["launches"], 1) / per_launch_s / 1e12
-        peak = fp64_gflops / 1e3
-        return {"kernel": kind, "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        peak = gflops / 1e3
+        return {"kernel": kind, "bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": ncu_traffic(kind),
-                "peak_source": "FP64 FMA throughput measured live by sl3dgpu_fp64_fma_peak (FP64 arithmetic: no FP64 "
-                               "figure in MEASURED_PEAKS.json)",
-                "share_of_timed": p["ms"] / sum(v["ms"] for v in prof.values())}
+                "peak_source": f"{bound.upper()} FMA throughput measured live by sl3dgpu_{bound}_fma_peak (CUDA-core "
+                               "arithmetic: MEASURED_PEAKS.json holds HBM and bf16 tensor figures only)",
+                "share_of_timed": share}
     achieved = p["bytes"] / max(p["launches"], 1) / per_launch_s / 1e9
     return {"kernel": kind, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peaks["hbm_gbs"], "traffic": ncu_traffic(kind), "peak_source": source,
-            "share_of_timed": p["ms"] / sum(v["ms"] for v in prof.values())}
+            "share_of_timed": share}
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
 # -- the CPU restatement (oracle), a bounded sample --------------------------------------------
@@ -316,6 +343,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-fp64-compare", action="store_true", help="skip the plain FP64 form's run")
     ap.add_argument("--lmax", type=int, default=LMAX, help="a smaller workload for development runs")
     args = ap.parse_args()
     if args.lmax != LMAX:
@@ -341,10 +370,10 @@ def main():
                 samples.append(r)
         value = float(np.median([s["value"] for s in samples]))
         base = samples[-1]
-        line = {"metric": "3D steps/sec at lmax=256 (FP64)", "value": value, "unit": "steps/s", "n_gpus": 0,
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": 0,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": workload_config(), "impl": "reference",
+                "data": "synthetic", "config": workload_config("fp64"), "impl": "reference",
                 "cpu_baseline": {"value": value, "unit": "steps/s", "cores": base["cores"], "kind": "port",
                                  "sample": base["sample"]},
                 "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -364,32 +393,57 @@ def main():
     from sl3dpp_gb300._lib import lib
     import ctypes
 
-    fp64 = ctypes.c_double()
+    fp64, fp32 = ctypes.c_double(), ctypes.c_double()
     lib().sl3dgpu_fp64_fma_peak(ctypes.byref(fp64))
-    r = gpu_arm(args, rank, world, device)
+    lib().sl3dgpu_fp32_fma_peak(ctypes.byref(fp32))
+    r = gpu_arm(args, rank, world, device, args.precision)
     steps_total = args.steps * world
     value = steps_total / r["seconds"]
     e2e = steps_total / r["e2e_seconds"]
     passes_per_step = r["passes"] / args.steps
-    line = {"metric": "3D steps/sec at lmax=256 (FP64)", "value": value, "unit": "steps/s", "n_gpus": world,
+    line = {"metric": METRIC if args.precision == "mixed" else "3D steps/sec at lmax=256 (plain FP64 GPU)",
+            "value": value, "unit": "steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["seconds"] * 1e3 / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded delta field and ice-cap load; random-free radial Earth)",
-            "config": workload_config(),
+            "config": workload_config(args.precision),
             "passes_per_step": passes_per_step,
+            "correction_passes_per_step": r["corrections"] / args.steps,
             "converged_steps": sum(int(i.converged) for i in r["infos"][args.warmup:]),
             "final_residual": r["infos"][-1].residual,
-            "roofline": roofline(r["profile"], fp64.value),
-            "kernel_ms": {k: round(v["ms"], 3) for k, v in r["profile"].items()},
+            "roofline": roofline(r["profile"], fp64.value, fp32.value),
+            "kernel_ms": {k: round(v["ms"], 3) for k, v in r["profile"].items() if v["launches"]},
             "gpu_launches": int(r["launches"]),
             "clocks": r["clocks"],
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 2 * r["load_bytes"],
                     "d2h_bytes_per_step": 2 * r["load_bytes"]},
-            "setup_seconds": r["setup_s"]}
+            "setup_seconds": r["setup_s"],
+            "fma_peaks_gflops": {"fp64": fp64.value, "fp32": fp32.value}}
+    fp64_passes = None
+    if args.precision == "mixed" and not args.no_fp64_compare:
+        mixed_surfaces = r["surfaces"]
+        del r
+        r64 = gpu_arm(args, rank, world, device, "fp64")
+        fp64_value = steps_total / r64["seconds"]
+        fp64_passes = r64["passes"] / args.steps
+        errs = [(rel_err(m[0], f[0]), rel_err(m[1], f[1])) for m, f in zip(mixed_surfaces, r64["surfaces"])]
+        line["fp64_gpu"] = {"value": fp64_value, "unit": "steps/s", "ms_per_step": r64["seconds"] * 1e3 / args.steps,
+                            "passes_per_step": fp64_passes,
+                            "e2e": steps_total / r64["e2e_seconds"],
+                            "kernel_ms": {k: round(v["ms"], 3) for k, v in r64["profile"].items() if v["launches"]},
+                            "roofline": roofline(r64["profile"], fp64.value, fp32.value),
+                            "clocks": r64["clocks"]}
+        line["speedup_vs_fp64_gpu"] = value / fp64_value
+        line["rel_err_vs_fp64"] = {"U": max(e[0] for e in errs), "phi": max(e[1] for e in errs),
+                                   "steps_compared": len(errs),
+                                   "per_step": [[round(a, 14), round(b, 14)] for a, b in errs]}
+    elif args.precision == "fp64":
+        fp64_passes = passes_per_step
     if rank == 0 and not args.no_cpu_baseline:
         try:
             sampler = CpuSampler()
-            line["cpu_baseline"] = {k: v for k, v in sampler.sample(passes_per_step, 2).items()
+            line["cpu_baseline"] = {k: v for k, v in sampler.sample(fp64_passes or PASSES_PER_STEP, 2).items()
                                     if k != "seconds_per_step"}
         except Exception as exc:  # the baseline is reported, not required
             line["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}

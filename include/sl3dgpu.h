@@ -141,6 +141,7 @@ typedef struct sl3dgpu_v3d_options {
   int anderson_memory;   /* 5 */
   double anderson_rate;  /* 0.5 */
   int precision;         /* 0: FP64 throughout; 1: mixed (see sl3dgpu_v3d_create) */
+  double correction_rtol; /* mixed form: relative change that ends an FP32 correction, 1e-5 */
 } sl3dgpu_v3d_options;
 
 /* Viscoelastic3D::StepInfo (Viscoelastic3D.hpp:357-375). */
@@ -149,6 +150,7 @@ typedef struct sl3dgpu_step_info {
   double residual;
   int converged;
   int mixed_passes;
+  int correction_passes; /* mixed form: FP32 correction passes (not counted in iterations) */
 } sl3dgpu_step_info;
 
 /* The configurations' Earth (radius 6371 km, fluid core to 3480 km, linear
@@ -162,7 +164,15 @@ int sl3dgpu_standard_earth(int elements, double kelvin_fraction, double kelvin_d
 /* The 3D operator: Viscoelastic3D's constructor (src/Viscoelastic3D.cpp:169-356)
  * over the layered Earth, at the Gauss memory points. The unrelaxed degree
  * systems are assembled on the host and factorised on the GPU; delta is zero
- * until sl3dgpu_v3d_set_delta. */
+ * until sl3dgpu_v3d_set_delta.
+ *
+ * precision 1 (the mixed form) keeps the FP64 passes and the stopping rule
+ * (relative change <= rtol on an FP64 pass, whose result is the step's) and
+ * replaces the iterations between FP64 passes by a correction solved in
+ * FP32 (transforms, band solves with FP32 copies of the FP64 factors, force
+ * and strain maps, Anderson mixing with FP64 Gram sums), iterated until its
+ * relative change is at most correction_rtol. No counterpart in the
+ * reference, whose Converge is FP64 throughout. */
 typedef struct sl3dgpu_v3d sl3dgpu_v3d;
 typedef struct sl3dgpu_v3d_state sl3dgpu_v3d_state;
 int sl3dgpu_v3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options* options,
@@ -204,6 +214,9 @@ void* sl3dgpu_v3d_stream(const sl3dgpu_v3d* op);
 /* The last step's pass residuals (RelativeChange per pass, the stages in
  * turn): returns their count, copying at most `capacity` into out. */
 int sl3dgpu_v3d_residual_history(const sl3dgpu_v3d* op, double* out, int capacity);
+/* The mixed form's last step: the relative change of every FP32 correction
+ * pass in turn (empty in the FP64 form). No reference counterpart. */
+int sl3dgpu_v3d_correction_history(const sl3dgpu_v3d* op, double* out, int capacity);
 /* A state's strain coefficients in the reference layouts, node-major blocks:
  * spin -2, spin -1, real spin 0 (GridCoupling::SpectralTensor). Host out. */
 int sl3dgpu_v3d_state_strain(sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, double* out);
@@ -214,13 +227,16 @@ long long sl3dgpu_launch_count(void);
 /* Per-kernel-kind CUDA-event timing of every launch (on its own stream) and
  * its algorithmic work: kinds 0 Legendre synthesis, 1 Legendre analysis,
  * 2 ring FFTs, 3 force assembly, 4 strain recovery, 5 band solves,
- * 6 streaming weights/memory, 7 Anderson sweeps, 8 other. */
+ * 6 streaming weights/memory, 7 Anderson sweeps, 8 other, and the mixed
+ * form's FP32 passes: 9 Legendre contractions, 10 ring FFTs, 11 band solves. */
 int sl3dgpu_profile_enable(int on);
 int sl3dgpu_profile_reset(void);
 int sl3dgpu_profile_read(int kind, double* ms, long long* launches, double* flops, double* bytes);
 /* The FP64 FMA throughput of the device (GFLOP/s), measured by a short
  * register-resident kernel: the FP64 path's compute roofline. */
 int sl3dgpu_fp64_fma_peak(double* gflops);
+/* The same for FP32 FMA (the mixed form's correction passes). */
+int sl3dgpu_fp32_fma_peak(double* gflops);
 
 #ifdef __cplusplus
 }

@@ -1064,6 +1064,7 @@ int oracle_v3d_step(oracle_v3d* h, oracle_state* state, double dt, int scheme, c
     info->residual = i.residual;
     info->converged = i.converged ? 1 : 0;
     info->mixed_passes = i.mixedPasses;
+    info->correction_passes = 0;
   }
   return 0;
 }

@@ -91,6 +91,7 @@ def lib() -> ctypes.CDLL:
         "sl3dgpu_profile_reset": (c_int, []),
         "sl3dgpu_profile_read": (c_int, [c_int, P_double, ctypes.POINTER(ctypes.c_longlong), P_double, P_double]),
         "sl3dgpu_fp64_fma_peak": (c_int, [P_double]),
+        "sl3dgpu_fp32_fma_peak": (c_int, [P_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

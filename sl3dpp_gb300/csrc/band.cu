@@ -166,84 +166,84 @@ struct WorkItem {
   int column;
 };
 
-__device__ inline double LoadRhs(const sl3dgpu_band_system& s, const double* rhs,
-                                 const double* scales, int j, int col) {
-  if (j == s.pinned0 || j == s.pinned1) return 0.0;
-  double b = rhs[s.rhs + static_cast<long long>(j) * s.nrhs + col];
+template <class T>
+__device__ inline T LoadRhs(const sl3dgpu_band_system& s, const T* rhs, const T* scales, int j, int col) {
+  if (j == s.pinned0 || j == s.pinned1) return T(0);
+  T b = rhs[s.rhs + static_cast<long long>(j) * s.nrhs + col];
   if (s.scale >= 0) b *= scales[s.scale + j];
   return b;
 }
 
-__global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items,
-                                    int itemCount, const double* bands, double* rhs,
-                                    const double* scales) {
+template <class T>
+__global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items, int itemCount,
+                                    const T* bands, T* rhs, const T* scales) {
   const int warp = blockIdx.x * (blockDim.x / kWarp) + threadIdx.x / kWarp;
   const int lane = threadIdx.x % kWarp;
-  extern __shared__ double ringAll[];
-  double* ring = ringAll + (threadIdx.x / kWarp) * kRing * kWarp;
+  extern __shared__ __align__(16) unsigned char ringBytes[];
+  T* ring = reinterpret_cast<T*>(ringBytes) + (threadIdx.x / kWarp) * kRing * kWarp;
   if (warp >= itemCount) return;
   const WorkItem item = items[warp];
   const sl3dgpu_band_system s = systems[item.system];
   const int col = item.column + lane;
   const bool live = col < s.nrhs;
   const int n = s.n, kd = s.ku, ld = kd + 1;
-  const double* ab = bands + s.band;
-  double* x = rhs + s.rhs;
+  const T* ab = bands + s.band;
+  T* x = rhs + s.rhs;
   // U^T y = b, forward.
   for (int j = 0; j < n; ++j) {
-    double sum = live ? LoadRhs(s, rhs, scales, j, col) : 0.0;
-    const double* column = ab + static_cast<long long>(j) * ld + kd - j;  // column[i] = U(i, j)
+    T sum = live ? LoadRhs(s, rhs, scales, j, col) : T(0);
+    const T* column = ab + static_cast<long long>(j) * ld + kd - j;  // column[i] = U(i, j)
     for (int i = max(0, j - kd); i < j; ++i) sum -= __ldg(column + i) * ring[(i % kRing) * kWarp + lane];
-    const double y = sum / __ldg(column + j);
+    const T y = sum / __ldg(column + j);
     ring[(j % kRing) * kWarp + lane] = y;
     if (live) x[static_cast<long long>(j) * s.nrhs + col] = y;
   }
   // U x = y, backward: row i takes its updates from j = i + kd down to i + 1.
   for (int i = n - 1; i >= 0; --i) {
-    double v = live ? x[static_cast<long long>(i) * s.nrhs + col] : 0.0;
+    T v = live ? x[static_cast<long long>(i) * s.nrhs + col] : T(0);
     for (int j = min(n - 1, i + kd); j > i; --j)
       v -= __ldg(ab + static_cast<long long>(j) * ld + kd + i - j) * ring[(j % kRing) * kWarp + lane];
     v /= __ldg(ab + static_cast<long long>(i) * ld + kd);
     ring[(i % kRing) * kWarp + lane] = v;
     if (live) {
-      double out = v;
+      T out = v;
       if (s.scale >= 0) out *= scales[s.scale + i];
       x[static_cast<long long>(i) * s.nrhs + col] = out;
     }
   }
 }
 
-__global__ void LuSolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items,
-                              int itemCount, const double* bands, const int* pivotsAll,
-                              double* rhs, const double* scales) {
+template <class T>
+__global__ void LuSolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items, int itemCount,
+                              const T* bands, const int* pivotsAll, T* rhs, const T* scales) {
   const int warp = blockIdx.x * (blockDim.x / kWarp) + threadIdx.x / kWarp;
   const int lane = threadIdx.x % kWarp;
-  extern __shared__ double ringAll[];
-  double* ring = ringAll + (threadIdx.x / kWarp) * kRing * kWarp;
+  extern __shared__ __align__(16) unsigned char ringBytes[];
+  T* ring = reinterpret_cast<T*>(ringBytes) + (threadIdx.x / kWarp) * kRing * kWarp;
   if (warp >= itemCount) return;
   const WorkItem item = items[warp];
   const sl3dgpu_band_system s = systems[item.system];
   const int col = item.column + lane;
   const bool live = col < s.nrhs;
   const int n = s.n, kl = s.kl, ku = s.ku, kv = kl + ku, ld = 2 * kl + ku + 1;
-  const double* ab = bands + s.band;
+  const T* ab = bands + s.band;
   const int* pivots = pivotsAll + s.pivots;
-  double* x = rhs + s.rhs;
+  T* x = rhs + s.rhs;
   auto at = [&](int i, int j) { return __ldg(ab + static_cast<long long>(j) * ld + kv + i - j); };
-  auto slot = [&](int i) -> double& { return ring[(i % kRing) * kWarp + lane]; };
+  auto slot = [&](int i) -> T& { return ring[(i % kRing) * kWarp + lane]; };
   // L y = P^T b: the window x_j .. x_{j+kl} in the ring, interchanges and
   // eliminations in turn.
-  for (int i = 0; i < min(kl, n); ++i) slot(i) = live ? LoadRhs(s, rhs, scales, i, col) : 0.0;
+  for (int i = 0; i < min(kl, n); ++i) slot(i) = live ? LoadRhs(s, rhs, scales, i, col) : T(0);
   for (int j = 0; j < n; ++j) {
-    if (j + kl < n) slot(j + kl) = live ? LoadRhs(s, rhs, scales, j + kl, col) : 0.0;
+    if (j + kl < n) slot(j + kl) = live ? LoadRhs(s, rhs, scales, j + kl, col) : T(0);
     if (j + 1 < n) {
       const int p = pivots[j];
       if (p != j) {
-        const double t = slot(p);
+        const T t = slot(p);
         slot(p) = slot(j);
         slot(j) = t;
       }
-      const double xj = slot(j);
+      const T xj = slot(j);
       const int lm = min(kl, n - 1 - j);
       for (int i = j + 1; i <= j + lm; ++i) slot(i) -= at(i, j) * xj;
     }
@@ -251,12 +251,12 @@ __global__ void LuSolveKernel(const sl3dgpu_band_system* systems, const WorkItem
   }
   // U x = y with kl + ku superdiagonals, backward.
   for (int i = n - 1; i >= 0; --i) {
-    double v = live ? x[static_cast<long long>(i) * s.nrhs + col] : 0.0;
+    T v = live ? x[static_cast<long long>(i) * s.nrhs + col] : T(0);
     for (int j = min(n - 1, i + kv); j > i; --j) v -= at(i, j) * slot(j);
     v /= at(i, i);
     slot(i) = v;
     if (live) {
-      double out = v;
+      T out = v;
       if (s.scale >= 0) out *= scales[s.scale + i];
       x[static_cast<long long>(i) * s.nrhs + col] = out;
     }
@@ -319,14 +319,15 @@ std::vector<int2> BandWorkItems(const sl3dgpu_band_system* hostSystems, int coun
   return items;
 }
 
-int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems,
-                   int count, const int2* devItems, int itemCount, const double* bands,
-                   const int* pivots, double* rhs, const double* scales, int lu,
-                   cudaStream_t stream) {
+namespace {
+template <class T>
+int SolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+               const int2* devItems, int itemCount, const T* bands, const int* pivots, T* rhs, const T* scales,
+               int lu, cudaStream_t stream) {
   if (itemCount == 0) return SL3DGPU_OK;
   if (int st = Validate(hostSystems, count, lu != 0); st != SL3DGPU_OK) return st;
   constexpr int warpsPerBlock = 4;
-  const size_t smem = static_cast<size_t>(warpsPerBlock) * kRing * kWarp * sizeof(double);
+  const size_t smem = static_cast<size_t>(warpsPerBlock) * kRing * kWarp * sizeof(T);
   const int blocks = (itemCount + warpsPerBlock - 1) / warpsPerBlock;
   const auto* items = reinterpret_cast<const WorkItem*>(devItems);
   double flops = 0.0, bytes = 0.0;
@@ -334,23 +335,38 @@ int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sys
     const auto& s = hostSystems[i];
     const double n = s.n, r = s.nrhs;
     flops += lu ? r * (2.0 * n * s.kl + 2.0 * n * (s.kl + s.ku) + n) : r * (4.0 * n * s.ku + 2.0 * n);
-    bytes += 4.0 * 8.0 * n * r + 8.0 * n * (lu ? 2 * s.kl + s.ku + 1 : s.ku + 1);
+    bytes += 4.0 * sizeof(T) * n * r + sizeof(T) * n * (lu ? 2 * s.kl + s.ku + 1 : s.ku + 1);
   }
-  prof::Scope scope(prof::kBandSolve, stream, flops, bytes);
+  prof::Scope scope(sizeof(T) == sizeof(float) ? prof::kBandSolve32 : prof::kBandSolve, stream, flops, bytes);
   if (lu) {
-    SL3D_CUDA(cudaFuncSetAttribute(LuSolveKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SL3D_CUDA(cudaFuncSetAttribute(LuSolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
-    LuSolveKernel<<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount,
-                                                                   bands, pivots, rhs, scales);
+    LuSolveKernel<T><<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount, bands, pivots,
+                                                                     rhs, scales);
   } else {
-    SL3D_CUDA(cudaFuncSetAttribute(CholeskySolveKernel,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SL3D_CUDA(cudaFuncSetAttribute(CholeskySolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
-    CholeskySolveKernel<<<blocks, warpsPerBlock * kWarp, smem, stream>>>(
-        devSystems, items, itemCount, bands, rhs, scales);
+    CholeskySolveKernel<T><<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount, bands,
+                                                                           rhs, scales);
   }
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
+}
+}  // namespace
+
+int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                   const int2* devItems, int itemCount, const double* bands, const int* pivots, double* rhs,
+                   const double* scales, int lu, cudaStream_t stream) {
+  return SolveBatch<double>(devSystems, hostSystems, count, devItems, itemCount, bands, pivots, rhs, scales, lu,
+                            stream);
+}
+
+// The same solves in FP32 (the mixed form's correction passes).
+int BandSolveBatchF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                    const int2* devItems, int itemCount, const float* bands, const int* pivots, float* rhs,
+                    const float* scales, int lu, cudaStream_t stream) {
+  return SolveBatch<float>(devSystems, hostSystems, count, devItems, itemCount, bands, pivots, rhs, scales, lu,
+                           stream);
 }
 
 }  // namespace sl3dgpu

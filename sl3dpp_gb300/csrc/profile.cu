@@ -113,33 +113,33 @@ extern "C" int sl3dgpu_profile_read(int kind, double* ms, long long* launches, d
 namespace {
 
 // Eight independent FMA chains per thread.
-__global__ void Fp64FmaKernel(double* out, int iters, double a, double b) {
-  double x[8];
+template <class T>
+__global__ void FmaKernel(T* out, int iters, T a, T b) {
+  T x[8];
   for (int i = 0; i < 8; ++i) x[i] = threadIdx.x + i;
   for (int i = 0; i < iters; ++i)
 #pragma unroll
     for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
-  double s = 0.0;
+  T s = 0;
   for (int k = 0; k < 8; ++k) s += x[k];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-}  // namespace
-
-extern "C" int sl3dgpu_fp64_fma_peak(double* gflops) {
+template <class T>
+int FmaPeak(double* gflops, int iters) {
   int sms = 0;
   SL3D_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
-  const int blocks = sms * 16, threads = 256, iters = 4096;
-  double* out = nullptr;
-  SL3D_CUDA(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  const int blocks = sms * 16, threads = 256;
+  T* out = nullptr;
+  SL3D_CUDA(cudaMalloc(&out, sizeof(T) * blocks * threads));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  Fp64FmaKernel<<<blocks, threads>>>(out, 16, 0.999, 0.001);
+  FmaKernel<T><<<blocks, threads>>>(out, 16, T(0.999), T(0.001));
   float best = 1e30f;
   for (int rep = 0; rep < 3; ++rep) {
     cudaEventRecord(e0);
-    Fp64FmaKernel<<<blocks, threads>>>(out, iters, 0.999, 0.001);
+    FmaKernel<T><<<blocks, threads>>>(out, iters, T(0.999), T(0.001));
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.0f;
@@ -157,3 +157,8 @@ extern "C" int sl3dgpu_fp64_fma_peak(double* gflops) {
   *gflops = 2.0 * 8 * iters * static_cast<double>(blocks) * threads / best / 1e6;
   return SL3DGPU_OK;
 }
+
+}  // namespace
+
+extern "C" int sl3dgpu_fp64_fma_peak(double* gflops) { return FmaPeak<double>(gflops, 4096); }
+extern "C" int sl3dgpu_fp32_fma_peak(double* gflops) { return FmaPeak<float>(gflops, 32768); }

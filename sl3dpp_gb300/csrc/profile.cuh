@@ -18,7 +18,10 @@ enum Kind {
   kStream = 6,
   kMixer = 7,
   kOther = 8,
-  kKinds = 9
+  kLegendre32 = 9,   // the mixed form's FP32 contractions (synthesis and analysis)
+  kRing32 = 10,      // its FP32 ring passes
+  kBandSolve32 = 11, // its FP32 band solves
+  kKinds = 12
 };
 
 // Counts one launch; with timing on, records its start event.

@@ -94,23 +94,24 @@ __global__ void WignerTableKernel(int lmax, int N, int ntheta, const double* the
 
 constexpr int kBM = 64, kBN = 64, kBK = 16;
 
-__global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, const double* A,
-                                                     const double* B, double* C, bool accumulate) {
+template <class T>
+__global__ void __launch_bounds__(256) GemmKernel(const GemmItem* items, const T* A, const T* B, T* C,
+                                                  bool accumulate) {
   const GemmItem it = items[blockIdx.z];
   const int i0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
   if (i0 >= it.M || n0 >= it.N) return;
-  __shared__ double As[kBK][kBM + 1];
-  __shared__ double Bs[kBK][kBN];
+  __shared__ T As[kBK][kBM + 1];
+  __shared__ T Bs[kBK][kBN];
   const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-  const double* a = A + it.a;
-  const double* b = B + it.b;
-  double acc[4][4] = {};
+  const T* a = A + it.a;
+  const T* b = B + it.b;
+  T acc[4][4] = {};
   for (int k0 = 0; k0 < it.K; k0 += kBK) {
     if (it.sAk == 1) {
       for (int e = tid; e < kBM * kBK; e += 256) {
         const int kk = e % kBK, ii = e / kBK;
         const int i = i0 + ii, k = k0 + kk;
-        As[kk][ii] = (i < it.M && k < it.K) ? a[static_cast<long long>(i) * it.sAi + k] : 0.0;
+        As[kk][ii] = (i < it.M && k < it.K) ? a[static_cast<long long>(i) * it.sAi + k] : T(0);
       }
     } else {
       for (int e = tid; e < kBM * kBK; e += 256) {
@@ -118,18 +119,18 @@ __global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, cons
         const int i = i0 + ii, k = k0 + kk;
         As[kk][ii] = (i < it.M && k < it.K)
                          ? a[static_cast<long long>(i) * it.sAi + static_cast<long long>(k) * it.sAk]
-                         : 0.0;
+                         : T(0);
       }
     }
     for (int e = tid; e < kBK * kBN; e += 256) {
       const int nn = e % kBN, kk = e / kBN;
       const int n = n0 + nn, k = k0 + kk;
-      Bs[kk][nn] = (n < it.N && k < it.K) ? b[static_cast<long long>(k) * it.ldb + n] : 0.0;
+      Bs[kk][nn] = (n < it.N && k < it.K) ? b[static_cast<long long>(k) * it.ldb + n] : T(0);
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < kBK; ++kk) {
-      double av[4], bv[4];
+      T av[4], bv[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r) av[r] = As[kk][ty + 16 * r];
 #pragma unroll
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, cons
     }
     __syncthreads();
   }
-  double* c = C + it.c;
+  T* c = C + it.c;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int i = i0 + ty + 16 * r;
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, cons
     for (int q = 0; q < 4; ++q) {
       const int n = n0 + tx + 16 * q;
       if (n >= it.N) continue;
-      double* out = c + static_cast<long long>(i) * it.ldc + n;
+      T* out = c + static_cast<long long>(i) * it.ldc + n;
       *out = accumulate ? acc[r][q] + *out : acc[r][q];
     }
   }
@@ -158,15 +159,41 @@ __global__ void __launch_bounds__(256) GemmF64Kernel(const GemmItem* items, cons
 
 // -- FFT ---------------------------------------------------------------------------------
 
-__device__ inline double2 Mul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+template <class T2>
+struct Real;
+template <>
+struct Real<double2> {
+  using type = double;
+};
+template <>
+struct Real<float2> {
+  using type = float;
+};
+
+template <class T2>
+__device__ inline T2 Make(typename Real<T2>::type x, typename Real<T2>::type y) {
+  T2 v;
+  v.x = x;
+  v.y = y;
+  return v;
 }
-__device__ inline double2 Add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ inline double2 Sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+template <class T2>
+__device__ inline T2 Mul(T2 a, T2 b) {
+  return Make<T2>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <class T2>
+__device__ inline T2 Add(T2 a, T2 b) {
+  return Make<T2>(a.x + b.x, a.y + b.y);
+}
+template <class T2>
+__device__ inline T2 Sub(T2 a, T2 b) {
+  return Make<T2>(a.x - b.x, a.y - b.y);
+}
 
 // e^{sign 2 pi i e / n} from the table of e^{2 pi i x / n}.
-__device__ inline double2 Twiddle(const double2* tw, int e, int n, int sign) {
-  double2 w = tw[e % n];
+template <class T2>
+__device__ inline T2 Twiddle(const T2* tw, int e, int n, int sign) {
+  T2 w = tw[e % n];
   if (sign < 0) w.y = -w.y;
   return w;
 }
@@ -174,11 +201,11 @@ __device__ inline double2 Twiddle(const double2* tw, int e, int n, int sign) {
 // Stockham autosort over `groups` transforms of length n held at
 // buf0 + g * n (ping-pong with buf1 + g * n); `sign` +1 synthesis, -1
 // analysis. Returns 0 when the result is in buf0, 1 in buf1.
-__device__ int StockhamFft(double2* buf0, double2* buf1, int groups, const FftPlan& plan,
-                           const double2* tw, int sign) {
+template <class T2>
+__device__ int StockhamFft(T2* buf0, T2* buf1, int groups, const FftPlan& plan, const T2* tw, int sign) {
   const int n = plan.n;
-  double2* src = buf0;
-  double2* dst = buf1;
+  T2* src = buf0;
+  T2* dst = buf1;
   int Ns = 1;
   for (int s = 0; s < plan.stages; ++s) {
     const int r = plan.radix[s];
@@ -186,10 +213,10 @@ __device__ int StockhamFft(double2* buf0, double2* buf1, int groups, const FftPl
     const int stride = n / (Ns * r);
     for (int t = threadIdx.x; t < groups * m; t += blockDim.x) {
       const int g = t / m, idx = t % m;
-      const double2* in = src + g * n;
-      double2* out = dst + g * n;
+      const T2* in = src + g * n;
+      T2* out = dst + g * n;
       const int k = idx % Ns;
-      double2 v[5];
+      T2 v[5];
       for (int q = 0; q < r; ++q) {
         v[q] = in[idx + q * m];
         if (q > 0 && k > 0) v[q] = Mul(v[q], Twiddle(tw, q * k * stride, n, sign));
@@ -199,24 +226,23 @@ __device__ int StockhamFft(double2* buf0, double2* buf1, int groups, const FftPl
         out[base] = Add(v[0], v[1]);
         out[base + Ns] = Sub(v[0], v[1]);
       } else if (r == 4) {
-        const double2 a0 = Add(v[0], v[2]), a1 = Sub(v[0], v[2]);
-        const double2 b0 = Add(v[1], v[3]), b1 = Sub(v[1], v[3]);
-        // i^sign * b1
-        const double2 ib1 = sign > 0 ? make_double2(-b1.y, b1.x) : make_double2(b1.y, -b1.x);
+        const T2 a0 = Add(v[0], v[2]), a1 = Sub(v[0], v[2]);
+        const T2 b0 = Add(v[1], v[3]), b1 = Sub(v[1], v[3]);
+        const T2 ib1 = sign > 0 ? Make<T2>(-b1.y, b1.x) : Make<T2>(b1.y, -b1.x);
         out[base] = Add(a0, b0);
         out[base + Ns] = Add(a1, ib1);
         out[base + 2 * Ns] = Sub(a0, b0);
         out[base + 3 * Ns] = Sub(a1, ib1);
       } else {
         for (int u = 0; u < r; ++u) {
-          double2 y = v[0];
+          T2 y = v[0];
           for (int q = 1; q < r; ++q) y = Add(y, Mul(v[q], Twiddle(tw, ((q * u) % r) * (n / r), n, sign)));
           out[base + u * Ns] = y;
         }
       }
     }
     __syncthreads();
-    double2* swap = src;
+    T2* swap = src;
     src = dst;
     dst = swap;
     Ns *= r;
@@ -231,21 +257,23 @@ constexpr int kRingGroup = 4;  // rings (fields at one colatitude) per CTA
 // memory.
 enum RingMode { kRingSynth = 0, kRingAnalyse = 1, kRingWeighted = 2 };
 
-__device__ void LoadSpectrum(double2* buf, int n, int groups, int lmax, int ntheta, int count, int j,
-                             int p0, bool real, const double2* spectra) {
-  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) buf[e] = make_double2(0.0, 0.0);
+
+template <class T2>
+__device__ void LoadSpectrum(T2* buf, int n, int groups, int lmax, int ntheta, int count, int j, int p0, bool real,
+                             const T2* spectra) {
+  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) buf[e] = Make<T2>(0, 0);
   __syncthreads();
   const int mcount = real ? lmax + 1 : 2 * lmax + 1;
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
-    const double2 v = spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
+    const T2 v = spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
     if (real) {
       if (m == 0) {
-        buf[g * n] = make_double2(v.x, 0.0);
+        buf[g * n] = Make<T2>(v.x, 0);
       } else {
         buf[g * n + m] = v;
-        buf[g * n + n - m] = make_double2(v.x, -v.y);
+        buf[g * n + n - m] = Make<T2>(v.x, -v.y);
       }
     } else {
       buf[g * n + ((m % n) + n) % n] = v;
@@ -254,29 +282,32 @@ __device__ void LoadSpectrum(double2* buf, int n, int groups, int lmax, int nthe
   __syncthreads();
 }
 
-__device__ void StoreSpectrum(const double2* res, int n, int groups, int lmax, int ntheta, int count,
-                              int j, int p0, bool real, double scale, double2* spectra) {
+template <class T2>
+__device__ void StoreSpectrum(const T2* res, int n, int groups, int lmax, int ntheta, int count, int j, int p0,
+                              bool real, typename Real<T2>::type scale, T2* spectra) {
   const int mcount = real ? lmax + 1 : 2 * lmax + 1;
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
-    const double2 v = res[g * n + ((m % n) + n) % n];
-    spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = make_double2(v.x * scale, v.y * scale);
+    const T2 v = res[g * n + ((m % n) + n) % n];
+    spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
   }
 }
 
-__global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan,
-                           const double2* tw, const double* weights, const double2* spectraIn,
-                           const void* fieldsIn, const double* pointWeight, void* fieldsOut,
-                           double2* spectraOut) {
-  extern __shared__ double2 smem[];
+template <class T2>
+__global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan, const T2* tw,
+                           const double* weights, const T2* spectraIn, const void* fieldsIn,
+                           const typename Real<T2>::type* pointWeight, void* fieldsOut, T2* spectraOut) {
+  using T = typename Real<T2>::type;
+  extern __shared__ __align__(16) unsigned char ringSmem[];
+  T2* smem = reinterpret_cast<T2*>(ringSmem);
   const int n = plan.n;
-  double2* buf0 = smem;
-  double2* buf1 = smem + kRingGroup * n;
+  T2* buf0 = smem;
+  T2* buf1 = smem + kRingGroup * n;
   const int j = blockIdx.y;
   const int p0 = blockIdx.x * kRingGroup;
   const int groups = min(kRingGroup, count - p0);
-  double2* res = buf0;
+  T2* res = buf0;
   if (mode == kRingSynth || mode == kRingWeighted) {
     LoadSpectrum(buf0, n, groups, lmax, ntheta, count, j, p0, real, spectraIn);
     res = StockhamFft(buf0, buf1, groups, plan, tw, +1) == 0 ? buf0 : buf1;
@@ -285,9 +316,9 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
         const int g = e / n, k = e % n;
         const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
         if (real)
-          static_cast<double*>(fieldsOut)[at] = res[e].x;
+          static_cast<T*>(fieldsOut)[at] = res[e].x;
         else
-          static_cast<double2*>(fieldsOut)[at] = res[e];
+          static_cast<T2*>(fieldsOut)[at] = res[e];
       }
       return;
     }
@@ -295,29 +326,33 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
     // imaginary part is dropped, as its synthesis does)
     for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
       const int g = e / n, k = e % n;
-      const double w = pointWeight[(static_cast<long long>(p0 + g) * ntheta + j) * n + k];
-      const double2 v = res[e];
-      res[e] = real ? make_double2(v.x * w, 0.0) : make_double2(v.x * w, v.y * w);
+      const T w = pointWeight[(static_cast<long long>(p0 + g) * ntheta + j) * n + k];
+      const T2 v = res[e];
+      res[e] = real ? Make<T2>(v.x * w, 0) : Make<T2>(v.x * w, v.y * w);
     }
     __syncthreads();
   } else {
     for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
       const int g = e / n, k = e % n;
       const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
-      double2 v = real ? make_double2(static_cast<const double*>(fieldsIn)[at], 0.0)
-                       : static_cast<const double2*>(fieldsIn)[at];
+      T2 v = real ? Make<T2>(static_cast<const T*>(fieldsIn)[at], 0) : static_cast<const T2*>(fieldsIn)[at];
       if (pointWeight != nullptr) {
-        const double w = pointWeight[at];
-        v = make_double2(v.x * w, v.y * w);
+        const T w = pointWeight[at];
+        v = Make<T2>(v.x * w, v.y * w);
       }
       buf0[e] = v;
     }
     __syncthreads();
   }
-  double2* other = res == buf0 ? buf1 : buf0;
-  const double2* out = StockhamFft(res, other, groups, plan, tw, -1) == 0 ? res : other;
-  const double scale = 2.0 * 3.14159265358979323846 / n * weights[j];
+  T2* other = res == buf0 ? buf1 : buf0;
+  const T2* out = StockhamFft(res, other, groups, plan, tw, -1) == 0 ? res : other;
+  const T scale = static_cast<T>(2.0 * 3.14159265358979323846 / n * weights[j]);
   StoreSpectrum(out, n, groups, lmax, ntheta, count, j, p0, real, scale, spectraOut);
+}
+
+__global__ void CastKernel(const double* in, long long n, float* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < n) out[i] = static_cast<float>(in[i]);
 }
 
 // -- layout permutations -------------------------------------------------------------------
@@ -457,11 +492,13 @@ Grid::~Grid() {
   cudaFree(dTheta);
   cudaFree(dWeights);
   cudaFree(dTwiddle);
+  cudaFree(dTwiddle32);
   for (auto& [key, b] : batches_) cudaFree(b.items);
   cudaFree(scratchSpectra_);
   cudaFree(scratchCoeffs_);
   for (auto& [N, t] : tables_) {
     cudaFree(t.values);
+    cudaFree(t.values32);
     cudaFree(t.dRowOffset);
   }
 }
@@ -557,7 +594,7 @@ int Grid::RunGemm(const Batch& b, const double* A, const double* B, double* C, b
   if (b.count == 0) return SL3DGPU_OK;
   dim3 grid((b.maxM + kBM - 1) / kBM, (b.maxN + kBN - 1) / kBN, static_cast<unsigned>(b.count));
   prof::Scope scope(b.analysis ? prof::kLegendreAnalysis : prof::kLegendreSynthesis, stream, b.flops);
-  GemmF64Kernel<<<grid, 256, 0, stream>>>(b.items, A, B, C, accumulate);
+  GemmKernel<double><<<grid, 256, 0, stream>>>(b.items, A, B, C, accumulate);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
@@ -594,7 +631,7 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
                cudaStream_t stream) {
   if (count == 0) return SL3DGPU_OK;
   const size_t smem = 2 * kRingGroup * static_cast<size_t>(g.nphi) * sizeof(double2);
-  SL3D_CUDA(cudaFuncSetAttribute(RingKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  SL3D_CUDA(cudaFuncSetAttribute(RingKernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
   dim3 grid((count + kRingGroup - 1) / kRingGroup, g.ntheta);
   // algorithmic traffic: the spectra and the grid values the mode reads and writes
@@ -604,7 +641,7 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   const double bytes = mode == kRingWeighted ? 2 * spec + wbytes : spec + field + wbytes;
   const double ffts = static_cast<double>(g.ntheta) * count * (mode == kRingWeighted ? 2 : 1);
   prof::Scope scope(prof::kRing, stream, ffts * 5.0 * g.nphi * std::log2(static_cast<double>(g.nphi)), bytes);
-  RingKernel<<<grid, 256, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
+  RingKernel<double2><<<grid, 256, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
                                           g.dWeights, reinterpret_cast<const double2*>(spectraIn),
                                           fieldsIn, weight, fieldsOut,
                                           reinterpret_cast<double2*>(spectraOut));
@@ -627,6 +664,82 @@ int Grid::RingWeighted(bool real, const double* spectraIn, int count, const doub
                        double* spectraOut, cudaStream_t stream) {
   return LaunchRing(*this, kRingWeighted, real, count, spectraIn, nullptr, weight, nullptr, spectraOut,
                     stream);
+}
+
+int Grid::Table32(int N, const SpinTable** out) {
+  const SpinTable* t = nullptr;
+  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+  auto& mt = tables_.at(N);
+  if (mt.values32 == nullptr) {
+    const long long n = static_cast<long long>(mt.rowOffset.back()) * ntheta;
+    SL3D_CUDA(cudaMalloc(&mt.values32, std::max<long long>(n, 1) * sizeof(float)));
+    prof::Scope scope(prof::kOther, nullptr);
+    CastKernel<<<static_cast<unsigned>((n + 255) / 256), 256>>>(mt.values, n, mt.values32);
+    SL3D_CHECK_LAUNCH();
+    if (dTwiddle32 == nullptr) {
+      SL3D_CUDA(cudaMalloc(&dTwiddle32, nphi * sizeof(float2)));
+      CastKernel<<<(2 * nphi + 255) / 256, 256>>>(reinterpret_cast<const double*>(dTwiddle), 2LL * nphi,
+                                                  reinterpret_cast<float*>(dTwiddle32));
+      SL3D_CHECK_LAUNCH();
+    }
+    SL3D_CUDA(cudaDeviceSynchronize());
+  }
+  *out = &mt;
+  return SL3DGPU_OK;
+}
+
+int Grid::RunGemmF(const Batch& b, const float* A, const float* B, float* C, bool accumulate, cudaStream_t stream) {
+  if (b.count == 0) return SL3DGPU_OK;
+  dim3 grid((b.maxM + kBM - 1) / kBM, (b.maxN + kBN - 1) / kBN, static_cast<unsigned>(b.count));
+  prof::Scope scope(prof::kLegendre32, stream, b.flops);
+  GemmKernel<float><<<grid, 256, 0, stream>>>(b.items, A, B, C, accumulate);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Grid::LegendreSynthesisF(int N, bool real, const float* coeffs, int P, int p0, int count, float* spectra,
+                             cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const SpinTable* t = nullptr;
+  if (int st = Table32(N, &t); st != SL3DGPU_OK) return st;
+  const Batch* b = nullptr;
+  if (int st = BatchFor(N, real, false, P, p0, count, &b); st != SL3DGPU_OK) return st;
+  const int mlo = real ? 0 : -lmax;
+  for (int m = mlo; m <= lmax; ++m)
+    if (t->Rows(m, lmax) == 0)
+      SL3D_CUDA(cudaMemsetAsync(spectra + static_cast<long long>(m - mlo) * ntheta * 2LL * count, 0,
+                                sizeof(float) * ntheta * 2 * count, stream));
+  return RunGemmF(*b, t->values32, coeffs, spectra, false, stream);
+}
+
+int Grid::LegendreAnalysisF(int N, bool real, const float* spectra, int P, int p0, int count, float* coeffs,
+                            bool accumulate, cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const SpinTable* t = nullptr;
+  if (int st = Table32(N, &t); st != SL3DGPU_OK) return st;
+  const Batch* b = nullptr;
+  if (int st = BatchFor(N, real, true, P, p0, count, &b); st != SL3DGPU_OK) return st;
+  return RunGemmF(*b, t->values32, spectra, coeffs, accumulate, stream);
+}
+
+int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const float* weight, float* spectraOut,
+                        cudaStream_t stream) {
+  if (count == 0) return SL3DGPU_OK;
+  const SpinTable* t = nullptr;
+  if (int st = Table32(0, &t); st != SL3DGPU_OK) return st;  // makes the FP32 twiddles
+  const size_t smem = 2 * kRingGroup * static_cast<size_t>(nphi) * sizeof(float2);
+  SL3D_CUDA(cudaFuncSetAttribute(RingKernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem)));
+  dim3 grid((count + kRingGroup - 1) / kRingGroup, ntheta);
+  const double spec = static_cast<double>(real ? lmax + 1 : 2 * lmax + 1) * ntheta * count * 8.0;
+  const double wbytes = static_cast<double>(ntheta) * nphi * count * 4.0;
+  prof::Scope scope(prof::kRing32, stream, 2.0 * ntheta * count * 5.0 * nphi * std::log2(static_cast<double>(nphi)),
+                    2 * spec + wbytes);
+  RingKernel<float2><<<grid, 256, smem, stream>>>(kRingWeighted, lmax, ntheta, count, real, plan, dTwiddle32,
+                                                  dWeights, reinterpret_cast<const float2*>(spectraIn), nullptr,
+                                                  weight, nullptr, reinterpret_cast<float2*>(spectraOut));
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
 }
 
 int Grid::ToDevice(int N, bool real, const double* ref, int count, double* dev,

@@ -38,6 +38,7 @@ struct SpinTable {
   int N = 0;
   std::vector<int> rowOffset;  // 2 lmax + 2 entries, cumulative rows by m index
   double* values = nullptr;    // device
+  float* values32 = nullptr;   // device FP32 copy, made on first use
   int* dRowOffset = nullptr;   // device copy of rowOffset
   int Rows(int m, int lmax) const { return rowOffset[m + lmax + 1] - rowOffset[m + lmax]; }
 };
@@ -58,6 +59,7 @@ class Grid {
   double* dTheta = nullptr;
   double* dWeights = nullptr;
   double2* dTwiddle = nullptr;
+  float2* dTwiddle32 = nullptr;
   FftPlan plan;
 
   // The table of spin N, built on first use (device kernel).
@@ -94,6 +96,15 @@ class Grid {
   int RingWeighted(bool real, const double* spectraIn, int count, const double* weight,
                    double* spectraOut, cudaStream_t stream);
 
+  // The same contraction and ring passes in FP32 (the mixed form's
+  // correction passes): FP32 copies of the table and twiddles, made once.
+  int LegendreSynthesisF(int N, bool real, const float* coeffs, int P, int p0, int count, float* spectra,
+                         cudaStream_t stream);
+  int LegendreAnalysisF(int N, bool real, const float* spectra, int P, int p0, int count, float* coeffs,
+                        bool accumulate, cudaStream_t stream);
+  int RingWeightedF(bool real, const float* spectraIn, int count, const float* weight, float* spectraOut,
+                    cudaStream_t stream);
+
   // Reference layout <-> device layout permutations.
   int ToDevice(int N, bool real, const double* ref, int count, double* dev, cudaStream_t stream);
   int FromDevice(int N, bool real, const double* dev, int count, double* ref, cudaStream_t stream);
@@ -117,6 +128,8 @@ class Grid {
   size_t scratchCoeffsSize_ = 0;
   int RunGemm(const Batch& b, const double* A, const double* B, double* C, bool accumulate,
               cudaStream_t stream);
+  int RunGemmF(const Batch& b, const float* A, const float* B, float* C, bool accumulate, cudaStream_t stream);
+  int Table32(int N, const SpinTable** out);
 };
 
 // Smallest 2^a 3^b 5^c at or above n.

@@ -12,6 +12,16 @@
 // strain recovery into the next iterate. The convergence measure and the
 // Anderson mixer (Gram least squares in FP64 on the device) close the loop;
 // the host reads three numbers per pass.
+//
+// The mixed form (precision 1) keeps that loop's FP64 passes and its stopping
+// rule, and between two of them solves for the correction in FP32: with
+// G(s) = B s + c the pass and r = G(s) - s its residual, the fixed point is
+// s + e with e = B e + r, and e is iterated (with the same Anderson
+// acceleration) through FP32 passes -- the FP32 table, ring FFTs, band solves
+// with the FP64 factors rounded to FP32, force and strain maps -- to a loose
+// relative change; s += e in FP64 and the next FP64 pass measures the true
+// residual. B has neither the fixed memory force nor the load, so the
+// correction passes need neither.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -33,6 +43,9 @@ int BandFactorBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sy
 int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
                    const int2* devItems, int itemCount, const double* bands, const int* pivots, double* rhs,
                    const double* scales, int lu, cudaStream_t stream);
+int BandSolveBatchF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                    const int2* devItems, int itemCount, const float* bands, const int* pivots, float* rhs,
+                    const float* scales, int lu, cudaStream_t stream);
 std::vector<int2> BandWorkItems(const sl3dgpu_band_system* hostSystems, int count);
 
 namespace {
@@ -90,6 +103,7 @@ struct Flavour {
   int scheme = 0;
   double dt = 0.0;
   Dev<double> bands, scales, units;
+  Dev<float> bands32, scales32;  // the mixed form's FP32 copies
   Dev<int> pivots;
   Dev<long long> unitOffset;
   std::vector<sl3dgpu_band_system> sphChol, sphLu, torChol;
@@ -159,6 +173,16 @@ class Viscoelastic3DGpu {
   Dev<double*> dGPtr, dFPtr;
   static constexpr int kMixBlocks = 1024;
 
+  // the mixed form's FP32 correction: iterate, next iterate, residual,
+  // analysed force, right-hand sides, spectra, weight and its own mixer
+  Dev<float2> e32, eNext32, r32, analysed32, rhsSph32, rhsTor32;
+  Dev<float> spectra32A, spectra32B, weight32;
+  int mixer32Memory = 0;
+  Dev<float> xPrev32, fPrev32;
+  std::vector<Dev<float>> dG32, dF32;
+  Dev<float*> dG32Ptr, dF32Ptr;
+  std::vector<double> correctionHistory;  // the last step's FP32 pass changes
+
   V3dState scratch;  // the second buffer set a step writes into
   std::vector<double> history;  // the last step's pass residuals, stages in turn
 
@@ -188,6 +212,13 @@ class Viscoelastic3DGpu {
   int RelativeChange(const double2* next, const double2* now, double* residual);
   int MixerReset();
   int MixerUpdate(int& count, int& slot, bool& first);
+  int WeightedPass32(const float2* strain, float2* out);  // assigns, lateral nodes
+  int Pass32(const Flavour& f, const float2* e, float2* next);
+  int Mixer32Reset();
+  int Mixer32Update(int& count, int& slot, bool& first);
+  int Correct(const Flavour& f, sl3dgpu_step_info& info);
+  int Converge(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
+  int ConvergeMixed(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
   int ElasticStrain(const V3dState& st, const double2* sigma);
   int StepOnce(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
                const double2* sigmaEnd, sl3dgpu_step_info& info);
@@ -205,8 +236,12 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     SetError("v3d: lmax >= 2, ngll >= 2, oversampling >= 1, anderson_memory in [0, 8]");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  if (opt.precision != 0) {
-    SetError("v3d: only the FP64 form (precision 0) is built in this library version");
+  if (opt.precision != 0 && opt.precision != 1) {
+    SetError("v3d: precision 0 (FP64) or 1 (mixed)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (opt.precision == 1 && !(opt.correction_rtol > 0.0 && opt.correction_rtol < 1.0)) {
+    SetError("v3d: the mixed form needs 0 < correction_rtol < 1");
     return SL3DGPU_ERR_ARGUMENT;
   }
   try {
@@ -361,6 +396,17 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   for (auto* b : {&sigma0, &sigmaMid, &sigma1, &surfaceOut}) SL3D_CUDA(b->Alloc(lm));
   SL3D_CUDA(changePartial.Alloc(3 * kChangeBlocks));
   SL3D_CUDA(changeResult.Alloc(3));
+  SL3D_CUDA(gammaOut.Alloc(16));
+  SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks) * 16));
+  if (options.precision == 1) {
+    for (auto* b : {&e32, &eNext32, &r32, &analysed32}) SL3D_CUDA(b->Alloc(spectralComplex));
+    SL3D_CUDA(rhsSph32.Alloc(rhsSphComplex));
+    SL3D_CUDA(rhsTor32.Alloc(std::max<long long>(rhsTorComplex, 1)));
+    SL3D_CUDA(spectra32A.Alloc(2 * spectra));
+    SL3D_CUDA(spectra32B.Alloc(2 * spectra));
+    SL3D_CUDA(weight32.Alloc(values));
+    SL3D_CUDA(cudaMemsetAsync(analysed32.p, 0, spectralComplex * sizeof(float2), stream));
+  }
   SL3D_TRY(AllocState(scratch));
   SL3D_TRY(BuildFlavour(reference->elastic, *elastic));
   SL3D_CUDA(cudaStreamSynchronize(stream));
@@ -410,6 +456,11 @@ int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
   lateralFirst = last >= 0 ? first : 0;
   lateralEnd = last >= 0 ? last + 1 : 0;
   SL3D_CUDA(cudaMemcpy(factor.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
+  if (options.precision == 1) {
+    // The correction's analysed force is written at the lateral columns only.
+    SL3D_CUDA(cudaMemsetAsync(analysed32.p, 0, spectralComplex * sizeof(float2), stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+  }
   return SL3DGPU_OK;
 }
 
@@ -621,6 +672,16 @@ int Viscoelastic3DGpu::BuildFlavour(const host::PointShear& shear, Flavour& f) {
                             f.units.p, f.scales.p, lu, stream));
     SL3D_CUDA(cudaStreamSynchronize(stream));
   }
+  if (options.precision == 1 && &f != elastic.get()) {
+    // The FP64 factors and scales rounded to FP32 for the correction passes.
+    SL3D_CUDA(f.bands32.Alloc(f.bands.n));
+    SL3D_CUDA(f.scales32.Alloc(f.scales.n));
+    LaunchCast(static_cast<long long>(f.bands.n), f.bands.p, f.bands32.p, stream);
+    SL3D_CHECK_LAUNCH();
+    LaunchCast(static_cast<long long>(f.scales.n), f.scales.p, f.scales32.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+  }
   return SL3DGPU_OK;
 }
 
@@ -770,11 +831,9 @@ int Viscoelastic3DGpu::MixerReset() {
     SL3D_CUDA(dFPtr.Upload(fp));
     SL3D_CUDA(xPrev.Alloc(n));
     SL3D_CUDA(fPrev.Alloc(n));
-    SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
-    SL3D_CUDA(gammaOut.Alloc(16));
-    SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks) * 16));
     mixerMemory = memory;
   }
+  if (gram.n < static_cast<size_t>(memory) * memory) SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
   SL3D_CUDA(cudaMemsetAsync(gram.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
   return SL3DGPU_OK;
 }
@@ -873,8 +932,30 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
                             stream));
   SL3D_TRY(AnalyseWeighted(*d0, weight.p, analysedStart.p));
 
-  // Converge (Viscoelastic3D.cpp:1916-1974).
   info = sl3dgpu_step_info{};
+  if (options.precision == 1) {
+    LaunchCast(values, weight.p, weight32.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(ConvergeMixed(*f, sigmaEnd, info));
+  } else {
+    SL3D_TRY(Converge(*f, sigmaEnd, info));
+  }
+  // Finish: synthesise the strain, advance the memory.
+  SL3D_TRY(Synthesise(s.p, out.strain));
+  for (int k = 0; k < K; ++k) {
+    LaunchAdvance(values, beta[k].p, out.strain.c0.p, out.strain.c1.p, out.strain.r.p, out.m[k].c0.p,
+                  out.m[k].c1.p, out.m[k].r.p, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  SL3D_CUDA(cudaMemcpyAsync(out.coeffs.p, s.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  out.hasStrain = out.hasCoeffs = true;
+  return SL3DGPU_OK;
+}
+
+// Converge (Viscoelastic3D.cpp:1916-1974): FP64 passes from the start
+// strain, plain until the residual ratio exceeds the Anderson rate, mixed
+// from then on.
+int Viscoelastic3DGpu::Converge(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info) {
   const bool adaptive = options.anderson_rate > 0.0;
   bool mixing = options.anderson_memory > 0 && !adaptive;
   bool firstMix = true;
@@ -882,7 +963,7 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   if (mixing) SL3D_TRY(MixerReset());
   double previous = 0.0;
   for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
-    SL3D_TRY(Pass(*f, s.p, iteration == 0, sigmaEnd, sNext.p));
+    SL3D_TRY(Pass(f, s.p, iteration == 0, sigmaEnd, sNext.p));
     double residual = 0.0;
     SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
     history.push_back(residual);
@@ -913,15 +994,181 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
       std::swap(s, sNext);
     }
   }
-  // Finish: synthesise the strain, advance the memory.
-  SL3D_TRY(Synthesise(s.p, out.strain));
-  for (int k = 0; k < K; ++k) {
-    LaunchAdvance(values, beta[k].p, out.strain.c0.p, out.strain.c1.p, out.strain.r.p, out.m[k].c0.p,
-                  out.m[k].c1.p, out.m[k].r.p, stream);
+  return SL3DGPU_OK;
+}
+
+// The mixed form's loop: the same FP64 passes and stopping rule, each FP64
+// pass that does not meet the tolerance followed by an FP32 correction.
+int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info) {
+  if (options.damping != 1.0) {
+    SetError("v3d: damping other than 1 is not built");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
+    SL3D_TRY(Pass(f, s.p, iteration == 0, sigmaEnd, sNext.p));
+    double residual = 0.0;
+    SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
+    history.push_back(residual);
+    info.iterations = iteration + 1;
+    info.residual = residual;
+    if (!std::isfinite(residual)) break;
+    if (residual <= options.rtol) {
+      info.converged = 1;
+      std::swap(s, sNext);
+      break;
+    }
+    // r = G(s) - s in FP32, e = B e + r, s += e.
+    LaunchResidual32(2 * spectralComplex, reinterpret_cast<const double*>(sNext.p),
+                     reinterpret_cast<const double*>(s.p), reinterpret_cast<float*>(r32.p), stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(Correct(f, info));
+    LaunchAddCorrection(2 * spectralComplex, reinterpret_cast<const float*>(e32.p), reinterpret_cast<double*>(s.p),
+                        stream);
     SL3D_CHECK_LAUNCH();
   }
-  SL3D_CUDA(cudaMemcpyAsync(out.coeffs.p, s.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
-  out.hasStrain = out.hasCoeffs = true;
+  return SL3DGPU_OK;
+}
+
+// -- the mixed form's FP32 correction ---------------------------------------------------------------
+
+// Analyse(W Synthesise(e)) over the lateral nodes into out's lateral columns
+// (the other columns stay zero).
+int Viscoelastic3DGpu::WeightedPass32(const float2* strain, float2* out) {
+  const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+  if (count <= 0) return SL3DGPU_OK;
+  const auto* in = reinterpret_cast<const float*>(strain);
+  auto* o = reinterpret_cast<float*>(out);
+  const float* w = weight32.p + p0 * fieldSize;
+  const long long offs[3] = {0, 2 * rows0 * P, 2 * (rows0 + rows1) * P};
+  const int spins[3] = {-2, -1, 0};
+  for (int c = 0; c < 3; ++c) {
+    const bool real = c == 2;
+    SL3D_TRY(grid->LegendreSynthesisF(spins[c], real, in + offs[c], P, p0, count, spectra32A.p, stream));
+    SL3D_TRY(grid->RingWeightedF(real, spectra32A.p, count, w, spectra32B.p, stream));
+    SL3D_TRY(grid->LegendreAnalysisF(spins[c], real, spectra32B.p, P, p0, count, o + offs[c], false, stream));
+  }
+  return SL3DGPU_OK;
+}
+
+// next = B e + r: the lateral force of e alone through the FP32 solves.
+int Viscoelastic3DGpu::Pass32(const Flavour& f, const float2* e, float2* next) {
+  SL3D_TRY(WeightedPass32(e, analysed32.p));
+  SL3D_CUDA(cudaMemsetAsync(rhsSph32.p, 0, rhsSphComplex * sizeof(float2), stream));
+  SL3D_CUDA(cudaMemsetAsync(rhsTor32.p, 0, std::max<long long>(rhsTorComplex, 1) * sizeof(float2), stream));
+  LaunchForces(geo, analysed32.p, rhsSph32.p, rhsTor32.p, stream);
+  SL3D_CHECK_LAUNCH();
+  auto* sph = reinterpret_cast<float*>(rhsSph32.p);
+  auto* tor = reinterpret_cast<float*>(rhsTor32.p);
+  SL3D_TRY(BandSolveBatchF(f.dSphChol.p, f.sphChol.data(), static_cast<int>(f.sphChol.size()), f.iSphChol.p,
+                           f.nSphChol, f.bands32.p, f.pivots.p, sph, f.scales32.p, 0, stream));
+  SL3D_TRY(BandSolveBatchF(f.dSphLu.p, f.sphLu.data(), static_cast<int>(f.sphLu.size()), f.iSphLu.p, f.nSphLu,
+                           f.bands32.p, f.pivots.p, sph, f.scales32.p, 1, stream));
+  SL3D_TRY(BandSolveBatchF(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
+                           f.nTorChol, f.bands32.p, f.pivots.p, tor, f.scales32.p, 0, stream));
+  LaunchStrain(geo, rhsSph32.p, rhsTor32.p, next, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchAddInPlace(2 * spectralComplex, reinterpret_cast<const float*>(r32.p), reinterpret_cast<float*>(next),
+                   stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::Mixer32Reset() {
+  const int memory = options.anderson_memory;
+  if (memory <= 0) return SL3DGPU_OK;
+  if (mixer32Memory != memory) {
+    const size_t n = 2 * spectralComplex;
+    dG32.resize(memory);
+    dF32.resize(memory);
+    std::vector<float*> gp(memory), fp(memory);
+    for (int i = 0; i < memory; ++i) {
+      SL3D_CUDA(dG32[i].Alloc(n));
+      SL3D_CUDA(dF32[i].Alloc(n));
+      gp[i] = dG32[i].p;
+      fp[i] = dF32[i].p;
+    }
+    SL3D_CUDA(dG32Ptr.Upload(gp));
+    SL3D_CUDA(dF32Ptr.Upload(fp));
+    SL3D_CUDA(xPrev32.Alloc(n));
+    SL3D_CUDA(fPrev32.Alloc(n));
+    mixer32Memory = memory;
+  }
+  if (gram.n < static_cast<size_t>(memory) * memory) SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
+  SL3D_CUDA(cudaMemsetAsync(gram.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
+  MixerArgsT<float> a{};
+  a.n = 2 * spectralComplex;
+  a.memory = options.anderson_memory;
+  a.x = reinterpret_cast<float*>(e32.p);
+  a.gx = reinterpret_cast<const float*>(eNext32.p);
+  a.xPrev = xPrev32.p;
+  a.fPrev = fPrev32.p;
+  a.dG = dG32Ptr.p;
+  a.dF = dF32Ptr.p;
+  a.partial = mixPartial.p;
+  a.blocks = static_cast<int>(std::min<long long>(kMixBlocks, a.n));
+  a.gram = gram.p;
+  a.gamma = gammaOut.p;
+  if (first) {
+    LaunchMixerFirst(a, stream);
+    SL3D_CHECK_LAUNCH();
+    first = false;
+    return SL3DGPU_OK;
+  }
+  a.slot = slot;
+  a.m = std::min(count + 1, a.memory);
+  LaunchMixerUpdate(a, stream);
+  SL3D_CHECK_LAUNCH();
+  count = a.m;
+  slot = (slot + 1) % a.memory;
+  return SL3DGPU_OK;
+}
+
+// e = B e + r from e = r, with the FP64 loop's Anderson schedule, until the
+// relative change is at most correction_rtol (or max_iterations passes).
+int Viscoelastic3DGpu::Correct(const Flavour& f, sl3dgpu_step_info& info) {
+  SL3D_CUDA(cudaMemcpyAsync(e32.p, r32.p, spectralComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+  const bool adaptive = options.anderson_rate > 0.0;
+  bool mixing = options.anderson_memory > 0 && !adaptive;
+  bool firstMix = true;
+  int count = 0, slot = 0;
+  if (mixing) SL3D_TRY(Mixer32Reset());
+  double previous = 0.0;
+  for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
+    SL3D_TRY(Pass32(f, e32.p, eNext32.p));
+    ++info.correction_passes;
+    LaunchRelativeChange(reinterpret_cast<const float*>(eNext32.p), reinterpret_cast<const float*>(e32.p),
+                         2 * spectralComplex, changePartial.p, kChangeBlocks, changeResult.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(hostResult, changeResult.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    if (hostResult[2] == 0.0) {
+      SetError("v3d: the FP32 correction left the finite range");
+      return SL3DGPU_ERR_RUNTIME;
+    }
+    const double change = hostResult[0] > 0.0 ? std::sqrt(hostResult[1]) / std::sqrt(hostResult[0]) : 0.0;
+    correctionHistory.push_back(change);
+    if (change <= options.correction_rtol) {
+      std::swap(e32, eNext32);
+      break;
+    }
+    if (adaptive && !mixing && options.anderson_memory > 0 && iteration > 0 &&
+        change > options.anderson_rate * previous) {
+      mixing = true;
+      firstMix = true;
+      count = slot = 0;
+      SL3D_TRY(Mixer32Reset());
+    }
+    previous = change;
+    if (mixing) {
+      SL3D_TRY(Mixer32Update(count, slot, firstMix));
+    } else {
+      std::swap(e32, eNext32);
+    }
+  }
   return SL3DGPU_OK;
 }
 
@@ -947,6 +1194,7 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   }
   sl3dgpu_step_info info{};
   history.clear();
+  correctionHistory.clear();
   if (scheme != 2 || dt == 0.0) {
     const int one = scheme == 2 ? 1 : scheme;
     SL3D_TRY(StepOnce(st, scratch, dt, one, s0, s1, info));
@@ -972,6 +1220,7 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     SL3D_TRY(StepOnce(scratch, scratch, h, 1, mid, s1, i2));
     info.iterations = i1.iterations + i2.iterations;
     info.mixed_passes = i1.mixed_passes + i2.mixed_passes;
+    info.correction_passes = i1.correction_passes + i2.correction_passes;
     info.residual = i2.residual;
     info.converged = i1.converged && i2.converged;
   }
@@ -1149,6 +1398,17 @@ extern "C" int sl3dgpu_v3d_residual_history(const sl3dgpu_v3d* h, double* out, i
     return SL3DGPU_ERR_ARGUMENT;
   }
   const auto& v = h->op.history;
+  if (out != nullptr)
+    for (int i = 0; i < capacity && i < static_cast<int>(v.size()); ++i) out[i] = v[i];
+  return static_cast<int>(v.size());
+}
+
+extern "C" int sl3dgpu_v3d_correction_history(const sl3dgpu_v3d* h, double* out, int capacity) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& v = h->op.correctionHistory;
   if (out != nullptr)
     for (int i = 0; i < capacity && i < static_cast<int>(v.size()); ++i) out[i] = v[i];
   return static_cast<int>(v.size());

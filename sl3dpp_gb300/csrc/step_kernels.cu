@@ -15,12 +15,45 @@
 namespace sl3dgpu {
 namespace {
 
+template <class T2>
+struct Scalar;
+template <>
+struct Scalar<double2> {
+  using type = double;
+};
+template <>
+struct Scalar<float2> {
+  using type = float;
+};
+
+template <class T2>
+__device__ inline T2 Cx(typename Scalar<T2>::type x, typename Scalar<T2>::type y) {
+  T2 v;
+  v.x = x;
+  v.y = y;
+  return v;
+}
 __device__ inline double2 C(double x, double y) { return make_double2(x, y); }
-__device__ inline double2 CAdd(double2 a, double2 b) { return C(a.x + b.x, a.y + b.y); }
-__device__ inline double2 CSub(double2 a, double2 b) { return C(a.x - b.x, a.y - b.y); }
-__device__ inline double2 CScale(double s, double2 a) { return C(s * a.x, s * a.y); }
-__device__ inline double2 CConj(double2 a) { return C(a.x, -a.y); }
-__device__ inline double2 CI(double2 a) { return C(-a.y, a.x); }  // i a
+template <class T2>
+__device__ inline T2 CAdd(T2 a, T2 b) {
+  return Cx<T2>(a.x + b.x, a.y + b.y);
+}
+template <class T2>
+__device__ inline T2 CSub(T2 a, T2 b) {
+  return Cx<T2>(a.x - b.x, a.y - b.y);
+}
+template <class T2>
+__device__ inline T2 CScale(typename Scalar<T2>::type s, T2 a) {
+  return Cx<T2>(s * a.x, s * a.y);
+}
+template <class T2>
+__device__ inline T2 CConj(T2 a) {
+  return Cx<T2>(a.x, -a.y);
+}
+template <class T2>
+__device__ inline T2 CI(T2 a) {  // i a
+  return Cx<T2>(-a.y, a.x);
+}
 
 __device__ inline void DecodeLm(int lm, int& l, int& m) {
   l = static_cast<int>((sqrt(8.0 * lm + 1.0) - 1.0) * 0.5);
@@ -39,39 +72,45 @@ __device__ inline long long RowR(const Geometry& g, int l, int m) {
   return g.rowOffR[m + g.lmax] - g.rowOffR[g.lmax] + (l - m);
 }
 
+template <class T2>
 struct Rows {
-  double2 u, v, w, du, dv, dw;
+  T2 u, v, w, du, dv, dw;
 };
 
 // ForceRowsFromComponents (SpinComponents.hpp:129-145).
-__device__ Rows ForceRows(int l, const double2 A[5], double r) {
-  const double zeta2 = l * (l + 1.0), zeta = sqrt(zeta2);
-  const double root = sqrt(fmax(zeta2 - 2.0, 0.0));
-  const double s2 = 1.41421356237309504880;
-  const double2 s13 = CAdd(A[1], A[3]), d13 = CSub(A[1], A[3]);
-  const double2 s04 = CAdd(A[0], A[4]), d04 = CSub(A[0], A[4]);
-  Rows rows;
-  rows.u = CSub(CScale(s2 * zeta, s13), CScale(4.0, A[2]));
-  rows.v = CSub(CAdd(CScale(zeta * root, s04), CScale(2.0 * zeta2, A[2])), CScale(s2 * zeta, s13));
+template <class T2>
+__device__ Rows<T2> ForceRows(int l, const T2 A[5], typename Scalar<T2>::type r) {
+  using T = typename Scalar<T2>::type;
+  const T zeta2 = l * (l + T(1)), zeta = sqrt(zeta2);
+  const T root = sqrt(fmax(zeta2 - T(2), T(0)));
+  const T s2 = T(1.41421356237309504880);
+  const T2 s13 = CAdd(A[1], A[3]), d13 = CSub(A[1], A[3]);
+  const T2 s04 = CAdd(A[0], A[4]), d04 = CSub(A[0], A[4]);
+  Rows<T2> rows;
+  rows.u = CSub(CScale(s2 * zeta, s13), CScale(T(4), A[2]));
+  rows.v = CSub(CAdd(CScale(zeta * root, s04), CScale(T(2) * zeta2, A[2])), CScale(s2 * zeta, s13));
   rows.w = CI(CSub(CScale(zeta * root, d04), CScale(s2 * zeta, d13)));
-  rows.du = CScale(4.0 * r, A[2]);
+  rows.du = CScale(T(4) * r, A[2]);
   rows.dv = CScale(s2 * zeta * r, s13);
   rows.dw = CI(CScale(s2 * zeta * r, d13));
   return rows;
 }
 
-__global__ void ForceKernel(Geometry g, const double2* spectral, double2* rhsSph, double2* rhsTor) {
+template <class T2>
+__global__ void ForceKernel(Geometry g, const T2* spectral, T2* rhsSph, T2* rhsTor) {
+  using T = typename Scalar<T2>::type;
   int l, m;
   DecodeLm(blockIdx.x, l, m);
   const DegreeInfo d = g.degrees[l];
   if (d.firstNode >= g.P) return;
-  extern __shared__ double2 rowsS[];  // (P - first) x 6
-  const double2* c0 = spectral;
-  const double2* c1 = spectral + g.rows0 * g.P;
-  const double2* cr = spectral + (g.rows0 + g.rows1) * g.P;
-  const double sign = (m % 2 == 0) ? 1.0 : -1.0;
+  extern __shared__ __align__(16) unsigned char forceSmem[];
+  T2* rowsS = reinterpret_cast<T2*>(forceSmem);  // (P - first) x 6
+  const T2* c0 = spectral;
+  const T2* c1 = spectral + g.rows0 * g.P;
+  const T2* cr = spectral + (g.rows0 + g.rows1) * g.P;
+  const T sign = (m % 2 == 0) ? T(1) : T(-1);
   for (int p = d.firstNode + threadIdx.x; p < g.P; p += blockDim.x) {
-    double2 A[5] = {C(0, 0), C(0, 0), C(0, 0), C(0, 0), C(0, 0)};
+    T2 A[5] = {Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0)};
     A[2] = cr[RowR(g, l, m) * g.P + p];
     if (l >= 1) {
       A[1] = c1[Row1(g, l, m) * g.P + p];
@@ -81,8 +120,8 @@ __global__ void ForceKernel(Geometry g, const double2* spectral, double2* rhsSph
       A[0] = c0[Row0(g, l, m) * g.P + p];
       A[4] = CScale(sign, CConj(c0[Row0(g, l, -m) * g.P + p]));
     }
-    const Rows rows = ForceRows(l, A, g.nodeR[p]);
-    double2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
+    const Rows<T2> rows = ForceRows<T2>(l, A, static_cast<T>(g.nodeR[p]));
+    T2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
     s[0] = rows.u;
     s[1] = rows.v;
     s[2] = rows.w;
@@ -93,7 +132,7 @@ __global__ void ForceKernel(Geometry g, const double2* spectral, double2* rhsSph
   __syncthreads();
   const int n = g.ngll, cols = l + 1;
   for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
-    double2 bU = C(0, 0), bV = C(0, 0), bW = C(0, 0);
+    T2 bU = Cx<T2>(0, 0), bV = Cx<T2>(0, 0), bW = Cx<T2>(0, 0);
     const int eHi = min(gn / (n - 1), g.elements - 1);
     const int iHi = gn - eHi * (n - 1);
     const int eLo = (iHi == 0 && eHi > 0) ? eHi - 1 : eHi;
@@ -105,10 +144,10 @@ __global__ void ForceKernel(Geometry g, const double2* spectral, double2* rhsSph
       for (int q = 0; q < g.np; ++q) {
         const int p = fn + q;
         const double r = g.nodeR[p];
-        const double2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
+        const T2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
         const double point = jac * g.pWeight[q] * r;
-        const double v = point * g.pValue[q * n + i];
-        const double deriv = g.pWeight[q] * g.pDeriv[q * n + i] * r;
+        const T v = static_cast<T>(point * g.pValue[q * n + i]);
+        const T deriv = static_cast<T>(g.pWeight[q] * g.pDeriv[q * n + i] * r);
         bU = CAdd(bU, CScale(v, s[0]));
         bV = CAdd(bV, CScale(v, s[1]));
         bU = CAdd(bU, CScale(deriv, s[3]));
@@ -129,23 +168,26 @@ __global__ void ForceKernel(Geometry g, const double2* spectral, double2* rhsSph
 
 // DeviatoricComponents (SpinComponents.hpp:53-72) into the stored blocks
 // (GridCoupling::Scatter, the -m twins from the derived components).
-__global__ void StrainKernel(Geometry g, const double2* solSph, const double2* solTor, double2* spectral) {
+template <class T2>
+__global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2* spectral) {
+  using T = typename Scalar<T2>::type;
   int l, m;
   DecodeLm(blockIdx.x, l, m);
   const DegreeInfo d = g.degrees[l];
-  extern __shared__ double2 vals[];  // (lastGlobal - firstGlobal + 1) x 3
-  double2* c0 = spectral;
-  double2* c1 = spectral + g.rows0 * g.P;
-  double2* cr = spectral + (g.rows0 + g.rows1) * g.P;
+  extern __shared__ __align__(16) unsigned char strainSmem[];
+  T2* vals = reinterpret_cast<T2*>(strainSmem);  // (lastGlobal - firstGlobal + 1) x 3
+  T2* c0 = spectral;
+  T2* c1 = spectral + g.rows0 * g.P;
+  T2* cr = spectral + (g.rows0 + g.rows1) * g.P;
   const int cols = l + 1;
   const bool any = d.firstNode < g.P;
   if (any) {
     for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
       const int dU = g.sphMap[d.sphMap + 2LL * gn], dV = g.sphMap[d.sphMap + 2LL * gn + 1];
-      double2* v = vals + static_cast<long long>(gn - d.firstGlobal) * 3;
-      v[0] = dU >= 0 ? solSph[d.sphRhs + static_cast<long long>(dU) * cols + m] : C(0, 0);
-      v[1] = dV >= 0 ? solSph[d.sphRhs + static_cast<long long>(dV) * cols + m] : C(0, 0);
-      double2 W = C(0, 0);
+      T2* v = vals + static_cast<long long>(gn - d.firstGlobal) * 3;
+      v[0] = dU >= 0 ? solSph[d.sphRhs + static_cast<long long>(dU) * cols + m] : Cx<T2>(0, 0);
+      v[1] = dV >= 0 ? solSph[d.sphRhs + static_cast<long long>(dV) * cols + m] : Cx<T2>(0, 0);
+      T2 W = Cx<T2>(0, 0);
       if (l >= 1) {
         const int dW = g.torMap[d.torMap + gn];
         if (dW >= 0) W = solTor[d.torRhs + static_cast<long long>(dW) * cols + m];
@@ -154,40 +196,42 @@ __global__ void StrainKernel(Geometry g, const double2* solSph, const double2* s
     }
   }
   __syncthreads();
-  const double sign = (m % 2 == 0) ? 1.0 : -1.0;
+  const T sign = (m % 2 == 0) ? T(1) : T(-1);
   const int n = g.ngll;
-  const double zeta2 = l * (l + 1.0), zeta = sqrt(zeta2);
-  const double s2 = 1.41421356237309504880;
+  const T zeta2 = l * (l + T(1)), zeta = sqrt(zeta2);
+  const T s2 = T(1.41421356237309504880);
   for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
-    double2 A[5] = {C(0, 0), C(0, 0), C(0, 0), C(0, 0), C(0, 0)};
+    T2 A[5] = {Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0)};
     if (any && p >= d.firstNode) {
       const int e = g.nodeElement[p], q = g.nodeQ[p];
-      const double r = g.nodeR[p], jac = g.elemJac[e];
-      double2 U = C(0, 0), V = C(0, 0), W = C(0, 0), rdU = C(0, 0), rdV = C(0, 0), rdW = C(0, 0);
+      const double rd = g.nodeR[p], jac = g.elemJac[e];
+      const T r = static_cast<T>(rd);
+      T2 U = Cx<T2>(0, 0), V = Cx<T2>(0, 0), W = Cx<T2>(0, 0), rdU = Cx<T2>(0, 0), rdV = Cx<T2>(0, 0),
+         rdW = Cx<T2>(0, 0);
       for (int i = 0; i < n; ++i) {
-        const double2* v = vals + static_cast<long long>(e * (n - 1) + i - d.firstGlobal) * 3;
-        const double val = g.pValue[q * n + i];
+        const T2* v = vals + static_cast<long long>(e * (n - 1) + i - d.firstGlobal) * 3;
+        const T val = static_cast<T>(g.pValue[q * n + i]);
         U = CAdd(U, CScale(val, v[0]));
         V = CAdd(V, CScale(val, v[1]));
         W = CAdd(W, CScale(val, v[2]));
-        const double b = r * g.pDeriv[q * n + i] / jac;
+        const T b = static_cast<T>(rd * g.pDeriv[q * n + i] / jac);
         rdU = CAdd(rdU, CScale(b, v[0]));
         rdV = CAdd(rdV, CScale(b, v[1]));
         rdW = CAdd(rdW, CScale(b, v[2]));
       }
-      const double2 t2 = CAdd(CSub(rdU, U), CScale(0.5 * zeta2, V));
-      A[2] = C(t2.x / (3.0 * r), t2.y / (3.0 * r));
+      const T2 t2 = CAdd(CSub(rdU, U), CScale(T(0.5) * zeta2, V));
+      A[2] = Cx<T2>(t2.x / (T(3) * r), t2.y / (T(3) * r));
       if (l >= 1) {
-        const double2 tangential = CAdd(CSub(rdV, V), U);
-        const double2 twist = CSub(W, rdW);
-        const double den = 2.0 * s2 * r;
-        const double2 a1 = CScale(zeta, CAdd(tangential, CI(twist)));
-        const double2 a3 = CScale(zeta, CSub(tangential, CI(twist)));
-        A[1] = C(a1.x / den, a1.y / den);
-        A[3] = C(a3.x / den, a3.y / den);
+        const T2 tangential = CAdd(CSub(rdV, V), U);
+        const T2 twist = CSub(W, rdW);
+        const T den = T(2) * s2 * r;
+        const T2 a1 = CScale(zeta, CAdd(tangential, CI(twist)));
+        const T2 a3 = CScale(zeta, CSub(tangential, CI(twist)));
+        A[1] = Cx<T2>(a1.x / den, a1.y / den);
+        A[3] = Cx<T2>(a3.x / den, a3.y / den);
       }
       if (l >= 2) {
-        const double factor = 0.5 * zeta * sqrt(zeta2 - 2.0) / r;
+        const T factor = T(0.5) * zeta * sqrt(zeta2 - T(2)) / r;
         A[0] = CScale(factor, CSub(V, CI(W)));
         A[4] = CScale(factor, CAdd(V, CI(W)));
       }
@@ -348,15 +392,17 @@ __global__ void CombineKernel(long long values, long long fieldSize, const doubl
 
 // -- the convergence measure ------------------------------------------------------------------
 
-__global__ void RelativeChangeKernel(const double2* next, const double2* now, long long n, double* partial) {
+template <class T2>
+__global__ void RelativeChangeKernel(const T2* next, const T2* now, long long n, double* partial) {
   __shared__ double s0[256], s1[256], s2[256];
   double scale = 0.0, diff = 0.0, finite = 1.0;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
-    const double2 a = next[i], b = now[i];
-    if (!(a.x - a.x == 0.0) || !(a.y - a.y == 0.0)) finite = 0.0;
-    scale = fmax(scale, a.x * a.x + a.y * a.y);
-    const double dx = a.x - b.x, dy = a.y - b.y;
+    const T2 a = next[i], b = now[i];
+    const double ax = a.x, ay = a.y;
+    if (!(ax - ax == 0.0) || !(ay - ay == 0.0)) finite = 0.0;
+    scale = fmax(scale, ax * ax + ay * ay);
+    const double dx = ax - static_cast<double>(b.x), dy = ay - static_cast<double>(b.y);
     diff = fmax(diff, dx * dx + dy * dy);
   }
   s0[threadIdx.x] = scale;
@@ -407,7 +453,8 @@ __global__ void ReduceMaxKernel(const double* partial, int count, double* result
 
 // -- the Anderson mixer ---------------------------------------------------------------------------
 
-__global__ void MixerFirstKernel(long long n, double* x, const double* gx, double* xPrev, double* fPrev) {
+template <class T>
+__global__ void MixerFirstKernel(long long n, T* x, const T* gx, T* xPrev, T* fPrev) {
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
     xPrev[i] = x[i];
@@ -421,27 +468,28 @@ constexpr int kMaxMemory = 8;
 
 // One block per fixed chunk of the vector (fixed by n alone): the new
 // differences, the stored iterate and residual, and the block's partial Gram
-// column and right-hand side, summed in a fixed tree order.
-__global__ void MixerSweepKernel(MixerArgs a) {
+// column and right-hand side (FP64), summed in a fixed tree order.
+template <class T>
+__global__ void MixerSweepKernel(MixerArgsT<T> a) {
   __shared__ double red[kMixThreads][2 * kMaxMemory];
   const long long begin = a.n * blockIdx.x / a.blocks, end = a.n * (blockIdx.x + 1) / a.blocks;
   double col[kMaxMemory], gam[kMaxMemory];
   for (int i = 0; i < a.m; ++i) col[i] = gam[i] = 0.0;
-  double* dFs = a.dF[a.slot];
-  double* dGs = a.dG[a.slot];
+  T* dFs = a.dF[a.slot];
+  T* dGs = a.dG[a.slot];
   for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
-    const double xs = a.x[at], gs = a.gx[at];
-    const double f = gs - xs;
-    const double dx = xs - a.xPrev[at];
-    const double df = f - a.fPrev[at];
+    const T xs = a.x[at], gs = a.gx[at];
+    const T f = gs - xs;
+    const T dx = xs - a.xPrev[at];
+    const T df = f - a.fPrev[at];
     dFs[at] = df;
     dGs[at] = dx + df;
     a.xPrev[at] = xs;
     a.fPrev[at] = f;
     for (int i = 0; i < a.m; ++i) {
-      const double di = i == a.slot ? df : a.dF[i][at];
-      col[i] += di * df;
-      gam[i] += di * f;
+      const double di = i == a.slot ? static_cast<double>(df) : static_cast<double>(a.dF[i][at]);
+      col[i] += di * static_cast<double>(df);
+      gam[i] += di * static_cast<double>(f);
     }
   }
   for (int i = 0; i < a.m; ++i) {
@@ -464,30 +512,41 @@ __global__ void MixerSweepKernel(MixerArgs a) {
     }
 }
 
-// The partials in block order, the Gram matrix's new row and column, and the
+// The partials in a fixed order (one warp per sum, lanes over the blocks,
+// then a fixed shuffle tree), the Gram matrix's new row and column, and the
 // least-squares coefficients (FP64, one thread; gamma[m] = 1 when they hold).
-__global__ void MixerSolveKernel(MixerArgs a) {
+__global__ void MixerSolveKernel(int m, int slot, int memory, int blocks, const double* partial, double* gram,
+                                 double* gamma) {
+  __shared__ double sums[2 * kMaxMemory];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (warp < 2 * m) {
+    const int i = warp < m ? warp : kMaxMemory + (warp - m);
+    double v = 0.0;
+    for (int b = lane; b < blocks; b += 32) v += partial[static_cast<long long>(b) * 2 * kMaxMemory + i];
+    for (int off = 16; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) sums[warp] = v;
+  }
+  __syncthreads();
   if (threadIdx.x != 0) return;
   double col[kMaxMemory], gam[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) col[i] = gam[i] = 0.0;
-  for (int b = 0; b < a.blocks; ++b)
-    for (int i = 0; i < a.m; ++i) {
-      col[i] += a.partial[static_cast<long long>(b) * 2 * kMaxMemory + i];
-      gam[i] += a.partial[static_cast<long long>(b) * 2 * kMaxMemory + kMaxMemory + i];
-    }
-  for (int i = 0; i < a.m; ++i) {
-    a.gram[a.slot * a.memory + i] = col[i];
-    a.gram[i * a.memory + a.slot] = col[i];
+  for (int i = 0; i < m; ++i) {
+    col[i] = sums[i];
+    gam[i] = sums[m + i];
+  }
+  for (int i = 0; i < m; ++i) {
+    gram[slot * memory + i] = col[i];
+    gram[i * memory + slot] = col[i];
   }
   double A[kMaxMemory * kMaxMemory], x[kMaxMemory];
-  for (int i = 0; i < a.m; ++i)
-    for (int j = 0; j < a.m; ++j) A[i * a.m + j] = a.gram[i * a.memory + j];
-  const bool ok = SymmetricLstsq(a.m, A, gam, x);
-  for (int i = 0; i < a.m; ++i) a.gamma[i] = x[i];
-  a.gamma[a.m] = ok ? 1.0 : 0.0;
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) A[i * m + j] = gram[i * memory + j];
+  const bool ok = SymmetricLstsq(m, A, gam, x);
+  for (int i = 0; i < m; ++i) gamma[i] = x[i];
+  gamma[m] = ok ? 1.0 : 0.0;
 }
 
-__global__ void MixerMixKernel(MixerArgs a) {
+template <class T>
+__global__ void MixerMixKernel(MixerArgsT<T> a) {
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   const bool ok = a.gamma[a.m] != 0.0;
   double g[kMaxMemory];
@@ -495,9 +554,35 @@ __global__ void MixerMixKernel(MixerArgs a) {
   for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < a.n; at += stride) {
     double value = a.gx[at];
     if (ok)
-      for (int i = 0; i < a.m; ++i) value -= g[i] * a.dG[i][at];
-    a.x[at] = value;
+      for (int i = 0; i < a.m; ++i) value -= g[i] * static_cast<double>(a.dG[i][at]);
+    a.x[at] = static_cast<T>(value);
   }
+}
+
+// -- the mixed form's refinement glue ----------------------------------------------------------
+
+__global__ void Residual32Kernel(long long n, const double* next, const double* now, float* r) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    r[i] = static_cast<float>(next[i] - now[i]);
+}
+
+__global__ void AddCorrectionKernel(long long n, const float* e, double* s) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    s[i] += static_cast<double>(e[i]);
+}
+
+__global__ void AddInPlaceKernel(long long n, const float* r, float* e) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    e[i] += r[i];
+}
+
+__global__ void CastKernel(long long n, const double* in, float* out) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    out[i] = static_cast<float>(in[i]);
 }
 
 __global__ void BlendKernel(long long n, double gamma, const double2* a, const double2* b, double2* out) {
@@ -514,22 +599,40 @@ int StreamBlocks(long long values) {
 
 }  // namespace
 
-void LaunchForces(const Geometry& g, const double2* spectral, double2* rhsSph, double2* rhsTor,
-                  cudaStream_t stream) {
+namespace {
+template <class T2>
+void Forces(const Geometry& g, const T2* spectral, T2* rhsSph, T2* rhsTor, cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
-  const size_t smem = static_cast<size_t>(g.P) * 6 * sizeof(double2);
-  cudaFuncSetAttribute(ForceKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  const size_t smem = static_cast<size_t>(g.P) * 6 * sizeof(T2);
+  cudaFuncSetAttribute(ForceKernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   prof::Scope scope(prof::kForce, stream);
-  ForceKernel<<<count, 128, smem, stream>>>(g, spectral, rhsSph, rhsTor);
+  ForceKernel<T2><<<count, 128, smem, stream>>>(g, spectral, rhsSph, rhsTor);
 }
 
+template <class T2>
+void Strain(const Geometry& g, const T2* solSph, const T2* solTor, T2* spectral, cudaStream_t stream) {
+  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 3 * sizeof(T2);
+  cudaFuncSetAttribute(StrainKernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  prof::Scope scope(prof::kStrain, stream);
+  StrainKernel<T2><<<count, 128, smem, stream>>>(g, solSph, solTor, spectral);
+}
+}  // namespace
+
+void LaunchForces(const Geometry& g, const double2* spectral, double2* rhsSph, double2* rhsTor,
+                  cudaStream_t stream) {
+  Forces(g, spectral, rhsSph, rhsTor, stream);
+}
+void LaunchForces(const Geometry& g, const float2* spectral, float2* rhsSph, float2* rhsTor, cudaStream_t stream) {
+  Forces(g, spectral, rhsSph, rhsTor, stream);
+}
 void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTor, double2* spectral,
                   cudaStream_t stream) {
-  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
-  const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 3 * sizeof(double2);
-  cudaFuncSetAttribute(StrainKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  prof::Scope scope(prof::kStrain, stream);
-  StrainKernel<<<count, 128, smem, stream>>>(g, solSph, solTor, spectral);
+  Strain(g, solSph, solTor, spectral, stream);
+}
+void LaunchStrain(const Geometry& g, const float2* solSph, const float2* solTor, float2* spectral,
+                  cudaStream_t stream) {
+  Strain(g, solSph, solTor, spectral, stream);
 }
 
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units, const long long* unitOffset,
@@ -573,33 +676,71 @@ void LaunchBlend(long long n, double gamma, const double2* a, const double2* b, 
   BlendKernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(n, gamma, a, b, out);
 }
 
-void LaunchRelativeChange(const double* next, const double* now, long long n, double* partial, int partialCount,
-                          double* result, cudaStream_t stream) {
+namespace {
+template <class T2>
+void RelChange(const T2* next, const T2* now, long long n, double* partial, int partialCount, double* result,
+               cudaStream_t stream) {
   {
-    prof::Scope scope(prof::kOther, stream, 0.0, n * 16.0);
-    RelativeChangeKernel<<<partialCount, 256, 0, stream>>>(reinterpret_cast<const double2*>(next),
-                                                        reinterpret_cast<const double2*>(now), n / 2, partial);
+    prof::Scope scope(prof::kOther, stream, 0.0, n * 2.0 * sizeof(T2));
+    RelativeChangeKernel<T2><<<partialCount, 256, 0, stream>>>(next, now, n, partial);
   }
   prof::Scope scope(prof::kOther, stream);
   ReduceMaxKernel<<<1, 256, 0, stream>>>(partial, partialCount, result);
 }
 
-void LaunchMixerFirst(const MixerArgs& a, cudaStream_t stream) {
-  prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 40.0);
-  MixerFirstKernel<<<StreamBlocks(a.n), 256, 0, stream>>>(a.n, a.x, a.gx, a.xPrev, a.fPrev);
+template <class T>
+void MixerFirst(const MixerArgsT<T>& a, cudaStream_t stream) {
+  prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 5.0 * sizeof(T));
+  MixerFirstKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a.n, a.x, a.gx, a.xPrev, a.fPrev);
 }
 
-void LaunchMixerUpdate(const MixerArgs& a, cudaStream_t stream) {
+template <class T>
+void MixerUpdate(const MixerArgsT<T>& a, cudaStream_t stream) {
   {
-    prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 8.0 * (6 + a.m));
-    MixerSweepKernel<<<a.blocks, kMixThreads, 0, stream>>>(a);
+    prof::Scope scope(prof::kMixer, stream, 0.0, a.n * sizeof(T) * (6 + a.m));
+    MixerSweepKernel<T><<<a.blocks, kMixThreads, 0, stream>>>(a);
   }
   {
     prof::Scope scope(prof::kOther, stream);
-    MixerSolveKernel<<<1, 32, 0, stream>>>(a);
+    MixerSolveKernel<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.m, a.slot, a.memory, a.blocks, a.partial, a.gram,
+                                                           a.gamma);
   }
-  prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 8.0 * (2 + a.m));
-  MixerMixKernel<<<StreamBlocks(a.n), 256, 0, stream>>>(a);
+  prof::Scope scope(prof::kMixer, stream, 0.0, a.n * sizeof(T) * (2 + a.m));
+  MixerMixKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a);
+}
+}  // namespace
+
+void LaunchRelativeChange(const double* next, const double* now, long long n, double* partial, int partialCount,
+                          double* result, cudaStream_t stream) {
+  RelChange(reinterpret_cast<const double2*>(next), reinterpret_cast<const double2*>(now), n / 2, partial,
+            partialCount, result, stream);
+}
+void LaunchRelativeChange(const float* next, const float* now, long long n, double* partial, int partialCount,
+                          double* result, cudaStream_t stream) {
+  RelChange(reinterpret_cast<const float2*>(next), reinterpret_cast<const float2*>(now), n / 2, partial,
+            partialCount, result, stream);
+}
+
+void LaunchMixerFirst(const MixerArgsT<double>& a, cudaStream_t stream) { MixerFirst(a, stream); }
+void LaunchMixerUpdate(const MixerArgsT<double>& a, cudaStream_t stream) { MixerUpdate(a, stream); }
+void LaunchMixerFirst(const MixerArgsT<float>& a, cudaStream_t stream) { MixerFirst(a, stream); }
+void LaunchMixerUpdate(const MixerArgsT<float>& a, cudaStream_t stream) { MixerUpdate(a, stream); }
+
+void LaunchResidual32(long long n, const double* next, const double* now, float* r, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 20.0);
+  Residual32Kernel<<<StreamBlocks(n), 256, 0, stream>>>(n, next, now, r);
+}
+void LaunchAddCorrection(long long n, const float* e, double* s, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 20.0);
+  AddCorrectionKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, e, s);
+}
+void LaunchAddInPlace(long long n, const float* r, float* e, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 12.0);
+  AddInPlaceKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, r, e);
+}
+void LaunchCast(long long n, const double* in, float* out, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 12.0);
+  CastKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, in, out);
 }
 
 }  // namespace sl3dgpu

@@ -1,6 +1,8 @@
 // Device kernels of the 3D step: the degree <-> spin-component maps (strain
 // recovery and memory-force assembly), the streaming step-weight and memory
 // kernels, the load channel, the convergence measure and the Anderson mixer.
+// The maps, the measure and the mixer come in FP64 and FP32 (the mixed
+// form's correction passes); the FP32 mixer keeps its Gram sums in FP64.
 #pragma once
 
 #include "common.cuh"
@@ -45,9 +47,12 @@ struct Geometry {
 // systems' right-hand sides (GridCoupling::SpheroidalForce/ToroidalForce).
 void LaunchForces(const Geometry& g, const double2* spectral, double2* rhsSph, double2* rhsTor,
                   cudaStream_t stream);
+void LaunchForces(const Geometry& g, const float2* spectral, float2* rhsSph, float2* rhsTor, cudaStream_t stream);
 // The deviatoric strain of every degree's solutions into a spectral tensor
 // (StrainOf: AddStrainOfSolution + DeviatoricComponents + Scatter).
 void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTor, double2* spectral,
+                  cudaStream_t stream);
+void LaunchStrain(const Geometry& g, const float2* solSph, const float2* solTor, float2* spectral,
                   cudaStream_t stream);
 // x += sigma_lm K^-1 Load for every degree (AddUnitChannels' load part).
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units,
@@ -93,31 +98,44 @@ void LaunchStageCombine(long long values, double r, const double2* a0, const dou
 void LaunchCombine(long long values, long long fieldSize, const double* mu, bool first,
                    const double2* m0, const double2* m1, const double* mr, double2* o0, double2* o1,
                    double* orr, cudaStream_t stream);
-
 // out = (1 - gamma) a + gamma b over complex values, a or b null for zero.
 void LaunchBlend(long long n, double gamma, const double2* a, const double2* b, double2* out, cudaStream_t stream);
 
-// RelativeChange: max |n|^2, max |n - o|^2 and finiteness over n doubles
-// (complex pairs), into result[3] on the device.
+// RelativeChange: max |n|^2, max |n - o|^2 and finiteness over n reals
+// (complex pairs), into result[3] (FP64) on the device.
 void LaunchRelativeChange(const double* next, const double* now, long long n, double* partial,
                           int partialCount, double* result, cudaStream_t stream);
+void LaunchRelativeChange(const float* next, const float* now, long long n, double* partial, int partialCount,
+                          double* result, cudaStream_t stream);
 
-// The Anderson mixer's sweeps (AndersonMixer.hpp:65-219).
-struct MixerArgs {
+// Refinement glue over n reals: r = next - now rounded to FP32; s += e;
+// e += r; out = FP32 of in.
+void LaunchResidual32(long long n, const double* next, const double* now, float* r, cudaStream_t stream);
+void LaunchAddCorrection(long long n, const float* e, double* s, cudaStream_t stream);
+void LaunchAddInPlace(long long n, const float* r, float* e, cudaStream_t stream);
+void LaunchCast(long long n, const double* in, float* out, cudaStream_t stream);
+
+// The Anderson mixer's sweeps (AndersonMixer.hpp:65-219), on vectors of
+// reals T with the Gram sums in FP64.
+template <class T>
+struct MixerArgsT {
   long long n;
   int m, slot, memory;
-  double* x;
-  const double* gx;
-  double* xPrev;
-  double* fPrev;
-  double** dG;  // device array of memory pointers
-  double** dF;
-  double* partial;  // blocks x 2m
+  T* x;
+  const T* gx;
+  T* xPrev;
+  T* fPrev;
+  T** dG;  // device array of memory pointers
+  T** dF;
+  double* partial;  // blocks x 2 x 8
   int blocks;
   double* gram;     // memory x memory
   double* gamma;    // m (+1 status)
 };
-void LaunchMixerFirst(const MixerArgs& a, cudaStream_t stream);
-void LaunchMixerUpdate(const MixerArgs& a, cudaStream_t stream);
+using MixerArgs = MixerArgsT<double>;
+void LaunchMixerFirst(const MixerArgsT<double>& a, cudaStream_t stream);
+void LaunchMixerUpdate(const MixerArgsT<double>& a, cudaStream_t stream);
+void LaunchMixerFirst(const MixerArgsT<float>& a, cudaStream_t stream);
+void LaunchMixerUpdate(const MixerArgsT<float>& a, cudaStream_t stream);
 
 }  // namespace sl3dgpu

@@ -36,12 +36,13 @@ class Options(ctypes.Structure):
     _fields_ = [("lmax", ctypes.c_int), ("ngll", ctypes.c_int), ("eps", ctypes.c_double),
                 ("oversampling", ctypes.c_double), ("max_iterations", ctypes.c_int),
                 ("rtol", ctypes.c_double), ("damping", ctypes.c_double), ("anderson_memory", ctypes.c_int),
-                ("anderson_rate", ctypes.c_double), ("precision", ctypes.c_int)]
+                ("anderson_rate", ctypes.c_double), ("precision", ctypes.c_int),
+                ("correction_rtol", ctypes.c_double)]
 
     @classmethod
     def defaults(cls, lmax: int, ngll: int = 5, **kw) -> "Options":
         o = cls(lmax=lmax, ngll=ngll, eps=1e-8, oversampling=1.5, max_iterations=40, rtol=1e-11,
-                damping=1.0, anderson_memory=5, anderson_rate=0.5, precision=0)
+                damping=1.0, anderson_memory=5, anderson_rate=0.5, precision=0, correction_rtol=1e-5)
         for k, v in kw.items():
             setattr(o, k, v)
         return o
@@ -51,7 +52,7 @@ class StepInfo(ctypes.Structure):
     """sl3dgpu_step_info (Viscoelastic3D::StepInfo)."""
 
     _fields_ = [("iterations", ctypes.c_int), ("residual", ctypes.c_double), ("converged", ctypes.c_int),
-                ("mixed_passes", ctypes.c_int)]
+                ("mixed_passes", ctypes.c_int), ("correction_passes", ctypes.c_int)]
 
 
 _SIGNED = False
@@ -78,6 +79,7 @@ def _signatures():
         "sl3dgpu_v3d_surface": (i, [v, i, v]),
         "sl3dgpu_v3d_state_strain": (i, [v, v, v]),
         "sl3dgpu_v3d_residual_history": (i, [v, P_double, i]),
+        "sl3dgpu_v3d_correction_history": (i, [v, P_double, i]),
         "sl3dgpu_v3d_step_device": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_stream": (v, [v]),
     }
@@ -198,6 +200,14 @@ class Viscoelastic3D:
         out = np.zeros(max(n, 0))
         if n > 0:
             lib().sl3dgpu_v3d_residual_history(self._h, out.ctypes.data_as(P_double), n)
+        return out
+
+    def correction_history(self) -> np.ndarray:
+        """The mixed form's last step: every FP32 correction pass's relative change."""
+        n = lib().sl3dgpu_v3d_correction_history(self._h, None, 0)
+        out = np.zeros(max(n, 0))
+        if n > 0:
+            lib().sl3dgpu_v3d_correction_history(self._h, out.ctypes.data_as(P_double), n)
         return out
 
     def Surface(self, component="U") -> np.ndarray:
