@@ -240,6 +240,8 @@ def gpu_arm(args, rank, world, device, precision):
         stop.synchronize()
     torch.cuda.synchronize()
     launches = lib().sl3dgpu_launch_count() - launches0
+    history = {"fp64_pass_residuals": [float(f"{v:.3e}") for v in op.residual_history()],
+               "correction_passes": int(op.correction_history().size)}
     lib().sl3dgpu_profile_enable(0)
     prof = profile_read()
     ms = start.elapsed_time(stop)
@@ -262,7 +264,7 @@ def gpu_arm(args, rank, world, device, precision):
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
     return {"op": op, "seconds": times[0].item(), "e2e_seconds": times[1].item(), "passes": passes,
-            "corrections": corrections, "surfaces": surfaces,
+            "corrections": corrections, "surfaces": surfaces, "history": history,
             "infos": infos, "profile": prof, "launches": launches, "clocks": clocks.summary(),
             "setup_s": setup_s, "load_bytes": int(full.numel() * 16)}
 
@@ -410,6 +412,7 @@ def main():
             "config": workload_config(args.precision),
             "passes_per_step": passes_per_step,
             "correction_passes_per_step": r["corrections"] / args.steps,
+            "last_step": r["history"],
             "converged_steps": sum(int(i.converged) for i in r["infos"][args.warmup:]),
             "final_residual": r["infos"][-1].residual,
             "roofline": roofline(r["profile"], fp64.value, fp32.value),

@@ -64,7 +64,7 @@ typedef struct sl3dgpu_band_system {
 int sl3dgpu_band_factor_batch(const sl3dgpu_band_system* dev_systems,
                               const sl3dgpu_band_system* host_systems, int count,
                               double* bands, int* pivots, int* info, int lu, void* stream);
-/* The work items of a batch solve: (system, first column) pairs, one per 32
+/* The work items of a batch solve: (system, first column) pairs, one per 64
  * right-hand sides; returns their count (items may be NULL to ask). */
 int sl3dgpu_band_work_items(const sl3dgpu_band_system* host_systems, int count, int* items,
                             int capacity);
@@ -141,7 +141,7 @@ typedef struct sl3dgpu_v3d_options {
   int anderson_memory;   /* 5 */
   double anderson_rate;  /* 0.5 */
   int precision;         /* 0: FP64 throughout; 1: mixed (see sl3dgpu_v3d_create) */
-  double correction_rtol; /* mixed form: relative change that ends an FP32 correction, 1e-5 */
+  double correction_rtol; /* mixed form: the finest relative change an FP32 correction iterates to, 1e-5 */
 } sl3dgpu_v3d_options;
 
 /* Viscoelastic3D::StepInfo (Viscoelastic3D.hpp:357-375). */
@@ -171,8 +171,9 @@ int sl3dgpu_standard_earth(int elements, double kelvin_fraction, double kelvin_d
  * replaces the iterations between FP64 passes by a correction solved in
  * FP32 (transforms, band solves with FP32 copies of the FP64 factors, force
  * and strain maps, Anderson mixing with FP64 Gram sums), iterated until its
- * relative change is at most correction_rtol. No counterpart in the
- * reference, whose Converge is FP64 throughout. */
+ * relative change is at most max(correction_rtol, 0.1 rtol / residual), the
+ * accuracy that brings the next FP64 residual under rtol. No counterpart in
+ * the reference, whose Converge is FP64 throughout. */
 typedef struct sl3dgpu_v3d sl3dgpu_v3d;
 typedef struct sl3dgpu_v3d_state sl3dgpu_v3d_state;
 int sl3dgpu_v3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options* options,

@@ -11,13 +11,15 @@
 //    columns a rank-1 step touches, 2kl+ku+1 rows deep for LU) is staged in
 //    shared memory as a ring and streamed column by column, so each band
 //    value is read from and written to HBM once;
-//  - solves: one warp per (system, 32 right-hand sides). Right-hand sides
-//    are stored row-major (dof-major, the columns fastest), so a warp's load
-//    of one dof across its 32 columns is one coalesced 256-byte access; a
-//    degree's 2(l+1) real columns (its orders m >= 0, real and imaginary
-//    parts) are its coalesced right-hand-side vectors. The recent solution
-//    values live in a per-warp shared-memory ring; the band values are
-//    broadcast reads. Optional diagonal scaling and pinned dofs are fused
+//  - solves: one warp per (system, 64 right-hand sides), two adjacent
+//    columns a lane (an order's real and imaginary parts). Right-hand sides
+//    are stored row-major (dof-major, the columns fastest), so a warp's rows
+//    are coalesced; a degree's 2(l+1) real columns (its orders m >= 0) are
+//    its right-hand-side vectors. Each substitution runs in chunks of rows:
+//    the next chunk's band columns and right-hand-side rows are copied into
+//    shared memory (cp.async) while the current one is solved, the recent
+//    solution values live in a per-warp shared-memory ring, and a band value
+//    read serves two columns. Optional diagonal scaling and pinned dofs are fused
 //    in (DegreeOperator::BeginSolve/FinishSolve, src/DegreeOperator.cpp:861-901).
 #include <algorithm>
 #include <vector>
@@ -166,101 +168,423 @@ struct WorkItem {
   int column;
 };
 
+constexpr int kSolveCols = 2 * kWarp;  // right-hand sides per warp: two adjacent columns a lane
+constexpr int kChunk = 16;             // rows staged per step
+constexpr int kBuffers = 3;            // staged chunks: the current one and two ahead
+
 template <class T>
-__device__ inline T LoadRhs(const sl3dgpu_band_system& s, const T* rhs, const T* scales, int j, int col) {
-  if (j == s.pinned0 || j == s.pinned1) return T(0);
-  T b = rhs[s.rhs + static_cast<long long>(j) * s.nrhs + col];
-  if (s.scale >= 0) b *= scales[s.scale + j];
+struct PairOf;
+template <>
+struct PairOf<float> {
+  using type = float2;
+};
+template <>
+struct PairOf<double> {
+  using type = double2;
+};
+
+// Asynchronous global -> shared copies of 4, 8 or 16 bytes, and their groups.
+template <class T>
+__device__ inline void CpAsync(T* dst, const T* src) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "copy size");
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+  else if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ inline void CpCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ inline void CpWaitAll() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+__device__ inline void CpWaitOne() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// A solve launch's per-warp shared-memory plan.
+struct SolvePlan {
+  int depth;    // ring slots: the solve's reach + 1
+  int bandCap;  // band values one staged chunk holds
+  template <class T>
+  __host__ __device__ long long Bytes() const {
+    const long long pairs = static_cast<long long>(depth) * kWarp + static_cast<long long>(kBuffers) * kChunk * kWarp;
+    const long long b = pairs * 2 * sizeof(T) + static_cast<long long>(kBuffers) * (bandCap + kChunk) * sizeof(T) +
+                        static_cast<long long>(kBuffers) * kChunk * sizeof(int);
+    return (b + 15) / 16 * 16;
+  }
+};
+
+// One warp's staging: the solution ring (depth x 32 lane pairs, each lane's
+// own columns), and kBuffers of band columns, right-hand-side rows (lane
+// pairs), row scales and pivots.
+template <class T>
+struct Stage {
+  using T2 = typename PairOf<T>::type;
+  T2* ring;
+  T2* rhs;      // [buffer][kChunk][32]
+  T* band;      // [buffer][bandCap]
+  T* scale;     // [buffer][kChunk]
+  int* pivot;   // [buffer][kChunk]
+  int bandCap;
+  __device__ Stage(unsigned char* base, const SolvePlan& plan) : bandCap(plan.bandCap) {
+    ring = reinterpret_cast<T2*>(base);
+    rhs = ring + static_cast<long long>(plan.depth) * kWarp;
+    band = reinterpret_cast<T*>(rhs + static_cast<long long>(kBuffers) * kChunk * kWarp);
+    scale = band + static_cast<long long>(kBuffers) * plan.bandCap;
+    pivot = reinterpret_cast<int*>(scale + kBuffers * kChunk);
+  }
+  __device__ T2* Rhs(int buf, int r) const { return rhs + (buf * kChunk + r) * kWarp; }
+  __device__ T* Band(int buf) const { return band + static_cast<long long>(buf) * bandCap; }
+  __device__ T Scale(int buf, int r) const { return scale[buf * kChunk + r]; }
+  __device__ int Pivot(int buf, int r) const { return pivot[buf * kChunk + r]; }
+};
+
+// The solve's view of one work item: the system, this lane's two columns.
+template <class T>
+struct Lane {
+  using T2 = typename PairOf<T>::type;
+  sl3dgpu_band_system s;
+  T* x;
+  int col;      // the lane's first column
+  bool live0, live1;
+  bool paired;  // both columns live and the pair 2 sizeof(T)-aligned
+  __device__ T2 Load(int row) const {
+    const T* at = x + static_cast<long long>(row) * s.nrhs + col;
+    if (paired) return *reinterpret_cast<const T2*>(at);
+    T2 v;
+    v.x = live0 ? at[0] : T(0);
+    v.y = live1 ? at[1] : T(0);
+    return v;
+  }
+  __device__ void Store(int row, T2 v) const {
+    T* at = x + static_cast<long long>(row) * s.nrhs + col;
+    if (paired) {
+      *reinterpret_cast<T2*>(at) = v;
+    } else {
+      if (live0) at[0] = v.x;
+      if (live1) at[1] = v.y;
+    }
+  }
+};
+
+// Stage band columns [c0, c1) (ld values each, contiguous), right-hand-side
+// rows [r0, r1) of this lane's columns, their scales and (pivots != null)
+// pivots [p0, p1) into buffer `buf`, as one copy group.
+template <class T>
+__device__ inline void StageChunk(const Stage<T>& st, int buf, const T* ab, int ld, int c0, int c1,
+                                  const Lane<T>& ln, int r0, int r1, const T* scales, const int* pivots, int p0,
+                                  int p1, int lane) {
+  using T2 = typename PairOf<T>::type;
+  const T* src = ab + static_cast<long long>(c0) * ld;
+  T* band = st.Band(buf);
+  const int count = (c1 - c0) * ld;
+  for (int e = lane; e < count; e += kWarp) CpAsync(band + e, src + e);
+  for (int r = r0; r < r1; ++r) {
+    T2* dst = st.Rhs(buf, r - r0) + lane;
+    const T* at = ln.x + static_cast<long long>(r) * ln.s.nrhs + ln.col;
+    if (ln.paired) {
+      CpAsync(dst, reinterpret_cast<const T2*>(at));
+    } else {
+      if (ln.live0) CpAsync(reinterpret_cast<T*>(dst), at);
+      if (ln.live1) CpAsync(reinterpret_cast<T*>(dst) + 1, at + 1);
+    }
+  }
+  if (ln.s.scale >= 0)
+    for (int r = r0 + lane; r < r1; r += kWarp) CpAsync(st.scale + buf * kChunk + (r - r0), scales + ln.s.scale + r);
+  if (pivots != nullptr)
+    for (int r = p0 + lane; r < p1; r += kWarp) CpAsync(st.pivot + buf * kChunk + (r - p0), pivots + r);
+  CpCommit();
+}
+
+// The chunks of one substitution through the staging buffers: chunk c is
+// staged two chunks ahead of its use, into buffer c % kBuffers.
+template <class StageFn, class SolveFn>
+__device__ inline void Pipeline(int chunks, StageFn stage, SolveFn solve) {
+  if (chunks > 0) stage(0);
+  if (chunks > 1) stage(1);
+  for (int c = 0; c < chunks; ++c) {
+    if (c + 1 < chunks)
+      CpWaitOne();
+    else
+      CpWaitAll();
+    __syncwarp();
+    if (c + 2 < chunks) stage(c + 2);  // its buffer held chunk c - 1, done
+    solve(c, c % kBuffers);
+    __syncwarp();
+  }
+}
+
+template <class T>
+__device__ inline typename PairOf<T>::type Scaled(typename PairOf<T>::type v, T f) {
+  v.x *= f;
+  v.y *= f;
+  return v;
+}
+
+// A right-hand side's value as the solve starts from it: zero at a pinned
+// dof, scaled by the row's factor otherwise.
+template <class T>
+__device__ inline typename PairOf<T>::type Start(const Lane<T>& ln, const Stage<T>& st, int buf, int r, int row,
+                                                 int lane) {
+  using T2 = typename PairOf<T>::type;
+  if (row == ln.s.pinned0 || row == ln.s.pinned1) {
+    T2 z;
+    z.x = z.y = T(0);
+    return z;
+  }
+  T2 b = st.Rhs(buf, r)[lane];
+  if (ln.s.scale >= 0) b = Scaled(b, st.Scale(buf, r));
   return b;
 }
 
 template <class T>
-__global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items, int itemCount,
-                                    const T* bands, T* rhs, const T* scales) {
-  const int warp = blockIdx.x * (blockDim.x / kWarp) + threadIdx.x / kWarp;
-  const int lane = threadIdx.x % kWarp;
-  extern __shared__ __align__(16) unsigned char ringBytes[];
-  T* ring = reinterpret_cast<T*>(ringBytes) + (threadIdx.x / kWarp) * kRing * kWarp;
-  if (warp >= itemCount) return;
-  const WorkItem item = items[warp];
-  const sl3dgpu_band_system s = systems[item.system];
-  const int col = item.column + lane;
-  const bool live = col < s.nrhs;
-  const int n = s.n, kd = s.ku, ld = kd + 1;
-  const T* ab = bands + s.band;
-  T* x = rhs + s.rhs;
-  // U^T y = b, forward.
-  for (int j = 0; j < n; ++j) {
-    T sum = live ? LoadRhs(s, rhs, scales, j, col) : T(0);
-    const T* column = ab + static_cast<long long>(j) * ld + kd - j;  // column[i] = U(i, j)
-    for (int i = max(0, j - kd); i < j; ++i) sum -= __ldg(column + i) * ring[(i % kRing) * kWarp + lane];
-    const T y = sum / __ldg(column + j);
-    ring[(j % kRing) * kWarp + lane] = y;
-    if (live) x[static_cast<long long>(j) * s.nrhs + col] = y;
-  }
-  // U x = y, backward: row i takes its updates from j = i + kd down to i + 1.
-  for (int i = n - 1; i >= 0; --i) {
-    T v = live ? x[static_cast<long long>(i) * s.nrhs + col] : T(0);
-    for (int j = min(n - 1, i + kd); j > i; --j)
-      v -= __ldg(ab + static_cast<long long>(j) * ld + kd + i - j) * ring[(j % kRing) * kWarp + lane];
-    v /= __ldg(ab + static_cast<long long>(i) * ld + kd);
-    ring[(i % kRing) * kWarp + lane] = v;
-    if (live) {
-      T out = v;
-      if (s.scale >= 0) out *= scales[s.scale + i];
-      x[static_cast<long long>(i) * s.nrhs + col] = out;
-    }
-  }
+__device__ inline Lane<T> LaneOf(const sl3dgpu_band_system& s, T* rhs, int column, int lane) {
+  using T2 = typename PairOf<T>::type;
+  Lane<T> ln;
+  ln.s = s;
+  ln.x = rhs + s.rhs;
+  ln.col = column + 2 * lane;
+  ln.live0 = ln.col < s.nrhs;
+  ln.live1 = ln.col + 1 < s.nrhs;
+  ln.paired = ln.live1 && (reinterpret_cast<unsigned long long>(ln.x + ln.col) % sizeof(T2) == 0) &&
+              (s.nrhs % 2 == 0);
+  return ln;
 }
 
+// The ring slot of row j given the slot of row j0 (rows within depth of it).
+__device__ inline int SlotBack(int slot, int t, int depth) {
+  const int k = slot - t;
+  return k < 0 ? k + depth : k;
+}
+__device__ inline int SlotAhead(int slot, int t, int depth) {
+  const int k = slot + t;
+  return k >= depth ? k - depth : k;
+}
+
+// U^T U x = b, warp per (system, 64 right-hand sides): the forward and the
+// backward substitution in chunks of rows whose band columns and
+// right-hand-side rows are staged in shared memory two chunks ahead; each
+// lane carries two columns (a band value read serves both), two independent
+// partial sums per column, and the diagonal's reciprocal formed off the
+// dependence chain.
+template <class T>
+__global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items, int itemCount,
+                                    const T* bands, T* rhs, const T* scales, SolvePlan plan) {
+  using T2 = typename PairOf<T>::type;
+  extern __shared__ __align__(16) unsigned char solveSmem[];
+  const int warpInBlock = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  const int warp = blockIdx.x * (blockDim.x / kWarp) + warpInBlock;
+  if (warp >= itemCount) return;
+  const Stage<T> st(solveSmem + warpInBlock * plan.Bytes<T>(), plan);
+  const WorkItem item = items[warp];
+  const Lane<T> ln = LaneOf(systems[item.system], rhs, item.column, lane);
+  const int n = ln.s.n, kd = ln.s.ku, ld = kd + 1, depth = plan.depth;
+  const T* ab = bands + ln.s.band;
+  T2* ring = st.ring + lane;
+  const int chunks = (n + kChunk - 1) / kChunk;
+  // U^T y = b, forward: chunk c holds rows [c kChunk, ...) and their columns.
+  int slot = 0;  // the ring slot of the current row (row mod depth)
+  Pipeline(
+      chunks,
+      [&](int c) {
+        const int j0 = c * kChunk, j1 = min(n, j0 + kChunk);
+        StageChunk(st, c % kBuffers, ab, ld, j0, j1, ln, j0, j1, scales, nullptr, 0, 0, lane);
+      },
+      [&](int c, int buf) {
+        const int j0 = c * kChunk, j1 = min(n, j0 + kChunk);
+        const T* band = st.Band(buf);
+        for (int j = j0; j < j1; ++j) {
+          const T* column = band + (j - j0) * ld + kd;  // column[-t] = U(j - t, j)
+          const T inv = T(1) / column[0];
+          T2 a = Start(ln, st, buf, j - j0, j, lane);
+          T2 b;
+          b.x = b.y = T(0);
+          const int reach = min(kd, j);
+          int t = 1;
+          for (; t + 1 <= reach; t += 2) {
+            const T u0 = column[-t], u1 = column[-t - 1];
+            const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
+            const T2 y1 = ring[SlotBack(slot, t + 1, depth) * kWarp];
+            a.x -= u0 * y0.x;
+            a.y -= u0 * y0.y;
+            b.x -= u1 * y1.x;
+            b.y -= u1 * y1.y;
+          }
+          if (t <= reach) {
+            const T u0 = column[-t];
+            const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
+            a.x -= u0 * y0.x;
+            a.y -= u0 * y0.y;
+          }
+          T2 y;
+          y.x = (a.x + b.x) * inv;
+          y.y = (a.y + b.y) * inv;
+          ring[slot * kWarp] = y;
+          ln.Store(j, y);
+          slot = SlotAhead(slot, 1, depth);
+        }
+      });
+  // U x = y, backward: chunk c holds rows [i0, i1) counted from the end and
+  // the columns [i0, i1 + kd) their updates come from.
+  slot = (n - 1) % depth;
+  Pipeline(
+      chunks,
+      [&](int c) {
+        const int i1 = n - c * kChunk, i0 = max(0, i1 - kChunk);
+        StageChunk(st, c % kBuffers, ab, ld, i0, min(n, i1 + kd), ln, i0, i1, scales, nullptr, 0, 0, lane);
+      },
+      [&](int c, int buf) {
+        const int i1 = n - c * kChunk, i0 = max(0, i1 - kChunk);
+        const T* band = st.Band(buf);
+        for (int i = i1 - 1; i >= i0; --i) {
+          const int r = i - i0;
+          const T inv = T(1) / band[r * ld + kd];
+          T2 a = st.Rhs(buf, r)[lane];
+          T2 b;
+          b.x = b.y = T(0);
+          const int reach = min(kd, n - 1 - i);
+          int t = 1;
+          for (; t + 1 <= reach; t += 2) {
+            const T u0 = band[(r + t) * ld + kd - t];  // U(i, i + t)
+            const T u1 = band[(r + t + 1) * ld + kd - t - 1];
+            const T2 y0 = ring[SlotAhead(slot, t, depth) * kWarp];
+            const T2 y1 = ring[SlotAhead(slot, t + 1, depth) * kWarp];
+            a.x -= u0 * y0.x;
+            a.y -= u0 * y0.y;
+            b.x -= u1 * y1.x;
+            b.y -= u1 * y1.y;
+          }
+          if (t <= reach) {
+            const T u0 = band[(r + t) * ld + kd - t];
+            const T2 y0 = ring[SlotAhead(slot, t, depth) * kWarp];
+            a.x -= u0 * y0.x;
+            a.y -= u0 * y0.y;
+          }
+          T2 v;
+          v.x = (a.x + b.x) * inv;
+          v.y = (a.y + b.y) * inv;
+          ring[slot * kWarp] = v;
+          if (ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
+          ln.Store(i, v);
+          slot = SlotBack(slot, 1, depth);
+        }
+      });
+}
+
+// P L U x = b (LAPACK dgbtrs's order), warp per (system, 64 right-hand
+// sides), staged like the Cholesky solve. Forward: the window x_j .. x_{j+kl}
+// in the ring, the interchanges and eliminations in turn; right-hand-side row
+// j + kl enters as row j is eliminated. Backward: U with kl + ku
+// superdiagonals.
 template <class T>
 __global__ void LuSolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items, int itemCount,
-                              const T* bands, const int* pivotsAll, T* rhs, const T* scales) {
-  const int warp = blockIdx.x * (blockDim.x / kWarp) + threadIdx.x / kWarp;
-  const int lane = threadIdx.x % kWarp;
-  extern __shared__ __align__(16) unsigned char ringBytes[];
-  T* ring = reinterpret_cast<T*>(ringBytes) + (threadIdx.x / kWarp) * kRing * kWarp;
+                              const T* bands, const int* pivotsAll, T* rhs, const T* scales, SolvePlan plan) {
+  using T2 = typename PairOf<T>::type;
+  extern __shared__ __align__(16) unsigned char solveSmem[];
+  const int warpInBlock = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  const int warp = blockIdx.x * (blockDim.x / kWarp) + warpInBlock;
   if (warp >= itemCount) return;
+  const Stage<T> st(solveSmem + warpInBlock * plan.Bytes<T>(), plan);
   const WorkItem item = items[warp];
-  const sl3dgpu_band_system s = systems[item.system];
-  const int col = item.column + lane;
-  const bool live = col < s.nrhs;
-  const int n = s.n, kl = s.kl, ku = s.ku, kv = kl + ku, ld = 2 * kl + ku + 1;
-  const T* ab = bands + s.band;
-  const int* pivots = pivotsAll + s.pivots;
-  T* x = rhs + s.rhs;
-  auto at = [&](int i, int j) { return __ldg(ab + static_cast<long long>(j) * ld + kv + i - j); };
-  auto slot = [&](int i) -> T& { return ring[(i % kRing) * kWarp + lane]; };
-  // L y = P^T b: the window x_j .. x_{j+kl} in the ring, interchanges and
-  // eliminations in turn.
-  for (int i = 0; i < min(kl, n); ++i) slot(i) = live ? LoadRhs(s, rhs, scales, i, col) : T(0);
-  for (int j = 0; j < n; ++j) {
-    if (j + kl < n) slot(j + kl) = live ? LoadRhs(s, rhs, scales, j + kl, col) : T(0);
-    if (j + 1 < n) {
-      const int p = pivots[j];
-      if (p != j) {
-        const T t = slot(p);
-        slot(p) = slot(j);
-        slot(j) = t;
-      }
-      const T xj = slot(j);
-      const int lm = min(kl, n - 1 - j);
-      for (int i = j + 1; i <= j + lm; ++i) slot(i) -= at(i, j) * xj;
+  const Lane<T> ln = LaneOf(systems[item.system], rhs, item.column, lane);
+  const int n = ln.s.n, kl = ln.s.kl, ku = ln.s.ku, kv = kl + ku, ld = 2 * kl + ku + 1, depth = plan.depth;
+  const T* ab = bands + ln.s.band;
+  const int* pivots = pivotsAll + ln.s.pivots;
+  T2* ring = st.ring + lane;
+  const int chunks = (n + kChunk - 1) / kChunk;
+  // The first kl rows of the window, before the chunks (row i in slot i).
+  for (int i = 0; i < min(kl, n); ++i) {
+    T2 b;
+    b.x = b.y = T(0);
+    if (i != ln.s.pinned0 && i != ln.s.pinned1) {
+      b = ln.Load(i);
+      if (ln.s.scale >= 0) b = Scaled(b, scales[ln.s.scale + i]);
     }
-    if (live) x[static_cast<long long>(j) * s.nrhs + col] = slot(j);
+    ring[i * kWarp] = b;
   }
-  // U x = y with kl + ku superdiagonals, backward.
-  for (int i = n - 1; i >= 0; --i) {
-    T v = live ? x[static_cast<long long>(i) * s.nrhs + col] : T(0);
-    for (int j = min(n - 1, i + kv); j > i; --j) v -= at(i, j) * slot(j);
-    v /= at(i, i);
-    slot(i) = v;
-    if (live) {
-      T out = v;
-      if (s.scale >= 0) out *= scales[s.scale + i];
-      x[static_cast<long long>(i) * s.nrhs + col] = out;
-    }
-  }
+  // Forward chunk c: rows j in [j0, j1), their columns and pivots, and the
+  // right-hand-side rows [j0 + kl, j1 + kl) that enter the window.
+  int slot = 0;
+  Pipeline(
+      chunks,
+      [&](int c) {
+        const int j0 = c * kChunk, j1 = min(n, j0 + kChunk);
+        StageChunk(st, c % kBuffers, ab, ld, j0, j1, ln, min(n, j0 + kl), min(n, j1 + kl), scales, pivots, j0, j1,
+                   lane);
+      },
+      [&](int c, int buf) {
+        const int j0 = c * kChunk, j1 = min(n, j0 + kChunk);
+        const T* band = st.Band(buf);
+        for (int j = j0; j < j1; ++j) {
+          if (j + kl < n) ring[SlotAhead(slot, kl, depth) * kWarp] = Start(ln, st, buf, j - j0, j + kl, lane);
+          T2 xj = ring[slot * kWarp];
+          if (j + 1 < n) {
+            // a pivot row lies within the window (dgbtrf's kl rows below);
+            // one outside it is ignored rather than followed out of the ring
+            const int p = st.Pivot(buf, j - j0);
+            if (p > j && p - j <= kl) {
+              T2* sp = ring + SlotAhead(slot, p - j, depth) * kWarp;
+              const T2 t = *sp;
+              *sp = xj;
+              xj = t;
+              ring[slot * kWarp] = xj;
+            }
+            const int lm = min(kl, n - 1 - j);
+            const T* column = band + (j - j0) * ld + kv;  // column[t] = L(j + t, j)
+            for (int t = 1; t <= lm; ++t) {
+              T2* si = ring + SlotAhead(slot, t, depth) * kWarp;
+              T2 v = *si;
+              v.x -= column[t] * xj.x;
+              v.y -= column[t] * xj.y;
+              *si = v;
+            }
+          }
+          ln.Store(j, xj);
+          slot = SlotAhead(slot, 1, depth);
+        }
+      });
+  // Backward chunk c: rows [i0, i1) from the end, columns [i0, i1 + kv).
+  slot = (n - 1) % depth;
+  Pipeline(
+      chunks,
+      [&](int c) {
+        const int i1 = n - c * kChunk, i0 = max(0, i1 - kChunk);
+        StageChunk(st, c % kBuffers, ab, ld, i0, min(n, i1 + kv), ln, i0, i1, scales, nullptr, 0, 0, lane);
+      },
+      [&](int c, int buf) {
+        const int i1 = n - c * kChunk, i0 = max(0, i1 - kChunk);
+        const T* band = st.Band(buf);
+        for (int i = i1 - 1; i >= i0; --i) {
+          const int r = i - i0;
+          const T inv = T(1) / band[r * ld + kv];
+          T2 a = st.Rhs(buf, r)[lane];
+          T2 b;
+          b.x = b.y = T(0);
+          const int reach = min(kv, n - 1 - i);
+          int t = 1;
+          for (; t + 1 <= reach; t += 2) {
+            const T u0 = band[(r + t) * ld + kv - t];  // U(i, i + t)
+            const T u1 = band[(r + t + 1) * ld + kv - t - 1];
+            const T2 y0 = ring[SlotAhead(slot, t, depth) * kWarp];
+            const T2 y1 = ring[SlotAhead(slot, t + 1, depth) * kWarp];
+            a.x -= u0 * y0.x;
+            a.y -= u0 * y0.y;
+            b.x -= u1 * y1.x;
+            b.y -= u1 * y1.y;
+          }
+          if (t <= reach) {
+            const T u0 = band[(r + t) * ld + kv - t];
+            const T2 y0 = ring[SlotAhead(slot, t, depth) * kWarp];
+            a.x -= u0 * y0.x;
+            a.y -= u0 * y0.y;
+          }
+          T2 v;
+          v.x = (a.x + b.x) * inv;
+          v.y = (a.y + b.y) * inv;
+          ring[slot * kWarp] = v;
+          if (ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
+          ln.Store(i, v);
+          slot = SlotBack(slot, 1, depth);
+        }
+      });
 }
 
 int Validate(const sl3dgpu_band_system* hostSystems, int count, bool lu) {
@@ -311,11 +635,11 @@ int BandFactorBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sy
   return SL3DGPU_OK;
 }
 
-// The work items of a batch: one per (system, 32 right-hand sides).
+// The work items of a batch: one per (system, 64 right-hand sides).
 std::vector<int2> BandWorkItems(const sl3dgpu_band_system* hostSystems, int count) {
   std::vector<int2> items;
   for (int i = 0; i < count; ++i)
-    for (int c = 0; c < hostSystems[i].nrhs; c += kWarp) items.push_back(make_int2(i, c));
+    for (int c = 0; c < hostSystems[i].nrhs; c += kSolveCols) items.push_back(make_int2(i, c));
   return items;
 }
 
@@ -326,8 +650,25 @@ int SolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system*
                int lu, cudaStream_t stream) {
   if (itemCount == 0) return SL3DGPU_OK;
   if (int st = Validate(hostSystems, count, lu != 0); st != SL3DGPU_OK) return st;
-  constexpr int warpsPerBlock = 4;
-  const size_t smem = static_cast<size_t>(warpsPerBlock) * kRing * kWarp * sizeof(T);
+  // The ring spans the solve's reach (kd; kl + ku for LU); a staged chunk the
+  // band columns of kChunk rows and of the reach beyond them.
+  int reach = 0, ldMax = 0;
+  for (int i = 0; i < count; ++i) {
+    const auto& s = hostSystems[i];
+    reach = std::max(reach, lu ? s.kl + s.ku : s.ku);
+    ldMax = std::max(ldMax, lu ? 2 * s.kl + s.ku + 1 : s.ku + 1);
+  }
+  SolvePlan plan{};
+  plan.depth = reach + 1;
+  plan.bandCap = (kChunk + reach) * ldMax;
+  const size_t perWarp = static_cast<size_t>(plan.Bytes<T>());
+  int warpsPerBlock = 4;
+  while (warpsPerBlock > 1 && perWarp * warpsPerBlock > 100 * 1024) warpsPerBlock /= 2;
+  const size_t smem = perWarp * warpsPerBlock;
+  if (smem > 200 * 1024) {
+    SetError("band solve: the staged band exceeds shared memory");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
   const int blocks = (itemCount + warpsPerBlock - 1) / warpsPerBlock;
   const auto* items = reinterpret_cast<const WorkItem*>(devItems);
   double flops = 0.0, bytes = 0.0;
@@ -342,12 +683,12 @@ int SolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system*
     SL3D_CUDA(cudaFuncSetAttribute(LuSolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
     LuSolveKernel<T><<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount, bands, pivots,
-                                                                     rhs, scales);
+                                                                     rhs, scales, plan);
   } else {
     SL3D_CUDA(cudaFuncSetAttribute(CholeskySolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
     CholeskySolveKernel<T><<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount, bands,
-                                                                           rhs, scales);
+                                                                           rhs, scales, plan);
   }
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;

@@ -32,6 +32,7 @@ namespace {
 // sides from a 256-byte boundary.
 constexpr long long kStaticDoubles = 1LL << 19;
 constexpr long long kItemsAt = 8;  // doubles reserved for the descriptor (56 bytes)
+constexpr int kSolveColumns = 64;  // right-hand sides per work item of the batched solve
 
 static __device__ __align__(256) double gSolveScratch[kStaticDoubles];
 
@@ -70,7 +71,7 @@ __global__ void DescribeKernel(double* base, int n, int kd, int nrhs, long long 
     s->pinned1 = -1;
   }
   auto* item = reinterpret_cast<int2*>(base + kItemsAt);
-  for (int i = threadIdx.x; i < items; i += blockDim.x) item[i] = make_int2(0, kWarp * i);
+  for (int i = threadIdx.x; i < items; i += blockDim.x) item[i] = make_int2(0, kSolveColumns * i);
 }
 
 // Column-major (n x nrhs) to row-major and back.
@@ -104,7 +105,7 @@ extern "C" int sl3dgpu_band_cholesky_solve_noalloc(const double* ab, int n, int 
     SetError("null band or right-hand sides");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  const int items = (nrhs + kWarp - 1) / kWarp;
+  const int items = (nrhs + kSolveColumns - 1) / kSolveColumns;
   const long long rhsAt = ((kItemsAt + items + 31) / 32) * 32;
   const long long need = rhsAt + static_cast<long long>(n) * nrhs;
   if (need > kStaticDoubles) {

@@ -10,7 +10,7 @@
 // The contraction is one dense matrix product per (spin, order) with the
 // batch's fields as columns, run here as a batched FP64 register-tiled GEMM;
 // the FFT is a mixed-radix (2, 3, 4, 5) Stockham transform in shared memory,
-// several rings per CTA.
+// one warp per ring (warp-synchronous stages), several rings per CTA.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -190,164 +190,221 @@ __device__ inline T2 Sub(T2 a, T2 b) {
   return Make<T2>(a.x - b.x, a.y - b.y);
 }
 
-// e^{sign 2 pi i e / n} from the table of e^{2 pi i x / n}.
-template <class T2>
-__device__ inline T2 Twiddle(const T2* tw, int e, int n, int sign) {
-  T2 w = tw[e % n];
-  if (sign < 0) w.y = -w.y;
-  return w;
+// The DFT of R values in registers, y_u = sum_q v_q e^{sign 2 pi i q u / R},
+// for the radices of the plans (2, 3, 4, 5), with the roots as constants.
+template <class T2, int R>
+__device__ inline void Butterfly(T2 (&v)[R], int sign) {
+  using T = typename Real<T2>::type;
+  auto I = [](T2 a) { return Make<T2>(-a.y, a.x); };  // i a
+  auto S = [](T k, T2 a) { return Make<T2>(k * a.x, k * a.y); };
+  const T sg = sign > 0 ? T(1) : T(-1);
+  if constexpr (R == 2) {
+    const T2 a = v[0], b = v[1];
+    v[0] = Add(a, b);
+    v[1] = Sub(a, b);
+  } else if constexpr (R == 3) {
+    const T2 t = Add(v[1], v[2]);
+    const T2 d = S(sg * T(0.86602540378443864676), Sub(v[1], v[2]));
+    const T2 a = Sub(v[0], S(T(0.5), t));
+    v[0] = Add(v[0], t);
+    v[1] = Add(a, I(d));
+    v[2] = Sub(a, I(d));
+  } else if constexpr (R == 4) {
+    const T2 a0 = Add(v[0], v[2]), a1 = Sub(v[0], v[2]);
+    const T2 b0 = Add(v[1], v[3]), b1 = S(sg, Sub(v[1], v[3]));
+    v[0] = Add(a0, b0);
+    v[1] = Add(a1, I(b1));
+    v[2] = Sub(a0, b0);
+    v[3] = Sub(a1, I(b1));
+  } else {
+    static_assert(R == 5, "radix");
+    const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);
+    const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);
+    const T2 t1 = Add(v[1], v[4]), t2 = Add(v[2], v[3]);
+    const T2 d1 = Sub(v[1], v[4]), d2 = Sub(v[2], v[3]);
+    const T2 a1 = Add(v[0], Add(S(c1, t1), S(c2, t2)));
+    const T2 a2 = Add(v[0], Add(S(c2, t1), S(c1, t2)));
+    const T2 b1 = S(sg, Add(S(s1, d1), S(s2, d2)));
+    const T2 b2 = S(sg, Sub(S(s2, d1), S(s1, d2)));
+    v[0] = Add(v[0], Add(t1, t2));
+    v[1] = Add(a1, I(b1));
+    v[4] = Sub(a1, I(b1));
+    v[2] = Add(a2, I(b2));
+    v[3] = Sub(a2, I(b2));
+  }
 }
 
-// Stockham autosort over `groups` transforms of length n held at
-// buf0 + g * n (ping-pong with buf1 + g * n); `sign` +1 synthesis, -1
-// analysis. Returns 0 when the result is in buf0, 1 in buf1.
+// One Stockham stage of radix R over one ring, by one warp: butterfly idx
+// takes in[idx + q m] (q < R), twiddled by e^{sign 2 pi i q k stride / n}
+// (k = idx mod Ns; the exponent stays below n), and writes
+// out[(idx / Ns) Ns R + k + u Ns].
+template <class T2, int R>
+__device__ inline void WarpStage(const T2* in, T2* out, int n, int Ns, const T2* tw, int sign, int lane) {
+  const int m = n / R;
+  const int stride = n / (Ns * R);
+  for (int idx = lane; idx < m; idx += kWarp) {
+    const int blk = idx / Ns, k = idx - blk * Ns;
+    T2 v[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = in[idx + q * m];
+    if (k > 0) {
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        T2 w = tw[q * k * stride];
+        if (sign < 0) w.y = -w.y;
+        v[q] = Mul(v[q], w);
+      }
+    }
+    Butterfly<T2, R>(v, sign);
+    const int base = blk * Ns * R + k;
+#pragma unroll
+    for (int u = 0; u < R; ++u) out[base + u * Ns] = v[u];
+  }
+}
+
+// The whole transform of one ring by one warp, ping-ponging between a and b;
+// returns 0 when the result is in a, 1 in b (the same for every ring).
 template <class T2>
-__device__ int StockhamFft(T2* buf0, T2* buf1, int groups, const FftPlan& plan, const T2* tw, int sign) {
-  const int n = plan.n;
-  T2* src = buf0;
-  T2* dst = buf1;
+__device__ int WarpFft(T2* a, T2* b, const FftPlan& plan, const T2* tw, int sign, int lane) {
+  T2* src = a;
+  T2* dst = b;
   int Ns = 1;
   for (int s = 0; s < plan.stages; ++s) {
     const int r = plan.radix[s];
-    const int m = n / r;
-    const int stride = n / (Ns * r);
-    for (int t = threadIdx.x; t < groups * m; t += blockDim.x) {
-      const int g = t / m, idx = t % m;
-      const T2* in = src + g * n;
-      T2* out = dst + g * n;
-      const int k = idx % Ns;
-      T2 v[5];
-      for (int q = 0; q < r; ++q) {
-        v[q] = in[idx + q * m];
-        if (q > 0 && k > 0) v[q] = Mul(v[q], Twiddle(tw, q * k * stride, n, sign));
-      }
-      const int base = (idx / Ns) * Ns * r + k;
-      if (r == 2) {
-        out[base] = Add(v[0], v[1]);
-        out[base + Ns] = Sub(v[0], v[1]);
-      } else if (r == 4) {
-        const T2 a0 = Add(v[0], v[2]), a1 = Sub(v[0], v[2]);
-        const T2 b0 = Add(v[1], v[3]), b1 = Sub(v[1], v[3]);
-        const T2 ib1 = sign > 0 ? Make<T2>(-b1.y, b1.x) : Make<T2>(b1.y, -b1.x);
-        out[base] = Add(a0, b0);
-        out[base + Ns] = Add(a1, ib1);
-        out[base + 2 * Ns] = Sub(a0, b0);
-        out[base + 3 * Ns] = Sub(a1, ib1);
-      } else {
-        for (int u = 0; u < r; ++u) {
-          T2 y = v[0];
-          for (int q = 1; q < r; ++q) y = Add(y, Mul(v[q], Twiddle(tw, ((q * u) % r) * (n / r), n, sign)));
-          out[base + u * Ns] = y;
-        }
-      }
-    }
-    __syncthreads();
-    T2* swap = src;
+    if (r == 4)
+      WarpStage<T2, 4>(src, dst, plan.n, Ns, tw, sign, lane);
+    else if (r == 2)
+      WarpStage<T2, 2>(src, dst, plan.n, Ns, tw, sign, lane);
+    else if (r == 3)
+      WarpStage<T2, 3>(src, dst, plan.n, Ns, tw, sign, lane);
+    else
+      WarpStage<T2, 5>(src, dst, plan.n, Ns, tw, sign, lane);
+    __syncwarp();
+    T2* t = src;
     src = dst;
-    dst = swap;
+    dst = t;
     Ns *= r;
   }
-  return src == buf0 ? 0 : 1;
+  return src == a ? 0 : 1;
 }
-
-constexpr int kRingGroup = 4;  // rings (fields at one colatitude) per CTA
 
 // Ring modes: spectra -> fields; fields (times an optional weight) ->
 // spectra; spectra -> fields -> weight -> spectra without leaving shared
 // memory.
 enum RingMode { kRingSynth = 0, kRingAnalyse = 1, kRingWeighted = 2 };
 
-
+// Rings per CTA (one warp each) so that a CTA's shared memory (the twiddles
+// and two buffers a ring) stays near 100 KB: two CTAs per SM.
 template <class T2>
-__device__ void LoadSpectrum(T2* buf, int n, int groups, int lmax, int ntheta, int count, int j, int p0, bool real,
-                             const T2* spectra) {
-  for (int e = threadIdx.x; e < groups * n; e += blockDim.x) buf[e] = Make<T2>(0, 0);
-  __syncthreads();
-  const int mcount = real ? lmax + 1 : 2 * lmax + 1;
-  for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
-    const int g = e % groups, mi = e / groups;
-    const int m = real ? mi : mi - lmax;
-    const T2 v = spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
-    if (real) {
-      if (m == 0) {
-        buf[g * n] = Make<T2>(v.x, 0);
-      } else {
-        buf[g * n + m] = v;
-        buf[g * n + n - m] = Make<T2>(v.x, -v.y);
-      }
-    } else {
-      buf[g * n + ((m % n) + n) % n] = v;
-    }
-  }
-  __syncthreads();
+int RingsPerCta(int n) {
+  const long long budget = 100 * 1024;
+  const long long ring = 2LL * n * sizeof(T2);
+  const long long g = (budget - static_cast<long long>(n) * sizeof(T2)) / ring;
+  return static_cast<int>(std::max(1LL, std::min(8LL, g)));
 }
 
 template <class T2>
-__device__ void StoreSpectrum(const T2* res, int n, int groups, int lmax, int ntheta, int count, int j, int p0,
-                              bool real, typename Real<T2>::type scale, T2* spectra) {
-  const int mcount = real ? lmax + 1 : 2 * lmax + 1;
-  for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
-    const int g = e % groups, mi = e / groups;
-    const int m = real ? mi : mi - lmax;
-    const T2 v = res[g * n + ((m % n) + n) % n];
-    spectra[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
-  }
+size_t RingSmem(int n, int rings) {
+  return (static_cast<size_t>(n) + 2ULL * rings * n) * sizeof(T2);
 }
 
+// One CTA per (colatitude j, group of G consecutive fields p0..p0+G-1), one
+// warp per ring. The spectra [m][j][p] are read and written by the whole CTA
+// with the G fields of an order adjacent; the transforms run warp-synchronous.
 template <class T2>
-__global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan, const T2* tw,
+__global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan, const T2* twGlobal,
                            const double* weights, const T2* spectraIn, const void* fieldsIn,
                            const typename Real<T2>::type* pointWeight, void* fieldsOut, T2* spectraOut) {
   using T = typename Real<T2>::type;
   extern __shared__ __align__(16) unsigned char ringSmem[];
-  T2* smem = reinterpret_cast<T2*>(ringSmem);
   const int n = plan.n;
-  T2* buf0 = smem;
-  T2* buf1 = smem + kRingGroup * n;
+  const int G = blockDim.x / kWarp;
+  const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  T2* tw = reinterpret_cast<T2*>(ringSmem);
+  T2* bufs = tw + n;
   const int j = blockIdx.y;
-  const int p0 = blockIdx.x * kRingGroup;
-  const int groups = min(kRingGroup, count - p0);
-  T2* res = buf0;
+  const int p0 = blockIdx.x * G;
+  const int groups = min(G, count - p0);
+  const int mcount = real ? lmax + 1 : 2 * lmax + 1;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = twGlobal[e];
+  T2* a = bufs + 2LL * warp * n;  // this warp's ring
+  T2* b = a + n;
+  int at = 0;  // which of a, b holds the ring's current values
   if (mode == kRingSynth || mode == kRingWeighted) {
-    LoadSpectrum(buf0, n, groups, lmax, ntheta, count, j, p0, real, spectraIn);
-    res = StockhamFft(buf0, buf1, groups, plan, tw, +1) == 0 ? buf0 : buf1;
-    if (mode == kRingSynth) {
-      for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
-        const int g = e / n, k = e % n;
-        const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
-        if (real)
-          static_cast<T*>(fieldsOut)[at] = res[e].x;
-        else
-          static_cast<T2*>(fieldsOut)[at] = res[e];
+    for (int e = threadIdx.x; e < G * n; e += blockDim.x) bufs[2LL * (e / n) * n + e % n] = Make<T2>(0, 0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
+      const int g = e % groups, mi = e / groups;
+      const int m = real ? mi : mi - lmax;
+      const T2 v = spectraIn[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
+      T2* ring = bufs + 2LL * g * n;
+      if (real) {
+        if (m == 0) {
+          ring[0] = Make<T2>(v.x, 0);
+        } else {
+          ring[m] = v;
+          ring[n - m] = Make<T2>(v.x, -v.y);
+        }
+      } else {
+        ring[m < 0 ? m + n : m] = v;
       }
-      return;
-    }
-    // the pointwise weight on the synthesised values (a real field's
-    // imaginary part is dropped, as its synthesis does)
-    for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
-      const int g = e / n, k = e % n;
-      const T w = pointWeight[(static_cast<long long>(p0 + g) * ntheta + j) * n + k];
-      const T2 v = res[e];
-      res[e] = real ? Make<T2>(v.x * w, 0) : Make<T2>(v.x * w, v.y * w);
     }
     __syncthreads();
+    if (warp < groups) {
+      at = WarpFft(a, b, plan, tw, +1, lane);
+      T2* res = at ? b : a;
+      const long long row = (static_cast<long long>(p0 + warp) * ntheta + j) * n;
+      if (mode == kRingSynth) {
+        for (int k = lane; k < n; k += kWarp) {
+          if (real)
+            static_cast<T*>(fieldsOut)[row + k] = res[k].x;
+          else
+            static_cast<T2*>(fieldsOut)[row + k] = res[k];
+        }
+      } else {
+        // the pointwise weight on the synthesised values (a real field's
+        // imaginary part is dropped, as its synthesis does)
+        for (int k = lane; k < n; k += kWarp) {
+          const T w = pointWeight[row + k];
+          const T2 v = res[k];
+          res[k] = real ? Make<T2>(v.x * w, 0) : Make<T2>(v.x * w, v.y * w);
+        }
+        __syncwarp();
+      }
+    }
+    if (mode == kRingSynth) return;
   } else {
-    for (int e = threadIdx.x; e < groups * n; e += blockDim.x) {
-      const int g = e / n, k = e % n;
-      const long long at = (static_cast<long long>(p0 + g) * ntheta + j) * n + k;
-      T2 v = real ? Make<T2>(static_cast<const T*>(fieldsIn)[at], 0) : static_cast<const T2*>(fieldsIn)[at];
-      if (pointWeight != nullptr) {
-        const T w = pointWeight[at];
-        v = Make<T2>(v.x * w, v.y * w);
+    __syncthreads();  // the twiddles
+    if (warp < groups) {
+      const long long row = (static_cast<long long>(p0 + warp) * ntheta + j) * n;
+      for (int k = lane; k < n; k += kWarp) {
+        T2 v = real ? Make<T2>(static_cast<const T*>(fieldsIn)[row + k], 0) : static_cast<const T2*>(fieldsIn)[row + k];
+        if (pointWeight != nullptr) {
+          const T w = pointWeight[row + k];
+          v = Make<T2>(v.x * w, v.y * w);
+        }
+        a[k] = v;
       }
-      buf0[e] = v;
+      __syncwarp();
     }
-    __syncthreads();
   }
-  T2* other = res == buf0 ? buf1 : buf0;
-  const T2* out = StockhamFft(res, other, groups, plan, tw, -1) == 0 ? res : other;
+  // the analysis transform from wherever the ring's values are; every ring
+  // has the same stage count, so the result's side is the same for all: a
+  // after two transforms, the stage parity's side after one
+  if (warp < groups) {
+    T2* x = at ? b : a;
+    T2* y = at ? a : b;
+    WarpFft(x, y, plan, tw, -1, lane);
+  }
+  const int out = mode == kRingWeighted ? 0 : plan.stages % 2;
+  __syncthreads();
   const T scale = static_cast<T>(2.0 * 3.14159265358979323846 / n * weights[j]);
-  StoreSpectrum(out, n, groups, lmax, ntheta, count, j, p0, real, scale, spectraOut);
+  for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
+    const int g = e % groups, mi = e / groups;
+    const int m = real ? mi : mi - lmax;
+    const T2 v = bufs[2LL * g * n + (out ? n : 0) + (m < 0 ? m + n : m)];
+    spectraOut[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
+  }
 }
 
 __global__ void CastKernel(const double* in, long long n, float* out) {
@@ -630,10 +687,11 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
                const void* fieldsIn, const double* weight, void* fieldsOut, double* spectraOut,
                cudaStream_t stream) {
   if (count == 0) return SL3DGPU_OK;
-  const size_t smem = 2 * kRingGroup * static_cast<size_t>(g.nphi) * sizeof(double2);
+  const int rings = RingsPerCta<double2>(g.nphi);
+  const size_t smem = RingSmem<double2>(g.nphi, rings);
   SL3D_CUDA(cudaFuncSetAttribute(RingKernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
-  dim3 grid((count + kRingGroup - 1) / kRingGroup, g.ntheta);
+  dim3 grid((count + rings - 1) / rings, g.ntheta);
   // algorithmic traffic: the spectra and the grid values the mode reads and writes
   const double spec = static_cast<double>(real ? g.lmax + 1 : 2 * g.lmax + 1) * g.ntheta * count * 16.0;
   const double field = static_cast<double>(g.ntheta) * g.nphi * count * (real ? 8.0 : 16.0);
@@ -641,7 +699,7 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   const double bytes = mode == kRingWeighted ? 2 * spec + wbytes : spec + field + wbytes;
   const double ffts = static_cast<double>(g.ntheta) * count * (mode == kRingWeighted ? 2 : 1);
   prof::Scope scope(prof::kRing, stream, ffts * 5.0 * g.nphi * std::log2(static_cast<double>(g.nphi)), bytes);
-  RingKernel<double2><<<grid, 256, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
+  RingKernel<double2><<<grid, rings * kWarp, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
                                           g.dWeights, reinterpret_cast<const double2*>(spectraIn),
                                           fieldsIn, weight, fieldsOut,
                                           reinterpret_cast<double2*>(spectraOut));
@@ -727,15 +785,16 @@ int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const floa
   if (count == 0) return SL3DGPU_OK;
   const SpinTable* t = nullptr;
   if (int st = Table32(0, &t); st != SL3DGPU_OK) return st;  // makes the FP32 twiddles
-  const size_t smem = 2 * kRingGroup * static_cast<size_t>(nphi) * sizeof(float2);
+  const int rings = RingsPerCta<float2>(nphi);
+  const size_t smem = RingSmem<float2>(nphi, rings);
   SL3D_CUDA(cudaFuncSetAttribute(RingKernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(smem)));
-  dim3 grid((count + kRingGroup - 1) / kRingGroup, ntheta);
+  dim3 grid((count + rings - 1) / rings, ntheta);
   const double spec = static_cast<double>(real ? lmax + 1 : 2 * lmax + 1) * ntheta * count * 8.0;
   const double wbytes = static_cast<double>(ntheta) * nphi * count * 4.0;
   prof::Scope scope(prof::kRing32, stream, 2.0 * ntheta * count * 5.0 * nphi * std::log2(static_cast<double>(nphi)),
                     2 * spec + wbytes);
-  RingKernel<float2><<<grid, 256, smem, stream>>>(kRingWeighted, lmax, ntheta, count, real, plan, dTwiddle32,
+  RingKernel<float2><<<grid, rings * kWarp, smem, stream>>>(kRingWeighted, lmax, ntheta, count, real, plan, dTwiddle32,
                                                   dWeights, reinterpret_cast<const float2*>(spectraIn), nullptr,
                                                   weight, nullptr, reinterpret_cast<float2*>(spectraOut));
   SL3D_CHECK_LAUNCH();

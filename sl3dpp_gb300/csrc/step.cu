@@ -172,6 +172,7 @@ class Viscoelastic3DGpu {
   std::vector<Dev<double>> dG, dF;
   Dev<double*> dGPtr, dFPtr;
   static constexpr int kMixBlocks = 1024;
+  static constexpr int kMixBlocks32 = 4096;  // FP32 sums: about a hundred products a thread
 
   // the mixed form's FP32 correction: iterate, next iterate, residual,
   // analysed force, right-hand sides, spectra, weight and its own mixer
@@ -216,7 +217,7 @@ class Viscoelastic3DGpu {
   int Pass32(const Flavour& f, const float2* e, float2* next);
   int Mixer32Reset();
   int Mixer32Update(int& count, int& slot, bool& first);
-  int Correct(const Flavour& f, sl3dgpu_step_info& info);
+  int Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info);
   int Converge(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
   int ConvergeMixed(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
   int ElasticStrain(const V3dState& st, const double2* sigma);
@@ -397,7 +398,7 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   SL3D_CUDA(changePartial.Alloc(3 * kChangeBlocks));
   SL3D_CUDA(changeResult.Alloc(3));
   SL3D_CUDA(gammaOut.Alloc(16));
-  SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks) * 16));
+  SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks32) * 16));
   if (options.precision == 1) {
     for (auto* b : {&e32, &eNext32, &r32, &analysed32}) SL3D_CUDA(b->Alloc(spectralComplex));
     SL3D_CUDA(rhsSph32.Alloc(rhsSphComplex));
@@ -1021,7 +1022,10 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
     LaunchResidual32(2 * spectralComplex, reinterpret_cast<const double*>(sNext.p),
                      reinterpret_cast<const double*>(s.p), reinterpret_cast<float*>(r32.p), stream);
     SL3D_CHECK_LAUNCH();
-    SL3D_TRY(Correct(f, info));
+    // The correction needs only the accuracy that brings the next FP64
+    // residual under rtol: r' is about (its relative change) x (residual),
+    // with a factor 10 to spare, and never finer than correction_rtol.
+    SL3D_TRY(Correct(f, std::max(options.correction_rtol, std::min(0.1, 0.1 * options.rtol / residual)), info));
     LaunchAddCorrection(2 * spectralComplex, reinterpret_cast<const float*>(e32.p), reinterpret_cast<double*>(s.p),
                         stream);
     SL3D_CHECK_LAUNCH();
@@ -1109,7 +1113,7 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
   a.dG = dG32Ptr.p;
   a.dF = dF32Ptr.p;
   a.partial = mixPartial.p;
-  a.blocks = static_cast<int>(std::min<long long>(kMixBlocks, a.n));
+  a.blocks = static_cast<int>(std::min<long long>(kMixBlocks32, a.n));
   a.gram = gram.p;
   a.gamma = gammaOut.p;
   if (first) {
@@ -1128,8 +1132,8 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
 }
 
 // e = B e + r from e = r, with the FP64 loop's Anderson schedule, until the
-// relative change is at most correction_rtol (or max_iterations passes).
-int Viscoelastic3DGpu::Correct(const Flavour& f, sl3dgpu_step_info& info) {
+// relative change is at most the tolerance (or max_iterations passes).
+int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info) {
   SL3D_CUDA(cudaMemcpyAsync(e32.p, r32.p, spectralComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
   const bool adaptive = options.anderson_rate > 0.0;
   bool mixing = options.anderson_memory > 0 && !adaptive;
@@ -1151,7 +1155,7 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, sl3dgpu_step_info& info) {
     }
     const double change = hostResult[0] > 0.0 ? std::sqrt(hostResult[1]) / std::sqrt(hostResult[0]) : 0.0;
     correctionHistory.push_back(change);
-    if (change <= options.correction_rtol) {
+    if (change <= tolerance) {
       std::swap(e32, eNext32);
       break;
     }

@@ -392,22 +392,25 @@ __global__ void CombineKernel(long long values, long long fieldSize, const doubl
 
 // -- the convergence measure ------------------------------------------------------------------
 
+// Per block: max |next|^2, max |next - now|^2 and finiteness, in the data's
+// precision (a maximum of squares loses nothing to the order).
 template <class T2>
 __global__ void RelativeChangeKernel(const T2* next, const T2* now, long long n, double* partial) {
+  using T = typename Scalar<T2>::type;
   __shared__ double s0[256], s1[256], s2[256];
-  double scale = 0.0, diff = 0.0, finite = 1.0;
+  T scale = 0, diff = 0;
+  bool finite = true;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
     const T2 a = next[i], b = now[i];
-    const double ax = a.x, ay = a.y;
-    if (!(ax - ax == 0.0) || !(ay - ay == 0.0)) finite = 0.0;
-    scale = fmax(scale, ax * ax + ay * ay);
-    const double dx = ax - static_cast<double>(b.x), dy = ay - static_cast<double>(b.y);
+    finite = finite && (a.x - a.x == T(0)) && (a.y - a.y == T(0));
+    scale = fmax(scale, a.x * a.x + a.y * a.y);
+    const T dx = a.x - b.x, dy = a.y - b.y;
     diff = fmax(diff, dx * dx + dy * dy);
   }
-  s0[threadIdx.x] = scale;
-  s1[threadIdx.x] = diff;
-  s2[threadIdx.x] = finite;
+  s0[threadIdx.x] = static_cast<double>(scale);
+  s1[threadIdx.x] = static_cast<double>(diff);
+  s2[threadIdx.x] = finite ? 1.0 : 0.0;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w /= 2) {
     if (threadIdx.x < w) {
@@ -466,17 +469,33 @@ __global__ void MixerFirstKernel(long long n, T* x, const T* gx, T* xPrev, T* fP
 constexpr int kMixThreads = 256;
 constexpr int kMaxMemory = 8;
 
+// The accumulation type of the mixer's per-thread sums: FP64 for the FP64
+// form, FP32 for the correction (a thread sums about a hundred products; the
+// warp and block sums and the Gram solve are FP64 in both).
+template <class T>
+struct MixAcc {
+  using type = double;
+};
+template <>
+struct MixAcc<float> {
+  using type = float;
+};
+
 // One block per fixed chunk of the vector (fixed by n alone): the new
 // differences, the stored iterate and residual, and the block's partial Gram
-// column and right-hand side (FP64), summed in a fixed tree order.
+// column and right-hand side, summed in a fixed order (thread, warp
+// shuffle tree, warps in turn).
 template <class T>
 __global__ void MixerSweepKernel(MixerArgsT<T> a) {
-  __shared__ double red[kMixThreads][2 * kMaxMemory];
+  using A = typename MixAcc<T>::type;
+  __shared__ double red[kMixThreads / 32][2 * kMaxMemory];
   const long long begin = a.n * blockIdx.x / a.blocks, end = a.n * (blockIdx.x + 1) / a.blocks;
-  double col[kMaxMemory], gam[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) col[i] = gam[i] = 0.0;
+  A col[kMaxMemory], gam[kMaxMemory];
+  for (int i = 0; i < kMaxMemory; ++i) col[i] = gam[i] = A(0);
   T* dFs = a.dF[a.slot];
   T* dGs = a.dG[a.slot];
+  const T* dF[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) dF[i] = a.dF[i];
   for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
     const T xs = a.x[at], gs = a.gx[at];
     const T f = gs - xs;
@@ -487,29 +506,32 @@ __global__ void MixerSweepKernel(MixerArgsT<T> a) {
     a.xPrev[at] = xs;
     a.fPrev[at] = f;
     for (int i = 0; i < a.m; ++i) {
-      const double di = i == a.slot ? static_cast<double>(df) : static_cast<double>(a.dF[i][at]);
-      col[i] += di * static_cast<double>(df);
-      gam[i] += di * static_cast<double>(f);
+      const A di = i == a.slot ? static_cast<A>(df) : static_cast<A>(dF[i][at]);
+      col[i] += di * static_cast<A>(df);
+      gam[i] += di * static_cast<A>(f);
     }
   }
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   for (int i = 0; i < a.m; ++i) {
-    red[threadIdx.x][i] = col[i];
-    red[threadIdx.x][kMaxMemory + i] = gam[i];
+    A c = col[i], g = gam[i];
+    for (int off = 16; off > 0; off /= 2) {
+      c += __shfl_down_sync(0xffffffffu, c, off);
+      g += __shfl_down_sync(0xffffffffu, g, off);
+    }
+    if (lane == 0) {
+      red[warp][i] = static_cast<double>(c);
+      red[warp][kMaxMemory + i] = static_cast<double>(g);
+    }
   }
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w /= 2) {
-    if (threadIdx.x < w)
-      for (int i = 0; i < a.m; ++i) {
-        red[threadIdx.x][i] += red[threadIdx.x + w][i];
-        red[threadIdx.x][kMaxMemory + i] += red[threadIdx.x + w][kMaxMemory + i];
-      }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0)
-    for (int i = 0; i < a.m; ++i) {
-      a.partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + i] = red[0][i];
-      a.partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + kMaxMemory + i] = red[0][kMaxMemory + i];
+  if (threadIdx.x < 2 * kMaxMemory) {
+    const int i = threadIdx.x;
+    if (i % kMaxMemory < a.m) {
+      double v = 0.0;
+      for (int w = 0; w < kMixThreads / 32; ++w) v += red[w][i];
+      a.partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + i] = v;
     }
+  }
 }
 
 // The partials in a fixed order (one warp per sum, lanes over the blocks,
@@ -547,14 +569,19 @@ __global__ void MixerSolveKernel(int m, int slot, int memory, int blocks, const 
 
 template <class T>
 __global__ void MixerMixKernel(MixerArgsT<T> a) {
+  using A = typename MixAcc<T>::type;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   const bool ok = a.gamma[a.m] != 0.0;
-  double g[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) g[i] = a.gamma[i];
+  A g[kMaxMemory];
+  const T* dG[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) {
+    g[i] = static_cast<A>(a.gamma[i]);
+    dG[i] = a.dG[i];
+  }
   for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < a.n; at += stride) {
-    double value = a.gx[at];
+    A value = a.gx[at];
     if (ok)
-      for (int i = 0; i < a.m; ++i) value -= g[i] * static_cast<double>(a.dG[i][at]);
+      for (int i = 0; i < a.m; ++i) value -= g[i] * static_cast<A>(dG[i][at]);
     a.x[at] = static_cast<T>(value);
   }
 }

@@ -130,7 +130,7 @@ def test_oracle_lu_reports_the_zero_pivot():
 # -- the GPU kernels ----------------------------------------------------------------------
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,kd,nrhs,seed", CHOLESKY_CASES + [(1803, 17, 514, 11)])
+@pytest.mark.parametrize("n,kd,nrhs,seed", CHOLESKY_CASES + [(1803, 17, 514, 11), (300, 17, 65, 13)])
 def test_gpu_cholesky_matches_oracle_and_lapack(gpu, n, kd, nrhs, seed):
     from sl3dpp_gb300.band import BandCholeskyFactor, BandCholeskySolve
 
@@ -153,7 +153,7 @@ def test_gpu_cholesky_matches_oracle_and_lapack(gpu, n, kd, nrhs, seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,kl,ku,nrhs,seed", LU_CASES + [(1803, 17, 17, 66, 12)])
+@pytest.mark.parametrize("n,kl,ku,nrhs,seed", LU_CASES + [(1803, 17, 17, 66, 12), (150, 5, 7, 129, 14)])
 def test_gpu_lu_matches_oracle_and_lapack(gpu, n, kl, ku, nrhs, seed):
     from sl3dpp_gb300.band import BandLuFactor, BandLuSolve
 
