@@ -142,6 +142,9 @@ typedef struct sl3dgpu_v3d_options {
   double anderson_rate;  /* 0.5 */
   int precision;         /* 0: FP64 throughout; 1: mixed (see sl3dgpu_v3d_create) */
   double correction_rtol; /* mixed form: the finest relative change an FP32 correction iterates to, 1e-5 */
+  int solver;             /* Options::StepSolver: 0 the fixed point, 1 conjugate gradients */
+  double solve_rtol;      /* conjugate gradients: relative residual (preconditioned energy norm), 1e-11 */
+  int solve_max_iterations; /* conjugate gradients: iteration budget, 200 */
 } sl3dgpu_v3d_options;
 
 /* Viscoelastic3D::StepInfo (Viscoelastic3D.hpp:357-375). */
@@ -151,6 +154,7 @@ typedef struct sl3dgpu_step_info {
   int converged;
   int mixed_passes;
   int correction_passes; /* mixed form: FP32 correction passes (not counted in iterations) */
+  int solve_iterations;  /* conjugate gradients: iterations (StepInfo::solveIterations) */
 } sl3dgpu_step_info;
 
 /* The configurations' Earth (radius 6371 km, fluid core to 3480 km, linear

@@ -332,6 +332,7 @@ struct Info {
   double residual = 0.0;
   bool converged = false;
   int mixedPasses = 0;
+  int solveIterations = 0;
 };
 
 // -- the Anderson mixer (AndersonMixer.hpp:65-219) ----------------------------------------------
@@ -742,6 +743,145 @@ class Viscoelastic3D {
     return reference_.pointItau[k][static_cast<std::size_t>(nd.element) * reference_.points.count + nd.q];
   }
 
+  // LateralPair (detail/LateralSolve.hpp:80-101): the m >= 0 columns of
+  // every degree, m > 0 weighted twice, Re(a conj b) summed.
+  static double Pair(const Solutions& a, const Solutions& b) {
+    double total = 0.0;
+    auto pair = [&](const std::vector<std::vector<C>>& x, const std::vector<std::vector<C>>& y) {
+      for (std::size_t l = 0; l < x.size() && l < y.size(); ++l) {
+        if (x[l].empty() || y[l].empty()) continue;
+        const std::size_t ndof = x[l].size() / (l + 1);
+        for (std::size_t m = 0; m <= l; ++m) {
+          const double w = m == 0 ? 1.0 : 2.0;
+          for (std::size_t d = 0; d < ndof; ++d)
+            total += w * (x[l][m * ndof + d] * std::conj(y[l][m * ndof + d])).real();
+        }
+      }
+    };
+    pair(a.sph, b.sph);
+    pair(a.tor, b.tor);
+    return total;
+  }
+
+  // y = K x - y per degree (ApplyLateralOperator, Viscoelastic3D.cpp:626-728):
+  // the complex columns as real pairs through the assembled bands.
+  void KxMinus(const Solutions& x, const Flavour& f, Solutions& y) const {
+    const int L = options_.lmax;
+#pragma omp parallel for schedule(dynamic)
+    for (int t = 0; t < 2 * L + 1; ++t) {
+      const bool tor = t > L;
+      const int l = tor ? t - L : t;
+      const auto& xl = tor ? x.tor[l] : x.sph[l];
+      auto& yl = tor ? y.tor[l] : y.sph[l];
+      if (xl.empty()) continue;
+      const int cols = l + 1;
+      const int ndof = static_cast<int>(xl.size()) / cols;
+      std::vector<double> real(static_cast<std::size_t>(ndof) * 2 * cols);
+      for (int c = 0; c < cols; ++c)
+        for (int d = 0; d < ndof; ++d) {
+          real[static_cast<std::size_t>(c) * ndof + d] = xl[static_cast<std::size_t>(c) * ndof + d].real();
+          real[static_cast<std::size_t>(cols + c) * ndof + d] = xl[static_cast<std::size_t>(c) * ndof + d].imag();
+        }
+      const auto k = tor ? f.tor[l]->Apply(real, 2 * cols) : f.sph[l]->Apply(real, 2 * cols);
+      for (int c = 0; c < cols; ++c)
+        for (int d = 0; d < ndof; ++d) {
+          const std::size_t at = static_cast<std::size_t>(c) * ndof + d;
+          yl[at] = C(k[at], k[static_cast<std::size_t>(cols + c) * ndof + d]) - yl[at];
+        }
+    }
+  }
+
+  static void Axpy(Solutions& y, double a, const Solutions& x) {
+    for (int kind = 0; kind < 2; ++kind) {
+      auto& Y = kind ? y.tor : y.sph;
+      const auto& X = kind ? x.tor : x.sph;
+      for (std::size_t l = 0; l < Y.size(); ++l)
+        for (std::size_t i = 0; i < Y[l].size(); ++i) Y[l][i] += a * X[l][i];
+    }
+  }
+
+  // The step closed by preconditioned conjugate gradients (Viscoelastic3D.cpp
+  // :2008-2015 through OpenStep::Forces/Solve, LateralConjugateGradients at
+  // detail/LateralSolve.hpp:112-181 with reduction 0 and no start): the
+  // reference solve as the preconditioner, K x minus the lateral force as
+  // the operator.
+  Solutions ConjugateGradients(const Spectral& fixedS, const Flavour& flavour, const std::vector<double>& weight,
+                               const C* load, bool lateral, Info& info) {
+    const int L = options_.lmax;
+    Solutions f;
+    Forces(fixedS, flavour, f.sph, f.tor);
+    if (load != nullptr)
+      for (int l = 0; l <= L; ++l) {
+        const auto vec = flavour.sph[l]->Load();
+        const int ndof = flavour.sph[l]->DofCount();
+        for (int m = 0; m <= l; ++m) {
+          const C a = load[OGrid::Index(l, m)];
+          if (a == C{}) continue;
+          for (int d = 0; d < ndof; ++d) f.sph[l][static_cast<std::size_t>(m) * ndof + d] += a * vec[d];
+        }
+      }
+    Tensor grid = ZeroTensor();
+    Spectral analysed = ZeroSpectral();
+    auto apply = [&](const Solutions& x) {
+      Spectral e = StrainOf(x, flavour);
+      Synthesise(e, grid);
+      for (std::size_t i = 0; i < weight.size(); ++i) {
+        grid.c0[i] *= weight[i];
+        grid.c1[i] *= weight[i];
+        grid.r[i] *= weight[i];
+      }
+      Analyse(grid, analysed);
+      Solutions y;
+      Forces(analysed, flavour, y.sph, y.tor);
+      KxMinus(x, flavour, y);
+      return y;
+    };
+    auto solve = [&](const Solutions& b) { return SolveForces(b.sph, b.tor, flavour); };
+    Solutions x = solve(f);
+    const double energy = Pair(x, f);
+    auto relative = [&](double v) { return energy > 0.0 ? std::sqrt(std::abs(v) / energy) : std::sqrt(std::abs(v)); };
+    info = Info{};
+    if (!lateral) {
+      info.converged = true;
+      info.residual = 0.0;
+      history_.push_back(0.0);
+      return x;
+    }
+    Solutions r = apply(x);
+    Axpy(r, -1.0, f);
+    Axpy(r, -2.0, r);  // r = f - A x
+    Solutions z = solve(r);
+    double rz = Pair(z, r);
+    info.residual = relative(rz);
+    history_.push_back(info.residual);
+    const double target = options_.solve_rtol;
+    Solutions p = z;
+    for (int iteration = 0; iteration < options_.solve_max_iterations; ++iteration) {
+      if (info.residual <= target) break;
+      const Solutions ap = apply(p);
+      const double curvature = Pair(p, ap);
+      const double alpha = rz / curvature;
+      Axpy(x, alpha, p);
+      Axpy(r, -alpha, ap);
+      z = solve(r);
+      const double next = Pair(z, r);
+      const double beta = next / rz;
+      rz = next;
+      for (int kind = 0; kind < 2; ++kind) {
+        auto& P = kind ? p.tor : p.sph;
+        const auto& Z = kind ? z.tor : z.sph;
+        for (std::size_t l = 0; l < P.size(); ++l)
+          for (std::size_t i = 0; i < P[l].size(); ++i) P[l][i] = Z[l][i] + beta * P[l][i];
+      }
+      info.solveIterations = iteration + 1;
+      info.residual = relative(rz);
+      history_.push_back(info.residual);
+    }
+    info.converged = info.residual <= target;
+    info.iterations = info.solveIterations;
+    return x;
+  }
+
   // One stage: StartStep, Converge(Respond + AddChannels + StrainOf), Finish.
   // With `samplePasses` >= 0: the bounded timing sample of a stage -- the
   // start (StartStep) and exactly that many passes, timed into tStart and
@@ -815,6 +955,16 @@ class Viscoelastic3D {
     }
     Spectral fixedS = ZeroSpectral();
     Analyse(fixed, fixedS);
+    Spectral s;
+    Solutions solutions;
+    if (options_.solver == 1 && samplePasses < 0) {
+      // the reference iterates whether or not the weight vanishes
+      // (OpenStep::Solve passes lateral = true)
+      solutions = ConjugateGradients(fixedS, flavour, weight, loadEnd, true, info);
+      s = StrainOf(solutions, flavour);
+    } else {
+      s = s0;
+    }
     // Respond: synthesise, weight, analyse, add the fixed force, solve.
     Tensor grid = ZeroTensor();
     Spectral analysed = ZeroSpectral();
@@ -832,7 +982,6 @@ class Viscoelastic3D {
       return SolveAll(analysed, flavour);
     };
     // The load channel at the stage's end time.
-    Solutions solutions;
     auto pass = [&](const Spectral& s) {
       solutions = respond(s);
       AddLoad(solutions, flavour, loadEnd);
@@ -852,7 +1001,7 @@ class Viscoelastic3D {
       return state;
     }
     // Converge (Viscoelastic3D.cpp:1916-1974).
-    Spectral s = s0;
+    if (options_.solver != 1) {
     info = Info{};
     const bool adaptive = options_.anderson_rate > 0.0;
     std::optional<Mixer> mixer;
@@ -891,6 +1040,7 @@ class Viscoelastic3D {
       } else {
         s = std::move(next);
       }
+    }
     }
     // Finish: synthesise the strain and advance the memory.
     State out;
@@ -954,6 +1104,7 @@ class Viscoelastic3D {
     out.t = state.t + dt;
     info.iterations = i1.iterations + i2.iterations;
     info.mixedPasses = i1.mixedPasses + i2.mixedPasses;
+    info.solveIterations = i1.solveIterations + i2.solveIterations;
     info.residual = i2.residual;
     info.converged = i1.converged && i2.converged;
     return out;
@@ -1065,6 +1216,7 @@ int oracle_v3d_step(oracle_v3d* h, oracle_state* state, double dt, int scheme, c
     info->converged = i.converged ? 1 : 0;
     info->mixed_passes = i.mixedPasses;
     info->correction_passes = 0;
+    info->solve_iterations = i.solveIterations;
   }
   return 0;
 }

@@ -240,6 +240,7 @@ class ToroidalOperator {
   int Dof(int node) const { return dof_[node]; }
   int SurfaceDof() const;
   const std::vector<int>& Pinned() const { return pinned_; }
+  const std::vector<double>& Band() const { return band_; }  // unscaled upper band
   const std::vector<double>& Scale() const { return scale_; }
   std::vector<double> ScaledCholeskyBand() const;  // pinned rows/cols the identity's
   std::vector<double> Apply(const std::vector<double>& x, int nrhs) const;

@@ -104,6 +104,11 @@ struct Flavour {
   double dt = 0.0;
   Dev<double> bands, scales, units;
   Dev<float> bands32, scales32;  // the mixed form's FP32 copies
+  // conjugate gradients: the assembled (unscaled) bands for K x, their
+  // systems, and the unsolved load force vectors (DegreeOperator::Load)
+  Dev<double> applyBands, loadForces;
+  Dev<sl3dgpu_band_system> dSphApply, dTorApply;
+  int nSphApply = 0, nTorApply = 0, maxApplyRows = 0;
   Dev<int> pivots;
   Dev<long long> unitOffset;
   std::vector<sl3dgpu_band_system> sphChol, sphLu, torChol;
@@ -184,6 +189,14 @@ class Viscoelastic3DGpu {
   Dev<float*> dG32Ptr, dF32Ptr;
   std::vector<double> correctionHistory;  // the last step's FP32 pass changes
 
+  // conjugate gradients (solver 1): forces, iterate, residual, preconditioned
+  // residual, direction and product, each the spheroidal then the toroidal
+  // right-hand sides; the pairing's chunks and partial sums
+  Dev<double2> cgF, cgX, cgR, cgZ, cgP, cgAp;
+  Dev<PairChunk> pairChunks;
+  int pairChunkCount = 0;
+  Dev<double> pairPartial, pairResult;
+
   V3dState scratch;  // the second buffer set a step writes into
   std::vector<double> history;  // the last step's pass residuals, stages in turn
 
@@ -218,6 +231,12 @@ class Viscoelastic3DGpu {
   int Mixer32Reset();
   int Mixer32Update(int& count, int& slot, bool& first);
   int Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info);
+  int SolveColumns(const Flavour& f, double2* sph, double2* tor);
+  int LateralForce(const double2* x, double2* out);
+  int ApplyOperator(const Flavour& f, const double2* x, double2* out);
+  int PairOf(const double2* a, const double2* b, double* out);
+  int ConvergeConjugateGradients(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
+  long long Columns() const { return rhsSphComplex + std::max<long long>(rhsTorComplex, 1); }
   int Converge(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
   int ConvergeMixed(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
   int ElasticStrain(const V3dState& st, const double2* sigma);
@@ -239,6 +258,14 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   }
   if (opt.precision != 0 && opt.precision != 1) {
     SetError("v3d: precision 0 (FP64) or 1 (mixed)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (opt.solver != 0 && opt.solver != 1) {
+    SetError("v3d: solver 0 (fixed point) or 1 (conjugate gradients)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (opt.solver == 1 && (opt.precision != 0 || !(opt.solve_rtol > 0.0) || opt.solve_max_iterations < 0)) {
+    SetError("v3d: conjugate gradients run in FP64 (precision 0) with solve_rtol > 0 and solve_max_iterations >= 0");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if (opt.precision == 1 && !(opt.correction_rtol > 0.0 && opt.correction_rtol < 1.0)) {
@@ -399,6 +426,32 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   SL3D_CUDA(changeResult.Alloc(3));
   SL3D_CUDA(gammaOut.Alloc(16));
   SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks32) * 16));
+  if (options.solver == 1) {
+    for (auto* b : {&cgF, &cgX, &cgR, &cgZ, &cgP, &cgAp}) {
+      SL3D_CUDA(b->Alloc(Columns()));
+      SL3D_CUDA(cudaMemsetAsync(b->p, 0, Columns() * sizeof(double2), stream));
+    }
+    // The pairing's chunks: every degree's spheroidal then toroidal block in
+    // spans of at most 16384 values.
+    std::vector<PairChunk> chunks;
+    auto add = [&](long long start, long long size, int cols) {
+      for (long long at = 0; at < size; at += 16384) {
+        PairChunk c{};
+        c.start = start + at;
+        c.end = start + std::min(size, at + 16384);
+        c.degreeStart = start;
+        c.cols = cols;
+        chunks.push_back(c);
+      }
+    };
+    for (int l = 0; l <= L; ++l) add(degrees[l].sphRhs, static_cast<long long>(degrees[l].sphNdof) * (l + 1), l + 1);
+    for (int l = 1; l <= L; ++l)
+      add(rhsSphComplex + degrees[l].torRhs, static_cast<long long>(degrees[l].torNdof) * (l + 1), l + 1);
+    pairChunkCount = static_cast<int>(chunks.size());
+    SL3D_CUDA(pairChunks.Upload(chunks));
+    SL3D_CUDA(pairPartial.Alloc(chunks.size()));
+    SL3D_CUDA(pairResult.Alloc(4));
+  }
   if (options.precision == 1) {
     for (auto* b : {&e32, &eNext32, &r32, &analysed32}) SL3D_CUDA(b->Alloc(spectralComplex));
     SL3D_CUDA(rhsSph32.Alloc(rhsSphComplex));
@@ -552,6 +605,34 @@ int Viscoelastic3DGpu::BuildFlavour(const host::PointShear& shear, Flavour& f) {
     cholDegree.push_back(l);
     cholKind.push_back(1);
   }
+  if (options.solver == 1 && &f != elastic.get()) {
+    // K x for conjugate gradients: the assembled upper bands, spheroidal
+    // degrees then toroidal, with their systems (right-hand sides in the
+    // combined spheroidal-then-toroidal columns).
+    std::vector<double> applyBands;
+    std::vector<sl3dgpu_band_system> sphApply, torApply;
+    int rows = 0;
+    for (int l = 0; l <= L; ++l) {
+      const auto& op = *sph[l];
+      sphApply.push_back(system(op.DofCount(), op.Bandwidth(), static_cast<long long>(applyBands.size()),
+                                2 * degrees[l].sphRhs, 2 * (l + 1), -1));
+      applyBands.insert(applyBands.end(), op.Band().begin(), op.Band().end());
+      rows = std::max(rows, op.DofCount());
+    }
+    for (int l = 1; l <= L; ++l) {
+      const auto& op = *tor[l];
+      torApply.push_back(system(op.DofCount(), op.Bandwidth(), static_cast<long long>(applyBands.size()),
+                                2 * (rhsSphComplex + degrees[l].torRhs), 2 * (l + 1), -1));
+      applyBands.insert(applyBands.end(), op.Band().begin(), op.Band().end());
+      rows = std::max(rows, op.DofCount());
+    }
+    SL3D_CUDA(f.applyBands.Upload(applyBands));
+    SL3D_CUDA(f.dSphApply.Upload(sphApply));
+    SL3D_CUDA(f.dTorApply.Upload(torApply));
+    f.nSphApply = static_cast<int>(sphApply.size());
+    f.nTorApply = static_cast<int>(torApply.size());
+    f.maxApplyRows = rows;
+  }
   // Factor the Cholesky candidates; the spheroidal failures fall back to LU.
   Dev<double> dBands;
   SL3D_CUDA(dBands.Upload(bands));
@@ -650,6 +731,7 @@ int Viscoelastic3DGpu::BuildFlavour(const host::PointShear& shear, Flavour& f) {
   }
   SL3D_CUDA(f.units.Upload(units));
   SL3D_CUDA(f.unitOffset.Upload(unitOffset));
+  if (options.solver == 1) SL3D_CUDA(f.loadForces.Upload(units));  // before the solve turns them into responses
   auto unitSystems = [&](const std::vector<sl3dgpu_band_system>& src) {
     std::vector<sl3dgpu_band_system> out;
     for (auto s : src) {
@@ -765,9 +847,11 @@ int Viscoelastic3DGpu::WeightedPass(const double2* strain, double2* out) {
 
 // -- a pass --------------------------------------------------------------------------------------------
 
-int Viscoelastic3DGpu::Solve(const Flavour& f) {
-  auto* sphD = reinterpret_cast<double*>(rhsSph.p);
-  auto* torD = reinterpret_cast<double*>(rhsTor.p);
+int Viscoelastic3DGpu::Solve(const Flavour& f) { return SolveColumns(f, rhsSph.p, rhsTor.p); }
+
+int Viscoelastic3DGpu::SolveColumns(const Flavour& f, double2* sph, double2* tor) {
+  auto* sphD = reinterpret_cast<double*>(sph);
+  auto* torD = reinterpret_cast<double*>(tor);
   SL3D_TRY(BandSolveBatch(f.dSphChol.p, f.sphChol.data(), static_cast<int>(f.sphChol.size()), f.iSphChol.p,
                           f.nSphChol, f.bands.p, f.pivots.p, sphD, f.scales.p, 0, stream));
   SL3D_TRY(BandSolveBatch(f.dSphLu.p, f.sphLu.data(), static_cast<int>(f.sphLu.size()), f.iSphLu.p, f.nSphLu,
@@ -934,7 +1018,9 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   SL3D_TRY(AnalyseWeighted(*d0, weight.p, analysedStart.p));
 
   info = sl3dgpu_step_info{};
-  if (options.precision == 1) {
+  if (options.solver == 1) {
+    SL3D_TRY(ConvergeConjugateGradients(*f, sigmaEnd, info));
+  } else if (options.precision == 1) {
     LaunchCast(values, weight.p, weight32.p, stream);
     SL3D_CHECK_LAUNCH();
     SL3D_TRY(ConvergeMixed(*f, sigmaEnd, info));
@@ -1176,6 +1262,122 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
   return SL3DGPU_OK;
 }
 
+// -- conjugate gradients (Options::solver = ConjugateGradients) ---------------------------------------
+
+// LateralForce (OpenStep::LateralForce): the strain of solutions x, its
+// laterally weighted grid analysed over the lateral nodes, and the force of
+// that on every degree's columns.
+int Viscoelastic3DGpu::LateralForce(const double2* x, double2* out) {
+  LaunchStrain(geo, x, x + rhsSphComplex, sNext.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_CUDA(cudaMemsetAsync(analysed.p, 0, spectralComplex * sizeof(double2), stream));
+  SL3D_TRY(WeightedPass(sNext.p, analysed.p));
+  SL3D_CUDA(cudaMemsetAsync(out, 0, Columns() * sizeof(double2), stream));
+  LaunchForces(geo, analysed.p, out, out + rhsSphComplex, stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+// ApplyLateralOperator (Viscoelastic3D.cpp:626-728): K x - LateralForce(x).
+int Viscoelastic3DGpu::ApplyOperator(const Flavour& f, const double2* x, double2* out) {
+  SL3D_TRY(LateralForce(x, out));
+  const auto* xd = reinterpret_cast<const double*>(x);
+  auto* od = reinterpret_cast<double*>(out);
+  LaunchBandApply(f.dSphApply.p, f.nSphApply, f.maxApplyRows, f.applyBands.p, xd, od, true, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchBandApply(f.dTorApply.p, f.nTorApply, f.maxApplyRows, f.applyBands.p, xd, od, true, stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+// LateralPair over every degree's m >= 0 columns, read back to the host.
+int Viscoelastic3DGpu::PairOf(const double2* a, const double2* b, double* out) {
+  LaunchPair(a, b, pairChunks.p, pairChunkCount, pairPartial.p, pairResult.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_CUDA(cudaMemcpyAsync(hostResult, pairResult.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  *out = hostResult[0];
+  return SL3DGPU_OK;
+}
+
+// The step closed by preconditioned conjugate gradients (Viscoelastic3D.cpp
+// :2008-2015; detail/LateralSolve.hpp:112-181): forces of the fixed memory
+// and the load channel, the solve from the reference response, the strain
+// of the solution.
+int Viscoelastic3DGpu::ConvergeConjugateGradients(const Flavour& f, const double2* sigmaEnd,
+                                                  sl3dgpu_step_info& info) {
+  const long long n = 2 * Columns();
+  auto* F = reinterpret_cast<double*>(cgF.p);
+  auto* X = reinterpret_cast<double*>(cgX.p);
+  auto* R = reinterpret_cast<double*>(cgR.p);
+  auto* Z = reinterpret_cast<double*>(cgZ.p);
+  auto* Pd = reinterpret_cast<double*>(cgP.p);
+  auto* AP = reinterpret_cast<double*>(cgAp.p);
+  // OpenStep::Forces: the fixed memory force, plus the load's force vectors.
+  SL3D_CUDA(cudaMemsetAsync(cgF.p, 0, Columns() * sizeof(double2), stream));
+  LaunchForces(geo, fixedS.p, cgF.p, cgF.p + rhsSphComplex, stream);
+  SL3D_CHECK_LAUNCH();
+  if (sigmaEnd != nullptr) {
+    LaunchAddLoad(geo, sigmaEnd, f.loadForces.p, f.unitOffset.p, cgF.p, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  // x = K^-1 f, the reference response; energy = <x, f>.
+  SL3D_CUDA(cudaMemcpyAsync(cgX.p, cgF.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_TRY(SolveColumns(f, cgX.p, cgX.p + rhsSphComplex));
+  double energy = 0.0;
+  SL3D_TRY(PairOf(cgX.p, cgF.p, &energy));
+  auto relative = [&](double value) {
+    return energy > 0.0 ? std::sqrt(std::abs(value) / energy) : std::sqrt(std::abs(value));
+  };
+  info.converged = 0;
+  {  // the reference iterates whether or not the weight vanishes (OpenStep::Solve: lateral = true)
+    // r = f - A x, z = M^-1 r, p = z.
+    SL3D_TRY(ApplyOperator(f, cgX.p, cgAp.p));
+    LaunchSub(n, F, AP, R, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(cgZ.p, cgR.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+    SL3D_TRY(SolveColumns(f, cgZ.p, cgZ.p + rhsSphComplex));
+    double rz = 0.0;
+    SL3D_TRY(PairOf(cgZ.p, cgR.p, &rz));
+    info.residual = relative(rz);
+    history.push_back(info.residual);
+    const double target = options.solve_rtol;
+    SL3D_CUDA(cudaMemcpyAsync(cgP.p, cgZ.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+    for (int iteration = 0; iteration < options.solve_max_iterations; ++iteration) {
+      if (info.residual <= target) break;
+      SL3D_TRY(ApplyOperator(f, cgP.p, cgAp.p));
+      double curvature = 0.0;
+      SL3D_TRY(PairOf(cgP.p, cgAp.p, &curvature));
+      const double alpha = rz / curvature;
+      LaunchAxpy(n, alpha, Pd, X, stream);
+      LaunchAxpy(n, -alpha, AP, R, stream);
+      SL3D_CHECK_LAUNCH();
+      SL3D_CUDA(cudaMemcpyAsync(cgZ.p, cgR.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+      SL3D_TRY(SolveColumns(f, cgZ.p, cgZ.p + rhsSphComplex));
+      double next = 0.0;
+      SL3D_TRY(PairOf(cgZ.p, cgR.p, &next));
+      const double beta = next / rz;
+      rz = next;
+      LaunchXpby(n, Z, beta, Pd, stream);
+      SL3D_CHECK_LAUNCH();
+      info.solve_iterations = iteration + 1;
+      info.residual = relative(rz);
+      history.push_back(info.residual);
+    }
+    if (info.residual <= target) info.converged = 1;
+  }
+  info.iterations = info.solve_iterations;
+  // The solutions (for Surface) and their strain.
+  SL3D_CUDA(cudaMemcpyAsync(rhsSph.p, cgX.p, rhsSphComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  if (rhsTorComplex > 0)
+    SL3D_CUDA(cudaMemcpyAsync(rhsTor.p, cgX.p + rhsSphComplex, rhsTorComplex * sizeof(double2),
+                              cudaMemcpyDeviceToDevice, stream));
+  LaunchStrain(geo, rhsSph.p, rhsTor.p, s.p, stream);
+  SL3D_CHECK_LAUNCH();
+  (void)Z;
+  return SL3DGPU_OK;
+}
+
 // Step (Viscoelastic3D.cpp:1982-2030): one stage, or Sdirk2's two backward
 // Euler stages of gamma dt, the second from (1 - r) m_n + r Y_1.
 int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1,
@@ -1225,6 +1427,7 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     info.iterations = i1.iterations + i2.iterations;
     info.mixed_passes = i1.mixed_passes + i2.mixed_passes;
     info.correction_passes = i1.correction_passes + i2.correction_passes;
+    info.solve_iterations = i1.solve_iterations + i2.solve_iterations;
     info.residual = i2.residual;
     info.converged = i1.converged && i2.converged;
   }

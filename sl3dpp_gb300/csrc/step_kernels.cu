@@ -586,6 +586,80 @@ __global__ void MixerMixKernel(MixerArgsT<T> a) {
   }
 }
 
+// -- conjugate gradients -----------------------------------------------------------------------
+
+// Warp per (system, row), lanes over the row's columns: the band entries of
+// the row are broadcast reads, the x rows coalesced (and L1/L2 hits for the
+// neighbouring rows' warps).
+__global__ void BandApplyKernel(const sl3dgpu_band_system* systems, const double* bands, const double* x, double* y,
+                                bool subtract) {
+  const sl3dgpu_band_system s = systems[blockIdx.y];
+  const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (row >= s.n) return;
+  const int kd = s.ku, ld = kd + 1, cols = s.nrhs;
+  const double* band = bands + s.band;
+  const double* xs = x + s.rhs;
+  double* ys = y + s.rhs + static_cast<long long>(row) * cols;
+  const int j0 = max(0, row - kd), j1 = min(s.n - 1, row + kd);
+  for (int c = lane; c < cols; c += 32) {
+    double sum = 0.0;
+    for (int j = j0; j <= j1; ++j) {
+      const int lo = min(row, j), hi = max(row, j);
+      sum += band[static_cast<long long>(hi) * ld + kd + lo - hi] * xs[static_cast<long long>(j) * cols + c];
+    }
+    ys[c] = subtract ? sum - ys[c] : sum;
+  }
+}
+
+__global__ void PairKernel(const double2* a, const double2* b, const PairChunk* chunks, double* partial) {
+  __shared__ double red[256];
+  const PairChunk c = chunks[blockIdx.x];
+  double sum = 0.0;
+  for (long long k = c.start + threadIdx.x; k < c.end; k += blockDim.x) {
+    const int m = static_cast<int>((k - c.degreeStart) % c.cols);
+    const double2 u = a[k], v = b[k];
+    sum += (m == 0 ? 1.0 : 2.0) * (u.x * v.x + u.y * v.y);
+  }
+  red[threadIdx.x] = sum;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w /= 2) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void SumKernel(const double* partial, int count, double* result) {
+  __shared__ double red[256];
+  double sum = 0.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) sum += partial[i];
+  red[threadIdx.x] = sum;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w /= 2) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) result[0] = red[0];
+}
+
+__global__ void AxpyKernel(long long n, double alpha, const double* x, double* y) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    y[i] += alpha * x[i];
+}
+
+__global__ void XpbyKernel(long long n, const double* x, double beta, double* y) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    y[i] = x[i] + beta * y[i];
+}
+
+__global__ void SubKernel(long long n, const double* a, const double* b, double* out) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    out[i] = a[i] - b[i];
+}
+
 // -- the mixed form's refinement glue ----------------------------------------------------------
 
 __global__ void Residual32Kernel(long long n, const double* next, const double* now, float* r) {
@@ -752,6 +826,38 @@ void LaunchMixerFirst(const MixerArgsT<double>& a, cudaStream_t stream) { MixerF
 void LaunchMixerUpdate(const MixerArgsT<double>& a, cudaStream_t stream) { MixerUpdate(a, stream); }
 void LaunchMixerFirst(const MixerArgsT<float>& a, cudaStream_t stream) { MixerFirst(a, stream); }
 void LaunchMixerUpdate(const MixerArgsT<float>& a, cudaStream_t stream) { MixerUpdate(a, stream); }
+
+void LaunchBandApply(const sl3dgpu_band_system* devSystems, int count, int maxRows, const double* bands,
+                     const double* x, double* y, bool subtract, cudaStream_t stream) {
+  if (count == 0 || maxRows == 0) return;
+  constexpr int kRowsPerBlock = 8;
+  prof::Scope scope(prof::kBandSolve, stream);
+  BandApplyKernel<<<dim3((maxRows + kRowsPerBlock - 1) / kRowsPerBlock, count), kRowsPerBlock * 32, 0, stream>>>(
+      devSystems, bands, x, y, subtract);
+}
+
+void LaunchPair(const double2* a, const double2* b, const PairChunk* chunks, int count, double* partial,
+                double* result, cudaStream_t stream) {
+  {
+    prof::Scope scope(prof::kOther, stream);
+    PairKernel<<<count, 256, 0, stream>>>(a, b, chunks, partial);
+  }
+  prof::Scope scope(prof::kOther, stream);
+  SumKernel<<<1, 256, 0, stream>>>(partial, count, result);
+}
+
+void LaunchAxpy(long long n, double alpha, const double* x, double* y, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 24.0);
+  AxpyKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, alpha, x, y);
+}
+void LaunchXpby(long long n, const double* x, double beta, double* y, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 24.0);
+  XpbyKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, x, beta, y);
+}
+void LaunchSub(long long n, const double* a, const double* b, double* out, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 24.0);
+  SubKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, a, b, out);
+}
 
 void LaunchResidual32(long long n, const double* next, const double* now, float* r, cudaStream_t stream) {
   prof::Scope scope(prof::kStream, stream, 0.0, n * 20.0);

@@ -115,6 +115,30 @@ void LaunchAddCorrection(long long n, const float* e, double* s, cudaStream_t st
 void LaunchAddInPlace(long long n, const float* r, float* e, cudaStream_t stream);
 void LaunchCast(long long n, const double* in, float* out, cudaStream_t stream);
 
+// -- conjugate gradients (detail/LateralSolve.hpp:71-181) --------------------------------------
+
+// y = A x for a batch of symmetric band systems (upper storage, kd + 1 rows,
+// DegreeOperator::ApplyBand) on row-major right-hand sides; with
+// subtract, y = A x - y. systems[i].band and .rhs are element offsets.
+void LaunchBandApply(const sl3dgpu_band_system* devSystems, int count, int maxRows, const double* bands,
+                     const double* x, double* y, bool subtract, cudaStream_t stream);
+
+// A span of one degree's [dof][l + 1] complex block for the weighted pairing.
+struct PairChunk {
+  long long start, end;  // complex offsets of the span
+  long long degreeStart; // the degree block's first value
+  int cols;              // l + 1
+  int pad;
+};
+// LateralPair: sum over the chunks of w_m Re(a conj b), w_m = 1 at m = 0 and
+// 2 above, into result[0] (FP64, fixed order). partial holds count doubles.
+void LaunchPair(const double2* a, const double2* b, const PairChunk* chunks, int count, double* partial,
+                double* result, cudaStream_t stream);
+// y += alpha x; y = x + beta y; out = a - b (n reals).
+void LaunchAxpy(long long n, double alpha, const double* x, double* y, cudaStream_t stream);
+void LaunchXpby(long long n, const double* x, double beta, double* y, cudaStream_t stream);
+void LaunchSub(long long n, const double* a, const double* b, double* out, cudaStream_t stream);
+
 // The Anderson mixer's sweeps (AndersonMixer.hpp:65-219), on vectors of
 // reals T with the Gram sums in FP64.
 template <class T>

@@ -37,12 +37,14 @@ class Options(ctypes.Structure):
                 ("oversampling", ctypes.c_double), ("max_iterations", ctypes.c_int),
                 ("rtol", ctypes.c_double), ("damping", ctypes.c_double), ("anderson_memory", ctypes.c_int),
                 ("anderson_rate", ctypes.c_double), ("precision", ctypes.c_int),
-                ("correction_rtol", ctypes.c_double)]
+                ("correction_rtol", ctypes.c_double), ("solver", ctypes.c_int),
+                ("solve_rtol", ctypes.c_double), ("solve_max_iterations", ctypes.c_int)]
 
     @classmethod
     def defaults(cls, lmax: int, ngll: int = 5, **kw) -> "Options":
         o = cls(lmax=lmax, ngll=ngll, eps=1e-8, oversampling=1.5, max_iterations=40, rtol=1e-11,
-                damping=1.0, anderson_memory=5, anderson_rate=0.5, precision=0, correction_rtol=1e-5)
+                damping=1.0, anderson_memory=5, anderson_rate=0.5, precision=0, correction_rtol=1e-5,
+                solver=0, solve_rtol=1e-11, solve_max_iterations=200)
         for k, v in kw.items():
             setattr(o, k, v)
         return o
@@ -52,7 +54,8 @@ class StepInfo(ctypes.Structure):
     """sl3dgpu_step_info (Viscoelastic3D::StepInfo)."""
 
     _fields_ = [("iterations", ctypes.c_int), ("residual", ctypes.c_double), ("converged", ctypes.c_int),
-                ("mixed_passes", ctypes.c_int), ("correction_passes", ctypes.c_int)]
+                ("mixed_passes", ctypes.c_int), ("correction_passes", ctypes.c_int),
+                ("solve_iterations", ctypes.c_int)]
 
 
 _SIGNED = False
