@@ -157,6 +157,45 @@ typedef struct sl3dgpu_step_info {
   int solve_iterations;  /* conjugate gradients: iterations (StepInfo::solveIterations) */
 } sl3dgpu_step_info;
 
+/* ElasticPerturbation3D (include/sl3dpp/ElasticPerturbation3D.hpp:77-225): the
+ * static gravitating elastic problem under lateral perturbations dMu, dKappa
+ * of the shear and bulk moduli. The coupling's nodes are the GLL nodes of
+ * every solid element above the one holding the centre; the reference systems
+ * are the elastic degree operators of the layered Earth. Moduli directions
+ * live on the grid values (node-major, colatitude, longitude) in the model's
+ * modulus unit (sl3dgpu_ep3d_scales); loads are non-dimensional surface
+ * densities in the real layout l(l+1)/2 + m. The operator holds one solution:
+ * SolveLoad's, Respond's or SolveLateral's, which Surface reads. */
+typedef struct sl3dgpu_ep3d sl3dgpu_ep3d;
+typedef struct sl3dgpu_ep3d_options {
+  int lmax;
+  int ngll;             /* GLL nodes per element */
+  double eps;           /* truncation level, 1e-8 */
+  double oversampling;  /* 1.5 */
+} sl3dgpu_ep3d_options;
+int sl3dgpu_ep3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_ep3d_options* options,
+                        sl3dgpu_ep3d** out);
+void sl3dgpu_ep3d_destroy(sl3dgpu_ep3d* op);
+int sl3dgpu_ep3d_shape(const sl3dgpu_ep3d* op, int* nodes, int* ntheta, int* nphi);
+int sl3dgpu_ep3d_nodes(const sl3dgpu_ep3d* op, double* radius, int* element);
+int sl3dgpu_ep3d_colatitudes(const sl3dgpu_ep3d* op, double* theta, double* weights);
+/* SI per model unit: length, modulus, surface density. */
+int sl3dgpu_ep3d_scales(const sl3dgpu_ep3d* op, double* length, double* modulus, double* surface_density);
+/* The directions (host or device arrays, either NULL for none). */
+int sl3dgpu_ep3d_set_moduli(sl3dgpu_ep3d* op, const double* d_mu, const double* d_kappa, int on_device);
+/* SolveLoad: the reference response to a load (host coefficients). */
+int sl3dgpu_ep3d_solve_load(sl3dgpu_ep3d* op, const double* load);
+/* Respond: the held solution x replaced by -K^-1 (dK) x (the Born response). */
+int sl3dgpu_ep3d_respond(sl3dgpu_ep3d* op);
+/* SolveLateral: (K_ref + dK) x = the load's forces by preconditioned
+ * conjugate gradients from the reference response (iterations, residual and
+ * convergence in info; the residuals after each iteration in the history). */
+int sl3dgpu_ep3d_solve_lateral(sl3dgpu_ep3d* op, const double* load, double rtol, int max_iterations,
+                               sl3dgpu_step_info* info);
+/* Surface U (0), V (1) or phi (2) of the held solution, (l, m >= 0). */
+int sl3dgpu_ep3d_surface(sl3dgpu_ep3d* op, int component, double* out);
+int sl3dgpu_ep3d_residual_history(const sl3dgpu_ep3d* op, double* out, int capacity);
+
 /* The configurations' Earth (radius 6371 km, fluid core to 3480 km, linear
  * mantle, 100 km elastic lid, 5e21 / 5e20 Pa s below / above 670 km), the
  * given element count spread over its four layers in proportion to

@@ -412,20 +412,33 @@ struct Node {
 
 class Viscoelastic3D {
  public:
-  Viscoelastic3D(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& options)
+  // staticPerturbation: ElasticPerturbation3D's coupling instead of the
+  // step's (src/ElasticPerturbation3D.cpp:46-73): the GLL nodes of every
+  // solid element above the one holding the centre, the unrelaxed material,
+  // the elastic operators without point shear.
+  Viscoelastic3D(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& options,
+                 bool staticPerturbation = false)
       : options_(options),
+        static_(staticPerturbation),
         earth_(ToLayers(layers, nlayers), Scales::Geophysical(layers[nlayers - 1].r1)),
         mesh_(RadialMesh::Create(earth_, options.ngll)),
         material_(Material::Create(earth_, mesh_)),
         rheology_(Rheology::FromEarth(earth_, material_)),
         reference_(rheology_, true),
-        grid_(options.lmax, options.oversampling) {
-    const auto& mesh = reference_.nodal.mesh;
+        grid_(options.lmax, options.oversampling),
+        gll_(MemoryPoints::Of(false, mesh_)) {
+    points_ = static_ ? &gll_ : &reference_.points;
+    nodal_ = static_ ? &material_ : &reference_.nodal;
+    const auto& mesh = nodal_->mesh;
     const int n = mesh.NGll();
-    const auto& pts = reference_.points;
+    const auto& pts = *points_;
     for (int e = 0; e < mesh.ElementCount(); ++e) {
       bool carries = false;
-      for (int i = 0; i < n; ++i) carries = carries || rheology_.IsActive(static_cast<std::size_t>(e) * n + i);
+      if (static_) {
+        carries = !material_.IsFluid(e) && !(e == 0 && mesh.Left(0) == 0.0);
+      } else {
+        for (int i = 0; i < n; ++i) carries = carries || rheology_.IsActive(static_cast<std::size_t>(e) * n + i);
+      }
       if (!carries) continue;
       for (int p = 0; p < pts.count; ++p) nodes_.push_back({e, p, pts.RadiusAt(mesh, e, p)});
     }
@@ -443,7 +456,7 @@ class Viscoelastic3D {
     }
     factor_.assign(static_cast<std::size_t>(NodeCount()) * grid_.FieldSize(), 1.0);
     // the elastic (unrelaxed) operators
-    elastic_ = BuildFlavour(reference_.elastic);
+    elastic_ = BuildFlavour(static_ ? nullptr : &reference_.elastic);
   }
 
   static std::vector<Layer> ToLayers(const sl3dgpu_layer* layers, int n) {
@@ -537,8 +550,8 @@ class Viscoelastic3D {
   // StrainOf: every degree's solution into a fresh spectral tensor.
   Spectral StrainOf(const Solutions& x, const Flavour& f) const {
     Spectral s = ZeroSpectral();
-    const auto& mesh = reference_.nodal.mesh;
-    const auto& pts = reference_.points;
+    const auto& mesh = nodal_->mesh;
+    const auto& pts = *points_;
     const int n = mesh.NGll();
     const int L = options_.lmax;
 #pragma omp parallel for schedule(dynamic)
@@ -581,8 +594,8 @@ class Viscoelastic3D {
   // SpheroidalForce + ToroidalForce.
   void Forces(const Spectral& w, const Flavour& f, std::vector<std::vector<C>>& sph,
               std::vector<std::vector<C>>& tor) const {
-    const auto& mesh = reference_.nodal.mesh;
-    const auto& pts = reference_.points;
+    const auto& mesh = nodal_->mesh;
+    const auto& pts = *points_;
     const int n = mesh.NGll();
     const int L = options_.lmax;
     sph.assign(L + 1, {});
@@ -662,9 +675,10 @@ class Viscoelastic3D {
     }
   }
 
-  std::unique_ptr<Flavour> BuildFlavour(const PointShear& shear) const {
+  std::unique_ptr<Flavour> BuildFlavour(const PointShear* shear) const {
     auto f = std::make_unique<Flavour>();
-    f->shear = shear;
+    if (shear != nullptr) f->shear = *shear;
+    const PointShear* use = shear != nullptr ? &f->shear : nullptr;
     const int L = options_.lmax;
     f->sph.resize(L + 1);
     f->tor.resize(L + 1);
@@ -673,7 +687,7 @@ class Viscoelastic3D {
     f->units.resize(L + 1);
 #pragma omp parallel for schedule(dynamic)
     for (int l = 0; l <= L; ++l) {
-      f->sph[l] = std::make_unique<DegreeOperator>(reference_.nodal, l, options_.eps, &f->shear);
+      f->sph[l] = std::make_unique<DegreeOperator>(*nodal_, l, options_.eps, use);
       f->sphF[l] = FactorSpheroidal(*f->sph[l]);
       const auto load = f->sph[l]->Load();
       std::vector<C> b(load.begin(), load.end());
@@ -681,7 +695,7 @@ class Viscoelastic3D {
       f->units[l].resize(x.size());
       for (std::size_t i = 0; i < x.size(); ++i) f->units[l][i] = x[i].real();
       if (l >= 1) {
-        f->tor[l] = std::make_unique<ToroidalOperator>(reference_.nodal, l, options_.eps, &f->shear);
+        f->tor[l] = std::make_unique<ToroidalOperator>(*nodal_, l, options_.eps, use);
         f->torF[l] = FactorToroidal(*f->tor[l]);
       }
     }
@@ -691,7 +705,8 @@ class Viscoelastic3D {
   const Flavour& FlavourOf(Scheme scheme, double dt) {
     for (auto& [key, f] : flavours_)
       if (key.first == static_cast<int>(scheme) && key.second == dt) return *f;
-    flavours_.emplace_back(std::make_pair(static_cast<int>(scheme), dt), BuildFlavour(reference_.StepShear(scheme, dt)));
+    const auto shear = reference_.StepShear(scheme, dt);
+    flavours_.emplace_back(std::make_pair(static_cast<int>(scheme), dt), BuildFlavour(&shear));
     return *flavours_.back().second;
   }
 
@@ -763,9 +778,10 @@ class Viscoelastic3D {
     return total;
   }
 
-  // y = K x - y per degree (ApplyLateralOperator, Viscoelastic3D.cpp:626-728):
-  // the complex columns as real pairs through the assembled bands.
-  void KxMinus(const Solutions& x, const Flavour& f, Solutions& y) const {
+  // y = K x + keep y per degree (ApplyLateralOperator, Viscoelastic3D.cpp:
+  // 626-728, keep -1; ElasticPerturbation3D::Apply, keep +1): the complex
+  // columns as real pairs through the assembled bands.
+  void AddKx(const Solutions& x, const Flavour& f, Solutions& y, double keep) const {
     const int L = options_.lmax;
 #pragma omp parallel for schedule(dynamic)
     for (int t = 0; t < 2 * L + 1; ++t) {
@@ -786,7 +802,7 @@ class Viscoelastic3D {
       for (int c = 0; c < cols; ++c)
         for (int d = 0; d < ndof; ++d) {
           const std::size_t at = static_cast<std::size_t>(c) * ndof + d;
-          yl[at] = C(k[at], k[static_cast<std::size_t>(cols + c) * ndof + d]) - yl[at];
+          yl[at] = C(k[at], k[static_cast<std::size_t>(cols + c) * ndof + d]) + keep * yl[at];
         }
     }
   }
@@ -833,10 +849,20 @@ class Viscoelastic3D {
       Analyse(grid, analysed);
       Solutions y;
       Forces(analysed, flavour, y.sph, y.tor);
-      KxMinus(x, flavour, y);
+      AddKx(x, flavour, y, -1.0);
       return y;
     };
     auto solve = [&](const Solutions& b) { return SolveForces(b.sph, b.tor, flavour); };
+    return LateralCG(f, apply, solve, options_.solve_rtol, options_.solve_max_iterations, lateral, info);
+  }
+
+  // LateralConjugateGradients (detail/LateralSolve.hpp:112-181; no start,
+  // reduction 0): from the reference response x = M^-1 f, the relative
+  // residual in the preconditioned energy norm, one history entry per
+  // iteration and the first.
+  template <class Apply, class Solve>
+  Solutions LateralCG(const Solutions& f, Apply&& apply, Solve&& solve, double rtol, int maxIterations, bool lateral,
+                      Info& info) {
     Solutions x = solve(f);
     const double energy = Pair(x, f);
     auto relative = [&](double v) { return energy > 0.0 ? std::sqrt(std::abs(v) / energy) : std::sqrt(std::abs(v)); };
@@ -854,9 +880,9 @@ class Viscoelastic3D {
     double rz = Pair(z, r);
     info.residual = relative(rz);
     history_.push_back(info.residual);
-    const double target = options_.solve_rtol;
+    const double target = rtol;
     Solutions p = z;
-    for (int iteration = 0; iteration < options_.solve_max_iterations; ++iteration) {
+    for (int iteration = 0; iteration < maxIterations; ++iteration) {
       if (info.residual <= target) break;
       const Solutions ap = apply(p);
       const double curvature = Pair(p, ap);
@@ -880,6 +906,169 @@ class Viscoelastic3D {
     info.converged = info.residual <= target;
     info.iterations = info.solveIterations;
     return x;
+  }
+
+  // -- the static perturbation problem (ElasticPerturbation3D) ---------------------------------
+
+  void SetModuli(const double* dMu, const double* dKappa) {
+    const std::size_t values = static_cast<std::size_t>(NodeCount()) * grid_.FieldSize();
+    dMu_.assign(dMu ? dMu : nullptr, dMu ? dMu + values : nullptr);
+    dKappa_.assign(dKappa ? dKappa : nullptr, dKappa ? dKappa + values : nullptr);
+  }
+
+  // AddDilatationOfSolution (src/GridCoupling.cpp:359-398): per node the
+  // real spin-0 coefficients r dU/dr + 2 U - l(l+1) V.
+  std::vector<C> DilatationOf(const Solutions& x) const {
+    const auto& mesh = nodal_->mesh;
+    const auto& pts = *points_;
+    const int n = mesh.NGll(), L = options_.lmax;
+    std::vector<C> scalar(static_cast<std::size_t>(NodeCount()) * grid_.RealSize());
+#pragma omp parallel for schedule(dynamic)
+    for (int l = L; l >= 0; --l) {
+      const auto& op = *elastic_->sph[l];
+      const int ndof = op.DofCount();
+      const double k2 = l * (l + 1.0);
+      for (int node = firstNode_[l]; node < NodeCount(); ++node) {
+        const int e = nodes_[node].element, q = nodes_[node].q;
+        const double r = nodes_[node].r, jac = mesh.Jacobian(e);
+        for (int m = 0; m <= l; ++m) {
+          C U{}, V{}, rdU{};
+          for (int i = 0; i < n; ++i) {
+            const int g = mesh.GlobalIndex(e, i);
+            const int dU = op.Dof(g, kU), dV = op.Dof(g, kV);
+            const C Ui = dU >= 0 ? x.sph[l][static_cast<std::size_t>(m) * ndof + dU] : C{};
+            const C Vi = dV >= 0 ? x.sph[l][static_cast<std::size_t>(m) * ndof + dV] : C{};
+            U += pts.Value(q, i) * Ui;
+            V += pts.Value(q, i) * Vi;
+            rdU += r * pts.Derivative(q, i) / jac * Ui;
+          }
+          scalar[static_cast<std::size_t>(node) * grid_.RealSize() + OGrid::Index(l, m)] = rdU + 2.0 * U - k2 * V;
+        }
+      }
+    }
+    return scalar;
+  }
+
+  // DilatationForce (src/GridCoupling.cpp:433-495), added onto sph.
+  void AddDilatationForce(const std::vector<C>& weighted, std::vector<std::vector<C>>& sph) const {
+    const auto& mesh = nodal_->mesh;
+    const auto& pts = *points_;
+    const int n = mesh.NGll(), L = options_.lmax;
+#pragma omp parallel for schedule(dynamic)
+    for (int l = L; l >= 0; --l) {
+      const auto& op = *elastic_->sph[l];
+      const int ndof = op.DofCount();
+      const double k2 = l * (l + 1.0);
+      auto& b = sph[l];
+      for (int node = firstNode_[l]; node < NodeCount(); ++node) {
+        const int e = nodes_[node].element, q = nodes_[node].q;
+        const double r = nodes_[node].r, jac = mesh.Jacobian(e);
+        for (int m = 0; m <= l; ++m) {
+          const C D = weighted[static_cast<std::size_t>(node) * grid_.RealSize() + OGrid::Index(l, m)];
+          const double point = jac * pts.weight[q];
+          for (int i = 0; i < n; ++i) {
+            const int g = mesh.GlobalIndex(e, i);
+            const int iU = op.Dof(g, kU), iV = op.Dof(g, kV);
+            const double v = point * pts.Value(q, i);
+            if (iU >= 0) b[static_cast<std::size_t>(m) * ndof + iU] += 2.0 * v * D;
+            if (iV >= 0) b[static_cast<std::size_t>(m) * ndof + iV] -= k2 * v * D;
+          }
+          for (int j = 0; j < n; ++j) {
+            const int jU = op.Dof(mesh.GlobalIndex(e, j), kU);
+            if (jU >= 0) b[static_cast<std::size_t>(m) * ndof + jU] += pts.weight[q] * pts.Derivative(q, j) * r * D;
+          }
+        }
+      }
+    }
+  }
+
+  // (dK) x (ElasticPerturbation3D::Force, src/ElasticPerturbation3D.cpp:140-226).
+  Solutions PerturbationForce(const Solutions& x) const {
+    const int L = options_.lmax;
+    Solutions out;
+    out.sph.assign(L + 1, {});
+    out.tor.assign(L + 1, {});
+    for (int l = 0; l <= L; ++l) {
+      out.sph[l].assign(static_cast<std::size_t>(elastic_->sph[l]->DofCount()) * (l + 1), C{});
+      if (l >= 1) out.tor[l].assign(static_cast<std::size_t>(elastic_->tor[l]->DofCount()) * (l + 1), C{});
+    }
+    if (!dMu_.empty()) {
+      Spectral e = StrainOf(x, *elastic_);
+      Tensor grid = ZeroTensor();
+      Synthesise(e, grid);
+      for (std::size_t i = 0; i < dMu_.size(); ++i) {
+        grid.c0[i] *= dMu_[i];
+        grid.c1[i] *= dMu_[i];
+        grid.r[i] *= dMu_[i];
+      }
+      Spectral weighted = ZeroSpectral();
+      Analyse(grid, weighted);
+      std::vector<std::vector<C>> fs, ft;
+      Forces(weighted, *elastic_, fs, ft);
+      out.sph = std::move(fs);
+      out.tor = std::move(ft);
+    }
+    if (!dKappa_.empty()) {
+      auto scalar = DilatationOf(x);
+      const auto fs = grid_.FieldSize();
+      std::vector<double> field(static_cast<std::size_t>(NodeCount()) * fs);
+#pragma omp parallel for schedule(dynamic)
+      for (int p = 0; p < NodeCount(); ++p) {
+        grid_.SynthReal(scalar.data() + static_cast<std::size_t>(p) * grid_.RealSize(), field.data() + p * fs);
+        for (std::size_t i = p * fs; i < (p + 1) * fs; ++i) field[i] *= dKappa_[i];
+        grid_.ExpandReal(field.data() + p * fs, scalar.data() + static_cast<std::size_t>(p) * grid_.RealSize());
+      }
+      AddDilatationForce(scalar, out.sph);
+    }
+    return out;
+  }
+
+  // SolveLoad (:98-126): the unit load responses times the coefficients.
+  void SolveLoad(const C* load) {
+    const int L = options_.lmax;
+    Solutions x;
+    x.sph.assign(L + 1, {});
+    x.tor.assign(L + 1, {});
+    for (int l = 0; l <= L; ++l) {
+      const int ndof = elastic_->sph[l]->DofCount();
+      x.sph[l].assign(static_cast<std::size_t>(ndof) * (l + 1), C{});
+      if (l >= 1) x.tor[l].assign(static_cast<std::size_t>(elastic_->tor[l]->DofCount()) * (l + 1), C{});
+      for (int m = 0; m <= l; ++m)
+        for (int d = 0; d < ndof; ++d)
+          x.sph[l][static_cast<std::size_t>(m) * ndof + d] = load[OGrid::Index(l, m)] * elastic_->units[l][d];
+    }
+    last_ = std::move(x);
+  }
+
+  // Respond (:474-479): -K^-1 (dK) x of the held solution.
+  void Respond() {
+    Solutions f = PerturbationForce(last_);
+    Axpy(f, -2.0, f);
+    last_ = SolveForces(f.sph, f.tor, *elastic_);
+  }
+
+  // SolveLateral for a load (:367-430): (K_ref + dK) x = LoadForces.
+  void SolveLateral(const C* load, double rtol, int maxIterations, Info& info) {
+    const int L = options_.lmax;
+    history_.clear();
+    Solutions f;
+    f.sph.assign(L + 1, {});
+    f.tor.assign(L + 1, {});
+    for (int l = 0; l <= L; ++l) {
+      const auto vec = elastic_->sph[l]->Load();
+      const int ndof = elastic_->sph[l]->DofCount();
+      f.sph[l].assign(static_cast<std::size_t>(ndof) * (l + 1), C{});
+      if (l >= 1) f.tor[l].assign(static_cast<std::size_t>(elastic_->tor[l]->DofCount()) * (l + 1), C{});
+      for (int m = 0; m <= l; ++m)
+        for (int d = 0; d < ndof; ++d) f.sph[l][static_cast<std::size_t>(m) * ndof + d] = load[OGrid::Index(l, m)] * vec[d];
+    }
+    auto apply = [&](const Solutions& x) {
+      Solutions y = PerturbationForce(x);
+      AddKx(x, *elastic_, y, 1.0);
+      return y;
+    };
+    auto solve = [&](const Solutions& b) { return SolveForces(b.sph, b.tor, *elastic_); };
+    last_ = LateralCG(f, apply, solve, rtol, maxIterations, !(dMu_.empty() && dKappa_.empty()), info);
   }
 
   // One stage: StartStep, Converge(Respond + AddChannels + StrainOf), Finish.
@@ -1136,8 +1325,13 @@ class Viscoelastic3D {
   RadialMesh mesh_;
   Material material_;
   Rheology rheology_;
+  bool static_ = false;
   ReferenceRheology reference_;
   OGrid grid_;
+  MemoryPoints gll_;
+  const MemoryPoints* points_ = nullptr;
+  const Material* nodal_ = nullptr;
+  std::vector<double> dMu_, dKappa_;  // static problem: the moduli directions (empty for none)
   std::vector<Node> nodes_;
   std::vector<int> firstNode_;
   std::vector<double> factor_;  // exp(-delta) per grid value
@@ -1258,6 +1452,43 @@ int oracle_v3d_state_strain(const oracle_state* s, double* out) {
 }
 
 }  // extern "C"
+
+// The static perturbation problem through the same handle.
+extern "C" oracle_v3d* oracle_ep3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_ep3d_options* o) {
+  sl3dgpu_v3d_options options{};
+  options.lmax = o->lmax;
+  options.ngll = o->ngll;
+  options.eps = o->eps;
+  options.oversampling = o->oversampling;
+  options.max_iterations = 1;
+  options.rtol = 1e-10;
+  options.damping = 1.0;
+  options.solver = 1;
+  auto h = new oracle_v3d;
+  h->op = std::make_unique<oracle::Viscoelastic3D>(layers, nlayers, options, true);
+  return h;
+}
+extern "C" double oracle_v3d_modulus_scale(const oracle_v3d* h) { return h->op->ModelScales().Modulus(); }
+extern "C" void oracle_ep3d_set_moduli(oracle_v3d* h, const double* d_mu, const double* d_kappa) {
+  h->op->SetModuli(d_mu, d_kappa);
+}
+extern "C" void oracle_ep3d_solve_load(oracle_v3d* h, const double* load) {
+  h->op->SolveLoad(reinterpret_cast<const C*>(load));
+}
+extern "C" void oracle_ep3d_respond(oracle_v3d* h) { h->op->Respond(); }
+extern "C" int oracle_ep3d_solve_lateral(oracle_v3d* h, const double* load, double rtol, int max_iterations,
+                                         sl3dgpu_step_info* info) {
+  oracle::Info i;
+  h->op->SolveLateral(reinterpret_cast<const C*>(load), rtol, max_iterations, i);
+  if (info) {
+    *info = sl3dgpu_step_info{};
+    info->iterations = i.iterations;
+    info->residual = i.residual;
+    info->converged = i.converged ? 1 : 0;
+    info->solve_iterations = i.solveIterations;
+  }
+  return 0;
+}
 
 extern "C" int oracle_standard_earth(int elements, double kelvin_fraction, double kelvin_div,
                                      sl3dgpu_layer* out) {

@@ -35,57 +35,14 @@
 #include "host/radial.hpp"
 #include "sht.cuh"
 #include "step_kernels.cuh"
+#include "systems.cuh"
 
 namespace sl3dgpu {
 
-int BandFactorBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
-                    double* bands, int* pivots, int* info, int lu, cudaStream_t stream);
-int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
-                   const int2* devItems, int itemCount, const double* bands, const int* pivots, double* rhs,
-                   const double* scales, int lu, cudaStream_t stream);
-int BandSolveBatchF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
-                    const int2* devItems, int itemCount, const float* bands, const int* pivots, float* rhs,
-                    const float* scales, int lu, cudaStream_t stream);
-std::vector<int2> BandWorkItems(const sl3dgpu_band_system* hostSystems, int count);
 
 namespace {
 
 using host::Scheme;
-
-// A device allocation owned by value.
-template <class T>
-struct Dev {
-  T* p = nullptr;
-  size_t n = 0;
-  Dev() = default;
-  Dev(const Dev&) = delete;
-  Dev& operator=(const Dev&) = delete;
-  Dev(Dev&& o) noexcept : p(o.p), n(o.n) {
-    o.p = nullptr;
-    o.n = 0;
-  }
-  Dev& operator=(Dev&& o) noexcept {
-    std::swap(p, o.p);
-    std::swap(n, o.n);
-    return *this;
-  }
-  ~Dev() { cudaFree(p); }
-  cudaError_t Alloc(size_t count) {
-    cudaFree(p);
-    p = nullptr;
-    n = count;
-    return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
-  }
-  cudaError_t Upload(const std::vector<T>& v) {
-    if (cudaError_t e = Alloc(v.size()); e != cudaSuccess) return e;
-    return v.empty() ? cudaSuccess : cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-  }
-};
-
-#define SL3D_TRY(expr)                            \
-  do {                                            \
-    if (int _st = (expr); _st != SL3DGPU_OK) return _st; \
-  } while (0)
 
 // A grid tensor: the spin -2 and -1 components complex, spin 0 real.
 struct GridTensor {
@@ -96,25 +53,6 @@ struct GridTensor {
     if (auto e = c1.Alloc(values); e != cudaSuccess) return e;
     return r.Alloc(values);
   }
-};
-
-// One flavour (scheme, dt): the factorised systems and the load units.
-struct Flavour {
-  int scheme = 0;
-  double dt = 0.0;
-  Dev<double> bands, scales, units;
-  Dev<float> bands32, scales32;  // the mixed form's FP32 copies
-  // conjugate gradients: the assembled (unscaled) bands for K x, their
-  // systems, and the unsolved load force vectors (DegreeOperator::Load)
-  Dev<double> applyBands, loadForces;
-  Dev<sl3dgpu_band_system> dSphApply, dTorApply;
-  int nSphApply = 0, nTorApply = 0, maxApplyRows = 0;
-  Dev<int> pivots;
-  Dev<long long> unitOffset;
-  std::vector<sl3dgpu_band_system> sphChol, sphLu, torChol;
-  Dev<sl3dgpu_band_system> dSphChol, dSphLu, dTorChol;
-  Dev<int2> iSphChol, iSphLu, iTorChol;
-  int nSphChol = 0, nSphLu = 0, nTorChol = 0;
 };
 
 }  // namespace
@@ -197,6 +135,15 @@ class Viscoelastic3DGpu {
   int pairChunkCount = 0;
   Dev<double> pairPartial, pairResult;
 
+  // The static perturbation problem (ElasticPerturbation3D): GLL nodes of the
+  // solid elements, the elastic systems, dMu as the tensor weight and dKappa
+  // on the dilatation companion.
+  bool staticMode = false;
+  std::unique_ptr<host::MemoryPoints> gllPoints;
+  Dev<double> kappaWeight;
+  Dev<double2> scalarD, scalarW;
+  bool hasMu = false, hasKappa = false;
+
   V3dState scratch;  // the second buffer set a step writes into
   std::vector<double> history;  // the last step's pass residuals, stages in turn
 
@@ -205,7 +152,14 @@ class Viscoelastic3DGpu {
     if (stream) cudaStreamDestroy(stream);
   }
 
-  int Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt);
+  int Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt, bool staticPerturbation = false);
+  // ElasticPerturbation3D: the moduli directions (either may be null), the
+  // reference load response, the Born response of the held solution, the
+  // full solve by conjugate gradients.
+  int SetModuli(const double* dMu, const double* dKappa, bool onDevice);
+  int SolveLoad(const double* load);
+  int Respond();
+  int SolveLateral(const double* load, double rtol, int maxIterations, sl3dgpu_step_info* info);
   int SetDelta(const double* samples, bool onDevice);
   int ZeroState(V3dState& st);
   int Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1, sl3dgpu_step_info* info,
@@ -236,6 +190,10 @@ class Viscoelastic3DGpu {
   int ApplyOperator(const Flavour& f, const double2* x, double2* out);
   int PairOf(const double2* a, const double2* b, double* out);
   int ConvergeConjugateGradients(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
+  int ConjugateGradients(const Flavour& f, bool lateral, double rtol, int maxIterations, sl3dgpu_step_info& info);
+  int PerturbationForce(const double2* x, double2* out);
+  int ApplyPerturbed(const Flavour& f, const double2* x, double2* out);
+  int HoldSolution(const double2* x);
   long long Columns() const { return rhsSphComplex + std::max<long long>(rhsTorComplex, 1); }
   int Converge(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
   int ConvergeMixed(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
@@ -249,8 +207,10 @@ class Viscoelastic3DGpu {
 
 // -- construction ----------------------------------------------------------------------------------
 
-int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt) {
+int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt,
+                              bool staticPerturbation) {
   options = opt;
+  staticMode = staticPerturbation;
   if (opt.lmax < 2 || opt.ngll < 2 || !(opt.oversampling >= 1.0) || opt.anderson_memory > 8 ||
       opt.anderson_memory < 0 || nlayers < 1) {
     SetError("v3d: lmax >= 2, ngll >= 2, oversampling >= 1, anderson_memory in [0, 8]");
@@ -295,16 +255,26 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   SL3D_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   SL3D_CUDA(cudaMallocHost(&hostResult, 8 * sizeof(double)));
   SL3D_TRY(Grid::Create(opt.lmax, 2, opt.oversampling, grid));
-  const auto& nodal = reference->nodal;
+  // The step: the long-term material, the Gauss memory points of every
+  // element where a branch relaxes. The static perturbation problem: the
+  // unrelaxed material and the GLL nodes of every solid element above the
+  // one holding the centre (ElasticPerturbation3D's coupling, src/
+  // ElasticPerturbation3D.cpp:46-73).
+  if (staticMode) gllPoints = std::make_unique<host::MemoryPoints>(host::MemoryPoints::Of(false, *mesh));
+  const auto& nodal = staticMode ? *material : reference->nodal;
   const auto& msh = nodal.mesh;
-  const auto& pts = reference->points;
+  const auto& pts = staticMode ? *gllPoints : reference->points;
+  const host::PointShear* elasticShear = staticMode ? nullptr : &reference->elastic;
   const int n = msh.NGll(), E = msh.ElementCount(), L = opt.lmax;
-  K = static_cast<int>(rheology->branches.size());
-  // The memory nodes: the Gauss points of every element where a branch relaxes.
+  K = staticMode ? 0 : static_cast<int>(rheology->branches.size());
   elemFirstNode.assign(E, -1);
   for (int e = 0; e < E; ++e) {
     bool carries = false;
-    for (int i = 0; i < n; ++i) carries = carries || rheology->IsActive(static_cast<size_t>(e) * n + i);
+    if (staticMode) {
+      carries = !material->IsFluid(e) && !(e == 0 && msh.Left(0) == 0.0);
+    } else {
+      for (int i = 0; i < n; ++i) carries = carries || rheology->IsActive(static_cast<size_t>(e) * n + i);
+    }
     if (!carries) continue;
     elemFirstNode[e] = static_cast<int>(nodeElement.size());
     for (int p = 0; p < pts.count; ++p) {
@@ -344,7 +314,7 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   degrees.resize(L + 1);
   long long sphOff = 0, torOff = 0;
   for (int l = 0; l <= L; ++l) {
-    host::DegreeOperator op(nodal, l, opt.eps, &reference->elastic);
+    host::DegreeOperator op(nodal, l, opt.eps, elasticShear);
     auto& d = degrees[l];
     d.firstNode = firstNode[l];
     d.firstGlobal = d.firstNode < P ? msh.GlobalIndex(nodeElement[d.firstNode], 0) : 0;
@@ -364,7 +334,7 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     d.torNdof = 0;
     d.torRhs = torOff;
     if (l >= 1) {
-      host::ToroidalOperator top(nodal, l, opt.eps, &reference->elastic);
+      host::ToroidalOperator top(nodal, l, opt.eps, elasticShear);
       d.torNdof = top.DofCount();
       torOff += static_cast<long long>(d.torNdof) * (l + 1);
       for (int gn = 0; gn < nglob; ++gn) torMap[d.torMap + gn] = top.Dof(gn);
@@ -415,8 +385,14 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   const size_t spectra = static_cast<size_t>(2 * L + 1) * grid->ntheta * P;
   SL3D_CUDA(spectraA.Alloc(spectra));
   SL3D_CUDA(spectraB.Alloc(spectra));
-  SL3D_CUDA(fixedGrid.Alloc(values));
-  SL3D_CUDA(dGrid.Alloc(values));
+  if (!staticMode) {
+    SL3D_CUDA(fixedGrid.Alloc(values));
+    SL3D_CUDA(dGrid.Alloc(values));
+  } else {
+    SL3D_CUDA(kappaWeight.Alloc(values));
+    SL3D_CUDA(scalarD.Alloc(rowsR * P));
+    SL3D_CUDA(scalarW.Alloc(rowsR * P));
+  }
   SL3D_CUDA(weight.Alloc(values));
   beta.resize(K);
   for (auto& b : beta) SL3D_CUDA(b.Alloc(values));
@@ -461,7 +437,7 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     SL3D_CUDA(weight32.Alloc(values));
     SL3D_CUDA(cudaMemsetAsync(analysed32.p, 0, spectralComplex * sizeof(float2), stream));
   }
-  SL3D_TRY(AllocState(scratch));
+  if (!staticMode) SL3D_TRY(AllocState(scratch));
   SL3D_TRY(BuildFlavour(reference->elastic, *elastic));
   SL3D_CUDA(cudaStreamSynchronize(stream));
   return SL3DGPU_OK;
@@ -521,251 +497,18 @@ int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
 // -- flavours: assembly on the host (once), factorisation on the device ----------------------------
 
 int Viscoelastic3DGpu::BuildFlavour(const host::PointShear& shear, Flavour& f) {
-  const int L = options.lmax;
-  const auto& nodal = reference->nodal;
-  std::vector<std::unique_ptr<host::DegreeOperator>> sph(L + 1);
-  std::vector<std::unique_ptr<host::ToroidalOperator>> tor(L + 1);
-  std::string failure;
-  {
-    const int threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    std::vector<std::thread> pool;
-    std::mutex lock;
-    for (int t = 0; t < threads; ++t)
-      pool.emplace_back([&, t] {
-        for (int l = L - t; l >= 0; l -= threads) {
-          try {
-            sph[l] = std::make_unique<host::DegreeOperator>(nodal, l, options.eps, &shear);
-            if (l >= 1) tor[l] = std::make_unique<host::ToroidalOperator>(nodal, l, options.eps, &shear);
-          } catch (const std::exception& e) {
-            std::lock_guard<std::mutex> g(lock);
-            failure = e.what();
-          }
-        }
-      });
-    for (auto& th : pool) th.join();
-  }
-  if (!failure.empty()) {
-    SetError("v3d: " + failure);
-    return SL3DGPU_ERR_RUNTIME;
-  }
-  // Bands, scales, systems: spheroidal degrees 0..L, toroidal 1..L.
-  std::vector<double> bands, scales;
-  std::vector<sl3dgpu_band_system> chol;  // all Cholesky candidates, sph then tor
-  std::vector<int> cholDegree, cholKind;  // degree, 0 sph 1 tor
-  std::vector<sl3dgpu_band_system> lu;
-  std::vector<int> luDegree;
-  std::vector<long long> sphScale(L + 1), torScale(L + 1);
-  for (int l = 0; l <= L; ++l) {
-    sphScale[l] = static_cast<long long>(scales.size());
-    scales.insert(scales.end(), sph[l]->Scale().begin(), sph[l]->Scale().end());
-  }
-  for (int l = 1; l <= L; ++l) {
-    torScale[l] = static_cast<long long>(scales.size());
-    scales.insert(scales.end(), tor[l]->Scale().begin(), tor[l]->Scale().end());
-  }
-  auto system = [](int n, int kd, long long band, long long rhs, int nrhs, long long scale) {
-    sl3dgpu_band_system s{};
-    s.n = n;
-    s.kl = kd;
-    s.ku = kd;
-    s.nrhs = nrhs;
-    s.band = band;
-    s.pivots = 0;
-    s.rhs = rhs;
-    s.scale = scale;
-    s.pinned0 = s.pinned1 = -1;
-    return s;
-  };
-  for (int l = 0; l <= L; ++l) {
-    const auto& op = *sph[l];
-    if (op.PositiveDiagonal()) {
-      const auto b = op.ScaledCholeskyBand();
-      chol.push_back(system(op.DofCount(), op.Bandwidth(), static_cast<long long>(bands.size()),
-                            2 * degrees[l].sphRhs, 2 * (l + 1), sphScale[l]));
-      bands.insert(bands.end(), b.begin(), b.end());
-      cholDegree.push_back(l);
-      cholKind.push_back(0);
-    } else {
-      luDegree.push_back(l);
-    }
-  }
-  for (int l = 1; l <= L; ++l) {
-    const auto& op = *tor[l];
-    const auto b = op.ScaledCholeskyBand();
-    auto s = system(op.DofCount(), op.Bandwidth(), static_cast<long long>(bands.size()), 2 * degrees[l].torRhs,
-                    2 * (l + 1), torScale[l]);
-    if (!op.Pinned().empty()) s.pinned0 = op.Pinned()[0];
-    if (op.Pinned().size() > 1) s.pinned1 = op.Pinned()[1];
-    if (op.Pinned().size() > 2) {
-      SetError("v3d: more than two solid regions");
-      return SL3DGPU_ERR_ARGUMENT;
-    }
-    chol.push_back(s);
-    bands.insert(bands.end(), b.begin(), b.end());
-    cholDegree.push_back(l);
-    cholKind.push_back(1);
-  }
-  if (options.solver == 1 && &f != elastic.get()) {
-    // K x for conjugate gradients: the assembled upper bands, spheroidal
-    // degrees then toroidal, with their systems (right-hand sides in the
-    // combined spheroidal-then-toroidal columns).
-    std::vector<double> applyBands;
-    std::vector<sl3dgpu_band_system> sphApply, torApply;
-    int rows = 0;
-    for (int l = 0; l <= L; ++l) {
-      const auto& op = *sph[l];
-      sphApply.push_back(system(op.DofCount(), op.Bandwidth(), static_cast<long long>(applyBands.size()),
-                                2 * degrees[l].sphRhs, 2 * (l + 1), -1));
-      applyBands.insert(applyBands.end(), op.Band().begin(), op.Band().end());
-      rows = std::max(rows, op.DofCount());
-    }
-    for (int l = 1; l <= L; ++l) {
-      const auto& op = *tor[l];
-      torApply.push_back(system(op.DofCount(), op.Bandwidth(), static_cast<long long>(applyBands.size()),
-                                2 * (rhsSphComplex + degrees[l].torRhs), 2 * (l + 1), -1));
-      applyBands.insert(applyBands.end(), op.Band().begin(), op.Band().end());
-      rows = std::max(rows, op.DofCount());
-    }
-    SL3D_CUDA(f.applyBands.Upload(applyBands));
-    SL3D_CUDA(f.dSphApply.Upload(sphApply));
-    SL3D_CUDA(f.dTorApply.Upload(torApply));
-    f.nSphApply = static_cast<int>(sphApply.size());
-    f.nTorApply = static_cast<int>(torApply.size());
-    f.maxApplyRows = rows;
-  }
-  // Factor the Cholesky candidates; the spheroidal failures fall back to LU.
-  Dev<double> dBands;
-  SL3D_CUDA(dBands.Upload(bands));
-  Dev<sl3dgpu_band_system> dChol;
-  SL3D_CUDA(dChol.Upload(chol));
-  Dev<int> info;
-  SL3D_CUDA(info.Alloc(chol.size()));
-  SL3D_TRY(BandFactorBatch(dChol.p, chol.data(), static_cast<int>(chol.size()), dBands.p, nullptr, info.p, 0, stream));
-  std::vector<int> hInfo(chol.size());
-  SL3D_CUDA(cudaMemcpyAsync(hInfo.data(), info.p, hInfo.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
-  SL3D_CUDA(cudaStreamSynchronize(stream));
-  std::vector<double> hostBands(bands.size());
-  SL3D_CUDA(cudaMemcpy(hostBands.data(), dBands.p, bands.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  std::vector<double> finalBands;
-  f.sphChol.clear();
-  f.sphLu.clear();
-  f.torChol.clear();
-  for (size_t i = 0; i < chol.size(); ++i) {
-    if (hInfo[i] != 0) {
-      if (cholKind[i] == 1) {
-        SetError("v3d: toroidal degree " + std::to_string(cholDegree[i]) + ": Cholesky failed");
-        return SL3DGPU_ERR_RUNTIME;
-      }
-      luDegree.push_back(cholDegree[i]);
-      continue;
-    }
-    auto s = chol[i];
-    const size_t len = static_cast<size_t>(s.ku + 1) * s.n;
-    const long long at = static_cast<long long>(finalBands.size());
-    finalBands.insert(finalBands.end(), hostBands.begin() + s.band, hostBands.begin() + s.band + len);
-    s.band = at;
-    (cholKind[i] == 0 ? f.sphChol : f.torChol).push_back(s);
-  }
-  std::sort(luDegree.begin(), luDegree.end());
-  std::vector<int> pivots;
-  if (!luDegree.empty()) {
-    std::vector<double> luBands;
-    std::vector<sl3dgpu_band_system> luSys;
-    for (int l : luDegree) {
-      const auto& op = *sph[l];
-      auto s = system(op.DofCount(), op.Bandwidth(), static_cast<long long>(luBands.size()), 2 * degrees[l].sphRhs,
-                      2 * (l + 1), sphScale[l]);
-      s.pivots = static_cast<long long>(pivots.size());
-      pivots.resize(pivots.size() + op.DofCount());
-      const auto b = op.ScaledLuBand();
-      luBands.insert(luBands.end(), b.begin(), b.end());
-      luSys.push_back(s);
-    }
-    Dev<double> dLu;
-    SL3D_CUDA(dLu.Upload(luBands));
-    Dev<sl3dgpu_band_system> dLuSys;
-    SL3D_CUDA(dLuSys.Upload(luSys));
-    Dev<int> dPiv, luInfo;
-    SL3D_CUDA(dPiv.Alloc(pivots.size()));
-    SL3D_CUDA(luInfo.Alloc(luSys.size()));
-    SL3D_TRY(BandFactorBatch(dLuSys.p, luSys.data(), static_cast<int>(luSys.size()), dLu.p, dPiv.p, luInfo.p, 1, stream));
-    std::vector<int> hLuInfo(luSys.size());
-    SL3D_CUDA(cudaMemcpy(hLuInfo.data(), luInfo.p, hLuInfo.size() * sizeof(int), cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < luSys.size(); ++i)
-      if (hLuInfo[i] != 0) {
-        SetError("v3d: degree " + std::to_string(luDegree[i]) + ": the banded LU factorisation failed (info = " +
-                 std::to_string(hLuInfo[i]) + ")");
-        return SL3DGPU_ERR_RUNTIME;
-      }
-    SL3D_CUDA(cudaMemcpy(luBands.data(), dLu.p, luBands.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    SL3D_CUDA(cudaMemcpy(pivots.data(), dPiv.p, pivots.size() * sizeof(int), cudaMemcpyDeviceToHost));
-    for (auto s : luSys) {
-      const size_t len = static_cast<size_t>(3 * s.ku + 1) * s.n;
-      const long long at = static_cast<long long>(finalBands.size());
-      finalBands.insert(finalBands.end(), luBands.begin() + s.band, luBands.begin() + s.band + len);
-      s.band = at;
-      f.sphLu.push_back(s);
-    }
-  }
-  SL3D_CUDA(f.bands.Upload(finalBands));
-  SL3D_CUDA(f.scales.Upload(scales));
-  SL3D_CUDA(f.pivots.Upload(pivots.empty() ? std::vector<int>{0} : pivots));
-  auto upload = [&](const std::vector<sl3dgpu_band_system>& sys, Dev<sl3dgpu_band_system>& d, Dev<int2>& items,
-                    int& count) -> int {
-    SL3D_CUDA(d.Upload(sys));
-    const auto list = BandWorkItems(sys.data(), static_cast<int>(sys.size()));
-    SL3D_CUDA(items.Upload(list));
-    count = static_cast<int>(list.size());
-    return SL3DGPU_OK;
-  };
-  SL3D_TRY(upload(f.sphChol, f.dSphChol, f.iSphChol, f.nSphChol));
-  SL3D_TRY(upload(f.sphLu, f.dSphLu, f.iSphLu, f.nSphLu));
-  SL3D_TRY(upload(f.torChol, f.dTorChol, f.iTorChol, f.nTorChol));
-  // The load units K^-1 Load per degree (AddUnitChannels' cached responses).
-  std::vector<double> units;
-  std::vector<long long> unitOffset(L + 1);
-  for (int l = 0; l <= L; ++l) {
-    unitOffset[l] = static_cast<long long>(units.size());
-    const auto load = sph[l]->Load();
-    units.insert(units.end(), load.begin(), load.end());
-  }
-  SL3D_CUDA(f.units.Upload(units));
-  SL3D_CUDA(f.unitOffset.Upload(unitOffset));
-  if (options.solver == 1) SL3D_CUDA(f.loadForces.Upload(units));  // before the solve turns them into responses
-  auto unitSystems = [&](const std::vector<sl3dgpu_band_system>& src) {
-    std::vector<sl3dgpu_band_system> out;
-    for (auto s : src) {
-      // the system's degree from its right-hand-side offset
-      int l = 0;
-      while (l < L && 2 * degrees[l + 1].sphRhs <= s.rhs) ++l;
-      s.rhs = unitOffset[l];
-      s.nrhs = 1;
-      out.push_back(s);
-    }
-    return out;
-  };
-  for (int lu = 0; lu < 2; ++lu) {
-    const auto sys = unitSystems(lu ? f.sphLu : f.sphChol);
-    if (sys.empty()) continue;
-    Dev<sl3dgpu_band_system> d;
-    Dev<int2> items;
-    int count = 0;
-    SL3D_TRY(upload(sys, d, items, count));
-    SL3D_TRY(BandSolveBatch(d.p, sys.data(), static_cast<int>(sys.size()), items.p, count, f.bands.p, f.pivots.p,
-                            f.units.p, f.scales.p, lu, stream));
-    SL3D_CUDA(cudaStreamSynchronize(stream));
-  }
-  if (options.precision == 1 && &f != elastic.get()) {
-    // The FP64 factors and scales rounded to FP32 for the correction passes.
-    SL3D_CUDA(f.bands32.Alloc(f.bands.n));
-    SL3D_CUDA(f.scales32.Alloc(f.scales.n));
-    LaunchCast(static_cast<long long>(f.bands.n), f.bands.p, f.bands32.p, stream);
-    SL3D_CHECK_LAUNCH();
-    LaunchCast(static_cast<long long>(f.scales.n), f.scales.p, f.scales32.p, stream);
-    SL3D_CHECK_LAUNCH();
-    SL3D_CUDA(cudaStreamSynchronize(stream));
-  }
-  return SL3DGPU_OK;
+  SystemsInput in;
+  in.nodal = staticMode ? material.get() : &reference->nodal;
+  in.shear = staticMode ? nullptr : &shear;
+  in.lmax = options.lmax;
+  in.eps = options.eps;
+  in.degrees = &degrees;
+  in.rhsSphComplex = rhsSphComplex;
+  const bool stepFlavour = &f != elastic.get();
+  in.apply = (options.solver == 1 && stepFlavour) || staticMode;
+  in.fp32 = options.precision == 1 && stepFlavour;
+  in.stream = stream;
+  return BuildSystems(in, f);
 }
 
 int Viscoelastic3DGpu::FlavourOf(int scheme, double dt, Flavour** out) {
@@ -1283,9 +1026,9 @@ int Viscoelastic3DGpu::ApplyOperator(const Flavour& f, const double2* x, double2
   SL3D_TRY(LateralForce(x, out));
   const auto* xd = reinterpret_cast<const double*>(x);
   auto* od = reinterpret_cast<double*>(out);
-  LaunchBandApply(f.dSphApply.p, f.nSphApply, f.maxApplyRows, f.applyBands.p, xd, od, true, stream);
+  LaunchBandApply(f.dSphApply.p, f.nSphApply, f.maxApplyRows, f.applyBands.p, xd, od, -1.0, stream);
   SL3D_CHECK_LAUNCH();
-  LaunchBandApply(f.dTorApply.p, f.nTorApply, f.maxApplyRows, f.applyBands.p, xd, od, true, stream);
+  LaunchBandApply(f.dTorApply.p, f.nTorApply, f.maxApplyRows, f.applyBands.p, xd, od, -1.0, stream);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
@@ -1300,12 +1043,13 @@ int Viscoelastic3DGpu::PairOf(const double2* a, const double2* b, double* out) {
   return SL3DGPU_OK;
 }
 
-// The step closed by preconditioned conjugate gradients (Viscoelastic3D.cpp
-// :2008-2015; detail/LateralSolve.hpp:112-181): forces of the fixed memory
-// and the load channel, the solve from the reference response, the strain
-// of the solution.
-int Viscoelastic3DGpu::ConvergeConjugateGradients(const Flavour& f, const double2* sigmaEnd,
-                                                  sl3dgpu_step_info& info) {
+// Preconditioned conjugate gradients (detail/LateralSolve.hpp:112-181, no
+// start, reduction 0) on the forces in cgF into cgX: the reference response
+// first, then the iteration on K x - LateralForce(x) (the step) or
+// K x + (dK) x (the static perturbation problem), the reference solves as
+// the preconditioner. `lateral` false stops at the reference response.
+int Viscoelastic3DGpu::ConjugateGradients(const Flavour& f, bool lateral, double rtol, int maxIterations,
+                                          sl3dgpu_step_info& info) {
   const long long n = 2 * Columns();
   auto* F = reinterpret_cast<double*>(cgF.p);
   auto* X = reinterpret_cast<double*>(cgX.p);
@@ -1313,14 +1057,9 @@ int Viscoelastic3DGpu::ConvergeConjugateGradients(const Flavour& f, const double
   auto* Z = reinterpret_cast<double*>(cgZ.p);
   auto* Pd = reinterpret_cast<double*>(cgP.p);
   auto* AP = reinterpret_cast<double*>(cgAp.p);
-  // OpenStep::Forces: the fixed memory force, plus the load's force vectors.
-  SL3D_CUDA(cudaMemsetAsync(cgF.p, 0, Columns() * sizeof(double2), stream));
-  LaunchForces(geo, fixedS.p, cgF.p, cgF.p + rhsSphComplex, stream);
-  SL3D_CHECK_LAUNCH();
-  if (sigmaEnd != nullptr) {
-    LaunchAddLoad(geo, sigmaEnd, f.loadForces.p, f.unitOffset.p, cgF.p, stream);
-    SL3D_CHECK_LAUNCH();
-  }
+  auto apply = [&](const double2* x, double2* out) {
+    return staticMode ? ApplyPerturbed(f, x, out) : ApplyOperator(f, x, out);
+  };
   // x = K^-1 f, the reference response; energy = <x, f>.
   SL3D_CUDA(cudaMemcpyAsync(cgX.p, cgF.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
   SL3D_TRY(SolveColumns(f, cgX.p, cgX.p + rhsSphComplex));
@@ -1330,51 +1069,207 @@ int Viscoelastic3DGpu::ConvergeConjugateGradients(const Flavour& f, const double
     return energy > 0.0 ? std::sqrt(std::abs(value) / energy) : std::sqrt(std::abs(value));
   };
   info.converged = 0;
-  {  // the reference iterates whether or not the weight vanishes (OpenStep::Solve: lateral = true)
-    // r = f - A x, z = M^-1 r, p = z.
-    SL3D_TRY(ApplyOperator(f, cgX.p, cgAp.p));
-    LaunchSub(n, F, AP, R, stream);
+  info.solve_iterations = 0;
+  if (!lateral) {
+    info.converged = 1;
+    info.residual = 0.0;
+    history.push_back(0.0);
+    return SL3DGPU_OK;
+  }
+  // r = f - A x, z = M^-1 r, p = z.
+  SL3D_TRY(apply(cgX.p, cgAp.p));
+  LaunchSub(n, F, AP, R, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_CUDA(cudaMemcpyAsync(cgZ.p, cgR.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_TRY(SolveColumns(f, cgZ.p, cgZ.p + rhsSphComplex));
+  double rz = 0.0;
+  SL3D_TRY(PairOf(cgZ.p, cgR.p, &rz));
+  info.residual = relative(rz);
+  history.push_back(info.residual);
+  SL3D_CUDA(cudaMemcpyAsync(cgP.p, cgZ.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  for (int iteration = 0; iteration < maxIterations; ++iteration) {
+    if (info.residual <= rtol) break;
+    SL3D_TRY(apply(cgP.p, cgAp.p));
+    double curvature = 0.0;
+    SL3D_TRY(PairOf(cgP.p, cgAp.p, &curvature));
+    const double alpha = rz / curvature;
+    LaunchAxpy(n, alpha, Pd, X, stream);
+    LaunchAxpy(n, -alpha, AP, R, stream);
     SL3D_CHECK_LAUNCH();
     SL3D_CUDA(cudaMemcpyAsync(cgZ.p, cgR.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
     SL3D_TRY(SolveColumns(f, cgZ.p, cgZ.p + rhsSphComplex));
-    double rz = 0.0;
-    SL3D_TRY(PairOf(cgZ.p, cgR.p, &rz));
+    double next = 0.0;
+    SL3D_TRY(PairOf(cgZ.p, cgR.p, &next));
+    const double beta = next / rz;
+    rz = next;
+    LaunchXpby(n, Z, beta, Pd, stream);
+    SL3D_CHECK_LAUNCH();
+    info.solve_iterations = iteration + 1;
     info.residual = relative(rz);
     history.push_back(info.residual);
-    const double target = options.solve_rtol;
-    SL3D_CUDA(cudaMemcpyAsync(cgP.p, cgZ.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
-    for (int iteration = 0; iteration < options.solve_max_iterations; ++iteration) {
-      if (info.residual <= target) break;
-      SL3D_TRY(ApplyOperator(f, cgP.p, cgAp.p));
-      double curvature = 0.0;
-      SL3D_TRY(PairOf(cgP.p, cgAp.p, &curvature));
-      const double alpha = rz / curvature;
-      LaunchAxpy(n, alpha, Pd, X, stream);
-      LaunchAxpy(n, -alpha, AP, R, stream);
-      SL3D_CHECK_LAUNCH();
-      SL3D_CUDA(cudaMemcpyAsync(cgZ.p, cgR.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
-      SL3D_TRY(SolveColumns(f, cgZ.p, cgZ.p + rhsSphComplex));
-      double next = 0.0;
-      SL3D_TRY(PairOf(cgZ.p, cgR.p, &next));
-      const double beta = next / rz;
-      rz = next;
-      LaunchXpby(n, Z, beta, Pd, stream);
-      SL3D_CHECK_LAUNCH();
-      info.solve_iterations = iteration + 1;
-      info.residual = relative(rz);
-      history.push_back(info.residual);
-    }
-    if (info.residual <= target) info.converged = 1;
   }
-  info.iterations = info.solve_iterations;
-  // The solutions (for Surface) and their strain.
-  SL3D_CUDA(cudaMemcpyAsync(rhsSph.p, cgX.p, rhsSphComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  if (info.residual <= rtol) info.converged = 1;
+  return SL3DGPU_OK;
+}
+
+// The solutions x (combined columns) as the operator's held solution, the
+// one Surface reads.
+int Viscoelastic3DGpu::HoldSolution(const double2* x) {
+  SL3D_CUDA(cudaMemcpyAsync(rhsSph.p, x, rhsSphComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
   if (rhsTorComplex > 0)
-    SL3D_CUDA(cudaMemcpyAsync(rhsTor.p, cgX.p + rhsSphComplex, rhsTorComplex * sizeof(double2),
-                              cudaMemcpyDeviceToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(rhsTor.p, x + rhsSphComplex, rhsTorComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                              stream));
+  return SL3DGPU_OK;
+}
+
+// The step closed by preconditioned conjugate gradients (Viscoelastic3D.cpp
+// :2008-2015): forces of the fixed memory and the load channel
+// (OpenStep::Forces), the solve (OpenStep::Solve, lateral always), the
+// strain of the solution.
+int Viscoelastic3DGpu::ConvergeConjugateGradients(const Flavour& f, const double2* sigmaEnd,
+                                                  sl3dgpu_step_info& info) {
+  SL3D_CUDA(cudaMemsetAsync(cgF.p, 0, Columns() * sizeof(double2), stream));
+  LaunchForces(geo, fixedS.p, cgF.p, cgF.p + rhsSphComplex, stream);
+  SL3D_CHECK_LAUNCH();
+  if (sigmaEnd != nullptr) {
+    LaunchAddLoad(geo, sigmaEnd, f.loadForces.p, f.unitOffset.p, cgF.p, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  SL3D_TRY(ConjugateGradients(f, true, options.solve_rtol, options.solve_max_iterations, info));
+  info.iterations = info.solve_iterations;
+  SL3D_TRY(HoldSolution(cgX.p));
   LaunchStrain(geo, rhsSph.p, rhsTor.p, s.p, stream);
   SL3D_CHECK_LAUNCH();
-  (void)Z;
+  return SL3DGPU_OK;
+}
+
+// -- the static perturbation problem (ElasticPerturbation3D) ----------------------------------------
+
+// The moduli directions over the grid values (node-major, colatitude,
+// longitude), either null; the transforms then run over the nodes where
+// one of them is non-zero.
+int Viscoelastic3DGpu::SetModuli(const double* dMu, const double* dKappa, bool onDevice) {
+  if (!staticMode) {
+    SetError("ep3d: not a static perturbation operator");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  hasMu = dMu != nullptr;
+  hasKappa = dKappa != nullptr;
+  std::vector<double> host(values);
+  std::vector<char> lateral(P, 0);
+  auto take = [&](const double* src, Dev<double>& dst) -> int {
+    if (src == nullptr) {
+      SL3D_CUDA(cudaMemset(dst.p, 0, values * sizeof(double)));
+      return SL3DGPU_OK;
+    }
+    if (onDevice) {
+      SL3D_CUDA(cudaMemcpy(host.data(), src, values * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+      std::memcpy(host.data(), src, values * sizeof(double));
+    }
+    for (int p = 0; p < P; ++p)
+      for (long long x = p * fieldSize; x < (p + 1) * fieldSize && !lateral[p]; ++x) lateral[p] = host[x] != 0.0;
+    SL3D_CUDA(cudaMemcpy(dst.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
+    return SL3DGPU_OK;
+  };
+  SL3D_TRY(take(dMu, weight));
+  SL3D_TRY(take(dKappa, kappaWeight));
+  int first = P, last = -1;
+  for (int p = 0; p < P; ++p)
+    if (lateral[p]) {
+      first = std::min(first, p);
+      last = std::max(last, p);
+    }
+  lateralFirst = last >= 0 ? first : 0;
+  lateralEnd = last >= 0 ? last + 1 : 0;
+  return SL3DGPU_OK;
+}
+
+// (dK) x (ElasticPerturbation3D::Force, src/ElasticPerturbation3D.cpp:140-
+// 226): the deviatoric strain weighted by dMu back as force, plus the
+// dilatation weighted by dKappa back as force.
+int Viscoelastic3DGpu::PerturbationForce(const double2* x, double2* out) {
+  SL3D_CUDA(cudaMemsetAsync(out, 0, Columns() * sizeof(double2), stream));
+  if (hasMu) {
+    LaunchStrain(geo, x, x + rhsSphComplex, sNext.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemsetAsync(analysed.p, 0, spectralComplex * sizeof(double2), stream));
+    SL3D_TRY(WeightedPass(sNext.p, analysed.p));
+    LaunchForces(geo, analysed.p, out, out + rhsSphComplex, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  if (hasKappa) {
+    LaunchDilatation(geo, x, scalarD.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemsetAsync(scalarW.p, 0, rowsR * P * sizeof(double2), stream));
+    const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+    if (count > 0) {
+      auto* a = reinterpret_cast<double*>(spectraA.p);
+      auto* b = reinterpret_cast<double*>(spectraB.p);
+      SL3D_TRY(grid->LegendreSynthesis(0, true, reinterpret_cast<const double*>(scalarD.p), P, p0, count, a, stream));
+      SL3D_TRY(grid->RingWeighted(true, a, count, kappaWeight.p + p0 * fieldSize, b, stream));
+      SL3D_TRY(grid->LegendreAnalysis(0, true, b, P, p0, count, reinterpret_cast<double*>(scalarW.p), false, stream));
+    }
+    LaunchDilatationForce(geo, scalarW.p, out, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  return SL3DGPU_OK;
+}
+
+// (K_ref + dK) x (ElasticPerturbation3D::Apply, :305-338).
+int Viscoelastic3DGpu::ApplyPerturbed(const Flavour& f, const double2* x, double2* out) {
+  SL3D_TRY(PerturbationForce(x, out));
+  const auto* xd = reinterpret_cast<const double*>(x);
+  auto* od = reinterpret_cast<double*>(out);
+  LaunchBandApply(f.dSphApply.p, f.nSphApply, f.maxApplyRows, f.applyBands.p, xd, od, 1.0, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchBandApply(f.dTorApply.p, f.nTorApply, f.maxApplyRows, f.applyBands.p, xd, od, 1.0, stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+// SolveLoad (:98-126): per degree the unit load response times the load's
+// coefficients, held as the solution.
+int Viscoelastic3DGpu::SolveLoad(const double* load) {
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  SL3D_CUDA(cudaMemcpyAsync(sigma0.p, load, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+  SL3D_CUDA(cudaMemsetAsync(cgX.p, 0, Columns() * sizeof(double2), stream));
+  LaunchAddLoad(geo, sigma0.p, elastic->units.p, elastic->unitOffset.p, cgX.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(HoldSolution(cgX.p));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+// Respond (:474-479): the held solution x replaced by its first-order change
+// -K^-1 (dK) x.
+int Viscoelastic3DGpu::Respond() {
+  SL3D_TRY(PerturbationForce(cgX.p, cgF.p));
+  SL3D_TRY(SolveColumns(*elastic, cgF.p, cgF.p + rhsSphComplex));
+  SL3D_CUDA(cudaMemsetAsync(cgX.p, 0, Columns() * sizeof(double2), stream));
+  LaunchAxpy(2 * Columns(), -1.0, reinterpret_cast<const double*>(cgF.p), reinterpret_cast<double*>(cgX.p), stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(HoldSolution(cgX.p));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+// SolveLateral for a load (:367-372, :374-430): (K_ref + dK) x = LoadForces,
+// conjugate gradients from the reference response; lateral unless neither
+// direction was given.
+int Viscoelastic3DGpu::SolveLateral(const double* load, double rtol, int maxIterations, sl3dgpu_step_info* out) {
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  history.clear();
+  SL3D_CUDA(cudaMemcpyAsync(sigma0.p, load, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+  SL3D_CUDA(cudaMemsetAsync(cgF.p, 0, Columns() * sizeof(double2), stream));
+  LaunchAddLoad(geo, sigma0.p, elastic->loadForces.p, elastic->unitOffset.p, cgF.p, stream);
+  SL3D_CHECK_LAUNCH();
+  sl3dgpu_step_info info{};
+  SL3D_TRY(ConjugateGradients(*elastic, hasMu || hasKappa, rtol, maxIterations, info));
+  info.iterations = info.solve_iterations;
+  SL3D_TRY(HoldSolution(cgX.p));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  if (out) *out = info;
   return SL3DGPU_OK;
 }
 
@@ -1633,4 +1528,134 @@ extern "C" int sl3dgpu_standard_earth(int elements, double kelvin_fraction, doub
                            L.mu0, L.mu1, L.viscosity, L.kelvin_fraction, L.kelvin_viscosity};
   }
   return static_cast<int>(layers.size());
+}
+
+// -- the C ABI of the static perturbation problem ---------------------------------------------------
+
+struct sl3dgpu_ep3d {
+  Viscoelastic3DGpu op;
+};
+
+extern "C" int sl3dgpu_ep3d_create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_ep3d_options* options,
+                                   sl3dgpu_ep3d** out) {
+  if (layers == nullptr || options == nullptr || out == nullptr) {
+    SetError("ep3d: null layers, options or output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  sl3dgpu_v3d_options o{};
+  o.lmax = options->lmax;
+  o.ngll = options->ngll;
+  o.eps = options->eps;
+  o.oversampling = options->oversampling;
+  o.max_iterations = 1;
+  o.rtol = 1e-10;
+  o.damping = 1.0;
+  o.solver = 1;
+  o.solve_rtol = 1e-10;
+  o.solve_max_iterations = 200;
+  auto h = std::make_unique<sl3dgpu_ep3d>();
+  if (int st = h->op.Create(layers, nlayers, o, true); st != SL3DGPU_OK) return st;
+  *out = h.release();
+  return SL3DGPU_OK;
+}
+
+extern "C" void sl3dgpu_ep3d_destroy(sl3dgpu_ep3d* h) { delete h; }
+
+extern "C" int sl3dgpu_ep3d_shape(const sl3dgpu_ep3d* h, int* nodes, int* ntheta, int* nphi) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (nodes) *nodes = h->op.P;
+  if (ntheta) *ntheta = h->op.grid->ntheta;
+  if (nphi) *nphi = h->op.grid->nphi;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_ep3d_nodes(const sl3dgpu_ep3d* h, double* radius, int* element) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (int p = 0; p < h->op.P; ++p) {
+    if (radius) radius[p] = h->op.nodeR[p];
+    if (element) element[p] = h->op.nodeElement[p];
+  }
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_ep3d_colatitudes(const sl3dgpu_ep3d* h, double* theta, double* weights) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (int j = 0; j < h->op.grid->ntheta; ++j) {
+    if (theta) theta[j] = h->op.grid->theta[j];
+    if (weights) weights[j] = h->op.grid->weights[j];
+  }
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_ep3d_scales(const sl3dgpu_ep3d* h, double* length, double* modulus, double* surface_density) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& sc = h->op.earth->scales();
+  if (length) *length = sc.length;
+  if (modulus) *modulus = sc.Modulus();
+  if (surface_density) *surface_density = sc.SurfaceDensity();
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_ep3d_set_moduli(sl3dgpu_ep3d* h, const double* d_mu, const double* d_kappa, int on_device) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SetModuli(d_mu, d_kappa, on_device != 0);
+}
+
+extern "C" int sl3dgpu_ep3d_solve_load(sl3dgpu_ep3d* h, const double* load) {
+  if (h == nullptr || load == nullptr) {
+    SetError("ep3d: null handle or load");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SolveLoad(load);
+}
+
+extern "C" int sl3dgpu_ep3d_respond(sl3dgpu_ep3d* h) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Respond();
+}
+
+extern "C" int sl3dgpu_ep3d_solve_lateral(sl3dgpu_ep3d* h, const double* load, double rtol, int max_iterations,
+                                          sl3dgpu_step_info* info) {
+  if (h == nullptr || load == nullptr || !(rtol > 0.0) || max_iterations < 0) {
+    SetError("ep3d: null handle or load, rtol > 0, max_iterations >= 0");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SolveLateral(load, rtol, max_iterations, info);
+}
+
+extern "C" int sl3dgpu_ep3d_surface(sl3dgpu_ep3d* h, int component, double* out) {
+  if (h == nullptr || out == nullptr) {
+    SetError("ep3d: null handle or output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Surface(component, out);
+}
+
+extern "C" int sl3dgpu_ep3d_residual_history(const sl3dgpu_ep3d* h, double* out, int capacity) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& v = h->op.history;
+  if (out != nullptr)
+    for (int i = 0; i < capacity && i < static_cast<int>(v.size()); ++i) out[i] = v[i];
+  return static_cast<int>(v.size());
 }

@@ -248,6 +248,92 @@ __global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2*
   }
 }
 
+// One block per (l, m >= 0), as StrainKernel: the degree's U, V at its
+// carrying elements' GLL nodes in shared memory, then per memory node the
+// dilatation rdU + 2 U - l(l+1) V.
+__global__ void DilatationKernel(Geometry g, const double2* solSph, double2* scalar) {
+  int l, m;
+  DecodeLm(blockIdx.x, l, m);
+  const DegreeInfo d = g.degrees[l];
+  extern __shared__ __align__(16) unsigned char dilSmem[];
+  double2* vals = reinterpret_cast<double2*>(dilSmem);  // (lastGlobal - firstGlobal + 1) x 2
+  const int cols = l + 1;
+  const bool any = d.firstNode < g.P;
+  if (any)
+    for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
+      const int dU = g.sphMap[d.sphMap + 2LL * gn], dV = g.sphMap[d.sphMap + 2LL * gn + 1];
+      double2* v = vals + static_cast<long long>(gn - d.firstGlobal) * 2;
+      v[0] = dU >= 0 ? solSph[d.sphRhs + static_cast<long long>(dU) * cols + m] : C(0, 0);
+      v[1] = dV >= 0 ? solSph[d.sphRhs + static_cast<long long>(dV) * cols + m] : C(0, 0);
+    }
+  __syncthreads();
+  const int n = g.ngll;
+  const double k2 = l * (l + 1.0);
+  for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
+    double2 D = C(0, 0);
+    if (any && p >= d.firstNode) {
+      const int e = g.nodeElement[p], q = g.nodeQ[p];
+      const double r = g.nodeR[p], jac = g.elemJac[e];
+      double2 U = C(0, 0), V = C(0, 0), rdU = C(0, 0);
+      for (int i = 0; i < n; ++i) {
+        const double2* v = vals + static_cast<long long>(e * (n - 1) + i - d.firstGlobal) * 2;
+        const double val = g.pValue[q * n + i];
+        U = CAdd(U, CScale(val, v[0]));
+        V = CAdd(V, CScale(val, v[1]));
+        rdU = CAdd(rdU, CScale(r * g.pDeriv[q * n + i] / jac, v[0]));
+      }
+      D = CSub(CAdd(rdU, CScale(2.0, U)), CScale(k2, V));
+    }
+    scalar[RowR(g, l, m) * g.P + p] = D;
+  }
+}
+
+// One block per (l, m >= 0), as ForceKernel: per global node of the degree's
+// range, the quadrature over its elements' memory points of
+// 2 w jac D Value (U), -l(l+1) w jac D Value (V) and w Deriv r D (U),
+// added onto the right-hand side.
+__global__ void DilatationForceKernel(Geometry g, const double2* scalar, double2* rhsSph) {
+  int l, m;
+  DecodeLm(blockIdx.x, l, m);
+  const DegreeInfo d = g.degrees[l];
+  if (d.firstNode >= g.P) return;
+  extern __shared__ __align__(16) unsigned char dfSmem[];
+  double2* Ds = reinterpret_cast<double2*>(dfSmem);  // (P - first)
+  for (int p = d.firstNode + threadIdx.x; p < g.P; p += blockDim.x) Ds[p - d.firstNode] = scalar[RowR(g, l, m) * g.P + p];
+  __syncthreads();
+  const int n = g.ngll, cols = l + 1;
+  const double k2 = l * (l + 1.0);
+  for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
+    double2 bU = C(0, 0), bV = C(0, 0);
+    const int eHi = min(gn / (n - 1), g.elements - 1);
+    const int iHi = gn - eHi * (n - 1);
+    const int eLo = (iHi == 0 && eHi > 0) ? eHi - 1 : eHi;
+    for (int e = eLo; e <= eHi; ++e) {
+      const int fn = g.elemFirstNode[e];
+      if (fn < 0 || fn < d.firstNode) continue;
+      const int i = e == eHi ? iHi : n - 1;
+      const double jac = g.elemJac[e];
+      for (int q = 0; q < g.np; ++q) {
+        const int p = fn + q;
+        const double2 D = Ds[p - d.firstNode];
+        const double point = jac * g.pWeight[q] * g.pValue[q * n + i];
+        bU = CAdd(bU, CScale(2.0 * point, D));
+        bV = CSub(bV, CScale(k2 * point, D));
+        bU = CAdd(bU, CScale(g.pWeight[q] * g.pDeriv[q * n + i] * g.nodeR[p], D));
+      }
+    }
+    const int dU = g.sphMap[d.sphMap + 2LL * gn], dV = g.sphMap[d.sphMap + 2LL * gn + 1];
+    if (dU >= 0) {
+      double2& x = rhsSph[d.sphRhs + static_cast<long long>(dU) * cols + m];
+      x = CAdd(x, bU);
+    }
+    if (dV >= 0) {
+      double2& x = rhsSph[d.sphRhs + static_cast<long long>(dV) * cols + m];
+      x = CAdd(x, bV);
+    }
+  }
+}
+
 __global__ void AddLoadKernel(Geometry g, const double2* sigma, const double* units,
                               const long long* unitOffset, double2* sol) {
   const int l = blockIdx.x;
@@ -592,7 +678,7 @@ __global__ void MixerMixKernel(MixerArgsT<T> a) {
 // the row are broadcast reads, the x rows coalesced (and L1/L2 hits for the
 // neighbouring rows' warps).
 __global__ void BandApplyKernel(const sl3dgpu_band_system* systems, const double* bands, const double* x, double* y,
-                                bool subtract) {
+                                double keep) {
   const sl3dgpu_band_system s = systems[blockIdx.y];
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
   if (row >= s.n) return;
@@ -607,7 +693,7 @@ __global__ void BandApplyKernel(const sl3dgpu_band_system* systems, const double
       const int lo = min(row, j), hi = max(row, j);
       sum += band[static_cast<long long>(hi) * ld + kd + lo - hi] * xs[static_cast<long long>(j) * cols + c];
     }
-    ys[c] = subtract ? sum - ys[c] : sum;
+    ys[c] = keep == 0.0 ? sum : sum + keep * ys[c];
   }
 }
 
@@ -736,6 +822,22 @@ void LaunchStrain(const Geometry& g, const float2* solSph, const float2* solTor,
   Strain(g, solSph, solTor, spectral, stream);
 }
 
+void LaunchDilatation(const Geometry& g, const double2* solSph, double2* scalar, cudaStream_t stream) {
+  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 2 * sizeof(double2);
+  cudaFuncSetAttribute(DilatationKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  prof::Scope scope(prof::kStrain, stream);
+  DilatationKernel<<<count, 128, smem, stream>>>(g, solSph, scalar);
+}
+
+void LaunchDilatationForce(const Geometry& g, const double2* scalar, double2* rhsSph, cudaStream_t stream) {
+  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
+  const size_t smem = static_cast<size_t>(g.P) * sizeof(double2);
+  cudaFuncSetAttribute(DilatationForceKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  prof::Scope scope(prof::kForce, stream);
+  DilatationForceKernel<<<count, 128, smem, stream>>>(g, scalar, rhsSph);
+}
+
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units, const long long* unitOffset,
                    double2* solSph, cudaStream_t stream) {
   prof::Scope scope(prof::kOther, stream);
@@ -828,12 +930,12 @@ void LaunchMixerFirst(const MixerArgsT<float>& a, cudaStream_t stream) { MixerFi
 void LaunchMixerUpdate(const MixerArgsT<float>& a, cudaStream_t stream) { MixerUpdate(a, stream); }
 
 void LaunchBandApply(const sl3dgpu_band_system* devSystems, int count, int maxRows, const double* bands,
-                     const double* x, double* y, bool subtract, cudaStream_t stream) {
+                     const double* x, double* y, double keep, cudaStream_t stream) {
   if (count == 0 || maxRows == 0) return;
   constexpr int kRowsPerBlock = 8;
   prof::Scope scope(prof::kBandSolve, stream);
   BandApplyKernel<<<dim3((maxRows + kRowsPerBlock - 1) / kRowsPerBlock, count), kRowsPerBlock * 32, 0, stream>>>(
-      devSystems, bands, x, y, subtract);
+      devSystems, bands, x, y, keep);
 }
 
 void LaunchPair(const double2* a, const double2* b, const PairChunk* chunks, int count, double* partial,

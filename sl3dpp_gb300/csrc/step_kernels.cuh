@@ -54,6 +54,13 @@ void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTo
                   cudaStream_t stream);
 void LaunchStrain(const Geometry& g, const float2* solSph, const float2* solTor, float2* spectral,
                   cudaStream_t stream);
+// The dilatation companion (GridCoupling::AddDilatationOfSolution,
+// src/GridCoupling.cpp:359-398): D_lm = r dU/dr + 2 U - l(l+1) V per memory
+// node into a real spin-0 spectral block (rowsR x P), every (l, m >= 0).
+void LaunchDilatation(const Geometry& g, const double2* solSph, double2* scalar, cudaStream_t stream);
+// GridCoupling::DilatationForce (:433-495): a weighted dilatation's force
+// added onto every degree's spheroidal right-hand sides.
+void LaunchDilatationForce(const Geometry& g, const double2* scalar, double2* rhsSph, cudaStream_t stream);
 // x += sigma_lm K^-1 Load for every degree (AddUnitChannels' load part).
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units,
                    const long long* unitOffset, double2* solSph, cudaStream_t stream);
@@ -118,10 +125,11 @@ void LaunchCast(long long n, const double* in, float* out, cudaStream_t stream);
 // -- conjugate gradients (detail/LateralSolve.hpp:71-181) --------------------------------------
 
 // y = A x for a batch of symmetric band systems (upper storage, kd + 1 rows,
-// DegreeOperator::ApplyBand) on row-major right-hand sides; with
-// subtract, y = A x - y. systems[i].band and .rhs are element offsets.
+// DegreeOperator::ApplyBand) on row-major right-hand sides: y = A x +
+// keep y (keep 0, or -1 / +1 to take or add a force). systems[i].band and
+// .rhs are element offsets.
 void LaunchBandApply(const sl3dgpu_band_system* devSystems, int count, int maxRows, const double* bands,
-                     const double* x, double* y, bool subtract, cudaStream_t stream);
+                     const double* x, double* y, double keep, cudaStream_t stream);
 
 // A span of one degree's [dof][l + 1] complex block for the weighted pairing.
 struct PairChunk {

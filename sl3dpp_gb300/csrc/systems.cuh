@@ -1,0 +1,97 @@
+// The degree systems of one operator flavour on the device: the host
+// assembly of every degree's spheroidal and toroidal band (DegreeOperator,
+// ToroidalOperator), their batched factorisation on the GPU (Cholesky, LU
+// with partial pivoting where the Cholesky fails, src/DegreeOperator.cpp:
+// 775-852), the work items of the batched solves, the load units
+// K^-1 Load, and on request the assembled bands for K x and FP32 copies.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+#include "host/radial.hpp"
+#include "step_kernels.cuh"
+
+namespace sl3dgpu {
+
+int BandFactorBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                    double* bands, int* pivots, int* info, int lu, cudaStream_t stream);
+int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                   const int2* devItems, int itemCount, const double* bands, const int* pivots, double* rhs,
+                   const double* scales, int lu, cudaStream_t stream);
+int BandSolveBatchF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                    const int2* devItems, int itemCount, const float* bands, const int* pivots, float* rhs,
+                    const float* scales, int lu, cudaStream_t stream);
+std::vector<int2> BandWorkItems(const sl3dgpu_band_system* hostSystems, int count);
+
+// A device allocation owned by value.
+template <class T>
+struct Dev {
+  T* p = nullptr;
+  size_t n = 0;
+  Dev() = default;
+  Dev(const Dev&) = delete;
+  Dev& operator=(const Dev&) = delete;
+  Dev(Dev&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  Dev& operator=(Dev&& o) noexcept {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+    return *this;
+  }
+  ~Dev() { cudaFree(p); }
+  cudaError_t Alloc(size_t count) {
+    cudaFree(p);
+    p = nullptr;
+    n = count;
+    return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+  }
+  cudaError_t Upload(const std::vector<T>& v) {
+    if (cudaError_t e = Alloc(v.size()); e != cudaSuccess) return e;
+    return v.empty() ? cudaSuccess : cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+
+#define SL3D_TRY(expr)                            \
+  do {                                            \
+    if (int _st = (expr); _st != SL3DGPU_OK) return _st; \
+  } while (0)
+
+// One flavour (scheme, dt): the factorised systems and the load units.
+struct Flavour {
+  int scheme = 0;
+  double dt = 0.0;
+  Dev<double> bands, scales, units;
+  Dev<float> bands32, scales32;  // the mixed form's FP32 copies
+  // conjugate gradients: the assembled (unscaled) bands for K x, their
+  // systems, and the unsolved load force vectors (DegreeOperator::Load)
+  Dev<double> applyBands, loadForces;
+  Dev<sl3dgpu_band_system> dSphApply, dTorApply;
+  int nSphApply = 0, nTorApply = 0, maxApplyRows = 0;
+  Dev<int> pivots;
+  Dev<long long> unitOffset;
+  std::vector<sl3dgpu_band_system> sphChol, sphLu, torChol;
+  Dev<sl3dgpu_band_system> dSphChol, dSphLu, dTorChol;
+  Dev<int2> iSphChol, iSphLu, iTorChol;
+  int nSphChol = 0, nSphLu = 0, nTorChol = 0;
+};
+
+
+// What a flavour is built from: the nodal material and its point shear (null
+// for the plain elastic operators), the degrees' right-hand-side layout.
+struct SystemsInput {
+  const host::Material* nodal = nullptr;
+  const host::PointShear* shear = nullptr;
+  int lmax = 0;
+  double eps = 1e-8;
+  const std::vector<DegreeInfo>* degrees = nullptr;
+  long long rhsSphComplex = 0;  // where the toroidal columns start in a combined vector
+  bool apply = false;           // keep the assembled bands and load vectors (K x, conjugate gradients)
+  bool fp32 = false;            // FP32 copies of the factors (the mixed form)
+  cudaStream_t stream = nullptr;
+};
+int BuildSystems(const SystemsInput& in, Flavour& f);
+
+}  // namespace sl3dgpu

@@ -160,6 +160,11 @@ def default_options(lmax, ngll=5, **kw):
     return o
 
 
+class EpOptions(_ct.Structure):
+    """sl3dgpu_ep3d_options (include/sl3dgpu.h)."""
+    _fields_ = [("lmax", _ct.c_int), ("ngll", _ct.c_int), ("eps", _ct.c_double), ("oversampling", _ct.c_double)]
+
+
 def _v3d_sigs(L):
     v, i, d = _ct.c_void_p, _ct.c_int, _ct.c_double
     sig = {
@@ -180,6 +185,12 @@ def _v3d_sigs(L):
         "oracle_v3d_residual_history": (i, [v, P_double, i]),
         "oracle_v3d_sample": (i, [v, v, d, v, v, i, P_double, P_double]),
         "oracle_threads": (i, []),
+        "oracle_ep3d_create": (v, [_ct.POINTER(Layer), i, _ct.POINTER(EpOptions)]),
+        "oracle_v3d_modulus_scale": (d, [v]),
+        "oracle_ep3d_set_moduli": (None, [v, v, v]),
+        "oracle_ep3d_solve_load": (None, [v, v]),
+        "oracle_ep3d_respond": (None, [v]),
+        "oracle_ep3d_solve_lateral": (i, [v, v, d, i, _ct.POINTER(StepInfo)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -261,3 +272,46 @@ class OracleStep:
         out = np.zeros((L + 1) * (L + 2) // 2, dtype=np.complex128)
         self.L.oracle_v3d_surface(self.h, component, out.ctypes.data)
         return out
+
+
+class OraclePerturbation(OracleStep):
+    """The oracle's ElasticPerturbation3D (CPU FP64): the static problem under
+    lateral moduli perturbations on the GLL nodes of the solid elements."""
+
+    def __init__(self, layers, lmax, ngll=5, eps=1e-8, oversampling=1.5):
+        self.L = load()
+        _v3d_sigs(self.L)
+        self.options = default_options(lmax, ngll)
+        self.h = self.L.oracle_ep3d_create(layers, len(layers), _ct.byref(EpOptions(lmax, ngll, eps, oversampling)))
+        self.P = self.L.oracle_v3d_node_count(self.h)
+        nt, nph = _ct.c_int(), _ct.c_int()
+        self.L.oracle_v3d_grid(self.h, _ct.byref(nt), _ct.byref(nph), None, None)
+        self.ntheta, self.nphi = nt.value, nph.value
+        self.theta = np.empty(self.ntheta)
+        self.weights = np.empty(self.ntheta)
+        self.L.oracle_v3d_grid(self.h, None, None, ptr(self.theta), ptr(self.weights))
+        self.radius = np.empty(self.P)
+        self.element = np.empty(self.P, dtype=np.int32)
+        self.L.oracle_v3d_nodes(self.h, ptr(self.radius), ptr(self.element))
+        self.sigma_scale = self.L.oracle_v3d_surface_density_scale(self.h)
+        self.modulus_scale = self.L.oracle_v3d_modulus_scale(self.h)
+        self.state = self.L.oracle_v3d_zero_state(self.h)
+        self._keep = []
+
+    def set_moduli(self, d_mu=None, d_kappa=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (d_mu, d_kappa)]
+        self._keep = arrs
+        self.L.oracle_ep3d_set_moduli(self.h, *(None if a is None else a.ctypes.data for a in arrs))
+
+    def solve_load(self, load):
+        load = np.ascontiguousarray(load, dtype=np.complex128)
+        self.L.oracle_ep3d_solve_load(self.h, load.ctypes.data)
+
+    def respond(self):
+        self.L.oracle_ep3d_respond(self.h)
+
+    def solve_lateral(self, load, rtol=1e-10, max_iterations=200):
+        load = np.ascontiguousarray(load, dtype=np.complex128)
+        info = StepInfo()
+        self.L.oracle_ep3d_solve_lateral(self.h, load.ctypes.data, rtol, max_iterations, _ct.byref(info))
+        return info
