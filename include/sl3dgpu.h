@@ -253,6 +253,32 @@ int sl3dgpu_v3d_step_device(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt
  * solutions: component 0 U, 1 V, 2 phi; complex m >= 0 columns per degree in
  * the l(l+1)/2 + m layout, into host memory. */
 int sl3dgpu_v3d_surface(sl3dgpu_v3d* op, int component, double* out);
+/* The warm-start hook (OpenStep::Converge's start, Viscoelastic3D.hpp:562-569):
+ * a guess of the strain coefficients at the end of the NEXT step, in the
+ * device layout a state's coefficients have (sl3dgpu_v3d_state_coefficients;
+ * 2 x spectral-size doubles, host or device). The step's last stage runs its
+ * first pass from both the plain start (the previous strain) and the guess
+ * and continues from the one with the smaller relative change, so a guess can
+ * cost a pass but never accuracy. NULL disarms; a guess serves one step. No
+ * reference counterpart for the choice (the reference takes the start as
+ * given). */
+int sl3dgpu_v3d_set_start(sl3dgpu_v3d* op, const double* coefficients, int on_device);
+/* Whether the last step kept its warm start (1) or discarded it (0). */
+int sl3dgpu_v3d_start_taken(const sl3dgpu_v3d* op);
+/* A state's strain coefficients in the device layout: their device address
+ * (NULL before a step) and their count of doubles. */
+int sl3dgpu_v3d_state_coefficients(const sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, const double** device,
+                                   long long* count);
+/* The same coefficients copied to a host array (count doubles). */
+int sl3dgpu_v3d_state_coefficients_host(const sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, double* out);
+/* Evolution3D::Run (src/Evolution3D.cpp:184-394) for a body without an ocean
+ * and without rotational feedback (GRDSolver::NoOceanState): node 0 the
+ * instantaneous elastic response to loads[0] (a dt = 0 step), then one step
+ * per node under the loads at its two ends. loads: nodes x (l(l+1)/2 + m)
+ * complex host coefficients; u, phi (nullable): the surface U and phi per
+ * node in the same layout; infos (nullable): each node's step info. */
+int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* times, int nodes, int scheme,
+                    const double* loads, double* u, double* phi, sl3dgpu_step_info* infos);
 /* The CUDA stream the operator's kernels run on. */
 void* sl3dgpu_v3d_stream(const sl3dgpu_v3d* op);
 /* The last step's pass residuals (RelativeChange per pass, the stages in

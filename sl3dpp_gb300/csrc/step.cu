@@ -144,6 +144,14 @@ class Viscoelastic3DGpu {
   Dev<double2> scalarD, scalarW;
   bool hasMu = false, hasKappa = false;
 
+  // The warm-start hook (Converge's start argument): a caller's guess of the
+  // strain coefficients at the end of the next step, tried against the plain
+  // start (the previous strain) on the step's last stage and kept only if its
+  // first residual is the smaller.
+  Dev<double2> guess, guessNext;
+  bool guessArmed = false, guessStage = false;
+  int guessTaken = 0;  // the last step: 1 when the guess was kept
+
   V3dState scratch;  // the second buffer set a step writes into
   std::vector<double> history;  // the last step's pass residuals, stages in turn
 
@@ -160,6 +168,11 @@ class Viscoelastic3DGpu {
   int SolveLoad(const double* load);
   int Respond();
   int SolveLateral(const double* load, double rtol, int maxIterations, sl3dgpu_step_info* info);
+  // The warm start of the next step (device layout of a state's coefficients).
+  int SetStart(const double* coefficients, bool onDevice);
+  // Evolution3D::Run without ocean or rotation: the march over the node times.
+  int Run(V3dState& st, const double* times, int nodes, int scheme, const double* loads, double* u, double* phi,
+          sl3dgpu_step_info* infos);
   int SetDelta(const double* samples, bool onDevice);
   int ZeroState(V3dState& st);
   int Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1, sl3dgpu_step_info* info,
@@ -191,6 +204,7 @@ class Viscoelastic3DGpu {
   int PairOf(const double2* a, const double2* b, double* out);
   int ConvergeConjugateGradients(const Flavour& f, const double2* sigmaEnd, sl3dgpu_step_info& info);
   int ConjugateGradients(const Flavour& f, bool lateral, double rtol, int maxIterations, sl3dgpu_step_info& info);
+  int FirstPass(const Flavour& f, const double2* sigmaEnd, double* residual);
   int PerturbationForce(const double2* x, double2* out);
   int ApplyPerturbed(const Flavour& f, const double2* x, double2* out);
   int HoldSolution(const double2* x);
@@ -793,9 +807,13 @@ int Viscoelastic3DGpu::Converge(const Flavour& f, const double2* sigmaEnd, sl3dg
   if (mixing) SL3D_TRY(MixerReset());
   double previous = 0.0;
   for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
-    SL3D_TRY(Pass(f, s.p, iteration == 0, sigmaEnd, sNext.p));
     double residual = 0.0;
-    SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
+    if (iteration == 0) {
+      SL3D_TRY(FirstPass(f, sigmaEnd, &residual));
+    } else {
+      SL3D_TRY(Pass(f, s.p, false, sigmaEnd, sNext.p));
+      SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
+    }
     history.push_back(residual);
     info.iterations = iteration + 1;
     info.residual = residual;
@@ -835,9 +853,13 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
     return SL3DGPU_ERR_ARGUMENT;
   }
   for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
-    SL3D_TRY(Pass(f, s.p, iteration == 0, sigmaEnd, sNext.p));
     double residual = 0.0;
-    SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
+    if (iteration == 0) {
+      SL3D_TRY(FirstPass(f, sigmaEnd, &residual));
+    } else {
+      SL3D_TRY(Pass(f, s.p, false, sigmaEnd, sNext.p));
+      SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
+    }
     history.push_back(residual);
     info.iterations = iteration + 1;
     info.residual = residual;
@@ -858,6 +880,77 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
     LaunchAddCorrection(2 * spectralComplex, reinterpret_cast<const float*>(e32.p), reinterpret_cast<double*>(s.p),
                         stream);
     SL3D_CHECK_LAUNCH();
+  }
+  return SL3DGPU_OK;
+}
+
+// The first pass of a stage: from the plain start (the force of the grid
+// strain in hand), and when a warm start is armed for this stage, also from
+// the guess; the iteration continues from whichever left the smaller
+// relative change (the guess discarded otherwise), its next iterate in sNext.
+int Viscoelastic3DGpu::FirstPass(const Flavour& f, const double2* sigmaEnd, double* residual) {
+  SL3D_TRY(Pass(f, s.p, true, sigmaEnd, sNext.p));
+  double plain = 0.0;
+  SL3D_TRY(RelativeChange(sNext.p, s.p, &plain));
+  *residual = plain;
+  if (!guessStage) return SL3DGPU_OK;
+  guessStage = false;
+  SL3D_TRY(Pass(f, guess.p, false, sigmaEnd, guessNext.p));
+  double tried = 0.0;
+  SL3D_TRY(RelativeChange(guessNext.p, guess.p, &tried));
+  if (std::isfinite(tried) && tried < plain) {
+    std::swap(s, guess);
+    std::swap(sNext, guessNext);
+    *residual = tried;
+    guessTaken = 1;
+  } else if (plain <= options.rtol) {
+    // the plain start converges at once: its solutions back for Surface
+    SL3D_TRY(Pass(f, s.p, true, sigmaEnd, sNext.p));
+  }
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::SetStart(const double* coefficients, bool onDevice) {
+  if (staticMode || options.solver == 1) {
+    SetError("v3d: the warm start applies to the fixed-point step");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (coefficients == nullptr) {
+    guessArmed = false;
+    return SL3DGPU_OK;
+  }
+  if (guess.n != static_cast<size_t>(spectralComplex)) {
+    SL3D_CUDA(guess.Alloc(spectralComplex));
+    SL3D_CUDA(guessNext.Alloc(spectralComplex));
+  }
+  SL3D_CUDA(cudaMemcpyAsync(guess.p, coefficients, spectralComplex * sizeof(double2),
+                            onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  guessArmed = true;
+  return SL3DGPU_OK;
+}
+
+// Evolution3D::Run with no ocean and no rotation (GRDSolver::NoOceanState,
+// RotationalFeedback::None): the direct load is the whole load, so each node
+// is one step under the loads at its ends; node 0 is the instantaneous
+// (elastic, dt = 0) response to its load (Evolution3D::Instantaneous). Per
+// node the surface U and phi coefficients (l, m >= 0) and the step's info.
+int Viscoelastic3DGpu::Run(V3dState& st, const double* times, int nodes, int scheme, const double* loads, double* u,
+                           double* phi, sl3dgpu_step_info* infos) {
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  for (int k = 0; k < nodes; ++k) {
+    const double* l1 = loads + 2 * lm * k;
+    const double* l0 = k > 0 ? loads + 2 * lm * (k - 1) : l1;
+    const double dt = k > 0 ? times[k] - times[k - 1] : 0.0;
+    if (!(dt >= 0.0)) {
+      SetError("v3d: node times must not decrease");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+    sl3dgpu_step_info info{};
+    SL3D_TRY(Step(st, dt, scheme, l0, l1, &info));
+    if (infos) infos[k] = info;
+    if (u) SL3D_TRY(Surface(0, u + 2 * lm * k));
+    if (phi) SL3D_TRY(Surface(2, phi + 2 * lm * k));
   }
   return SL3DGPU_OK;
 }
@@ -1296,8 +1389,10 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   sl3dgpu_step_info info{};
   history.clear();
   correctionHistory.clear();
+  guessTaken = 0;
   if (scheme != 2 || dt == 0.0) {
     const int one = scheme == 2 ? 1 : scheme;
+    guessStage = guessArmed;
     SL3D_TRY(StepOnce(st, scratch, dt, one, s0, s1, info));
   } else {
     const double gamma = host::kSdirk2Gamma;
@@ -1318,6 +1413,7 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
                          scratch.m[k].r.p, stream);
       SL3D_CHECK_LAUNCH();
     }
+    guessStage = guessArmed;
     SL3D_TRY(StepOnce(scratch, scratch, h, 1, mid, s1, i2));
     info.iterations = i1.iterations + i2.iterations;
     info.mixed_passes = i1.mixed_passes + i2.mixed_passes;
@@ -1326,6 +1422,7 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     info.residual = i2.residual;
     info.converged = i1.converged && i2.converged;
   }
+  guessArmed = false;  // a warm start serves one step
   std::swap(st.m, scratch.m);
   std::swap(st.strain, scratch.strain);
   std::swap(st.coeffs, scratch.coeffs);
@@ -1474,6 +1571,45 @@ extern "C" int sl3dgpu_v3d_step_device(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state,
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.Step(state->st, dt, scheme, load0, load1, info, true);
+}
+
+extern "C" int sl3dgpu_v3d_set_start(sl3dgpu_v3d* h, const double* coefficients, int on_device) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SetStart(coefficients, on_device != 0);
+}
+
+extern "C" int sl3dgpu_v3d_start_taken(const sl3dgpu_v3d* h) { return h == nullptr ? 0 : h->op.guessTaken; }
+
+extern "C" int sl3dgpu_v3d_state_coefficients(const sl3dgpu_v3d* h, const sl3dgpu_v3d_state* state,
+                                              const double** device, long long* count) {
+  if (h == nullptr || state == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (device) *device = state->st.hasCoeffs ? reinterpret_cast<const double*>(state->st.coeffs.p) : nullptr;
+  if (count) *count = 2 * h->op.spectralComplex;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_state_coefficients_host(const sl3dgpu_v3d* h, const sl3dgpu_v3d_state* state, double* out) {
+  if (h == nullptr || state == nullptr || out == nullptr || !state->st.hasCoeffs) {
+    SetError("v3d: null argument or a state without strain coefficients");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SL3D_CUDA(cudaMemcpy(out, state->st.coeffs.p, h->op.spectralComplex * sizeof(double2), cudaMemcpyDeviceToHost));
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_run(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const double* times, int nodes, int scheme,
+                               const double* loads, double* u, double* phi, sl3dgpu_step_info* infos) {
+  if (h == nullptr || state == nullptr || times == nullptr || loads == nullptr || nodes < 0) {
+    SetError("v3d: null argument or negative node count");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Run(state->st, times, nodes, scheme, loads, u, phi, infos);
 }
 
 extern "C" int sl3dgpu_v3d_surface(sl3dgpu_v3d* h, int component, double* out) {

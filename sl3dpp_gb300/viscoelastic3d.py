@@ -85,6 +85,11 @@ def _signatures():
         "sl3dgpu_v3d_correction_history": (i, [v, P_double, i]),
         "sl3dgpu_v3d_step_device": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_stream": (v, [v]),
+        "sl3dgpu_v3d_set_start": (i, [v, v, i]),
+        "sl3dgpu_v3d_start_taken": (i, [v]),
+        "sl3dgpu_v3d_state_coefficients": (i, [v, v, ctypes.POINTER(c_void_p), ctypes.POINTER(ctypes.c_longlong)]),
+        "sl3dgpu_v3d_run": (i, [v, v, P_double, i, i, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_state_coefficients_host": (i, [v, v, v]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -115,6 +120,21 @@ class State:
         if h is not None and h.value:
             lib().sl3dgpu_v3d_free_state(h)
             self._h = None
+
+    def device_coefficients(self):
+        """(device address, count of doubles) of the strain coefficients in
+        the device layout (address 0 before the first step)."""
+        ptr, count = c_void_p(), ctypes.c_longlong()
+        check(lib().sl3dgpu_v3d_state_coefficients(self._op._h, self._h, ctypes.byref(ptr), ctypes.byref(count)))
+        return ptr.value or 0, count.value
+
+    def device_layout_coefficients(self) -> np.ndarray:
+        """A host copy of the strain coefficients in the device layout (what
+        Viscoelastic3D.set_start takes)."""
+        _, count = self.device_coefficients()
+        out = np.zeros(count, dtype=np.float64)
+        check(lib().sl3dgpu_v3d_state_coefficients_host(self._op._h, self._h, out.ctypes.data))
+        return out
 
     def strain_coefficients(self) -> np.ndarray:
         """The strain coefficients, reference layouts (node-major spin -2, -1, 0 blocks)."""
@@ -192,6 +212,22 @@ class Viscoelastic3D:
                                             None if load1 is None else load1.data_ptr(), ctypes.byref(info)))
         return info
 
+    def set_start(self, coefficients) -> None:
+        """The warm start of the next step (Converge's start): coefficients in
+        the device layout (a CUDA torch tensor of doubles, or a numpy array),
+        None to disarm. Kept only if its first residual beats the plain start's."""
+        if coefficients is None:
+            check(lib().sl3dgpu_v3d_set_start(self._h, None, 0))
+        elif hasattr(coefficients, "data_ptr"):
+            check(lib().sl3dgpu_v3d_set_start(self._h, coefficients.data_ptr(), 1))
+        else:
+            arr = np.ascontiguousarray(coefficients, dtype=np.float64)
+            check(lib().sl3dgpu_v3d_set_start(self._h, arr.ctypes.data, 0))
+
+    @property
+    def start_taken(self) -> bool:
+        return bool(lib().sl3dgpu_v3d_start_taken(self._h))
+
     @property
     def stream(self) -> int:
         """The CUDA stream (cudaStream_t) the operator's kernels run on."""
@@ -218,3 +254,34 @@ class Viscoelastic3D:
         out = np.zeros((self.lmax + 1) * (self.lmax + 2) // 2, dtype=np.complex128)
         check(lib().sl3dgpu_v3d_surface(self._h, code, out.ctypes.data))
         return out
+
+
+class Evolution3D:
+    """Evolution3D::Run for a body without an ocean and without rotational
+    feedback (GRDSolver::NoOceanState): node 0 is the instantaneous elastic
+    response, each later node one step of the operator under the direct
+    loads at its two ends. Snapshots carry the surface U and phi
+    coefficients (l, m >= 0) and the node's step info."""
+
+    def __init__(self, op: Viscoelastic3D, scheme="sdirk2"):
+        self.op = op
+        self.scheme = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+
+    def Run(self, times, loads, state: State | None = None):
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        loads = np.ascontiguousarray(loads, dtype=np.complex128)
+        n = times.size
+        lm = (self.op.lmax + 1) * (self.op.lmax + 2) // 2
+        if loads.shape != (n, lm):
+            raise ValueError("one load (l(l+1)/2 + m coefficients) per node")
+        state = state if state is not None else self.op.ZeroState()
+        U = np.zeros((n, lm), dtype=np.complex128)
+        phi = np.zeros((n, lm), dtype=np.complex128)
+        infos = (StepInfo * max(n, 1))()
+        check(lib().sl3dgpu_v3d_run(self.op._h, state._h, times.ctypes.data_as(P_double), n, self.scheme,
+                                    loads.ctypes.data, U.ctypes.data, phi.ctypes.data, infos))
+        return {"U": U, "phi": phi, "infos": [infos[k] for k in range(n)], "state": state}
+
+    def Instantaneous(self, load):
+        out = self.Run(np.zeros(1), np.asarray(load)[None, :])
+        return {"U": out["U"][0], "phi": out["phi"][0]}
