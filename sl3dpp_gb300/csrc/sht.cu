@@ -18,6 +18,7 @@
 
 #include "profile.cuh"
 #include "sht.cuh"
+#include "tc_gemm.cuh"
 
 namespace sl3dgpu {
 
@@ -546,6 +547,9 @@ int Grid::Create(int lmax, int nmax, double oversampling, std::unique_ptr<Grid>&
 }
 
 Grid::~Grid() {
+  cudaFree(dTcError_);
+  cudaFree(splitHi_);
+  cudaFree(splitLo_);
   cudaFree(dTheta);
   cudaFree(dWeights);
   cudaFree(dTwiddle);
@@ -556,6 +560,7 @@ Grid::~Grid() {
   for (auto& [N, t] : tables_) {
     cudaFree(t.values);
     cudaFree(t.values32);
+    cudaFree(t.values32Lo);
     cudaFree(t.dRowOffset);
   }
 }
@@ -731,9 +736,14 @@ int Grid::Table32(int N, const SpinTable** out) {
   if (mt.values32 == nullptr) {
     const long long n = static_cast<long long>(mt.rowOffset.back()) * ntheta;
     SL3D_CUDA(cudaMalloc(&mt.values32, std::max<long long>(n, 1) * sizeof(float)));
+    SL3D_CUDA(cudaMalloc(&mt.values32Lo, std::max<long long>(n, 1) * sizeof(float)));
     prof::Scope scope(prof::kOther, nullptr);
-    CastKernel<<<static_cast<unsigned>((n + 255) / 256), 256>>>(mt.values, n, mt.values32);
+    LaunchSplitTf32(n, mt.values, mt.values32, mt.values32Lo, nullptr);
     SL3D_CHECK_LAUNCH();
+    if (dTcError_ == nullptr) {
+      SL3D_CUDA(cudaMalloc(&dTcError_, sizeof(int)));
+      SL3D_CUDA(cudaMemset(dTcError_, 0, sizeof(int)));
+    }
     if (dTwiddle32 == nullptr) {
       SL3D_CUDA(cudaMalloc(&dTwiddle32, nphi * sizeof(float2)));
       CastKernel<<<(2 * nphi + 255) / 256, 256>>>(reinterpret_cast<const double*>(dTwiddle), 2LL * nphi,
@@ -746,12 +756,39 @@ int Grid::Table32(int N, const SpinTable** out) {
   return SL3DGPU_OK;
 }
 
-int Grid::RunGemmF(const Batch& b, const float* A, const float* B, float* C, bool accumulate, cudaStream_t stream) {
+// The FP32 contractions run on the tensor cores (3xTF32, tc_gemm.cu).
+int Grid::RunGemmF(const Batch& b, const float* aHi, const float* aLo, const float* B, long long rows, int width,
+                   long long ld, long long offset, float* C, bool accumulate, cudaStream_t stream) {
   if (b.count == 0) return SL3DGPU_OK;
-  dim3 grid((b.maxM + kBM - 1) / kBM, (b.maxN + kBN - 1) / kBN, static_cast<unsigned>(b.count));
+  const size_t need = static_cast<size_t>(rows) * ld;
+  if (need > splitSize_) {
+    cudaFree(splitHi_);
+    cudaFree(splitLo_);
+    splitHi_ = splitLo_ = nullptr;
+    splitSize_ = 0;
+    SL3D_CUDA(cudaMalloc(&splitHi_, need * sizeof(float)));
+    SL3D_CUDA(cudaMalloc(&splitLo_, need * sizeof(float)));
+    splitSize_ = need;
+  }
+  {
+    prof::Scope scope(prof::kStream, stream, 0.0, 12.0 * rows * width);
+    LaunchSplitTf32Rows(rows, width, ld, B + offset, splitHi_ + offset, splitLo_ + offset, stream);
+    SL3D_CHECK_LAUNCH();
+  }
   prof::Scope scope(prof::kLegendre32, stream, b.flops);
-  GemmKernel<float><<<grid, 256, 0, stream>>>(b.items, A, B, C, accumulate);
-  SL3D_CHECK_LAUNCH();
+  return RunGemmTc(b.items, b.count, b.maxM, b.maxN, aHi, aLo, splitHi_, splitLo_, C, accumulate, dTcError_, stream);
+}
+
+int Grid::TensorCoreStatus(cudaStream_t stream) {
+  if (dTcError_ == nullptr) return SL3DGPU_OK;
+  int flag = 0;
+  SL3D_CUDA(cudaMemcpyAsync(&flag, dTcError_, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  if (flag != 0) {
+    SL3D_CUDA(cudaMemsetAsync(dTcError_, 0, sizeof(int), stream));
+    SetError("a tensor-core contraction gave up waiting for its completion");
+    return SL3DGPU_ERR_WAIT;
+  }
   return SL3DGPU_OK;
 }
 
@@ -767,7 +804,9 @@ int Grid::LegendreSynthesisF(int N, bool real, const float* coeffs, int P, int p
     if (t->Rows(m, lmax) == 0)
       SL3D_CUDA(cudaMemsetAsync(spectra + static_cast<long long>(m - mlo) * ntheta * 2LL * count, 0,
                                 sizeof(float) * ntheta * 2 * count, stream));
-  return RunGemmF(*b, t->values32, coeffs, spectra, false, stream);
+  // B: the coefficients' rows, columns p0 .. p0 + count (complex)
+  const long long rows = real ? RealRows() : SpinRows(N);
+  return RunGemmF(*b, t->values32, t->values32Lo, coeffs, rows, 2 * count, 2LL * P, 2LL * p0, spectra, false, stream);
 }
 
 int Grid::LegendreAnalysisF(int N, bool real, const float* spectra, int P, int p0, int count, float* coeffs,
@@ -777,7 +816,10 @@ int Grid::LegendreAnalysisF(int N, bool real, const float* spectra, int P, int p
   if (int st = Table32(N, &t); st != SL3DGPU_OK) return st;
   const Batch* b = nullptr;
   if (int st = BatchFor(N, real, true, P, p0, count, &b); st != SL3DGPU_OK) return st;
-  return RunGemmF(*b, t->values32, spectra, coeffs, accumulate, stream);
+  // B: the spectra, [m][j][count] complex, whole
+  const long long rows = static_cast<long long>(real ? lmax + 1 : 2 * lmax + 1) * ntheta;
+  return RunGemmF(*b, t->values32, t->values32Lo, spectra, rows, 2 * count, 2LL * count, 0, coeffs, accumulate,
+                  stream);
 }
 
 int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const float* weight, float* spectraOut,

@@ -38,7 +38,8 @@ struct SpinTable {
   int N = 0;
   std::vector<int> rowOffset;  // 2 lmax + 2 entries, cumulative rows by m index
   double* values = nullptr;    // device
-  float* values32 = nullptr;   // device FP32 copy, made on first use
+  float* values32 = nullptr;   // device TF32 high part of the table, made on first use
+  float* values32Lo = nullptr; // and its low part (value - high, FP32): the 3xTF32 split
   int* dRowOffset = nullptr;   // device copy of rowOffset
   int Rows(int m, int lmax) const { return rowOffset[m + lmax + 1] - rowOffset[m + lmax]; }
 };
@@ -100,6 +101,9 @@ class Grid {
   // correction passes): FP32 copies of the table and twiddles, made once.
   int LegendreSynthesisF(int N, bool real, const float* coeffs, int P, int p0, int count, float* spectra,
                          cudaStream_t stream);
+  // Whether a tensor-core contraction gave up waiting since the last call
+  // (reads and clears the device flag; synchronises the stream).
+  int TensorCoreStatus(cudaStream_t stream);
   int LegendreAnalysisF(int N, bool real, const float* spectra, int P, int p0, int count, float* coeffs,
                         bool accumulate, cudaStream_t stream);
   int RingWeightedF(bool real, const float* spectraIn, int count, const float* weight, float* spectraOut,
@@ -128,7 +132,14 @@ class Grid {
   size_t scratchCoeffsSize_ = 0;
   int RunGemm(const Batch& b, const double* A, const double* B, double* C, bool accumulate,
               cudaStream_t stream);
-  int RunGemmF(const Batch& b, const float* A, const float* B, float* C, bool accumulate, cudaStream_t stream);
+  // B's 3xTF32 split: `rows` rows of `width` values from column `offset`,
+  // `ld` apart, from B (the items' B offsets count from B).
+  int RunGemmF(const Batch& b, const float* aHi, const float* aLo, const float* B, long long rows, int width,
+               long long ld, long long offset, float* C, bool accumulate, cudaStream_t stream);
+  int* dTcError_ = nullptr;  // set by a tensor-core wait that gave up
+  float* splitHi_ = nullptr;  // B's split, grown on demand
+  float* splitLo_ = nullptr;
+  size_t splitSize_ = 0;
   int Table32(int N, const SpinTable** out);
 };
 

@@ -877,6 +877,7 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
     // residual under rtol: r' is about (its relative change) x (residual),
     // with a factor 10 to spare, and never finer than correction_rtol.
     SL3D_TRY(Correct(f, std::max(options.correction_rtol, std::min(0.1, 0.1 * options.rtol / residual)), info));
+    SL3D_TRY(grid->TensorCoreStatus(stream));
     LaunchAddCorrection(2 * spectralComplex, reinterpret_cast<const float*>(e32.p), reinterpret_cast<double*>(s.p),
                         stream);
     SL3D_CHECK_LAUNCH();
