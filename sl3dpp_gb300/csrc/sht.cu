@@ -548,19 +548,21 @@ int Grid::Create(int lmax, int nmax, double oversampling, std::unique_ptr<Grid>&
 
 Grid::~Grid() {
   cudaFree(dTcError_);
-  cudaFree(splitHi_);
-  cudaFree(splitLo_);
+  for (auto& [key, panel] : panels_) cudaFree(panel);
   cudaFree(dTheta);
   cudaFree(dWeights);
   cudaFree(dTwiddle);
   cudaFree(dTwiddle32);
-  for (auto& [key, b] : batches_) cudaFree(b.items);
+  for (auto& [key, b] : batches_) {
+    cudaFree(b.items);
+    cudaFree(b.tcItems);
+    cudaFree(b.packed);
+  }
   cudaFree(scratchSpectra_);
   cudaFree(scratchCoeffs_);
   for (auto& [N, t] : tables_) {
     cudaFree(t.values);
-    cudaFree(t.values32);
-    cudaFree(t.values32Lo);
+
     cudaFree(t.dRowOffset);
   }
 }
@@ -647,6 +649,31 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
     SL3D_CUDA(cudaMalloc(&b.items, items.size() * sizeof(GemmItem)));
     SL3D_CUDA(cudaMemcpy(b.items, items.data(), items.size() * sizeof(GemmItem), cudaMemcpyHostToDevice));
   }
+  // The tensor-core form's tiles: 128-row tiles of A in the spin's panel,
+  // 16-deep K steps, one column tile when N fits.
+  b.tileN = b.maxN <= kTcMaxTileN ? (b.maxN + 15) / 16 * 16 : kTcMaxTileN;
+  for (const auto& g : items) {
+    TcItemHost h{};
+    h.M = g.M;
+    h.N = g.N;
+    h.K = g.K;
+    h.mTiles = (g.M + kTcTileM - 1) / kTcTileM;
+    h.kSteps = (g.K + kTcTileK - 1) / kTcTileK;
+    h.nTiles = b.tileN > 0 ? (g.N + b.tileN - 1) / b.tileN : 0;
+    h.ldc = g.ldc;
+    h.ldb = g.ldb;
+    h.aPanel = b.panelFloats;
+    h.bPack = b.packedFloats;
+    h.b = g.b;
+    h.c = g.c;
+    b.panelFloats += static_cast<long long>(h.mTiles) * h.kSteps * 2 * kTcTileM * kTcTileK;
+    b.packedFloats += static_cast<long long>(h.nTiles) * h.kSteps * 2 * b.tileN * kTcTileK;
+    b.maxMTiles = std::max(b.maxMTiles, h.mTiles);
+    b.maxNTiles = std::max(b.maxNTiles, h.nTiles);
+    b.maxATiles = std::max(b.maxATiles, h.mTiles * h.kSteps);
+    b.maxBTiles = std::max(b.maxBTiles, h.nTiles * h.kSteps);
+    b.tcHost.push_back(h);
+  }
   *out = &batches_.emplace(key, b).first->second;
   return SL3DGPU_OK;
 }
@@ -729,54 +756,62 @@ int Grid::RingWeighted(bool real, const double* spectraIn, int count, const doub
                     stream);
 }
 
+// The spin's table (FP64; the tensor-core panels are made from it) and the
+// FP32 twiddles of the correction's ring passes, made once.
 int Grid::Table32(int N, const SpinTable** out) {
-  const SpinTable* t = nullptr;
-  if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
-  auto& mt = tables_.at(N);
-  if (mt.values32 == nullptr) {
-    const long long n = static_cast<long long>(mt.rowOffset.back()) * ntheta;
-    SL3D_CUDA(cudaMalloc(&mt.values32, std::max<long long>(n, 1) * sizeof(float)));
-    SL3D_CUDA(cudaMalloc(&mt.values32Lo, std::max<long long>(n, 1) * sizeof(float)));
-    prof::Scope scope(prof::kOther, nullptr);
-    LaunchSplitTf32(n, mt.values, mt.values32, mt.values32Lo, nullptr);
+  if (int st = Table(N, out); st != SL3DGPU_OK) return st;
+  if (dTwiddle32 == nullptr) {
+    SL3D_CUDA(cudaMalloc(&dTwiddle32, nphi * sizeof(float2)));
+    CastKernel<<<(2 * nphi + 255) / 256, 256>>>(reinterpret_cast<const double*>(dTwiddle), 2LL * nphi,
+                                                reinterpret_cast<float*>(dTwiddle32));
     SL3D_CHECK_LAUNCH();
-    if (dTcError_ == nullptr) {
-      SL3D_CUDA(cudaMalloc(&dTcError_, sizeof(int)));
-      SL3D_CUDA(cudaMemset(dTcError_, 0, sizeof(int)));
-    }
-    if (dTwiddle32 == nullptr) {
-      SL3D_CUDA(cudaMalloc(&dTwiddle32, nphi * sizeof(float2)));
-      CastKernel<<<(2 * nphi + 255) / 256, 256>>>(reinterpret_cast<const double*>(dTwiddle), 2LL * nphi,
-                                                  reinterpret_cast<float*>(dTwiddle32));
-      SL3D_CHECK_LAUNCH();
-    }
     SL3D_CUDA(cudaDeviceSynchronize());
   }
-  *out = &mt;
   return SL3DGPU_OK;
 }
 
-// The FP32 contractions run on the tensor cores (3xTF32, tc_gemm.cu).
-int Grid::RunGemmF(const Batch& b, const float* aHi, const float* aLo, const float* B, long long rows, int width,
-                   long long ld, long long offset, float* C, bool accumulate, cudaStream_t stream) {
+// The FP32 contractions run on the tensor cores (3xTF32, tc_gemm.cu): the
+// spin's table panel for this direction made on first use, the batch's items
+// and packed-B buffer on its first use, then B packed and the contraction.
+int Grid::RunGemmF(int N, bool real, Batch& b, const float* B, float* C, bool accumulate, cudaStream_t stream) {
   if (b.count == 0) return SL3DGPU_OK;
-  const size_t need = static_cast<size_t>(rows) * ld;
-  if (need > splitSize_) {
-    cudaFree(splitHi_);
-    cudaFree(splitLo_);
-    splitHi_ = splitLo_ = nullptr;
-    splitSize_ = 0;
-    SL3D_CUDA(cudaMalloc(&splitHi_, need * sizeof(float)));
-    SL3D_CUDA(cudaMalloc(&splitLo_, need * sizeof(float)));
-    splitSize_ = need;
+  static_assert(sizeof(TcItemHost) == sizeof(TcItem), "host and device tensor-core items agree");
+  if (dTcError_ == nullptr) {
+    SL3D_CUDA(cudaMalloc(&dTcError_, sizeof(int)));
+    SL3D_CUDA(cudaMemset(dTcError_, 0, sizeof(int)));
+  }
+  if (b.tcItems == nullptr) {
+    SL3D_CUDA(cudaMalloc(&b.tcItems, b.tcHost.size() * sizeof(TcItem)));
+    SL3D_CUDA(cudaMemcpy(b.tcItems, b.tcHost.data(), b.tcHost.size() * sizeof(TcItem), cudaMemcpyHostToDevice));
+    SL3D_CUDA(cudaMalloc(&b.packed, std::max<long long>(b.packedFloats, 1) * sizeof(float)));
+  }
+  const auto* items = static_cast<const TcItem*>(b.tcItems);
+  const std::array<int, 3> key{N, real ? 1 : 0, b.analysis ? 1 : 0};
+  auto found = panels_.find(key);
+  if (found == panels_.end()) {
+    const SpinTable* t = nullptr;
+    if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+    float* panel = nullptr;
+    SL3D_CUDA(cudaMalloc(&panel, std::max<long long>(b.panelFloats, 1) * sizeof(float)));
+    prof::Scope scope(prof::kOther, stream);
+    LaunchPanelA(b.items, items, b.count, b.maxATiles, t->values, panel, stream);
+    SL3D_CHECK_LAUNCH();
+    found = panels_.emplace(key, panel).first;
   }
   {
-    prof::Scope scope(prof::kStream, stream, 0.0, 12.0 * rows * width);
-    LaunchSplitTf32Rows(rows, width, ld, B + offset, splitHi_ + offset, splitLo_ + offset, stream);
+    prof::Scope scope(prof::kStream, stream, 0.0, 12.0 * b.packedFloats / 2);
+    LaunchPackB(items, b.count, b.maxBTiles, b.tileN, B, b.packed, stream);
     SL3D_CHECK_LAUNCH();
   }
   prof::Scope scope(prof::kLegendre32, stream, b.flops);
-  return RunGemmTc(b.items, b.count, b.maxM, b.maxN, aHi, aLo, splitHi_, splitLo_, C, accumulate, dTcError_, stream);
+  return RunGemmTc(items, b.count, b.maxMTiles, b.maxNTiles, b.tileN, found->second, b.packed, C, accumulate,
+                   dTcError_, stream);
+}
+
+Grid::Batch* Grid::MutableBatch(int N, bool real, bool analysis, int P, int p0, int count) {
+  const Batch* b = nullptr;
+  if (BatchFor(N, real, analysis, P, p0, count, &b) != SL3DGPU_OK) return nullptr;
+  return const_cast<Batch*>(b);
 }
 
 int Grid::TensorCoreStatus(cudaStream_t stream) {
@@ -797,16 +832,14 @@ int Grid::LegendreSynthesisF(int N, bool real, const float* coeffs, int P, int p
   if (count == 0) return SL3DGPU_OK;
   const SpinTable* t = nullptr;
   if (int st = Table32(N, &t); st != SL3DGPU_OK) return st;
-  const Batch* b = nullptr;
-  if (int st = BatchFor(N, real, false, P, p0, count, &b); st != SL3DGPU_OK) return st;
+  Batch* b = MutableBatch(N, real, false, P, p0, count);
+  if (b == nullptr) return SL3DGPU_ERR_CUDA;
   const int mlo = real ? 0 : -lmax;
   for (int m = mlo; m <= lmax; ++m)
     if (t->Rows(m, lmax) == 0)
       SL3D_CUDA(cudaMemsetAsync(spectra + static_cast<long long>(m - mlo) * ntheta * 2LL * count, 0,
                                 sizeof(float) * ntheta * 2 * count, stream));
-  // B: the coefficients' rows, columns p0 .. p0 + count (complex)
-  const long long rows = real ? RealRows() : SpinRows(N);
-  return RunGemmF(*b, t->values32, t->values32Lo, coeffs, rows, 2 * count, 2LL * P, 2LL * p0, spectra, false, stream);
+  return RunGemmF(N, real, *b, coeffs, spectra, false, stream);
 }
 
 int Grid::LegendreAnalysisF(int N, bool real, const float* spectra, int P, int p0, int count, float* coeffs,
@@ -814,12 +847,9 @@ int Grid::LegendreAnalysisF(int N, bool real, const float* spectra, int P, int p
   if (count == 0) return SL3DGPU_OK;
   const SpinTable* t = nullptr;
   if (int st = Table32(N, &t); st != SL3DGPU_OK) return st;
-  const Batch* b = nullptr;
-  if (int st = BatchFor(N, real, true, P, p0, count, &b); st != SL3DGPU_OK) return st;
-  // B: the spectra, [m][j][count] complex, whole
-  const long long rows = static_cast<long long>(real ? lmax + 1 : 2 * lmax + 1) * ntheta;
-  return RunGemmF(*b, t->values32, t->values32Lo, spectra, rows, 2 * count, 2LL * count, 0, coeffs, accumulate,
-                  stream);
+  Batch* b = MutableBatch(N, real, true, P, p0, count);
+  if (b == nullptr) return SL3DGPU_ERR_CUDA;
+  return RunGemmF(N, real, *b, spectra, coeffs, accumulate, stream);
 }
 
 int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const float* weight, float* spectraOut,

@@ -38,8 +38,6 @@ struct SpinTable {
   int N = 0;
   std::vector<int> rowOffset;  // 2 lmax + 2 entries, cumulative rows by m index
   double* values = nullptr;    // device
-  float* values32 = nullptr;   // device TF32 high part of the table, made on first use
-  float* values32Lo = nullptr; // and its low part (value - high, FP32): the 3xTF32 split
   int* dRowOffset = nullptr;   // device copy of rowOffset
   int Rows(int m, int lmax) const { return rowOffset[m + lmax + 1] - rowOffset[m + lmax]; }
 };
@@ -48,6 +46,14 @@ struct GemmItem {
   int M, N, K, pad;
   long long a, b, c;
   int sAi, sAk, ldb, ldc;
+};
+
+// A tensor-core item's host description (mirrors TcItem in tc_gemm.cuh).
+struct TcItemHost {
+  int M, N, K, mTiles;
+  int kSteps, nTiles, ldc, ldb;
+  long long aPanel, bPack;
+  long long b, c;
 };
 
 class Grid {
@@ -123,23 +129,29 @@ class Grid {
     int count = 0, maxM = 0, maxN = 0;
     bool analysis = false;
     double flops = 0.0;  // 2 M N K summed over the items
+    // the tensor-core form (FP32): its items, tile width and extents, the
+    // packed B (made on first use) and the key of its table panel
+    std::vector<TcItemHost> tcHost;
+    void* tcItems = nullptr;
+    int tileN = 0, maxMTiles = 0, maxNTiles = 0, maxATiles = 0, maxBTiles = 0;
+    long long panelFloats = 0, packedFloats = 0;
+    float* packed = nullptr;
   };
+  // The table pre-tiled for the tensor cores per (spin, real, direction).
+  std::map<std::array<int, 3>, float*> panels_;
   std::map<std::array<long long, 6>, Batch> batches_;
   int BatchFor(int N, bool real, bool analysis, int P, int p0, int count, const Batch** out);
+  Batch* MutableBatch(int N, bool real, bool analysis, int P, int p0, int count);
   double* scratchSpectra_ = nullptr;
   size_t scratchSpectraSize_ = 0;
   double* scratchCoeffs_ = nullptr;
   size_t scratchCoeffsSize_ = 0;
   int RunGemm(const Batch& b, const double* A, const double* B, double* C, bool accumulate,
               cudaStream_t stream);
-  // B's 3xTF32 split: `rows` rows of `width` values from column `offset`,
-  // `ld` apart, from B (the items' B offsets count from B).
-  int RunGemmF(const Batch& b, const float* aHi, const float* aLo, const float* B, long long rows, int width,
-               long long ld, long long offset, float* C, bool accumulate, cudaStream_t stream);
+  // The FP32 contraction on the tensor cores (tc_gemm.cu): the spin's table
+  // panel (made on first use), B packed, the contraction.
+  int RunGemmF(int N, bool real, Batch& b, const float* B, float* C, bool accumulate, cudaStream_t stream);
   int* dTcError_ = nullptr;  // set by a tensor-core wait that gave up
-  float* splitHi_ = nullptr;  // B's split, grown on demand
-  float* splitLo_ = nullptr;
-  size_t splitSize_ = 0;
   int Table32(int N, const SpinTable** out);
 };
 

@@ -1,15 +1,15 @@
 // The FP32 Legendre contraction on the tcgen05 tensor cores (see tc_gemm.cuh).
 //
-// One CTA of four warps per (item, 128-row tile, column tile). K runs in
-// steps of 16, three in flight: the CTA copies a step's A and B high and low
-// parts into shared memory (cp.async, the canonical no-swizzle K-major layout
-// of 8-row x 16-byte core matrices) two steps ahead of its use; one elected
-// thread issues the step's six tcgen05.mma (two 8-deep slices x three
-// products) into the FP32 accumulator in tensor memory and commits them to
-// the step buffer's mbarrier, which the CTA waits on (with an iteration
-// limit) before refilling that buffer. The epilogue reads the accumulator
-// back with tcgen05.ld, one TMEM lane quarter per warp, and stores (or adds)
-// the rows in range.
+// One CTA of four warps per (128-row tile, item, column tile). One elected
+// thread runs the K loop: for each 16-deep step it arms the step buffer's
+// "full" mbarrier with the expected byte count and issues two TMA bulk copies
+// (the A tile's high and low parts, 16 KB; B's, 2 x tileN x 64 B) into it,
+// three steps in flight; when a step's copies have landed it issues the six
+// tcgen05.mma of the step (two 8-deep slices x three products) into the FP32
+// accumulator in tensor memory and commits them to the buffer's "empty"
+// mbarrier, which frees the buffer for the step three ahead. Every wait has an
+// iteration limit. The epilogue reads the accumulator with tcgen05.ld, one
+// TMEM lane quarter per warp, and stores (or adds) the rows in range.
 #include <cstdint>
 
 #include "profile.cuh"
@@ -18,13 +18,10 @@
 namespace sl3dgpu {
 namespace {
 
-constexpr int kTM = 128;      // rows per tile (the MMA's M)
-constexpr int kTK = 16;       // K per staged step (two 8-deep MMA slices)
-constexpr int kStages = 3;    // staged steps in flight
+constexpr int kStages = 3;
 constexpr int kThreads = 128;
 constexpr int kWaitLimit = 1 << 22;
-
-constexpr int kAFloats = kTM * kTK;  // one part of A's tile
+constexpr int kATileFloats = kTcTileM * kTcTileK;  // one part: 2048 floats, 8 KB
 
 __device__ inline uint32_t SmemAddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
@@ -53,14 +50,10 @@ __device__ inline float RoundTf32(float x) {
   return __uint_as_float(r);
 }
 
-// Index (in floats) of element (row, k) of a K-major tile of `rows` rows in
-// the core-matrix layout [k / 4][row / 8][row % 8][k % 4].
+// Index (in floats) of element (row, k) of a K-major 16-deep tile of `rows`
+// rows in the core-matrix layout [k / 4][row / 8][row % 8][k % 4].
 __device__ inline int TileIndex(int row, int k, int rows) {
   return (k >> 2) * (rows * 4) + (row >> 3) * 32 + (row & 7) * 4 + (k & 3);
-}
-
-__device__ inline void CopyAsync4(float* dst, const float* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(SmemAddr(dst)), "l"(src) : "memory");
 }
 
 __device__ inline bool WaitParity(uint32_t bar, uint32_t phase) {
@@ -86,25 +79,81 @@ __host__ __device__ constexpr uint32_t TmemColumns(int n) {
   return c;
 }
 
-// The kernel: per CTA one (item, 128-row tile, column tile of tileN).
-// Shared memory: kStages x {A hi, A lo, B hi, B lo} tiles, then the
-// mbarriers and the tensor-memory address.
-__global__ void __launch_bounds__(kThreads) TcGemmKernel(const GemmItem* items, const float* aHi, const float* aLo,
-                                                         const float* bHi, const float* bLo, float* C,
-                                                         bool accumulate, int tileN, int* errorFlag) {
-  const GemmItem it = items[blockIdx.y];
-  const int i0 = blockIdx.x * kTM, n0 = blockIdx.z * tileN;
-  if (i0 >= it.M || n0 >= it.N) return;  // the whole CTA, before any tensor-memory work
+__global__ void PanelAKernel(const GemmItem* items, const TcItem* tcItems, const double* table, float* panels) {
+  const GemmItem g = items[blockIdx.y];
+  const TcItem it = tcItems[blockIdx.y];
+  const long long total = static_cast<long long>(it.mTiles) * it.kSteps * kATileFloats;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int e = static_cast<int>(t % kATileFloats);
+    const long long tile = t / kATileFloats;
+    const int ks = static_cast<int>(tile % it.kSteps), mt = static_cast<int>(tile / it.kSteps);
+    const int r = e % kTcTileM, kk = e / kTcTileM;
+    const int i = mt * kTcTileM + r, k = ks * kTcTileK + kk;
+    const double v = (i < g.M && k < g.K) ? table[g.a + static_cast<long long>(i) * g.sAi +
+                                                  static_cast<long long>(k) * g.sAk]
+                                          : 0.0;
+    const float hi = RoundTf32(static_cast<float>(v));
+    float* out = panels + it.aPanel + tile * 2 * kATileFloats;
+    out[TileIndex(r, kk, kTcTileM)] = hi;
+    out[kATileFloats + TileIndex(r, kk, kTcTileM)] = static_cast<float>(v - static_cast<double>(hi));
+  }
+}
+
+// A thread per (tile, 4-deep K group, column): four coalesced reads down
+// B's column, one 16-byte store of each part (a core-matrix row).
+__global__ void PackBKernel(const TcItem* tcItems, int tileN, const float* B, float* packed) {
+  const TcItem it = tcItems[blockIdx.y];
+  const int tileFloats = tileN * kTcTileK;
+  const int groups = kTcTileK / 4;
+  const long long total = static_cast<long long>(it.nTiles) * it.kSteps * groups * tileN;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int nn = static_cast<int>(t % tileN);
+    const long long rest = t / tileN;
+    const int g = static_cast<int>(rest % groups);
+    const long long tile = rest / groups;
+    const int ks = static_cast<int>(tile % it.kSteps), nt = static_cast<int>(tile / it.kSteps);
+    const int n = nt * tileN + nn, k0 = ks * kTcTileK + 4 * g;
+    float v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      v[q] = (n < it.N && k0 + q < it.K) ? B[it.b + static_cast<long long>(k0 + q) * it.ldb + n] : 0.0f;
+    float4 hi, lo;
+    hi.x = RoundTf32(v[0]);
+    hi.y = RoundTf32(v[1]);
+    hi.z = RoundTf32(v[2]);
+    hi.w = RoundTf32(v[3]);
+    lo.x = v[0] - hi.x;
+    lo.y = v[1] - hi.y;
+    lo.z = v[2] - hi.z;
+    lo.w = v[3] - hi.w;
+    float* out = packed + it.bPack + tile * 2 * tileFloats + TileIndex(nn, 4 * g, tileN);
+    *reinterpret_cast<float4*>(out) = hi;
+    *reinterpret_cast<float4*>(out + tileFloats) = lo;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) TcGemmKernel(const TcItem* tcItems, int tileN, const float* panels,
+                                                         const float* packed, float* C, bool accumulate,
+                                                         int* errorFlag) {
+  const TcItem it = tcItems[blockIdx.y];
+  const int mt = blockIdx.x, nt = blockIdx.z;
+  if (mt >= it.mTiles || nt >= it.nTiles) return;  // the whole CTA, before any tensor-memory work
+  const int i0 = mt * kTcTileM, n0 = nt * tileN;
   const int nCols = min(tileN, it.N - n0);
   const int nMma = (nCols + 15) / 16 * 16;  // the MMA's N: a multiple of 16
-  const int bFloats = tileN * kTK;
   const uint32_t tmemColumns = TmemColumns(tileN);
+  const int bTileFloats = tileN * kTcTileK;
+  const uint32_t aBytes = 2 * kATileFloats * sizeof(float), bBytes = 2 * bTileFloats * sizeof(float);
 
   extern __shared__ __align__(128) unsigned char tcSmem[];
-  float* stage0 = reinterpret_cast<float*>(tcSmem);
-  const int stageFloats = 2 * kAFloats + 2 * bFloats;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(stage0 + kStages * stageFloats);
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(bar + kStages);
+  float* sA = reinterpret_cast<float*>(tcSmem);  // kStages x (hi | lo)
+  float* sB = sA + kStages * 2 * kATileFloats;   // kStages x (hi | lo)
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + kStages * 2 * bTileFloats);
+  uint64_t* empty = full + kStages;
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(empty + kStages);
+  __shared__ int okShared;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 
   if (warp == 0) {
@@ -114,8 +163,10 @@ __global__ void __launch_bounds__(kThreads) TcGemmKernel(const GemmItem* items, 
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(bar + s)), "r"(1) : "memory");
+    for (int s = 0; s < kStages; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(full + s)), "r"(1) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(empty + s)), "r"(1) : "memory");
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -123,111 +174,57 @@ __global__ void __launch_bounds__(kThreads) TcGemmKernel(const GemmItem* items, 
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmemSlot;
 
-  const float* ah = aHi + it.a;
-  const float* al = aLo + it.a;
-  const float* bh = bHi + it.b;
-  const float* bl = bLo + it.b;
-  const uint32_t idesc = InstrDescriptor(nMma, kTM);
-  const int steps = (it.K + kTK - 1) / kTK;
-
-  // Stage step `step` into buffer `buf`: cp.async of every element in range,
-  // plain zero stores outside, one copy group per thread.
-  auto stage = [&](int step, int buf) {
-    float* sAh = stage0 + buf * stageFloats;
-    float* sAl = sAh + kAFloats;
-    float* sBh = sAl + kAFloats;
-    float* sBl = sBh + bFloats;
-    const int k0 = step * kTK;
-    if (it.sAk == 1) {
-      for (int e = tid; e < kTM * kTK; e += kThreads) {
-        const int kk = e % kTK, ii = e / kTK;
-        const int i = i0 + ii, k = k0 + kk;
-        const int at = TileIndex(ii, kk, kTM);
-        if (i < it.M && k < it.K) {
-          const long long g = static_cast<long long>(i) * it.sAi + k;
-          CopyAsync4(sAh + at, ah + g);
-          CopyAsync4(sAl + at, al + g);
-        } else {
-          sAh[at] = 0.0f;
-          sAl[at] = 0.0f;
-        }
+  if (tid == 0) {
+    const float* aSrc = panels + it.aPanel + static_cast<long long>(mt) * it.kSteps * 2 * kATileFloats;
+    const float* bSrc = packed + it.bPack + static_cast<long long>(nt) * it.kSteps * 2 * bTileFloats;
+    const uint32_t idesc = InstrDescriptor(nMma, kTcTileM);
+    uint32_t phaseFull[kStages] = {0, 0, 0}, phaseEmpty[kStages] = {0, 0, 0};
+    bool ok = true;
+    // Arm buffer ks % kStages for step ks and issue its two copies; a buffer
+    // in use is first freed by its MMAs' commit.
+    auto issue = [&](int ks) {
+      const int buf = ks % kStages;
+      if (ks >= kStages) {
+        ok = ok && WaitParity(SmemAddr(empty + buf), phaseEmpty[buf]);
+        phaseEmpty[buf] ^= 1u;
       }
-    } else {
-      for (int e = tid; e < kTM * kTK; e += kThreads) {
-        const int ii = e % kTM, kk = e / kTM;
-        const int i = i0 + ii, k = k0 + kk;
-        const int at = TileIndex(ii, kk, kTM);
-        if (i < it.M && k < it.K) {
-          const long long g = static_cast<long long>(i) * it.sAi + static_cast<long long>(k) * it.sAk;
-          CopyAsync4(sAh + at, ah + g);
-          CopyAsync4(sAl + at, al + g);
-        } else {
-          sAh[at] = 0.0f;
-          sAl[at] = 0.0f;
-        }
-      }
-    }
-    for (int e = tid; e < nMma * kTK; e += kThreads) {
-      const int nn = e % nMma, kk = e / nMma;
-      const int n = n0 + nn, k = k0 + kk;
-      const int at = TileIndex(nn, kk, tileN);
-      if (nn < nCols && k < it.K) {
-        const long long g = static_cast<long long>(k) * it.ldb + n;
-        CopyAsync4(sBh + at, bh + g);
-        CopyAsync4(sBl + at, bl + g);
-      } else {
-        sBh[at] = 0.0f;
-        sBl[at] = 0.0f;
-      }
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-  };
-
-  uint32_t phase[kStages] = {0, 0, 0};
-  bool used[kStages] = {false, false, false};
-  bool ok = true;
-  for (int s = 0; s < min(kStages - 1, steps); ++s) stage(s, s);
-  for (int s = 0; s < steps && ok; ++s) {
-    const int buf = s % kStages;
-    // the step two ahead, into the buffer the previous step's MMAs read
-    const int ahead = s + kStages - 1;
-    if (ahead < steps) {
-      const int nb = ahead % kStages;
-      if (used[nb]) {
-        ok = WaitParity(SmemAddr(bar + nb), phase[nb]);
-        phase[nb] ^= 1u;
-        used[nb] = false;
-        if (!ok) break;
-      }
-      stage(ahead, nb);
-      asm volatile("cp.async.wait_group %0;\n" ::"n"(kStages - 1) : "memory");
-    } else if (s + 1 < steps) {
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-    } else {
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    }
-    // this step's copies (and zero stores) visible to the tensor core
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+      if (!ok) return;
+      const uint32_t bar = SmemAddr(full + buf);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(aBytes + bBytes)
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              SmemAddr(sA + buf * 2 * kATileFloats)),
+          "l"(aSrc + static_cast<long long>(ks) * 2 * kATileFloats), "r"(aBytes), "r"(bar)
+          : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              SmemAddr(sB + buf * 2 * bTileFloats)),
+          "l"(bSrc + static_cast<long long>(ks) * 2 * bTileFloats), "r"(bBytes), "r"(bar)
+          : "memory");
+    };
+    for (int ks = 0; ks < min(kStages - 1, it.kSteps); ++ks) issue(ks);
+    for (int ks = 0; ks < it.kSteps && ok; ++ks) {
+      if (ks + kStages - 1 < it.kSteps) issue(ks + kStages - 1);
+      if (!ok) break;
+      const int buf = ks % kStages;
+      ok = WaitParity(SmemAddr(full + buf), phaseFull[buf]);
+      phaseFull[buf] ^= 1u;
+      if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const float* sAh = stage0 + buf * stageFloats;
-      const float* sAl = sAh + kAFloats;
-      const float* sBh = sAl + kAFloats;
-      const float* sBl = sBh + bFloats;
-      const uint32_t aLbo = kTM * 16, bLbo = tileN * 16, sbo = 128;
+      const uint32_t aHi = SmemAddr(sA + buf * 2 * kATileFloats), aLo = aHi + kATileFloats * 4;
+      const uint32_t bHi = SmemAddr(sB + buf * 2 * bTileFloats), bLo = bHi + bTileFloats * 4;
+      const uint32_t aLbo = kTcTileM * 16, bLbo = tileN * 16, sbo = 128;
 #pragma unroll
-      for (int q = 0; q < kTK / 8; ++q) {
+      for (int q = 0; q < kTcTileK / 8; ++q) {
         const uint32_t aOff = q * 2 * aLbo, bOff = q * 2 * bLbo;
-        const uint64_t dAh = Descriptor(SmemAddr(sAh) + aOff, aLbo, sbo);
-        const uint64_t dAl = Descriptor(SmemAddr(sAl) + aOff, aLbo, sbo);
-        const uint64_t dBh = Descriptor(SmemAddr(sBh) + bOff, bLbo, sbo);
-        const uint64_t dBl = Descriptor(SmemAddr(sBl) + bOff, bLbo, sbo);
+        const uint64_t dAh = Descriptor(aHi + aOff, aLbo, sbo), dAl = Descriptor(aLo + aOff, aLbo, sbo);
+        const uint64_t dBh = Descriptor(bHi + bOff, bLbo, sbo), dBl = Descriptor(bLo + bOff, bLbo, sbo);
         const uint64_t as[3] = {dAh, dAh, dAl};
         const uint64_t bs[3] = {dBh, dBl, dBh};
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-          const uint32_t enable = (s > 0 || q > 0 || p > 0) ? 1u : 0u;
+          const uint32_t enable = (ks > 0 || q > 0 || p > 0) ? 1u : 0u;
           asm volatile(
               "{\n\t.reg .pred r;\n\t"
               "setp.ne.b32 r, %4, 0;\n\t"
@@ -237,21 +234,20 @@ __global__ void __launch_bounds__(kThreads) TcGemmKernel(const GemmItem* items, 
         }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       SmemAddr(bar + buf))
+                       SmemAddr(empty + buf))
                    : "memory");
     }
-    used[buf] = true;
+    // The last step's commit covers every MMA before it.
+    if (ok && it.kSteps > 0) {
+      const int last = (it.kSteps - 1) % kStages;
+      ok = WaitParity(SmemAddr(empty + last), phaseEmpty[last]);
+    }
+    okShared = ok ? 1 : 0;
+    if (!ok) atomicExch(errorFlag, 1);
   }
-  // The last step's commit covers every MMA before it.
-  if (ok && steps > 0) {
-    const int last = (steps - 1) % kStages;
-    ok = WaitParity(SmemAddr(bar + last), phase[last]);
-  }
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (!ok) {
-    if (tid == 0) atomicExch(errorFlag, 1);
-  } else {
+  if (okShared) {
     // Epilogue: this warp's TMEM lane quarter, 16 columns at a time.
     const int i = i0 + 32 * warp + lane;
     float* c = C + it.c + static_cast<long long>(i) * it.ldc + n0;
@@ -284,74 +280,34 @@ __global__ void __launch_bounds__(kThreads) TcGemmKernel(const GemmItem* items, 
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmemColumns) : "memory");
 }
 
-__global__ void SplitTf32Kernel(long long n, const float* x, float* hi, float* lo) {
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
-    const float v = x[i];
-    const float h = RoundTf32(v);
-    hi[i] = h;
-    lo[i] = v - h;
-  }
-}
-
-__global__ void SplitTf32FromDoubleKernel(long long n, const double* x, float* hi, float* lo) {
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
-    const double v = x[i];
-    const float h = RoundTf32(static_cast<float>(v));
-    hi[i] = h;
-    lo[i] = static_cast<float>(v - static_cast<double>(h));
-  }
-}
-
 }  // namespace
 
-int RunGemmTc(const GemmItem* items, int count, int maxM, int maxN, const float* aHi, const float* aLo,
-              const float* bHi, const float* bLo, float* C, bool accumulate, int* errorFlag, cudaStream_t stream) {
-  if (count == 0 || maxM == 0 || maxN == 0) return SL3DGPU_OK;
-  // One column tile when N fits (the common case), else tiles of kTcTileN.
-  const int tileN = maxN <= kTcTileN ? (maxN + 15) / 16 * 16 : kTcTileN;
-  const size_t smem = static_cast<size_t>(kStages) * (2 * kAFloats + 2 * tileN * kTK) * sizeof(float) +
-                      kStages * sizeof(uint64_t) + 16;
+void LaunchPanelA(const GemmItem* items, const TcItem* tcItems, int count, int maxTiles, const double* table,
+                  float* panels, cudaStream_t stream) {
+  if (count == 0) return;
+  const long long perItem = static_cast<long long>(maxTiles) * kATileFloats;
+  const unsigned blocks = static_cast<unsigned>(std::min<long long>((perItem + 255) / 256, 4096));
+  PanelAKernel<<<dim3(blocks, count), 256, 0, stream>>>(items, tcItems, table, panels);
+}
+
+void LaunchPackB(const TcItem* tcItems, int count, int maxTiles, int tileN, const float* B, float* packed,
+                 cudaStream_t stream) {
+  if (count == 0) return;
+  const long long perItem = static_cast<long long>(maxTiles) * tileN * (kTcTileK / 4);
+  const unsigned blocks = static_cast<unsigned>(std::min<long long>((perItem + 255) / 256, 4096));
+  PackBKernel<<<dim3(blocks, count), 256, 0, stream>>>(tcItems, tileN, B, packed);
+}
+
+int RunGemmTc(const TcItem* tcItems, int count, int maxMTiles, int maxNTiles, int tileN, const float* panels,
+              const float* packed, float* C, bool accumulate, int* errorFlag, cudaStream_t stream) {
+  if (count == 0 || maxMTiles == 0 || maxNTiles == 0) return SL3DGPU_OK;
+  const size_t smem = static_cast<size_t>(kStages) * 2 * (kATileFloats + tileN * kTcTileK) * sizeof(float) +
+                      2 * kStages * sizeof(uint64_t) + 16;
   SL3D_CUDA(cudaFuncSetAttribute(TcGemmKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  dim3 grid((maxM + kTM - 1) / kTM, static_cast<unsigned>(count), (maxN + tileN - 1) / tileN);
-  TcGemmKernel<<<grid, kThreads, smem, stream>>>(items, aHi, aLo, bHi, bLo, C, accumulate, tileN, errorFlag);
+  dim3 grid(static_cast<unsigned>(maxMTiles), static_cast<unsigned>(count), static_cast<unsigned>(maxNTiles));
+  TcGemmKernel<<<grid, kThreads, smem, stream>>>(tcItems, tileN, panels, packed, C, accumulate, errorFlag);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
 
-namespace {
-__global__ void SplitRowsKernel(long long rows, int width, long long ld, const float* x, float* hi, float* lo) {
-  const long long total = rows * width;
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total; t += stride) {
-    const long long at = (t / width) * ld + t % width;
-    const float v = x[at];
-    const float h = RoundTf32(v);
-    hi[at] = h;
-    lo[at] = v - h;
-  }
-}
-}  // namespace
-
-void LaunchSplitTf32Rows(long long rows, int width, long long ld, const float* x, float* hi, float* lo,
-                         cudaStream_t stream) {
-  const long long blocks = std::min<long long>((rows * width + 255) / 256, 152LL * 32);
-  SplitRowsKernel<<<static_cast<unsigned>(std::max<long long>(blocks, 1)), 256, 0, stream>>>(rows, width, ld, x, hi,
-                                                                                             lo);
-}
-
-void LaunchSplitTf32(long long n, const float* x, float* hi, float* lo, cudaStream_t stream) {
-  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 32);
-  SplitTf32Kernel<<<static_cast<unsigned>(std::max<long long>(blocks, 1)), 256, 0, stream>>>(n, x, hi, lo);
-}
-
-}  // namespace sl3dgpu
-
-namespace sl3dgpu {
-void LaunchSplitTf32(long long n, const double* x, float* hi, float* lo, cudaStream_t stream) {
-  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 32);
-  SplitTf32FromDoubleKernel<<<static_cast<unsigned>(std::max<long long>(blocks, 1)), 256, 0, stream>>>(n, x, hi,
-                                                                                                        lo);
-}
 }  // namespace sl3dgpu

@@ -1,9 +1,14 @@
 // The FP32 Legendre contraction on the 5th-generation tensor cores
 // (tcgen05, sm_103a): C(i, n) (+)= sum_k A(i, k) B(k, n) for a batch of
-// items, as three TF32 products per K step (A_hi B_hi + A_hi B_lo + A_lo B_hi,
+// items, as three TF32 products per K slice (A_hi B_hi + A_hi B_lo + A_lo B_hi,
 // the "3xTF32" split, about FP32 accuracy) accumulated in FP32 in tensor
-// memory. A's split is precomputed (the table); B's is made by a split pass
-// before the contraction.
+// memory.
+//
+// Both operands reach shared memory by TMA bulk copies of ready-made tiles:
+// A (the Legendre table) is pre-tiled once per (spin, direction) into
+// "panels" of 128 x 16 tiles in the canonical K-major core-matrix layout,
+// high part then low part; B is packed per call the same way (tileN x 16
+// tiles) by a split-and-pack pass.
 #pragma once
 
 #include "common.cuh"
@@ -11,26 +16,30 @@
 
 namespace sl3dgpu {
 
-// The largest N (real columns) one tile holds; wider items take several
-// tiles along N.
-constexpr int kTcTileN = 256;
+constexpr int kTcTileM = 128;  // rows per tile (the MMA's M)
+constexpr int kTcTileK = 16;   // K per tile (two 8-deep MMA slices)
+constexpr int kTcMaxTileN = 256;
 
-// items: device array of count GemmItems (a, b, c offsets in floats);
-// maxM / maxN: the largest M and N over the items (the grid's extent).
-// errorFlag: a device int set non-zero if a tensor-core completion wait
-// gives up (the launch then leaves C unspecified and the caller reports it).
-// A and B come split (hi, lo); the shared memory is three staged steps of
-// A (2 x 8 KB) and B (2 x N x 64 B), at most 147 KB.
-int RunGemmTc(const GemmItem* items, int count, int maxM, int maxN, const float* aHi, const float* aLo,
-              const float* bHi, const float* bLo, float* C, bool accumulate, int* errorFlag, cudaStream_t stream);
+// One item of a tensor-core batch, beside its GemmItem.
+struct TcItem {
+  int M, N, K, mTiles;   // rows, real columns, depth; 128-row tiles
+  int kSteps, nTiles, ldc, ldb;
+  long long aPanel;      // floats: the item's panel, [mTile][kStep][hi 2048 | lo 2048]
+  long long bPack;       // floats: the item's packed B, [nTile][kStep][hi tileN*16 | lo tileN*16]
+  long long b, c;        // floats: B's source and C's offsets
+};
 
-// hi = x rounded to TF32, lo = x - hi (both stored as FP32), elementwise.
-void LaunchSplitTf32(long long n, const float* x, float* hi, float* lo, cudaStream_t stream);
-// The split of `width` values from each of `rows` rows `ld` apart (the same
-// offsets in hi and lo).
-void LaunchSplitTf32Rows(long long rows, int width, long long ld, const float* x, float* hi, float* lo,
-                         cudaStream_t stream);
-// The same from FP64 values (the Legendre table): lo = FP32 of x - hi.
-void LaunchSplitTf32(long long n, const double* x, float* hi, float* lo, cudaStream_t stream);
+// Fill the items' A panels from the FP64 table (A(i, k) = table[a + i sAi +
+// k sAk], zero outside M x K). maxTiles: the most (mTiles x kSteps) of an item.
+void LaunchPanelA(const GemmItem* items, const TcItem* tcItems, int count, int maxTiles, const double* table,
+                  float* panels, cudaStream_t stream);
+// Split and pack B into the items' tiles. maxTiles: the most (nTiles x kSteps).
+void LaunchPackB(const TcItem* tcItems, int count, int maxTiles, int tileN, const float* B, float* packed,
+                 cudaStream_t stream);
+// The contraction: per CTA one (128-row tile, item, column tile).
+// errorFlag: a device int set non-zero if a completion wait gives up (the
+// launch then leaves C unspecified and the caller reports it).
+int RunGemmTc(const TcItem* tcItems, int count, int maxMTiles, int maxNTiles, int tileN, const float* panels,
+              const float* packed, float* C, bool accumulate, int* errorFlag, cudaStream_t stream);
 
 }  // namespace sl3dgpu
