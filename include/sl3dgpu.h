@@ -145,6 +145,9 @@ typedef struct sl3dgpu_v3d_options {
   int solver;             /* Options::StepSolver: 0 the fixed point, 1 conjugate gradients */
   double solve_rtol;      /* conjugate gradients: relative residual (preconditioned energy norm), 1e-11 */
   int solve_max_iterations; /* conjugate gradients: iteration budget, 200 */
+  int warm_start;           /* 0: each step starts from the previous strain (the reference's start);
+                               1: also guesses 2 s_n - s_{n-1}, the mixed form's FP32 correction
+                               starting from it (the FP64 form tries it as a first pass) */
 } sl3dgpu_v3d_options;
 
 /* Viscoelastic3D::StepInfo (Viscoelastic3D.hpp:357-375). */

@@ -61,8 +61,10 @@ struct V3dState {
   std::vector<GridTensor> m;
   GridTensor strain;
   Dev<double2> coeffs;
+  Dev<double2> prev;  // the step before's coefficients (warm_start 1)
   bool hasStrain = false;
   bool hasCoeffs = false;
+  bool hasPrev = false;
 };
 
 class Viscoelastic3DGpu {
@@ -116,6 +118,7 @@ class Viscoelastic3DGpu {
   Dev<double*> dGPtr, dFPtr;
   static constexpr int kMixBlocks = 1024;
   static constexpr int kMixBlocks32 = 4096;  // FP32 sums: about a hundred products a thread
+  static constexpr double kWarmKeep = 0.3;   // the largest first change a kept warm start may show
 
   // the mixed form's FP32 correction: iterate, next iterate, residual,
   // analysed force, right-hand sides, spectra, weight and its own mixer
@@ -148,8 +151,9 @@ class Viscoelastic3DGpu {
   // strain coefficients at the end of the next step, tried against the plain
   // start (the previous strain) on the step's last stage and kept only if its
   // first residual is the smaller.
-  Dev<double2> guess, guessNext;
-  bool guessArmed = false, guessStage = false;
+  Dev<double2> guess, guessNext, guessMid;
+  bool guessArmed = false;
+  const double2* stageGuess = nullptr;  // the guess the running stage may take
   int guessTaken = 0;  // the last step: 1 when the guess was kept
 
   V3dState scratch;  // the second buffer set a step writes into
@@ -197,7 +201,7 @@ class Viscoelastic3DGpu {
   int Pass32(const Flavour& f, const float2* e, float2* next);
   int Mixer32Reset();
   int Mixer32Update(int& count, int& slot, bool& first);
-  int Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info);
+  int Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info, const double2* warm);
   int SolveColumns(const Flavour& f, double2* sph, double2* tor);
   int LateralForce(const double2* x, double2* out);
   int ApplyOperator(const Flavour& f, const double2* x, double2* out);
@@ -240,6 +244,10 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   }
   if (opt.solver == 1 && (opt.precision != 0 || !(opt.solve_rtol > 0.0) || opt.solve_max_iterations < 0)) {
     SetError("v3d: conjugate gradients run in FP64 (precision 0) with solve_rtol > 0 and solve_max_iterations >= 0");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (opt.warm_start != 0 && opt.warm_start != 1) {
+    SetError("v3d: warm_start 0 (the previous step's strain) or 1 (the extrapolation of the last two)");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if (opt.precision == 1 && !(opt.correction_rtol > 0.0 && opt.correction_rtol < 1.0)) {
@@ -462,7 +470,8 @@ int Viscoelastic3DGpu::AllocState(V3dState& st) {
   for (auto& t : st.m) SL3D_CUDA(t.Alloc(values));
   SL3D_CUDA(st.strain.Alloc(values));
   SL3D_CUDA(st.coeffs.Alloc(spectralComplex));
-  st.hasStrain = st.hasCoeffs = false;
+  if (options.warm_start == 1) SL3D_CUDA(st.prev.Alloc(spectralComplex));
+  st.hasStrain = st.hasCoeffs = st.hasPrev = false;
   return SL3DGPU_OK;
 }
 
@@ -852,14 +861,14 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
     SetError("v3d: damping other than 1 is not built");
     return SL3DGPU_ERR_ARGUMENT;
   }
+  // A guess of the stage's end strain (the caller's, or the extrapolation of
+  // warm_start 1) starts the first correction: e = guess - s.
+  const double2* warm = stageGuess;
+  stageGuess = nullptr;
   for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
     double residual = 0.0;
-    if (iteration == 0) {
-      SL3D_TRY(FirstPass(f, sigmaEnd, &residual));
-    } else {
-      SL3D_TRY(Pass(f, s.p, false, sigmaEnd, sNext.p));
-      SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
-    }
+    SL3D_TRY(Pass(f, s.p, iteration == 0, sigmaEnd, sNext.p));
+    SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
     history.push_back(residual);
     info.iterations = iteration + 1;
     info.residual = residual;
@@ -876,7 +885,9 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
     // The correction needs only the accuracy that brings the next FP64
     // residual under rtol: r' is about (its relative change) x (residual),
     // with a factor 10 to spare, and never finer than correction_rtol.
-    SL3D_TRY(Correct(f, std::max(options.correction_rtol, std::min(0.1, 0.1 * options.rtol / residual)), info));
+    SL3D_TRY(Correct(f, std::max(options.correction_rtol, std::min(0.1, 0.1 * options.rtol / residual)), info,
+                     warm));
+    warm = nullptr;
     SL3D_TRY(grid->TensorCoreStatus(stream));
     LaunchAddCorrection(2 * spectralComplex, reinterpret_cast<const float*>(e32.p), reinterpret_cast<double*>(s.p),
                         stream);
@@ -894,8 +905,8 @@ int Viscoelastic3DGpu::FirstPass(const Flavour& f, const double2* sigmaEnd, doub
   double plain = 0.0;
   SL3D_TRY(RelativeChange(sNext.p, s.p, &plain));
   *residual = plain;
-  if (!guessStage) return SL3DGPU_OK;
-  guessStage = false;
+  if (stageGuess == nullptr) return SL3DGPU_OK;
+  stageGuess = nullptr;
   SL3D_TRY(Pass(f, guess.p, false, sigmaEnd, guessNext.p));
   double tried = 0.0;
   SL3D_TRY(RelativeChange(guessNext.p, guess.p, &tried));
@@ -1056,14 +1067,22 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
 
 // e = B e + r from e = r, with the FP64 loop's Anderson schedule, until the
 // relative change is at most the tolerance (or max_iterations passes).
-int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info) {
-  SL3D_CUDA(cudaMemcpyAsync(e32.p, r32.p, spectralComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info, const double2* warm) {
+  if (warm != nullptr) {
+    // the guess's correction e = guess - s (FP32)
+    LaunchResidual32(2 * spectralComplex, reinterpret_cast<const double*>(warm), reinterpret_cast<const double*>(s.p),
+                     reinterpret_cast<float*>(e32.p), stream);
+    SL3D_CHECK_LAUNCH();
+  } else {
+    SL3D_CUDA(cudaMemcpyAsync(e32.p, r32.p, spectralComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+  }
   const bool adaptive = options.anderson_rate > 0.0;
   bool mixing = options.anderson_memory > 0 && !adaptive;
   bool firstMix = true;
   int count = 0, slot = 0;
   if (mixing) SL3D_TRY(Mixer32Reset());
   double previous = 0.0;
+  int first = 0;  // the iteration the plain start's sequence begins at
   for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
     SL3D_TRY(Pass32(f, e32.p, eNext32.p));
     ++info.correction_passes;
@@ -1078,11 +1097,22 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
     }
     const double change = hostResult[0] > 0.0 ? std::sqrt(hostResult[1]) / std::sqrt(hostResult[0]) : 0.0;
     correctionHistory.push_back(change);
+    if (warm != nullptr && iteration == 0) {
+      // A guess whose first change is not well below the plain start's
+      // (about rho / (1 + rho), near a half) is dropped: restart from e = r.
+      warm = nullptr;
+      if (change > kWarmKeep) {
+        SL3D_CUDA(cudaMemcpyAsync(e32.p, r32.p, spectralComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+        first = iteration + 1;
+        continue;
+      }
+      guessTaken = 1;
+    }
     if (change <= tolerance) {
       std::swap(e32, eNext32);
       break;
     }
-    if (adaptive && !mixing && options.anderson_memory > 0 && iteration > 0 &&
+    if (adaptive && !mixing && options.anderson_memory > 0 && iteration > first &&
         change > options.anderson_rate * previous) {
       mixing = true;
       firstMix = true;
@@ -1391,9 +1421,21 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   history.clear();
   correctionHistory.clear();
   guessTaken = 0;
+  // The guess of the step's end strain: the caller's, else (warm_start 1)
+  // the linear extrapolation 2 s_n - s_{n-1} of the last two steps.
+  bool haveGuess = guessArmed;
+  if (!haveGuess && options.warm_start == 1 && st.hasCoeffs && st.hasPrev && dt > 0.0) {
+    if (guess.n != static_cast<size_t>(spectralComplex)) {
+      SL3D_CUDA(guess.Alloc(spectralComplex));
+      SL3D_CUDA(guessNext.Alloc(spectralComplex));
+    }
+    LaunchBlend(spectralComplex, 2.0, st.prev.p, st.coeffs.p, guess.p, stream);
+    SL3D_CHECK_LAUNCH();
+    haveGuess = true;
+  }
   if (scheme != 2 || dt == 0.0) {
     const int one = scheme == 2 ? 1 : scheme;
-    guessStage = guessArmed;
+    stageGuess = haveGuess ? guess.p : nullptr;
     SL3D_TRY(StepOnce(st, scratch, dt, one, s0, s1, info));
   } else {
     const double gamma = host::kSdirk2Gamma;
@@ -1406,6 +1448,15 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
       mid = sigmaMid.p;
     }
     sl3dgpu_step_info i1{}, i2{};
+    // the first stage's guess (the mixed form, which takes it at no FP64
+    // cost): (1 - gamma) s_n + gamma guess
+    stageGuess = nullptr;
+    if (haveGuess && options.precision == 1 && st.hasCoeffs) {
+      if (guessMid.n != static_cast<size_t>(spectralComplex)) SL3D_CUDA(guessMid.Alloc(spectralComplex));
+      LaunchBlend(spectralComplex, gamma, st.coeffs.p, guess.p, guessMid.p, stream);
+      SL3D_CHECK_LAUNCH();
+      stageGuess = guessMid.p;
+    }
     SL3D_TRY(StepOnce(st, scratch, h, 1, s0, mid, i1));
     // the second stage's memory (1 - r) m_n + r Y_1, formed in place in Y_1
     const double r = (1.0 - gamma) / gamma;
@@ -1414,7 +1465,7 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
                          scratch.m[k].r.p, stream);
       SL3D_CHECK_LAUNCH();
     }
-    guessStage = guessArmed;
+    stageGuess = haveGuess ? guess.p : nullptr;
     SL3D_TRY(StepOnce(scratch, scratch, h, 1, mid, s1, i2));
     info.iterations = i1.iterations + i2.iterations;
     info.mixed_passes = i1.mixed_passes + i2.mixed_passes;
@@ -1424,6 +1475,12 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     info.converged = i1.converged && i2.converged;
   }
   guessArmed = false;  // a warm start serves one step
+  stageGuess = nullptr;
+  if (options.warm_start == 1 && st.hasCoeffs) {
+    SL3D_CUDA(cudaMemcpyAsync(st.prev.p, st.coeffs.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                              stream));
+    st.hasPrev = true;
+  }
   std::swap(st.m, scratch.m);
   std::swap(st.strain, scratch.strain);
   std::swap(st.coeffs, scratch.coeffs);

@@ -142,7 +142,8 @@ class Options(_ct.Structure):
                 ("max_iterations", _ct.c_int), ("rtol", _ct.c_double), ("damping", _ct.c_double),
                 ("anderson_memory", _ct.c_int), ("anderson_rate", _ct.c_double), ("precision", _ct.c_int),
                 ("correction_rtol", _ct.c_double), ("solver", _ct.c_int),
-                ("solve_rtol", _ct.c_double), ("solve_max_iterations", _ct.c_int)]
+                ("solve_rtol", _ct.c_double), ("solve_max_iterations", _ct.c_int),
+                ("warm_start", _ct.c_int)]
 
 
 class StepInfo(_ct.Structure):
@@ -154,7 +155,7 @@ class StepInfo(_ct.Structure):
 def default_options(lmax, ngll=5, **kw):
     o = Options(lmax=lmax, ngll=ngll, eps=1e-8, oversampling=1.5, max_iterations=40, rtol=1e-11, damping=1.0,
                 anderson_memory=5, anderson_rate=0.5, precision=0, correction_rtol=1e-5,
-                solver=0, solve_rtol=1e-11, solve_max_iterations=200)
+                solver=0, solve_rtol=1e-11, solve_max_iterations=200, warm_start=0)
     for k, v in kw.items():
         setattr(o, k, v)
     return o

@@ -95,3 +95,29 @@ def test_mixed_and_fp64_gpu_forms_agree_and_fp64_passes_drop(gpu):
     for comp in (0, 1):
         assert rel(results[1][comp], results[0][comp]) < TOL_MIXED
     assert results[1][2] * 3 <= results[0][2]
+
+
+@pytest.mark.gpu
+def test_mixed_warm_start_extrapolation_saves_correction_passes(gpu):
+    # warm_start 1: the extrapolation 2 s_n - s_{n-1} starts the FP32
+    # correction; same results (1e-8 against the oracle), fewer passes
+    lmax = 12
+    o, g0 = _pair(lmax, 20, 5, rms=1.0, ldelta=5, seed=5, precision=1, rtol=1e-10, max_iterations=60)
+    _, g1 = _pair(lmax, 20, 5, rms=1.0, ldelta=5, seed=5, precision=1, rtol=1e-10, max_iterations=60,
+                  warm_start=1)
+    load = cap_load(lmax, o.sigma_scale, 2000.0)
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    s0, s1 = g0.ZeroState(), g1.ZeroState()
+    saved = 0
+    for n in range(5):
+        l0, l1 = load * n / 10, load * (n + 1) / 10
+        io = o.step(dt, 2, l0, l1)
+        i0 = g0.Step(s0, dt, 2, l0, l1)
+        i1 = g1.Step(s1, dt, 2, l0, l1)
+        assert io.converged == i0.converged == i1.converged == 1
+        for comp in (0, 2):
+            assert rel(g1.Surface(comp), o.surface(comp)) < TOL_MIXED, (n, comp)
+        if n >= 2:
+            assert g1.start_taken
+            saved += i0.correction_passes - i1.correction_passes
+    assert saved > 0
