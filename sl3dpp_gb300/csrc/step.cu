@@ -57,14 +57,20 @@ struct GridTensor {
 
 }  // namespace
 
+// A state: the memory tensors and the strain on the grid at the lateral
+// nodes [latFirst, latEnd), the memory as spectral coefficients at the
+// others (mSpec, the same [row][node] layout as the strain coefficients),
+// and the strain coefficients at every node.
 struct V3dState {
   std::vector<GridTensor> m;
+  std::vector<Dev<double2>> mSpec;
   GridTensor strain;
   Dev<double2> coeffs;
   Dev<double2> prev;  // the step before's coefficients (warm_start 1)
   bool hasStrain = false;
   bool hasCoeffs = false;
   bool hasPrev = false;
+  int latFirst = 0, latEnd = 0;  // the lateral range the state is laid out for
 };
 
 class Viscoelastic3DGpu {
@@ -189,6 +195,14 @@ class Viscoelastic3DGpu {
   int BuildFlavour(const host::PointShear& shear, Flavour& f);
   int FlavourOf(int scheme, double dt, Flavour** out);
   int Synthesise(const double2* spectral, GridTensor& out);
+  // Over the nodes [p0, p0 + count) only (the spectral arrays keep their
+  // every-node layout; the grid fields their node-major one).
+  int SynthesiseRange(const double2* spectral, GridTensor& out, int p0, int count);
+  int AnalyseRange(const GridTensor& in, double2* spectral, int p0, int count);
+  // A state laid out for another lateral range moved to the current one.
+  int AdaptState(V3dState& st);
+  SpectralMemoryArgs SpectralArgs(int scheme, double dt, const V3dState& in, V3dState& out, const double2* strain,
+                                  double2* fixed) const;
   int Analyse(const GridTensor& in, double2* spectral);
   int AnalyseWeighted(const GridTensor& in, const double* w, double2* spectral);  // accumulate, lateral nodes
   int WeightedPass(const double2* strain, double2* out);                           // accumulate, lateral nodes
@@ -468,6 +482,8 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
 int Viscoelastic3DGpu::AllocState(V3dState& st) {
   st.m.resize(K);
   for (auto& t : st.m) SL3D_CUDA(t.Alloc(values));
+  st.mSpec.resize(K);
+  for (auto& c : st.mSpec) SL3D_CUDA(c.Alloc(spectralComplex));
   SL3D_CUDA(st.strain.Alloc(values));
   SL3D_CUDA(st.coeffs.Alloc(spectralComplex));
   if (options.warm_start == 1) SL3D_CUDA(st.prev.Alloc(spectralComplex));
@@ -482,6 +498,9 @@ int Viscoelastic3DGpu::ZeroState(V3dState& st) {
     SL3D_CUDA(cudaMemsetAsync(t.c1.p, 0, values * sizeof(double2), stream));
     SL3D_CUDA(cudaMemsetAsync(t.r.p, 0, values * sizeof(double), stream));
   }
+  for (auto& c : st.mSpec) SL3D_CUDA(cudaMemsetAsync(c.p, 0, spectralComplex * sizeof(double2), stream));
+  st.latFirst = lateralFirst;
+  st.latEnd = lateralEnd;
   SL3D_CUDA(cudaStreamSynchronize(stream));
   return SL3DGPU_OK;
 }
@@ -574,6 +593,82 @@ int Viscoelastic3DGpu::Analyse(const GridTensor& in, double2* spectral) {
   SL3D_TRY(grid->LegendreAnalysis(-1, false, spectra, P, 0, P, base + 2 * rows0 * P, false, stream));
   SL3D_TRY(grid->RingAnalysis(true, in.r.p, P, spectra, stream));
   return grid->LegendreAnalysis(0, true, spectra, P, 0, P, base + 2 * (rows0 + rows1) * P, false, stream);
+}
+
+int Viscoelastic3DGpu::SynthesiseRange(const double2* spectral, GridTensor& out, int p0, int count) {
+  if (count <= 0) return SL3DGPU_OK;
+  const auto* base = reinterpret_cast<const double*>(spectral);
+  auto* spectra = reinterpret_cast<double*>(spectraA.p);
+  const long long off = p0 * fieldSize;
+  SL3D_TRY(grid->LegendreSynthesis(-2, false, base, P, p0, count, spectra, stream));
+  SL3D_TRY(grid->RingSynthesis(false, spectra, count, reinterpret_cast<double*>(out.c0.p + off), stream));
+  SL3D_TRY(grid->LegendreSynthesis(-1, false, base + 2 * rows0 * P, P, p0, count, spectra, stream));
+  SL3D_TRY(grid->RingSynthesis(false, spectra, count, reinterpret_cast<double*>(out.c1.p + off), stream));
+  SL3D_TRY(grid->LegendreSynthesis(0, true, base + 2 * (rows0 + rows1) * P, P, p0, count, spectra, stream));
+  return grid->RingSynthesis(true, spectra, count, out.r.p + off, stream);
+}
+
+int Viscoelastic3DGpu::AnalyseRange(const GridTensor& in, double2* spectral, int p0, int count) {
+  if (count <= 0) return SL3DGPU_OK;
+  auto* base = reinterpret_cast<double*>(spectral);
+  auto* spectra = reinterpret_cast<double*>(spectraA.p);
+  const long long off = p0 * fieldSize;
+  SL3D_TRY(grid->RingAnalysis(false, reinterpret_cast<const double*>(in.c0.p + off), count, spectra, stream));
+  SL3D_TRY(grid->LegendreAnalysis(-2, false, spectra, P, p0, count, base, false, stream));
+  SL3D_TRY(grid->RingAnalysis(false, reinterpret_cast<const double*>(in.c1.p + off), count, spectra, stream));
+  SL3D_TRY(grid->LegendreAnalysis(-1, false, spectra, P, p0, count, base + 2 * rows0 * P, false, stream));
+  SL3D_TRY(grid->RingAnalysis(true, in.r.p + off, count, spectra, stream));
+  return grid->LegendreAnalysis(0, true, spectra, P, p0, count, base + 2 * (rows0 + rows1) * P, false, stream);
+}
+
+// The nodes a state holds on the grid follow the operator's lateral range;
+// after set_delta moved it, the nodes that became lateral get their grid
+// memory and strain by synthesis, those that left it their coefficients by
+// analysis (exact for these band-limited fields, to rounding).
+int Viscoelastic3DGpu::AdaptState(V3dState& st) {
+  if (st.latFirst == lateralFirst && st.latEnd == lateralEnd) return SL3DGPU_OK;
+  auto pieces = [](int a0, int a1, int b0, int b1) {
+    // [a0, a1) minus [b0, b1), at most two intervals
+    std::vector<std::pair<int, int>> out;
+    if (a1 <= a0) return out;
+    if (b1 <= b0 || b1 <= a0 || b0 >= a1) {
+      out.emplace_back(a0, a1);
+      return out;
+    }
+    if (a0 < b0) out.emplace_back(a0, b0);
+    if (b1 < a1) out.emplace_back(b1, a1);
+    return out;
+  };
+  for (auto [p0, p1] : pieces(lateralFirst, lateralEnd, st.latFirst, st.latEnd)) {
+    for (int k = 0; k < K; ++k) SL3D_TRY(SynthesiseRange(st.mSpec[k].p, st.m[k], p0, p1 - p0));
+    if (st.hasCoeffs) SL3D_TRY(SynthesiseRange(st.coeffs.p, st.strain, p0, p1 - p0));
+  }
+  for (auto [p0, p1] : pieces(st.latFirst, st.latEnd, lateralFirst, lateralEnd))
+    for (int k = 0; k < K; ++k) SL3D_TRY(AnalyseRange(st.m[k], st.mSpec[k].p, p0, p1 - p0));
+  st.latFirst = lateralFirst;
+  st.latEnd = lateralEnd;
+  return SL3DGPU_OK;
+}
+
+SpectralMemoryArgs Viscoelastic3DGpu::SpectralArgs(int scheme, double dt, const V3dState& in, V3dState& out,
+                                                   const double2* strain, double2* fixed) const {
+  SpectralMemoryArgs a{};
+  a.branches = K;
+  a.scheme = scheme == static_cast<int>(Scheme::BackwardEuler) ? 1 : 0;
+  a.dt = dt;
+  a.rows = rows0 + rows1 + rowsR;
+  a.P = P;
+  a.pLat0 = lateralFirst;
+  a.pLat1 = lateralEnd;
+  a.muBranch = muBranch.p;
+  a.itauRef = itauRef.p;
+  for (int k = 0; k < K; ++k) {
+    a.in[k] = in.mSpec[k].p;
+    a.out[k] = out.mSpec[k].p;
+  }
+  a.s = strain;
+  a.fixedS = fixed;
+  return a;
 }
 
 // Analyse(w f) over the lateral nodes, added to what the spectral tensor holds.
@@ -721,12 +816,25 @@ int Viscoelastic3DGpu::MixerUpdate(int& count, int& slot, bool& first) {
 // SolveElastic + StrainCoefficients into s: the memory force sum_k mu_k m_k,
 // the unrelaxed systems, the load channel at the state's time.
 int Viscoelastic3DGpu::ElasticStrain(const V3dState& st, const double2* sigma) {
-  for (int k = 0; k < K; ++k) {
-    LaunchCombine(values, fieldSize, muBranch.p + static_cast<long long>(k) * P, k == 0, st.m[k].c0.p,
-                  st.m[k].c1.p, st.m[k].r.p, fixedGrid.c0.p, fixedGrid.c1.p, fixedGrid.r.p, stream);
+  // the memory force: on the grid at the lateral nodes, analysed; from the
+  // coefficients at the others
+  const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+  const long long off = p0 * fieldSize, n = static_cast<long long>(count) * fieldSize;
+  for (int k = 0; k < K && count > 0; ++k) {
+    LaunchCombine(n, fieldSize, muBranch.p + static_cast<long long>(k) * P + p0, k == 0, st.m[k].c0.p + off,
+                  st.m[k].c1.p + off, st.m[k].r.p + off, fixedGrid.c0.p + off, fixedGrid.c1.p + off,
+                  fixedGrid.r.p + off, stream);
     SL3D_CHECK_LAUNCH();
   }
-  SL3D_TRY(Analyse(fixedGrid, analysedStart.p));
+  if (count > 0 && K == 0) {
+    SL3D_CUDA(cudaMemsetAsync(fixedGrid.c0.p + off, 0, n * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(fixedGrid.c1.p + off, 0, n * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(fixedGrid.r.p + off, 0, n * sizeof(double), stream));
+  }
+  SL3D_TRY(AnalyseRange(fixedGrid, analysedStart.p, p0, count));
+  V3dState& mutableSt = const_cast<V3dState&>(st);
+  LaunchSpectralSum(SpectralArgs(0, 0.0, st, mutableSt, nullptr, analysedStart.p), stream);
+  SL3D_CHECK_LAUNCH();
   return Pass(*elastic, nullptr, true, sigma, s.p);
 }
 
@@ -734,18 +842,20 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
                                 const double2* sigmaEnd, sl3dgpu_step_info& info) {
   Flavour* f = nullptr;
   SL3D_TRY(FlavourOf(scheme, dt, &f));
-  // The start strain: the cached coefficients, else the analysed cached grid
-  // strain, else a consistent unrelaxed solve.
+  SL3D_TRY(AdaptState(in));
+  const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+  const long long begin = p0 * fieldSize, end = static_cast<long long>(lateralEnd) * fieldSize;
+  // The start strain: the cached coefficients, else a consistent unrelaxed
+  // solve (a state's grid strain is kept only beside its coefficients).
   if (in.hasCoeffs) {
     SL3D_CUDA(cudaMemcpyAsync(s.p, in.coeffs.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
-  } else if (in.hasStrain) {
-    SL3D_TRY(Analyse(in.strain, s.p));
   } else {
     SL3D_TRY(ElasticStrain(in, sigmaStart));
   }
+  // The start strain on the grid, needed at the lateral nodes only.
   const GridTensor* d0 = &in.strain;
   if (!in.hasStrain) {
-    SL3D_TRY(Synthesise(s.p, dGrid));
+    SL3D_TRY(SynthesiseRange(s.p, dGrid, p0, count));
     d0 = &dGrid;
   }
   // Weights, decayed memory (into the output state's memory), lateral
@@ -755,6 +865,8 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   w.scheme = scheme == static_cast<int>(Scheme::BackwardEuler) ? 1 : 0;
   w.dt = dt;
   w.values = values;
+  w.begin = begin;
+  w.end = end;
   w.fieldSize = fieldSize;
   w.factor = factor.p;
   w.muBranch = muBranch.p;
@@ -777,7 +889,11 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   w.fixedr = fixedGrid.r.p;
   LaunchWeights(w, stream);
   SL3D_CHECK_LAUNCH();
-  SL3D_TRY(Analyse(fixedGrid, fixedS.p));
+  // The fixed force: analysed at the lateral nodes, from the coefficients
+  // (decayed in place into the output state) at the others.
+  SL3D_TRY(AnalyseRange(fixedGrid, fixedS.p, p0, count));
+  LaunchSpectralStart(SpectralArgs(scheme, dt, in, out, s.p, fixedS.p), stream);
+  SL3D_CHECK_LAUNCH();
   // The first pass's force from the grid strain in hand: Analyse(W d0) + fixed.
   SL3D_CUDA(cudaMemcpyAsync(analysedStart.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
                             stream));
@@ -793,15 +909,21 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   } else {
     SL3D_TRY(Converge(*f, sigmaEnd, info));
   }
-  // Finish: synthesise the strain, advance the memory.
-  SL3D_TRY(Synthesise(s.p, out.strain));
-  for (int k = 0; k < K; ++k) {
-    LaunchAdvance(values, beta[k].p, out.strain.c0.p, out.strain.c1.p, out.strain.r.p, out.m[k].c0.p,
-                  out.m[k].c1.p, out.m[k].r.p, stream);
+  // Finish: the strain on the grid and the memory advanced at the lateral
+  // nodes, the coefficients advanced at the others.
+  SL3D_TRY(SynthesiseRange(s.p, out.strain, p0, count));
+  for (int k = 0; k < K && count > 0; ++k) {
+    LaunchAdvance(end - begin, beta[k].p + begin, out.strain.c0.p + begin, out.strain.c1.p + begin,
+                  out.strain.r.p + begin, out.m[k].c0.p + begin, out.m[k].c1.p + begin, out.m[k].r.p + begin,
+                  stream);
     SL3D_CHECK_LAUNCH();
   }
+  LaunchSpectralAdvance(SpectralArgs(scheme, dt, out, out, s.p, nullptr), stream);
+  SL3D_CHECK_LAUNCH();
   SL3D_CUDA(cudaMemcpyAsync(out.coeffs.p, s.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
   out.hasStrain = out.hasCoeffs = true;
+  out.latFirst = lateralFirst;
+  out.latEnd = lateralEnd;
   return SL3DGPU_OK;
 }
 
@@ -1460,9 +1582,15 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     SL3D_TRY(StepOnce(st, scratch, h, 1, s0, mid, i1));
     // the second stage's memory (1 - r) m_n + r Y_1, formed in place in Y_1
     const double r = (1.0 - gamma) / gamma;
+    const long long begin = lateralFirst * fieldSize, end = static_cast<long long>(lateralEnd) * fieldSize;
     for (int k = 0; k < K; ++k) {
-      LaunchStageCombine(values, r, st.m[k].c0.p, st.m[k].c1.p, st.m[k].r.p, scratch.m[k].c0.p, scratch.m[k].c1.p,
-                         scratch.m[k].r.p, stream);
+      if (end > begin) {
+        LaunchStageCombine(end - begin, r, st.m[k].c0.p + begin, st.m[k].c1.p + begin, st.m[k].r.p + begin,
+                           scratch.m[k].c0.p + begin, scratch.m[k].c1.p + begin, scratch.m[k].r.p + begin, stream);
+        SL3D_CHECK_LAUNCH();
+      }
+      LaunchSpectralCombine(rows0 + rows1 + rowsR, P, lateralFirst, lateralEnd, r, st.mSpec[k].p,
+                            scratch.mSpec[k].p, stream);
       SL3D_CHECK_LAUNCH();
     }
     stageGuess = haveGuess ? guess.p : nullptr;
@@ -1482,8 +1610,11 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     st.hasPrev = true;
   }
   std::swap(st.m, scratch.m);
+  std::swap(st.mSpec, scratch.mSpec);
   std::swap(st.strain, scratch.strain);
   std::swap(st.coeffs, scratch.coeffs);
+  std::swap(st.latFirst, scratch.latFirst);
+  std::swap(st.latEnd, scratch.latEnd);
   st.hasStrain = st.hasCoeffs = true;
   SL3D_CUDA(cudaStreamSynchronize(stream));
   if (infoOut) *infoOut = info;

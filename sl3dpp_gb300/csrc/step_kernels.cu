@@ -368,10 +368,29 @@ __device__ inline double Phi1(double h, double e) {
   return (1.0 - e) / h;
 }
 
+// A stage's weights at one grid value of step h = dt itau: the decay e, the
+// start strain's share alpha and the end strain's share beta
+// (ExponentialTrapezoidWeights or BackwardEulerWeight).
+__device__ inline void StageWeights(int scheme, double h, double& e, double& alpha, double& beta) {
+  if (scheme == 1) {
+    const double wbe = 1.0 / (1.0 + h);
+    e = wbe;
+    alpha = 0.0;
+    beta = 1.0 - wbe;
+  } else {
+    const double ex = exp(-h);
+    const double phi1 = Phi1(h, ex);
+    e = ex;
+    alpha = phi1 - ex;
+    beta = 1.0 - phi1;
+  }
+}
+
 __global__ void WeightsKernel(WeightsArgs a) {
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   const int P = static_cast<int>(a.values / a.fieldSize);
-  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < a.values; x += stride) {
+  for (long long x = a.begin + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < a.end;
+       x += stride) {
     const int node = static_cast<int>(x / a.fieldSize);
     double w = 0.0;
     double2 f0 = C(0, 0), f1 = C(0, 0);
@@ -672,6 +691,75 @@ __global__ void MixerMixKernel(MixerArgsT<T> a) {
   }
 }
 
+// -- the memory at the non-lateral nodes, spectrally ----------------------------------------------
+
+__device__ inline bool NonLateral(int p, int pLat0, int pLat1) { return p < pLat0 || p >= pLat1; }
+
+__global__ void SpectralStartKernel(SpectralMemoryArgs a) {
+  const long long total = a.rows * a.P;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total; i += stride) {
+    const int p = static_cast<int>(i % a.P);
+    if (!NonLateral(p, a.pLat0, a.pLat1)) continue;
+    const double2 s0 = a.s[i];
+    double2 fixed = C(0, 0);
+    for (int k = 0; k < a.branches; ++k) {
+      double e, alpha, beta;
+      StageWeights(a.scheme, a.dt * a.itauRef[static_cast<long long>(k) * a.P + p], e, alpha, beta);
+      const double2 m = a.in[k][i];
+      const double2 o = C(e * m.x + alpha * s0.x, e * m.y + alpha * s0.y);
+      a.out[k][i] = o;
+      const double mu = a.muBranch[static_cast<long long>(k) * a.P + p];
+      fixed = C(fixed.x + mu * o.x, fixed.y + mu * o.y);
+    }
+    a.fixedS[i] = fixed;
+  }
+}
+
+__global__ void SpectralAdvanceKernel(SpectralMemoryArgs a) {
+  const long long total = a.rows * a.P;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total; i += stride) {
+    const int p = static_cast<int>(i % a.P);
+    if (!NonLateral(p, a.pLat0, a.pLat1)) continue;
+    const double2 s1 = a.s[i];
+    for (int k = 0; k < a.branches; ++k) {
+      double e, alpha, beta;
+      StageWeights(a.scheme, a.dt * a.itauRef[static_cast<long long>(k) * a.P + p], e, alpha, beta);
+      const double2 m = a.out[k][i];
+      a.out[k][i] = C(m.x + beta * s1.x, m.y + beta * s1.y);
+    }
+  }
+}
+
+__global__ void SpectralSumKernel(SpectralMemoryArgs a) {
+  const long long total = a.rows * a.P;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total; i += stride) {
+    const int p = static_cast<int>(i % a.P);
+    if (!NonLateral(p, a.pLat0, a.pLat1)) continue;
+    double2 fixed = C(0, 0);
+    for (int k = 0; k < a.branches; ++k) {
+      const double mu = a.muBranch[static_cast<long long>(k) * a.P + p];
+      const double2 m = a.in[k][i];
+      fixed = C(fixed.x + mu * m.x, fixed.y + mu * m.y);
+    }
+    a.fixedS[i] = fixed;
+  }
+}
+
+__global__ void SpectralCombineKernel(long long rows, int P, int pLat0, int pLat1, double r, const double2* a,
+                                      double2* out) {
+  const long long total = rows * P;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total; i += stride) {
+    const int p = static_cast<int>(i % P);
+    if (!NonLateral(p, pLat0, pLat1)) continue;
+    const double2 x = a[i], y = out[i];
+    out[i] = C((1.0 - r) * x.x + r * y.x, (1.0 - r) * x.y + r * y.y);
+  }
+}
+
 // -- conjugate gradients -----------------------------------------------------------------------
 
 // Warp per (system, row), lanes over the row's columns: the band entries of
@@ -851,8 +939,31 @@ void LaunchSurface(const Geometry& g, const double2* solSph, int component, doub
 }
 
 void LaunchWeights(const WeightsArgs& a, cudaStream_t stream) {
-  prof::Scope scope(prof::kStream, stream, 0.0, a.values * (8.0 + a.branches * 96.0 + 40.0 + 48.0));
-  WeightsKernel<<<StreamBlocks(a.values), 256, 0, stream>>>(a);
+  prof::Scope scope(prof::kStream, stream, 0.0, (a.end - a.begin) * (8.0 + a.branches * 96.0 + 40.0 + 48.0));
+  if (a.end <= a.begin) return;
+  WeightsKernel<<<StreamBlocks(a.end - a.begin), 256, 0, stream>>>(a);
+}
+
+void LaunchSpectralStart(const SpectralMemoryArgs& a, cudaStream_t stream) {
+  const long long n = a.rows * a.P;
+  prof::Scope scope(prof::kStream, stream, 0.0, n * (16.0 + a.branches * 32.0 + 16.0));
+  SpectralStartKernel<<<StreamBlocks(n), 256, 0, stream>>>(a);
+}
+void LaunchSpectralAdvance(const SpectralMemoryArgs& a, cudaStream_t stream) {
+  const long long n = a.rows * a.P;
+  prof::Scope scope(prof::kStream, stream, 0.0, n * (16.0 + a.branches * 32.0));
+  SpectralAdvanceKernel<<<StreamBlocks(n), 256, 0, stream>>>(a);
+}
+void LaunchSpectralSum(const SpectralMemoryArgs& a, cudaStream_t stream) {
+  const long long n = a.rows * a.P;
+  prof::Scope scope(prof::kStream, stream, 0.0, n * (a.branches * 16.0 + 16.0));
+  SpectralSumKernel<<<StreamBlocks(n), 256, 0, stream>>>(a);
+}
+void LaunchSpectralCombine(long long rows, int P, int pLat0, int pLat1, double r, const double2* a, double2* out,
+                           cudaStream_t stream) {
+  const long long n = rows * P;
+  prof::Scope scope(prof::kStream, stream, 0.0, n * 48.0);
+  SpectralCombineKernel<<<StreamBlocks(n), 256, 0, stream>>>(rows, P, pLat0, pLat1, r, a, out);
 }
 
 void LaunchAdvance(long long values, const double* beta, const double2* d0, const double2* d1, const double* dr,

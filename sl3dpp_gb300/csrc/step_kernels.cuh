@@ -74,6 +74,7 @@ struct WeightsArgs {
   int branches;
   int scheme;  // 0 trapezoid, 1 backward Euler
   double dt;
+  long long begin, end;  // the grid values worked on (the lateral nodes')
   long long values, fieldSize;
   const double* factor;     // exp(-delta)
   const double* muBranch;   // [k][P]
@@ -105,6 +106,33 @@ void LaunchStageCombine(long long values, double r, const double2* a0, const dou
 void LaunchCombine(long long values, long long fieldSize, const double* mu, bool first,
                    const double2* m0, const double2* m1, const double* mr, double2* o0, double2* o1,
                    double* orr, cudaStream_t stream);
+// The memory at the nodes outside [pLat0, pLat1) carried as spectral
+// coefficients ([row][node], the three components' rows together): there
+// exp(-delta) = 1, the step weights are one per node, and StartStep's decay
+// and fixed force, Finish's advance and Sdirk2's stage combination act on the
+// coefficients themselves (a transform of a node's grid values is exact for
+// these band-limited fields, so the results are the grid route's to rounding).
+struct SpectralMemoryArgs {
+  int branches, scheme;
+  double dt;
+  long long rows;
+  int P, pLat0, pLat1;
+  const double* muBranch;  // [k][P]
+  const double* itauRef;   // [k][P]
+  const double2* in[2];    // memory coefficients per branch
+  double2* out[2];         // (may alias in)
+  const double2* s;        // strain coefficients: the start's, or the end's for the advance
+  double2* fixedS;         // StartStep: sum_k mu_k of the decayed memory
+};
+// out_k = e_k in_k + alpha_k s; fixedS = sum_k mu_k out_k.
+void LaunchSpectralStart(const SpectralMemoryArgs& a, cudaStream_t stream);
+// out_k += beta_k s.
+void LaunchSpectralAdvance(const SpectralMemoryArgs& a, cudaStream_t stream);
+// fixedS = sum_k mu_k in_k (the unrelaxed solve's memory force).
+void LaunchSpectralSum(const SpectralMemoryArgs& a, cudaStream_t stream);
+// out = (1 - r) a + r out at the non-lateral columns.
+void LaunchSpectralCombine(long long rows, int P, int pLat0, int pLat1, double r, const double2* a, double2* out,
+                           cudaStream_t stream);
 // out = (1 - gamma) a + gamma b over complex values, a or b null for zero.
 void LaunchBlend(long long n, double gamma, const double2* a, const double2* b, double2* out, cudaStream_t stream);
 
