@@ -128,7 +128,17 @@ class Viscoelastic3DGpu {
 
   // the mixed form's FP32 correction: iterate, next iterate, residual,
   // analysed force, right-hand sides, spectra, weight and its own mixer
-  Dev<float2> e32, eNext32, r32, analysed32, rhsSph32, rhsTor32;
+  Dev<float2> e32, r32, rhsSph32, rhsTor32;  // every node
+  // the correction's iterate, next iterate, residual and analysed force at
+  // the lateral nodes only, compact [row][lateral node]; the geometry seen
+  // from those nodes (renumbered from 0)
+  Dev<float2> eL, eNextL, rL, analysedL;
+  long long compactComplex = 0;
+  Geometry geoL{};
+  Dev<int> dElemFirstNodeL;
+  Dev<DegreeInfo> dDegreesL;
+  int geoLFirst = -1, geoLEnd = -1;
+  size_t mixer32Size = 0;
   Dev<float> spectra32A, spectra32B, weight32;
   int mixer32Memory = 0;
   Dev<float> xPrev32, fPrev32;
@@ -211,7 +221,8 @@ class Viscoelastic3DGpu {
   int RelativeChange(const double2* next, const double2* now, double* residual);
   int MixerReset();
   int MixerUpdate(int& count, int& slot, bool& first);
-  int WeightedPass32(const float2* strain, float2* out);  // assigns, lateral nodes
+  int PrepareLateral();
+  int WeightedPass32(const float2* strain, float2* out);  // compact lateral arrays
   int Pass32(const Flavour& f, const float2* e, float2* next);
   int Mixer32Reset();
   int Mixer32Update(int& count, int& slot, bool& first);
@@ -465,13 +476,12 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     SL3D_CUDA(pairResult.Alloc(4));
   }
   if (options.precision == 1) {
-    for (auto* b : {&e32, &eNext32, &r32, &analysed32}) SL3D_CUDA(b->Alloc(spectralComplex));
+    for (auto* b : {&e32, &r32}) SL3D_CUDA(b->Alloc(spectralComplex));
     SL3D_CUDA(rhsSph32.Alloc(rhsSphComplex));
     SL3D_CUDA(rhsTor32.Alloc(std::max<long long>(rhsTorComplex, 1)));
     SL3D_CUDA(spectra32A.Alloc(2 * spectra));
     SL3D_CUDA(spectra32B.Alloc(2 * spectra));
     SL3D_CUDA(weight32.Alloc(values));
-    SL3D_CUDA(cudaMemsetAsync(analysed32.p, 0, spectralComplex * sizeof(float2), stream));
   }
   if (!staticMode) SL3D_TRY(AllocState(scratch));
   SL3D_TRY(BuildFlavour(reference->elastic, *elastic));
@@ -525,14 +535,11 @@ int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
       last = std::max(last, p);
     }
   }
-  lateralFirst = last >= 0 ? first : 0;
-  lateralEnd = last >= 0 ? last + 1 : 0;
+  // whole elements: the range starts at its first node's element's first
+  // node and ends at its last node's element's last
+  lateralFirst = last >= 0 ? elemFirstNode[nodeElement[first]] : 0;
+  lateralEnd = last >= 0 ? elemFirstNode[nodeElement[last]] + geo.np : 0;
   SL3D_CUDA(cudaMemcpy(factor.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
-  if (options.precision == 1) {
-    // The correction's analysed force is written at the lateral columns only.
-    SL3D_CUDA(cudaMemsetAsync(analysed32.p, 0, spectralComplex * sizeof(float2), stream));
-    SL3D_CUDA(cudaStreamSynchronize(stream));
-  }
   return SL3DGPU_OK;
 }
 
@@ -1091,31 +1098,61 @@ int Viscoelastic3DGpu::Run(V3dState& st, const double* times, int nodes, int sch
 
 // -- the mixed form's FP32 correction ---------------------------------------------------------------
 
-// Analyse(W Synthesise(e)) over the lateral nodes into out's lateral columns
-// (the other columns stay zero).
+// The correction's view of the lateral nodes: the geometry with the nodes
+// [lateralFirst, lateralEnd) renumbered from 0 (whole elements), and the
+// compact buffers, rebuilt when the range moves.
+int Viscoelastic3DGpu::PrepareLateral() {
+  if (geoLFirst == lateralFirst && geoLEnd == lateralEnd) return SL3DGPU_OK;
+  const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+  std::vector<int> efn(elemFirstNode.size(), -1);
+  for (size_t e = 0; e < elemFirstNode.size(); ++e) {
+    const int fn = elemFirstNode[e];
+    if (fn >= p0 && fn < lateralEnd) efn[e] = fn - p0;
+  }
+  std::vector<DegreeInfo> dl = degrees;
+  for (auto& d : dl) d.firstNode = std::min(std::max(d.firstNode - p0, 0), count);
+  SL3D_CUDA(dElemFirstNodeL.Upload(efn));
+  SL3D_CUDA(dDegreesL.Upload(dl));
+  geoL = geo;
+  geoL.P = count;
+  geoL.nodeElement = dNodeElement.p + p0;
+  geoL.nodeQ = dNodeQ.p + p0;
+  geoL.nodeR = dNodeR.p + p0;
+  geoL.elemFirstNode = dElemFirstNodeL.p;
+  geoL.degrees = dDegreesL.p;
+  compactComplex = (rows0 + rows1 + rowsR) * count;
+  for (auto* b : {&eL, &eNextL, &rL, &analysedL}) SL3D_CUDA(b->Alloc(std::max<long long>(compactComplex, 1)));
+  geoLFirst = lateralFirst;
+  geoLEnd = lateralEnd;
+  return SL3DGPU_OK;
+}
+
+// Analyse(W Synthesise(e)) of a compact lateral iterate into a compact
+// lateral force.
 int Viscoelastic3DGpu::WeightedPass32(const float2* strain, float2* out) {
   const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
   if (count <= 0) return SL3DGPU_OK;
   const auto* in = reinterpret_cast<const float*>(strain);
   auto* o = reinterpret_cast<float*>(out);
   const float* w = weight32.p + p0 * fieldSize;
-  const long long offs[3] = {0, 2 * rows0 * P, 2 * (rows0 + rows1) * P};
+  const long long offs[3] = {0, 2 * rows0 * count, 2 * (rows0 + rows1) * count};
   const int spins[3] = {-2, -1, 0};
   for (int c = 0; c < 3; ++c) {
     const bool real = c == 2;
-    SL3D_TRY(grid->LegendreSynthesisF(spins[c], real, in + offs[c], P, p0, count, spectra32A.p, stream));
+    SL3D_TRY(grid->LegendreSynthesisF(spins[c], real, in + offs[c], count, 0, count, spectra32A.p, stream));
     SL3D_TRY(grid->RingWeightedF(real, spectra32A.p, count, w, spectra32B.p, stream));
-    SL3D_TRY(grid->LegendreAnalysisF(spins[c], real, spectra32B.p, P, p0, count, o + offs[c], false, stream));
+    SL3D_TRY(grid->LegendreAnalysisF(spins[c], real, spectra32B.p, count, 0, count, o + offs[c], false, stream));
   }
   return SL3DGPU_OK;
 }
 
-// next = B e + r: the lateral force of e alone through the FP32 solves.
+// next = B e + r on the lateral nodes: the lateral force of e alone through
+// the FP32 solves (their solutions, every degree, left in rhs*32).
 int Viscoelastic3DGpu::Pass32(const Flavour& f, const float2* e, float2* next) {
-  SL3D_TRY(WeightedPass32(e, analysed32.p));
+  SL3D_TRY(WeightedPass32(e, analysedL.p));
   SL3D_CUDA(cudaMemsetAsync(rhsSph32.p, 0, rhsSphComplex * sizeof(float2), stream));
   SL3D_CUDA(cudaMemsetAsync(rhsTor32.p, 0, std::max<long long>(rhsTorComplex, 1) * sizeof(float2), stream));
-  LaunchForces(geo, analysed32.p, rhsSph32.p, rhsTor32.p, stream);
+  LaunchForces(geoL, analysedL.p, rhsSph32.p, rhsTor32.p, stream);
   SL3D_CHECK_LAUNCH();
   auto* sph = reinterpret_cast<float*>(rhsSph32.p);
   auto* tor = reinterpret_cast<float*>(rhsTor32.p);
@@ -1125,10 +1162,9 @@ int Viscoelastic3DGpu::Pass32(const Flavour& f, const float2* e, float2* next) {
                            f.bands32.p, f.pivots.p, sph, f.scales32.p, 1, stream));
   SL3D_TRY(BandSolveBatchF(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
                            f.nTorChol, f.bands32.p, f.pivots.p, tor, f.scales32.p, 0, stream));
-  LaunchStrain(geo, rhsSph32.p, rhsTor32.p, next, stream);
+  LaunchStrain(geoL, rhsSph32.p, rhsTor32.p, next, stream);
   SL3D_CHECK_LAUNCH();
-  LaunchAddInPlace(2 * spectralComplex, reinterpret_cast<const float*>(r32.p), reinterpret_cast<float*>(next),
-                   stream);
+  LaunchAddInPlace(2 * compactComplex, reinterpret_cast<const float*>(rL.p), reinterpret_cast<float*>(next), stream);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
@@ -1136,8 +1172,8 @@ int Viscoelastic3DGpu::Pass32(const Flavour& f, const float2* e, float2* next) {
 int Viscoelastic3DGpu::Mixer32Reset() {
   const int memory = options.anderson_memory;
   if (memory <= 0) return SL3DGPU_OK;
-  if (mixer32Memory != memory) {
-    const size_t n = 2 * spectralComplex;
+  const size_t n = 2 * compactComplex;
+  if (mixer32Memory != memory || mixer32Size != n) {
     dG32.resize(memory);
     dF32.resize(memory);
     std::vector<float*> gp(memory), fp(memory);
@@ -1152,6 +1188,7 @@ int Viscoelastic3DGpu::Mixer32Reset() {
     SL3D_CUDA(xPrev32.Alloc(n));
     SL3D_CUDA(fPrev32.Alloc(n));
     mixer32Memory = memory;
+    mixer32Size = n;
   }
   if (gram.n < static_cast<size_t>(memory) * memory) SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
   SL3D_CUDA(cudaMemsetAsync(gram.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
@@ -1160,10 +1197,10 @@ int Viscoelastic3DGpu::Mixer32Reset() {
 
 int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
   MixerArgsT<float> a{};
-  a.n = 2 * spectralComplex;
+  a.n = 2 * compactComplex;
   a.memory = options.anderson_memory;
-  a.x = reinterpret_cast<float*>(e32.p);
-  a.gx = reinterpret_cast<const float*>(eNext32.p);
+  a.x = reinterpret_cast<float*>(eL.p);
+  a.gx = reinterpret_cast<const float*>(eNextL.p);
   a.xPrev = xPrev32.p;
   a.fPrev = fPrev32.p;
   a.dG = dG32Ptr.p;
@@ -1188,15 +1225,25 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
 }
 
 // e = B e + r from e = r, with the FP64 loop's Anderson schedule, until the
-// relative change is at most the tolerance (or max_iterations passes).
+// relative change is at most the tolerance (or max_iterations passes). B
+// reads e at the lateral nodes only, so the iteration runs on their compact
+// columns; e at every node is B e + r of the last pass's solutions, left in
+// e32 for s += e.
 int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info, const double2* warm) {
+  SL3D_TRY(PrepareLateral());
+  const long long rows = rows0 + rows1 + rowsR;
+  const int p0 = lateralFirst, lateral = lateralEnd - lateralFirst;
+  LaunchGatherColumns(rows, P, p0, lateral, r32.p, rL.p, stream);
+  SL3D_CHECK_LAUNCH();
   if (warm != nullptr) {
-    // the guess's correction e = guess - s (FP32)
+    // the guess's correction e = guess - s (FP32), its lateral columns
     LaunchResidual32(2 * spectralComplex, reinterpret_cast<const double*>(warm), reinterpret_cast<const double*>(s.p),
                      reinterpret_cast<float*>(e32.p), stream);
     SL3D_CHECK_LAUNCH();
+    LaunchGatherColumns(rows, P, p0, lateral, e32.p, eL.p, stream);
+    SL3D_CHECK_LAUNCH();
   } else {
-    SL3D_CUDA(cudaMemcpyAsync(e32.p, r32.p, spectralComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(eL.p, rL.p, compactComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
   }
   const bool adaptive = options.anderson_rate > 0.0;
   bool mixing = options.anderson_memory > 0 && !adaptive;
@@ -1204,12 +1251,13 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
   int count = 0, slot = 0;
   if (mixing) SL3D_TRY(Mixer32Reset());
   double previous = 0.0;
-  int first = 0;  // the iteration the plain start's sequence begins at
+  int first = 0;       // the iteration the plain start's sequence begins at
+  bool fresh = false;  // the solutions in rhs*32 are the pass of the final e
   for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
-    SL3D_TRY(Pass32(f, e32.p, eNext32.p));
+    SL3D_TRY(Pass32(f, eL.p, eNextL.p));
     ++info.correction_passes;
-    LaunchRelativeChange(reinterpret_cast<const float*>(eNext32.p), reinterpret_cast<const float*>(e32.p),
-                         2 * spectralComplex, changePartial.p, kChangeBlocks, changeResult.p, stream);
+    LaunchRelativeChange(reinterpret_cast<const float*>(eNextL.p), reinterpret_cast<const float*>(eL.p),
+                         2 * compactComplex, changePartial.p, kChangeBlocks, changeResult.p, stream);
     SL3D_CHECK_LAUNCH();
     SL3D_CUDA(cudaMemcpyAsync(hostResult, changeResult.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
     SL3D_CUDA(cudaStreamSynchronize(stream));
@@ -1224,14 +1272,15 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
       // (about rho / (1 + rho), near a half) is dropped: restart from e = r.
       warm = nullptr;
       if (change > kWarmKeep) {
-        SL3D_CUDA(cudaMemcpyAsync(e32.p, r32.p, spectralComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+        SL3D_CUDA(cudaMemcpyAsync(eL.p, rL.p, compactComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         first = iteration + 1;
         continue;
       }
       guessTaken = 1;
     }
     if (change <= tolerance) {
-      std::swap(e32, eNext32);
+      std::swap(eL, eNextL);
+      fresh = true;
       break;
     }
     if (adaptive && !mixing && options.anderson_memory > 0 && iteration > first &&
@@ -1245,9 +1294,19 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
     if (mixing) {
       SL3D_TRY(Mixer32Update(count, slot, firstMix));
     } else {
-      std::swap(e32, eNext32);
+      std::swap(eL, eNextL);
     }
   }
+  if (!fresh) {
+    // out of passes on a mixed iterate: one more pass for its solutions
+    SL3D_TRY(Pass32(f, eL.p, eNextL.p));
+    ++info.correction_passes;
+  }
+  // e at every node: the strain of the last solutions, plus r.
+  LaunchStrain(geo, rhsSph32.p, rhsTor32.p, e32.p, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchAddInPlace(2 * spectralComplex, reinterpret_cast<const float*>(r32.p), reinterpret_cast<float*>(e32.p), stream);
+  SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
 

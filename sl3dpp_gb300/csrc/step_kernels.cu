@@ -1084,6 +1084,24 @@ void LaunchAddInPlace(long long n, const float* r, float* e, cudaStream_t stream
   prof::Scope scope(prof::kStream, stream, 0.0, n * 12.0);
   AddInPlaceKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, r, e);
 }
+namespace {
+__global__ void GatherColumnsKernel(long long rows, int P, int p0, int count, const float2* in, float2* out) {
+  const long long total = rows * count;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total; t += stride) {
+    const long long row = t / count;
+    out[t] = in[row * P + p0 + t % count];
+  }
+}
+}  // namespace
+
+void LaunchGatherColumns(long long rows, int P, int p0, int count, const float2* in, float2* out,
+                         cudaStream_t stream) {
+  if (rows * count == 0) return;
+  prof::Scope scope(prof::kStream, stream, 0.0, rows * count * 16.0);
+  GatherColumnsKernel<<<StreamBlocks(rows * count), 256, 0, stream>>>(rows, P, p0, count, in, out);
+}
+
 void LaunchCast(long long n, const double* in, float* out, cudaStream_t stream) {
   prof::Scope scope(prof::kStream, stream, 0.0, n * 12.0);
   CastKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, in, out);

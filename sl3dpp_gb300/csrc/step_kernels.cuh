@@ -149,6 +149,10 @@ void LaunchResidual32(long long n, const double* next, const double* now, float*
 void LaunchAddCorrection(long long n, const float* e, double* s, cudaStream_t stream);
 void LaunchAddInPlace(long long n, const float* r, float* e, cudaStream_t stream);
 void LaunchCast(long long n, const double* in, float* out, cudaStream_t stream);
+// out[row][c] = in[row][p0 + c] for c < count: the lateral columns of an
+// every-node [row][P] array, compact.
+void LaunchGatherColumns(long long rows, int P, int p0, int count, const float2* in, float2* out,
+                         cudaStream_t stream);
 
 // -- conjugate gradients (detail/LateralSolve.hpp:71-181) --------------------------------------
 
