@@ -74,6 +74,20 @@ int sl3dgpu_band_solve_batch(const sl3dgpu_band_system* dev_systems,
                              const int* dev_items, int item_count, const double* bands,
                              const int* pivots, double* rhs, const double* scales, int lu,
                              void* stream);
+/* The same Cholesky solves in FP32 (float bands, right-hand sides and
+ * scales; the systems' offsets count floats), optionally over row windows:
+ * dev_windows holds {lo, hi} per system, the right-hand side being zero
+ * outside rows lo..hi. mode 0: every row (dev_windows NULL); 1: both
+ * substitutions over rows lo..n-1 only (rows below lo are left as they
+ * are); 2: the backward substitution's rows 0..lo-1, after a mode-1 solve,
+ * from the solution at rows lo..lo+kd-1. Modes 1 then 2 give mode 0's
+ * solution. (The mixed-precision step's correction passes, whose forces reach
+ * a band of rows; no reference counterpart: LAPACK dpbtrs solves every row.) */
+int sl3dgpu_band_solve_batch_f32(const sl3dgpu_band_system* dev_systems,
+                                 const sl3dgpu_band_system* host_systems, int count,
+                                 const int* dev_items, int item_count, const float* bands,
+                                 float* rhs, const float* scales, const int* dev_windows,
+                                 int mode, void* stream);
 
 /* A banded Cholesky solve (the factor from sl3dgpu_band_cholesky_factor,
  * LAPACK upper storage, and n x nrhs column-major right-hand sides,

@@ -78,6 +78,8 @@ def lib() -> ctypes.CDLL:
         "sl3dgpu_band_work_items": (c_int, [c_void_p, c_int, c_void_p, c_int]),
         "sl3dgpu_band_solve_batch": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                              c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+        "sl3dgpu_band_solve_batch_f32": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                                                 c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
         "sl3dgpu_grid_create": (c_int, [c_int, c_int, c_double, ctypes.POINTER(c_void_p)]),
         "sl3dgpu_grid_destroy": (None, [c_void_p]),
         "sl3dgpu_grid_shape": (c_int, [c_void_p, P_int, P_int]),

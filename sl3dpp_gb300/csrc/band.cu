@@ -266,18 +266,19 @@ struct Lane {
 };
 
 // Stage band columns [c0, c1) (ld values each, contiguous), right-hand-side
-// rows [r0, r1) of this lane's columns, their scales and (pivots != null)
-// pivots [p0, p1) into buffer `buf`, as one copy group.
+// rows [r0, min(r1, rhsEnd)) of this lane's columns, the scales of rows
+// [r0, r1) and (pivots != null) pivots [p0, p1) into buffer `buf`, as one
+// copy group.
 template <class T>
 __device__ inline void StageChunk(const Stage<T>& st, int buf, const T* ab, int ld, int c0, int c1,
                                   const Lane<T>& ln, int r0, int r1, const T* scales, const int* pivots, int p0,
-                                  int p1, int lane) {
+                                  int p1, int lane, int rhsEnd = 0x7fffffff) {
   using T2 = typename PairOf<T>::type;
   const T* src = ab + static_cast<long long>(c0) * ld;
   T* band = st.Band(buf);
   const int count = (c1 - c0) * ld;
   for (int e = lane; e < count; e += kWarp) CpAsync(band + e, src + e);
-  for (int r = r0; r < r1; ++r) {
+  for (int r = r0; r < min(r1, rhsEnd); ++r) {
     T2* dst = st.Rhs(buf, r - r0) + lane;
     const T* at = ln.x + static_cast<long long>(r) * ln.s.nrhs + ln.col;
     if (ln.paired) {
@@ -359,15 +360,30 @@ __device__ inline int SlotAhead(int slot, int t, int depth) {
   return k >= depth ? k - depth : k;
 }
 
+// Which rows a Cholesky solve covers (per system, windows[system] = {lo, hi}:
+// the right-hand side is zero outside rows [lo, hi]).
+enum SolveMode {
+  kSolveAll = 0,         // every row (no windows)
+  kSolveWindow = 1,      // rows lo .. n - 1 of both substitutions: y = 0 below lo
+  kSolveCompletion = 2,  // the backward substitution's rows 0 .. lo - 1 after a
+                         // windowed solve, from x at rows lo .. lo + kd - 1
+};
+
 // U^T U x = b, warp per (system, 64 right-hand sides): the forward and the
 // backward substitution in chunks of rows whose band columns and
 // right-hand-side rows are staged in shared memory two chunks ahead; each
 // lane carries two columns (a band value read serves both), two independent
 // partial sums per column, and the diagonal's reciprocal formed off the
 // dependence chain.
+//
+// With windows, a right-hand side that is zero below row lo has y = 0 there,
+// so the forward substitution starts at lo; the backward one stops at lo
+// (kSolveWindow), and a later completion launch finishes rows below lo from
+// the stored x (unscaled again) with y = 0.
 template <class T>
 __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items, int itemCount,
-                                    const T* bands, T* rhs, const T* scales, SolvePlan plan) {
+                                    const T* bands, T* rhs, const T* scales, SolvePlan plan, const int2* windows,
+                                    int mode) {
   using T2 = typename PairOf<T>::type;
   extern __shared__ __align__(16) unsigned char solveSmem[];
   const int warpInBlock = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
@@ -379,67 +395,91 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
   const int n = ln.s.n, kd = ln.s.ku, ld = kd + 1, depth = plan.depth;
   const T* ab = bands + ln.s.band;
   T2* ring = st.ring + lane;
-  const int chunks = (n + kChunk - 1) / kChunk;
-  // U^T y = b, forward: chunk c holds rows [c kChunk, ...) and their columns.
-  int slot = 0;  // the ring slot of the current row (row mod depth)
+  int lo = 0, hi = n - 1;
+  if (mode != kSolveAll) {
+    const int2 w = windows[item.system];
+    lo = min(max(w.x, 0), n);
+    hi = min(w.y, n - 1);
+  }
+  T2 zero;
+  zero.x = zero.y = T(0);
+  if (mode == kSolveCompletion) {
+    // x at rows lo .. lo + kd - 1 (stored scaled) seeds the ring
+    for (int r = lo; r < min(n, lo + kd); ++r) {
+      T2 v = ln.Load(r);
+      if (ln.s.scale >= 0) {
+        const T f = scales[ln.s.scale + r];
+        v.x /= f;
+        v.y /= f;
+      }
+      ring[(r % depth) * kWarp] = v;
+    }
+  } else {
+    // U^T y = b, forward: chunk c holds rows [lo + c kChunk, ...) and their
+    // columns; right-hand-side rows above hi are zero and not read.
+    const int chunks = (n - lo + kChunk - 1) / kChunk;
+    int slot = lo % depth;  // the ring slot of the current row (row mod depth)
+    Pipeline(
+        chunks,
+        [&](int c) {
+          const int j0 = lo + c * kChunk, j1 = min(n, j0 + kChunk);
+          StageChunk(st, c % kBuffers, ab, ld, j0, j1, ln, j0, min(j1, hi + 1), scales, nullptr, 0, 0, lane);
+        },
+        [&](int c, int buf) {
+          const int j0 = lo + c * kChunk, j1 = min(n, j0 + kChunk);
+          const T* band = st.Band(buf);
+          for (int j = j0; j < j1; ++j) {
+            const T* column = band + (j - j0) * ld + kd;  // column[-t] = U(j - t, j)
+            const T inv = T(1) / column[0];
+            T2 a = j <= hi ? Start(ln, st, buf, j - j0, j, lane) : zero;
+            T2 b = zero;
+            const int reach = min(kd, j - lo);
+            int t = 1;
+            for (; t + 1 <= reach; t += 2) {
+              const T u0 = column[-t], u1 = column[-t - 1];
+              const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
+              const T2 y1 = ring[SlotBack(slot, t + 1, depth) * kWarp];
+              a.x -= u0 * y0.x;
+              a.y -= u0 * y0.y;
+              b.x -= u1 * y1.x;
+              b.y -= u1 * y1.y;
+            }
+            if (t <= reach) {
+              const T u0 = column[-t];
+              const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
+              a.x -= u0 * y0.x;
+              a.y -= u0 * y0.y;
+            }
+            T2 y;
+            y.x = (a.x + b.x) * inv;
+            y.y = (a.y + b.y) * inv;
+            ring[slot * kWarp] = y;
+            ln.Store(j, y);
+            slot = SlotAhead(slot, 1, depth);
+          }
+        });
+  }
+  // U x = y, backward over rows [bottom, top): chunk c holds rows [i0, i1)
+  // counted from the top and the columns [i0, i1 + kd) their updates come
+  // from; below lo (completion) y = 0 and is not read.
+  const int top = mode == kSolveCompletion ? lo : n, bottom = mode == kSolveCompletion ? 0 : lo;
+  const int rhsEnd = mode == kSolveCompletion ? 0 : n;
+  const int chunks = (top - bottom + kChunk - 1) / kChunk;
+  int slot = ((top - 1) % depth + depth) % depth;
   Pipeline(
       chunks,
       [&](int c) {
-        const int j0 = c * kChunk, j1 = min(n, j0 + kChunk);
-        StageChunk(st, c % kBuffers, ab, ld, j0, j1, ln, j0, j1, scales, nullptr, 0, 0, lane);
+        const int i1 = top - c * kChunk, i0 = max(bottom, i1 - kChunk);
+        StageChunk(st, c % kBuffers, ab, ld, i0, min(n, i1 + kd), ln, i0, i1, scales, nullptr, 0, 0, lane, rhsEnd);
       },
       [&](int c, int buf) {
-        const int j0 = c * kChunk, j1 = min(n, j0 + kChunk);
-        const T* band = st.Band(buf);
-        for (int j = j0; j < j1; ++j) {
-          const T* column = band + (j - j0) * ld + kd;  // column[-t] = U(j - t, j)
-          const T inv = T(1) / column[0];
-          T2 a = Start(ln, st, buf, j - j0, j, lane);
-          T2 b;
-          b.x = b.y = T(0);
-          const int reach = min(kd, j);
-          int t = 1;
-          for (; t + 1 <= reach; t += 2) {
-            const T u0 = column[-t], u1 = column[-t - 1];
-            const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
-            const T2 y1 = ring[SlotBack(slot, t + 1, depth) * kWarp];
-            a.x -= u0 * y0.x;
-            a.y -= u0 * y0.y;
-            b.x -= u1 * y1.x;
-            b.y -= u1 * y1.y;
-          }
-          if (t <= reach) {
-            const T u0 = column[-t];
-            const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
-            a.x -= u0 * y0.x;
-            a.y -= u0 * y0.y;
-          }
-          T2 y;
-          y.x = (a.x + b.x) * inv;
-          y.y = (a.y + b.y) * inv;
-          ring[slot * kWarp] = y;
-          ln.Store(j, y);
-          slot = SlotAhead(slot, 1, depth);
-        }
-      });
-  // U x = y, backward: chunk c holds rows [i0, i1) counted from the end and
-  // the columns [i0, i1 + kd) their updates come from.
-  slot = (n - 1) % depth;
-  Pipeline(
-      chunks,
-      [&](int c) {
-        const int i1 = n - c * kChunk, i0 = max(0, i1 - kChunk);
-        StageChunk(st, c % kBuffers, ab, ld, i0, min(n, i1 + kd), ln, i0, i1, scales, nullptr, 0, 0, lane);
-      },
-      [&](int c, int buf) {
-        const int i1 = n - c * kChunk, i0 = max(0, i1 - kChunk);
+        const int i1 = top - c * kChunk, i0 = max(bottom, i1 - kChunk);
         const T* band = st.Band(buf);
         for (int i = i1 - 1; i >= i0; --i) {
           const int r = i - i0;
           const T inv = T(1) / band[r * ld + kd];
-          T2 a = st.Rhs(buf, r)[lane];
-          T2 b;
-          b.x = b.y = T(0);
+          T2 a = rhsEnd > 0 ? st.Rhs(buf, r)[lane] : zero;
+          T2 b = zero;
           const int reach = min(kd, n - 1 - i);
           int t = 1;
           for (; t + 1 <= reach; t += 2) {
@@ -647,8 +687,12 @@ namespace {
 template <class T>
 int SolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
                const int2* devItems, int itemCount, const T* bands, const int* pivots, T* rhs, const T* scales,
-               int lu, cudaStream_t stream) {
+               int lu, cudaStream_t stream, const int2* windows = nullptr, int mode = kSolveAll) {
   if (itemCount == 0) return SL3DGPU_OK;
+  if ((mode != kSolveAll) != (windows != nullptr) || (lu && mode != kSolveAll)) {
+    SetError("band solve: row windows go with a windowed Cholesky solve");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
   if (int st = Validate(hostSystems, count, lu != 0); st != SL3DGPU_OK) return st;
   // The ring spans the solve's reach (kd; kl + ku for LU); a staged chunk the
   // band columns of kChunk rows and of the reach beyond them.
@@ -688,7 +732,7 @@ int SolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system*
     SL3D_CUDA(cudaFuncSetAttribute(CholeskySolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
     CholeskySolveKernel<T><<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount, bands,
-                                                                           rhs, scales, plan);
+                                                                           rhs, scales, plan, windows, mode);
   }
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
@@ -708,6 +752,52 @@ int BandSolveBatchF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sy
                     const float* scales, int lu, cudaStream_t stream) {
   return SolveBatch<float>(devSystems, hostSystems, count, devItems, itemCount, bands, pivots, rhs, scales, lu,
                            stream);
+}
+
+int BandSolveWindowF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                     const int2* devItems, int itemCount, const float* bands, float* rhs, const float* scales,
+                     const int2* windows, bool completion, cudaStream_t stream) {
+  return SolveBatch<float>(devSystems, hostSystems, count, devItems, itemCount, bands, nullptr, rhs, scales, 0,
+                           stream, windows, completion ? kSolveCompletion : kSolveWindow);
+}
+
+namespace {
+// One block per system of up to three lists: rows [lo, hi] of its right-hand
+// sides set to zero.
+struct ZeroList {
+  const sl3dgpu_band_system* systems;
+  const int2* windows;
+  int count;
+  float* rhs;
+};
+__global__ void ZeroRowsKernel(ZeroList a, ZeroList b, ZeroList c) {
+  int i = blockIdx.x;
+  const ZeroList* list = &a;
+  if (i >= a.count) {
+    i -= a.count;
+    list = &b;
+    if (i >= b.count) {
+      i -= b.count;
+      list = &c;
+    }
+  }
+  const sl3dgpu_band_system s = list->systems[i];
+  const int2 w = list->windows[i];
+  const int lo = max(w.x, 0), hi = min(w.y, s.n - 1);
+  if (hi < lo) return;
+  float* base = list->rhs + s.rhs + static_cast<long long>(lo) * s.nrhs;
+  const long long count = static_cast<long long>(hi - lo + 1) * s.nrhs;
+  for (long long e = threadIdx.x; e < count; e += blockDim.x) base[e] = 0.0f;
+}
+}  // namespace
+
+void LaunchZeroRows(const sl3dgpu_band_system* s0, const int2* w0, int n0, float* rhs0,
+                    const sl3dgpu_band_system* s1, const int2* w1, int n1, float* rhs1,
+                    const sl3dgpu_band_system* s2, const int2* w2, int n2, float* rhs2, cudaStream_t stream) {
+  const int blocks = n0 + n1 + n2;
+  if (blocks == 0) return;
+  ZeroRowsKernel<<<blocks, 256, 0, stream>>>(ZeroList{s0, w0, n0, rhs0}, ZeroList{s1, w1, n1, rhs1},
+                                             ZeroList{s2, w2, n2, rhs2});
 }
 
 }  // namespace sl3dgpu
@@ -877,6 +967,24 @@ extern "C" int sl3dgpu_band_solve_batch(const sl3dgpu_band_system* dev_systems,
                                         int lu, void* stream) {
   return BandSolveBatch(dev_systems, host_systems, count, reinterpret_cast<const int2*>(dev_items),
                         item_count, bands, pivots, rhs, scales, lu, AsStream(stream));
+}
+
+extern "C" int sl3dgpu_band_solve_batch_f32(const sl3dgpu_band_system* dev_systems,
+                                            const sl3dgpu_band_system* host_systems, int count,
+                                            const int* dev_items, int item_count, const float* bands,
+                                            float* rhs, const float* scales, const int* dev_windows,
+                                            int mode, void* stream) {
+  const auto* items = reinterpret_cast<const int2*>(dev_items);
+  const auto* windows = reinterpret_cast<const int2*>(dev_windows);
+  if (mode == 0)
+    return SolveBatch<float>(dev_systems, host_systems, count, items, item_count, bands, nullptr, rhs, scales, 0,
+                             AsStream(stream), windows, kSolveAll);
+  if (mode != 1 && mode != 2) {
+    SetError("band solve: mode must be 0, 1 or 2");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return BandSolveWindowF(dev_systems, host_systems, count, items, item_count, bands, rhs, scales, windows,
+                          mode == 2, AsStream(stream));
 }
 
 extern "C" int sl3dgpu_band_work_items(const sl3dgpu_band_system* host_systems, int count,

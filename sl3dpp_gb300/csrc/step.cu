@@ -138,6 +138,11 @@ class Viscoelastic3DGpu {
   Dev<int> dElemFirstNodeL;
   Dev<DegreeInfo> dDegreesL;
   int geoLFirst = -1, geoLEnd = -1;
+  // the dof maps (host copies) and, per degree, the rows {lo, hi} the
+  // lateral nodes' forces reach in its spheroidal and toroidal systems
+  std::vector<int> hostSphMap, hostTorMap;
+  std::vector<int2> sphWindow, torWindow;
+  int SolveWindows(const Flavour& f);
   size_t mixer32Size = 0;
   Dev<float> spectra32A, spectra32B, weight32;
   int mixer32Memory = 0;
@@ -389,6 +394,8 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   }
   rhsSphComplex = sphOff;
   rhsTorComplex = torOff;
+  hostSphMap = sphMap;
+  hostTorMap = torMap;
 
   std::vector<double> elemJac(E);
   for (int e = 0; e < E; ++e) elemJac[e] = msh.Jacobian(e);
@@ -1109,8 +1116,36 @@ int Viscoelastic3DGpu::PrepareLateral() {
     const int fn = elemFirstNode[e];
     if (fn >= p0 && fn < lateralEnd) efn[e] = fn - p0;
   }
+  // The global nodes of the lateral elements; each degree's force and
+  // strain stay within them, and so do the rows its forces reach.
+  const int n = geo.ngll;
+  const int g0 = count > 0 ? nodeElement[p0] * (n - 1) : 0;
+  const int g1 = count > 0 ? nodeElement[lateralEnd - 1] * (n - 1) + n - 1 : -1;
   std::vector<DegreeInfo> dl = degrees;
-  for (auto& d : dl) d.firstNode = std::min(std::max(d.firstNode - p0, 0), count);
+  sphWindow.assign(degrees.size(), make_int2(1 << 30, -1));
+  torWindow.assign(degrees.size(), make_int2(1 << 30, -1));
+  for (size_t l = 0; l < dl.size(); ++l) {
+    auto& d = dl[l];
+    d.firstNode = std::min(std::max(d.firstNode - p0, 0), count);
+    d.firstGlobal = std::max(d.firstGlobal, g0);
+    d.lastGlobal = std::min(d.lastGlobal, g1);
+    if (d.firstNode >= count || d.firstGlobal > d.lastGlobal) {
+      d.firstNode = count;
+      d.firstGlobal = 0;
+      d.lastGlobal = -1;
+      continue;
+    }
+    auto widen = [](int2& w, int dof) {
+      if (dof < 0) return;
+      w.x = std::min(w.x, dof);
+      w.y = std::max(w.y, dof);
+    };
+    for (int gn = d.firstGlobal; gn <= d.lastGlobal; ++gn) {
+      widen(sphWindow[l], hostSphMap[d.sphMap + 2LL * gn]);
+      widen(sphWindow[l], hostSphMap[d.sphMap + 2LL * gn + 1]);
+      if (l >= 1) widen(torWindow[l], hostTorMap[d.torMap + gn]);
+    }
+  }
   SL3D_CUDA(dElemFirstNodeL.Upload(efn));
   SL3D_CUDA(dDegreesL.Upload(dl));
   geoL = geo;
@@ -1146,22 +1181,52 @@ int Viscoelastic3DGpu::WeightedPass32(const float2* strain, float2* out) {
   return SL3DGPU_OK;
 }
 
+// The flavour's per-system row windows for the current lateral range: a
+// Cholesky system's from its degree (its right-hand sides are the degree's
+// 2 (l + 1) real columns), an LU system's every row (solved whole).
+int Viscoelastic3DGpu::SolveWindows(const Flavour& f) {
+  if (f.windowFirst == geoLFirst && f.windowEnd == geoLEnd) return SL3DGPU_OK;
+  auto build = [](const std::vector<sl3dgpu_band_system>& systems, const std::vector<int2>* perDegree,
+                  Dev<int2>& out) -> int {
+    std::vector<int2> w;
+    w.reserve(systems.size());
+    for (const auto& s : systems) {
+      const int l = s.nrhs / 2 - 1;
+      w.push_back(perDegree ? (*perDegree)[l] : make_int2(0, s.n - 1));
+    }
+    SL3D_CUDA(out.Upload(w));
+    return SL3DGPU_OK;
+  };
+  SL3D_TRY(build(f.sphChol, &sphWindow, f.wSphChol));
+  SL3D_TRY(build(f.sphLu, nullptr, f.wSphLu));
+  SL3D_TRY(build(f.torChol, &torWindow, f.wTorChol));
+  f.windowFirst = geoLFirst;
+  f.windowEnd = geoLEnd;
+  return SL3DGPU_OK;
+}
+
 // next = B e + r on the lateral nodes: the lateral force of e alone through
-// the FP32 solves (their solutions, every degree, left in rhs*32).
+// the FP32 solves. The forces reach only the lateral rows of each system, so
+// the substitutions run over those rows and above (row windows); their
+// solutions are complete from the lowest lateral row up, and the end of
+// Correct finishes the rows below for the last pass.
 int Viscoelastic3DGpu::Pass32(const Flavour& f, const float2* e, float2* next) {
   SL3D_TRY(WeightedPass32(e, analysedL.p));
-  SL3D_CUDA(cudaMemsetAsync(rhsSph32.p, 0, rhsSphComplex * sizeof(float2), stream));
-  SL3D_CUDA(cudaMemsetAsync(rhsTor32.p, 0, std::max<long long>(rhsTorComplex, 1) * sizeof(float2), stream));
-  LaunchForces(geoL, analysedL.p, rhsSph32.p, rhsTor32.p, stream);
-  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(SolveWindows(f));
   auto* sph = reinterpret_cast<float*>(rhsSph32.p);
   auto* tor = reinterpret_cast<float*>(rhsTor32.p);
-  SL3D_TRY(BandSolveBatchF(f.dSphChol.p, f.sphChol.data(), static_cast<int>(f.sphChol.size()), f.iSphChol.p,
-                           f.nSphChol, f.bands32.p, f.pivots.p, sph, f.scales32.p, 0, stream));
+  LaunchZeroRows(f.dSphChol.p, f.wSphChol.p, static_cast<int>(f.sphChol.size()), sph, f.dSphLu.p, f.wSphLu.p,
+                 static_cast<int>(f.sphLu.size()), sph, f.dTorChol.p, f.wTorChol.p,
+                 static_cast<int>(f.torChol.size()), tor, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchForces(geoL, analysedL.p, rhsSph32.p, rhsTor32.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(BandSolveWindowF(f.dSphChol.p, f.sphChol.data(), static_cast<int>(f.sphChol.size()), f.iSphChol.p,
+                            f.nSphChol, f.bands32.p, sph, f.scales32.p, f.wSphChol.p, false, stream));
   SL3D_TRY(BandSolveBatchF(f.dSphLu.p, f.sphLu.data(), static_cast<int>(f.sphLu.size()), f.iSphLu.p, f.nSphLu,
                            f.bands32.p, f.pivots.p, sph, f.scales32.p, 1, stream));
-  SL3D_TRY(BandSolveBatchF(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
-                           f.nTorChol, f.bands32.p, f.pivots.p, tor, f.scales32.p, 0, stream));
+  SL3D_TRY(BandSolveWindowF(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
+                            f.nTorChol, f.bands32.p, tor, f.scales32.p, f.wTorChol.p, false, stream));
   LaunchStrain(geoL, rhsSph32.p, rhsTor32.p, next, stream);
   SL3D_CHECK_LAUNCH();
   LaunchAddInPlace(2 * compactComplex, reinterpret_cast<const float*>(rL.p), reinterpret_cast<float*>(next), stream);
@@ -1302,7 +1367,14 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
     SL3D_TRY(Pass32(f, eL.p, eNextL.p));
     ++info.correction_passes;
   }
-  // e at every node: the strain of the last solutions, plus r.
+  // the last pass's solutions below the lateral rows (y = 0 there), then
+  // e at every node: the strain of those solutions, plus r
+  auto* sph = reinterpret_cast<float*>(rhsSph32.p);
+  auto* tor = reinterpret_cast<float*>(rhsTor32.p);
+  SL3D_TRY(BandSolveWindowF(f.dSphChol.p, f.sphChol.data(), static_cast<int>(f.sphChol.size()), f.iSphChol.p,
+                            f.nSphChol, f.bands32.p, sph, f.scales32.p, f.wSphChol.p, true, stream));
+  SL3D_TRY(BandSolveWindowF(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
+                            f.nTorChol, f.bands32.p, tor, f.scales32.p, f.wTorChol.p, true, stream));
   LaunchStrain(geo, rhsSph32.p, rhsTor32.p, e32.p, stream);
   SL3D_CHECK_LAUNCH();
   LaunchAddInPlace(2 * spectralComplex, reinterpret_cast<const float*>(r32.p), reinterpret_cast<float*>(e32.p), stream);

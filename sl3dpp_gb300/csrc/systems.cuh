@@ -22,6 +22,17 @@ int BandSolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sys
 int BandSolveBatchF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
                     const int2* devItems, int itemCount, const float* bands, const int* pivots, float* rhs,
                     const float* scales, int lu, cudaStream_t stream);
+// The FP32 Cholesky solves over row windows (windows[system] = {lo, hi}, the
+// right-hand side zero outside [lo, hi]): the substitutions' rows lo .. n - 1,
+// or (completion) the backward substitution's rows 0 .. lo - 1 after them.
+int BandSolveWindowF(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system* hostSystems, int count,
+                     const int2* devItems, int itemCount, const float* bands, float* rhs, const float* scales,
+                     const int2* windows, bool completion, cudaStream_t stream);
+// Rows [lo, hi] of the systems' right-hand sides (up to three lists, each
+// with its own right-hand-side array) set to zero.
+void LaunchZeroRows(const sl3dgpu_band_system* s0, const int2* w0, int n0, float* rhs0,
+                    const sl3dgpu_band_system* s1, const int2* w1, int n1, float* rhs1,
+                    const sl3dgpu_band_system* s2, const int2* w2, int n2, float* rhs2, cudaStream_t stream);
 std::vector<int2> BandWorkItems(const sl3dgpu_band_system* hostSystems, int count);
 
 // A device allocation owned by value.
@@ -76,6 +87,10 @@ struct Flavour {
   Dev<sl3dgpu_band_system> dSphChol, dSphLu, dTorChol;
   Dev<int2> iSphChol, iSphLu, iTorChol;
   int nSphChol = 0, nSphLu = 0, nTorChol = 0;
+  // The FP32 correction's row windows per system ({lo, hi}: the rows its
+  // lateral forces reach), for the lateral node range [windowFirst, windowEnd).
+  mutable int windowFirst = -1, windowEnd = -1;
+  mutable Dev<int2> wSphChol, wSphLu, wTorChol;
 };
 
 

@@ -191,3 +191,91 @@ def test_gpu_failure_indices_match(gpu):
     want = o.oracle_band_lu_factor(_oracle.ptr(ours.copy()), n, kl, ku, _oracle.ptr(pivots))
     assert want > 0
     assert BandLuFactor(ours.copy(), n, kl, ku, np.zeros(n, dtype=np.int32)) == want
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scaled", [False, True])
+def test_gpu_fp32_row_windows_complete_to_the_every_row_solve(gpu, scaled):
+    """The FP32 solves of the mixed form's correction passes, whose forces
+    reach a band of rows: right-hand sides zero outside rows [lo, hi] solved
+    over rows lo..n-1 (mode 1) and then below lo (mode 2) give the every-row
+    FP32 solve (mode 0) -- the rows from lo up identically (the skipped
+    products are exact zeros), the rows below within FP32 rounding (the
+    completion restarts from the stored, scaled solution) -- and that solve
+    agrees with the FP64 oracle to FP32 accuracy. Windows cover an empty
+    range, the first row, an interior band and the last rows."""
+    import torch
+
+    from sl3dpp_gb300 import _lib
+    from sl3dpp_gb300.band import BandCholeskyFactor
+
+    o = _oracle.load()
+    shapes = [(1803, 17, 130, (1210, 1400)), (481, 5, 64, (0, 30)), (300, 14, 66, (100, 90)),
+              (200, 4, 7, (150, 199)), (97, 17, 514, (40, 60))]
+    systems, bands, rhs64, scales, windows = [], [], [], [], []
+    band_off = rhs_off = scale_off = 0
+    for k, (n, kd, nrhs, (lo, hi)) in enumerate(shapes):
+        ab = symmetric_band(n, kd, 2.0 * kd + 1.0, 40 + k)
+        assert BandCholeskyFactor(ab, n, kd) == 0
+        b = uniform(n * nrhs, 50 + k).reshape(n, nrhs)
+        b[:lo] = 0.0
+        b[hi + 1:] = 0.0
+        s = _lib.BandSystem(n=n, kl=kd, ku=kd, nrhs=nrhs, band=band_off, pivots=0, rhs=rhs_off,
+                            scale=scale_off if scaled else -1, pinned0=-1, pinned1=-1)
+        systems.append(s)
+        bands.append(ab)
+        rhs64.append(b)
+        scales.append(np.random.default_rng(60 + k).uniform(0.5, 2.0, n))
+        windows.append((lo if lo <= hi else n, hi))
+        band_off += ab.size
+        rhs_off += b.size
+        scale_off += n
+    host = (_lib.BandSystem * len(systems))(*systems)
+    count = _lib.lib().sl3dgpu_band_work_items(host, len(systems), None, 0)
+    items = np.zeros(2 * count, dtype=np.int32)
+    assert _lib.lib().sl3dgpu_band_work_items(host, len(systems), items.ctypes.data, count) == count
+    dev = lambda a, dt: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=gpu)
+    d_sys = torch.tensor(np.frombuffer(bytes(host), dtype=np.uint8), device=gpu)
+    d_items = dev(items, torch.int32)
+    d_bands = dev(np.concatenate(bands), torch.float32)
+    d_scales = dev(np.concatenate(scales), torch.float32)
+    d_windows = dev(np.array(windows, dtype=np.int32).ravel(), torch.int32)
+    b0 = np.concatenate([b.ravel() for b in rhs64]).astype(np.float32)
+    stream = torch.cuda.current_stream().cuda_stream
+    solve = _lib.lib().sl3dgpu_band_solve_batch_f32
+
+    def run(modes):
+        x = dev(b0, torch.float32)
+        for mode in modes:
+            st = solve(d_sys.data_ptr(), host, len(systems), d_items.data_ptr(), count, d_bands.data_ptr(),
+                       x.data_ptr(), d_scales.data_ptr(), d_windows.data_ptr() if mode else None, mode, stream)
+            assert st == _lib.OK
+        torch.cuda.synchronize()
+        return x.cpu().numpy()
+
+    full = run([0])
+    windowed = run([1, 2])
+    partial = run([1])
+    at = 0
+    for k, (n, kd, nrhs, _) in enumerate(shapes):
+        lo = windows[k][0]
+        f = full[at:at + n * nrhs].reshape(n, nrhs)
+        w = windowed[at:at + n * nrhs].reshape(n, nrhs)
+        p = partial[at:at + n * nrhs].reshape(n, nrhs)
+        assert np.array_equal(p[lo:], f[lo:]), k
+        assert np.array_equal(w[lo:], f[lo:]), k
+        if scaled and np.any(f):
+            assert rel(w, f) < 1e-5, k
+        else:
+            assert np.array_equal(w, f), k
+        # the FP32 solve against the FP64 oracle (scaling: D^-1 A^-1 D^-1 b as
+        # the scaled systems solve, x = D (U^T U)^-1 D b)
+        d = scales[k] if scaled else np.ones(n)
+        want = (rhs64[k] * d[:, None]).T.copy().ravel()
+        o.oracle_band_cholesky_solve(_oracle.ptr(bands[k]), n, kd, _oracle.ptr(want), nrhs)
+        want = want.reshape(nrhs, n).T * d[:, None]
+        if np.any(want):
+            assert rel(f.astype(np.float64), want) < 1e-4, k
+        else:
+            assert not np.any(f), k
+        at += n * nrhs
