@@ -79,6 +79,10 @@ def workload_config(precision="mixed"):
             "warm_start": ("the previous step's strain, and the extrapolation 2 s_n - s_{n-1} of the last two "
                            "steps as the FP32 correction's start" if precision == "mixed" else
                            "the previous step's strain coefficients (the reference's plain warm start)"),
+            "fp64_contractions": ("the FP64 passes' Legendre contractions emulated on the tensor cores: 7 BF16 "
+                                  "slices a value under power-of-two row/column scales, exact FP32 slice products, "
+                                  "levels joined in FP64 (about 49 bits)" if precision == "mixed" else
+                                  "FP64 units"),
             "l2": "working set far above L2 (memory tensors ~3.3 GB per array)",
             "parallelism": "replicas (one independent operator per GPU)"}
 
@@ -146,7 +150,8 @@ class ClockSampler:
 # -- the GPU arm --------------------------------------------------------------------------------
 
 KIND_NAMES = ["legendre_synthesis", "legendre_analysis", "ring_fft", "force_assembly", "strain_recovery",
-              "band_solve", "streaming", "anderson", "other", "legendre_f32", "ring_fft_f32", "band_solve_f32"]
+              "band_solve", "streaming", "anderson", "other", "legendre_f32", "ring_fft_f32", "band_solve_f32",
+              "legendre_f64_tc"]
 
 
 def profile_read():
@@ -194,7 +199,8 @@ def build_operator(device, precision):
                         Options.defaults(LMAX, NGLL, rtol=RTOL, max_iterations=MAX_ITERATIONS,
                                          precision=1 if precision == "mixed" else 0,
                                          correction_rtol=CORRECTION_RTOL,
-                                         warm_start=1 if precision == "mixed" else 0))
+                                         warm_start=1 if precision == "mixed" else 0,
+                                         fp64_emulation=1 if precision == "mixed" else 0))
     grid = SurfaceGrid(LMAX, 0, 1.5)
     c = configs.delta_coefficients(LMAX, LDELTA, DELTA_RMS, DELTA_SEED)
     pattern = grid.SynthesiseBatch(torch.tensor(c, device=device), 1)
@@ -284,6 +290,14 @@ def roofline(prof, fp64_gflops, fp32_gflops):
     share = p["ms"] / sum(v["ms"] for v in prof.values())
     compute = {"legendre_synthesis": ("fp64", fp64_gflops), "legendre_analysis": ("fp64", fp64_gflops),
                "legendre_f32": ("fp32", fp32_gflops)}
+    if p["flops"] > 0 and kind == "legendre_f64_tc":
+        # algorithmic FP64 flops against the measured dense BF16 tensor rate
+        # (the 28 slice products a step are not counted)
+        achieved = p["flops"] / max(p["launches"], 1) / per_launch_s / 1e12
+        peak = peaks["bf16_tflops"]
+        return {"kernel": kind, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": ncu_traffic(kind), "peak_source": source,
+                "share_of_timed": share}
     if p["flops"] > 0 and kind in compute:
         bound, gflops = compute[kind]
         achieved = p["flops"] / max(p["launches"], 1) / per_launch_s / 1e12

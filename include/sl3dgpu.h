@@ -111,6 +111,11 @@ typedef struct sl3dgpu_grid sl3dgpu_grid;
 int sl3dgpu_grid_create(int lmax, int nmax, double oversampling, sl3dgpu_grid** out);
 void sl3dgpu_grid_destroy(sl3dgpu_grid* grid);
 int sl3dgpu_grid_shape(const sl3dgpu_grid* grid, int* ntheta, int* nphi);
+/* The grid's FP64 Legendre contractions: 0 on the FP64 units, 1 emulated on
+ * the tensor cores (seven BF16 slices a value under a power-of-two scale per
+ * row and column, exact FP32 products, levels joined in FP64: about 49 bits
+ * of each operand; depths beyond 448 stay on the FP64 units). */
+int sl3dgpu_grid_set_fp64_emulation(sl3dgpu_grid* grid, int on);
 /* Host copies of the colatitudes and their Gauss-Legendre weights. */
 int sl3dgpu_grid_colatitudes(const sl3dgpu_grid* grid, double* theta, double* weights);
 /* SurfaceGrid::SynthesiseSpinBatch / ExpandSpinBatch (SurfaceGrid.hpp:217-253):
@@ -162,6 +167,8 @@ typedef struct sl3dgpu_v3d_options {
   int warm_start;           /* 0: each step starts from the previous strain (the reference's start);
                                1: also guesses 2 s_n - s_{n-1}, the mixed form's FP32 correction
                                starting from it (the FP64 form tries it as a first pass) */
+  int fp64_emulation;       /* 0: the FP64 Legendre contractions on the FP64 units; 1: emulated on
+                               the tensor cores (sl3dgpu_grid_set_fp64_emulation) */
 } sl3dgpu_v3d_options;
 
 /* Viscoelastic3D::StepInfo (Viscoelastic3D.hpp:357-375). */
@@ -315,7 +322,8 @@ long long sl3dgpu_launch_count(void);
  * its algorithmic work: kinds 0 Legendre synthesis, 1 Legendre analysis,
  * 2 ring FFTs, 3 force assembly, 4 strain recovery, 5 band solves,
  * 6 streaming weights/memory, 7 Anderson sweeps, 8 other, and the mixed
- * form's FP32 passes: 9 Legendre contractions, 10 ring FFTs, 11 band solves. */
+ * form's FP32 passes: 9 Legendre contractions, 10 ring FFTs, 11 band solves;
+ * 12 the FP64 Legendre contractions emulated on the tensor cores. */
 int sl3dgpu_profile_enable(int on);
 int sl3dgpu_profile_reset(void);
 int sl3dgpu_profile_read(int kind, double* ms, long long* launches, double* flops, double* bytes);

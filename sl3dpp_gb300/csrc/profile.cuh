@@ -21,7 +21,8 @@ enum Kind {
   kLegendre32 = 9,   // the mixed form's FP32 contractions (synthesis and analysis)
   kRing32 = 10,      // its FP32 ring passes
   kBandSolve32 = 11, // its FP32 band solves
-  kKinds = 12
+  kLegendre64Tc = 12, // FP64 contractions emulated on the tensor cores (both directions)
+  kKinds = 13
 };
 
 // Counts one launch; with timing on, records its start event.

@@ -549,6 +549,10 @@ int Grid::Create(int lmax, int nmax, double oversampling, std::unique_ptr<Grid>&
 Grid::~Grid() {
   cudaFree(dTcError_);
   for (auto& [key, panel] : panels_) cudaFree(panel);
+  for (auto& [key, panel] : panels64_) {
+    cudaFree(panel.slices);
+    cudaFree(panel.rowExp);
+  }
   cudaFree(dTheta);
   cudaFree(dWeights);
   cudaFree(dTwiddle);
@@ -557,6 +561,9 @@ Grid::~Grid() {
     cudaFree(b.items);
     cudaFree(b.tcItems);
     cudaFree(b.packed);
+    cudaFree(b.tc64Items);
+    cudaFree(b.packed64);
+    cudaFree(b.colExp);
   }
   cudaFree(scratchSpectra_);
   cudaFree(scratchCoeffs_);
@@ -640,6 +647,7 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
     }
     b.maxM = std::max(b.maxM, it.M);
     b.maxN = std::max(b.maxN, it.N);
+    b.maxK = std::max(b.maxK, it.K);
     b.flops += 2.0 * it.M * it.N * it.K;
     items.push_back(it);
   }
@@ -673,6 +681,30 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
     b.maxATiles = std::max(b.maxATiles, h.mTiles * h.kSteps);
     b.maxBTiles = std::max(b.maxBTiles, h.nTiles * h.kSteps);
     b.tcHost.push_back(h);
+    // the FP64 emulation's tiles: 128 rows, 64 columns, 16 deep, seven
+    // slices a tile
+    Tc64Item e{};
+    e.M = g.M;
+    e.N = g.N;
+    e.K = g.K;
+    e.mTiles = h.mTiles;
+    e.kSteps = h.kSteps;
+    e.nTiles = (g.N + kTc64TileN - 1) / kTc64TileN;
+    e.ldc = g.ldc;
+    e.ldb = g.ldb;
+    e.aPanel = b.panel64;
+    e.bPack = b.packed64Count;
+    e.b = g.b;
+    e.c = g.c;
+    e.rowExp = b.rowExps;
+    e.colExp = b.colExps;
+    b.panel64 += static_cast<long long>(e.mTiles) * e.kSteps * kTc64Slices * kTcTileM * kTcTileK;
+    b.packed64Count += static_cast<long long>(e.nTiles) * e.kSteps * kTc64Slices * kTc64TileN * kTcTileK;
+    b.rowExps += g.M;
+    b.colExps += g.N;
+    b.maxNTiles64 = std::max(b.maxNTiles64, e.nTiles);
+    b.maxBTiles64 = std::max(b.maxBTiles64, e.nTiles * e.kSteps);
+    b.tc64Host.push_back(e);
   }
   *out = &batches_.emplace(key, b).first->second;
   return SL3DGPU_OK;
@@ -688,6 +720,48 @@ int Grid::RunGemm(const Batch& b, const double* A, const double* B, double* C, b
   return SL3DGPU_OK;
 }
 
+// The FP64 contraction emulated on the tensor cores: the spin's split
+// panel for this direction made on first use, the batch's items, packed-B
+// buffer and column exponents on its first use; then B split and packed, and
+// the contraction.
+int Grid::RunGemm64(int N, bool real, Batch& b, const double* B, double* C, bool accumulate,
+                    cudaStream_t stream) {
+  if (b.count == 0) return SL3DGPU_OK;
+  if (dTcError_ == nullptr) {
+    SL3D_CUDA(cudaMalloc(&dTcError_, sizeof(int)));
+    SL3D_CUDA(cudaMemset(dTcError_, 0, sizeof(int)));
+  }
+  if (b.tc64Items == nullptr) {
+    SL3D_CUDA(cudaMalloc(&b.tc64Items, b.tc64Host.size() * sizeof(Tc64Item)));
+    SL3D_CUDA(cudaMemcpy(b.tc64Items, b.tc64Host.data(), b.tc64Host.size() * sizeof(Tc64Item),
+                         cudaMemcpyHostToDevice));
+    SL3D_CUDA(cudaMalloc(&b.packed64, std::max<long long>(b.packed64Count, 1) * sizeof(uint16_t)));
+    SL3D_CUDA(cudaMalloc(&b.colExp, std::max<long long>(b.colExps, 1) * sizeof(int)));
+  }
+  const std::array<int, 3> key{N, real ? 1 : 0, b.analysis ? 1 : 0};
+  auto found = panels64_.find(key);
+  if (found == panels64_.end()) {
+    const SpinTable* t = nullptr;
+    if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
+    Panel64 panel;
+    SL3D_CUDA(cudaMalloc(&panel.slices, std::max<long long>(b.panel64, 1) * sizeof(uint16_t)));
+    SL3D_CUDA(cudaMalloc(&panel.rowExp, std::max<long long>(b.rowExps, 1) * sizeof(int)));
+    prof::Scope scope(prof::kOther, stream);
+    LaunchPanelA64(b.items, b.tc64Items, b.count, b.maxM, b.maxATiles, t->values, panel.rowExp, panel.slices,
+                   stream);
+    SL3D_CHECK_LAUNCH();
+    found = panels64_.emplace(key, panel).first;
+  }
+  {
+    prof::Scope scope(prof::kStream, stream, 0.0, 8.0 * b.colExps + 2.0 * b.packed64Count);
+    LaunchPackB64(b.tc64Items, b.count, b.maxN, b.maxBTiles64, B, b.colExp, b.packed64, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  prof::Scope scope(prof::kLegendre64Tc, stream, b.flops);
+  return RunGemm64Tc(b.tc64Items, b.count, b.maxMTiles, b.maxNTiles64, found->second.slices, b.packed64,
+                     found->second.rowExp, b.colExp, C, accumulate, dTcError_, stream);
+}
+
 int Grid::LegendreSynthesis(int N, bool real, const double* coeffs, int P, int p0, int count,
                             double* spectra, cudaStream_t stream) {
   if (count == 0) return SL3DGPU_OK;
@@ -701,6 +775,8 @@ int Grid::LegendreSynthesis(int N, bool real, const double* coeffs, int P, int p
     if (t->Rows(m, lmax) == 0)
       SL3D_CUDA(cudaMemsetAsync(spectra + static_cast<long long>(m - mlo) * ntheta * 2LL * count, 0,
                                 sizeof(double) * ntheta * 2 * count, stream));
+  if (emulateFp64 && b->maxK <= kTc64MaxK)
+    return RunGemm64(N, real, *MutableBatch(N, real, false, P, p0, count), coeffs, spectra, false, stream);
   return RunGemm(*b, t->values, coeffs, spectra, false, stream);
 }
 
@@ -711,6 +787,8 @@ int Grid::LegendreAnalysis(int N, bool real, const double* spectra, int P, int p
   if (int st = Table(N, &t); st != SL3DGPU_OK) return st;
   const Batch* b = nullptr;
   if (int st = BatchFor(N, real, true, P, p0, count, &b); st != SL3DGPU_OK) return st;
+  if (emulateFp64 && b->maxK <= kTc64MaxK)
+    return RunGemm64(N, real, *MutableBatch(N, real, true, P, p0, count), spectra, coeffs, accumulate, stream);
   return RunGemm(*b, t->values, spectra, coeffs, accumulate, stream);
 }
 
@@ -951,6 +1029,15 @@ extern "C" int sl3dgpu_grid_shape(const sl3dgpu_grid* grid, int* ntheta, int* np
   }
   if (ntheta) *ntheta = grid->grid->ntheta;
   if (nphi) *nphi = grid->grid->nphi;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_grid_set_fp64_emulation(sl3dgpu_grid* grid, int on) {
+  if (grid == nullptr || (on != 0 && on != 1)) {
+    SetError("grid: null handle, or fp64 emulation not 0 or 1");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  grid->grid->emulateFp64 = on != 0;
   return SL3DGPU_OK;
 }
 

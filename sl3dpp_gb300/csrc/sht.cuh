@@ -18,6 +18,7 @@
 #pragma once
 
 #include <array>
+#include <cstdint>
 #include <map>
 #include <memory>
 #include <vector>
@@ -48,6 +49,18 @@ struct GemmItem {
   int sAi, sAk, ldb, ldc;
 };
 
+// One item of the FP64 contraction emulated on the tensor cores: 128-row
+// tiles of A, 64-column tiles of B, 16-deep steps.
+struct Tc64Item {
+  int M, N, K, mTiles;
+  int kSteps, nTiles, ldc, ldb;
+  long long aPanel;  // BF16 values: the item's panel, [mTile][kStep][slice][128 x 16]
+  long long bPack;   // BF16 values: its packed B, [nTile][kStep][slice][64 x 16]
+  long long b, c;    // FP64 offsets of B's source and of C
+  long long rowExp;  // ints: the power-of-two exponents of its M rows of A
+  long long colExp;  // ints: those of its N columns of B (per call)
+};
+
 // A tensor-core item's host description (mirrors TcItem in tc_gemm.cuh).
 struct TcItemHost {
   int M, N, K, mTiles;
@@ -62,6 +75,10 @@ class Grid {
   ~Grid();
 
   int lmax = 0, nmax = 0, band = 0, ntheta = 0, nphi = 0;
+  // The FP64 contractions emulated on the tensor cores (tc_gemm64.cu)
+  // rather than run on the FP64 units; batches deeper than the emulation's
+  // exactness bound keep the FP64 units.
+  bool emulateFp64 = false;
   std::vector<double> theta, weights;  // host copies
   double* dTheta = nullptr;
   double* dWeights = nullptr;
@@ -136,7 +153,24 @@ class Grid {
     int tileN = 0, maxMTiles = 0, maxNTiles = 0, maxATiles = 0, maxBTiles = 0;
     long long panelFloats = 0, packedFloats = 0;
     float* packed = nullptr;
+    int maxK = 0;
+    // the FP64 emulation's form: items, extents, packed B and column
+    // exponents (made on first use)
+    std::vector<Tc64Item> tc64Host;
+    Tc64Item* tc64Items = nullptr;
+    int maxNTiles64 = 0, maxBTiles64 = 0;
+    long long panel64 = 0, packed64Count = 0, rowExps = 0, colExps = 0;
+    uint16_t* packed64 = nullptr;
+    int* colExp = nullptr;
   };
+  // The table split for the FP64 emulation per (spin, real, direction): its
+  // slice panels and row exponents.
+  struct Panel64 {
+    uint16_t* slices = nullptr;
+    int* rowExp = nullptr;
+  };
+  std::map<std::array<int, 3>, Panel64> panels64_;
+  int RunGemm64(int N, bool real, Batch& b, const double* B, double* C, bool accumulate, cudaStream_t stream);
   // The table pre-tiled for the tensor cores per (spin, real, direction).
   std::map<std::array<int, 3>, float*> panels_;
   std::map<std::array<long long, 6>, Batch> batches_;

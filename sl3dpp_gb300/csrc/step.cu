@@ -280,6 +280,10 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     SetError("v3d: warm_start 0 (the previous step's strain) or 1 (the extrapolation of the last two)");
     return SL3DGPU_ERR_ARGUMENT;
   }
+  if (opt.fp64_emulation != 0 && opt.fp64_emulation != 1) {
+    SetError("v3d: fp64_emulation 0 (the FP64 units) or 1 (the tensor cores)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
   if (opt.precision == 1 && !(opt.correction_rtol > 0.0 && opt.correction_rtol < 1.0)) {
     SetError("v3d: the mixed form needs 0 < correction_rtol < 1");
     return SL3DGPU_ERR_ARGUMENT;
@@ -307,6 +311,7 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   SL3D_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   SL3D_CUDA(cudaMallocHost(&hostResult, 8 * sizeof(double)));
   SL3D_TRY(Grid::Create(opt.lmax, 2, opt.oversampling, grid));
+  grid->emulateFp64 = opt.fp64_emulation == 1;
   // The step: the long-term material, the Gauss memory points of every
   // element where a branch relaxes. The static perturbation problem: the
   // unrelaxed material and the GLL nodes of every solid element above the
@@ -935,6 +940,9 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   LaunchSpectralAdvance(SpectralArgs(scheme, dt, out, out, s.p, nullptr), stream);
   SL3D_CHECK_LAUNCH();
   SL3D_CUDA(cudaMemcpyAsync(out.coeffs.p, s.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  // a tensor-core contraction that gave up waiting leaves its output
+  // unspecified: the step fails rather than return it
+  if (grid->emulateFp64) SL3D_TRY(grid->TensorCoreStatus(stream));
   out.hasStrain = out.hasCoeffs = true;
   out.latFirst = lateralFirst;
   out.latEnd = lateralEnd;

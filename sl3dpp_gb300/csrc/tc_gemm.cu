@@ -20,22 +20,7 @@ namespace {
 
 constexpr int kStages = 3;
 constexpr int kThreads = 128;
-constexpr int kWaitLimit = 1 << 22;
 constexpr int kATileFloats = kTcTileM * kTcTileK;  // one part: 2048 floats, 8 KB
-
-__device__ inline uint32_t SmemAddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-// Shared-memory matrix descriptor, no swizzle, K-major: start address,
-// leading byte offset (between core matrices along K), stride byte offset
-// (between 8-row groups along M/N), descriptor version 1.
-__device__ inline uint64_t Descriptor(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
-  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
-  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
-  d |= static_cast<uint64_t>(1) << 46;
-  return d;
-}
 
 // Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B,
 // both K-major, N and M.
@@ -54,21 +39,6 @@ __device__ inline float RoundTf32(float x) {
 // rows in the core-matrix layout [k / 4][row / 8][row % 8][k % 4].
 __device__ inline int TileIndex(int row, int k, int rows) {
   return (k >> 2) * (rows * 4) + (row >> 3) * 32 + (row & 7) * 4 + (k & 3);
-}
-
-__device__ inline bool WaitParity(uint32_t bar, uint32_t phase) {
-  for (int i = 0; i < kWaitLimit; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(bar), "r"(phase)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 
 // Tensor-memory columns for an accumulator of n columns: a power of two, at

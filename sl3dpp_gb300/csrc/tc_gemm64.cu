@@ -1,0 +1,357 @@
+// The FP64 Legendre contraction emulated on the tcgen05 tensor cores (see
+// tc_gemm.cuh): C(i, n) (+)= sum_k A(i, k) B(k, n) in FP64 from exact BF16
+// slice products (the Ozaki splitting).
+//
+// Splitting. Row i of A has the exponent e_i with max_k |A(i, k)| < 2^{e_i},
+// column n of B the exponent f_n likewise; x = A(i, k) 2^{-e_i} (|x| < 1) is
+// written x = sum_{p < 7} s_p 2^{-7 (p + 1)} + r with integers |s_0| <= 128,
+// |s_p| <= 64 (p > 0) and |r| <= 2^{-50}, each step exact in FP64 (x 2^7,
+// then less the nearest integer). The integers are exact in BF16.
+//
+// Products. Level d = p + q gathers sum_k s_p(A) s_q(B) over p + q = d, at
+// most (d + 3) 2^12 per k in magnitude, so below 2^24 -- exact in the FP32
+// accumulator -- for K <= 455 at d = 6. The levels d < 7 are kept (28
+// products per 16-deep step) and joined in FP64:
+//   C(i, n) = 2^{e_i + f_n} sum_d 2^{-7 (d + 2)} acc_d(i, n).
+//
+// Kernel. One CTA of four warps per (64-column tile, 128-row tile, item),
+// the column tiles of a row tile adjacent in the launch so that its A panel
+// is read from HBM once. One elected thread runs the K loop as the FP32
+// contraction does (tc_gemm.cu): it arms a stage's "full" mbarrier, issues
+// two TMA bulk copies (A's seven slices, 28 KB; B's, 14 KB), four stages in
+// flight, and when they have landed issues the step's 28 tcgen05.mma
+// kind::f16 into the level accumulators (tensor-memory columns 64 d ..
+// 64 d + 63 of 512) and commits them to the stage's "empty" mbarrier. Every
+// wait has an iteration limit. The epilogue reads the seven levels with
+// tcgen05.ld, one lane quarter per warp, joins them in FP64 and stores (or
+// adds) the rows in range.
+#include <cstdint>
+
+#include "profile.cuh"
+#include "tc_gemm.cuh"
+
+namespace sl3dgpu {
+namespace {
+
+constexpr int kSlices = kTc64Slices;
+constexpr int kTileN = kTc64TileN;
+constexpr int kStages = 4;
+constexpr int kThreads = 128;
+constexpr int kATile = kTcTileM * kTcTileK;  // BF16 values of one slice of an A tile: 2048 (4 KB)
+constexpr int kBTile = kTileN * kTcTileK;    // of a B tile: 1024 (2 KB)
+constexpr uint32_t kTmemColumns = 512;       // 7 levels x 64 columns, rounded up to a power of two
+
+static_assert(kSlices * kTileN <= static_cast<int>(kTmemColumns), "the levels fit in tensor memory");
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M.
+__host__ __device__ constexpr uint32_t InstrDescriptorBf16(int n, int m) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(n >> 3) << 17) |
+         (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+// The BF16 bits of an integer of magnitude at most 256 (exact: its float has
+// at most eight significant bits, all in the upper half).
+__device__ inline uint32_t Bf16Bits(double integer) {
+  return __float_as_uint(static_cast<float>(integer)) >> 16;
+}
+
+// x (|x| < 1) as kSlices integer slices, packed as BF16 bits.
+__device__ inline void Split(double x, uint32_t (&s)[kSlices]) {
+#pragma unroll
+  for (int p = 0; p < kSlices; ++p) {
+    const double y = x * 128.0;
+    const double r = rint(y);
+    s[p] = Bf16Bits(r);
+    x = y - r;
+  }
+}
+
+// The exponent e with max < 2^e (0 for max = 0).
+__device__ inline int ExponentAbove(double max) {
+  int e = 0;
+  frexp(max, &e);
+  return e;
+}
+
+// Offset (in BF16 values) of element (row, k) of a K-major 16-deep tile of
+// `rows` rows in the core-matrix layout [k / 8][row / 8][row % 8][k % 8].
+__device__ inline int Tile16Index(int row, int k, int rows) {
+  return (k >> 3) * (rows * 8) + (row >> 3) * 64 + (row & 7) * 8 + (k & 7);
+}
+
+// Eight consecutive-k slices of one row (s[q][p]: value q, slice p) stored as
+// one 16-byte core-matrix row per slice.
+__device__ inline void StoreSlices(uint16_t* tile, int sliceStride, int at, const uint32_t (&s)[8][kSlices]) {
+#pragma unroll
+  for (int p = 0; p < kSlices; ++p) {
+    uint4 v;
+    v.x = s[0][p] | (s[1][p] << 16);
+    v.y = s[2][p] | (s[3][p] << 16);
+    v.z = s[4][p] | (s[5][p] << 16);
+    v.w = s[6][p] | (s[7][p] << 16);
+    *reinterpret_cast<uint4*>(tile + p * sliceStride + at) = v;
+  }
+}
+
+// Row exponents of A, one thread per (item, row): the maximum over the
+// item's depth.
+__global__ void RowExpKernel(const GemmItem* items, const Tc64Item* tcItems, const double* table, int* rowExp) {
+  const GemmItem g = items[blockIdx.y];
+  const Tc64Item it = tcItems[blockIdx.y];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.M; i += gridDim.x * blockDim.x) {
+    double mx = 0.0;
+    for (int k = 0; k < g.K; ++k)
+      mx = fmax(mx, fabs(table[g.a + static_cast<long long>(i) * g.sAi + static_cast<long long>(k) * g.sAk]));
+    rowExp[it.rowExp + i] = ExponentAbove(mx);
+  }
+}
+
+// A's panel: one thread per (item, tile, 8-deep K group, row).
+__global__ void PanelA64Kernel(const GemmItem* items, const Tc64Item* tcItems, const double* table,
+                               const int* rowExp, uint16_t* panels) {
+  const GemmItem g = items[blockIdx.y];
+  const Tc64Item it = tcItems[blockIdx.y];
+  const long long total = static_cast<long long>(it.mTiles) * it.kSteps * 2 * kTcTileM;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int r = static_cast<int>(t % kTcTileM);
+    const long long rest = t / kTcTileM;
+    const int kg = static_cast<int>(rest % 2);
+    const long long tile = rest / 2;
+    const int ks = static_cast<int>(tile % it.kSteps), mt = static_cast<int>(tile / it.kSteps);
+    const int i = mt * kTcTileM + r, k0 = ks * kTcTileK + 8 * kg;
+    const int e = i < g.M ? rowExp[it.rowExp + i] : 0;
+    uint32_t s[8][kSlices];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = k0 + q;
+      const double v = (i < g.M && k < g.K) ? table[g.a + static_cast<long long>(i) * g.sAi +
+                                                    static_cast<long long>(k) * g.sAk]
+                                            : 0.0;
+      Split(ldexp(v, -e), s[q]);
+    }
+    StoreSlices(panels + it.aPanel + tile * kSlices * kATile, kATile, Tile16Index(r, 8 * kg, kTcTileM), s);
+  }
+}
+
+// Column exponents of B, one thread per (item, column).
+__global__ void ColExpKernel(const Tc64Item* tcItems, const double* B, int* colExp) {
+  const Tc64Item it = tcItems[blockIdx.y];
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < it.N; n += gridDim.x * blockDim.x) {
+    double mx = 0.0;
+    for (int k = 0; k < it.K; ++k) mx = fmax(mx, fabs(B[it.b + static_cast<long long>(k) * it.ldb + n]));
+    colExp[it.colExp + n] = ExponentAbove(mx);
+  }
+}
+
+// B packed: one thread per (item, tile, 8-deep K group, column); a warp's
+// reads of one k are 32 consecutive columns.
+__global__ void PackB64Kernel(const Tc64Item* tcItems, const double* B, const int* colExp, uint16_t* packed) {
+  const Tc64Item it = tcItems[blockIdx.y];
+  const long long total = static_cast<long long>(it.nTiles) * it.kSteps * 2 * kTileN;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int nn = static_cast<int>(t % kTileN);
+    const long long rest = t / kTileN;
+    const int kg = static_cast<int>(rest % 2);
+    const long long tile = rest / 2;
+    const int ks = static_cast<int>(tile % it.kSteps), nt = static_cast<int>(tile / it.kSteps);
+    const int n = nt * kTileN + nn, k0 = ks * kTcTileK + 8 * kg;
+    const int e = n < it.N ? colExp[it.colExp + n] : 0;
+    uint32_t s[8][kSlices];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = k0 + q;
+      const double v = (n < it.N && k < it.K) ? B[it.b + static_cast<long long>(k) * it.ldb + n] : 0.0;
+      Split(ldexp(v, -e), s[q]);
+    }
+    StoreSlices(packed + it.bPack + tile * kSlices * kBTile, kBTile, Tile16Index(nn, 8 * kg, kTileN), s);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcItems, const uint16_t* panels,
+                                                           const uint16_t* packed, const int* rowExp,
+                                                           const int* colExp, double* C, bool accumulate,
+                                                           int* errorFlag) {
+  const Tc64Item it = tcItems[blockIdx.z];
+  const int nt = blockIdx.x, mt = blockIdx.y;
+  if (mt >= it.mTiles || nt >= it.nTiles) return;  // the whole CTA, before any tensor-memory work
+  const int i0 = mt * kTcTileM, n0 = nt * kTileN;
+  const int nCols = min(kTileN, it.N - n0);
+  constexpr uint32_t aBytes = kSlices * kATile * 2, bBytes = kSlices * kBTile * 2;
+
+  extern __shared__ __align__(128) unsigned char tc64Smem[];
+  uint16_t* sA = reinterpret_cast<uint16_t*>(tc64Smem);  // kStages x kSlices x kATile
+  uint16_t* sB = sA + kStages * kSlices * kATile;          // kStages x kSlices x kBTile
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + kStages * kSlices * kBTile);
+  uint64_t* empty = full + kStages;
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(empty + kStages);
+  __shared__ int okShared;
+  const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(SmemAddr(tmemSlot)),
+                 "r"(kTmemColumns)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(full + s)), "r"(1) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(empty + s)), "r"(1) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmemSlot;
+
+  if (tid == 0) {
+    const uint16_t* aSrc = panels + it.aPanel + static_cast<long long>(mt) * it.kSteps * kSlices * kATile;
+    const uint16_t* bSrc = packed + it.bPack + static_cast<long long>(nt) * it.kSteps * kSlices * kBTile;
+    constexpr uint32_t idesc = InstrDescriptorBf16(kTileN, kTcTileM);
+    uint32_t phaseFull[kStages] = {0, 0, 0, 0}, phaseEmpty[kStages] = {0, 0, 0, 0};
+    bool ok = true;
+    auto issue = [&](int ks) {
+      const int buf = ks % kStages;
+      if (ks >= kStages) {
+        ok = ok && WaitParity(SmemAddr(empty + buf), phaseEmpty[buf]);
+        phaseEmpty[buf] ^= 1u;
+      }
+      if (!ok) return;
+      const uint32_t bar = SmemAddr(full + buf);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(aBytes + bBytes)
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              SmemAddr(sA + buf * kSlices * kATile)),
+          "l"(aSrc + static_cast<long long>(ks) * kSlices * kATile), "r"(aBytes), "r"(bar)
+          : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              SmemAddr(sB + buf * kSlices * kBTile)),
+          "l"(bSrc + static_cast<long long>(ks) * kSlices * kBTile), "r"(bBytes), "r"(bar)
+          : "memory");
+    };
+    for (int ks = 0; ks < min(kStages - 1, it.kSteps); ++ks) issue(ks);
+    for (int ks = 0; ks < it.kSteps && ok; ++ks) {
+      if (ks + kStages - 1 < it.kSteps) issue(ks + kStages - 1);
+      if (!ok) break;
+      const int buf = ks % kStages;
+      ok = WaitParity(SmemAddr(full + buf), phaseFull[buf]);
+      phaseFull[buf] ^= 1u;
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t aBase = SmemAddr(sA + buf * kSlices * kATile);
+      const uint32_t bBase = SmemAddr(sB + buf * kSlices * kBTile);
+      constexpr uint32_t aLbo = kTcTileM * 16, bLbo = kTileN * 16, sbo = 128;
+#pragma unroll
+      for (int d = 0; d < kSlices; ++d) {
+#pragma unroll
+        for (int p = 0; p <= d; ++p) {
+          const uint64_t dA = Descriptor(aBase + p * kATile * 2, aLbo, sbo);
+          const uint64_t dB = Descriptor(bBase + (d - p) * kBTile * 2, bLbo, sbo);
+          const uint32_t enable = (ks > 0 || p > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred r;\n\t"
+              "setp.ne.b32 r, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, r;\n\t}" ::"r"(tmem + d * kTileN),
+              "l"(dA), "l"(dB), "r"(idesc), "r"(enable)
+              : "memory");
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       SmemAddr(empty + buf))
+                   : "memory");
+    }
+    // The last step's commit covers every MMA before it.
+    if (ok && it.kSteps > 0) {
+      const int last = (it.kSteps - 1) % kStages;
+      ok = WaitParity(SmemAddr(empty + last), phaseEmpty[last]);
+    }
+    okShared = ok ? 1 : 0;
+    if (!ok) atomicExch(errorFlag, 1);
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (okShared) {
+    // Epilogue: this warp's lane quarter (32 rows), 16 columns at a time, the
+    // seven levels joined in FP64, smallest first.
+    const int i = i0 + 32 * warp + lane;
+    const int e = i < it.M ? rowExp[it.rowExp + i] : 0;
+    double* c = C + it.c + static_cast<long long>(i) * it.ldc + n0;
+    for (int c0 = 0; c0 < kTileN; c0 += 16) {
+      uint32_t r[kSlices][16];
+#pragma unroll
+      for (int d = 0; d < kSlices; ++d) {
+        const uint32_t addr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(d * kTileN + c0);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];"
+            : "=r"(r[d][0]), "=r"(r[d][1]), "=r"(r[d][2]), "=r"(r[d][3]), "=r"(r[d][4]), "=r"(r[d][5]),
+              "=r"(r[d][6]), "=r"(r[d][7]), "=r"(r[d][8]), "=r"(r[d][9]), "=r"(r[d][10]), "=r"(r[d][11]),
+              "=r"(r[d][12]), "=r"(r[d][13]), "=r"(r[d][14]), "=r"(r[d][15])
+            : "r"(addr)
+            : "memory");
+      }
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (i < it.M) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int n = c0 + q;
+          if (n >= nCols) continue;
+          double sum = 0.0;
+#pragma unroll
+          for (int d = kSlices - 1; d >= 0; --d)
+            sum += ldexp(static_cast<double>(__uint_as_float(r[d][q])), -7 * (d + 2));
+          const double v = ldexp(sum, e + colExp[it.colExp + n0 + n]);
+          c[n] = accumulate ? c[n] + v : v;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemColumns) : "memory");
+}
+
+}  // namespace
+
+void LaunchPanelA64(const GemmItem* items, const Tc64Item* tcItems, int count, int maxM, int maxATiles,
+                    const double* table, int* rowExp, uint16_t* panels, cudaStream_t stream) {
+  if (count == 0) return;
+  RowExpKernel<<<dim3(static_cast<unsigned>((maxM + 127) / 128), count), 128, 0, stream>>>(items, tcItems, table,
+                                                                                          rowExp);
+  const long long perItem = static_cast<long long>(maxATiles) * 2 * kTcTileM;
+  const unsigned blocks = static_cast<unsigned>(std::min<long long>((perItem + 255) / 256, 4096));
+  PanelA64Kernel<<<dim3(blocks, count), 256, 0, stream>>>(items, tcItems, table, rowExp, panels);
+}
+
+void LaunchPackB64(const Tc64Item* tcItems, int count, int maxN, int maxBTiles, const double* B, int* colExp,
+                   uint16_t* packed, cudaStream_t stream) {
+  if (count == 0) return;
+  ColExpKernel<<<dim3(static_cast<unsigned>((maxN + 127) / 128), count), 128, 0, stream>>>(tcItems, B, colExp);
+  const long long perItem = static_cast<long long>(maxBTiles) * 2 * kTileN;
+  const unsigned blocks = static_cast<unsigned>(std::min<long long>((perItem + 255) / 256, 4096));
+  PackB64Kernel<<<dim3(blocks, count), 256, 0, stream>>>(tcItems, B, colExp, packed);
+}
+
+int RunGemm64Tc(const Tc64Item* tcItems, int count, int maxMTiles, int maxNTiles, const uint16_t* panels,
+                const uint16_t* packed, const int* rowExp, const int* colExp, double* C, bool accumulate,
+                int* errorFlag, cudaStream_t stream) {
+  if (count == 0 || maxMTiles == 0 || maxNTiles == 0) return SL3DGPU_OK;
+  constexpr size_t smem = static_cast<size_t>(kStages) * kSlices * (kATile + kBTile) * sizeof(uint16_t) +
+                          2 * kStages * sizeof(uint64_t) + 16;
+  static_assert(smem <= 227 * 1024, "the stages fit in shared memory");
+  SL3D_CUDA(cudaFuncSetAttribute(TcGemm64Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  dim3 grid(static_cast<unsigned>(maxNTiles), static_cast<unsigned>(maxMTiles), static_cast<unsigned>(count));
+  TcGemm64Kernel<<<grid, kThreads, smem, stream>>>(tcItems, panels, packed, rowExp, colExp, C, accumulate,
+                                                   errorFlag);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+}  // namespace sl3dgpu

@@ -30,10 +30,15 @@ def _stream() -> int:
 class SurfaceGrid:
     """A device grid handle (SurfaceGrid's shared Wigner table, on the GPU)."""
 
-    def __init__(self, lmax: int, nmax: int = 0, oversampling: float = 1.0):
+    def __init__(self, lmax: int, nmax: int = 0, oversampling: float = 1.0, fp64_emulation: bool = False):
+        """fp64_emulation: the Legendre contractions emulated on the tensor
+        cores (BF16 slices, exact products, FP64 joins) rather than run on the
+        FP64 units."""
         handle = c_void_p()
         check(lib().sl3dgpu_grid_create(lmax, nmax, float(oversampling), ctypes.byref(handle)))
         self._handle = handle
+        if fp64_emulation:
+            check(lib().sl3dgpu_grid_set_fp64_emulation(handle, 1))
         self.lmax = lmax
         self.nmax = nmax
         nt, nph = ctypes.c_int(), ctypes.c_int()

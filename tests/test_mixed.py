@@ -121,3 +121,25 @@ def test_mixed_warm_start_extrapolation_saves_correction_passes(gpu):
             assert g1.start_taken
             saved += i0.correction_passes - i1.correction_passes
     assert saved > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fp64_contractions_emulated_on_the_tensor_cores_keep_the_bar(gpu, precision):
+    # fp64_emulation 1: the FP64 passes' Legendre contractions from exact
+    # BF16 slice products; the steps still meet the oracle at the form's bar
+    # (1e-10 FP64, 1e-8 mixed) with the oracle's pass counts or fewer
+    lmax = 12
+    tol = 1e-10 if precision == 0 else TOL_MIXED
+    o, g = _pair(lmax, 20, 5, rms=1.0, ldelta=5, seed=5, precision=precision, rtol=1e-10, max_iterations=60,
+                 fp64_emulation=1, warm_start=1)
+    load = cap_load(lmax, o.sigma_scale, 2000.0)
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    state = g.ZeroState()
+    for n in range(4):
+        l0, l1 = load * n / 10, load * (n + 1) / 10
+        io = o.step(dt, 2, l0, l1)
+        ig = g.Step(state, dt, 2, l0, l1)
+        assert io.converged == ig.converged == 1
+        for comp in (0, 2):
+            assert rel(g.Surface(comp), o.surface(comp)) < tol, (n, comp)

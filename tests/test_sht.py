@@ -143,10 +143,10 @@ def test_oracle_reality_relation_of_the_basis():
 
 # -- the GPU grid --------------------------------------------------------------------------
 
-def _grid_and_oracle_grid(lmax, oversampling, nmax=2):
+def _grid_and_oracle_grid(lmax, oversampling, nmax=2, fp64_emulation=False):
     from sl3dpp_gb300.grid import SurfaceGrid
 
-    g = SurfaceGrid(lmax, nmax, oversampling)
+    g = SurfaceGrid(lmax, nmax, oversampling, fp64_emulation)
     theta, w, nphi = _oracle.grid(lmax, oversampling)
     assert g.ntheta == theta.size and g.nphi == nphi
     assert np.max(np.abs(g.theta - theta)) < 1e-15
@@ -155,11 +155,14 @@ def _grid_and_oracle_grid(lmax, oversampling, nmax=2):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("emulated", [False, True])
 @pytest.mark.parametrize("lmax,oversampling,count", [(12, 1.0, 3), (16, 1.5, 5), (33, 1.5, 2)])
-def test_gpu_spin_transforms_match_oracle(gpu, lmax, oversampling, count):
+def test_gpu_spin_transforms_match_oracle(gpu, lmax, oversampling, count, emulated):
+    """Both forms of the FP64 contraction, the FP64 units' and the tensor
+    cores' emulation, at the FP64 bar (1e-12 of the largest value)."""
     import torch
 
-    g, theta, w, nphi = _grid_and_oracle_grid(lmax, oversampling)
+    g, theta, w, nphi = _grid_and_oracle_grid(lmax, oversampling, fp64_emulation=emulated)
     for N in (-2, -1, 0, 1, 2):
         cs = [random_spin_coefficients(lmax, N, salt=17 * p) for p in range(count)]
         want = np.concatenate([_oracle.synthesise_spin(lmax, N, theta, nphi, c) for c in cs])
@@ -173,11 +176,12 @@ def test_gpu_spin_transforms_match_oracle(gpu, lmax, oversampling, count):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("emulated", [False, True])
 @pytest.mark.parametrize("lmax,oversampling,count", [(12, 1.0, 3), (32, 1.5, 4)])
-def test_gpu_real_transforms_match_oracle(gpu, lmax, oversampling, count):
+def test_gpu_real_transforms_match_oracle(gpu, lmax, oversampling, count, emulated):
     import torch
 
-    g, theta, w, nphi = _grid_and_oracle_grid(lmax, oversampling)
+    g, theta, w, nphi = _grid_and_oracle_grid(lmax, oversampling, fp64_emulation=emulated)
     cs = [hermitian_real_coefficients(lmax, salt=3 * p) for p in range(count)]
     want = np.concatenate([_oracle.synthesise_real(lmax, theta, nphi, c) for c in cs])
     got = g.SynthesiseBatch(torch.tensor(np.concatenate(cs), device=gpu), count).cpu().numpy()
@@ -193,13 +197,14 @@ def test_gpu_real_transforms_match_oracle(gpu, lmax, oversampling, count):
 
 
 @pytest.mark.gpu
-def test_gpu_round_trip_at_lmax_256(gpu):
+@pytest.mark.parametrize("emulated", [False, True])
+def test_gpu_round_trip_at_lmax_256(gpu, emulated):
     import torch
 
     lmax = 256
     from sl3dpp_gb300.grid import SurfaceGrid
 
-    g = SurfaceGrid(lmax, 2, 1.5)
+    g = SurfaceGrid(lmax, 2, 1.5, emulated)
     assert (g.ntheta, g.nphi) == (385, 800)
     rng = np.random.default_rng(5)
     for N in (-2, -1):
@@ -207,3 +212,26 @@ def test_gpu_round_trip_at_lmax_256(gpu):
         c = torch.tensor(rng.standard_normal(2 * size).view(np.complex128), device=gpu)
         back = g.ExpandSpinBatch(N, g.SynthesiseSpinBatch(N, c, 1), 1)
         assert (back - c).abs().max().item() < 1e-11 * c.abs().max().item()
+
+
+@pytest.mark.gpu
+def test_gpu_emulated_fp64_contraction_agrees_with_the_fp64_units(gpu):
+    """The tensor-core emulation against the FP64 units on the same inputs at
+    lmax 256 (depth 385 in the analysis, near the exactness bound): agreement
+    to about 2^-45 of the largest value, both directions, coefficients whose
+    magnitudes span ten decades."""
+    import torch
+
+    from sl3dpp_gb300.grid import SurfaceGrid
+
+    lmax = 256
+    native, emulated = SurfaceGrid(lmax, 2, 1.5), SurfaceGrid(lmax, 2, 1.5, True)
+    rng = np.random.default_rng(9)
+    for N in (-2, 0):
+        size = native.SpinCoefficientSize(N)
+        mag = 10.0 ** rng.uniform(-10, 0, size)
+        c = torch.tensor((rng.standard_normal(2 * size).view(np.complex128)) * mag, device=gpu)
+        fa, fb = native.SynthesiseSpinBatch(N, c, 1), emulated.SynthesiseSpinBatch(N, c, 1)
+        assert (fa - fb).abs().max().item() < 3e-14 * fa.abs().max().item(), N
+        ba, bb = native.ExpandSpinBatch(N, fa, 1), emulated.ExpandSpinBatch(N, fa, 1)
+        assert (ba - bb).abs().max().item() < 3e-14 * ba.abs().max().item(), N
