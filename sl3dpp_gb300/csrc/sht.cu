@@ -754,7 +754,7 @@ int Grid::RunGemm64(int N, bool real, Batch& b, const double* B, double* C, bool
   }
   {
     prof::Scope scope(prof::kStream, stream, 0.0, 8.0 * b.colExps + 2.0 * b.packed64Count);
-    LaunchPackB64(b.tc64Items, b.count, b.maxN, b.maxBTiles64, B, b.colExp, b.packed64, stream);
+    LaunchPackB64(b.tc64Items, b.count, b.maxNTiles64, B, b.colExp, b.packed64, stream);
     SL3D_CHECK_LAUNCH();
   }
   prof::Scope scope(prof::kLegendre64Tc, stream, b.flops);

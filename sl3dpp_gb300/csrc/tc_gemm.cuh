@@ -94,7 +94,7 @@ constexpr int kTc64MaxK = 448;   // the exactness bound on the depth, with margi
 
 void LaunchPanelA64(const GemmItem* items, const Tc64Item* tcItems, int count, int maxM, int maxATiles,
                     const double* table, int* rowExp, uint16_t* panels, cudaStream_t stream);
-void LaunchPackB64(const Tc64Item* tcItems, int count, int maxN, int maxBTiles, const double* B, int* colExp,
+void LaunchPackB64(const Tc64Item* tcItems, int count, int maxNTiles, const double* B, int* colExp,
                    uint16_t* packed, cudaStream_t stream);
 int RunGemm64Tc(const Tc64Item* tcItems, int count, int maxMTiles, int maxNTiles, const uint16_t* panels,
                 const uint16_t* packed, const int* rowExp, const int* colExp, double* C, bool accumulate,

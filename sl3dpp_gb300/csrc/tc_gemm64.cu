@@ -4,15 +4,19 @@
 //
 // Splitting. Row i of A has the exponent e_i with max_k |A(i, k)| < 2^{e_i},
 // column n of B the exponent f_n likewise; x = A(i, k) 2^{-e_i} (|x| < 1) is
-// written x = sum_{p < 7} s_p 2^{-7 (p + 1)} + r with integers |s_0| <= 128,
-// |s_p| <= 64 (p > 0) and |r| <= 2^{-50}, each step exact in FP64 (x 2^7,
-// then less the nearest integer). The integers are exact in BF16.
+// rounded to X = round(x 2^49), an integer below 2^49 read off the double's
+// bits, and X is written in balanced base-2^7 digits,
+// X = sum_{p < 7} s_p 2^{7 (6 - p)}, |s_p| <= 64 for p > 0 and |s_0| <= 128:
+// x = sum_p s_p 2^{-7 (p + 1)} to within 2^{-50}. Integer arithmetic only
+// (the FP64 units of this part are slow); the digits are exact in BF16.
 //
 // Products. Level d = p + q gathers sum_k s_p(A) s_q(B) over p + q = d, at
 // most (d + 3) 2^12 per k in magnitude, so below 2^24 -- exact in the FP32
 // accumulator -- for K <= 455 at d = 6. The levels d < 7 are kept (28
-// products per 16-deep step) and joined in FP64:
-//   C(i, n) = 2^{e_i + f_n} sum_d 2^{-7 (d + 2)} acc_d(i, n).
+// products per 16-deep step) and joined exactly as integers,
+// H = acc_0 2^14 + acc_1 2^7 + acc_2 and L = acc_3 2^21 + acc_4 2^14 +
+// acc_5 2^7 + acc_6, then in FP64:
+//   C(i, n) = 2^{e_i + f_n} (2^{-28} H + 2^{-56} L).
 //
 // Kernel. One CTA of four warps per (64-column tile, 128-row tile, item),
 // the column tiles of a row tile adjacent in the launch so that its A panel
@@ -52,26 +56,42 @@ __host__ __device__ constexpr uint32_t InstrDescriptorBf16(int n, int m) {
 
 // The BF16 bits of an integer of magnitude at most 256 (exact: its float has
 // at most eight significant bits, all in the upper half).
-__device__ inline uint32_t Bf16Bits(double integer) {
-  return __float_as_uint(static_cast<float>(integer)) >> 16;
+__device__ inline uint32_t Bf16Bits(int integer) { return __float_as_uint(static_cast<float>(integer)) >> 16; }
+
+// The exponent e with |v| < 2^e for the largest |v| of a set, from the
+// largest magnitude's bits (0 for zero; subnormals count as below 2^-1022).
+__device__ inline int ExponentAbove(unsigned long long magnitudeBits) {
+  if (magnitudeBits == 0) return 0;
+  const int biased = static_cast<int>(magnitudeBits >> 52);
+  return biased == 0 ? -1022 : biased - 1022;
 }
 
-// x (|x| < 1) as kSlices integer slices, packed as BF16 bits.
-__device__ inline void Split(double x, uint32_t (&s)[kSlices]) {
+// v (|v| < 2^e) as kSlices balanced base-2^7 digits of round(v 2^{49 - e}),
+// packed as BF16 bits.
+__device__ inline void Split(double v, int e, uint32_t (&s)[kSlices]) {
+  const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(v));
+  const int biased = static_cast<int>((bits >> 52) & 0x7FF);
+  const long long mantissa = static_cast<long long>(bits & ((1ULL << 52) - 1)) | (biased ? (1LL << 52) : 0LL);
+  // v = mantissa 2^{E - 52}, E <= e - 1, so X = mantissa 2^{E - e - 3}: a
+  // right shift by t >= 4, rounded to nearest
+  const int E = biased ? biased - 1023 : -1022;
+  const int t = e - E + 3;
+  long long X = 0;
+  if (t < 63) X = (mantissa + (1LL << (t - 1))) >> t;
+  if (bits >> 63) X = -X;
 #pragma unroll
-  for (int p = 0; p < kSlices; ++p) {
-    const double y = x * 128.0;
-    const double r = rint(y);
+  for (int p = kSlices - 1; p > 0; --p) {
+    int r = static_cast<int>(X & 127);
+    if (r >= 64) r -= 128;
     s[p] = Bf16Bits(r);
-    x = y - r;
+    X = (X - r) >> 7;
   }
+  s[0] = Bf16Bits(static_cast<int>(X));
 }
 
-// The exponent e with max < 2^e (0 for max = 0).
-__device__ inline int ExponentAbove(double max) {
-  int e = 0;
-  frexp(max, &e);
-  return e;
+// 2^k as a double (exact), by its bits in the normal range.
+__device__ inline double Pow2(int k) {
+  return (k >= -1022 && k <= 1023) ? __longlong_as_double(static_cast<long long>(k + 1023) << 52) : ldexp(1.0, k);
 }
 
 // Offset (in BF16 values) of element (row, k) of a K-major 16-deep tile of
@@ -100,9 +120,11 @@ __global__ void RowExpKernel(const GemmItem* items, const Tc64Item* tcItems, con
   const GemmItem g = items[blockIdx.y];
   const Tc64Item it = tcItems[blockIdx.y];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.M; i += gridDim.x * blockDim.x) {
-    double mx = 0.0;
-    for (int k = 0; k < g.K; ++k)
-      mx = fmax(mx, fabs(table[g.a + static_cast<long long>(i) * g.sAi + static_cast<long long>(k) * g.sAk]));
+    unsigned long long mx = 0;
+    for (int k = 0; k < g.K; ++k) {
+      const double v = table[g.a + static_cast<long long>(i) * g.sAi + static_cast<long long>(k) * g.sAk];
+      mx = max(mx, static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7FFFFFFFFFFFFFFFULL);
+    }
     rowExp[it.rowExp + i] = ExponentAbove(mx);
   }
 }
@@ -129,44 +151,49 @@ __global__ void PanelA64Kernel(const GemmItem* items, const Tc64Item* tcItems, c
       const double v = (i < g.M && k < g.K) ? table[g.a + static_cast<long long>(i) * g.sAi +
                                                     static_cast<long long>(k) * g.sAk]
                                             : 0.0;
-      Split(ldexp(v, -e), s[q]);
+      Split(v, e, s[q]);
     }
     StoreSlices(panels + it.aPanel + tile * kSlices * kATile, kATile, Tile16Index(r, 8 * kg, kTcTileM), s);
   }
 }
 
-// Column exponents of B, one thread per (item, column).
-__global__ void ColExpKernel(const Tc64Item* tcItems, const double* B, int* colExp) {
-  const Tc64Item it = tcItems[blockIdx.y];
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < it.N; n += gridDim.x * blockDim.x) {
-    double mx = 0.0;
-    for (int k = 0; k < it.K; ++k) mx = fmax(mx, fabs(B[it.b + static_cast<long long>(k) * it.ldb + n]));
-    colExp[it.colExp + n] = ExponentAbove(mx);
-  }
-}
+// B's column exponents and packed slices, one CTA of 256 threads per
+// (column tile, item): 64 columns x 4 lanes along k. The exponents first
+// (each lane's maximum over its k, then over the four lanes), then the
+// slices, 8-deep k groups in turn; a warp's reads of one k are 32
+// consecutive columns and its stores of one slice 512 contiguous bytes.
+constexpr int kPackThreads = 256, kPackLanes = kPackThreads / kTileN;
 
-// B packed: one thread per (item, tile, 8-deep K group, column); a warp's
-// reads of one k are 32 consecutive columns.
-__global__ void PackB64Kernel(const Tc64Item* tcItems, const double* B, const int* colExp, uint16_t* packed) {
+__global__ void __launch_bounds__(kPackThreads) PackB64Kernel(const Tc64Item* tcItems, const double* B, int* colExp,
+                                                              uint16_t* packed) {
   const Tc64Item it = tcItems[blockIdx.y];
-  const long long total = static_cast<long long>(it.nTiles) * it.kSteps * 2 * kTileN;
-  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
-       t += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const int nn = static_cast<int>(t % kTileN);
-    const long long rest = t / kTileN;
-    const int kg = static_cast<int>(rest % 2);
-    const long long tile = rest / 2;
-    const int ks = static_cast<int>(tile % it.kSteps), nt = static_cast<int>(tile / it.kSteps);
-    const int n = nt * kTileN + nn, k0 = ks * kTcTileK + 8 * kg;
-    const int e = n < it.N ? colExp[it.colExp + n] : 0;
+  const int nt = blockIdx.x;
+  if (nt >= it.nTiles) return;
+  __shared__ unsigned long long largest[kPackLanes][kTileN];
+  const int nn = threadIdx.x % kTileN, lane = threadIdx.x / kTileN;
+  const int n = nt * kTileN + nn;
+  const double* col = B + it.b + n;
+  unsigned long long mx = 0;
+  if (n < it.N)
+    for (int k = lane; k < it.K; k += kPackLanes)
+      mx = max(mx, static_cast<unsigned long long>(__double_as_longlong(col[static_cast<long long>(k) * it.ldb])) &
+                       0x7FFFFFFFFFFFFFFFULL);
+  largest[lane][nn] = mx;
+  __syncthreads();
+  for (int q = 0; q < kPackLanes; ++q) mx = max(mx, largest[q][nn]);
+  const int e = ExponentAbove(mx);
+  if (lane == 0 && n < it.N) colExp[it.colExp + n] = e;
+  uint16_t* base = packed + it.bPack + static_cast<long long>(nt) * it.kSteps * kSlices * kBTile;
+  for (int group = lane; group < 2 * it.kSteps; group += kPackLanes) {
+    const int ks = group / 2, kg = group % 2, k0 = 8 * group;
     uint32_t s[8][kSlices];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = k0 + q;
-      const double v = (n < it.N && k < it.K) ? B[it.b + static_cast<long long>(k) * it.ldb + n] : 0.0;
-      Split(ldexp(v, -e), s[q]);
+      const double v = (n < it.N && k < it.K) ? col[static_cast<long long>(k) * it.ldb] : 0.0;
+      Split(v, e, s[q]);
     }
-    StoreSlices(packed + it.bPack + tile * kSlices * kBTile, kBTile, Tile16Index(nn, 8 * kg, kTileN), s);
+    StoreSlices(base + static_cast<long long>(ks) * kSlices * kBTile, kBTile, Tile16Index(nn, 8 * kg, kTileN), s);
   }
 }
 
@@ -302,11 +329,13 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
         for (int q = 0; q < 16; ++q) {
           const int n = c0 + q;
           if (n >= nCols) continue;
-          double sum = 0.0;
+          long long acc[kSlices];
 #pragma unroll
-          for (int d = kSlices - 1; d >= 0; --d)
-            sum += ldexp(static_cast<double>(__uint_as_float(r[d][q])), -7 * (d + 2));
-          const double v = ldexp(sum, e + colExp[it.colExp + n0 + n]);
+          for (int d = 0; d < kSlices; ++d) acc[d] = __float2int_rn(__uint_as_float(r[d][q]));
+          const long long H = (acc[0] << 14) + (acc[1] << 7) + acc[2];
+          const long long L = (acc[3] << 21) + (acc[4] << 14) + (acc[5] << 7) + acc[6];
+          const int scale = e + colExp[it.colExp + n0 + n];
+          const double v = fma(static_cast<double>(H), Pow2(scale - 28), static_cast<double>(L) * Pow2(scale - 56));
           c[n] = accumulate ? c[n] + v : v;
         }
       }
@@ -330,13 +359,11 @@ void LaunchPanelA64(const GemmItem* items, const Tc64Item* tcItems, int count, i
   PanelA64Kernel<<<dim3(blocks, count), 256, 0, stream>>>(items, tcItems, table, rowExp, panels);
 }
 
-void LaunchPackB64(const Tc64Item* tcItems, int count, int maxN, int maxBTiles, const double* B, int* colExp,
+void LaunchPackB64(const Tc64Item* tcItems, int count, int maxNTiles, const double* B, int* colExp,
                    uint16_t* packed, cudaStream_t stream) {
-  if (count == 0) return;
-  ColExpKernel<<<dim3(static_cast<unsigned>((maxN + 127) / 128), count), 128, 0, stream>>>(tcItems, B, colExp);
-  const long long perItem = static_cast<long long>(maxBTiles) * 2 * kTileN;
-  const unsigned blocks = static_cast<unsigned>(std::min<long long>((perItem + 255) / 256, 4096));
-  PackB64Kernel<<<dim3(blocks, count), 256, 0, stream>>>(tcItems, B, colExp, packed);
+  if (count == 0 || maxNTiles == 0) return;
+  PackB64Kernel<<<dim3(static_cast<unsigned>(maxNTiles), count), kPackThreads, 0, stream>>>(tcItems, B, colExp,
+                                                                                           packed);
 }
 
 int RunGemm64Tc(const Tc64Item* tcItems, int count, int maxMTiles, int maxNTiles, const uint16_t* panels,
