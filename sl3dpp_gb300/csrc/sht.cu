@@ -289,6 +289,110 @@ __device__ int WarpFft(T2* a, T2* b, const FftPlan& plan, const T2* tw, int sign
   return src == a ? 0 : 1;
 }
 
+// -- two-stage ring transforms in registers -----------------------------------------------
+//
+// For n = R1 R2 with R1, R2 <= 32 the ring transform is two Stockham stages
+// of radix R1 and R2 with one butterfly a lane: stage A (R2 butterflies)
+// takes a[idx + q R2] (q < R1) and writes b[idx R1 + u]; stage B (R1
+// butterflies) takes b[idx + q R1] twiddled by e^{sign 2 pi i q idx / n} and
+// writes a[idx + u R1]. Each butterfly is an R-point transform held in
+// registers (RegFft: the Stockham algorithm again, radices 4, 2, 3, 5, every
+// index a compile-time constant). The stage-B twiddles are kept as
+// twB[q R1 + idx], so a warp's loads of one q are consecutive.
+
+// The radix of the next in-register stage of an R-point transform.
+__host__ __device__ constexpr int NextRadix(int r) { return r % 4 == 0 ? 4 : r % 2 == 0 ? 2 : r % 3 == 0 ? 3 : 5; }
+
+// Whether an R-point transform factors into the radices 2, 3, 4, 5.
+__host__ __device__ constexpr bool Smooth(int r) {
+  while (r > 1) {
+    const int f = NextRadix(r);
+    if (r % f != 0) return false;
+    r /= f;
+  }
+  return true;
+}
+
+// The in-register stages of an R-point transform from stage width Ns on;
+// tw[j] = e^{2 pi i j / n} (n a multiple of R), Sign +1 or -1.
+template <class T2, int R, int Ns, int Sign, int n>
+__device__ inline void RegStages(T2 (&x)[R], const T2* tw) {
+  if constexpr (Ns < R) {
+    constexpr int Rr = NextRadix(R / Ns);
+    constexpr int m = R / Rr;
+    T2 y[R];
+#pragma unroll
+    for (int b = 0; b < m; ++b) {
+      const int k = b % Ns;
+      T2 v[Rr];
+#pragma unroll
+      for (int q = 0; q < Rr; ++q) {
+        v[q] = x[b + q * m];
+        if (q > 0 && k > 0) {
+          T2 w = tw[(n / (Ns * Rr)) * q * k];
+          if (Sign < 0) w.y = -w.y;
+          v[q] = Mul(v[q], w);
+        }
+      }
+      Butterfly<T2, Rr>(v, Sign);
+      const int base = (b / Ns) * Ns * Rr + k;
+#pragma unroll
+      for (int u = 0; u < Rr; ++u) y[base + u * Ns] = v[u];
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) x[i] = y[i];
+    RegStages<T2, R, Ns * Rr, Sign, n>(x, tw);
+  }
+}
+
+// The whole ring's transform, from and back into a (b the scratch).
+template <class T2, int R1, int R2, int Sign>
+__device__ inline void RingFft2(T2* a, T2* b, const T2* tw, const T2* twB, int lane) {
+  static_assert(R1 <= kWarp && R2 <= kWarp && Smooth(R1) && Smooth(R2), "a butterfly a lane, radices 2-5");
+  constexpr int n = R1 * R2;
+  if (lane < R2) {
+    T2 v[R1];
+#pragma unroll
+    for (int q = 0; q < R1; ++q) v[q] = a[lane + q * R2];
+    RegStages<T2, R1, 1, Sign, n>(v, tw);
+#pragma unroll
+    for (int u = 0; u < R1; ++u) b[lane * R1 + u] = v[u];
+  }
+  __syncwarp();
+  if (lane < R1) {
+    T2 v[R2];
+#pragma unroll
+    for (int q = 0; q < R2; ++q) {
+      v[q] = b[lane + q * R1];
+      if (q > 0) {
+        T2 w = twB[q * R1 + lane];
+        if (Sign < 0) w.y = -w.y;
+        v[q] = Mul(v[q], w);
+      }
+    }
+    RegStages<T2, R2, 1, Sign, n>(v, tw);
+#pragma unroll
+    for (int u = 0; u < R2; ++u) a[lane + u * R1] = v[u];
+  }
+  __syncwarp();
+}
+
+// A ring's transform by the kernel's form: the two-stage one (R1 > 0; the
+// result back in a) or the plan's stages (the result's side returned).
+template <class T2, int R1, int R2>
+__device__ inline int RingTransform(T2* a, T2* b, const FftPlan& plan, const T2* tw, const T2* twB, int sign,
+                                    int lane) {
+  if constexpr (R1 > 0) {
+    if (sign > 0)
+      RingFft2<T2, R1, R2, 1>(a, b, tw, twB, lane);
+    else
+      RingFft2<T2, R1, R2, -1>(a, b, tw, twB, lane);
+    return 0;
+  } else {
+    return WarpFft(a, b, plan, tw, sign, lane);
+  }
+}
+
 // Ring modes: spectra -> fields; fields (times an optional weight) ->
 // spectra; spectra -> fields -> weight -> spectra without leaving shared
 // memory.
@@ -300,19 +404,19 @@ template <class T2>
 int RingsPerCta(int n) {
   const long long budget = 100 * 1024;
   const long long ring = 2LL * n * sizeof(T2);
-  const long long g = (budget - static_cast<long long>(n) * sizeof(T2)) / ring;
+  const long long g = (budget - 2LL * n * sizeof(T2)) / ring;
   return static_cast<int>(std::max(1LL, std::min(8LL, g)));
 }
 
 template <class T2>
 size_t RingSmem(int n, int rings) {
-  return (static_cast<size_t>(n) + 2ULL * rings * n) * sizeof(T2);
+  return (2ULL * n + 2ULL * rings * n) * sizeof(T2);
 }
 
 // One CTA per (colatitude j, group of G consecutive fields p0..p0+G-1), one
 // warp per ring. The spectra [m][j][p] are read and written by the whole CTA
 // with the G fields of an order adjacent; the transforms run warp-synchronous.
-template <class T2>
+template <class T2, int R1, int R2>
 __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan, const T2* twGlobal,
                            const double* weights, const T2* spectraIn, const void* fieldsIn,
                            const typename Real<T2>::type* pointWeight, void* fieldsOut, T2* spectraOut) {
@@ -322,12 +426,15 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
   const int G = blockDim.x / kWarp;
   const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   T2* tw = reinterpret_cast<T2*>(ringSmem);
-  T2* bufs = tw + n;
+  T2* twB = tw + n;  // the two-stage form's stage-B twiddles
+  T2* bufs = twB + n;
   const int j = blockIdx.y;
   const int p0 = blockIdx.x * G;
   const int groups = min(G, count - p0);
   const int mcount = real ? lmax + 1 : 2 * lmax + 1;
   for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = twGlobal[e];
+  if constexpr (R1 > 0)
+    for (int e = threadIdx.x; e < n; e += blockDim.x) twB[e] = twGlobal[(e / R1) * (e % R1)];
   T2* a = bufs + 2LL * warp * n;  // this warp's ring
   T2* b = a + n;
   int at = 0;  // which of a, b holds the ring's current values
@@ -352,7 +459,7 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
     }
     __syncthreads();
     if (warp < groups) {
-      at = WarpFft(a, b, plan, tw, +1, lane);
+      at = RingTransform<T2, R1, R2>(a, b, plan, tw, twB, +1, lane);
       T2* res = at ? b : a;
       const long long row = (static_cast<long long>(p0 + warp) * ntheta + j) * n;
       if (mode == kRingSynth) {
@@ -395,9 +502,9 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
   if (warp < groups) {
     T2* x = at ? b : a;
     T2* y = at ? a : b;
-    WarpFft(x, y, plan, tw, -1, lane);
+    RingTransform<T2, R1, R2>(x, y, plan, tw, twB, -1, lane);
   }
-  const int out = mode == kRingWeighted ? 0 : plan.stages % 2;
+  const int out = (mode == kRingWeighted || R1 > 0) ? 0 : plan.stages % 2;
   __syncthreads();
   const T scale = static_cast<T>(2.0 * 3.14159265358979323846 / n * weights[j]);
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
@@ -405,6 +512,24 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
     const int m = real ? mi : mi - lmax;
     const T2 v = bufs[2LL * g * n + (out ? n : 0) + (m < 0 ? m + n : m)];
     spectraOut[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
+  }
+}
+
+// The ring kernel for a ring of n longitudes: the two-stage register form
+// for the sizes it is built for, else the plan's stages.
+template <class T2>
+using RingFn = void (*)(int, int, int, int, bool, FftPlan, const T2*, const double*, const T2*, const void*,
+                        const typename Real<T2>::type*, void*, T2*);
+
+template <class T2>
+RingFn<T2> RingKernelFor(int n) {
+  switch (n) {
+    case 800: return RingKernel<T2, 25, 32>;
+    case 400: return RingKernel<T2, 16, 25>;
+    case 50: return RingKernel<T2, 5, 10>;
+    case 40: return RingKernel<T2, 5, 8>;
+    case 25: return RingKernel<T2, 5, 5>;
+    default: return RingKernel<T2, 0, 0>;
   }
 }
 
@@ -799,8 +924,8 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   if (count == 0) return SL3DGPU_OK;
   const int rings = RingsPerCta<double2>(g.nphi);
   const size_t smem = RingSmem<double2>(g.nphi, rings);
-  SL3D_CUDA(cudaFuncSetAttribute(RingKernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem)));
+  const RingFn<double2> kernel = RingKernelFor<double2>(g.nphi);
+  SL3D_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   dim3 grid((count + rings - 1) / rings, g.ntheta);
   // algorithmic traffic: the spectra and the grid values the mode reads and writes
   const double spec = static_cast<double>(real ? g.lmax + 1 : 2 * g.lmax + 1) * g.ntheta * count * 16.0;
@@ -809,7 +934,7 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   const double bytes = mode == kRingWeighted ? 2 * spec + wbytes : spec + field + wbytes;
   const double ffts = static_cast<double>(g.ntheta) * count * (mode == kRingWeighted ? 2 : 1);
   prof::Scope scope(prof::kRing, stream, ffts * 5.0 * g.nphi * std::log2(static_cast<double>(g.nphi)), bytes);
-  RingKernel<double2><<<grid, rings * kWarp, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
+  kernel<<<grid, rings * kWarp, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
                                           g.dWeights, reinterpret_cast<const double2*>(spectraIn),
                                           fieldsIn, weight, fieldsOut,
                                           reinterpret_cast<double2*>(spectraOut));
@@ -937,14 +1062,14 @@ int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const floa
   if (int st = Table32(0, &t); st != SL3DGPU_OK) return st;  // makes the FP32 twiddles
   const int rings = RingsPerCta<float2>(nphi);
   const size_t smem = RingSmem<float2>(nphi, rings);
-  SL3D_CUDA(cudaFuncSetAttribute(RingKernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem)));
+  const RingFn<float2> kernel = RingKernelFor<float2>(nphi);
+  SL3D_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   dim3 grid((count + rings - 1) / rings, ntheta);
   const double spec = static_cast<double>(real ? lmax + 1 : 2 * lmax + 1) * ntheta * count * 8.0;
   const double wbytes = static_cast<double>(ntheta) * nphi * count * 4.0;
   prof::Scope scope(prof::kRing32, stream, 2.0 * ntheta * count * 5.0 * nphi * std::log2(static_cast<double>(nphi)),
                     2 * spec + wbytes);
-  RingKernel<float2><<<grid, rings * kWarp, smem, stream>>>(kRingWeighted, lmax, ntheta, count, real, plan, dTwiddle32,
+  kernel<<<grid, rings * kWarp, smem, stream>>>(kRingWeighted, lmax, ntheta, count, real, plan, dTwiddle32,
                                                   dWeights, reinterpret_cast<const float2*>(spectraIn), nullptr,
                                                   weight, nullptr, reinterpret_cast<float2*>(spectraOut));
   SL3D_CHECK_LAUNCH();
