@@ -345,25 +345,31 @@ __device__ inline void RegStages(T2 (&x)[R], const T2* tw) {
   }
 }
 
-// The whole ring's transform, from and back into a (b the scratch).
+// The whole ring's transform in place: every lane reads its butterfly's
+// values into registers before any lane writes.
 template <class T2, int R1, int R2, int Sign>
-__device__ inline void RingFft2(T2* a, T2* b, const T2* tw, const T2* twB, int lane) {
+__device__ inline void RingFft2(T2* a, const T2* tw, const T2* twB, int lane) {
   static_assert(R1 <= kWarp && R2 <= kWarp && Smooth(R1) && Smooth(R2), "a butterfly a lane, radices 2-5");
   constexpr int n = R1 * R2;
-  if (lane < R2) {
+  {
     T2 v[R1];
+    if (lane < R2) {
 #pragma unroll
-    for (int q = 0; q < R1; ++q) v[q] = a[lane + q * R2];
-    RegStages<T2, R1, 1, Sign, n>(v, tw);
+      for (int q = 0; q < R1; ++q) v[q] = a[lane + q * R2];
+      RegStages<T2, R1, 1, Sign, n>(v, tw);
+    }
+    __syncwarp();
+    if (lane < R2) {
 #pragma unroll
-    for (int u = 0; u < R1; ++u) b[lane * R1 + u] = v[u];
+      for (int u = 0; u < R1; ++u) a[lane * R1 + u] = v[u];
+    }
+    __syncwarp();
   }
-  __syncwarp();
+  T2 v[R2];
   if (lane < R1) {
-    T2 v[R2];
 #pragma unroll
     for (int q = 0; q < R2; ++q) {
-      v[q] = b[lane + q * R1];
+      v[q] = a[lane + q * R1];
       if (q > 0) {
         T2 w = twB[q * R1 + lane];
         if (Sign < 0) w.y = -w.y;
@@ -371,6 +377,9 @@ __device__ inline void RingFft2(T2* a, T2* b, const T2* tw, const T2* twB, int l
       }
     }
     RegStages<T2, R2, 1, Sign, n>(v, tw);
+  }
+  __syncwarp();
+  if (lane < R1) {
 #pragma unroll
     for (int u = 0; u < R2; ++u) a[lane + u * R1] = v[u];
   }
@@ -384,9 +393,9 @@ __device__ inline int RingTransform(T2* a, T2* b, const FftPlan& plan, const T2*
                                     int lane) {
   if constexpr (R1 > 0) {
     if (sign > 0)
-      RingFft2<T2, R1, R2, 1>(a, b, tw, twB, lane);
+      RingFft2<T2, R1, R2, 1>(a, tw, twB, lane);
     else
-      RingFft2<T2, R1, R2, -1>(a, b, tw, twB, lane);
+      RingFft2<T2, R1, R2, -1>(a, tw, twB, lane);
     return 0;
   } else {
     return WarpFft(a, b, plan, tw, sign, lane);
@@ -399,30 +408,34 @@ __device__ inline int RingTransform(T2* a, T2* b, const FftPlan& plan, const T2*
 enum RingMode { kRingSynth = 0, kRingAnalyse = 1, kRingWeighted = 2 };
 
 // Rings per CTA (one warp each) so that a CTA's shared memory (the twiddles
-// and two buffers a ring) stays near 100 KB: two CTAs per SM.
+// and the rings' buffers: two for the planned stages, one for the two-stage
+// form, which works in place) stays near 100 KB.
 template <class T2>
-int RingsPerCta(int n) {
+int RingsPerCta(int n, int buffers) {
   const long long budget = 100 * 1024;
-  const long long ring = 2LL * n * sizeof(T2);
+  const long long ring = static_cast<long long>(buffers) * n * sizeof(T2);
   const long long g = (budget - 2LL * n * sizeof(T2)) / ring;
   return static_cast<int>(std::max(1LL, std::min(8LL, g)));
 }
 
+// The twiddles (two tables of n) and `buffers` rings of n per warp.
 template <class T2>
-size_t RingSmem(int n, int rings) {
-  return (2ULL * n + 2ULL * rings * n) * sizeof(T2);
+size_t RingSmem(int n, int rings, int buffers) {
+  return (2ULL * n + static_cast<unsigned long long>(buffers) * rings * n) * sizeof(T2);
 }
 
 // One CTA per (colatitude j, group of G consecutive fields p0..p0+G-1), one
 // warp per ring. The spectra [m][j][p] are read and written by the whole CTA
 // with the G fields of an order adjacent; the transforms run warp-synchronous.
 template <class T2, int R1, int R2>
-__global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan, const T2* twGlobal,
-                           const double* weights, const T2* spectraIn, const void* fieldsIn,
-                           const typename Real<T2>::type* pointWeight, void* fieldsOut, T2* spectraOut) {
+__global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
+    RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan, const T2* twGlobal,
+               const double* weights, const T2* spectraIn, const void* fieldsIn,
+               const typename Real<T2>::type* pointWeight, void* fieldsOut, T2* spectraOut) {
   using T = typename Real<T2>::type;
   extern __shared__ __align__(16) unsigned char ringSmem[];
-  const int n = plan.n;
+  const int n = R1 > 0 ? R1 * R2 : plan.n;  // a constant in the two-stage form
+  constexpr int buffers = R1 > 0 ? 1 : 2;
   const int G = blockDim.x / kWarp;
   const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   T2* tw = reinterpret_cast<T2*>(ringSmem);
@@ -435,17 +448,19 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
   for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = twGlobal[e];
   if constexpr (R1 > 0)
     for (int e = threadIdx.x; e < n; e += blockDim.x) twB[e] = twGlobal[(e / R1) * (e % R1)];
-  T2* a = bufs + 2LL * warp * n;  // this warp's ring
-  T2* b = a + n;
+  T2* a = bufs + static_cast<long long>(buffers) * warp * n;  // this warp's ring
+  T2* b = buffers == 2 ? a + n : a;
   int at = 0;  // which of a, b holds the ring's current values
   if (mode == kRingSynth || mode == kRingWeighted) {
-    for (int e = threadIdx.x; e < G * n; e += blockDim.x) bufs[2LL * (e / n) * n + e % n] = Make<T2>(0, 0);
+    for (int e = threadIdx.x; e < G * n; e += blockDim.x)
+      bufs[static_cast<long long>(buffers) * (e / n) * n + e % n] = Make<T2>(0, 0);
     __syncthreads();
+#pragma unroll 4
     for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
       const int g = e % groups, mi = e / groups;
       const int m = real ? mi : mi - lmax;
       const T2 v = spectraIn[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
-      T2* ring = bufs + 2LL * g * n;
+      T2* ring = bufs + static_cast<long long>(buffers) * g * n;
       if (real) {
         if (m == 0) {
           ring[0] = Make<T2>(v.x, 0);
@@ -472,6 +487,7 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
       } else {
         // the pointwise weight on the synthesised values (a real field's
         // imaginary part is dropped, as its synthesis does)
+#pragma unroll 5
         for (int k = lane; k < n; k += kWarp) {
           const T w = pointWeight[row + k];
           const T2 v = res[k];
@@ -485,6 +501,7 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
     __syncthreads();  // the twiddles
     if (warp < groups) {
       const long long row = (static_cast<long long>(p0 + warp) * ntheta + j) * n;
+#pragma unroll 5
       for (int k = lane; k < n; k += kWarp) {
         T2 v = real ? Make<T2>(static_cast<const T*>(fieldsIn)[row + k], 0) : static_cast<const T2*>(fieldsIn)[row + k];
         if (pointWeight != nullptr) {
@@ -507,10 +524,11 @@ __global__ void RingKernel(int mode, int lmax, int ntheta, int count, bool real,
   const int out = (mode == kRingWeighted || R1 > 0) ? 0 : plan.stages % 2;
   __syncthreads();
   const T scale = static_cast<T>(2.0 * 3.14159265358979323846 / n * weights[j]);
+#pragma unroll 4
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
-    const T2 v = bufs[2LL * g * n + (out ? n : 0) + (m < 0 ? m + n : m)];
+    const T2 v = bufs[static_cast<long long>(buffers) * g * n + (out ? n : 0) + (m < 0 ? m + n : m)];
     spectraOut[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
   }
 }
@@ -522,14 +540,15 @@ using RingFn = void (*)(int, int, int, int, bool, FftPlan, const T2*, const doub
                         const typename Real<T2>::type*, void*, T2*);
 
 template <class T2>
-RingFn<T2> RingKernelFor(int n) {
+RingFn<T2> RingKernelFor(int n, int* buffers) {
+  *buffers = 1;
   switch (n) {
     case 800: return RingKernel<T2, 25, 32>;
     case 400: return RingKernel<T2, 16, 25>;
     case 50: return RingKernel<T2, 5, 10>;
     case 40: return RingKernel<T2, 5, 8>;
     case 25: return RingKernel<T2, 5, 5>;
-    default: return RingKernel<T2, 0, 0>;
+    default: *buffers = 2; return RingKernel<T2, 0, 0>;
   }
 }
 
@@ -922,9 +941,10 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
                const void* fieldsIn, const double* weight, void* fieldsOut, double* spectraOut,
                cudaStream_t stream) {
   if (count == 0) return SL3DGPU_OK;
-  const int rings = RingsPerCta<double2>(g.nphi);
-  const size_t smem = RingSmem<double2>(g.nphi, rings);
-  const RingFn<double2> kernel = RingKernelFor<double2>(g.nphi);
+  int buffers = 2;
+  const RingFn<double2> kernel = RingKernelFor<double2>(g.nphi, &buffers);
+  const int rings = RingsPerCta<double2>(g.nphi, buffers);
+  const size_t smem = RingSmem<double2>(g.nphi, rings, buffers);
   SL3D_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   dim3 grid((count + rings - 1) / rings, g.ntheta);
   // algorithmic traffic: the spectra and the grid values the mode reads and writes
@@ -1060,9 +1080,10 @@ int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const floa
   if (count == 0) return SL3DGPU_OK;
   const SpinTable* t = nullptr;
   if (int st = Table32(0, &t); st != SL3DGPU_OK) return st;  // makes the FP32 twiddles
-  const int rings = RingsPerCta<float2>(nphi);
-  const size_t smem = RingSmem<float2>(nphi, rings);
-  const RingFn<float2> kernel = RingKernelFor<float2>(nphi);
+  int buffers = 2;
+  const RingFn<float2> kernel = RingKernelFor<float2>(nphi, &buffers);
+  const int rings = RingsPerCta<float2>(nphi, buffers);
+  const size_t smem = RingSmem<float2>(nphi, rings, buffers);
   SL3D_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   dim3 grid((count + rings - 1) / rings, ntheta);
   const double spec = static_cast<double>(real ? lmax + 1 : 2 * lmax + 1) * ntheta * count * 8.0;
