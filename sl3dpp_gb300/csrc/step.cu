@@ -96,6 +96,8 @@ class Viscoelastic3DGpu {
   Geometry geo{};
   Dev<int> dNodeElement, dNodeQ, dElemFirstNode, dSphMap, dTorMap;
   Dev<double> dNodeR, dElemJac, dValue, dDeriv, dWeight;
+  Dev<double> dCoef64;  // the node coefficient tables (Geometry::coef64/coef32)
+  Dev<float> dCoef32;
   Dev<DegreeInfo> dDegrees;
   std::vector<DegreeInfo> degrees;
   long long rhsSphComplex = 0, rhsTorComplex = 0;
@@ -421,7 +423,18 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   SL3D_TRY(grid->Table(0, &tr));
   geo = Geometry{L, P, n, pts.count, E, dNodeElement.p, dNodeQ.p, dNodeR.p, dElemFirstNode.p, dElemJac.p,
                  dValue.p, dDeriv.p, dWeight.p, t0->dRowOffset, t1->dRowOffset, tr->dRowOffset,
-                 rows0, rows1, rowsR, dDegrees.p, dSphMap.p, dTorMap.p};
+                 rows0, rows1, rowsR, dDegrees.p, dSphMap.p, dTorMap.p, {}, {}};
+  {
+    const auto coef = NodeCoefficients(P, n, nodeElement, nodeQ, nodeR, elemJac, pts.value, pts.derivative,
+                                       pts.weight);
+    SL3D_CUDA(dCoef64.Upload(coef));
+    SL3D_CUDA(dCoef32.Upload(std::vector<float>(coef.begin(), coef.end())));
+    const size_t plane = static_cast<size_t>(P) * n;
+    for (int w = 0; w < 4; ++w) {
+      geo.coef64[w] = dCoef64.p + w * plane;
+      geo.coef32[w] = dCoef32.p + w * plane;
+    }
+  }
 
   // Branch moduli and reference inverse times at the nodes; exp(-delta) = 1.
   std::vector<double> mu(static_cast<size_t>(K) * P), itau(static_cast<size_t>(K) * P);
@@ -1161,6 +1174,10 @@ int Viscoelastic3DGpu::PrepareLateral() {
   geoL.nodeElement = dNodeElement.p + p0;
   geoL.nodeQ = dNodeQ.p + p0;
   geoL.nodeR = dNodeR.p + p0;
+  for (int w = 0; w < 4; ++w) {
+    geoL.coef64[w] = geo.coef64[w] + static_cast<long long>(p0) * geo.ngll;
+    geoL.coef32[w] = geo.coef32[w] + static_cast<long long>(p0) * geo.ngll;
+  }
   geoL.elemFirstNode = dElemFirstNodeL.p;
   geoL.degrees = dDegreesL.p;
   compactComplex = (rows0 + rows1 + rowsR) * count;

@@ -56,7 +56,7 @@ __device__ inline T2 CI(T2 a) {  // i a
 }
 
 __device__ inline void DecodeLm(int lm, int& l, int& m) {
-  l = static_cast<int>((sqrt(8.0 * lm + 1.0) - 1.0) * 0.5);
+  l = static_cast<int>((sqrtf(8.0f * lm + 1.0f) - 1.0f) * 0.5f);  // a guess; the loops settle it
   while (l * (l + 1) / 2 > lm) --l;
   while ((l + 1) * (l + 2) / 2 <= lm) ++l;
   m = lm - l * (l + 1) / 2;
@@ -70,6 +70,17 @@ __device__ inline long long Row1(const Geometry& g, int l, int m) {
 }
 __device__ inline long long RowR(const Geometry& g, int l, int m) {
   return g.rowOffR[m + g.lmax] - g.rowOffR[g.lmax] + (l - m);
+}
+
+template <class T>
+__device__ inline const T* Coef(const Geometry& g, int which);
+template <>
+__device__ inline const double* Coef<double>(const Geometry& g, int which) {
+  return g.coef64[which];
+}
+template <>
+__device__ inline const float* Coef<float>(const Geometry& g, int which) {
+  return g.coef32[which];
 }
 
 template <class T2>
@@ -136,18 +147,17 @@ __global__ void ForceKernel(Geometry g, const T2* spectral, T2* rhsSph, T2* rhsT
     const int eHi = min(gn / (n - 1), g.elements - 1);
     const int iHi = gn - eHi * (n - 1);
     const int eLo = (iHi == 0 && eHi > 0) ? eHi - 1 : eHi;
+    const T* fValue = Coef<T>(g, kForceValue);
+    const T* fDeriv = Coef<T>(g, kForceDeriv);
     for (int e = eLo; e <= eHi; ++e) {
       const int fn = g.elemFirstNode[e];
       if (fn < 0 || fn < d.firstNode) continue;
       const int i = e == eHi ? iHi : n - 1;
-      const double jac = g.elemJac[e];
       for (int q = 0; q < g.np; ++q) {
         const int p = fn + q;
-        const double r = g.nodeR[p];
         const T2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
-        const double point = jac * g.pWeight[q] * r;
-        const T v = static_cast<T>(point * g.pValue[q * n + i]);
-        const T deriv = static_cast<T>(g.pWeight[q] * g.pDeriv[q * n + i] * r);
+        const T v = fValue[p * n + i];
+        const T deriv = fDeriv[p * n + i];
         bU = CAdd(bU, CScale(v, s[0]));
         bV = CAdd(bV, CScale(v, s[1]));
         bU = CAdd(bU, CScale(deriv, s[3]));
@@ -203,18 +213,19 @@ __global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2*
   for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
     T2 A[5] = {Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0)};
     if (any && p >= d.firstNode) {
-      const int e = g.nodeElement[p], q = g.nodeQ[p];
-      const double rd = g.nodeR[p], jac = g.elemJac[e];
-      const T r = static_cast<T>(rd);
+      const int e = g.nodeElement[p];
+      const T r = static_cast<T>(g.nodeR[p]);
+      const T* sValue = Coef<T>(g, kStrainValue) + p * n;
+      const T* sDeriv = Coef<T>(g, kStrainDeriv) + p * n;
       T2 U = Cx<T2>(0, 0), V = Cx<T2>(0, 0), W = Cx<T2>(0, 0), rdU = Cx<T2>(0, 0), rdV = Cx<T2>(0, 0),
          rdW = Cx<T2>(0, 0);
       for (int i = 0; i < n; ++i) {
         const T2* v = vals + static_cast<long long>(e * (n - 1) + i - d.firstGlobal) * 3;
-        const T val = static_cast<T>(g.pValue[q * n + i]);
+        const T val = sValue[i];
         U = CAdd(U, CScale(val, v[0]));
         V = CAdd(V, CScale(val, v[1]));
         W = CAdd(W, CScale(val, v[2]));
-        const T b = static_cast<T>(rd * g.pDeriv[q * n + i] / jac);
+        const T b = sDeriv[i];
         rdU = CAdd(rdU, CScale(b, v[0]));
         rdV = CAdd(rdV, CScale(b, v[1]));
         rdW = CAdd(rdW, CScale(b, v[2]));
@@ -642,12 +653,17 @@ __global__ void MixerSweepKernel(MixerArgsT<T> a) {
 // The partials in a fixed order (one warp per sum, lanes over the blocks,
 // then a fixed shuffle tree), the Gram matrix's new row and column, and the
 // least-squares coefficients (FP64, one thread; gamma[m] = 1 when they hold).
-__global__ void MixerSolveKernel(int m, int slot, int memory, int blocks, const double* partial, double* gram,
+// The mixer's small solve for m = M columns (a compile-time order, so its
+// matrices stay in registers): the new Gram column and right-hand side from
+// the sweep's block partial sums, the Gram matrix's slot updated, gamma
+// solved (gamma[M] = 1 on success).
+template <int M>
+__global__ void MixerSolveKernel(int slot, int memory, int blocks, const double* partial, double* gram,
                                  double* gamma) {
   __shared__ double sums[2 * kMaxMemory];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  if (warp < 2 * m) {
-    const int i = warp < m ? warp : kMaxMemory + (warp - m);
+  if (warp < 2 * M) {
+    const int i = warp < M ? warp : kMaxMemory + (warp - M);
     double v = 0.0;
     for (int b = lane; b < blocks; b += 32) v += partial[static_cast<long long>(b) * 2 * kMaxMemory + i];
     for (int off = 16; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off);
@@ -655,21 +671,21 @@ __global__ void MixerSolveKernel(int m, int slot, int memory, int blocks, const 
   }
   __syncthreads();
   if (threadIdx.x != 0) return;
-  double col[kMaxMemory], gam[kMaxMemory];
-  for (int i = 0; i < m; ++i) {
-    col[i] = sums[i];
-    gam[i] = sums[m + i];
+  double gam[M], A[M * M], x[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    gam[i] = sums[M + i];
+    gram[slot * memory + i] = sums[i];
+    gram[i * memory + slot] = sums[i];
   }
-  for (int i = 0; i < m; ++i) {
-    gram[slot * memory + i] = col[i];
-    gram[i * memory + slot] = col[i];
-  }
-  double A[kMaxMemory * kMaxMemory], x[kMaxMemory];
-  for (int i = 0; i < m; ++i)
-    for (int j = 0; j < m; ++j) A[i * m + j] = gram[i * memory + j];
-  const bool ok = SymmetricLstsq(m, A, gam, x);
-  for (int i = 0; i < m; ++i) gamma[i] = x[i];
-  gamma[m] = ok ? 1.0 : 0.0;
+#pragma unroll
+  for (int i = 0; i < M; ++i)
+#pragma unroll
+    for (int j = 0; j < M; ++j) A[i * M + j] = gram[i * memory + j];
+  const bool ok = SymmetricLstsqOf<M>(A, gam, x);
+#pragma unroll
+  for (int i = 0; i < M; ++i) gamma[i] = x[i];
+  gamma[M] = ok ? 1.0 : 0.0;
 }
 
 template <class T>
@@ -1016,8 +1032,18 @@ void MixerUpdate(const MixerArgsT<T>& a, cudaStream_t stream) {
   }
   {
     prof::Scope scope(prof::kOther, stream);
-    MixerSolveKernel<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.m, a.slot, a.memory, a.blocks, a.partial, a.gram,
-                                                           a.gamma);
+    auto solve = MixerSolveKernel<1>;
+    switch (a.m) {
+      case 2: solve = MixerSolveKernel<2>; break;
+      case 3: solve = MixerSolveKernel<3>; break;
+      case 4: solve = MixerSolveKernel<4>; break;
+      case 5: solve = MixerSolveKernel<5>; break;
+      case 6: solve = MixerSolveKernel<6>; break;
+      case 7: solve = MixerSolveKernel<7>; break;
+      case 8: solve = MixerSolveKernel<8>; break;
+      default: break;
+    }
+    solve<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.slot, a.memory, a.blocks, a.partial, a.gram, a.gamma);
   }
   prof::Scope scope(prof::kMixer, stream, 0.0, a.n * sizeof(T) * (2 + a.m));
   MixerMixKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a);
@@ -1107,4 +1133,26 @@ void LaunchCast(long long n, const double* in, float* out, cudaStream_t stream) 
   CastKernel<<<StreamBlocks(n), 256, 0, stream>>>(n, in, out);
 }
 
+}  // namespace sl3dgpu
+
+namespace sl3dgpu {
+std::vector<double> NodeCoefficients(int P, int ngll, const std::vector<int>& nodeElement,
+                                     const std::vector<int>& nodeQ, const std::vector<double>& nodeR,
+                                     const std::vector<double>& elemJac, const std::vector<double>& value,
+                                     const std::vector<double>& deriv, const std::vector<double>& weight) {
+  const size_t plane = static_cast<size_t>(P) * ngll;
+  std::vector<double> out(4 * plane);
+  for (int p = 0; p < P; ++p) {
+    const int e = nodeElement[p], q = nodeQ[p];
+    const double r = nodeR[p], jac = elemJac[e];
+    for (int i = 0; i < ngll; ++i) {
+      const size_t at = static_cast<size_t>(p) * ngll + i;
+      out[kStrainValue * plane + at] = value[q * ngll + i];
+      out[kStrainDeriv * plane + at] = r * deriv[q * ngll + i] / jac;
+      out[kForceValue * plane + at] = jac * weight[q] * r * value[q * ngll + i];
+      out[kForceDeriv * plane + at] = weight[q] * deriv[q * ngll + i] * r;
+    }
+  }
+  return out;
+}
 }  // namespace sl3dgpu

@@ -5,6 +5,8 @@
 // form's correction passes); the FP32 mixer keeps its Gram sums in FP64.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace sl3dgpu {
@@ -41,7 +43,18 @@ struct Geometry {
   const DegreeInfo* degrees;
   const int* sphMap;         // (g, {U, V}) per degree
   const int* torMap;         // g per degree
+  // Per memory node p and GLL node i (p-major, ngll a row), in FP64 and FP32:
+  // [kStrainValue] Value(q_p, i); [kStrainDeriv] r_p Deriv(q_p, i) / jac;
+  // [kForceValue] jac w_q r_p Value(q_p, i); [kForceDeriv] w_q Deriv(q_p, i) r_p.
+  const double* coef64[4];
+  const float* coef32[4];
 };
+enum NodeCoefficient { kStrainValue = 0, kStrainDeriv = 1, kForceValue = 2, kForceDeriv = 3 };
+// The node coefficient tables of a geometry, host FP64 (4 x P x ngll).
+std::vector<double> NodeCoefficients(int P, int ngll, const std::vector<int>& nodeElement,
+                                     const std::vector<int>& nodeQ, const std::vector<double>& nodeR,
+                                     const std::vector<double>& elemJac, const std::vector<double>& value,
+                                     const std::vector<double>& deriv, const std::vector<double>& weight);
 
 // The memory force of an analysed (mu-weighted) tensor into the degree
 // systems' right-hand sides (GridCoupling::SpheroidalForce/ToroidalForce).
