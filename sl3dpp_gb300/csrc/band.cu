@@ -20,7 +20,10 @@
 //    shared memory (cp.async) while the current one is solved, the recent
 //    solution values live in a per-warp shared-memory ring, and a band value
 //    read serves two columns. Optional diagonal scaling and pinned dofs are fused
-//    in (DegreeOperator::BeginSolve/FinishSolve, src/DegreeOperator.cpp:861-901).
+//    in (DegreeOperator::BeginSolve/FinishSolve, src/DegreeOperator.cpp:861-901);
+//  - FP32 Cholesky solves may run over row windows: a right-hand side that is
+//    zero below row lo has y = 0 there, so the substitutions cover rows
+//    lo .. n - 1, and a completion launch finishes the rows below.
 #include <algorithm>
 #include <vector>
 
