@@ -418,10 +418,12 @@ int RingsPerCta(int n, int buffers) {
   return static_cast<int>(std::max(1LL, std::min(8LL, g)));
 }
 
-// The twiddles (two tables of n) and `buffers` rings of n per warp.
+// The twiddles (two tables of n) and `buffers` rings of n per warp, one
+// value of padding after each warp's.
 template <class T2>
 size_t RingSmem(int n, int rings, int buffers) {
-  return (2ULL * n + static_cast<unsigned long long>(buffers) * rings * n) * sizeof(T2);
+  return (2ULL * n + static_cast<unsigned long long>(rings) * (static_cast<unsigned long long>(buffers) * n + 1)) *
+         sizeof(T2);
 }
 
 // One CTA per (colatitude j, group of G consecutive fields p0..p0+G-1), one
@@ -436,6 +438,9 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   extern __shared__ __align__(16) unsigned char ringSmem[];
   const int n = R1 > 0 ? R1 * R2 : plan.n;  // a constant in the two-stage form
   constexpr int buffers = R1 > 0 ? 1 : 2;
+  // a warp's rings one value apart beyond their buffers, so that the G
+  // rings' values of one order fall in different banks
+  const long long ringStride = static_cast<long long>(buffers) * n + 1;
   const int G = blockDim.x / kWarp;
   const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   T2* tw = reinterpret_cast<T2*>(ringSmem);
@@ -448,19 +453,19 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = twGlobal[e];
   if constexpr (R1 > 0)
     for (int e = threadIdx.x; e < n; e += blockDim.x) twB[e] = twGlobal[(e / R1) * (e % R1)];
-  T2* a = bufs + static_cast<long long>(buffers) * warp * n;  // this warp's ring
+  T2* a = bufs + ringStride * warp;  // this warp's ring
   T2* b = buffers == 2 ? a + n : a;
   int at = 0;  // which of a, b holds the ring's current values
   if (mode == kRingSynth || mode == kRingWeighted) {
     for (int e = threadIdx.x; e < G * n; e += blockDim.x)
-      bufs[static_cast<long long>(buffers) * (e / n) * n + e % n] = Make<T2>(0, 0);
+      bufs[ringStride * (e / n) + e % n] = Make<T2>(0, 0);
     __syncthreads();
 #pragma unroll 4
     for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
       const int g = e % groups, mi = e / groups;
       const int m = real ? mi : mi - lmax;
       const T2 v = spectraIn[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
-      T2* ring = bufs + static_cast<long long>(buffers) * g * n;
+      T2* ring = bufs + ringStride * g;
       if (real) {
         if (m == 0) {
           ring[0] = Make<T2>(v.x, 0);
@@ -528,7 +533,7 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
-    const T2 v = bufs[static_cast<long long>(buffers) * g * n + (out ? n : 0) + (m < 0 ? m + n : m)];
+    const T2 v = bufs[ringStride * g + (out ? n : 0) + (m < 0 ? m + n : m)];
     spectraOut[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
   }
 }
