@@ -303,6 +303,20 @@ int sl3dgpu_v3d_state_coefficients_host(const sl3dgpu_v3d* op, const sl3dgpu_v3d
  * node in the same layout; infos (nullable): each node's step info. */
 int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* times, int nodes, int scheme,
                     const double* loads, double* u, double* phi, sl3dgpu_step_info* infos);
+/* Many independent runs at once (an ensemble: the reference's calibration and
+ * line-search workloads run Evolution3D per member): run i is
+ * sl3dgpu_v3d_run(ops[i], states[i], times[i], nodes[i], scheme, loads[i],
+ * u[i], phi[i], infos[i]) (u, phi, infos nullable as arrays). `threads` host
+ * threads (0: one per run up to the host's cores) drive the runs; each
+ * operator keeps its own stream, so the runs' kernels overlap on the GPU.
+ * statuses[i] receives run i's status; the call returns the first failure's
+ * (its text in sl3dgpu_last_error) or 0. Operators and states must be
+ * distinct. No reference counterpart (the reference runs members one by one
+ * or in separate processes). */
+int sl3dgpu_v3d_run_many(int count, sl3dgpu_v3d* const* ops, sl3dgpu_v3d_state* const* states,
+                         const double* const* times, const int* nodes, int scheme,
+                         const double* const* loads, double* const* u, double* const* phi,
+                         sl3dgpu_step_info* const* infos, int threads, int* statuses);
 /* The CUDA stream the operator's kernels run on. */
 void* sl3dgpu_v3d_stream(const sl3dgpu_v3d* op);
 /* The last step's pass residuals (RelativeChange per pass, the stages in

@@ -665,13 +665,10 @@ int BandFactorBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_sy
   }
   prof::Scope scope(prof::kOther, stream);
   if (lu) {
-    SL3D_CUDA(cudaFuncSetAttribute(LuFactorKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem)));
+    SL3D_CUDA(AllowDynamicSmem(LuFactorKernel));
     LuFactorKernel<<<count, 128, smem, stream>>>(devSystems, bands, pivots, info);
   } else {
-    SL3D_CUDA(cudaFuncSetAttribute(CholeskyFactorKernel,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem)));
+    SL3D_CUDA(AllowDynamicSmem(CholeskyFactorKernel));
     CholeskyFactorKernel<<<count, 128, smem, stream>>>(devSystems, bands, info);
   }
   SL3D_CHECK_LAUNCH();
@@ -727,13 +724,11 @@ int SolveBatch(const sl3dgpu_band_system* devSystems, const sl3dgpu_band_system*
   }
   prof::Scope scope(sizeof(T) == sizeof(float) ? prof::kBandSolve32 : prof::kBandSolve, stream, flops, bytes);
   if (lu) {
-    SL3D_CUDA(cudaFuncSetAttribute(LuSolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem)));
+    SL3D_CUDA(AllowDynamicSmem(LuSolveKernel<T>));
     LuSolveKernel<T><<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount, bands, pivots,
                                                                      rhs, scales, plan);
   } else {
-    SL3D_CUDA(cudaFuncSetAttribute(CholeskySolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(smem)));
+    SL3D_CUDA(AllowDynamicSmem(CholeskySolveKernel<T>));
     CholeskySolveKernel<T><<<blocks, warpsPerBlock * kWarp, smem, stream>>>(devSystems, items, itemCount, bands,
                                                                            rhs, scales, plan, windows, mode);
   }

@@ -33,6 +33,25 @@ void SetError(const std::string& text);
 
 inline cudaStream_t AsStream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Allow a kernel all the dynamic shared memory the device's opt-in limit
+// leaves beside its static shared memory. The attribute is global to the
+// function, so it takes one value for every caller: host threads driving
+// problems of different sizes would otherwise race between setting it and
+// launching. Occupancy follows each launch's actual dynamic size.
+template <class F>
+inline cudaError_t AllowDynamicSmem(F* kernel) {
+  static const int optin = [] {
+    int device = 0, bytes = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&bytes, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    return bytes;
+  }();
+  cudaFuncAttributes a{};
+  if (const cudaError_t e = cudaFuncGetAttributes(&a, kernel); e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - static_cast<int>(a.sharedSizeBytes));
+}
+
 constexpr int kWarp = 32;
 
 }  // namespace sl3dgpu

@@ -950,7 +950,7 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   const RingFn<double2> kernel = RingKernelFor<double2>(g.nphi, &buffers);
   const int rings = RingsPerCta<double2>(g.nphi, buffers);
   const size_t smem = RingSmem<double2>(g.nphi, rings, buffers);
-  SL3D_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  SL3D_CUDA(AllowDynamicSmem(kernel));
   dim3 grid((count + rings - 1) / rings, g.ntheta);
   // algorithmic traffic: the spectra and the grid values the mode reads and writes
   const double spec = static_cast<double>(real ? g.lmax + 1 : 2 * g.lmax + 1) * g.ntheta * count * 16.0;
@@ -1089,7 +1089,7 @@ int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const floa
   const RingFn<float2> kernel = RingKernelFor<float2>(nphi, &buffers);
   const int rings = RingsPerCta<float2>(nphi, buffers);
   const size_t smem = RingSmem<float2>(nphi, rings, buffers);
-  SL3D_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  SL3D_CUDA(AllowDynamicSmem(kernel));
   dim3 grid((count + rings - 1) / rings, ntheta);
   const double spec = static_cast<double>(real ? lmax + 1 : 2 * lmax + 1) * ntheta * count * 8.0;
   const double wbytes = static_cast<double>(ntheta) * nphi * count * 4.0;

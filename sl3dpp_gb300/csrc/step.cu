@@ -23,6 +23,7 @@
 // residual. B has neither the fixed memory force nor the load, so the
 // correction passes need neither.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -564,6 +565,7 @@ int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
   // node and ends at its last node's element's last
   lateralFirst = last >= 0 ? elemFirstNode[nodeElement[first]] : 0;
   lateralEnd = last >= 0 ? elemFirstNode[nodeElement[last]] + geo.np : 0;
+  SL3D_CUDA(cudaStreamSynchronize(stream));  // no earlier kernel of the operator still reads it
   SL3D_CUDA(cudaMemcpy(factor.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
   return SL3DGPU_OK;
 }
@@ -1571,6 +1573,7 @@ int Viscoelastic3DGpu::SetModuli(const double* dMu, const double* dKappa, bool o
     }
     for (int p = 0; p < P; ++p)
       for (long long x = p * fieldSize; x < (p + 1) * fieldSize && !lateral[p]; ++x) lateral[p] = host[x] != 0.0;
+    SL3D_CUDA(cudaStreamSynchronize(stream));  // no earlier kernel of the operator still reads it
     SL3D_CUDA(cudaMemcpy(dst.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
     return SL3DGPU_OK;
   };
@@ -1944,6 +1947,7 @@ extern "C" int sl3dgpu_v3d_state_coefficients_host(const sl3dgpu_v3d* h, const s
     SetError("v3d: null argument or a state without strain coefficients");
     return SL3DGPU_ERR_ARGUMENT;
   }
+  SL3D_CUDA(cudaStreamSynchronize(h->op.stream));  // the legacy-stream copy does not wait for it
   SL3D_CUDA(cudaMemcpy(out, state->st.coeffs.p, h->op.spectralComplex * sizeof(double2), cudaMemcpyDeviceToHost));
   return SL3DGPU_OK;
 }
@@ -1955,6 +1959,51 @@ extern "C" int sl3dgpu_v3d_run(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const d
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.Run(state->st, times, nodes, scheme, loads, u, phi, infos);
+}
+
+// Independent runs driven by a pool of host threads, one run at a time per
+// thread; each operator's kernels stay on its own stream, so the runs'
+// kernels overlap on the GPU. A worker's error text is kept per run and the
+// first failure's text becomes the caller's.
+extern "C" int sl3dgpu_v3d_run_many(int count, sl3dgpu_v3d* const* ops, sl3dgpu_v3d_state* const* states,
+                                    const double* const* times, const int* nodes, int scheme,
+                                    const double* const* loads, double* const* u, double* const* phi,
+                                    sl3dgpu_step_info* const* infos, int threads, int* statuses) {
+  if (count < 0 || (count > 0 && (ops == nullptr || states == nullptr || times == nullptr || nodes == nullptr ||
+                                  loads == nullptr || statuses == nullptr))) {
+    SetError("v3d: run_many needs the operators, states, times, node counts, loads and statuses");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (int i = 0; i < count; ++i)
+    for (int j = 0; j < i; ++j)
+      if (ops[i] == ops[j] || states[i] == states[j]) {
+        SetError("v3d: run_many's runs need distinct operators and states");
+        return SL3DGPU_ERR_ARGUMENT;
+      }
+  int device = 0;
+  SL3D_CUDA(cudaGetDevice(&device));
+  const int cores = std::max(1, static_cast<int>(std::thread::hardware_concurrency()));
+  const int workers = std::max(1, std::min(count, threads > 0 ? threads : cores));
+  std::vector<std::string> errors(count);
+  std::atomic<int> next{0};
+  auto work = [&] {
+    cudaSetDevice(device);
+    for (int i = next.fetch_add(1); i < count; i = next.fetch_add(1)) {
+      statuses[i] = sl3dgpu_v3d_run(ops[i], states[i], times[i], nodes[i], scheme, loads[i], u ? u[i] : nullptr,
+                                    phi ? phi[i] : nullptr, infos ? infos[i] : nullptr);
+      if (statuses[i] != SL3DGPU_OK) errors[i] = sl3dgpu_last_error();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int w = 1; w < workers; ++w) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  for (int i = 0; i < count; ++i)
+    if (statuses[i] != SL3DGPU_OK) {
+      SetError("v3d: run " + std::to_string(i) + ": " + errors[i]);
+      return statuses[i];
+    }
+  return SL3DGPU_OK;
 }
 
 extern "C" int sl3dgpu_v3d_surface(sl3dgpu_v3d* h, int component, double* out) {

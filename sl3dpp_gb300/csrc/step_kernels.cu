@@ -895,7 +895,7 @@ template <class T2>
 void Forces(const Geometry& g, const T2* spectral, T2* rhsSph, T2* rhsTor, cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   const size_t smem = static_cast<size_t>(g.P) * 6 * sizeof(T2);
-  cudaFuncSetAttribute(ForceKernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  AllowDynamicSmem(ForceKernel<T2>);
   prof::Scope scope(prof::kForce, stream);
   ForceKernel<T2><<<count, 128, smem, stream>>>(g, spectral, rhsSph, rhsTor);
 }
@@ -904,7 +904,7 @@ template <class T2>
 void Strain(const Geometry& g, const T2* solSph, const T2* solTor, T2* spectral, cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 3 * sizeof(T2);
-  cudaFuncSetAttribute(StrainKernel<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  AllowDynamicSmem(StrainKernel<T2>);
   prof::Scope scope(prof::kStrain, stream);
   StrainKernel<T2><<<count, 128, smem, stream>>>(g, solSph, solTor, spectral);
 }
@@ -929,7 +929,7 @@ void LaunchStrain(const Geometry& g, const float2* solSph, const float2* solTor,
 void LaunchDilatation(const Geometry& g, const double2* solSph, double2* scalar, cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 2 * sizeof(double2);
-  cudaFuncSetAttribute(DilatationKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  AllowDynamicSmem(DilatationKernel);
   prof::Scope scope(prof::kStrain, stream);
   DilatationKernel<<<count, 128, smem, stream>>>(g, solSph, scalar);
 }
@@ -937,7 +937,7 @@ void LaunchDilatation(const Geometry& g, const double2* solSph, double2* scalar,
 void LaunchDilatationForce(const Geometry& g, const double2* scalar, double2* rhsSph, cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   const size_t smem = static_cast<size_t>(g.P) * sizeof(double2);
-  cudaFuncSetAttribute(DilatationForceKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  AllowDynamicSmem(DilatationForceKernel);
   prof::Scope scope(prof::kForce, stream);
   DilatationForceKernel<<<count, 128, smem, stream>>>(g, scalar, rhsSph);
 }

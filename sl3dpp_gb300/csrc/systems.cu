@@ -183,6 +183,9 @@ int BuildSystems(const SystemsInput& in, Flavour& f) {
     SL3D_CUDA(dPiv.Alloc(pivots.size()));
     SL3D_CUDA(luInfo.Alloc(luSys.size()));
     SL3D_TRY(BandFactorBatch(dLuSys.p, luSys.data(), static_cast<int>(luSys.size()), dLu.p, dPiv.p, luInfo.p, 1, stream));
+    // the copies below run on the legacy stream, which does not wait for
+    // this non-blocking one: the factors and pivots must be complete first
+    SL3D_CUDA(cudaStreamSynchronize(stream));
     std::vector<int> hLuInfo(luSys.size());
     SL3D_CUDA(cudaMemcpy(hLuInfo.data(), luInfo.p, hLuInfo.size() * sizeof(int), cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < luSys.size(); ++i)

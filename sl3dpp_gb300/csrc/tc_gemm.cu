@@ -273,7 +273,7 @@ int RunGemmTc(const TcItem* tcItems, int count, int maxMTiles, int maxNTiles, in
   if (count == 0 || maxMTiles == 0 || maxNTiles == 0) return SL3DGPU_OK;
   const size_t smem = static_cast<size_t>(kStages) * 2 * (kATileFloats + tileN * kTcTileK) * sizeof(float) +
                       2 * kStages * sizeof(uint64_t) + 16;
-  SL3D_CUDA(cudaFuncSetAttribute(TcGemmKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  SL3D_CUDA(AllowDynamicSmem(TcGemmKernel));
   dim3 grid(static_cast<unsigned>(maxMTiles), static_cast<unsigned>(count), static_cast<unsigned>(maxNTiles));
   TcGemmKernel<<<grid, kThreads, smem, stream>>>(tcItems, tileN, panels, packed, C, accumulate, errorFlag);
   SL3D_CHECK_LAUNCH();

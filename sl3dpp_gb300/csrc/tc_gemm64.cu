@@ -373,7 +373,7 @@ int RunGemm64Tc(const Tc64Item* tcItems, int count, int maxMTiles, int maxNTiles
   constexpr size_t smem = static_cast<size_t>(kStages) * kSlices * (kATile + kBTile) * sizeof(uint16_t) +
                           2 * kStages * sizeof(uint64_t) + 16;
   static_assert(smem <= 227 * 1024, "the stages fit in shared memory");
-  SL3D_CUDA(cudaFuncSetAttribute(TcGemm64Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  SL3D_CUDA(AllowDynamicSmem(TcGemm64Kernel));
   dim3 grid(static_cast<unsigned>(maxNTiles), static_cast<unsigned>(maxMTiles), static_cast<unsigned>(count));
   TcGemm64Kernel<<<grid, kThreads, smem, stream>>>(tcItems, panels, packed, rowExp, colExp, C, accumulate,
                                                    errorFlag);

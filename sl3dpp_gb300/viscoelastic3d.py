@@ -92,6 +92,7 @@ def _signatures():
         "sl3dgpu_v3d_start_taken": (i, [v]),
         "sl3dgpu_v3d_state_coefficients": (i, [v, v, ctypes.POINTER(c_void_p), ctypes.POINTER(ctypes.c_longlong)]),
         "sl3dgpu_v3d_run": (i, [v, v, P_double, i, i, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_run_many": (i, [i, v, v, v, v, i, v, v, v, v, i, v]),
         "sl3dgpu_v3d_state_coefficients_host": (i, [v, v, v]),
     }
     for name, (res, args) in sig.items():
