@@ -710,6 +710,7 @@ Grid::~Grid() {
     cudaFree(b.items);
     cudaFree(b.tcItems);
     cudaFree(b.packed);
+    cudaFree(b.dTcTiles);
     cudaFree(b.tc64Items);
     cudaFree(b.packed64);
     cudaFree(b.colExp);
@@ -829,6 +830,9 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
     b.maxNTiles = std::max(b.maxNTiles, h.nTiles);
     b.maxATiles = std::max(b.maxATiles, h.mTiles * h.kSteps);
     b.maxBTiles = std::max(b.maxBTiles, h.nTiles * h.kSteps);
+    for (int mt = 0; mt < h.mTiles; ++mt)
+      for (int nt = 0; nt < h.nTiles; ++nt)
+        b.tcTiles.push_back(make_int4(static_cast<int>(b.tcHost.size()), mt, nt, 0));
     b.tcHost.push_back(h);
     // the FP64 emulation's tiles: 128 rows, 64 columns, 16 deep, seven
     // slices a tile
@@ -1012,6 +1016,9 @@ int Grid::RunGemmF(int N, bool real, Batch& b, const float* B, float* C, bool ac
     SL3D_CUDA(cudaMalloc(&b.tcItems, b.tcHost.size() * sizeof(TcItem)));
     SL3D_CUDA(cudaMemcpy(b.tcItems, b.tcHost.data(), b.tcHost.size() * sizeof(TcItem), cudaMemcpyHostToDevice));
     SL3D_CUDA(cudaMalloc(&b.packed, std::max<long long>(b.packedFloats, 1) * sizeof(float)));
+    SL3D_CUDA(cudaMalloc(&b.dTcTiles, std::max<size_t>(b.tcTiles.size(), 1) * sizeof(int4)));
+    if (!b.tcTiles.empty())
+      SL3D_CUDA(cudaMemcpy(b.dTcTiles, b.tcTiles.data(), b.tcTiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
   }
   const auto* items = static_cast<const TcItem*>(b.tcItems);
   const std::array<int, 3> key{N, real ? 1 : 0, b.analysis ? 1 : 0};
@@ -1032,8 +1039,8 @@ int Grid::RunGemmF(int N, bool real, Batch& b, const float* B, float* C, bool ac
     SL3D_CHECK_LAUNCH();
   }
   prof::Scope scope(prof::kLegendre32, stream, b.flops);
-  return RunGemmTc(items, b.count, b.maxMTiles, b.maxNTiles, b.tileN, found->second, b.packed, C, accumulate,
-                   dTcError_, stream);
+  return RunGemmTc(items, b.dTcTiles, static_cast<int>(b.tcTiles.size()), b.tileN, found->second, b.packed, C,
+                   accumulate, dTcError_, stream);
 }
 
 Grid::Batch* Grid::MutableBatch(int N, bool real, bool analysis, int P, int p0, int count) {

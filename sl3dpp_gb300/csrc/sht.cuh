@@ -153,6 +153,8 @@ class Grid {
     int tileN = 0, maxMTiles = 0, maxNTiles = 0, maxATiles = 0, maxBTiles = 0;
     long long panelFloats = 0, packedFloats = 0;
     float* packed = nullptr;
+    std::vector<int4> tcTiles;  // {item, row tile, column tile}, column tiles of a row tile adjacent
+    int4* dTcTiles = nullptr;
     int maxK = 0;
     // the FP64 emulation's form: items, extents, packed B and column
     // exponents (made on first use)

@@ -18,8 +18,6 @@
 namespace sl3dgpu {
 namespace {
 
-constexpr int kStages = 3;
-constexpr int kThreads = 128;
 constexpr int kATileFloats = kTcTileM * kTcTileK;  // one part: 2048 floats, 8 KB
 
 // Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B,
@@ -104,150 +102,235 @@ __global__ void PackBKernel(const TcItem* tcItems, int tileN, const float* B, fl
   }
 }
 
-__global__ void __launch_bounds__(kThreads) TcGemmKernel(const TcItem* tcItems, int tileN, const float* panels,
-                                                         const float* packed, float* C, bool accumulate,
-                                                         int* errorFlag) {
-  const TcItem it = tcItems[blockIdx.y];
-  const int mt = blockIdx.x, nt = blockIdx.z;
-  if (mt >= it.mTiles || nt >= it.nTiles) return;  // the whole CTA, before any tensor-memory work
-  const int i0 = mt * kTcTileM, n0 = nt * tileN;
-  const int nCols = min(tileN, it.N - n0);
-  const int nMma = (nCols + 15) / 16 * 16;  // the MMA's N: a multiple of 16
-  const uint32_t tmemColumns = TmemColumns(tileN);
+// The persistent, warp-specialised contraction: one CTA per SM walks the
+// batch's tile list (tile t, t + gridDim.x, ...). Warp 0 (one lane) is the TMA
+// producer, filling a ring of `stages` shared-memory stages (the A tile's
+// two parts and B's) ahead of use; warp 1 (one lane) issues each step's six
+// MMAs into one of two TMEM accumulators and commits them to the stage's
+// "empty" barrier, and a tile's last step also to its accumulator's "full"
+// barrier; warps 2-5 drain a full accumulator (each its TMEM lane quarter,
+// warp % 4) to C and release it. The epilogue of one tile thus overlaps the
+// main loop of the next, and the copies never wait for an epilogue. Stage g
+// of the CTA's step sequence uses ring slot g % stages in use round
+// g / stages; tile i uses accumulator i % 2 in round i / 2. Every wait is
+// bounded: one that gives up sets the error flag and a shared abort flag that
+// ends the other roles' loops; before TMEM is freed the MMA lane waits for its
+// issued MMAs and the producer for its issued copies (bounded too).
+constexpr int kPersistentThreads = 192;
+
+__global__ void __launch_bounds__(kPersistentThreads, 1)
+    TcGemmKernel(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN, int stages,
+                 const float* panels, const float* packed, float* C, bool accumulate, int* errorFlag) {
   const int bTileFloats = tileN * kTcTileK;
+  const uint32_t accColumns = TmemColumns(tileN);
   const uint32_t aBytes = 2 * kATileFloats * sizeof(float), bBytes = 2 * bTileFloats * sizeof(float);
 
   extern __shared__ __align__(128) unsigned char tcSmem[];
-  float* sA = reinterpret_cast<float*>(tcSmem);  // kStages x (hi | lo)
-  float* sB = sA + kStages * 2 * kATileFloats;   // kStages x (hi | lo)
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + kStages * 2 * bTileFloats);
-  uint64_t* empty = full + kStages;
-  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(empty + kStages);
-  __shared__ int okShared;
+  float* sA = reinterpret_cast<float*>(tcSmem);  // stages x (hi | lo)
+  float* sB = sA + stages * 2 * kATileFloats;    // stages x (hi | lo)
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + stages * 2 * bTileFloats);
+  uint64_t* empty = full + stages;
+  uint64_t* accFull = empty + stages;  // 2
+  uint64_t* accEmpty = accFull + 2;    // 2
+  uint64_t* drain = accEmpty + 2;
+  uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(drain + 1);
+  __shared__ volatile int abortFlag;
+  __shared__ float rowsOut[4][32][33];  // each epilogue warp's 32 x 32 block, padded
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(SmemAddr(tmemSlot)),
-                 "r"(tmemColumns)
+                 "r"(2 * accColumns)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    abortFlag = 0;
+    for (int s = 0; s < stages; ++s) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(full + s)), "r"(1) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(empty + s)), "r"(1) : "memory");
     }
+    for (int a = 0; a < 2; ++a) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(accFull + a)), "r"(1) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(accEmpty + a)), "r"(128) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(drain)), "r"(1) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmemSlot;
+  auto giveUp = [&] {
+    abortFlag = 1;
+    atomicExch(errorFlag, 1);
+  };
 
-  if (tid == 0) {
-    const float* aSrc = panels + it.aPanel + static_cast<long long>(mt) * it.kSteps * 2 * kATileFloats;
-    const float* bSrc = packed + it.bPack + static_cast<long long>(nt) * it.kSteps * 2 * bTileFloats;
-    const uint32_t idesc = InstrDescriptor(nMma, kTcTileM);
-    uint32_t phaseFull[kStages] = {0, 0, 0}, phaseEmpty[kStages] = {0, 0, 0};
-    bool ok = true;
-    // Arm buffer ks % kStages for step ks and issue its two copies; a buffer
-    // in use is first freed by its MMAs' commit.
-    auto issue = [&](int ks) {
-      const int buf = ks % kStages;
-      if (ks >= kStages) {
-        ok = ok && WaitParity(SmemAddr(empty + buf), phaseEmpty[buf]);
-        phaseEmpty[buf] ^= 1u;
-      }
-      if (!ok) return;
-      const uint32_t bar = SmemAddr(full + buf);
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(aBytes + bBytes)
-                   : "memory");
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              SmemAddr(sA + buf * 2 * kATileFloats)),
-          "l"(aSrc + static_cast<long long>(ks) * 2 * kATileFloats), "r"(aBytes), "r"(bar)
-          : "memory");
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              SmemAddr(sB + buf * 2 * bTileFloats)),
-          "l"(bSrc + static_cast<long long>(ks) * 2 * bTileFloats), "r"(bBytes), "r"(bar)
-          : "memory");
-    };
-    for (int ks = 0; ks < min(kStages - 1, it.kSteps); ++ks) issue(ks);
-    for (int ks = 0; ks < it.kSteps && ok; ++ks) {
-      if (ks + kStages - 1 < it.kSteps) issue(ks + kStages - 1);
-      if (!ok) break;
-      const int buf = ks % kStages;
-      ok = WaitParity(SmemAddr(full + buf), phaseFull[buf]);
-      phaseFull[buf] ^= 1u;
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t aHi = SmemAddr(sA + buf * 2 * kATileFloats), aLo = aHi + kATileFloats * 4;
-      const uint32_t bHi = SmemAddr(sB + buf * 2 * bTileFloats), bLo = bHi + bTileFloats * 4;
-      const uint32_t aLbo = kTcTileM * 16, bLbo = tileN * 16, sbo = 128;
-#pragma unroll
-      for (int q = 0; q < kTcTileK / 8; ++q) {
-        const uint32_t aOff = q * 2 * aLbo, bOff = q * 2 * bLbo;
-        const uint64_t dAh = Descriptor(aHi + aOff, aLbo, sbo), dAl = Descriptor(aLo + aOff, aLbo, sbo);
-        const uint64_t dBh = Descriptor(bHi + bOff, bLbo, sbo), dBl = Descriptor(bLo + bOff, bLbo, sbo);
-        const uint64_t as[3] = {dAh, dAh, dAl};
-        const uint64_t bs[3] = {dBh, dBl, dBh};
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-          const uint32_t enable = (ks > 0 || q > 0 || p > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n\t.reg .pred r;\n\t"
-              "setp.ne.b32 r, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, r;\n\t}" ::"r"(tmem),
-              "l"(as[p]), "l"(bs[p]), "r"(idesc), "r"(enable)
-              : "memory");
+  if (warp == 0 && lane == 0) {
+    // -- producer --------------------------------------------------------------
+    long long g = 0;
+    for (int t = blockIdx.x; t < tileCount && !abortFlag; t += gridDim.x) {
+      const int4 tile = tiles[t];
+      const TcItem it = tcItems[tile.x];
+      const float* aSrc = panels + it.aPanel + static_cast<long long>(tile.y) * it.kSteps * 2 * kATileFloats;
+      const float* bSrc = packed + it.bPack + static_cast<long long>(tile.z) * it.kSteps * 2 * bTileFloats;
+      for (int ks = 0; ks < it.kSteps; ++ks, ++g) {
+        const int slot = static_cast<int>(g % stages);
+        const long long round = g / stages;
+        if (round > 0 && !WaitParity(SmemAddr(empty + slot), static_cast<uint32_t>((round - 1) & 1))) {
+          giveUp();
+          break;
         }
+        if (abortFlag) break;
+        const uint32_t bar = SmemAddr(full + slot);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(aBytes + bBytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                SmemAddr(sA + slot * 2 * kATileFloats)),
+            "l"(aSrc + static_cast<long long>(ks) * 2 * kATileFloats), "r"(aBytes), "r"(bar)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                SmemAddr(sB + slot * 2 * bTileFloats)),
+            "l"(bSrc + static_cast<long long>(ks) * 2 * bTileFloats), "r"(bBytes), "r"(bar)
+            : "memory");
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       SmemAddr(empty + buf))
-                   : "memory");
     }
-    // The last step's commit covers every MMA before it.
-    if (ok && it.kSteps > 0) {
-      const int last = (it.kSteps - 1) % kStages;
-      ok = WaitParity(SmemAddr(empty + last), phaseEmpty[last]);
-    }
-    okShared = ok ? 1 : 0;
-    if (!ok) atomicExch(errorFlag, 1);
-  }
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (okShared) {
-    // Epilogue: this warp's TMEM lane quarter, 16 columns at a time.
-    const int i = i0 + 32 * warp + lane;
-    float* c = C + it.c + static_cast<long long>(i) * it.ldc + n0;
-    for (int c0 = 0; c0 < nMma; c0 += 16) {
-      uint32_t r[16];
-      const uint32_t addr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(c0);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-          "%15}, [%16];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(addr)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (i < it.M) {
+    // the copies issued last land before the CTA can end (the MMA lane has
+    // waited for all it consumed; on an abort some may be unconsumed)
+    for (long long q = g > stages ? g - stages : 0; q < g; ++q)
+      WaitParity(SmemAddr(full + static_cast<int>(q % stages)), static_cast<uint32_t>((q / stages) & 1));
+  } else if (warp == 1 && lane == 0) {
+    // -- MMA issue ---------------------------------------------------------------
+    long long g = 0;
+    int local = 0;
+    bool issued = false;
+    for (int t = blockIdx.x; t < tileCount && !abortFlag; t += gridDim.x, ++local) {
+      const int4 tile = tiles[t];
+      const TcItem it = tcItems[tile.x];
+      const int nCols = min(tileN, it.N - tile.z * tileN);
+      const uint32_t idesc = InstrDescriptor((nCols + 15) / 16 * 16, kTcTileM);
+      const int acc = local & 1;
+      const int use = local >> 1;
+      if (use > 0 && !WaitParity(SmemAddr(accEmpty + acc), static_cast<uint32_t>((use - 1) & 1))) {
+        giveUp();
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d = tmem + acc * accColumns;
+      bool ok = true;
+      for (int ks = 0; ks < it.kSteps; ++ks, ++g) {
+        const int slot = static_cast<int>(g % stages);
+        if (!WaitParity(SmemAddr(full + slot), static_cast<uint32_t>((g / stages) & 1)) || abortFlag) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t aHi = SmemAddr(sA + slot * 2 * kATileFloats), aLo = aHi + kATileFloats * 4;
+        const uint32_t bHi = SmemAddr(sB + slot * 2 * bTileFloats), bLo = bHi + bTileFloats * 4;
+        const uint32_t aLbo = kTcTileM * 16, bLbo = tileN * 16, sbo = 128;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int n = c0 + q;
-          if (n < nCols) {
-            const float v = __uint_as_float(r[q]);
-            c[n] = accumulate ? c[n] + v : v;
+        for (int q = 0; q < kTcTileK / 8; ++q) {
+          const uint32_t aOff = q * 2 * aLbo, bOff = q * 2 * bLbo;
+          const uint64_t dAh = Descriptor(aHi + aOff, aLbo, sbo), dAl = Descriptor(aLo + aOff, aLbo, sbo);
+          const uint64_t dBh = Descriptor(bHi + bOff, bLbo, sbo), dBl = Descriptor(bLo + bOff, bLbo, sbo);
+          const uint64_t as[3] = {dAh, dAh, dAl};
+          const uint64_t bs[3] = {dBh, dBl, dBh};
+#pragma unroll
+          for (int p = 0; p < 3; ++p) {
+            const uint32_t enable = (ks > 0 || q > 0 || p > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred r;\n\t"
+                "setp.ne.b32 r, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, r;\n\t}" ::"r"(d),
+                "l"(as[p]), "l"(bs[p]), "r"(idesc), "r"(enable)
+                : "memory");
           }
         }
+        issued = true;
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         SmemAddr(empty + slot))
+                     : "memory");
       }
+      if (!ok) {
+        giveUp();
+        break;
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       SmemAddr(accFull + acc))
+                   : "memory");
+    }
+    // every MMA issued has completed before TMEM is freed
+    if (issued) {
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       SmemAddr(drain))
+                   : "memory");
+      if (!WaitParity(SmemAddr(drain), 0)) atomicExch(errorFlag, 1);
+    }
+  } else if (warp >= 2) {
+    // -- epilogue ----------------------------------------------------------------
+    const int quarter = warp % 4;
+    int local = 0;
+    for (int t = blockIdx.x; t < tileCount && !abortFlag; t += gridDim.x, ++local) {
+      const int4 tile = tiles[t];
+      const TcItem it = tcItems[tile.x];
+      const int acc = local & 1;
+      if (!WaitParity(SmemAddr(accFull + acc), static_cast<uint32_t>((local >> 1) & 1))) {
+        giveUp();
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int n0 = tile.z * tileN;
+      const int nCols = min(tileN, it.N - n0), nMma = (nCols + 15) / 16 * 16;
+      // TMEM gives a lane one row; the rows go out through shared memory so
+      // that each store instruction writes one row's 32 consecutive columns
+      const int row0 = tile.y * kTcTileM + 32 * quarter;
+      float(*block)[33] = rowsOut[warp - 2];
+      for (int c0 = 0; c0 < nMma; c0 += 32) {
+        uint32_t r[32];
+        const uint32_t addr =
+            tmem + (static_cast<uint32_t>(32 * quarter) << 16) + acc * accColumns + static_cast<uint32_t>(c0);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(addr)
+            : "memory");
+        if (c0 + 16 < nMma)
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+              "%14, %15}, [%16];"
+              : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+                "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                "=r"(r[30]), "=r"(r[31])
+              : "r"(addr + 16)
+              : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int q = 0; q < 32; ++q) block[lane][q] = __uint_as_float(r[q]);
+        __syncwarp();
+        const int n = c0 + lane;
+        for (int rr = 0; rr < 32; ++rr) {
+          const int i = row0 + rr;
+          if (i < it.M && n < nCols) {
+            float* c = C + it.c + static_cast<long long>(i) * it.ldc + n0 + n;
+            const float v = block[rr][lane];
+            *c = accumulate ? *c + v : v;
+          }
+        }
+        __syncwarp();
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(SmemAddr(accEmpty + acc)) : "memory");
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmemColumns) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * accColumns)
+                 : "memory");
 }
 
 }  // namespace
@@ -268,14 +351,22 @@ void LaunchPackB(const TcItem* tcItems, int count, int maxTiles, int tileN, cons
   PackBKernel<<<dim3(blocks, count), 256, 0, stream>>>(tcItems, tileN, B, packed);
 }
 
-int RunGemmTc(const TcItem* tcItems, int count, int maxMTiles, int maxNTiles, int tileN, const float* panels,
+int RunGemmTc(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN, const float* panels,
               const float* packed, float* C, bool accumulate, int* errorFlag, cudaStream_t stream) {
-  if (count == 0 || maxMTiles == 0 || maxNTiles == 0) return SL3DGPU_OK;
-  const size_t smem = static_cast<size_t>(kStages) * 2 * (kATileFloats + tileN * kTcTileK) * sizeof(float) +
-                      2 * kStages * sizeof(uint64_t) + 16;
+  if (tileCount == 0) return SL3DGPU_OK;
+  static const int sms = [] {
+    int device = 0, count = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, device);
+    return std::max(count, 1);
+  }();
+  const size_t stageBytes = 2 * (kATileFloats + static_cast<size_t>(tileN) * kTcTileK) * sizeof(float);
+  const int stages = static_cast<int>(std::min<size_t>(8, std::max<size_t>(2, (200 * 1024) / stageBytes)));
+  const size_t smem = stages * stageBytes + (2 * stages + 5) * sizeof(uint64_t) + 16;
   SL3D_CUDA(AllowDynamicSmem(TcGemmKernel));
-  dim3 grid(static_cast<unsigned>(maxMTiles), static_cast<unsigned>(count), static_cast<unsigned>(maxNTiles));
-  TcGemmKernel<<<grid, kThreads, smem, stream>>>(tcItems, tileN, panels, packed, C, accumulate, errorFlag);
+  const int blocks = std::min(tileCount, sms);
+  TcGemmKernel<<<blocks, kPersistentThreads, smem, stream>>>(tcItems, tiles, tileCount, tileN, stages, panels,
+                                                            packed, C, accumulate, errorFlag);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }

@@ -72,10 +72,11 @@ void LaunchPanelA(const GemmItem* items, const TcItem* tcItems, int count, int m
 // Split and pack B into the items' tiles. maxTiles: the most (nTiles x kSteps).
 void LaunchPackB(const TcItem* tcItems, int count, int maxTiles, int tileN, const float* B, float* packed,
                  cudaStream_t stream);
-// The contraction: per CTA one (128-row tile, item, column tile).
-// errorFlag: a device int set non-zero if a completion wait gives up (the
-// launch then leaves C unspecified and the caller reports it).
-int RunGemmTc(const TcItem* tcItems, int count, int maxMTiles, int maxNTiles, int tileN, const float* panels,
+// The contraction over a tile list ({item, row tile, column tile} per
+// entry), persistent CTAs, one per SM. errorFlag: a device int set non-zero
+// if a completion wait gives up (the launch then leaves C unspecified and
+// the caller reports it).
+int RunGemmTc(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN, const float* panels,
               const float* packed, float* C, bool accumulate, int* errorFlag, cudaStream_t stream);
 
 // -- FP64 emulated on the tensor cores (tc_gemm64.cu) ------------------------------------

@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
   uint64_t* empty = full + kStages;
   uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(empty + kStages);
   __shared__ int okShared;
+  __shared__ double rowsOut[4][32][17];  // each warp's 32 x 16 block, padded
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 
   if (warp == 0) {
@@ -305,10 +306,9 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (okShared) {
     // Epilogue: this warp's lane quarter (32 rows), 16 columns at a time, the
-    // seven levels joined in FP64, smallest first.
+    // seven levels joined as integers and then in FP64.
     const int i = i0 + 32 * warp + lane;
     const int e = i < it.M ? rowExp[it.rowExp + i] : 0;
-    double* c = C + it.c + static_cast<long long>(i) * it.ldc + n0;
     for (int c0 = 0; c0 < kTileN; c0 += 16) {
       uint32_t r[kSlices][16];
 #pragma unroll
@@ -324,21 +324,34 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
             : "memory");
       }
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (i < it.M) {
+      // the joined values of this lane's row, then out through shared memory
+      // so that a store instruction writes two rows' 16 consecutive columns
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int n = c0 + q;
-          if (n >= nCols) continue;
+      for (int q = 0; q < 16; ++q) {
+        const int n = c0 + q;
+        double v = 0.0;
+        if (i < it.M && n < nCols) {
           long long acc[kSlices];
 #pragma unroll
           for (int d = 0; d < kSlices; ++d) acc[d] = __float2int_rn(__uint_as_float(r[d][q]));
           const long long H = (acc[0] << 14) + (acc[1] << 7) + acc[2];
           const long long L = (acc[3] << 21) + (acc[4] << 14) + (acc[5] << 7) + acc[6];
           const int scale = e + colExp[it.colExp + n0 + n];
-          const double v = fma(static_cast<double>(H), Pow2(scale - 28), static_cast<double>(L) * Pow2(scale - 56));
-          c[n] = accumulate ? c[n] + v : v;
+          v = fma(static_cast<double>(H), Pow2(scale - 28), static_cast<double>(L) * Pow2(scale - 56));
+        }
+        rowsOut[warp][lane][q] = v;
+      }
+      __syncwarp();
+      const int n = c0 + (lane & 15);
+      for (int rr = lane >> 4; rr < 32; rr += 2) {
+        const int row = i0 + 32 * warp + rr;
+        if (row < it.M && n < nCols) {
+          double* dst = C + it.c + static_cast<long long>(row) * it.ldc + n0 + n;
+          const double v = rowsOut[warp][rr][lane & 15];
+          *dst = accumulate ? *dst + v : v;
         }
       }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
