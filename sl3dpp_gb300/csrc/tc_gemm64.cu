@@ -15,8 +15,8 @@
 // accumulator -- for K <= 455 at d = 6. The levels d < 7 are kept (28
 // products per 16-deep step) and joined exactly as integers,
 // H = acc_0 2^14 + acc_1 2^7 + acc_2 and L = acc_3 2^21 + acc_4 2^14 +
-// acc_5 2^7 + acc_6, then in FP64:
-//   C(i, n) = 2^{e_i + f_n} (2^{-28} H + 2^{-56} L).
+// acc_5 2^7 + acc_6, and C(i, n) = 2^{e_i + f_n} (2^{-28} H + 2^{-56} L) is
+// rounded once to FP64 from that exact integer, by integer arithmetic.
 //
 // Kernel. One CTA of four warps per (64-column tile, 128-row tile, item),
 // the column tiles of a row tile adjacent in the launch so that its A panel
@@ -89,9 +89,40 @@ __device__ inline void Split(double v, int e, uint32_t (&s)[kSlices]) {
   s[0] = Bf16Bits(static_cast<int>(X));
 }
 
-// 2^k as a double (exact), by its bits in the normal range.
-__device__ inline double Pow2(int k) {
-  return (k >= -1022 && k <= 1023) ? __longlong_as_double(static_cast<long long>(k + 1023) << 52) : ldexp(1.0, k);
+// (H 2^28 + L) 2^(scale - 56) as a double, rounded to nearest even, by
+// integer arithmetic (the exact 128-bit integer's top 53 bits and its
+// exponent written into the bits); values outside the normal range take the
+// slow path through ldexp.
+__device__ inline double JoinToDouble(long long H, long long L, int scale) {
+  const __int128 T = (static_cast<__int128>(H) << 28) + L;
+  if (T == 0) return 0.0;
+  const bool negative = T < 0;
+  const unsigned __int128 m = negative ? -static_cast<unsigned __int128>(T) : static_cast<unsigned __int128>(T);
+  const unsigned long long top = static_cast<unsigned long long>(m >> 64), low = static_cast<unsigned long long>(m);
+  const int bits = top ? 128 - __clzll(top) : 64 - __clzll(low);  // the integer's bit length
+  const int shift = bits - 53;
+  unsigned long long mantissa;
+  int exponent = bits - 1 + scale - 56;
+  if (shift > 0) {
+    const unsigned __int128 q = m >> shift;
+    const unsigned __int128 rem = m - (q << shift), half = static_cast<unsigned __int128>(1) << (shift - 1);
+    mantissa = static_cast<unsigned long long>(q);
+    if (rem > half || (rem == half && (mantissa & 1))) ++mantissa;
+    if (mantissa >> 53) {
+      mantissa >>= 1;
+      ++exponent;
+    }
+  } else {
+    mantissa = static_cast<unsigned long long>(m) << -shift;
+  }
+  if (exponent < -1022 || exponent > 1023) {
+    const double v = ldexp(static_cast<double>(mantissa), exponent - 52);
+    return negative ? -v : v;
+  }
+  const unsigned long long out = (negative ? (1ULL << 63) : 0ULL) |
+                                 (static_cast<unsigned long long>(exponent + 1023) << 52) |
+                                 (mantissa & ((1ULL << 52) - 1));
+  return __longlong_as_double(static_cast<long long>(out));
 }
 
 // Offset (in BF16 values) of element (row, k) of a K-major 16-deep tile of
@@ -306,7 +337,7 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (okShared) {
     // Epilogue: this warp's lane quarter (32 rows), 16 columns at a time, the
-    // seven levels joined as integers and then in FP64.
+    // seven levels joined as integers and rounded once to FP64.
     const int i = i0 + 32 * warp + lane;
     const int e = i < it.M ? rowExp[it.rowExp + i] : 0;
     for (int c0 = 0; c0 < kTileN; c0 += 16) {
@@ -336,8 +367,7 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
           for (int d = 0; d < kSlices; ++d) acc[d] = __float2int_rn(__uint_as_float(r[d][q]));
           const long long H = (acc[0] << 14) + (acc[1] << 7) + acc[2];
           const long long L = (acc[3] << 21) + (acc[4] << 14) + (acc[5] << 7) + acc[6];
-          const int scale = e + colExp[it.colExp + n0 + n];
-          v = fma(static_cast<double>(H), Pow2(scale - 28), static_cast<double>(L) * Pow2(scale - 56));
+          v = JoinToDouble(H, L, e + colExp[it.colExp + n0 + n]);
         }
         rowsOut[warp][lane][q] = v;
       }
