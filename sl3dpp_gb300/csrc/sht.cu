@@ -446,9 +446,14 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   T2* tw = reinterpret_cast<T2*>(ringSmem);
   T2* twB = tw + n;  // the two-stage form's stage-B twiddles
   T2* bufs = twB + n;
+  // A real field's ring shares one complex transform with the next field's
+  // (z = x + i y; Z_m = X_m + i Y_m, X_m = (Z_m + conj Z_{n-m}) / 2,
+  // Y_m = (Z_m - conj Z_{n-m}) / 2i): a warp carries two real fields.
+  const int perRing = real ? 2 : 1;
   const int j = blockIdx.y;
-  const int p0 = blockIdx.x * G;
-  const int groups = min(G, count - p0);
+  const int p0 = blockIdx.x * G * perRing;
+  const int groups = min(G * perRing, count - p0);  // fields of this CTA
+  const int rings = (groups + perRing - 1) / perRing;
   const int mcount = real ? lmax + 1 : 2 * lmax + 1;
   for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = twGlobal[e];
   if constexpr (R1 > 0)
@@ -456,47 +461,55 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   T2* a = bufs + ringStride * warp;  // this warp's ring
   T2* b = buffers == 2 ? a + n : a;
   int at = 0;  // which of a, b holds the ring's current values
+  // the rows of this warp's fields (the second of a real pair may not exist)
+  const int f0 = p0 + perRing * warp, f1 = real ? f0 + 1 : f0;
+  const bool second = real && f1 < p0 + groups;
+  const long long row0 = (static_cast<long long>(f0) * ntheta + j) * n;
+  const long long row1 = (static_cast<long long>(f1) * ntheta + j) * n;
   if (mode == kRingSynth || mode == kRingWeighted) {
     for (int e = threadIdx.x; e < G * n; e += blockDim.x)
       bufs[ringStride * (e / n) + e % n] = Make<T2>(0, 0);
     __syncthreads();
 #pragma unroll 4
-    for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
-      const int g = e % groups, mi = e / groups;
+    for (int e = threadIdx.x; e < mcount * rings; e += blockDim.x) {
+      const int r = e % rings, mi = e / rings;
       const int m = real ? mi : mi - lmax;
-      const T2 v = spectraIn[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g];
-      T2* ring = bufs + ringStride * g;
+      const long long at0 = (static_cast<long long>(mi) * ntheta + j) * count + p0 + perRing * r;
+      const T2 v = spectraIn[at0];
+      T2* ring = bufs + ringStride * r;
       if (real) {
+        const T2 u = perRing * r + 1 < groups ? spectraIn[at0 + 1] : Make<T2>(0, 0);
         if (m == 0) {
-          ring[0] = Make<T2>(v.x, 0);
+          ring[0] = Make<T2>(v.x, u.x);
         } else {
-          ring[m] = v;
-          ring[n - m] = Make<T2>(v.x, -v.y);
+          ring[m] = Make<T2>(v.x - u.y, v.y + u.x);      // v + i u
+          ring[n - m] = Make<T2>(v.x + u.y, u.x - v.y);  // conj(v) + i conj(u)
         }
       } else {
         ring[m < 0 ? m + n : m] = v;
       }
     }
     __syncthreads();
-    if (warp < groups) {
+    if (warp < rings) {
       at = RingTransform<T2, R1, R2>(a, b, plan, tw, twB, +1, lane);
       T2* res = at ? b : a;
-      const long long row = (static_cast<long long>(p0 + warp) * ntheta + j) * n;
       if (mode == kRingSynth) {
         for (int k = lane; k < n; k += kWarp) {
-          if (real)
-            static_cast<T*>(fieldsOut)[row + k] = res[k].x;
-          else
-            static_cast<T2*>(fieldsOut)[row + k] = res[k];
+          if (real) {
+            static_cast<T*>(fieldsOut)[row0 + k] = res[k].x;
+            if (second) static_cast<T*>(fieldsOut)[row1 + k] = res[k].y;
+          } else {
+            static_cast<T2*>(fieldsOut)[row0 + k] = res[k];
+          }
         }
       } else {
-        // the pointwise weight on the synthesised values (a real field's
-        // imaginary part is dropped, as its synthesis does)
+        // the pointwise weights on the synthesised values
 #pragma unroll 5
         for (int k = lane; k < n; k += kWarp) {
-          const T w = pointWeight[row + k];
+          const T w0 = pointWeight[row0 + k];
+          const T w1 = real ? (second ? pointWeight[row1 + k] : T(0)) : w0;
           const T2 v = res[k];
-          res[k] = real ? Make<T2>(v.x * w, 0) : Make<T2>(v.x * w, v.y * w);
+          res[k] = Make<T2>(v.x * w0, v.y * w1);
         }
         __syncwarp();
       }
@@ -504,14 +517,20 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
     if (mode == kRingSynth) return;
   } else {
     __syncthreads();  // the twiddles
-    if (warp < groups) {
-      const long long row = (static_cast<long long>(p0 + warp) * ntheta + j) * n;
+    if (warp < rings) {
 #pragma unroll 5
       for (int k = lane; k < n; k += kWarp) {
-        T2 v = real ? Make<T2>(static_cast<const T*>(fieldsIn)[row + k], 0) : static_cast<const T2*>(fieldsIn)[row + k];
+        T2 v;
+        if (real) {
+          v = Make<T2>(static_cast<const T*>(fieldsIn)[row0 + k],
+                       second ? static_cast<const T*>(fieldsIn)[row1 + k] : T(0));
+        } else {
+          v = static_cast<const T2*>(fieldsIn)[row0 + k];
+        }
         if (pointWeight != nullptr) {
-          const T w = pointWeight[row + k];
-          v = Make<T2>(v.x * w, v.y * w);
+          const T w0 = pointWeight[row0 + k];
+          const T w1 = real ? (second ? pointWeight[row1 + k] : T(0)) : w0;
+          v = Make<T2>(v.x * w0, v.y * w1);
         }
         a[k] = v;
       }
@@ -521,7 +540,7 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   // the analysis transform from wherever the ring's values are; every ring
   // has the same stage count, so the result's side is the same for all: a
   // after two transforms, the stage parity's side after one
-  if (warp < groups) {
+  if (warp < rings) {
     T2* x = at ? b : a;
     T2* y = at ? a : b;
     RingTransform<T2, R1, R2>(x, y, plan, tw, twB, -1, lane);
@@ -533,7 +552,16 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
-    const T2 v = bufs[ringStride * g + (out ? n : 0) + (m < 0 ? m + n : m)];
+    const T2* ring = bufs + ringStride * (g / perRing) + (out ? n : 0);
+    T2 v;
+    if (real) {
+      const T2 z = ring[m], w = ring[m == 0 ? 0 : n - m];  // Z_m and Z_{n-m}
+      // X_m = (Z_m + conj Z_{n-m}) / 2, Y_m = (Z_m - conj Z_{n-m}) / 2i
+      v = g % 2 == 0 ? Make<T2>(T(0.5) * (z.x + w.x), T(0.5) * (z.y - w.y))
+                     : Make<T2>(T(0.5) * (z.y + w.y), T(0.5) * (w.x - z.x));
+    } else {
+      v = ring[m < 0 ? m + n : m];
+    }
     spectraOut[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
   }
 }
@@ -955,13 +983,15 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   const int rings = RingsPerCta<double2>(g.nphi, buffers);
   const size_t smem = RingSmem<double2>(g.nphi, rings, buffers);
   SL3D_CUDA(AllowDynamicSmem(kernel));
-  dim3 grid((count + rings - 1) / rings, g.ntheta);
+  const int fields = real ? 2 * rings : rings;  // real fields go two to a ring
+  dim3 grid((count + fields - 1) / fields, g.ntheta);
   // algorithmic traffic: the spectra and the grid values the mode reads and writes
   const double spec = static_cast<double>(real ? g.lmax + 1 : 2 * g.lmax + 1) * g.ntheta * count * 16.0;
   const double field = static_cast<double>(g.ntheta) * g.nphi * count * (real ? 8.0 : 16.0);
   const double wbytes = weight ? static_cast<double>(g.ntheta) * g.nphi * count * 8.0 : 0.0;
   const double bytes = mode == kRingWeighted ? 2 * spec + wbytes : spec + field + wbytes;
-  const double ffts = static_cast<double>(g.ntheta) * count * (mode == kRingWeighted ? 2 : 1);
+  // a real field's transform counts half a complex one (two share a ring)
+  const double ffts = static_cast<double>(g.ntheta) * count * (mode == kRingWeighted ? 2 : 1) * (real ? 0.5 : 1.0);
   prof::Scope scope(prof::kRing, stream, ffts * 5.0 * g.nphi * std::log2(static_cast<double>(g.nphi)), bytes);
   kernel<<<grid, rings * kWarp, smem, stream>>>(mode, g.lmax, g.ntheta, count, real, g.plan, g.dTwiddle,
                                           g.dWeights, reinterpret_cast<const double2*>(spectraIn),
@@ -1097,10 +1127,12 @@ int Grid::RingWeightedF(bool real, const float* spectraIn, int count, const floa
   const int rings = RingsPerCta<float2>(nphi, buffers);
   const size_t smem = RingSmem<float2>(nphi, rings, buffers);
   SL3D_CUDA(AllowDynamicSmem(kernel));
-  dim3 grid((count + rings - 1) / rings, ntheta);
+  const int fields = real ? 2 * rings : rings;  // real fields go two to a ring
+  dim3 grid((count + fields - 1) / fields, ntheta);
   const double spec = static_cast<double>(real ? lmax + 1 : 2 * lmax + 1) * ntheta * count * 8.0;
   const double wbytes = static_cast<double>(ntheta) * nphi * count * 4.0;
-  prof::Scope scope(prof::kRing32, stream, 2.0 * ntheta * count * 5.0 * nphi * std::log2(static_cast<double>(nphi)),
+  prof::Scope scope(prof::kRing32, stream,
+                    (real ? 1.0 : 2.0) * ntheta * count * 5.0 * nphi * std::log2(static_cast<double>(nphi)),
                     2 * spec + wbytes);
   kernel<<<grid, rings * kWarp, smem, stream>>>(kRingWeighted, lmax, ntheta, count, real, plan, dTwiddle32,
                                                   dWeights, reinterpret_cast<const float2*>(spectraIn), nullptr,
