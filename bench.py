@@ -280,32 +280,27 @@ def gpu_arm(args, rank, world, device, precision):
 
 
 def roofline(prof, fp64_gflops, fp32_gflops):
-    """The dominant kernel kind against its bound: the contractions against
-    the FMA throughput of their precision, measured live; the rest against the
-    measured HBM copy bandwidth."""
+    """The dominant kernel kind against the bound of its work: the FP64
+    Legendre GEMM and the FP64 ring FFTs against the FP64 FMA throughput
+    measured live, the emulated FP64 contraction against the measured BF16
+    tensor rate (algorithmic FP64 flops), the rest -- the 3xTF32 contraction
+    streaming its table panels included -- against the measured HBM copy
+    bandwidth with their algorithmic bytes."""
     kind = max(prof, key=lambda k: prof[k]["ms"])
     p = prof[kind]
     peaks, source = measured_peaks()
     per_launch_s = p["ms"] / 1e3 / max(p["launches"], 1)
     share = p["ms"] / sum(v["ms"] for v in prof.values())
-    compute = {"legendre_synthesis": ("fp64", fp64_gflops), "legendre_analysis": ("fp64", fp64_gflops),
-               "legendre_f32": ("fp32", fp32_gflops)}
-    if p["flops"] > 0 and kind == "legendre_f64_tc":
-        # algorithmic FP64 flops against the measured dense BF16 tensor rate
-        # (the 28 slice products a step are not counted)
+    flops_bound = {"legendre_synthesis": ("fp64", fp64_gflops / 1e3), "legendre_analysis": ("fp64", fp64_gflops / 1e3),
+                   "ring_fft": ("fp64", fp64_gflops / 1e3), "legendre_f64_tc": ("tensor", peaks["bf16_tflops"])}
+    if p["flops"] > 0 and kind in flops_bound:
+        bound, peak = flops_bound[kind]
         achieved = p["flops"] / max(p["launches"], 1) / per_launch_s / 1e12
-        peak = peaks["bf16_tflops"]
-        return {"kernel": kind, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": ncu_traffic(kind), "peak_source": source,
-                "share_of_timed": share}
-    if p["flops"] > 0 and kind in compute:
-        bound, gflops = compute[kind]
-        achieved = p["flops"] / max(p["launches"], 1) / per_launch_s / 1e12
-        peak = gflops / 1e3
+        peak_source = (source + " (dense BF16; the 28 slice products a step are not counted)" if bound == "tensor"
+                       else "FP64 FMA throughput measured live by sl3dgpu_fp64_fma_peak (CUDA-core arithmetic: "
+                            "MEASURED_PEAKS.json holds HBM and bf16 tensor figures only)")
         return {"kernel": kind, "bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": ncu_traffic(kind),
-                "peak_source": f"{bound.upper()} FMA throughput measured live by sl3dgpu_{bound}_fma_peak (CUDA-core "
-                               "arithmetic: MEASURED_PEAKS.json holds HBM and bf16 tensor figures only)",
+                "frac": achieved / peak, "traffic": ncu_traffic(kind), "peak_source": peak_source,
                 "share_of_timed": share}
     achieved = p["bytes"] / max(p["launches"], 1) / per_launch_s / 1e9
     return {"kernel": kind, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",

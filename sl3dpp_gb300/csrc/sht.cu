@@ -827,6 +827,7 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
     b.maxN = std::max(b.maxN, it.N);
     b.maxK = std::max(b.maxK, it.K);
     b.flops += 2.0 * it.M * it.N * it.K;
+    b.outputs += static_cast<double>(it.M) * it.N;
     items.push_back(it);
   }
   b.count = static_cast<int>(items.size());
@@ -1068,7 +1069,10 @@ int Grid::RunGemmF(int N, bool real, Batch& b, const float* B, float* C, bool ac
     LaunchPackB(items, b.count, b.maxBTiles, b.tileN, B, b.packed, stream);
     SL3D_CHECK_LAUNCH();
   }
-  prof::Scope scope(prof::kLegendre32, stream, b.flops);
+  // algorithmic traffic: the table panel once, B's packed tiles once per
+  // row tile, C once
+  prof::Scope scope(prof::kLegendre32, stream, b.flops,
+                    4.0 * b.panelFloats + 4.0 * b.packedFloats * b.maxMTiles + 4.0 * b.outputs);
   return RunGemmTc(items, b.dTcTiles, static_cast<int>(b.tcTiles.size()), b.tileN, found->second, b.packed, C,
                    accumulate, dTcError_, stream);
 }

@@ -145,7 +145,8 @@ class Grid {
     GemmItem* items = nullptr;
     int count = 0, maxM = 0, maxN = 0;
     bool analysis = false;
-    double flops = 0.0;  // 2 M N K summed over the items
+    double flops = 0.0;    // 2 M N K summed over the items
+    double outputs = 0.0;  // M N summed over the items
     // the tensor-core form (FP32): its items, tile width and extents, the
     // packed B (made on first use) and the key of its table panel
     std::vector<TcItemHost> tcHost;
