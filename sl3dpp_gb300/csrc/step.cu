@@ -122,7 +122,12 @@ class Viscoelastic3DGpu {
 
   // mixer
   int mixerMemory = 0;
-  Dev<double> xPrev, fPrev, gram, gammaOut, mixPartial;
+  Dev<double> xPrev, fPrev, gammaOut, mixPartial, mixSums;
+  // the Anderson least squares runs on the host: each mixer's Gram matrix,
+  // and pinned room for an update's sums (16) and gamma (9)
+  std::vector<double> gram64, gram32;
+  double* hostMix = nullptr;
+  int MixerHostSolve(std::vector<double>& gram, int m, int slot, int memory);
   std::vector<Dev<double>> dG, dF;
   Dev<double*> dGPtr, dFPtr;
   static constexpr int kMixBlocks = 1024;
@@ -185,6 +190,7 @@ class Viscoelastic3DGpu {
 
   ~Viscoelastic3DGpu() {
     if (hostResult) cudaFreeHost(hostResult);
+    if (hostMix) cudaFreeHost(hostMix);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -313,6 +319,8 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   }
   SL3D_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   SL3D_CUDA(cudaMallocHost(&hostResult, 8 * sizeof(double)));
+  SL3D_CUDA(cudaMallocHost(&hostMix, 32 * sizeof(double)));
+  SL3D_CUDA(mixSums.Alloc(2 * kMixMaxMemory));
   SL3D_TRY(Grid::Create(opt.lmax, 2, opt.oversampling, grid));
   grid->emulateFp64 = opt.fp64_emulation == 1;
   // The step: the long-term material, the Gauss memory points of every
@@ -813,8 +821,7 @@ int Viscoelastic3DGpu::MixerReset() {
     SL3D_CUDA(fPrev.Alloc(n));
     mixerMemory = memory;
   }
-  if (gram.n < static_cast<size_t>(memory) * memory) SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
-  SL3D_CUDA(cudaMemsetAsync(gram.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
+  gram64.assign(static_cast<size_t>(memory) * memory, 0.0);
   return SL3DGPU_OK;
 }
 
@@ -830,7 +837,6 @@ int Viscoelastic3DGpu::MixerUpdate(int& count, int& slot, bool& first) {
   a.dF = dFPtr.p;
   a.partial = mixPartial.p;
   a.blocks = static_cast<int>(std::min<long long>(kMixBlocks, a.n));
-  a.gram = gram.p;
   a.gamma = gammaOut.p;
   if (first) {
     LaunchMixerFirst(a, stream);
@@ -840,7 +846,10 @@ int Viscoelastic3DGpu::MixerUpdate(int& count, int& slot, bool& first) {
   }
   a.slot = slot;
   a.m = std::min(count + 1, a.memory);
-  LaunchMixerUpdate(a, stream);
+  LaunchMixerSweep(a, mixSums.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(MixerHostSolve(gram64, a.m, a.slot, a.memory));
+  LaunchMixerMix(a, stream);
   SL3D_CHECK_LAUNCH();
   count = a.m;
   slot = (slot + 1) % a.memory;
@@ -1282,8 +1291,21 @@ int Viscoelastic3DGpu::Mixer32Reset() {
     mixer32Memory = memory;
     mixer32Size = n;
   }
-  if (gram.n < static_cast<size_t>(memory) * memory) SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
-  SL3D_CUDA(cudaMemsetAsync(gram.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
+  gram32.assign(static_cast<size_t>(memory) * memory, 0.0);
+  return SL3DGPU_OK;
+}
+
+// An update's least squares on the host: the sweep's sums back (the stream
+// synchronised), the Gram column and gamma by MixerSolve, gamma to the device
+// for the mix (the pinned copy is not touched again before the next update,
+// which follows a synchronisation).
+int Viscoelastic3DGpu::MixerHostSolve(std::vector<double>& gram, int m, int slot, int memory) {
+  SL3D_CUDA(cudaMemcpyAsync(hostMix, mixSums.p, 2 * kMixMaxMemory * sizeof(double), cudaMemcpyDeviceToHost,
+                            stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  double* gamma = hostMix + 2 * kMixMaxMemory;
+  MixerSolve(gram.data(), m, slot, memory, hostMix, gamma);
+  SL3D_CUDA(cudaMemcpyAsync(gammaOut.p, gamma, (m + 1) * sizeof(double), cudaMemcpyHostToDevice, stream));
   return SL3DGPU_OK;
 }
 
@@ -1299,7 +1321,6 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
   a.dF = dF32Ptr.p;
   a.partial = mixPartial.p;
   a.blocks = static_cast<int>(std::min<long long>(kMixBlocks32, a.n));
-  a.gram = gram.p;
   a.gamma = gammaOut.p;
   if (first) {
     LaunchMixerFirst(a, stream);
@@ -1309,7 +1330,10 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
   }
   a.slot = slot;
   a.m = std::min(count + 1, a.memory);
-  LaunchMixerUpdate(a, stream);
+  LaunchMixerSweep(a, mixSums.p, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(MixerHostSolve(gram32, a.m, a.slot, a.memory));
+  LaunchMixerMix(a, stream);
   SL3D_CHECK_LAUNCH();
   count = a.m;
   slot = (slot + 1) % a.memory;

@@ -653,39 +653,16 @@ __global__ void MixerSweepKernel(MixerArgsT<T> a) {
 // The partials in a fixed order (one warp per sum, lanes over the blocks,
 // then a fixed shuffle tree), the Gram matrix's new row and column, and the
 // least-squares coefficients (FP64, one thread; gamma[m] = 1 when they hold).
-// The mixer's small solve for m = M columns (a compile-time order, so its
-// matrices stay in registers): the new Gram column and right-hand side from
-// the sweep's block partial sums, the Gram matrix's slot updated, gamma
-// solved (gamma[M] = 1 on success).
-template <int M>
-__global__ void MixerSolveKernel(int slot, int memory, int blocks, const double* partial, double* gram,
-                                 double* gamma) {
-  __shared__ double sums[2 * kMaxMemory];
+// The sweep's block partial sums reduced to the new Gram column (m values)
+// and the right-hand side (m values, from index kMaxMemory), a warp each.
+__global__ void MixerReduceKernel(int m, int blocks, const double* partial, double* sums) {
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  if (warp < 2 * M) {
-    const int i = warp < M ? warp : kMaxMemory + (warp - M);
-    double v = 0.0;
-    for (int b = lane; b < blocks; b += 32) v += partial[static_cast<long long>(b) * 2 * kMaxMemory + i];
-    for (int off = 16; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (lane == 0) sums[warp] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  double gam[M], A[M * M], x[M];
-#pragma unroll
-  for (int i = 0; i < M; ++i) {
-    gam[i] = sums[M + i];
-    gram[slot * memory + i] = sums[i];
-    gram[i * memory + slot] = sums[i];
-  }
-#pragma unroll
-  for (int i = 0; i < M; ++i)
-#pragma unroll
-    for (int j = 0; j < M; ++j) A[i * M + j] = gram[i * memory + j];
-  const bool ok = SymmetricLstsqOf<M>(A, gam, x);
-#pragma unroll
-  for (int i = 0; i < M; ++i) gamma[i] = x[i];
-  gamma[M] = ok ? 1.0 : 0.0;
+  if (warp >= 2 * m) return;
+  const int i = warp < m ? warp : kMaxMemory + (warp - m);
+  double v = 0.0;
+  for (int b = lane; b < blocks; b += 32) v += partial[static_cast<long long>(b) * 2 * kMaxMemory + i];
+  for (int off = 16; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off);
+  if (lane == 0) sums[i] = v;
 }
 
 template <class T>
@@ -1025,26 +1002,17 @@ void MixerFirst(const MixerArgsT<T>& a, cudaStream_t stream) {
 }
 
 template <class T>
-void MixerUpdate(const MixerArgsT<T>& a, cudaStream_t stream) {
+void MixerSweep(const MixerArgsT<T>& a, double* sums, cudaStream_t stream) {
   {
     prof::Scope scope(prof::kMixer, stream, 0.0, a.n * sizeof(T) * (6 + a.m));
     MixerSweepKernel<T><<<a.blocks, kMixThreads, 0, stream>>>(a);
   }
-  {
-    prof::Scope scope(prof::kOther, stream);
-    auto solve = MixerSolveKernel<1>;
-    switch (a.m) {
-      case 2: solve = MixerSolveKernel<2>; break;
-      case 3: solve = MixerSolveKernel<3>; break;
-      case 4: solve = MixerSolveKernel<4>; break;
-      case 5: solve = MixerSolveKernel<5>; break;
-      case 6: solve = MixerSolveKernel<6>; break;
-      case 7: solve = MixerSolveKernel<7>; break;
-      case 8: solve = MixerSolveKernel<8>; break;
-      default: break;
-    }
-    solve<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.slot, a.memory, a.blocks, a.partial, a.gram, a.gamma);
-  }
+  prof::Scope scope(prof::kOther, stream);
+  MixerReduceKernel<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.m, a.blocks, a.partial, sums);
+}
+
+template <class T>
+void MixerMix(const MixerArgsT<T>& a, cudaStream_t stream) {
   prof::Scope scope(prof::kMixer, stream, 0.0, a.n * sizeof(T) * (2 + a.m));
   MixerMixKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a);
 }
@@ -1062,9 +1030,11 @@ void LaunchRelativeChange(const float* next, const float* now, long long n, doub
 }
 
 void LaunchMixerFirst(const MixerArgsT<double>& a, cudaStream_t stream) { MixerFirst(a, stream); }
-void LaunchMixerUpdate(const MixerArgsT<double>& a, cudaStream_t stream) { MixerUpdate(a, stream); }
+void LaunchMixerSweep(const MixerArgsT<double>& a, double* sums, cudaStream_t stream) { MixerSweep(a, sums, stream); }
+void LaunchMixerMix(const MixerArgsT<double>& a, cudaStream_t stream) { MixerMix(a, stream); }
 void LaunchMixerFirst(const MixerArgsT<float>& a, cudaStream_t stream) { MixerFirst(a, stream); }
-void LaunchMixerUpdate(const MixerArgsT<float>& a, cudaStream_t stream) { MixerUpdate(a, stream); }
+void LaunchMixerSweep(const MixerArgsT<float>& a, double* sums, cudaStream_t stream) { MixerSweep(a, sums, stream); }
+void LaunchMixerMix(const MixerArgsT<float>& a, cudaStream_t stream) { MixerMix(a, stream); }
 
 void LaunchBandApply(const sl3dgpu_band_system* devSystems, int count, int maxRows, const double* bands,
                      const double* x, double* y, double keep, cudaStream_t stream) {
@@ -1154,5 +1124,21 @@ std::vector<double> NodeCoefficients(int P, int ngll, const std::vector<int>& no
     }
   }
   return out;
+}
+}  // namespace sl3dgpu
+
+namespace sl3dgpu {
+bool MixerSolve(double* gram, int m, int slot, int memory, const double* sums, double* gamma) {
+  for (int i = 0; i < m; ++i) {
+    gram[slot * memory + i] = sums[i];
+    gram[i * memory + slot] = sums[i];
+  }
+  double A[kMixMaxMemory * kMixMaxMemory], x[kMixMaxMemory];
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) A[i * m + j] = gram[i * memory + j];
+  const bool ok = SymmetricLstsq(m, A, sums + kMixMaxMemory, x);
+  for (int i = 0; i < m; ++i) gamma[i] = x[i];
+  gamma[m] = ok ? 1.0 : 0.0;
+  return ok;
 }
 }  // namespace sl3dgpu

@@ -210,9 +210,21 @@ struct MixerArgsT {
   double* gamma;    // m (+1 status)
 };
 using MixerArgs = MixerArgsT<double>;
+constexpr int kMixMaxMemory = 8;  // the most history columns; sums hold 2 x this
 void LaunchMixerFirst(const MixerArgsT<double>& a, cudaStream_t stream);
-void LaunchMixerUpdate(const MixerArgsT<double>& a, cudaStream_t stream);
 void LaunchMixerFirst(const MixerArgsT<float>& a, cudaStream_t stream);
-void LaunchMixerUpdate(const MixerArgsT<float>& a, cudaStream_t stream);
+// An update's device part: the history sweep and its reduction to the new
+// Gram column (sums[0..m)) and right-hand side (sums[8..8+m)); then, after
+// the host's MixerSolve has put gamma (m values and a status) in a.gamma,
+// the mix.
+void LaunchMixerSweep(const MixerArgsT<double>& a, double* sums, cudaStream_t stream);
+void LaunchMixerMix(const MixerArgsT<double>& a, cudaStream_t stream);
+void LaunchMixerSweep(const MixerArgsT<float>& a, double* sums, cudaStream_t stream);
+void LaunchMixerMix(const MixerArgsT<float>& a, cudaStream_t stream);
+// The update's small least-squares solve on the host (FP64): the Gram
+// matrix's slot column from the sums, then gamma by SymmetricLstsq
+// (gamma[m] = 1 on success, 0 when it failed and the mix takes the plain
+// step). gram: memory x memory, kept by the caller.
+bool MixerSolve(double* gram, int m, int slot, int memory, const double* sums, double* gamma);
 
 }  // namespace sl3dgpu
