@@ -53,7 +53,8 @@ RAMP_STEPS = 10
 DT_YEARS = 500.0
 RTOL = 1e-10
 MAX_ITERATIONS = 60
-CORRECTION_RTOL = 1e-5
+CORRECTION_RTOL = 3e-6
+CORRECTION_MEMORY = 8
 METRIC = "3D steps/sec at lmax=256: mixed+warm-start vs plain FP64 GPU at rel err <=1e-8"
 # The FP64 fixed point's passes per step at this workload (both stages),
 # measured by the GPU arm (identical iterate sequences on both arms, pinned
@@ -76,6 +77,7 @@ def workload_config(precision="mixed"):
             "dt_years": DT_YEARS, "scheme": "sdirk2", "rtol": RTOL, "max_iterations": MAX_ITERATIONS,
             "anderson_memory": 5, "oversampling": 1.5, "precision": precision,
             "correction_rtol": CORRECTION_RTOL if precision == "mixed" else None,
+            "correction_memory": CORRECTION_MEMORY if precision == "mixed" else None,
             "warm_start": ("the previous step's strain, and the extrapolation 2 s_n - s_{n-1} of the last two "
                            "steps as the FP32 correction's start" if precision == "mixed" else
                            "the previous step's strain coefficients (the reference's plain warm start)"),
@@ -198,7 +200,7 @@ def build_operator(device, precision):
     op = Viscoelastic3D(standard_earth(ELEMENTS),
                         Options.defaults(LMAX, NGLL, rtol=RTOL, max_iterations=MAX_ITERATIONS,
                                          precision=1 if precision == "mixed" else 0,
-                                         correction_rtol=CORRECTION_RTOL,
+                                         correction_rtol=CORRECTION_RTOL, correction_memory=CORRECTION_MEMORY,
                                          warm_start=1 if precision == "mixed" else 0,
                                          fp64_emulation=1 if precision == "mixed" else 0))
     grid = SurfaceGrid(LMAX, 0, 1.5)
@@ -390,6 +392,7 @@ def ensemble_line(args):
 # -- main ------------------------------------------------------------------------------------------
 
 def main():
+    global CORRECTION_RTOL, CORRECTION_MEMORY
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
@@ -399,12 +402,15 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip the plain FP64 form's run")
     ap.add_argument("--lmax", type=int, default=LMAX, help="a smaller workload for development runs")
+    ap.add_argument("--correction-rtol", type=float, default=CORRECTION_RTOL)
+    ap.add_argument("--correction-memory", type=int, default=CORRECTION_MEMORY)
     ap.add_argument("--ensemble", type=int, default=0, metavar="MEMBERS",
                     help="instead: the ensemble workload (MEMBERS independent evolutions, lmax 32-128, 20 steps "
                          "each) run concurrently and one by one")
     args = ap.parse_args()
     if args.lmax != LMAX:
         _rescale(args.lmax)
+    CORRECTION_RTOL, CORRECTION_MEMORY = args.correction_rtol, args.correction_memory
     if args.warmup < 3:
         raise SystemExit("at least three warm-up steps")
     rank = int(os.environ.get("RANK", "0"))

@@ -577,7 +577,7 @@ RingFn<T2> RingKernelFor(int n, int* buffers) {
   *buffers = 1;
   switch (n) {
     case 800: return RingKernel<T2, 25, 32>;
-    case 400: return RingKernel<T2, 16, 25>;
+    case 400: return RingKernel<T2, 25, 16>;  // R1 odd: stage A's stores are bank-conflict free
     case 50: return RingKernel<T2, 5, 10>;
     case 40: return RingKernel<T2, 5, 8>;
     case 25: return RingKernel<T2, 5, 5>;

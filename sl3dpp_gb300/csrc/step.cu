@@ -239,6 +239,8 @@ class Viscoelastic3DGpu {
   int WeightedPass32(const float2* strain, float2* out);  // compact lateral arrays
   int Pass32(const Flavour& f, const float2* e, float2* next);
   int Mixer32Reset();
+  // the FP32 correction's Anderson history (correction_memory, else anderson_memory)
+  int CorrectionMemory() const { return options.correction_memory > 0 ? options.correction_memory : options.anderson_memory; }
   int Mixer32Update(int& count, int& slot, bool& first);
   int Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info, const double2* warm);
   int SolveColumns(const Flavour& f, double2* sph, double2* tor);
@@ -291,6 +293,10 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   }
   if (opt.fp64_emulation != 0 && opt.fp64_emulation != 1) {
     SetError("v3d: fp64_emulation 0 (the FP64 units) or 1 (the tensor cores)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (opt.correction_memory < 0 || opt.correction_memory > 8) {
+    SetError("v3d: correction_memory in [0, 8] (0: anderson_memory)");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if (opt.precision == 1 && !(opt.correction_rtol > 0.0 && opt.correction_rtol < 1.0)) {
@@ -1271,7 +1277,7 @@ int Viscoelastic3DGpu::Pass32(const Flavour& f, const float2* e, float2* next) {
 }
 
 int Viscoelastic3DGpu::Mixer32Reset() {
-  const int memory = options.anderson_memory;
+  const int memory = CorrectionMemory();
   if (memory <= 0) return SL3DGPU_OK;
   const size_t n = 2 * compactComplex;
   if (mixer32Memory != memory || mixer32Size != n) {
@@ -1312,7 +1318,7 @@ int Viscoelastic3DGpu::MixerHostSolve(std::vector<double>& gram, int m, int slot
 int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
   MixerArgsT<float> a{};
   a.n = 2 * compactComplex;
-  a.memory = options.anderson_memory;
+  a.memory = CorrectionMemory();
   a.x = reinterpret_cast<float*>(eL.p);
   a.gx = reinterpret_cast<const float*>(eNextL.p);
   a.xPrev = xPrev32.p;
@@ -1362,7 +1368,7 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
     SL3D_CUDA(cudaMemcpyAsync(eL.p, rL.p, compactComplex * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
   }
   const bool adaptive = options.anderson_rate > 0.0;
-  bool mixing = options.anderson_memory > 0 && !adaptive;
+  bool mixing = CorrectionMemory() > 0 && !adaptive;
   bool firstMix = true;
   int count = 0, slot = 0;
   if (mixing) SL3D_TRY(Mixer32Reset());
@@ -1399,7 +1405,7 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
       fresh = true;
       break;
     }
-    if (adaptive && !mixing && options.anderson_memory > 0 && iteration > first &&
+    if (adaptive && !mixing && CorrectionMemory() > 0 && iteration > first &&
         change > options.anderson_rate * previous) {
       mixing = true;
       firstMix = true;

@@ -18,17 +18,22 @@
 // acc_5 2^7 + acc_6, and C(i, n) = 2^{e_i + f_n} (2^{-28} H + 2^{-56} L) is
 // rounded once to FP64 from that exact integer, by integer arithmetic.
 //
-// Kernel. One CTA of four warps per (64-column tile, 128-row tile, item),
+// Kernel. One CTA of eight warps per (64-column tile, 128-row tile, item),
 // the column tiles of a row tile adjacent in the launch so that its A panel
 // is read from HBM once. One elected thread runs the K loop as the FP32
 // contraction does (tc_gemm.cu): it arms a stage's "full" mbarrier, issues
 // two TMA bulk copies (A's seven slices, 28 KB; B's, 14 KB), four stages in
-// flight, and when they have landed issues the step's 28 tcgen05.mma
-// kind::f16 into the level accumulators (tensor-memory columns 64 d ..
-// 64 d + 63 of 512) and commits them to the stage's "empty" mbarrier. Every
-// wait has an iteration limit. The epilogue reads the seven levels with
-// tcgen05.ld, one lane quarter per warp, joins them in FP64 and stores (or
-// adds) the rows in range.
+// flight, and when they have landed issues the step's tcgen05.mma kind::f16
+// into the level accumulators (tensor-memory columns 64 d .. 64 d + 63 of
+// 512) and commits them to the stage's "empty" mbarrier. B's seven slices
+// are stored as one 448-row operand, slice q in rows 64 q .. 64 q + 63, so
+// that one MMA of N = 64 c multiplies A's slice p by c consecutive slices
+// q0 .. q0 + c - 1 into the c consecutive levels p + q0 ..: the 28 products
+// of a step take 10 MMAs of N up to 256 rather than 28 of N = 64 (the same
+// tensor work, in fewer instructions for the one issuing thread). Every wait
+// has an iteration limit. The epilogue reads the seven levels with
+// tcgen05.ld, two warps per lane quarter (a column half each), joins them in
+// FP64 and stores (or adds) the rows in range.
 #include <cstdint>
 
 #include "profile.cuh"
@@ -40,9 +45,11 @@ namespace {
 constexpr int kSlices = kTc64Slices;
 constexpr int kTileN = kTc64TileN;
 constexpr int kStages = 4;
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;  // eight warps: two per tensor-memory lane quarter in the epilogue
 constexpr int kATile = kTcTileM * kTcTileK;  // BF16 values of one slice of an A tile: 2048 (4 KB)
 constexpr int kBTile = kTileN * kTcTileK;    // of a B tile: 1024 (2 KB)
+constexpr int kBRows = kSlices * kTileN;     // B's slices as one operand of 448 rows
+constexpr int kBSlice = kTileN * 8;          // BF16 offset of the next slice's rows (8 row groups of 64)
 constexpr uint32_t kTmemColumns = 512;       // 7 levels x 64 columns, rounded up to a power of two
 
 static_assert(kSlices * kTileN <= static_cast<int>(kTmemColumns), "the levels fit in tensor memory");
@@ -224,7 +231,7 @@ __global__ void __launch_bounds__(kPackThreads) PackB64Kernel(const Tc64Item* tc
       const double v = (n < it.N && k < it.K) ? col[static_cast<long long>(k) * it.ldb] : 0.0;
       Split(v, e, s[q]);
     }
-    StoreSlices(base + static_cast<long long>(ks) * kSlices * kBTile, kBTile, Tile16Index(nn, 8 * kg, kTileN), s);
+    StoreSlices(base + static_cast<long long>(ks) * kSlices * kBTile, kBSlice, Tile16Index(nn, 8 * kg, kBRows), s);
   }
 }
 
@@ -246,7 +253,7 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
   uint64_t* empty = full + kStages;
   uint32_t* tmemSlot = reinterpret_cast<uint32_t*>(empty + kStages);
   __shared__ int okShared;
-  __shared__ double rowsOut[4][32][17];  // each warp's 32 x 16 block, padded
+  __shared__ double rowsOut[kThreads / 32][32][17];  // each warp's 32 x 16 block, padded
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
 
   if (warp == 0) {
@@ -270,7 +277,6 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
   if (tid == 0) {
     const uint16_t* aSrc = panels + it.aPanel + static_cast<long long>(mt) * it.kSteps * kSlices * kATile;
     const uint16_t* bSrc = packed + it.bPack + static_cast<long long>(nt) * it.kSteps * kSlices * kBTile;
-    constexpr uint32_t idesc = InstrDescriptorBf16(kTileN, kTcTileM);
     uint32_t phaseFull[kStages] = {0, 0, 0, 0}, phaseEmpty[kStages] = {0, 0, 0, 0};
     bool ok = true;
     auto issue = [&](int ks) {
@@ -305,19 +311,22 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t aBase = SmemAddr(sA + buf * kSlices * kATile);
       const uint32_t bBase = SmemAddr(sB + buf * kSlices * kBTile);
-      constexpr uint32_t aLbo = kTcTileM * 16, bLbo = kTileN * 16, sbo = 128;
+      constexpr uint32_t aLbo = kTcTileM * 16, bLbo = kBRows * 16, sbo = 128;
+      // A's slice p against B's slices q0 .. q0 + c - 1 (c <= 4, N = 64 c),
+      // levels p + q0 .. p + q0 + c - 1; p = 0 writes every level first.
 #pragma unroll
-      for (int d = 0; d < kSlices; ++d) {
+      for (int p = 0; p < kSlices; ++p) {
+        const uint64_t dA = Descriptor(aBase + p * kATile * 2, aLbo, sbo);
+        const uint32_t enable = (ks > 0 || p > 0) ? 1u : 0u;
 #pragma unroll
-        for (int p = 0; p <= d; ++p) {
-          const uint64_t dA = Descriptor(aBase + p * kATile * 2, aLbo, sbo);
-          const uint64_t dB = Descriptor(bBase + (d - p) * kBTile * 2, bLbo, sbo);
-          const uint32_t enable = (ks > 0 || p > 0) ? 1u : 0u;
+        for (int q0 = 0; q0 < kSlices - p; q0 += 4) {
+          const int c = min(4, kSlices - p - q0);
+          const uint64_t dB = Descriptor(bBase + q0 * kBSlice * 2, bLbo, sbo);
           asm volatile(
               "{\n\t.reg .pred r;\n\t"
               "setp.ne.b32 r, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, r;\n\t}" ::"r"(tmem + d * kTileN),
-              "l"(dA), "l"(dB), "r"(idesc), "r"(enable)
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, r;\n\t}" ::"r"(tmem + (p + q0) * kTileN),
+              "l"(dA), "l"(dB), "r"(InstrDescriptorBf16(c * kTileN, kTcTileM)), "r"(enable)
               : "memory");
         }
       }
@@ -336,15 +345,18 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (okShared) {
-    // Epilogue: this warp's lane quarter (32 rows), 16 columns at a time, the
-    // seven levels joined as integers and rounded once to FP64.
-    const int i = i0 + 32 * warp + lane;
+    // Epilogue: this warp's lane quarter (32 rows) and column half, 16
+    // columns at a time, the seven levels joined as integers and rounded
+    // once to FP64.
+    const int quarter = warp % 4, half = warp / 4;
+    const int i = i0 + 32 * quarter + lane;
     const int e = i < it.M ? rowExp[it.rowExp + i] : 0;
-    for (int c0 = 0; c0 < kTileN; c0 += 16) {
+    for (int c0 = half * (kTileN / 2); c0 < (half + 1) * (kTileN / 2); c0 += 16) {
       uint32_t r[kSlices][16];
 #pragma unroll
       for (int d = 0; d < kSlices; ++d) {
-        const uint32_t addr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(d * kTileN + c0);
+        const uint32_t addr =
+            tmem + (static_cast<uint32_t>(32 * quarter) << 16) + static_cast<uint32_t>(d * kTileN + c0);
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
             "%14, %15}, [%16];"
@@ -374,7 +386,7 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
       __syncwarp();
       const int n = c0 + (lane & 15);
       for (int rr = lane >> 4; rr < 32; rr += 2) {
-        const int row = i0 + 32 * warp + rr;
+        const int row = i0 + 32 * quarter + rr;
         if (row < it.M && n < nCols) {
           double* dst = C + it.c + static_cast<long long>(row) * it.ldc + n0 + n;
           const double v = rowsOut[warp][rr][lane & 15];

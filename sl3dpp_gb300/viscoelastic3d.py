@@ -40,14 +40,14 @@ class Options(ctypes.Structure):
                 ("correction_rtol", ctypes.c_double), ("solver", ctypes.c_int),
                 ("solve_rtol", ctypes.c_double), ("solve_max_iterations", ctypes.c_int),
                 ("warm_start", ctypes.c_int),
-                ("fp64_emulation", ctypes.c_int)]
+                ("fp64_emulation", ctypes.c_int), ("correction_memory", ctypes.c_int)]
 
     @classmethod
     def defaults(cls, lmax: int, ngll: int = 5, **kw) -> "Options":
         o = cls(lmax=lmax, ngll=ngll, eps=1e-8, oversampling=1.5, max_iterations=40, rtol=1e-11,
                 damping=1.0, anderson_memory=5, anderson_rate=0.5, precision=0, correction_rtol=1e-5,
                 solver=0, solve_rtol=1e-11, solve_max_iterations=200, warm_start=0,
-                fp64_emulation=0)
+                fp64_emulation=0, correction_memory=0)
         for k, v in kw.items():
             setattr(o, k, v)
         return o
