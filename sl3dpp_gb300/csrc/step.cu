@@ -155,8 +155,8 @@ class Viscoelastic3DGpu {
   Dev<float> spectra32A, spectra32B, weight32;
   int mixer32Memory = 0;
   Dev<float> xPrev32, fPrev32;
-  std::vector<Dev<float>> dG32, dF32;
-  Dev<float*> dG32Ptr, dF32Ptr;
+  std::vector<Dev<__nv_bfloat16>> dG32, dF32;  // the correction's history, BF16
+  Dev<__nv_bfloat16*> dG32Ptr, dF32Ptr;
   std::vector<double> correctionHistory;  // the last step's FP32 pass changes
 
   // conjugate gradients (solver 1): forces, iterate, residual, preconditioned
@@ -1283,7 +1283,7 @@ int Viscoelastic3DGpu::Mixer32Reset() {
   if (mixer32Memory != memory || mixer32Size != n) {
     dG32.resize(memory);
     dF32.resize(memory);
-    std::vector<float*> gp(memory), fp(memory);
+    std::vector<__nv_bfloat16*> gp(memory), fp(memory);
     for (int i = 0; i < memory; ++i) {
       SL3D_CUDA(dG32[i].Alloc(n));
       SL3D_CUDA(dF32[i].Alloc(n));

@@ -7,6 +7,7 @@
 // the per-node values staged in shared memory so that every dof is written by
 // exactly one thread (no atomics, a fixed summation order).
 #include <cmath>
+#include <type_traits>
 
 #include "host/lstsq.hpp"
 #include "profile.cuh"
@@ -601,34 +602,20 @@ struct MixAcc<float> {
 // differences, the stored iterate and residual, and the block's partial Gram
 // column and right-hand side, summed in a fixed order (thread, warp
 // shuffle tree, warps in turn).
-template <class T>
-__global__ void MixerSweepKernel(MixerArgsT<T> a) {
-  using A = typename MixAcc<T>::type;
+// A history value stored and read back (identity for the FP64 form).
+__device__ inline double ToHistory(double v, double*) { return v; }
+__device__ inline __nv_bfloat16 ToHistory(float v, __nv_bfloat16*) { return __float2bfloat16_rn(v); }
+__device__ inline double FromHistory(double v) { return v; }
+__device__ inline float FromHistory(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// A block's partial Gram column and right-hand side: warp shuffle trees,
+// then the warps in turn, written to partial[block][0..m) and [8..8+m).
+template <class A>
+__device__ inline void MixerBlockPartials(const A (&col)[kMaxMemory], const A (&gam)[kMaxMemory], int m,
+                                          double* partial) {
   __shared__ double red[kMixThreads / 32][2 * kMaxMemory];
-  const long long begin = a.n * blockIdx.x / a.blocks, end = a.n * (blockIdx.x + 1) / a.blocks;
-  A col[kMaxMemory], gam[kMaxMemory];
-  for (int i = 0; i < kMaxMemory; ++i) col[i] = gam[i] = A(0);
-  T* dFs = a.dF[a.slot];
-  T* dGs = a.dG[a.slot];
-  const T* dF[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) dF[i] = a.dF[i];
-  for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
-    const T xs = a.x[at], gs = a.gx[at];
-    const T f = gs - xs;
-    const T dx = xs - a.xPrev[at];
-    const T df = f - a.fPrev[at];
-    dFs[at] = df;
-    dGs[at] = dx + df;
-    a.xPrev[at] = xs;
-    a.fPrev[at] = f;
-    for (int i = 0; i < a.m; ++i) {
-      const A di = i == a.slot ? static_cast<A>(df) : static_cast<A>(dF[i][at]);
-      col[i] += di * static_cast<A>(df);
-      gam[i] += di * static_cast<A>(f);
-    }
-  }
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  for (int i = 0; i < a.m; ++i) {
+  for (int i = 0; i < m; ++i) {
     A c = col[i], g = gam[i];
     for (int off = 16; off > 0; off /= 2) {
       c += __shfl_down_sync(0xffffffffu, c, off);
@@ -642,12 +629,77 @@ __global__ void MixerSweepKernel(MixerArgsT<T> a) {
   __syncthreads();
   if (threadIdx.x < 2 * kMaxMemory) {
     const int i = threadIdx.x;
-    if (i % kMaxMemory < a.m) {
+    if (i % kMaxMemory < m) {
       double v = 0.0;
       for (int w = 0; w < kMixThreads / 32; ++w) v += red[w][i];
-      a.partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + i] = v;
+      partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + i] = v;
     }
   }
+}
+
+template <class T>
+__global__ void MixerSweepKernel(MixerArgsT<T> a) {
+  using A = typename MixAcc<T>::type;
+  using H = typename MixerArgsT<T>::H;
+  const long long begin = a.n * blockIdx.x / a.blocks, end = a.n * (blockIdx.x + 1) / a.blocks;
+  A col[kMaxMemory], gam[kMaxMemory];
+  for (int i = 0; i < kMaxMemory; ++i) col[i] = gam[i] = A(0);
+  H* dFs = a.dF[a.slot];
+  H* dGs = a.dG[a.slot];
+  const H* dF[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) dF[i] = a.dF[i];
+  for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
+    const T xs = a.x[at], gs = a.gx[at];
+    const T f = gs - xs;
+    const T dx = xs - a.xPrev[at];
+    const H dfStored = ToHistory(f - a.fPrev[at], dFs);
+    dFs[at] = dfStored;
+    dGs[at] = ToHistory(dx + (f - a.fPrev[at]), dGs);
+    a.xPrev[at] = xs;
+    a.fPrev[at] = f;
+    // the new column as stored, so that the Gram matrix is the stored vectors'
+    const A df = static_cast<A>(FromHistory(dfStored));
+    for (int i = 0; i < a.m; ++i) {
+      const A di = i == a.slot ? df : static_cast<A>(FromHistory(dF[i][at]));
+      col[i] += di * df;
+      gam[i] += di * static_cast<A>(f);
+    }
+  }
+  MixerBlockPartials(col, gam, a.m, a.partial);
+}
+
+// Two values a thread (FP32 iterate, BF16 history): the same sweep as
+// MixerSweepKernel<float> with 8-byte and 4-byte accesses.
+__global__ void MixerSweepPairsKernel(MixerArgsT<float> a) {
+  const long long pairs = a.n / 2;
+  const long long begin = pairs * blockIdx.x / a.blocks, end = pairs * (blockIdx.x + 1) / a.blocks;
+  float col[kMaxMemory], gam[kMaxMemory];
+  for (int i = 0; i < kMaxMemory; ++i) col[i] = gam[i] = 0.0f;
+  auto* x = reinterpret_cast<const float2*>(a.x);
+  auto* gx = reinterpret_cast<const float2*>(a.gx);
+  auto* xPrev = reinterpret_cast<float2*>(a.xPrev);
+  auto* fPrev = reinterpret_cast<float2*>(a.fPrev);
+  auto* dFs = reinterpret_cast<__nv_bfloat162*>(a.dF[a.slot]);
+  auto* dGs = reinterpret_cast<__nv_bfloat162*>(a.dG[a.slot]);
+  const __nv_bfloat162* dF[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) dF[i] = reinterpret_cast<const __nv_bfloat162*>(a.dF[i]);
+  for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
+    const float2 xs = x[at], gs = gx[at], xp = xPrev[at], fp = fPrev[at];
+    const float2 f = make_float2(gs.x - xs.x, gs.y - xs.y);
+    const float2 dfRaw = make_float2(f.x - fp.x, f.y - fp.y);
+    const __nv_bfloat162 dfStored = __floats2bfloat162_rn(dfRaw.x, dfRaw.y);
+    dFs[at] = dfStored;
+    dGs[at] = __floats2bfloat162_rn(xs.x - xp.x + dfRaw.x, xs.y - xp.y + dfRaw.y);
+    xPrev[at] = xs;
+    fPrev[at] = f;
+    const float2 df = __bfloat1622float2(dfStored);
+    for (int i = 0; i < a.m; ++i) {
+      const float2 di = i == a.slot ? df : __bfloat1622float2(dF[i][at]);
+      col[i] += di.x * df.x + di.y * df.y;
+      gam[i] += di.x * f.x + di.y * f.y;
+    }
+  }
+  MixerBlockPartials(col, gam, a.m, a.partial);
 }
 
 // The partials in a fixed order (one warp per sum, lanes over the blocks,
@@ -671,7 +723,7 @@ __global__ void MixerMixKernel(MixerArgsT<T> a) {
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   const bool ok = a.gamma[a.m] != 0.0;
   A g[kMaxMemory];
-  const T* dG[kMaxMemory];
+  const typename MixerArgsT<T>::H* dG[kMaxMemory];
   for (int i = 0; i < a.m; ++i) {
     g[i] = static_cast<A>(a.gamma[i]);
     dG[i] = a.dG[i];
@@ -679,8 +731,32 @@ __global__ void MixerMixKernel(MixerArgsT<T> a) {
   for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < a.n; at += stride) {
     A value = a.gx[at];
     if (ok)
-      for (int i = 0; i < a.m; ++i) value -= g[i] * static_cast<A>(dG[i][at]);
+      for (int i = 0; i < a.m; ++i) value -= g[i] * static_cast<A>(FromHistory(dG[i][at]));
     a.x[at] = static_cast<T>(value);
+  }
+}
+
+__global__ void MixerMixPairsKernel(MixerArgsT<float> a) {
+  const long long pairs = a.n / 2;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const bool ok = a.gamma[a.m] != 0.0;
+  float g[kMaxMemory];
+  const __nv_bfloat162* dG[kMaxMemory];
+  for (int i = 0; i < a.m; ++i) {
+    g[i] = static_cast<float>(a.gamma[i]);
+    dG[i] = reinterpret_cast<const __nv_bfloat162*>(a.dG[i]);
+  }
+  auto* x = reinterpret_cast<float2*>(a.x);
+  auto* gx = reinterpret_cast<const float2*>(a.gx);
+  for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < pairs; at += stride) {
+    float2 v = gx[at];
+    if (ok)
+      for (int i = 0; i < a.m; ++i) {
+        const float2 d = __bfloat1622float2(dG[i][at]);
+        v.x -= g[i] * d.x;
+        v.y -= g[i] * d.y;
+      }
+    x[at] = v;
   }
 }
 
@@ -1004,8 +1080,12 @@ void MixerFirst(const MixerArgsT<T>& a, cudaStream_t stream) {
 template <class T>
 void MixerSweep(const MixerArgsT<T>& a, double* sums, cudaStream_t stream) {
   {
-    prof::Scope scope(prof::kMixer, stream, 0.0, a.n * sizeof(T) * (6 + a.m));
-    MixerSweepKernel<T><<<a.blocks, kMixThreads, 0, stream>>>(a);
+    using H = typename MixerArgsT<T>::H;
+    prof::Scope scope(prof::kMixer, stream, 0.0, a.n * (6.0 * sizeof(T) + (a.m + 1.0) * sizeof(H)));
+    if constexpr (std::is_same_v<T, float>)
+      MixerSweepPairsKernel<<<a.blocks, kMixThreads, 0, stream>>>(a);
+    else
+      MixerSweepKernel<T><<<a.blocks, kMixThreads, 0, stream>>>(a);
   }
   prof::Scope scope(prof::kOther, stream);
   MixerReduceKernel<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.m, a.blocks, a.partial, sums);
@@ -1013,8 +1093,12 @@ void MixerSweep(const MixerArgsT<T>& a, double* sums, cudaStream_t stream) {
 
 template <class T>
 void MixerMix(const MixerArgsT<T>& a, cudaStream_t stream) {
-  prof::Scope scope(prof::kMixer, stream, 0.0, a.n * sizeof(T) * (2 + a.m));
-  MixerMixKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a);
+  prof::Scope scope(prof::kMixer, stream, 0.0,
+                    a.n * (2.0 * sizeof(T) + a.m * sizeof(typename MixerArgsT<T>::H)));
+  if constexpr (std::is_same_v<T, float>)
+    MixerMixPairsKernel<<<StreamBlocks(a.n / 2), 256, 0, stream>>>(a);
+  else
+    MixerMixKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a);
 }
 }  // namespace
 

@@ -7,6 +7,8 @@
 
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace sl3dgpu {
@@ -193,17 +195,31 @@ void LaunchXpby(long long n, const double* x, double beta, double* y, cudaStream
 void LaunchSub(long long n, const double* a, const double* b, double* out, cudaStream_t stream);
 
 // The Anderson mixer's sweeps (AndersonMixer.hpp:65-219), on vectors of
-// reals T with the Gram sums in FP64.
+// reals T with the Gram sums in FP64. The history columns (the differences
+// dF, dG) are stored as MixHistory<T>: FP64 for the FP64 form; BF16 for the
+// FP32 correction, whose least squares then runs on the rounded columns
+// (the Gram matrix is that of the stored vectors, the mix uses the same
+// ones) -- the pass's own residual stays FP32 and decides convergence.
+template <class T>
+struct MixHistory {
+  using type = T;
+};
+template <>
+struct MixHistory<float> {
+  using type = __nv_bfloat16;
+};
+
 template <class T>
 struct MixerArgsT {
+  using H = typename MixHistory<T>::type;
   long long n;
   int m, slot, memory;
   T* x;
   const T* gx;
   T* xPrev;
   T* fPrev;
-  T** dG;  // device array of memory pointers
-  T** dF;
+  H** dG;  // device array of memory pointers
+  H** dF;
   double* partial;  // blocks x 2 x 8
   int blocks;
   double* gram;     // memory x memory
