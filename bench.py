@@ -54,7 +54,7 @@ DT_YEARS = 500.0
 RTOL = 1e-10
 MAX_ITERATIONS = 60
 CORRECTION_RTOL = 3e-6
-CORRECTION_MEMORY = 8
+CORRECTION_MEMORY = 10
 METRIC = "3D steps/sec at lmax=256: mixed+warm-start vs plain FP64 GPU at rel err <=1e-8"
 # The FP64 fixed point's passes per step at this workload (both stages),
 # measured by the GPU arm (identical iterate sequences on both arms, pinned

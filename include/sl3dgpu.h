@@ -169,7 +169,7 @@ typedef struct sl3dgpu_v3d_options {
                                starting from it (the FP64 form tries it as a first pass) */
   int fp64_emulation;       /* 0: the FP64 Legendre contractions on the FP64 units; 1: emulated on
                                the tensor cores (sl3dgpu_grid_set_fp64_emulation) */
-  int correction_memory;    /* mixed form: the FP32 correction's Anderson history, 0..8; 0 takes
+  int correction_memory;    /* mixed form: the FP32 correction's Anderson history, 0..16; 0 takes
                                anderson_memory */
 } sl3dgpu_v3d_options;
 

@@ -1,5 +1,5 @@
 // The Anderson mixer's small least-squares solve, gamma = argmin |A gamma - b|
-// for the symmetric positive semi-definite m x m Gram matrix A (m <= 8):
+// for the symmetric positive semi-definite m x m Gram matrix A (m <= 16):
 // cyclic Jacobi eigen-decomposition, directions whose |eigenvalue| is at or
 // below machine epsilon times the largest dropped -- the minimum-norm
 // solution LAPACK's dgelss gives with rcond < 0 (the reference's call,
@@ -104,6 +104,14 @@ SL3D_HD inline bool SymmetricLstsq(int m, const double* A /* m x m, row-major */
     case 6: return SymmetricLstsqOf<6>(A, b, x);
     case 7: return SymmetricLstsqOf<7>(A, b, x);
     case 8: return SymmetricLstsqOf<8>(A, b, x);
+    case 9: return SymmetricLstsqOf<9>(A, b, x);
+    case 10: return SymmetricLstsqOf<10>(A, b, x);
+    case 11: return SymmetricLstsqOf<11>(A, b, x);
+    case 12: return SymmetricLstsqOf<12>(A, b, x);
+    case 13: return SymmetricLstsqOf<13>(A, b, x);
+    case 14: return SymmetricLstsqOf<14>(A, b, x);
+    case 15: return SymmetricLstsqOf<15>(A, b, x);
+    case 16: return SymmetricLstsqOf<16>(A, b, x);
     default: return false;
   }
 }

@@ -295,8 +295,8 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     SetError("v3d: fp64_emulation 0 (the FP64 units) or 1 (the tensor cores)");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  if (opt.correction_memory < 0 || opt.correction_memory > 8) {
-    SetError("v3d: correction_memory in [0, 8] (0: anderson_memory)");
+  if (opt.correction_memory < 0 || opt.correction_memory > kMixMaxMemory) {
+    SetError("v3d: correction_memory in [0, 16] (0: anderson_memory)");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if (opt.precision == 1 && !(opt.correction_rtol > 0.0 && opt.correction_rtol < 1.0)) {
@@ -325,7 +325,7 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   }
   SL3D_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   SL3D_CUDA(cudaMallocHost(&hostResult, 8 * sizeof(double)));
-  SL3D_CUDA(cudaMallocHost(&hostMix, 32 * sizeof(double)));
+  SL3D_CUDA(cudaMallocHost(&hostMix, 4 * kMixMaxMemory * sizeof(double)));  // sums, then gamma
   SL3D_CUDA(mixSums.Alloc(2 * kMixMaxMemory));
   SL3D_TRY(Grid::Create(opt.lmax, 2, opt.oversampling, grid));
   grid->emulateFp64 = opt.fp64_emulation == 1;
@@ -487,8 +487,8 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   for (auto* b : {&sigma0, &sigmaMid, &sigma1, &surfaceOut}) SL3D_CUDA(b->Alloc(lm));
   SL3D_CUDA(changePartial.Alloc(3 * kChangeBlocks));
   SL3D_CUDA(changeResult.Alloc(3));
-  SL3D_CUDA(gammaOut.Alloc(16));
-  SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks32) * 16));
+  SL3D_CUDA(gammaOut.Alloc(kMixMaxMemory + 1));
+  SL3D_CUDA(mixPartial.Alloc(static_cast<size_t>(kMixBlocks32) * 2 * kMixMaxMemory));
   if (options.solver == 1) {
     for (auto* b : {&cgF, &cgX, &cgR, &cgZ, &cgP, &cgAp}) {
       SL3D_CUDA(b->Alloc(Columns()));

@@ -584,7 +584,7 @@ __global__ void MixerFirstKernel(long long n, T* x, const T* gx, T* xPrev, T* fP
 }
 
 constexpr int kMixThreads = 256;
-constexpr int kMaxMemory = 8;
+constexpr int kMaxMemory = kMixMaxMemory;
 
 // The accumulation type of the mixer's per-thread sums: FP64 for the FP64
 // form, FP32 for the correction (a thread sums about a hundred products; the

@@ -226,7 +226,7 @@ struct MixerArgsT {
   double* gamma;    // m (+1 status)
 };
 using MixerArgs = MixerArgsT<double>;
-constexpr int kMixMaxMemory = 8;  // the most history columns; sums hold 2 x this
+constexpr int kMixMaxMemory = 16;  // the most history columns; sums hold 2 x this
 void LaunchMixerFirst(const MixerArgsT<double>& a, cudaStream_t stream);
 void LaunchMixerFirst(const MixerArgsT<float>& a, cudaStream_t stream);
 // An update's device part: the history sweep and its reduction to the new
