@@ -125,6 +125,15 @@ int sl3dgpu_synthesise_spin_batch(sl3dgpu_grid* grid, int N, const double* coeff
                                   double* fields, void* stream);
 int sl3dgpu_expand_spin_batch(sl3dgpu_grid* grid, int N, const double* fields, int count,
                               double* coeffs, void* stream);
+/* The Legendre stage alone of SurfaceGrid's transforms (SurfaceGrid.hpp:217-253,
+ * the contraction inside Synthesise/Expand), in the device layouts: spin-N
+ * coefficients [row][count] complex (rows in (m, l) order, m from -lmax, or
+ * m >= 0 for a real spin-0 field) <-> spectra [m][colatitude][count]
+ * complex. fp32 = 0: FP64 (the FP64 units, or the tensor-core emulation the
+ * grid is set to); 1: FP32 buffers through the 3xTF32 tensor-core
+ * contraction of the mixed form's correction passes. */
+int sl3dgpu_legendre_device(sl3dgpu_grid* grid, int N, int real, int analysis, int fp32, const void* in,
+                            int count, void* out, void* stream);
 /* SurfaceGrid::SynthesiseBatch / ExpandBatch (SurfaceGrid.hpp:164-185): real
  * spin-0 fields from and to m >= 0 coefficients. */
 int sl3dgpu_synthesise_batch(sl3dgpu_grid* grid, const double* coeffs, int count,

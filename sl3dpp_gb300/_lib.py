@@ -86,6 +86,8 @@ def lib() -> ctypes.CDLL:
         "sl3dgpu_grid_set_fp64_emulation": (c_int, [c_void_p, c_int]),
         "sl3dgpu_grid_colatitudes": (c_int, [c_void_p, P_double, P_double]),
         "sl3dgpu_synthesise_spin_batch": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+        "sl3dgpu_legendre_device": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p,
+                                            c_void_p]),
         "sl3dgpu_expand_spin_batch": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
         "sl3dgpu_synthesise_batch": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
         "sl3dgpu_expand_batch": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),

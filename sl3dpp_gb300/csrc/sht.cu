@@ -1300,6 +1300,26 @@ extern "C" int sl3dgpu_expand_spin_batch(sl3dgpu_grid* grid, int N, const double
   return Expand(grid, N, false, fields, count, coeffs, stream);
 }
 
+extern "C" int sl3dgpu_legendre_device(sl3dgpu_grid* grid, int N, int real, int analysis, int fp32, const void* in,
+                                       int count, void* out, void* stream) {
+  if (grid == nullptr || count < 0 || (real && N != 0)) {
+    SetError("legendre: null grid, negative count, or a real field of nonzero spin");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto& g = *grid->grid;
+  const cudaStream_t s = AsStream(stream);
+  if (fp32) {
+    return analysis ? g.LegendreAnalysisF(N, real != 0, static_cast<const float*>(in), count, 0, count,
+                                          static_cast<float*>(out), false, s)
+                    : g.LegendreSynthesisF(N, real != 0, static_cast<const float*>(in), count, 0, count,
+                                           static_cast<float*>(out), s);
+  }
+  return analysis ? g.LegendreAnalysis(N, real != 0, static_cast<const double*>(in), count,
+                                       static_cast<double*>(out), s)
+                  : g.LegendreSynthesis(N, real != 0, static_cast<const double*>(in), count,
+                                        static_cast<double*>(out), s);
+}
+
 extern "C" int sl3dgpu_synthesise_batch(sl3dgpu_grid* grid, const double* coeffs, int count,
                                         double* fields, void* stream) {
   return Synthesise(grid, 0, true, coeffs, count, fields, stream);

@@ -131,7 +131,7 @@ class Viscoelastic3DGpu {
   std::vector<Dev<double>> dG, dF;
   Dev<double*> dGPtr, dFPtr;
   static constexpr int kMixBlocks = 1024;
-  static constexpr int kMixBlocks32 = 4096;  // FP32 sums: about a hundred products a thread
+  static constexpr int kMixBlocks32 = 1216;  // 8 a multiprocessor; FP32 sums of about a hundred products a thread
   static constexpr double kWarmKeep = 0.3;   // the largest first change a kept warm start may show
 
   // the mixed form's FP32 correction: iterate, next iterate, residual,

@@ -598,24 +598,25 @@ struct MixAcc<float> {
   using type = float;
 };
 
-// One block per fixed chunk of the vector (fixed by n alone): the new
-// differences, the stored iterate and residual, and the block's partial Gram
-// column and right-hand side, summed in a fixed order (thread, warp
-// shuffle tree, warps in turn).
 // A history value stored and read back (identity for the FP64 form).
 __device__ inline double ToHistory(double v, double*) { return v; }
 __device__ inline __nv_bfloat16 ToHistory(float v, __nv_bfloat16*) { return __float2bfloat16_rn(v); }
 __device__ inline double FromHistory(double v) { return v; }
 __device__ inline float FromHistory(__nv_bfloat16 v) { return __bfloat162float(v); }
 
+// The sweep and mix kernels take the history count M as a template
+// argument, so that their per-column arrays (pointers, sums, gamma) stay in
+// registers; LaunchForMemory picks the instance for a.m.
+
 // A block's partial Gram column and right-hand side: warp shuffle trees,
-// then the warps in turn, written to partial[block][0..m) and [8..8+m).
-template <class A>
-__device__ inline void MixerBlockPartials(const A (&col)[kMaxMemory], const A (&gam)[kMaxMemory], int m,
-                                          double* partial) {
+// then the warps in turn, written to partial[block][0..M) and
+// [kMaxMemory..kMaxMemory + M).
+template <int M, class A>
+__device__ inline void MixerBlockPartials(const A (&col)[M + 1], const A (&gam)[M + 1], double* partial) {
   __shared__ double red[kMixThreads / 32][2 * kMaxMemory];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  for (int i = 0; i < m; ++i) {
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
     A c = col[i], g = gam[i];
     for (int off = 16; off > 0; off /= 2) {
       c += __shfl_down_sync(0xffffffffu, c, off);
@@ -629,7 +630,7 @@ __device__ inline void MixerBlockPartials(const A (&col)[kMaxMemory], const A (&
   __syncthreads();
   if (threadIdx.x < 2 * kMaxMemory) {
     const int i = threadIdx.x;
-    if (i % kMaxMemory < m) {
+    if (i % kMaxMemory < M) {
       double v = 0.0;
       for (int w = 0; w < kMixThreads / 32; ++w) v += red[w][i];
       partial[static_cast<long long>(blockIdx.x) * 2 * kMaxMemory + i] = v;
@@ -637,17 +638,22 @@ __device__ inline void MixerBlockPartials(const A (&col)[kMaxMemory], const A (&
   }
 }
 
-template <class T>
+// One block per fixed chunk of the vector (fixed by n alone): the new
+// differences, the stored iterate and residual, and the block's partial Gram
+// column and right-hand side, summed in a fixed order.
+template <class T, int M>
 __global__ void MixerSweepKernel(MixerArgsT<T> a) {
   using A = typename MixAcc<T>::type;
   using H = typename MixerArgsT<T>::H;
   const long long begin = a.n * blockIdx.x / a.blocks, end = a.n * (blockIdx.x + 1) / a.blocks;
-  A col[kMaxMemory], gam[kMaxMemory];
-  for (int i = 0; i < kMaxMemory; ++i) col[i] = gam[i] = A(0);
+  A col[M + 1], gam[M + 1];
+#pragma unroll
+  for (int i = 0; i <= M; ++i) col[i] = gam[i] = A(0);
   H* dFs = a.dF[a.slot];
   H* dGs = a.dG[a.slot];
-  const H* dF[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) dF[i] = a.dF[i];
+  const H* dF[M + 1];
+#pragma unroll
+  for (int i = 0; i < M; ++i) dF[i] = a.dF[i];
   for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
     const T xs = a.x[at], gs = a.gx[at];
     const T f = gs - xs;
@@ -659,30 +665,34 @@ __global__ void MixerSweepKernel(MixerArgsT<T> a) {
     a.fPrev[at] = f;
     // the new column as stored, so that the Gram matrix is the stored vectors'
     const A df = static_cast<A>(FromHistory(dfStored));
-    for (int i = 0; i < a.m; ++i) {
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
       const A di = i == a.slot ? df : static_cast<A>(FromHistory(dF[i][at]));
       col[i] += di * df;
       gam[i] += di * static_cast<A>(f);
     }
   }
-  MixerBlockPartials(col, gam, a.m, a.partial);
+  MixerBlockPartials<M>(col, gam, a.partial);
 }
 
 // Two values a thread (FP32 iterate, BF16 history): the same sweep as
-// MixerSweepKernel<float> with 8-byte and 4-byte accesses.
+// MixerSweepKernel<float, M> with 8-byte and 4-byte accesses.
+template <int M>
 __global__ void MixerSweepPairsKernel(MixerArgsT<float> a) {
   const long long pairs = a.n / 2;
   const long long begin = pairs * blockIdx.x / a.blocks, end = pairs * (blockIdx.x + 1) / a.blocks;
-  float col[kMaxMemory], gam[kMaxMemory];
-  for (int i = 0; i < kMaxMemory; ++i) col[i] = gam[i] = 0.0f;
+  float col[M + 1], gam[M + 1];
+#pragma unroll
+  for (int i = 0; i <= M; ++i) col[i] = gam[i] = 0.0f;
   auto* x = reinterpret_cast<const float2*>(a.x);
   auto* gx = reinterpret_cast<const float2*>(a.gx);
   auto* xPrev = reinterpret_cast<float2*>(a.xPrev);
   auto* fPrev = reinterpret_cast<float2*>(a.fPrev);
   auto* dFs = reinterpret_cast<__nv_bfloat162*>(a.dF[a.slot]);
   auto* dGs = reinterpret_cast<__nv_bfloat162*>(a.dG[a.slot]);
-  const __nv_bfloat162* dF[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) dF[i] = reinterpret_cast<const __nv_bfloat162*>(a.dF[i]);
+  const __nv_bfloat162* dF[M + 1];
+#pragma unroll
+  for (int i = 0; i < M; ++i) dF[i] = reinterpret_cast<const __nv_bfloat162*>(a.dF[i]);
   for (long long at = begin + threadIdx.x; at < end; at += blockDim.x) {
     const float2 xs = x[at], gs = gx[at], xp = xPrev[at], fp = fPrev[at];
     const float2 f = make_float2(gs.x - xs.x, gs.y - xs.y);
@@ -693,20 +703,19 @@ __global__ void MixerSweepPairsKernel(MixerArgsT<float> a) {
     xPrev[at] = xs;
     fPrev[at] = f;
     const float2 df = __bfloat1622float2(dfStored);
-    for (int i = 0; i < a.m; ++i) {
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
       const float2 di = i == a.slot ? df : __bfloat1622float2(dF[i][at]);
       col[i] += di.x * df.x + di.y * df.y;
       gam[i] += di.x * f.x + di.y * f.y;
     }
   }
-  MixerBlockPartials(col, gam, a.m, a.partial);
+  MixerBlockPartials<M>(col, gam, a.partial);
 }
 
-// The partials in a fixed order (one warp per sum, lanes over the blocks,
-// then a fixed shuffle tree), the Gram matrix's new row and column, and the
-// least-squares coefficients (FP64, one thread; gamma[m] = 1 when they hold).
 // The sweep's block partial sums reduced to the new Gram column (m values)
-// and the right-hand side (m values, from index kMaxMemory), a warp each.
+// and the right-hand side (m values, from index kMaxMemory), a warp each, in
+// a fixed order (lanes over the blocks, then a fixed shuffle tree).
 __global__ void MixerReduceKernel(int m, int blocks, const double* partial, double* sums) {
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (warp >= 2 * m) return;
@@ -717,32 +726,36 @@ __global__ void MixerReduceKernel(int m, int blocks, const double* partial, doub
   if (lane == 0) sums[i] = v;
 }
 
-template <class T>
+template <class T, int M>
 __global__ void MixerMixKernel(MixerArgsT<T> a) {
   using A = typename MixAcc<T>::type;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  const bool ok = a.gamma[a.m] != 0.0;
-  A g[kMaxMemory];
-  const typename MixerArgsT<T>::H* dG[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) {
+  const bool ok = a.gamma[M] != 0.0;
+  A g[M + 1];
+  const typename MixerArgsT<T>::H* dG[M + 1];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
     g[i] = static_cast<A>(a.gamma[i]);
     dG[i] = a.dG[i];
   }
   for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < a.n; at += stride) {
     A value = a.gx[at];
     if (ok)
-      for (int i = 0; i < a.m; ++i) value -= g[i] * static_cast<A>(FromHistory(dG[i][at]));
+#pragma unroll
+      for (int i = 0; i < M; ++i) value -= g[i] * static_cast<A>(FromHistory(dG[i][at]));
     a.x[at] = static_cast<T>(value);
   }
 }
 
+template <int M>
 __global__ void MixerMixPairsKernel(MixerArgsT<float> a) {
   const long long pairs = a.n / 2;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  const bool ok = a.gamma[a.m] != 0.0;
-  float g[kMaxMemory];
-  const __nv_bfloat162* dG[kMaxMemory];
-  for (int i = 0; i < a.m; ++i) {
+  const bool ok = a.gamma[M] != 0.0;
+  float g[M + 1];
+  const __nv_bfloat162* dG[M + 1];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
     g[i] = static_cast<float>(a.gamma[i]);
     dG[i] = reinterpret_cast<const __nv_bfloat162*>(a.dG[i]);
   }
@@ -751,12 +764,25 @@ __global__ void MixerMixPairsKernel(MixerArgsT<float> a) {
   for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < pairs; at += stride) {
     float2 v = gx[at];
     if (ok)
-      for (int i = 0; i < a.m; ++i) {
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
         const float2 d = __bfloat1622float2(dG[i][at]);
         v.x -= g[i] * d.x;
         v.y -= g[i] * d.y;
       }
     x[at] = v;
+  }
+}
+
+// Calls f(std::integral_constant<int, M>{}) for M = m (0 <= m <= kMaxMemory).
+template <int M = 0, class F>
+void ForMemory(int m, F&& f) {
+  if constexpr (M <= kMaxMemory) {
+    if (m == M) {
+      f(std::integral_constant<int, M>{});
+      return;
+    }
+    ForMemory<M + 1>(m, f);
   }
 }
 
@@ -1082,10 +1108,12 @@ void MixerSweep(const MixerArgsT<T>& a, double* sums, cudaStream_t stream) {
   {
     using H = typename MixerArgsT<T>::H;
     prof::Scope scope(prof::kMixer, stream, 0.0, a.n * (6.0 * sizeof(T) + (a.m + 1.0) * sizeof(H)));
-    if constexpr (std::is_same_v<T, float>)
-      MixerSweepPairsKernel<<<a.blocks, kMixThreads, 0, stream>>>(a);
-    else
-      MixerSweepKernel<T><<<a.blocks, kMixThreads, 0, stream>>>(a);
+    ForMemory(a.m, [&](auto M) {
+      if constexpr (std::is_same_v<T, float>)
+        MixerSweepPairsKernel<M()><<<a.blocks, kMixThreads, 0, stream>>>(a);
+      else
+        MixerSweepKernel<T, M()><<<a.blocks, kMixThreads, 0, stream>>>(a);
+    });
   }
   prof::Scope scope(prof::kOther, stream);
   MixerReduceKernel<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.m, a.blocks, a.partial, sums);
@@ -1095,10 +1123,12 @@ template <class T>
 void MixerMix(const MixerArgsT<T>& a, cudaStream_t stream) {
   prof::Scope scope(prof::kMixer, stream, 0.0,
                     a.n * (2.0 * sizeof(T) + a.m * sizeof(typename MixerArgsT<T>::H)));
-  if constexpr (std::is_same_v<T, float>)
-    MixerMixPairsKernel<<<StreamBlocks(a.n / 2), 256, 0, stream>>>(a);
-  else
-    MixerMixKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a);
+  ForMemory(a.m, [&](auto M) {
+    if constexpr (std::is_same_v<T, float>)
+      MixerMixPairsKernel<M()><<<StreamBlocks(a.n / 2), 256, 0, stream>>>(a);
+    else
+      MixerMixKernel<T, M()><<<StreamBlocks(a.n), 256, 0, stream>>>(a);
+  });
 }
 }  // namespace
 

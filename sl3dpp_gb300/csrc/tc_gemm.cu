@@ -1,15 +1,16 @@
 // The FP32 Legendre contraction on the tcgen05 tensor cores (see tc_gemm.cuh).
 //
-// One CTA of four warps per (128-row tile, item, column tile). One elected
-// thread runs the K loop: for each 16-deep step it arms the step buffer's
-// "full" mbarrier with the expected byte count and issues two TMA bulk copies
-// (the A tile's high and low parts, 16 KB; B's, 2 x tileN x 64 B) into it,
-// three steps in flight; when a step's copies have landed it issues the six
-// tcgen05.mma of the step (two 8-deep slices x three products) into the FP32
-// accumulator in tensor memory and commits them to the buffer's "empty"
-// mbarrier, which frees the buffer for the step three ahead. Every wait has an
-// iteration limit. The epilogue reads the accumulator with tcgen05.ld, one
-// TMEM lane quarter per warp, and stores (or adds) the rows in range.
+// A persistent, warp-specialised kernel (TcGemmKernel, below): a TMA
+// producer lane fills a ring of shared-memory stages (the A tile's high and
+// low TF32 parts, 16 KB; B's, 2 x tileN x 64 B), an MMA lane issues each
+// 16-deep step's tcgen05.mma kind::tf32 into one of two TMEM accumulators,
+// and four epilogue warps drain the other. B's high and low parts form one
+// operand of 2 tileN rows, so that for tileN <= 128 the products A_hi B_hi
+// and A_hi B_lo are one MMA of N = 2 tileN into the accumulator's two column
+// halves, and A_lo B_hi a second MMA into the first half: two MMAs per 8-deep
+// slice instead of three (an M = 128 MMA costs about the same below N = 128
+// as at N = 128, so the wide one is nearly free). The epilogue sums the
+// halves. Every wait has an iteration limit.
 #include <cstdint>
 
 #include "profile.cuh"
@@ -96,9 +97,11 @@ __global__ void PackBKernel(const TcItem* tcItems, int tileN, const float* B, fl
     lo.y = v[1] - hi.y;
     lo.z = v[2] - hi.z;
     lo.w = v[3] - hi.w;
-    float* out = packed + it.bPack + tile * 2 * tileFloats + TileIndex(nn, 4 * g, tileN);
-    *reinterpret_cast<float4*>(out) = hi;
-    *reinterpret_cast<float4*>(out + tileFloats) = lo;
+    // one operand of 2 tileN rows: the high parts in rows 0 .. tileN - 1,
+    // the low parts below them
+    float* out = packed + it.bPack + tile * 2 * tileFloats;
+    *reinterpret_cast<float4*>(out + TileIndex(nn, 4 * g, 2 * tileN)) = hi;
+    *reinterpret_cast<float4*>(out + TileIndex(tileN + nn, 4 * g, 2 * tileN)) = lo;
   }
 }
 
@@ -122,7 +125,10 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
     TcGemmKernel(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN, int stages,
                  const float* panels, const float* packed, float* C, bool accumulate, int* errorFlag) {
   const int bTileFloats = tileN * kTcTileK;
-  const uint32_t accColumns = TmemColumns(tileN);
+  // tileN <= 128: A_hi B_hi and A_hi B_lo in one MMA of N = 2 tileN, into
+  // the accumulator's two column halves (summed by the epilogue)
+  const bool fused = 2 * tileN <= 256;
+  const uint32_t accColumns = TmemColumns(fused ? 2 * tileN : tileN);
   const uint32_t aBytes = 2 * kATileFloats * sizeof(float), bBytes = 2 * bTileFloats * sizeof(float);
 
   extern __shared__ __align__(128) unsigned char tcSmem[];
@@ -211,6 +217,7 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
       const TcItem it = tcItems[tile.x];
       const int nCols = min(tileN, it.N - tile.z * tileN);
       const uint32_t idesc = InstrDescriptor((nCols + 15) / 16 * 16, kTcTileM);
+      const uint32_t idescPair = InstrDescriptor(2 * tileN, kTcTileM);
       const int acc = local & 1;
       const int use = local >> 1;
       if (use > 0 && !WaitParity(SmemAddr(accEmpty + acc), static_cast<uint32_t>((use - 1) & 1))) {
@@ -228,24 +235,41 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t aHi = SmemAddr(sA + slot * 2 * kATileFloats), aLo = aHi + kATileFloats * 4;
-        const uint32_t bHi = SmemAddr(sB + slot * 2 * bTileFloats), bLo = bHi + bTileFloats * 4;
-        const uint32_t aLbo = kTcTileM * 16, bLbo = tileN * 16, sbo = 128;
+        const uint32_t bHi = SmemAddr(sB + slot * 2 * bTileFloats), bLo = bHi + tileN * 16;
+        const uint32_t aLbo = kTcTileM * 16, bLbo = 2 * tileN * 16, sbo = 128;
 #pragma unroll
         for (int q = 0; q < kTcTileK / 8; ++q) {
           const uint32_t aOff = q * 2 * aLbo, bOff = q * 2 * bLbo;
           const uint64_t dAh = Descriptor(aHi + aOff, aLbo, sbo), dAl = Descriptor(aLo + aOff, aLbo, sbo);
           const uint64_t dBh = Descriptor(bHi + bOff, bLbo, sbo), dBl = Descriptor(bLo + bOff, bLbo, sbo);
-          const uint64_t as[3] = {dAh, dAh, dAl};
-          const uint64_t bs[3] = {dBh, dBl, dBh};
-#pragma unroll
-          for (int p = 0; p < 3; ++p) {
-            const uint32_t enable = (ks > 0 || q > 0 || p > 0) ? 1u : 0u;
+          const uint32_t enable = (ks > 0 || q > 0) ? 1u : 0u;
+          if (fused) {
+            // A_hi [B_hi; B_lo] into both halves, then A_lo B_hi into the first
             asm volatile(
                 "{\n\t.reg .pred r;\n\t"
                 "setp.ne.b32 r, %4, 0;\n\t"
                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, r;\n\t}" ::"r"(d),
-                "l"(as[p]), "l"(bs[p]), "r"(idesc), "r"(enable)
+                "l"(dAh), "l"(dBh), "r"(idescPair), "r"(enable)
                 : "memory");
+            asm volatile(
+                "{\n\t.reg .pred r;\n\t"
+                "setp.ne.b32 r, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, r;\n\t}" ::"r"(d),
+                "l"(dAl), "l"(dBh), "r"(idesc), "r"(1u)
+                : "memory");
+          } else {
+            const uint64_t as[3] = {dAh, dAh, dAl};
+            const uint64_t bs[3] = {dBh, dBl, dBh};
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+              const uint32_t on = (enable || p > 0) ? 1u : 0u;
+              asm volatile(
+                  "{\n\t.reg .pred r;\n\t"
+                  "setp.ne.b32 r, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, r;\n\t}" ::"r"(d),
+                  "l"(as[p]), "l"(bs[p]), "r"(idesc), "r"(on)
+                  : "memory");
+            }
           }
         }
         issued = true;
@@ -310,6 +334,28 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int q = 0; q < 32; ++q) block[lane][q] = __uint_as_float(r[q]);
+        if (fused) {
+          // the A_hi B_lo half, tileN columns on
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+              "%14, %15}, [%16];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+              : "r"(addr + tileN)
+              : "memory");
+          if (c0 + 16 < nMma)
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                "%13, %14, %15}, [%16];"
+                : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+                  "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                  "=r"(r[30]), "=r"(r[31])
+                : "r"(addr + tileN + 16)
+                : "memory");
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int q = 0; q < 32; ++q) block[lane][q] += __uint_as_float(r[q]);
+        }
         __syncwarp();
         const int n = c0 + lane;
         for (int rr = 0; rr < 32; ++rr) {

@@ -385,13 +385,19 @@ __global__ void __launch_bounds__(kThreads) TcGemm64Kernel(const Tc64Item* tcIte
       }
       __syncwarp();
       const int n = c0 + (lane & 15);
-      for (int rr = lane >> 4; rr < 32; rr += 2) {
-        const int row = i0 + 32 * quarter + rr;
-        if (row < it.M && n < nCols) {
-          double* dst = C + it.c + static_cast<long long>(row) * it.ldc + n0 + n;
-          const double v = rowsOut[warp][rr][lane & 15];
-          *dst = accumulate ? *dst + v : v;
-        }
+      // this lane's 16 rows' old values first (loads in flight together), then the stores
+      double old[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int row = i0 + 32 * quarter + 2 * q + (lane >> 4);
+        old[q] = (accumulate && row < it.M && n < nCols) ? C[it.c + static_cast<long long>(row) * it.ldc + n0 + n]
+                                                         : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int rr = 2 * q + (lane >> 4), row = i0 + 32 * quarter + rr;
+        if (row < it.M && n < nCols)
+          C[it.c + static_cast<long long>(row) * it.ldc + n0 + n] = old[q] + rowsOut[warp][rr][lane & 15];
       }
       __syncwarp();
     }

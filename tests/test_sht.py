@@ -235,3 +235,46 @@ def test_gpu_emulated_fp64_contraction_agrees_with_the_fp64_units(gpu):
         assert (fa - fb).abs().max().item() < 3e-14 * fa.abs().max().item(), N
         ba, bb = native.ExpandSpinBatch(N, fa, 1), emulated.ExpandSpinBatch(N, fa, 1)
         assert (ba - bb).abs().max().item() < 3e-14 * ba.abs().max().item(), N
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lmax,count", [(33, 5), (64, 40), (64, 80)])
+@pytest.mark.parametrize("N,real", [(-2, False), (-1, False), (0, True)])
+def test_gpu_fp32_tensor_core_contraction_matches_fp64(gpu, lmax, count, N, real):
+    """The 3xTF32 tensor-core contraction of the correction passes (FP32
+    buffers) against the FP64 one on the same inputs, both directions, in the
+    device layouts: within 4e-6 of the largest value. count 5 and 40 take the
+    paired MMA (B's high and low parts in one operand, 2 x 16 and 2 x 80
+    columns), count 80 (160 columns) the three separate products."""
+    import torch
+
+    from sl3dpp_gb300 import _lib
+    from sl3dpp_gb300.grid import SurfaceGrid
+
+    g = SurfaceGrid(lmax, 2, 1.5)
+    lib = _lib.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    rows = g.CoefficientSize() if real else g.SpinCoefficientSize(N)
+    mcount = lmax + 1 if real else 2 * lmax + 1
+    rng = np.random.default_rng(100 * lmax + 7 * count - N)
+    coeffs = torch.tensor(rng.standard_normal(rows * count * 2), device=gpu)
+    spectra = torch.tensor(rng.standard_normal(mcount * g.ntheta * count * 2), device=gpu)
+    for analysis, src, size in ((0, coeffs, mcount * g.ntheta * count * 2), (1, spectra, rows * count * 2)):
+        out64 = torch.zeros(size, dtype=torch.float64, device=gpu)
+        out32 = torch.zeros(size, dtype=torch.float32, device=gpu)
+        src32 = src.float().contiguous()
+        _lib.check(lib.sl3dgpu_legendre_device(g._handle, N, int(real), analysis, 0, src.data_ptr(), count,
+                                               out64.data_ptr(), stream))
+        _lib.check(lib.sl3dgpu_legendre_device(g._handle, N, int(real), analysis, 1, src32.data_ptr(), count,
+                                               out32.data_ptr(), stream))
+        torch.cuda.synchronize()
+        # the FP64 contraction of the FP32-rounded input is the reference
+        ref = torch.zeros(size, dtype=torch.float64, device=gpu)
+        rounded = src32.double()
+        _lib.check(lib.sl3dgpu_legendre_device(g._handle, N, int(real), analysis, 0, rounded.data_ptr(), count,
+                                               ref.data_ptr(), stream))
+        torch.cuda.synchronize()
+        scale = ref.abs().max().item()
+        assert scale > 0
+        assert (out32.double() - ref).abs().max().item() < 4e-6 * scale, (analysis, N)
+        assert (out64 - ref).abs().max().item() < 1e-6 * scale  # the rounding of the input only
