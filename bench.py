@@ -176,9 +176,13 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+# The committed ncu summary holding a kernel kind's DRAM bytes per launch.
+TRAFFIC_PROFILES = {"ring_fft": "ring_fft_f64_3d_step_lmax256.md"}
+
+
 def ncu_traffic(kernel: str):
     """DRAM bytes per launch from the committed ncu summary of a kernel, if any."""
-    path = ROOT / "profiles" / f"{kernel}.md"
+    path = ROOT / "profiles" / TRAFFIC_PROFILES.get(kernel, f"{kernel}.md")
     if not path.exists():
         return None
     for line in path.read_text().splitlines():
