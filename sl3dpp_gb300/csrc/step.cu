@@ -1269,9 +1269,7 @@ int Viscoelastic3DGpu::Pass32(const Flavour& f, const float2* e, float2* next) {
                            f.bands32.p, f.pivots.p, sph, f.scales32.p, 1, stream));
   SL3D_TRY(BandSolveWindowF(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
                             f.nTorChol, f.bands32.p, tor, f.scales32.p, f.wTorChol.p, false, stream));
-  LaunchStrain(geoL, rhsSph32.p, rhsTor32.p, next, stream);
-  SL3D_CHECK_LAUNCH();
-  LaunchAddInPlace(2 * compactComplex, reinterpret_cast<const float*>(rL.p), reinterpret_cast<float*>(next), stream);
+  LaunchStrain(geoL, rhsSph32.p, rhsTor32.p, next, stream, rL.p);  // B e + r
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
@@ -1432,9 +1430,7 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
                             f.nSphChol, f.bands32.p, sph, f.scales32.p, f.wSphChol.p, true, stream));
   SL3D_TRY(BandSolveWindowF(f.dTorChol.p, f.torChol.data(), static_cast<int>(f.torChol.size()), f.iTorChol.p,
                             f.nTorChol, f.bands32.p, tor, f.scales32.p, f.wTorChol.p, true, stream));
-  LaunchStrain(geo, rhsSph32.p, rhsTor32.p, e32.p, stream);
-  SL3D_CHECK_LAUNCH();
-  LaunchAddInPlace(2 * spectralComplex, reinterpret_cast<const float*>(r32.p), reinterpret_cast<float*>(e32.p), stream);
+  LaunchStrain(geo, rhsSph32.p, rhsTor32.p, e32.p, stream, r32.p);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }

@@ -180,7 +180,7 @@ __global__ void ForceKernel(Geometry g, const T2* spectral, T2* rhsSph, T2* rhsT
 // DeviatoricComponents (SpinComponents.hpp:53-72) into the stored blocks
 // (GridCoupling::Scatter, the -m twins from the derived components).
 template <class T2>
-__global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2* spectral) {
+__global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2* spectral, const T2* add) {
   using T = typename Scalar<T2>::type;
   int l, m;
   DecodeLm(blockIdx.x, l, m);
@@ -248,15 +248,20 @@ __global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2*
         A[4] = CScale(factor, CAdd(V, CI(W)));
       }
     }
+    // every value written once; `add` (same layout), when given, added to it
+    auto put = [&](T2* base, long long at, T2 v) {
+      const long long i = (base - spectral) + at;
+      spectral[i] = add != nullptr ? CAdd(v, add[i]) : v;
+    };
     if (l >= 2) {
-      c0[Row0(g, l, m) * g.P + p] = A[0];
-      if (m > 0) c0[Row0(g, l, -m) * g.P + p] = CScale(sign, CConj(A[4]));
+      put(c0, Row0(g, l, m) * g.P + p, A[0]);
+      if (m > 0) put(c0, Row0(g, l, -m) * g.P + p, CScale(sign, CConj(A[4])));
     }
     if (l >= 1) {
-      c1[Row1(g, l, m) * g.P + p] = A[1];
-      if (m > 0) c1[Row1(g, l, -m) * g.P + p] = CScale(sign, CConj(A[3]));
+      put(c1, Row1(g, l, m) * g.P + p, A[1]);
+      if (m > 0) put(c1, Row1(g, l, -m) * g.P + p, CScale(sign, CConj(A[3])));
     }
-    cr[RowR(g, l, m) * g.P + p] = A[2];
+    put(cr, RowR(g, l, m) * g.P + p, A[2]);
   }
 }
 
@@ -980,12 +985,13 @@ void Forces(const Geometry& g, const T2* spectral, T2* rhsSph, T2* rhsTor, cudaS
 }
 
 template <class T2>
-void Strain(const Geometry& g, const T2* solSph, const T2* solTor, T2* spectral, cudaStream_t stream) {
+void Strain(const Geometry& g, const T2* solSph, const T2* solTor, T2* spectral, const T2* add,
+            cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 3 * sizeof(T2);
   AllowDynamicSmem(StrainKernel<T2>);
   prof::Scope scope(prof::kStrain, stream);
-  StrainKernel<T2><<<count, 128, smem, stream>>>(g, solSph, solTor, spectral);
+  StrainKernel<T2><<<count, 128, smem, stream>>>(g, solSph, solTor, spectral, add);
 }
 }  // namespace
 
@@ -997,12 +1003,12 @@ void LaunchForces(const Geometry& g, const float2* spectral, float2* rhsSph, flo
   Forces(g, spectral, rhsSph, rhsTor, stream);
 }
 void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTor, double2* spectral,
-                  cudaStream_t stream) {
-  Strain(g, solSph, solTor, spectral, stream);
+                  cudaStream_t stream, const double2* add) {
+  Strain(g, solSph, solTor, spectral, add, stream);
 }
 void LaunchStrain(const Geometry& g, const float2* solSph, const float2* solTor, float2* spectral,
-                  cudaStream_t stream) {
-  Strain(g, solSph, solTor, spectral, stream);
+                  cudaStream_t stream, const float2* add) {
+  Strain(g, solSph, solTor, spectral, add, stream);
 }
 
 void LaunchDilatation(const Geometry& g, const double2* solSph, double2* scalar, cudaStream_t stream) {

@@ -64,11 +64,12 @@ void LaunchForces(const Geometry& g, const double2* spectral, double2* rhsSph, d
                   cudaStream_t stream);
 void LaunchForces(const Geometry& g, const float2* spectral, float2* rhsSph, float2* rhsTor, cudaStream_t stream);
 // The deviatoric strain of every degree's solutions into a spectral tensor
-// (StrainOf: AddStrainOfSolution + DeviatoricComponents + Scatter).
+// (StrainOf: AddStrainOfSolution + DeviatoricComponents + Scatter), plus
+// `add` (a tensor of the same layout) when given.
 void LaunchStrain(const Geometry& g, const double2* solSph, const double2* solTor, double2* spectral,
-                  cudaStream_t stream);
+                  cudaStream_t stream, const double2* add = nullptr);
 void LaunchStrain(const Geometry& g, const float2* solSph, const float2* solTor, float2* spectral,
-                  cudaStream_t stream);
+                  cudaStream_t stream, const float2* add = nullptr);
 // The dilatation companion (GridCoupling::AddDilatationOfSolution,
 // src/GridCoupling.cpp:359-398): D_lm = r dU/dr + 2 U - l(l+1) V per memory
 // node into a real spin-0 spectral block (rowsR x P), every (l, m >= 0).
