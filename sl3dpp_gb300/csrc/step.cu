@@ -438,7 +438,8 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   SL3D_TRY(grid->Table(0, &tr));
   geo = Geometry{L, P, n, pts.count, E, dNodeElement.p, dNodeQ.p, dNodeR.p, dElemFirstNode.p, dElemJac.p,
                  dValue.p, dDeriv.p, dWeight.p, t0->dRowOffset, t1->dRowOffset, tr->dRowOffset,
-                 rows0, rows1, rowsR, dDegrees.p, dSphMap.p, dTorMap.p, {}, {}};
+                 rows0, rows1, rowsR, dDegrees.p, dSphMap.p, dTorMap.p, {}, {}, 0};
+  for (const auto& d : degrees) geo.maxGlobals = std::max(geo.maxGlobals, d.lastGlobal - d.firstGlobal + 1);
   {
     const auto coef = NodeCoefficients(P, n, nodeElement, nodeQ, nodeR, elemJac, pts.value, pts.derivative,
                                        pts.weight);
@@ -1197,6 +1198,8 @@ int Viscoelastic3DGpu::PrepareLateral() {
   }
   geoL.elemFirstNode = dElemFirstNodeL.p;
   geoL.degrees = dDegreesL.p;
+  geoL.maxGlobals = 0;
+  for (const auto& d : dl) geoL.maxGlobals = std::max(geoL.maxGlobals, d.lastGlobal - d.firstGlobal + 1);
   compactComplex = (rows0 + rows1 + rowsR) * count;
   for (auto* b : {&eL, &eNextL, &rL, &analysedL}) SL3D_CUDA(b->Alloc(std::max<long long>(compactComplex, 1)));
   geoLFirst = lateralFirst;

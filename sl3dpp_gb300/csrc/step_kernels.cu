@@ -108,20 +108,57 @@ __device__ Rows<T2> ForceRows(int l, const T2 A[5], typename Scalar<T2>::type r)
   return rows;
 }
 
-template <class T2>
-__global__ void ForceKernel(Geometry g, const T2* spectral, T2* rhsSph, T2* rhsTor) {
+// -- the force and strain maps over chunks of MC orders ------------------------------------------
+//
+// One block per (degree l, MC consecutive orders m0 .. m0 + MC - 1 <= l),
+// the orders of a chunk side by side, so that the degree systems' right-hand
+// sides and solutions, stored [dof][m] (m fastest), are read and written in
+// runs of MC consecutive values, and the spectral rows [row][node] in runs
+// of nodes. Every value is written by exactly one thread (no atomics, a fixed
+// summation order); the sums per value are those of the reference's
+// per-(l, m) loops.
+
+// Blocks before degree l: sum over l' < l of (floor(l' / MC) + 1).
+template <int MC>
+__device__ inline int ChunksBefore(int l) {
+  const int q = l / MC;
+  return l + MC * q * (q - 1) / 2 + q * (l - q * MC);
+}
+template <int MC>
+__device__ inline void DecodeChunk(int b, int lmax, int& l, int& m0) {
+  int lo = 0, hi = lmax;  // the largest l with ChunksBefore(l) <= b
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (ChunksBefore<MC>(mid) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  l = lo;
+  m0 = (b - ChunksBefore<MC>(l)) * MC;
+}
+
+// The memory force of an analysed (mu-weighted) tensor into the degree
+// systems' right-hand sides (GridCoupling::SpheroidalForce/ToroidalForce,
+// src/GridCoupling.cpp:613-809): per memory node the six force rows of the
+// order's spin components, then per global node of the degree's carrying
+// elements the quadrature over its elements' points.
+template <class T2, int MC>
+__global__ void ForceChunkKernel(Geometry g, const T2* spectral, T2* rhsSph, T2* rhsTor) {
   using T = typename Scalar<T2>::type;
-  int l, m;
-  DecodeLm(blockIdx.x, l, m);
+  int l, m0;
+  DecodeChunk<MC>(blockIdx.x, g.lmax, l, m0);
+  const int mc = min(MC, l + 1 - m0);  // orders in this chunk
   const DegreeInfo d = g.degrees[l];
   if (d.firstNode >= g.P) return;
-  extern __shared__ __align__(16) unsigned char forceSmem[];
-  T2* rowsS = reinterpret_cast<T2*>(forceSmem);  // (P - first) x 6
+  const int np = g.P - d.firstNode;
+  const int pPad = np | 1;  // odd row length: the epilogue's reads across orders miss no bank twice
+  extern __shared__ __align__(16) unsigned char forceChunkSmem[];
+  T2* rowsS = reinterpret_cast<T2*>(forceChunkSmem);  // [6][MC][pPad]
   const T2* c0 = spectral;
   const T2* c1 = spectral + g.rows0 * g.P;
   const T2* cr = spectral + (g.rows0 + g.rows1) * g.P;
-  const T sign = (m % 2 == 0) ? T(1) : T(-1);
-  for (int p = d.firstNode + threadIdx.x; p < g.P; p += blockDim.x) {
+  for (int t = threadIdx.x; t < mc * np; t += blockDim.x) {
+    const int mi = t / np, p = d.firstNode + t % np, m = m0 + mi;
+    const T sign = (m % 2 == 0) ? T(1) : T(-1);
     T2 A[5] = {Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0)};
     A[2] = cr[RowR(g, l, m) * g.P + p];
     if (l >= 1) {
@@ -133,40 +170,45 @@ __global__ void ForceKernel(Geometry g, const T2* spectral, T2* rhsSph, T2* rhsT
       A[4] = CScale(sign, CConj(c0[Row0(g, l, -m) * g.P + p]));
     }
     const Rows<T2> rows = ForceRows<T2>(l, A, static_cast<T>(g.nodeR[p]));
-    T2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
+    T2* s = rowsS + static_cast<long long>(mi) * pPad + (p - d.firstNode);
+    const long long k = static_cast<long long>(MC) * pPad;
     s[0] = rows.u;
-    s[1] = rows.v;
-    s[2] = rows.w;
-    s[3] = rows.du;
-    s[4] = rows.dv;
-    s[5] = rows.dw;
+    s[k] = rows.v;
+    s[2 * k] = rows.w;
+    s[3 * k] = rows.du;
+    s[4 * k] = rows.dv;
+    s[5 * k] = rows.dw;
   }
   __syncthreads();
   const int n = g.ngll, cols = l + 1;
-  for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
+  const int globals = d.lastGlobal - d.firstGlobal + 1;
+  const T* fValue = Coef<T>(g, kForceValue);
+  const T* fDeriv = Coef<T>(g, kForceDeriv);
+  for (int t = threadIdx.x; t < globals * mc; t += blockDim.x) {
+    const int mi = t % mc, gn = d.firstGlobal + t / mc;
     T2 bU = Cx<T2>(0, 0), bV = Cx<T2>(0, 0), bW = Cx<T2>(0, 0);
     const int eHi = min(gn / (n - 1), g.elements - 1);
     const int iHi = gn - eHi * (n - 1);
     const int eLo = (iHi == 0 && eHi > 0) ? eHi - 1 : eHi;
-    const T* fValue = Coef<T>(g, kForceValue);
-    const T* fDeriv = Coef<T>(g, kForceDeriv);
     for (int e = eLo; e <= eHi; ++e) {
       const int fn = g.elemFirstNode[e];
       if (fn < 0 || fn < d.firstNode) continue;
       const int i = e == eHi ? iHi : n - 1;
       for (int q = 0; q < g.np; ++q) {
         const int p = fn + q;
-        const T2* s = rowsS + static_cast<long long>(p - d.firstNode) * 6;
+        const T2* s = rowsS + static_cast<long long>(mi) * pPad + (p - d.firstNode);
+        const long long k = static_cast<long long>(MC) * pPad;
         const T v = fValue[p * n + i];
         const T deriv = fDeriv[p * n + i];
         bU = CAdd(bU, CScale(v, s[0]));
-        bV = CAdd(bV, CScale(v, s[1]));
-        bU = CAdd(bU, CScale(deriv, s[3]));
-        bV = CAdd(bV, CScale(deriv, s[4]));
-        bW = CAdd(bW, CScale(v, s[2]));
-        bW = CAdd(bW, CScale(deriv, s[5]));
+        bV = CAdd(bV, CScale(v, s[k]));
+        bU = CAdd(bU, CScale(deriv, s[3 * k]));
+        bV = CAdd(bV, CScale(deriv, s[4 * k]));
+        bW = CAdd(bW, CScale(v, s[2 * k]));
+        bW = CAdd(bW, CScale(deriv, s[5 * k]));
       }
     }
+    const int m = m0 + mi;
     const int dU = g.sphMap[d.sphMap + 2LL * gn], dV = g.sphMap[d.sphMap + 2LL * gn + 1];
     if (dU >= 0) rhsSph[d.sphRhs + static_cast<long long>(dU) * cols + m] = bU;
     if (dV >= 0) rhsSph[d.sphRhs + static_cast<long long>(dV) * cols + m] = bV;
@@ -177,41 +219,52 @@ __global__ void ForceKernel(Geometry g, const T2* spectral, T2* rhsSph, T2* rhsT
   }
 }
 
-// DeviatoricComponents (SpinComponents.hpp:53-72) into the stored blocks
-// (GridCoupling::Scatter, the -m twins from the derived components).
-template <class T2>
-__global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2* spectral, const T2* add) {
+// StrainOf (AddStrainOfSolution + DeviatoricComponents, SpinComponents.hpp:
+// 53-72, + Scatter with the -m twins from the derived components): the
+// degree's U, V, W at the carrying elements' GLL nodes, then per memory node
+// the five deviatoric components; `add` (the same layout), when given, added.
+template <class T2, int MC>
+__global__ void StrainChunkKernel(Geometry g, const T2* solSph, const T2* solTor, T2* spectral, const T2* add) {
   using T = typename Scalar<T2>::type;
-  int l, m;
-  DecodeLm(blockIdx.x, l, m);
+  int l, m0;
+  DecodeChunk<MC>(blockIdx.x, g.lmax, l, m0);
+  const int mc = min(MC, l + 1 - m0);
   const DegreeInfo d = g.degrees[l];
-  extern __shared__ __align__(16) unsigned char strainSmem[];
-  T2* vals = reinterpret_cast<T2*>(strainSmem);  // (lastGlobal - firstGlobal + 1) x 3
+  extern __shared__ __align__(16) unsigned char strainChunkSmem[];
+  T2* vals = reinterpret_cast<T2*>(strainChunkSmem);  // [global node][3 MC + 1]
+  constexpr int kRow = 3 * MC + 1;                    // odd: reads across nodes miss no bank twice
   T2* c0 = spectral;
   T2* c1 = spectral + g.rows0 * g.P;
   T2* cr = spectral + (g.rows0 + g.rows1) * g.P;
   const int cols = l + 1;
   const bool any = d.firstNode < g.P;
   if (any) {
-    for (int gn = d.firstGlobal + threadIdx.x; gn <= d.lastGlobal; gn += blockDim.x) {
+    const int globals = d.lastGlobal - d.firstGlobal + 1;
+    for (int t = threadIdx.x; t < globals * mc; t += blockDim.x) {
+      const int mi = t % mc, gn = d.firstGlobal + t / mc, m = m0 + mi;
       const int dU = g.sphMap[d.sphMap + 2LL * gn], dV = g.sphMap[d.sphMap + 2LL * gn + 1];
-      T2* v = vals + static_cast<long long>(gn - d.firstGlobal) * 3;
+      T2* v = vals + static_cast<long long>(gn - d.firstGlobal) * kRow + mi;
       v[0] = dU >= 0 ? solSph[d.sphRhs + static_cast<long long>(dU) * cols + m] : Cx<T2>(0, 0);
-      v[1] = dV >= 0 ? solSph[d.sphRhs + static_cast<long long>(dV) * cols + m] : Cx<T2>(0, 0);
+      v[MC] = dV >= 0 ? solSph[d.sphRhs + static_cast<long long>(dV) * cols + m] : Cx<T2>(0, 0);
       T2 W = Cx<T2>(0, 0);
       if (l >= 1) {
         const int dW = g.torMap[d.torMap + gn];
         if (dW >= 0) W = solTor[d.torRhs + static_cast<long long>(dW) * cols + m];
       }
-      v[2] = W;
+      v[2 * MC] = W;
     }
   }
   __syncthreads();
-  const T sign = (m % 2 == 0) ? T(1) : T(-1);
   const int n = g.ngll;
   const T zeta2 = l * (l + T(1)), zeta = sqrt(zeta2);
   const T s2 = T(1.41421356237309504880);
-  for (int p = threadIdx.x; p < g.P; p += blockDim.x) {
+  auto put = [&](T2* base, long long at, T2 v) {
+    const long long i = (base - spectral) + at;
+    spectral[i] = add != nullptr ? CAdd(v, add[i]) : v;
+  };
+  for (int t = threadIdx.x; t < mc * g.P; t += blockDim.x) {
+    const int mi = t / g.P, p = t % g.P, m = m0 + mi;
+    const T sign = (m % 2 == 0) ? T(1) : T(-1);
     T2 A[5] = {Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0), Cx<T2>(0, 0)};
     if (any && p >= d.firstNode) {
       const int e = g.nodeElement[p];
@@ -221,15 +274,15 @@ __global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2*
       T2 U = Cx<T2>(0, 0), V = Cx<T2>(0, 0), W = Cx<T2>(0, 0), rdU = Cx<T2>(0, 0), rdV = Cx<T2>(0, 0),
          rdW = Cx<T2>(0, 0);
       for (int i = 0; i < n; ++i) {
-        const T2* v = vals + static_cast<long long>(e * (n - 1) + i - d.firstGlobal) * 3;
+        const T2* v = vals + static_cast<long long>(e * (n - 1) + i - d.firstGlobal) * kRow + mi;
         const T val = sValue[i];
         U = CAdd(U, CScale(val, v[0]));
-        V = CAdd(V, CScale(val, v[1]));
-        W = CAdd(W, CScale(val, v[2]));
+        V = CAdd(V, CScale(val, v[MC]));
+        W = CAdd(W, CScale(val, v[2 * MC]));
         const T b = sDeriv[i];
         rdU = CAdd(rdU, CScale(b, v[0]));
-        rdV = CAdd(rdV, CScale(b, v[1]));
-        rdW = CAdd(rdW, CScale(b, v[2]));
+        rdV = CAdd(rdV, CScale(b, v[MC]));
+        rdW = CAdd(rdW, CScale(b, v[2 * MC]));
       }
       const T2 t2 = CAdd(CSub(rdU, U), CScale(T(0.5) * zeta2, V));
       A[2] = Cx<T2>(t2.x / (T(3) * r), t2.y / (T(3) * r));
@@ -248,11 +301,6 @@ __global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2*
         A[4] = CScale(factor, CAdd(V, CI(W)));
       }
     }
-    // every value written once; `add` (same layout), when given, added to it
-    auto put = [&](T2* base, long long at, T2 v) {
-      const long long i = (base - spectral) + at;
-      spectral[i] = add != nullptr ? CAdd(v, add[i]) : v;
-    };
     if (l >= 2) {
       put(c0, Row0(g, l, m) * g.P + p, A[0]);
       if (m > 0) put(c0, Row0(g, l, -m) * g.P + p, CScale(sign, CConj(A[4])));
@@ -265,7 +313,7 @@ __global__ void StrainKernel(Geometry g, const T2* solSph, const T2* solTor, T2*
   }
 }
 
-// One block per (l, m >= 0), as StrainKernel: the degree's U, V at its
+// One block per (l, m >= 0): the degree's U, V at its
 // carrying elements' GLL nodes in shared memory, then per memory node the
 // dilatation rdU + 2 U - l(l+1) V.
 __global__ void DilatationKernel(Geometry g, const double2* solSph, double2* scalar) {
@@ -305,7 +353,7 @@ __global__ void DilatationKernel(Geometry g, const double2* solSph, double2* sca
   }
 }
 
-// One block per (l, m >= 0), as ForceKernel: per global node of the degree's
+// One block per (l, m >= 0): per global node of the degree's
 // range, the quadrature over its elements' memory points of
 // 2 w jac D Value (U), -l(l+1) w jac D Value (V) and w Deriv r D (U),
 // added onto the right-hand side.
@@ -975,23 +1023,61 @@ int StreamBlocks(long long values) {
 }  // namespace
 
 namespace {
+// Orders a block of the chunked maps takes: the most (up to 32) whose
+// shared-memory rows fit a budget that leaves room for two blocks an SM.
+constexpr size_t kChunkSmemBudget = 110 * 1024;
+inline int ChunkOrders(size_t bytesPerOrder, size_t fixedBytes) {
+  int mc = 32;
+  while (mc > 1 && fixedBytes + bytesPerOrder * mc > kChunkSmemBudget) mc /= 2;
+  return mc;
+}
+inline int ChunkBlocks(int lmax, int mc) {  // sum over l <= lmax of (floor(l / mc) + 1)
+  long long blocks = 0;
+  for (int l = 0; l <= lmax; ++l) blocks += l / mc + 1;
+  return static_cast<int>(blocks);
+}
+
+template <class T2, int MC>
+void ForcesWith(const Geometry& g, const T2* spectral, T2* rhsSph, T2* rhsTor, cudaStream_t stream) {
+  const size_t smem = static_cast<size_t>(6) * MC * (g.P | 1) * sizeof(T2);
+  AllowDynamicSmem(ForceChunkKernel<T2, MC>);
+  ForceChunkKernel<T2, MC><<<ChunkBlocks(g.lmax, MC), 256, smem, stream>>>(g, spectral, rhsSph, rhsTor);
+}
+
+template <class T2, int MC>
+void StrainWith(const Geometry& g, const T2* solSph, const T2* solTor, T2* spectral, const T2* add,
+                cudaStream_t stream) {
+  const size_t smem = static_cast<size_t>(std::max(g.maxGlobals, 1)) * (3 * MC + 1) * sizeof(T2);
+  AllowDynamicSmem(StrainChunkKernel<T2, MC>);
+  StrainChunkKernel<T2, MC><<<ChunkBlocks(g.lmax, MC), 256, smem, stream>>>(g, solSph, solTor, spectral, add);
+}
+
 template <class T2>
 void Forces(const Geometry& g, const T2* spectral, T2* rhsSph, T2* rhsTor, cudaStream_t stream) {
-  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
-  const size_t smem = static_cast<size_t>(g.P) * 6 * sizeof(T2);
-  AllowDynamicSmem(ForceKernel<T2>);
   prof::Scope scope(prof::kForce, stream);
-  ForceKernel<T2><<<count, 128, smem, stream>>>(g, spectral, rhsSph, rhsTor);
+  switch (ChunkOrders(static_cast<size_t>(6) * (g.P | 1) * sizeof(T2), 0)) {
+    case 32: return ForcesWith<T2, 32>(g, spectral, rhsSph, rhsTor, stream);
+    case 16: return ForcesWith<T2, 16>(g, spectral, rhsSph, rhsTor, stream);
+    case 8: return ForcesWith<T2, 8>(g, spectral, rhsSph, rhsTor, stream);
+    case 4: return ForcesWith<T2, 4>(g, spectral, rhsSph, rhsTor, stream);
+    case 2: return ForcesWith<T2, 2>(g, spectral, rhsSph, rhsTor, stream);
+    default: return ForcesWith<T2, 1>(g, spectral, rhsSph, rhsTor, stream);
+  }
 }
 
 template <class T2>
 void Strain(const Geometry& g, const T2* solSph, const T2* solTor, T2* spectral, const T2* add,
             cudaStream_t stream) {
-  const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
-  const size_t smem = static_cast<size_t>(g.elements * (g.ngll - 1) + 1) * 3 * sizeof(T2);
-  AllowDynamicSmem(StrainKernel<T2>);
   prof::Scope scope(prof::kStrain, stream);
-  StrainKernel<T2><<<count, 128, smem, stream>>>(g, solSph, solTor, spectral, add);
+  const size_t globals = static_cast<size_t>(std::max(g.maxGlobals, 1));
+  switch (ChunkOrders(globals * 3 * sizeof(T2), globals * sizeof(T2))) {
+    case 32: return StrainWith<T2, 32>(g, solSph, solTor, spectral, add, stream);
+    case 16: return StrainWith<T2, 16>(g, solSph, solTor, spectral, add, stream);
+    case 8: return StrainWith<T2, 8>(g, solSph, solTor, spectral, add, stream);
+    case 4: return StrainWith<T2, 4>(g, solSph, solTor, spectral, add, stream);
+    case 2: return StrainWith<T2, 2>(g, solSph, solTor, spectral, add, stream);
+    default: return StrainWith<T2, 1>(g, solSph, solTor, spectral, add, stream);
+  }
 }
 }  // namespace
 

@@ -50,6 +50,7 @@ struct Geometry {
   // [kForceValue] jac w_q r_p Value(q_p, i); [kForceDeriv] w_q Deriv(q_p, i) r_p.
   const double* coef64[4];
   const float* coef32[4];
+  int maxGlobals;  // the most global nodes a degree's carrying elements span (shared-memory sizing)
 };
 enum NodeCoefficient { kStrainValue = 0, kStrainDeriv = 1, kForceValue = 2, kForceDeriv = 3 };
 // The node coefficient tables of a geometry, host FP64 (4 x P x ngll).
