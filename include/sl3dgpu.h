@@ -111,6 +111,8 @@ typedef struct sl3dgpu_grid sl3dgpu_grid;
 int sl3dgpu_grid_create(int lmax, int nmax, double oversampling, sl3dgpu_grid** out);
 void sl3dgpu_grid_destroy(sl3dgpu_grid* grid);
 int sl3dgpu_grid_shape(const sl3dgpu_grid* grid, int* ntheta, int* nphi);
+/* SurfaceGrid::LMax (SurfaceGrid.hpp): the grid's degree bound, -1 for a null grid. */
+int sl3dgpu_grid_lmax(const sl3dgpu_grid* grid);
 /* The grid's FP64 Legendre contractions: 0 on the FP64 units, 1 emulated on
  * the tensor cores (seven BF16 slices a value under a power-of-two scale per
  * row and column, exact FP32 products, levels joined in FP64: about 49 bits
@@ -140,6 +142,31 @@ int sl3dgpu_synthesise_batch(sl3dgpu_grid* grid, const double* coeffs, int count
                              double* fields, void* stream);
 int sl3dgpu_expand_batch(sl3dgpu_grid* grid, const double* fields, int count, double* coeffs,
                          void* stream);
+
+/* ---- the sea-level equation (include/sl3dpp/SeaLevel.hpp, src/SeaLevel.cpp) -----
+ * GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) for a direct surface
+ * load on a body without rotational feedback (RotationalFeedback::None), in
+ * the solver's non-dimensional units: per-degree load Love numbers h, k
+ * (lmax + 1 each, the sums h_u + h_phi and k_u + k_phi the reference forms)
+ * and optionally the tangential l (may be null), surface gravity g, water
+ * density and the sea-floor radius; the ocean function and the direct load
+ * (sigma_d, the reference's GeneralisedForcing::directLoad) as device fields
+ * on the grid. The load's fixed point runs under Anderson mixing of its
+ * coefficients (anderson_memory columns, 0 for plain iteration) until the
+ * largest change of the ocean's sea level is at most rtol of its largest
+ * value (or max_iterations). Outputs are device fields; displacement,
+ * potential and tangential_potential may be null. */
+typedef struct sl3dgpu_sle_result {
+  double uniform_shift; /* Response::uniformShift: the conservation's uniform part, last formed */
+  double error;         /* Response::error: the last relative change of the ocean's sea level */
+  int iterations;       /* Response::iterations */
+  int converged;        /* Response::converged */
+} sl3dgpu_sle_result;
+int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const double* h, const double* k, const double* l, double g,
+                      double water_density, double radius, double rtol, int max_iterations, int anderson_memory,
+                      const double* ocean, const double* direct_load, double* sea_level_change,
+                      double* displacement, double* potential, double* tangential_potential,
+                      sl3dgpu_sle_result* result, void* stream);
 
 /* ---- the 3D viscoelastic step (include/sl3dpp/Viscoelastic3D.hpp:79-837) -----
  * A layered Earth (SI), each field linear in radius within its layer: the

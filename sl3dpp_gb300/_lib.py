@@ -45,6 +45,12 @@ class BandSystem(ctypes.Structure):
     ]
 
 
+class SleResult(ctypes.Structure):
+    """sl3dgpu_sle_result: GRDSolver::Response's scalars."""
+    _fields_ = [("uniform_shift", ctypes.c_double), ("error", ctypes.c_double), ("iterations", ctypes.c_int),
+                ("converged", ctypes.c_int)]
+
+
 class Sl3dgpuError(RuntimeError):
     """A failed sl3dgpu call (the reference's std::runtime_error and friends)."""
 
@@ -83,6 +89,10 @@ def lib() -> ctypes.CDLL:
         "sl3dgpu_grid_create": (c_int, [c_int, c_int, c_double, ctypes.POINTER(c_void_p)]),
         "sl3dgpu_grid_destroy": (None, [c_void_p]),
         "sl3dgpu_grid_shape": (c_int, [c_void_p, P_int, P_int]),
+        "sl3dgpu_grid_lmax": (c_int, [c_void_p]),
+        "sl3dgpu_sle_solve": (c_int, [c_void_p, P_double, P_double, P_double, c_double, c_double, c_double, c_double,
+                                      c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      ctypes.POINTER(SleResult), c_void_p]),
         "sl3dgpu_grid_set_fp64_emulation": (c_int, [c_void_p, c_int]),
         "sl3dgpu_grid_colatitudes": (c_int, [c_void_p, P_double, P_double]),
         "sl3dgpu_synthesise_spin_batch": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),

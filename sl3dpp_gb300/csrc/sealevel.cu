@@ -1,0 +1,374 @@
+// The sea-level equation's load fixed point on the GPU: GRDSolver::
+// SolveGeneralised (src/SeaLevel.cpp:397-736) for a direct surface load on a
+// body without rotational feedback (RotationalFeedback::None), in the
+// solver's non-dimensional units.
+//
+// Given per-degree load Love numbers h_l, k_l (and, optionally, the
+// tangential l_l), surface gravity g, water density rho_w, the sea-floor
+// radius a, an ocean function C and a direct load sigma_d on the surface grid:
+//
+//   A       = a^2 int C dOmega, 1/A (0 without an ocean)       (:570-574)
+//   s_mean  = -a^2 int sigma_d dOmega / (A rho_w)                (:577-581)
+//   L_0     = Expand(sigma_d + rho_w C s_mean)                   (:672-676)
+//   repeat  S    = Synthesise(-(h_l + k_l / g) L_lm)             (:625-631)
+//           S   += s_mean - a^2 int C S dOmega / A               (:655-661)
+//           stop when max|C S - C S_prev| <= rtol max|C S|       (:683-692)
+//           L   <- Anderson(L, Expand(sigma_d + rho_w C S))      (:694-699)
+//   then the displacement, potential and tangential potential as
+//   Synthesise(h_l L), Synthesise(k_l L), Synthesise(l_l L)      (:702-713).
+//
+// The transforms are the grid's (sht.cu), the mixer the Anderson sweeps of
+// the 3D step (step_kernels.cu) with the reference's memory and plain start;
+// the integrals sum each ring in a fixed tree and the rings in order (the
+// grid's Integrate, SurfaceGrid.hpp:257-267); the stopping test's maxima are
+// order-free. A few scalars per iteration come to the host: the integral, the
+// two maxima and the mixer's Gram column.
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "profile.cuh"
+#include "sl3dgpu.h"
+#include "step_kernels.cuh"
+#include "systems.cuh"
+
+namespace sl3dgpu {
+namespace {
+
+constexpr int kRingThreads = 256;
+
+// partial[j] = w_j sum_k a(j, k) [b(j, k)]: one block per ring, a fixed tree.
+__global__ void RingSumKernel(int nphi, const double* weights, const double* a, const double* b, double* partial) {
+  __shared__ double red[kRingThreads];
+  const int j = blockIdx.x;
+  const double* ra = a + static_cast<long long>(j) * nphi;
+  const double* rb = b ? b + static_cast<long long>(j) * nphi : nullptr;
+  double v = 0.0;
+  for (int k = threadIdx.x; k < nphi; k += blockDim.x) v += rb ? ra[k] * rb[k] : ra[k];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s /= 2) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[j] = weights[j] * red[0];
+}
+
+// out[x] = f[l] in[x] over the (l, m >= 0) coefficients, Index(l, m) = l(l+1)/2 + m.
+__global__ void ScaleDegreesKernel(int lmax, const double* f, const double2* in, double2* out) {
+  const long long count = static_cast<long long>(lmax + 1) * (lmax + 2) / 2;
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i >= count) return;
+  int l = static_cast<int>((sqrt(8.0 * static_cast<double>(i) + 1.0) - 1.0) * 0.5);
+  while (static_cast<long long>(l) * (l + 1) / 2 > i) --l;
+  while (static_cast<long long>(l + 1) * (l + 2) / 2 <= i) ++l;
+  const double2 v = in[i];
+  out[i] = make_double2(f[l] * v.x, f[l] * v.y);
+}
+
+// seeded[x] = sigma_d[x] + rho_w C[x] s_mean
+__global__ void SeedKernel(long long n, const double* direct, const double* ocean, double rhoMean, double* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < n) out[i] = direct[i] + rhoMean * ocean[i];
+}
+
+// S += shift; C S; the next load sigma_d + rho_w C S; per block the largest
+// |C S - C S_prev| and |C S| (blockIdx-ordered partials), C S kept for the next test.
+__global__ void ShiftAndLoadKernel(long long n, double shift, double rho, const double* direct, const double* ocean,
+                                   double* slc, double* oceanSlc, double* newLoad, bool havePrev, double* maxima) {
+  __shared__ double red[2][kRingThreads];
+  double dmax = 0.0, smax = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double s = slc[i] + shift;
+    slc[i] = s;
+    const double cs = ocean[i] * s;
+    if (havePrev) dmax = fmax(dmax, fabs(cs - oceanSlc[i]));
+    smax = fmax(smax, fabs(cs));
+    oceanSlc[i] = cs;
+    newLoad[i] = direct[i] + rho * cs;
+  }
+  red[0][threadIdx.x] = dmax;
+  red[1][threadIdx.x] = smax;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s /= 2) {
+    if (threadIdx.x < s) {
+      red[0][threadIdx.x] = fmax(red[0][threadIdx.x], red[0][threadIdx.x + s]);
+      red[1][threadIdx.x] = fmax(red[1][threadIdx.x], red[1][threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    maxima[2 * blockIdx.x] = red[0][0];
+    maxima[2 * blockIdx.x + 1] = red[1][0];
+  }
+}
+
+// per block the largest |a|
+__global__ void MaxAbsKernel(long long n, const double* a, double* maxima) {
+  __shared__ double red[kRingThreads];
+  double v = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    v = fmax(v, fabs(a[i]));
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s /= 2) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) maxima[2 * blockIdx.x + 1] = red[0];
+}
+
+constexpr int kMaxBlocks = 304;  // two a multiprocessor for the pointwise pass
+
+struct SleRun {
+  sl3dgpu_grid* grid;
+  cudaStream_t stream;
+  int lmax = 0, ntheta = 0, nphi = 0;
+  long long fieldSize = 0, coefCount = 0;
+  double r2 = 0.0, dphi = 0.0;
+  Dev<double> weights, ringPartial, maxima, loadLm, newLoadLm, scaledLm, factors;
+  Dev<double> seeded, slc, oceanSlc, newLoad;
+  std::vector<double> hostRing, hostMaxima;
+
+  // a^2 int a (b) dOmega, the rings in order
+  int Integrate(const double* a, const double* b, double* out) {
+    RingSumKernel<<<ntheta, kRingThreads, 0, stream>>>(nphi, weights.p, a, b, ringPartial.p);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(hostRing.data(), ringPartial.p, ntheta * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    double sum = 0.0;
+    for (int j = 0; j < ntheta; ++j) sum += hostRing[j];
+    *out = r2 * sum * dphi;
+    return SL3DGPU_OK;
+  }
+
+  // field = Synthesise(f_l coefficients)
+  int SynthesiseScaled(const double* f, const double* coeffs, double* field) {
+    SL3D_CUDA(cudaMemcpyAsync(factors.p, f, (lmax + 1) * sizeof(double), cudaMemcpyHostToDevice, stream));
+    const unsigned blocks = static_cast<unsigned>((coefCount + 255) / 256);
+    ScaleDegreesKernel<<<blocks, 256, 0, stream>>>(lmax, factors.p, reinterpret_cast<const double2*>(coeffs),
+                                                   reinterpret_cast<double2*>(scaledLm.p));
+    SL3D_CHECK_LAUNCH();
+    return sl3dgpu_synthesise_batch(grid, scaledLm.p, 1, field, stream);
+  }
+};
+
+// The Anderson mixer of the load coefficients (AndersonMixer::Update, the
+// reference's plain form: the first call the image, then memory columns).
+struct LoadMixer {
+  int memory = 0, count = 0, slot = 0;
+  bool first = true;
+  std::vector<Dev<double>> dG, dF;
+  Dev<double*> dGPtr, dFPtr;
+  Dev<double> xPrev, fPrev, partial, sums, gamma;
+  std::vector<double> gram, hostSums;
+
+  int Init(int m, long long n) {
+    memory = m;
+    if (memory <= 0) return SL3DGPU_OK;
+    dG.resize(memory);
+    dF.resize(memory);
+    std::vector<double*> gp(memory), fp(memory);
+    for (int i = 0; i < memory; ++i) {
+      SL3D_CUDA(dG[i].Alloc(n));
+      SL3D_CUDA(dF[i].Alloc(n));
+      gp[i] = dG[i].p;
+      fp[i] = dF[i].p;
+    }
+    SL3D_CUDA(dGPtr.Upload(gp));
+    SL3D_CUDA(dFPtr.Upload(fp));
+    SL3D_CUDA(xPrev.Alloc(n));
+    SL3D_CUDA(fPrev.Alloc(n));
+    SL3D_CUDA(partial.Alloc(static_cast<size_t>(1024) * 2 * kMixMaxMemory));
+    SL3D_CUDA(sums.Alloc(2 * kMixMaxMemory));
+    SL3D_CUDA(gamma.Alloc(kMixMaxMemory + 1));
+    gram.assign(static_cast<size_t>(memory) * memory, 0.0);
+    hostSums.assign(4 * kMixMaxMemory, 0.0);
+    return SL3DGPU_OK;
+  }
+
+  // x <- the mixed iterate from x and its image gx
+  int Update(double* x, const double* gx, long long n, cudaStream_t stream) {
+    if (memory <= 0) {
+      SL3D_CUDA(cudaMemcpyAsync(x, gx, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+      return SL3DGPU_OK;
+    }
+    MixerArgs a{};
+    a.n = n;
+    a.memory = memory;
+    a.x = x;
+    a.gx = gx;
+    a.xPrev = xPrev.p;
+    a.fPrev = fPrev.p;
+    a.dG = dGPtr.p;
+    a.dF = dFPtr.p;
+    a.partial = partial.p;
+    a.blocks = static_cast<int>(std::min<long long>(1024, n));
+    a.gamma = gamma.p;
+    if (first) {
+      LaunchMixerFirst(a, stream);
+      SL3D_CHECK_LAUNCH();
+      first = false;
+      return SL3DGPU_OK;
+    }
+    a.slot = slot;
+    a.m = std::min(count + 1, memory);
+    LaunchMixerSweep(a, sums.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(hostSums.data(), sums.p, 2 * kMixMaxMemory * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    double* g = hostSums.data() + 2 * kMixMaxMemory;
+    MixerSolve(gram.data(), a.m, a.slot, a.memory, hostSums.data(), g);
+    SL3D_CUDA(cudaMemcpyAsync(gamma.p, g, (a.m + 1) * sizeof(double), cudaMemcpyHostToDevice, stream));
+    LaunchMixerMix(a, stream);
+    SL3D_CHECK_LAUNCH();
+    count = a.m;
+    slot = (slot + 1) % memory;
+    return SL3DGPU_OK;
+  }
+};
+
+}  // namespace
+}  // namespace sl3dgpu
+
+using namespace sl3dgpu;
+
+extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const double* h, const double* k, const double* lt, double g,
+                                 double water_density, double radius, double rtol, int max_iterations,
+                                 int anderson_memory, const double* ocean, const double* direct_load,
+                                 double* sea_level_change, double* displacement, double* potential,
+                                 double* tangential_potential, sl3dgpu_sle_result* result, void* stream) {
+  if (grid == nullptr || h == nullptr || k == nullptr || ocean == nullptr || direct_load == nullptr ||
+      sea_level_change == nullptr || result == nullptr) {
+    SetError("sle: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (!(g > 0.0) || !(water_density > 0.0) || !(radius > 0.0) || !(rtol >= 0.0) || max_iterations < 0 ||
+      anderson_memory < 0 || anderson_memory > kMixMaxMemory) {
+    SetError("sle: g, water_density and radius > 0, rtol >= 0, max_iterations >= 0, anderson_memory in [0, 16]");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SleRun run;
+  run.grid = grid;
+  run.stream = AsStream(stream);
+  int ntheta = 0, nphi = 0;
+  SL3D_TRY(sl3dgpu_grid_shape(grid, &ntheta, &nphi));
+  run.lmax = sl3dgpu_grid_lmax(grid);
+  if (run.lmax < 0) return SL3DGPU_ERR_ARGUMENT;
+  run.ntheta = ntheta;
+  run.nphi = nphi;
+  run.fieldSize = static_cast<long long>(ntheta) * nphi;
+  run.coefCount = static_cast<long long>(run.lmax + 1) * (run.lmax + 2) / 2;
+  run.r2 = radius * radius;
+  run.dphi = 2.0 * 3.14159265358979323846 / nphi;
+  std::vector<double> theta(ntheta), w(ntheta);
+  SL3D_TRY(sl3dgpu_grid_colatitudes(grid, theta.data(), w.data()));
+  SL3D_CUDA(run.weights.Upload(w));
+  SL3D_CUDA(run.ringPartial.Alloc(ntheta));
+  run.hostRing.assign(ntheta, 0.0);
+  const int blocks = static_cast<int>(std::min<long long>(kMaxBlocks, (run.fieldSize + 255) / 256));
+  SL3D_CUDA(run.maxima.Alloc(2 * blocks));
+  run.hostMaxima.assign(2 * blocks, 0.0);
+  for (auto* d : {&run.loadLm, &run.newLoadLm, &run.scaledLm}) SL3D_CUDA(d->Alloc(2 * run.coefCount));
+  SL3D_CUDA(run.factors.Alloc(run.lmax + 1));
+  for (auto* d : {&run.seeded, &run.slc, &run.oceanSlc, &run.newLoad}) SL3D_CUDA(d->Alloc(run.fieldSize));
+  const cudaStream_t s = run.stream;
+  const int L = run.lmax;
+  std::vector<double> slcFactor(L + 1);
+  for (int l = 0; l <= L; ++l) slcFactor[l] = -(h[l] + k[l] / g);
+
+  *result = sl3dgpu_sle_result{0.0, 0.0, 0, 1};
+  auto zero = [&](double* f) -> int {
+    if (f) SL3D_CUDA(cudaMemsetAsync(f, 0, run.fieldSize * sizeof(double), s));
+    return SL3DGPU_OK;
+  };
+  // Without a load there is nothing to solve (the reference's !anyForcing).
+  double loadIntegral = 0.0, loadScale = 0.0;
+  SL3D_TRY(run.Integrate(direct_load, nullptr, &loadIntegral));
+  {
+    MaxAbsKernel<<<blocks, kRingThreads, 0, s>>>(run.fieldSize, direct_load, run.maxima.p);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(run.hostMaxima.data(), run.maxima.p, 2 * blocks * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+    SL3D_CUDA(cudaStreamSynchronize(s));
+    for (int b = 0; b < blocks; ++b) loadScale = std::max(loadScale, run.hostMaxima[2 * b + 1]);
+  }
+  if (loadScale == 0.0) {
+    SL3D_TRY(zero(sea_level_change));
+    SL3D_TRY(zero(displacement));
+    SL3D_TRY(zero(potential));
+    SL3D_TRY(zero(tangential_potential));
+    return SL3DGPU_OK;
+  }
+  double oceanArea = 0.0;
+  SL3D_TRY(run.Integrate(ocean, nullptr, &oceanArea));
+  const double perOceanArea = oceanArea > 0.0 ? 1.0 / oceanArea : 0.0;
+  const double meanSlc = -loadIntegral * perOceanArea / water_density;
+
+  // the seed: sigma_d + rho_w C s_mean, expanded
+  {
+    const unsigned b = static_cast<unsigned>((run.fieldSize + 255) / 256);
+    SeedKernel<<<b, 256, 0, s>>>(run.fieldSize, direct_load, ocean, water_density * meanSlc, run.seeded.p);
+    SL3D_CHECK_LAUNCH();
+  }
+  SL3D_TRY(sl3dgpu_expand_batch(grid, run.seeded.p, 1, run.loadLm.p, s));
+
+  LoadMixer mixer;
+  SL3D_TRY(mixer.Init(anderson_memory, 2 * run.coefCount));
+  double err = INFINITY, shift = 0.0;
+  bool converged = false, havePrev = false;
+  int count = 0;
+  while (count < max_iterations) {
+    // the sea level change of the load, its uniform part by conservation
+    SL3D_TRY(run.SynthesiseScaled(slcFactor.data(), run.loadLm.p, run.slc.p));
+    double cs = 0.0;
+    SL3D_TRY(run.Integrate(ocean, run.slc.p, &cs));
+    shift = meanSlc - cs * perOceanArea;
+    ShiftAndLoadKernel<<<blocks, kRingThreads, 0, s>>>(run.fieldSize, shift, water_density, direct_load, ocean,
+                                                       run.slc.p, run.oceanSlc.p, run.newLoad.p, havePrev,
+                                                       run.maxima.p);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(run.hostMaxima.data(), run.maxima.p, 2 * blocks * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+    SL3D_CUDA(cudaStreamSynchronize(s));
+    if (havePrev) {
+      double diff = 0.0, scale = 0.0;
+      for (int b = 0; b < blocks; ++b) {
+        diff = std::max(diff, run.hostMaxima[2 * b]);
+        scale = std::max(scale, run.hostMaxima[2 * b + 1]);
+      }
+      err = scale > 0.0 ? diff / scale : 0.0;
+      if (err <= rtol) {
+        converged = true;
+        break;
+      }
+    }
+    havePrev = true;
+    SL3D_TRY(sl3dgpu_expand_batch(grid, run.newLoad.p, 1, run.newLoadLm.p, s));
+    SL3D_TRY(mixer.Update(run.loadLm.p, run.newLoadLm.p, 2 * run.coefCount, s));
+    ++count;
+  }
+  // the sea level change is the last one formed; the other fields from the load it came from
+  SL3D_CUDA(cudaMemcpyAsync(sea_level_change, run.slc.p, run.fieldSize * sizeof(double), cudaMemcpyDeviceToDevice,
+                            s));
+  if (displacement) SL3D_TRY(run.SynthesiseScaled(h, run.loadLm.p, displacement));
+  if (potential) SL3D_TRY(run.SynthesiseScaled(k, run.loadLm.p, potential));
+  if (tangential_potential) {
+    if (lt) {
+      std::vector<double> tan(lt, lt + L + 1);
+      tan[0] = 0.0;  // a degree-0 field has no tangential part
+      SL3D_TRY(run.SynthesiseScaled(tan.data(), run.loadLm.p, tangential_potential));
+    } else {
+      SL3D_TRY(zero(tangential_potential));
+    }
+  }
+  SL3D_CUDA(cudaStreamSynchronize(s));
+  *result = sl3dgpu_sle_result{shift, err, count, converged ? 1 : 0};
+  return SL3DGPU_OK;
+}

@@ -1216,6 +1216,14 @@ extern "C" int sl3dgpu_grid_create(int lmax, int nmax, double oversampling, sl3d
 
 extern "C" void sl3dgpu_grid_destroy(sl3dgpu_grid* grid) { delete grid; }
 
+extern "C" int sl3dgpu_grid_lmax(const sl3dgpu_grid* grid) {
+  if (grid == nullptr) {
+    SetError("null grid");
+    return -1;
+  }
+  return grid->grid->lmax;
+}
+
 extern "C" int sl3dgpu_grid_shape(const sl3dgpu_grid* grid, int* ntheta, int* nphi) {
   if (grid == nullptr) {
     SetError("null grid");

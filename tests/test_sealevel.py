@@ -1,0 +1,112 @@
+"""The sea-level equation's load fixed point (GRDSolver::SolveGeneralised,
+src/SeaLevel.cpp:397-736, direct load, no rotational feedback): the oracle's
+numpy restatement checked on the reference's structural identities
+(tests/TestSeaLevel.cpp:135-206: the rigid-earth eustatic limit, the ocean
+gaining the mass the load lost), then the GPU solver against the oracle and
+the same identities. Synthetic Love numbers and state; non-dimensional."""
+
+import numpy as np
+import pytest
+
+from oracle import sealevel as sle_oracle
+from tests import _oracle
+
+
+def problem(lmax, rigid=False, ocean_on=True):
+    theta, w, nphi = _oracle.grid(lmax, 1.0)
+    tt, pp = np.meshgrid(theta, 2 * np.pi * np.arange(nphi) / nphi, indexing="ij")
+    ocean = (np.cos(tt) < 0.4 + 0.2 * np.sin(2 * pp)).astype(np.float64).ravel()
+    if not ocean_on:
+        ocean[:] = 0.0
+    land = 1.0 - (np.cos(tt) < 0.4 + 0.2 * np.sin(2 * pp)).astype(np.float64)
+    load = (-0.5 * np.exp(-(((tt - 0.3) / 0.2) ** 2)) * (1.0 + 0.3 * np.cos(pp)) * land).ravel()
+    degrees = np.arange(lmax + 1, dtype=np.float64)
+    h = np.where(degrees > 0, -1.2 / (degrees + 1.0), 0.0)
+    k = np.where(degrees > 0, -0.5 / (degrees + 1.0), 0.0)
+    lt = np.where(degrees > 0, 0.3 / (degrees + 1.0), 0.0)
+    if rigid:
+        h[:] = k[:] = lt[:] = 0.0
+    synth = lambda c: _oracle.synthesise_real(lmax, theta, nphi, c)
+    expand = lambda f: _oracle.expand_real(lmax, theta, w, nphi, f)
+    integ = lambda f: float(np.sum(w * f.reshape(theta.size, nphi).sum(axis=1)) * 2 * np.pi / nphi)
+    return dict(theta=theta, w=w, nphi=nphi, ocean=ocean, load=load, h=h, k=k, lt=lt, synth=synth,
+                expand=expand, integ=integ)
+
+
+def oracle_solve(p, **kw):
+    return sle_oracle.solve_generalised(p["synth"], p["expand"], p["integ"], p["h"], p["k"], p["lt"], 1.0, 1.0, 1.0,
+                                        p["ocean"], p["load"], **kw)
+
+
+def test_oracle_rigid_earth_is_the_eustatic_value():
+    p = problem(12, rigid=True)
+    r = oracle_solve(p, rtol=1e-12, max_iterations=50)
+    eustatic = -p["integ"](p["load"]) / p["integ"](p["ocean"])  # rho_w = a = 1
+    assert r["converged"]
+    assert np.max(np.abs(r["sea_level_change"] - eustatic)) < 1e-12 * abs(eustatic)
+    assert np.max(np.abs(r["displacement"])) == 0.0
+
+
+def test_oracle_ocean_gains_the_mass_the_load_lost():
+    p = problem(16)
+    r = oracle_solve(p, rtol=1e-12, max_iterations=200)
+    assert r["converged"] and r["iterations"] < 60
+    gained = p["integ"](p["ocean"] * r["sea_level_change"])
+    assert abs(gained + p["integ"](p["load"])) < 1e-10 * abs(p["integ"](p["load"]))
+    # the fingerprint's shape: far-field rise, near-field fall
+    s = r["sea_level_change"]
+    assert s.min() < 0.0 < s.max()
+
+
+def _gpu_solve(gpu, p, lmax, **kw):
+    import torch
+
+    from sl3dpp_gb300.grid import SurfaceGrid
+    from sl3dpp_gb300.sealevel import SeaLevelSolver
+
+    grid = SurfaceGrid(lmax, 0, 1.0)
+    assert grid.ntheta == p["theta"].size and grid.nphi == p["nphi"]
+    solver = SeaLevelSolver(grid, p["h"], p["k"], p["lt"], 1.0, 1.0, 1.0)
+    r = solver.solve_generalised(torch.tensor(p["ocean"], device=gpu), torch.tensor(p["load"], device=gpu), **kw)
+    return {k: (v.cpu().numpy() if hasattr(v, "cpu") else v) for k, v in r.items()}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lmax,memory", [(16, 5), (24, 5), (24, 0)])
+def test_gpu_sea_level_matches_oracle(gpu, lmax, memory):
+    p = problem(lmax)
+    want = oracle_solve(p, rtol=1e-11, max_iterations=300, anderson_memory=memory)
+    got = _gpu_solve(gpu, p, lmax, rtol=1e-11, max_iterations=300, anderson_memory=memory)
+    assert want["converged"] and got["converged"]
+    assert got["iterations"] == want["iterations"]
+    for key in ("sea_level_change", "displacement", "potential", "tangential_potential"):
+        scale = np.max(np.abs(want[key]))
+        assert np.max(np.abs(got[key] - want[key])) < 1e-10 * scale, key
+    assert abs(got["uniform_shift"] - want["uniform_shift"]) < 1e-10 * abs(want["uniform_shift"])
+
+
+@pytest.mark.gpu
+def test_gpu_sea_level_identities(gpu):
+    lmax = 20
+    rigid = problem(lmax, rigid=True)
+    r = _gpu_solve(gpu, rigid, lmax, rtol=1e-12, max_iterations=50)
+    eustatic = -rigid["integ"](rigid["load"]) / rigid["integ"](rigid["ocean"])
+    assert r["converged"]
+    assert np.max(np.abs(r["sea_level_change"] - eustatic)) < 1e-11 * abs(eustatic)
+    assert np.max(np.abs(r["displacement"])) < 1e-15
+    p = problem(lmax)
+    r = _gpu_solve(gpu, p, lmax, rtol=1e-12, max_iterations=200)
+    gained = p["integ"](p["ocean"] * r["sea_level_change"])
+    assert abs(gained + p["integ"](p["load"])) < 1e-10 * abs(p["integ"](p["load"]))
+    # no load: nothing to solve, zero fields (the reference's !anyForcing)
+    p0 = dict(p, load=np.zeros_like(p["load"]))
+    r = _gpu_solve(gpu, p0, lmax)
+    assert r["converged"] and r["iterations"] == 0
+    assert np.max(np.abs(r["sea_level_change"])) == 0.0
+    # no ocean: no water to conserve, the load alone (no shift)
+    dry = problem(lmax, ocean_on=False)
+    r = _gpu_solve(gpu, dry, lmax, rtol=1e-12, max_iterations=20)
+    want = oracle_solve(dry, rtol=1e-12, max_iterations=20)
+    assert r["uniform_shift"] == 0.0 and r["converged"] and r["iterations"] == want["iterations"]
+    assert np.max(np.abs(r["sea_level_change"] - want["sea_level_change"])) < 1e-12 * np.max(
+        np.abs(want["sea_level_change"]))
