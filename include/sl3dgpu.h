@@ -144,29 +144,53 @@ int sl3dgpu_expand_batch(sl3dgpu_grid* grid, const double* fields, int count, do
                          void* stream);
 
 /* ---- the sea-level equation (include/sl3dpp/SeaLevel.hpp, src/SeaLevel.cpp) -----
- * GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) for a direct surface
- * load on a body without rotational feedback (RotationalFeedback::None), in
- * the solver's non-dimensional units: per-degree load Love numbers h, k
- * (lmax + 1 each, the sums h_u + h_phi and k_u + k_phi the reference forms)
- * and optionally the tangential l (may be null), surface gravity g, water
- * density and the sea-floor radius; the ocean function and the direct load
- * (sigma_d, the reference's GeneralisedForcing::directLoad) as device fields
- * on the grid. The load's fixed point runs under Anderson mixing of its
- * coefficients (anderson_memory columns, 0 for plain iteration) until the
+ * GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) without rotational
+ * feedback (RotationalFeedback::None), in the solver's non-dimensional units,
+ * for the forcing channels of the coupled Evolution3D closure
+ * (src/Evolution3D.cpp:320-333). The body: per-degree load Love numbers h, k
+ * (lmax + 1 each: the sums h_u + h_phi and k_u + k_phi the reference's
+ * constructor forms, src/SeaLevel.cpp:163-171), the tangential l (may be
+ * null), the tidal ht, kt, lt (may be null without a tide), surface gravity,
+ * water density and the sea-floor radius; host arrays. The forcing:
+ * GeneralisedForcing's channels as device arrays, each may be null -- fields
+ * on the grid (directLoad, directLoadOutsideWaterBudget, solidSurfaceChange)
+ * or (l, m >= 0) complex coefficients as (re, im) pairs (the ready
+ * displacement, potential, tangential and toroidal responses, the tide,
+ * degrees 2 and up). The load's fixed point runs under Anderson mixing of
+ * its coefficients (anderson_memory columns, 0 for plain iteration) until the
  * largest change of the ocean's sea level is at most rtol of its largest
- * value (or max_iterations). Outputs are device fields; displacement,
- * potential and tangential_potential may be null. */
+ * value (or max_iterations). Outputs are device fields; all but
+ * sea_level_change may be null. */
+typedef struct sl3dgpu_sle_body {
+  const double* h;
+  const double* k;
+  const double* l;
+  const double* ht;
+  const double* kt;
+  const double* lt;
+  double g, water_density, radius;
+} sl3dgpu_sle_body;
+typedef struct sl3dgpu_sle_forcing {
+  const double* direct_load;            /* field: in the water budget */
+  const double* direct_load_outside;    /* field: outside it */
+  const double* solid_surface_change;   /* field: a layer on the solid surface */
+  const double* displacement_response;  /* coefficients */
+  const double* potential_response;
+  const double* tangential_response;
+  const double* toroidal_response;      /* carried to the response alone */
+  const double* tide;                   /* coefficients, degrees >= 2 */
+} sl3dgpu_sle_forcing;
 typedef struct sl3dgpu_sle_result {
   double uniform_shift; /* Response::uniformShift: the conservation's uniform part, last formed */
   double error;         /* Response::error: the last relative change of the ocean's sea level */
   int iterations;       /* Response::iterations */
   int converged;        /* Response::converged */
 } sl3dgpu_sle_result;
-int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const double* h, const double* k, const double* l, double g,
-                      double water_density, double radius, double rtol, int max_iterations, int anderson_memory,
-                      const double* ocean, const double* direct_load, double* sea_level_change,
-                      double* displacement, double* potential, double* tangential_potential,
-                      sl3dgpu_sle_result* result, void* stream);
+int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
+                      const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations, int anderson_memory,
+                      double* sea_level_change, double* displacement, double* potential,
+                      double* tangential_potential, double* toroidal_potential, sl3dgpu_sle_result* result,
+                      void* stream);
 
 /* ---- the 3D viscoelastic step (include/sl3dpp/Viscoelastic3D.hpp:79-837) -----
  * A layered Earth (SI), each field linear in radius within its layer: the

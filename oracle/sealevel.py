@@ -62,36 +62,76 @@ class AndersonMixer:
         return gx - gamma @ self.dG[:m]
 
 
-def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density, radius, ocean, direct_load,
-                      rtol=1e-9, max_iterations=1000, anderson_memory=5):
-    """The load fixed point of the sea-level equation (SeaLevel.cpp:563-713
-    with no static terms, tide, layer or rotation). synthesise(coeffs) and
-    expand(field) are the grid's real transforms in the reference's (l, m >= 0)
-    layout, integrate(field) its quadrature over the unit sphere."""
+def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density, radius, ocean, direct_load=None,
+                      rtol=1e-9, max_iterations=1000, anderson_memory=5, direct_load_outside=None,
+                      solid_surface_change=None, displacement_response=None, potential_response=None,
+                      tangential_response=None, toroidal_response=None, tide=None, ht=None, kt=None, lt_tide=None):
+    """The load fixed point of the sea-level equation (SeaLevel.cpp:397-736
+    with RotationalFeedback::None) for the channels the coupled Evolution3D
+    closure uses. synthesise(coeffs) and expand(field) are the grid's real
+    transforms in the reference's (l, m >= 0) layout, integrate(field) its
+    quadrature over the unit sphere."""
     h = np.asarray(h, dtype=np.float64)
     k = np.asarray(k, dtype=np.float64)
     lmax = h.size - 1
     degree = np.concatenate([np.full(l + 1, l) for l in range(lmax + 1)])
+    ncoef = degree.size
+    size = ocean.size
     out = {"uniform_shift": 0.0, "iterations": 0, "error": 0.0, "converged": True}
-    zeros = np.zeros_like(direct_load)
-    if np.max(np.abs(direct_load)) == 0.0:  # no forcing (:562)
-        out.update(sea_level_change=zeros, displacement=zeros, potential=zeros, tangential_potential=zeros)
+    nz = lambda a: a is not None and np.max(np.abs(a)) > 0.0
+    # the toroidal potential is carried, whatever else is solved (:561-563)
+    toroidal = synthesise(toroidal_response) if toroidal_response is not None else np.zeros(size)
+    any_static = nz(displacement_response) or nz(potential_response) or nz(tide) or nz(solid_surface_change)
+    any_tan = nz(displacement_response) or nz(potential_response) or nz(tangential_response) or nz(tide)
+    if not (nz(direct_load) or nz(direct_load_outside) or any_static or any_tan):
+        zeros = np.zeros(size)
+        out.update(sea_level_change=zeros, displacement=zeros, potential=zeros, tangential_potential=zeros,
+                   toroidal_potential=toroidal)
         return out
+    zc = np.zeros(ncoef, dtype=np.complex128)
+    static_disp, static_grav, static_tan = zc.copy(), zc.copy(), zc.copy()
+    if nz(displacement_response):
+        static_disp += displacement_response
+    if nz(potential_response):
+        static_grav += potential_response
+    if nz(tangential_response):
+        static_tan += tangential_response
+    if nz(tide):  # :533-545
+        lt_t = np.zeros(lmax + 1) if lt_tide is None else np.array(lt_tide, dtype=np.float64)
+        ht_, kt_ = np.array(ht, dtype=np.float64), np.array(kt, dtype=np.float64)
+        ht_[0] = kt_[0] = lt_t[0] = 0.0
+        static_disp += ht_[degree] * tide
+        static_grav += kt_[degree] * tide
+        static_tan += lt_t[degree] * tide
+    static_slc = -(static_disp + static_grav / g)  # :590-600
+    if nz(tide):
+        static_slc -= tide / g
+    if nz(solid_surface_change):
+        static_slc -= expand(solid_surface_change)
     surface = lambda f: radius * radius * integrate(f)  # IntegrateSurface
     ocean_area = surface(ocean)
     per_area = 1.0 / ocean_area if ocean_area > 0.0 else 0.0  # InverseOceanArea
-    mean_slc = -surface(direct_load) * per_area / water_density
+    direct = np.zeros(size)
+    mean_slc = 0.0
+    if direct_load is not None:
+        direct = direct_load.copy()
+        mean_slc = -surface(direct_load) * per_area / water_density
+    if direct_load_outside is not None:
+        direct = direct + direct_load_outside
     slc_factor = -(h + k / g)
-    load_lm = expand(direct_load + water_density * ocean * mean_slc)
+    load_lm = expand(direct + water_density * ocean * mean_slc)
     mixer = AndersonMixer(anderson_memory)
     prev = None
-    slc = zeros
+    slc = np.zeros(size)
     err = np.inf
     converged = False
     count = 0
     shift = 0.0
     while count < max_iterations:
-        slc = synthesise(slc_factor[degree] * load_lm)
+        lm = slc_factor[degree] * load_lm
+        if any_static:
+            lm = lm + static_slc
+        slc = synthesise(lm)
         shift = mean_slc - surface(ocean * slc) * per_area
         slc = slc + shift
         ocean_slc = ocean * slc
@@ -102,13 +142,14 @@ def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density,
                 converged = True
                 break
         prev = ocean_slc
-        new_lm = expand(direct_load + water_density * prev)
+        new_lm = expand(direct + water_density * prev)
         mixed = mixer.update(load_lm.view(np.float64), new_lm.view(np.float64))
         load_lm = mixed.view(np.complex128)
         count += 1
     tan = np.zeros(lmax + 1) if lt is None else np.array(lt, dtype=np.float64)
     tan[0] = 0.0
-    out.update(sea_level_change=slc, displacement=synthesise(h[degree] * load_lm),
-               potential=synthesise(k[degree] * load_lm), tangential_potential=synthesise(tan[degree] * load_lm),
+    out.update(sea_level_change=slc, displacement=synthesise(h[degree] * load_lm + static_disp),
+               potential=synthesise(k[degree] * load_lm + static_grav),
+               tangential_potential=synthesise(tan[degree] * load_lm + static_tan), toroidal_potential=toroidal,
                uniform_shift=shift, iterations=count, error=err, converged=converged)
     return out

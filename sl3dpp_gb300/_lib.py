@@ -45,6 +45,20 @@ class BandSystem(ctypes.Structure):
     ]
 
 
+class SleBody(ctypes.Structure):
+    """sl3dgpu_sle_body: the solver's Love numbers (host arrays) and constants."""
+    _fields_ = [("h", P_double), ("k", P_double), ("l", P_double), ("ht", P_double), ("kt", P_double),
+                ("lt", P_double), ("g", ctypes.c_double), ("water_density", ctypes.c_double),
+                ("radius", ctypes.c_double)]
+
+
+class SleForcing(ctypes.Structure):
+    """sl3dgpu_sle_forcing: GeneralisedForcing's channels (device pointers or null)."""
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("direct_load", "direct_load_outside", "solid_surface_change", "displacement_response",
+                 "potential_response", "tangential_response", "toroidal_response", "tide")]
+
+
 class SleResult(ctypes.Structure):
     """sl3dgpu_sle_result: GRDSolver::Response's scalars."""
     _fields_ = [("uniform_shift", ctypes.c_double), ("error", ctypes.c_double), ("iterations", ctypes.c_int),
@@ -90,8 +104,8 @@ def lib() -> ctypes.CDLL:
         "sl3dgpu_grid_destroy": (None, [c_void_p]),
         "sl3dgpu_grid_shape": (c_int, [c_void_p, P_int, P_int]),
         "sl3dgpu_grid_lmax": (c_int, [c_void_p]),
-        "sl3dgpu_sle_solve": (c_int, [c_void_p, P_double, P_double, P_double, c_double, c_double, c_double, c_double,
-                                      c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+        "sl3dgpu_sle_solve": (c_int, [c_void_p, ctypes.POINTER(SleBody), c_void_p, ctypes.POINTER(SleForcing),
+                                      c_double, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       ctypes.POINTER(SleResult), c_void_p]),
         "sl3dgpu_grid_set_fp64_emulation": (c_int, [c_void_p, c_int]),
         "sl3dgpu_grid_colatitudes": (c_int, [c_void_p, P_double, P_double]),

@@ -1,21 +1,28 @@
 // The sea-level equation's load fixed point on the GPU: GRDSolver::
-// SolveGeneralised (src/SeaLevel.cpp:397-736) for a direct surface load on a
-// body without rotational feedback (RotationalFeedback::None), in the
-// solver's non-dimensional units.
+// SolveGeneralised (src/SeaLevel.cpp:397-736) without rotational feedback
+// (RotationalFeedback::None), in the solver's non-dimensional units, for the
+// forcing channels the coupled Evolution3D closure uses
+// (src/Evolution3D.cpp:320-333): the direct load in and outside the water
+// budget, a layer on the solid surface, a prescribed tide, and the ready
+// displacement, potential and tangential responses.
 //
-// Given per-degree load Love numbers h_l, k_l (and, optionally, the
-// tangential l_l), surface gravity g, water density rho_w, the sea-floor
-// radius a, an ocean function C and a direct load sigma_d on the surface grid:
+// With per-degree load Love numbers h_l, k_l (l_l tangential), tidal ones,
+// surface gravity g, water density rho_w, the sea-floor radius a, an ocean
+// function C and the direct load sigma_d on the surface grid:
 //
+//   static  D_s = R_u + h^t T,  G_s = R_phi + k^t T,  V_s = R_v + l^t T
+//           S_s = -(D_s + G_s / g) - T / g - Expand(layer)      (:520-545, :586-600)
 //   A       = a^2 int C dOmega, 1/A (0 without an ocean)       (:570-574)
 //   s_mean  = -a^2 int sigma_d dOmega / (A rho_w)                (:577-581)
-//   L_0     = Expand(sigma_d + rho_w C s_mean)                   (:672-676)
-//   repeat  S    = Synthesise(-(h_l + k_l / g) L_lm)             (:625-631)
+//   sigma   = sigma_d + sigma_outside                             (:582-587)
+//   L_0     = Expand(sigma + rho_w C s_mean)                     (:672-676)
+//   repeat  S    = Synthesise(-(h_l + k_l / g) L_lm + S_s)       (:625-634)
 //           S   += s_mean - a^2 int C S dOmega / A               (:655-661)
 //           stop when max|C S - C S_prev| <= rtol max|C S|       (:683-692)
-//           L   <- Anderson(L, Expand(sigma_d + rho_w C S))      (:694-699)
+//           L   <- Anderson(L, Expand(sigma + rho_w C S))        (:694-699)
 //   then the displacement, potential and tangential potential as
-//   Synthesise(h_l L), Synthesise(k_l L), Synthesise(l_l L)      (:702-713).
+//   Synthesise(h_l L + D_s), Synthesise(k_l L + G_s), Synthesise(l_l L + V_s)
+//   (:702-720), the toroidal response carried as Synthesise(R_w).
 //
 // The transforms are the grid's (sht.cu), the mixer the Anderson sweeps of
 // the 3D step (step_kernels.cu) with the reference's memory and plain start;
@@ -56,8 +63,10 @@ __global__ void RingSumKernel(int nphi, const double* weights, const double* a, 
   if (threadIdx.x == 0) partial[j] = weights[j] * red[0];
 }
 
-// out[x] = f[l] in[x] over the (l, m >= 0) coefficients, Index(l, m) = l(l+1)/2 + m.
-__global__ void ScaleDegreesKernel(int lmax, const double* f, const double2* in, double2* out) {
+// out[x] = f[l] in[x] + c add[x] over the (l, m >= 0) coefficients,
+// Index(l, m) = l(l+1)/2 + m (add may be null).
+__global__ void ScaleDegreesKernel(int lmax, const double* f, const double2* in, const double2* add, double c,
+                                   double2* out) {
   const long long count = static_cast<long long>(lmax + 1) * (lmax + 2) / 2;
   const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
   if (i >= count) return;
@@ -65,7 +74,24 @@ __global__ void ScaleDegreesKernel(int lmax, const double* f, const double2* in,
   while (static_cast<long long>(l) * (l + 1) / 2 > i) --l;
   while (static_cast<long long>(l + 1) * (l + 2) / 2 <= i) ++l;
   const double2 v = in[i];
-  out[i] = make_double2(f[l] * v.x, f[l] * v.y);
+  double2 o = make_double2(f[l] * v.x, f[l] * v.y);
+  if (add != nullptr) {
+    o.x += c * add[i].x;
+    o.y += c * add[i].y;
+  }
+  out[i] = o;
+}
+
+// out[x] = a[x] + c b[x] over complex coefficients
+__global__ void AxpyKernel(long long count, const double2* a, const double2* b, double c, double2* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < count) out[i] = make_double2(a[i].x + c * b[i].x, a[i].y + c * b[i].y);
+}
+
+// out[x] = a[x] + b[x] over a field
+__global__ void AddFieldKernel(long long n, const double* a, const double* b, double* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < n) out[i] = a[i] + b[i];
 }
 
 // seeded[x] = sigma_d[x] + rho_w C[x] s_mean
@@ -147,14 +173,40 @@ struct SleRun {
     return SL3DGPU_OK;
   }
 
-  // field = Synthesise(f_l coefficients)
-  int SynthesiseScaled(const double* f, const double* coeffs, double* field) {
+  // out = f_l coefficients + c add (add may be null)
+  int ScaleDegrees(const double* f, const double* coeffs, const double* add, double c, double* out) {
     SL3D_CUDA(cudaMemcpyAsync(factors.p, f, (lmax + 1) * sizeof(double), cudaMemcpyHostToDevice, stream));
     const unsigned blocks = static_cast<unsigned>((coefCount + 255) / 256);
     ScaleDegreesKernel<<<blocks, 256, 0, stream>>>(lmax, factors.p, reinterpret_cast<const double2*>(coeffs),
-                                                   reinterpret_cast<double2*>(scaledLm.p));
+                                                   reinterpret_cast<const double2*>(add), c,
+                                                   reinterpret_cast<double2*>(out));
     SL3D_CHECK_LAUNCH();
+    return SL3DGPU_OK;
+  }
+  // field = Synthesise(f_l coefficients + add)
+  int SynthesiseScaled(const double* f, const double* coeffs, double* field, const double* add = nullptr) {
+    SL3D_TRY(ScaleDegrees(f, coeffs, add, 1.0, scaledLm.p));
     return sl3dgpu_synthesise_batch(grid, scaledLm.p, 1, field, stream);
+  }
+  // out = a + c b (complex coefficients)
+  int Axpy(const double* a, const double* b, double c, double* out) {
+    AxpyKernel<<<static_cast<unsigned>((coefCount + 255) / 256), 256, 0, stream>>>(
+        coefCount, reinterpret_cast<const double2*>(a), reinterpret_cast<const double2*>(b), c,
+        reinterpret_cast<double2*>(out));
+    SL3D_CHECK_LAUNCH();
+    return SL3DGPU_OK;
+  }
+  // the largest |a| over n values (field or coefficients viewed as reals)
+  int MaxAbs(const double* a, long long n, double* out) {
+    const int b = static_cast<int>(std::min<long long>(kMaxBlocks, (n + 255) / 256));
+    MaxAbsKernel<<<b, kRingThreads, 0, stream>>>(n, a, maxima.p);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(hostMaxima.data(), maxima.p, 2 * b * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    double m = 0.0;
+    for (int i = 0; i < b; ++i) m = std::max(m, hostMaxima[2 * i + 1]);
+    *out = m;
+    return SL3DGPU_OK;
   }
 };
 
@@ -239,19 +291,24 @@ struct LoadMixer {
 
 using namespace sl3dgpu;
 
-extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const double* h, const double* k, const double* lt, double g,
-                                 double water_density, double radius, double rtol, int max_iterations,
-                                 int anderson_memory, const double* ocean, const double* direct_load,
-                                 double* sea_level_change, double* displacement, double* potential,
-                                 double* tangential_potential, sl3dgpu_sle_result* result, void* stream) {
-  if (grid == nullptr || h == nullptr || k == nullptr || ocean == nullptr || direct_load == nullptr ||
-      sea_level_change == nullptr || result == nullptr) {
+extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
+                                 const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations,
+                                 int anderson_memory, double* sea_level_change, double* displacement,
+                                 double* potential, double* tangential_potential, double* toroidal_potential,
+                                 sl3dgpu_sle_result* result, void* stream) {
+  if (grid == nullptr || body == nullptr || body->h == nullptr || body->k == nullptr || ocean == nullptr ||
+      forcing == nullptr || sea_level_change == nullptr || result == nullptr) {
     SetError("sle: null argument");
     return SL3DGPU_ERR_ARGUMENT;
   }
+  const double g = body->g, water_density = body->water_density, radius = body->radius;
   if (!(g > 0.0) || !(water_density > 0.0) || !(radius > 0.0) || !(rtol >= 0.0) || max_iterations < 0 ||
       anderson_memory < 0 || anderson_memory > kMixMaxMemory) {
     SetError("sle: g, water_density and radius > 0, rtol >= 0, max_iterations >= 0, anderson_memory in [0, 16]");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (forcing->tide != nullptr && (body->ht == nullptr || body->kt == nullptr)) {
+    SetError("sle: a tide needs the tidal Love numbers ht and kt");
     return SL3DGPU_ERR_ARGUMENT;
   }
   SleRun run;
@@ -273,64 +330,142 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const double* h, const doub
   SL3D_CUDA(run.ringPartial.Alloc(ntheta));
   run.hostRing.assign(ntheta, 0.0);
   const int blocks = static_cast<int>(std::min<long long>(kMaxBlocks, (run.fieldSize + 255) / 256));
-  SL3D_CUDA(run.maxima.Alloc(2 * blocks));
-  run.hostMaxima.assign(2 * blocks, 0.0);
+  SL3D_CUDA(run.maxima.Alloc(2 * kMaxBlocks));
+  run.hostMaxima.assign(2 * kMaxBlocks, 0.0);
   for (auto* d : {&run.loadLm, &run.newLoadLm, &run.scaledLm}) SL3D_CUDA(d->Alloc(2 * run.coefCount));
   SL3D_CUDA(run.factors.Alloc(run.lmax + 1));
   for (auto* d : {&run.seeded, &run.slc, &run.oceanSlc, &run.newLoad}) SL3D_CUDA(d->Alloc(run.fieldSize));
   const cudaStream_t s = run.stream;
   const int L = run.lmax;
+  const long long nc = 2 * run.coefCount;  // coefficients as reals
   std::vector<double> slcFactor(L + 1);
-  for (int l = 0; l <= L; ++l) slcFactor[l] = -(h[l] + k[l] / g);
+  for (int l = 0; l <= L; ++l) slcFactor[l] = -(body->h[l] + body->k[l] / g);
+  std::vector<double> tangential(L + 1, 0.0);
+  if (body->l != nullptr)
+    for (int l = 1; l <= L; ++l) tangential[l] = body->l[l];  // a degree-0 field has no tangential part
 
-  *result = sl3dgpu_sle_result{0.0, 0.0, 0, 1};
+  // which channels carry something (the reference's MaxAbs > 0 tests)
+  auto nonzero = [&](const double* a, long long n, bool* out) -> int {
+    double m = 0.0;
+    if (a != nullptr) SL3D_TRY(run.MaxAbs(a, n, &m));
+    *out = m > 0.0;
+    return SL3DGPU_OK;
+  };
+  bool hasDirect, hasOutside, hasLayer, hasDisp, hasPot, hasTan, hasTide, hasToroidal;
+  SL3D_TRY(nonzero(forcing->direct_load, run.fieldSize, &hasDirect));
+  SL3D_TRY(nonzero(forcing->direct_load_outside, run.fieldSize, &hasOutside));
+  SL3D_TRY(nonzero(forcing->solid_surface_change, run.fieldSize, &hasLayer));
+  SL3D_TRY(nonzero(forcing->displacement_response, nc, &hasDisp));
+  SL3D_TRY(nonzero(forcing->potential_response, nc, &hasPot));
+  SL3D_TRY(nonzero(forcing->tangential_response, nc, &hasTan));
+  SL3D_TRY(nonzero(forcing->tide, nc, &hasTide));
+  SL3D_TRY(nonzero(forcing->toroidal_response, nc, &hasToroidal));
+  if (hasTide) {
+    // RequireTideDegrees (src/SeaLevel.cpp:83-96): no degree-0 or degree-1 part
+    std::vector<double> low(6);
+    SL3D_CUDA(cudaMemcpyAsync(low.data(), forcing->tide, 6 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SL3D_CUDA(cudaStreamSynchronize(s));
+    for (double v : low)
+      if (v != 0.0) {
+        SetError("sle: the tide has no degree-0 or degree-1 part: tides are taken relative to the centre of mass, "
+                 "degree 2 and up");
+        return SL3DGPU_ERR_ARGUMENT;
+      }
+  }
   auto zero = [&](double* f) -> int {
     if (f) SL3D_CUDA(cudaMemsetAsync(f, 0, run.fieldSize * sizeof(double), s));
     return SL3DGPU_OK;
   };
-  // Without a load there is nothing to solve (the reference's !anyForcing).
-  double loadIntegral = 0.0, loadScale = 0.0;
-  SL3D_TRY(run.Integrate(direct_load, nullptr, &loadIntegral));
-  {
-    MaxAbsKernel<<<blocks, kRingThreads, 0, s>>>(run.fieldSize, direct_load, run.maxima.p);
-    SL3D_CHECK_LAUNCH();
-    SL3D_CUDA(cudaMemcpyAsync(run.hostMaxima.data(), run.maxima.p, 2 * blocks * sizeof(double),
-                              cudaMemcpyDeviceToHost, s));
-    SL3D_CUDA(cudaStreamSynchronize(s));
-    for (int b = 0; b < blocks; ++b) loadScale = std::max(loadScale, run.hostMaxima[2 * b + 1]);
+  *result = sl3dgpu_sle_result{0.0, 0.0, 0, 1};
+  // the toroidal potential is carried, whatever else is solved (:561-563)
+  if (toroidal_potential != nullptr) {
+    if (forcing->toroidal_response != nullptr)
+      SL3D_TRY(sl3dgpu_synthesise_batch(grid, forcing->toroidal_response, 1, toroidal_potential, s));
+    else
+      SL3D_TRY(zero(toroidal_potential));
   }
-  if (loadScale == 0.0) {
+  const bool anyForcing = hasDirect || hasOutside || hasLayer || hasDisp || hasPot || hasTan || hasTide;
+  if (!anyForcing) {
     SL3D_TRY(zero(sea_level_change));
     SL3D_TRY(zero(displacement));
     SL3D_TRY(zero(potential));
     SL3D_TRY(zero(tangential_potential));
+    SL3D_CUDA(cudaStreamSynchronize(s));
     return SL3DGPU_OK;
   }
+
+  // The static (load-independent) coefficient terms.
+  const bool anyStatic = hasDisp || hasPot || hasTide || hasLayer;
+  const bool anyStaticTan = hasDisp || hasPot || hasTan || hasTide;
+  Dev<double> staticDisp, staticGrav, staticTan, staticSlc, scratch;
+  const std::vector<double> zeros(L + 1, 0.0);
+  if (anyStatic || anyStaticTan) {
+    for (auto* d : {&staticDisp, &staticGrav, &staticTan, &staticSlc, &scratch}) {
+      SL3D_CUDA(d->Alloc(nc));
+      SL3D_CUDA(cudaMemsetAsync(d->p, 0, nc * sizeof(double), s));
+    }
+    if (hasDisp) SL3D_TRY(run.Axpy(staticDisp.p, forcing->displacement_response, 1.0, staticDisp.p));
+    if (hasPot) SL3D_TRY(run.Axpy(staticGrav.p, forcing->potential_response, 1.0, staticGrav.p));
+    if (hasTan) SL3D_TRY(run.Axpy(staticTan.p, forcing->tangential_response, 1.0, staticTan.p));
+    if (hasTide) {
+      // the body's answer to the prescribed potential (:533-545)
+      std::vector<double> ht(body->ht, body->ht + L + 1), kt(body->kt, body->kt + L + 1), lt(L + 1, 0.0);
+      if (body->lt != nullptr)
+        for (int l = 1; l <= L; ++l) lt[l] = body->lt[l];
+      ht[0] = kt[0] = 0.0;
+      SL3D_TRY(run.ScaleDegrees(ht.data(), forcing->tide, staticDisp.p, 1.0, staticDisp.p));
+      SL3D_TRY(run.ScaleDegrees(kt.data(), forcing->tide, staticGrav.p, 1.0, staticGrav.p));
+      SL3D_TRY(run.ScaleDegrees(lt.data(), forcing->tide, staticTan.p, 1.0, staticTan.p));
+    }
+    // S_s = -(D_s + G_s / g) - T / g - Expand(layer) (:590-600)
+    SL3D_TRY(run.Axpy(staticDisp.p, staticGrav.p, 1.0 / g, staticSlc.p));
+    SL3D_TRY(run.ScaleDegrees(zeros.data(), staticSlc.p, staticSlc.p, -1.0, staticSlc.p));
+    if (hasTide) SL3D_TRY(run.Axpy(staticSlc.p, forcing->tide, -1.0 / g, staticSlc.p));
+    if (hasLayer) {
+      SL3D_TRY(sl3dgpu_expand_batch(grid, forcing->solid_surface_change, 1, scratch.p, s));
+      SL3D_TRY(run.Axpy(staticSlc.p, scratch.p, -1.0, staticSlc.p));
+    }
+  }
+  const double* slcAdd = anyStatic ? staticSlc.p : nullptr;
+
   double oceanArea = 0.0;
   SL3D_TRY(run.Integrate(ocean, nullptr, &oceanArea));
   const double perOceanArea = oceanArea > 0.0 ? 1.0 / oceanArea : 0.0;
-  const double meanSlc = -loadIntegral * perOceanArea / water_density;
-
-  // the seed: sigma_d + rho_w C s_mean, expanded
-  {
-    const unsigned b = static_cast<unsigned>((run.fieldSize + 255) / 256);
-    SeedKernel<<<b, 256, 0, s>>>(run.fieldSize, direct_load, ocean, water_density * meanSlc, run.seeded.p);
+  // the direct load in the water budget sets the mean; one outside it loads
+  // the body and moves no water (:577-587)
+  double meanSlc = 0.0;
+  Dev<double> directData;
+  SL3D_CUDA(directData.Alloc(run.fieldSize));
+  SL3D_CUDA(cudaMemsetAsync(directData.p, 0, run.fieldSize * sizeof(double), s));
+  const unsigned fb = static_cast<unsigned>((run.fieldSize + 255) / 256);
+  if (forcing->direct_load != nullptr) {
+    double loadIntegral = 0.0;
+    SL3D_TRY(run.Integrate(forcing->direct_load, nullptr, &loadIntegral));
+    meanSlc = -loadIntegral * perOceanArea / water_density;
+    SL3D_CUDA(cudaMemcpyAsync(directData.p, forcing->direct_load, run.fieldSize * sizeof(double),
+                              cudaMemcpyDeviceToDevice, s));
+  }
+  if (forcing->direct_load_outside != nullptr) {
+    AddFieldKernel<<<fb, 256, 0, s>>>(run.fieldSize, directData.p, forcing->direct_load_outside, directData.p);
     SL3D_CHECK_LAUNCH();
   }
+  // the seed: sigma + rho_w C s_mean, expanded
+  SeedKernel<<<fb, 256, 0, s>>>(run.fieldSize, directData.p, ocean, water_density * meanSlc, run.seeded.p);
+  SL3D_CHECK_LAUNCH();
   SL3D_TRY(sl3dgpu_expand_batch(grid, run.seeded.p, 1, run.loadLm.p, s));
 
   LoadMixer mixer;
-  SL3D_TRY(mixer.Init(anderson_memory, 2 * run.coefCount));
+  SL3D_TRY(mixer.Init(anderson_memory, nc));
   double err = INFINITY, shift = 0.0;
   bool converged = false, havePrev = false;
   int count = 0;
   while (count < max_iterations) {
     // the sea level change of the load, its uniform part by conservation
-    SL3D_TRY(run.SynthesiseScaled(slcFactor.data(), run.loadLm.p, run.slc.p));
+    SL3D_TRY(run.SynthesiseScaled(slcFactor.data(), run.loadLm.p, run.slc.p, slcAdd));
     double cs = 0.0;
     SL3D_TRY(run.Integrate(ocean, run.slc.p, &cs));
     shift = meanSlc - cs * perOceanArea;
-    ShiftAndLoadKernel<<<blocks, kRingThreads, 0, s>>>(run.fieldSize, shift, water_density, direct_load, ocean,
+    ShiftAndLoadKernel<<<blocks, kRingThreads, 0, s>>>(run.fieldSize, shift, water_density, directData.p, ocean,
                                                        run.slc.p, run.oceanSlc.p, run.newLoad.p, havePrev,
                                                        run.maxima.p);
     SL3D_CHECK_LAUNCH();
@@ -351,23 +486,21 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const double* h, const doub
     }
     havePrev = true;
     SL3D_TRY(sl3dgpu_expand_batch(grid, run.newLoad.p, 1, run.newLoadLm.p, s));
-    SL3D_TRY(mixer.Update(run.loadLm.p, run.newLoadLm.p, 2 * run.coefCount, s));
+    SL3D_TRY(mixer.Update(run.loadLm.p, run.newLoadLm.p, nc, s));
     ++count;
   }
-  // the sea level change is the last one formed; the other fields from the load it came from
+  // the sea level change is the last one formed; the other fields from the
+  // load it came from, with the static terms (:702-720)
   SL3D_CUDA(cudaMemcpyAsync(sea_level_change, run.slc.p, run.fieldSize * sizeof(double), cudaMemcpyDeviceToDevice,
                             s));
-  if (displacement) SL3D_TRY(run.SynthesiseScaled(h, run.loadLm.p, displacement));
-  if (potential) SL3D_TRY(run.SynthesiseScaled(k, run.loadLm.p, potential));
-  if (tangential_potential) {
-    if (lt) {
-      std::vector<double> tan(lt, lt + L + 1);
-      tan[0] = 0.0;  // a degree-0 field has no tangential part
-      SL3D_TRY(run.SynthesiseScaled(tan.data(), run.loadLm.p, tangential_potential));
-    } else {
-      SL3D_TRY(zero(tangential_potential));
-    }
-  }
+  const bool withStatic = anyStatic || anyStaticTan;
+  if (displacement)
+    SL3D_TRY(run.SynthesiseScaled(body->h, run.loadLm.p, displacement, withStatic ? staticDisp.p : nullptr));
+  if (potential)
+    SL3D_TRY(run.SynthesiseScaled(body->k, run.loadLm.p, potential, withStatic ? staticGrav.p : nullptr));
+  if (tangential_potential)
+    SL3D_TRY(run.SynthesiseScaled(tangential.data(), run.loadLm.p, tangential_potential,
+                                  withStatic ? staticTan.p : nullptr));
   SL3D_CUDA(cudaStreamSynchronize(s));
   *result = sl3dgpu_sle_result{shift, err, count, converged ? 1 : 0};
   return SL3DGPU_OK;

@@ -1,17 +1,20 @@
 """The sea-level equation on the GPU: GRDSolver (include/sl3dpp/SeaLevel.hpp,
-src/SeaLevel.cpp) for a direct surface load on a body without rotational
-feedback, in the solver's non-dimensional units.
+src/SeaLevel.cpp) without rotational feedback, in the solver's
+non-dimensional units.
 
-`SeaLevelSolver(grid, h, k, l, g, water_density, radius)` holds the per-degree
-load Love numbers (the sums h_u + h_phi and k_u + k_phi the reference's
-constructor forms, src/SeaLevel.cpp:163-171; the tangential l optional) and
-the body's constants; `solve_generalised(ocean, direct_load)` is
-GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) with
-GeneralisedForcing's directLoad alone and RotationalFeedback::None: the load
-fixed point under Anderson mixing with the water's conservation imposed as a
-uniform shift, returning the relative sea level change, displacement,
-potential and tangential potential on the grid and the Response scalars.
-Fields are torch CUDA tensors (float64, the grid's colatitude-major layout).
+`SeaLevelSolver(grid, h, k, l, ht, kt, lt, g, water_density, radius)` holds
+the per-degree load Love numbers (the sums h_u + h_phi and k_u + k_phi the
+reference's constructor forms, src/SeaLevel.cpp:163-171), the tangential and
+tidal ones (optional) and the body's constants; `solve_generalised(ocean,
+...)` is GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) with
+RotationalFeedback::None for GeneralisedForcing's channels of the coupled
+Evolution3D closure (src/Evolution3D.cpp:320-333): the direct load in and
+outside the water budget, a layer on the solid surface, the ready
+displacement, potential, tangential and toroidal responses and a tide. It
+returns the relative sea level change, displacement, potential, tangential
+and toroidal potentials on the grid and the Response scalars. Fields and
+coefficients are torch CUDA tensors (float64 fields in the grid's
+colatitude-major layout; complex128 (l, m >= 0) coefficients).
 """
 
 from __future__ import annotations
@@ -21,40 +24,70 @@ import ctypes
 import numpy as np
 import torch
 
-from ._lib import P_double, SleResult, check, lib
+from ._lib import P_double, SleBody, SleForcing, SleResult, check, lib
 from .grid import SurfaceGrid
+
+_FIELDS = ("direct_load", "direct_load_outside", "solid_surface_change")
+_COEFFS = ("displacement_response", "potential_response", "tangential_response", "toroidal_response", "tide")
 
 
 class SeaLevelSolver:
-    def __init__(self, grid: SurfaceGrid, h, k, l=None, g: float = 1.0, water_density: float = 1.0,
-                 radius: float = 1.0):
+    def __init__(self, grid: SurfaceGrid, h, k, l=None, ht=None, kt=None, lt=None, g: float = 1.0,
+                 water_density: float = 1.0, radius: float = 1.0):
         lmax = grid.lmax
         self.grid = grid
-        self.h = np.ascontiguousarray(h, dtype=np.float64)
-        self.k = np.ascontiguousarray(k, dtype=np.float64)
-        self.l = None if l is None else np.ascontiguousarray(l, dtype=np.float64)
-        for name, v in (("h", self.h), ("k", self.k), ("l", self.l)):
-            if v is not None and v.size < lmax + 1:
-                raise ValueError(f"the Love numbers {name} reach degree {v.size - 1}, the grid needs {lmax}")
+        self.arrays = {}
+        for name, v in (("h", h), ("k", k), ("l", l), ("ht", ht), ("kt", kt), ("lt", lt)):
+            if v is None:
+                self.arrays[name] = None
+                continue
+            a = np.ascontiguousarray(v, dtype=np.float64)
+            if a.size < lmax + 1:
+                raise ValueError(f"the Love numbers {name} reach degree {a.size - 1}, the grid needs {lmax}")
+            self.arrays[name] = a
+        if self.arrays["h"] is None or self.arrays["k"] is None:
+            raise ValueError("the load Love numbers h and k are required")
         self.g, self.water_density, self.radius = float(g), float(water_density), float(radius)
 
-    def solve_generalised(self, ocean: torch.Tensor, direct_load: torch.Tensor, rtol: float = 1e-9,
-                          max_iterations: int = 1000, anderson_memory: int = 5) -> dict:
-        size = self.grid.FieldSize()
-        for name, f in (("ocean function", ocean), ("direct load", direct_load)):
+    def solve_generalised(self, ocean: torch.Tensor, rtol: float = 1e-9, max_iterations: int = 1000,
+                          anderson_memory: int = 5, **forcing) -> dict:
+        size, ncoef = self.grid.FieldSize(), self.grid.CoefficientSize()
+        unknown = set(forcing) - set(_FIELDS) - set(_COEFFS)
+        if unknown:
+            raise ValueError(f"unknown forcing channels {sorted(unknown)}")
+
+        def field(name, f):
             if f.dtype != torch.float64 or not f.is_cuda or f.numel() != size or not f.is_contiguous():
                 raise ValueError(f"the {name} must be a contiguous float64 CUDA field on the grid")
+            return f
+
+        field("ocean function", ocean)
+        f = SleForcing()
+        keep = []
+        for name in _FIELDS:
+            if forcing.get(name) is not None:
+                setattr(f, name, field(name, forcing[name]).data_ptr())
+        for name in _COEFFS:
+            c = forcing.get(name)
+            if c is None:
+                continue
+            if c.dtype != torch.complex128 or not c.is_cuda or c.numel() != ncoef or not c.is_contiguous():
+                raise ValueError(f"the {name} must be contiguous complex128 CUDA coefficients of the grid")
+            keep.append(c)
+            setattr(f, name, c.data_ptr())
+        a = self.arrays
+        body = SleBody(*(a[n].ctypes.data_as(P_double) if a[n] is not None else None
+                         for n in ("h", "k", "l", "ht", "kt", "lt")), self.g, self.water_density, self.radius)
         out = {key: torch.empty(size, dtype=torch.float64, device=ocean.device)
-               for key in ("sea_level_change", "displacement", "potential", "tangential_potential")}
+               for key in ("sea_level_change", "displacement", "potential", "tangential_potential",
+                           "toroidal_potential")}
         res = SleResult()
         stream = torch.cuda.current_stream().cuda_stream
-        lt = self.l.ctypes.data_as(P_double) if self.l is not None else None
-        check(lib().sl3dgpu_sle_solve(self.grid._handle, self.h.ctypes.data_as(P_double),
-                                      self.k.ctypes.data_as(P_double), lt, self.g, self.water_density, self.radius,
-                                      float(rtol), int(max_iterations), int(anderson_memory), ocean.data_ptr(),
-                                      direct_load.data_ptr(), out["sea_level_change"].data_ptr(),
-                                      out["displacement"].data_ptr(), out["potential"].data_ptr(),
-                                      out["tangential_potential"].data_ptr(), ctypes.byref(res), stream))
+        check(lib().sl3dgpu_sle_solve(self.grid._handle, ctypes.byref(body), ocean.data_ptr(), ctypes.byref(f),
+                                      float(rtol), int(max_iterations), int(anderson_memory),
+                                      out["sea_level_change"].data_ptr(), out["displacement"].data_ptr(),
+                                      out["potential"].data_ptr(), out["tangential_potential"].data_ptr(),
+                                      out["toroidal_potential"].data_ptr(), ctypes.byref(res), stream))
         out.update(uniform_shift=res.uniform_shift, error=res.error, iterations=res.iterations,
                    converged=bool(res.converged))
         return out

@@ -66,8 +66,10 @@ def _gpu_solve(gpu, p, lmax, **kw):
 
     grid = SurfaceGrid(lmax, 0, 1.0)
     assert grid.ntheta == p["theta"].size and grid.nphi == p["nphi"]
-    solver = SeaLevelSolver(grid, p["h"], p["k"], p["lt"], 1.0, 1.0, 1.0)
-    r = solver.solve_generalised(torch.tensor(p["ocean"], device=gpu), torch.tensor(p["load"], device=gpu), **kw)
+    solver = SeaLevelSolver(grid, p["h"], p["k"], p["lt"], p.get("ht"), p.get("kt"), p.get("lt_tide"), 1.0, 1.0, 1.0)
+    channels = {name: torch.tensor(v, device=gpu) for name, v in kw.pop("channels", {}).items()}
+    r = solver.solve_generalised(torch.tensor(p["ocean"], device=gpu), direct_load=torch.tensor(p["load"], device=gpu),
+                                 **channels, **kw)
     return {k: (v.cpu().numpy() if hasattr(v, "cpu") else v) for k, v in r.items()}
 
 
@@ -110,3 +112,58 @@ def test_gpu_sea_level_identities(gpu):
     assert r["uniform_shift"] == 0.0 and r["converged"] and r["iterations"] == want["iterations"]
     assert np.max(np.abs(r["sea_level_change"] - want["sea_level_change"])) < 1e-12 * np.max(
         np.abs(want["sea_level_change"]))
+
+
+def channel_forcing(p, lmax, seed=5):
+    """The coupled closure's other channels: ready responses, a tide (degrees
+    2 and up), a load outside the water budget, a layer on the solid surface."""
+    rng = np.random.default_rng(seed)
+    ncoef = (lmax + 1) * (lmax + 2) // 2
+    degree = np.concatenate([np.full(l + 1, l) for l in range(lmax + 1)])
+    m = np.concatenate([np.arange(l + 1) for l in range(lmax + 1)])
+
+    def coeffs(scale):
+        c = (rng.standard_normal(ncoef) + 1j * rng.standard_normal(ncoef)) * scale / (1.0 + degree) ** 2
+        c[m == 0] = c[m == 0].real  # a real field's m = 0 coefficients are real
+        return c
+
+    tide = coeffs(0.05)
+    tide[degree < 2] = 0.0
+    tt, pp = np.meshgrid(p["theta"], 2 * np.pi * np.arange(p["nphi"]) / p["nphi"], indexing="ij")
+    outside = (0.05 * np.sin(3 * pp) * np.sin(tt) ** 3).ravel()
+    layer = (0.02 * np.cos(tt) ** 2).ravel()
+    degrees = np.arange(lmax + 1, dtype=np.float64)
+    extra = dict(ht=-0.4 / (degrees + 1.0), kt=0.2 / (degrees + 1.0), lt_tide=0.1 / (degrees + 1.0))
+    return dict(displacement_response=coeffs(0.01), potential_response=coeffs(0.02),
+                tangential_response=coeffs(0.01), toroidal_response=coeffs(0.01), tide=tide,
+                direct_load_outside=outside, solid_surface_change=layer), extra
+
+
+def test_oracle_channels_keep_the_water_budget():
+    """The responses, tide and layer move the sea level but only the direct
+    load in the budget changes the water's mass (:577-587)."""
+    lmax = 14
+    p = problem(lmax)
+    ch, extra = channel_forcing(p, lmax)
+    r = sle_oracle.solve_generalised(p["synth"], p["expand"], p["integ"], p["h"], p["k"], p["lt"], 1.0, 1.0, 1.0,
+                                     p["ocean"], p["load"], rtol=1e-12, max_iterations=300, **ch,
+                                     ht=extra["ht"], kt=extra["kt"], lt_tide=extra["lt_tide"])
+    assert r["converged"]
+    gained = p["integ"](p["ocean"] * r["sea_level_change"])
+    assert abs(gained + p["integ"](p["load"])) < 1e-10 * abs(p["integ"](p["load"]))
+    assert np.max(np.abs(r["toroidal_potential"] - p["synth"](ch["toroidal_response"]))) == 0.0
+
+
+@pytest.mark.gpu
+def test_gpu_sea_level_channels_match_oracle(gpu):
+    lmax = 18
+    p = problem(lmax)
+    ch, extra = channel_forcing(p, lmax)
+    want = sle_oracle.solve_generalised(p["synth"], p["expand"], p["integ"], p["h"], p["k"], p["lt"], 1.0, 1.0,
+                                        1.0, p["ocean"], p["load"], rtol=1e-11, max_iterations=300, **ch,
+                                        ht=extra["ht"], kt=extra["kt"], lt_tide=extra["lt_tide"])
+    got = _gpu_solve(gpu, dict(p, **extra), lmax, rtol=1e-11, max_iterations=300, channels=ch)
+    assert want["converged"] and got["converged"] and got["iterations"] == want["iterations"]
+    for key in ("sea_level_change", "displacement", "potential", "tangential_potential", "toroidal_potential"):
+        scale = np.max(np.abs(want[key]))
+        assert np.max(np.abs(got[key] - want[key])) < 1e-10 * scale, key
