@@ -169,6 +169,14 @@ typedef struct sl3dgpu_sle_body {
   const double* kt;
   const double* lt;
   double g, water_density, radius;
+  /* rotational feedback (RotationalFeedback: 0 None, 1 Axial, 2 Full; the
+   * tidal ht and kt required with it) and its constants, non-dimensional:
+   * the rotation frequency, the polar and equatorial moments of inertia,
+   * the gravitational constant, the centrifugal Love numbers h_c, k_c and
+   * the inertia-trace numbers m_u, m_phi, m_c (src/SeaLevel.cpp:194-247) */
+  int rotation;
+  double omega, polar_moment, equatorial_moment, gravitational_constant;
+  double hc, kc, m_u, m_phi, m_c;
 } sl3dgpu_sle_body;
 typedef struct sl3dgpu_sle_forcing {
   const double* direct_load;            /* field: in the water budget */
@@ -179,12 +187,15 @@ typedef struct sl3dgpu_sle_forcing {
   const double* tangential_response;
   const double* toroidal_response;      /* carried to the response alone */
   const double* tide;                   /* coefficients, degrees >= 2 */
+  double inertia_moment_change;         /* GeneralisedForcing::inertiaMomentChange */
+  double angular_momentum_change[3];    /* GeneralisedForcing::angularMomentumChange */
 } sl3dgpu_sle_forcing;
 typedef struct sl3dgpu_sle_result {
   double uniform_shift; /* Response::uniformShift: the conservation's uniform part, last formed */
   double error;         /* Response::error: the last relative change of the ocean's sea level */
   int iterations;       /* Response::iterations */
   int converged;        /* Response::converged */
+  double angular_velocity[3]; /* Response::angularVelocity (zero without rotational feedback) */
 } sl3dgpu_sle_result;
 int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
                       const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations, int anderson_memory,

@@ -62,10 +62,74 @@ class AndersonMixer:
         return gx - gamma @ self.dG[:m]
 
 
+def _block_of(c):
+    """BlockOf (src/SeaLevel.cpp:33-36): [[(2,0), cos], [0, sin]] of the (2, 1)
+    real pair (ShConventions.hpp:48-54)."""
+    r2 = np.sqrt(2.0)
+    return np.array([[c[3].real, -r2 * c[4].real], [0.0, r2 * c[4].imag]])
+
+
+def _set_block(c, b):
+    """SetBlock (src/SeaLevel.cpp:38-42)."""
+    r2 = np.sqrt(2.0)
+    c[3] = b[0, 0]
+    c[4] = complex(-b[0, 1] / r2, b[1, 1] / r2)
+
+
+def _add_block(c, b):
+    """AddBlock (src/SeaLevel.cpp:44-48)."""
+    r2 = np.sqrt(2.0)
+    c[3] += b[0, 0]
+    c[4] += complex(-b[0, 1] / r2, b[1, 1] / r2)
+
+
+class _RotationFactors:
+    """The constructor's rotational factors (src/SeaLevel.cpp:220-247)."""
+
+    def __init__(self, rotation, h, k, ht, kt, radius, omega, polar, equatorial, G, hc, kc, m_u, m_phi, m_c):
+        pi, a, w = np.pi, radius, omega
+        self.transverse = rotation == 2
+        self.h2, self.k2, self.ht2, self.kt2 = h[2], k[2], ht[2], kt[2]
+        self.hc, self.kc, self.mu, self.mphi, self.mc = hc, kc, m_u, m_phi, m_c
+        self.rotation = np.sqrt(4.0 * pi / 15.0) * w * a * a
+        self.inertia = np.sqrt(5.0 / (12.0 * pi)) * w * a ** 3 / (G * (polar - equatorial))
+        self.axial_rotation = np.sqrt(16.0 * pi / 45.0) * w * a * a
+        self.uniform_rotation = -np.sqrt(16.0 * pi / 9.0) * w * a * a
+        self.axial_inertia = np.sqrt(5.0 / (9.0 * pi)) * w * a ** 3 / (G * polar)
+        self.inverse_inertia_difference = 1.0 / (polar - equatorial)
+        self.inverse_polar_inertia = 1.0 / polar
+        self.trace = (4.0 / 3.0) * w / polar
+        self.shell = (2.0 / 3.0) * w * a ** 4 * np.sqrt(4.0 * pi) / polar
+        self.rotation_denominator = 1.0 - self.inertia * self.kt2 * self.rotation
+        self.axial_rotation_denominator = (1.0 + self.axial_inertia * self.kt2 * self.axial_rotation +
+                                           self.trace * self.mc * self.uniform_rotation)
+
+
+def _rotation(s, load2, load0, static_disp2, static_grav2, inertia_moment, angular_momentum):
+    """GRDSolver::Rotation (src/SeaLevel.cpp:348-395) with no displacement or
+    potential load channels."""
+    grav = s.k2 * load2 + static_grav2
+    disp = s.h2 * load2 + static_disp2
+    transverse = np.array([s.inertia * grav[0, 1], s.inertia * grav[1, 1]])
+    axial = -s.axial_inertia * grav[0, 0] - s.trace * ((s.mu + s.mphi) * load0 + inertia_moment) - s.shell * load0
+    transverse -= s.inverse_inertia_difference * np.asarray(angular_momentum[:2])
+    axial += s.inverse_polar_inertia * angular_momentum[2]
+    omega = np.zeros(3)
+    if s.transverse:
+        omega[:2] = transverse / s.rotation_denominator
+    omega[2] = axial / s.axial_rotation_denominator
+    centrifugal = np.array([[s.axial_rotation * omega[2], s.rotation * omega[0]], [0.0, s.rotation * omega[1]]])
+    centrifugal0 = s.uniform_rotation * omega[2]
+    return dict(omega=omega, disp2=disp + s.ht2 * centrifugal, grav2=grav + s.kt2 * centrifugal,
+                centrifugal=centrifugal, centrifugal0=centrifugal0)
+
+
 def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density, radius, ocean, direct_load=None,
                       rtol=1e-9, max_iterations=1000, anderson_memory=5, direct_load_outside=None,
                       solid_surface_change=None, displacement_response=None, potential_response=None,
-                      tangential_response=None, toroidal_response=None, tide=None, ht=None, kt=None, lt_tide=None):
+                      tangential_response=None, toroidal_response=None, tide=None, ht=None, kt=None, lt_tide=None,
+                      rotation=0, omega=0.0, polar=0.0, equatorial=0.0, G=0.0, hc=0.0, kc=0.0, m_u=0.0, m_phi=0.0,
+                      m_c=0.0, inertia_moment_change=0.0, angular_momentum_change=(0.0, 0.0, 0.0)):
     """The load fixed point of the sea-level equation (SeaLevel.cpp:397-736
     with RotationalFeedback::None) for the channels the coupled Evolution3D
     closure uses. synthesise(coeffs) and expand(field) are the grid's real
@@ -77,7 +141,7 @@ def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density,
     degree = np.concatenate([np.full(l + 1, l) for l in range(lmax + 1)])
     ncoef = degree.size
     size = ocean.size
-    out = {"uniform_shift": 0.0, "iterations": 0, "error": 0.0, "converged": True}
+    out = {"uniform_shift": 0.0, "iterations": 0, "error": 0.0, "converged": True, "angular_velocity": np.zeros(3)}
     nz = lambda a: a is not None and np.max(np.abs(a)) > 0.0
     # the toroidal potential is carried, whatever else is solved (:561-563)
     toroidal = synthesise(toroidal_response) if toroidal_response is not None else np.zeros(size)
@@ -120,6 +184,16 @@ def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density,
         direct = direct + direct_load_outside
     slc_factor = -(h + k / g)
     load_lm = expand(direct + water_density * ocean * mean_slc)
+    rot = None
+    if rotation:
+        rot = _RotationFactors(rotation, h, k, np.asarray(ht), np.asarray(kt), radius, omega, polar, equatorial, G,
+                               hc, kc, m_u, m_phi, m_c)
+        static_disp2, static_grav2 = _block_of(static_disp), _block_of(static_grav)
+        tide2 = _block_of(tide) if nz(tide) else np.zeros((2, 2))
+        layer2 = _block_of(expand(solid_surface_change)) if nz(solid_surface_change) else np.zeros((2, 2))
+        rotate = lambda lm: _rotation(rot, _block_of(lm), lm[0].real, static_disp2, static_grav2,
+                                      inertia_moment_change, angular_momentum_change)
+    omega_out = np.zeros(3)
     mixer = AndersonMixer(anderson_memory)
     prev = None
     slc = np.zeros(size)
@@ -131,6 +205,11 @@ def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density,
         lm = slc_factor[degree] * load_lm
         if any_static:
             lm = lm + static_slc
+        if rot is not None:  # :625-640
+            r = rotate(load_lm)
+            omega_out = r["omega"]
+            _set_block(lm, -(r["disp2"] + (r["grav2"] + r["centrifugal"] + tide2) / g + layer2))
+            lm[0] -= (rot.hc + (rot.kc + 1.0) / g) * r["centrifugal0"]
         slc = synthesise(lm)
         shift = mean_slc - surface(ocean * slc) * per_area
         slc = slc + shift
@@ -148,8 +227,18 @@ def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density,
         count += 1
     tan = np.zeros(lmax + 1) if lt is None else np.array(lt, dtype=np.float64)
     tan[0] = 0.0
-    out.update(sea_level_change=slc, displacement=synthesise(h[degree] * load_lm + static_disp),
-               potential=synthesise(k[degree] * load_lm + static_grav),
-               tangential_potential=synthesise(tan[degree] * load_lm + static_tan), toroidal_potential=toroidal,
-               uniform_shift=shift, iterations=count, error=err, converged=converged)
+    disp_lm = h[degree] * load_lm + static_disp
+    pot_lm = k[degree] * load_lm + static_grav
+    tan_lm = tan[degree] * load_lm + static_tan
+    if rot is not None:  # :714-724
+        r = rotate(load_lm)
+        _set_block(disp_lm, r["disp2"])
+        _set_block(pot_lm, r["grav2"])
+        disp_lm[0] += rot.hc * r["centrifugal0"]
+        pot_lm[0] += rot.kc * r["centrifugal0"]
+        lt2 = 0.0 if lt_tide is None else lt_tide[2]
+        _add_block(tan_lm, lt2 * r["centrifugal"])
+    out.update(sea_level_change=slc, displacement=synthesise(disp_lm), potential=synthesise(pot_lm),
+               tangential_potential=synthesise(tan_lm), toroidal_potential=toroidal, uniform_shift=shift,
+               iterations=count, error=err, converged=converged, angular_velocity=omega_out)
     return out

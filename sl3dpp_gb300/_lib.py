@@ -49,20 +49,24 @@ class SleBody(ctypes.Structure):
     """sl3dgpu_sle_body: the solver's Love numbers (host arrays) and constants."""
     _fields_ = [("h", P_double), ("k", P_double), ("l", P_double), ("ht", P_double), ("kt", P_double),
                 ("lt", P_double), ("g", ctypes.c_double), ("water_density", ctypes.c_double),
-                ("radius", ctypes.c_double)]
+                ("radius", ctypes.c_double), ("rotation", ctypes.c_int), ("omega", ctypes.c_double),
+                ("polar_moment", ctypes.c_double), ("equatorial_moment", ctypes.c_double),
+                ("gravitational_constant", ctypes.c_double), ("hc", ctypes.c_double), ("kc", ctypes.c_double),
+                ("m_u", ctypes.c_double), ("m_phi", ctypes.c_double), ("m_c", ctypes.c_double)]
 
 
 class SleForcing(ctypes.Structure):
     """sl3dgpu_sle_forcing: GeneralisedForcing's channels (device pointers or null)."""
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("direct_load", "direct_load_outside", "solid_surface_change", "displacement_response",
-                 "potential_response", "tangential_response", "toroidal_response", "tide")]
+                 "potential_response", "tangential_response", "toroidal_response", "tide")] + [
+                ("inertia_moment_change", ctypes.c_double), ("angular_momentum_change", ctypes.c_double * 3)]
 
 
 class SleResult(ctypes.Structure):
     """sl3dgpu_sle_result: GRDSolver::Response's scalars."""
     _fields_ = [("uniform_shift", ctypes.c_double), ("error", ctypes.c_double), ("iterations", ctypes.c_int),
-                ("converged", ctypes.c_int)]
+                ("converged", ctypes.c_int), ("angular_velocity", ctypes.c_double * 3)]
 
 
 class Sl3dgpuError(RuntimeError):

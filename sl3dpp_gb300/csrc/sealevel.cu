@@ -31,6 +31,7 @@
 // order-free. A few scalars per iteration come to the host: the integral, the
 // two maxima and the mixer's Gram column.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -286,6 +287,95 @@ struct LoadMixer {
   }
 };
 
+// -- the degree-2 / degree-0 rotational feedback (GRDSolver::Rotation,
+// src/SeaLevel.cpp:340-395), on the host: a handful of coefficients an
+// iteration, in the real (cos, sin) pairs of the (2, 1) coefficient
+// (ShConventions.hpp:40-54) ---------------------------------------------------
+
+using Block2 = std::array<std::array<double, 2>, 2>;  // [0][0] (2,0); [0][1], [1][1] (2,1) cos, sin
+
+Block2 Scaled(const Block2& b, double c) { return {{{c * b[0][0], c * b[0][1]}, {c * b[1][0], c * b[1][1]}}}; }
+Block2 Plus(const Block2& a, const Block2& b) {
+  return {{{a[0][0] + b[0][0], a[0][1] + b[0][1]}, {a[1][0] + b[1][0], a[1][1] + b[1][1]}}};
+}
+// BlockOf: from the (2, 0) and (2, 1) coefficients (re, im pairs)
+Block2 BlockOf(const double* c20, const double* c21) {
+  const double r2 = std::sqrt(2.0);
+  return {{{c20[0], -r2 * c21[0]}, {0.0, r2 * c21[1]}}};
+}
+// SetBlock's (2, 0) and (2, 1) coefficients from a block
+void FromBlock(const Block2& b, double* c20, double* c21) {
+  const double r2 = std::sqrt(2.0);
+  c20[0] = b[0][0];
+  c20[1] = 0.0;
+  c21[0] = -b[0][1] / r2;
+  c21[1] = b[1][1] / r2;
+}
+
+struct RotationFactors {
+  bool on = false, transverse = false;
+  double h2, k2, ht2, kt2, hc, kc, mu, mphi, mc;
+  double rotation, inertia, axialRotation, uniformRotation, axialInertia, inverseInertiaDifference,
+      inversePolarInertia, trace, shell, rotationDenominator, axialRotationDenominator;
+  // the constructor's factors (src/SeaLevel.cpp:220-247)
+  void Init(const sl3dgpu_sle_body& b) {
+    on = b.rotation != 0;
+    transverse = b.rotation == 2;
+    if (!on) return;
+    const double pi = 3.14159265358979323846, a = b.radius, w = b.omega, G = b.gravitational_constant;
+    const double C = b.polar_moment, A = b.equatorial_moment;
+    h2 = b.h[2];
+    k2 = b.k[2];
+    ht2 = b.ht[2];
+    kt2 = b.kt[2];
+    hc = b.hc;
+    kc = b.kc;
+    mu = b.m_u;
+    mphi = b.m_phi;
+    mc = b.m_c;
+    rotation = std::sqrt(4.0 * pi / 15.0) * w * a * a;
+    inertia = std::sqrt(5.0 / (12.0 * pi)) * w * a * a * a / (G * (C - A));
+    axialRotation = std::sqrt(16.0 * pi / 45.0) * w * a * a;
+    uniformRotation = -std::sqrt(16.0 * pi / 9.0) * w * a * a;
+    axialInertia = std::sqrt(5.0 / (9.0 * pi)) * w * a * a * a / (G * C);
+    inverseInertiaDifference = 1.0 / (C - A);
+    inversePolarInertia = 1.0 / C;
+    trace = (4.0 / 3.0) * w / C;
+    shell = (2.0 / 3.0) * w * std::pow(a, 4) * std::sqrt(4.0 * pi) / C;
+    rotationDenominator = 1.0 - inertia * kt2 * rotation;
+    axialRotationDenominator = 1.0 + axialInertia * kt2 * axialRotation + trace * mc * uniformRotation;
+  }
+};
+
+struct Rotation {
+  std::array<double, 3> omega{0.0, 0.0, 0.0};
+  Block2 disp2{}, grav2{}, centrifugal{};
+  double centrifugal0 = 0.0;
+  // GRDSolver::Rotation's constructor with no displacement or potential
+  // load channels (displacementLoad0 = potentialLoad0 = 0)
+  Rotation(const RotationFactors& s, const Block2& load2, double load0, const Block2& staticDisp2,
+           const Block2& staticGrav2, double inertiaMoment, const double* angularMomentum) {
+    const Block2 gravForcing = Plus(Scaled(load2, s.k2), staticGrav2);
+    const Block2 dispForcing = Plus(Scaled(load2, s.h2), staticDisp2);
+    double transverse[2] = {s.inertia * gravForcing[0][1], s.inertia * gravForcing[1][1]};
+    double axial = -s.axialInertia * gravForcing[0][0] - s.trace * ((s.mu + s.mphi) * load0 + inertiaMoment) -
+                   s.shell * load0;
+    for (int i = 0; i < 2; ++i) transverse[i] -= s.inverseInertiaDifference * angularMomentum[i];
+    axial += s.inversePolarInertia * angularMomentum[2];
+    if (s.transverse) {
+      omega[0] = transverse[0] / s.rotationDenominator;
+      omega[1] = transverse[1] / s.rotationDenominator;
+    }
+    omega[2] = axial / s.axialRotationDenominator;
+    centrifugal[0][1] = s.rotation * omega[0];
+    centrifugal[1][1] = s.rotation * omega[1];
+    centrifugal[0][0] = s.axialRotation * omega[2];
+    centrifugal0 = s.uniformRotation * omega[2];
+    disp2 = Plus(dispForcing, Scaled(centrifugal, s.ht2));
+    grav2 = Plus(gravForcing, Scaled(centrifugal, s.kt2));
+  }
+};
+
 }  // namespace
 }  // namespace sl3dgpu
 
@@ -311,6 +401,14 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
     SetError("sle: a tide needs the tidal Love numbers ht and kt");
     return SL3DGPU_ERR_ARGUMENT;
   }
+  if (body->rotation < 0 || body->rotation > 2 ||
+      (body->rotation != 0 && (body->ht == nullptr || body->kt == nullptr || !(body->polar_moment > 0.0) ||
+                               !(body->polar_moment != body->equatorial_moment) ||
+                               !(body->gravitational_constant > 0.0)))) {
+    SetError("sle: rotation 0 (none), 1 (axial) or 2 (full); with feedback, the tidal ht and kt, the moments of "
+             "inertia (polar > 0, unequal) and the gravitational constant");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
   SleRun run;
   run.grid = grid;
   run.stream = AsStream(stream);
@@ -322,6 +420,10 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   run.nphi = nphi;
   run.fieldSize = static_cast<long long>(ntheta) * nphi;
   run.coefCount = static_cast<long long>(run.lmax + 1) * (run.lmax + 2) / 2;
+  if (body->rotation != 0 && run.lmax < 2) {
+    SetError("sle: rotational feedback needs degree 2 on the grid");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
   run.r2 = radius * radius;
   run.dphi = 2.0 * 3.14159265358979323846 / nphi;
   std::vector<double> theta(ntheta), w(ntheta);
@@ -376,7 +478,7 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
     if (f) SL3D_CUDA(cudaMemsetAsync(f, 0, run.fieldSize * sizeof(double), s));
     return SL3DGPU_OK;
   };
-  *result = sl3dgpu_sle_result{0.0, 0.0, 0, 1};
+  *result = sl3dgpu_sle_result{0.0, 0.0, 0, 1, {0.0, 0.0, 0.0}};
   // the toroidal potential is carried, whatever else is solved (:561-563)
   if (toroidal_potential != nullptr) {
     if (forcing->toroidal_response != nullptr)
@@ -454,6 +556,57 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   SL3D_CHECK_LAUNCH();
   SL3D_TRY(sl3dgpu_expand_batch(grid, run.seeded.p, 1, run.loadLm.p, s));
 
+  // The rotational feedback's fixed blocks (src/SeaLevel.cpp:604-608).
+  RotationFactors rf;
+  rf.Init(*body);
+  Block2 staticDisp2{}, staticGrav2{}, tide2{}, layer2{};
+  auto headOf = [&](const double* coeffs, double* head) -> int {  // coefficients 0 .. 4 as (re, im)
+    SL3D_CUDA(cudaMemcpyAsync(head, coeffs, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SL3D_CUDA(cudaStreamSynchronize(s));
+    return SL3DGPU_OK;
+  };
+  if (rf.on) {
+    double head[10];
+    if (anyStatic || anyStaticTan) {
+      SL3D_TRY(headOf(staticDisp.p, head));
+      staticDisp2 = BlockOf(head + 6, head + 8);
+      SL3D_TRY(headOf(staticGrav.p, head));
+      staticGrav2 = BlockOf(head + 6, head + 8);
+    }
+    if (hasTide) {
+      SL3D_TRY(headOf(forcing->tide, head));
+      tide2 = BlockOf(head + 6, head + 8);
+    }
+    if (hasLayer) {
+      SL3D_TRY(headOf(scratch.p, head));  // the layer's expansion
+      layer2 = BlockOf(head + 6, head + 8);
+    }
+  }
+  std::array<double, 3> omega{0.0, 0.0, 0.0};
+  // out = f_l L + add, then (rotating) its degree-0/2 coefficients set by
+  // `patch` from the rotation of the load L, and synthesised
+  auto synthesisePatched = [&](const double* f, const double* add, double* field, auto&& patch) -> int {
+    SL3D_TRY(run.ScaleDegrees(f, run.loadLm.p, add, 1.0, run.scaledLm.p));
+    if (rf.on) {
+      double load[10], out[10];
+      SL3D_TRY(headOf(run.loadLm.p, load));
+      SL3D_TRY(headOf(run.scaledLm.p, out));
+      const Rotation rot(rf, BlockOf(load + 6, load + 8), load[0], staticDisp2, staticGrav2,
+                         forcing->inertia_moment_change, forcing->angular_momentum_change);
+      patch(rot, out);
+      SL3D_CUDA(cudaMemcpyAsync(run.scaledLm.p, out, 10 * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    return sl3dgpu_synthesise_batch(grid, run.scaledLm.p, 1, field, s);
+  };
+  // the sea level change's blocks (src/SeaLevel.cpp:625-640)
+  auto slcPatch = [&](const Rotation& rot, double* out) {
+    omega = rot.omega;
+    const Block2 b =
+        Scaled(Plus(Plus(rot.disp2, Scaled(Plus(Plus(rot.grav2, rot.centrifugal), tide2), 1.0 / g)), layer2), -1.0);
+    FromBlock(b, out + 6, out + 8);
+    out[0] -= (rf.hc + (rf.kc + 1.0) / g) * rot.centrifugal0;  // uniform: absorbed by conservation
+  };
+
   LoadMixer mixer;
   SL3D_TRY(mixer.Init(anderson_memory, nc));
   double err = INFINITY, shift = 0.0;
@@ -461,7 +614,7 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   int count = 0;
   while (count < max_iterations) {
     // the sea level change of the load, its uniform part by conservation
-    SL3D_TRY(run.SynthesiseScaled(slcFactor.data(), run.loadLm.p, run.slc.p, slcAdd));
+    SL3D_TRY(synthesisePatched(slcFactor.data(), slcAdd, run.slc.p, slcPatch));
     double cs = 0.0;
     SL3D_TRY(run.Integrate(ocean, run.slc.p, &cs));
     shift = meanSlc - cs * perOceanArea;
@@ -494,14 +647,30 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   SL3D_CUDA(cudaMemcpyAsync(sea_level_change, run.slc.p, run.fieldSize * sizeof(double), cudaMemcpyDeviceToDevice,
                             s));
   const bool withStatic = anyStatic || anyStaticTan;
+  const double lt2 = body->lt != nullptr ? body->lt[2] : 0.0;
   if (displacement)
-    SL3D_TRY(run.SynthesiseScaled(body->h, run.loadLm.p, displacement, withStatic ? staticDisp.p : nullptr));
+    SL3D_TRY(synthesisePatched(body->h, withStatic ? staticDisp.p : nullptr, displacement,
+                               [&](const Rotation& rot, double* out) {
+                                 FromBlock(rot.disp2, out + 6, out + 8);
+                                 out[0] += rf.hc * rot.centrifugal0;
+                               }));
   if (potential)
-    SL3D_TRY(run.SynthesiseScaled(body->k, run.loadLm.p, potential, withStatic ? staticGrav.p : nullptr));
+    SL3D_TRY(synthesisePatched(body->k, withStatic ? staticGrav.p : nullptr, potential,
+                               [&](const Rotation& rot, double* out) {
+                                 FromBlock(rot.grav2, out + 6, out + 8);
+                                 out[0] += rf.kc * rot.centrifugal0;
+                               }));
   if (tangential_potential)
-    SL3D_TRY(run.SynthesiseScaled(tangential.data(), run.loadLm.p, tangential_potential,
-                                  withStatic ? staticTan.p : nullptr));
+    SL3D_TRY(synthesisePatched(tangential.data(), withStatic ? staticTan.p : nullptr, tangential_potential,
+                               [&](const Rotation& rot, double* out) {
+                                 double c20[2], c21[2];
+                                 FromBlock(Scaled(rot.centrifugal, lt2), c20, c21);
+                                 out[6] += c20[0];
+                                 out[7] += c20[1];
+                                 out[8] += c21[0];
+                                 out[9] += c21[1];
+                               }));
   SL3D_CUDA(cudaStreamSynchronize(s));
-  *result = sl3dgpu_sle_result{shift, err, count, converged ? 1 : 0};
+  *result = sl3dgpu_sle_result{shift, err, count, converged ? 1 : 0, {omega[0], omega[1], omega[2]}};
   return SL3DGPU_OK;
 }

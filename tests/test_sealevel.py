@@ -66,7 +66,8 @@ def _gpu_solve(gpu, p, lmax, **kw):
 
     grid = SurfaceGrid(lmax, 0, 1.0)
     assert grid.ntheta == p["theta"].size and grid.nphi == p["nphi"]
-    solver = SeaLevelSolver(grid, p["h"], p["k"], p["lt"], p.get("ht"), p.get("kt"), p.get("lt_tide"), 1.0, 1.0, 1.0)
+    solver = SeaLevelSolver(grid, p["h"], p["k"], p["lt"], p.get("ht"), p.get("kt"), p.get("lt_tide"), 1.0, 1.0, 1.0,
+                            **p.get("rotation", {}))
     channels = {name: torch.tensor(v, device=gpu) for name, v in kw.pop("channels", {}).items()}
     r = solver.solve_generalised(torch.tensor(p["ocean"], device=gpu), direct_load=torch.tensor(p["load"], device=gpu),
                                  **channels, **kw)
@@ -167,3 +168,52 @@ def test_gpu_sea_level_channels_match_oracle(gpu):
     for key in ("sea_level_change", "displacement", "potential", "tangential_potential", "toroidal_potential"):
         scale = np.max(np.abs(want[key]))
         assert np.max(np.abs(got[key] - want[key])) < 1e-10 * scale, key
+
+
+ROTATION = dict(omega=0.5, polar_moment=0.33, equatorial_moment=0.32, gravitational_constant=1.0, hc=0.1, kc=0.05,
+                m_u=0.01, m_phi=0.02, m_c=0.03)
+
+
+def rotation_oracle(p, ch, extra, rotation, **kw):
+    r = ROTATION
+    return sle_oracle.solve_generalised(p["synth"], p["expand"], p["integ"], p["h"], p["k"], p["lt"], 1.0, 1.0, 1.0,
+                                        p["ocean"], p["load"], **ch, ht=extra["ht"], kt=extra["kt"],
+                                        lt_tide=extra["lt_tide"], rotation=rotation, omega=r["omega"],
+                                        polar=r["polar_moment"], equatorial=r["equatorial_moment"],
+                                        G=r["gravitational_constant"], hc=r["hc"], kc=r["kc"], m_u=r["m_u"],
+                                        m_phi=r["m_phi"], m_c=r["m_c"], **kw)
+
+
+def test_oracle_rotation_moves_the_pole_and_keeps_the_budget():
+    """Full feedback (tests/TestSeaLevel.cpp:167-206's checks): an off-axis
+    load moves the pole; the ocean still gains the mass the load lost."""
+    lmax = 12
+    p = problem(lmax)
+    ch, extra = channel_forcing(p, lmax)
+    r = rotation_oracle(p, {}, extra, 2, rtol=1e-12, max_iterations=300)
+    assert r["converged"]
+    assert np.hypot(r["angular_velocity"][0], r["angular_velocity"][1]) > 0.0
+    gained = p["integ"](p["ocean"] * r["sea_level_change"])
+    assert abs(gained + p["integ"](p["load"])) < 1e-10 * abs(p["integ"](p["load"]))
+    axial = rotation_oracle(p, {}, extra, 1, rtol=1e-12, max_iterations=300)
+    assert axial["angular_velocity"][0] == 0.0 and axial["angular_velocity"][1] == 0.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rotation,with_channels", [(2, False), (2, True), (1, True)])
+def test_gpu_sea_level_rotation_matches_oracle(gpu, rotation, with_channels):
+    lmax = 16
+    p = problem(lmax)
+    ch, extra = channel_forcing(p, lmax)
+    ch = ch if with_channels else {}
+    kw = dict(inertia_moment_change=0.002, angular_momentum_change=(0.001, -0.002, 0.0005))
+    want = rotation_oracle(p, ch, extra, rotation, rtol=1e-11, max_iterations=300, **kw)
+    q = dict(p, **extra, rotation=dict(ROTATION, rotation=rotation))
+    got = _gpu_solve(gpu, q, lmax, rtol=1e-11, max_iterations=300, channels=ch, **kw)
+    # the last change sits near rtol in one case: the stopping pass may differ by one
+    assert want["converged"] and got["converged"] and abs(got["iterations"] - want["iterations"]) <= 1
+    for key in ("sea_level_change", "displacement", "potential", "tangential_potential"):
+        scale = np.max(np.abs(want[key]))
+        assert np.max(np.abs(got[key] - want[key])) < 1e-10 * scale, key
+    w = np.asarray(want["angular_velocity"])
+    assert np.max(np.abs(np.asarray(got["angular_velocity"]) - w)) < 1e-10 * np.max(np.abs(w))
