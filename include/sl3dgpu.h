@@ -343,6 +343,15 @@ void sl3dgpu_v3d_free_state(sl3dgpu_v3d_state* state);
  * advances in place. */
 int sl3dgpu_v3d_step(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme,
                      const double* load0, const double* load1, sl3dgpu_step_info* info);
+/* The same step with the tide channel beside the load (Viscoelastic3D::Step's
+ * tide, AddUnitChannels at Viscoelastic3D.cpp:1029-1073: the tide's (l, m >= 0)
+ * coefficients at the step's start and end times times each degree's
+ * K^-1 Tide, degree 0 with power 2); either pair may be null, all four are
+ * host or (on_device) device pointers. A tide with degree-1 coefficients is
+ * refused (TideColumns, Viscoelastic3D.cpp:137-154). */
+int sl3dgpu_v3d_step_tide(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme,
+                          const double* load0, const double* load1, const double* tide0, const double* tide1,
+                          int on_device, sl3dgpu_step_info* info);
 /* The same step with the load coefficients in device memory. */
 int sl3dgpu_v3d_step_device(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme,
                             const double* load0, const double* load1, sl3dgpu_step_info* info);

@@ -312,7 +312,8 @@ struct Flavour {
   std::vector<std::unique_ptr<DegreeOperator>> sph;
   std::vector<std::unique_ptr<ToroidalOperator>> tor;
   std::vector<Factor> sphF, torF;
-  std::vector<std::vector<double>> units;  // K^-1 Load per degree
+  std::vector<std::vector<double>> units;      // K^-1 Load per degree
+  std::vector<std::vector<double>> tideUnits;  // K^-1 Tide per degree (degree 0 with power 2)
   PointShear shear;
 };
 
@@ -662,18 +663,26 @@ class Viscoelastic3D {
     return SolveForces(sph, tor, f);
   }
 
-  // x += sigma_lm K^-1 Load (AddUnitChannels, the load channel alone).
-  void AddLoad(Solutions& x, const Flavour& f, const C* load) const {
-    if (load == nullptr) return;
-    for (int l = 0; l <= options_.lmax; ++l) {
-      const int ndof = f.sph[l]->DofCount();
-      for (int m = 0; m <= l; ++m) {
-        const C a = load[OGrid::Index(l, m)];
-        if (a == C{}) continue;
-        for (int d = 0; d < ndof; ++d) x.sph[l][static_cast<std::size_t>(m) * ndof + d] += a * f.units[l][d];
+  // x += sigma_lm K^-1 Load + tide_lm K^-1 Tide (AddUnitChannels,
+  // Viscoelastic3D.cpp:1029-1073: the load column, then the tide's).
+  void AddLoad(Solutions& x, const Flavour& f, const C* load, const C* tide = nullptr) const {
+    for (int which = 0; which < 2; ++which) {
+      const C* columns = which == 0 ? load : tide;
+      if (columns == nullptr) continue;
+      const auto& units = which == 0 ? f.units : f.tideUnits;
+      for (int l = 0; l <= options_.lmax; ++l) {
+        const int ndof = f.sph[l]->DofCount();
+        for (int m = 0; m <= l; ++m) {
+          const C a = columns[OGrid::Index(l, m)];
+          if (a == C{}) continue;
+          for (int d = 0; d < ndof; ++d) x.sph[l][static_cast<std::size_t>(m) * ndof + d] += a * units[l][d];
+        }
       }
     }
   }
+  // the running stage's tide at its start and end (null: none)
+  const C* tideStart_ = nullptr;
+  const C* tideEnd_ = nullptr;
 
   std::unique_ptr<Flavour> BuildFlavour(const PointShear* shear) const {
     auto f = std::make_unique<Flavour>();
@@ -685,6 +694,7 @@ class Viscoelastic3D {
     f->sphF.resize(L + 1);
     f->torF.resize(L + 1);
     f->units.resize(L + 1);
+    f->tideUnits.resize(L + 1);
 #pragma omp parallel for schedule(dynamic)
     for (int l = 0; l <= L; ++l) {
       f->sph[l] = std::make_unique<DegreeOperator>(*nodal_, l, options_.eps, use);
@@ -694,6 +704,11 @@ class Viscoelastic3D {
       const auto x = SolveComplex(f->sphF[l], b, 1);
       f->units[l].resize(x.size());
       for (std::size_t i = 0; i < x.size(); ++i) f->units[l][i] = x[i].real();
+      const auto tide = f->sph[l]->Tide(l == 0 ? 2 : -1);
+      std::vector<C> bt(tide.begin(), tide.end());
+      const auto xt = SolveComplex(f->sphF[l], bt, 1);
+      f->tideUnits[l].resize(xt.size());
+      for (std::size_t i = 0; i < xt.size(); ++i) f->tideUnits[l][i] = xt[i].real();
       if (l >= 1) {
         f->tor[l] = std::make_unique<ToroidalOperator>(*nodal_, l, options_.eps, use);
         f->torF[l] = FactorToroidal(*f->tor[l]);
@@ -745,7 +760,7 @@ class Viscoelastic3D {
     Spectral weighted = ZeroSpectral();
     Analyse(combined, weighted);
     auto solutions = SolveAll(weighted, *elastic_);
-    AddLoad(solutions, *elastic_, load);
+    AddLoad(solutions, *elastic_, load, tideStart_);
     return StrainOf(solutions, *elastic_);
   }
 
@@ -826,16 +841,19 @@ class Viscoelastic3D {
     const int L = options_.lmax;
     Solutions f;
     Forces(fixedS, flavour, f.sph, f.tor);
-    if (load != nullptr)
+    for (int which = 0; which < 2; ++which) {
+      const C* columns = which == 0 ? load : tideEnd_;
+      if (columns == nullptr) continue;
       for (int l = 0; l <= L; ++l) {
-        const auto vec = flavour.sph[l]->Load();
+        const auto vec = which == 0 ? flavour.sph[l]->Load() : flavour.sph[l]->Tide(l == 0 ? 2 : -1);
         const int ndof = flavour.sph[l]->DofCount();
         for (int m = 0; m <= l; ++m) {
-          const C a = load[OGrid::Index(l, m)];
+          const C a = columns[OGrid::Index(l, m)];
           if (a == C{}) continue;
           for (int d = 0; d < ndof; ++d) f.sph[l][static_cast<std::size_t>(m) * ndof + d] += a * vec[d];
         }
       }
+    }
     Tensor grid = ZeroTensor();
     Spectral analysed = ZeroSpectral();
     auto apply = [&](const Solutions& x) {
@@ -1173,7 +1191,7 @@ class Viscoelastic3D {
     // The load channel at the stage's end time.
     auto pass = [&](const Spectral& s) {
       solutions = respond(s);
-      AddLoad(solutions, flavour, loadEnd);
+      AddLoad(solutions, flavour, loadEnd, tideEnd_);
       return StrainOf(solutions, flavour);
     };
     if (samplePasses >= 0) {
@@ -1253,8 +1271,15 @@ class Viscoelastic3D {
 
   // Step (Viscoelastic3D.cpp:1982-2030): one stage, or Sdirk2's two backward
   // Euler stages of gamma dt, the second from (1 - r) m_n + r Y_1.
-  State Step(const State& state, double dt, Scheme scheme, const C* load0, const C* load1, Info& info) {
+  State Step(const State& state, double dt, Scheme scheme, const C* load0, const C* load1, Info& info,
+             const C* tide0 = nullptr, const C* tide1 = nullptr) {
     history_.clear();
+    struct Reset {
+      Viscoelastic3D* self;
+      ~Reset() { self->tideStart_ = self->tideEnd_ = nullptr; }
+    } reset{this};
+    tideStart_ = tide0;
+    tideEnd_ = tide1;
     if (scheme != Scheme::Sdirk2 || dt == 0.0) {
       const Scheme one = scheme == Scheme::Sdirk2 ? Scheme::BackwardEuler : scheme;
       return StepOnce(state, dt, one, load0, load1, info, last_);
@@ -1270,6 +1295,15 @@ class Viscoelastic3D {
         loadMid[i] = (1.0 - gamma) * (load0 ? load0[i] : C{}) + gamma * (load1 ? load1[i] : C{});
       mid = loadMid.data();
     }
+    std::vector<C> tideMid;
+    const C* tmid = nullptr;
+    if (tide0 != nullptr || tide1 != nullptr) {
+      tideMid.assign(size, C{});
+      for (std::size_t i = 0; i < size; ++i)
+        tideMid[i] = (1.0 - gamma) * (tide0 ? tide0[i] : C{}) + gamma * (tide1 ? tide1[i] : C{});
+      tmid = tideMid.data();
+    }
+    tideEnd_ = tmid;
     Info i1, i2;
     State y1 = StepOnce(state, h, Scheme::BackwardEuler, load0, mid, i1, last_);
     const double r = (1.0 - gamma) / gamma;
@@ -1289,6 +1323,8 @@ class Viscoelastic3D {
     }
     from.strain = y1.strain;
     from.strainCoefficients = y1.strainCoefficients;
+    tideStart_ = tmid;
+    tideEnd_ = tide1;
     State out = StepOnce(from, h, Scheme::BackwardEuler, mid, load1, i2, last_);
     out.t = state.t + dt;
     info.iterations = i1.iterations + i2.iterations;
@@ -1401,6 +1437,27 @@ int oracle_v3d_step(oracle_v3d* h, oracle_state* state, double dt, int scheme, c
   try {
     state->s = h->op->Step(state->s, dt, static_cast<sl3dgpu::host::Scheme>(scheme),
                            reinterpret_cast<const C*>(load0), reinterpret_cast<const C*>(load1), i);
+  } catch (const std::exception&) {
+    return -3;
+  }
+  if (info) {
+    info->iterations = i.iterations;
+    info->residual = i.residual;
+    info->converged = i.converged ? 1 : 0;
+    info->mixed_passes = i.mixedPasses;
+    info->correction_passes = 0;
+    info->solve_iterations = i.solveIterations;
+  }
+  return 0;
+}
+
+int oracle_v3d_step_tide(oracle_v3d* h, oracle_state* state, double dt, int scheme, const double* load0,
+                         const double* load1, const double* tide0, const double* tide1, sl3dgpu_step_info* info) {
+  oracle::Info i;
+  try {
+    state->s = h->op->Step(state->s, dt, static_cast<sl3dgpu::host::Scheme>(scheme),
+                           reinterpret_cast<const C*>(load0), reinterpret_cast<const C*>(load1), i,
+                           reinterpret_cast<const C*>(tide0), reinterpret_cast<const C*>(tide1));
   } catch (const std::exception&) {
     return -3;
   }

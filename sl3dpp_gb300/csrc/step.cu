@@ -210,7 +210,8 @@ class Viscoelastic3DGpu {
   int SetDelta(const double* samples, bool onDevice);
   int ZeroState(V3dState& st);
   int Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1, sl3dgpu_step_info* info,
-           bool onDevice = false);
+           bool onDevice = false, const double* tide0 = nullptr, const double* tide1 = nullptr);
+  Dev<double2> tideDev0, tideDev1, tideDevMid;
   int Surface(int component, double* out);
   int StrainReference(const V3dState& st, double* out);
 
@@ -231,7 +232,11 @@ class Viscoelastic3DGpu {
   int AnalyseWeighted(const GridTensor& in, const double* w, double2* spectral);  // accumulate, lateral nodes
   int WeightedPass(const double2* strain, double2* out);                           // accumulate, lateral nodes
   int Solve(const Flavour& f);
-  int Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma, double2* next);
+  int Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma, const double2* tide,
+           double2* next);
+  // the running stage's tide coefficients at its start and end (null: none)
+  const double2* tideStart = nullptr;
+  const double2* tideEnd = nullptr;
   int RelativeChange(const double2* next, const double2* now, double* residual);
   int MixerReset();
   int MixerUpdate(int& count, int& slot, bool& first);
@@ -771,6 +776,7 @@ int Viscoelastic3DGpu::SolveColumns(const Flavour& f, double2* sph, double2* tor
 }
 
 int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma,
+                            const double2* tide,
                             double2* next) {
   const double2* force = analysedStart.p;
   if (!useStart) {
@@ -784,8 +790,8 @@ int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useSta
   LaunchForces(geo, force, rhsSph.p, rhsTor.p, stream);
   SL3D_CHECK_LAUNCH();
   SL3D_TRY(Solve(f));
-  if (sigma != nullptr) {
-    LaunchAddLoad(geo, sigma, f.units.p, f.unitOffset.p, rhsSph.p, stream);
+  if (sigma != nullptr || tide != nullptr) {
+    LaunchAddLoad(geo, sigma, f.units.p, f.unitOffset.p, rhsSph.p, stream, tide, f.tideUnits.p);
     SL3D_CHECK_LAUNCH();
   }
   LaunchStrain(geo, rhsSph.p, rhsTor.p, next, stream);
@@ -885,7 +891,7 @@ int Viscoelastic3DGpu::ElasticStrain(const V3dState& st, const double2* sigma) {
   V3dState& mutableSt = const_cast<V3dState&>(st);
   LaunchSpectralSum(SpectralArgs(0, 0.0, st, mutableSt, nullptr, analysedStart.p), stream);
   SL3D_CHECK_LAUNCH();
-  return Pass(*elastic, nullptr, true, sigma, s.p);
+  return Pass(*elastic, nullptr, true, sigma, tideStart, s.p);
 }
 
 int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
@@ -995,7 +1001,7 @@ int Viscoelastic3DGpu::Converge(const Flavour& f, const double2* sigmaEnd, sl3dg
     if (iteration == 0) {
       SL3D_TRY(FirstPass(f, sigmaEnd, &residual));
     } else {
-      SL3D_TRY(Pass(f, s.p, false, sigmaEnd, sNext.p));
+      SL3D_TRY(Pass(f, s.p, false, sigmaEnd, tideEnd, sNext.p));
       SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
     }
     history.push_back(residual);
@@ -1042,7 +1048,7 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
   stageGuess = nullptr;
   for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
     double residual = 0.0;
-    SL3D_TRY(Pass(f, s.p, iteration == 0, sigmaEnd, sNext.p));
+    SL3D_TRY(Pass(f, s.p, iteration == 0, sigmaEnd, tideEnd, sNext.p));
     SL3D_TRY(RelativeChange(sNext.p, s.p, &residual));
     history.push_back(residual);
     info.iterations = iteration + 1;
@@ -1076,13 +1082,13 @@ int Viscoelastic3DGpu::ConvergeMixed(const Flavour& f, const double2* sigmaEnd, 
 // the guess; the iteration continues from whichever left the smaller
 // relative change (the guess discarded otherwise), its next iterate in sNext.
 int Viscoelastic3DGpu::FirstPass(const Flavour& f, const double2* sigmaEnd, double* residual) {
-  SL3D_TRY(Pass(f, s.p, true, sigmaEnd, sNext.p));
+  SL3D_TRY(Pass(f, s.p, true, sigmaEnd, tideEnd, sNext.p));
   double plain = 0.0;
   SL3D_TRY(RelativeChange(sNext.p, s.p, &plain));
   *residual = plain;
   if (stageGuess == nullptr) return SL3DGPU_OK;
   stageGuess = nullptr;
-  SL3D_TRY(Pass(f, guess.p, false, sigmaEnd, guessNext.p));
+  SL3D_TRY(Pass(f, guess.p, false, sigmaEnd, tideEnd, guessNext.p));
   double tried = 0.0;
   SL3D_TRY(RelativeChange(guessNext.p, guess.p, &tried));
   if (std::isfinite(tried) && tried < plain) {
@@ -1092,7 +1098,7 @@ int Viscoelastic3DGpu::FirstPass(const Flavour& f, const double2* sigmaEnd, doub
     guessTaken = 1;
   } else if (plain <= options.rtol) {
     // the plain start converges at once: its solutions back for Surface
-    SL3D_TRY(Pass(f, s.p, true, sigmaEnd, sNext.p));
+    SL3D_TRY(Pass(f, s.p, true, sigmaEnd, tideEnd, sNext.p));
   }
   return SL3DGPU_OK;
 }
@@ -1564,8 +1570,8 @@ int Viscoelastic3DGpu::ConvergeConjugateGradients(const Flavour& f, const double
   SL3D_CUDA(cudaMemsetAsync(cgF.p, 0, Columns() * sizeof(double2), stream));
   LaunchForces(geo, fixedS.p, cgF.p, cgF.p + rhsSphComplex, stream);
   SL3D_CHECK_LAUNCH();
-  if (sigmaEnd != nullptr) {
-    LaunchAddLoad(geo, sigmaEnd, f.loadForces.p, f.unitOffset.p, cgF.p, stream);
+  if (sigmaEnd != nullptr || tideEnd != nullptr) {
+    LaunchAddLoad(geo, sigmaEnd, f.loadForces.p, f.unitOffset.p, cgF.p, stream, tideEnd, f.tideForces.p);
     SL3D_CHECK_LAUNCH();
   }
   SL3D_TRY(ConjugateGradients(f, true, options.solve_rtol, options.solve_max_iterations, info));
@@ -1710,12 +1716,34 @@ int Viscoelastic3DGpu::SolveLateral(const double* load, double rtol, int maxIter
 // Step (Viscoelastic3D.cpp:1982-2030): one stage, or Sdirk2's two backward
 // Euler stages of gamma dt, the second from (1 - r) m_n + r Y_1.
 int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1,
-                            sl3dgpu_step_info* infoOut, bool onDevice) {
+                            sl3dgpu_step_info* infoOut, bool onDevice, const double* tide0, const double* tide1) {
   if (!(dt >= 0.0) || scheme < 0 || scheme > 2) {
     SetError("v3d: dt >= 0 and a scheme of 0 (trapezoid), 1 (backward Euler) or 2 (Sdirk2)");
     return SL3DGPU_ERR_ARGUMENT;
   }
   const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  // The tide channel (TideColumns, Viscoelastic3D.cpp:137-154): its degree-1
+  // columns must vanish, a tide being taken relative to the centre of mass.
+  const double2* t0 = nullptr;
+  const double2* t1 = nullptr;
+  for (int end = 0; end < 2; ++end) {
+    const double* tide = end ? tide1 : tide0;
+    if (tide == nullptr) continue;
+    Dev<double2>& dev = end ? tideDev1 : tideDev0;
+    if (dev.n != lm) SL3D_CUDA(dev.Alloc(lm));
+    SL3D_CUDA(cudaMemcpyAsync(dev.p, tide, lm * sizeof(double2),
+                              onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+    double2 degreeOne[2];
+    SL3D_CUDA(cudaMemcpyAsync(degreeOne, dev.p + 1, 2 * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    for (const auto& v : degreeOne)
+      if (v.x != 0.0 || v.y != 0.0) {
+        SetError("v3d: a tide channel has no degree-1 part: tides are taken relative to the centre of mass, its "
+                 "degree-1 columns must vanish");
+        return SL3DGPU_ERR_ARGUMENT;
+      }
+    (end ? t1 : t0) = dev.p;
+  }
   const double2* s0 = nullptr;
   const double2* s1 = nullptr;
   const cudaMemcpyKind kind = onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -1743,6 +1771,8 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     SL3D_CHECK_LAUNCH();
     haveGuess = true;
   }
+  tideStart = t0;
+  tideEnd = t1;
   if (scheme != 2 || dt == 0.0) {
     const int one = scheme == 2 ? 1 : scheme;
     stageGuess = haveGuess ? guess.p : nullptr;
@@ -1757,6 +1787,14 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
       SL3D_CHECK_LAUNCH();
       mid = sigmaMid.p;
     }
+    const double2* tmid = nullptr;
+    if (t0 || t1) {
+      if (tideDevMid.n != lm) SL3D_CUDA(tideDevMid.Alloc(lm));
+      LaunchBlend(static_cast<long long>(lm), gamma, t0, t1, tideDevMid.p, stream);
+      SL3D_CHECK_LAUNCH();
+      tmid = tideDevMid.p;
+    }
+    tideEnd = tmid;
     sl3dgpu_step_info i1{}, i2{};
     // the first stage's guess (the mixed form, which takes it at no FP64
     // cost): (1 - gamma) s_n + gamma guess
@@ -1782,6 +1820,8 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
       SL3D_CHECK_LAUNCH();
     }
     stageGuess = haveGuess ? guess.p : nullptr;
+    tideStart = tmid;
+    tideEnd = t1;
     SL3D_TRY(StepOnce(scratch, scratch, h, 1, mid, s1, i2));
     info.iterations = i1.iterations + i2.iterations;
     info.mixed_passes = i1.mixed_passes + i2.mixed_passes;
@@ -1792,6 +1832,7 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   }
   guessArmed = false;  // a warm start serves one step
   stageGuess = nullptr;
+  tideStart = tideEnd = nullptr;
   if (options.warm_start == 1 && st.hasCoeffs) {
     SL3D_CUDA(cudaMemcpyAsync(st.prev.p, st.coeffs.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
                               stream));
@@ -1948,6 +1989,16 @@ extern "C" int sl3dgpu_v3d_step_device(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state,
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.Step(state->st, dt, scheme, load0, load1, info, true);
+}
+
+extern "C" int sl3dgpu_v3d_step_tide(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, double dt, int scheme,
+                                     const double* load0, const double* load1, const double* tide0,
+                                     const double* tide1, int on_device, sl3dgpu_step_info* info) {
+  if (h == nullptr || state == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Step(state->st, dt, scheme, load0, load1, info, on_device != 0, tide0, tide1);
 }
 
 extern "C" int sl3dgpu_v3d_set_start(sl3dgpu_v3d* h, const double* coefficients, int on_device) {

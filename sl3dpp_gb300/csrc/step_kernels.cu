@@ -399,19 +399,26 @@ __global__ void DilatationForceKernel(Geometry g, const double2* scalar, double2
   }
 }
 
-__global__ void AddLoadKernel(Geometry g, const double2* sigma, const double* units,
-                              const long long* unitOffset, double2* sol) {
+// x += sigma_lm units_l (+ tide_lm tideUnits_l): AddUnitChannels
+// (Viscoelastic3D.cpp:1029-1073), the load column then the tide's; either
+// coefficient array may be null.
+__global__ void AddLoadKernel(Geometry g, const double2* sigma, const double* units, const double2* tide,
+                              const double* tideUnits, const long long* unitOffset, double2* sol) {
   const int l = blockIdx.x;
   const DegreeInfo d = g.degrees[l];
   const int cols = l + 1;
   const long long total = static_cast<long long>(d.sphNdof) * cols;
   for (long long t = threadIdx.x; t < total; t += blockDim.x) {
     const int dof = static_cast<int>(t / cols), m = static_cast<int>(t % cols);
-    const double2 a = sigma[l * (l + 1) / 2 + m];
-    if (a.x == 0.0 && a.y == 0.0) continue;
-    const double u = units[unitOffset[l] + dof];
     double2& x = sol[d.sphRhs + t];
-    x = CAdd(x, CScale(u, a));
+    if (sigma != nullptr) {
+      const double2 a = sigma[l * (l + 1) / 2 + m];
+      if (a.x != 0.0 || a.y != 0.0) x = CAdd(x, CScale(units[unitOffset[l] + dof], a));
+    }
+    if (tide != nullptr) {
+      const double2 a = tide[l * (l + 1) / 2 + m];
+      if (a.x != 0.0 || a.y != 0.0) x = CAdd(x, CScale(tideUnits[unitOffset[l] + dof], a));
+    }
   }
 }
 
@@ -1114,9 +1121,10 @@ void LaunchDilatationForce(const Geometry& g, const double2* scalar, double2* rh
 }
 
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units, const long long* unitOffset,
-                   double2* solSph, cudaStream_t stream) {
+                   double2* solSph, cudaStream_t stream, const double2* tide, const double* tideUnits) {
+  if (sigma == nullptr && tide == nullptr) return;
   prof::Scope scope(prof::kOther, stream);
-  AddLoadKernel<<<g.lmax + 1, 256, 0, stream>>>(g, sigma, units, unitOffset, solSph);
+  AddLoadKernel<<<g.lmax + 1, 256, 0, stream>>>(g, sigma, units, tide, tideUnits, unitOffset, solSph);
 }
 
 void LaunchSurface(const Geometry& g, const double2* solSph, int component, double2* out, cudaStream_t stream) {

@@ -78,9 +78,11 @@ void LaunchDilatation(const Geometry& g, const double2* solSph, double2* scalar,
 // GridCoupling::DilatationForce (:433-495): a weighted dilatation's force
 // added onto every degree's spheroidal right-hand sides.
 void LaunchDilatationForce(const Geometry& g, const double2* scalar, double2* rhsSph, cudaStream_t stream);
-// x += sigma_lm K^-1 Load for every degree (AddUnitChannels' load part).
+// x += sigma_lm K^-1 Load (+ tide_lm K^-1 Tide) for every degree
+// (AddUnitChannels); sigma or tide may be null.
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units,
-                   const long long* unitOffset, double2* solSph, cudaStream_t stream);
+                   const long long* unitOffset, double2* solSph, cudaStream_t stream,
+                   const double2* tide = nullptr, const double* tideUnits = nullptr);
 // Surface values of a component (U, V or phi) for every (l, m >= 0).
 void LaunchSurface(const Geometry& g, const double2* solSph, int component, double2* out,
                    cudaStream_t stream);

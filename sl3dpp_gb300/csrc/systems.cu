@@ -219,16 +219,24 @@ int BuildSystems(const SystemsInput& in, Flavour& f) {
   SL3D_TRY(upload(f.sphLu, f.dSphLu, f.iSphLu, f.nSphLu));
   SL3D_TRY(upload(f.torChol, f.dTorChol, f.iTorChol, f.nTorChol));
   // The load units K^-1 Load per degree (AddUnitChannels' cached responses).
-  std::vector<double> units;
+  // The tide channel's, K^-1 Tide with the degree's power (degree 0 the
+  // spherical mean of a centrifugal change, power 2: Viscoelastic3D.cpp:1049).
+  std::vector<double> units, tides;
   std::vector<long long> unitOffset(L + 1);
   for (int l = 0; l <= L; ++l) {
     unitOffset[l] = static_cast<long long>(units.size());
     const auto load = sph[l]->Load();
     units.insert(units.end(), load.begin(), load.end());
+    const auto tide = sph[l]->Tide(l == 0 ? 2 : -1);
+    tides.insert(tides.end(), tide.begin(), tide.end());
   }
   SL3D_CUDA(f.units.Upload(units));
+  SL3D_CUDA(f.tideUnits.Upload(tides));
   SL3D_CUDA(f.unitOffset.Upload(unitOffset));
-  if (in.apply) SL3D_CUDA(f.loadForces.Upload(units));  // before the solve turns them into responses
+  if (in.apply) {  // before the solve turns them into responses
+    SL3D_CUDA(f.loadForces.Upload(units));
+    SL3D_CUDA(f.tideForces.Upload(tides));
+  }
   auto unitSystems = [&](const std::vector<sl3dgpu_band_system>& src) {
     std::vector<sl3dgpu_band_system> out;
     for (auto s : src) {
@@ -250,6 +258,8 @@ int BuildSystems(const SystemsInput& in, Flavour& f) {
     SL3D_TRY(upload(sys, d, items, count));
     SL3D_TRY(BandSolveBatch(d.p, sys.data(), static_cast<int>(sys.size()), items.p, count, f.bands.p, f.pivots.p,
                             f.units.p, f.scales.p, lu, stream));
+    SL3D_TRY(BandSolveBatch(d.p, sys.data(), static_cast<int>(sys.size()), items.p, count, f.bands.p, f.pivots.p,
+                            f.tideUnits.p, f.scales.p, lu, stream));
     SL3D_CUDA(cudaStreamSynchronize(stream));
   }
   if (in.fp32) {

@@ -75,6 +75,9 @@ struct Flavour {
   int scheme = 0;
   double dt = 0.0;
   Dev<double> bands, scales, units;
+  // the tide channel's units K^-1 Tide per degree (the same offsets as units)
+  // and, for conjugate gradients, the unsolved vectors
+  Dev<double> tideUnits, tideForces;
   Dev<float> bands32, scales32;  // the mixed form's FP32 copies
   // conjugate gradients: the assembled (unscaled) bands for K x, their
   // systems, and the unsolved load force vectors (DegreeOperator::Load)

@@ -87,6 +87,7 @@ def _signatures():
         "sl3dgpu_v3d_residual_history": (i, [v, P_double, i]),
         "sl3dgpu_v3d_correction_history": (i, [v, P_double, i]),
         "sl3dgpu_v3d_step_device": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_step_tide": (i, [v, v, d, i, v, v, v, v, i, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_stream": (v, [v]),
         "sl3dgpu_v3d_set_start": (i, [v, v, i]),
         "sl3dgpu_v3d_start_taken": (i, [v]),
@@ -196,15 +197,26 @@ class Viscoelastic3D:
     def ZeroState(self) -> State:
         return State(self)
 
-    def Step(self, state: State, dt: float, scheme="sdirk2", load0=None, load1=None) -> StepInfo:
-        """One step of length dt (non-dimensional) under the load channel."""
+    def Step(self, state: State, dt: float, scheme="sdirk2", load0=None, load1=None, tide0=None,
+             tide1=None) -> StepInfo:
+        """One step of length dt (non-dimensional) under the load channel and,
+        given, the tide channel (Viscoelastic3D::Step's load and tide: (l, m >= 0)
+        coefficients at the step's start and end; a tide has no degree-0 or
+        degree-1 part beyond its degree-0 centrifugal mean)."""
         code = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
         info = StepInfo()
         a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.complex128)
         b = None if load1 is None else np.ascontiguousarray(load1, dtype=np.complex128)
-        check(lib().sl3dgpu_v3d_step(self._h, state._h, float(dt), code,
-                                     None if a is None else a.ctypes.data,
-                                     None if b is None else b.ctypes.data, ctypes.byref(info)))
+        if tide0 is None and tide1 is None:
+            check(lib().sl3dgpu_v3d_step(self._h, state._h, float(dt), code,
+                                         None if a is None else a.ctypes.data,
+                                         None if b is None else b.ctypes.data, ctypes.byref(info)))
+            return info
+        c = None if tide0 is None else np.ascontiguousarray(tide0, dtype=np.complex128)
+        e = None if tide1 is None else np.ascontiguousarray(tide1, dtype=np.complex128)
+        ptr = lambda x: None if x is None else x.ctypes.data
+        check(lib().sl3dgpu_v3d_step_tide(self._h, state._h, float(dt), code, ptr(a), ptr(b), ptr(c), ptr(e), 0,
+                                          ctypes.byref(info)))
         return info
 
     def StepDevice(self, state: State, dt: float, scheme, load0, load1) -> StepInfo:

@@ -181,6 +181,7 @@ def _v3d_sigs(L):
         "oracle_v3d_zero_state": (v, [v]),
         "oracle_v3d_free_state": (None, [v]),
         "oracle_v3d_step": (i, [v, v, d, i, v, v, _ct.POINTER(StepInfo)]),
+        "oracle_v3d_step_tide": (i, [v, v, d, i, v, v, v, v, _ct.POINTER(StepInfo)]),
         "oracle_v3d_surface": (None, [v, i, v]),
         "oracle_v3d_state_strain": (i, [v, v]),
         "oracle_v3d_residual_history": (i, [v, P_double, i]),
@@ -241,13 +242,15 @@ class OracleStep:
         assert samples.size == self.P * self.ntheta * self.nphi
         self.L.oracle_v3d_set_delta(self.h, ptr(samples))
 
-    def step(self, dt, scheme=2, load0=None, load1=None):
+    def step(self, dt, scheme=2, load0=None, load1=None, tide0=None, tide1=None):
         info = StepInfo()
-        a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.complex128)
-        b = None if load1 is None else np.ascontiguousarray(load1, dtype=np.complex128)
-        st = self.L.oracle_v3d_step(self.h, self.state, dt, scheme,
-                                    None if a is None else a.ctypes.data, None if b is None else b.ctypes.data,
-                                    _ct.byref(info))
+        cols = [None if c is None else np.ascontiguousarray(c, dtype=np.complex128)
+                for c in (load0, load1, tide0, tide1)]
+        p = [None if c is None else c.ctypes.data for c in cols]
+        if tide0 is None and tide1 is None:
+            st = self.L.oracle_v3d_step(self.h, self.state, dt, scheme, p[0], p[1], _ct.byref(info))
+        else:
+            st = self.L.oracle_v3d_step_tide(self.h, self.state, dt, scheme, *p, _ct.byref(info))
         assert st == 0
         return info
 

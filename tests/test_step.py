@@ -64,6 +64,40 @@ def test_lateral_viscosity_couples_orders():
     assert np.max(np.abs(U[rest])) > 1e-6 * np.max(np.abs(U[zonal]))
 
 
+def tide_columns(lmax, scale=1e-4):
+    """A degree-2 tide (orders 0 and 2) with a degree-0 centrifugal mean."""
+    t = np.zeros((lmax + 1) * (lmax + 2) // 2, dtype=np.complex128)
+    t[configs.real_index(0, 0)] = 0.3 * scale
+    t[configs.real_index(2, 0)] = scale
+    t[configs.real_index(2, 2)] = (0.5 - 0.25j) * scale
+    return t
+
+
+def test_tide_channel_is_degree_local_and_superposes_with_the_load():
+    # zero lateral contrast: the tide moves only its own degrees and orders,
+    # and a step under load and tide is the sum of the two steps apart
+    # (AddUnitChannels adds both columns to the same right-hand side)
+    lmax = 8
+    dt = None
+    out = []
+    for use_load, use_tide in ((True, False), (False, True), (True, True)):
+        st = O.OracleStep(O.standard_earth(20), O.default_options(lmax))
+        load = cap_load(lmax, st.sigma_scale, 2000.0)
+        tide = tide_columns(lmax)
+        dt = 500 * configs.SECONDS_PER_YEAR / st.time_scale
+        for n in range(2):
+            info = st.step(dt, 2, load * n / 10 if use_load else None, load * (n + 1) / 10 if use_load else None,
+                           tide * n if use_tide else None, tide * (n + 1) if use_tide else None)
+            assert info.converged
+        out.append(st.surface(0))
+    U_load, U_tide, U_both = out
+    touched = [configs.real_index(l, m) for l, m in ((0, 0), (2, 0), (2, 2))]
+    rest = np.setdiff1d(np.arange(U_tide.size), touched)
+    assert np.max(np.abs(U_tide[rest])) < 1e-14 * np.max(np.abs(U_tide))
+    assert abs(U_tide[configs.real_index(2, 2)] / U_tide[configs.real_index(2, 0)] - (0.5 - 0.25j)) < 1e-12
+    assert rel(U_both, U_load + U_tide) < 1e-12
+
+
 # -- the GPU step against the oracle ------------------------------------------------------------
 
 def _pair(lmax, elements, ngll, kelvin=0.0, rms=0.5, ldelta=4, seed=11, **opt):
@@ -155,3 +189,39 @@ def test_gpu_residual_history_matches_oracle_at_high_contrast(gpu):
     ho, hg = o.residual_history(), g.residual_history()
     assert ho.size == hg.size == 80
     assert np.max(np.abs(hg - ho) / ho) < 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", [2, 0])
+def test_gpu_step_with_tide_matches_oracle(gpu, scheme):
+    # the tide channel beside the load under a lateral contrast: the tide's
+    # columns enter every pass's right-hand side (and, in Sdirk2, its blend
+    # at the inner stage time) as in the oracle
+    lmax = 8
+    o, g = _pair(lmax, 20, 5)
+    state = g.ZeroState()
+    load = cap_load(lmax, o.sigma_scale, 2000.0)
+    tide = tide_columns(lmax)
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    for n in range(2):
+        l0, l1 = load * n / 10, load * (n + 1) / 10
+        t0, t1 = tide * np.cos(n), tide * np.cos(n + 1)
+        io = o.step(dt, scheme, l0, l1, t0, t1)
+        ig = g.Step(state, dt, scheme, l0, l1, t0, t1)
+        assert ig.converged == io.converged == 1
+        for comp in (0, 2):
+            assert rel(g.Surface(comp), o.surface(comp)) < TOL, (n, comp)
+
+
+@pytest.mark.gpu
+def test_gpu_step_refuses_a_degree_one_tide(gpu):
+    from sl3dpp_gb300._lib import Sl3dgpuError
+
+    lmax = 8
+    o, g = _pair(lmax, 20, 5, rms=0.0)
+    state = g.ZeroState()
+    tide = tide_columns(lmax)
+    tide[configs.real_index(1, 1)] = 1e-6
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    with pytest.raises(Sl3dgpuError, match="degree-1"):
+        g.Step(state, dt, 2, None, None, None, tide)
