@@ -202,21 +202,32 @@ __device__ inline void CpCommit() { asm volatile("cp.async.commit_group;\n" ::: 
 __device__ inline void CpWaitAll() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 __device__ inline void CpWaitOne() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
+// The solution ring's slots: in FP64 twice the depth, the Cholesky
+// substitution keeping a mirror of every slot at slot + depth so that its
+// reads need no wrap (fewer integer instructions beside the FP64 ones, which
+// bound it); in FP32 the wrapped ring alone (the mirror's larger staging cost
+// the windowed FP32 solves more than the wrap did).
+template <class T>
+__host__ __device__ constexpr int RingSlots(int depth) {
+  return sizeof(T) == sizeof(double) ? 2 * depth : depth;
+}
+
 // A solve launch's per-warp shared-memory plan.
 struct SolvePlan {
   int depth;    // ring slots: the solve's reach + 1
   int bandCap;  // band values one staged chunk holds
   template <class T>
   __host__ __device__ long long Bytes() const {
-    const long long pairs = static_cast<long long>(depth) * kWarp + static_cast<long long>(kBuffers) * kChunk * kWarp;
+    const long long pairs = static_cast<long long>(RingSlots<T>(depth)) * kWarp +
+                            static_cast<long long>(kBuffers) * kChunk * kWarp;
     const long long b = pairs * 2 * sizeof(T) + static_cast<long long>(kBuffers) * (bandCap + kChunk) * sizeof(T) +
                         static_cast<long long>(kBuffers) * kChunk * sizeof(int);
     return (b + 15) / 16 * 16;
   }
 };
 
-// One warp's staging: the solution ring (depth x 32 lane pairs, each lane's
-// own columns), and kBuffers of band columns, right-hand-side rows (lane
+// One warp's staging: the solution ring (RingSlots x 32 lane pairs, each
+// lane's own columns; in FP64 slots depth.. mirror slots 0..), and kBuffers of band columns, right-hand-side rows (lane
 // pairs), row scales and pivots.
 template <class T>
 struct Stage {
@@ -229,7 +240,7 @@ struct Stage {
   int bandCap;
   __device__ Stage(unsigned char* base, const SolvePlan& plan) : bandCap(plan.bandCap) {
     ring = reinterpret_cast<T2*>(base);
-    rhs = ring + static_cast<long long>(plan.depth) * kWarp;
+    rhs = ring + static_cast<long long>(RingSlots<T>(plan.depth)) * kWarp;
     band = reinterpret_cast<T*>(rhs + static_cast<long long>(kBuffers) * kChunk * kWarp);
     scale = band + static_cast<long long>(kBuffers) * plan.bandCap;
     pivot = reinterpret_cast<int*>(scale + kBuffers * kChunk);
@@ -396,6 +407,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
   const WorkItem item = items[warp];
   const Lane<T> ln = LaneOf(systems[item.system], rhs, item.column, lane);
   const int n = ln.s.n, kd = ln.s.ku, ld = kd + 1, depth = plan.depth;
+  constexpr bool kMirror = RingSlots<T>(1) == 2;
   const T* ab = bands + ln.s.band;
   T2* ring = st.ring + lane;
   int lo = 0, hi = n - 1;
@@ -416,6 +428,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
         v.y /= f;
       }
       ring[(r % depth) * kWarp] = v;
+      if constexpr (kMirror) ring[(r % depth + depth) * kWarp] = v;
     }
   } else {
     // U^T y = b, forward: chunk c holds rows [lo + c kChunk, ...) and their
@@ -437,11 +450,13 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
             T2 a = j <= hi ? Start(ln, st, buf, j - j0, j, lane) : zero;
             T2 b = zero;
             const int reach = min(kd, j - lo);
+            // row j - t: slot + depth - t of the mirrored ring, else wrapped
+            const T2* back = ring + (slot + depth) * kWarp;
             int t = 1;
             for (; t + 1 <= reach; t += 2) {
               const T u0 = column[-t], u1 = column[-t - 1];
-              const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
-              const T2 y1 = ring[SlotBack(slot, t + 1, depth) * kWarp];
+              const T2 y0 = kMirror ? back[-t * kWarp] : ring[SlotBack(slot, t, depth) * kWarp];
+              const T2 y1 = kMirror ? back[-(t + 1) * kWarp] : ring[SlotBack(slot, t + 1, depth) * kWarp];
               a.x -= u0 * y0.x;
               a.y -= u0 * y0.y;
               b.x -= u1 * y1.x;
@@ -449,7 +464,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
             }
             if (t <= reach) {
               const T u0 = column[-t];
-              const T2 y0 = ring[SlotBack(slot, t, depth) * kWarp];
+              const T2 y0 = kMirror ? back[-t * kWarp] : ring[SlotBack(slot, t, depth) * kWarp];
               a.x -= u0 * y0.x;
               a.y -= u0 * y0.y;
             }
@@ -457,6 +472,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
             y.x = (a.x + b.x) * inv;
             y.y = (a.y + b.y) * inv;
             ring[slot * kWarp] = y;
+            if constexpr (kMirror) ring[(slot + depth) * kWarp] = y;
             ln.Store(j, y);
             slot = SlotAhead(slot, 1, depth);
           }
@@ -484,12 +500,14 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
           T2 a = rhsEnd > 0 ? st.Rhs(buf, r)[lane] : zero;
           T2 b = zero;
           const int reach = min(kd, n - 1 - i);
+          // row i + t: slot + t of the mirrored ring, else wrapped
+          const T2* ahead = ring + slot * kWarp;
           int t = 1;
           for (; t + 1 <= reach; t += 2) {
             const T u0 = band[(r + t) * ld + kd - t];  // U(i, i + t)
             const T u1 = band[(r + t + 1) * ld + kd - t - 1];
-            const T2 y0 = ring[SlotAhead(slot, t, depth) * kWarp];
-            const T2 y1 = ring[SlotAhead(slot, t + 1, depth) * kWarp];
+            const T2 y0 = kMirror ? ahead[t * kWarp] : ring[SlotAhead(slot, t, depth) * kWarp];
+            const T2 y1 = kMirror ? ahead[(t + 1) * kWarp] : ring[SlotAhead(slot, t + 1, depth) * kWarp];
             a.x -= u0 * y0.x;
             a.y -= u0 * y0.y;
             b.x -= u1 * y1.x;
@@ -497,7 +515,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
           }
           if (t <= reach) {
             const T u0 = band[(r + t) * ld + kd - t];
-            const T2 y0 = ring[SlotAhead(slot, t, depth) * kWarp];
+            const T2 y0 = kMirror ? ahead[t * kWarp] : ring[SlotAhead(slot, t, depth) * kWarp];
             a.x -= u0 * y0.x;
             a.y -= u0 * y0.y;
           }
@@ -505,6 +523,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
           v.x = (a.x + b.x) * inv;
           v.y = (a.y + b.y) * inv;
           ring[slot * kWarp] = v;
+          if constexpr (kMirror) ring[(slot + depth) * kWarp] = v;
           if (ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
           ln.Store(i, v);
           slot = SlotBack(slot, 1, depth);

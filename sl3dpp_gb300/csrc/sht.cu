@@ -402,6 +402,9 @@ __device__ inline int RingTransform(T2* a, T2* b, const FftPlan& plan, const T2*
   }
 }
 
+// A hint that the line holding p will be read soon (no register waits on it).
+__device__ inline void PrefetchL2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Ring modes: spectra -> fields; fields (times an optional weight) ->
 // spectra; spectra -> fields -> weight -> spectra without leaving shared
 // memory.
@@ -455,6 +458,20 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   const int groups = min(G * perRing, count - p0);  // fields of this CTA
   const int rings = (groups + perRing - 1) / perRing;
   const int mcount = real ? lmax + 1 : 2 * lmax + 1;
+  if (mode == kRingSynth || mode == kRingWeighted) {
+    // ask L2 for this CTA's spectra (one line an order) and, weighted, for
+    // the rings' point weights (read after the synthesis): their DRAM
+    // latency then overlaps the twiddle loads and the transform
+    for (int mi = threadIdx.x; mi < mcount; mi += blockDim.x)
+      PrefetchL2(spectraIn + (static_cast<long long>(mi) * ntheta + j) * count + p0);
+    if (mode == kRingWeighted) {
+      const int f = p0 + perRing * (threadIdx.x / kWarp) + (threadIdx.x % 2);
+      const int lines = (n * static_cast<int>(sizeof(T)) + 127) / 128;
+      if (f < p0 + groups && f < count)
+        for (int k = (threadIdx.x % kWarp) / 2; k < lines; k += kWarp / 2)
+          PrefetchL2(pointWeight + (static_cast<long long>(f) * ntheta + j) * n + k * (128 / sizeof(T)));
+    }
+  }
   for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = twGlobal[e];
   if constexpr (R1 > 0)
     for (int e = threadIdx.x; e < n; e += blockDim.x) twB[e] = twGlobal[(e / R1) * (e % R1)];
