@@ -394,6 +394,124 @@ enum SolveMode {
 // so the forward substitution starts at lo; the backward one stops at lo
 // (kSolveWindow), and a later completion launch finishes rows below lo from
 // the stored x (unscaled again) with y = 0.
+// The FP32 substitutions with the last 32 solutions of a lane in registers
+// (bandwidth KD a compile-time constant): chunks of kChunk = 16 rows, row k
+// of chunk c in slot 16 (c % 2) + k of the window, so that every index is a
+// constant in each of the two phases. The solve is bound by instructions per
+// row at a few warps an SM; this drops the shared-memory ring's loads and
+// its wrap arithmetic, reads the band at constant offsets, and sums the
+// terms t >= 2 before the one that waits on the row just solved.
+constexpr int kWindow = 32;
+static_assert(kWindow == 2 * kChunk, "the window holds two chunks");
+
+template <int KD, int PHASE, bool FORWARD>
+__device__ __forceinline__ void WindowChunk(const Lane<float>& ln, const Stage<float>& st, int buf, int rowBase,
+                                            int rows, int hi, bool rhsLive, float2 (&w)[kWindow], int lane) {
+  constexpr int LD = KD + 1;
+  const float* band = st.Band(buf);
+#pragma unroll
+  for (int k = 0; k < kChunk; ++k) {
+    if (k < rows) {
+      // forward: row j = rowBase + k, U(j - t, j) = column[-t];
+      // backward: row i = rowBase - k, U(i, i + t) = at[t (LD - 1)]
+      const int row = FORWARD ? rowBase + k : rowBase - k;
+      const int r = FORWARD ? k : rows - 1 - k;
+      const float* at = band + r * LD + KD;
+      float2 acc0, acc1, acc2, acc3;
+      if (FORWARD)
+        acc0 = row <= hi ? Start(ln, st, buf, r, row, lane) : make_float2(0.0f, 0.0f);
+      else
+        acc0 = rhsLive ? st.Rhs(buf, r)[lane] : make_float2(0.0f, 0.0f);
+      acc1 = acc2 = acc3 = make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int t = KD; t >= 2; --t) {
+        const float u = FORWARD ? at[-t] : at[t * (LD - 1)];
+        const float2 y = w[(PHASE + k - t) & (kWindow - 1)];
+        float2& acc = (t & 3) == 0 ? acc0 : (t & 3) == 1 ? acc1 : (t & 3) == 2 ? acc2 : acc3;
+        acc.x -= u * y.x;
+        acc.y -= u * y.y;
+      }
+      float2 sum = make_float2((acc0.x + acc1.x) + (acc2.x + acc3.x), (acc0.y + acc1.y) + (acc2.y + acc3.y));
+      const float u1 = FORWARD ? at[-1] : at[LD - 1];
+      const float2 y1 = w[(PHASE + k - 1) & (kWindow - 1)];
+      sum.x -= u1 * y1.x;
+      sum.y -= u1 * y1.y;
+      const float inv = 1.0f / at[0];
+      float2 v = make_float2(sum.x * inv, sum.y * inv);
+      w[(PHASE + k) & (kWindow - 1)] = v;
+      if (!FORWARD && ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
+      ln.Store(row, v);
+    }
+  }
+}
+
+// The FP32 ring form's row sum in the register form's order, so that a row
+// comes out the same whichever form solves it: the terms t = reach .. 2 into
+// four sums by t % 4 (descending t), the sums paired, then the t = 1 term.
+// `at` points at the row's diagonal (forward: U(j - t, j) = at[-t];
+// backward: U(i, i + t) = at[t (ld - 1)]); the ring holds row j - t (i + t)
+// at SlotBack (SlotAhead) of `slot`.
+template <bool FORWARD>
+__device__ __forceinline__ float2 RowSum32(float2 start, const float* at, int ld, int reach, const float2* ring,
+                                           int slot, int depth) {
+  float2 a0 = start, a1 = make_float2(0.0f, 0.0f), a2 = a1, a3 = a1;
+  for (int t = reach; t >= 2; --t) {
+    const float u = FORWARD ? at[-t] : at[t * (ld - 1)];
+    const float2 y = ring[(FORWARD ? SlotBack(slot, t, depth) : SlotAhead(slot, t, depth)) * kWarp];
+    switch (t & 3) {
+      case 0: a0.x -= u * y.x; a0.y -= u * y.y; break;
+      case 1: a1.x -= u * y.x; a1.y -= u * y.y; break;
+      case 2: a2.x -= u * y.x; a2.y -= u * y.y; break;
+      default: a3.x -= u * y.x; a3.y -= u * y.y; break;
+    }
+  }
+  float2 sum = make_float2((a0.x + a1.x) + (a2.x + a3.x), (a0.y + a1.y) + (a2.y + a3.y));
+  if (reach >= 1) {
+    const float u1 = FORWARD ? at[-1] : at[ld - 1];
+    const float2 y1 = ring[(FORWARD ? SlotBack(slot, 1, depth) : SlotAhead(slot, 1, depth)) * kWarp];
+    sum.x -= u1 * y1.x;
+    sum.y -= u1 * y1.y;
+  }
+  return sum;
+}
+
+// Slots 32 - KD .. 31 of the window from the wrapped ring: the KD rows before
+// a substitution's third chunk. Slot s holds row first + s (forward) or
+// first - s (backward); the ring holds row i at slot i % depth.
+template <int KD, bool FORWARD>
+__device__ __forceinline__ void WindowLoad(const float2* ring, int first, int depth, float2 (&w)[kWindow]) {
+#pragma unroll
+  for (int s = kWindow - KD; s < kWindow; ++s) {
+    const int row = FORWARD ? first + s : first - s;
+    w[s] = ring[(row % depth) * kWarp];
+  }
+}
+
+// The register form for chunk c >= 2 of a substitution, when the bandwidth
+// is one it is built for (the operators' 3 (ngll - 1) + 2 and ngll - 1 for
+// ngll 5 and 6); false: the ring form solves the chunk.
+template <bool FORWARD>
+__device__ __forceinline__ bool WindowSolve(int kd, int c, const Lane<float>& ln, const Stage<float>& st, int buf,
+                                            const float2* ring, int first, int depth, int rowBase, int rows, int hi,
+                                            bool rhsLive, float2 (&w)[kWindow], int lane) {
+#define SL3D_WINDOW_CASE(KD)                                                                                 \
+  case KD:                                                                                                   \
+    if (c == 2) WindowLoad<KD, FORWARD>(ring, first, depth, w);                                              \
+    if (c % 2 == 0)                                                                                          \
+      WindowChunk<KD, 0, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                         \
+    else                                                                                                     \
+      WindowChunk<KD, kChunk, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                    \
+    return true;
+  switch (kd) {
+    SL3D_WINDOW_CASE(4)
+    SL3D_WINDOW_CASE(5)
+    SL3D_WINDOW_CASE(14)
+    SL3D_WINDOW_CASE(17)
+    default: return false;
+  }
+#undef SL3D_WINDOW_CASE
+}
+
 template <class T>
 __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const WorkItem* items, int itemCount,
                                     const T* bands, T* rhs, const T* scales, SolvePlan plan, const int2* windows,
@@ -418,6 +536,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
   }
   T2 zero;
   zero.x = zero.y = T(0);
+  float2 window[kWindow];  // the FP32 register form's last solutions
   if (mode == kSolveCompletion) {
     // x at rows lo .. lo + kd - 1 (stored scaled) seeds the ring
     for (int r = lo; r < min(n, lo + kd); ++r) {
@@ -443,6 +562,10 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
         },
         [&](int c, int buf) {
           const int j0 = lo + c * kChunk, j1 = min(n, j0 + kChunk);
+          if constexpr (sizeof(T) == sizeof(float)) {
+            if (c >= 2 && WindowSolve<true>(kd, c, ln, st, buf, ring, lo, depth, j0, j1 - j0, hi, true, window, lane))
+              return;
+          }
           const T* band = st.Band(buf);
           for (int j = j0; j < j1; ++j) {
             const T* column = band + (j - j0) * ld + kd;  // column[-t] = U(j - t, j)
@@ -450,6 +573,14 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
             T2 a = j <= hi ? Start(ln, st, buf, j - j0, j, lane) : zero;
             T2 b = zero;
             const int reach = min(kd, j - lo);
+            if constexpr (sizeof(T) == sizeof(float)) {
+              const float2 sum = RowSum32<true>(a, column, ld, reach, ring, slot, depth);
+              const T2 y = make_float2(sum.x * inv, sum.y * inv);
+              ring[slot * kWarp] = y;
+              ln.Store(j, y);
+              slot = SlotAhead(slot, 1, depth);
+              continue;
+            }
             // row j - t: slot + depth - t of the mirrored ring, else wrapped
             const T2* back = ring + (slot + depth) * kWarp;
             int t = 1;
@@ -493,6 +624,11 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
       },
       [&](int c, int buf) {
         const int i1 = top - c * kChunk, i0 = max(bottom, i1 - kChunk);
+        if constexpr (sizeof(T) == sizeof(float)) {
+          if (c >= 2 &&
+              WindowSolve<false>(kd, c, ln, st, buf, ring, top - 1, depth, i1 - 1, i1 - i0, 0, rhsEnd > 0, window, lane))
+            return;
+        }
         const T* band = st.Band(buf);
         for (int i = i1 - 1; i >= i0; --i) {
           const int r = i - i0;
@@ -500,6 +636,15 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
           T2 a = rhsEnd > 0 ? st.Rhs(buf, r)[lane] : zero;
           T2 b = zero;
           const int reach = min(kd, n - 1 - i);
+          if constexpr (sizeof(T) == sizeof(float)) {
+            const float2 sum = RowSum32<false>(a, band + r * ld + kd, ld, reach, ring, slot, depth);
+            T2 v = make_float2(sum.x * inv, sum.y * inv);
+            ring[slot * kWarp] = v;
+            if (ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
+            ln.Store(i, v);
+            slot = SlotBack(slot, 1, depth);
+            continue;
+          }
           // row i + t: slot + t of the mirrored ring, else wrapped
           const T2* ahead = ring + slot * kWarp;
           int t = 1;
