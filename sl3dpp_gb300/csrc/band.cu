@@ -394,21 +394,25 @@ enum SolveMode {
 // so the forward substitution starts at lo; the backward one stops at lo
 // (kSolveWindow), and a later completion launch finishes rows below lo from
 // the stored x (unscaled again) with y = 0.
-// The FP32 substitutions with the last 32 solutions of a lane in registers
-// (bandwidth KD a compile-time constant): chunks of kChunk = 16 rows, row k
-// of chunk c in slot 16 (c % 2) + k of the window, so that every index is a
-// constant in each of the two phases. The solve is bound by instructions per
-// row at a few warps an SM; this drops the shared-memory ring's loads and
-// its wrap arithmetic, reads the band at constant offsets, and sums the
-// terms t >= 2 before the one that waits on the row just solved.
+// The substitutions with the last 32 solutions of a lane in registers
+// (bandwidth KD a compile-time constant; the FP32 solves use it): chunks of
+// kChunk = 16 rows, row k of chunk c in slot 16 (c % 2) + k of the window,
+// so that every index is a constant in each of the two phases. The solve is
+// bound by instructions per row at a few warps an SM; this drops the
+// shared-memory ring's loads and its wrap arithmetic, reads the band at
+// constant offsets, and sums the terms t >= 2 before the one that waits on
+// the row just solved.
 constexpr int kWindow = 32;
 static_assert(kWindow == 2 * kChunk, "the window holds two chunks");
 
-template <int KD, int PHASE, bool FORWARD>
-__device__ __forceinline__ void WindowChunk(const Lane<float>& ln, const Stage<float>& st, int buf, int rowBase,
-                                            int rows, int hi, bool rhsLive, float2 (&w)[kWindow], int lane) {
+template <class T, int KD, int PHASE, bool FORWARD>
+__device__ __forceinline__ void WindowChunk(const Lane<T>& ln, const Stage<T>& st, int buf, int rowBase, int rows,
+                                            int hi, bool rhsLive, typename PairOf<T>::type (&w)[kWindow], int lane) {
+  using T2 = typename PairOf<T>::type;
   constexpr int LD = KD + 1;
-  const float* band = st.Band(buf);
+  const T* band = st.Band(buf);
+  T2 zero;
+  zero.x = zero.y = T(0);
 #pragma unroll
   for (int k = 0; k < kChunk; ++k) {
     if (k < rows) {
@@ -416,28 +420,32 @@ __device__ __forceinline__ void WindowChunk(const Lane<float>& ln, const Stage<f
       // backward: row i = rowBase - k, U(i, i + t) = at[t (LD - 1)]
       const int row = FORWARD ? rowBase + k : rowBase - k;
       const int r = FORWARD ? k : rows - 1 - k;
-      const float* at = band + r * LD + KD;
-      float2 acc0, acc1, acc2, acc3;
+      const T* at = band + r * LD + KD;
+      T2 acc0, acc1, acc2, acc3;
       if (FORWARD)
-        acc0 = row <= hi ? Start(ln, st, buf, r, row, lane) : make_float2(0.0f, 0.0f);
+        acc0 = row <= hi ? Start(ln, st, buf, r, row, lane) : zero;
       else
-        acc0 = rhsLive ? st.Rhs(buf, r)[lane] : make_float2(0.0f, 0.0f);
-      acc1 = acc2 = acc3 = make_float2(0.0f, 0.0f);
+        acc0 = rhsLive ? st.Rhs(buf, r)[lane] : zero;
+      acc1 = acc2 = acc3 = zero;
 #pragma unroll
       for (int t = KD; t >= 2; --t) {
-        const float u = FORWARD ? at[-t] : at[t * (LD - 1)];
-        const float2 y = w[(PHASE + k - t) & (kWindow - 1)];
-        float2& acc = (t & 3) == 0 ? acc0 : (t & 3) == 1 ? acc1 : (t & 3) == 2 ? acc2 : acc3;
+        const T u = FORWARD ? at[-t] : at[t * (LD - 1)];
+        const T2 y = w[(PHASE + k - t) & (kWindow - 1)];
+        T2& acc = (t & 3) == 0 ? acc0 : (t & 3) == 1 ? acc1 : (t & 3) == 2 ? acc2 : acc3;
         acc.x -= u * y.x;
         acc.y -= u * y.y;
       }
-      float2 sum = make_float2((acc0.x + acc1.x) + (acc2.x + acc3.x), (acc0.y + acc1.y) + (acc2.y + acc3.y));
-      const float u1 = FORWARD ? at[-1] : at[LD - 1];
-      const float2 y1 = w[(PHASE + k - 1) & (kWindow - 1)];
+      T2 sum;
+      sum.x = (acc0.x + acc1.x) + (acc2.x + acc3.x);
+      sum.y = (acc0.y + acc1.y) + (acc2.y + acc3.y);
+      const T u1 = FORWARD ? at[-1] : at[LD - 1];
+      const T2 y1 = w[(PHASE + k - 1) & (kWindow - 1)];
       sum.x -= u1 * y1.x;
       sum.y -= u1 * y1.y;
-      const float inv = 1.0f / at[0];
-      float2 v = make_float2(sum.x * inv, sum.y * inv);
+      const T inv = T(1) / at[0];
+      T2 v;
+      v.x = sum.x * inv;
+      v.y = sum.y * inv;
       w[(PHASE + k) & (kWindow - 1)] = v;
       if (!FORWARD && ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
       ln.Store(row, v);
@@ -478,8 +486,8 @@ __device__ __forceinline__ float2 RowSum32(float2 start, const float* at, int ld
 // Slots 32 - KD .. 31 of the window from the wrapped ring: the KD rows before
 // a substitution's third chunk. Slot s holds row first + s (forward) or
 // first - s (backward); the ring holds row i at slot i % depth.
-template <int KD, bool FORWARD>
-__device__ __forceinline__ void WindowLoad(const float2* ring, int first, int depth, float2 (&w)[kWindow]) {
+template <class T2, int KD, bool FORWARD>
+__device__ __forceinline__ void WindowLoad(const T2* ring, int first, int depth, T2 (&w)[kWindow]) {
 #pragma unroll
   for (int s = kWindow - KD; s < kWindow; ++s) {
     const int row = FORWARD ? first + s : first - s;
@@ -490,17 +498,18 @@ __device__ __forceinline__ void WindowLoad(const float2* ring, int first, int de
 // The register form for chunk c >= 2 of a substitution, when the bandwidth
 // is one it is built for (the operators' 3 (ngll - 1) + 2 and ngll - 1 for
 // ngll 5 and 6); false: the ring form solves the chunk.
-template <bool FORWARD>
-__device__ __forceinline__ bool WindowSolve(int kd, int c, const Lane<float>& ln, const Stage<float>& st, int buf,
-                                            const float2* ring, int first, int depth, int rowBase, int rows, int hi,
-                                            bool rhsLive, float2 (&w)[kWindow], int lane) {
+template <class T, bool FORWARD>
+__device__ __forceinline__ bool WindowSolve(int kd, int c, const Lane<T>& ln, const Stage<T>& st, int buf,
+                                            const typename PairOf<T>::type* ring, int first, int depth, int rowBase,
+                                            int rows, int hi, bool rhsLive, typename PairOf<T>::type (&w)[kWindow],
+                                            int lane) {
 #define SL3D_WINDOW_CASE(KD)                                                                                 \
   case KD:                                                                                                   \
-    if (c == 2) WindowLoad<KD, FORWARD>(ring, first, depth, w);                                              \
+    if (c == 2) WindowLoad<typename PairOf<T>::type, KD, FORWARD>(ring, first, depth, w);                    \
     if (c % 2 == 0)                                                                                          \
-      WindowChunk<KD, 0, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                         \
+      WindowChunk<T, KD, 0, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                      \
     else                                                                                                     \
-      WindowChunk<KD, kChunk, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                    \
+      WindowChunk<T, KD, kChunk, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                 \
     return true;
   switch (kd) {
     SL3D_WINDOW_CASE(4)
@@ -536,7 +545,11 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
   }
   T2 zero;
   zero.x = zero.y = T(0);
-  float2 window[kWindow];  // the FP32 register form's last solutions
+  // The register form in FP32 only: FP64's solves are bound by its FP64
+  // unit, and its window's 128 registers slowed them (the mirrored ring
+  // serves them better).
+  constexpr bool kWindowForm = sizeof(T) == sizeof(float);
+  T2 window[kWindow];  // the register form's last solutions
   if (mode == kSolveCompletion) {
     // x at rows lo .. lo + kd - 1 (stored scaled) seeds the ring
     for (int r = lo; r < min(n, lo + kd); ++r) {
@@ -562,10 +575,9 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
         },
         [&](int c, int buf) {
           const int j0 = lo + c * kChunk, j1 = min(n, j0 + kChunk);
-          if constexpr (sizeof(T) == sizeof(float)) {
-            if (c >= 2 && WindowSolve<true>(kd, c, ln, st, buf, ring, lo, depth, j0, j1 - j0, hi, true, window, lane))
-              return;
-          }
+          if (kWindowForm && c >= 2 &&
+              WindowSolve<T, true>(kd, c, ln, st, buf, ring, lo, depth, j0, j1 - j0, hi, true, window, lane))
+            return;
           const T* band = st.Band(buf);
           for (int j = j0; j < j1; ++j) {
             const T* column = band + (j - j0) * ld + kd;  // column[-t] = U(j - t, j)
@@ -624,11 +636,9 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
       },
       [&](int c, int buf) {
         const int i1 = top - c * kChunk, i0 = max(bottom, i1 - kChunk);
-        if constexpr (sizeof(T) == sizeof(float)) {
-          if (c >= 2 &&
-              WindowSolve<false>(kd, c, ln, st, buf, ring, top - 1, depth, i1 - 1, i1 - i0, 0, rhsEnd > 0, window, lane))
-            return;
-        }
+        if (kWindowForm && c >= 2 &&
+            WindowSolve<T, false>(kd, c, ln, st, buf, ring, top - 1, depth, i1 - 1, i1 - i0, 0, rhsEnd > 0, window, lane))
+          return;
         const T* band = st.Band(buf);
         for (int i = i1 - 1; i >= i0; --i) {
           const int r = i - i0;
