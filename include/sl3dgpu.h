@@ -355,10 +355,16 @@ int sl3dgpu_v3d_step_tide(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, 
 /* The same step with the load coefficients in device memory. */
 int sl3dgpu_v3d_step_device(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme,
                             const double* load0, const double* load1, sl3dgpu_step_info* info);
-/* Viscoelastic3D::Surface (Viscoelastic3D.cpp:2032-2051) of the last step's
- * solutions: component 0 U, 1 V, 2 phi; complex m >= 0 columns per degree in
- * the l(l+1)/2 + m layout, into host memory. */
+/* Viscoelastic3D::Surface (Viscoelastic3D.cpp:2050-2081) of the last step's
+ * solutions: component 0 U, 1 V, 2 phi; component 3 W is SurfaceToroidal
+ * (:2083-2112, zero at degree 0); complex m >= 0 columns per degree in the
+ * l(l+1)/2 + m layout, into host memory. */
 int sl3dgpu_v3d_surface(sl3dgpu_v3d* op, int component, double* out);
+/* Viscoelastic3D::InertiaMoment (Viscoelastic3D.cpp:2032-2048) of the last
+ * step's solutions: sqrt(4 pi) int rho U r^3 dr of their degree-0 radial
+ * displacement (the degree-0 moment row of detail/ViscoelasticDegree.hpp:
+ * 142-161), in the operator's non-dimensional units. */
+int sl3dgpu_v3d_inertia_moment(sl3dgpu_v3d* op, double* out);
 /* The warm-start hook (OpenStep::Converge's start, Viscoelastic3D.hpp:562-569):
  * a guess of the strain coefficients at the end of the NEXT step, in the
  * device layout a state's coefficients have (sl3dgpu_v3d_state_coefficients;

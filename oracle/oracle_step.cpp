@@ -1336,8 +1336,43 @@ class Viscoelastic3D {
   }
 
   // Surface (Viscoelastic3D.cpp:2032-2051): U, V or phi at the surface node.
+  // InertiaMoment (Viscoelastic3D.cpp:2032-2048 with the degree-0 moment row
+  // of detail/ViscoelasticDegree.hpp:142-161): sqrt(4 pi) sum over the
+  // degree's elements and their GLL nodes of w_q J_e rho r^3 times the real
+  // part of the last solutions' degree-0 U at that node's dof.
+  double InertiaMoment() const {
+    if (last_.sph.empty()) return 0.0;
+    const auto& op = *elastic_->sph[0];
+    const auto& mesh = nodal_->mesh;
+    const int n = mesh.NGll();
+    double sum = 0.0;
+    for (int e = 0; e < mesh.ElementCount(); ++e)
+      for (int q = 0; q < n; ++q) {
+        const int dof = op.Dof(mesh.GlobalIndex(e, q), kU);
+        if (dof < 0) continue;
+        const double r = mesh.Radius(e, q);
+        sum += mesh.Weights()[q] * mesh.Jacobian(e) * nodal_->rho[static_cast<std::size_t>(e) * n + q] * r * r * r *
+               last_.sph[0][dof].real();
+      }
+    return std::sqrt(4.0 * 3.14159265358979323846) * sum;
+  }
+
+  // Surface (component 0 U, 1 V, 2 phi) and SurfaceToroidal (component 3,
+  // W): Viscoelastic3D.cpp:2050-2112, the surface dof of each degree's
+  // last solutions, zero where the degree has none.
   void Surface(int component, C* out) const {
     const int L = options_.lmax;
+    if (component == 3) {
+      for (int l = 0; l <= L; ++l) {
+        const ToroidalOperator* op = l >= 1 ? elastic_->tor[l].get() : nullptr;
+        const int dof = op != nullptr ? op->SurfaceDof() : -1;
+        for (int m = 0; m <= l; ++m)
+          out[OGrid::Index(l, m)] = dof >= 0 && !last_.tor.empty()
+                                        ? last_.tor[l][static_cast<std::size_t>(m) * op->DofCount() + dof]
+                                        : C{};
+      }
+      return;
+    }
     for (int l = 0; l <= L; ++l) {
       const auto& op = *elastic_->sph[l];
       const int dof = op.SurfaceDof(component);
@@ -1491,6 +1526,8 @@ int oracle_v3d_sample(oracle_v3d* h, oracle_state* state, double dt, const doubl
 }
 
 int oracle_threads(void) { return omp_get_max_threads(); }
+
+double oracle_v3d_inertia_moment(const oracle_v3d* h) { return h->op->InertiaMoment(); }
 
 void oracle_v3d_surface(const oracle_v3d* h, int component, double* out) {
   h->op->Surface(component, reinterpret_cast<C*>(out));

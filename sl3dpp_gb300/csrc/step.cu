@@ -213,6 +213,8 @@ class Viscoelastic3DGpu {
            bool onDevice = false, const double* tide0 = nullptr, const double* tide1 = nullptr);
   Dev<double2> tideDev0, tideDev1, tideDevMid;
   int Surface(int component, double* out);
+  int InertiaMoment(double* out);
+  std::vector<double> momentRow;  // the degree-0 inertia-moment row over its dofs
   int StrainReference(const V3dState& st, double* out);
 
  private:
@@ -399,6 +401,20 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     d.firstGlobal = d.firstNode < P ? msh.GlobalIndex(nodeElement[d.firstNode], 0) : 0;
     d.lastGlobal = d.firstNode < P ? msh.GlobalIndex(nodeElement[P - 1], n - 1) : -1;
     d.sphNdof = op.DofCount();
+    if (l == 0) {
+      // sqrt(4 pi) w_q J_e rho r^3 at each GLL node's U dof, over the whole
+      // mesh (detail/ViscoelasticDegree.hpp:142-161)
+      momentRow.assign(static_cast<size_t>(d.sphNdof), 0.0);
+      const int ng = msh.NGll();
+      for (int e = 0; e < msh.ElementCount(); ++e)
+        for (int q = 0; q < ng; ++q) {
+          const int dof = op.Dof(msh.GlobalIndex(e, q), host::kU);
+          if (dof < 0) continue;
+          const double r = msh.Radius(e, q);
+          momentRow[dof] += std::sqrt(4.0 * 3.14159265358979323846) * msh.Weights()[q] * msh.Jacobian(e) *
+                            nodal.rho[static_cast<size_t>(e) * ng + q] * r * r * r;
+        }
+    }
     d.surfaceU = op.SurfaceDof(host::kU);
     d.surfaceV = op.SurfaceDof(host::kV);
     d.surfacePhi = op.SurfaceDof(host::kPhi);
@@ -412,9 +428,11 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     }
     d.torNdof = 0;
     d.torRhs = torOff;
+    d.surfaceW = -1;
     if (l >= 1) {
       host::ToroidalOperator top(nodal, l, opt.eps, elasticShear);
       d.torNdof = top.DofCount();
+      d.surfaceW = top.SurfaceDof();
       torOff += static_cast<long long>(d.torNdof) * (l + 1);
       for (int gn = 0; gn < nglob; ++gn) torMap[d.torMap + gn] = top.Dof(gn);
     }
@@ -1851,15 +1869,30 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
 }
 
 int Viscoelastic3DGpu::Surface(int component, double* out) {
-  if (component < 0 || component > 2) {
-    SetError("v3d: component 0 (U), 1 (V) or 2 (phi)");
+  if (component < 0 || component > 3) {
+    SetError("v3d: component 0 (U), 1 (V), 2 (phi) or 3 (W, toroidal)");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  LaunchSurface(geo, rhsSph.p, component, surfaceOut.p, stream);
+  LaunchSurface(geo, rhsSph.p, rhsTor.p, component, surfaceOut.p, stream);
   SL3D_CHECK_LAUNCH();
   const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
   SL3D_CUDA(cudaMemcpyAsync(out, surfaceOut.p, lm * sizeof(double2), cudaMemcpyDeviceToHost, stream));
   SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+// InertiaMoment (Viscoelastic3D.cpp:2032-2048): the degree-0 moment row
+// (detail/ViscoelasticDegree.hpp:142-161) against the real part of the last
+// solutions' degree-0 column.
+int Viscoelastic3DGpu::InertiaMoment(double* out) {
+  const int ndof = degrees[0].sphNdof;
+  std::vector<double2> x(static_cast<size_t>(ndof));
+  SL3D_CUDA(cudaMemcpyAsync(x.data(), rhsSph.p + degrees[0].sphRhs, ndof * sizeof(double2), cudaMemcpyDeviceToHost,
+                            stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  double sum = 0.0;
+  for (int d = 0; d < ndof; ++d) sum += momentRow[d] * x[d].x;
+  *out = sum;
   return SL3DGPU_OK;
 }
 
@@ -2084,6 +2117,14 @@ extern "C" int sl3dgpu_v3d_run_many(int count, sl3dgpu_v3d* const* ops, sl3dgpu_
       return statuses[i];
     }
   return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_inertia_moment(sl3dgpu_v3d* h, double* out) {
+  if (h == nullptr || out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.InertiaMoment(out);
 }
 
 extern "C" int sl3dgpu_v3d_surface(sl3dgpu_v3d* h, int component, double* out) {

@@ -422,13 +422,17 @@ __global__ void AddLoadKernel(Geometry g, const double2* sigma, const double* un
   }
 }
 
-__global__ void SurfaceKernel(Geometry g, const double2* sol, int component, double2* out) {
+__global__ void SurfaceKernel(Geometry g, const double2* sol, const double2* solTor, int component, double2* out) {
   const int lm = blockIdx.x * blockDim.x + threadIdx.x;
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   if (lm >= count) return;
   int l, m;
   DecodeLm(lm, l, m);
   const DegreeInfo d = g.degrees[l];
+  if (component == 3) {  // SurfaceToroidal: W
+    out[lm] = d.surfaceW >= 0 ? solTor[d.torRhs + static_cast<long long>(d.surfaceW) * (l + 1) + m] : C(0, 0);
+    return;
+  }
   const int dof = component == 0 ? d.surfaceU : component == 1 ? d.surfaceV : d.surfacePhi;
   out[lm] = dof >= 0 ? sol[d.sphRhs + static_cast<long long>(dof) * (l + 1) + m] : C(0, 0);
 }
@@ -1127,10 +1131,11 @@ void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units,
   AddLoadKernel<<<g.lmax + 1, 256, 0, stream>>>(g, sigma, units, tide, tideUnits, unitOffset, solSph);
 }
 
-void LaunchSurface(const Geometry& g, const double2* solSph, int component, double2* out, cudaStream_t stream) {
+void LaunchSurface(const Geometry& g, const double2* solSph, const double2* solTor, int component, double2* out,
+                   cudaStream_t stream) {
   const int count = (g.lmax + 1) * (g.lmax + 2) / 2;
   prof::Scope scope(prof::kOther, stream);
-  SurfaceKernel<<<(count + 127) / 128, 128, 0, stream>>>(g, solSph, component, out);
+  SurfaceKernel<<<(count + 127) / 128, 128, 0, stream>>>(g, solSph, solTor, component, out);
 }
 
 void LaunchWeights(const WeightsArgs& a, cudaStream_t stream) {

@@ -21,7 +21,7 @@ struct DegreeInfo {
   int firstGlobal;    // global node range of the carrying elements from it
   int lastGlobal;
   int sphNdof, torNdof;
-  int surfaceU, surfaceV, surfacePhi;
+  int surfaceU, surfaceV, surfacePhi, surfaceW;  // -1: none
   long long sphMap, torMap;  // offsets into the dof maps
   long long sphRhs, torRhs;  // complex offsets of the degree's [dof][l+1] blocks
 };
@@ -83,8 +83,9 @@ void LaunchDilatationForce(const Geometry& g, const double2* scalar, double2* rh
 void LaunchAddLoad(const Geometry& g, const double2* sigma, const double* units,
                    const long long* unitOffset, double2* solSph, cudaStream_t stream,
                    const double2* tide = nullptr, const double* tideUnits = nullptr);
-// Surface values of a component (U, V or phi) for every (l, m >= 0).
-void LaunchSurface(const Geometry& g, const double2* solSph, int component, double2* out,
+// Surface values of a component (0 U, 1 V, 2 phi from the spheroidal
+// solutions; 3 W from the toroidal ones) for every (l, m >= 0).
+void LaunchSurface(const Geometry& g, const double2* solSph, const double2* solTor, int component, double2* out,
                    cudaStream_t stream);
 
 // The step weights, decayed memory, lateral weight and fixed force

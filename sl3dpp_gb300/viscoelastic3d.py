@@ -17,7 +17,7 @@ import numpy as np
 from ._lib import P_double, P_int, c_void_p, check, lib
 
 SCHEMES = {"exponential_trapezoid": 0, "backward_euler": 1, "sdirk2": 2}
-COMPONENTS = {"U": 0, "V": 1, "phi": 2}
+COMPONENTS = {"U": 0, "V": 1, "phi": 2, "W": 3}
 
 
 class Layer(ctypes.Structure):
@@ -83,6 +83,7 @@ def _signatures():
         "sl3dgpu_v3d_free_state": (None, [v]),
         "sl3dgpu_v3d_step": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_surface": (i, [v, i, v]),
+        "sl3dgpu_v3d_inertia_moment": (i, [v, P_double]),
         "sl3dgpu_v3d_state_strain": (i, [v, v, v]),
         "sl3dgpu_v3d_residual_history": (i, [v, P_double, i]),
         "sl3dgpu_v3d_correction_history": (i, [v, P_double, i]),
@@ -270,6 +271,16 @@ class Viscoelastic3D:
         out = np.zeros((self.lmax + 1) * (self.lmax + 2) // 2, dtype=np.complex128)
         check(lib().sl3dgpu_v3d_surface(self._h, code, out.ctypes.data))
         return out
+
+    def SurfaceToroidal(self) -> np.ndarray:
+        """Viscoelastic3D::SurfaceToroidal: the surface W per (l, m >= 0)."""
+        return self.Surface(3)
+
+    def InertiaMoment(self) -> float:
+        """Viscoelastic3D::InertiaMoment of the last step's solutions."""
+        out = ctypes.c_double()
+        check(lib().sl3dgpu_v3d_inertia_moment(self._h, ctypes.byref(out)))
+        return out.value
 
 
 class Evolution3D:

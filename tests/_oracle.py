@@ -183,6 +183,7 @@ def _v3d_sigs(L):
         "oracle_v3d_step": (i, [v, v, d, i, v, v, _ct.POINTER(StepInfo)]),
         "oracle_v3d_step_tide": (i, [v, v, d, i, v, v, v, v, _ct.POINTER(StepInfo)]),
         "oracle_v3d_surface": (None, [v, i, v]),
+        "oracle_v3d_inertia_moment": (d, [v]),
         "oracle_v3d_state_strain": (i, [v, v]),
         "oracle_v3d_residual_history": (i, [v, P_double, i]),
         "oracle_v3d_sample": (i, [v, v, d, v, v, i, P_double, P_double]),

@@ -47,6 +47,15 @@ def test_zero_lateral_step_decouples_and_converges_in_two_passes():
         rest = np.setdiff1d(np.arange(U.size), zonal)
         assert np.max(np.abs(U[rest])) < 1e-12 * np.max(np.abs(U[zonal]))
         assert U[configs.real_index(2, 0)].real < 0.0  # the load depresses the surface
+        # no lateral contrast: no toroidal motion beyond the transforms' rounding
+        assert np.max(np.abs(st.surface(3))) < 1e-12 * np.max(np.abs(U))
+    # the degree-0 inertia moment is linear in the load's degree-0 part
+    moment = st.L.oracle_v3d_inertia_moment(st.h)
+    assert moment != 0.0
+    st2 = O.OracleStep(O.standard_earth(20), O.default_options(lmax))
+    for n in range(2):
+        st2.step(dt, 2, 2 * load * n / 10, 2 * load * (n + 1) / 10)
+    assert abs(st2.L.oracle_v3d_inertia_moment(st2.h) - 2 * moment) < 1e-12 * abs(moment)
 
 
 def test_lateral_viscosity_couples_orders():
@@ -132,6 +141,12 @@ def test_gpu_step_matches_oracle(gpu, scheme):
         assert abs(ig.iterations - io.iterations) <= 1
         for comp in (0, 2):
             assert rel(g.Surface(comp), o.surface(comp)) < TOL, (n, comp)
+        # SurfaceToroidal: W from the lateral coupling alone, on U's scale
+        W, Wo, U = g.SurfaceToroidal(), o.surface(3), o.surface(0)
+        assert np.max(np.abs(Wo)) > 1e-8 * np.max(np.abs(U))
+        assert np.max(np.abs(W - Wo)) < TOL * np.max(np.abs(U)), n
+        assert abs(g.InertiaMoment() - o.L.oracle_v3d_inertia_moment(o.h)) <= TOL * abs(
+            o.L.oracle_v3d_inertia_moment(o.h)), n
     want = np.zeros(g.spectral_size, dtype=np.complex128)
     o.L.oracle_v3d_state_strain(o.state, want.ctypes.data)
     assert rel(state.strain_coefficients(), want) < TOL
