@@ -293,6 +293,31 @@ int sl3dgpu_ep3d_solve_lateral(sl3dgpu_ep3d* op, const double* load, double rtol
 int sl3dgpu_ep3d_surface(sl3dgpu_ep3d* op, int component, double* out);
 int sl3dgpu_ep3d_residual_history(const sl3dgpu_ep3d* op, double* out, int capacity);
 
+/* ---- one degree's system (include/sl3dpp/DegreeOperator.hpp:94-384) -------
+ * DegreeOperator (toroidal = 0) or ToroidalOperator (toroidal = 1, l >= 1) of
+ * degree l on the unrelaxed material of a layered earth meshed with ngll GLL
+ * nodes an element, truncated at eps (src/DegreeOperator.cpp:24-505,
+ * src/ToroidalOperator.cpp): the symmetric-scaled band factorised at
+ * creation on the GPU (Cholesky, or LU when a diagonal is not positive or
+ * Cholesky meets a non-positive pivot: UsedCholesky). Dof(node, component)
+ * over the mesh's global GLL nodes (-1: no dof), SurfaceDof, the Load and
+ * Tide(power) vectors (spheroidal), Apply (K x, host), and Solve (K^-1 b in
+ * place on the GPU, pinned rows zero); vectors are ndof long, nrhs columns
+ * of ndof end to end. */
+typedef struct sl3dgpu_degree sl3dgpu_degree;
+int sl3dgpu_degree_create(const sl3dgpu_layer* layers, int nlayers, int ngll, int l, double eps, int toroidal,
+                          sl3dgpu_degree** out);
+void sl3dgpu_degree_destroy(sl3dgpu_degree* op);
+int sl3dgpu_degree_dof_count(const sl3dgpu_degree* op);
+int sl3dgpu_degree_bandwidth(const sl3dgpu_degree* op);
+int sl3dgpu_degree_used_cholesky(const sl3dgpu_degree* op);
+int sl3dgpu_degree_dof(const sl3dgpu_degree* op, int node, int component);
+int sl3dgpu_degree_surface_dof(const sl3dgpu_degree* op, int component);
+int sl3dgpu_degree_load(const sl3dgpu_degree* op, double* out);
+int sl3dgpu_degree_tide(const sl3dgpu_degree* op, int power, double* out);
+int sl3dgpu_degree_apply(const sl3dgpu_degree* op, const double* x, int nrhs, double* y);
+int sl3dgpu_degree_solve(const sl3dgpu_degree* op, double* b, int nrhs);
+
 /* The configurations' Earth (radius 6371 km, fluid core to 3480 km, linear
  * mantle, 100 km elastic lid, 5e21 / 5e20 Pa s below / above 670 km), the
  * given element count spread over its four layers in proportion to
