@@ -25,6 +25,7 @@
 //    zero below row lo has y = 0 there, so the substitutions cover rows
 //    lo .. n - 1, and a completion launch finishes the rows below.
 #include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -394,63 +395,90 @@ enum SolveMode {
 // so the forward substitution starts at lo; the backward one stops at lo
 // (kSolveWindow), and a later completion launch finishes rows below lo from
 // the stored x (unscaled again) with y = 0.
-// The substitutions with the last 32 solutions of a lane in registers
-// (bandwidth KD a compile-time constant; the FP32 solves use it): chunks of
-// kChunk = 16 rows, row k of chunk c in slot 16 (c % 2) + k of the window,
-// so that every index is a constant in each of the two phases. The solve is
-// bound by instructions per row at a few warps an SM; this drops the
-// shared-memory ring's loads and its wrap arithmetic, reads the band at
+// The substitutions with a lane's recent solutions in registers (bandwidth
+// KD a compile-time constant; the FP32 solves use it): a chunk of kChunk = 16
+// rows writes cur[0..15], and old[d] holds the row d + 1 before the chunk's
+// first, so that every index is a constant and one unrolled chunk serves
+// every chunk; after the chunk old shifts by 16 (2 KD moves at most). The
+// solve is bound by instructions per row at a few warps an SM; this drops
+// the shared-memory ring's loads and its wrap arithmetic, reads the band at
 // constant offsets, and sums the terms t >= 2 before the one that waits on
 // the row just solved.
-constexpr int kWindow = 32;
-static_assert(kWindow == 2 * kChunk, "the window holds two chunks");
+template <class T2, int KD>
+struct Window {
+  T2 cur[kChunk];
+  T2 old[KD];
+  // row k - t of the chunk (k - t < 0: before it)
+  template <int K, int TT>
+  __device__ __forceinline__ const T2& At() const {
+    if constexpr (K - TT >= 0)
+      return cur[K - TT];
+    else
+      return old[TT - K - 1];
+  }
+  __device__ __forceinline__ void Shift() {
+#pragma unroll
+    for (int d = KD - 1; d >= kChunk; --d) old[d] = old[d - kChunk];
+#pragma unroll
+    for (int d = 0; d < (KD < kChunk ? KD : kChunk); ++d) old[d] = cur[kChunk - 1 - d];
+  }
+};
 
-template <class T, int KD, int PHASE, bool FORWARD>
-__device__ __forceinline__ void WindowChunk(const Lane<T>& ln, const Stage<T>& st, int buf, int rowBase, int rows,
-                                            int hi, bool rhsLive, typename PairOf<T>::type (&w)[kWindow], int lane) {
+template <class T, int KD, bool FORWARD, int K>
+__device__ __forceinline__ void WindowRow(const Lane<T>& ln, const Stage<T>& st, int buf, int rowBase, int rows,
+                                          int hi, bool rhsLive, Window<typename PairOf<T>::type, KD>& w,
+                                          int lane) {
   using T2 = typename PairOf<T>::type;
   constexpr int LD = KD + 1;
-  const T* band = st.Band(buf);
+  // forward: row j = rowBase + K, U(j - t, j) = at[-t];
+  // backward: row i = rowBase - K, U(i, i + t) = at[t (LD - 1)]
+  const int row = FORWARD ? rowBase + K : rowBase - K;
+  const int r = FORWARD ? K : rows - 1 - K;
+  const T* at = st.Band(buf) + r * LD + KD;
   T2 zero;
   zero.x = zero.y = T(0);
-#pragma unroll
-  for (int k = 0; k < kChunk; ++k) {
-    if (k < rows) {
-      // forward: row j = rowBase + k, U(j - t, j) = column[-t];
-      // backward: row i = rowBase - k, U(i, i + t) = at[t (LD - 1)]
-      const int row = FORWARD ? rowBase + k : rowBase - k;
-      const int r = FORWARD ? k : rows - 1 - k;
-      const T* at = band + r * LD + KD;
-      T2 acc0, acc1, acc2, acc3;
-      if (FORWARD)
-        acc0 = row <= hi ? Start(ln, st, buf, r, row, lane) : zero;
-      else
-        acc0 = rhsLive ? st.Rhs(buf, r)[lane] : zero;
-      acc1 = acc2 = acc3 = zero;
-#pragma unroll
-      for (int t = KD; t >= 2; --t) {
-        const T u = FORWARD ? at[-t] : at[t * (LD - 1)];
-        const T2 y = w[(PHASE + k - t) & (kWindow - 1)];
-        T2& acc = (t & 3) == 0 ? acc0 : (t & 3) == 1 ? acc1 : (t & 3) == 2 ? acc2 : acc3;
-        acc.x -= u * y.x;
-        acc.y -= u * y.y;
-      }
-      T2 sum;
-      sum.x = (acc0.x + acc1.x) + (acc2.x + acc3.x);
-      sum.y = (acc0.y + acc1.y) + (acc2.y + acc3.y);
-      const T u1 = FORWARD ? at[-1] : at[LD - 1];
-      const T2 y1 = w[(PHASE + k - 1) & (kWindow - 1)];
-      sum.x -= u1 * y1.x;
-      sum.y -= u1 * y1.y;
-      const T inv = T(1) / at[0];
-      T2 v;
-      v.x = sum.x * inv;
-      v.y = sum.y * inv;
-      w[(PHASE + k) & (kWindow - 1)] = v;
-      if (!FORWARD && ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
-      ln.Store(row, v);
-    }
-  }
+  T2 acc0, acc1 = zero, acc2 = zero, acc3 = zero;
+  if (FORWARD)
+    acc0 = row <= hi ? Start(ln, st, buf, r, row, lane) : zero;
+  else
+    acc0 = rhsLive ? st.Rhs(buf, r)[lane] : zero;
+  [&]<int... TS>(std::integer_sequence<int, TS...>) {
+    // t = KD .. 2 into the sums by t % 4
+    (
+        [&] {
+          constexpr int t = KD - TS;
+          const T u = FORWARD ? at[-t] : at[t * (LD - 1)];
+          const T2 y = w.template At<K, t>();
+          T2& acc = (t & 3) == 0 ? acc0 : (t & 3) == 1 ? acc1 : (t & 3) == 2 ? acc2 : acc3;
+          acc.x -= u * y.x;
+          acc.y -= u * y.y;
+        }(),
+        ...);
+  }(std::make_integer_sequence<int, KD - 1>{});
+  T2 sum;
+  sum.x = (acc0.x + acc1.x) + (acc2.x + acc3.x);
+  sum.y = (acc0.y + acc1.y) + (acc2.y + acc3.y);
+  const T u1 = FORWARD ? at[-1] : at[LD - 1];
+  const T2 y1 = w.template At<K, 1>();
+  sum.x -= u1 * y1.x;
+  sum.y -= u1 * y1.y;
+  const T inv = T(1) / at[0];
+  T2 v;
+  v.x = sum.x * inv;
+  v.y = sum.y * inv;
+  w.cur[K] = v;
+  if (!FORWARD && ln.s.scale >= 0) v = Scaled(v, st.Scale(buf, r));
+  ln.Store(row, v);
+}
+
+template <class T, int KD, bool FORWARD>
+__device__ __forceinline__ void WindowChunk(const Lane<T>& ln, const Stage<T>& st, int buf, int rowBase, int rows,
+                                            int hi, bool rhsLive, Window<typename PairOf<T>::type, KD>& w,
+                                            int lane) {
+  [&]<int... KS>(std::integer_sequence<int, KS...>) {
+    ((KS < rows ? WindowRow<T, KD, FORWARD, KS>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane) : void()), ...);
+  }(std::make_integer_sequence<int, kChunk>{});
+  w.Shift();
 }
 
 // The FP32 ring form's row sum in the register form's order, so that a row
@@ -483,33 +511,41 @@ __device__ __forceinline__ float2 RowSum32(float2 start, const float* at, int ld
   return sum;
 }
 
-// Slots 32 - KD .. 31 of the window from the wrapped ring: the KD rows before
-// a substitution's third chunk. Slot s holds row first + s (forward) or
-// first - s (backward); the ring holds row i at slot i % depth.
+// old[0 .. KD - 1] from the wrapped ring: the KD rows before a
+// substitution's third chunk, row first + 31 - d (forward) or first - 31 + d
+// (backward) at old[d]; the ring holds row i at slot i % depth.
 template <class T2, int KD, bool FORWARD>
-__device__ __forceinline__ void WindowLoad(const T2* ring, int first, int depth, T2 (&w)[kWindow]) {
+__device__ __forceinline__ void WindowLoad(const T2* ring, int first, int depth, Window<T2, KD>& w) {
 #pragma unroll
-  for (int s = kWindow - KD; s < kWindow; ++s) {
-    const int row = FORWARD ? first + s : first - s;
-    w[s] = ring[(row % depth) * kWarp];
+  for (int d = 0; d < KD; ++d) {
+    const int row = FORWARD ? first + 2 * kChunk - 1 - d : first - 2 * kChunk + 1 + d;
+    w.old[d] = ring[(row % depth) * kWarp];
   }
 }
 
 // The register form for chunk c >= 2 of a substitution, when the bandwidth
 // is one it is built for (the operators' 3 (ngll - 1) + 2 and ngll - 1 for
-// ngll 5 and 6); false: the ring form solves the chunk.
+// ngll 5 and 6); false: the ring form solves the chunk. The windows of the
+// four bandwidths share the kernel's registers (a union: one is live).
+template <class T2>
+union WindowSet {
+  Window<T2, 4> w4;
+  Window<T2, 5> w5;
+  Window<T2, 14> w14;
+  Window<T2, 17> w17;
+  __device__ WindowSet() {}
+};
+
 template <class T, bool FORWARD>
 __device__ __forceinline__ bool WindowSolve(int kd, int c, const Lane<T>& ln, const Stage<T>& st, int buf,
                                             const typename PairOf<T>::type* ring, int first, int depth, int rowBase,
-                                            int rows, int hi, bool rhsLive, typename PairOf<T>::type (&w)[kWindow],
+                                            int rows, int hi, bool rhsLive, WindowSet<typename PairOf<T>::type>& ws,
                                             int lane) {
-#define SL3D_WINDOW_CASE(KD)                                                                                 \
-  case KD:                                                                                                   \
-    if (c == 2) WindowLoad<typename PairOf<T>::type, KD, FORWARD>(ring, first, depth, w);                    \
-    if (c % 2 == 0)                                                                                          \
-      WindowChunk<T, KD, 0, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                      \
-    else                                                                                                     \
-      WindowChunk<T, KD, kChunk, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane);                 \
+  using T2 = typename PairOf<T>::type;
+#define SL3D_WINDOW_CASE(KD)                                                             \
+  case KD:                                                                               \
+    if (c == 2) WindowLoad<T2, KD, FORWARD>(ring, first, depth, ws.w##KD);               \
+    WindowChunk<T, KD, FORWARD>(ln, st, buf, rowBase, rows, hi, rhsLive, ws.w##KD, lane); \
     return true;
   switch (kd) {
     SL3D_WINDOW_CASE(4)
@@ -549,7 +585,7 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
   // unit, and its window's 128 registers slowed them (the mirrored ring
   // serves them better).
   constexpr bool kWindowForm = sizeof(T) == sizeof(float);
-  T2 window[kWindow];  // the register form's last solutions
+  WindowSet<T2> window;  // the register form's recent solutions
   if (mode == kSolveCompletion) {
     // x at rows lo .. lo + kd - 1 (stored scaled) seeds the ring
     for (int r = lo; r < min(n, lo + kd); ++r) {
