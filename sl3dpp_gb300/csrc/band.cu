@@ -426,7 +426,7 @@ struct Window {
 
 template <class T, int KD, bool FORWARD, int K>
 __device__ __forceinline__ void WindowRow(const Lane<T>& ln, const Stage<T>& st, int buf, int rowBase, int rows,
-                                          int hi, bool rhsLive, Window<typename PairOf<T>::type, KD>& w,
+                                          int hi, bool rhsLive, Window<typename PairOf<T>::type, KD>& w, T laneInv,
                                           int lane) {
   using T2 = typename PairOf<T>::type;
   constexpr int LD = KD + 1;
@@ -462,7 +462,7 @@ __device__ __forceinline__ void WindowRow(const Lane<T>& ln, const Stage<T>& st,
   const T2 y1 = w.template At<K, 1>();
   sum.x -= u1 * y1.x;
   sum.y -= u1 * y1.y;
-  const T inv = T(1) / at[0];
+  const T inv = __shfl_sync(0xffffffffu, laneInv, K);  // 1 / U(row, row), from lane K
   T2 v;
   v.x = sum.x * inv;
   v.y = sum.y * inv;
@@ -475,8 +475,14 @@ template <class T, int KD, bool FORWARD>
 __device__ __forceinline__ void WindowChunk(const Lane<T>& ln, const Stage<T>& st, int buf, int rowBase, int rows,
                                             int hi, bool rhsLive, Window<typename PairOf<T>::type, KD>& w,
                                             int lane) {
+  // the chunk's reciprocal diagonals, row k's in lane k, computed together
+  // off the substitution's dependency chain
+  T laneInv = T(1);
+  if (lane < rows) laneInv = T(1) / st.Band(buf)[(FORWARD ? lane : rows - 1 - lane) * (KD + 1) + KD];
   [&]<int... KS>(std::integer_sequence<int, KS...>) {
-    ((KS < rows ? WindowRow<T, KD, FORWARD, KS>(ln, st, buf, rowBase, rows, hi, rhsLive, w, lane) : void()), ...);
+    ((KS < rows ? WindowRow<T, KD, FORWARD, KS>(ln, st, buf, rowBase, rows, hi, rhsLive, w, laneInv, lane)
+                : void()),
+     ...);
   }(std::make_integer_sequence<int, kChunk>{});
   w.Shift();
 }
