@@ -621,9 +621,12 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
               WindowSolve<T, true>(kd, c, ln, st, buf, ring, lo, depth, j0, j1 - j0, hi, true, window, lane))
             return;
           const T* band = st.Band(buf);
+          // the chunk's reciprocal diagonals, row j0 + k's in lane k: one
+          // division a lane instead of one a row on every lane
+          const T laneInv = lane < j1 - j0 ? T(1) / band[lane * ld + kd] : T(1);
           for (int j = j0; j < j1; ++j) {
             const T* column = band + (j - j0) * ld + kd;  // column[-t] = U(j - t, j)
-            const T inv = T(1) / column[0];
+            const T inv = __shfl_sync(0xffffffffu, laneInv, j - j0);
             T2 a = j <= hi ? Start(ln, st, buf, j - j0, j, lane) : zero;
             T2 b = zero;
             const int reach = min(kd, j - lo);
@@ -682,9 +685,10 @@ __global__ void CholeskySolveKernel(const sl3dgpu_band_system* systems, const Wo
             WindowSolve<T, false>(kd, c, ln, st, buf, ring, top - 1, depth, i1 - 1, i1 - i0, 0, rhsEnd > 0, window, lane))
           return;
         const T* band = st.Band(buf);
+        const T laneInv = lane < i1 - i0 ? T(1) / band[lane * ld + kd] : T(1);  // row i0 + k's in lane k
         for (int i = i1 - 1; i >= i0; --i) {
           const int r = i - i0;
-          const T inv = T(1) / band[r * ld + kd];
+          const T inv = __shfl_sync(0xffffffffu, laneInv, r);
           T2 a = rhsEnd > 0 ? st.Rhs(buf, r)[lane] : zero;
           T2 b = zero;
           const int reach = min(kd, n - 1 - i);
