@@ -582,12 +582,31 @@ __global__ void RelativeChangeKernel(const T2* next, const T2* now, long long n,
   T scale = 0, diff = 0;
   bool finite = true;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
-    const T2 a = next[i], b = now[i];
-    finite = finite && (a.x - a.x == T(0)) && (a.y - a.y == T(0));
-    scale = fmax(scale, a.x * a.x + a.y * a.y);
-    const T dx = a.x - b.x, dy = a.y - b.y;
-    diff = fmax(diff, dx * dx + dy * dy);
+  if constexpr (sizeof(T) == sizeof(double)) {
+    // FP64: the finiteness test and the maxima on the bits (a square is
+    // never negative, and non-negative doubles order as their bit patterns),
+    // so that only the squares and differences use GB300's small FP64 unit
+    unsigned long long scaleBits = 0, diffBits = 0, nonFinite = 0;
+    constexpr unsigned long long kExp = 0x7ff0000000000000ull;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
+      const T2 a = next[i], b = now[i];
+      const unsigned long long ax = __double_as_longlong(a.x), ay = __double_as_longlong(a.y);
+      nonFinite |= static_cast<unsigned long long>((ax & kExp) == kExp) | static_cast<unsigned long long>((ay & kExp) == kExp);
+      const double dx = a.x - b.x, dy = a.y - b.y;
+      scaleBits = max(scaleBits, static_cast<unsigned long long>(__double_as_longlong(a.x * a.x + a.y * a.y)));
+      diffBits = max(diffBits, static_cast<unsigned long long>(__double_as_longlong(dx * dx + dy * dy)));
+    }
+    scale = __longlong_as_double(static_cast<long long>(scaleBits));
+    diff = __longlong_as_double(static_cast<long long>(diffBits));
+    finite = nonFinite == 0;
+  } else {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
+      const T2 a = next[i], b = now[i];
+      finite = finite && (a.x - a.x == T(0)) && (a.y - a.y == T(0));
+      scale = fmax(scale, a.x * a.x + a.y * a.y);
+      const T dx = a.x - b.x, dy = a.y - b.y;
+      diff = fmax(diff, dx * dx + dy * dy);
+    }
   }
   s0[threadIdx.x] = static_cast<double>(scale);
   s1[threadIdx.x] = static_cast<double>(diff);
