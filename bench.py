@@ -355,44 +355,6 @@ class CpuSampler:
                 "seconds_per_step": step_s}
 
 
-# -- the ensemble workload ----------------------------------------------------------------------
-
-def ensemble_line(args):
-    """Member-steps per second of the ensemble (seeded members, 20 Sdirk2
-    steps each, mixed form with warm start), the members run concurrently by
-    sl3dgpu_v3d_run_many, then one by one; host wall clock around each run
-    (every run ends with its surface fields on the host). A warm-up runs every
-    member two steps first."""
-    from sl3dpp_gb300._lib import lib
-    from sl3dpp_gb300.ensemble import Ensemble, ensemble_members
-
-    t0 = time.perf_counter()
-    members = ensemble_members(args.ensemble, seed=4)
-    ens = Ensemble(members, precision=1)
-    setup = time.perf_counter() - t0
-    ens.run(steps=2)
-    launches0 = lib().sl3dgpu_launch_count()
-    together = ens.run()
-    launches = lib().sl3dgpu_launch_count() - launches0
-    alone = ens.run_sequential()
-    worst = max(float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
-                for a, b in zip(together["U"], alone["U"]))
-    steps = ens.member_steps()
-    value = steps / together["seconds"]
-    counts = {l: sum(1 for m in members if m["lmax"] == l) for l in sorted({m["lmax"] for m in members})}
-    return {"metric": f"ensemble member-steps/s ({len(members)} members, lmax 32-128, 20 Sdirk2 steps each)",
-            "value": value, "unit": "member-steps/s", "n_gpus": 1, "steps": 20, "warmup": 2,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
-            "data": "synthetic (seeded delta fields and ice caps)",
-            "config": {"workload": "ensemble_config4", "members": len(members), "members_per_lmax": counts,
-                       "seed": 4, "precision": "mixed", "warm_start": 1, "fp64_emulation": 1,
-                       "parallelism": "one stream per member, a native host thread pool (sl3dgpu_v3d_run_many)"},
-            "concurrent_seconds": together["seconds"], "sequential_value": steps / alone["seconds"],
-            "sequential_seconds": alone["seconds"], "concurrent_speedup": alone["seconds"] / together["seconds"],
-            "max_rel_diff_concurrent_vs_sequential": worst, "member_steps": steps, "gpu_launches": launches,
-            "setup_seconds": setup}
-
-
 # -- main ------------------------------------------------------------------------------------------
 
 def main():
@@ -408,9 +370,6 @@ def main():
     ap.add_argument("--lmax", type=int, default=LMAX, help="a smaller workload for development runs")
     ap.add_argument("--correction-rtol", type=float, default=CORRECTION_RTOL)
     ap.add_argument("--correction-memory", type=int, default=CORRECTION_MEMORY)
-    ap.add_argument("--ensemble", type=int, default=0, metavar="MEMBERS",
-                    help="instead: the ensemble workload (MEMBERS independent evolutions, lmax 32-128, 20 steps "
-                         "each) run concurrently and one by one")
     args = ap.parse_args()
     if args.lmax != LMAX:
         _rescale(args.lmax)
@@ -459,10 +418,6 @@ def main():
     from sl3dpp_gb300._lib import lib
     import ctypes
 
-    if args.ensemble > 0:
-        if rank == 0:
-            print(json.dumps(ensemble_line(args)), flush=True)
-        return
     fp64, fp32 = ctypes.c_double(), ctypes.c_double()
     lib().sl3dgpu_fp64_fma_peak(ctypes.byref(fp64))
     lib().sl3dgpu_fp32_fma_peak(ctypes.byref(fp32))

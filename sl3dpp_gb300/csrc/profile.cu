@@ -21,7 +21,10 @@ std::atomic<bool> timing{false};
 std::mutex lock;
 std::vector<Record> records;
 std::vector<cudaEvent_t> pool;
-cudaEvent_t open[kKinds];
+// The open start event of each kind, per host thread: threads driving
+// operators on their own streams (sl3dgpu_v3d_run_many) each pair their own
+// starts and stops.
+thread_local cudaEvent_t open[kKinds];
 double totalMs[kKinds], totalFlops[kKinds], totalBytes[kKinds];
 long long counts[kKinds];
 

@@ -733,9 +733,9 @@ int Grid::Create(int lmax, int nmax, double oversampling, std::unique_ptr<Grid>&
   SL3D_CUDA(cudaMalloc(&g->dTheta, g->ntheta * sizeof(double)));
   SL3D_CUDA(cudaMalloc(&g->dWeights, g->ntheta * sizeof(double)));
   SL3D_CUDA(cudaMalloc(&g->dTwiddle, g->nphi * sizeof(double2)));
-  SL3D_CUDA(cudaMemcpy(g->dTheta, g->theta.data(), g->ntheta * sizeof(double), cudaMemcpyHostToDevice));
-  SL3D_CUDA(cudaMemcpy(g->dWeights, g->weights.data(), g->ntheta * sizeof(double), cudaMemcpyHostToDevice));
-  SL3D_CUDA(cudaMemcpy(g->dTwiddle, tw.data(), g->nphi * sizeof(double2), cudaMemcpyHostToDevice));
+  SL3D_CUDA(CopyIn(g->dTheta, g->theta.data(), g->ntheta * sizeof(double)));
+  SL3D_CUDA(CopyIn(g->dWeights, g->weights.data(), g->ntheta * sizeof(double)));
+  SL3D_CUDA(CopyIn(g->dTwiddle, tw.data(), g->nphi * sizeof(double2)));
   out = std::move(g);
   return SL3DGPU_OK;
 }
@@ -786,8 +786,7 @@ int Grid::Table(int N, const SpinTable** out) {
     const size_t size = static_cast<size_t>(t.rowOffset.back()) * ntheta;
     SL3D_CUDA(cudaMalloc(&t.values, std::max<size_t>(size, 1) * sizeof(double)));
     SL3D_CUDA(cudaMalloc(&t.dRowOffset, t.rowOffset.size() * sizeof(int)));
-    SL3D_CUDA(cudaMemcpy(t.dRowOffset, t.rowOffset.data(), t.rowOffset.size() * sizeof(int),
-                         cudaMemcpyHostToDevice));
+    SL3D_CUDA(CopyIn(t.dRowOffset, t.rowOffset.data(), t.rowOffset.size() * sizeof(int)));
     dim3 grid((ntheta + 127) / 128, 2 * lmax + 1);
     prof::Scope scope(prof::kOther, nullptr);
     WignerTableKernel<<<grid, 128>>>(lmax, N, ntheta, dTheta, t.dRowOffset, t.values);
@@ -851,7 +850,7 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
   b.analysis = analysis;
   if (b.count > 0) {
     SL3D_CUDA(cudaMalloc(&b.items, items.size() * sizeof(GemmItem)));
-    SL3D_CUDA(cudaMemcpy(b.items, items.data(), items.size() * sizeof(GemmItem), cudaMemcpyHostToDevice));
+    SL3D_CUDA(CopyIn(b.items, items.data(), items.size() * sizeof(GemmItem)));
   }
   // The tensor-core form's tiles: 128-row tiles of A in the spin's panel,
   // 16-deep K steps, one column tile when N fits.
@@ -928,12 +927,11 @@ int Grid::RunGemm64(int N, bool real, Batch& b, const double* B, double* C, bool
   if (b.count == 0) return SL3DGPU_OK;
   if (dTcError_ == nullptr) {
     SL3D_CUDA(cudaMalloc(&dTcError_, sizeof(int)));
-    SL3D_CUDA(cudaMemset(dTcError_, 0, sizeof(int)));
+    SL3D_CUDA(ZeroIn(dTcError_, sizeof(int)));
   }
   if (b.tc64Items == nullptr) {
     SL3D_CUDA(cudaMalloc(&b.tc64Items, b.tc64Host.size() * sizeof(Tc64Item)));
-    SL3D_CUDA(cudaMemcpy(b.tc64Items, b.tc64Host.data(), b.tc64Host.size() * sizeof(Tc64Item),
-                         cudaMemcpyHostToDevice));
+    SL3D_CUDA(CopyIn(b.tc64Items, b.tc64Host.data(), b.tc64Host.size() * sizeof(Tc64Item)));
     SL3D_CUDA(cudaMalloc(&b.packed64, std::max<long long>(b.packed64Count, 1) * sizeof(uint16_t)));
     SL3D_CUDA(cudaMalloc(&b.colExp, std::max<long long>(b.colExps, 1) * sizeof(int)));
   }
@@ -1058,15 +1056,15 @@ int Grid::RunGemmF(int N, bool real, Batch& b, const float* B, float* C, bool ac
   static_assert(sizeof(TcItemHost) == sizeof(TcItem), "host and device tensor-core items agree");
   if (dTcError_ == nullptr) {
     SL3D_CUDA(cudaMalloc(&dTcError_, sizeof(int)));
-    SL3D_CUDA(cudaMemset(dTcError_, 0, sizeof(int)));
+    SL3D_CUDA(ZeroIn(dTcError_, sizeof(int)));
   }
   if (b.tcItems == nullptr) {
     SL3D_CUDA(cudaMalloc(&b.tcItems, b.tcHost.size() * sizeof(TcItem)));
-    SL3D_CUDA(cudaMemcpy(b.tcItems, b.tcHost.data(), b.tcHost.size() * sizeof(TcItem), cudaMemcpyHostToDevice));
+    SL3D_CUDA(CopyIn(b.tcItems, b.tcHost.data(), b.tcHost.size() * sizeof(TcItem)));
     SL3D_CUDA(cudaMalloc(&b.packed, std::max<long long>(b.packedFloats, 1) * sizeof(float)));
     SL3D_CUDA(cudaMalloc(&b.dTcTiles, std::max<size_t>(b.tcTiles.size(), 1) * sizeof(int4)));
     if (!b.tcTiles.empty())
-      SL3D_CUDA(cudaMemcpy(b.dTcTiles, b.tcTiles.data(), b.tcTiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
+      SL3D_CUDA(CopyIn(b.dTcTiles, b.tcTiles.data(), b.tcTiles.size() * sizeof(int4)));
   }
   const auto* items = static_cast<const TcItem*>(b.tcItems);
   const std::array<int, 3> key{N, real ? 1 : 0, b.analysis ? 1 : 0};

@@ -604,7 +604,7 @@ int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
   lateralFirst = last >= 0 ? elemFirstNode[nodeElement[first]] : 0;
   lateralEnd = last >= 0 ? elemFirstNode[nodeElement[last]] + geo.np : 0;
   SL3D_CUDA(cudaStreamSynchronize(stream));  // no earlier kernel of the operator still reads it
-  SL3D_CUDA(cudaMemcpy(factor.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
+  SL3D_CUDA(CopyIn(factor.p, host.data(), values * sizeof(double)));
   return SL3DGPU_OK;
 }
 
@@ -1616,7 +1616,7 @@ int Viscoelastic3DGpu::SetModuli(const double* dMu, const double* dKappa, bool o
   std::vector<char> lateral(P, 0);
   auto take = [&](const double* src, Dev<double>& dst) -> int {
     if (src == nullptr) {
-      SL3D_CUDA(cudaMemset(dst.p, 0, values * sizeof(double)));
+      SL3D_CUDA(ZeroIn(dst.p, values * sizeof(double)));
       return SL3DGPU_OK;
     }
     if (onDevice) {
@@ -1627,7 +1627,7 @@ int Viscoelastic3DGpu::SetModuli(const double* dMu, const double* dKappa, bool o
     for (int p = 0; p < P; ++p)
       for (long long x = p * fieldSize; x < (p + 1) * fieldSize && !lateral[p]; ++x) lateral[p] = host[x] != 0.0;
     SL3D_CUDA(cudaStreamSynchronize(stream));  // no earlier kernel of the operator still reads it
-    SL3D_CUDA(cudaMemcpy(dst.p, host.data(), values * sizeof(double), cudaMemcpyHostToDevice));
+    SL3D_CUDA(CopyIn(dst.p, host.data(), values * sizeof(double)));
     return SL3DGPU_OK;
   };
   SL3D_TRY(take(dMu, weight));

@@ -574,7 +574,12 @@ __global__ void CombineKernel(long long values, long long fieldSize, const doubl
 // -- the convergence measure ------------------------------------------------------------------
 
 // Per block: max |next|^2, max |next - now|^2 and finiteness, in the data's
-// precision (a maximum of squares loses nothing to the order).
+// precision (a maximum of squares loses nothing to the order). Both iterates
+// must be finite: the reference tests `next` alone, where a non-finite `now`
+// can only come from its previous pass; here `now` may be a caller's or an
+// extrapolated guess, and a NaN in it would otherwise vanish from the
+// maxima (a NaN with its sign bit set is the largest bit pattern, and fmax
+// drops NaNs), under-reporting the change.
 template <class T2>
 __global__ void RelativeChangeKernel(const T2* next, const T2* now, long long n, double* partial) {
   using T = typename Scalar<T2>::type;
@@ -591,7 +596,9 @@ __global__ void RelativeChangeKernel(const T2* next, const T2* now, long long n,
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
       const T2 a = next[i], b = now[i];
       const unsigned long long ax = __double_as_longlong(a.x), ay = __double_as_longlong(a.y);
-      nonFinite |= static_cast<unsigned long long>((ax & kExp) == kExp) | static_cast<unsigned long long>((ay & kExp) == kExp);
+      const unsigned long long bx = __double_as_longlong(b.x), by = __double_as_longlong(b.y);
+      nonFinite |= static_cast<unsigned long long>((ax & kExp) == kExp) | static_cast<unsigned long long>((ay & kExp) == kExp) |
+                   static_cast<unsigned long long>((bx & kExp) == kExp) | static_cast<unsigned long long>((by & kExp) == kExp);
       const double dx = a.x - b.x, dy = a.y - b.y;
       scaleBits = max(scaleBits, static_cast<unsigned long long>(__double_as_longlong(a.x * a.x + a.y * a.y)));
       diffBits = max(diffBits, static_cast<unsigned long long>(__double_as_longlong(dx * dx + dy * dy)));
@@ -602,7 +609,7 @@ __global__ void RelativeChangeKernel(const T2* next, const T2* now, long long n,
   } else {
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
       const T2 a = next[i], b = now[i];
-      finite = finite && (a.x - a.x == T(0)) && (a.y - a.y == T(0));
+      finite = finite && (a.x - a.x == T(0)) && (a.y - a.y == T(0)) && (b.x - b.x == T(0)) && (b.y - b.y == T(0));
       scale = fmax(scale, a.x * a.x + a.y * a.y);
       const T dx = a.x - b.x, dy = a.y - b.y;
       diff = fmax(diff, dx * dx + dy * dy);

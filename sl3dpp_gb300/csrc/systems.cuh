@@ -61,7 +61,7 @@ struct Dev {
   }
   cudaError_t Upload(const std::vector<T>& v) {
     if (cudaError_t e = Alloc(v.size()); e != cudaSuccess) return e;
-    return v.empty() ? cudaSuccess : cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return CopyIn(p, v.data(), v.size() * sizeof(T));
   }
 };
 

@@ -23,6 +23,15 @@ def _entry():
     return fn
 
 
+def dense_upper(ab, n, kd):
+    """The symmetric matrix whose upper band LAPACK stores in ab."""
+    a = np.zeros((n, n))
+    for j in range(n):
+        for i in range(max(0, j - kd), j + 1):
+            a[i, j] = a[j, i] = ab[j * (kd + 1) + kd + i - j]
+    return a
+
+
 @pytest.mark.gpu
 def test_no_alloc_solve_matches_the_allocating_solve(gpu):
     import torch
@@ -33,6 +42,7 @@ def test_no_alloc_solve_matches_the_allocating_solve(gpu):
     solve = _entry()
     n, kd = 1803, 17  # the largest degree system's shape at lmax 256
     ab = symmetric_band(n, kd, 2.0 * kd + 1.0, 21)
+    dense = dense_upper(ab, n, kd)
     assert BandCholeskyFactor(ab, n, kd) == 0
     d_ab = torch.tensor(ab, device=gpu)
     stream = torch.cuda.current_stream().cuda_stream
@@ -43,7 +53,36 @@ def test_no_alloc_solve_matches_the_allocating_solve(gpu):
         d_b = torch.tensor(b, device=gpu)
         assert solve(d_ab.data_ptr(), n, kd, d_b.data_ptr(), nrhs, stream) == _lib.OK
         torch.cuda.synchronize()
-        assert rel(d_b.cpu().numpy(), want) < TOL
+        got = d_b.cpu().numpy()
+        assert rel(got, want) < TOL
+        # and against a dense solve of the same system (numpy's LAPACK), so
+        # that the entry point's own packing is checked by other arithmetic
+        exact = np.linalg.solve(dense, b.reshape(nrhs, n).T).T.reshape(-1)
+        assert rel(got, exact) < 1e-11
+
+
+@pytest.mark.gpu
+def test_no_alloc_solve_single_column_small_system(gpu):
+    """One right-hand side (not a multiple of the 64-column work item) on a
+    small system, against a dense solve."""
+    import torch
+
+    from sl3dpp_gb300 import _lib
+    from sl3dpp_gb300.band import BandCholeskyFactor
+
+    solve = _entry()
+    stream = torch.cuda.current_stream().cuda_stream
+    for n, kd, nrhs, seed in [(40, 5, 1, 31), (97, 14, 3, 32)]:
+        ab = symmetric_band(n, kd, 2.0 * kd + 1.0, seed)
+        dense = dense_upper(ab, n, kd)
+        assert BandCholeskyFactor(ab, n, kd) == 0
+        b = uniform(n * nrhs, seed + 100)
+        d_ab = torch.tensor(ab, device=gpu)
+        d_b = torch.tensor(b, device=gpu)
+        assert solve(d_ab.data_ptr(), n, kd, d_b.data_ptr(), nrhs, stream) == _lib.OK
+        torch.cuda.synchronize()
+        exact = np.linalg.solve(dense, b.reshape(nrhs, n).T).T.reshape(-1)
+        assert rel(d_b.cpu().numpy(), exact) < 1e-12
 
 
 @pytest.mark.gpu
