@@ -316,6 +316,11 @@ int sl3dgpu_degree_surface_dof(const sl3dgpu_degree* op, int component);
 int sl3dgpu_degree_load(const sl3dgpu_degree* op, double* out);
 int sl3dgpu_degree_tide(const sl3dgpu_degree* op, int power, double* out);
 int sl3dgpu_degree_apply(const sl3dgpu_degree* op, const double* x, int nrhs, double* y);
+/* The assembled, unscaled upper band ((kd + 1) x ndof, LAPACK storage): the
+ * matrix DegreeOperator / ToroidalOperator hold before Factorise scales it
+ * (src/DegreeOperator.cpp:253-474, src/ToroidalOperator.cpp), assembled on
+ * the GPU. */
+int sl3dgpu_degree_band(const sl3dgpu_degree* op, double* out);
 int sl3dgpu_degree_solve(const sl3dgpu_degree* op, double* b, int nrhs);
 
 /* The configurations' Earth (radius 6371 km, fluid core to 3480 km, linear
@@ -390,6 +395,15 @@ int sl3dgpu_v3d_surface(sl3dgpu_v3d* op, int component, double* out);
  * displacement (the degree-0 moment row of detail/ViscoelasticDegree.hpp:
  * 142-161), in the operator's non-dimensional units. */
 int sl3dgpu_v3d_inertia_moment(sl3dgpu_v3d* op, double* out);
+/* The assembled, unscaled upper band of degree l's spheroidal (toroidal = 0)
+ * or toroidal (1, l >= 1) system in the flavour of one scheme (0 exponential
+ * trapezoid, 1 backward Euler; Sdirk2's stages are backward Euler flavours)
+ * and step length dt (0: the elastic flavour) -- the reference's flavour
+ * systems (Viscoelastic3D.cpp:535-558, DegreeOperator.cpp:253-474) with the
+ * flavour's point shear, assembled on the GPU. out NULL asks the order n and
+ * bandwidth kd; capacity counts doubles. */
+int sl3dgpu_v3d_assembled_band(sl3dgpu_v3d* op, int scheme, double dt, int toroidal, int l, double* out,
+                               long long capacity, int* n, int* kd);
 /* The warm-start hook (OpenStep::Converge's start, Viscoelastic3D.hpp:562-569):
  * a guess of the strain coefficients at the end of the NEXT step, in the
  * device layout a state's coefficients have (sl3dgpu_v3d_state_coefficients;

@@ -15,20 +15,18 @@ import sys
 HERE = pathlib.Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIBRARY = BUILD / "liboracle.so"
-PRODUCT_HOST = HERE.parent / "sl3dpp_gb300" / "csrc" / "host"
 
 
 def _sources() -> list[pathlib.Path]:
-    # the oracle's own restatement, plus the library's host-side radial setup
-    # (mesh, material, rheology, degree systems), which it shares
-    return sorted(HERE.glob("*.cpp")) + sorted(PRODUCT_HOST.glob("radial.cpp"))
+    # the oracle's own restatement alone: it shares no source with the library
+    return sorted(HERE.glob("*.cpp"))
 
 
 def _stale(sources: list[pathlib.Path]) -> bool:
     if not LIBRARY.exists():
         return True
     built = LIBRARY.stat().st_mtime
-    inputs = sources + list(HERE.glob("*.h")) + list(PRODUCT_HOST.glob("*.hpp")) + list(PRODUCT_HOST.glob("*.cpp"))
+    inputs = sources + list(HERE.glob("*.h")) + list(HERE.glob("*.hpp")) + [pathlib.Path(__file__)]
     return any(p.stat().st_mtime > built for p in inputs)
 
 
@@ -39,7 +37,7 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
     BUILD.mkdir(exist_ok=True)
     tmp = LIBRARY.with_suffix(".so.tmp")
     cmd = ["g++", "-O2", "-std=c++23", "-fPIC", "-shared", "-fopenmp", "-I", str(HERE),
-           "-I", str(PRODUCT_HOST), *map(str, sources), "-o", str(tmp)]
+           *map(str, sources), "-o", str(tmp)]
     result = subprocess.run(cmd, capture_output=True, text=True)
     if result.returncode != 0:
         raise RuntimeError(f"building the oracle failed:\n{' '.join(cmd)}\n{result.stderr}")

@@ -15,13 +15,13 @@
 //    1885-1974 (Finish, Converge), 1982-2030 (Step, Sdirk2 by recipe),
 //    2032-2079 (Surface);
 //  - include/sl3dpp/detail/AndersonMixer.hpp:65-219 (the mixer, its Gram
-//    least squares by the symmetric minimum-norm solve of lstsq.hpp in place
-//    of LAPACK's dgelss);
+//    least squares by the SVD minimum-norm solve of oracle_lstsq.hpp in
+//    place of LAPACK's dgelss);
 //  - include/sl3dpp/StepRecipe.hpp, src/StepRecipe.cpp (Sdirk2's stages).
 // The radial setup (mesh, material, rheology, degree systems) is the
-// library's host code (sl3dpp_gb300/csrc/host/radial.cpp), shared; the
-// factorisations, solves, transforms and every per-pass operation are
-// restated here on the CPU.
+// oracle's own (oracle_radial.cpp), independent of the library's GPU
+// assembly; the factorisations, solves, transforms and every per-pass
+// operation are restated here on the CPU.
 
 #include <algorithm>
 #include <cmath>
@@ -36,14 +36,14 @@
 #include <omp.h>
 
 #include "../include/sl3dgpu.h"
-#include "lstsq.hpp"
+#include "oracle_lstsq.hpp"
 #include "oracle.h"
-#include "radial.hpp"
+#include "oracle_radial.hpp"
 
 namespace oracle {
 
 using C = std::complex<double>;
-using namespace sl3dgpu::host;
+using namespace orc;
 
 // -- FFT (recursive mixed radix 2, 3, 5) --------------------------------------------------------
 
@@ -387,7 +387,7 @@ class Mixer {
     std::vector<double> a(static_cast<std::size_t>(m) * m), g(m);
     for (int i = 0; i < m; ++i)
       for (int j = 0; j < m; ++j) a[static_cast<std::size_t>(i) * m + j] = gram_[static_cast<std::size_t>(i) * memory_ + j];
-    if (!sl3dgpu::SymmetricLstsq(m, a.data(), gamma.data(), g.data())) {
+    if (!orc::SvdLstsq(m, a.data(), gamma.data(), g.data())) {
       sweep([&](std::size_t s, std::size_t j, std::size_t) { xs[s][j] = gs[s][j]; });
       return;
     }
@@ -425,7 +425,7 @@ class Viscoelastic3D {
         mesh_(RadialMesh::Create(earth_, options.ngll)),
         material_(Material::Create(earth_, mesh_)),
         rheology_(Rheology::FromEarth(earth_, material_)),
-        reference_(rheology_, true),
+        reference_(rheology_),
         grid_(options.lmax, options.oversampling),
         gll_(MemoryPoints::Of(false, mesh_)) {
     points_ = static_ ? &gll_ : &reference_.points;
@@ -813,7 +813,8 @@ class Viscoelastic3D {
           real[static_cast<std::size_t>(c) * ndof + d] = xl[static_cast<std::size_t>(c) * ndof + d].real();
           real[static_cast<std::size_t>(cols + c) * ndof + d] = xl[static_cast<std::size_t>(c) * ndof + d].imag();
         }
-      const auto k = tor ? f.tor[l]->Apply(real, 2 * cols) : f.sph[l]->Apply(real, 2 * cols);
+      const auto k = tor ? ApplySymmetricBand(f.tor[l]->Band(), ndof, f.tor[l]->Bandwidth(), real, 2 * cols)
+                         : ApplySymmetricBand(f.sph[l]->Band(), ndof, f.sph[l]->Bandwidth(), real, 2 * cols);
       for (int c = 0; c < cols; ++c)
         for (int d = 0; d < ndof; ++d) {
           const std::size_t at = static_cast<std::size_t>(c) * ndof + d;
@@ -1470,7 +1471,7 @@ int oracle_v3d_step(oracle_v3d* h, oracle_state* state, double dt, int scheme, c
                     const double* load1, sl3dgpu_step_info* info) {
   oracle::Info i;
   try {
-    state->s = h->op->Step(state->s, dt, static_cast<sl3dgpu::host::Scheme>(scheme),
+    state->s = h->op->Step(state->s, dt, static_cast<orc::Scheme>(scheme),
                            reinterpret_cast<const C*>(load0), reinterpret_cast<const C*>(load1), i);
   } catch (const std::exception&) {
     return -3;
@@ -1490,7 +1491,7 @@ int oracle_v3d_step_tide(oracle_v3d* h, oracle_state* state, double dt, int sche
                          const double* load1, const double* tide0, const double* tide1, sl3dgpu_step_info* info) {
   oracle::Info i;
   try {
-    state->s = h->op->Step(state->s, dt, static_cast<sl3dgpu::host::Scheme>(scheme),
+    state->s = h->op->Step(state->s, dt, static_cast<orc::Scheme>(scheme),
                            reinterpret_cast<const C*>(load0), reinterpret_cast<const C*>(load1), i,
                            reinterpret_cast<const C*>(tide0), reinterpret_cast<const C*>(tide1));
   } catch (const std::exception&) {
@@ -1586,7 +1587,7 @@ extern "C" int oracle_ep3d_solve_lateral(oracle_v3d* h, const double* load, doub
 
 extern "C" int oracle_standard_earth(int elements, double kelvin_fraction, double kelvin_div,
                                      sl3dgpu_layer* out) {
-  const auto layers = sl3dgpu::host::StandardEarthLayers(elements, kelvin_fraction, kelvin_div);
+  const auto layers = orc::StandardEarthLayers(elements, kelvin_fraction, kelvin_div);
   for (std::size_t i = 0; i < layers.size(); ++i) {
     const auto& L = layers[i];
     out[i] = sl3dgpu_layer{L.r0, L.r1, L.fluid ? 1 : 0, L.elements, L.rho0, L.rho1, L.kappa0, L.kappa1,

@@ -33,7 +33,8 @@
 #include <thread>
 #include <vector>
 
-#include "host/radial.hpp"
+#include "assemble.cuh"
+#include "host/earth.hpp"
 #include "sht.cuh"
 #include "step_kernels.cuh"
 #include "systems.cuh"
@@ -77,11 +78,17 @@ struct V3dState {
 class Viscoelastic3DGpu {
  public:
   sl3dgpu_v3d_options options{};
-  std::unique_ptr<host::LayeredEarth> earth;
+  std::unique_ptr<host::LayeredBody> earth;
   std::unique_ptr<host::RadialMesh> mesh;
   std::unique_ptr<host::Material> material;
   std::unique_ptr<host::Rheology> rheology;
-  std::unique_ptr<host::ReferenceRheology> reference;
+  std::unique_ptr<host::RelaxingBody> reference;
+  // The degrees' unknowns and the flavours' assembly: every degree's layout,
+  // the plan of their bands and the nodal material on the device.
+  std::vector<host::SpheroidalLayout> sphLayouts;
+  std::vector<host::ToroidalLayout> torLayouts;
+  AssemblyPlan plan;
+  DeviceMaterial deviceMaterial;
   std::unique_ptr<Grid> grid;
   cudaStream_t stream = nullptr;
 
@@ -216,6 +223,9 @@ class Viscoelastic3DGpu {
   int InertiaMoment(double* out);
   std::vector<double> momentRow;  // the degree-0 inertia-moment row over its dofs
   int StrainReference(const V3dState& st, double* out);
+  // The assembled (unscaled) upper band of degree l's spheroidal or
+  // toroidal system in the flavour (scheme, dt); dt = 0 the elastic one.
+  int AssembledBand(int scheme, double dt, int toroidal, int l, double* out, long long capacity, int* n, int* kd);
 
  private:
   int AllocState(V3dState& st);
@@ -317,11 +327,11 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
       ls[i] = host::Layer{s.r0, s.r1, s.fluid != 0, s.rho0, s.rho1, s.kappa0, s.kappa1, s.mu0, s.mu1,
                           s.viscosity, s.kelvin_fraction, s.kelvin_viscosity, s.elements};
     }
-    earth = std::make_unique<host::LayeredEarth>(ls, host::Scales::Geophysical(layers[nlayers - 1].r1));
+    earth = std::make_unique<host::LayeredBody>(ls, host::Scales::Geophysical(layers[nlayers - 1].r1));
     mesh = std::make_unique<host::RadialMesh>(host::RadialMesh::Create(*earth, opt.ngll));
     material = std::make_unique<host::Material>(host::Material::Create(*earth, *mesh));
-    rheology = std::make_unique<host::Rheology>(host::Rheology::FromEarth(*earth, *material));
-    reference = std::make_unique<host::ReferenceRheology>(*rheology, true);
+    rheology = std::make_unique<host::Rheology>(host::Rheology::FromBody(*earth, *material));
+    reference = std::make_unique<host::RelaxingBody>(*rheology);
   } catch (const std::exception& e) {
     SetError(std::string("v3d: ") + e.what());
     return SL3DGPU_ERR_ARGUMENT;
@@ -345,7 +355,6 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   const auto& nodal = staticMode ? *material : reference->nodal;
   const auto& msh = nodal.mesh;
   const auto& pts = staticMode ? *gllPoints : reference->points;
-  const host::PointShear* elasticShear = staticMode ? nullptr : &reference->elastic;
   const int n = msh.NGll(), E = msh.ElementCount(), L = opt.lmax;
   K = staticMode ? 0 : static_cast<int>(rheology->branches.size());
   elemFirstNode.assign(E, -1);
@@ -394,8 +403,18 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
   std::vector<int> sphMap(static_cast<size_t>(L + 1) * nglob * 2, -1), torMap(static_cast<size_t>(L + 1) * nglob, -1);
   degrees.resize(L + 1);
   long long sphOff = 0, torOff = 0;
+  try {
+    for (int l = 0; l <= L; ++l) sphLayouts.emplace_back(nodal, l, opt.eps);
+    for (int l = 1; l <= L; ++l) torLayouts.emplace_back(nodal, l, opt.eps);
+  } catch (const std::exception& e) {
+    SetError(std::string("v3d: ") + e.what());
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (const auto& layout : sphLayouts) plan.Add(layout);
+  for (const auto& layout : torLayouts) plan.Add(layout);
+  SL3D_TRY(deviceMaterial.Upload(nodal, pts));
   for (int l = 0; l <= L; ++l) {
-    host::DegreeOperator op(nodal, l, opt.eps, elasticShear);
+    const host::SpheroidalLayout& op = sphLayouts[l];
     auto& d = degrees[l];
     d.firstNode = firstNode[l];
     d.firstGlobal = d.firstNode < P ? msh.GlobalIndex(nodeElement[d.firstNode], 0) : 0;
@@ -430,7 +449,7 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     d.torRhs = torOff;
     d.surfaceW = -1;
     if (l >= 1) {
-      host::ToroidalOperator top(nodal, l, opt.eps, elasticShear);
+      const host::ToroidalLayout& top = torLayouts[l - 1];
       d.torNdof = top.DofCount();
       d.surfaceW = top.SurfaceDof();
       torOff += static_cast<long long>(d.torNdof) * (l + 1);
@@ -612,10 +631,11 @@ int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
 
 int Viscoelastic3DGpu::BuildFlavour(const host::PointShear& shear, Flavour& f) {
   SystemsInput in;
-  in.nodal = staticMode ? material.get() : &reference->nodal;
+  in.material = &deviceMaterial;
+  in.plan = &plan;
+  in.sph = &sphLayouts;
   in.shear = staticMode ? nullptr : &shear;
   in.lmax = options.lmax;
-  in.eps = options.eps;
   in.degrees = &degrees;
   in.rhsSphComplex = rhsSphComplex;
   const bool stepFlavour = &f != elastic.get();
@@ -1600,6 +1620,30 @@ int Viscoelastic3DGpu::ConvergeConjugateGradients(const Flavour& f, const double
   return SL3DGPU_OK;
 }
 
+int Viscoelastic3DGpu::AssembledBand(int scheme, double dt, int toroidal, int l, double* out, long long capacity,
+                                     int* n, int* kd) {
+  const int L = options.lmax;
+  if (l < (toroidal ? 1 : 0) || l > L || scheme < 0 || scheme > 1 || !(dt >= 0.0)) {
+    SetError("v3d: a degree in range (toroidal from 1), scheme 0 (exponential trapezoid) or 1 (backward Euler) "
+             "and dt >= 0");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  Flavour* f = elastic.get();
+  if (dt > 0.0) SL3D_TRY(FlavourOf(scheme, dt, &f));
+  const AssemblySystem& sys = plan.systems[toroidal ? L + l : l];
+  const long long size = static_cast<long long>(sys.kd + 1) * sys.ndof;
+  if (n) *n = sys.ndof;
+  if (kd) *kd = sys.kd;
+  if (out == nullptr) return SL3DGPU_OK;
+  if (capacity < size) {
+    SetError("v3d: the band needs " + std::to_string(size) + " values");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SL3D_CUDA(cudaMemcpyAsync(out, f->applyBands.p + sys.band, size * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
 // -- the static perturbation problem (ElasticPerturbation3D) ----------------------------------------
 
 // The moduli directions over the grid values (node-major, colatitude,
@@ -2117,6 +2161,15 @@ extern "C" int sl3dgpu_v3d_run_many(int count, sl3dgpu_v3d* const* ops, sl3dgpu_
       return statuses[i];
     }
   return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_assembled_band(sl3dgpu_v3d* h, int scheme, double dt, int toroidal, int l, double* out,
+                                          long long capacity, int* n, int* kd) {
+  if (h == nullptr) {
+    SetError("v3d: null operator");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.AssembledBand(scheme, dt, toroidal, l, out, capacity, n, kd);
 }
 
 extern "C" int sl3dgpu_v3d_inertia_moment(sl3dgpu_v3d* h, double* out) {

@@ -1,7 +1,7 @@
-// The degree systems of one operator flavour on the device: the host
-// assembly of every degree's spheroidal and toroidal band (DegreeOperator,
-// ToroidalOperator), their batched factorisation on the GPU (Cholesky, LU
-// with partial pivoting where the Cholesky fails, src/DegreeOperator.cpp:
+// The degree systems of one operator flavour on the device: every degree's
+// spheroidal and toroidal band assembled and scaled on the GPU (assemble.cu),
+// their batched factorisation (Cholesky, LU with partial pivoting where the
+// Cholesky fails or a diagonal is not positive, src/DegreeOperator.cpp:
 // 775-852), the work items of the batched solves, the load units
 // K^-1 Load, and on request the assembled bands for K x and FP32 copies.
 #pragma once
@@ -9,7 +9,7 @@
 #include <vector>
 
 #include "common.cuh"
-#include "host/radial.hpp"
+#include "host/earth.hpp"
 #include "step_kernels.cuh"
 
 namespace sl3dgpu {
@@ -79,8 +79,9 @@ struct Flavour {
   // and, for conjugate gradients, the unsolved vectors
   Dev<double> tideUnits, tideForces;
   Dev<float> bands32, scales32;  // the mixed form's FP32 copies
-  // conjugate gradients: the assembled (unscaled) bands for K x, their
-  // systems, and the unsolved load force vectors (DegreeOperator::Load)
+  // the assembled (unscaled) bands in assembly-plan order, kept for K x;
+  // for conjugate gradients their systems and the unsolved load force
+  // vectors (DegreeOperator::Load)
   Dev<double> applyBands, loadForces;
   Dev<sl3dgpu_band_system> dSphApply, dTorApply;
   int nSphApply = 0, nTorApply = 0, maxApplyRows = 0;
@@ -97,13 +98,20 @@ struct Flavour {
 };
 
 
-// What a flavour is built from: the nodal material and its point shear (null
-// for the plain elastic operators), the degrees' right-hand-side layout.
+struct DeviceMaterial;
+struct AssemblyPlan;
+
+// What a flavour is built from: the operator's material on the device and
+// its degrees' assembly plan (spheroidal degrees 0..lmax, then toroidal
+// 1..lmax), the spheroidal layouts (load and tide vectors), the flavour's
+// point shear (null for the plain elastic operators of the static problem)
+// and the degrees' right-hand-side layout.
 struct SystemsInput {
-  const host::Material* nodal = nullptr;
+  const DeviceMaterial* material = nullptr;
+  const AssemblyPlan* plan = nullptr;
+  const std::vector<host::SpheroidalLayout>* sph = nullptr;
   const host::PointShear* shear = nullptr;
   int lmax = 0;
-  double eps = 1e-8;
   const std::vector<DegreeInfo>* degrees = nullptr;
   long long rhsSphComplex = 0;  // where the toroidal columns start in a combined vector
   bool apply = false;           // keep the assembled bands and load vectors (K x, conjugate gradients)

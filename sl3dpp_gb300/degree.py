@@ -34,6 +34,7 @@ def _signatures():
             ("sl3dgpu_degree_load", i, [v, P_double]),
             ("sl3dgpu_degree_tide", i, [v, i, P_double]),
             ("sl3dgpu_degree_apply", i, [v, P_double, i, P_double]),
+            ("sl3dgpu_degree_band", i, [v, P_double]),
             ("sl3dgpu_degree_solve", i, [v, P_double, i])):
         fn = getattr(L, name)
         fn.restype, fn.argtypes = res, args
@@ -74,6 +75,13 @@ class DegreeOperator:
     def SurfaceDof(self, component: int = 0) -> int:
         out = lib().sl3dgpu_degree_surface_dof(self._h, component)
         return out if out >= -1 else check(out)
+
+    def Band(self) -> np.ndarray:
+        """The assembled, unscaled upper band as a (ndof, kd + 1) array (LAPACK
+        storage, one stored column per row)."""
+        out = np.empty((self.DofCount(), self.Bandwidth() + 1))
+        check(lib().sl3dgpu_degree_band(self._h, _p(out)))
+        return out
 
     def Load(self) -> np.ndarray:
         out = np.zeros(self.DofCount())

@@ -96,6 +96,7 @@ def _signatures():
         "sl3dgpu_v3d_run": (i, [v, v, P_double, i, i, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_run_many": (i, [i, v, v, v, v, i, v, v, v, v, i, v]),
         "sl3dgpu_v3d_state_coefficients_host": (i, [v, v, v]),
+        "sl3dgpu_v3d_assembled_band": (i, [v, i, d, i, i, P_double, ctypes.c_longlong, P_int, P_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -275,6 +276,19 @@ class Viscoelastic3D:
     def SurfaceToroidal(self) -> np.ndarray:
         """Viscoelastic3D::SurfaceToroidal: the surface W per (l, m >= 0)."""
         return self.Surface(3)
+
+    def assembled_band(self, l: int, toroidal: bool = False, scheme: int = 1, dt: float = 0.0) -> np.ndarray:
+        """Degree l's assembled, unscaled upper band ((kd + 1) x ndof, LAPACK
+        storage, column-major as a (ndof, kd + 1) array) in the flavour of
+        `scheme` (0 exponential trapezoid, 1 backward Euler) and `dt` (0: the
+        elastic flavour), as the GPU assembled it."""
+        n, kd = ctypes.c_int(), ctypes.c_int()
+        check(lib().sl3dgpu_v3d_assembled_band(self._h, scheme, dt, int(toroidal), l, None, 0, ctypes.byref(n),
+                                                ctypes.byref(kd)))
+        out = np.empty((n.value, kd.value + 1))
+        check(lib().sl3dgpu_v3d_assembled_band(self._h, scheme, dt, int(toroidal), l,
+                                                out.ctypes.data_as(P_double), out.size, None, None))
+        return out
 
     def InertiaMoment(self) -> float:
         """Viscoelastic3D::InertiaMoment of the last step's solutions."""

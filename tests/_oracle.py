@@ -37,6 +37,7 @@ def load() -> ctypes.CDLL:
         "oracle_expand_spin": (None, [i, i, i, i, P_double, P_double, P_double, P_double]),
         "oracle_synthesise_real": (None, [i, i, i, P_double, P_double, P_double]),
         "oracle_expand_real": (None, [i, i, i, P_double, P_double, P_double, P_double]),
+        "oracle_degree_band": (i, [v, i, i, d, i, i, d, i, i, P_double, P_int, P_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -44,6 +45,21 @@ def load() -> ctypes.CDLL:
         fn.argtypes = args
     _lib = L
     return L
+
+
+def degree_band(layers, ngll: int, l: int, toroidal: bool = False, relaxed: bool = True, scheme: int = 1,
+                dt: float = 0.0, eps: float = 1e-8) -> np.ndarray:
+    """The oracle's assembled, unscaled upper band of one degree, (ndof, kd + 1):
+    relaxed, the 3D step's flavour (long-term material, the point shear of a
+    step of `scheme` and model-unit length `dt`, 0 the elastic one); else the
+    unrelaxed material without point shear."""
+    L = load()
+    n, kd = ctypes.c_int(), ctypes.c_int()
+    args = (ctypes.cast(layers, ctypes.c_void_p), len(layers), ngll, eps, int(relaxed), scheme, dt, int(toroidal), l)
+    assert L.oracle_degree_band(*args, None, ctypes.byref(n), ctypes.byref(kd)) == 0
+    out = np.empty((n.value, kd.value + 1))
+    assert L.oracle_degree_band(*args, ptr(out), ctypes.byref(n), ctypes.byref(kd)) == 0
+    return out
 
 
 def ptr(a: np.ndarray):

@@ -123,7 +123,7 @@ def test_gpu_static_perturbation_matches_the_oracle(gpu):
     o = O.OraclePerturbation(_layers(), lmax)
     g = ElasticPerturbation3D(_layers(product=True), lmax)
     assert (g.node_count, g.ntheta, g.nphi) == (o.P, o.ntheta, o.nphi)
-    assert np.max(np.abs(g.radius - o.radius)) == 0.0
+    assert np.max(np.abs(g.radius - o.radius)) < 1e-14  # separate setups, the same nodes to rounding
     mu = _nodal(o, "mu")
     r = o.radius
     d_mu = _lateral(o, 0.1 * mu.max() * (0.5 + r * r),

@@ -116,7 +116,7 @@ def _pair(lmax, elements, ngll, kelvin=0.0, rms=0.5, ldelta=4, seed=11, **opt):
     o = O.OracleStep(layers_o, O.default_options(lmax, ngll, **opt))
     g = Viscoelastic3D(standard_earth(elements, kelvin, 10.0), Options.defaults(lmax, ngll, **opt))
     assert (g.node_count, g.ntheta, g.nphi) == (o.P, o.ntheta, o.nphi)
-    assert np.max(np.abs(g.radius - o.radius)) == 0.0
+    assert np.max(np.abs(g.radius - o.radius)) < 1e-14  # separate setups, the same nodes to rounding
     assert np.max(np.abs(g.theta - o.theta)) < 1e-15
     if rms > 0:
         d = delta_for(o, lmax, ldelta, rms, seed)
