@@ -56,3 +56,47 @@ def cap_field(theta: np.ndarray, nphi: int, alpha_deg: float, thickness: float) 
     """Surface density (kg m^-2) of a polar cap on a grid, colatitude-major."""
     ring = np.where(theta < np.radians(alpha_deg), RHO_ICE * thickness, 0.0)
     return np.repeat(ring, nphi)
+
+
+def legacy_deck_layers(knots: np.ndarray, max_element: float = 20e3):
+    """Layers from a legacy sl3d 1D model's knots (rows r [m], rho [kg m^-3],
+    kappa [GPa], mu [GPa], log10 viscosity [Pa s], 0 meaning none; a radius
+    repeated at a discontinuity): one layer per interval of non-zero
+    thickness, its fields linear between the knots, fluid where the shear
+    modulus vanishes at both ends, the interval's viscosity from its lower
+    knot, and elements no wider than max_element. The reference reads the
+    same format (Deck::ReadLegacySl3d) and interpolates by natural cubic
+    splines; with knots 20-40 km apart the linear form differs from it by
+    far less than the physical comparisons made with it."""
+    from .viscoelastic3d import Layer
+
+    out = []
+    for a, b in zip(knots[:-1], knots[1:]):
+        if not b[0] > a[0]:
+            continue
+        fluid = a[3] == 0.0 and b[3] == 0.0
+        out.append(Layer(r0=a[0], r1=b[0], fluid=int(fluid),
+                         elements=max(1, int(np.ceil((b[0] - a[0]) / max_element))),
+                         rho0=a[1], rho1=b[1], kappa0=a[2] * 1e9, kappa1=b[2] * 1e9,
+                         mu0=0.0 if fluid else a[3] * 1e9, mu1=0.0 if fluid else b[3] * 1e9,
+                         viscosity=10.0 ** a[4] if a[4] > 0.0 else 0.0, kelvin_fraction=0.0, kelvin_viscosity=0.0))
+    return (Layer * len(out))(*out)
+
+
+def fortran_gate_delta(theta: np.ndarray, nphi: int) -> np.ndarray:
+    """The Fortran visco_test's lateral pattern s = s(r) exp(0.3 (Y_2,-2 +
+    Y_2,2)) as a log-viscosity perturbation on a grid: delta = -0.6 c22
+    sin^2 theta cos 2 phi, c22 = sqrt(15 / (2 pi)) / 4, as the reference's
+    gate writes it (benchmarks/fortran_gate.cpp)."""
+    c22 = 0.25 * np.sqrt(15.0 / (2.0 * np.pi))
+    phi = 2.0 * np.pi * np.arange(nphi) / nphi
+    return (-0.6 * c22 * np.sin(theta)[:, None] ** 2 * np.cos(2.0 * phi)[None, :]).ravel()
+
+
+def fortran_gate_load_rate(lmax: int) -> np.ndarray:
+    """The visco_test's zonal load rate per degree, kg m^-2 s^-1 (degree 0 none):
+    exp(-2 pi (l + 1) / 10.5) sqrt((2 l + 1) / 4 pi) 5515 / 30 yr."""
+    l = np.arange(lmax + 1, dtype=np.float64)
+    rate = np.exp(-2.0 * np.pi * (l + 1) / 10.5) * np.sqrt((2 * l + 1) / (4 * np.pi)) * 5515.0 / (30 * SECONDS_PER_YEAR)
+    rate[0] = 0.0
+    return rate
