@@ -390,6 +390,11 @@ int sl3dgpu_v3d_step_device(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt
  * (:2083-2112, zero at degree 0); complex m >= 0 columns per degree in the
  * l(l+1)/2 + m layout, into host memory. */
 int sl3dgpu_v3d_surface(sl3dgpu_v3d* op, int component, double* out);
+/* The same surface coefficients written into a device buffer of
+ * (lmax + 1)(lmax + 2) / 2 complex values, stream-ordered on the operator's
+ * stream (sl3dgpu_v3d_stream) with no host wait: a driver collecting every
+ * step's surface keeps the steps back to back. */
+int sl3dgpu_v3d_surface_device(sl3dgpu_v3d* op, int component, double* device_out);
 /* Viscoelastic3D::InertiaMoment (Viscoelastic3D.cpp:2032-2048) of the last
  * step's solutions: sqrt(4 pi) int rho U r^3 dr of their degree-0 radial
  * displacement (the degree-0 moment row of detail/ViscoelasticDegree.hpp:

@@ -1197,14 +1197,14 @@ class Viscoelastic3D {
     };
     if (samplePasses >= 0) {
       if (tStart) *tStart = omp_get_wtime() - clock0;
-      const double clock1 = omp_get_wtime();
       Spectral it = s0;
       for (int k = 0; k < samplePasses; ++k) {
+        const double clock1 = omp_get_wtime();
         Spectral next = pass(it);
         info.residual = RelativeChange(next, it);
         it = std::move(next);
+        if (tPasses) tPasses[k] = omp_get_wtime() - clock1;  // each pass's seconds
       }
-      if (tPasses) *tPasses = omp_get_wtime() - clock1;
       solutionsOut = std::move(solutions);
       return state;
     }

@@ -219,7 +219,7 @@ class Viscoelastic3DGpu {
   int Step(V3dState& st, double dt, int scheme, const double* load0, const double* load1, sl3dgpu_step_info* info,
            bool onDevice = false, const double* tide0 = nullptr, const double* tide1 = nullptr);
   Dev<double2> tideDev0, tideDev1, tideDevMid;
-  int Surface(int component, double* out);
+  int Surface(int component, double* out, bool deviceOut = false);
   int InertiaMoment(double* out);
   std::vector<double> momentRow;  // the degree-0 inertia-moment row over its dofs
   int StrainReference(const V3dState& st, double* out);
@@ -1912,10 +1912,15 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   return SL3DGPU_OK;
 }
 
-int Viscoelastic3DGpu::Surface(int component, double* out) {
+int Viscoelastic3DGpu::Surface(int component, double* out, bool deviceOut) {
   if (component < 0 || component > 3) {
     SetError("v3d: component 0 (U), 1 (V), 2 (phi) or 3 (W, toroidal)");
     return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (deviceOut) {  // stream-ordered into the caller's device buffer, no wait
+    LaunchSurface(geo, rhsSph.p, rhsTor.p, component, reinterpret_cast<double2*>(out), stream);
+    SL3D_CHECK_LAUNCH();
+    return SL3DGPU_OK;
   }
   LaunchSurface(geo, rhsSph.p, rhsTor.p, component, surfaceOut.p, stream);
   SL3D_CHECK_LAUNCH();
@@ -2186,6 +2191,14 @@ extern "C" int sl3dgpu_v3d_surface(sl3dgpu_v3d* h, int component, double* out) {
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.Surface(component, out);
+}
+
+extern "C" int sl3dgpu_v3d_surface_device(sl3dgpu_v3d* h, int component, double* device_out) {
+  if (h == nullptr || device_out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Surface(component, device_out, true);
 }
 
 extern "C" int sl3dgpu_v3d_state_strain(sl3dgpu_v3d* h, const sl3dgpu_v3d_state* state, double* out) {

@@ -97,6 +97,7 @@ def _signatures():
         "sl3dgpu_v3d_run_many": (i, [i, v, v, v, v, i, v, v, v, v, i, v]),
         "sl3dgpu_v3d_state_coefficients_host": (i, [v, v, v]),
         "sl3dgpu_v3d_assembled_band": (i, [v, i, d, i, i, P_double, ctypes.c_longlong, P_int, P_int]),
+        "sl3dgpu_v3d_surface_device": (i, [v, i, v]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -272,6 +273,13 @@ class Viscoelastic3D:
         out = np.zeros((self.lmax + 1) * (self.lmax + 2) // 2, dtype=np.complex128)
         check(lib().sl3dgpu_v3d_surface(self._h, code, out.ctypes.data))
         return out
+
+    def SurfaceDevice(self, component, out) -> None:
+        """The surface coefficients into a CUDA complex128 tensor of (lmax + 1)(lmax + 2) / 2
+        values, stream-ordered on the operator's stream, without waiting."""
+        code = COMPONENTS[component] if isinstance(component, str) else int(component)
+        assert out.is_cuda and out.numel() == (self.lmax + 1) * (self.lmax + 2) // 2 and out.is_contiguous()
+        check(lib().sl3dgpu_v3d_surface_device(self._h, code, out.data_ptr()))
 
     def SurfaceToroidal(self) -> np.ndarray:
         """Viscoelastic3D::SurfaceToroidal: the surface W per (l, m >= 0)."""

@@ -272,14 +272,16 @@ class OracleStep:
         return info
 
     def sample(self, dt, passes, load0=None, load1=None):
-        """Seconds of a backward Euler stage's start and of `passes` passes."""
+        """Seconds of a backward Euler stage's start, and of each of `passes`
+        passes after it (an array)."""
         a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.complex128)
         b = None if load1 is None else np.ascontiguousarray(load1, dtype=np.complex128)
-        t0, t1 = _ct.c_double(), _ct.c_double()
+        t0 = _ct.c_double()
+        each = np.zeros(max(passes, 1))
         st = self.L.oracle_v3d_sample(self.h, self.state, dt, None if a is None else a.ctypes.data,
-                                      None if b is None else b.ctypes.data, passes, _ct.byref(t0), _ct.byref(t1))
+                                      None if b is None else b.ctypes.data, passes, _ct.byref(t0), ptr(each))
         assert st == 0
-        return t0.value, t1.value
+        return t0.value, each[:passes]
 
     def residual_history(self):
         n = self.L.oracle_v3d_residual_history(self.h, None, 0)
