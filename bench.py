@@ -223,14 +223,16 @@ def build_operator(device, precision, emulation=None):
     return op, full, dt
 
 
-def gpu_arm(args, rank, world, device, precision, emulation=None, e2e=True):
-    """Steps W .. W + K - 1 of the workload, twice from the same start: timed
-    with the loads resident in device memory (CUDA events on the operator's
-    stream; each step's surface U and phi copied into device buffers,
-    stream-ordered, for the error comparison), then -- the state rebuilt by
-    the same W warm-up steps -- end to end through the C ABI with the loads
-    copied from pinned host memory and U and phi read back every step (host
-    wall clock)."""
+def gpu_arm(args, rank, world, device, precision, emulation=None, e2e=True, profile_apart=True):
+    """Steps W .. W + K - 1 of the workload, from the same warmed start each
+    time: timed with the loads resident in device memory (CUDA events on the
+    operator's stream; each step's surface U and phi copied into device
+    buffers, stream-ordered, for the error comparison); with profile_apart,
+    once more with the per-kernel timing events on, for the breakdown (else
+    the timed run carries them); then end to end through the C ABI with the
+    loads copied from pinned host memory and U and phi read back every step
+    (host wall clock). The state is rebuilt by the same W warm-up steps
+    before each run."""
     import torch
 
     from sl3dpp_gb300._lib import lib
@@ -252,7 +254,7 @@ def gpu_arm(args, rank, world, device, precision, emulation=None, e2e=True):
     state = warm_state()
     stream = torch.cuda.ExternalStream(op.stream, device=device)
     lib().sl3dgpu_profile_reset()
-    lib().sl3dgpu_profile_enable(1)
+    lib().sl3dgpu_profile_enable(0 if profile_apart else 1)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -277,10 +279,22 @@ def gpu_arm(args, rank, world, device, precision, emulation=None, e2e=True):
     history = {"fp64_pass_residuals": [float(f"{v:.3e}") for v in op.residual_history()],
                "correction_passes": int(op.correction_history().size)}
     lib().sl3dgpu_profile_enable(0)
-    prof = profile_read()
     ms = start.elapsed_time(stop)
     surfaces = surfaces_dev.cpu().numpy()
     del state
+    if profile_apart:
+        # the per-kind breakdown from the same steps run again with the
+        # kernel timing events on (they cost a few per cent of a step)
+        state = warm_state()
+        lib().sl3dgpu_profile_reset()
+        lib().sl3dgpu_profile_enable(1)
+        for k in range(args.steps):
+            n = args.warmup + k
+            op.StepDevice(state, dt, "sdirk2", loads[n], loads[n + 1])
+        torch.cuda.synchronize()
+        lib().sl3dgpu_profile_enable(0)
+        del state
+    prof = profile_read()
     e2e_s = float("nan")
     if e2e:
         host_loads = [l.cpu().pin_memory().numpy() for l in loads]
@@ -408,6 +422,58 @@ def config1_cpu_run():
             "cores": O.load().oracle_threads(), "kind": "port", "extrapolated": False}
 
 
+# -- the Legendre contraction alone -------------------------------------------------------------
+
+def legendre_case(args, device):
+    """The mixed form's correction contraction alone at the workload's size:
+    the 3xTF32 tensor-core Legendre analysis and synthesis of spin -2 over
+    the 55 lateral nodes of the lmax-256 grid (FP32 device buffers, random
+    values), timed with CUDA events -- the case a single-kernel profile of
+    TcGemmKernel runs (a few hundred MB on the device)."""
+    import ctypes
+
+    import torch
+
+    from sl3dpp_gb300._lib import lib
+    from sl3dpp_gb300.grid import SurfaceGrid
+
+    count, N = 55, -2
+    g = SurfaceGrid(LMAX, 2, 1.5)
+    rows = (LMAX + 1) ** 2 - N * N
+    gen = torch.Generator(device=device).manual_seed(5)
+    coeffs = torch.randn(rows * count * 2, dtype=torch.float32, device=device, generator=gen)
+    spectra = torch.randn((2 * LMAX + 1) * g.ntheta * count * 2, dtype=torch.float32, device=device, generator=gen)
+    out_c = torch.empty_like(coeffs)
+    out_s = torch.empty_like(spectra)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def once():
+        lib().sl3dgpu_legendre_device(g._handle, N, 0, 1, 1, ctypes.c_void_p(spectra.data_ptr()), count,
+                                      ctypes.c_void_p(out_c.data_ptr()), ctypes.c_void_p(stream))
+        lib().sl3dgpu_legendre_device(g._handle, N, 0, 0, 1, ctypes.c_void_p(coeffs.data_ptr()), count,
+                                      ctypes.c_void_p(out_s.data_ptr()), ctypes.c_void_p(stream))
+
+    for _ in range(args.warmup):
+        once()
+    torch.cuda.synchronize()
+    lib().sl3dgpu_profile_reset()
+    lib().sl3dgpu_profile_enable(1)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        once()
+    stop.record()
+    stop.synchronize()
+    lib().sl3dgpu_profile_enable(0)
+    prof = profile_read()["legendre_f32"]
+    ms = start.elapsed_time(stop)
+    flops = prof["flops"] / max(prof["launches"], 1)
+    per_launch = prof["ms"] / max(prof["launches"], 1)
+    return {"case": f"legendre_f32 spin -2, lmax {LMAX}, {count} nodes, analysis + synthesis",
+            "ms_per_pair": ms / args.steps, "launches": prof["launches"], "ms_per_launch": per_launch,
+            "algorithmic_tflops": flops / (per_launch / 1e3) / 1e12 if per_launch > 0 else None}
+
+
 # -- main ------------------------------------------------------------------------------------------
 
 def main():
@@ -423,6 +489,8 @@ def main():
     ap.add_argument("--lmax", type=int, default=LMAX, help="a smaller workload for development runs")
     ap.add_argument("--correction-rtol", type=float, default=CORRECTION_RTOL)
     ap.add_argument("--correction-memory", type=int, default=CORRECTION_MEMORY)
+    ap.add_argument("--legendre-case", action="store_true",
+                    help="instead: the FP32 tensor-core Legendre contraction alone at the workload's lmax")
     args = ap.parse_args()
     if args.lmax != LMAX:
         _rescale(args.lmax)
@@ -474,6 +542,10 @@ def main():
     from sl3dpp_gb300._lib import lib
     import ctypes
 
+    if args.legendre_case:
+        if rank == 0:
+            print(json.dumps(legendre_case(args, device)), flush=True)
+        return
     fp64, fp32 = ctypes.c_double(), ctypes.c_double()
     lib().sl3dgpu_fp64_fma_peak(ctypes.byref(fp64))
     lib().sl3dgpu_fp32_fma_peak(ctypes.byref(fp32))
@@ -494,7 +566,8 @@ def main():
             "last_step": r["history"],
             "converged_steps": sum(int(i.converged) for i in r["infos"]),
             "timing": ("value: steps W .. W + K - 1 with device-resident loads, CUDA events on the operator's "
-                       "stream; e2e: the same steps from the same warmed state, host loads and surface read-back"),
+                       "stream, kernel timing events off; kernel_ms: the same steps again with them on; e2e: the "
+                       "same steps from the same warmed state, host loads and surface read-back"),
             "final_residual": r["infos"][-1].residual,
             "roofline": roofline(r["profile"], fp64.value, fp32.value),
             "kernel_ms": {k: round(v["ms"], 3) for k, v in r["profile"].items() if v["launches"]},
@@ -512,7 +585,8 @@ def main():
         # the plain FP64 form as the reference computes it (the FP64 units),
         # and with its Legendre contractions emulated on the tensor cores
         for name, emulation in (("fp64_gpu", 0), ("fp64_gpu_tc_emulated", 1)):
-            rr = gpu_arm(args, rank, world, device, "fp64", emulation=emulation, e2e=False)
+            # timed with the kernel events on: a few ms of a 2-5 s step
+            rr = gpu_arm(args, rank, world, device, "fp64", emulation=emulation, e2e=False, profile_apart=False)
             errs = [(rel_err(m[0], f[0]), rel_err(m[1], f[1])) for m, f in zip(mixed_surfaces, rr["surfaces"])]
             arms[name] = rr
             line[name] = {"value": steps_total / rr["seconds"], "unit": "steps/s",

@@ -8,9 +8,10 @@
   and modulus ratio 0.5, delta to degree 32 at RMS 1.0): the first three
   passes of a backward Euler stage, pass for pass.
 - lmax 256 (120 elements of order 5, Maxwell, delta to degree 64 at RMS 1.0,
-  the benchmark's workload): the first two passes of the benchmark's first
-  Sdirk2 stage, pass for pass, FP64 form; and the mixed form's converged
-  stage against the FP64 form's at the mixed form's bar, 1e-8.
+  the benchmark's workload): the first two passes of a backward Euler stage
+  of the benchmark's first-stage length, pass for pass, FP64 form; and the
+  benchmark's first Sdirk2 step in the mixed form against the FP64 form at
+  the mixed form's bar, 1e-8.
 
 A stage cut at a pass budget returns unconverged with its last iterate on
 both sides, so the comparison covers the stage start, the passes and the
@@ -90,15 +91,17 @@ def test_gpu_lmax256_mixed_stage_meets_its_bar_against_fp64(gpu):
     o = O.OracleStep(O.standard_earth(120), O.default_options(lmax, 6))  # the grid and delta samples only
     d = delta_for(o, lmax, 64, 1.0, 1)
     full = cap_load(lmax, o.sigma_scale, 2000.0)
-    h = GAMMA * 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
     out = []
     for mixed in (0, 1):
         g = Viscoelastic3D(standard_earth(120), Options.defaults(
-            lmax, 6, rtol=1e-10, max_iterations=60, precision=mixed, correction_rtol=3e-6, correction_memory=10,
+            lmax, 6, rtol=1e-10, max_iterations=150, precision=mixed, correction_rtol=3e-6, correction_memory=10,
             fp64_emulation=mixed))
         g.set_delta(d)
-        info = g.Step(g.ZeroState(), h, 1, 0.5 * full, 0.6 * full)
-        assert info.converged
+        # the benchmark's first step: from rest the plain FP64 fixed point takes
+        # about 60 passes a stage (residual ratio ~0.7 a pass) to reach 1e-10
+        info = g.Step(g.ZeroState(), dt, 2, 0.0 * full, 0.1 * full)
+        assert info.converged, (mixed, info.iterations, info.residual, g.residual_history())
         out.append((g.Surface(0), g.Surface(2)))
         del g
     (U64, P64), (U32, P32) = out
