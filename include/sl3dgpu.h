@@ -395,6 +395,58 @@ int sl3dgpu_v3d_surface(sl3dgpu_v3d* op, int component, double* out);
  * stream (sl3dgpu_v3d_stream) with no host wait: a driver collecting every
  * step's surface keeps the steps back to back. */
 int sl3dgpu_v3d_surface_device(sl3dgpu_v3d* op, int component, double* device_out);
+/* The memory nodes [first, end) where the lateral weight may be non-zero
+ * (whole elements; empty until delta is set): Analyse(W d) vanishes
+ * outside, so only these nodes' strain enters the next pass. */
+int sl3dgpu_v3d_lateral_range(const sl3dgpu_v3d* op, int* first, int* end);
+/* Per memory node, the slowest Prony branch's reference inverse relaxation
+ * time (model units): PointItau of the radial reference (Viscoelastic.hpp:
+ * 367-372). */
+int sl3dgpu_v3d_node_relaxation(const sl3dgpu_v3d* op, double* itau);
+
+/* ---- the learned warm start (Converge's start, Viscoelastic3D.hpp:562-569) ----
+ * No counterpart in the reference, which starts each step from the previous
+ * step's strain. A network (16 features -> `depth` hidden layers of `hidden`
+ * GELU units -> 16 outputs; BF16 tensor-core products, FP32 masters and
+ * accumulation) predicts, per degree, lateral memory node and spin block, the
+ * coefficients (a, b, c) of Delta_n+1 = a Delta_n + b Delta_n-1 +
+ * c Delta_n-2 from statistics of the last three strain changes over the
+ * block's orders; the guess for sl3dgpu_v3d_set_start is s_n + Delta_n+1 at
+ * the lateral nodes and s_n + Delta_n elsewhere. Trained on the GPU on pairs
+ * the plain iteration produced; the step takes a guess only when its first
+ * residual beats the plain start's. */
+typedef struct sl3dgpu_wsnet sl3dgpu_wsnet;
+int sl3dgpu_wsnet_create(int hidden, int depth, unsigned long long seed, sl3dgpu_wsnet** out);
+void sl3dgpu_wsnet_destroy(sl3dgpu_wsnet* net);
+long long sl3dgpu_wsnet_parameter_count(const sl3dgpu_wsnet* net);
+/* The FP32 master parameters (per layer: weights out x in row-major, then biases). */
+int sl3dgpu_wsnet_parameters(const sl3dgpu_wsnet* net, float* out);
+int sl3dgpu_wsnet_set_parameters(sl3dgpu_wsnet* net, const float* in);
+/* The operator layout the network reads: lmax, the lateral node count and
+ * per lateral node its depth fraction in the lateral zone and log10(dt itau) / 4. */
+int sl3dgpu_wsnet_bind(sl3dgpu_wsnet* net, int lmax, int lateral, const double* depth, const double* relax);
+/* A batch of training pairs: per pair device pointers to the changes
+ * Delta_n-2, Delta_n-1, Delta_n and the target Delta_n+1 as compact lateral
+ * columns ([row][lateral] FP32 complex, rows in the bound layout's order),
+ * host arrays of the load ratios and of the normalisers (the extrapolation's
+ * squared error of each pair). The loss is the pairs' mean squared error of
+ * the predicted change over the extrapolation's. gradient: the loss and the
+ * FP32 gradient (grad may be NULL); train_step: one Adam step at rate lr. */
+int sl3dgpu_wsnet_gradient(sl3dgpu_wsnet* net, int pairs, const void* const* d2, const void* const* d1,
+                           const void* const* d0, const void* const* target, const float* ratio,
+                           const float* norm, float* grad, float* loss);
+int sl3dgpu_wsnet_train_step(sl3dgpu_wsnet* net, int pairs, const void* const* d2, const void* const* d1,
+                             const void* const* d0, const void* const* target, const float* ratio,
+                             const float* norm, float lr, float* loss);
+/* The guess of the next step's end strain from the last four snapshots of a
+ * state's strain coefficients (device layout of sl3dgpu_v3d_state_coefficients,
+ * P nodes), the lateral range's first node, and the load ratio; ordered on
+ * `stream` (device pointers). */
+int sl3dgpu_wsnet_predict(sl3dgpu_wsnet* net, int P, int lateral_first, const double* s_n, const double* s_nm1,
+                          const double* s_nm2, const double* s_nm3, double ratio, double* guess, void* stream);
+/* The network's tensor-core product alone: C = A B^T, FP32 row-major A (M x K),
+ * B (N x K), C (M x N), device pointers, operands rounded to BF16, FP32 sums. */
+int sl3dgpu_wsnet_gemm(sl3dgpu_wsnet* net, const float* A, const float* B, int M, int N, int K, float* C);
 /* Viscoelastic3D::InertiaMoment (Viscoelastic3D.cpp:2032-2048) of the last
  * step's solutions: sqrt(4 pi) int rho U r^3 dr of their degree-0 radial
  * displacement (the degree-0 moment row of detail/ViscoelasticDegree.hpp:
@@ -427,6 +479,10 @@ int sl3dgpu_v3d_state_coefficients(const sl3dgpu_v3d* op, const sl3dgpu_v3d_stat
                                    long long* count);
 /* The same coefficients copied to a host array (count doubles). */
 int sl3dgpu_v3d_state_coefficients_host(const sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, double* out);
+/* The same coefficients copied into a caller's device buffer (device
+ * layout, 2 x count doubles), ordered on the operator's stream, which it
+ * waits for. */
+int sl3dgpu_v3d_state_coefficients_copy(const sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, double* device_out);
 /* Evolution3D::Run (src/Evolution3D.cpp:184-394) for a body without an ocean
  * and without rotational feedback (GRDSolver::NoOceanState): node 0 the
  * instantaneous elastic response to loads[0] (a dt = 0 step), then one step

@@ -2011,6 +2011,30 @@ extern "C" int sl3dgpu_v3d_nodes(const sl3dgpu_v3d* h, double* radius, int* elem
   return SL3DGPU_OK;
 }
 
+extern "C" int sl3dgpu_v3d_lateral_range(const sl3dgpu_v3d* h, int* first, int* end) {
+  if (h == nullptr || first == nullptr || end == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  *first = h->op.lateralFirst;
+  *end = h->op.lateralEnd;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_node_relaxation(const sl3dgpu_v3d* h, double* itau) {
+  if (h == nullptr || itau == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  // the slowest branch's reference inverse relaxation time at each node
+  const auto& ref = *h->op.reference;
+  for (int p = 0; p < h->op.P; ++p) {
+    const size_t at = static_cast<size_t>(h->op.nodeElement[p]) * ref.points.count + h->op.nodeQ[p];
+    itau[p] = ref.pointItau.empty() ? 0.0 : ref.pointItau[0][at];
+  }
+  return SL3DGPU_OK;
+}
+
 extern "C" int sl3dgpu_v3d_colatitudes(const sl3dgpu_v3d* h, double* theta, double* weights) {
   if (h == nullptr) {
     SetError("v3d: null handle");
@@ -2101,6 +2125,18 @@ extern "C" int sl3dgpu_v3d_state_coefficients(const sl3dgpu_v3d* h, const sl3dgp
   }
   if (device) *device = state->st.hasCoeffs ? reinterpret_cast<const double*>(state->st.coeffs.p) : nullptr;
   if (count) *count = 2 * h->op.spectralComplex;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_state_coefficients_copy(const sl3dgpu_v3d* h, const sl3dgpu_v3d_state* state,
+                                                   double* device_out) {
+  if (h == nullptr || state == nullptr || device_out == nullptr || !state->st.hasCoeffs) {
+    SetError("v3d: null argument or a state without strain coefficients");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SL3D_CUDA(cudaMemcpyAsync(device_out, state->st.coeffs.p, h->op.spectralComplex * sizeof(double2),
+                            cudaMemcpyDeviceToDevice, h->op.stream));
+  SL3D_CUDA(cudaStreamSynchronize(h->op.stream));
   return SL3DGPU_OK;
 }
 
