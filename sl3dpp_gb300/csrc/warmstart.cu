@@ -511,21 +511,28 @@ namespace {
 
 int EnsureCapacity(sl3dgpu_wsnet& n, int units) {
   if (units <= n.capacity) return SL3DGPU_OK;
-  const int cap = std::max(units, 2 * n.capacity);
+  size_t widest = kFeatures;
+  for (int i = 0; i < n.Layers(); ++i) widest = std::max<size_t>(widest, n.out[i]);
+  // at least the widest layer, so that the packed weights (widest x widest)
+  // fit the operand buffers whatever the batch
+  const int cap = std::max({units, 2 * n.capacity, static_cast<int>(widest)});
   n.Z.resize(n.Layers());
   n.H.resize(n.Layers() + 1);
   SL3D_CUDA(n.H[0].Alloc(static_cast<size_t>(cap) * kFeatures));
-  size_t widest = kFeatures;
   for (int i = 0; i < n.Layers(); ++i) {
     SL3D_CUDA(n.Z[i].Alloc(static_cast<size_t>(cap) * n.out[i]));
     SL3D_CUDA(n.H[i + 1].Alloc(static_cast<size_t>(cap) * n.out[i]));
-    widest = std::max<size_t>(widest, n.out[i]);
   }
   SL3D_CUDA(n.dA.Alloc(static_cast<size_t>(cap) * widest));
   SL3D_CUDA(n.dB.Alloc(static_cast<size_t>(cap) * widest));
-  const size_t pad = static_cast<size_t>(cap + kTcTileM) * (widest + kTcTileK);
-  SL3D_CUDA(n.packA.Alloc(pad + static_cast<size_t>(widest + kTcTileM) * (cap + kTcTileK)));
-  SL3D_CUDA(n.packB.Alloc(pad + static_cast<size_t>(widest + kNetTileN) * (cap + kTcTileK)));
+  // A packs at most (cap + 127) x (widest + 15) values (a batch's rows by a
+  // layer's width) or (widest + 127) x (cap + 15) (a weight gradient's),
+  // B likewise with 64-row tiles; the weights themselves, (widest + 127) x
+  // (widest + 15), fit the first form since cap >= widest
+  SL3D_CUDA(n.packA.Alloc(static_cast<size_t>(cap + kTcTileM) * (widest + kTcTileK) +
+                          static_cast<size_t>(widest + kTcTileM) * (cap + kTcTileK)));
+  SL3D_CUDA(n.packB.Alloc(static_cast<size_t>(cap + kNetTileN) * (widest + kTcTileK) +
+                          static_cast<size_t>(widest + kNetTileN) * (cap + kTcTileK)));
   n.capacity = cap;
   n.widest = static_cast<int>(widest);
   return SL3DGPU_OK;
@@ -562,7 +569,11 @@ int Gemm(sl3dgpu_wsnet& n, const float* A, long long aR, long long aK, const flo
   g.C = C;
   g.ldc = ldc;
   g.accumulate = accumulate ? 1 : 0;
-  constexpr size_t smem = kNetStages * (kATileNet + kBTileNet) * sizeof(uint16_t) + (2 * kNetStages + 1) * 8 + 16;
+  // the stages need 12 KB; asking 29 KB keeps at most seven CTAs on an SM,
+  // whose 64 tensor-memory columns each then never exceed the SM's 512
+  constexpr size_t smem = 29 * 1024;
+  static_assert(kNetStages * (kATileNet + kBTileNet) * sizeof(uint16_t) + (2 * kNetStages + 1) * 8 + 16 <= smem,
+                "the stages fit");
   prof::Scope scope(prof::kOther, n.stream);
   NetGemmKernel<<<dim3(g.nTiles, g.mTiles), kNetThreads, smem, n.stream>>>(g, n.error.p);
   SL3D_CHECK_LAUNCH();

@@ -211,6 +211,9 @@ class LearnedStart:
             return False
         ratio = load_ratio(self.loads[-2], self.loads[-1], next_load)
         s3, s2, s1, s0 = self.snapshots
+        L = self.op.lmax
+        rows = 2 * (L + 1) ** 2 - 5 + (L + 1) * (L + 2) // 2  # spin -2, -1 and real spin 0 rows
+        assert all(s.numel() == rows * self.op.node_count for s in self.snapshots)
         guess = torch.empty_like(s0)
         check(lib().sl3dgpu_wsnet_predict(self.net._h, self.op.node_count, self.p0, s0.data_ptr(), s1.data_ptr(),
                                           s2.data_ptr(), s3.data_ptr(), ratio, guess.data_ptr(), self.op.stream))
@@ -279,15 +282,17 @@ def pairs_of(run):
 
 
 def train(net: WarmStartNet, pairs, epochs: int, batch: int = 16, lr: float = 3e-4, seed: int = 0,
-          log=None) -> list[float]:
-    """Adam over shuffled batches; returns each epoch's mean loss."""
+          log=None, decay: bool = False) -> list[float]:
+    """Adam over shuffled batches (the rate cosine-decayed to a tenth over
+    the epochs with decay); returns each epoch's mean loss."""
     rng = np.random.default_rng(seed)
     history = []
     for epoch in range(epochs):
         order = rng.permutation(len(pairs))
         losses = []
+        rate = lr * (0.55 + 0.45 * np.cos(np.pi * epoch / max(epochs - 1, 1))) if decay else lr
         for k in range(0, len(order) - batch + 1, batch):
-            losses.append(net.train_step([pairs[i] for i in order[k:k + batch]], lr))
+            losses.append(net.train_step([pairs[i] for i in order[k:k + batch]], rate))
         history.append(float(np.mean(losses)))
         if log:
             log(f"epoch {epoch}: loss {history[-1]:.4f}")
@@ -363,6 +368,7 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--decay", action="store_true", help="cosine-decay the rate to a tenth over the epochs")
     args = ap.parse_args(argv)
     rng = np.random.default_rng(args.seed)
     t0 = time.time()
@@ -378,7 +384,7 @@ def main(argv=None):
     net.bind(32, *layout)
     torch.cuda.synchronize()
     t1 = time.time()
-    history = train(net, pairs, args.epochs, args.batch, args.lr, args.seed, log=print)
+    history = train(net, pairs, args.epochs, args.batch, args.lr, args.seed, log=print, decay=args.decay)
     net.save(args.out)
     print(json.dumps({"pairs": len(pairs), "runs": args.runs, "generation_s": gen_s,
                       "training_s": time.time() - t1, "loss_first_epoch": history[0], "loss_last_epoch": history[-1],
