@@ -474,6 +474,39 @@ def legendre_case(args, device):
             "algorithmic_tflops": flops / (per_launch / 1e3) / 1e12 if per_launch > 0 else None}
 
 
+# -- the learned warm start ----------------------------------------------------------------------
+
+def warmstart_case(args):
+    """Config 5, bounded: held-out delta fields (degree 32, RMS 1.0; seeds
+    outside the training runs') at lmax 128 (80 elements of order 5), 16
+    Sdirk2 steps each, with and without the committed network -- the plain
+    FP64 form against its own start (the previous step's strain), the mixed
+    form against its extrapolated start; passes a step, steps/s (host wall
+    clock, synchronised each step) and the largest relative difference of
+    the surface U between the two runs."""
+    from sl3dpp_gb300 import warmstart as W
+
+    net = W.WarmStartNet.load(W.default_weights())
+    out = {"case": "learned warm start, lmax 128, 80 elements of order 5, delta degree 32 RMS 1.0, 16 Sdirk2 "
+                   "steps of 500 yr, held-out seeds 90001-90002",
+           "parameters": net.parameter_count, "forms": {}}
+    for name, precision in (("fp64", 0), ("mixed", 1)):
+        rows = []
+        for seed in (90_001, 90_002):
+            kw = dict(seed=seed, steps=16, lmax=128, elements=80, ngll=6, rms=1.0, ldelta=32, precision=precision)
+            plain, learned = W.evaluate(None, **kw), W.evaluate(net, **kw)
+            err = max(float(np.max(np.abs(a - b)) / np.max(np.abs(b))) for a, b in zip(learned["U"], plain["U"]))
+            work = (lambda r: [p + c for p, c in zip(r["passes"], r["corrections"])])
+            rows.append({"seed": seed, "passes_plain": plain["passes"], "passes_learned": learned["passes"],
+                         "correction_passes_plain": plain["corrections"],
+                         "correction_passes_learned": learned["corrections"], "taken": sum(learned["taken"]),
+                         "steps_per_s_plain": 16 / plain["seconds"], "steps_per_s_learned": 16 / learned["seconds"],
+                         "total_passes_plain": sum(work(plain)), "total_passes_learned": sum(work(learned)),
+                         "max_rel_diff_U": err})
+        out["forms"][name] = rows
+    return out
+
+
 # -- main ------------------------------------------------------------------------------------------
 
 def main():
@@ -489,6 +522,8 @@ def main():
     ap.add_argument("--lmax", type=int, default=LMAX, help="a smaller workload for development runs")
     ap.add_argument("--correction-rtol", type=float, default=CORRECTION_RTOL)
     ap.add_argument("--correction-memory", type=int, default=CORRECTION_MEMORY)
+    ap.add_argument("--warmstart-case", action="store_true",
+                    help="instead: the learned warm start against the plain starts on held-out fields at lmax 128")
     ap.add_argument("--legendre-case", action="store_true",
                     help="instead: the FP32 tensor-core Legendre contraction alone at the workload's lmax")
     args = ap.parse_args()
@@ -542,6 +577,10 @@ def main():
     from sl3dpp_gb300._lib import lib
     import ctypes
 
+    if args.warmstart_case:
+        if rank == 0:
+            print(json.dumps(warmstart_case(args)), flush=True)
+        return
     if args.legendre_case:
         if rank == 0:
             print(json.dumps(legendre_case(args, device)), flush=True)
