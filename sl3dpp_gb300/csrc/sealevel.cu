@@ -218,8 +218,7 @@ struct LoadMixer {
   bool first = true;
   std::vector<Dev<double>> dG, dF;
   Dev<double*> dGPtr, dFPtr;
-  Dev<double> xPrev, fPrev, partial, sums, gamma;
-  std::vector<double> gram, hostSums;
+  Dev<double> xPrev, fPrev, partial, sums, gamma, gram;  // the Gram matrix on the device
 
   int Init(int m, long long n) {
     memory = m;
@@ -240,8 +239,8 @@ struct LoadMixer {
     SL3D_CUDA(partial.Alloc(static_cast<size_t>(1024) * 2 * kMixMaxMemory));
     SL3D_CUDA(sums.Alloc(2 * kMixMaxMemory));
     SL3D_CUDA(gamma.Alloc(kMixMaxMemory + 1));
-    gram.assign(static_cast<size_t>(memory) * memory, 0.0);
-    hostSums.assign(4 * kMixMaxMemory, 0.0);
+    SL3D_CUDA(gram.Alloc(static_cast<size_t>(memory) * memory));
+    SL3D_CUDA(ZeroIn(gram.p, static_cast<size_t>(memory) * memory * sizeof(double)));
     return SL3DGPU_OK;
   }
 
@@ -273,12 +272,8 @@ struct LoadMixer {
     a.m = std::min(count + 1, memory);
     LaunchMixerSweep(a, sums.p, stream);
     SL3D_CHECK_LAUNCH();
-    SL3D_CUDA(cudaMemcpyAsync(hostSums.data(), sums.p, 2 * kMixMaxMemory * sizeof(double), cudaMemcpyDeviceToHost,
-                              stream));
-    SL3D_CUDA(cudaStreamSynchronize(stream));
-    double* g = hostSums.data() + 2 * kMixMaxMemory;
-    MixerSolve(gram.data(), a.m, a.slot, a.memory, hostSums.data(), g);
-    SL3D_CUDA(cudaMemcpyAsync(gamma.p, g, (a.m + 1) * sizeof(double), cudaMemcpyHostToDevice, stream));
+    LaunchMixerGram(gram.p, a.m, a.slot, a.memory, sums.p, gamma.p, stream);  // one FP64 warp, no host round trip
+    SL3D_CHECK_LAUNCH();
     LaunchMixerMix(a, stream);
     SL3D_CHECK_LAUNCH();
     count = a.m;

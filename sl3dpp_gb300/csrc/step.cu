@@ -132,9 +132,10 @@ class Viscoelastic3DGpu {
   Dev<double> xPrev, fPrev, gammaOut, mixPartial, mixSums;
   // the Anderson least squares runs on the host: each mixer's Gram matrix,
   // and pinned room for an update's sums (16) and gamma (9)
-  std::vector<double> gram64, gram32;
+  // the mixers' Gram matrices (memory x memory), on the device
+  Dev<double> gram64, gram32;
   double* hostMix = nullptr;
-  int MixerHostSolve(std::vector<double>& gram, int m, int slot, int memory);
+  int MixerDeviceSolve(Dev<double>& gram, int m, int slot, int memory);
   std::vector<Dev<double>> dG, dF;
   Dev<double*> dGPtr, dFPtr;
   static constexpr int kMixBlocks = 1024;
@@ -872,7 +873,8 @@ int Viscoelastic3DGpu::MixerReset() {
     SL3D_CUDA(fPrev.Alloc(n));
     mixerMemory = memory;
   }
-  gram64.assign(static_cast<size_t>(memory) * memory, 0.0);
+  if (gram64.n < static_cast<size_t>(memory) * memory) SL3D_CUDA(gram64.Alloc(static_cast<size_t>(memory) * memory));
+  SL3D_CUDA(cudaMemsetAsync(gram64.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
   return SL3DGPU_OK;
 }
 
@@ -899,7 +901,7 @@ int Viscoelastic3DGpu::MixerUpdate(int& count, int& slot, bool& first) {
   a.m = std::min(count + 1, a.memory);
   LaunchMixerSweep(a, mixSums.p, stream);
   SL3D_CHECK_LAUNCH();
-  SL3D_TRY(MixerHostSolve(gram64, a.m, a.slot, a.memory));
+  SL3D_TRY(MixerDeviceSolve(gram64, a.m, a.slot, a.memory));
   LaunchMixerMix(a, stream);
   SL3D_CHECK_LAUNCH();
   count = a.m;
@@ -1342,21 +1344,17 @@ int Viscoelastic3DGpu::Mixer32Reset() {
     mixer32Memory = memory;
     mixer32Size = n;
   }
-  gram32.assign(static_cast<size_t>(memory) * memory, 0.0);
+  if (gram32.n < static_cast<size_t>(memory) * memory) SL3D_CUDA(gram32.Alloc(static_cast<size_t>(memory) * memory));
+  SL3D_CUDA(cudaMemsetAsync(gram32.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), stream));
   return SL3DGPU_OK;
 }
 
-// An update's least squares on the host: the sweep's sums back (the stream
-// synchronised), the Gram column and gamma by MixerSolve, gamma to the device
-// for the mix (the pinned copy is not touched again before the next update,
-// which follows a synchronisation).
-int Viscoelastic3DGpu::MixerHostSolve(std::vector<double>& gram, int m, int slot, int memory) {
-  SL3D_CUDA(cudaMemcpyAsync(hostMix, mixSums.p, 2 * kMixMaxMemory * sizeof(double), cudaMemcpyDeviceToHost,
-                            stream));
-  SL3D_CUDA(cudaStreamSynchronize(stream));
-  double* gamma = hostMix + 2 * kMixMaxMemory;
-  MixerSolve(gram.data(), m, slot, memory, hostMix, gamma);
-  SL3D_CUDA(cudaMemcpyAsync(gammaOut.p, gamma, (m + 1) * sizeof(double), cudaMemcpyHostToDevice, stream));
+// An update's least squares on the device: the sweep's sums, the Gram
+// column and gamma by one FP64 warp (LaunchMixerGram), ordered on the
+// stream before the mix -- no host round trip.
+int Viscoelastic3DGpu::MixerDeviceSolve(Dev<double>& gram, int m, int slot, int memory) {
+  LaunchMixerGram(gram.p, m, slot, memory, mixSums.p, gammaOut.p, stream);
+  SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
 
@@ -1383,7 +1381,7 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
   a.m = std::min(count + 1, a.memory);
   LaunchMixerSweep(a, mixSums.p, stream);
   SL3D_CHECK_LAUNCH();
-  SL3D_TRY(MixerHostSolve(gram32, a.m, a.slot, a.memory));
+  SL3D_TRY(MixerDeviceSolve(gram32, a.m, a.slot, a.memory));
   LaunchMixerMix(a, stream);
   SL3D_CHECK_LAUNCH();
   count = a.m;

@@ -1373,6 +1373,127 @@ std::vector<double> NodeCoefficients(int P, int ngll, const std::vector<int>& no
 }  // namespace sl3dgpu
 
 namespace sl3dgpu {
+namespace {
+
+// The Anderson update's least squares on the device, one FP64 warp: the
+// Gram matrix's slot column and row from the sweep's sums, then gamma =
+// argmin |G gamma - b| by the cyclic Jacobi eigen-decomposition of the
+// symmetric G with eigenvalues at or below machine epsilon times the largest
+// dropped -- the minimum-norm solution of LAPACK's dgelss with rcond < 0,
+// the reference's call (include/sl3dpp/detail/AndersonMixer.hpp:186-211).
+// The same arithmetic, in the same order, as SymmetricLstsq (host/
+// lstsq.hpp): each rotation's angle on lane 0, its column, row and
+// eigenvector updates one lane per index; every sum in the host's order.
+__global__ void __launch_bounds__(32) MixerGramKernel(double* gram, int m, int slot, int memory,
+                                                      const double* sums, double* gamma) {
+  constexpr int M = kMixMaxMemory;
+  __shared__ double a[M][M + 1], v[M][M + 1];
+  __shared__ double rot[2];
+  __shared__ int flag;
+  const int lane = threadIdx.x;
+  if (lane < m) {
+    gram[slot * memory + lane] = sums[lane];
+    gram[lane * memory + slot] = sums[lane];
+  }
+  __syncwarp();
+  __threadfence_block();
+  for (int j = 0; j < m; ++j)
+    if (lane < m) {
+      a[lane][j] = 0.5 * (gram[lane * memory + j] + gram[j * memory + lane]);
+      v[lane][j] = lane == j ? 1.0 : 0.0;
+    }
+  __syncwarp();
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    if (lane == 0) {
+      double off = 0.0, diag = 0.0;
+      for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) (i == j ? diag : off) += a[i][j] * a[i][j];
+      flag = (off <= 1e-32 * diag || off == 0.0) ? 1 : 0;
+    }
+    __syncwarp();
+    if (flag) break;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        if (lane == 0) {
+          if (a[p][q] == 0.0) {
+            rot[0] = 0.0;
+            flag = 1;
+          } else {
+            const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+            const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            const double c = 1.0 / sqrt(t * t + 1.0);
+            rot[0] = c;
+            rot[1] = t * c;
+            flag = 0;
+          }
+        }
+        __syncwarp();
+        if (flag) {  // a[p][q] vanishes: no rotation
+          __syncwarp();
+          continue;
+        }
+        const double c = rot[0], sn = rot[1];
+        if (lane < m) {
+          const double akp = a[lane][p], akq = a[lane][q];
+          a[lane][p] = c * akp - sn * akq;
+          a[lane][q] = sn * akp + c * akq;
+        }
+        __syncwarp();
+        if (lane < m) {
+          const double apk = a[p][lane], aqk = a[q][lane];
+          a[p][lane] = c * apk - sn * aqk;
+          a[q][lane] = sn * apk + c * aqk;
+          const double vkp = v[lane][p], vkq = v[lane][q];
+          v[lane][p] = c * vkp - sn * vkq;
+          v[lane][q] = sn * vkp + c * vkq;
+        }
+        __syncwarp();
+      }
+    if (lane == 0) flag = 0;
+    __syncwarp();
+  }
+  // the solve: projections of b on the kept eigenvectors
+  __shared__ double proj[M], y[M];
+  __shared__ double cut;
+  if (lane == 0) {
+    double largest = 0.0;
+    for (int i = 0; i < m; ++i) largest = fmax(largest, fabs(a[i][i]));
+    cut = 2.220446049250313e-16 * largest;
+  }
+  __syncwarp();
+  const double* b = sums + kMixMaxMemory;
+  if (lane < m) {
+    double pr = 0.0;
+    for (int i = 0; i < m; ++i) pr += v[i][lane] * b[i];
+    proj[lane] = pr;
+  }
+  __syncwarp();
+  if (lane < m) {
+    double yi = 0.0;
+    for (int k = 0; k < m; ++k) {
+      const double lambda = a[k][k];
+      if (!(fabs(lambda) > cut)) continue;
+      yi += v[lane][k] * proj[k] / lambda;
+    }
+    y[lane] = yi;
+    gamma[lane] = yi;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    bool finite = true;
+    for (int i = 0; i < m; ++i)
+      if (!(y[i] - y[i] == 0.0)) finite = false;
+    gamma[m] = finite ? 1.0 : 0.0;
+  }
+}
+
+}  // namespace
+
+void LaunchMixerGram(double* gram, int m, int slot, int memory, const double* sums, double* gamma,
+                     cudaStream_t stream) {
+  MixerGramKernel<<<1, 32, 0, stream>>>(gram, m, slot, memory, sums, gamma);
+}
+
 bool MixerSolve(double* gram, int m, int slot, int memory, const double* sums, double* gamma) {
   for (int i = 0; i < m; ++i) {
     gram[slot * memory + i] = sums[i];

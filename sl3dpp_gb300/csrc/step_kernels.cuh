@@ -247,5 +247,10 @@ void LaunchMixerMix(const MixerArgsT<float>& a, cudaStream_t stream);
 // (gamma[m] = 1 on success, 0 when it failed and the mix takes the plain
 // step). gram: memory x memory, kept by the caller.
 bool MixerSolve(double* gram, int m, int slot, int memory, const double* sums, double* gamma);
+// The same on the device, one FP64 warp, ordered on the stream: gram
+// (memory x memory, device) updated from sums (device), gamma (m values and
+// the status) written for the mix. No host round trip.
+void LaunchMixerGram(double* gram, int m, int slot, int memory, const double* sums, double* gamma,
+                     cudaStream_t stream);
 
 }  // namespace sl3dgpu
