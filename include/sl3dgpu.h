@@ -332,9 +332,9 @@ int sl3dgpu_standard_earth(int elements, double kelvin_fraction, double kelvin_d
                            sl3dgpu_layer* layers);
 
 /* The 3D operator: Viscoelastic3D's constructor (src/Viscoelastic3D.cpp:169-356)
- * over the layered Earth, at the Gauss memory points. The unrelaxed degree
- * systems are assembled on the host and factorised on the GPU; delta is zero
- * until sl3dgpu_v3d_set_delta.
+ * over the layered Earth, at the Gauss memory points. The degree systems
+ * are assembled and factorised on the GPU; delta is zero until
+ * sl3dgpu_v3d_set_delta.
  *
  * precision 1 (the mixed form) keeps the FP64 passes and the stopping rule
  * (relative change <= rtol on an FP64 pass, whose result is the step's) and
