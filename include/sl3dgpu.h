@@ -144,17 +144,18 @@ int sl3dgpu_expand_batch(sl3dgpu_grid* grid, const double* fields, int count, do
                          void* stream);
 
 /* ---- the sea-level equation (include/sl3dpp/SeaLevel.hpp, src/SeaLevel.cpp) -----
- * GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) without rotational
- * feedback (RotationalFeedback::None), in the solver's non-dimensional units,
- * for the forcing channels of the coupled Evolution3D closure
- * (src/Evolution3D.cpp:320-333). The body: per-degree load Love numbers h, k
+ * GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) with rotational
+ * feedback None, Axial or Full, in the solver's non-dimensional units, for
+ * GeneralisedForcing's channels (those of the coupled Evolution3D closure,
+ * src/Evolution3D.cpp:320-333, and the load channels beside them). The body: per-degree load Love numbers h, k
  * (lmax + 1 each: the sums h_u + h_phi and k_u + k_phi the reference's
  * constructor forms, src/SeaLevel.cpp:163-171), the tangential l (may be
  * null), the tidal ht, kt, lt (may be null without a tide), surface gravity,
  * water density and the sea-floor radius; host arrays. The forcing:
  * GeneralisedForcing's channels as device arrays, each may be null -- fields
- * on the grid (directLoad, directLoadOutsideWaterBudget, solidSurfaceChange)
- * or (l, m >= 0) complex coefficients as (re, im) pairs (the ready
+ * on the grid (directLoad, directLoadOutsideWaterBudget, solidSurfaceChange,
+ * displacementLoad, potentialLoad, tangentialTraction) or (l, m >= 0)
+ * complex coefficients as (re, im) pairs (the ready
  * displacement, potential, tangential and toroidal responses, the tide,
  * degrees 2 and up). The load's fixed point runs under Anderson mixing of
  * its coefficients (anderson_memory columns, 0 for plain iteration) until the
@@ -177,6 +178,14 @@ typedef struct sl3dgpu_sle_body {
   int rotation;
   double omega, polar_moment, equatorial_moment, gravitational_constant;
   double hc, kc, m_u, m_phi, m_c;
+  /* the channels' own numbers (lmax + 1 each; null where the channel is
+   * unused): h_u, k_u, l_u answer a displacement load, h_phi, k_phi, l_phi a
+   * potential load, h_v, k_v, l_v a tangential traction (LoveNumbers'
+   * columns, src/SeaLevel.cpp:163-193; degree 0 of the l's and of the v's is
+   * not read) */
+  const double *h_u, *k_u, *l_u;
+  const double *h_phi, *k_phi, *l_phi;
+  const double *h_v, *k_v, *l_v;
 } sl3dgpu_sle_body;
 typedef struct sl3dgpu_sle_forcing {
   const double* direct_load;            /* field: in the water budget */
@@ -189,6 +198,9 @@ typedef struct sl3dgpu_sle_forcing {
   const double* tide;                   /* coefficients, degrees >= 2 */
   double inertia_moment_change;         /* GeneralisedForcing::inertiaMomentChange */
   double angular_momentum_change[3];    /* GeneralisedForcing::angularMomentumChange */
+  const double* displacement_load;      /* field: a surface load seen through h_u, k_u, l_u */
+  const double* potential_load;         /* field: one seen through h_phi, k_phi, l_phi */
+  const double* tangential_traction;    /* field: a traction seen through h_v, k_v, l_v (degrees >= 1) */
 } sl3dgpu_sle_forcing;
 typedef struct sl3dgpu_sle_result {
   double uniform_shift; /* Response::uniformShift: the conservation's uniform part, last formed */

@@ -52,7 +52,8 @@ class SleBody(ctypes.Structure):
                 ("radius", ctypes.c_double), ("rotation", ctypes.c_int), ("omega", ctypes.c_double),
                 ("polar_moment", ctypes.c_double), ("equatorial_moment", ctypes.c_double),
                 ("gravitational_constant", ctypes.c_double), ("hc", ctypes.c_double), ("kc", ctypes.c_double),
-                ("m_u", ctypes.c_double), ("m_phi", ctypes.c_double), ("m_c", ctypes.c_double)]
+                ("m_u", ctypes.c_double), ("m_phi", ctypes.c_double), ("m_c", ctypes.c_double)] + [
+                (name, P_double) for name in ("h_u", "k_u", "l_u", "h_phi", "k_phi", "l_phi", "h_v", "k_v", "l_v")]
 
 
 class SleForcing(ctypes.Structure):
@@ -60,7 +61,8 @@ class SleForcing(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("direct_load", "direct_load_outside", "solid_surface_change", "displacement_response",
                  "potential_response", "tangential_response", "toroidal_response", "tide")] + [
-                ("inertia_moment_change", ctypes.c_double), ("angular_momentum_change", ctypes.c_double * 3)]
+                ("inertia_moment_change", ctypes.c_double), ("angular_momentum_change", ctypes.c_double * 3)] + [
+                (name, ctypes.c_void_p) for name in ("displacement_load", "potential_load", "tangential_traction")]
 
 
 class SleResult(ctypes.Structure):

@@ -346,15 +346,19 @@ struct Rotation {
   std::array<double, 3> omega{0.0, 0.0, 0.0};
   Block2 disp2{}, grav2{}, centrifugal{};
   double centrifugal0 = 0.0;
-  // GRDSolver::Rotation's constructor with no displacement or potential
-  // load channels (displacementLoad0 = potentialLoad0 = 0)
+  // GRDSolver::Rotation's constructor (src/SeaLevel.cpp:348-392): the
+  // degree-0 parts of the displacement and potential load channels enter the
+  // axial trace and shell terms
   Rotation(const RotationFactors& s, const Block2& load2, double load0, const Block2& staticDisp2,
-           const Block2& staticGrav2, double inertiaMoment, const double* angularMomentum) {
+           const Block2& staticGrav2, double displacementLoad0, double potentialLoad0, double inertiaMoment,
+           const double* angularMomentum) {
     const Block2 gravForcing = Plus(Scaled(load2, s.k2), staticGrav2);
     const Block2 dispForcing = Plus(Scaled(load2, s.h2), staticDisp2);
     double transverse[2] = {s.inertia * gravForcing[0][1], s.inertia * gravForcing[1][1]};
-    double axial = -s.axialInertia * gravForcing[0][0] - s.trace * ((s.mu + s.mphi) * load0 + inertiaMoment) -
-                   s.shell * load0;
+    double axial = -s.axialInertia * gravForcing[0][0] -
+                   s.trace * ((s.mu + s.mphi) * load0 + s.mu * displacementLoad0 + s.mphi * potentialLoad0 +
+                              inertiaMoment) -
+                   s.shell * (load0 + potentialLoad0);
     for (int i = 0; i < 2; ++i) transverse[i] -= s.inverseInertiaDifference * angularMomentum[i];
     axial += s.inversePolarInertia * angularMomentum[2];
     if (s.transverse) {
@@ -390,6 +394,13 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   if (!(g > 0.0) || !(water_density > 0.0) || !(radius > 0.0) || !(rtol >= 0.0) || max_iterations < 0 ||
       anderson_memory < 0 || anderson_memory > kMixMaxMemory) {
     SetError("sle: g, water_density and radius > 0, rtol >= 0, max_iterations >= 0, anderson_memory in [0, 16]");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if ((forcing->displacement_load != nullptr && (body->h_u == nullptr || body->k_u == nullptr)) ||
+      (forcing->potential_load != nullptr && (body->h_phi == nullptr || body->k_phi == nullptr)) ||
+      (forcing->tangential_traction != nullptr && (body->h_v == nullptr || body->k_v == nullptr))) {
+    SetError("sle: a displacement load needs h_u and k_u, a potential load h_phi and k_phi, a tangential traction "
+             "h_v and k_v");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if (forcing->tide != nullptr && (body->ht == nullptr || body->kt == nullptr)) {
@@ -448,7 +459,8 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
     *out = m > 0.0;
     return SL3DGPU_OK;
   };
-  bool hasDirect, hasOutside, hasLayer, hasDisp, hasPot, hasTan, hasTide, hasToroidal;
+  bool hasDirect, hasOutside, hasLayer, hasDisp, hasPot, hasTan, hasTide, hasToroidal, hasDispLoad, hasPotLoad,
+      hasTraction;
   SL3D_TRY(nonzero(forcing->direct_load, run.fieldSize, &hasDirect));
   SL3D_TRY(nonzero(forcing->direct_load_outside, run.fieldSize, &hasOutside));
   SL3D_TRY(nonzero(forcing->solid_surface_change, run.fieldSize, &hasLayer));
@@ -457,6 +469,10 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   SL3D_TRY(nonzero(forcing->tangential_response, nc, &hasTan));
   SL3D_TRY(nonzero(forcing->tide, nc, &hasTide));
   SL3D_TRY(nonzero(forcing->toroidal_response, nc, &hasToroidal));
+  SL3D_TRY(nonzero(forcing->displacement_load, run.fieldSize, &hasDispLoad));
+  SL3D_TRY(nonzero(forcing->potential_load, run.fieldSize, &hasPotLoad));
+  SL3D_TRY(nonzero(forcing->tangential_traction, run.fieldSize, &hasTraction));
+  const bool hasLoadChannel = hasDispLoad || hasPotLoad || hasTraction;
   if (hasTide) {
     // RequireTideDegrees (src/SeaLevel.cpp:83-96): no degree-0 or degree-1 part
     std::vector<double> low(6);
@@ -481,7 +497,8 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
     else
       SL3D_TRY(zero(toroidal_potential));
   }
-  const bool anyForcing = hasDirect || hasOutside || hasLayer || hasDisp || hasPot || hasTan || hasTide;
+  const bool anyForcing = hasDirect || hasOutside || hasLayer || hasDisp || hasPot || hasTan || hasTide ||
+                          hasLoadChannel;
   if (!anyForcing) {
     SL3D_TRY(zero(sea_level_change));
     SL3D_TRY(zero(displacement));
@@ -492,8 +509,9 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   }
 
   // The static (load-independent) coefficient terms.
-  const bool anyStatic = hasDisp || hasPot || hasTide || hasLayer;
-  const bool anyStaticTan = hasDisp || hasPot || hasTan || hasTide;
+  const bool anyStatic = hasDisp || hasPot || hasTide || hasLayer || hasLoadChannel;
+  const bool anyStaticTan = hasDisp || hasPot || hasTan || hasTide || hasLoadChannel;
+  double displacementLoad0 = 0.0, potentialLoad0 = 0.0;
   Dev<double> staticDisp, staticGrav, staticTan, staticSlc, scratch;
   const std::vector<double> zeros(L + 1, 0.0);
   if (anyStatic || anyStaticTan) {
@@ -514,6 +532,32 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
       SL3D_TRY(run.ScaleDegrees(kt.data(), forcing->tide, staticGrav.p, 1.0, staticGrav.p));
       SL3D_TRY(run.ScaleDegrees(lt.data(), forcing->tide, staticTan.p, 1.0, staticTan.p));
     }
+    // the load channels through their own numbers (:453-502): D_s += h_c L,
+    // G_s += k_c L, T_s += l_c L with L the channel's expansion; a traction
+    // from degree 1, the l's without degree 0
+    auto channel = [&](const double* field, const double* hc, const double* kc, const double* lc, int first,
+                       double* degree0) -> int {
+      SL3D_TRY(sl3dgpu_expand_batch(grid, field, 1, scratch.p, s));
+      std::vector<double> hf(L + 1, 0.0), kf(L + 1, 0.0), lf(L + 1, 0.0);
+      for (int l = first; l <= L; ++l) {
+        hf[l] = hc[l];
+        kf[l] = kc[l];
+        if (lc != nullptr && l >= 1) lf[l] = lc[l];
+      }
+      SL3D_TRY(run.ScaleDegrees(hf.data(), scratch.p, staticDisp.p, 1.0, staticDisp.p));
+      SL3D_TRY(run.ScaleDegrees(kf.data(), scratch.p, staticGrav.p, 1.0, staticGrav.p));
+      SL3D_TRY(run.ScaleDegrees(lf.data(), scratch.p, staticTan.p, 1.0, staticTan.p));
+      if (degree0 != nullptr) {
+        SL3D_CUDA(cudaMemcpyAsync(degree0, scratch.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+        SL3D_CUDA(cudaStreamSynchronize(s));
+      }
+      return SL3DGPU_OK;
+    };
+    if (hasDispLoad)
+      SL3D_TRY(channel(forcing->displacement_load, body->h_u, body->k_u, body->l_u, 0, &displacementLoad0));
+    if (hasPotLoad)
+      SL3D_TRY(channel(forcing->potential_load, body->h_phi, body->k_phi, body->l_phi, 0, &potentialLoad0));
+    if (hasTraction) SL3D_TRY(channel(forcing->tangential_traction, body->h_v, body->k_v, body->l_v, 1, nullptr));
     // S_s = -(D_s + G_s / g) - T / g - Expand(layer) (:590-600)
     SL3D_TRY(run.Axpy(staticDisp.p, staticGrav.p, 1.0 / g, staticSlc.p));
     SL3D_TRY(run.ScaleDegrees(zeros.data(), staticSlc.p, staticSlc.p, -1.0, staticSlc.p));
@@ -586,8 +630,8 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
       double load[10], out[10];
       SL3D_TRY(headOf(run.loadLm.p, load));
       SL3D_TRY(headOf(run.scaledLm.p, out));
-      const Rotation rot(rf, BlockOf(load + 6, load + 8), load[0], staticDisp2, staticGrav2,
-                         forcing->inertia_moment_change, forcing->angular_momentum_change);
+      const Rotation rot(rf, BlockOf(load + 6, load + 8), load[0], staticDisp2, staticGrav2, displacementLoad0,
+                         potentialLoad0, forcing->inertia_moment_change, forcing->angular_momentum_change);
       patch(rot, out);
       SL3D_CUDA(cudaMemcpyAsync(run.scaledLm.p, out, 10 * sizeof(double), cudaMemcpyHostToDevice, s));
     }

@@ -9,7 +9,8 @@ feedback, its rotation constants; `solve_generalised(ocean, ...)` is
 GRDSolver::SolveGeneralised (src/SeaLevel.cpp:397-736) for GeneralisedForcing's
 channels of the coupled Evolution3D closure (src/Evolution3D.cpp:320-333):
 the direct load in and outside the water budget, a layer on the solid
-surface, the ready displacement, potential, tangential and toroidal
+surface, the displacement and potential loads and the tangential traction
+(through the channel numbers), the ready displacement, potential, tangential and toroidal
 responses, a tide, and the inertia-moment and angular-momentum changes. It
 returns the relative sea level change, displacement, potential, tangential
 and toroidal potentials on the grid and the Response scalars (with the
@@ -28,7 +29,9 @@ import torch
 from ._lib import P_double, SleBody, SleForcing, SleResult, check, lib
 from .grid import SurfaceGrid
 
-_FIELDS = ("direct_load", "direct_load_outside", "solid_surface_change")
+_FIELDS = ("direct_load", "direct_load_outside", "solid_surface_change", "displacement_load", "potential_load",
+           "tangential_traction")
+_CHANNEL_NUMBERS = ("h_u", "k_u", "l_u", "h_phi", "k_phi", "l_phi", "h_v", "k_v", "l_v")
 _COEFFS = ("displacement_response", "potential_response", "tangential_response", "toroidal_response", "tide")
 
 
@@ -36,15 +39,25 @@ class SeaLevelSolver:
     def __init__(self, grid: SurfaceGrid, h, k, l=None, ht=None, kt=None, lt=None, g: float = 1.0,
                  water_density: float = 1.0, radius: float = 1.0, rotation: int = 0, omega: float = 0.0,
                  polar_moment: float = 0.0, equatorial_moment: float = 0.0, gravitational_constant: float = 0.0,
-                 hc: float = 0.0, kc: float = 0.0, m_u: float = 0.0, m_phi: float = 0.0, m_c: float = 0.0):
+                 hc: float = 0.0, kc: float = 0.0, m_u: float = 0.0, m_phi: float = 0.0, m_c: float = 0.0,
+                 channel_numbers: dict | None = None):
         """rotation: RotationalFeedback 0 None, 1 Axial, 2 Full, with the
         body's non-dimensional rotation frequency, moments of inertia,
         gravitational constant, centrifugal (h_c, k_c) and inertia-trace
-        (m_u, m_phi, m_c) numbers (src/SeaLevel.cpp:194-247)."""
+        (m_u, m_phi, m_c) numbers (src/SeaLevel.cpp:194-247).
+        channel_numbers: the load channels' own per-degree numbers, keys
+        h_u, k_u, l_u (a displacement load), h_phi, k_phi, l_phi (a potential
+        load), h_v, k_v, l_v (a tangential traction)."""
         lmax = grid.lmax
         self.grid = grid
         self.arrays = {}
-        for name, v in (("h", h), ("k", k), ("l", l), ("ht", ht), ("kt", kt), ("lt", lt)):
+        channel_numbers = dict(channel_numbers or {})
+        unknown = set(channel_numbers) - set(_CHANNEL_NUMBERS)
+        if unknown:
+            raise ValueError(f"unknown channel numbers {sorted(unknown)}")
+        named = [("h", h), ("k", k), ("l", l), ("ht", ht), ("kt", kt), ("lt", lt)]
+        named += [(n, channel_numbers.get(n)) for n in _CHANNEL_NUMBERS]
+        for name, v in named:
             if v is None:
                 self.arrays[name] = None
                 continue
@@ -89,9 +102,9 @@ class SeaLevelSolver:
             keep.append(c)
             setattr(f, name, c.data_ptr())
         a = self.arrays
-        body = SleBody(*(a[n].ctypes.data_as(P_double) if a[n] is not None else None
-                         for n in ("h", "k", "l", "ht", "kt", "lt")), self.g, self.water_density, self.radius,
-                       *self.rotation)
+        ptr = lambda n: a[n].ctypes.data_as(P_double) if a[n] is not None else None
+        body = SleBody(*(ptr(n) for n in ("h", "k", "l", "ht", "kt", "lt")), self.g, self.water_density,
+                       self.radius, *self.rotation, *(ptr(n) for n in _CHANNEL_NUMBERS))
         out = {key: torch.empty(size, dtype=torch.float64, device=ocean.device)
                for key in ("sea_level_change", "displacement", "potential", "tangential_potential",
                            "toroidal_potential")}
