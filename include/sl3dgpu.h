@@ -517,6 +517,57 @@ int sl3dgpu_v3d_run_many(int count, sl3dgpu_v3d* const* ops, sl3dgpu_v3d_state* 
                          const double* const* times, const int* nodes, int scheme,
                          const double* const* loads, double* const* u, double* const* phi,
                          sl3dgpu_step_info* const* infos, int threads, int* statuses);
+/* ---- the ocean closure (Evolution3D, src/Evolution3D.cpp:184-394) ----------
+ * The coupled fixed point of a step under an ocean with frozen shorelines:
+ * in every pass the surface responses of the degree solves (before the load
+ * and tide channels) and their inertia moment close the sea-level equation
+ * (GRDSolver::SolveGeneralised) on the pass flavour's effective Love numbers,
+ * under the stage's direct load; its total load (the direct load and the
+ * ocean's) and the centrifugal potential of its angular velocity are the
+ * pass's load and tide channels (Coupled::Closure, :296-339). The sea-level
+ * grid is the operator's lmax at oversampling 1 (sl3dgpu_v3d_ocean_grid);
+ * fields on it are colatitude-major. Built for the FP64 fixed point
+ * (precision 0, solver 0); no prescribed tide beside it. */
+typedef struct sl3dgpu_v3d_ocean {
+  const double* ocean_function; /* host field on the sea-level grid (1 ocean, 0 land) */
+  int rotation;                 /* RotationalFeedback: 0 None, 1 Axial, 2 Full */
+  double water_density;         /* kg m^-3 (SeaLevelParameters: 1000) */
+  double rotation_frequency;    /* s^-1 (7.27220521664304e-05) */
+  double polar_moment;          /* kg m^2 (8.0359e37) */
+  double equatorial_moment;     /* kg m^2 (8.0096e37) */
+  double rtol;                  /* the sea-level solve's (Evolution3D::Options::rtol) */
+  int max_iterations;           /* its budget */
+  int anderson_memory;          /* its mixer's columns, 0..16 */
+} sl3dgpu_v3d_ocean;
+/* Sets (NULL: removes) the ocean of the operator's steps. */
+int sl3dgpu_v3d_set_ocean(sl3dgpu_v3d* op, const sl3dgpu_v3d_ocean* ocean);
+/* The sea-level grid: its shape, colatitudes and quadrature weights (either nullable). */
+int sl3dgpu_v3d_ocean_grid(sl3dgpu_v3d* op, int* ntheta, int* nphi, double* theta, double* weights);
+/* One coupled step: the direct (non-ocean) load at the step's start and end
+ * as host fields on the sea-level grid, non-dimensional surface density
+ * (NULL: zero); the stages take their linear combination (detail::AtStage).
+ * A dt = 0 step is Evolution3D::Start's instantaneous response. */
+int sl3dgpu_v3d_step_ocean(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme, const double* load0,
+                           const double* load1, sl3dgpu_step_info* info);
+/* Evolution3D::Run with the ocean: node 0 the instantaneous response, then a
+ * step per node. loads: nodes x the sea-level grid's field; u, phi,
+ * sea_level (nullable): nodes x (l(l+1)/2 + m) complex coefficients of the
+ * surface U, phi and the relative sea level change; angular_velocity
+ * (nullable): nodes x 3; infos (nullable). */
+int sl3dgpu_v3d_run_ocean(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* times, int nodes, int scheme,
+                          const double* loads, double* u, double* phi, double* sea_level, double* angular_velocity,
+                          sl3dgpu_step_info* infos);
+/* The last closure's relative sea level change, (l, m >= 0) complex host
+ * coefficients in the model's length unit (nullable), its angular velocity
+ * (3, nullable) and its solve's scalars (nullable). */
+int sl3dgpu_v3d_sea_level(sl3dgpu_v3d* op, double* coefficients, double* angular_velocity,
+                          sl3dgpu_sle_result* result);
+/* The effective Love numbers of a one-stage flavour (scheme 0 or 1, step
+ * length dt, 0 the elastic solid; ComputeLoveNumbers on the flavour's solid,
+ * src/LoveNumbers.cpp:92-176): h, k, l, h_t, k_t, l_t per degree (lmax + 1
+ * each, the tidal ones from degree 2), then h_c, k_c, the load's inertia
+ * number m_u + m_phi and m_c; 6 (lmax + 1) + 4 doubles. */
+int sl3dgpu_v3d_effective_love(sl3dgpu_v3d* op, int scheme, double dt, double* out);
 /* The CUDA stream the operator's kernels run on. */
 void* sl3dgpu_v3d_stream(const sl3dgpu_v3d* op);
 /* The last step's pass residuals (RelativeChange per pass, the stages in

@@ -40,6 +40,16 @@
 #include "oracle.h"
 #include "oracle_radial.hpp"
 
+// The ocean closure's callback (Evolution3D's Coupled::Closure,
+// src/Evolution3D.cpp:296-339): given the stage's end time, the flavour's
+// effective Love numbers (h, k, l, h_t, k_t, l_t per degree, then h_c, k_c,
+// the load's inertia number and the centrifugal one), the surface U, V and
+// phi of a pass's degree solves and their inertia moment, it writes the
+// pass's load and tide channels ((l, m >= 0) complex coefficients).
+extern "C" typedef void (*oracle_closure_fn)(void* user, double t, const double* love, int love_count,
+                                            const double* u, const double* v, const double* phi, double inertia,
+                                            double* sigma, double* psi);
+
 namespace oracle {
 
 using C = std::complex<double>;
@@ -474,6 +484,9 @@ class Viscoelastic3D {
   const OGrid& Grid() const { return grid_; }
   const std::vector<Node>& Nodes() const { return nodes_; }
   const Scales& ModelScales() const { return earth_.scales(); }
+  double SurfaceRadius() const { return material_.radius; }
+  double SurfaceGravity() const { return material_.surfaceGravity; }
+  double GravitationalConstant() const { return material_.G; }
   int Lmax() const { return options_.lmax; }
 
   void SetDelta(const double* samples) {
@@ -743,7 +756,7 @@ class Viscoelastic3D {
 
   // SolveElastic + StrainCoefficients: the start strain under the memory and
   // the load channel at the state's time, through the unrelaxed operators.
-  Spectral ElasticStrainCoefficients(const State& state, const C* load) const {
+  Spectral ElasticStrainCoefficients(const State& state, const C* load) {
     Tensor combined = ZeroTensor();
     const auto fs = grid_.FieldSize();
     for (std::size_t k = 0; k < state.m.size(); ++k) {
@@ -760,9 +773,88 @@ class Viscoelastic3D {
     Spectral weighted = ZeroSpectral();
     Analyse(combined, weighted);
     auto solutions = SolveAll(weighted, *elastic_);
-    AddLoad(solutions, *elastic_, load, tideStart_);
+    if (closure_ != nullptr) {
+      Close(solutions, *elastic_, state.t);
+      AddLoad(solutions, *elastic_, closureSigma_.data(), closurePsi_.data());
+    } else {
+      AddLoad(solutions, *elastic_, load, tideStart_);
+    }
     return StrainOf(solutions, *elastic_);
   }
+
+  // -- the ocean closure ---------------------------------------------------------------------------
+
+  void SetClosure(oracle_closure_fn fn, void* user) {
+    closure_ = fn;
+    closureUser_ = user;
+    closureSigma_.assign(grid_.RealSize(), C{});
+    closurePsi_.assign(grid_.RealSize(), C{});
+  }
+
+  // sqrt(4 pi) sum w_q J_e rho r^3 x_U over degree 0's U dofs (the moment
+  // of a degree-0 solution column x, its real part)
+  template <class T>
+  double MomentOf(const T* x) const {
+    const auto& op = *elastic_->sph[0];
+    const auto& mesh = nodal_->mesh;
+    const int n = mesh.NGll();
+    double sum = 0.0;
+    for (int e = 0; e < mesh.ElementCount(); ++e)
+      for (int q = 0; q < n; ++q) {
+        const int dof = op.Dof(mesh.GlobalIndex(e, q), kU);
+        if (dof < 0) continue;
+        const double r = mesh.Radius(e, q);
+        sum += mesh.Weights()[q] * mesh.Jacobian(e) * nodal_->rho[static_cast<std::size_t>(e) * n + q] * r * r * r *
+               std::real(x[dof]);
+      }
+    return std::sqrt(4.0 * 3.14159265358979323846) * sum;
+  }
+
+  // ComputeLoveNumbers (src/LoveNumbers.cpp:92-176) on a flavour's solid,
+  // from its unit channels: the surface U, phi and V of K^-1 Load and
+  // K^-1 Tide per degree, degree 0's centrifugal column, and the moments.
+  std::vector<double> EffectiveLove(const Flavour& f) const {
+    const int L = options_.lmax;
+    std::vector<double> out(6 * (L + 1) + 4, 0.0);
+    auto value = [](const std::vector<double>& x, int dof) { return dof >= 0 ? x[dof] : 0.0; };
+    for (int l = 0; l <= L; ++l) {
+      const auto& op = *f.sph[l];
+      const int iU = op.SurfaceDof(kU), iV = op.SurfaceDof(kV), iP = op.SurfaceDof(kPhi);
+      out[l] = value(f.units[l], iU);
+      out[(L + 1) + l] = value(f.units[l], iP);
+      out[2 * (L + 1) + l] = l >= 1 ? value(f.units[l], iV) : 0.0;
+      if (l >= 2) {
+        out[3 * (L + 1) + l] = value(f.tideUnits[l], iU);
+        out[4 * (L + 1) + l] = value(f.tideUnits[l], iP);
+        out[5 * (L + 1) + l] = value(f.tideUnits[l], iV);
+      }
+    }
+    const auto& op0 = *f.sph[0];
+    out[6 * (L + 1)] = value(f.tideUnits[0], op0.SurfaceDof(kU));
+    out[6 * (L + 1) + 1] = value(f.tideUnits[0], op0.SurfaceDof(kPhi));
+    out[6 * (L + 1) + 2] = MomentOf(f.units[0].data());
+    out[6 * (L + 1) + 3] = MomentOf(f.tideUnits[0].data());
+    return out;
+  }
+  std::vector<double> EffectiveLoveOf(Scheme scheme, double dt) { return EffectiveLove(FlavourOf(scheme, dt)); }
+
+  // One pass's closure: the responses' surface and moment to the callback,
+  // its channels into closureSigma_ / closurePsi_.
+  void Close(const Solutions& x, const Flavour& f, double t) {
+    const auto love = EffectiveLove(f);
+    const auto size = grid_.RealSize();
+    std::vector<C> u(size), v(size), phi(size);
+    SurfaceOf(x, 0, u.data());
+    SurfaceOf(x, 1, v.data());
+    SurfaceOf(x, 2, phi.data());
+    const double inertia = x.sph.empty() ? 0.0 : MomentOf(x.sph[0].data());
+    closure_(closureUser_, t, love.data(), static_cast<int>(love.size()), reinterpret_cast<const double*>(u.data()),
+             reinterpret_cast<const double*>(v.data()), reinterpret_cast<const double*>(phi.data()), inertia,
+             reinterpret_cast<double*>(closureSigma_.data()), reinterpret_cast<double*>(closurePsi_.data()));
+  }
+  oracle_closure_fn closure_ = nullptr;
+  void* closureUser_ = nullptr;
+  std::vector<C> closureSigma_, closurePsi_;
 
   double MuBranch(std::size_t k, int node) const {
     const auto& nd = nodes_[node];
@@ -1192,7 +1284,12 @@ class Viscoelastic3D {
     // The load channel at the stage's end time.
     auto pass = [&](const Spectral& s) {
       solutions = respond(s);
-      AddLoad(solutions, flavour, loadEnd, tideEnd_);
+      if (closure_ != nullptr) {
+        Close(solutions, flavour, state.t + dt);
+        AddLoad(solutions, flavour, closureSigma_.data(), closurePsi_.data());
+      } else {
+        AddLoad(solutions, flavour, loadEnd, tideEnd_);
+      }
       return StrainOf(solutions, flavour);
     };
     if (samplePasses >= 0) {
@@ -1361,7 +1458,9 @@ class Viscoelastic3D {
   // Surface (component 0 U, 1 V, 2 phi) and SurfaceToroidal (component 3,
   // W): Viscoelastic3D.cpp:2050-2112, the surface dof of each degree's
   // last solutions, zero where the degree has none.
-  void Surface(int component, C* out) const {
+  void Surface(int component, C* out) const { SurfaceOf(last_, component, out); }
+  void SurfaceOf(const Solutions& x, int component, C* out) const {
+    const auto& last_ = x;
     const int L = options_.lmax;
     if (component == 3) {
       for (int l = 0; l <= L; ++l) {
@@ -1527,6 +1626,28 @@ int oracle_v3d_sample(oracle_v3d* h, oracle_state* state, double dt, const doubl
 }
 
 int oracle_threads(void) { return omp_get_max_threads(); }
+
+// The ocean closure: each pass's load and tide channels from the callback
+// (NULL: the plain load channel again).
+void oracle_v3d_set_closure(oracle_v3d* h, oracle_closure_fn fn, void* user) { h->op->SetClosure(fn, user); }
+
+// A one-stage flavour's effective Love numbers (6 (lmax + 1) + 4 doubles).
+void oracle_v3d_effective_love(oracle_v3d* h, int scheme, double dt, double* out) {
+  const auto love = h->op->EffectiveLoveOf(static_cast<orc::Scheme>(scheme), dt);
+  std::copy(love.begin(), love.end(), out);
+}
+
+// The body's surface radius and gravity, G (model units), and the scales
+// (SI per unit of length, mass and time).
+void oracle_v3d_body(const oracle_v3d* h, double* out) {
+  const auto& sc = h->op->ModelScales();
+  out[0] = h->op->SurfaceRadius();
+  out[1] = h->op->SurfaceGravity();
+  out[2] = h->op->GravitationalConstant();
+  out[3] = sc.length;
+  out[4] = sc.mass;
+  out[5] = sc.time;
+}
 
 double oracle_v3d_inertia_moment(const oracle_v3d* h) { return h->op->InertiaMoment(); }
 

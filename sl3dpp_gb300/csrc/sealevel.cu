@@ -1,22 +1,26 @@
 // The sea-level equation's load fixed point on the GPU: GRDSolver::
-// SolveGeneralised (src/SeaLevel.cpp:397-736) without rotational feedback
-// (RotationalFeedback::None), in the solver's non-dimensional units, for the
-// forcing channels the coupled Evolution3D closure uses
-// (src/Evolution3D.cpp:320-333): the direct load in and outside the water
-// budget, a layer on the solid surface, a prescribed tide, and the ready
-// displacement, potential and tangential responses.
+// SolveGeneralised (src/SeaLevel.cpp:397-736) with rotational feedback None,
+// Axial or Full, in the solver's non-dimensional units, for GeneralisedForcing's
+// channels: the direct load in and outside the water budget, a layer on the
+// solid surface, a prescribed tide, the displacement and potential loads and
+// the tangential traction (each through its own Love numbers), and the ready
+// displacement, potential and tangential responses of the coupled Evolution3D
+// closure (src/Evolution3D.cpp:320-333).
 //
 // With per-degree load Love numbers h_l, k_l (l_l tangential), tidal ones,
 // surface gravity g, water density rho_w, the sea-floor radius a, an ocean
 // function C and the direct load sigma_d on the surface grid:
 //
-//   static  D_s = R_u + h^t T,  G_s = R_phi + k^t T,  V_s = R_v + l^t T
-//           S_s = -(D_s + G_s / g) - T / g - Expand(layer)      (:520-545, :586-600)
+//   static  D_s = R_u + h^t T + sum_c h^c E_c,  G_s = R_phi + k^t T + sum_c k^c E_c,
+//           V_s = R_v + l^t T + sum_c l^c E_c  (E_c a load channel's expansion)
+//           S_s = -(D_s + G_s / g) - T / g - Expand(layer)      (:453-545, :586-600)
 //   A       = a^2 int C dOmega, 1/A (0 without an ocean)       (:570-574)
 //   s_mean  = -a^2 int sigma_d dOmega / (A rho_w)                (:577-581)
 //   sigma   = sigma_d + sigma_outside                             (:582-587)
 //   L_0     = Expand(sigma + rho_w C s_mean)                     (:672-676)
 //   repeat  S    = Synthesise(-(h_l + k_l / g) L_lm + S_s)       (:625-634)
+//           (rotating: its degree-2 and degree-0 coefficients from the
+//           rotation block of the load, :625-640)
 //           S   += s_mean - a^2 int C S dOmega / A               (:655-661)
 //           stop when max|C S - C S_prev| <= rtol max|C S|       (:683-692)
 //           L   <- Anderson(L, Expand(sigma + rho_w C S))        (:694-699)
@@ -29,7 +33,9 @@
 // the integrals sum each ring in a fixed tree and the rings in order (the
 // grid's Integrate, SurfaceGrid.hpp:257-267); the stopping test's maxima are
 // order-free. A few scalars per iteration come to the host: the integral, the
-// two maxima and the mixer's Gram column.
+// two maxima and the rotation block's coefficients. A workspace (SleWorkspace)
+// keeps the buffers between solves on one grid, so that the coupled closure's
+// solve in every pass of a step allocates nothing.
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -41,6 +47,7 @@
 #include "sl3dgpu.h"
 #include "step_kernels.cuh"
 #include "systems.cuh"
+#include "sealevel.cuh"
 
 namespace sl3dgpu {
 namespace {
@@ -376,15 +383,86 @@ struct Rotation {
 };
 
 }  // namespace
-}  // namespace sl3dgpu
 
-using namespace sl3dgpu;
+// The workspace one solver keeps between solves on one grid: the run's
+// buffers, the mixer and the static terms.
+struct SleWorkspace {
+  sl3dgpu_grid* grid = nullptr;
+  SleRun run;
+  LoadMixer mixer;
+  int mixerMemory = -1;
+  Dev<double> staticDisp, staticGrav, staticTan, staticSlc, scratch, directData;
+  std::vector<double> theta;
 
-extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
-                                 const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations,
-                                 int anderson_memory, double* sea_level_change, double* displacement,
-                                 double* potential, double* tangential_potential, double* toroidal_potential,
-                                 sl3dgpu_sle_result* result, void* stream) {
+  // the grid's sizes, quadrature and buffers (once per grid)
+  int Prepare(sl3dgpu_grid* g) {
+    if (grid == g) return SL3DGPU_OK;
+    grid = nullptr;
+    run.grid = g;
+    int ntheta = 0, nphi = 0;
+    SL3D_TRY(sl3dgpu_grid_shape(g, &ntheta, &nphi));
+    run.lmax = sl3dgpu_grid_lmax(g);
+    if (run.lmax < 0) return SL3DGPU_ERR_ARGUMENT;
+    run.ntheta = ntheta;
+    run.nphi = nphi;
+    run.fieldSize = static_cast<long long>(ntheta) * nphi;
+    run.coefCount = static_cast<long long>(run.lmax + 1) * (run.lmax + 2) / 2;
+    run.dphi = 2.0 * 3.14159265358979323846 / nphi;
+    std::vector<double> w(ntheta);
+    theta.assign(ntheta, 0.0);
+    SL3D_TRY(sl3dgpu_grid_colatitudes(g, theta.data(), w.data()));
+    SL3D_CUDA(run.weights.Upload(w));
+    SL3D_CUDA(run.ringPartial.Alloc(ntheta));
+    run.hostRing.assign(ntheta, 0.0);
+    SL3D_CUDA(run.maxima.Alloc(2 * kMaxBlocks));
+    run.hostMaxima.assign(2 * kMaxBlocks, 0.0);
+    const long long nc = 2 * run.coefCount;
+    for (auto* d : {&run.loadLm, &run.newLoadLm, &run.scaledLm}) SL3D_CUDA(d->Alloc(nc));
+    SL3D_CUDA(run.factors.Alloc(run.lmax + 1));
+    for (auto* d : {&run.seeded, &run.slc, &run.oceanSlc, &run.newLoad}) SL3D_CUDA(d->Alloc(run.fieldSize));
+    for (auto* d : {&staticDisp, &staticGrav, &staticTan, &staticSlc, &scratch}) SL3D_CUDA(d->Alloc(nc));
+    SL3D_CUDA(directData.Alloc(run.fieldSize));
+    mixerMemory = -1;
+    grid = g;
+    return SL3DGPU_OK;
+  }
+  // the mixer at its plain start, with `memory` columns
+  int ResetMixer(int memory, cudaStream_t s) {
+    if (mixerMemory != memory) {
+      mixer = LoadMixer{};
+      SL3D_TRY(mixer.Init(memory, 2 * run.coefCount));
+      mixerMemory = memory;
+      return SL3DGPU_OK;
+    }
+    mixer.first = true;
+    mixer.count = mixer.slot = 0;
+    if (memory > 0)
+      SL3D_CUDA(cudaMemsetAsync(mixer.gram.p, 0, static_cast<size_t>(memory) * memory * sizeof(double), s));
+    return SL3DGPU_OK;
+  }
+};
+
+SleWorkspace* NewSleWorkspace() { return new SleWorkspace; }
+void FreeSleWorkspace(SleWorkspace* ws) { delete ws; }
+
+int CentrifugalCoefficients(const sl3dgpu_sle_body& body, const double omega[3], double out[6]) {
+  RotationFactors rf;
+  rf.Init(body);
+  for (int i = 0; i < 6; ++i) out[i] = 0.0;
+  if (!rf.on) return SL3DGPU_OK;
+  // (0, 0), (2, 0) and (2, 1) of CentrifugalCoefficients (src/SeaLevel.cpp:249-258);
+  // the (2, 1) pair as the complex coefficient (ShConventions.hpp:40-45)
+  out[0] = rf.uniformRotation * omega[2];
+  out[2] = rf.axialRotation * omega[2];
+  out[4] = -rf.rotation * omega[0] / std::sqrt(2.0);
+  out[5] = rf.rotation * omega[1] / std::sqrt(2.0);
+  return SL3DGPU_OK;
+}
+
+int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
+                  const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations, int anderson_memory,
+                  double* sea_level_change, double* displacement, double* potential, double* tangential_potential,
+                  double* toroidal_potential, double* total_load, sl3dgpu_sle_result* result, cudaStream_t stream) {
   if (grid == nullptr || body == nullptr || body->h == nullptr || body->k == nullptr || ocean == nullptr ||
       forcing == nullptr || sea_level_change == nullptr || result == nullptr) {
     SetError("sle: null argument");
@@ -415,34 +493,15 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
              "inertia (polar > 0, unequal) and the gravitational constant");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  SleRun run;
-  run.grid = grid;
-  run.stream = AsStream(stream);
-  int ntheta = 0, nphi = 0;
-  SL3D_TRY(sl3dgpu_grid_shape(grid, &ntheta, &nphi));
-  run.lmax = sl3dgpu_grid_lmax(grid);
-  if (run.lmax < 0) return SL3DGPU_ERR_ARGUMENT;
-  run.ntheta = ntheta;
-  run.nphi = nphi;
-  run.fieldSize = static_cast<long long>(ntheta) * nphi;
-  run.coefCount = static_cast<long long>(run.lmax + 1) * (run.lmax + 2) / 2;
+  SL3D_TRY(ws.Prepare(grid));
+  SleRun& run = ws.run;
+  run.stream = stream;
+  run.r2 = radius * radius;
   if (body->rotation != 0 && run.lmax < 2) {
     SetError("sle: rotational feedback needs degree 2 on the grid");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  run.r2 = radius * radius;
-  run.dphi = 2.0 * 3.14159265358979323846 / nphi;
-  std::vector<double> theta(ntheta), w(ntheta);
-  SL3D_TRY(sl3dgpu_grid_colatitudes(grid, theta.data(), w.data()));
-  SL3D_CUDA(run.weights.Upload(w));
-  SL3D_CUDA(run.ringPartial.Alloc(ntheta));
-  run.hostRing.assign(ntheta, 0.0);
   const int blocks = static_cast<int>(std::min<long long>(kMaxBlocks, (run.fieldSize + 255) / 256));
-  SL3D_CUDA(run.maxima.Alloc(2 * kMaxBlocks));
-  run.hostMaxima.assign(2 * kMaxBlocks, 0.0);
-  for (auto* d : {&run.loadLm, &run.newLoadLm, &run.scaledLm}) SL3D_CUDA(d->Alloc(2 * run.coefCount));
-  SL3D_CUDA(run.factors.Alloc(run.lmax + 1));
-  for (auto* d : {&run.seeded, &run.slc, &run.oceanSlc, &run.newLoad}) SL3D_CUDA(d->Alloc(run.fieldSize));
   const cudaStream_t s = run.stream;
   const int L = run.lmax;
   const long long nc = 2 * run.coefCount;  // coefficients as reals
@@ -504,6 +563,7 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
     SL3D_TRY(zero(displacement));
     SL3D_TRY(zero(potential));
     SL3D_TRY(zero(tangential_potential));
+    if (total_load != nullptr) SL3D_CUDA(cudaMemsetAsync(total_load, 0, nc * sizeof(double), s));
     SL3D_CUDA(cudaStreamSynchronize(s));
     return SL3DGPU_OK;
   }
@@ -512,13 +572,12 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   const bool anyStatic = hasDisp || hasPot || hasTide || hasLayer || hasLoadChannel;
   const bool anyStaticTan = hasDisp || hasPot || hasTan || hasTide || hasLoadChannel;
   double displacementLoad0 = 0.0, potentialLoad0 = 0.0;
-  Dev<double> staticDisp, staticGrav, staticTan, staticSlc, scratch;
+  Dev<double>&staticDisp = ws.staticDisp, &staticGrav = ws.staticGrav, &staticTan = ws.staticTan,
+             &staticSlc = ws.staticSlc, &scratch = ws.scratch;
   const std::vector<double> zeros(L + 1, 0.0);
   if (anyStatic || anyStaticTan) {
-    for (auto* d : {&staticDisp, &staticGrav, &staticTan, &staticSlc, &scratch}) {
-      SL3D_CUDA(d->Alloc(nc));
+    for (auto* d : {&staticDisp, &staticGrav, &staticTan, &staticSlc, &scratch})
       SL3D_CUDA(cudaMemsetAsync(d->p, 0, nc * sizeof(double), s));
-    }
     if (hasDisp) SL3D_TRY(run.Axpy(staticDisp.p, forcing->displacement_response, 1.0, staticDisp.p));
     if (hasPot) SL3D_TRY(run.Axpy(staticGrav.p, forcing->potential_response, 1.0, staticGrav.p));
     if (hasTan) SL3D_TRY(run.Axpy(staticTan.p, forcing->tangential_response, 1.0, staticTan.p));
@@ -575,8 +634,7 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   // the direct load in the water budget sets the mean; one outside it loads
   // the body and moves no water (:577-587)
   double meanSlc = 0.0;
-  Dev<double> directData;
-  SL3D_CUDA(directData.Alloc(run.fieldSize));
+  Dev<double>& directData = ws.directData;
   SL3D_CUDA(cudaMemsetAsync(directData.p, 0, run.fieldSize * sizeof(double), s));
   const unsigned fb = static_cast<unsigned>((run.fieldSize + 255) / 256);
   if (forcing->direct_load != nullptr) {
@@ -646,8 +704,8 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
     out[0] -= (rf.hc + (rf.kc + 1.0) / g) * rot.centrifugal0;  // uniform: absorbed by conservation
   };
 
-  LoadMixer mixer;
-  SL3D_TRY(mixer.Init(anderson_memory, nc));
+  SL3D_TRY(ws.ResetMixer(anderson_memory, s));
+  LoadMixer& mixer = ws.mixer;
   double err = INFINITY, shift = 0.0;
   bool converged = false, havePrev = false;
   int count = 0;
@@ -709,7 +767,25 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
                                  out[8] += c21[0];
                                  out[9] += c21[1];
                                }));
+  // TotalLoadCoefficients (src/Evolution3D.cpp:237-249): the direct loads and
+  // the ocean's, rho_w C S of the last sea level change
+  if (total_load != nullptr) SL3D_TRY(sl3dgpu_expand_batch(grid, run.newLoad.p, 1, total_load, s));
   SL3D_CUDA(cudaStreamSynchronize(s));
   *result = sl3dgpu_sle_result{shift, err, count, converged ? 1 : 0, {omega[0], omega[1], omega[2]}};
   return SL3DGPU_OK;
+}
+
+}  // namespace sl3dgpu
+
+using namespace sl3dgpu;
+
+extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
+                                 const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations,
+                                 int anderson_memory, double* sea_level_change, double* displacement,
+                                 double* potential, double* tangential_potential, double* toroidal_potential,
+                                 sl3dgpu_sle_result* result, void* stream) {
+  SleWorkspace ws;
+  return SeaLevelSolve(ws, grid, body, ocean, forcing, rtol, max_iterations, anderson_memory, sea_level_change,
+                       displacement, potential, tangential_potential, toroidal_potential, nullptr, result,
+                       AsStream(stream));
 }

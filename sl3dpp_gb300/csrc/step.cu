@@ -35,6 +35,7 @@
 
 #include "assemble.cuh"
 #include "host/earth.hpp"
+#include "sealevel.cuh"
 #include "sht.cuh"
 #include "step_kernels.cuh"
 #include "systems.cuh"
@@ -195,6 +196,40 @@ class Viscoelastic3DGpu {
 
   V3dState scratch;  // the second buffer set a step writes into
   std::vector<double> history;  // the last step's pass residuals, stages in turn
+
+  // The ocean closure (Evolution3D's Coupled::Closure, src/Evolution3D.cpp:
+  // 296-339, frozen shorelines): in every pass the surface responses of the
+  // degree solves (before the channels) close the sea-level equation on the
+  // flavour's effective Love numbers, on the sea-level grid, and its total
+  // load and centrifugal potential become the pass's load and tide channels.
+  struct Ocean {
+    bool on = false;
+    sl3dgpu_grid* grid = nullptr;  // the sea-level grid (lmax, spin 0, oversampling 1)
+    SleWorkspace* ws = nullptr;
+    sl3dgpu_sle_body body{};       // the constants, model units; the Love arrays per flavour
+    double rtol = 1e-10;
+    int maxIterations = 200, memory = 5;
+    long long fieldSize = 0;
+    Dev<double> function, load0, load1, stageLoad, slc;
+    Dev<double2> U, V, Phi, sigma, psi;
+    double cStart = 0.0, cEnd = 1.0;  // the running stage's start and end as fractions of the step
+    sl3dgpu_sle_result last{};        // the last closure's solve
+    bool solved = false;
+    ~Ocean() {
+      if (ws) FreeSleWorkspace(ws);
+      if (grid) sl3dgpu_grid_destroy(grid);
+    }
+  } ocean;
+  int SetOcean(const sl3dgpu_v3d_ocean* o);
+  int StageLoad(double c);
+  int EffectiveLove(const Flavour& f, const std::vector<double>** out);
+  int EffectiveLoveOf(int scheme, double dt, const std::vector<double>** out);
+  int Closure(const Flavour& f);
+  int StepOcean(V3dState& st, double dt, int scheme, const double* load0, const double* load1,
+                sl3dgpu_step_info* info);
+  int RunOcean(V3dState& st, const double* times, int nodes, int scheme, const double* loads, double* u, double* phi,
+               double* slc, double* omega, sl3dgpu_step_info* infos);
+  int SeaLevel(double* coefficients, double* omega, sl3dgpu_sle_result* result);
 
   ~Viscoelastic3DGpu() {
     if (hostResult) cudaFreeHost(hostResult);
@@ -829,6 +864,12 @@ int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useSta
   LaunchForces(geo, force, rhsSph.p, rhsTor.p, stream);
   SL3D_CHECK_LAUNCH();
   SL3D_TRY(Solve(f));
+  if (ocean.on) {
+    // the pass's closure sets its load and tide channels
+    SL3D_TRY(Closure(f));
+    sigma = ocean.sigma.p;
+    tide = ocean.psi.p;
+  }
   if (sigma != nullptr || tide != nullptr) {
     LaunchAddLoad(geo, sigma, f.units.p, f.unitOffset.p, rhsSph.p, stream, tide, f.tideUnits.p);
     SL3D_CHECK_LAUNCH();
@@ -946,8 +987,10 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   if (in.hasCoeffs) {
     SL3D_CUDA(cudaMemcpyAsync(s.p, in.coeffs.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
   } else {
+    if (ocean.on) SL3D_TRY(StageLoad(ocean.cStart));  // the start's closure under the load at the state's time
     SL3D_TRY(ElasticStrain(in, sigmaStart));
   }
+  if (ocean.on) SL3D_TRY(StageLoad(ocean.cEnd));
   // The start strain on the grid, needed at the lateral nodes only.
   const GridTensor* d0 = &in.strain;
   if (!in.hasStrain) {
@@ -1185,6 +1228,240 @@ int Viscoelastic3DGpu::Run(V3dState& st, const double* times, int nodes, int sch
     if (u) SL3D_TRY(Surface(0, u + 2 * lm * k));
     if (phi) SL3D_TRY(Surface(2, phi + 2 * lm * k));
   }
+  return SL3DGPU_OK;
+}
+
+// -- the ocean closure ---------------------------------------------------------------------------------
+
+namespace {
+// out = (1 - c) a + c b over a field
+__global__ void BlendFieldKernel(long long n, double c, const double* a, const double* b, double* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < n) out[i] = (1.0 - c) * a[i] + c * b[i];
+}
+}  // namespace
+
+// The sea-level body of the operator's Earth in its model units: the
+// surface gravity and radius (the sea floor at the surface), water density,
+// rotation and moments of inertia (SeaLevelParameters, include/sl3dpp/
+// SeaLevel.hpp:54-68, SI on input), G = 1 in the geophysical scales.
+int Viscoelastic3DGpu::SetOcean(const sl3dgpu_v3d_ocean* o) {
+  if (o == nullptr) {
+    ocean.on = false;
+    return SL3DGPU_OK;
+  }
+  if (staticMode || options.solver != 0 || options.precision != 0) {
+    SetError("v3d: the ocean closure is built for the FP64 fixed point (precision 0, solver 0)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (o->ocean_function == nullptr || o->rotation < 0 || o->rotation > 2 || !(o->water_density > 0.0) ||
+      !(o->rtol > 0.0) || o->max_iterations < 1 || o->anderson_memory < 0 || o->anderson_memory > 16 ||
+      (o->rotation != 0 && (!(o->rotation_frequency > 0.0) || !(o->polar_moment > 0.0) ||
+                            !(o->polar_moment != o->equatorial_moment)))) {
+    SetError("v3d: an ocean needs its function, rotation 0, 1 or 2 (with a rotation frequency and unequal "
+             "moments of inertia), water density > 0, rtol > 0, max_iterations >= 1 and anderson_memory in "
+             "[0, 16]");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (ocean.grid == nullptr) {
+    SL3D_TRY(sl3dgpu_grid_create(options.lmax, 0, 1.0, &ocean.grid));
+    ocean.ws = NewSleWorkspace();
+  }
+  int nt = 0, np = 0;
+  SL3D_TRY(sl3dgpu_grid_shape(ocean.grid, &nt, &np));
+  ocean.fieldSize = static_cast<long long>(nt) * np;
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  std::vector<double> function(o->ocean_function, o->ocean_function + ocean.fieldSize);
+  SL3D_CUDA(ocean.function.Upload(function));
+  for (auto* d : {&ocean.load0, &ocean.load1, &ocean.stageLoad, &ocean.slc}) SL3D_CUDA(d->Alloc(ocean.fieldSize));
+  for (auto* d : {&ocean.U, &ocean.V, &ocean.Phi, &ocean.sigma, &ocean.psi}) SL3D_CUDA(d->Alloc(lm));
+  SL3D_CUDA(ZeroIn(ocean.psi.p, lm * sizeof(double2)));
+  SL3D_CUDA(ZeroIn(ocean.load0.p, ocean.fieldSize * sizeof(double)));
+  SL3D_CUDA(ZeroIn(ocean.load1.p, ocean.fieldSize * sizeof(double)));
+  const auto& sc = earth->scales();
+  sl3dgpu_sle_body& b = ocean.body;
+  b = sl3dgpu_sle_body{};
+  b.g = material->surfaceGravity;
+  b.radius = material->radius;
+  b.water_density = o->water_density / sc.Density();
+  b.rotation = o->rotation;
+  b.omega = o->rotation_frequency * sc.time;
+  b.polar_moment = o->polar_moment / sc.Factor(1, 2, 0);
+  b.equatorial_moment = o->equatorial_moment / sc.Factor(1, 2, 0);
+  b.gravitational_constant = material->G;
+  ocean.rtol = o->rtol;
+  ocean.maxIterations = o->max_iterations;
+  ocean.memory = o->anderson_memory;
+  ocean.solved = false;
+  ocean.on = true;
+  return SL3DGPU_OK;
+}
+
+// The running stage's direct load: (1 - c) of the step's start load and c of its end's.
+int Viscoelastic3DGpu::StageLoad(double c) {
+  BlendFieldKernel<<<static_cast<unsigned>((ocean.fieldSize + 255) / 256), 256, 0, stream>>>(
+      ocean.fieldSize, c, ocean.load0.p, ocean.load1.p, ocean.stageLoad.p);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+// A flavour's effective Love numbers (ComputeLoveNumbers, src/LoveNumbers.cpp:
+// 92-176, on the flavour's solid): the surface U, V and phi of its unit
+// channels K^-1 Load and K^-1 Tide per degree, degree 0's centrifugal column
+// for h_c, k_c, and the inertia moments of degree 0's load and centrifugal
+// solutions (the moment row of InertiaMoment).
+int Viscoelastic3DGpu::EffectiveLove(const Flavour& f, const std::vector<double>** out) {
+  Flavour& mf = const_cast<Flavour&>(f);
+  if (mf.effectiveLove.empty()) {
+    const int L = options.lmax;
+    std::vector<double> units(f.units.n), tides(f.tideUnits.n);
+    std::vector<long long> offset(L + 1);
+    SL3D_CUDA(cudaMemcpyAsync(units.data(), f.units.p, units.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream));
+    SL3D_CUDA(cudaMemcpyAsync(tides.data(), f.tideUnits.p, tides.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream));
+    SL3D_CUDA(cudaMemcpyAsync(offset.data(), f.unitOffset.p, offset.size() * sizeof(long long),
+                              cudaMemcpyDeviceToHost, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    std::vector<double> love(6 * (L + 1) + 4, 0.0);
+    auto at = [&](const std::vector<double>& v, int l, int dof) { return dof >= 0 ? v[offset[l] + dof] : 0.0; };
+    for (int l = 0; l <= L; ++l) {
+      const DegreeInfo& d = degrees[l];
+      love[l] = at(units, l, d.surfaceU);
+      love[(L + 1) + l] = at(units, l, d.surfacePhi);
+      love[2 * (L + 1) + l] = l >= 1 ? at(units, l, d.surfaceV) : 0.0;
+      if (l >= 2) {  // the tidal numbers from degree 2 (degree 0 carries the centrifugal column)
+        love[3 * (L + 1) + l] = at(tides, l, d.surfaceU);
+        love[4 * (L + 1) + l] = at(tides, l, d.surfacePhi);
+        love[5 * (L + 1) + l] = at(tides, l, d.surfaceV);
+      }
+    }
+    double m = 0.0, mc = 0.0;
+    for (int dof = 0; dof < degrees[0].sphNdof; ++dof) {
+      m += momentRow[dof] * units[offset[0] + dof];
+      mc += momentRow[dof] * tides[offset[0] + dof];
+    }
+    love[6 * (L + 1)] = at(tides, 0, degrees[0].surfaceU);
+    love[6 * (L + 1) + 1] = at(tides, 0, degrees[0].surfacePhi);
+    love[6 * (L + 1) + 2] = m;
+    love[6 * (L + 1) + 3] = mc;
+    mf.effectiveLove = std::move(love);
+  }
+  *out = &mf.effectiveLove;
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::EffectiveLoveOf(int scheme, double dt, const std::vector<double>** out) {
+  Flavour* f = nullptr;
+  SL3D_TRY(FlavourOf(scheme, dt, &f));
+  return EffectiveLove(*f, out);
+}
+
+// Closure (src/Evolution3D.cpp:296-339, frozen shorelines): the surface
+// responses of the pass's degree solves and their inertia moment close the
+// sea-level equation on the flavour's effective numbers under the stage's
+// direct load; its total load and the centrifugal potential of its angular
+// velocity are the pass's load and tide channels.
+int Viscoelastic3DGpu::Closure(const Flavour& f) {
+  const std::vector<double>* love = nullptr;
+  SL3D_TRY(EffectiveLove(f, &love));
+  const int L = options.lmax;
+  LaunchSurface(geo, rhsSph.p, rhsTor.p, 0, ocean.U.p, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchSurface(geo, rhsSph.p, rhsTor.p, 1, ocean.V.p, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchSurface(geo, rhsSph.p, rhsTor.p, 2, ocean.Phi.p, stream);
+  SL3D_CHECK_LAUNCH();
+  double moment = 0.0;
+  SL3D_TRY(InertiaMoment(&moment));
+  sl3dgpu_sle_body b = ocean.body;
+  const double* v = love->data();
+  b.h = v;
+  b.k = v + (L + 1);
+  b.l = v + 2 * (L + 1);
+  b.ht = v + 3 * (L + 1);
+  b.kt = v + 4 * (L + 1);
+  b.lt = v + 5 * (L + 1);
+  b.hc = v[6 * (L + 1)];
+  b.kc = v[6 * (L + 1) + 1];
+  b.m_u = v[6 * (L + 1) + 2];  // the load's whole trace number (no displacement or potential load channel)
+  b.m_phi = 0.0;
+  b.m_c = v[6 * (L + 1) + 3];
+  sl3dgpu_sle_forcing forcing{};
+  forcing.direct_load = ocean.stageLoad.p;
+  forcing.displacement_response = reinterpret_cast<const double*>(ocean.U.p);
+  forcing.potential_response = reinterpret_cast<const double*>(ocean.Phi.p);
+  forcing.tangential_response = reinterpret_cast<const double*>(ocean.V.p);
+  forcing.inertia_moment_change = moment;
+  SL3D_TRY(SeaLevelSolve(*ocean.ws, ocean.grid, &b, ocean.function.p, &forcing, ocean.rtol, ocean.maxIterations,
+                         ocean.memory, ocean.slc.p, nullptr, nullptr, nullptr, nullptr,
+                         reinterpret_cast<double*>(ocean.sigma.p), &ocean.last, stream));
+  double psi[6];
+  SL3D_TRY(CentrifugalCoefficients(b, ocean.last.angular_velocity, psi));
+  // (0, 0) at 0, (2, 0) at 3, (2, 1) at 4 of the l(l+1)/2 + m layout
+  if (b.rotation != 0) {
+    SL3D_CUDA(cudaMemcpyAsync(ocean.psi.p, psi, sizeof(double2), cudaMemcpyHostToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(ocean.psi.p + 3, psi + 2, 2 * sizeof(double2), cudaMemcpyHostToDevice, stream));
+  }
+  ocean.solved = true;
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::StepOcean(V3dState& st, double dt, int scheme, const double* load0, const double* load1,
+                                 sl3dgpu_step_info* info) {
+  if (!ocean.on) {
+    SetError("v3d: no ocean is set (sl3dgpu_v3d_set_ocean)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const size_t bytes = ocean.fieldSize * sizeof(double);
+  if (load0) SL3D_CUDA(cudaMemcpyAsync(ocean.load0.p, load0, bytes, cudaMemcpyHostToDevice, stream));
+  else SL3D_CUDA(cudaMemsetAsync(ocean.load0.p, 0, bytes, stream));
+  if (load1) SL3D_CUDA(cudaMemcpyAsync(ocean.load1.p, load1, bytes, cudaMemcpyHostToDevice, stream));
+  else SL3D_CUDA(cudaMemsetAsync(ocean.load1.p, 0, bytes, stream));
+  return Step(st, dt, scheme, nullptr, nullptr, info);
+}
+
+// Evolution3D::March for frozen shorelines (src/Evolution3D.cpp:521-821):
+// node 0 the instantaneous response closed by the sea-level equation (a
+// zero-length step), then one step per node, each pass closed.
+int Viscoelastic3DGpu::RunOcean(V3dState& st, const double* times, int nodes, int scheme, const double* loads,
+                                double* u, double* phi, double* slc, double* omega, sl3dgpu_step_info* infos) {
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  for (int k = 0; k < nodes; ++k) {
+    const double* l1 = loads + ocean.fieldSize * k;
+    const double* l0 = k > 0 ? loads + ocean.fieldSize * (k - 1) : l1;
+    const double dt = k > 0 ? times[k] - times[k - 1] : 0.0;
+    if (!(dt >= 0.0)) {
+      SetError("v3d: node times must not decrease");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+    sl3dgpu_step_info info{};
+    SL3D_TRY(StepOcean(st, dt, scheme, l0, l1, &info));
+    if (infos) infos[k] = info;
+    if (u) SL3D_TRY(Surface(0, u + 2 * lm * k));
+    if (phi) SL3D_TRY(Surface(2, phi + 2 * lm * k));
+    if (slc || omega)
+      SL3D_TRY(SeaLevel(slc ? slc + 2 * lm * k : nullptr, omega ? omega + 3 * k : nullptr, nullptr));
+  }
+  return SL3DGPU_OK;
+}
+
+// The last closure's relative sea level change as (l, m >= 0) coefficients
+// (host), its angular velocity and its solve's scalars.
+int Viscoelastic3DGpu::SeaLevel(double* coefficients, double* omega, sl3dgpu_sle_result* result) {
+  if (!ocean.on || !ocean.solved) {
+    SetError("v3d: no sea-level closure has run (an ocean and a step)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (coefficients) {
+    const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+    SL3D_TRY(sl3dgpu_expand_batch(ocean.grid, ocean.slc.p, 1, reinterpret_cast<double*>(ocean.U.p), stream));
+    SL3D_CUDA(cudaMemcpyAsync(coefficients, ocean.U.p, lm * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+  }
+  if (omega)
+    for (int i = 0; i < 3; ++i) omega[i] = ocean.last.angular_velocity[i];
+  if (result) *result = ocean.last;
   return SL3DGPU_OK;
 }
 
@@ -1836,6 +2113,8 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   if (scheme != 2 || dt == 0.0) {
     const int one = scheme == 2 ? 1 : scheme;
     stageGuess = haveGuess ? guess.p : nullptr;
+    ocean.cStart = 0.0;
+    ocean.cEnd = 1.0;
     SL3D_TRY(StepOnce(st, scratch, dt, one, s0, s1, info));
   } else {
     const double gamma = host::kSdirk2Gamma;
@@ -1865,6 +2144,8 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
       SL3D_CHECK_LAUNCH();
       stageGuess = guessMid.p;
     }
+    ocean.cStart = 0.0;
+    ocean.cEnd = gamma;
     SL3D_TRY(StepOnce(st, scratch, h, 1, s0, mid, i1));
     // the second stage's memory (1 - r) m_n + r Y_1, formed in place in Y_1
     const double r = (1.0 - gamma) / gamma;
@@ -1882,6 +2163,8 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
     stageGuess = haveGuess ? guess.p : nullptr;
     tideStart = tmid;
     tideEnd = t1;
+    ocean.cStart = gamma;
+    ocean.cEnd = 1.0;
     SL3D_TRY(StepOnce(scratch, scratch, h, 1, mid, s1, i2));
     info.iterations = i1.iterations + i2.iterations;
     info.mixed_passes = i1.mixed_passes + i2.mixed_passes;
@@ -2145,6 +2428,80 @@ extern "C" int sl3dgpu_v3d_state_coefficients_host(const sl3dgpu_v3d* h, const s
   }
   SL3D_CUDA(cudaStreamSynchronize(h->op.stream));  // the legacy-stream copy does not wait for it
   SL3D_CUDA(cudaMemcpy(out, state->st.coeffs.p, h->op.spectralComplex * sizeof(double2), cudaMemcpyDeviceToHost));
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_set_ocean(sl3dgpu_v3d* h, const sl3dgpu_v3d_ocean* ocean) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SetOcean(ocean);
+}
+
+extern "C" int sl3dgpu_v3d_ocean_grid(sl3dgpu_v3d* h, int* ntheta, int* nphi, double* theta, double* weights) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto& op = h->op;
+  if (op.ocean.grid == nullptr) {
+    SL3D_TRY(sl3dgpu_grid_create(op.options.lmax, 0, 1.0, &op.ocean.grid));
+    op.ocean.ws = NewSleWorkspace();
+  }
+  int nt = 0, np = 0;
+  SL3D_TRY(sl3dgpu_grid_shape(op.ocean.grid, &nt, &np));
+  if (ntheta) *ntheta = nt;
+  if (nphi) *nphi = np;
+  if (theta != nullptr || weights != nullptr) {
+    std::vector<double> th(nt), w(nt);
+    SL3D_TRY(sl3dgpu_grid_colatitudes(op.ocean.grid, th.data(), w.data()));
+    if (theta) std::copy(th.begin(), th.end(), theta);
+    if (weights) std::copy(w.begin(), w.end(), weights);
+  }
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_step_ocean(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, double dt, int scheme,
+                                      const double* load0, const double* load1, sl3dgpu_step_info* info) {
+  if (h == nullptr || state == nullptr) {
+    SetError("v3d: null handle or state");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StepOcean(state->st, dt, scheme, load0, load1, info);
+}
+
+extern "C" int sl3dgpu_v3d_run_ocean(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const double* times, int nodes,
+                                     int scheme, const double* loads, double* u, double* phi, double* sea_level,
+                                     double* angular_velocity, sl3dgpu_step_info* infos) {
+  if (h == nullptr || state == nullptr || times == nullptr || loads == nullptr || nodes < 0) {
+    SetError("v3d: null argument or negative node count");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (!h->op.ocean.on) {
+    SetError("v3d: no ocean is set (sl3dgpu_v3d_set_ocean)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.RunOcean(state->st, times, nodes, scheme, loads, u, phi, sea_level, angular_velocity, infos);
+}
+
+extern "C" int sl3dgpu_v3d_sea_level(sl3dgpu_v3d* h, double* coefficients, double* angular_velocity,
+                                     sl3dgpu_sle_result* result) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SeaLevel(coefficients, angular_velocity, result);
+}
+
+extern "C" int sl3dgpu_v3d_effective_love(sl3dgpu_v3d* h, int scheme, double dt, double* out) {
+  if (h == nullptr || out == nullptr || scheme < 0 || scheme > 1 || !(dt >= 0.0) || h->op.staticMode) {
+    SetError("v3d: effective Love numbers of a one-stage flavour (scheme 0 or 1, dt >= 0) of the step operator");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const std::vector<double>* love = nullptr;
+  SL3D_TRY(h->op.EffectiveLoveOf(scheme, dt, &love));
+  std::copy(love->begin(), love->end(), out);
   return SL3DGPU_OK;
 }
 

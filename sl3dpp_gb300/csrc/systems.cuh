@@ -95,6 +95,10 @@ struct Flavour {
   // lateral forces reach), for the lateral node range [windowFirst, windowEnd).
   mutable int windowFirst = -1, windowEnd = -1;
   mutable Dev<int2> wSphChol, wSphLu, wTorChol;
+  // The flavour's effective Love numbers for the sea-level closure, built on
+  // first use: h, k, l, ht, kt, lt per degree (lmax + 1 each), then h_c,
+  // k_c, the load's inertia-trace number m and the centrifugal one m_c.
+  std::vector<double> effectiveLove;
 };
 
 

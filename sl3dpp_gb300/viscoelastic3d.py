@@ -53,6 +53,23 @@ class Options(ctypes.Structure):
         return o
 
 
+class OceanOptions(ctypes.Structure):
+    """sl3dgpu_v3d_ocean: the ocean of the coupled step (SI), SeaLevelParameters'
+    defaults (include/sl3dpp/SeaLevel.hpp:54-68) for the body's constants."""
+
+    _fields_ = [("ocean_function", c_void_p), ("rotation", ctypes.c_int), ("water_density", ctypes.c_double),
+                ("rotation_frequency", ctypes.c_double), ("polar_moment", ctypes.c_double),
+                ("equatorial_moment", ctypes.c_double), ("rtol", ctypes.c_double),
+                ("max_iterations", ctypes.c_int), ("anderson_memory", ctypes.c_int)]
+
+
+class SleResult(ctypes.Structure):
+    """sl3dgpu_sle_result."""
+
+    _fields_ = [("uniform_shift", ctypes.c_double), ("error", ctypes.c_double), ("iterations", ctypes.c_int),
+                ("converged", ctypes.c_int), ("angular_velocity", ctypes.c_double * 3)]
+
+
 class StepInfo(ctypes.Structure):
     """sl3dgpu_step_info (Viscoelastic3D::StepInfo)."""
 
@@ -98,6 +115,12 @@ def _signatures():
         "sl3dgpu_v3d_state_coefficients_host": (i, [v, v, v]),
         "sl3dgpu_v3d_assembled_band": (i, [v, i, d, i, i, P_double, ctypes.c_longlong, P_int, P_int]),
         "sl3dgpu_v3d_surface_device": (i, [v, i, v]),
+        "sl3dgpu_v3d_set_ocean": (i, [v, ctypes.POINTER(OceanOptions)]),
+        "sl3dgpu_v3d_ocean_grid": (i, [v, P_int, P_int, P_double, P_double]),
+        "sl3dgpu_v3d_step_ocean": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_run_ocean": (i, [v, v, P_double, i, i, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_sea_level": (i, [v, v, v, ctypes.POINTER(SleResult)]),
+        "sl3dgpu_v3d_effective_love": (i, [v, i, d, P_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -304,6 +327,66 @@ class Viscoelastic3D:
         check(lib().sl3dgpu_v3d_inertia_moment(self._h, ctypes.byref(out)))
         return out.value
 
+    # -- the ocean closure (Evolution3D's Coupled::Closure, frozen shorelines)
+
+    def ocean_grid(self):
+        """The sea-level grid: (colatitudes, quadrature weights, longitudes)."""
+        nt, nph = ctypes.c_int(), ctypes.c_int()
+        check(lib().sl3dgpu_v3d_ocean_grid(self._h, ctypes.byref(nt), ctypes.byref(nph), None, None))
+        theta, w = np.empty(nt.value), np.empty(nt.value)
+        check(lib().sl3dgpu_v3d_ocean_grid(self._h, None, None, theta.ctypes.data_as(P_double),
+                                           w.ctypes.data_as(P_double)))
+        return theta, w, nph.value
+
+    def set_ocean(self, ocean_function, rotation: int = 1, water_density: float = 1000.0,
+                  rotation_frequency: float = 7.27220521664304e-05, polar_moment: float = 8.0359e37,
+                  equatorial_moment: float = 8.0096e37, rtol: float = 1e-10, max_iterations: int = 200,
+                  anderson_memory: int = 5) -> None:
+        """The ocean of the coupled steps (None removes it): its function on
+        the sea-level grid, the rotational feedback (0 None, 1 Axial, 2 Full)
+        and the sea-level solve's tolerance, budget and mixer."""
+        if ocean_function is None:
+            check(lib().sl3dgpu_v3d_set_ocean(self._h, None))
+            return
+        theta, _, nphi = self.ocean_grid()
+        f = np.ascontiguousarray(ocean_function, dtype=np.float64).ravel()
+        if f.size != theta.size * nphi:
+            raise ValueError("the ocean function lives on the sea-level grid")
+        o = OceanOptions(f.ctypes.data, int(rotation), float(water_density), float(rotation_frequency),
+                         float(polar_moment), float(equatorial_moment), float(rtol), int(max_iterations),
+                         int(anderson_memory))
+        check(lib().sl3dgpu_v3d_set_ocean(self._h, ctypes.byref(o)))
+
+    def StepOcean(self, state: State, dt: float, scheme="sdirk2", load0=None, load1=None) -> StepInfo:
+        """One coupled step under the direct (non-ocean) load fields on the
+        sea-level grid at the step's start and end (non-dimensional)."""
+        code = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        info = StepInfo()
+        a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.float64)
+        b = None if load1 is None else np.ascontiguousarray(load1, dtype=np.float64)
+        check(lib().sl3dgpu_v3d_step_ocean(self._h, state._h, float(dt), code, None if a is None else a.ctypes.data,
+                                           None if b is None else b.ctypes.data, ctypes.byref(info)))
+        return info
+
+    def SeaLevel(self):
+        """The last closure's relative sea level change ((l, m >= 0)
+        coefficients, model length unit), angular velocity and solve scalars."""
+        out = np.zeros((self.lmax + 1) * (self.lmax + 2) // 2, dtype=np.complex128)
+        omega = np.zeros(3)
+        res = SleResult()
+        check(lib().sl3dgpu_v3d_sea_level(self._h, out.ctypes.data, omega.ctypes.data, ctypes.byref(res)))
+        return out, omega, res
+
+    def effective_love(self, scheme: int, dt: float) -> dict:
+        """A one-stage flavour's effective Love numbers (model units)."""
+        L = self.lmax
+        out = np.zeros(6 * (L + 1) + 4)
+        check(lib().sl3dgpu_v3d_effective_love(self._h, int(scheme), float(dt), out.ctypes.data_as(P_double)))
+        names = ("h", "k", "l", "ht", "kt", "lt")
+        love = {n: out[i * (L + 1):(i + 1) * (L + 1)].copy() for i, n in enumerate(names)}
+        love.update(hc=out[6 * (L + 1)], kc=out[6 * (L + 1) + 1], m=out[6 * (L + 1) + 2], mc=out[6 * (L + 1) + 3])
+        return love
+
 
 class Evolution3D:
     """Evolution3D::Run for a body without an ocean and without rotational
@@ -334,3 +417,23 @@ class Evolution3D:
     def Instantaneous(self, load):
         out = self.Run(np.zeros(1), np.asarray(load)[None, :])
         return {"U": out["U"][0], "phi": out["phi"][0]}
+
+    def RunOcean(self, times, loads, state: State | None = None):
+        """Evolution3D::Run with the operator's ocean (set_ocean): loads are
+        the direct (non-ocean) load fields on the sea-level grid per node;
+        snapshots carry U, phi and the relative sea level change as
+        coefficients and the angular velocity."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        theta, _, nphi = self.op.ocean_grid()
+        n = times.size
+        loads = np.ascontiguousarray(loads, dtype=np.float64).reshape(n, theta.size * nphi)
+        lm = (self.op.lmax + 1) * (self.op.lmax + 2) // 2
+        state = state if state is not None else self.op.ZeroState()
+        U, phi, slc = (np.zeros((n, lm), dtype=np.complex128) for _ in range(3))
+        omega = np.zeros((n, 3))
+        infos = (StepInfo * max(n, 1))()
+        check(lib().sl3dgpu_v3d_run_ocean(self.op._h, state._h, times.ctypes.data_as(P_double), n, self.scheme,
+                                          loads.ctypes.data, U.ctypes.data, phi.ctypes.data, slc.ctypes.data,
+                                          omega.ctypes.data, infos))
+        return {"U": U, "phi": phi, "sea_level": slc, "omega": omega, "infos": [infos[k] for k in range(n)],
+                "state": state}

@@ -159,7 +159,7 @@ class Options(_ct.Structure):
                 ("anderson_memory", _ct.c_int), ("anderson_rate", _ct.c_double), ("precision", _ct.c_int),
                 ("correction_rtol", _ct.c_double), ("solver", _ct.c_int),
                 ("solve_rtol", _ct.c_double), ("solve_max_iterations", _ct.c_int),
-                ("warm_start", _ct.c_int)]
+                ("warm_start", _ct.c_int), ("fp64_emulation", _ct.c_int), ("correction_memory", _ct.c_int)]
 
 
 class StepInfo(_ct.Structure):
@@ -171,7 +171,8 @@ class StepInfo(_ct.Structure):
 def default_options(lmax, ngll=5, **kw):
     o = Options(lmax=lmax, ngll=ngll, eps=1e-8, oversampling=1.5, max_iterations=40, rtol=1e-11, damping=1.0,
                 anderson_memory=5, anderson_rate=0.5, precision=0, correction_rtol=1e-5,
-                solver=0, solve_rtol=1e-11, solve_max_iterations=200, warm_start=0)
+                solver=0, solve_rtol=1e-11, solve_max_iterations=200, warm_start=0, fp64_emulation=0,
+                correction_memory=0)
     for k, v in kw.items():
         setattr(o, k, v)
     return o
@@ -180,6 +181,12 @@ def default_options(lmax, ngll=5, **kw):
 class EpOptions(_ct.Structure):
     """sl3dgpu_ep3d_options (include/sl3dgpu.h)."""
     _fields_ = [("lmax", _ct.c_int), ("ngll", _ct.c_int), ("eps", _ct.c_double), ("oversampling", _ct.c_double)]
+
+
+# oracle_closure_fn (oracle_step.cpp)
+_CLOSURE = _ct.CFUNCTYPE(None, _ct.c_void_p, _ct.c_double, _ct.POINTER(_ct.c_double), _ct.c_int,
+                         _ct.POINTER(_ct.c_double), _ct.POINTER(_ct.c_double), _ct.POINTER(_ct.c_double),
+                         _ct.c_double, _ct.POINTER(_ct.c_double), _ct.POINTER(_ct.c_double))
 
 
 def _v3d_sigs(L):
@@ -210,6 +217,9 @@ def _v3d_sigs(L):
         "oracle_ep3d_solve_load": (None, [v, v]),
         "oracle_ep3d_respond": (None, [v]),
         "oracle_ep3d_solve_lateral": (i, [v, v, d, i, _ct.POINTER(StepInfo)]),
+        "oracle_v3d_set_closure": (None, [v, _CLOSURE, v]),
+        "oracle_v3d_effective_love": (None, [v, i, d, P_double]),
+        "oracle_v3d_body": (None, [v, P_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -295,6 +305,62 @@ class OracleStep:
         out = np.zeros((L + 1) * (L + 2) // 2, dtype=np.complex128)
         self.L.oracle_v3d_surface(self.h, component, out.ctypes.data)
         return out
+
+    # -- the ocean closure (oracle/coupled.py)
+
+    def body(self):
+        out = np.zeros(6)
+        self.L.oracle_v3d_body(self.h, ptr(out))
+        return dict(radius=out[0], g=out[1], G=out[2], length=out[3], mass=out[4], time=out[5])
+
+    def effective_love(self, scheme, dt):
+        L = self.options.lmax
+        out = np.zeros(6 * (L + 1) + 4)
+        self.L.oracle_v3d_effective_love(self.h, scheme, dt, ptr(out))
+        return out
+
+    def set_ocean(self, ocean, **kw):
+        """Closes every pass with the sea-level equation over `ocean` (a
+        field on the sea-level grid, lmax at oversampling 1), the closure of
+        oracle/coupled.py; kw: OceanClosure's constants."""
+        from oracle.coupled import OceanClosure
+
+        lmax = self.options.lmax
+        theta, w, nphi = grid(lmax, 1.0)
+        self.sle_grid = (theta, w, nphi)
+        transforms = (lambda c: synthesise_real(lmax, theta, nphi, c),
+                      lambda f: expand_real(lmax, theta, w, nphi, f),
+                      lambda f: float(np.sum(w * f.reshape(theta.size, nphi).sum(axis=1)) * 2 * np.pi / nphi))
+        self.closure = OceanClosure(lmax, transforms, self.body(), ocean, **kw)
+        size = (lmax + 1) * (lmax + 2) // 2
+
+        def callback(user, t, love, count, u, v, phi, inertia, sigma, psi):
+            love_a = np.ctypeslib.as_array(love, (count,)).copy()
+            cx = lambda q: np.ctypeslib.as_array(q, (2 * size,)).view(np.complex128).copy()
+            s, p = self.closure(t, love_a, cx(u), cx(v), cx(phi), inertia)
+            np.ctypeslib.as_array(sigma, (2 * size,))[:] = s.view(np.float64)
+            np.ctypeslib.as_array(psi, (2 * size,))[:] = p.view(np.float64)
+
+        self._callback = _CLOSURE(callback)
+        self.L.oracle_v3d_set_closure(self.h, self._callback, None)
+        self.t = 0.0
+
+    def step_ocean(self, dt, scheme=2, load0=None, load1=None):
+        """One coupled step under the direct load fields at its two ends."""
+        n = self.sle_grid[0].size * self.sle_grid[2]
+        zero = np.zeros(n)
+        self.closure.set_step_loads(self.t, zero if load0 is None else load0, self.t + dt,
+                                    zero if load1 is None else load1)
+        info = self.step(dt, scheme)
+        self.t += dt
+        return info
+
+    def sea_level(self):
+        """The last closure's relative sea level change (coefficients) and angular velocity."""
+        lmax = self.options.lmax
+        theta, w, nphi = self.sle_grid
+        last = self.closure.last
+        return expand_real(lmax, theta, w, nphi, last["sea_level_change"]), np.asarray(last["angular_velocity"])
 
 
 class OraclePerturbation(OracleStep):
