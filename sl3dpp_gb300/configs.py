@@ -39,6 +39,29 @@ def delta_coefficients(lmax: int, ldelta: int, rms: float, seed: int) -> np.ndar
     return c * (rms / np.sqrt(ms)) if ms > 0 else c
 
 
+def land_field_coefficients(lmax: int, seed: int, ldegree: int = 12) -> np.ndarray:
+    """A seeded smooth field (degrees 1..ldegree, amplitude 1/(l + 1)) whose
+    upper part becomes land: real spin-0 coefficients."""
+    rng = np.random.default_rng(seed)
+    c = np.zeros((lmax + 1) * (lmax + 2) // 2, dtype=np.complex128)
+    for l in range(1, min(lmax, ldegree) + 1):
+        for m in range(l + 1):
+            a = rng.standard_normal() + (1j * rng.standard_normal() if m else 0.0)
+            c[real_index(l, m)] = a / (l + 1)
+    return c
+
+
+def ocean_from_field(field: np.ndarray, weights: np.ndarray, nphi: int, land_fraction: float = 0.3) -> np.ndarray:
+    """The ocean function (1 ocean, 0 land) of thresholding a field on a
+    grid so that its largest values cover `land_fraction` of the area."""
+    area = np.repeat(np.asarray(weights)[:, None], nphi, axis=1).ravel()
+    order = np.argsort(np.asarray(field).ravel(), kind="stable")[::-1]
+    covered = np.cumsum(area[order]) / area.sum()
+    land = np.zeros(area.size)
+    land[order[covered <= land_fraction]] = 1.0
+    return 1.0 - land
+
+
 def delta_indicator(radius_nd: np.ndarray, top_depth: float = 100e3, bottom_depth: float = 670e3,
                     surface: float = EARTH_RADIUS) -> np.ndarray:
     """1 where a (non-dimensional) radius lies between the two depths."""

@@ -26,23 +26,11 @@ GAMMA = 0.29289321881345247560
 
 
 def ocean_mask(lmax, land_fraction=0.3, seed=11):
-    """A land mask by thresholding a seeded smooth field at the given
-    fraction of the grid's area (the ocean 1 where it is not land)."""
+    """The ocean of config 2's kind: land where a seeded smooth field is
+    highest, over the given fraction of the area."""
     theta, w, nphi = O.grid(lmax, 1.0)
-    rng = np.random.default_rng(seed)
-    size = (lmax + 1) * (lmax + 2) // 2
-    c = np.zeros(size, dtype=np.complex128)
-    for l in range(1, min(lmax, 12) + 1):
-        for m in range(l + 1):
-            a = rng.standard_normal() + (1j * rng.standard_normal() if m else 0.0)
-            c[l * (l + 1) // 2 + m] = a / (l + 1)
-    field = O.synthesise_real(lmax, theta, nphi, c).reshape(theta.size, nphi)
-    area = np.repeat(w[:, None], nphi, axis=1)
-    order = np.argsort(field, axis=None)[::-1]
-    cum = np.cumsum(area.ravel()[order]) / area.sum()
-    land = np.zeros(field.size)
-    land[order[cum <= land_fraction]] = 1.0
-    return 1.0 - land
+    field = O.synthesise_real(lmax, theta, nphi, configs.land_field_coefficients(lmax, seed))
+    return configs.ocean_from_field(field, w, nphi, land_fraction)
 
 
 def cap_field(lmax, sigma_scale, thickness, alpha=15.0):
