@@ -546,7 +546,7 @@ int sl3dgpu_v3d_ocean_grid(sl3dgpu_v3d* op, int* ntheta, int* nphi, double* thet
 /* One coupled step: the direct (non-ocean) load at the step's start and end
  * as host fields on the sea-level grid, non-dimensional surface density
  * (NULL: zero); the stages take their linear combination (detail::AtStage).
- * A dt = 0 step is Evolution3D::Start's instantaneous response. */
+ * A dt = 0 step is Evolution3D::Start's instantaneous response to load1. */
 int sl3dgpu_v3d_step_ocean(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme, const double* load0,
                            const double* load1, sl3dgpu_step_info* info);
 /* Evolution3D::Run with the ocean: node 0 the instantaneous response, then a

@@ -53,7 +53,7 @@ class OceanClosure:
         """detail::AtStage: the two ends' fields combined linearly in the
         stage's position t."""
         (t0, a), (t1, b) = self.loads
-        c = 0.0 if t1 == t0 else (t - t0) / (t1 - t0)
+        c = 1.0 if t1 == t0 else (t - t0) / (t1 - t0)  # a zero-length step: its end's load
         return (1.0 - c) * a + c * b
 
     def centrifugal(self, omega):

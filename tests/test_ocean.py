@@ -129,9 +129,13 @@ def test_gpu_effective_love_numbers_match_the_oracle(gpu):
     for scheme, length in [(1, 0.0), (1, GAMMA * dt), (0, dt)]:
         want = o.effective_love(scheme, length)
         got = g.effective_love(scheme, length)
-        flat = np.concatenate([got[k] for k in ("h", "k", "l", "ht", "kt", "lt")] +
-                              [np.array([got["hc"], got["kc"], got["m"], got["mc"]])])
-        assert np.max(np.abs(flat - want) / np.maximum(np.abs(want), 1e-300 + np.max(np.abs(want)) * 1e-6)) < 1e-10
+        n = lmax + 1
+        # each number family against its own largest value (k_c vanishes to
+        # rounding: a degree-0 mass redistribution leaves the outer potential)
+        for i, name in enumerate(("h", "k", "l", "ht", "kt", "lt")):
+            assert rel(got[name], want[i * n:(i + 1) * n]) < 1e-10, (scheme, length, name)
+        axial = np.array([got["hc"], got["kc"], got["m"], got["mc"]])
+        assert rel(axial, want[6 * n:]) < 1e-10, (scheme, length, axial, want[6 * n:])
 
 
 @pytest.mark.gpu
@@ -144,7 +148,7 @@ def test_gpu_coupled_steps_match_the_oracle(gpu, scheme, rotation):
     dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
     state = g.ZeroState()
     # node 0: the instantaneous response, then four steps of a growing cap
-    schedule = [(0.0, 0.0, 0.1)] + [(dt, 0.1 * n, 0.1 * (n + 1)) for n in range(1, 5)]
+    schedule = [(0.0, 0.1, 0.1)] + [(dt, 0.1 * n, 0.1 * (n + 1)) for n in range(1, 5)]
     for length, a, b in schedule:
         io = o.step_ocean(length, scheme, a * ice, b * ice)
         ig = g.StepOcean(state, length, scheme, a * ice, b * ice)
