@@ -517,6 +517,55 @@ int sl3dgpu_v3d_run_many(int count, sl3dgpu_v3d* const* ops, sl3dgpu_v3d_state* 
                          const double* const* times, const int* nodes, int scheme,
                          const double* const* loads, double* const* u, double* const* phi,
                          sl3dgpu_step_info* const* infos, int threads, int* statuses);
+/* ---- the open step (Viscoelastic3D::OpenStep, include/sl3dpp/Viscoelastic3D.hpp:440-640) ----
+ * One stage opened on the operator's own buffers, for a driver's own
+ * within-step iteration (one open step per operator at a time). Strain
+ * coefficients are device arrays in the device layout
+ * (sl3dgpu_v3d_layout's `spectral` complex values); solutions live in the
+ * operator and are read by sl3dgpu_v3d_surface / sl3dgpu_v3d_inertia_moment.
+ * start_step: StartStep of one stage (scheme 0 or 1, length dt) from the
+ * state; load0 (host coefficients, nullable) the load at the state's time
+ * when the state carries no strain. step_respond: Respond, the solutions of
+ * the memory and lateral force of a strain (NULL: the start strain), no
+ * channels. step_add_channels: AddChannels (host (l, m >= 0) coefficients,
+ * either nullable; a tide's degree-1 part refused). step_strain_of:
+ * StrainOf of the solutions. step_converge: Close under known channels, the
+ * operator's own fixed point (or conjugate gradients / the mixed form, as its
+ * options say) from the start strain; the strain (nullable device out).
+ * step_finish: Finish with a strain (NULL: the converged one), the state
+ * advanced in place; the step closes. relative_change: Converge's measure
+ * between two strains. */
+int sl3dgpu_v3d_start_step(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme, const double* load0);
+int sl3dgpu_v3d_step_start_strain(sl3dgpu_v3d* op, double* device_out);
+int sl3dgpu_v3d_step_respond(sl3dgpu_v3d* op, const double* strain);
+int sl3dgpu_v3d_step_add_channels(sl3dgpu_v3d* op, const double* load, const double* tide);
+int sl3dgpu_v3d_step_strain_of(sl3dgpu_v3d* op, double* device_out);
+int sl3dgpu_v3d_step_converge(sl3dgpu_v3d* op, const double* load, const double* tide, double* device_strain,
+                              sl3dgpu_step_info* info);
+int sl3dgpu_v3d_step_finish(sl3dgpu_v3d* op, const double* strain);
+int sl3dgpu_v3d_relative_change(sl3dgpu_v3d* op, const double* next, const double* now, double* out);
+
+/* ---- the grid coupling (GridCoupling, include/sl3dpp/GridCoupling.hpp:82-428) ----
+ * The maps between the operator's tensor fields and the degree systems, on
+ * device arrays: sizes (complex spectral coefficients, grid values at every
+ * node, spheroidal and toroidal solution values) from sl3dgpu_v3d_layout;
+ * degree l's solutions are [dof][l + 1] blocks at sl3dgpu_v3d_solution_layout's
+ * offsets. synthesise_tensor / analyse_tensor: Synthesise / Analyse of the
+ * spin -2, spin -1 (complex) and spin 0 (real) components at every node;
+ * degree_forces: SpheroidalForce / ToroidalForce of an analysed tensor into
+ * the systems' right-hand sides; strain_of_solutions: AddStrainOfSolution
+ * with the deviatoric components, the strain coefficients of solutions. */
+int sl3dgpu_v3d_layout(const sl3dgpu_v3d* op, long long* spectral, long long* grid_values, long long* spheroidal,
+                       long long* toroidal);
+int sl3dgpu_v3d_solution_layout(const sl3dgpu_v3d* op, int l, long long* sph_offset, int* sph_dofs,
+                                long long* tor_offset, int* tor_dofs);
+int sl3dgpu_v3d_synthesise_tensor(sl3dgpu_v3d* op, const double* spectral, double* c0, double* c1, double* r);
+int sl3dgpu_v3d_analyse_tensor(sl3dgpu_v3d* op, const double* c0, const double* c1, const double* r,
+                               double* spectral);
+int sl3dgpu_v3d_degree_forces(sl3dgpu_v3d* op, const double* spectral, double* spheroidal, double* toroidal);
+int sl3dgpu_v3d_strain_of_solutions(sl3dgpu_v3d* op, const double* spheroidal, const double* toroidal,
+                                    double* spectral);
+
 /* ---- the ocean closure (Evolution3D, src/Evolution3D.cpp:184-394) ----------
  * The coupled fixed point of a step under an ocean with frozen shorelines:
  * in every pass the surface responses of the degree solves (before the load

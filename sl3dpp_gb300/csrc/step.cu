@@ -280,6 +280,7 @@ class Viscoelastic3DGpu {
   int AnalyseWeighted(const GridTensor& in, const double* w, double2* spectral);  // accumulate, lateral nodes
   int WeightedPass(const double2* strain, double2* out);                           // accumulate, lateral nodes
   int Solve(const Flavour& f);
+  int Respond(const Flavour& f, const double2* strain, bool useStart);
   int Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma, const double2* tide,
            double2* next);
   // the running stage's tide coefficients at its start and end (null: none)
@@ -312,6 +313,42 @@ class Viscoelastic3DGpu {
   int ElasticStrain(const V3dState& st, const double2* sigma);
   int StepOnce(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
                const double2* sigmaEnd, sl3dgpu_step_info& info);
+  int StartStage(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart, Flavour** f);
+  int FinishStage(V3dState& out, double dt, int scheme);
+  int Adopt(V3dState& st);
+
+ public:
+  // The open step: one stage opened on the operator's buffers (s holds the
+  // start strain; rhsSph / rhsTor the last Respond's solutions).
+  struct OpenStage {
+    bool open = false;
+    V3dState* st = nullptr;
+    Flavour* f = nullptr;
+    int scheme = 0;
+    double dt = 0.0;
+  } opened;
+  int OpenStart(V3dState& st, double dt, int scheme, const double* load0);
+  int OpenCheck() const;
+  int OpenChannels(const double* load, const double* tide);
+  int OpenConverge(const double* load, const double* tide, sl3dgpu_step_info* info);
+  int OpenFinish(const double2* strain);
+  int OpenRespond(const double2* strain) {
+    SL3D_TRY(OpenCheck());
+    SL3D_TRY(Respond(*opened.f, strain, strain == nullptr));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    return SL3DGPU_OK;
+  }
+  // GridCoupling's maps on the operator's nodes and grid (device arrays in
+  // the device layouts): Synthesise / Analyse of a tensor field, the degree
+  // forces of an analysed tensor, the strain of solutions.
+  int TensorSynthesise(const double2* spectral, double2* c0, double2* c1, double* r);
+  int TensorAnalyse(const double2* c0, const double2* c1, const double* r, double2* spectral);
+  int DegreeForces(const double2* spectral, double2* sph, double2* tor);
+  int StrainOfSolutions(const double2* sph, const double2* tor, double2* spectral);
+  int Change(const double2* next, const double2* now, double* out) {
+    SL3D_TRY(RelativeChange(next, now, out));
+    return SL3DGPU_OK;
+  }
   double2* Block(double2* base, int spin) const {
     return base + (spin == -2 ? 0 : spin == -1 ? rows0 * P : (rows0 + rows1) * P);
   }
@@ -849,9 +886,10 @@ int Viscoelastic3DGpu::SolveColumns(const Flavour& f, double2* sph, double2* tor
                         f.nTorChol, f.bands.p, f.pivots.p, torD, f.scales.p, 0, stream);
 }
 
-int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma,
-                            const double2* tide,
-                            double2* next) {
+// Respond (Viscoelastic3D.hpp OpenStep::Respond): the solutions of the
+// memory and lateral force of a strain (the start strain's force, already
+// analysed, when useStart) through the flavour's systems, no channels.
+int Viscoelastic3DGpu::Respond(const Flavour& f, const double2* strain, bool useStart) {
   const double2* force = analysedStart.p;
   if (!useStart) {
     SL3D_CUDA(cudaMemcpyAsync(analysed.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
@@ -863,7 +901,13 @@ int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useSta
   SL3D_CUDA(cudaMemsetAsync(rhsTor.p, 0, std::max<long long>(rhsTorComplex, 1) * sizeof(double2), stream));
   LaunchForces(geo, force, rhsSph.p, rhsTor.p, stream);
   SL3D_CHECK_LAUNCH();
-  SL3D_TRY(Solve(f));
+  return Solve(f);
+}
+
+int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useStart, const double2* sigma,
+                            const double2* tide,
+                            double2* next) {
+  SL3D_TRY(Respond(f, strain, useStart));
   if (ocean.on) {
     // the pass's closure sets its load and tide channels
     SL3D_TRY(Closure(f));
@@ -975,10 +1019,15 @@ int Viscoelastic3DGpu::ElasticStrain(const V3dState& st, const double2* sigma) {
   return Pass(*elastic, nullptr, true, sigma, tideStart, s.p);
 }
 
-int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
-                                const double2* sigmaEnd, sl3dgpu_step_info& info) {
+// StartStep (Viscoelastic3D.cpp:1223-1378): the stage's flavour, the start
+// strain in s, the weights, the decayed memory (into `out`), the lateral
+// weight and the fixed force, analysed; the first pass's force in
+// analysedStart.
+int Viscoelastic3DGpu::StartStage(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
+                                  Flavour** flavourOut) {
   Flavour* f = nullptr;
   SL3D_TRY(FlavourOf(scheme, dt, &f));
+  *flavourOut = f;
   SL3D_TRY(AdaptState(in));
   const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
   const long long begin = p0 * fieldSize, end = static_cast<long long>(lateralEnd) * fieldSize;
@@ -1037,19 +1086,15 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   SL3D_CUDA(cudaMemcpyAsync(analysedStart.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
                             stream));
   SL3D_TRY(AnalyseWeighted(*d0, weight.p, analysedStart.p));
+  return SL3DGPU_OK;
+}
 
-  info = sl3dgpu_step_info{};
-  if (options.solver == 1) {
-    SL3D_TRY(ConvergeConjugateGradients(*f, sigmaEnd, info));
-  } else if (options.precision == 1) {
-    LaunchCast(values, weight.p, weight32.p, stream);
-    SL3D_CHECK_LAUNCH();
-    SL3D_TRY(ConvergeMixed(*f, sigmaEnd, info));
-  } else {
-    SL3D_TRY(Converge(*f, sigmaEnd, info));
-  }
-  // Finish: the strain on the grid and the memory advanced at the lateral
-  // nodes, the coefficients advanced at the others.
+// Finish (Viscoelastic3D.cpp:1885-1914) for the strain coefficients in s:
+// the strain on the grid and the memory advanced at the lateral nodes, the
+// coefficients advanced at the others, the state's coefficients cached.
+int Viscoelastic3DGpu::FinishStage(V3dState& out, double dt, int scheme) {
+  const int p0 = lateralFirst, count = lateralEnd - lateralFirst;
+  const long long begin = p0 * fieldSize, end = static_cast<long long>(lateralEnd) * fieldSize;
   SL3D_TRY(SynthesiseRange(s.p, out.strain, p0, count));
   for (int k = 0; k < K && count > 0; ++k) {
     LaunchAdvance(end - begin, beta[k].p + begin, out.strain.c0.p + begin, out.strain.c1.p + begin,
@@ -1067,6 +1112,23 @@ int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int sche
   out.latFirst = lateralFirst;
   out.latEnd = lateralEnd;
   return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::StepOnce(V3dState& in, V3dState& out, double dt, int scheme, const double2* sigmaStart,
+                                const double2* sigmaEnd, sl3dgpu_step_info& info) {
+  Flavour* f = nullptr;
+  SL3D_TRY(StartStage(in, out, dt, scheme, sigmaStart, &f));
+  info = sl3dgpu_step_info{};
+  if (options.solver == 1) {
+    SL3D_TRY(ConvergeConjugateGradients(*f, sigmaEnd, info));
+  } else if (options.precision == 1) {
+    LaunchCast(values, weight.p, weight32.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(ConvergeMixed(*f, sigmaEnd, info));
+  } else {
+    SL3D_TRY(Converge(*f, sigmaEnd, info));
+  }
+  return FinishStage(out, dt, scheme);
 }
 
 // Converge (Viscoelastic3D.cpp:1916-1974): FP64 passes from the start
@@ -2176,6 +2238,14 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   guessArmed = false;  // a warm start serves one step
   stageGuess = nullptr;
   tideStart = tideEnd = nullptr;
+  SL3D_TRY(Adopt(st));
+  if (infoOut) *infoOut = info;
+  return SL3DGPU_OK;
+}
+
+// The state takes the finished stage's buffers (the scratch set), keeping
+// its coefficients as the step before's under warm_start 1.
+int Viscoelastic3DGpu::Adopt(V3dState& st) {
   if (options.warm_start == 1 && st.hasCoeffs) {
     SL3D_CUDA(cudaMemcpyAsync(st.prev.p, st.coeffs.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
                               stream));
@@ -2189,8 +2259,148 @@ int Viscoelastic3DGpu::Step(V3dState& st, double dt, int scheme, const double* l
   std::swap(st.latEnd, scratch.latEnd);
   st.hasStrain = st.hasCoeffs = true;
   SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+// -- GridCoupling's maps (include/sl3dpp/GridCoupling.hpp:82-428) ---------------------------------------
+
+int Viscoelastic3DGpu::TensorSynthesise(const double2* spectral, double2* c0, double2* c1, double* r) {
+  SL3D_TRY(Synthesise(spectral, dGrid));
+  SL3D_CUDA(cudaMemcpyAsync(c0, dGrid.c0.p, values * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_CUDA(cudaMemcpyAsync(c1, dGrid.c1.p, values * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_CUDA(cudaMemcpyAsync(r, dGrid.r.p, values * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::TensorAnalyse(const double2* c0, const double2* c1, const double* r, double2* spectral) {
+  SL3D_CUDA(cudaMemcpyAsync(dGrid.c0.p, c0, values * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_CUDA(cudaMemcpyAsync(dGrid.c1.p, c1, values * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_CUDA(cudaMemcpyAsync(dGrid.r.p, r, values * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  SL3D_TRY(Analyse(dGrid, spectral));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::DegreeForces(const double2* spectral, double2* sph, double2* tor) {
+  SL3D_CUDA(cudaMemsetAsync(sph, 0, rhsSphComplex * sizeof(double2), stream));
+  if (rhsTorComplex > 0) SL3D_CUDA(cudaMemsetAsync(tor, 0, rhsTorComplex * sizeof(double2), stream));
+  LaunchForces(geo, spectral, sph, tor, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::StrainOfSolutions(const double2* sph, const double2* tor, double2* spectral) {
+  LaunchStrain(geo, sph, tor, spectral, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+// -- the open step (Viscoelastic3D::OpenStep, include/sl3dpp/Viscoelastic3D.hpp:440-640) ------------
+
+int Viscoelastic3DGpu::OpenStart(V3dState& st, double dt, int scheme, const double* load0) {
+  if (opened.open) {
+    SetError("v3d: a step is open on this operator: finish it first (one open step per operator)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (!(dt >= 0.0) || scheme < 0 || scheme > 1 || staticMode || ocean.on) {
+    SetError("v3d: an open step is one stage (scheme 0 or 1, dt >= 0) of the step operator without an ocean");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  const double2* s0 = nullptr;
+  if (load0 != nullptr) {
+    SL3D_CUDA(cudaMemcpyAsync(sigma0.p, load0, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    s0 = sigma0.p;
+  }
+  history.clear();
+  tideStart = tideEnd = nullptr;
+  ocean.cStart = 0.0;
+  ocean.cEnd = 1.0;
+  Flavour* f = nullptr;
+  SL3D_TRY(StartStage(st, scratch, dt, scheme, s0, &f));
+  opened = OpenStage{true, &st, f, scheme, dt};
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::OpenCheck() const {
+  if (!opened.open) {
+    SetError("v3d: no open step (sl3dgpu_v3d_start_step)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::OpenChannels(const double* load, const double* tide) {
+  SL3D_TRY(OpenCheck());
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  const double2* sigma = nullptr;
+  const double2* psi = nullptr;
+  if (load != nullptr) {
+    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, load, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    sigma = sigma1.p;
+  }
+  if (tide != nullptr) {
+    const double2* t = reinterpret_cast<const double2*>(tide);
+    if (t[1].x != 0.0 || t[1].y != 0.0 || t[2].x != 0.0 || t[2].y != 0.0) {
+      SetError("v3d: a tide channel has no degree-1 part: tides are taken relative to the centre of mass");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+    if (tideDev1.n != lm) SL3D_CUDA(tideDev1.Alloc(lm));
+    SL3D_CUDA(cudaMemcpyAsync(tideDev1.p, tide, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    psi = tideDev1.p;
+  }
+  if (sigma != nullptr || psi != nullptr) {
+    LaunchAddLoad(geo, sigma, opened.f->units.p, opened.f->unitOffset.p, rhsSph.p, stream, psi,
+                  opened.f->tideUnits.p);
+    SL3D_CHECK_LAUNCH();
+  }
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::OpenConverge(const double* load, const double* tide, sl3dgpu_step_info* infoOut) {
+  SL3D_TRY(OpenCheck());
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  const double2* sigma = nullptr;
+  if (load != nullptr) {
+    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, load, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    sigma = sigma1.p;
+  }
+  tideEnd = nullptr;
+  if (tide != nullptr) {
+    if (tideDev1.n != lm) SL3D_CUDA(tideDev1.Alloc(lm));
+    SL3D_CUDA(cudaMemcpyAsync(tideDev1.p, tide, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    tideEnd = tideDev1.p;
+  }
+  sl3dgpu_step_info info{};
+  history.clear();
+  const Flavour& f = *opened.f;
+  if (options.solver == 1) {
+    SL3D_TRY(ConvergeConjugateGradients(f, sigma, info));
+  } else if (options.precision == 1) {
+    LaunchCast(values, weight.p, weight32.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(ConvergeMixed(f, sigma, info));
+  } else {
+    SL3D_TRY(Converge(f, sigma, info));
+  }
+  tideEnd = nullptr;
+  SL3D_CUDA(cudaStreamSynchronize(stream));
   if (infoOut) *infoOut = info;
   return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::OpenFinish(const double2* strain) {
+  SL3D_TRY(OpenCheck());
+  if (strain != nullptr)
+    SL3D_CUDA(cudaMemcpyAsync(s.p, strain, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_TRY(FinishStage(scratch, opened.dt, opened.scheme));
+  V3dState& st = *opened.st;
+  opened = OpenStage{};
+  return Adopt(st);
 }
 
 int Viscoelastic3DGpu::Surface(int component, double* out, bool deviceOut) {
@@ -2429,6 +2639,162 @@ extern "C" int sl3dgpu_v3d_state_coefficients_host(const sl3dgpu_v3d* h, const s
   SL3D_CUDA(cudaStreamSynchronize(h->op.stream));  // the legacy-stream copy does not wait for it
   SL3D_CUDA(cudaMemcpy(out, state->st.coeffs.p, h->op.spectralComplex * sizeof(double2), cudaMemcpyDeviceToHost));
   return SL3DGPU_OK;
+}
+
+// -- the open step and the grid coupling --------------------------------------------------------------
+
+namespace {
+int NeedStepOperator(const sl3dgpu_v3d* h) {
+  if (h == nullptr || h->op.staticMode) {
+    SetError("v3d: a step operator (not the static problem's) is required");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return SL3DGPU_OK;
+}
+}  // namespace
+
+extern "C" int sl3dgpu_v3d_start_step(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, double dt, int scheme,
+                                      const double* load0) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (state == nullptr) {
+    SetError("v3d: null state");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.OpenStart(state->st, dt, scheme, load0);
+}
+
+extern "C" int sl3dgpu_v3d_step_start_strain(sl3dgpu_v3d* h, double* device_out) {
+  SL3D_TRY(NeedStepOperator(h));
+  SL3D_TRY(h->op.OpenCheck());
+  if (device_out == nullptr) {
+    SetError("v3d: null output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto& op = h->op;
+  SL3D_CUDA(cudaMemcpyAsync(device_out, op.s.p, op.spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            op.stream));
+  SL3D_CUDA(cudaStreamSynchronize(op.stream));
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_step_respond(sl3dgpu_v3d* h, const double* strain) {
+  SL3D_TRY(NeedStepOperator(h));
+  return h->op.OpenRespond(reinterpret_cast<const double2*>(strain));
+}
+
+extern "C" int sl3dgpu_v3d_step_add_channels(sl3dgpu_v3d* h, const double* load, const double* tide) {
+  SL3D_TRY(NeedStepOperator(h));
+  return h->op.OpenChannels(load, tide);
+}
+
+extern "C" int sl3dgpu_v3d_step_strain_of(sl3dgpu_v3d* h, double* device_out) {
+  SL3D_TRY(NeedStepOperator(h));
+  SL3D_TRY(h->op.OpenCheck());
+  if (device_out == nullptr) {
+    SetError("v3d: null output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  auto& op = h->op;
+  return op.StrainOfSolutions(op.rhsSph.p, op.rhsTor.p, reinterpret_cast<double2*>(device_out));
+}
+
+extern "C" int sl3dgpu_v3d_step_converge(sl3dgpu_v3d* h, const double* load, const double* tide,
+                                         double* device_strain, sl3dgpu_step_info* info) {
+  SL3D_TRY(NeedStepOperator(h));
+  auto& op = h->op;
+  SL3D_TRY(op.OpenConverge(load, tide, info));
+  if (device_strain != nullptr) {
+    SL3D_CUDA(cudaMemcpyAsync(device_strain, op.s.p, op.spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                              op.stream));
+    SL3D_CUDA(cudaStreamSynchronize(op.stream));
+  }
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_step_finish(sl3dgpu_v3d* h, const double* strain) {
+  SL3D_TRY(NeedStepOperator(h));
+  return h->op.OpenFinish(reinterpret_cast<const double2*>(strain));
+}
+
+extern "C" int sl3dgpu_v3d_relative_change(sl3dgpu_v3d* h, const double* next, const double* now, double* out) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (next == nullptr || now == nullptr || out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.Change(reinterpret_cast<const double2*>(next), reinterpret_cast<const double2*>(now), out);
+}
+
+extern "C" int sl3dgpu_v3d_layout(const sl3dgpu_v3d* h, long long* spectral, long long* grid_values,
+                                  long long* spheroidal, long long* toroidal) {
+  if (h == nullptr) {
+    SetError("v3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& op = h->op;
+  if (spectral) *spectral = op.spectralComplex;
+  if (grid_values) *grid_values = op.values;
+  if (spheroidal) *spheroidal = op.rhsSphComplex;
+  if (toroidal) *toroidal = op.rhsTorComplex;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_solution_layout(const sl3dgpu_v3d* h, int l, long long* sph_offset, int* sph_dofs,
+                                           long long* tor_offset, int* tor_dofs) {
+  if (h == nullptr || l < 0 || l > h->op.options.lmax) {
+    SetError("v3d: a handle and 0 <= l <= lmax");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& d = h->op.degrees[l];
+  if (sph_offset) *sph_offset = d.sphRhs;
+  if (sph_dofs) *sph_dofs = d.sphNdof;
+  if (tor_offset) *tor_offset = d.torRhs;
+  if (tor_dofs) *tor_dofs = d.torNdof;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_synthesise_tensor(sl3dgpu_v3d* h, const double* spectral, double* c0, double* c1,
+                                             double* r) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (spectral == nullptr || c0 == nullptr || c1 == nullptr || r == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.TensorSynthesise(reinterpret_cast<const double2*>(spectral), reinterpret_cast<double2*>(c0),
+                                reinterpret_cast<double2*>(c1), r);
+}
+
+extern "C" int sl3dgpu_v3d_analyse_tensor(sl3dgpu_v3d* h, const double* c0, const double* c1, const double* r,
+                                          double* spectral) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (spectral == nullptr || c0 == nullptr || c1 == nullptr || r == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.TensorAnalyse(reinterpret_cast<const double2*>(c0), reinterpret_cast<const double2*>(c1), r,
+                             reinterpret_cast<double2*>(spectral));
+}
+
+extern "C" int sl3dgpu_v3d_degree_forces(sl3dgpu_v3d* h, const double* spectral, double* spheroidal,
+                                         double* toroidal) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (spectral == nullptr || spheroidal == nullptr || (toroidal == nullptr && h->op.rhsTorComplex > 0)) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.DegreeForces(reinterpret_cast<const double2*>(spectral), reinterpret_cast<double2*>(spheroidal),
+                            reinterpret_cast<double2*>(toroidal));
+}
+
+extern "C" int sl3dgpu_v3d_strain_of_solutions(sl3dgpu_v3d* h, const double* spheroidal, const double* toroidal,
+                                               double* spectral) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (spectral == nullptr || spheroidal == nullptr || (toroidal == nullptr && h->op.rhsTorComplex > 0)) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StrainOfSolutions(reinterpret_cast<const double2*>(spheroidal),
+                                 reinterpret_cast<const double2*>(toroidal), reinterpret_cast<double2*>(spectral));
 }
 
 extern "C" int sl3dgpu_v3d_set_ocean(sl3dgpu_v3d* h, const sl3dgpu_v3d_ocean* ocean) {

@@ -121,6 +121,21 @@ def _signatures():
         "sl3dgpu_v3d_run_ocean": (i, [v, v, P_double, i, i, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_sea_level": (i, [v, v, v, ctypes.POINTER(SleResult)]),
         "sl3dgpu_v3d_effective_love": (i, [v, i, d, P_double]),
+        "sl3dgpu_v3d_start_step": (i, [v, v, d, i, v]),
+        "sl3dgpu_v3d_step_start_strain": (i, [v, v]),
+        "sl3dgpu_v3d_step_respond": (i, [v, v]),
+        "sl3dgpu_v3d_step_add_channels": (i, [v, v, v]),
+        "sl3dgpu_v3d_step_strain_of": (i, [v, v]),
+        "sl3dgpu_v3d_step_converge": (i, [v, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_step_finish": (i, [v, v]),
+        "sl3dgpu_v3d_relative_change": (i, [v, v, v, P_double]),
+        "sl3dgpu_v3d_layout": (i, [v] + [ctypes.POINTER(ctypes.c_longlong)] * 4),
+        "sl3dgpu_v3d_solution_layout": (i, [v, i, ctypes.POINTER(ctypes.c_longlong), P_int,
+                                            ctypes.POINTER(ctypes.c_longlong), P_int]),
+        "sl3dgpu_v3d_synthesise_tensor": (i, [v, v, v, v, v]),
+        "sl3dgpu_v3d_analyse_tensor": (i, [v, v, v, v, v]),
+        "sl3dgpu_v3d_degree_forces": (i, [v, v, v, v]),
+        "sl3dgpu_v3d_strain_of_solutions": (i, [v, v, v, v]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -327,6 +342,60 @@ class Viscoelastic3D:
         check(lib().sl3dgpu_v3d_inertia_moment(self._h, ctypes.byref(out)))
         return out.value
 
+    def StartStep(self, state: State, dt: float, scheme=1, load0=None) -> OpenStep:
+        """Viscoelastic3D::StartStep: one stage opened for a driver's own iteration."""
+        return OpenStep(self, state, dt, scheme, load0)
+
+    def layout(self) -> dict:
+        """The device layouts' sizes: complex spectral coefficients, grid values
+        (every node), spheroidal and toroidal solution values."""
+        vals = [ctypes.c_longlong() for _ in range(4)]
+        check(lib().sl3dgpu_v3d_layout(self._h, *(ctypes.byref(x) for x in vals)))
+        return dict(zip(("spectral", "grid", "spheroidal", "toroidal"), (x.value for x in vals)))
+
+    def solution_layout(self, l: int) -> dict:
+        so, to = ctypes.c_longlong(), ctypes.c_longlong()
+        sn, tn = ctypes.c_int(), ctypes.c_int()
+        check(lib().sl3dgpu_v3d_solution_layout(self._h, l, ctypes.byref(so), ctypes.byref(sn), ctypes.byref(to),
+                                                ctypes.byref(tn)))
+        return {"sph_offset": so.value, "sph_dofs": sn.value, "tor_offset": to.value, "tor_dofs": tn.value}
+
+    # -- GridCoupling's maps (CUDA tensors in the device layouts)
+
+    def SynthesiseTensor(self, spectral):
+        import torch
+
+        n = self.layout()["grid"]
+        c0 = torch.empty(n, dtype=torch.complex128, device="cuda")
+        c1 = torch.empty(n, dtype=torch.complex128, device="cuda")
+        r = torch.empty(n, dtype=torch.float64, device="cuda")
+        check(lib().sl3dgpu_v3d_synthesise_tensor(self._h, spectral.data_ptr(), c0.data_ptr(), c1.data_ptr(),
+                                                  r.data_ptr()))
+        return c0, c1, r
+
+    def AnalyseTensor(self, c0, c1, r):
+        import torch
+
+        out = torch.empty(self.layout()["spectral"], dtype=torch.complex128, device="cuda")
+        check(lib().sl3dgpu_v3d_analyse_tensor(self._h, c0.data_ptr(), c1.data_ptr(), r.data_ptr(), out.data_ptr()))
+        return out
+
+    def DegreeForces(self, spectral):
+        import torch
+
+        lay = self.layout()
+        sph = torch.empty(lay["spheroidal"], dtype=torch.complex128, device="cuda")
+        tor = torch.empty(max(lay["toroidal"], 1), dtype=torch.complex128, device="cuda")
+        check(lib().sl3dgpu_v3d_degree_forces(self._h, spectral.data_ptr(), sph.data_ptr(), tor.data_ptr()))
+        return sph, tor
+
+    def StrainOfSolutions(self, sph, tor):
+        import torch
+
+        out = torch.empty(self.layout()["spectral"], dtype=torch.complex128, device="cuda")
+        check(lib().sl3dgpu_v3d_strain_of_solutions(self._h, sph.data_ptr(), tor.data_ptr(), out.data_ptr()))
+        return out
+
     # -- the ocean closure (Evolution3D's Coupled::Closure, frozen shorelines)
 
     def ocean_grid(self):
@@ -386,6 +455,66 @@ class Viscoelastic3D:
         love = {n: out[i * (L + 1):(i + 1) * (L + 1)].copy() for i, n in enumerate(names)}
         love.update(hc=out[6 * (L + 1)], kc=out[6 * (L + 1) + 1], m=out[6 * (L + 1) + 2], mc=out[6 * (L + 1) + 3])
         return love
+
+
+class OpenStep:
+    """Viscoelastic3D::OpenStep (include/sl3dpp/Viscoelastic3D.hpp:440-640): one
+    stage opened on the operator's buffers for a driver's own within-step
+    iteration. Strain coefficients are CUDA complex128 tensors in the device
+    layout; the solutions stay in the operator (Surface, InertiaMoment read
+    them)."""
+
+    def __init__(self, op: "Viscoelastic3D", state: State, dt: float, scheme=1, load0=None):
+        import torch
+
+        self.op, self.state = op, state
+        code = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        a = None if load0 is None else np.ascontiguousarray(load0, dtype=np.complex128)
+        check(lib().sl3dgpu_v3d_start_step(op._h, state._h, float(dt), code, None if a is None else a.ctypes.data))
+        self.size = op.layout()["spectral"]
+        self._torch = torch
+
+    def _new(self):
+        return self._torch.empty(self.size, dtype=self._torch.complex128, device="cuda")
+
+    def StartStrain(self):
+        out = self._new()
+        check(lib().sl3dgpu_v3d_step_start_strain(self.op._h, out.data_ptr()))
+        return out
+
+    def Respond(self, strain=None) -> None:
+        """The channel-free solutions of a strain (None: the start strain)."""
+        check(lib().sl3dgpu_v3d_step_respond(self.op._h, None if strain is None else strain.data_ptr()))
+
+    def AddChannels(self, load=None, tide=None) -> None:
+        a = None if load is None else np.ascontiguousarray(load, dtype=np.complex128)
+        b = None if tide is None else np.ascontiguousarray(tide, dtype=np.complex128)
+        check(lib().sl3dgpu_v3d_step_add_channels(self.op._h, None if a is None else a.ctypes.data,
+                                                  None if b is None else b.ctypes.data))
+
+    def StrainOf(self):
+        out = self._new()
+        check(lib().sl3dgpu_v3d_step_strain_of(self.op._h, out.data_ptr()))
+        return out
+
+    def RelativeChange(self, next_, now) -> float:
+        out = ctypes.c_double()
+        check(lib().sl3dgpu_v3d_relative_change(self.op._h, next_.data_ptr(), now.data_ptr(), ctypes.byref(out)))
+        return out.value
+
+    def Close(self, load=None, tide=None):
+        """The stage under known channels by the operator's own iteration."""
+        a = None if load is None else np.ascontiguousarray(load, dtype=np.complex128)
+        b = None if tide is None else np.ascontiguousarray(tide, dtype=np.complex128)
+        out = self._new()
+        info = StepInfo()
+        check(lib().sl3dgpu_v3d_step_converge(self.op._h, None if a is None else a.ctypes.data,
+                                              None if b is None else b.ctypes.data, out.data_ptr(),
+                                              ctypes.byref(info)))
+        return out, info
+
+    def Finish(self, strain=None) -> None:
+        check(lib().sl3dgpu_v3d_step_finish(self.op._h, None if strain is None else strain.data_ptr()))
 
 
 class Evolution3D:
