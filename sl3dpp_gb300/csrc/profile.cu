@@ -75,6 +75,10 @@ void End(int kind, cudaStream_t stream, double flops, double bytes) {
   }
 }
 
+bool TimingOn() { return timing.load(std::memory_order_relaxed); }
+long long Launches() { return launches.load(std::memory_order_relaxed); }
+void AddLaunches(long long n) { launches.fetch_add(n, std::memory_order_relaxed); }
+
 }  // namespace sl3dgpu::prof
 
 using namespace sl3dgpu;

@@ -29,6 +29,12 @@ enum Kind {
 void Begin(int kind, cudaStream_t stream);
 // Records the end event of the launch begun last on this kind, with its work.
 void End(int kind, cudaStream_t stream, double flops, double bytes);
+// Whether per-kind event timing is on (a CUDA graph cannot hold its events).
+bool TimingOn();
+// The launch count, and launches made by a replayed graph (or a capture's,
+// taken back: captured kernels do not run then).
+long long Launches();
+void AddLaunches(long long n);
 
 struct Scope {
   int kind;

@@ -25,6 +25,8 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -35,6 +37,7 @@
 
 #include "assemble.cuh"
 #include "host/earth.hpp"
+#include "profile.cuh"
 #include "sealevel.cuh"
 #include "sht.cuh"
 #include "step_kernels.cuh"
@@ -167,6 +170,21 @@ class Viscoelastic3DGpu {
   std::vector<Dev<__nv_bfloat16>> dG32, dF32;  // the correction's history, BF16
   Dev<__nv_bfloat16*> dG32Ptr, dF32Ptr;
   std::vector<double> correctionHistory;  // the last step's FP32 pass changes
+  // The FP32 correction's loop as a CUDA graph: a while node over one pass,
+  // its relative change, the device-side decision (CorrectionControl) and
+  // the mixer's kernels, rebuilt when anything it captured moved (keyed by
+  // the flavour, the lateral range and every buffer it reads or writes).
+  struct CorrectionGraph {
+    std::vector<long long> key;
+    cudaGraphExec_t exec = nullptr;
+    long long launchesPerPass = 0;
+  };
+  std::vector<CorrectionGraph> correctionGraphs;
+  Dev<CorrectionControl> correctionControl;
+  bool useGraphs = true;  // SL3DGPU_NO_GRAPHS=1 keeps the loop on the host
+  std::vector<long long> CorrectionKey(const Flavour& f) const;
+  int CorrectionGraphFor(const Flavour& f, CorrectionGraph** out);
+  int CaptureCorrectionBody(const Flavour& f, cudaGraphConditionalHandle handle);
 
   // conjugate gradients (solver 1): forces, iterate, residual, preconditioned
   // residual, direction and product, each the spheroidal then the toroidal
@@ -232,6 +250,8 @@ class Viscoelastic3DGpu {
   int SeaLevel(double* coefficients, double* omega, sl3dgpu_sle_result* result);
 
   ~Viscoelastic3DGpu() {
+    for (auto& g : correctionGraphs)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
     if (hostResult) cudaFreeHost(hostResult);
     if (hostMix) cudaFreeHost(hostMix);
     if (stream) cudaStreamDestroy(stream);
@@ -358,6 +378,7 @@ class Viscoelastic3DGpu {
 
 int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl3dgpu_v3d_options& opt,
                               bool staticPerturbation) {
+  if (const char* off = std::getenv("SL3DGPU_NO_GRAPHS"); off != nullptr && off[0] == '1') useGraphs = false;
   options = opt;
   staticMode = staticPerturbation;
   if (opt.lmax < 2 || opt.ngll < 2 || !(opt.oversampling >= 1.0) || opt.anderson_memory > 8 ||
@@ -703,6 +724,8 @@ int Viscoelastic3DGpu::SetDelta(const double* samples, bool onDevice) {
 // -- flavours: assembly on the host (once), factorisation on the device ----------------------------
 
 int Viscoelastic3DGpu::BuildFlavour(const host::PointShear& shear, Flavour& f) {
+  static std::atomic<long long> built{0};
+  f.id = ++built;
   SystemsInput in;
   in.material = &deviceMaterial;
   in.plan = &plan;
@@ -1733,6 +1756,114 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
 // reads e at the lateral nodes only, so the iteration runs on their compact
 // columns; e at every node is B e + r of the last pass's solutions, left in
 // e32 for s += e.
+// What a captured correction loop depends on: the flavour, the lateral
+// range, the mixer's memory and every buffer its kernels were given.
+std::vector<long long> Viscoelastic3DGpu::CorrectionKey(const Flavour& f) const {
+  auto at = [](const void* p) { return static_cast<long long>(reinterpret_cast<uintptr_t>(p)); };
+  return {f.id, f.windowFirst, f.windowEnd, lateralFirst, lateralEnd, compactComplex, CorrectionMemory(),
+          mixer32Memory, at(eL.p), at(eNextL.p), at(rL.p), at(analysedL.p), at(rhsSph32.p), at(rhsTor32.p),
+          at(spectra32A.p), at(spectra32B.p), at(weight32.p), at(xPrev32.p), at(fPrev32.p), at(dG32Ptr.p),
+          at(dF32Ptr.p), at(gram32.p), at(mixPartial.p), at(mixSums.p), at(gammaOut.p), at(changePartial.p),
+          at(changeResult.p), at(correctionControl.p), at(dDegreesL.p), at(dElemFirstNodeL.p),
+          at(f.wSphChol.p), at(f.wSphLu.p), at(f.wTorChol.p)};
+}
+
+// One pass of the loop and its decision, enqueued on the capturing stream.
+int Viscoelastic3DGpu::CaptureCorrectionBody(const Flavour& f, cudaGraphConditionalHandle handle) {
+  SL3D_TRY(Pass32(f, eL.p, eNextL.p));
+  LaunchRelativeChange(reinterpret_cast<const float*>(eNextL.p), reinterpret_cast<const float*>(eL.p),
+                       2 * compactComplex, changePartial.p, kChangeBlocks, changeResult.p, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchCorrectionControl(correctionControl.p, changeResult.p, handle, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchCopyIfPlain(correctionControl.p, eNextL.p, eL.p, compactComplex, stream);
+  SL3D_CHECK_LAUNCH();
+  const int memory = CorrectionMemory();
+  if (memory <= 0) return SL3DGPU_OK;
+  LaunchGramResetIf(correctionControl.p, gram32.p, memory, stream);
+  SL3D_CHECK_LAUNCH();
+  MixerArgsT<float> a{};
+  a.n = 2 * compactComplex;
+  a.memory = memory;
+  a.m = memory;  // the kernels' instance; the runtime m comes from the control
+  a.slot = 0;
+  a.x = reinterpret_cast<float*>(eL.p);
+  a.gx = reinterpret_cast<const float*>(eNextL.p);
+  a.xPrev = xPrev32.p;
+  a.fPrev = fPrev32.p;
+  a.dG = dG32Ptr.p;
+  a.dF = dF32Ptr.p;
+  a.partial = mixPartial.p;
+  a.blocks = static_cast<int>(std::min<long long>(kMixBlocks32, a.n));
+  a.gamma = gammaOut.p;
+  a.live = reinterpret_cast<const int*>(correctionControl.p);
+  LaunchMixerFirst(a, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchMixerSweep(a, mixSums.p, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchMixerGram(gram32.p, memory, 0, memory, mixSums.p, gammaOut.p, stream, a.live);
+  SL3D_CHECK_LAUNCH();
+  LaunchMixerMix(a, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchMixerAdvanceIf(correctionControl.p, stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+// The loop's graph for the flavour: found by key, else captured (a while
+// node whose body is one pass and its decision) and instantiated.
+int Viscoelastic3DGpu::CorrectionGraphFor(const Flavour& f, CorrectionGraph** out) {
+  if (CorrectionMemory() > kMixMaxMemory) return SL3DGPU_ERR_ARGUMENT;
+  if (correctionControl.n == 0) SL3D_CUDA(correctionControl.Alloc(1));
+  if (CorrectionMemory() > 0 && (mixer32Memory != CorrectionMemory() || mixer32Size != 2 * compactComplex))
+    SL3D_TRY(Mixer32Reset());  // the history buffers the graph will hold
+  const auto key = CorrectionKey(f);
+  for (auto& g : correctionGraphs)
+    if (g.key == key) {
+      *out = &g;
+      return SL3DGPU_OK;
+    }
+  cudaGraph_t graph = nullptr;
+  SL3D_CUDA(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle handle;
+  cudaGraphNodeParams params{};
+  cudaGraphNode_t node;
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;
+  auto fail = [&](int status) {
+    cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return status;
+  };
+  if (cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+    return fail(SL3DGPU_ERR_CUDA);
+  params.type = cudaGraphNodeTypeConditional;
+  params.conditional.handle = handle;
+  params.conditional.type = cudaGraphCondTypeWhile;
+  params.conditional.size = 1;
+  if (cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &params) != cudaSuccess) return fail(SL3DGPU_ERR_CUDA);
+  cudaGraph_t body = params.conditional.phGraph_out[0];
+  if (cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+      cudaSuccess)
+    return fail(SL3DGPU_ERR_CUDA);
+  const long long before = prof::Launches();
+  const int st = CaptureCorrectionBody(f, handle);
+  launches = prof::Launches() - before;
+  prof::AddLaunches(-launches);  // captured, not launched
+  cudaGraph_t captured = nullptr;
+  const cudaError_t ended = cudaStreamEndCapture(stream, &captured);
+  if (st != SL3DGPU_OK || ended != cudaSuccess) return fail(SL3DGPU_ERR_CUDA);
+  if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) return fail(SL3DGPU_ERR_CUDA);
+  cudaGraphDestroy(graph);
+  if (correctionGraphs.size() >= 4) {
+    cudaGraphExecDestroy(correctionGraphs.front().exec);
+    correctionGraphs.erase(correctionGraphs.begin());
+  }
+  correctionGraphs.push_back(CorrectionGraph{key, exec, launches});
+  *out = &correctionGraphs.back();
+  return SL3DGPU_OK;
+}
+
 int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_info& info, const double2* warm) {
   SL3D_TRY(PrepareLateral());
   const long long rows = rows0 + rows1 + rowsR;
@@ -1757,7 +1888,19 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
   double previous = 0.0;
   int first = 0;       // the iteration the plain start's sequence begins at
   bool fresh = false;  // the solutions in rhs*32 are the pass of the final e
-  for (int iteration = 0; iteration < options.max_iterations; ++iteration) {
+  bool triedGraph = false;
+  CorrectionGraph* graph = nullptr;
+  int iteration = 0;
+  for (; iteration < options.max_iterations; ++iteration) {
+    // after the first pass (and the warm start's decision) the loop runs on
+    // the device, as a CUDA graph, when it can
+    if (iteration >= 1 && !triedGraph && useGraphs && !prof::TimingOn()) {
+      triedGraph = true;
+      if (CorrectionGraphFor(f, &graph) == SL3DGPU_OK) break;
+      graph = nullptr;
+      useGraphs = false;  // the capture was refused: the host loop carries on
+      cudaGetLastError();
+    }
     SL3D_TRY(Pass32(f, eL.p, eNextL.p));
     ++info.correction_passes;
     LaunchRelativeChange(reinterpret_cast<const float*>(eNextL.p), reinterpret_cast<const float*>(eL.p),
@@ -1800,6 +1943,36 @@ int Viscoelastic3DGpu::Correct(const Flavour& f, double tolerance, sl3dgpu_step_
     } else {
       std::swap(eL, eNextL);
     }
+  }
+  if (graph != nullptr) {
+    // the same loop from this iteration on the device: the host state in, the
+    // graph's while node over the passes, the outcome out
+    CorrectionControl c{};
+    c.slot = slot;
+    c.iteration = iteration;
+    c.first = first;
+    c.mixing = mixing ? 1 : 0;
+    c.firstMix = firstMix ? 1 : 0;
+    c.count = count;
+    c.memory = CorrectionMemory();
+    c.maxIterations = options.max_iterations;
+    c.tolerance = tolerance;
+    c.rate = adaptive ? options.anderson_rate : 0.0;
+    c.previous = previous;
+    const size_t head = offsetof(CorrectionControl, history);
+    SL3D_CUDA(cudaMemcpyAsync(correctionControl.p, &c, head, cudaMemcpyHostToDevice, stream));
+    SL3D_CUDA(cudaGraphLaunch(graph->exec, stream));
+    SL3D_CUDA(cudaMemcpyAsync(&c, correctionControl.p, sizeof(CorrectionControl), cudaMemcpyDeviceToHost, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    const int passes = c.historyCount;
+    prof::AddLaunches(graph->launchesPerPass * passes);
+    info.correction_passes += passes;
+    for (int i = 0; i < std::min(passes, kCorrectionHistory); ++i) correctionHistory.push_back(c.history[i]);
+    if (c.status != 0) {
+      SetError("v3d: the FP32 correction left the finite range");
+      return SL3DGPU_ERR_RUNTIME;
+    }
+    fresh = c.fresh != 0;
   }
   if (!fresh) {
     // out of passes on a mixed iterate: one more pass for its solutions

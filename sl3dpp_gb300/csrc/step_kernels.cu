@@ -664,7 +664,8 @@ __global__ void ReduceMaxKernel(const double* partial, int count, double* result
 // -- the Anderson mixer ---------------------------------------------------------------------------
 
 template <class T>
-__global__ void MixerFirstKernel(long long n, T* x, const T* gx, T* xPrev, T* fPrev) {
+__global__ void MixerFirstKernel(long long n, T* x, const T* gx, T* xPrev, T* fPrev, const int* live) {
+  if (live != nullptr && live[0] != kLiveFirst) return;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) {
     xPrev[i] = x[i];
@@ -735,12 +736,18 @@ template <class T, int M>
 __global__ void MixerSweepKernel(MixerArgsT<T> a) {
   using A = typename MixAcc<T>::type;
   using H = typename MixerArgsT<T>::H;
+  int m = M, slot = a.slot;
+  if (a.live != nullptr) {
+    if (a.live[0] != kLiveUpdate) return;
+    m = a.live[1];
+    slot = a.live[2];
+  }
   const long long begin = a.n * blockIdx.x / a.blocks, end = a.n * (blockIdx.x + 1) / a.blocks;
   A col[M + 1], gam[M + 1];
 #pragma unroll
   for (int i = 0; i <= M; ++i) col[i] = gam[i] = A(0);
-  H* dFs = a.dF[a.slot];
-  H* dGs = a.dG[a.slot];
+  H* dFs = a.dF[slot];
+  H* dGs = a.dG[slot];
   const H* dF[M + 1];
 #pragma unroll
   for (int i = 0; i < M; ++i) dF[i] = a.dF[i];
@@ -757,7 +764,8 @@ __global__ void MixerSweepKernel(MixerArgsT<T> a) {
     const A df = static_cast<A>(FromHistory(dfStored));
 #pragma unroll
     for (int i = 0; i < M; ++i) {
-      const A di = i == a.slot ? df : static_cast<A>(FromHistory(dF[i][at]));
+      if (i >= m) break;
+      const A di = i == slot ? df : static_cast<A>(FromHistory(dF[i][at]));
       col[i] += di * df;
       gam[i] += di * static_cast<A>(f);
     }
@@ -769,6 +777,12 @@ __global__ void MixerSweepKernel(MixerArgsT<T> a) {
 // MixerSweepKernel<float, M> with 8-byte and 4-byte accesses.
 template <int M>
 __global__ void MixerSweepPairsKernel(MixerArgsT<float> a) {
+  int m = M, slot = a.slot;
+  if (a.live != nullptr) {
+    if (a.live[0] != kLiveUpdate) return;
+    m = a.live[1];
+    slot = a.live[2];
+  }
   const long long pairs = a.n / 2;
   const long long begin = pairs * blockIdx.x / a.blocks, end = pairs * (blockIdx.x + 1) / a.blocks;
   float col[M + 1], gam[M + 1];
@@ -778,8 +792,8 @@ __global__ void MixerSweepPairsKernel(MixerArgsT<float> a) {
   auto* gx = reinterpret_cast<const float2*>(a.gx);
   auto* xPrev = reinterpret_cast<float2*>(a.xPrev);
   auto* fPrev = reinterpret_cast<float2*>(a.fPrev);
-  auto* dFs = reinterpret_cast<__nv_bfloat162*>(a.dF[a.slot]);
-  auto* dGs = reinterpret_cast<__nv_bfloat162*>(a.dG[a.slot]);
+  auto* dFs = reinterpret_cast<__nv_bfloat162*>(a.dF[slot]);
+  auto* dGs = reinterpret_cast<__nv_bfloat162*>(a.dG[slot]);
   const __nv_bfloat162* dF[M + 1];
 #pragma unroll
   for (int i = 0; i < M; ++i) dF[i] = reinterpret_cast<const __nv_bfloat162*>(a.dF[i]);
@@ -795,7 +809,8 @@ __global__ void MixerSweepPairsKernel(MixerArgsT<float> a) {
     const float2 df = __bfloat1622float2(dfStored);
 #pragma unroll
     for (int i = 0; i < M; ++i) {
-      const float2 di = i == a.slot ? df : __bfloat1622float2(dF[i][at]);
+      if (i >= m) break;
+      const float2 di = i == slot ? df : __bfloat1622float2(dF[i][at]);
       col[i] += di.x * df.x + di.y * df.y;
       gam[i] += di.x * f.x + di.y * f.y;
     }
@@ -806,7 +821,11 @@ __global__ void MixerSweepPairsKernel(MixerArgsT<float> a) {
 // The sweep's block partial sums reduced to the new Gram column (m values)
 // and the right-hand side (m values, from index kMaxMemory), a warp each, in
 // a fixed order (lanes over the blocks, then a fixed shuffle tree).
-__global__ void MixerReduceKernel(int m, int blocks, const double* partial, double* sums) {
+__global__ void MixerReduceKernel(int m, int blocks, const double* partial, double* sums, const int* live) {
+  if (live != nullptr) {
+    if (live[0] != kLiveUpdate) return;
+    m = live[1];
+  }
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (warp >= 2 * m) return;
   const int i = warp < m ? warp : kMaxMemory + (warp - m);
@@ -819,34 +838,47 @@ __global__ void MixerReduceKernel(int m, int blocks, const double* partial, doub
 template <class T, int M>
 __global__ void MixerMixKernel(MixerArgsT<T> a) {
   using A = typename MixAcc<T>::type;
+  int m = M;
+  if (a.live != nullptr) {
+    if (a.live[0] != kLiveUpdate) return;
+    m = a.live[1];
+  }
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  const bool ok = a.gamma[M] != 0.0;
+  const bool ok = a.gamma[m] != 0.0;
   A g[M + 1];
   const typename MixerArgsT<T>::H* dG[M + 1];
 #pragma unroll
   for (int i = 0; i < M; ++i) {
-    g[i] = static_cast<A>(a.gamma[i]);
+    g[i] = i < m ? static_cast<A>(a.gamma[i]) : A(0);
     dG[i] = a.dG[i];
   }
   for (long long at = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; at < a.n; at += stride) {
     A value = a.gx[at];
     if (ok)
 #pragma unroll
-      for (int i = 0; i < M; ++i) value -= g[i] * static_cast<A>(FromHistory(dG[i][at]));
+      for (int i = 0; i < M; ++i) {
+        if (i >= m) break;
+        value -= g[i] * static_cast<A>(FromHistory(dG[i][at]));
+      }
     a.x[at] = static_cast<T>(value);
   }
 }
 
 template <int M>
 __global__ void MixerMixPairsKernel(MixerArgsT<float> a) {
+  int m = M;
+  if (a.live != nullptr) {
+    if (a.live[0] != kLiveUpdate) return;
+    m = a.live[1];
+  }
   const long long pairs = a.n / 2;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  const bool ok = a.gamma[M] != 0.0;
+  const bool ok = a.gamma[m] != 0.0;
   float g[M + 1];
   const __nv_bfloat162* dG[M + 1];
 #pragma unroll
   for (int i = 0; i < M; ++i) {
-    g[i] = static_cast<float>(a.gamma[i]);
+    g[i] = i < m ? static_cast<float>(a.gamma[i]) : 0.0f;
     dG[i] = reinterpret_cast<const __nv_bfloat162*>(a.dG[i]);
   }
   auto* x = reinterpret_cast<float2*>(a.x);
@@ -856,6 +888,7 @@ __global__ void MixerMixPairsKernel(MixerArgsT<float> a) {
     if (ok)
 #pragma unroll
       for (int i = 0; i < M; ++i) {
+        if (i >= m) break;
         const float2 d = __bfloat1622float2(dG[i][at]);
         v.x -= g[i] * d.x;
         v.y -= g[i] * d.y;
@@ -1231,7 +1264,7 @@ void RelChange(const T2* next, const T2* now, long long n, double* partial, int 
 template <class T>
 void MixerFirst(const MixerArgsT<T>& a, cudaStream_t stream) {
   prof::Scope scope(prof::kMixer, stream, 0.0, a.n * 5.0 * sizeof(T));
-  MixerFirstKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a.n, a.x, a.gx, a.xPrev, a.fPrev);
+  MixerFirstKernel<T><<<StreamBlocks(a.n), 256, 0, stream>>>(a.n, a.x, a.gx, a.xPrev, a.fPrev, a.live);
 }
 
 template <class T>
@@ -1247,7 +1280,7 @@ void MixerSweep(const MixerArgsT<T>& a, double* sums, cudaStream_t stream) {
     });
   }
   prof::Scope scope(prof::kOther, stream);
-  MixerReduceKernel<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.m, a.blocks, a.partial, sums);
+  MixerReduceKernel<<<1, 32 * 2 * kMaxMemory, 0, stream>>>(a.m, a.blocks, a.partial, sums, a.live);
 }
 
 template <class T>
@@ -1385,7 +1418,12 @@ namespace {
 // lstsq.hpp): each rotation's angle on lane 0, its column, row and
 // eigenvector updates one lane per index; every sum in the host's order.
 __global__ void __launch_bounds__(32) MixerGramKernel(double* gram, int m, int slot, int memory,
-                                                      const double* sums, double* gamma) {
+                                                      const double* sums, double* gamma, const int* live) {
+  if (live != nullptr) {
+    if (live[0] != kLiveUpdate) return;
+    m = live[1];
+    slot = live[2];
+  }
   constexpr int M = kMixMaxMemory;
   __shared__ double a[M][M + 1], v[M][M + 1];
   __shared__ double rot[2];
@@ -1490,8 +1528,98 @@ __global__ void __launch_bounds__(32) MixerGramKernel(double* gram, int m, int s
 }  // namespace
 
 void LaunchMixerGram(double* gram, int m, int slot, int memory, const double* sums, double* gamma,
-                     cudaStream_t stream) {
-  MixerGramKernel<<<1, 32, 0, stream>>>(gram, m, slot, memory, sums, gamma);
+                     cudaStream_t stream, const int* live) {
+  MixerGramKernel<<<1, 32, 0, stream>>>(gram, m, slot, memory, sums, gamma, live);
+}
+
+// -- the FP32 correction's loop on the device ------------------------------------------------------
+
+namespace {
+
+// The host loop's decisions (Viscoelastic3DGpu::Correct) made on the device:
+// the same tests, in the same order, on the same numbers.
+__global__ void CorrectionControlKernel(CorrectionControl* c, const double* r, cudaGraphConditionalHandle handle) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (r[2] == 0.0) {  // the iterate left the finite range
+    c->status = 1;
+    c->action = kLiveStop;
+    cudaGraphSetConditional(handle, 0);
+    return;
+  }
+  const double change = r[0] > 0.0 ? sqrt(r[1]) / sqrt(r[0]) : 0.0;
+  if (c->historyCount < kCorrectionHistory) c->history[c->historyCount] = change;
+  ++c->historyCount;
+  const int iteration = c->iteration;
+  c->iteration = iteration + 1;
+  if (change <= c->tolerance) {
+    c->action = kLiveCopy;
+    c->fresh = 1;
+    cudaGraphSetConditional(handle, 0);
+    return;
+  }
+  if (c->rate > 0.0 && !c->mixing && c->memory > 0 && iteration > c->first && change > c->rate * c->previous) {
+    c->mixing = 1;
+    c->firstMix = 1;
+    c->count = 0;
+    c->slot = 0;
+    c->resetGram = 1;
+  }
+  c->previous = change;
+  if (c->mixing) {
+    if (c->firstMix) {
+      c->action = kLiveFirst;
+      c->firstMix = 0;
+    } else {
+      c->action = kLiveUpdate;
+      c->m = min(c->count + 1, c->memory);
+    }
+  } else {
+    c->action = kLiveCopy;
+  }
+  cudaGraphSetConditional(handle, c->iteration < c->maxIterations ? 1u : 0u);
+}
+
+__global__ void CopyIfPlainKernel(const CorrectionControl* c, const float2* from, float2* to, long long n) {
+  if (c->action != kLiveCopy) return;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    to[i] = from[i];
+}
+
+__global__ void GramResetIfKernel(CorrectionControl* c, double* gram, int count) {
+  if (!c->resetGram) return;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) gram[i] = 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0) c->resetGram = 0;
+}
+
+__global__ void MixerAdvanceIfKernel(CorrectionControl* c) {
+  if (threadIdx.x != 0 || c->action != kLiveUpdate) return;
+  c->count = c->m;
+  c->slot = (c->slot + 1) % c->memory;
+}
+
+}  // namespace
+
+void LaunchCorrectionControl(CorrectionControl* c, const double* result, cudaGraphConditionalHandle handle,
+                             cudaStream_t stream) {
+  prof::Scope scope(prof::kOther, stream);
+  CorrectionControlKernel<<<1, 32, 0, stream>>>(c, result, handle);
+}
+
+void LaunchCopyIfPlain(const CorrectionControl* c, const float2* from, float2* to, long long n, cudaStream_t stream) {
+  prof::Scope scope(prof::kMixer, stream);
+  CopyIfPlainKernel<<<StreamBlocks(n), 256, 0, stream>>>(c, from, to, n);
+}
+
+void LaunchGramResetIf(CorrectionControl* c, double* gram, int memory, cudaStream_t stream) {
+  prof::Scope scope(prof::kOther, stream);
+  GramResetIfKernel<<<1, 256, 0, stream>>>(c, gram, memory * memory);
+}
+
+void LaunchMixerAdvanceIf(CorrectionControl* c, cudaStream_t stream) {
+  prof::Scope scope(prof::kOther, stream);
+  MixerAdvanceIfKernel<<<1, 32, 0, stream>>>(c);
 }
 
 bool MixerSolve(double* gram, int m, int slot, int memory, const double* sums, double* gamma) {

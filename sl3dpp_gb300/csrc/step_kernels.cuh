@@ -229,6 +229,11 @@ struct MixerArgsT {
   int blocks;
   double* gram;     // memory x memory
   double* gamma;    // m (+1 status)
+  // Under a CUDA graph the pass's mixer work is decided on the device: live
+  // points at a CorrectionControl's {action, m, slot}, the kernels taking
+  // m and slot from it and doing nothing unless the action is theirs (the
+  // template history count is then the mixer's memory, the runtime m <= it).
+  const int* live = nullptr;
 };
 using MixerArgs = MixerArgsT<double>;
 constexpr int kMixMaxMemory = 16;  // the most history columns; sums hold 2 x this
@@ -251,6 +256,36 @@ bool MixerSolve(double* gram, int m, int slot, int memory, const double* sums, d
 // (memory x memory, device) updated from sums (device), gamma (m values and
 // the status) written for the mix. No host round trip.
 void LaunchMixerGram(double* gram, int m, int slot, int memory, const double* sums, double* gamma,
-                     cudaStream_t stream);
+                     cudaStream_t stream, const int* live = nullptr);
+
+// -- the FP32 correction's loop on the device (a CUDA graph's while node) -------------------------
+
+// What a pass's mixer kernels do: nothing (the loop stops), the plain step
+// (the next iterate copied over the iterate), the mixer's first call, an update.
+constexpr int kLiveStop = 0, kLiveCopy = 1, kLiveFirst = 2, kLiveUpdate = 3;
+constexpr int kCorrectionHistory = 1024;
+// The loop's state in device memory: the correction loop of the mixed form
+// (its host form in step.cu, Viscoelastic3DGpu::Correct) decided pass by
+// pass by CorrectionControlKernel. The first three ints are the mixer
+// kernels' `live` view.
+struct CorrectionControl {
+  int action, m, slot;
+  int iteration, first, mixing, firstMix, count, memory, maxIterations;
+  int fresh, status, resetGram, historyCount;
+  double tolerance, rate, previous;
+  double history[kCorrectionHistory];
+};
+// After a pass's relative change (result: scale, diff, finite flag): the
+// change recorded, the stopping test, the switch to mixing, the pass's
+// mixer action, and the while node's condition (continue while not
+// converged, finite and within the pass budget).
+void LaunchCorrectionControl(CorrectionControl* c, const double* result, cudaGraphConditionalHandle handle,
+                             cudaStream_t stream);
+// to = from where the pass's action is the plain step.
+void LaunchCopyIfPlain(const CorrectionControl* c, const float2* from, float2* to, long long n, cudaStream_t stream);
+// The mixer's Gram matrix zeroed when the loop switched to mixing.
+void LaunchGramResetIf(CorrectionControl* c, double* gram, int memory, cudaStream_t stream);
+// The mixer's count and slot moved on after an update.
+void LaunchMixerAdvanceIf(CorrectionControl* c, cudaStream_t stream);
 
 }  // namespace sl3dgpu

@@ -74,6 +74,7 @@ struct Dev {
 struct Flavour {
   int scheme = 0;
   double dt = 0.0;
+  long long id = 0;  // unique per flavour built (a graph captured on it is keyed by it)
   Dev<double> bands, scales, units;
   // the tide channel's units K^-1 Tide per degree (the same offsets as units)
   // and, for conjugate gradients, the unsolved vectors

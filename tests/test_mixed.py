@@ -143,3 +143,40 @@ def test_fp64_contractions_emulated_on_the_tensor_cores_keep_the_bar(gpu, precis
         assert io.converged == ig.converged == 1
         for comp in (0, 2):
             assert rel(g.Surface(comp), o.surface(comp)) < tol, (n, comp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("memory,rate", [(10, 0.5), (5, 0.0)])
+def test_correction_loop_on_the_device_is_the_host_loop(gpu, monkeypatch, memory, rate):
+    """The FP32 correction's loop run as a CUDA graph (a while node whose
+    body is one pass and the device's decision) takes the host loop's
+    decisions on the same numbers: the same passes, the same changes, the
+    same results, bit for bit -- adaptive mixing (rate 0.5) and mixing from
+    the start (rate 0)."""
+    from sl3dpp_gb300 import _lib
+
+    lmax = 12
+    runs = {}
+    for graphs in (True, False):
+        if graphs:
+            monkeypatch.delenv("SL3DGPU_NO_GRAPHS", raising=False)
+        else:
+            monkeypatch.setenv("SL3DGPU_NO_GRAPHS", "1")
+        o, g = _pair(lmax, 20, 5, rms=1.0, ldelta=5, seed=5, precision=1, rtol=1e-10, max_iterations=60,
+                     correction_memory=memory, anderson_rate=rate)
+        load = cap_load(lmax, o.sigma_scale, 2000.0)
+        dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+        state = g.ZeroState()
+        before = _lib.lib().sl3dgpu_launch_count()
+        out = []
+        for n in range(3):
+            info = g.Step(state, dt, 2, load * n / 10, load * (n + 1) / 10)
+            assert info.converged == 1
+            out.append((info.iterations, info.correction_passes, g.correction_history(), g.Surface(0), g.Surface(2)))
+        runs[graphs] = (out, _lib.lib().sl3dgpu_launch_count() - before)
+    for (a, b) in zip(runs[True][0], runs[False][0]):
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.array_equal(a[2], b[2])
+        assert np.array_equal(a[3], b[3]) and np.array_equal(a[4], b[4])
+    # the graph's kernels are counted as launched
+    assert runs[True][1] > 0.8 * runs[False][1]
