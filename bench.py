@@ -570,6 +570,50 @@ def ocean_case(args, device):
             "axial_angular_velocity": float(omega[2] / op.time_scale)}
 
 
+# -- config 4: the ensemble ----------------------------------------------------------------------
+
+def ensemble_case(args):
+    """Config 4: the seeded members (48 by default; lmax from {32, 64, 96,
+    128}, delta RMS 0.3-1.5 to degree lmax / 4, a cap of 5-20 degrees to 2 km
+    over 10 steps of 500 yr, 20 Sdirk2 steps, 40-80 elements of order 4) in
+    the mixed form with the extrapolated warm start. The autotuner picks the
+    queue order and the members in flight; then the whole ensemble runs
+    concurrently (sl3dgpu_v3d_run_many) and one member after another, each
+    timed by the host clock around the call (inputs and outputs on the host,
+    a run's copies inside it). Aggregate member-steps/s for both; the
+    concurrent snapshots against the one-by-one ones; per-instance error of
+    U and phi against the plain FP64 GPU form (itself pinned to the FP64
+    oracle) for one member of each lmax."""
+    from sl3dpp_gb300.ensemble import Ensemble, autotune, ensemble_members
+
+    members = ensemble_members(args.ensemble_members, seed=4, steps=args.ensemble_steps)
+    ens = Ensemble(members, precision=1)
+    tune = autotune(ens, probe_steps=1)
+    together = ens.run(threads=tune["threads"], order=tune["order"])
+    alone = ens.run_sequential()
+    steps = ens.member_steps()
+    same = max(float(np.max(np.abs(together["U"][k] - alone["U"][k])) / np.max(np.abs(alone["U"][k])))
+               for k in range(len(members)))
+    picks = []
+    for lmax in sorted({m["lmax"] for m in members}):
+        picks.append(next(k for k, m in enumerate(members) if m["lmax"] == lmax))
+    ref = Ensemble([members[k] for k in picks], precision=0).run_sequential()
+    errors = []
+    for j, k in enumerate(picks):
+        err = lambda a, b: float(max(np.max(np.abs(a[n] - b[n])) / np.max(np.abs(b[n])) for n in range(1, len(b))))
+        errors.append({"member": k, "lmax": members[k]["lmax"], "U": err(together["U"][k], ref["U"][j]),
+                       "phi": err(together["phi"][k], ref["phi"][j])})
+    passes = [sum(i.iterations for i in infos[1:]) for infos in together["infos"]]
+    return {"case": f"config 4: {len(members)} members, lmax 32-128, mixed form, {args.ensemble_steps} Sdirk2 steps",
+            "member_steps": steps, "concurrent_steps_per_s": steps / together["seconds"],
+            "sequential_steps_per_s": steps / alone["seconds"],
+            "speedup_concurrent": alone["seconds"] / together["seconds"],
+            "threads": tune["threads"], "probe_seconds": tune["probe_seconds"],
+            "order_first": tune["order"][:8], "concurrent_vs_sequential_max_rel_U": same,
+            "fp64_passes_per_member": passes, "per_instance_error_vs_fp64": errors,
+            "lmax_counts": {str(l): sum(1 for m in members if m["lmax"] == l) for l in (32, 64, 96, 128)}}
+
+
 # -- main ------------------------------------------------------------------------------------------
 
 def main():
@@ -591,6 +635,10 @@ def main():
                     help="instead: the FP32 tensor-core Legendre contraction alone at the workload's lmax")
     ap.add_argument("--ocean-case", action="store_true",
                     help="instead: config 2, the coupled step under an ocean at lmax 128, 50 steps")
+    ap.add_argument("--ensemble-case", action="store_true",
+                    help="instead: config 4, the seeded ensemble (autotuned schedule, concurrent and one by one)")
+    ap.add_argument("--ensemble-members", type=int, default=48)
+    ap.add_argument("--ensemble-steps", type=int, default=20)
     args = ap.parse_args()
     if args.lmax != LMAX:
         _rescale(args.lmax)
@@ -653,6 +701,10 @@ def main():
     if args.ocean_case:
         if rank == 0:
             print(json.dumps(ocean_case(args, device)), flush=True)
+        return
+    if args.ensemble_case:
+        if rank == 0:
+            print(json.dumps(ensemble_case(args)), flush=True)
         return
     fp64, fp32 = ctypes.c_double(), ctypes.c_double()
     lib().sl3dgpu_fp64_fma_peak(ctypes.byref(fp64))

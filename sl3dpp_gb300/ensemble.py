@@ -5,7 +5,9 @@ Evolution3D run with its own lateral viscosity and ice history).
 Each member is a `Viscoelastic3D` operator with its own state and CUDA
 stream; `Ensemble.run` hands all members to `sl3dgpu_v3d_run_many`, whose
 native thread pool drives them concurrently so that the small members'
-kernels overlap on the GPU. `Ensemble.run_sequential` runs them one after
+kernels overlap on the GPU; `autotune` chooses the pool's queue order
+(longest member first) and its size (the members in flight) by measuring
+them. `Ensemble.run_sequential` runs them one after
 another through the same per-member entry point (the comparison, and the
 parity check: both give the same snapshots).
 
@@ -90,21 +92,27 @@ class Ensemble:
         infos = [(StepInfo * t.size)() for t in self.times]
         return U, phi, infos
 
-    def run(self, threads: int = 0, steps: int | None = None) -> dict:
+    def run(self, threads: int = 0, steps: int | None = None, order=None) -> dict:
         """Every member from a zero state, concurrently (the first `steps`
-        steps of each, all by default); wall-clock seconds."""
+        steps of each, all by default), the pool taking the members in
+        `order` (a permutation, index order by default); wall-clock seconds.
+        Outputs stay in member order."""
         n = len(self.ops)
+        order = list(range(n)) if order is None else list(order)
+        if sorted(order) != list(range(n)):
+            raise ValueError("order is a permutation of the members")
         states = [op.ZeroState() for op in self.ops]
         U, phi, infos = self._outputs()
         P = ctypes.c_void_p
-        ops = (P * n)(*[op._h.value for op in self.ops])
-        sts = (P * n)(*[s._h.value for s in states])
-        times = (P * n)(*[t.ctypes.data for t in self.times])
-        nodes = (ctypes.c_int * n)(*[t.size if steps is None else min(t.size, steps + 1) for t in self.times])
-        loads = (P * n)(*[ld.ctypes.data for ld in self.loads])
-        us = (P * n)(*[u.ctypes.data for u in U])
-        ps = (P * n)(*[p.ctypes.data for p in phi])
-        inf = (P * n)(*[ctypes.cast(i, P).value for i in infos])
+        ops = (P * n)(*[self.ops[k]._h.value for k in order])
+        sts = (P * n)(*[states[k]._h.value for k in order])
+        times = (P * n)(*[self.times[k].ctypes.data for k in order])
+        nodes = (ctypes.c_int * n)(*[self.times[k].size if steps is None else min(self.times[k].size, steps + 1)
+                                     for k in order])
+        loads = (P * n)(*[self.loads[k].ctypes.data for k in order])
+        us = (P * n)(*[U[k].ctypes.data for k in order])
+        ps = (P * n)(*[phi[k].ctypes.data for k in order])
+        inf = (P * n)(*[ctypes.cast(infos[k], P).value for k in order])
         statuses = (ctypes.c_int * n)()
         t0 = time.perf_counter()
         check(lib().sl3dgpu_v3d_run_many(n, ops, sts, times, nodes, self.scheme, loads, us, ps, inf, threads,
@@ -126,5 +134,44 @@ class Ensemble:
         return {"U": U, "phi": phi, "infos": [[i[k] for k in range(len(i))] for i in infos], "seconds": wall,
                 "states": states}
 
-    def member_steps(self) -> int:
-        return sum(t.size - 1 for t in self.times)
+    def member_steps(self, steps: int | None = None) -> int:
+        return sum(t.size - 1 if steps is None else min(t.size - 1, steps) for t in self.times)
+
+    def member_seconds(self, steps: int = 1) -> list[float]:
+        """Each member's first `steps` steps run alone (node 0 and the steps),
+        wall-clock seconds: the schedule's cost model."""
+        out = []
+        for k, op in enumerate(self.ops):
+            state = op.ZeroState()
+            U = np.zeros((steps + 1, self.loads[k].shape[1]), dtype=np.complex128)
+            phi = np.zeros_like(U)
+            infos = (StepInfo * (steps + 1))()
+            t0 = time.perf_counter()
+            check(lib().sl3dgpu_v3d_run(op._h, state._h, self.times[k].ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        steps + 1, self.scheme, self.loads[k].ctypes.data, U.ctypes.data,
+                                        phi.ctypes.data, infos))
+            out.append(time.perf_counter() - t0)
+        return out
+
+
+def autotune(ens: Ensemble, probe_steps: int = 2, thread_choices=None) -> dict:
+    """The ensemble's queue schedule and concurrency, chosen by measurement.
+
+    The members' costs are measured (each member's first step alone), the
+    queue ordered longest first (the pool then ends with the short members,
+    which fill the GPU's gaps -- LPT scheduling), and each candidate number of
+    concurrent members (host threads, one member each) timed over the first
+    `probe_steps` steps of the whole ensemble in that order; the fastest is
+    kept. Returns the order, the threads, and every measurement."""
+    n = len(ens.ops)
+    cost = ens.member_seconds(1)
+    order = sorted(range(n), key=lambda k: -cost[k])
+    if thread_choices is None:
+        thread_choices = sorted({max(1, n // 8), max(1, n // 4), max(1, n // 2), n})
+    timings = {}
+    for threads in thread_choices:
+        r = ens.run(threads=threads, steps=probe_steps, order=order)
+        timings[threads] = r["seconds"]
+    best = min(timings, key=timings.get)
+    return {"order": order, "threads": best, "probe_seconds": timings, "member_seconds": cost,
+            "probe_steps": probe_steps}

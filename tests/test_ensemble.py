@@ -58,3 +58,27 @@ def test_run_many_refuses_shared_operators(gpu):
                                            2, (P * 2)(ens.loads[0].ctypes.data, ens.loads[0].ctypes.data),
                                            None, None, None, 0, st)
     assert code == _lib.ERR_ARGUMENT and b"distinct" in _lib.lib().sl3dgpu_last_error()
+
+
+@pytest.mark.gpu
+def test_autotuned_schedule_runs_longest_first_and_keeps_the_results(gpu):
+    """The autotuner's queue order puts the costlier members first and its
+    chosen concurrency is one it measured; a run in that order gives every
+    member the one-by-one run's snapshots (outputs stay in member order)."""
+    from sl3dpp_gb300.ensemble import Ensemble, autotune
+
+    members = ensemble_members(6, seed=9, steps=2, lmax_choices=(8, 16))
+    for m in members:
+        m["elements"] = 20
+    ens = Ensemble(members, precision=1)
+    tune = autotune(ens, probe_steps=1, thread_choices=[1, 3, 6])
+    cost = tune["member_seconds"]
+    assert sorted(tune["order"]) == list(range(6))
+    assert all(cost[a] >= cost[b] for a, b in zip(tune["order"], tune["order"][1:]))
+    assert tune["threads"] in (1, 3, 6) and set(tune["probe_seconds"]) == {1, 3, 6}
+    together = ens.run(threads=tune["threads"], order=tune["order"])
+    alone = ens.run_sequential()
+    for k in range(len(members)):
+        for key in ("U", "phi"):
+            a, b = together[key][k], alone[key][k]
+            assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b)), (k, key)
