@@ -517,6 +517,15 @@ int sl3dgpu_v3d_run_many(int count, sl3dgpu_v3d* const* ops, sl3dgpu_v3d_state* 
                          const double* const* times, const int* nodes, int scheme,
                          const double* const* loads, double* const* u, double* const* phi,
                          sl3dgpu_step_info* const* infos, int threads, int* statuses);
+/* A state as bytes, for checkpoints (Evolution3D::Checkpoint's memory and
+ * strain, src/Evolution3D.cpp:146-167): the byte count, the state copied to
+ * a host buffer of that size, and a state (from sl3dgpu_v3d_zero_state)
+ * replaced by saved bytes -- refused unless an operator of the same shape
+ * saved them. A run resumed from saved bytes continues bit for bit. */
+long long sl3dgpu_v3d_state_bytes(const sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state);
+int sl3dgpu_v3d_state_save(sl3dgpu_v3d* op, const sl3dgpu_v3d_state* state, void* out, long long capacity);
+int sl3dgpu_v3d_state_load(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const void* in, long long bytes);
+
 /* ---- the open step (Viscoelastic3D::OpenStep, include/sl3dpp/Viscoelastic3D.hpp:440-640) ----
  * One stage opened on the operator's own buffers, for a driver's own
  * within-step iteration (one open step per operator at a time). Strain

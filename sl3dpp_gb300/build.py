@@ -75,5 +75,32 @@ def build(force: bool = False, verbose: bool = False) -> pathlib.Path:
     return LIBRARY
 
 
+APP = HERE / "sl3d"
+APP_DIR = CSRC / "app"
+
+
+def build_app(force: bool = False, verbose: bool = False) -> pathlib.Path:
+    """The sl3d front end (csrc/app, host C++ over the C ABI) linked against
+    libsl3dgpu.so beside it (found through $ORIGIN)."""
+    library = build(verbose=verbose)
+    sources = sorted(APP_DIR.glob("*.cpp"))
+    inputs = sources + list(APP_DIR.glob("*.hpp")) + list(INCLUDE.glob("*.h")) + [library]
+    if not force and APP.exists() and all(p.stat().st_mtime <= APP.stat().st_mtime for p in inputs):
+        return APP
+    cuda = pathlib.Path(_nvcc()).resolve().parent.parent
+    tmp = APP.with_suffix(".tmp")
+    cmd = ["g++", "-O2", "-std=c++23", "-I", str(INCLUDE), "-I", str(cuda / "include"), *map(str, sources),
+           "-o", str(tmp), "-L", str(HERE), "-lsl3dgpu", "-Wl,-rpath,$ORIGIN", "-L", str(cuda / "lib64"),
+           "-lcudart"]
+    result = subprocess.run(cmd, capture_output=True, text=True)
+    if result.returncode != 0:
+        raise RuntimeError(f"building sl3d failed:\n{' '.join(cmd)}\n{result.stderr}")
+    os.replace(tmp, APP)
+    if verbose:
+        print(f"built {APP}", file=sys.stderr)
+    return APP
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True)
+    build_app(force="--force" in sys.argv, verbose=True)

@@ -365,6 +365,12 @@ class Viscoelastic3DGpu {
   int TensorAnalyse(const double2* c0, const double2* c1, const double* r, double2* spectral);
   int DegreeForces(const double2* spectral, double2* sph, double2* tor);
   int StrainOfSolutions(const double2* sph, const double2* tor, double2* spectral);
+  // A state as bytes (checkpoints): a header, each branch's memory on the
+  // grid at the lateral nodes and as coefficients, the strain likewise, the
+  // coefficients (and the step before's under warm_start 1).
+  long long StateBytes(const V3dState& st) const;
+  int SaveState(const V3dState& st, char* out, long long capacity);
+  int LoadState(V3dState& st, const char* in, long long bytes);
   int Change(const double2* next, const double2* now, double* out) {
     SL3D_TRY(RelativeChange(next, now, out));
     return SL3DGPU_OK;
@@ -2435,6 +2441,113 @@ int Viscoelastic3DGpu::Adopt(V3dState& st) {
   return SL3DGPU_OK;
 }
 
+// -- a state as bytes -----------------------------------------------------------------------------------
+
+namespace {
+struct StateHeader {
+  char magic[8];  // "SL3DGST1"
+  long long K, values, spectralComplex, fieldSize;
+  int latFirst, latEnd, hasStrain, hasCoeffs, hasPrev, pad;
+};
+constexpr char kStateMagic[8] = {'S', 'L', '3', 'D', 'G', 'S', 'T', '1'};
+}  // namespace
+
+long long Viscoelastic3DGpu::StateBytes(const V3dState& st) const {
+  const long long lateral = static_cast<long long>(st.latEnd - st.latFirst) * fieldSize;
+  const long long grid = lateral * static_cast<long long>(2 * sizeof(double2) + sizeof(double));
+  const long long spec = spectralComplex * static_cast<long long>(sizeof(double2));
+  return static_cast<long long>(sizeof(StateHeader)) + K * (grid + spec) + (st.hasStrain ? grid : 0) +
+         (st.hasCoeffs ? spec : 0) + (st.hasPrev ? spec : 0);
+}
+
+int Viscoelastic3DGpu::SaveState(const V3dState& st, char* out, long long capacity) {
+  if (capacity < StateBytes(st)) {
+    SetError("v3d: the buffer is smaller than the state (sl3dgpu_v3d_state_bytes)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  StateHeader h{};
+  std::memcpy(h.magic, kStateMagic, 8);
+  h.K = K;
+  h.values = values;
+  h.spectralComplex = spectralComplex;
+  h.fieldSize = fieldSize;
+  h.latFirst = st.latFirst;
+  h.latEnd = st.latEnd;
+  h.hasStrain = st.hasStrain;
+  h.hasCoeffs = st.hasCoeffs;
+  h.hasPrev = st.hasPrev;
+  std::memcpy(out, &h, sizeof(h));
+  char* at = out + sizeof(h);
+  const long long begin = static_cast<long long>(st.latFirst) * fieldSize;
+  const long long lateral = static_cast<long long>(st.latEnd - st.latFirst) * fieldSize;
+  auto take = [&](const void* device, size_t bytes) -> int {
+    if (bytes > 0) SL3D_CUDA(cudaMemcpyAsync(at, device, bytes, cudaMemcpyDeviceToHost, stream));
+    at += bytes;
+    return SL3DGPU_OK;
+  };
+  auto grid = [&](const GridTensor& g) -> int {
+    SL3D_TRY(take(g.c0.p + begin, lateral * sizeof(double2)));
+    SL3D_TRY(take(g.c1.p + begin, lateral * sizeof(double2)));
+    return take(g.r.p + begin, lateral * sizeof(double));
+  };
+  for (int k = 0; k < K; ++k) {
+    SL3D_TRY(grid(st.m[k]));
+    SL3D_TRY(take(st.mSpec[k].p, spectralComplex * sizeof(double2)));
+  }
+  if (st.hasStrain) SL3D_TRY(grid(st.strain));
+  if (st.hasCoeffs) SL3D_TRY(take(st.coeffs.p, spectralComplex * sizeof(double2)));
+  if (st.hasPrev) SL3D_TRY(take(st.prev.p, spectralComplex * sizeof(double2)));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::LoadState(V3dState& st, const char* in, long long bytes) {
+  StateHeader h{};
+  if (bytes < static_cast<long long>(sizeof(h))) {
+    SetError("v3d: not a state (too short)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  std::memcpy(&h, in, sizeof(h));
+  if (std::memcmp(h.magic, kStateMagic, 8) != 0 || h.K != K || h.values != values ||
+      h.spectralComplex != spectralComplex || h.fieldSize != fieldSize || h.latFirst < 0 || h.latEnd > P ||
+      h.latFirst > h.latEnd || (h.hasPrev && options.warm_start != 1)) {
+    SetError("v3d: the state was not saved by an operator of this shape");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SL3D_TRY(AllocState(st));
+  st.latFirst = h.latFirst;
+  st.latEnd = h.latEnd;
+  st.hasStrain = h.hasStrain != 0;
+  st.hasCoeffs = h.hasCoeffs != 0;
+  st.hasPrev = h.hasPrev != 0;
+  if (bytes != StateBytes(st)) {
+    SetError("v3d: the state's size does not match its header");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const char* at = in + sizeof(h);
+  const long long begin = static_cast<long long>(st.latFirst) * fieldSize;
+  const long long lateral = static_cast<long long>(st.latEnd - st.latFirst) * fieldSize;
+  auto give = [&](void* device, size_t n) -> int {
+    if (n > 0) SL3D_CUDA(cudaMemcpyAsync(device, at, n, cudaMemcpyHostToDevice, stream));
+    at += n;
+    return SL3DGPU_OK;
+  };
+  auto grid = [&](GridTensor& g) -> int {
+    SL3D_TRY(give(g.c0.p + begin, lateral * sizeof(double2)));
+    SL3D_TRY(give(g.c1.p + begin, lateral * sizeof(double2)));
+    return give(g.r.p + begin, lateral * sizeof(double));
+  };
+  for (int k = 0; k < K; ++k) {
+    SL3D_TRY(grid(st.m[k]));
+    SL3D_TRY(give(st.mSpec[k].p, spectralComplex * sizeof(double2)));
+  }
+  if (st.hasStrain) SL3D_TRY(grid(st.strain));
+  if (st.hasCoeffs) SL3D_TRY(give(st.coeffs.p, spectralComplex * sizeof(double2)));
+  if (st.hasPrev) SL3D_TRY(give(st.prev.p, spectralComplex * sizeof(double2)));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
 // -- GridCoupling's maps (include/sl3dpp/GridCoupling.hpp:82-428) ---------------------------------------
 
 int Viscoelastic3DGpu::TensorSynthesise(const double2* spectral, double2* c0, double2* c1, double* r) {
@@ -2968,6 +3081,30 @@ extern "C" int sl3dgpu_v3d_strain_of_solutions(sl3dgpu_v3d* h, const double* sph
   }
   return h->op.StrainOfSolutions(reinterpret_cast<const double2*>(spheroidal),
                                  reinterpret_cast<const double2*>(toroidal), reinterpret_cast<double2*>(spectral));
+}
+
+extern "C" long long sl3dgpu_v3d_state_bytes(const sl3dgpu_v3d* h, const sl3dgpu_v3d_state* state) {
+  if (h == nullptr || state == nullptr) {
+    SetError("v3d: null handle or state");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StateBytes(state->st);
+}
+
+extern "C" int sl3dgpu_v3d_state_save(sl3dgpu_v3d* h, const sl3dgpu_v3d_state* state, void* out, long long capacity) {
+  if (h == nullptr || state == nullptr || out == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.SaveState(state->st, static_cast<char*>(out), capacity);
+}
+
+extern "C" int sl3dgpu_v3d_state_load(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const void* in, long long bytes) {
+  if (h == nullptr || state == nullptr || in == nullptr) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.LoadState(state->st, static_cast<const char*>(in), bytes);
 }
 
 extern "C" int sl3dgpu_v3d_set_ocean(sl3dgpu_v3d* h, const sl3dgpu_v3d_ocean* ocean) {

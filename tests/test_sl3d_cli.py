@@ -1,0 +1,164 @@
+"""The sl3d front end (sl3dpp_gb300/csrc/app/sl3d.cpp): the reference's
+`sl3d solve` for a 3D run through time (apps/SolveCommand.cpp:1747-1795) with
+its disk checkpoints (:239-290) and restart.
+
+Without a GPU: configs are read and checked (`sl3d check`): unknown members,
+bad values and missing blocks are refused; the run hash depends on the
+members that decide the computation and not on the key order or on the
+members that only steer the run. On the GPU: a run's surface table is the
+library's own evolution (Evolution3D.Run through the C ABI) on the same
+inputs, number for number; a run stopped after a node and restarted from its
+checkpoint writes the uninterrupted run's table bit for bit; another run's
+checkpoint is refused; an ocean run writes the sea level beside U and phi
+and restarts alike."""
+
+import json
+import pathlib
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def sl3d():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from sl3dpp_gb300 import build
+
+    return build.APP
+
+
+def run(binary, mode, config, tmp_path, name="config.json", timeout=600):
+    path = tmp_path / name
+    path.write_text(json.dumps(config))
+    return subprocess.run([str(binary), mode, str(path)], capture_output=True, text=True, timeout=timeout)
+
+
+def base(tmp_path, lmax=8, nodes=5, **extra):
+    config = {
+        "model": {"earth": "standard", "elements": 20},
+        "mesh": {"lmax": lmax, "ngll": 5},
+        "lateral": {"viscosity": {"seed": 3, "degree": 4, "rms": 0.8}},
+        "forcing": {"ice": {"cap_degrees": 15, "thickness_m": 2000, "ramp_nodes": 4}},
+        "time": {"step_yr": 500, "nodes": nodes},
+        "solve": {"scheme": "sdirk2", "precision": "fp64", "rtol": 1e-10, "max_iterations": 60},
+        "output": {"file": str(tmp_path / "surface.txt")},
+    }
+    config.update(extra)
+    return config
+
+
+def run_hash(result):
+    assert result.returncode == 0, result.stderr
+    return result.stdout.split("run hash ")[1].split(",")[0]
+
+
+def test_check_reads_the_config_and_hashes_what_decides_the_run(sl3d, tmp_path):
+    cfg = base(tmp_path)
+    h = run_hash(run(sl3d, "check", cfg, tmp_path))
+    # key order and the steering members leave the hash alone
+    steered = dict(reversed(list(base(tmp_path).items())))
+    steered.update(checkpoint={"directory": str(tmp_path / "ck"), "stride": 2}, restart=True, stop_after_node=2,
+                   output={"file": str(tmp_path / "other.txt")})
+    assert run_hash(run(sl3d, "check", steered, tmp_path)) == h
+    # a deciding member changes it
+    other = base(tmp_path)
+    other["lateral"]["viscosity"]["rms"] = 0.9
+    assert run_hash(run(sl3d, "check", other, tmp_path)) != h
+    other = base(tmp_path, nodes=6)
+    assert run_hash(run(sl3d, "check", other, tmp_path)) != h
+
+
+@pytest.mark.parametrize("change,text", [
+    (lambda c: c.update(colour="blue"), "unknown member \"colour\""),
+    (lambda c: c["solve"].update(scheme="leapfrog"), "solve.scheme"),
+    (lambda c: c.pop("model"), "a model is required"),
+    (lambda c: c["time"].update(step_yr=-1), "step_yr > 0"),
+    (lambda c: c.update(restart=True), "checkpoint directory"),
+    (lambda c: c["ocean"].update(rotation="sideways") if "ocean" in c else c.update(ocean={"rotation": "sideways"}),
+     "ocean.rotation"),
+])
+def test_check_refuses_bad_configs(sl3d, tmp_path, change, text):
+    cfg = base(tmp_path)
+    change(cfg)
+    result = run(sl3d, "check", cfg, tmp_path)
+    assert result.returncode == 2 and text in result.stderr, result.stderr
+
+
+def test_check_refuses_broken_json(sl3d, tmp_path):
+    path = tmp_path / "broken.json"
+    path.write_text('{"model": {"earth": "standard"},}')
+    result = subprocess.run([str(sl3d), "check", str(path)], capture_output=True, text=True)
+    assert result.returncode == 2 and "offset" in result.stderr
+
+
+def table(path):
+    return np.loadtxt(path, comments="#")
+
+
+@pytest.mark.gpu
+def test_gpu_solve_is_the_library_evolution(gpu, sl3d, tmp_path):
+    import torch
+
+    from sl3dpp_gb300 import configs
+    from sl3dpp_gb300.grid import SurfaceGrid
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D, Options, Viscoelastic3D, standard_earth
+
+    lmax, nodes = 8, 5
+    coeffs = configs.delta_coefficients(lmax, 4, 0.8, 7)
+    (tmp_path / "delta.bin").write_bytes(np.ascontiguousarray(coeffs, dtype=np.complex128).tobytes())
+    cfg = base(tmp_path, lmax, nodes)
+    cfg["lateral"] = {"viscosity": {"coefficients": str(tmp_path / "delta.bin")}}
+    result = run(sl3d, "solve", cfg, tmp_path)
+    assert result.returncode == 0, result.stdout + result.stderr
+    got = table(tmp_path / "surface.txt")
+    # the same run through the library's Python binding
+    op = Viscoelastic3D(standard_earth(20), Options.defaults(lmax, 5, rtol=1e-10, max_iterations=60))
+    pattern = SurfaceGrid(lmax, 0, 1.5).SynthesiseBatch(torch.tensor(coeffs, device=gpu), 1)
+    ind = torch.tensor(configs.delta_indicator(op.radius), device=gpu)
+    op.set_delta((ind[:, None] * pattern[None, :]).contiguous().view(-1))
+    exact = SurfaceGrid(lmax, 0, 1.0)
+    cap = configs.cap_field(exact.theta, exact.nphi, 15.0, 2000.0)
+    full = (exact.ExpandBatch(torch.tensor(cap, device=gpu), 1) / op.surface_density_scale).cpu().numpy()
+    times = np.arange(nodes) * 500 * configs.SECONDS_PER_YEAR / op.time_scale
+    loads = np.minimum(np.arange(nodes), 4)[:, None] / 4 * full[None, :]
+    want = Evolution3D(op, "sdirk2").Run(times, loads)
+    lm = (lmax + 1) * (lmax + 2) // 2
+    U = (got[:, 4] + 1j * got[:, 5]).reshape(nodes, lm) / op.length_scale
+    phi = (got[:, 6] + 1j * got[:, 7]).reshape(nodes, lm) / (op.length_scale / op.time_scale) ** 2
+    assert np.max(np.abs(U - want["U"])) <= 1e-15 * np.max(np.abs(want["U"]))
+    assert np.max(np.abs(phi - want["phi"])) <= 1e-15 * np.max(np.abs(want["phi"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ocean", [False, True])
+def test_gpu_restart_continues_the_run_bit_for_bit(gpu, sl3d, tmp_path, ocean):
+    extra = {"ocean": {"land_fraction": 0.3, "seed": 11, "rotation": "axial"}} if ocean else {}
+    whole = base(tmp_path, nodes=6, **extra)
+    whole["output"] = {"file": str(tmp_path / "whole.txt")}
+    whole["checkpoint"] = {"directory": str(tmp_path / "ck_whole"), "stride": 2}
+    assert run(sl3d, "solve", whole, tmp_path).returncode == 0
+    part = base(tmp_path, nodes=6, **extra)
+    part["output"] = {"file": str(tmp_path / "resumed.txt")}
+    part["checkpoint"] = {"directory": str(tmp_path / "ck"), "stride": 2}
+    part["stop_after_node"] = 3
+    first = run(sl3d, "solve", part, tmp_path)
+    assert first.returncode == 0 and "stopped after node 3" in first.stdout, first.stdout + first.stderr
+    assert not (tmp_path / "resumed.txt").exists()
+    assert sorted(p.name for p in (tmp_path / "ck").glob("*.ckpt")) == ["node_000000.ckpt", "node_000002.ckpt"]
+    part.pop("stop_after_node")
+    part["restart"] = True
+    second = run(sl3d, "solve", part, tmp_path)
+    assert second.returncode == 0 and "resumed after node 2" in second.stdout, second.stdout + second.stderr
+    assert (tmp_path / "resumed.txt").read_bytes() == (tmp_path / "whole.txt").read_bytes()
+    columns = table(tmp_path / "whole.txt").shape[1]
+    assert columns == (10 if ocean else 8)
+    # another run's checkpoints are refused
+    other = dict(part)
+    other["lateral"] = {"viscosity": {"seed": 4, "degree": 4, "rms": 0.8}}
+    refused = run(sl3d, "solve", other, tmp_path)
+    assert refused.returncode == 1 and "belongs to another run" in refused.stderr, refused.stderr
