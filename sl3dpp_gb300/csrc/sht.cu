@@ -12,6 +12,7 @@
 // the FFT is a mixed-radix (2, 3, 4, 5) Stockham transform in shared memory,
 // one warp per ring (warp-synchronous stages), several rings per CTA.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -1079,17 +1080,25 @@ int Grid::RunGemmF(int N, bool real, Batch& b, const float* B, float* C, bool ac
     SL3D_CHECK_LAUNCH();
     found = panels_.emplace(key, panel).first;
   }
-  {
+  // B split and packed inside the contraction (B and C never overlap here:
+  // the packing warps read B while other CTAs' epilogues write C); with
+  // SL3DGPU_PACKB=1 by the separate pass, through HBM
+  static const bool separatePack = [] {
+    const char* v = std::getenv("SL3DGPU_PACKB");
+    return v != nullptr && v[0] == '1';
+  }();
+  if (separatePack) {
     prof::Scope scope(prof::kStream, stream, 0.0, 12.0 * b.packedFloats / 2);
     LaunchPackB(items, b.count, b.maxBTiles, b.tileN, B, b.packed, stream);
     SL3D_CHECK_LAUNCH();
   }
-  // algorithmic traffic: the table panel once, B's packed tiles once per
-  // row tile, C once
+  // algorithmic traffic: the table panel once, B once per row tile (4 bytes
+  // a value read in the contraction; 8 from the packed tiles), C once
   prof::Scope scope(prof::kLegendre32, stream, b.flops,
-                    4.0 * b.panelFloats + 4.0 * b.packedFloats * b.maxMTiles + 4.0 * b.outputs);
-  return RunGemmTc(items, b.dTcTiles, static_cast<int>(b.tcTiles.size()), b.tileN, found->second, b.packed, C,
-                   accumulate, dTcError_, stream);
+                    4.0 * b.panelFloats + (separatePack ? 4.0 : 2.0) * b.packedFloats * b.maxMTiles +
+                        4.0 * b.outputs);
+  return RunGemmTc(items, b.dTcTiles, static_cast<int>(b.tcTiles.size()), b.tileN, found->second, b.packed,
+                   separatePack ? nullptr : B, C, accumulate, dTcError_, stream);
 }
 
 Grid::Batch* Grid::MutableBatch(int N, bool real, bool analysis, int P, int p0, int count) {

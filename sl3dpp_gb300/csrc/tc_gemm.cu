@@ -2,7 +2,8 @@
 //
 // A persistent, warp-specialised kernel (TcGemmKernel, below): a TMA
 // producer lane fills a ring of shared-memory stages (the A tile's high and
-// low TF32 parts, 16 KB; B's, 2 x tileN x 64 B), an MMA lane issues each
+// low TF32 parts, 16 KB; B's, 2 x tileN x 64 B, split and packed there by two
+// warps from B's source), an MMA lane issues each
 // 16-deep step's tcgen05.mma kind::tf32 into one of two TMEM accumulators,
 // and four epilogue warps drain the other. B's high and low parts form one
 // operand of 2 tileN rows, so that for tileN <= 128 the products A_hi B_hi
@@ -119,11 +120,23 @@ __global__ void PackBKernel(const TcItem* tcItems, int tileN, const float* B, fl
 // bounded: one that gives up sets the error flag and a shared abort flag that
 // ends the other roles' loops; before TMEM is freed the MMA lane waits for its
 // issued MMAs and the producer for its issued copies (bounded too).
-constexpr int kPersistentThreads = 192;
+//
+// With rawB, B is not packed beforehand: the packing warps (6 .. 9, a step
+// each in turn) read the step's 16 x tileN slice of B straight from its
+// source (four coalesced reads down a column a lane, per 4-deep group),
+// split it into its TF32 high and low parts and store them in the stage's B
+// tile in the core-matrix layout, then fence the stores for the tensor
+// cores' (async) proxy and arrive on the stage's "full" barrier beside the
+// producer's A copy -- the packing pass and its round trip through HBM are
+// gone, and B is read at 4 bytes a value.
+constexpr int kPackWarps = 4;  // warps 6 .. 9, a step each in turn
+constexpr int kPersistentThreads = 32 * (6 + kPackWarps);
+constexpr int kPackChunk = 16;  // (column, group) items a lane loads before it stores (64 reads in flight)
 
 __global__ void __launch_bounds__(kPersistentThreads, 1)
     TcGemmKernel(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN, int stages,
-                 const float* panels, const float* packed, float* C, bool accumulate, int* errorFlag) {
+                 const float* panels, const float* packed, const float* rawB, float* C, bool accumulate,
+                 int* errorFlag) {
   const int bTileFloats = tileN * kTcTileK;
   // tileN <= 128: A_hi B_hi and A_hi B_lo in one MMA of N = 2 tileN, into
   // the accumulator's two column halves (summed by the epilogue)
@@ -150,10 +163,11 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  const uint32_t fullCount = rawB != nullptr ? 1 + 32 : 1;  // the producer, and the packing warp of the step
   if (tid == 0) {
     abortFlag = 0;
     for (int s = 0; s < stages; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(full + s)), "r"(1) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(full + s)), "r"(fullCount) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(empty + s)), "r"(1) : "memory");
     }
     for (int a = 0; a < 2; ++a) {
@@ -189,18 +203,20 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
         }
         if (abortFlag) break;
         const uint32_t bar = SmemAddr(full + slot);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(aBytes + bBytes)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                     "r"(rawB != nullptr ? aBytes : aBytes + bBytes)
                      : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                 SmemAddr(sA + slot * 2 * kATileFloats)),
             "l"(aSrc + static_cast<long long>(ks) * 2 * kATileFloats), "r"(aBytes), "r"(bar)
             : "memory");
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                SmemAddr(sB + slot * 2 * bTileFloats)),
-            "l"(bSrc + static_cast<long long>(ks) * 2 * bTileFloats), "r"(bBytes), "r"(bar)
-            : "memory");
+        if (rawB == nullptr)
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                  SmemAddr(sB + slot * 2 * bTileFloats)),
+              "l"(bSrc + static_cast<long long>(ks) * 2 * bTileFloats), "r"(bBytes), "r"(bar)
+              : "memory");
       }
     }
     // the copies issued last land before the CTA can end (the MMA lane has
@@ -291,6 +307,69 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
                        SmemAddr(drain))
                    : "memory");
       if (!WaitParity(SmemAddr(drain), 0)) atomicExch(errorFlag, 1);
+    }
+  } else if (warp >= 6) {
+    // -- B's split and pack, in shared memory: packing warp p takes the
+    // steps g = p, p + kPackWarps, ..., so that kPackWarps steps' reads are in
+    // flight; a lane loads all its items' values before it converts and
+    // stores any (its loads overlap)
+    if (rawB != nullptr) {
+      const int packer = warp - 6;
+      const int groups = kTcTileK / 4;
+      long long g = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < tileCount && !abortFlag && ok; t += gridDim.x) {
+        const int4 tile = tiles[t];
+        const TcItem it = tcItems[tile.x];
+        const int nBase = tile.z * tileN;
+        const int items = tileN * groups;
+        for (int ks = 0; ks < it.kSteps; ++ks, ++g) {
+          if (static_cast<int>(g % kPackWarps) != packer) continue;
+          const int slot = static_cast<int>(g % stages);
+          const long long round = g / stages;
+          if (round > 0 && !WaitParity(SmemAddr(empty + slot), static_cast<uint32_t>((round - 1) & 1))) {
+            ok = false;
+            break;
+          }
+          if (abortFlag) break;
+          float* out = sB + slot * 2 * bTileFloats;
+          for (int first = 0; first < items; first += 32 * kPackChunk) {
+            float v[kPackChunk][4];
+#pragma unroll
+            for (int j = 0; j < kPackChunk; ++j) {
+              const int item = first + lane + 32 * j;
+              const int nn = item % tileN, grp = item / tileN;
+              const int n = nBase + nn, k0 = ks * kTcTileK + 4 * grp;
+              const bool in = item < items && n < it.N;
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                v[j][q] = (in && k0 + q < it.K) ? __ldg(rawB + it.b + static_cast<long long>(k0 + q) * it.ldb + n)
+                                                : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < kPackChunk; ++j) {
+              const int item = first + lane + 32 * j;
+              if (item >= items) break;
+              const int nn = item % tileN, grp = item / tileN;
+              float4 hi, lo;
+              hi.x = RoundTf32(v[j][0]);
+              hi.y = RoundTf32(v[j][1]);
+              hi.z = RoundTf32(v[j][2]);
+              hi.w = RoundTf32(v[j][3]);
+              lo.x = v[j][0] - hi.x;
+              lo.y = v[j][1] - hi.y;
+              lo.z = v[j][2] - hi.z;
+              lo.w = v[j][3] - hi.w;
+              *reinterpret_cast<float4*>(out + TileIndex(nn, 4 * grp, 2 * tileN)) = hi;
+              *reinterpret_cast<float4*>(out + TileIndex(tileN + nn, 4 * grp, 2 * tileN)) = lo;
+            }
+          }
+          // the stores visible to the tensor cores before the stage is full
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(SmemAddr(full + slot)) : "memory");
+        }
+      }
+      if (!ok) giveUp();
     }
   } else if (warp >= 2) {
     // -- epilogue ----------------------------------------------------------------
@@ -398,7 +477,8 @@ void LaunchPackB(const TcItem* tcItems, int count, int maxTiles, int tileN, cons
 }
 
 int RunGemmTc(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN, const float* panels,
-              const float* packed, float* C, bool accumulate, int* errorFlag, cudaStream_t stream) {
+              const float* packed, const float* rawB, float* C, bool accumulate, int* errorFlag,
+              cudaStream_t stream) {
   if (tileCount == 0) return SL3DGPU_OK;
   static const int sms = [] {
     int device = 0, count = 0;
@@ -412,7 +492,7 @@ int RunGemmTc(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN
   SL3D_CUDA(AllowDynamicSmem(TcGemmKernel));
   const int blocks = std::min(tileCount, sms);
   TcGemmKernel<<<blocks, kPersistentThreads, smem, stream>>>(tcItems, tiles, tileCount, tileN, stages, panels,
-                                                            packed, C, accumulate, errorFlag);
+                                                            packed, rawB, C, accumulate, errorFlag);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }

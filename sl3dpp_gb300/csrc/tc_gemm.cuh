@@ -4,11 +4,12 @@
 // the "3xTF32" split, about FP32 accuracy) accumulated in FP32 in tensor
 // memory.
 //
-// Both operands reach shared memory by TMA bulk copies of ready-made tiles:
-// A (the Legendre table) is pre-tiled once per (spin, direction) into
-// "panels" of 128 x 16 tiles in the canonical K-major core-matrix layout,
-// high part then low part; B is packed per call the same way (tileN x 16
-// tiles) by a split-and-pack pass.
+// A (the Legendre table) reaches shared memory by TMA bulk copies of
+// ready-made tiles: pre-tiled once per (spin, direction) into "panels" of
+// 128 x 16 tiles in the canonical K-major core-matrix layout, high part then
+// low part. B is split and packed the same way (tileN x 16 tiles) inside the
+// contraction, from its source, by two warps (or, the older form, by a
+// separate split-and-pack pass through HBM).
 #pragma once
 
 #include <cstdint>
@@ -76,8 +77,11 @@ void LaunchPackB(const TcItem* tcItems, int count, int maxTiles, int tileN, cons
 // entry), persistent CTAs, one per SM. errorFlag: a device int set non-zero
 // if a completion wait gives up (the launch then leaves C unspecified and
 // the caller reports it).
+// rawB non-null: B is split and packed inside the kernel from its source
+// (packed is then not read); null: from the packed tiles (LaunchPackB).
 int RunGemmTc(const TcItem* tcItems, const int4* tiles, int tileCount, int tileN, const float* panels,
-              const float* packed, float* C, bool accumulate, int* errorFlag, cudaStream_t stream);
+              const float* packed, const float* rawB, float* C, bool accumulate, int* errorFlag,
+              cudaStream_t stream);
 
 // -- FP64 emulated on the tensor cores (tc_gemm64.cu) ------------------------------------
 //
