@@ -223,6 +223,27 @@ def build_operator(device, precision, emulation=None):
     return op, full, dt
 
 
+def max_over_ranks(values, device=None):
+    """The largest of each value over the ranks (the slowest rank's times):
+    an all-reduce MAX over the process group (on the device under NCCL, on
+    the host under gloo); the values themselves with one rank."""
+    import torch
+
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    on = device if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=on)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu().tolist()]
+
+
+def aggregate_rate(steps_per_rank: int, world: int, seconds: float) -> float:
+    """Whole-job steps/s: every rank's steps (replicas of the workload, the
+    weak-scaling form) over the slowest rank's time."""
+    return steps_per_rank * world / seconds
+
+
 def gpu_arm(args, rank, world, device, precision, emulation=None, e2e=True, profile_apart=True):
     """Steps W .. W + K - 1 of the workload, from the same warmed start each
     time: timed with the loads resident in device memory (CUDA events on the
@@ -312,10 +333,8 @@ def gpu_arm(args, rank, world, device, precision, emulation=None, e2e=True, prof
                 raise RuntimeError(f"non-finite surface at end-to-end step {n}")
         e2e_s = time.perf_counter() - t0
         del state
-    times = torch.tensor([ms / 1e3, e2e_s], device=device, dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    return {"op": op, "seconds": times[0].item(), "e2e_seconds": times[1].item(), "passes": passes,
+    seconds, e2e_seconds = max_over_ranks([ms / 1e3, e2e_s], device)
+    return {"op": op, "seconds": seconds, "e2e_seconds": e2e_seconds, "passes": passes,
             "corrections": corrections, "surfaces": surfaces, "history": history,
             "infos": infos, "profile": prof, "launches": launches, "clocks": clocks.summary(),
             "setup_s": setup_s, "load_bytes": int(full.numel() * 16)}
@@ -715,8 +734,8 @@ def main():
     lib().sl3dgpu_fp32_fma_peak(ctypes.byref(fp32))
     r = gpu_arm(args, rank, world, device, args.precision)
     steps_total = args.steps * world
-    value = steps_total / r["seconds"]
-    e2e = steps_total / r["e2e_seconds"]
+    value = aggregate_rate(args.steps, world, r["seconds"])
+    e2e = aggregate_rate(args.steps, world, r["e2e_seconds"])
     passes_per_step = r["passes"] / args.steps
     line = {"metric": METRIC if args.precision == "mixed" else "3D steps/sec at lmax=256 (plain FP64 GPU)",
             "value": value, "unit": "steps/s", "n_gpus": world,
