@@ -304,6 +304,19 @@ int sl3dgpu_ep3d_solve_lateral(sl3dgpu_ep3d* op, const double* load, double rtol
 /* Surface U (0), V (1) or phi (2) of the held solution, (l, m >= 0). */
 int sl3dgpu_ep3d_surface(sl3dgpu_ep3d* op, int component, double* out);
 int sl3dgpu_ep3d_residual_history(const sl3dgpu_ep3d* op, double* out, int capacity);
+/* Force and Apply (ElasticPerturbation3D.hpp:98-130) on solutions held in
+ * device memory: the spheroidal then the toroidal systems' complex values
+ * (sl3dgpu_ep3d_layout's counts; degree l's block [dof][l + 1] at
+ * sl3dgpu_v3d_solution_layout's offsets of the same shape), x and out
+ * distinct. force: (dK) x under the set directions; apply: (K_ref + dK) x;
+ * load_forces: LoadForces, the unit load vectors times a load's host
+ * coefficients (spheroidal; toroidal zero); solution: the held solution
+ * copied out. */
+int sl3dgpu_ep3d_layout(const sl3dgpu_ep3d* op, long long* spheroidal, long long* toroidal);
+int sl3dgpu_ep3d_force(sl3dgpu_ep3d* op, const double* x, double* out);
+int sl3dgpu_ep3d_apply(sl3dgpu_ep3d* op, const double* x, double* out);
+int sl3dgpu_ep3d_load_forces(sl3dgpu_ep3d* op, const double* load, double* out);
+int sl3dgpu_ep3d_solution(sl3dgpu_ep3d* op, double* out);
 
 /* ---- one degree's system (include/sl3dpp/DegreeOperator.hpp:94-384) -------
  * DegreeOperator (toroidal = 0) or ToroidalOperator (toroidal = 1, l >= 1) of

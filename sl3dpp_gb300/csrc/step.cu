@@ -371,6 +371,35 @@ class Viscoelastic3DGpu {
   long long StateBytes(const V3dState& st) const;
   int SaveState(const V3dState& st, char* out, long long capacity);
   int LoadState(V3dState& st, const char* in, long long bytes);
+  // ElasticPerturbation3D::Force / Apply / LoadForces on device solutions
+  // in the [spheroidal | toroidal] layout, and the held solution.
+  int StaticForce(const double2* x, double2* out) {
+    SL3D_TRY(PerturbationForce(x, out));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    return SL3DGPU_OK;
+  }
+  int StaticApply(const double2* x, double2* out) {
+    SL3D_TRY(ApplyPerturbed(*elastic, x, out));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    return SL3DGPU_OK;
+  }
+  int StaticLoadForces(const double* load, double2* out) {
+    const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+    SL3D_CUDA(cudaMemcpyAsync(sigma0.p, load, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    SL3D_CUDA(cudaMemsetAsync(out, 0, Columns() * sizeof(double2), stream));
+    LaunchAddLoad(geo, sigma0.p, elastic->loadForces.p, elastic->unitOffset.p, out, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    return SL3DGPU_OK;
+  }
+  int StaticSolution(double2* out) {
+    SL3D_CUDA(cudaMemcpyAsync(out, rhsSph.p, rhsSphComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+    if (rhsTorComplex > 0)
+      SL3D_CUDA(cudaMemcpyAsync(out + rhsSphComplex, rhsTor.p, rhsTorComplex * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    return SL3DGPU_OK;
+  }
   int Change(const double2* next, const double2* now, double* out) {
     SL3D_TRY(RelativeChange(next, now, out));
     return SL3DGPU_OK;
@@ -3414,6 +3443,48 @@ extern "C" int sl3dgpu_ep3d_respond(sl3dgpu_ep3d* h) {
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.Respond();
+}
+
+extern "C" int sl3dgpu_ep3d_layout(const sl3dgpu_ep3d* h, long long* spheroidal, long long* toroidal) {
+  if (h == nullptr) {
+    SetError("ep3d: null handle");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (spheroidal) *spheroidal = h->op.rhsSphComplex;
+  if (toroidal) *toroidal = h->op.rhsTorComplex;
+  return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_ep3d_force(sl3dgpu_ep3d* h, const double* x, double* out) {
+  if (h == nullptr || x == nullptr || out == nullptr || x == out) {
+    SetError("ep3d: a handle and distinct device solutions and output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StaticForce(reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(out));
+}
+
+extern "C" int sl3dgpu_ep3d_apply(sl3dgpu_ep3d* h, const double* x, double* out) {
+  if (h == nullptr || x == nullptr || out == nullptr || x == out) {
+    SetError("ep3d: a handle and distinct device solutions and output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StaticApply(reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(out));
+}
+
+extern "C" int sl3dgpu_ep3d_load_forces(sl3dgpu_ep3d* h, const double* load, double* out) {
+  if (h == nullptr || load == nullptr || out == nullptr) {
+    SetError("ep3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StaticLoadForces(load, reinterpret_cast<double2*>(out));
+}
+
+extern "C" int sl3dgpu_ep3d_solution(sl3dgpu_ep3d* h, double* out) {
+  if (h == nullptr || out == nullptr) {
+    SetError("ep3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StaticSolution(reinterpret_cast<double2*>(out));
 }
 
 extern "C" int sl3dgpu_ep3d_solve_lateral(sl3dgpu_ep3d* h, const double* load, double rtol, int max_iterations,

@@ -46,6 +46,11 @@ def _signatures():
         "sl3dgpu_ep3d_solve_lateral": (i, [v, v, d, i, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_ep3d_surface": (i, [v, i, v]),
         "sl3dgpu_ep3d_residual_history": (i, [v, P_double, i]),
+        "sl3dgpu_ep3d_layout": (i, [v, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+        "sl3dgpu_ep3d_force": (i, [v, v, v]),
+        "sl3dgpu_ep3d_apply": (i, [v, v, v]),
+        "sl3dgpu_ep3d_load_forces": (i, [v, v, v]),
+        "sl3dgpu_ep3d_solution": (i, [v, v]),
     }
     L = lib()
     for name, (res, args) in sig.items():
@@ -136,6 +141,40 @@ class ElasticPerturbation3D:
         code = COMPONENTS[component] if isinstance(component, str) else int(component)
         out = np.zeros((self.lmax + 1) * (self.lmax + 2) // 2, dtype=np.complex128)
         check(lib().sl3dgpu_ep3d_surface(self._h, code, out.ctypes.data))
+        return out
+
+    # -- Force / Apply / LoadForces on device solutions (CUDA complex128
+    # tensors in the spheroidal-then-toroidal layout)
+
+    def _solutions(self):
+        import torch
+
+        s, tor = ctypes.c_longlong(), ctypes.c_longlong()
+        check(lib().sl3dgpu_ep3d_layout(self._h, ctypes.byref(s), ctypes.byref(tor)))
+        return torch.zeros(s.value + max(tor.value, 1), dtype=torch.complex128, device="cuda")
+
+    def Solution(self):
+        """The held solution (SolveLoad's, Respond's or SolveLateral's)."""
+        out = self._solutions()
+        check(lib().sl3dgpu_ep3d_solution(self._h, out.data_ptr()))
+        return out
+
+    def Force(self, x):
+        """ElasticPerturbation3D::Force: (dK) x under the set directions."""
+        out = self._solutions()
+        check(lib().sl3dgpu_ep3d_force(self._h, x.data_ptr(), out.data_ptr()))
+        return out
+
+    def Apply(self, x):
+        """ElasticPerturbation3D::Apply: (K_ref + dK) x."""
+        out = self._solutions()
+        check(lib().sl3dgpu_ep3d_apply(self._h, x.data_ptr(), out.data_ptr()))
+        return out
+
+    def LoadForces(self, load):
+        out = self._solutions()
+        load = self._load(load)
+        check(lib().sl3dgpu_ep3d_load_forces(self._h, load.ctypes.data, out.data_ptr()))
         return out
 
     def residual_history(self) -> np.ndarray:

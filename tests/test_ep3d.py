@@ -151,3 +151,36 @@ def test_gpu_static_perturbation_matches_the_oracle(gpu):
         assert np.max(np.abs(hg[big] - ho[big]) / ho[big]) < 1e-6
         for comp in (0, 1, 2):
             assert rel(g.Surface(comp), o.surface(comp)) < TOL
+
+
+@pytest.mark.gpu
+def test_gpu_force_and_apply_are_the_solves_operators(gpu):
+    """Force and Apply through the C ABI (ElasticPerturbation3D.hpp:98-130)
+    agree with the solves: SolveLoad's solution x has K_ref x = LoadForces,
+    so Apply(x) - Force(x) is the load's forces; SolveLateral's solution
+    satisfies Apply(x) = LoadForces to its tolerance; Force is linear and
+    vanishes without directions."""
+    import torch
+
+    from sl3dpp_gb300.elastic_perturbation3d import ElasticPerturbation3D
+
+    lmax = 8
+    o = O.OraclePerturbation(_layers(), lmax)
+    g = ElasticPerturbation3D(_layers(product=True), lmax)
+    mu = _nodal(o, "mu")
+    r = o.radius
+    d_mu = _lateral(o, 0.1 * mu.max() * (0.5 + r * r),
+                    lambda t, p: np.sin(t) * np.cos(t) * np.cos(p) + 0.3 * np.cos(2 * p) * np.sin(t) ** 2)
+    load = _load(lmax, 1e3 / o.sigma_scale)
+    g.set_moduli(d_mu, None)
+    g.SolveLoad(load)
+    x = g.Solution()
+    f = g.LoadForces(load)
+    scale = torch.max(torch.abs(f)).item()
+    assert (torch.max(torch.abs(g.Apply(x) - g.Force(x) - f)) / scale).item() < 1e-10
+    assert (torch.max(torch.abs(g.Force(2.0 * x) - 2.0 * g.Force(x))) / scale).item() < 1e-13
+    g.SolveLateral(load, rtol=1e-12)
+    y = g.Solution()
+    assert (torch.max(torch.abs(g.Apply(y) - f)) / scale).item() < 1e-9
+    g.set_moduli(None, None)
+    assert torch.max(torch.abs(g.Force(y))).item() == 0.0
