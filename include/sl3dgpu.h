@@ -565,6 +565,17 @@ int sl3dgpu_v3d_step_strain_of(sl3dgpu_v3d* op, double* device_out);
 int sl3dgpu_v3d_step_converge(sl3dgpu_v3d* op, const double* load, const double* tide, double* device_strain,
                               sl3dgpu_step_info* info);
 int sl3dgpu_v3d_step_finish(sl3dgpu_v3d* op, const double* strain);
+/* The conjugate-gradient close's pieces (options.solver = 1): step_forces,
+ * OpenStep::Forces -- the degree forces of the fixed memory force and of
+ * the channels (host coefficients, nullable) into device solutions laid out
+ * spheroidal then toroidal (sl3dgpu_v3d_layout's counts); step_apply,
+ * OpenStep::Apply -- (K_eff - P^T W S) x; step_solve, OpenStep::Solve -- the
+ * solutions for given forces by preconditioned conjugate gradients from the
+ * reference response (out nullable; the solutions are also held, so
+ * step_strain_of and the surface read them). */
+int sl3dgpu_v3d_step_forces(sl3dgpu_v3d* op, const double* load, const double* tide, double* out);
+int sl3dgpu_v3d_step_apply(sl3dgpu_v3d* op, const double* x, double* out);
+int sl3dgpu_v3d_step_solve(sl3dgpu_v3d* op, const double* forces, double* out, sl3dgpu_step_info* info);
 int sl3dgpu_v3d_relative_change(sl3dgpu_v3d* op, const double* next, const double* now, double* out);
 
 /* ---- the grid coupling (GridCoupling, include/sl3dpp/GridCoupling.hpp:82-428) ----

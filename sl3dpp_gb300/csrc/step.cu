@@ -352,6 +352,13 @@ class Viscoelastic3DGpu {
   int OpenChannels(const double* load, const double* tide);
   int OpenConverge(const double* load, const double* tide, sl3dgpu_step_info* info);
   int OpenFinish(const double2* strain);
+  // OpenStep::Forces / Apply / Solve (the conjugate-gradient close, under
+  // Options::solver = ConjugateGradients): the step's degree forces (the
+  // fixed memory force's and the channels'), (K_eff - P^T W S) x, and the
+  // solutions for given forces from the reference response.
+  int OpenForces(const double* load, const double* tide, double2* out);
+  int OpenApply(const double2* x, double2* out);
+  int OpenSolve(const double2* forces, double2* out, sl3dgpu_step_info* info);
   int OpenRespond(const double2* strain) {
     SL3D_TRY(OpenCheck());
     SL3D_TRY(Respond(*opened.f, strain, strain == nullptr));
@@ -2708,6 +2715,66 @@ int Viscoelastic3DGpu::OpenConverge(const double* load, const double* tide, sl3d
   return SL3DGPU_OK;
 }
 
+int Viscoelastic3DGpu::OpenForces(const double* load, const double* tide, double2* out) {
+  SL3D_TRY(OpenCheck());
+  if (options.solver != 1) {
+    SetError("v3d: the open step's forces and operator are the conjugate-gradient close's (solver 1)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  const Flavour& f = *opened.f;
+  SL3D_CUDA(cudaMemsetAsync(out, 0, Columns() * sizeof(double2), stream));
+  LaunchForces(geo, fixedS.p, out, out + rhsSphComplex, stream);
+  SL3D_CHECK_LAUNCH();
+  const double2* sigma = nullptr;
+  const double2* psi = nullptr;
+  if (load != nullptr) {
+    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, load, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    sigma = sigma1.p;
+  }
+  if (tide != nullptr) {
+    if (tideDev1.n != lm) SL3D_CUDA(tideDev1.Alloc(lm));
+    SL3D_CUDA(cudaMemcpyAsync(tideDev1.p, tide, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    psi = tideDev1.p;
+  }
+  if (sigma != nullptr || psi != nullptr) {
+    LaunchAddLoad(geo, sigma, f.loadForces.p, f.unitOffset.p, out, stream, psi, f.tideForces.p);
+    SL3D_CHECK_LAUNCH();
+  }
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::OpenApply(const double2* x, double2* out) {
+  SL3D_TRY(OpenCheck());
+  if (options.solver != 1) {
+    SetError("v3d: the open step's forces and operator are the conjugate-gradient close's (solver 1)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SL3D_TRY(ApplyOperator(*opened.f, x, out));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::OpenSolve(const double2* forces, double2* out, sl3dgpu_step_info* infoOut) {
+  SL3D_TRY(OpenCheck());
+  if (options.solver != 1) {
+    SetError("v3d: the open step's forces and operator are the conjugate-gradient close's (solver 1)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SL3D_CUDA(cudaMemcpyAsync(cgF.p, forces, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  sl3dgpu_step_info info{};
+  history.clear();
+  SL3D_TRY(ConjugateGradients(*opened.f, true, options.solve_rtol, options.solve_max_iterations, info));
+  info.iterations = info.solve_iterations;
+  SL3D_TRY(HoldSolution(cgX.p));
+  if (out != nullptr)
+    SL3D_CUDA(cudaMemcpyAsync(out, cgX.p, Columns() * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  if (infoOut) *infoOut = info;
+  return SL3DGPU_OK;
+}
+
 int Viscoelastic3DGpu::OpenFinish(const double2* strain) {
   SL3D_TRY(OpenCheck());
   if (strain != nullptr)
@@ -3024,6 +3091,33 @@ extern "C" int sl3dgpu_v3d_step_converge(sl3dgpu_v3d* h, const double* load, con
     SL3D_CUDA(cudaStreamSynchronize(op.stream));
   }
   return SL3DGPU_OK;
+}
+
+extern "C" int sl3dgpu_v3d_step_forces(sl3dgpu_v3d* h, const double* load, const double* tide, double* out) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (out == nullptr) {
+    SetError("v3d: null output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.OpenForces(load, tide, reinterpret_cast<double2*>(out));
+}
+
+extern "C" int sl3dgpu_v3d_step_apply(sl3dgpu_v3d* h, const double* x, double* out) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (x == nullptr || out == nullptr || x == out) {
+    SetError("v3d: distinct device solutions and output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.OpenApply(reinterpret_cast<const double2*>(x), reinterpret_cast<double2*>(out));
+}
+
+extern "C" int sl3dgpu_v3d_step_solve(sl3dgpu_v3d* h, const double* forces, double* out, sl3dgpu_step_info* info) {
+  SL3D_TRY(NeedStepOperator(h));
+  if (forces == nullptr) {
+    SetError("v3d: null forces");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.OpenSolve(reinterpret_cast<const double2*>(forces), reinterpret_cast<double2*>(out), info);
 }
 
 extern "C" int sl3dgpu_v3d_step_finish(sl3dgpu_v3d* h, const double* strain) {

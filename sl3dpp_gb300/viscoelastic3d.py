@@ -128,6 +128,9 @@ def _signatures():
         "sl3dgpu_v3d_step_strain_of": (i, [v, v]),
         "sl3dgpu_v3d_step_converge": (i, [v, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_step_finish": (i, [v, v]),
+        "sl3dgpu_v3d_step_forces": (i, [v, v, v, v]),
+        "sl3dgpu_v3d_step_apply": (i, [v, v, v]),
+        "sl3dgpu_v3d_step_solve": (i, [v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_relative_change": (i, [v, v, v, P_double]),
         "sl3dgpu_v3d_layout": (i, [v] + [ctypes.POINTER(ctypes.c_longlong)] * 4),
         "sl3dgpu_v3d_solution_layout": (i, [v, i, ctypes.POINTER(ctypes.c_longlong), P_int,
@@ -515,6 +518,32 @@ class OpenStep:
 
     def Finish(self, strain=None) -> None:
         check(lib().sl3dgpu_v3d_step_finish(self.op._h, None if strain is None else strain.data_ptr()))
+
+    # the conjugate-gradient close's pieces (Options solver = 1)
+
+    def _columns(self):
+        lay = self.op.layout()
+        return self._torch.zeros(lay["spheroidal"] + max(lay["toroidal"], 1), dtype=self._torch.complex128,
+                                 device="cuda")
+
+    def Forces(self, load=None, tide=None):
+        a = None if load is None else np.ascontiguousarray(load, dtype=np.complex128)
+        b = None if tide is None else np.ascontiguousarray(tide, dtype=np.complex128)
+        out = self._columns()
+        check(lib().sl3dgpu_v3d_step_forces(self.op._h, None if a is None else a.ctypes.data,
+                                            None if b is None else b.ctypes.data, out.data_ptr()))
+        return out
+
+    def Apply(self, x):
+        out = self._columns()
+        check(lib().sl3dgpu_v3d_step_apply(self.op._h, x.data_ptr(), out.data_ptr()))
+        return out
+
+    def Solve(self, forces):
+        out = self._columns()
+        info = StepInfo()
+        check(lib().sl3dgpu_v3d_step_solve(self.op._h, forces.data_ptr(), out.data_ptr(), ctypes.byref(info)))
+        return out, info
 
 
 class Evolution3D:

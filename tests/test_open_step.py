@@ -121,3 +121,32 @@ def test_gpu_grid_coupling_identities(gpu):
     step.Finish(mine)
     layout = op.solution_layout(3)
     assert layout["sph_dofs"] > 0 and layout["tor_dofs"] > 0
+
+
+@pytest.mark.gpu
+def test_gpu_conjugate_gradient_close_through_the_open_step(gpu):
+    """Under the conjugate-gradient step solver: Forces, Solve and Apply of
+    the open step (OpenStep::Forces / Solve / Apply) close the stage as the
+    operator's own Step does -- the solution satisfies Apply(x) = Forces to
+    the solve's tolerance, its strain finishes the stage to the step's
+    surface and state."""
+    import torch
+
+    lmax = 10
+    opt = dict(rtol=1e-11, max_iterations=80, solver=1, solve_rtol=1e-12, solve_max_iterations=300)
+    o, ref, drv = _ops(lmax, **opt)
+    full = cap_load(lmax, o.sigma_scale, 2000.0)
+    h = GAMMA * 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    s_ref, s_drv = ref.ZeroState(), drv.ZeroState()
+    info = ref.Step(s_ref, h, "backward_euler", 0 * full, full)
+    step = drv.StartStep(s_drv, h, 1, 0 * full)
+    f = step.Forces(full)
+    x, si = step.Solve(f)
+    assert si.converged and si.solve_iterations == info.solve_iterations
+    resid = (torch.max(torch.abs(step.Apply(x) - f)) / torch.max(torch.abs(f))).item()
+    assert resid < 1e-9, resid
+    strain = step.StrainOf()
+    step.Finish(strain)
+    for comp in (0, 2):
+        assert rel(drv.Surface(comp), ref.Surface(comp)) < 1e-13
+    assert rel(s_drv.strain_coefficients(), s_ref.strain_coefficients()) < 1e-13
