@@ -32,8 +32,9 @@
 // the 3D step (step_kernels.cu) with the reference's memory and plain start;
 // the integrals sum each ring in a fixed tree and the rings in order (the
 // grid's Integrate, SurfaceGrid.hpp:257-267); the stopping test's maxima are
-// order-free. A few scalars per iteration come to the host: the integral, the
-// two maxima and the rotation block's coefficients. A workspace (SleWorkspace)
+// order-free. The rotation block (RotationPatchKernel) and the conservation's
+// shift (ShiftKernel) are formed on the device; an iteration brings one
+// thing to the host, the stopping test's maxima. A workspace (SleWorkspace)
 // keeps the buffers between solves on one grid, so that the coupled closure's
 // solve in every pass of a step allocates nothing.
 #include <algorithm>
@@ -110,9 +111,11 @@ __global__ void SeedKernel(long long n, const double* direct, const double* ocea
 
 // S += shift; C S; the next load sigma_d + rho_w C S; per block the largest
 // |C S - C S_prev| and |C S| (blockIdx-ordered partials), C S kept for the next test.
-__global__ void ShiftAndLoadKernel(long long n, double shift, double rho, const double* direct, const double* ocean,
-                                   double* slc, double* oceanSlc, double* newLoad, bool havePrev, double* maxima) {
+__global__ void ShiftAndLoadKernel(long long n, const double* shiftPtr, double rho, const double* direct,
+                                   const double* ocean, double* slc, double* oceanSlc, double* newLoad, bool havePrev,
+                                   double* maxima) {
   __shared__ double red[2][kRingThreads];
+  const double shift = *shiftPtr;
   double dmax = 0.0, smax = 0.0;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
@@ -217,6 +220,94 @@ struct SleRun {
     return SL3DGPU_OK;
   }
 };
+
+// The conservation's uniform shift on the device: a^2 dphi sum_rings of the
+// ring partials of C S, in order (the host's Integrate), then s_mean minus
+// it over the ocean's area (src/SeaLevel.cpp:655-661).
+__global__ void ShiftKernel(const double* ringPartial, int ntheta, double scale, double meanSlc, double perOceanArea,
+                            double* shift) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double sum = 0.0;
+  for (int j = 0; j < ntheta; ++j) sum += ringPartial[j];
+  shift[0] = meanSlc - scale * sum * perOceanArea;
+}
+
+// GRDSolver::Rotation's inputs that do not change within a solve: the
+// factors of the constructor (src/SeaLevel.cpp:220-247), the static blocks
+// and scalars of the forcing. Blocks as {(2,0), cos(2,1), 0, sin(2,1)}.
+struct RotationInputs {
+  int transverse;
+  double h2, k2, ht2, kt2, hc, kc, mu, mphi, mc, g, lt2;
+  double rotation, inertia, axialRotation, uniformRotation, axialInertia, inverseInertiaDifference,
+      inversePolarInertia, trace, shell, rotationDenominator, axialRotationDenominator;
+  double staticDisp2[4], staticGrav2[4], tide2[4], layer2[4];
+  double displacementLoad0, potentialLoad0, inertiaMoment, angularMomentum[3];
+};
+
+// The rotation block of the load's (2, 0), (2, 1) and (0, 0) coefficients
+// (GRDSolver::Rotation, src/SeaLevel.cpp:348-392), and the patch of a
+// scaled coefficient vector's degree-0/2 entries, on the device: mode 0 the
+// sea level change's (and the angular velocity out), 1 the displacement's,
+// 2 the potential's, 3 the tangential potential's (src/SeaLevel.cpp:625-640,
+// 714-724). One thread; the host solve's arithmetic in its order.
+__global__ void RotationPatchKernel(const RotationInputs* p, const double* load, double* out, double* omegaOut,
+                                    int mode) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double r2 = sqrt(2.0);
+  // BlockOf of the load: (2,0) re, -sqrt2 re (2,1), sqrt2 im (2,1)
+  const double l00 = load[6], l01 = -r2 * load[8], l11 = r2 * load[9];
+  const double load0 = load[0];
+  const double grav00 = p->k2 * l00 + p->staticGrav2[0], grav01 = p->k2 * l01 + p->staticGrav2[1],
+               grav11 = p->k2 * l11 + p->staticGrav2[3];
+  const double disp00 = p->h2 * l00 + p->staticDisp2[0], disp01 = p->h2 * l01 + p->staticDisp2[1],
+               disp11 = p->h2 * l11 + p->staticDisp2[3];
+  double transverse0 = p->inertia * grav01, transverse1 = p->inertia * grav11;
+  double axial = -p->axialInertia * grav00 -
+                 p->trace * ((p->mu + p->mphi) * load0 + p->mu * p->displacementLoad0 + p->mphi * p->potentialLoad0 +
+                             p->inertiaMoment) -
+                 p->shell * (load0 + p->potentialLoad0);
+  transverse0 -= p->inverseInertiaDifference * p->angularMomentum[0];
+  transverse1 -= p->inverseInertiaDifference * p->angularMomentum[1];
+  axial += p->inversePolarInertia * p->angularMomentum[2];
+  double omega0 = 0.0, omega1 = 0.0;
+  if (p->transverse) {
+    omega0 = transverse0 / p->rotationDenominator;
+    omega1 = transverse1 / p->rotationDenominator;
+  }
+  const double omega2 = axial / p->axialRotationDenominator;
+  const double c00 = p->axialRotation * omega2, c01 = p->rotation * omega0, c11 = p->rotation * omega1;
+  const double centrifugal0 = p->uniformRotation * omega2;
+  const double d00 = disp00 + p->ht2 * c00, d01 = disp01 + p->ht2 * c01, d11 = disp11 + p->ht2 * c11;
+  const double g00 = grav00 + p->kt2 * c00, g01 = grav01 + p->kt2 * c01, g11 = grav11 + p->kt2 * c11;
+  // FromBlock into out[6..9]: (2,0) = b00, (2,1) = (-b01 / sqrt2, b11 / sqrt2)
+  auto put = [&](double b00, double b01, double b11) {
+    out[6] = b00;
+    out[7] = 0.0;
+    out[8] = -b01 / r2;
+    out[9] = b11 / r2;
+  };
+  const double ig = 1.0 / p->g;
+  if (mode == 0) {
+    omegaOut[0] = omega0;
+    omegaOut[1] = omega1;
+    omegaOut[2] = omega2;
+    const double s00 = -((d00 + ((g00 + c00) + p->tide2[0]) * ig) + p->layer2[0]);
+    const double s01 = -((d01 + ((g01 + c01) + p->tide2[1]) * ig) + p->layer2[1]);
+    const double s11 = -((d11 + ((g11 + c11) + p->tide2[3]) * ig) + p->layer2[3]);
+    put(s00, s01, s11);
+    out[0] -= (p->hc + (p->kc + 1.0) / p->g) * centrifugal0;
+  } else if (mode == 1) {
+    put(d00, d01, d11);
+    out[0] += p->hc * centrifugal0;
+  } else if (mode == 2) {
+    put(g00, g01, g11);
+    out[0] += p->kc * centrifugal0;
+  } else {
+    out[6] += p->lt2 * c00;
+    out[8] += -(p->lt2 * c01) / r2;
+    out[9] += (p->lt2 * c11) / r2;
+  }
+}
 
 // The Anderson mixer of the load coefficients (AndersonMixer::Update, the
 // reference's plain form: the first call the image, then memory columns).
@@ -349,39 +440,6 @@ struct RotationFactors {
   }
 };
 
-struct Rotation {
-  std::array<double, 3> omega{0.0, 0.0, 0.0};
-  Block2 disp2{}, grav2{}, centrifugal{};
-  double centrifugal0 = 0.0;
-  // GRDSolver::Rotation's constructor (src/SeaLevel.cpp:348-392): the
-  // degree-0 parts of the displacement and potential load channels enter the
-  // axial trace and shell terms
-  Rotation(const RotationFactors& s, const Block2& load2, double load0, const Block2& staticDisp2,
-           const Block2& staticGrav2, double displacementLoad0, double potentialLoad0, double inertiaMoment,
-           const double* angularMomentum) {
-    const Block2 gravForcing = Plus(Scaled(load2, s.k2), staticGrav2);
-    const Block2 dispForcing = Plus(Scaled(load2, s.h2), staticDisp2);
-    double transverse[2] = {s.inertia * gravForcing[0][1], s.inertia * gravForcing[1][1]};
-    double axial = -s.axialInertia * gravForcing[0][0] -
-                   s.trace * ((s.mu + s.mphi) * load0 + s.mu * displacementLoad0 + s.mphi * potentialLoad0 +
-                              inertiaMoment) -
-                   s.shell * (load0 + potentialLoad0);
-    for (int i = 0; i < 2; ++i) transverse[i] -= s.inverseInertiaDifference * angularMomentum[i];
-    axial += s.inversePolarInertia * angularMomentum[2];
-    if (s.transverse) {
-      omega[0] = transverse[0] / s.rotationDenominator;
-      omega[1] = transverse[1] / s.rotationDenominator;
-    }
-    omega[2] = axial / s.axialRotationDenominator;
-    centrifugal[0][1] = s.rotation * omega[0];
-    centrifugal[1][1] = s.rotation * omega[1];
-    centrifugal[0][0] = s.axialRotation * omega[2];
-    centrifugal0 = s.uniformRotation * omega[2];
-    disp2 = Plus(dispForcing, Scaled(centrifugal, s.ht2));
-    grav2 = Plus(gravForcing, Scaled(centrifugal, s.kt2));
-  }
-};
-
 }  // namespace
 
 // The workspace one solver keeps between solves on one grid: the run's
@@ -392,6 +450,8 @@ struct SleWorkspace {
   LoadMixer mixer;
   int mixerMemory = -1;
   Dev<double> staticDisp, staticGrav, staticTan, staticSlc, scratch, directData;
+  Dev<double> shift, omega, slcFactor;  // the conservation's shift, the angular velocity, -(h + k / g) per degree
+  Dev<RotationInputs> rotation;
   std::vector<double> theta;
 
   // the grid's sizes, quadrature and buffers (once per grid)
@@ -422,6 +482,10 @@ struct SleWorkspace {
     for (auto* d : {&run.seeded, &run.slc, &run.oceanSlc, &run.newLoad}) SL3D_CUDA(d->Alloc(run.fieldSize));
     for (auto* d : {&staticDisp, &staticGrav, &staticTan, &staticSlc, &scratch}) SL3D_CUDA(d->Alloc(nc));
     SL3D_CUDA(directData.Alloc(run.fieldSize));
+    SL3D_CUDA(shift.Alloc(1));
+    SL3D_CUDA(omega.Alloc(3));
+    SL3D_CUDA(slcFactor.Alloc(run.lmax + 1));
+    SL3D_CUDA(rotation.Alloc(1));
     mixerMemory = -1;
     grid = g;
     return SL3DGPU_OK;
@@ -679,43 +743,86 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
       layer2 = BlockOf(head + 6, head + 8);
     }
   }
-  std::array<double, 3> omega{0.0, 0.0, 0.0};
-  // out = f_l L + add, then (rotating) its degree-0/2 coefficients set by
-  // `patch` from the rotation of the load L, and synthesised
-  auto synthesisePatched = [&](const double* f, const double* add, double* field, auto&& patch) -> int {
-    SL3D_TRY(run.ScaleDegrees(f, run.loadLm.p, add, 1.0, run.scaledLm.p));
+  // The rotation's inputs on the device (the static blocks read back once
+  // above), so that each iteration's patch needs no host round trip.
+  if (rf.on) {
+    RotationInputs in{};
+    in.transverse = rf.transverse ? 1 : 0;
+    in.h2 = rf.h2;
+    in.k2 = rf.k2;
+    in.ht2 = rf.ht2;
+    in.kt2 = rf.kt2;
+    in.hc = rf.hc;
+    in.kc = rf.kc;
+    in.mu = rf.mu;
+    in.mphi = rf.mphi;
+    in.mc = rf.mc;
+    in.g = g;
+    in.lt2 = body->lt != nullptr ? body->lt[2] : 0.0;
+    in.rotation = rf.rotation;
+    in.inertia = rf.inertia;
+    in.axialRotation = rf.axialRotation;
+    in.uniformRotation = rf.uniformRotation;
+    in.axialInertia = rf.axialInertia;
+    in.inverseInertiaDifference = rf.inverseInertiaDifference;
+    in.inversePolarInertia = rf.inversePolarInertia;
+    in.trace = rf.trace;
+    in.shell = rf.shell;
+    in.rotationDenominator = rf.rotationDenominator;
+    in.axialRotationDenominator = rf.axialRotationDenominator;
+    auto flat = [](const Block2& b, double* out) {
+      out[0] = b[0][0];
+      out[1] = b[0][1];
+      out[2] = b[1][0];
+      out[3] = b[1][1];
+    };
+    flat(staticDisp2, in.staticDisp2);
+    flat(staticGrav2, in.staticGrav2);
+    flat(tide2, in.tide2);
+    flat(layer2, in.layer2);
+    in.displacementLoad0 = displacementLoad0;
+    in.potentialLoad0 = potentialLoad0;
+    in.inertiaMoment = forcing->inertia_moment_change;
+    for (int i = 0; i < 3; ++i) in.angularMomentum[i] = forcing->angular_momentum_change[i];
+    SL3D_CUDA(cudaMemcpyAsync(ws.rotation.p, &in, sizeof(in), cudaMemcpyHostToDevice, s));
+  }
+  SL3D_CUDA(cudaMemsetAsync(ws.omega.p, 0, 3 * sizeof(double), s));
+  SL3D_CUDA(cudaMemsetAsync(ws.shift.p, 0, sizeof(double), s));
+  // out = f_l L + add, then (rotating) its degree-0/2 coefficients patched by
+  // the rotation of the load L on the device, and synthesised
+  auto synthesisePatched = [&](const double* f, bool factorsOnDevice, const double* add, double* field,
+                               int mode) -> int {
+    if (factorsOnDevice) {
+      ScaleDegreesKernel<<<static_cast<unsigned>((run.coefCount + 255) / 256), 256, 0, s>>>(
+          L, f, reinterpret_cast<const double2*>(run.loadLm.p), reinterpret_cast<const double2*>(add), 1.0,
+          reinterpret_cast<double2*>(run.scaledLm.p));
+      SL3D_CHECK_LAUNCH();
+    } else {
+      SL3D_TRY(run.ScaleDegrees(f, run.loadLm.p, add, 1.0, run.scaledLm.p));
+    }
     if (rf.on) {
-      double load[10], out[10];
-      SL3D_TRY(headOf(run.loadLm.p, load));
-      SL3D_TRY(headOf(run.scaledLm.p, out));
-      const Rotation rot(rf, BlockOf(load + 6, load + 8), load[0], staticDisp2, staticGrav2, displacementLoad0,
-                         potentialLoad0, forcing->inertia_moment_change, forcing->angular_momentum_change);
-      patch(rot, out);
-      SL3D_CUDA(cudaMemcpyAsync(run.scaledLm.p, out, 10 * sizeof(double), cudaMemcpyHostToDevice, s));
+      RotationPatchKernel<<<1, 32, 0, s>>>(ws.rotation.p, run.loadLm.p, run.scaledLm.p, ws.omega.p, mode);
+      SL3D_CHECK_LAUNCH();
     }
     return sl3dgpu_synthesise_batch(grid, run.scaledLm.p, 1, field, s);
   };
-  // the sea level change's blocks (src/SeaLevel.cpp:625-640)
-  auto slcPatch = [&](const Rotation& rot, double* out) {
-    omega = rot.omega;
-    const Block2 b =
-        Scaled(Plus(Plus(rot.disp2, Scaled(Plus(Plus(rot.grav2, rot.centrifugal), tide2), 1.0 / g)), layer2), -1.0);
-    FromBlock(b, out + 6, out + 8);
-    out[0] -= (rf.hc + (rf.kc + 1.0) / g) * rot.centrifugal0;  // uniform: absorbed by conservation
-  };
+  SL3D_CUDA(cudaMemcpyAsync(ws.slcFactor.p, slcFactor.data(), (L + 1) * sizeof(double), cudaMemcpyHostToDevice, s));
 
   SL3D_TRY(ws.ResetMixer(anderson_memory, s));
   LoadMixer& mixer = ws.mixer;
-  double err = INFINITY, shift = 0.0;
+  double err = INFINITY;
   bool converged = false, havePrev = false;
   int count = 0;
   while (count < max_iterations) {
-    // the sea level change of the load, its uniform part by conservation
-    SL3D_TRY(synthesisePatched(slcFactor.data(), slcAdd, run.slc.p, slcPatch));
-    double cs = 0.0;
-    SL3D_TRY(run.Integrate(ocean, run.slc.p, &cs));
-    shift = meanSlc - cs * perOceanArea;
-    ShiftAndLoadKernel<<<blocks, kRingThreads, 0, s>>>(run.fieldSize, shift, water_density, directData.p, ocean,
+    // the sea level change of the load, its uniform part by conservation:
+    // one host round trip an iteration, the stopping test's maxima
+    SL3D_TRY(synthesisePatched(ws.slcFactor.p, true, slcAdd, run.slc.p, 0));
+    RingSumKernel<<<run.ntheta, kRingThreads, 0, s>>>(run.nphi, run.weights.p, ocean, run.slc.p, run.ringPartial.p);
+    SL3D_CHECK_LAUNCH();
+    ShiftKernel<<<1, 32, 0, s>>>(run.ringPartial.p, run.ntheta, run.r2 * run.dphi, meanSlc, perOceanArea,
+                                 ws.shift.p);
+    SL3D_CHECK_LAUNCH();
+    ShiftAndLoadKernel<<<blocks, kRingThreads, 0, s>>>(run.fieldSize, ws.shift.p, water_density, directData.p, ocean,
                                                        run.slc.p, run.oceanSlc.p, run.newLoad.p, havePrev,
                                                        run.maxima.p);
     SL3D_CHECK_LAUNCH();
@@ -744,34 +851,19 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
   SL3D_CUDA(cudaMemcpyAsync(sea_level_change, run.slc.p, run.fieldSize * sizeof(double), cudaMemcpyDeviceToDevice,
                             s));
   const bool withStatic = anyStatic || anyStaticTan;
-  const double lt2 = body->lt != nullptr ? body->lt[2] : 0.0;
   if (displacement)
-    SL3D_TRY(synthesisePatched(body->h, withStatic ? staticDisp.p : nullptr, displacement,
-                               [&](const Rotation& rot, double* out) {
-                                 FromBlock(rot.disp2, out + 6, out + 8);
-                                 out[0] += rf.hc * rot.centrifugal0;
-                               }));
-  if (potential)
-    SL3D_TRY(synthesisePatched(body->k, withStatic ? staticGrav.p : nullptr, potential,
-                               [&](const Rotation& rot, double* out) {
-                                 FromBlock(rot.grav2, out + 6, out + 8);
-                                 out[0] += rf.kc * rot.centrifugal0;
-                               }));
+    SL3D_TRY(synthesisePatched(body->h, false, withStatic ? staticDisp.p : nullptr, displacement, 1));
+  if (potential) SL3D_TRY(synthesisePatched(body->k, false, withStatic ? staticGrav.p : nullptr, potential, 2));
   if (tangential_potential)
-    SL3D_TRY(synthesisePatched(tangential.data(), withStatic ? staticTan.p : nullptr, tangential_potential,
-                               [&](const Rotation& rot, double* out) {
-                                 double c20[2], c21[2];
-                                 FromBlock(Scaled(rot.centrifugal, lt2), c20, c21);
-                                 out[6] += c20[0];
-                                 out[7] += c20[1];
-                                 out[8] += c21[0];
-                                 out[9] += c21[1];
-                               }));
+    SL3D_TRY(synthesisePatched(tangential.data(), false, withStatic ? staticTan.p : nullptr, tangential_potential, 3));
   // TotalLoadCoefficients (src/Evolution3D.cpp:237-249): the direct loads and
   // the ocean's, rho_w C S of the last sea level change
   if (total_load != nullptr) SL3D_TRY(sl3dgpu_expand_batch(grid, run.newLoad.p, 1, total_load, s));
+  double tail[4];
+  SL3D_CUDA(cudaMemcpyAsync(tail, ws.shift.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  SL3D_CUDA(cudaMemcpyAsync(tail + 1, ws.omega.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   SL3D_CUDA(cudaStreamSynchronize(s));
-  *result = sl3dgpu_sle_result{shift, err, count, converged ? 1 : 0, {omega[0], omega[1], omega[2]}};
+  *result = sl3dgpu_sle_result{tail[0], err, count, converged ? 1 : 0, {tail[1], tail[2], tail[3]}};
   return SL3DGPU_OK;
 }
 
