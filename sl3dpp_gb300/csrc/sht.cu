@@ -159,6 +159,93 @@ __global__ void __launch_bounds__(256) GemmKernel(const GemmItem* items, const T
   }
 }
 
+// -- the same contraction for a few columns (N <= 16) --------------------------------------
+//
+// A batch of one to eight fields (the sea-level grid's single load, a few
+// stacked channels) has N = 2 to 16 columns; the 64 x 64 tile above would
+// spend 64 columns of FP64 FMAs on them, and FP64 is GB300's slow pipe. These
+// kernels do only the N columns and stream the table once.
+
+constexpr int kNarrowN = 16;
+
+// Analysis (A row-major in k, sAk = 1): one warp per output row, the lanes
+// over k (coalesced reads of the row), a shuffle sum at the end.
+template <int NT>
+__global__ void __launch_bounds__(256) GemmRowsNarrowKernel(const GemmItem* items, const double* A,
+                                                            const double* B, double* C, bool accumulate) {
+  const GemmItem it = items[blockIdx.y];
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (i >= it.M) return;  // uniform over the warp
+  const double* a = A + it.a + static_cast<long long>(i) * it.sAi;
+  const double* b = B + it.b;
+  double acc[NT] = {};
+  for (int k = lane; k < it.K; k += 32) {
+    const double av = a[k];
+    const double* bk = b + static_cast<long long>(k) * it.ldb;
+#pragma unroll
+    for (int n = 0; n < NT; ++n)
+      if (n < it.N) acc[n] = fma(av, bk[n], acc[n]);
+  }
+#pragma unroll
+  for (int n = 0; n < NT; ++n)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc[n] += __shfl_xor_sync(0xffffffffu, acc[n], off);
+  if (lane != 0) return;
+  double* c = C + it.c + static_cast<long long>(i) * it.ldc;
+#pragma unroll
+  for (int n = 0; n < NT; ++n)
+    if (n < it.N) c[n] = accumulate ? acc[n] + c[n] : acc[n];
+}
+
+// Synthesis (A column-major in i, sAi = 1): 32 output rows a block, one a
+// lane (coalesced reads down the table's columns), k split over the eight
+// warps and the partial sums added in shared memory.
+template <int NT>
+__global__ void __launch_bounds__(256) GemmColsNarrowKernel(const GemmItem* items, const double* A,
+                                                            const double* B, double* C, bool accumulate) {
+  __shared__ double part[8][NT][32];
+  const GemmItem it = items[blockIdx.y];
+  const int lane = threadIdx.x & 31, group = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  if (blockIdx.x * 32 >= it.M) return;  // uniform over the block
+  const double* b = B + it.b;
+  double acc[NT] = {};
+  if (i < it.M) {
+    const double* a = A + it.a + i;
+#pragma unroll 4
+    for (int k = group; k < it.K; k += 8) {
+      const double av = a[static_cast<long long>(k) * it.sAk];
+      const double* bk = b + static_cast<long long>(k) * it.ldb;
+#pragma unroll
+      for (int n = 0; n < NT; ++n)
+        if (n < it.N) acc[n] = fma(av, bk[n], acc[n]);
+    }
+  }
+#pragma unroll
+  for (int n = 0; n < NT; ++n) part[group][n][lane] = acc[n];
+  __syncthreads();
+  if (group != 0 || i >= it.M) return;
+  double* c = C + it.c + static_cast<long long>(i) * it.ldc;
+#pragma unroll
+  for (int n = 0; n < NT; ++n) {
+    if (n >= it.N) break;
+    double s = part[0][n][lane];
+#pragma unroll
+    for (int g = 1; g < 8; ++g) s += part[g][n][lane];
+    c[n] = accumulate ? s + c[n] : s;
+  }
+}
+
+template <int NT>
+void LaunchNarrow(bool analysis, int maxM, int count, const GemmItem* items, const double* A, const double* B,
+                  double* C, bool accumulate, cudaStream_t stream) {
+  if (analysis)
+    GemmRowsNarrowKernel<NT><<<dim3((maxM + 7) / 8, count), 256, 0, stream>>>(items, A, B, C, accumulate);
+  else
+    GemmColsNarrowKernel<NT><<<dim3((maxM + 31) / 32, count), 256, 0, stream>>>(items, A, B, C, accumulate);
+}
+
 // -- FFT ---------------------------------------------------------------------------------
 
 template <class T2>
@@ -912,8 +999,22 @@ int Grid::BatchFor(int N, bool real, bool analysis, int P, int p0, int count, co
 int Grid::RunGemm(const Batch& b, const double* A, const double* B, double* C, bool accumulate,
                   cudaStream_t stream) {
   if (b.count == 0) return SL3DGPU_OK;
-  dim3 grid((b.maxM + kBM - 1) / kBM, (b.maxN + kBN - 1) / kBN, static_cast<unsigned>(b.count));
   prof::Scope scope(b.analysis ? prof::kLegendreAnalysis : prof::kLegendreSynthesis, stream, b.flops);
+  // the batch's items all have the direction's layout: analysis sAk = 1,
+  // synthesis sAi = 1 (BatchFor)
+  if (b.maxN <= kNarrowN) {
+    if (b.maxN <= 2)
+      LaunchNarrow<2>(b.analysis, b.maxM, b.count, b.items, A, B, C, accumulate, stream);
+    else if (b.maxN <= 4)
+      LaunchNarrow<4>(b.analysis, b.maxM, b.count, b.items, A, B, C, accumulate, stream);
+    else if (b.maxN <= 8)
+      LaunchNarrow<8>(b.analysis, b.maxM, b.count, b.items, A, B, C, accumulate, stream);
+    else
+      LaunchNarrow<16>(b.analysis, b.maxM, b.count, b.items, A, B, C, accumulate, stream);
+    SL3D_CHECK_LAUNCH();
+    return SL3DGPU_OK;
+  }
+  dim3 grid((b.maxM + kBM - 1) / kBM, (b.maxN + kBN - 1) / kBN, static_cast<unsigned>(b.count));
   GemmKernel<double><<<grid, 256, 0, stream>>>(b.items, A, B, C, accumulate);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;

@@ -156,10 +156,13 @@ def _grid_and_oracle_grid(lmax, oversampling, nmax=2, fp64_emulation=False):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("emulated", [False, True])
-@pytest.mark.parametrize("lmax,oversampling,count", [(12, 1.0, 3), (16, 1.5, 5), (33, 1.5, 2)])
+@pytest.mark.parametrize("lmax,oversampling,count", [(12, 1.0, 1), (12, 1.0, 3), (16, 1.5, 5), (33, 1.5, 2),
+                                                     (20, 1.0, 9)])
 def test_gpu_spin_transforms_match_oracle(gpu, lmax, oversampling, count, emulated):
     """Both forms of the FP64 contraction, the FP64 units' and the tensor
-    cores' emulation, at the FP64 bar (1e-12 of the largest value)."""
+    cores' emulation, at the FP64 bar (1e-12 of the largest value). Counts 1
+    to 8 (2 to 16 columns) take the FP64 units' few-column kernels, 9 the
+    tiled one."""
     import torch
 
     g, theta, w, nphi = _grid_and_oracle_grid(lmax, oversampling, fp64_emulation=emulated)
@@ -177,7 +180,8 @@ def test_gpu_spin_transforms_match_oracle(gpu, lmax, oversampling, count, emulat
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("emulated", [False, True])
-@pytest.mark.parametrize("lmax,oversampling,count", [(12, 1.0, 3), (32, 1.5, 4)])
+@pytest.mark.parametrize("lmax,oversampling,count", [(12, 1.0, 1), (12, 1.0, 3), (32, 1.5, 4), (24, 1.5, 8),
+                                                     (20, 1.0, 9)])
 def test_gpu_real_transforms_match_oracle(gpu, lmax, oversampling, count, emulated):
     import torch
 
