@@ -215,6 +215,55 @@ int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const do
                       double* tangential_potential, double* toroidal_potential, sl3dgpu_sle_result* result,
                       void* stream);
 
+/* ---- the nonlinear sea-level solve: migrating shorelines
+ * (GRDSolver::SolveNonlinear, include/sl3dpp/SeaLevel.hpp:418-481,
+ * src/SeaLevel.cpp:970-1289) ------------------------------------------------
+ * A plain fixed point from a state: each iteration the load of the current
+ * ocean function and sea level change, its sea level change (the
+ * generalised solve's Love numbers, static terms and rotational feedback),
+ * the water budget closed by a uniform shift, and the ocean function
+ * re-derived by flotation, rho_w SL - rho_i I > 0 where no land is held.
+ * Fields on the grid, device pointers, non-dimensional like the body. */
+typedef struct sl3dgpu_sle_state {  /* GRDSolver::State */
+  const double* ice_thickness;
+  const double* sea_level;            /* the sea surface over the solid surface (ocean depth) */
+  const double* ocean_function;       /* 1 ocean, 0 land; flotation's for a migrating run */
+  const unsigned char* forced_land;   /* nonzero: held at C = 0 (NULL: none) */
+} sl3dgpu_sle_state;
+typedef struct sl3dgpu_sle_nonlinear_forcing {  /* GRDSolver::NonlinearForcing; NULL: absent */
+  const double* ice_thickness_change;   /* field: its grounded part loads the body from the water budget */
+  const double* direct_load;            /* field: in the water budget */
+  const double* direct_load_outside;    /* field: outside it */
+  const double* solid_surface_change;   /* field: a layer on the solid surface */
+  const double* dynamic_sea_level_change; /* field: a given change of the sea surface over the oceans */
+  const double* displacement_response;  /* coefficients: ready responses */
+  const double* potential_response;
+  const double* tangential_response;
+  const double* toroidal_response;      /* carried to the response alone */
+  const double* tide;                   /* coefficients, degrees >= 2 */
+  double inertia_moment_change;         /* NonlinearForcing::inertiaMomentChange */
+  int hold_land;                        /* 0: the state's forced_land; 1: forced_land below (NULL: none held) */
+  const unsigned char* forced_land;
+} sl3dgpu_sle_nonlinear_forcing;
+/* The solve (max_iterations: the reference's default 50). Outputs, any NULL:
+ * the relative sea level change, displacement, potential, tangential and
+ * toroidal potentials (fields); the final state's sea level and ocean
+ * function (fields); the load the final state carries relative to the one
+ * given, (l, m >= 0) complex coefficients (NonlinearResponse::
+ * loadCoefficients). result: the last shift, error, iterations, whether it
+ * converged and the angular velocity. A state without ocean is refused. */
+int sl3dgpu_sle_solve_nonlinear(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, double ice_density,
+                                const sl3dgpu_sle_state* state, const sl3dgpu_sle_nonlinear_forcing* forcing,
+                                double rtol, int max_iterations, double* sea_level_change, double* displacement,
+                                double* potential, double* tangential_potential, double* toroidal_potential,
+                                double* final_sea_level, double* final_ocean_function, double* load_coefficients,
+                                sl3dgpu_sle_result* result, void* stream);
+/* GRDSolver::MakeState's ocean function (src/SeaLevel.cpp:279-300) over n
+ * points: 1 where rho_w sea_level - rho_i ice > 0 and no land is held. */
+int sl3dgpu_sle_flotation(long long n, double water_density, double ice_density, const double* ice,
+                          const double* sea_level, const unsigned char* forced_land, double* ocean_function,
+                          void* stream);
+
 /* ---- the 3D viscoelastic step (include/sl3dpp/Viscoelastic3D.hpp:79-837) -----
  * A layered Earth (SI), each field linear in radius within its layer: the
  * host-side counterpart of the reference's EarthModel + RadialMesh + Material
@@ -620,6 +669,18 @@ typedef struct sl3dgpu_v3d_ocean {
   double rtol;                  /* the sea-level solve's (Evolution3D::Options::rtol) */
   int max_iterations;           /* its budget */
   int anderson_memory;          /* its mixer's columns, 0..16 */
+  /* migrating shorelines (Evolution3D::RunMigrating, src/Evolution3D.cpp:
+   * 117-133; Coupled::Closure's nonlinear branch :308-319): every pass
+   * solves GRDSolver::SolveNonlinear from the background state below under
+   * the stage's ice. ocean_function may then be NULL (flotation's is taken;
+   * one given must equal it). Fields are host fields on the sea-level grid
+   * in the model's length unit. */
+  int migrating;                      /* 0: frozen shorelines, 1: migrating */
+  double ice_density;                 /* kg m^-3 (SeaLevelParameters: 917) */
+  const double* ice_thickness;        /* the background's ice thickness */
+  const double* sea_level;            /* its sea level (the sea surface over the solid surface) */
+  const unsigned char* forced_land;   /* the land held at C = 0 (NULL: none) */
+  int max_nonlinear_iterations;       /* Evolution3D::Options::max_nonlinear_iterations */
 } sl3dgpu_v3d_ocean;
 /* Sets (NULL: removes) the ocean of the operator's steps. */
 int sl3dgpu_v3d_set_ocean(sl3dgpu_v3d* op, const sl3dgpu_v3d_ocean* ocean);
@@ -639,6 +700,23 @@ int sl3dgpu_v3d_step_ocean(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt,
 int sl3dgpu_v3d_run_ocean(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* times, int nodes, int scheme,
                           const double* loads, double* u, double* phi, double* sea_level, double* angular_velocity,
                           sl3dgpu_step_info* infos);
+/* One coupled step under migrating shorelines: the ice thickness at the
+ * step's start and end (host fields, model length) and the direct loads
+ * beside it (NULL: none); a dt = 0 step is the start's solve
+ * (src/Evolution3D.cpp:690-700). */
+int sl3dgpu_v3d_step_migrating(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, double dt, int scheme, const double* ice0,
+                               const double* ice1, const double* load0, const double* load1,
+                               sl3dgpu_step_info* info);
+/* Evolution3D::RunMigrating: ice (nodes x field), loads (nodes x field;
+ * NULL: none, node 0 then undisturbed at the background, whose ice must be
+ * the first node's), the outputs of sl3dgpu_v3d_run_ocean and each node's
+ * ocean function (ocean_functions: nodes x field, nullable). */
+int sl3dgpu_v3d_run_migrating(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* times, int nodes, int scheme,
+                              const double* ice, const double* loads, double* u, double* phi, double* sea_level,
+                              double* angular_velocity, double* ocean_functions, sl3dgpu_step_info* infos);
+/* The last closure's ocean function (the fixed one under frozen
+ * shorelines), a host field on the sea-level grid. */
+int sl3dgpu_v3d_ocean_function(sl3dgpu_v3d* op, double* out);
 /* The last closure's relative sea level change, (l, m >= 0) complex host
  * coefficients in the model's length unit (nullable), its angular velocity
  * (3, nullable) and its solve's scalars (nullable). */

@@ -1,5 +1,6 @@
 """The oracle's ocean closure: a restatement of Evolution3D's Coupled::Closure
-(src/Evolution3D.cpp:296-339, frozen shorelines) and of the pieces it uses
+(src/Evolution3D.cpp:296-339, frozen and migrating shorelines) and of the
+pieces it uses
 -- GRDSolver's constructor constants (src/SeaLevel.cpp:142-247),
 TotalLoadCoefficients (:237-249 of Evolution3D.cpp) and
 CentrifugalCoefficients (src/SeaLevel.cpp:249-258) -- around the numpy
@@ -86,3 +87,54 @@ class OceanClosure:
         # TotalLoadCoefficients: the direct load and the ocean's
         sigma = self.expand(direct + self.water_density * self.ocean * out["sea_level_change"])
         return sigma, self.centrifugal(out["angular_velocity"])
+
+
+class MigratingClosure(OceanClosure):
+    """The closure under migrating shorelines (Coupled::Closure's migrating
+    branch, src/Evolution3D.cpp:308-319): each pass solves the nonlinear
+    sea-level equation (oracle/sealevel.py solve_nonlinear, GRDSolver::
+    SolveNonlinear) from the background state, the stage's ice thickness
+    change from the background's and the responses entering as ready
+    channels; the pass's load channel is the solve's carried load (grounded
+    ice, water and direct loads relative to the background), its tide
+    channel the centrifugal potential. `state` = dict(ice, sea_level,
+    forced_land) in model units; its ocean function is flotation's
+    (CheckMigratingStart, src/Shorelines.cpp:9-35)."""
+
+    def __init__(self, lmax, transforms, body, state, ice_density=917.0, max_nonlinear_iterations=50, **kw):
+        density = body["mass"] / body["length"] ** 3
+        self.ice_density = ice_density / density
+        super().__init__(lmax, transforms, body, np.zeros_like(np.asarray(state["ice"], dtype=np.float64)), **kw)
+        ice = np.asarray(state["ice"], dtype=np.float64)
+        sea = np.asarray(state["sea_level"], dtype=np.float64)
+        land = state.get("forced_land")
+        self.ocean = sealevel.flotation(ice, sea, self.water_density, self.ice_density, land)
+        self.state = dict(ice=ice, sea_level=sea, ocean=self.ocean, forced_land=land)
+        self.max_nonlinear_iterations = max_nonlinear_iterations
+        self.ice = None
+        self.current_ocean = self.ocean.copy()
+
+    def set_step_ice(self, t0, ice0, t1, ice1):
+        """The ice thickness at the step's two ends (model length)."""
+        self.ice = ((float(t0), np.asarray(ice0, dtype=np.float64)), (float(t1), np.asarray(ice1, dtype=np.float64)))
+
+    def _ice_at(self, t):
+        (t0, a), (t1, b) = self.ice
+        c = 1.0 if t1 == t0 else (t - t0) / (t1 - t0)
+        return (1.0 - c) * a + c * b
+
+    def __call__(self, t, love, U, V, phi, inertia):
+        n = self.lmax + 1
+        h, k, l, ht, kt, lt = (love[i * n:(i + 1) * n] for i in range(6))
+        hc, kc, m, mc = love[6 * n:6 * n + 4]
+        direct = self.direct_load(t) if self.loads is not None else None
+        out = sealevel.solve_nonlinear(
+            self.synthesise, self.expand, self.integrate, h, k, l, self.g, self.water_density, self.ice_density,
+            self.radius, self.state, ice_change=self._ice_at(t) - self.state["ice"], direct_load=direct,
+            displacement_response=U, potential_response=phi, tangential_response=V, ht=ht, kt=kt, lt_tide=lt,
+            rotation=self.rotation, omega=self.omega, polar=self.polar, equatorial=self.equatorial, G=self.G, hc=hc,
+            kc=kc, m_u=m, m_phi=0.0, m_c=mc, inertia_moment_change=inertia, rtol=self.rtol,
+            max_iterations=self.max_nonlinear_iterations)
+        self.last = out
+        self.current_ocean = out["ocean"]
+        return out["load_coefficients"], self.centrifugal(out["angular_velocity"])

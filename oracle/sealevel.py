@@ -1,7 +1,9 @@
 """The oracle's sea-level equation: a numpy restatement of GRDSolver::
 SolveGeneralised (src/SeaLevel.cpp:397-736) with its forcing channels and
 rotational feedback, and of the plain Anderson mixer it runs
-(include/sl3dpp/detail/AndersonMixer.hpp:65-219). Test infrastructure: the
+(include/sl3dpp/detail/AndersonMixer.hpp:65-219); the nonlinear solve with
+migrating shorelines, GRDSolver::SolveNonlinear (src/SeaLevel.cpp:970-1289),
+and the flotation of MakeState (:279-300). Test infrastructure: the
 checker the GPU solver (sl3dgpu_sle_solve) is compared with; it takes the
 grid's transforms and quadrature as arguments.
 
@@ -268,3 +270,162 @@ def solve_generalised(synthesise, expand, integrate, h, k, lt, g, water_density,
                tangential_potential=synthesise(tan_lm), toroidal_potential=toroidal, uniform_shift=shift,
                iterations=count, error=err, converged=converged, angular_velocity=omega_out)
     return out
+
+
+def flotation(ice, sea_level, water_density, ice_density, forced_land=None):
+    """GRDSolver::MakeState's ocean function (src/SeaLevel.cpp:279-300):
+    1 where the water column floats the ice (rho_w SL - rho_i I > 0) and the
+    point is not held as land, else 0."""
+    floats = water_density * np.asarray(sea_level) - ice_density * np.asarray(ice) > 0.0
+    if forced_land is not None:
+        floats &= np.asarray(forced_land) == 0
+    return floats.astype(np.float64)
+
+
+def solve_nonlinear(synthesise, expand, integrate, h, k, l, g, water_density, ice_density, radius, state,
+                    ice_change=None, direct_load=None, direct_load_outside=None, solid_surface_change=None,
+                    dynamic_sea_level_change=None, displacement_response=None, potential_response=None,
+                    tangential_response=None, toroidal_response=None, tide=None, ht=None, kt=None, lt_tide=None,
+                    rotation=0, omega=0.0, polar=0.0, equatorial=0.0, G=0.0, hc=0.0, kc=0.0, m_u=0.0, m_phi=0.0,
+                    m_c=0.0, inertia_moment_change=0.0, forced_land="state", rtol=1e-9, max_iterations=50):
+    """GRDSolver::SolveNonlinear (src/SeaLevel.cpp:970-1289): the sea level
+    equation with migrating shorelines, a plain fixed point from the state
+    given. `state` = dict(ice, sea_level, ocean, forced_land) (fields; the
+    mask may be None). Each iteration: the total load of the current ocean
+    function and sea level change (the grounded ice's and the water's
+    changes from the state, formed from the changes, :1098-1110, and the
+    direct loads), expanded; the sea level change of the load
+    (-(h + k / g), the static terms and the rotation block); the water
+    budget closed by a uniform shift over the current ocean (:1163-1180);
+    then the new ocean function by flotation. Stops when the largest change
+    of the sea level change between iterates is within rtol of its size,
+    taken before and after the shift (:1196-1208). forced_land: "state" for
+    the state's mask, else the mask held at this solve (None: none)."""
+    h = np.asarray(h, dtype=np.float64)
+    k = np.asarray(k, dtype=np.float64)
+    lmax = h.size - 1
+    degree = np.concatenate([np.full(m + 1, m) for m in range(lmax + 1)])
+    ice0 = np.asarray(state["ice"], dtype=np.float64)
+    bathy0 = np.asarray(state["sea_level"], dtype=np.float64)
+    ocean0 = np.asarray(state["ocean"], dtype=np.float64)
+    held = state.get("forced_land") if isinstance(forced_land, str) else forced_land
+    size = ocean0.size
+    surface = lambda f: radius * radius * integrate(f)  # IntegrateSurface
+    if not surface(ocean0) > 0.0:
+        raise ValueError("the nonlinear sea level solve needs a state with an ocean")
+    tidal = tide is not None and np.max(np.abs(tide)) > 0.0
+    static_disp = static_grav = static_slc = None
+    if displacement_response is not None or potential_response is not None or tidal:
+        static_disp = np.zeros(degree.size, dtype=np.complex128)
+        static_grav = np.zeros(degree.size, dtype=np.complex128)
+        if displacement_response is not None:
+            static_disp = np.array(displacement_response, dtype=np.complex128)
+        if potential_response is not None:
+            static_grav = np.array(potential_response, dtype=np.complex128)
+        if tidal:
+            ht_, kt_ = np.array(ht, dtype=np.float64), np.array(kt, dtype=np.float64)
+            ht_[0] = kt_[0] = 0.0
+            static_disp = static_disp + ht_[degree] * tide
+            static_grav = static_grav + kt_[degree] * tide
+        static_slc = -(static_disp + static_grav / g)
+        if tidal:
+            static_slc = static_slc - tide / g
+    layer2 = np.zeros((2, 2))
+    if solid_surface_change is not None:
+        layer_lm = expand(solid_surface_change)
+        if static_slc is None:
+            static_slc = np.zeros(degree.size, dtype=np.complex128)
+        static_slc = static_slc - layer_lm
+        layer2 = _block_of(layer_lm)
+    tide2 = _block_of(tide) if tidal else np.zeros((2, 2))
+    dice = np.zeros(size) if ice_change is None else np.asarray(ice_change, dtype=np.float64)
+    new_ice = ice0 + dice
+    direct = None
+    direct_mass = 0.0
+    if direct_load is not None:
+        direct = np.array(direct_load, dtype=np.float64)
+        direct_mass = surface(direct)
+    if direct_load_outside is not None:
+        direct = (np.zeros(size) if direct is None else direct) + direct_load_outside
+    grounded = lambda c: ice_density * ((1.0 - c) * dice - (c - ocean0) * ice0)
+    water = lambda c, change: water_density * (c * change + (c - ocean0) * bathy0)
+    slc_factor = -(h + k / g)
+    rot = None
+    if rotation:
+        rot = _RotationFactors(rotation, h, k, np.asarray(ht), np.asarray(kt), radius, omega, polar, equatorial, G,
+                               hc, kc, m_u, m_phi, m_c)
+        sd2 = _block_of(static_disp) if static_disp is not None else np.zeros((2, 2))
+        sg2 = _block_of(static_grav) if static_grav is not None else np.zeros((2, 2))
+        rotate = lambda lm: _rotation(rot, _block_of(lm), lm[0].real, sd2, sg2, inertia_moment_change, (0.0, 0.0, 0.0))
+    ocean = ocean0.copy()
+    change = np.zeros(size)
+    slc_data = np.zeros(size)
+    omega_out = np.zeros(3)
+    last = None
+    shift = 0.0
+    err = np.inf
+    converged = False
+    count = 0
+    load_lm = np.zeros(degree.size, dtype=np.complex128)
+    while count < max_iterations:
+        total = grounded(ocean) + water(ocean, change)
+        if direct is not None:
+            total = total + direct
+        load_lm = expand(total)
+        slc_lm = slc_factor[degree] * load_lm
+        if static_slc is not None:
+            slc_lm = slc_lm + static_slc
+        if rot is not None:
+            last = rotate(load_lm)
+            omega_out = last["omega"]
+            _set_block(slc_lm, -(last["disp2"] + (last["grav2"] + last["centrifugal"] + tide2) / g + layer2))
+            slc_lm[0] -= (rot.hc + (rot.kc + 1.0) / g) * last["centrifugal0"]
+        local = synthesise(slc_lm)
+        raw = local if dynamic_sea_level_change is None else local + dynamic_sea_level_change
+        unbalanced = grounded(ocean) + water(ocean, raw)
+        shift = -(surface(unbalanced) + direct_mass) / (water_density * surface(ocean))
+        new_slc = local + shift
+        new_change = raw + shift
+        floats = water_density * (bathy0 + new_change) - ice_density * new_ice > 0.0
+        if held is not None:
+            floats &= np.asarray(held) == 0
+        top = max(np.max(np.abs(slc_data)), np.max(np.abs(local)) if count > 0 else 0.0)
+        if top > 0.0:
+            err = np.max(np.abs(new_slc - slc_data)) / top
+        else:
+            err = 0.0 if np.max(np.abs(new_slc)) == 0.0 else 1.0
+        slc_data, change, ocean = new_slc, new_change, floats.astype(np.float64)
+        count += 1
+        if err <= rtol:
+            converged = True
+            break
+    tan = np.zeros(lmax + 1) if l is None else np.array(l, dtype=np.float64)
+    tan[0] = 0.0
+    disp_lm = h[degree] * load_lm
+    pot_lm = k[degree] * load_lm
+    if static_disp is not None:
+        disp_lm = disp_lm + static_disp
+        pot_lm = pot_lm + static_grav
+    tan_lm = tan[degree] * load_lm
+    if tangential_response is not None:
+        tan_lm = tan_lm + tangential_response
+    if tidal:
+        lt_t = np.zeros(lmax + 1) if lt_tide is None else np.array(lt_tide, dtype=np.float64)
+        lt_t[0] = 0.0
+        tan_lm = tan_lm + lt_t[degree] * tide
+    if rot is not None and last is not None:
+        _set_block(disp_lm, last["disp2"])
+        _set_block(pot_lm, last["grav2"])
+        disp_lm[0] += rot.hc * last["centrifugal0"]
+        pot_lm[0] += rot.kc * last["centrifugal0"]
+        lt2 = 0.0 if lt_tide is None else lt_tide[2]
+        _add_block(tan_lm, lt2 * last["centrifugal"])
+    carried = grounded(ocean) + water(ocean, change)
+    if direct is not None:
+        carried = carried + direct
+    return dict(sea_level_change=slc_data, displacement=synthesise(disp_lm), potential=synthesise(pot_lm),
+                tangential_potential=synthesise(tan_lm),
+                toroidal_potential=synthesise(toroidal_response) if toroidal_response is not None else None,
+                angular_velocity=omega_out, uniform_shift=shift, iterations=count, error=err, converged=converged,
+                ice=new_ice, sea_level=bathy0 + change, ocean=ocean, ocean_area=surface(ocean),
+                load_coefficients=expand(carried))

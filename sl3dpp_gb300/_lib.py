@@ -65,6 +65,22 @@ class SleForcing(ctypes.Structure):
                 (name, ctypes.c_void_p) for name in ("displacement_load", "potential_load", "tangential_traction")]
 
 
+class SleState(ctypes.Structure):
+    """sl3dgpu_sle_state: GRDSolver::State's fields (device pointers; the land mask may be null)."""
+    _fields_ = [(name, ctypes.c_void_p) for name in ("ice_thickness", "sea_level", "ocean_function",
+                                                     "forced_land")]
+
+
+class SleNonlinearForcing(ctypes.Structure):
+    """sl3dgpu_sle_nonlinear_forcing: NonlinearForcing's channels (device pointers or null)."""
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("ice_thickness_change", "direct_load", "direct_load_outside", "solid_surface_change",
+                 "dynamic_sea_level_change", "displacement_response", "potential_response", "tangential_response",
+                 "toroidal_response", "tide")] + [
+                ("inertia_moment_change", ctypes.c_double), ("hold_land", ctypes.c_int),
+                ("forced_land", ctypes.c_void_p)]
+
+
 class SleResult(ctypes.Structure):
     """sl3dgpu_sle_result: GRDSolver::Response's scalars."""
     _fields_ = [("uniform_shift", ctypes.c_double), ("error", ctypes.c_double), ("iterations", ctypes.c_int),
@@ -113,6 +129,12 @@ def lib() -> ctypes.CDLL:
         "sl3dgpu_sle_solve": (c_int, [c_void_p, ctypes.POINTER(SleBody), c_void_p, ctypes.POINTER(SleForcing),
                                       c_double, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       ctypes.POINTER(SleResult), c_void_p]),
+        "sl3dgpu_sle_solve_nonlinear": (c_int, [c_void_p, ctypes.POINTER(SleBody), c_double,
+                                                ctypes.POINTER(SleState), ctypes.POINTER(SleNonlinearForcing),
+                                                c_double, c_int] + [c_void_p] * 8 + [ctypes.POINTER(SleResult),
+                                                                                      c_void_p]),
+        "sl3dgpu_sle_flotation": (c_int, [ctypes.c_longlong, c_double, c_double, c_void_p, c_void_p, c_void_p,
+                                          c_void_p, c_void_p]),
         "sl3dgpu_grid_set_fp64_emulation": (c_int, [c_void_p, c_int]),
         "sl3dgpu_grid_colatitudes": (c_int, [c_void_p, P_double, P_double]),
         "sl3dgpu_synthesise_spin_batch": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),

@@ -37,6 +37,16 @@
 // thing to the host, the stopping test's maxima. A workspace (SleWorkspace)
 // keeps the buffers between solves on one grid, so that the coupled closure's
 // solve in every pass of a step allocates nothing.
+//
+// GRDSolver::SolveNonlinear (src/SeaLevel.cpp:970-1289), migrating
+// shorelines, shares the static terms and the rotation patch: a plain fixed
+// point from a state (ice I0, sea level SL0, ocean function C0), each
+// iteration the load of the grounded ice's and the water's changes at the
+// current ocean function C and change dS (BudgetLoadKernel), its sea level
+// change synthesised, the water budget closed by a uniform shift over the
+// current ocean (BudgetRingKernel, BudgetShiftKernel) and C re-derived by
+// flotation, rho_w (SL0 + dS) - rho_i (I0 + dI) > 0 off the land held
+// (BudgetUpdateKernel).
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -453,6 +463,10 @@ struct SleWorkspace {
   Dev<double> shift, omega, slcFactor;  // the conservation's shift, the angular velocity, -(h + k / g) per degree
   Dev<RotationInputs> rotation;
   std::vector<double> theta;
+  // the nonlinear solve's iterates: the ocean function, the sea level change
+  // from the state, the sea level change's last value and the local one,
+  // and the water budget's ring partials
+  Dev<double> nlOcean, nlChange, nlSlc, nlLocal, nlRingUnbalanced, nlRingOcean;
 
   // the grid's sizes, quadrature and buffers (once per grid)
   int Prepare(sl3dgpu_grid* g) {
@@ -486,8 +500,17 @@ struct SleWorkspace {
     SL3D_CUDA(omega.Alloc(3));
     SL3D_CUDA(slcFactor.Alloc(run.lmax + 1));
     SL3D_CUDA(rotation.Alloc(1));
+    for (auto* d : {&nlOcean, &nlChange, &nlSlc, &nlLocal, &nlRingUnbalanced, &nlRingOcean}) *d = Dev<double>();
     mixerMemory = -1;
     grid = g;
+    return SL3DGPU_OK;
+  }
+  // the nonlinear solve's buffers (on its first use on the grid)
+  int PrepareNonlinear() {
+    if (nlOcean.p != nullptr) return SL3DGPU_OK;
+    for (auto* d : {&nlOcean, &nlChange, &nlSlc, &nlLocal}) SL3D_CUDA(d->Alloc(run.fieldSize));
+    SL3D_CUDA(nlRingUnbalanced.Alloc(run.ntheta));
+    SL3D_CUDA(nlRingOcean.Alloc(run.ntheta));
     return SL3DGPU_OK;
   }
   // the mixer at its plain start, with `memory` columns
@@ -523,19 +546,26 @@ int CentrifugalCoefficients(const sl3dgpu_sle_body& body, const double omega[3],
   return SL3DGPU_OK;
 }
 
-int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
-                  const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations, int anderson_memory,
-                  double* sea_level_change, double* displacement, double* potential, double* tangential_potential,
-                  double* toroidal_potential, double* total_load, sl3dgpu_sle_result* result, cudaStream_t stream) {
-  if (grid == nullptr || body == nullptr || body->h == nullptr || body->k == nullptr || ocean == nullptr ||
-      forcing == nullptr || sea_level_change == nullptr || result == nullptr) {
-    SetError("sle: null argument");
-    return SL3DGPU_ERR_ARGUMENT;
-  }
+namespace {
+
+// What a solve's forcing carries (the reference's MaxAbs > 0 tests) and
+// whether it rotates: the generalised and the nonlinear solves share it.
+struct SleSetup {
+  bool hasDirect = false, hasOutside = false, hasLayer = false, hasDisp = false, hasPot = false, hasTan = false,
+       hasTide = false, hasLoadChannel = false;
+  bool anyStatic = false, anyStaticTan = false, rotating = false;
+  std::vector<double> tangential;  // the load's l per degree, degree 0 zero
+};
+
+// The body's checks, the grid's workspace, -(h + k / g) on the device, the
+// static coefficient terms (src/SeaLevel.cpp:453-545, :586-600: D_s, G_s,
+// V_s, S_s) and the rotation's fixed inputs (:604-608) on the device; the
+// angular velocity and the shift zeroed.
+int PrepareSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* body,
+                 const sl3dgpu_sle_forcing* forcing, cudaStream_t s, SleSetup* su) {
   const double g = body->g, water_density = body->water_density, radius = body->radius;
-  if (!(g > 0.0) || !(water_density > 0.0) || !(radius > 0.0) || !(rtol >= 0.0) || max_iterations < 0 ||
-      anderson_memory < 0 || anderson_memory > kMixMaxMemory) {
-    SetError("sle: g, water_density and radius > 0, rtol >= 0, max_iterations >= 0, anderson_memory in [0, 16]");
+  if (!(g > 0.0) || !(water_density > 0.0) || !(radius > 0.0)) {
+    SetError("sle: g, water_density and radius > 0");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if ((forcing->displacement_load != nullptr && (body->h_u == nullptr || body->k_u == nullptr)) ||
@@ -559,43 +589,40 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
   }
   SL3D_TRY(ws.Prepare(grid));
   SleRun& run = ws.run;
-  run.stream = stream;
+  run.stream = s;
   run.r2 = radius * radius;
   if (body->rotation != 0 && run.lmax < 2) {
     SetError("sle: rotational feedback needs degree 2 on the grid");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  const int blocks = static_cast<int>(std::min<long long>(kMaxBlocks, (run.fieldSize + 255) / 256));
-  const cudaStream_t s = run.stream;
   const int L = run.lmax;
   const long long nc = 2 * run.coefCount;  // coefficients as reals
   std::vector<double> slcFactor(L + 1);
   for (int l = 0; l <= L; ++l) slcFactor[l] = -(body->h[l] + body->k[l] / g);
-  std::vector<double> tangential(L + 1, 0.0);
+  SL3D_CUDA(cudaMemcpyAsync(ws.slcFactor.p, slcFactor.data(), (L + 1) * sizeof(double), cudaMemcpyHostToDevice, s));
+  su->tangential.assign(L + 1, 0.0);
   if (body->l != nullptr)
-    for (int l = 1; l <= L; ++l) tangential[l] = body->l[l];  // a degree-0 field has no tangential part
+    for (int l = 1; l <= L; ++l) su->tangential[l] = body->l[l];  // a degree-0 field has no tangential part
 
-  // which channels carry something (the reference's MaxAbs > 0 tests)
   auto nonzero = [&](const double* a, long long n, bool* out) -> int {
     double m = 0.0;
     if (a != nullptr) SL3D_TRY(run.MaxAbs(a, n, &m));
     *out = m > 0.0;
     return SL3DGPU_OK;
   };
-  bool hasDirect, hasOutside, hasLayer, hasDisp, hasPot, hasTan, hasTide, hasToroidal, hasDispLoad, hasPotLoad,
-      hasTraction;
-  SL3D_TRY(nonzero(forcing->direct_load, run.fieldSize, &hasDirect));
-  SL3D_TRY(nonzero(forcing->direct_load_outside, run.fieldSize, &hasOutside));
-  SL3D_TRY(nonzero(forcing->solid_surface_change, run.fieldSize, &hasLayer));
-  SL3D_TRY(nonzero(forcing->displacement_response, nc, &hasDisp));
-  SL3D_TRY(nonzero(forcing->potential_response, nc, &hasPot));
-  SL3D_TRY(nonzero(forcing->tangential_response, nc, &hasTan));
-  SL3D_TRY(nonzero(forcing->tide, nc, &hasTide));
-  SL3D_TRY(nonzero(forcing->toroidal_response, nc, &hasToroidal));
+  bool hasDispLoad, hasPotLoad, hasTraction;
+  SL3D_TRY(nonzero(forcing->direct_load, run.fieldSize, &su->hasDirect));
+  SL3D_TRY(nonzero(forcing->direct_load_outside, run.fieldSize, &su->hasOutside));
+  SL3D_TRY(nonzero(forcing->solid_surface_change, run.fieldSize, &su->hasLayer));
+  SL3D_TRY(nonzero(forcing->displacement_response, nc, &su->hasDisp));
+  SL3D_TRY(nonzero(forcing->potential_response, nc, &su->hasPot));
+  SL3D_TRY(nonzero(forcing->tangential_response, nc, &su->hasTan));
+  SL3D_TRY(nonzero(forcing->tide, nc, &su->hasTide));
   SL3D_TRY(nonzero(forcing->displacement_load, run.fieldSize, &hasDispLoad));
   SL3D_TRY(nonzero(forcing->potential_load, run.fieldSize, &hasPotLoad));
   SL3D_TRY(nonzero(forcing->tangential_traction, run.fieldSize, &hasTraction));
-  const bool hasLoadChannel = hasDispLoad || hasPotLoad || hasTraction;
+  su->hasLoadChannel = hasDispLoad || hasPotLoad || hasTraction;
+  const bool hasTide = su->hasTide, hasLayer = su->hasLayer;
   if (hasTide) {
     // RequireTideDegrees (src/SeaLevel.cpp:83-96): no degree-0 or degree-1 part
     std::vector<double> low(6);
@@ -608,43 +635,20 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
         return SL3DGPU_ERR_ARGUMENT;
       }
   }
-  auto zero = [&](double* f) -> int {
-    if (f) SL3D_CUDA(cudaMemsetAsync(f, 0, run.fieldSize * sizeof(double), s));
-    return SL3DGPU_OK;
-  };
-  *result = sl3dgpu_sle_result{0.0, 0.0, 0, 1, {0.0, 0.0, 0.0}};
-  // the toroidal potential is carried, whatever else is solved (:561-563)
-  if (toroidal_potential != nullptr) {
-    if (forcing->toroidal_response != nullptr)
-      SL3D_TRY(sl3dgpu_synthesise_batch(grid, forcing->toroidal_response, 1, toroidal_potential, s));
-    else
-      SL3D_TRY(zero(toroidal_potential));
-  }
-  const bool anyForcing = hasDirect || hasOutside || hasLayer || hasDisp || hasPot || hasTan || hasTide ||
-                          hasLoadChannel;
-  if (!anyForcing) {
-    SL3D_TRY(zero(sea_level_change));
-    SL3D_TRY(zero(displacement));
-    SL3D_TRY(zero(potential));
-    SL3D_TRY(zero(tangential_potential));
-    if (total_load != nullptr) SL3D_CUDA(cudaMemsetAsync(total_load, 0, nc * sizeof(double), s));
-    SL3D_CUDA(cudaStreamSynchronize(s));
-    return SL3DGPU_OK;
-  }
 
   // The static (load-independent) coefficient terms.
-  const bool anyStatic = hasDisp || hasPot || hasTide || hasLayer || hasLoadChannel;
-  const bool anyStaticTan = hasDisp || hasPot || hasTan || hasTide || hasLoadChannel;
+  su->anyStatic = su->hasDisp || su->hasPot || hasTide || hasLayer || su->hasLoadChannel;
+  su->anyStaticTan = su->hasDisp || su->hasPot || su->hasTan || hasTide || su->hasLoadChannel;
   double displacementLoad0 = 0.0, potentialLoad0 = 0.0;
   Dev<double>&staticDisp = ws.staticDisp, &staticGrav = ws.staticGrav, &staticTan = ws.staticTan,
              &staticSlc = ws.staticSlc, &scratch = ws.scratch;
   const std::vector<double> zeros(L + 1, 0.0);
-  if (anyStatic || anyStaticTan) {
+  if (su->anyStatic || su->anyStaticTan) {
     for (auto* d : {&staticDisp, &staticGrav, &staticTan, &staticSlc, &scratch})
       SL3D_CUDA(cudaMemsetAsync(d->p, 0, nc * sizeof(double), s));
-    if (hasDisp) SL3D_TRY(run.Axpy(staticDisp.p, forcing->displacement_response, 1.0, staticDisp.p));
-    if (hasPot) SL3D_TRY(run.Axpy(staticGrav.p, forcing->potential_response, 1.0, staticGrav.p));
-    if (hasTan) SL3D_TRY(run.Axpy(staticTan.p, forcing->tangential_response, 1.0, staticTan.p));
+    if (su->hasDisp) SL3D_TRY(run.Axpy(staticDisp.p, forcing->displacement_response, 1.0, staticDisp.p));
+    if (su->hasPot) SL3D_TRY(run.Axpy(staticGrav.p, forcing->potential_response, 1.0, staticGrav.p));
+    if (su->hasTan) SL3D_TRY(run.Axpy(staticTan.p, forcing->tangential_response, 1.0, staticTan.p));
     if (hasTide) {
       // the body's answer to the prescribed potential (:533-545)
       std::vector<double> ht(body->ht, body->ht + L + 1), kt(body->kt, body->kt + L + 1), lt(L + 1, 0.0);
@@ -690,45 +694,22 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
       SL3D_TRY(run.Axpy(staticSlc.p, scratch.p, -1.0, staticSlc.p));
     }
   }
-  const double* slcAdd = anyStatic ? staticSlc.p : nullptr;
 
-  double oceanArea = 0.0;
-  SL3D_TRY(run.Integrate(ocean, nullptr, &oceanArea));
-  const double perOceanArea = oceanArea > 0.0 ? 1.0 / oceanArea : 0.0;
-  // the direct load in the water budget sets the mean; one outside it loads
-  // the body and moves no water (:577-587)
-  double meanSlc = 0.0;
-  Dev<double>& directData = ws.directData;
-  SL3D_CUDA(cudaMemsetAsync(directData.p, 0, run.fieldSize * sizeof(double), s));
-  const unsigned fb = static_cast<unsigned>((run.fieldSize + 255) / 256);
-  if (forcing->direct_load != nullptr) {
-    double loadIntegral = 0.0;
-    SL3D_TRY(run.Integrate(forcing->direct_load, nullptr, &loadIntegral));
-    meanSlc = -loadIntegral * perOceanArea / water_density;
-    SL3D_CUDA(cudaMemcpyAsync(directData.p, forcing->direct_load, run.fieldSize * sizeof(double),
-                              cudaMemcpyDeviceToDevice, s));
-  }
-  if (forcing->direct_load_outside != nullptr) {
-    AddFieldKernel<<<fb, 256, 0, s>>>(run.fieldSize, directData.p, forcing->direct_load_outside, directData.p);
-    SL3D_CHECK_LAUNCH();
-  }
-  // the seed: sigma + rho_w C s_mean, expanded
-  SeedKernel<<<fb, 256, 0, s>>>(run.fieldSize, directData.p, ocean, water_density * meanSlc, run.seeded.p);
-  SL3D_CHECK_LAUNCH();
-  SL3D_TRY(sl3dgpu_expand_batch(grid, run.seeded.p, 1, run.loadLm.p, s));
-
-  // The rotational feedback's fixed blocks (src/SeaLevel.cpp:604-608).
+  // The rotational feedback's fixed blocks (src/SeaLevel.cpp:604-608), read
+  // back once, and the rotation's inputs on the device, so that each
+  // iteration's patch needs no host round trip.
   RotationFactors rf;
   rf.Init(*body);
-  Block2 staticDisp2{}, staticGrav2{}, tide2{}, layer2{};
-  auto headOf = [&](const double* coeffs, double* head) -> int {  // coefficients 0 .. 4 as (re, im)
-    SL3D_CUDA(cudaMemcpyAsync(head, coeffs, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    SL3D_CUDA(cudaStreamSynchronize(s));
-    return SL3DGPU_OK;
-  };
+  su->rotating = rf.on;
   if (rf.on) {
+    Block2 staticDisp2{}, staticGrav2{}, tide2{}, layer2{};
+    auto headOf = [&](const double* coeffs, double* head) -> int {  // coefficients 0 .. 4 as (re, im)
+      SL3D_CUDA(cudaMemcpyAsync(head, coeffs, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      SL3D_CUDA(cudaStreamSynchronize(s));
+      return SL3DGPU_OK;
+    };
     double head[10];
-    if (anyStatic || anyStaticTan) {
+    if (su->anyStatic || su->anyStaticTan) {
       SL3D_TRY(headOf(staticDisp.p, head));
       staticDisp2 = BlockOf(head + 6, head + 8);
       SL3D_TRY(headOf(staticGrav.p, head));
@@ -742,10 +723,6 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
       SL3D_TRY(headOf(scratch.p, head));  // the layer's expansion
       layer2 = BlockOf(head + 6, head + 8);
     }
-  }
-  // The rotation's inputs on the device (the static blocks read back once
-  // above), so that each iteration's patch needs no host round trip.
-  if (rf.on) {
     RotationInputs in{};
     in.transverse = rf.transverse ? 1 : 0;
     in.h2 = rf.h2;
@@ -788,25 +765,221 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
   }
   SL3D_CUDA(cudaMemsetAsync(ws.omega.p, 0, 3 * sizeof(double), s));
   SL3D_CUDA(cudaMemsetAsync(ws.shift.p, 0, sizeof(double), s));
-  // out = f_l L + add, then (rotating) its degree-0/2 coefficients patched by
-  // the rotation of the load L on the device, and synthesised
-  auto synthesisePatched = [&](const double* f, bool factorsOnDevice, const double* add, double* field,
-                               int mode) -> int {
-    if (factorsOnDevice) {
-      ScaleDegreesKernel<<<static_cast<unsigned>((run.coefCount + 255) / 256), 256, 0, s>>>(
-          L, f, reinterpret_cast<const double2*>(run.loadLm.p), reinterpret_cast<const double2*>(add), 1.0,
-          reinterpret_cast<double2*>(run.scaledLm.p));
-      SL3D_CHECK_LAUNCH();
-    } else {
-      SL3D_TRY(run.ScaleDegrees(f, run.loadLm.p, add, 1.0, run.scaledLm.p));
+  return SL3DGPU_OK;
+}
+
+// field = Synthesise(f_l L + add) of the run's load L (f on the device or the
+// host), its degree-0/2 coefficients patched first by the rotation of L when
+// `patch` (mode: RotationPatchKernel's).
+int SynthesisePatched(SleWorkspace& ws, bool patch, const double* f, bool factorsOnDevice, const double* add,
+                      double* field, int mode) {
+  SleRun& run = ws.run;
+  const cudaStream_t s = run.stream;
+  if (factorsOnDevice) {
+    ScaleDegreesKernel<<<static_cast<unsigned>((run.coefCount + 255) / 256), 256, 0, s>>>(
+        run.lmax, f, reinterpret_cast<const double2*>(run.loadLm.p), reinterpret_cast<const double2*>(add), 1.0,
+        reinterpret_cast<double2*>(run.scaledLm.p));
+    SL3D_CHECK_LAUNCH();
+  } else {
+    SL3D_TRY(run.ScaleDegrees(f, run.loadLm.p, add, 1.0, run.scaledLm.p));
+  }
+  if (patch) {
+    RotationPatchKernel<<<1, 32, 0, s>>>(ws.rotation.p, run.loadLm.p, run.scaledLm.p, ws.omega.p, mode);
+    SL3D_CHECK_LAUNCH();
+  }
+  return sl3dgpu_synthesise_batch(run.grid, run.scaledLm.p, 1, field, s);
+}
+
+// -- the nonlinear solve's pointwise work (src/SeaLevel.cpp:1098-1217) ----------------------------------
+
+// The changes of grounded ice and of ocean water per unit area from the
+// state, at ocean function c and sea level change `change`
+// (groundedIceChangeAt, waterChangeAt: :1100-1110).
+struct Budget {
+  double rhoI, rhoW;
+  const double *dice, *ice0, *ocean0, *sea0;
+  __device__ double Grounded(long long i, double c) const {
+    const double di = dice ? dice[i] : 0.0;
+    return rhoI * ((1.0 - c) * di - (c - ocean0[i]) * ice0[i]);
+  }
+  __device__ double Water(long long i, double c, double change) const {
+    return rhoW * (c * change + (c - ocean0[i]) * sea0[i]);
+  }
+};
+
+// out = grounded + water (+ direct): the total load (:1131-1136) and the
+// carried one (:1277-1283)
+__global__ void BudgetLoadKernel(long long n, Budget b, const double* ocean, const double* change, const double* direct,
+                                 double* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  double v = b.Grounded(i, ocean[i]) + b.Water(i, ocean[i], change[i]);
+  if (direct) v += direct[i];
+  out[i] = v;
+}
+
+// Per ring, w_j sum_k of what the water holds before the shift
+// (unbalanced, :1167-1171, with the local change plus the dynamic one) and of
+// the ocean function: one block a ring, a fixed tree (the grid's Integrate).
+__global__ void BudgetRingKernel(int nphi, const double* weights, Budget b, const double* ocean, const double* local,
+                                 const double* dynamic, double* unbalancedPartial, double* oceanPartial) {
+  __shared__ double red[2][kRingThreads];
+  const int j = blockIdx.x;
+  const long long base = static_cast<long long>(j) * nphi;
+  double u = 0.0, c = 0.0;
+  for (int k = threadIdx.x; k < nphi; k += blockDim.x) {
+    const long long i = base + k;
+    const double raw = dynamic ? local[i] + dynamic[i] : local[i];
+    u += b.Grounded(i, ocean[i]) + b.Water(i, ocean[i], raw);
+    c += ocean[i];
+  }
+  red[0][threadIdx.x] = u;
+  red[1][threadIdx.x] = c;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s /= 2) {
+    if (threadIdx.x < s) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + s];
+      red[1][threadIdx.x] += red[1][threadIdx.x + s];
     }
-    if (rf.on) {
-      RotationPatchKernel<<<1, 32, 0, s>>>(ws.rotation.p, run.loadLm.p, run.scaledLm.p, ws.omega.p, mode);
-      SL3D_CHECK_LAUNCH();
-    }
-    return sl3dgpu_synthesise_batch(grid, run.scaledLm.p, 1, field, s);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    unbalancedPartial[j] = weights[j] * red[0][0];
+    oceanPartial[j] = weights[j] * red[1][0];
+  }
+}
+
+// The eustatic shift (:1172-1176): what the water must lose, over the
+// current ocean's water mass per unit height; the rings in order.
+__global__ void BudgetShiftKernel(const double* unbalancedPartial, const double* oceanPartial, int ntheta, double scale,
+                                  double rhoW, double directMass, double* shift) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double su = 0.0, sc = 0.0;
+  for (int j = 0; j < ntheta; ++j) {
+    su += unbalancedPartial[j];
+    sc += oceanPartial[j];
+  }
+  const double oceanDensityArea = rhoW * (scale * sc);
+  shift[0] = -(scale * su + directMass) / oceanDensityArea;
+}
+
+// The iterate's update (:1178-1217): the shifted sea level changes, the
+// ocean function by flotation (not where land is held), and per block the
+// largest |new - previous|, |previous|, |local| and |new| of the sea level
+// change (blockIdx-ordered partials).
+__global__ void BudgetUpdateKernel(long long n, const double* shiftPtr, Budget b, const double* local,
+                                   const double* dynamic, const unsigned char* held, double* slc, double* change,
+                                   double* ocean, double* maxima) {
+  __shared__ double red[4][kRingThreads];
+  const double shift = *shiftPtr;
+  double m[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const double raw = dynamic ? local[i] + dynamic[i] : local[i];
+    const double newSlc = local[i] + shift, newChange = raw + shift;
+    const double newIce = b.dice ? b.ice0[i] + b.dice[i] : b.ice0[i];
+    const double newBathy = b.sea0[i] + newChange;
+    const bool land = held != nullptr && held[i] != 0;
+    const double previous = slc[i];
+    m[0] = fmax(m[0], fabs(newSlc - previous));
+    m[1] = fmax(m[1], fabs(previous));
+    m[2] = fmax(m[2], fabs(local[i]));
+    m[3] = fmax(m[3], fabs(newSlc));
+    slc[i] = newSlc;
+    change[i] = newChange;
+    ocean[i] = !land && b.rhoW * newBathy - b.rhoI * newIce > 0.0 ? 1.0 : 0.0;
+  }
+  for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = m[q];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s /= 2) {
+    if (threadIdx.x < s)
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = fmax(red[q][threadIdx.x], red[q][threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 4; ++q) maxima[4 * blockIdx.x + q] = red[q][0];
+}
+
+// MakeState's ocean function (src/SeaLevel.cpp:279-300)
+__global__ void FlotationKernel(long long n, double rhoW, double rhoI, const double* ice, const double* sea,
+                                const unsigned char* held, double* ocean) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const bool floats = rhoW * sea[i] - rhoI * ice[i] > 0.0;
+  const bool land = held != nullptr && held[i] != 0;
+  ocean[i] = floats && !land ? 1.0 : 0.0;
+}
+
+}  // namespace
+
+int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, const double* ocean,
+                  const sl3dgpu_sle_forcing* forcing, double rtol, int max_iterations, int anderson_memory,
+                  double* sea_level_change, double* displacement, double* potential, double* tangential_potential,
+                  double* toroidal_potential, double* total_load, sl3dgpu_sle_result* result, cudaStream_t stream) {
+  if (grid == nullptr || body == nullptr || body->h == nullptr || body->k == nullptr || ocean == nullptr ||
+      forcing == nullptr || sea_level_change == nullptr || result == nullptr) {
+    SetError("sle: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (!(rtol >= 0.0) || max_iterations < 0 || anderson_memory < 0 || anderson_memory > kMixMaxMemory) {
+    SetError("sle: rtol >= 0, max_iterations >= 0, anderson_memory in [0, 16]");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  SleSetup su;
+  SL3D_TRY(PrepareSolve(ws, grid, body, forcing, stream, &su));
+  SleRun& run = ws.run;
+  const double water_density = body->water_density;
+  const int blocks = static_cast<int>(std::min<long long>(kMaxBlocks, (run.fieldSize + 255) / 256));
+  const cudaStream_t s = stream;
+  const long long nc = 2 * run.coefCount;  // coefficients as reals
+  auto zero = [&](double* f) -> int {
+    if (f) SL3D_CUDA(cudaMemsetAsync(f, 0, run.fieldSize * sizeof(double), s));
+    return SL3DGPU_OK;
   };
-  SL3D_CUDA(cudaMemcpyAsync(ws.slcFactor.p, slcFactor.data(), (L + 1) * sizeof(double), cudaMemcpyHostToDevice, s));
+  *result = sl3dgpu_sle_result{0.0, 0.0, 0, 1, {0.0, 0.0, 0.0}};
+  // the toroidal potential is carried, whatever else is solved (:561-563)
+  if (toroidal_potential != nullptr) {
+    if (forcing->toroidal_response != nullptr)
+      SL3D_TRY(sl3dgpu_synthesise_batch(grid, forcing->toroidal_response, 1, toroidal_potential, s));
+    else
+      SL3D_TRY(zero(toroidal_potential));
+  }
+  const bool anyForcing = su.hasDirect || su.hasOutside || su.anyStatic || su.anyStaticTan;
+  if (!anyForcing) {
+    SL3D_TRY(zero(sea_level_change));
+    SL3D_TRY(zero(displacement));
+    SL3D_TRY(zero(potential));
+    SL3D_TRY(zero(tangential_potential));
+    if (total_load != nullptr) SL3D_CUDA(cudaMemsetAsync(total_load, 0, nc * sizeof(double), s));
+    SL3D_CUDA(cudaStreamSynchronize(s));
+    return SL3DGPU_OK;
+  }
+  const double* slcAdd = su.anyStatic ? ws.staticSlc.p : nullptr;
+
+  double oceanArea = 0.0;
+  SL3D_TRY(run.Integrate(ocean, nullptr, &oceanArea));
+  const double perOceanArea = oceanArea > 0.0 ? 1.0 / oceanArea : 0.0;
+  // the direct load in the water budget sets the mean; one outside it loads
+  // the body and moves no water (:577-587)
+  double meanSlc = 0.0;
+  Dev<double>& directData = ws.directData;
+  SL3D_CUDA(cudaMemsetAsync(directData.p, 0, run.fieldSize * sizeof(double), s));
+  const unsigned fb = static_cast<unsigned>((run.fieldSize + 255) / 256);
+  if (forcing->direct_load != nullptr) {
+    double loadIntegral = 0.0;
+    SL3D_TRY(run.Integrate(forcing->direct_load, nullptr, &loadIntegral));
+    meanSlc = -loadIntegral * perOceanArea / water_density;
+    SL3D_CUDA(cudaMemcpyAsync(directData.p, forcing->direct_load, run.fieldSize * sizeof(double),
+                              cudaMemcpyDeviceToDevice, s));
+  }
+  if (forcing->direct_load_outside != nullptr) {
+    AddFieldKernel<<<fb, 256, 0, s>>>(run.fieldSize, directData.p, forcing->direct_load_outside, directData.p);
+    SL3D_CHECK_LAUNCH();
+  }
+  // the seed: sigma + rho_w C s_mean, expanded
+  SeedKernel<<<fb, 256, 0, s>>>(run.fieldSize, directData.p, ocean, water_density * meanSlc, run.seeded.p);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(sl3dgpu_expand_batch(grid, run.seeded.p, 1, run.loadLm.p, s));
 
   SL3D_TRY(ws.ResetMixer(anderson_memory, s));
   LoadMixer& mixer = ws.mixer;
@@ -816,7 +989,7 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
   while (count < max_iterations) {
     // the sea level change of the load, its uniform part by conservation:
     // one host round trip an iteration, the stopping test's maxima
-    SL3D_TRY(synthesisePatched(ws.slcFactor.p, true, slcAdd, run.slc.p, 0));
+    SL3D_TRY(SynthesisePatched(ws, su.rotating, ws.slcFactor.p, true, slcAdd, run.slc.p, 0));
     RingSumKernel<<<run.ntheta, kRingThreads, 0, s>>>(run.nphi, run.weights.p, ocean, run.slc.p, run.ringPartial.p);
     SL3D_CHECK_LAUNCH();
     ShiftKernel<<<1, 32, 0, s>>>(run.ringPartial.p, run.ntheta, run.r2 * run.dphi, meanSlc, perOceanArea,
@@ -850,12 +1023,15 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
   // load it came from, with the static terms (:702-720)
   SL3D_CUDA(cudaMemcpyAsync(sea_level_change, run.slc.p, run.fieldSize * sizeof(double), cudaMemcpyDeviceToDevice,
                             s));
-  const bool withStatic = anyStatic || anyStaticTan;
+  const bool withStatic = su.anyStatic || su.anyStaticTan;
   if (displacement)
-    SL3D_TRY(synthesisePatched(body->h, false, withStatic ? staticDisp.p : nullptr, displacement, 1));
-  if (potential) SL3D_TRY(synthesisePatched(body->k, false, withStatic ? staticGrav.p : nullptr, potential, 2));
+    SL3D_TRY(SynthesisePatched(ws, su.rotating, body->h, false, withStatic ? ws.staticDisp.p : nullptr, displacement,
+                               1));
+  if (potential)
+    SL3D_TRY(SynthesisePatched(ws, su.rotating, body->k, false, withStatic ? ws.staticGrav.p : nullptr, potential, 2));
   if (tangential_potential)
-    SL3D_TRY(synthesisePatched(tangential.data(), false, withStatic ? staticTan.p : nullptr, tangential_potential, 3));
+    SL3D_TRY(SynthesisePatched(ws, su.rotating, su.tangential.data(), false, withStatic ? ws.staticTan.p : nullptr,
+                               tangential_potential, 3));
   // TotalLoadCoefficients (src/Evolution3D.cpp:237-249): the direct loads and
   // the ocean's, rho_w C S of the last sea level change
   if (total_load != nullptr) SL3D_TRY(sl3dgpu_expand_batch(grid, run.newLoad.p, 1, total_load, s));
@@ -864,6 +1040,164 @@ int SeaLevelSolve(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* 
   SL3D_CUDA(cudaMemcpyAsync(tail + 1, ws.omega.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   SL3D_CUDA(cudaStreamSynchronize(s));
   *result = sl3dgpu_sle_result{tail[0], err, count, converged ? 1 : 0, {tail[1], tail[2], tail[3]}};
+  return SL3DGPU_OK;
+}
+
+// GRDSolver::SolveNonlinear (src/SeaLevel.cpp:970-1289): a plain fixed point
+// from the state given, each iteration the total load of the current ocean
+// function and sea level change expanded, its sea level change (the
+// generalised solve's factors, static terms and rotation patch) synthesised,
+// the water budget closed by a uniform shift over the current ocean, the
+// ocean function re-derived by flotation. One host round trip an
+// iteration: the stopping test's maxima.
+int SeaLevelSolveNonlinear(SleWorkspace& ws, sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, double ice_density,
+                           const sl3dgpu_sle_state* state, const sl3dgpu_sle_nonlinear_forcing* forcing, double rtol,
+                           int max_iterations, double* sea_level_change, double* displacement, double* potential,
+                           double* tangential_potential, double* toroidal_potential, double* final_sea_level,
+                           double* final_ocean_function, double* load_coefficients, sl3dgpu_sle_result* result,
+                           cudaStream_t stream) {
+  if (grid == nullptr || body == nullptr || body->h == nullptr || body->k == nullptr || state == nullptr ||
+      state->ice_thickness == nullptr || state->sea_level == nullptr || state->ocean_function == nullptr ||
+      forcing == nullptr || result == nullptr) {
+    SetError("sle: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (!(ice_density > 0.0) || !(rtol >= 0.0) || max_iterations < 0) {
+    SetError("sle: ice_density > 0, rtol >= 0, max_iterations >= 0");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  // the channels the nonlinear solve shares with the generalised one
+  sl3dgpu_sle_forcing shared{};
+  shared.solid_surface_change = forcing->solid_surface_change;
+  shared.displacement_response = forcing->displacement_response;
+  shared.potential_response = forcing->potential_response;
+  shared.tangential_response = forcing->tangential_response;
+  shared.toroidal_response = forcing->toroidal_response;
+  shared.tide = forcing->tide;
+  shared.inertia_moment_change = forcing->inertia_moment_change;
+  SleSetup su;
+  SL3D_TRY(PrepareSolve(ws, grid, body, &shared, stream, &su));
+  SL3D_TRY(ws.PrepareNonlinear());
+  SleRun& run = ws.run;
+  const cudaStream_t s = stream;
+  const long long n = run.fieldSize, nc = 2 * run.coefCount;
+  const size_t bytes = n * sizeof(double);
+  const unsigned fb = static_cast<unsigned>((n + 255) / 256);
+  const int blocks = static_cast<int>(std::min<long long>(kMaxBlocks / 2, (n + 255) / 256));
+  double oceanArea = 0.0;
+  SL3D_TRY(run.Integrate(state->ocean_function, nullptr, &oceanArea));
+  if (!(oceanArea > 0.0)) {
+    SetError("sle: the nonlinear sea level solve needs a state with an ocean: the shorelines of a body without one "
+             "do not migrate");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const unsigned char* held = forcing->hold_land ? forcing->forced_land : state->forced_land;
+  // the direct loads: the one inside the water budget takes its mass from
+  // the ocean, the one outside it moves no water (:1085-1096)
+  const double* direct = nullptr;
+  double directMass = 0.0;
+  if (forcing->direct_load != nullptr) {
+    SL3D_TRY(run.Integrate(forcing->direct_load, nullptr, &directMass));
+    SL3D_CUDA(cudaMemcpyAsync(ws.directData.p, forcing->direct_load, bytes, cudaMemcpyDeviceToDevice, s));
+    direct = ws.directData.p;
+  }
+  if (forcing->direct_load_outside != nullptr) {
+    if (direct == nullptr) SL3D_CUDA(cudaMemsetAsync(ws.directData.p, 0, bytes, s));
+    AddFieldKernel<<<fb, 256, 0, s>>>(n, ws.directData.p, forcing->direct_load_outside, ws.directData.p);
+    SL3D_CHECK_LAUNCH();
+    direct = ws.directData.p;
+  }
+  const Budget budget{ice_density,           body->water_density, forcing->ice_thickness_change,
+                      state->ice_thickness,  state->ocean_function, state->sea_level};
+  const double* dynamic = forcing->dynamic_sea_level_change;
+  const double* slcAdd = su.anyStatic ? ws.staticSlc.p : nullptr;
+  SL3D_CUDA(cudaMemcpyAsync(ws.nlOcean.p, state->ocean_function, bytes, cudaMemcpyDeviceToDevice, s));
+  SL3D_CUDA(cudaMemsetAsync(ws.nlChange.p, 0, bytes, s));
+  SL3D_CUDA(cudaMemsetAsync(ws.nlSlc.p, 0, bytes, s));
+  SL3D_CUDA(cudaMemsetAsync(run.loadLm.p, 0, nc * sizeof(double), s));
+  *result = sl3dgpu_sle_result{0.0, INFINITY, 0, 0, {0.0, 0.0, 0.0}};
+  double err = INFINITY;
+  bool converged = false;
+  int count = 0;
+  while (count < max_iterations) {
+    BudgetLoadKernel<<<fb, 256, 0, s>>>(n, budget, ws.nlOcean.p, ws.nlChange.p, direct, run.newLoad.p);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(sl3dgpu_expand_batch(grid, run.newLoad.p, 1, run.loadLm.p, s));
+    SL3D_TRY(SynthesisePatched(ws, su.rotating, ws.slcFactor.p, true, slcAdd, ws.nlLocal.p, 0));
+    BudgetRingKernel<<<run.ntheta, kRingThreads, 0, s>>>(run.nphi, run.weights.p, budget, ws.nlOcean.p,
+                                                         ws.nlLocal.p, dynamic, ws.nlRingUnbalanced.p,
+                                                         ws.nlRingOcean.p);
+    SL3D_CHECK_LAUNCH();
+    BudgetShiftKernel<<<1, 32, 0, s>>>(ws.nlRingUnbalanced.p, ws.nlRingOcean.p, run.ntheta, run.r2 * run.dphi,
+                                       body->water_density, directMass, ws.shift.p);
+    SL3D_CHECK_LAUNCH();
+    BudgetUpdateKernel<<<blocks, kRingThreads, 0, s>>>(n, ws.shift.p, budget, ws.nlLocal.p, dynamic, held, ws.nlSlc.p,
+                                                       ws.nlChange.p, ws.nlOcean.p, run.maxima.p);
+    SL3D_CHECK_LAUNCH();
+    SL3D_CUDA(cudaMemcpyAsync(run.hostMaxima.data(), run.maxima.p, 4 * blocks * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+    SL3D_CUDA(cudaStreamSynchronize(s));
+    double m[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < blocks; ++b)
+      for (int q = 0; q < 4; ++q) m[q] = std::max(m[q], run.hostMaxima[4 * b + q]);
+    // the change against the size of the change, before the shift as well
+    // as after (:1196-1208)
+    const double top = std::max(m[1], count > 0 ? m[2] : 0.0);
+    err = top > 0.0 ? m[0] / top : (m[3] == 0.0 ? 0.0 : 1.0);
+    ++count;
+    if (err <= rtol) {
+      converged = true;
+      break;
+    }
+  }
+  if (sea_level_change) SL3D_CUDA(cudaMemcpyAsync(sea_level_change, ws.nlSlc.p, bytes, cudaMemcpyDeviceToDevice, s));
+  // the responses of the last load, with the static terms (:1221-1262)
+  const bool withStatic = su.anyStatic || su.anyStaticTan;
+  const bool patch = su.rotating && count > 0;
+  if (displacement)
+    SL3D_TRY(SynthesisePatched(ws, patch, body->h, false, withStatic ? ws.staticDisp.p : nullptr, displacement, 1));
+  if (potential)
+    SL3D_TRY(SynthesisePatched(ws, patch, body->k, false, withStatic ? ws.staticGrav.p : nullptr, potential, 2));
+  if (tangential_potential)
+    SL3D_TRY(SynthesisePatched(ws, patch, su.tangential.data(), false, withStatic ? ws.staticTan.p : nullptr,
+                               tangential_potential, 3));
+  if (toroidal_potential) {
+    if (forcing->toroidal_response != nullptr)
+      SL3D_TRY(sl3dgpu_synthesise_batch(grid, forcing->toroidal_response, 1, toroidal_potential, s));
+    else
+      SL3D_CUDA(cudaMemsetAsync(toroidal_potential, 0, bytes, s));
+  }
+  // the final state (:1264-1271) and the load it carries (:1276-1284)
+  if (final_sea_level) {
+    AddFieldKernel<<<fb, 256, 0, s>>>(n, state->sea_level, ws.nlChange.p, final_sea_level);
+    SL3D_CHECK_LAUNCH();
+  }
+  if (final_ocean_function)
+    SL3D_CUDA(cudaMemcpyAsync(final_ocean_function, ws.nlOcean.p, bytes, cudaMemcpyDeviceToDevice, s));
+  if (load_coefficients) {
+    BudgetLoadKernel<<<fb, 256, 0, s>>>(n, budget, ws.nlOcean.p, ws.nlChange.p, direct, run.newLoad.p);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(sl3dgpu_expand_batch(grid, run.newLoad.p, 1, load_coefficients, s));
+  }
+  double tail[4];
+  SL3D_CUDA(cudaMemcpyAsync(tail, ws.shift.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  SL3D_CUDA(cudaMemcpyAsync(tail + 1, ws.omega.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SL3D_CUDA(cudaStreamSynchronize(s));
+  *result = sl3dgpu_sle_result{tail[0], err, count, converged ? 1 : 0, {tail[1], tail[2], tail[3]}};
+  return SL3DGPU_OK;
+}
+
+int Flotation(long long n, double water_density, double ice_density, const double* ice, const double* sea_level,
+              const unsigned char* forced_land, double* ocean_function, cudaStream_t stream) {
+  if (n < 0 || ice == nullptr || sea_level == nullptr || ocean_function == nullptr || !(water_density > 0.0) ||
+      !(ice_density > 0.0)) {
+    SetError("sle: flotation needs the ice and sea level fields, the output and densities > 0");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (n == 0) return SL3DGPU_OK;
+  FlotationKernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(n, water_density, ice_density, ice,
+                                                                                sea_level, forced_land, ocean_function);
+  SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
 
@@ -880,4 +1214,24 @@ extern "C" int sl3dgpu_sle_solve(sl3dgpu_grid* grid, const sl3dgpu_sle_body* bod
   return SeaLevelSolve(ws, grid, body, ocean, forcing, rtol, max_iterations, anderson_memory, sea_level_change,
                        displacement, potential, tangential_potential, toroidal_potential, nullptr, result,
                        AsStream(stream));
+}
+
+extern "C" int sl3dgpu_sle_solve_nonlinear(sl3dgpu_grid* grid, const sl3dgpu_sle_body* body, double ice_density,
+                                           const sl3dgpu_sle_state* state,
+                                           const sl3dgpu_sle_nonlinear_forcing* forcing, double rtol,
+                                           int max_iterations, double* sea_level_change, double* displacement,
+                                           double* potential, double* tangential_potential,
+                                           double* toroidal_potential, double* final_sea_level,
+                                           double* final_ocean_function, double* load_coefficients,
+                                           sl3dgpu_sle_result* result, void* stream) {
+  SleWorkspace ws;
+  return SeaLevelSolveNonlinear(ws, grid, body, ice_density, state, forcing, rtol, max_iterations, sea_level_change,
+                                displacement, potential, tangential_potential, toroidal_potential, final_sea_level,
+                                final_ocean_function, load_coefficients, result, AsStream(stream));
+}
+
+extern "C" int sl3dgpu_sle_flotation(long long n, double water_density, double ice_density, const double* ice,
+                                     const double* sea_level, const unsigned char* forced_land,
+                                     double* ocean_function, void* stream) {
+  return Flotation(n, water_density, ice_density, ice, sea_level, forced_land, ocean_function, AsStream(stream));
 }

@@ -233,6 +233,16 @@ class Viscoelastic3DGpu {
     double cStart = 0.0, cEnd = 1.0;  // the running stage's start and end as fractions of the step
     sl3dgpu_sle_result last{};        // the last closure's solve
     bool solved = false;
+    // Migrating shorelines (Coupled::Closure's nonlinear branch,
+    // src/Evolution3D.cpp:308-319): the background state (ice, sea level,
+    // flotation's ocean function in `function`, the land held), the ice at
+    // the running step's two ends and the stage's change from the
+    // background, and the last closure's ocean function.
+    bool migrating = false, hasLand = false, hasLoads = false;
+    double iceDensity = 0.0;
+    int maxNonlinear = 50;
+    Dev<double> ice, seaLevel, ice0, ice1, stageIceChange, current;
+    Dev<unsigned char> land;
     ~Ocean() {
       if (ws) FreeSleWorkspace(ws);
       if (grid) sl3dgpu_grid_destroy(grid);
@@ -248,6 +258,11 @@ class Viscoelastic3DGpu {
   int RunOcean(V3dState& st, const double* times, int nodes, int scheme, const double* loads, double* u, double* phi,
                double* slc, double* omega, sl3dgpu_step_info* infos);
   int SeaLevel(double* coefficients, double* omega, sl3dgpu_sle_result* result);
+  int StepMigrating(V3dState& st, double dt, int scheme, const double* ice0, const double* ice1, const double* load0,
+                    const double* load1, sl3dgpu_step_info* info);
+  int RunMigrating(V3dState& st, const double* times, int nodes, int scheme, const double* ice, const double* loads,
+                   double* u, double* phi, double* slc, double* omega, double* oceans, sl3dgpu_step_info* infos);
+  int OceanFunction(double* out);
 
   ~Viscoelastic3DGpu() {
     for (auto& g : correctionGraphs)
@@ -1366,6 +1381,12 @@ __global__ void BlendFieldKernel(long long n, double c, const double* a, const d
   const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
   if (i < n) out[i] = (1.0 - c) * a[i] + c * b[i];
 }
+// out = ((1 - c) a + c b) - background over a field
+__global__ void StageChangeKernel(long long n, double c, const double* a, const double* b, const double* background,
+                                  double* out) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < n) out[i] = ((1.0 - c) * a[i] + c * b[i]) - background[i];
+}
 }  // namespace
 
 // The sea-level body of the operator's Earth in its model units: the
@@ -1381,13 +1402,20 @@ int Viscoelastic3DGpu::SetOcean(const sl3dgpu_v3d_ocean* o) {
     SetError("v3d: the ocean closure is built for the FP64 fixed point (precision 0, solver 0)");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  if (o->ocean_function == nullptr || o->rotation < 0 || o->rotation > 2 || !(o->water_density > 0.0) ||
+  if ((o->ocean_function == nullptr && !o->migrating) || o->rotation < 0 || o->rotation > 2 ||
+      !(o->water_density > 0.0) ||
       !(o->rtol > 0.0) || o->max_iterations < 1 || o->anderson_memory < 0 || o->anderson_memory > 16 ||
       (o->rotation != 0 && (!(o->rotation_frequency > 0.0) || !(o->polar_moment > 0.0) ||
                             !(o->polar_moment != o->equatorial_moment)))) {
     SetError("v3d: an ocean needs its function, rotation 0, 1 or 2 (with a rotation frequency and unequal "
              "moments of inertia), water density > 0, rtol > 0, max_iterations >= 1 and anderson_memory in "
              "[0, 16]");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (o->migrating && (o->ice_thickness == nullptr || o->sea_level == nullptr || !(o->ice_density > 0.0) ||
+                       o->max_nonlinear_iterations < 1)) {
+    SetError("v3d: migrating shorelines need the background's ice thickness and sea level, an ice density > 0 and "
+             "max_nonlinear_iterations >= 1");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if (ocean.grid == nullptr) {
@@ -1398,14 +1426,50 @@ int Viscoelastic3DGpu::SetOcean(const sl3dgpu_v3d_ocean* o) {
   SL3D_TRY(sl3dgpu_grid_shape(ocean.grid, &nt, &np));
   ocean.fieldSize = static_cast<long long>(nt) * np;
   const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
-  std::vector<double> function(o->ocean_function, o->ocean_function + ocean.fieldSize);
-  SL3D_CUDA(ocean.function.Upload(function));
+  const auto& scales = earth->scales();
+  ocean.migrating = o->migrating != 0;
+  if (ocean.migrating) {
+    // the background state, its ocean function by flotation
+    // (CheckMigratingStart, src/Shorelines.cpp:9-35: a prescribed one must
+    // be flotation's)
+    const size_t n = static_cast<size_t>(ocean.fieldSize);
+    SL3D_CUDA(ocean.ice.Upload(std::vector<double>(o->ice_thickness, o->ice_thickness + n)));
+    SL3D_CUDA(ocean.seaLevel.Upload(std::vector<double>(o->sea_level, o->sea_level + n)));
+    ocean.hasLand = o->forced_land != nullptr;
+    if (ocean.hasLand)
+      SL3D_CUDA(ocean.land.Upload(std::vector<unsigned char>(o->forced_land, o->forced_land + n)));
+    ocean.iceDensity = o->ice_density / scales.Density();
+    ocean.maxNonlinear = o->max_nonlinear_iterations;
+    SL3D_CUDA(ocean.function.Alloc(n));
+    SL3D_TRY(Flotation(ocean.fieldSize, o->water_density / scales.Density(), ocean.iceDensity, ocean.ice.p,
+                       ocean.seaLevel.p, ocean.hasLand ? ocean.land.p : nullptr, ocean.function.p, stream));
+    if (o->ocean_function != nullptr) {
+      std::vector<double> got(n);
+      SL3D_CUDA(cudaMemcpyAsync(got.data(), ocean.function.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+      SL3D_CUDA(cudaStreamSynchronize(stream));
+      for (size_t i = 0; i < n; ++i)
+        if (got[i] != o->ocean_function[i]) {
+          SetError("v3d: migrating shorelines follow the flotation condition from the first node, so the "
+                   "background state must not prescribe its ocean function");
+          return SL3DGPU_ERR_ARGUMENT;
+        }
+    }
+    for (auto* d : {&ocean.ice0, &ocean.ice1, &ocean.stageIceChange, &ocean.current}) SL3D_CUDA(d->Alloc(n));
+    SL3D_CUDA(cudaMemcpyAsync(ocean.current.p, ocean.function.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                              stream));
+    SL3D_CUDA(cudaMemcpyAsync(ocean.ice0.p, ocean.ice.p, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(ocean.ice1.p, ocean.ice.p, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+  } else {
+    std::vector<double> function(o->ocean_function, o->ocean_function + ocean.fieldSize);
+    SL3D_CUDA(ocean.function.Upload(function));
+  }
   for (auto* d : {&ocean.load0, &ocean.load1, &ocean.stageLoad, &ocean.slc}) SL3D_CUDA(d->Alloc(ocean.fieldSize));
   for (auto* d : {&ocean.U, &ocean.V, &ocean.Phi, &ocean.sigma, &ocean.psi}) SL3D_CUDA(d->Alloc(lm));
   SL3D_CUDA(ZeroIn(ocean.psi.p, lm * sizeof(double2)));
   SL3D_CUDA(ZeroIn(ocean.load0.p, ocean.fieldSize * sizeof(double)));
   SL3D_CUDA(ZeroIn(ocean.load1.p, ocean.fieldSize * sizeof(double)));
-  const auto& sc = earth->scales();
+  ocean.hasLoads = false;
+  const auto& sc = scales;
   sl3dgpu_sle_body& b = ocean.body;
   b = sl3dgpu_sle_body{};
   b.g = material->surfaceGravity;
@@ -1426,9 +1490,15 @@ int Viscoelastic3DGpu::SetOcean(const sl3dgpu_v3d_ocean* o) {
 
 // The running stage's direct load: (1 - c) of the step's start load and c of its end's.
 int Viscoelastic3DGpu::StageLoad(double c) {
-  BlendFieldKernel<<<static_cast<unsigned>((ocean.fieldSize + 255) / 256), 256, 0, stream>>>(
-      ocean.fieldSize, c, ocean.load0.p, ocean.load1.p, ocean.stageLoad.p);
+  const unsigned blocks = static_cast<unsigned>((ocean.fieldSize + 255) / 256);
+  BlendFieldKernel<<<blocks, 256, 0, stream>>>(ocean.fieldSize, c, ocean.load0.p, ocean.load1.p, ocean.stageLoad.p);
   SL3D_CHECK_LAUNCH();
+  if (ocean.migrating) {
+    // the stage's ice less the background's (src/Evolution3D.cpp:717-722)
+    StageChangeKernel<<<blocks, 256, 0, stream>>>(ocean.fieldSize, c, ocean.ice0.p, ocean.ice1.p, ocean.ice.p,
+                                                  ocean.stageIceChange.p);
+    SL3D_CHECK_LAUNCH();
+  }
   return SL3DGPU_OK;
 }
 
@@ -1514,15 +1584,33 @@ int Viscoelastic3DGpu::Closure(const Flavour& f) {
   b.m_u = v[6 * (L + 1) + 2];  // the load's whole trace number (no displacement or potential load channel)
   b.m_phi = 0.0;
   b.m_c = v[6 * (L + 1) + 3];
-  sl3dgpu_sle_forcing forcing{};
-  forcing.direct_load = ocean.stageLoad.p;
-  forcing.displacement_response = reinterpret_cast<const double*>(ocean.U.p);
-  forcing.potential_response = reinterpret_cast<const double*>(ocean.Phi.p);
-  forcing.tangential_response = reinterpret_cast<const double*>(ocean.V.p);
-  forcing.inertia_moment_change = moment;
-  SL3D_TRY(SeaLevelSolve(*ocean.ws, ocean.grid, &b, ocean.function.p, &forcing, ocean.rtol, ocean.maxIterations,
-                         ocean.memory, ocean.slc.p, nullptr, nullptr, nullptr, nullptr,
-                         reinterpret_cast<double*>(ocean.sigma.p), &ocean.last, stream));
+  if (ocean.migrating) {
+    // the nonlinear equation from the background under the stage's ice
+    // change (and direct load, where given), the responses as ready channels
+    const sl3dgpu_sle_state state{ocean.ice.p, ocean.seaLevel.p, ocean.function.p,
+                                  ocean.hasLand ? ocean.land.p : nullptr};
+    sl3dgpu_sle_nonlinear_forcing moving{};
+    moving.ice_thickness_change = ocean.stageIceChange.p;
+    moving.direct_load = ocean.hasLoads ? ocean.stageLoad.p : nullptr;
+    moving.displacement_response = reinterpret_cast<const double*>(ocean.U.p);
+    moving.potential_response = reinterpret_cast<const double*>(ocean.Phi.p);
+    moving.tangential_response = reinterpret_cast<const double*>(ocean.V.p);
+    moving.inertia_moment_change = moment;
+    SL3D_TRY(SeaLevelSolveNonlinear(*ocean.ws, ocean.grid, &b, ocean.iceDensity, &state, &moving, ocean.rtol,
+                                    ocean.maxNonlinear, ocean.slc.p, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                    ocean.current.p, reinterpret_cast<double*>(ocean.sigma.p), &ocean.last,
+                                    stream));
+  } else {
+    sl3dgpu_sle_forcing forcing{};
+    forcing.direct_load = ocean.stageLoad.p;
+    forcing.displacement_response = reinterpret_cast<const double*>(ocean.U.p);
+    forcing.potential_response = reinterpret_cast<const double*>(ocean.Phi.p);
+    forcing.tangential_response = reinterpret_cast<const double*>(ocean.V.p);
+    forcing.inertia_moment_change = moment;
+    SL3D_TRY(SeaLevelSolve(*ocean.ws, ocean.grid, &b, ocean.function.p, &forcing, ocean.rtol, ocean.maxIterations,
+                           ocean.memory, ocean.slc.p, nullptr, nullptr, nullptr, nullptr,
+                           reinterpret_cast<double*>(ocean.sigma.p), &ocean.last, stream));
+  }
   double psi[6];
   SL3D_TRY(CentrifugalCoefficients(b, ocean.last.angular_velocity, psi));
   // (0, 0) at 0, (2, 0) at 3, (2, 1) at 4 of the l(l+1)/2 + m layout
@@ -1538,6 +1626,10 @@ int Viscoelastic3DGpu::StepOcean(V3dState& st, double dt, int scheme, const doub
                                  sl3dgpu_step_info* info) {
   if (!ocean.on) {
     SetError("v3d: no ocean is set (sl3dgpu_v3d_set_ocean)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (ocean.migrating) {
+    SetError("v3d: the ocean's shorelines migrate: its steps take the ice (sl3dgpu_v3d_step_migrating)");
     return SL3DGPU_ERR_ARGUMENT;
   }
   const size_t bytes = ocean.fieldSize * sizeof(double);
@@ -1589,6 +1681,108 @@ int Viscoelastic3DGpu::SeaLevel(double* coefficients, double* omega, sl3dgpu_sle
   if (omega)
     for (int i = 0; i < 3; ++i) omega[i] = ocean.last.angular_velocity[i];
   if (result) *result = ocean.last;
+  return SL3DGPU_OK;
+}
+
+// One coupled step under migrating shorelines: the ice thickness at the
+// step's two ends (host fields, model length), the direct loads beside it
+// (NULL: none); the stages take their combinations (detail::AtStage).
+int Viscoelastic3DGpu::StepMigrating(V3dState& st, double dt, int scheme, const double* ice0, const double* ice1,
+                                     const double* load0, const double* load1, sl3dgpu_step_info* info) {
+  if (!ocean.on || !ocean.migrating) {
+    SetError("v3d: no ocean with migrating shorelines is set (sl3dgpu_v3d_set_ocean, migrating = 1)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (ice0 == nullptr || ice1 == nullptr) {
+    SetError("v3d: a migrating step needs the ice thickness at both its ends");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const size_t bytes = ocean.fieldSize * sizeof(double);
+  SL3D_CUDA(cudaMemcpyAsync(ocean.ice0.p, ice0, bytes, cudaMemcpyHostToDevice, stream));
+  SL3D_CUDA(cudaMemcpyAsync(ocean.ice1.p, ice1, bytes, cudaMemcpyHostToDevice, stream));
+  ocean.hasLoads = load0 != nullptr || load1 != nullptr;
+  if (load0) SL3D_CUDA(cudaMemcpyAsync(ocean.load0.p, load0, bytes, cudaMemcpyHostToDevice, stream));
+  else SL3D_CUDA(cudaMemsetAsync(ocean.load0.p, 0, bytes, stream));
+  if (load1) SL3D_CUDA(cudaMemcpyAsync(ocean.load1.p, load1, bytes, cudaMemcpyHostToDevice, stream));
+  else SL3D_CUDA(cudaMemsetAsync(ocean.load1.p, 0, bytes, stream));
+  return Step(st, dt, scheme, nullptr, nullptr, info);
+}
+
+// Evolution3D::RunMigrating (src/Evolution3D.cpp:117-133, March :540-821):
+// node 0 undisturbed at the background (its ice must be the history's
+// first, CheckMigratingStart) or, with direct loads, the start's solve (a
+// zero-length step, :690-700); then a step per node, every pass closed by the
+// nonlinear equation. ice: nodes x field; loads: nodes x field or NULL;
+// oceans (nullable): nodes x field, each node's ocean function.
+int Viscoelastic3DGpu::RunMigrating(V3dState& st, const double* times, int nodes, int scheme, const double* ice,
+                                    const double* loads, double* u, double* phi, double* slc, double* omega,
+                                    double* oceans, sl3dgpu_step_info* infos) {
+  if (!ocean.on || !ocean.migrating) {
+    SetError("v3d: no ocean with migrating shorelines is set (sl3dgpu_v3d_set_ocean, migrating = 1)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  const long long n = ocean.fieldSize;
+  for (int k = 0; k < nodes; ++k) {
+    const double* i1 = ice + n * k;
+    const double* i0 = k > 0 ? ice + n * (k - 1) : i1;
+    const double* l1 = loads ? loads + n * k : nullptr;
+    const double* l0 = loads ? (k > 0 ? loads + n * (k - 1) : l1) : nullptr;
+    const double dt = k > 0 ? times[k] - times[k - 1] : 0.0;
+    if (!(dt >= 0.0)) {
+      SetError("v3d: node times must not decrease");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+    sl3dgpu_step_info info{};
+    info.converged = 1;
+    if (k == 0 && loads == nullptr) {
+      // the background is the state at the first node: undisturbed
+      std::vector<double> background(n);
+      SL3D_CUDA(cudaMemcpyAsync(background.data(), ocean.ice.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+      SL3D_CUDA(cudaStreamSynchronize(stream));
+      double scale = 0.0, worst = 0.0;
+      for (long long i = 0; i < n; ++i) {
+        scale = std::max(scale, std::abs(i1[i]));
+        worst = std::max(worst, std::abs(background[i] - i1[i]));
+      }
+      if (worst > 1e-6 * scale) {
+        SetError("v3d: the background state's ice thickness is not the history's at the first node; build the "
+                 "state at times[0]");
+        return SL3DGPU_ERR_ARGUMENT;
+      }
+      SL3D_CUDA(cudaMemcpyAsync(ocean.current.p, ocean.function.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                stream));
+      SL3D_CUDA(cudaMemsetAsync(ocean.sigma.p, 0, lm * sizeof(double2), stream));
+      SL3D_CUDA(cudaMemsetAsync(ocean.psi.p, 0, lm * sizeof(double2), stream));
+      if (u) std::fill(u, u + 2 * lm, 0.0);
+      if (phi) std::fill(phi, phi + 2 * lm, 0.0);
+      if (slc) std::fill(slc, slc + 2 * lm, 0.0);
+      if (omega) std::fill(omega, omega + 3, 0.0);
+      if (oceans) SL3D_TRY(OceanFunction(oceans));
+      if (infos) infos[0] = info;
+      continue;
+    }
+    SL3D_TRY(StepMigrating(st, dt, scheme, i0, i1, l0, l1, &info));
+    if (infos) infos[k] = info;
+    if (u) SL3D_TRY(Surface(0, u + 2 * lm * k));
+    if (phi) SL3D_TRY(Surface(2, phi + 2 * lm * k));
+    if (slc || omega)
+      SL3D_TRY(SeaLevel(slc ? slc + 2 * lm * k : nullptr, omega ? omega + 3 * k : nullptr, nullptr));
+    if (oceans) SL3D_TRY(OceanFunction(oceans + n * k));
+  }
+  return SL3DGPU_OK;
+}
+
+// The ocean function of the last closure (migrating shorelines; the fixed
+// one otherwise), a host field on the sea-level grid.
+int Viscoelastic3DGpu::OceanFunction(double* out) {
+  if (!ocean.on) {
+    SetError("v3d: no ocean is set (sl3dgpu_v3d_set_ocean)");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const double* src = ocean.migrating ? ocean.current.p : ocean.function.p;
+  SL3D_CUDA(cudaMemcpyAsync(out, src, ocean.fieldSize * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
   return SL3DGPU_OK;
 }
 
@@ -3282,6 +3476,36 @@ extern "C" int sl3dgpu_v3d_run_ocean(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, c
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.RunOcean(state->st, times, nodes, scheme, loads, u, phi, sea_level, angular_velocity, infos);
+}
+
+extern "C" int sl3dgpu_v3d_step_migrating(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, double dt, int scheme,
+                                          const double* ice0, const double* ice1, const double* load0,
+                                          const double* load1, sl3dgpu_step_info* info) {
+  if (h == nullptr || state == nullptr) {
+    SetError("v3d: null handle or state");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.StepMigrating(state->st, dt, scheme, ice0, ice1, load0, load1, info);
+}
+
+extern "C" int sl3dgpu_v3d_run_migrating(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const double* times, int nodes,
+                                         int scheme, const double* ice, const double* loads, double* u, double* phi,
+                                         double* sea_level, double* angular_velocity, double* ocean_functions,
+                                         sl3dgpu_step_info* infos) {
+  if (h == nullptr || state == nullptr || times == nullptr || ice == nullptr || nodes < 0) {
+    SetError("v3d: null argument or negative node count");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.RunMigrating(state->st, times, nodes, scheme, ice, loads, u, phi, sea_level, angular_velocity,
+                            ocean_functions, infos);
+}
+
+extern "C" int sl3dgpu_v3d_ocean_function(sl3dgpu_v3d* h, double* out) {
+  if (h == nullptr || out == nullptr) {
+    SetError("v3d: null handle or output");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.OceanFunction(out);
 }
 
 extern "C" int sl3dgpu_v3d_sea_level(sl3dgpu_v3d* h, double* coefficients, double* angular_velocity,

@@ -60,7 +60,9 @@ class OceanOptions(ctypes.Structure):
     _fields_ = [("ocean_function", c_void_p), ("rotation", ctypes.c_int), ("water_density", ctypes.c_double),
                 ("rotation_frequency", ctypes.c_double), ("polar_moment", ctypes.c_double),
                 ("equatorial_moment", ctypes.c_double), ("rtol", ctypes.c_double),
-                ("max_iterations", ctypes.c_int), ("anderson_memory", ctypes.c_int)]
+                ("max_iterations", ctypes.c_int), ("anderson_memory", ctypes.c_int),
+                ("migrating", ctypes.c_int), ("ice_density", ctypes.c_double), ("ice_thickness", c_void_p),
+                ("sea_level", c_void_p), ("forced_land", c_void_p), ("max_nonlinear_iterations", ctypes.c_int)]
 
 
 class SleResult(ctypes.Structure):
@@ -120,6 +122,9 @@ def _signatures():
         "sl3dgpu_v3d_step_ocean": (i, [v, v, d, i, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_run_ocean": (i, [v, v, P_double, i, i, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_sea_level": (i, [v, v, v, ctypes.POINTER(SleResult)]),
+        "sl3dgpu_v3d_step_migrating": (i, [v, v, d, i, v, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_run_migrating": (i, [v, v, P_double, i, i, v, v, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_ocean_function": (i, [v, v]),
         "sl3dgpu_v3d_effective_love": (i, [v, i, d, P_double]),
         "sl3dgpu_v3d_start_step": (i, [v, v, d, i, v]),
         "sl3dgpu_v3d_step_start_strain": (i, [v, v]),
@@ -429,6 +434,50 @@ class Viscoelastic3D:
                          int(anderson_memory))
         check(lib().sl3dgpu_v3d_set_ocean(self._h, ctypes.byref(o)))
 
+    def set_migrating_ocean(self, ice_thickness, sea_level, forced_land=None, rotation: int = 1,
+                            water_density: float = 1000.0, ice_density: float = 917.0,
+                            rotation_frequency: float = 7.27220521664304e-05, polar_moment: float = 8.0359e37,
+                            equatorial_moment: float = 8.0096e37, rtol: float = 1e-10,
+                            max_nonlinear_iterations: int = 50, ocean_function=None) -> None:
+        """An ocean whose shorelines migrate (Evolution3D::RunMigrating): the
+        background state's ice thickness and sea level (fields on the
+        sea-level grid, model length unit) and the land held (a mask, None:
+        none); its ocean function is flotation's (a given one must equal
+        it). Every pass solves the nonlinear sea-level equation from it."""
+        theta, _, nphi = self.ocean_grid()
+        n = theta.size * nphi
+        ice = np.ascontiguousarray(ice_thickness, dtype=np.float64).ravel()
+        sea = np.ascontiguousarray(sea_level, dtype=np.float64).ravel()
+        land = None if forced_land is None else np.ascontiguousarray(forced_land, dtype=np.uint8).ravel()
+        given = None if ocean_function is None else np.ascontiguousarray(ocean_function, dtype=np.float64).ravel()
+        if ice.size != n or sea.size != n or (land is not None and land.size != n) or \
+                (given is not None and given.size != n):
+            raise ValueError("the background's fields live on the sea-level grid")
+        o = OceanOptions(None if given is None else given.ctypes.data, int(rotation), float(water_density),
+                         float(rotation_frequency), float(polar_moment), float(equatorial_moment), float(rtol), 1,
+                         0, 1, float(ice_density), ice.ctypes.data, sea.ctypes.data,
+                         None if land is None else land.ctypes.data, int(max_nonlinear_iterations))
+        check(lib().sl3dgpu_v3d_set_ocean(self._h, ctypes.byref(o)))
+
+    def StepMigrating(self, state: State, dt: float, scheme="sdirk2", ice0=None, ice1=None, load0=None,
+                      load1=None) -> StepInfo:
+        """One coupled step under migrating shorelines: the ice thickness at
+        the step's two ends and the direct loads beside it (None: none)."""
+        code = SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
+        arrays = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (ice0, ice1, load0, load1)]
+        info = StepInfo()
+        check(lib().sl3dgpu_v3d_step_migrating(self._h, state._h, float(dt), code,
+                                               *(None if a is None else a.ctypes.data for a in arrays),
+                                               ctypes.byref(info)))
+        return info
+
+    def OceanFunction(self):
+        """The last closure's ocean function (a field on the sea-level grid)."""
+        theta, _, nphi = self.ocean_grid()
+        out = np.zeros(theta.size * nphi)
+        check(lib().sl3dgpu_v3d_ocean_function(self._h, out.ctypes.data))
+        return out
+
     def StepOcean(self, state: State, dt: float, scheme="sdirk2", load0=None, load1=None) -> StepInfo:
         """One coupled step under the direct (non-ocean) load fields on the
         sea-level grid at the step's start and end (non-dimensional)."""
@@ -595,3 +644,27 @@ class Evolution3D:
                                           omega.ctypes.data, infos))
         return {"U": U, "phi": phi, "sea_level": slc, "omega": omega, "infos": [infos[k] for k in range(n)],
                 "state": state}
+
+    def RunMigrating(self, times, ice, loads=None, state: State | None = None):
+        """Evolution3D::RunMigrating with the operator's migrating ocean
+        (set_migrating_ocean): the ice thickness per node (and direct loads,
+        None: none) on the sea-level grid; snapshots carry U, phi, the
+        relative sea level change, the angular velocity and each node's
+        ocean function."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        theta, _, nphi = self.op.ocean_grid()
+        n, size = times.size, theta.size * nphi
+        ice = np.ascontiguousarray(ice, dtype=np.float64).reshape(n, size)
+        loads = None if loads is None else np.ascontiguousarray(loads, dtype=np.float64).reshape(n, size)
+        lm = (self.op.lmax + 1) * (self.op.lmax + 2) // 2
+        state = state if state is not None else self.op.ZeroState()
+        U, phi, slc = (np.zeros((n, lm), dtype=np.complex128) for _ in range(3))
+        omega = np.zeros((n, 3))
+        oceans = np.zeros((n, size))
+        infos = (StepInfo * max(n, 1))()
+        check(lib().sl3dgpu_v3d_run_migrating(self.op._h, state._h, times.ctypes.data_as(P_double), n, self.scheme,
+                                              ice.ctypes.data, None if loads is None else loads.ctypes.data,
+                                              U.ctypes.data, phi.ctypes.data, slc.ctypes.data, omega.ctypes.data,
+                                              oceans.ctypes.data, infos))
+        return {"U": U, "phi": phi, "sea_level": slc, "omega": omega, "ocean": oceans,
+                "infos": [infos[k] for k in range(n)], "state": state}

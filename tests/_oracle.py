@@ -345,6 +345,48 @@ class OracleStep:
         self.L.oracle_v3d_set_closure(self.h, self._callback, None)
         self.t = 0.0
 
+    def set_migrating(self, ice, sea_level, forced_land=None, **kw):
+        """Closes every pass with the nonlinear sea-level equation from the
+        background (ice, sea_level, forced_land on the sea-level grid, model
+        length), oracle/coupled.py's MigratingClosure; kw: its constants."""
+        from oracle.coupled import MigratingClosure
+
+        lmax = self.options.lmax
+        theta, w, nphi = grid(lmax, 1.0)
+        self.sle_grid = (theta, w, nphi)
+        transforms = (lambda c: synthesise_real(lmax, theta, nphi, c),
+                      lambda f: expand_real(lmax, theta, w, nphi, f),
+                      lambda f: float(np.sum(w * f.reshape(theta.size, nphi).sum(axis=1)) * 2 * np.pi / nphi))
+        state = dict(ice=ice, sea_level=sea_level, forced_land=forced_land)
+        self.closure = MigratingClosure(lmax, transforms, self.body(), state, **kw)
+        size = (lmax + 1) * (lmax + 2) // 2
+
+        def callback(user, t, love, count, u, v, phi, inertia, sigma, psi):
+            love_a = np.ctypeslib.as_array(love, (count,)).copy()
+            cx = lambda q: np.ctypeslib.as_array(q, (2 * size,)).view(np.complex128).copy()
+            s, p = self.closure(t, love_a, cx(u), cx(v), cx(phi), inertia)
+            np.ctypeslib.as_array(sigma, (2 * size,))[:] = s.view(np.float64)
+            np.ctypeslib.as_array(psi, (2 * size,))[:] = p.view(np.float64)
+
+        self._callback = _CLOSURE(callback)
+        self.L.oracle_v3d_set_closure(self.h, self._callback, None)
+        self.t = 0.0
+
+    def step_migrating(self, dt, scheme, ice0, ice1, load0=None, load1=None):
+        """One coupled step under migrating shorelines: the ice at its two
+        ends and the direct loads beside it (None: none)."""
+        self.closure.set_step_ice(self.t, ice0, self.t + dt, ice1)
+        if load0 is None and load1 is None:
+            self.closure.loads = None
+        else:
+            n = self.sle_grid[0].size * self.sle_grid[2]
+            zero = np.zeros(n)
+            self.closure.set_step_loads(self.t, zero if load0 is None else load0, self.t + dt,
+                                        zero if load1 is None else load1)
+        info = self.step(dt, scheme)
+        self.t += dt
+        return info
+
     def step_ocean(self, dt, scheme=2, load0=None, load1=None):
         """One coupled step under the direct load fields at its two ends."""
         n = self.sle_grid[0].size * self.sle_grid[2]

@@ -35,7 +35,7 @@ def _rank(rank, world, port, out):
 def test_two_gloo_ranks_take_the_slowest_times():
     world = 2
     port = _free_port()
-    with mp.Manager() as manager:
+    with mp.get_context("spawn").Manager() as manager:
         out = manager.dict()
         mp.start_processes(_rank, args=(world, port, out), nprocs=world, start_method="spawn")
         results = dict(out)
