@@ -279,6 +279,78 @@ __device__ inline T2 Sub(T2 a, T2 b) {
   return Make<T2>(a.x - b.x, a.y - b.y);
 }
 
+// A double-float value, hi + lo with |lo| <= ulp(hi) / 2 (about 48
+// significant bits): the FP64 ring transforms' arithmetic on the FP32 pipe
+// when the grid emulates FP64 (the FP64 pipe is GB300's slow one). Dekker's
+// and Knuth's error-free transformations -- TwoSum, FastTwoSum and the
+// FMA-based TwoProduct -- in their usual double-single forms: a sum's
+// error is bounded by about 2^-46 (|a| + |b|) (the "sloppy" addition, whose
+// bound is normwise, which is what a transform's error analysis uses), a
+// product's by about 2^-46 |a b|. The _rn intrinsics keep the compiler from
+// contracting the error terms into FMAs.
+struct Df {
+  float hi, lo;
+  __host__ __device__ constexpr Df() : hi(0.0f), lo(0.0f) {}
+  __host__ __device__ constexpr Df(float h, float l) : hi(h), lo(l) {}
+  // the nearest double-float of d (constant-folded for literal constants)
+  __host__ __device__ constexpr Df(double d)
+      : hi(static_cast<float>(d)), lo(static_cast<float>(d - static_cast<double>(static_cast<float>(d)))) {}
+  __host__ __device__ constexpr Df(int i) : Df(static_cast<double>(i)) {}
+  __device__ explicit operator double() const { return static_cast<double>(hi) + static_cast<double>(lo); }
+  __device__ explicit operator float() const { return __fadd_rn(hi, lo); }
+};
+struct Df2 {
+  Df x, y;
+};
+template <>
+struct Real<Df2> {
+  using type = Df;
+};
+
+// FastTwoSum of s and an error term e (|s| >= |e| or s = 0)
+__device__ inline Df Renormalise(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return Df(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ inline Df operator+(Df a, Df b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));  // TwoSum's error
+  return Renormalise(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ inline Df operator-(Df a) { return Df(-a.hi, -a.lo); }
+__device__ inline Df operator-(Df a, Df b) { return a + (-b); }
+__device__ inline Df operator*(Df a, Df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);  // TwoProduct's error
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return Renormalise(p, e);
+}
+
+// A value of the storage type in the compute type, and back.
+template <class C2, class T2>
+__device__ inline C2 ToCompute(T2 v) {
+  if constexpr (std::is_same_v<C2, T2>)
+    return v;
+  else
+    return Make<C2>(typename Real<C2>::type(v.x), typename Real<C2>::type(v.y));
+}
+template <class T, class C>
+__device__ inline T ToStorage(C v) {
+  if constexpr (std::is_same_v<T, C>)
+    return v;
+  else
+    return static_cast<T>(v);
+}
+template <class T2, class C2>
+__device__ inline T2 ToStorage2(C2 v) {
+  if constexpr (std::is_same_v<T2, C2>)
+    return v;
+  else
+    return Make<T2>(ToStorage<typename Real<T2>::type>(v.x), ToStorage<typename Real<T2>::type>(v.y));
+}
+
 // The DFT of R values in registers, y_u = sum_q v_q e^{sign 2 pi i q u / R},
 // for the radices of the plans (2, 3, 4, 5), with the roots as constants.
 template <class T2, int R>
@@ -520,12 +592,17 @@ size_t RingSmem(int n, int rings, int buffers) {
 // One CTA per (colatitude j, group of G consecutive fields p0..p0+G-1), one
 // warp per ring. The spectra [m][j][p] are read and written by the whole CTA
 // with the G fields of an order adjacent; the transforms run warp-synchronous.
-template <class T2, int R1, int R2>
+//
+// T2 is the values' type in memory, C2 the transform's arithmetic: the same
+// type, or double-float (Df2) for FP64 values under FP64 emulation.
+template <class T2, class C2, int R1, int R2>
 __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
     RingKernel(int mode, int lmax, int ntheta, int count, bool real, FftPlan plan, const T2* twGlobal,
                const double* weights, const T2* spectraIn, const void* fieldsIn,
                const typename Real<T2>::type* pointWeight, void* fieldsOut, T2* spectraOut) {
+  static_assert(sizeof(C2) == sizeof(T2), "the shared-memory layout is sized by the storage type");
   using T = typename Real<T2>::type;
+  using C = typename Real<C2>::type;
   extern __shared__ __align__(16) unsigned char ringSmem[];
   const int n = R1 > 0 ? R1 * R2 : plan.n;  // a constant in the two-stage form
   constexpr int buffers = R1 > 0 ? 1 : 2;
@@ -534,9 +611,9 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   const long long ringStride = static_cast<long long>(buffers) * n + 1;
   const int G = blockDim.x / kWarp;
   const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
-  T2* tw = reinterpret_cast<T2*>(ringSmem);
-  T2* twB = tw + n;  // the two-stage form's stage-B twiddles
-  T2* bufs = twB + n;
+  C2* tw = reinterpret_cast<C2*>(ringSmem);
+  C2* twB = tw + n;  // the two-stage form's stage-B twiddles
+  C2* bufs = twB + n;
   // A real field's ring shares one complex transform with the next field's
   // (z = x + i y; Z_m = X_m + i Y_m, X_m = (Z_m + conj Z_{n-m}) / 2,
   // Y_m = (Z_m - conj Z_{n-m}) / 2i): a warp carries two real fields.
@@ -560,11 +637,11 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
           PrefetchL2(pointWeight + (static_cast<long long>(f) * ntheta + j) * n + k * (128 / sizeof(T)));
     }
   }
-  for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = twGlobal[e];
+  for (int e = threadIdx.x; e < n; e += blockDim.x) tw[e] = ToCompute<C2>(twGlobal[e]);
   if constexpr (R1 > 0)
-    for (int e = threadIdx.x; e < n; e += blockDim.x) twB[e] = twGlobal[(e / R1) * (e % R1)];
-  T2* a = bufs + ringStride * warp;  // this warp's ring
-  T2* b = buffers == 2 ? a + n : a;
+    for (int e = threadIdx.x; e < n; e += blockDim.x) twB[e] = ToCompute<C2>(twGlobal[(e / R1) * (e % R1)]);
+  C2* a = bufs + ringStride * warp;  // this warp's ring
+  C2* b = buffers == 2 ? a + n : a;
   int at = 0;  // which of a, b holds the ring's current values
   // the rows of this warp's fields (the second of a real pair may not exist)
   const int f0 = p0 + perRing * warp, f1 = real ? f0 + 1 : f0;
@@ -573,22 +650,22 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   const long long row1 = (static_cast<long long>(f1) * ntheta + j) * n;
   if (mode == kRingSynth || mode == kRingWeighted) {
     for (int e = threadIdx.x; e < G * n; e += blockDim.x)
-      bufs[ringStride * (e / n) + e % n] = Make<T2>(0, 0);
+      bufs[ringStride * (e / n) + e % n] = Make<C2>(0, 0);
     __syncthreads();
 #pragma unroll 4
     for (int e = threadIdx.x; e < mcount * rings; e += blockDim.x) {
       const int r = e % rings, mi = e / rings;
       const int m = real ? mi : mi - lmax;
       const long long at0 = (static_cast<long long>(mi) * ntheta + j) * count + p0 + perRing * r;
-      const T2 v = spectraIn[at0];
-      T2* ring = bufs + ringStride * r;
+      const C2 v = ToCompute<C2>(spectraIn[at0]);
+      C2* ring = bufs + ringStride * r;
       if (real) {
-        const T2 u = perRing * r + 1 < groups ? spectraIn[at0 + 1] : Make<T2>(0, 0);
+        const C2 u = perRing * r + 1 < groups ? ToCompute<C2>(spectraIn[at0 + 1]) : Make<C2>(0, 0);
         if (m == 0) {
-          ring[0] = Make<T2>(v.x, u.x);
+          ring[0] = Make<C2>(v.x, u.x);
         } else {
-          ring[m] = Make<T2>(v.x - u.y, v.y + u.x);      // v + i u
-          ring[n - m] = Make<T2>(v.x + u.y, u.x - v.y);  // conj(v) + i conj(u)
+          ring[m] = Make<C2>(v.x - u.y, v.y + u.x);      // v + i u
+          ring[n - m] = Make<C2>(v.x + u.y, u.x - v.y);  // conj(v) + i conj(u)
         }
       } else {
         ring[m < 0 ? m + n : m] = v;
@@ -596,25 +673,25 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
     }
     __syncthreads();
     if (warp < rings) {
-      at = RingTransform<T2, R1, R2>(a, b, plan, tw, twB, +1, lane);
-      T2* res = at ? b : a;
+      at = RingTransform<C2, R1, R2>(a, b, plan, tw, twB, +1, lane);
+      C2* res = at ? b : a;
       if (mode == kRingSynth) {
         for (int k = lane; k < n; k += kWarp) {
           if (real) {
-            static_cast<T*>(fieldsOut)[row0 + k] = res[k].x;
-            if (second) static_cast<T*>(fieldsOut)[row1 + k] = res[k].y;
+            static_cast<T*>(fieldsOut)[row0 + k] = ToStorage<T>(res[k].x);
+            if (second) static_cast<T*>(fieldsOut)[row1 + k] = ToStorage<T>(res[k].y);
           } else {
-            static_cast<T2*>(fieldsOut)[row0 + k] = res[k];
+            static_cast<T2*>(fieldsOut)[row0 + k] = ToStorage2<T2>(res[k]);
           }
         }
       } else {
         // the pointwise weights on the synthesised values
 #pragma unroll 5
         for (int k = lane; k < n; k += kWarp) {
-          const T w0 = pointWeight[row0 + k];
-          const T w1 = real ? (second ? pointWeight[row1 + k] : T(0)) : w0;
-          const T2 v = res[k];
-          res[k] = Make<T2>(v.x * w0, v.y * w1);
+          const C w0 = C(pointWeight[row0 + k]);
+          const C w1 = real ? (second ? C(pointWeight[row1 + k]) : C(0)) : w0;
+          const C2 v = res[k];
+          res[k] = Make<C2>(v.x * w0, v.y * w1);
         }
         __syncwarp();
       }
@@ -625,17 +702,17 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
     if (warp < rings) {
 #pragma unroll 5
       for (int k = lane; k < n; k += kWarp) {
-        T2 v;
+        C2 v;
         if (real) {
-          v = Make<T2>(static_cast<const T*>(fieldsIn)[row0 + k],
-                       second ? static_cast<const T*>(fieldsIn)[row1 + k] : T(0));
+          v = Make<C2>(C(static_cast<const T*>(fieldsIn)[row0 + k]),
+                       second ? C(static_cast<const T*>(fieldsIn)[row1 + k]) : C(0));
         } else {
-          v = static_cast<const T2*>(fieldsIn)[row0 + k];
+          v = ToCompute<C2>(static_cast<const T2*>(fieldsIn)[row0 + k]);
         }
         if (pointWeight != nullptr) {
-          const T w0 = pointWeight[row0 + k];
-          const T w1 = real ? (second ? pointWeight[row1 + k] : T(0)) : w0;
-          v = Make<T2>(v.x * w0, v.y * w1);
+          const C w0 = C(pointWeight[row0 + k]);
+          const C w1 = real ? (second ? C(pointWeight[row1 + k]) : C(0)) : w0;
+          v = Make<C2>(v.x * w0, v.y * w1);
         }
         a[k] = v;
       }
@@ -646,28 +723,29 @@ __global__ void __launch_bounds__(256, (R1 > 0 && sizeof(T2) == 8) ? 3 : 1)
   // has the same stage count, so the result's side is the same for all: a
   // after two transforms, the stage parity's side after one
   if (warp < rings) {
-    T2* x = at ? b : a;
-    T2* y = at ? a : b;
-    RingTransform<T2, R1, R2>(x, y, plan, tw, twB, -1, lane);
+    C2* x = at ? b : a;
+    C2* y = at ? a : b;
+    RingTransform<C2, R1, R2>(x, y, plan, tw, twB, -1, lane);
   }
   const int out = (mode == kRingWeighted || R1 > 0) ? 0 : plan.stages % 2;
   __syncthreads();
-  const T scale = static_cast<T>(2.0 * 3.14159265358979323846 / n * weights[j]);
+  const C scale = C(static_cast<T>(2.0 * 3.14159265358979323846 / n * weights[j]));
 #pragma unroll 4
   for (int e = threadIdx.x; e < mcount * groups; e += blockDim.x) {
     const int g = e % groups, mi = e / groups;
     const int m = real ? mi : mi - lmax;
-    const T2* ring = bufs + ringStride * (g / perRing) + (out ? n : 0);
-    T2 v;
+    const C2* ring = bufs + ringStride * (g / perRing) + (out ? n : 0);
+    C2 v;
     if (real) {
-      const T2 z = ring[m], w = ring[m == 0 ? 0 : n - m];  // Z_m and Z_{n-m}
+      const C2 z = ring[m], w = ring[m == 0 ? 0 : n - m];  // Z_m and Z_{n-m}
       // X_m = (Z_m + conj Z_{n-m}) / 2, Y_m = (Z_m - conj Z_{n-m}) / 2i
-      v = g % 2 == 0 ? Make<T2>(T(0.5) * (z.x + w.x), T(0.5) * (z.y - w.y))
-                     : Make<T2>(T(0.5) * (z.y + w.y), T(0.5) * (w.x - z.x));
+      v = g % 2 == 0 ? Make<C2>(C(0.5) * (z.x + w.x), C(0.5) * (z.y - w.y))
+                     : Make<C2>(C(0.5) * (z.y + w.y), C(0.5) * (w.x - z.x));
     } else {
       v = ring[m < 0 ? m + n : m];
     }
-    spectraOut[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] = Make<T2>(v.x * scale, v.y * scale);
+    spectraOut[(static_cast<long long>(mi) * ntheta + j) * count + p0 + g] =
+        ToStorage2<T2>(Make<C2>(v.x * scale, v.y * scale));
   }
 }
 
@@ -677,16 +755,16 @@ template <class T2>
 using RingFn = void (*)(int, int, int, int, bool, FftPlan, const T2*, const double*, const T2*, const void*,
                         const typename Real<T2>::type*, void*, T2*);
 
-template <class T2>
+template <class T2, class C2 = T2>
 RingFn<T2> RingKernelFor(int n, int* buffers) {
   *buffers = 1;
   switch (n) {
-    case 800: return RingKernel<T2, 25, 32>;
-    case 400: return RingKernel<T2, 25, 16>;  // R1 odd: stage A's stores are bank-conflict free
-    case 50: return RingKernel<T2, 5, 10>;
-    case 40: return RingKernel<T2, 5, 8>;
-    case 25: return RingKernel<T2, 5, 5>;
-    default: *buffers = 2; return RingKernel<T2, 0, 0>;
+    case 800: return RingKernel<T2, C2, 25, 32>;
+    case 400: return RingKernel<T2, C2, 25, 16>;  // R1 odd: stage A's stores are bank-conflict free
+    case 50: return RingKernel<T2, C2, 5, 10>;
+    case 40: return RingKernel<T2, C2, 5, 8>;
+    case 25: return RingKernel<T2, C2, 5, 5>;
+    default: *buffers = 2; return RingKernel<T2, C2, 0, 0>;
   }
 }
 
@@ -1092,12 +1170,25 @@ int Grid::LegendreAnalysis(int N, bool real, const double* spectra, int P, int p
 }
 
 namespace {
+// Under FP64 emulation the FP64 rings' transforms run in double-float on the
+// FP32 pipe, unless SL3DGPU_FP64_RINGS=1 keeps them on the FP64 pipe.
+bool DoubleFloatRings(const Grid& g) {
+  static const bool fp64 = [] {
+    const char* v = std::getenv("SL3DGPU_FP64_RINGS");
+    return v != nullptr && v[0] == '1';
+  }();
+  return g.emulateFp64 && !fp64;
+}
+
 int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spectraIn,
                const void* fieldsIn, const double* weight, void* fieldsOut, double* spectraOut,
                cudaStream_t stream) {
   if (count == 0) return SL3DGPU_OK;
   int buffers = 2;
-  const RingFn<double2> kernel = RingKernelFor<double2>(g.nphi, &buffers);
+  // double-float takes the planned stages: the two-stage form's unrolled
+  // register transforms would outgrow the instruction cache in it
+  const RingFn<double2> kernel =
+      DoubleFloatRings(g) ? RingKernel<double2, Df2, 0, 0> : RingKernelFor<double2>(g.nphi, &buffers);
   const int rings = RingsPerCta<double2>(g.nphi, buffers);
   const size_t smem = RingSmem<double2>(g.nphi, rings, buffers);
   SL3D_CUDA(AllowDynamicSmem(kernel));
