@@ -1979,7 +1979,8 @@ int Viscoelastic3DGpu::Mixer32Update(int& count, int& slot, bool& first) {
   a.m = std::min(count + 1, a.memory);
   LaunchMixerSweep(a, mixSums.p, stream);
   SL3D_CHECK_LAUNCH();
-  SL3D_TRY(MixerDeviceSolve(gram32, a.m, a.slot, a.memory));
+  LaunchMixerGram(gram32.p, a.m, a.slot, a.memory, mixSums.p, gammaOut.p, stream, nullptr, true);
+  SL3D_CHECK_LAUNCH();
   LaunchMixerMix(a, stream);
   SL3D_CHECK_LAUNCH();
   count = a.m;
@@ -2037,7 +2038,7 @@ int Viscoelastic3DGpu::CaptureCorrectionBody(const Flavour& f, cudaGraphConditio
   SL3D_CHECK_LAUNCH();
   LaunchMixerSweep(a, mixSums.p, stream);
   SL3D_CHECK_LAUNCH();
-  LaunchMixerGram(gram32.p, memory, 0, memory, mixSums.p, gammaOut.p, stream, a.live);
+  LaunchMixerGram(gram32.p, memory, 0, memory, mixSums.p, gammaOut.p, stream, a.live, true);
   SL3D_CHECK_LAUNCH();
   LaunchMixerMix(a, stream);
   SL3D_CHECK_LAUNCH();

@@ -1410,15 +1410,28 @@ namespace {
 
 // The Anderson update's least squares on the device, one FP64 warp: the
 // Gram matrix's slot column and row from the sweep's sums, then gamma =
-// argmin |G gamma - b| by the cyclic Jacobi eigen-decomposition of the
-// symmetric G with eigenvalues at or below machine epsilon times the largest
-// dropped -- the minimum-norm solution of LAPACK's dgelss with rcond < 0,
-// the reference's call (include/sl3dpp/detail/AndersonMixer.hpp:186-211).
-// The same arithmetic, in the same order, as SymmetricLstsq (host/
-// lstsq.hpp): each rotation's angle on lane 0, its column, row and
-// eigenvector updates one lane per index; every sum in the host's order.
+// argmin |G gamma - b| by a Jacobi eigen-decomposition of the symmetric G
+// with eigenvalues at or below machine epsilon times the largest dropped --
+// the minimum-norm solution of LAPACK's dgelss with rcond < 0, the
+// reference's call (include/sl3dpp/detail/AndersonMixer.hpp:186-211).
+// Parallel Jacobi in the round-robin order (Brent and Luk): each round
+// rotates m/2 disjoint index pairs at once -- their angles on as many
+// lanes, then the row and column updates one lane per (pair, index) -- so
+// that a sweep is m - 1 rounds of one rotation's latency rather than
+// m (m - 1) / 2 (the FP64 divisions and square roots on GB300's slow FP64
+// pipe set the pace). Sweeps until the off-diagonal mass is below 1e-32 of
+// the diagonal's, as the host's SymmetricLstsq (host/lstsq.hpp).
+//
+// With `cholesky` (the FP32 correction's mixer, called every pass) the
+// system is first solved by a Cholesky factorisation, a column a step:
+// when every pivot is above 1e-13 of the largest diagonal value the Gram
+// matrix is far from the eigenvalue cut, the minimum-norm solution is its
+// solution, and the factorisation's m square roots replace the Jacobi
+// sweeps' rotations; otherwise (a numerically singular Gram) the
+// eigen-decomposition decides.
 __global__ void __launch_bounds__(32) MixerGramKernel(double* gram, int m, int slot, int memory,
-                                                      const double* sums, double* gamma, const int* live) {
+                                                      const double* sums, double* gamma, const int* live,
+                                                      bool cholesky) {
   if (live != nullptr) {
     if (live[0] != kLiveUpdate) return;
     m = live[1];
@@ -1426,8 +1439,8 @@ __global__ void __launch_bounds__(32) MixerGramKernel(double* gram, int m, int s
   }
   constexpr int M = kMixMaxMemory;
   __shared__ double a[M][M + 1], v[M][M + 1];
-  __shared__ double rot[2];
-  __shared__ int flag;
+  __shared__ double rotC[M / 2], rotS[M / 2];
+  __shared__ int rotP[M / 2], rotQ[M / 2];
   const int lane = threadIdx.x;
   if (lane < m) {
     gram[slot * memory + lane] = sums[lane];
@@ -1441,54 +1454,124 @@ __global__ void __launch_bounds__(32) MixerGramKernel(double* gram, int m, int s
       v[lane][j] = lane == j ? 1.0 : 0.0;
     }
   __syncwarp();
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    if (lane == 0) {
-      double off = 0.0, diag = 0.0;
-      for (int i = 0; i < m; ++i)
-        for (int j = 0; j < m; ++j) (i == j ? diag : off) += a[i][j] * a[i][j];
-      flag = (off <= 1e-32 * diag || off == 0.0) ? 1 : 0;
+  if (cholesky) {
+    // L L^T = G in v's lower triangle, lane i the row i
+    __shared__ double inv[M], rhs[M];
+    double dmax = 0.0;
+    for (int i = 0; i < m; ++i) dmax = fmax(dmax, a[i][i]);
+    bool regular = true;
+    for (int k = 0; k < m; ++k) {
+      double sk = 0.0;
+      if (lane >= k && lane < m) {
+        sk = a[lane][k];
+        for (int j = 0; j < k; ++j) sk -= v[lane][j] * v[k][j];
+      }
+      const double d = __shfl_sync(0xffffffffu, sk, k);  // the pivot, on every lane
+      if (!(d > 1e-13 * dmax)) {
+        regular = false;
+        break;
+      }
+      const double r = sqrt(d), ir = 1.0 / r;
+      if (lane == k) {
+        v[k][k] = r;
+        inv[k] = ir;
+      }
+      if (lane > k && lane < m) v[lane][k] = sk * ir;
+      __syncwarp();
     }
     __syncwarp();
-    if (flag) break;
-    for (int p = 0; p < m; ++p)
-      for (int q = p + 1; q < m; ++q) {
-        if (lane == 0) {
-          if (a[p][q] == 0.0) {
-            rot[0] = 0.0;
-            flag = 1;
-          } else {
-            const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
-            const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            const double c = 1.0 / sqrt(t * t + 1.0);
-            rot[0] = c;
-            rot[1] = t * c;
-            flag = 0;
-          }
-        }
+    if (regular) {
+      // L y = b, then L^T x = y, a column at a time
+      const double* bsum = sums + kMixMaxMemory;
+      if (lane < m) rhs[lane] = bsum[lane];
+      __syncwarp();
+      for (int k = 0; k < m; ++k) {
+        const double yk = rhs[k] * inv[k];
         __syncwarp();
-        if (flag) {  // a[p][q] vanishes: no rotation
-          __syncwarp();
-          continue;
-        }
-        const double c = rot[0], sn = rot[1];
-        if (lane < m) {
-          const double akp = a[lane][p], akq = a[lane][q];
-          a[lane][p] = c * akp - sn * akq;
-          a[lane][q] = sn * akp + c * akq;
-        }
-        __syncwarp();
-        if (lane < m) {
-          const double apk = a[p][lane], aqk = a[q][lane];
-          a[p][lane] = c * apk - sn * aqk;
-          a[q][lane] = sn * apk + c * aqk;
-          const double vkp = v[lane][p], vkq = v[lane][q];
-          v[lane][p] = c * vkp - sn * vkq;
-          v[lane][q] = sn * vkp + c * vkq;
-        }
+        if (lane == k) rhs[k] = yk;
+        if (lane > k && lane < m) rhs[lane] -= v[lane][k] * yk;
         __syncwarp();
       }
-    if (lane == 0) flag = 0;
+      for (int k = m - 1; k >= 0; --k) {
+        const double xk = rhs[k] * inv[k];
+        __syncwarp();
+        if (lane == k) rhs[k] = xk;
+        if (lane < k) rhs[lane] -= v[k][lane] * xk;
+        __syncwarp();
+      }
+      if (lane < m) gamma[lane] = rhs[lane];
+      __syncwarp();
+      if (lane == 0) {
+        bool finite = true;
+        for (int i = 0; i < m; ++i)
+          if (!(rhs[i] - rhs[i] == 0.0)) finite = false;
+        gamma[m] = finite ? 1.0 : 0.0;
+      }
+      return;
+    }
+    // a numerically singular Gram: the eigen-decomposition from the identity
+    for (int j = 0; j < m; ++j)
+      if (lane < m) v[lane][j] = lane == j ? 1.0 : 0.0;
     __syncwarp();
+  }
+  const int even = m + (m & 1);  // a padding index m when m is odd (it rotates nothing)
+  const int pairs = even / 2;
+  for (int sweep = 0; sweep < 60 && m > 1; ++sweep) {
+    // the off-diagonal and diagonal masses, a lane a row
+    double off = 0.0, diag = 0.0;
+    if (lane < m)
+      for (int j = 0; j < m; ++j) (lane == j ? diag : off) += a[lane][j] * a[lane][j];
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      diag += __shfl_xor_sync(0xffffffffu, diag, o);
+    }
+    if (off <= 1e-32 * diag || off == 0.0) break;
+    for (int round = 0; round < even - 1; ++round) {
+      // the round's pairs: position 0 fixed, the others turned by `round`
+      if (lane < pairs) {
+        auto at = [&](int pos) { return pos == 0 ? 0 : 1 + (pos - 1 + round) % (even - 1); };
+        int p = at(lane), q = at(even - 1 - lane);
+        if (p > q) {
+          const int t = p;
+          p = q;
+          q = t;
+        }
+        double c = 1.0, sn = 0.0;
+        if (q < m && a[p][q] != 0.0) {
+          const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+          const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+          c = 1.0 / sqrt(t * t + 1.0);
+          sn = t * c;
+        }
+        rotC[lane] = c;
+        rotS[lane] = sn;
+        rotP[lane] = p;
+        rotQ[lane] = q < m ? q : -1;
+      }
+      __syncwarp();
+      // A <- A J (columns p, q), then A <- J^T A (rows p, q) and V <- V J
+      for (int e = lane; e < pairs * m; e += 32) {
+        const int i = e / m, k = e % m, p = rotP[i], q = rotQ[i];
+        if (q < 0 || rotS[i] == 0.0) continue;
+        const double c = rotC[i], sn = rotS[i];
+        const double akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - sn * akq;
+        a[k][q] = sn * akp + c * akq;
+      }
+      __syncwarp();
+      for (int e = lane; e < pairs * m; e += 32) {
+        const int i = e / m, k = e % m, p = rotP[i], q = rotQ[i];
+        if (q < 0 || rotS[i] == 0.0) continue;
+        const double c = rotC[i], sn = rotS[i];
+        const double apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - sn * aqk;
+        a[q][k] = sn * apk + c * aqk;
+        const double vkp = v[k][p], vkq = v[k][q];
+        v[k][p] = c * vkp - sn * vkq;
+        v[k][q] = sn * vkp + c * vkq;
+      }
+      __syncwarp();
+    }
   }
   // the solve: projections of b on the kept eigenvectors
   __shared__ double proj[M], y[M];
@@ -1528,8 +1611,9 @@ __global__ void __launch_bounds__(32) MixerGramKernel(double* gram, int m, int s
 }  // namespace
 
 void LaunchMixerGram(double* gram, int m, int slot, int memory, const double* sums, double* gamma,
-                     cudaStream_t stream, const int* live) {
-  MixerGramKernel<<<1, 32, 0, stream>>>(gram, m, slot, memory, sums, gamma, live);
+                     cudaStream_t stream, const int* live, bool cholesky) {
+  prof::Scope scope(prof::kMixer, stream);
+  MixerGramKernel<<<1, 32, 0, stream>>>(gram, m, slot, memory, sums, gamma, live, cholesky);
 }
 
 // -- the FP32 correction's loop on the device ------------------------------------------------------

@@ -256,7 +256,7 @@ bool MixerSolve(double* gram, int m, int slot, int memory, const double* sums, d
 // (memory x memory, device) updated from sums (device), gamma (m values and
 // the status) written for the mix. No host round trip.
 void LaunchMixerGram(double* gram, int m, int slot, int memory, const double* sums, double* gamma,
-                     cudaStream_t stream, const int* live = nullptr);
+                     cudaStream_t stream, const int* live = nullptr, bool cholesky = false);
 
 // -- the FP32 correction's loop on the device (a CUDA graph's while node) -------------------------
 
