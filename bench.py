@@ -182,7 +182,7 @@ def measured_peaks():
 
 
 # The committed ncu summary holding a kernel kind's DRAM bytes per launch.
-TRAFFIC_PROFILES = {"ring_fft": "ring_fft_f64_3d_step_lmax256.md"}
+TRAFFIC_PROFILES = {"ring_fft": "ring_fft_df_3d_step_lmax256.md", "legendre_f32": "tcgemm_3d_step_lmax256_traffic.md"}
 
 
 def ncu_traffic(kernel: str):
@@ -344,7 +344,7 @@ def gpu_arm(args, rank, world, device, precision, emulation=None, e2e=True, prof
 
 def roofline(prof, fp64_gflops, fp32_gflops, double_float_rings=False):
     """The dominant kernel kind against the bound of its work: the FP64
-    Legendre GEMM and the FP64 ring FFTs against the FP64 FMA throughput
+    Legendre GEMM, the FP64 ring FFTs and band solves against the FP64 FMA throughput
     measured live, the emulated FP64 contraction against the measured BF16
     tensor rate (algorithmic FP64 flops), the rest -- the 3xTF32 contraction
     streaming its table panels included -- against the measured HBM copy
@@ -358,7 +358,8 @@ def roofline(prof, fp64_gflops, fp32_gflops, double_float_rings=False):
     per_launch_s = p["ms"] / 1e3 / max(p["launches"], 1)
     share = p["ms"] / sum(v["ms"] for v in prof.values())
     flops_bound = {"legendre_synthesis": ("fp64", fp64_gflops / 1e3), "legendre_analysis": ("fp64", fp64_gflops / 1e3),
-                   "ring_fft": ("fp64", fp64_gflops / 1e3), "legendre_f64_tc": ("tensor", peaks["bf16_tflops"])}
+                   "ring_fft": ("fp64", fp64_gflops / 1e3), "band_solve": ("fp64", fp64_gflops / 1e3),
+                   "legendre_f64_tc": ("tensor", peaks["bf16_tflops"])}
     if p["flops"] > 0 and kind in flops_bound:
         bound, peak = flops_bound[kind]
         achieved = p["flops"] / max(p["launches"], 1) / per_launch_s / 1e12
