@@ -27,9 +27,15 @@
 //               cap of ice (917 kg m^-3) growing linearly to its thickness
 //               over the first ramp_nodes nodes, then held
 //   ocean       (optional) {"land_fraction" (0.3), "seed" (11), "rotation":
-//               "none" | "axial" | "full"} frozen shorelines over a land mask
-//               thresholded from a seeded smooth field; each pass closed by
-//               the sea-level equation (sl3dgpu_v3d_set_ocean)
+//               "none" | "axial" | "full", "shorelines": "frozen" |
+//               "migrating", "depth_m" (1500)} frozen shorelines over a land
+//               mask thresholded from a seeded smooth field, each pass closed
+//               by the sea-level equation (sl3dgpu_v3d_set_ocean); or
+//               migrating ones (Evolution3D::RunMigrating): a background sea
+//               level from the same field (ocean depth up to depth_m, land
+//               where the field is above the threshold) with no ice, the cap
+//               as an ice thickness history, each pass closed by the
+//               nonlinear sea-level equation and flotation
 //   time        {"step_yr", "nodes"} or {"times_yr": [...]} on the run's clock
 //   solve       {"scheme": "sdirk2" | "exponential_trapezoid" |
 //               "backward_euler", "step_solver": "fixed_point" |
@@ -112,8 +118,8 @@ struct Config {
   double capDegrees = 15.0, thicknessM = 2000.0;
   int rampNodes = 10;
   // ocean
-  bool ocean = false;
-  double landFraction = 0.3;
+  bool ocean = false, migrating = false;
+  double landFraction = 0.3, depthM = 1500.0;
   uint64_t oceanSeed = 11;
   int rotation = 0;
   // time and scheme
@@ -281,9 +287,16 @@ Config ReadConfig(const std::string& path) {
   // ocean
   if (const Value* ocean = Find(root, "ocean")) {
     const Object& o = ocean->Members("ocean");
-    OnlyKeys(o, {"land_fraction", "seed", "rotation"}, "ocean");
+    OnlyKeys(o, {"land_fraction", "seed", "rotation", "shorelines", "depth_m"}, "ocean");
     c.ocean = true;
     c.landFraction = NumberOr(o, "land_fraction", 0.3);
+    c.depthM = NumberOr(o, "depth_m", 1500.0);
+    if (const Value* sh = Find(o, "shorelines")) {
+      const std::string& name = sh->String("ocean.shorelines");
+      if (name != "frozen" && name != "migrating") throw std::invalid_argument("ocean.shorelines: frozen or migrating");
+      c.migrating = name == "migrating";
+    }
+    if (!(c.depthM > 0.0)) throw std::invalid_argument("ocean.depth_m > 0");
     c.oceanSeed = static_cast<uint64_t>(NumberOr(o, "seed", 11));
     if (const Value* r = Find(o, "rotation")) {
       const std::string& name = r->String("ocean.rotation");
@@ -566,6 +579,8 @@ int Solve(const Config& c) {
   }
 
   // the ice cap, on the sea-level grid (the ocean closure's) or as coefficients
+  std::vector<double> seaLevel, backgroundIce, oceanWeights;
+  int oceanNphi = 0;
   sl3dgpu_grid* exact = nullptr;
   Check(sl3dgpu_grid_create(lmax, 0, 1.0, &exact), "grid");
   int et = 0, ep = 0;
@@ -587,13 +602,34 @@ int Solve(const Config& c) {
     for (int j = 0; j < et; ++j) total += weights[j] * ep;
     std::vector<double> oceanFunction(field.size(), 1.0);
     double covered = 0.0;
+    size_t landCount = 0;
     for (size_t i : order) {
       covered += weights[i / ep];
       if (covered / total > c.landFraction) break;
       oceanFunction[i] = 0.0;
+      ++landCount;
     }
     sl3dgpu_v3d_ocean o{oceanFunction.data(), c.rotation, 1000.0, 7.27220521664304e-05, 8.0359e37, 8.0096e37,
                         c.options.rtol, 200, c.options.anderson_memory};
+    if (c.migrating) {
+      // the background: ocean depth below the threshold value, land height
+      // above it, up to depth_m; no ice (the history's first node)
+      const double threshold = landCount < order.size() ? field[order[landCount]] : field[order.back()];
+      double span = 0.0;
+      for (double v : field) span = std::max(span, std::abs(threshold - v));
+      seaLevel.resize(field.size());
+      for (size_t i = 0; i < field.size(); ++i)
+        seaLevel[i] = c.depthM * (threshold - field[i]) / std::max(span, 1e-300) / length;
+      backgroundIce.assign(field.size(), 0.0);
+      o.ocean_function = nullptr;
+      o.migrating = 1;
+      o.ice_density = kIceDensity;
+      o.ice_thickness = backgroundIce.data();
+      o.sea_level = seaLevel.data();
+      o.max_nonlinear_iterations = 200;
+      oceanWeights = weights;
+      oceanNphi = ep;
+    }
     Check(sl3dgpu_v3d_set_ocean(op, &o), "ocean");
   }
   sl3dgpu_grid_destroy(exact);
@@ -619,7 +655,35 @@ int Solve(const Config& c) {
     const double dt = node > 0 ? (c.timesYr[node] - c.timesYr[node - 1]) * kYear / time : 0.0;
     sl3dgpu_step_info info{};
     NodeRecord rec;
-    if (c.ocean) {
+    if (c.migrating && node == 0) {
+      // undisturbed at the background (the history's first ice is none)
+      info.converged = 1;
+      rec.seaLevel.assign(lm, Complex{});
+    } else if (c.migrating) {
+      // the cap's thickness at the step's two ends (model length)
+      load0.assign(cap.size(), 0.0);
+      load1.assign(cap.size(), 0.0);
+      const double toThickness = sigma / (kIceDensity * length);
+      for (size_t i = 0; i < cap.size(); ++i) {
+        load0[i] = ramp(before) * cap[i] * toThickness;
+        load1[i] = ramp(node) * cap[i] * toThickness;
+      }
+      Check(sl3dgpu_v3d_step_migrating(op, state, dt, c.scheme, load0.data(), load1.data(), nullptr, nullptr, &info),
+            "step");
+      rec.seaLevel.resize(lm);
+      Check(sl3dgpu_v3d_sea_level(op, reinterpret_cast<double*>(rec.seaLevel.data()), nullptr, nullptr),
+            "sea level");
+      for (auto& v : rec.seaLevel) v *= length;
+      // the ocean's share of the area under the node's shorelines
+      std::vector<double> function(cap.size());
+      Check(sl3dgpu_v3d_ocean_function(op, function.data()), "ocean function");
+      double wet = 0.0, all = 0.0;
+      for (size_t i = 0; i < function.size(); ++i) {
+        wet += oceanWeights[i / oceanNphi] * function[i];
+        all += oceanWeights[i / oceanNphi];
+      }
+      std::printf("sl3d: node %zu ocean fraction %.9f\n", node, wet / all);
+    } else if (c.ocean) {
       load0.assign(cap.size(), 0.0);
       load1.assign(cap.size(), 0.0);
       for (size_t i = 0; i < cap.size(); ++i) {
@@ -647,10 +711,12 @@ int Solve(const Config& c) {
     rec.iterations = info.iterations;
     rec.converged = info.converged;
     rec.residual = info.residual;
-    rec.U.resize(lm);
-    rec.phi.resize(lm);
-    Check(sl3dgpu_v3d_surface(op, 0, reinterpret_cast<double*>(rec.U.data())), "surface");
-    Check(sl3dgpu_v3d_surface(op, 2, reinterpret_cast<double*>(rec.phi.data())), "surface");
+    rec.U.assign(lm, Complex{});
+    rec.phi.assign(lm, Complex{});
+    if (!(c.migrating && node == 0)) {
+      Check(sl3dgpu_v3d_surface(op, 0, reinterpret_cast<double*>(rec.U.data())), "surface");
+      Check(sl3dgpu_v3d_surface(op, 2, reinterpret_cast<double*>(rec.phi.data())), "surface");
+    }
     const double potential = length * length / (time * time);
     for (auto& v : rec.U) v *= length;
     for (auto& v : rec.phi) v *= potential;

@@ -9,8 +9,10 @@ members that only steer the run. On the GPU: a run's surface table is the
 library's own evolution (Evolution3D.Run through the C ABI) on the same
 inputs, number for number; a run stopped after a node and restarted from its
 checkpoint writes the uninterrupted run's table bit for bit; another run's
-checkpoint is refused; an ocean run writes the sea level beside U and phi
-and restarts alike."""
+checkpoint is refused; an ocean run, frozen or migrating, writes the sea
+level beside U and phi and restarts alike; the migrating run's growing cap
+moves the shorelines (the ocean's share of the area changes from node to
+node)."""
 
 import json
 import pathlib
@@ -81,6 +83,8 @@ def test_check_reads_the_config_and_hashes_what_decides_the_run(sl3d, tmp_path):
     (lambda c: c.update(restart=True), "checkpoint directory"),
     (lambda c: c["ocean"].update(rotation="sideways") if "ocean" in c else c.update(ocean={"rotation": "sideways"}),
      "ocean.rotation"),
+    (lambda c: c.update(ocean={"shorelines": "wandering"}), "ocean.shorelines"),
+    (lambda c: c.update(ocean={"shorelines": "migrating", "depth_m": -5}), "ocean.depth_m"),
 ])
 def test_check_refuses_bad_configs(sl3d, tmp_path, change, text):
     cfg = base(tmp_path)
@@ -135,9 +139,10 @@ def test_gpu_solve_is_the_library_evolution(gpu, sl3d, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ocean", [False, True])
+@pytest.mark.parametrize("ocean", ["none", "frozen", "migrating"])
 def test_gpu_restart_continues_the_run_bit_for_bit(gpu, sl3d, tmp_path, ocean):
-    extra = {"ocean": {"land_fraction": 0.3, "seed": 11, "rotation": "axial"}} if ocean else {}
+    extra = {} if ocean == "none" else {"ocean": {"land_fraction": 0.3, "seed": 11, "rotation": "axial",
+                                                  "shorelines": ocean}}
     whole = base(tmp_path, nodes=6, **extra)
     whole["output"] = {"file": str(tmp_path / "whole.txt")}
     whole["checkpoint"] = {"directory": str(tmp_path / "ck_whole"), "stride": 2}
@@ -156,9 +161,31 @@ def test_gpu_restart_continues_the_run_bit_for_bit(gpu, sl3d, tmp_path, ocean):
     assert second.returncode == 0 and "resumed after node 2" in second.stdout, second.stdout + second.stderr
     assert (tmp_path / "resumed.txt").read_bytes() == (tmp_path / "whole.txt").read_bytes()
     columns = table(tmp_path / "whole.txt").shape[1]
-    assert columns == (10 if ocean else 8)
+    assert columns == (8 if ocean == "none" else 10)
     # another run's checkpoints are refused
     other = dict(part)
     other["lateral"] = {"viscosity": {"seed": 4, "degree": 4, "rms": 0.8}}
     refused = run(sl3d, "solve", other, tmp_path)
     assert refused.returncode == 1 and "belongs to another run" in refused.stderr, refused.stderr
+
+
+@pytest.mark.gpu
+def test_gpu_migrating_run_moves_the_shorelines(gpu, sl3d, tmp_path):
+    """A cap growing to 500 m over a quarter of the sphere, 70% of which is
+    ocean up to 1.5 km deep: the ice grounds where it outweighs the water
+    column, deeper as it thickens, and the falling sea level dries the
+    shallowest coasts, so the ocean's share of the area changes from node to
+    node; node 0 is the undisturbed background (zero response)."""
+    cfg = base(tmp_path, nodes=5, ocean={"land_fraction": 0.3, "seed": 11, "rotation": "axial",
+                                         "shorelines": "migrating", "depth_m": 1500})
+    # a cap over a quarter of the sphere, thickening through the shallower
+    # depths (2 km would take about 900 m of sea level and dry this ocean)
+    cfg["forcing"] = {"ice": {"cap_degrees": 60, "thickness_m": 500, "ramp_nodes": 4}}
+    result = run(sl3d, "solve", cfg, tmp_path)
+    assert result.returncode == 0, result.stdout + result.stderr
+    fractions = [float(line.split("ocean fraction ")[1]) for line in result.stdout.splitlines()
+                 if "ocean fraction" in line]
+    assert len(fractions) == 4 and len(set(fractions)) > 1, fractions
+    got = table(tmp_path / "surface.txt")
+    assert np.all(got[got[:, 0] == 0][:, 4:] == 0.0)
+    assert np.max(np.abs(got[got[:, 0] == 4][:, 8:10])) > 0.0
