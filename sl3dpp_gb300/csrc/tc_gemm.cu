@@ -327,12 +327,10 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
           if (static_cast<int>(g % kPackWarps) != packer) continue;
           const int slot = static_cast<int>(g % stages);
           const long long round = g / stages;
-          if (round > 0 && !WaitParity(SmemAddr(empty + slot), static_cast<uint32_t>((round - 1) & 1))) {
-            ok = false;
-            break;
-          }
-          if (abortFlag) break;
           float* out = sB + slot * 2 * bTileFloats;
+          // B's values are read before the slot is waited for (they go to
+          // registers): their global latency overlaps the wait
+          bool waited = false;
           for (int first = 0; first < items; first += 32 * kPackChunk) {
             float v[kPackChunk][4];
 #pragma unroll
@@ -345,6 +343,14 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
               for (int q = 0; q < 4; ++q)
                 v[j][q] = (in && k0 + q < it.K) ? __ldg(rawB + it.b + static_cast<long long>(k0 + q) * it.ldb + n)
                                                 : 0.0f;
+            }
+            if (!waited) {
+              waited = true;
+              if (round > 0 && !WaitParity(SmemAddr(empty + slot), static_cast<uint32_t>((round - 1) & 1))) {
+                ok = false;
+                break;
+              }
+              if (abortFlag) break;
             }
 #pragma unroll
             for (int j = 0; j < kPackChunk; ++j) {
@@ -364,6 +370,7 @@ __global__ void __launch_bounds__(kPersistentThreads, 1)
               *reinterpret_cast<float4*>(out + TileIndex(tileN + nn, 4 * grp, 2 * tileN)) = lo;
             }
           }
+          if (!ok || abortFlag) break;
           // the stores visible to the tensor cores before the stage is full
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(SmemAddr(full + slot)) : "memory");
