@@ -35,6 +35,13 @@ const char* sl3dgpu_last_error(void);
 /* Library version string. */
 const char* sl3dgpu_version(void);
 
+/* Device memory for callers without a CUDA toolchain of their own (the C++
+ * classes' device buffers): allocate (*out NULL for 0 bytes), free, and a
+ * synchronous copy between any two of host and device memory. */
+int sl3dgpu_device_alloc(long long bytes, void** out);
+int sl3dgpu_device_free(void* p);
+int sl3dgpu_device_copy(void* dst, const void* src, long long bytes);
+
 /* ---- band solvers (include/sl3dpp/detail/BandSolvers.hpp:24-49) -----------
  * Host-pointer drop-ins of detail::BandCholeskyFactor / BandCholeskySolve /
  * BandLuFactor / BandLuSolve (src/BandSolvers.cpp:23-139): the same storage,

@@ -9,7 +9,9 @@
 //   DegreeOperator, ToroidalOperator
 //                          include/sl3dpp/DegreeOperator.hpp:94-384
 //   SurfaceGrid            include/sl3dpp/SurfaceGrid.hpp:58-287
-//   Viscoelastic3D         include/sl3dpp/Viscoelastic3D.hpp:79-837
+//   Viscoelastic3D         include/sl3dpp/Viscoelastic3D.hpp:79-837, with
+//                          its OpenStep (:440-640) and the GridCoupling maps
+//                          (include/sl3dpp/GridCoupling.hpp:82-428)
 //   ElasticPerturbation3D  include/sl3dpp/ElasticPerturbation3D.hpp:77-225
 // Errors: a bad argument throws std::invalid_argument, anything else that
 // fails std::runtime_error, with the library's text (the reference's
@@ -27,10 +29,14 @@
 //    times, the Sdirk2 stages taking the linear interpolation between them;
 //  - Options carries the GPU forms (mixed precision, warm starts,
 //    tensor-core FP64 contractions) beside the reference's fields, and
-//    refuses the reference's options this build does not implement.
+//    refuses the reference's options this build does not implement;
+//  - the open step's spectral tensors and the degree systems' solutions are
+//    flat complex vectors in the GPU's layouts (Viscoelastic3D::Layout), the
+//    library's device arrays copied in and out by the classes.
 #pragma once
 
 #include <complex>
+#include <cstddef>
 #include <functional>
 #include <map>
 #include <memory>
@@ -38,6 +44,7 @@
 #include <span>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "sl3dgpu.h"
@@ -88,6 +95,44 @@ std::vector<Complex> Flatten(const F& callable, int lmax, double t) {
     for (int m = 0; m <= l; ++m) out[l * (l + 1) / 2 + m] = (*columns)[m];
   }
   return out;
+}
+
+// n values of T in device memory (the library's allocator), freed with the
+// object; host vectors go in and out by copy.
+template <class T>
+class DeviceVector {
+ public:
+  DeviceVector() = default;
+  explicit DeviceVector(std::size_t n) : n_(n) {
+    void* p = nullptr;
+    Check(sl3dgpu_device_alloc(static_cast<long long>(n * sizeof(T)), &p));
+    p_.reset(static_cast<T*>(p));
+  }
+  explicit DeviceVector(std::span<const T> host) : DeviceVector(host.size()) { Upload(host); }
+  void Upload(std::span<const T> host) {
+    if (host.size() != n_) throw std::invalid_argument("a device vector is copied whole");
+    Check(sl3dgpu_device_copy(p_.get(), host.data(), static_cast<long long>(n_ * sizeof(T))));
+  }
+  [[nodiscard]] std::vector<T> Download() const {
+    std::vector<T> out(n_);
+    Check(sl3dgpu_device_copy(out.data(), p_.get(), static_cast<long long>(n_ * sizeof(T))));
+    return out;
+  }
+  [[nodiscard]] T* data() const { return p_.get(); }
+  [[nodiscard]] double* doubles() const { return reinterpret_cast<double*>(p_.get()); }
+  [[nodiscard]] std::size_t size() const { return n_; }
+
+ private:
+  struct Free {
+    void operator()(T* p) const { sl3dgpu_device_free(p); }
+  };
+  std::unique_ptr<T, Free> p_;
+  std::size_t n_ = 0;
+};
+
+// A host coefficient vector for the C ABI (empty: none).
+inline const double* Raw(std::span<const Complex> v) {
+  return v.empty() ? nullptr : reinterpret_cast<const double*>(v.data());
 }
 
 }  // namespace gpu
@@ -417,11 +462,176 @@ class Viscoelastic3D {
   }
   [[nodiscard]] sl3dgpu_v3d* Handle() const { return h_.get(); }
 
+  // -- GridCoupling (include/sl3dpp/GridCoupling.hpp:82-428) ------------------------------------------
+
+  // The sizes of the GPU layouts: complex spectral coefficients of a tensor
+  // over every node, grid values at every node, and the spheroidal and
+  // toroidal systems' complex solution values.
+  struct Layout {
+    long long spectral = 0, gridValues = 0, spheroidal = 0, toroidal = 0;
+  };
+  [[nodiscard]] Layout GetLayout() const {
+    Layout l;
+    gpu::Check(sl3dgpu_v3d_layout(h_.get(), &l.spectral, &l.gridValues, &l.spheroidal, &l.toroidal));
+    return l;
+  }
+  // A tensor field on every node's grid: its spin -2 and spin -1 components
+  // (complex) and its spin 0 component (real), node-major.
+  struct TensorField {
+    std::vector<Complex> c0, c1;
+    std::vector<double> r;
+  };
+  // Synthesise / Analyse of a spectral tensor (GridCoupling::Synthesise,
+  // Analyse).
+  [[nodiscard]] TensorField Synthesise(std::span<const Complex> spectral) const {
+    const auto l = GetLayout();
+    Expect(spectral.size(), l.spectral, "a spectral tensor");
+    gpu::DeviceVector<Complex> in(spectral), c0(l.gridValues), c1(l.gridValues);
+    gpu::DeviceVector<double> r(l.gridValues);
+    gpu::Check(sl3dgpu_v3d_synthesise_tensor(h_.get(), in.doubles(), c0.doubles(), c1.doubles(), r.data()));
+    return TensorField{c0.Download(), c1.Download(), r.Download()};
+  }
+  [[nodiscard]] std::vector<Complex> Analyse(const TensorField& field) const {
+    const auto l = GetLayout();
+    Expect(field.c0.size(), l.gridValues, "a tensor field's spin -2 component");
+    Expect(field.c1.size(), l.gridValues, "a tensor field's spin -1 component");
+    Expect(field.r.size(), l.gridValues, "a tensor field's spin 0 component");
+    gpu::DeviceVector<Complex> c0(std::span<const Complex>(field.c0)), c1(std::span<const Complex>(field.c1)),
+        out(l.spectral);
+    gpu::DeviceVector<double> r(std::span<const double>(field.r));
+    gpu::Check(sl3dgpu_v3d_analyse_tensor(h_.get(), c0.doubles(), c1.doubles(), r.data(), out.doubles()));
+    return out.Download();
+  }
+  // SpheroidalForce / ToroidalForce of an analysed tensor: the degree
+  // systems' right-hand sides, spheroidal then toroidal.
+  [[nodiscard]] std::pair<std::vector<Complex>, std::vector<Complex>> DegreeForces(
+      std::span<const Complex> spectral) const {
+    const auto l = GetLayout();
+    Expect(spectral.size(), l.spectral, "a spectral tensor");
+    gpu::DeviceVector<Complex> in(spectral), sph(l.spheroidal), tor(l.toroidal);
+    gpu::Check(sl3dgpu_v3d_degree_forces(h_.get(), in.doubles(), sph.doubles(), tor.doubles()));
+    return {sph.Download(), tor.Download()};
+  }
+  // AddStrainOfSolution: the strain coefficients of the systems' solutions.
+  [[nodiscard]] std::vector<Complex> StrainOfSolutions(std::span<const Complex> spheroidal,
+                                                       std::span<const Complex> toroidal) const {
+    const auto l = GetLayout();
+    Expect(spheroidal.size(), l.spheroidal, "the spheroidal solutions");
+    Expect(toroidal.size(), l.toroidal, "the toroidal solutions");
+    gpu::DeviceVector<Complex> sph(spheroidal), tor(toroidal), out(l.spectral);
+    gpu::Check(sl3dgpu_v3d_strain_of_solutions(h_.get(), sph.doubles(), tor.doubles(), out.doubles()));
+    return out.Download();
+  }
+
+  // -- OpenStep (Viscoelastic3D.hpp:440-640) ------------------------------------------------------------
+
+  // One stage opened on the operator's buffers for a driver's own
+  // within-step iteration (one open step per operator at a time); strains
+  // are spectral tensors in the GPU layout, the solutions stay in the
+  // operator (Surface and InertiaMoment read them).
+  class OpenStep {
+   public:
+    // the start strain of the stage
+    [[nodiscard]] std::vector<Complex> StartStrain() {
+      gpu::Check(sl3dgpu_v3d_step_start_strain(op_->h_.get(), strain_.doubles()));
+      return strain_.Download();
+    }
+    // Respond: the solutions of the memory and lateral force of a strain
+    // (empty: the start strain), no channels.
+    void Respond(std::span<const Complex> strain = {}) {
+      if (!strain.empty()) Put(strain);
+      gpu::Check(sl3dgpu_v3d_step_respond(op_->h_.get(), strain.empty() ? nullptr : strain_.doubles()));
+    }
+    // AddChannels: the load and tide channels' responses added (host
+    // (l, m >= 0) coefficients, either empty).
+    void AddChannels(std::span<const Complex> load, std::span<const Complex> tide = {}) {
+      gpu::Check(sl3dgpu_v3d_step_add_channels(op_->h_.get(), gpu::Raw(load), gpu::Raw(tide)));
+    }
+    // StrainOf: the strain coefficients of the solutions.
+    [[nodiscard]] std::vector<Complex> StrainOf() {
+      gpu::Check(sl3dgpu_v3d_step_strain_of(op_->h_.get(), strain_.doubles()));
+      return strain_.Download();
+    }
+    // Converge's measure between two strains.
+    [[nodiscard]] double RelativeChange(std::span<const Complex> next, std::span<const Complex> now) {
+      Put(next);
+      gpu::DeviceVector<Complex> b(now);
+      double out = 0.0;
+      gpu::Check(sl3dgpu_v3d_relative_change(op_->h_.get(), strain_.doubles(), b.doubles(), &out));
+      return out;
+    }
+    // Close under known channels: the operator's own fixed point (or
+    // conjugate gradients, or the mixed form, as its options say) from the
+    // start strain; the converged strain and the iteration's info.
+    [[nodiscard]] std::pair<std::vector<Complex>, StepInfo> Close(std::span<const Complex> load,
+                                                                 std::span<const Complex> tide = {}) {
+      sl3dgpu_step_info info{};
+      gpu::Check(sl3dgpu_v3d_step_converge(op_->h_.get(), gpu::Raw(load), gpu::Raw(tide), strain_.doubles(), &info));
+      return {strain_.Download(), Info(info)};
+    }
+    // Finish with a strain (empty: the converged one): the state advances
+    // in place and the step closes.
+    void Finish(std::span<const Complex> strain = {}) {
+      if (!strain.empty()) Put(strain);
+      gpu::Check(sl3dgpu_v3d_step_finish(op_->h_.get(), strain.empty() ? nullptr : strain_.doubles()));
+      state_->t += dt_;
+    }
+    // The conjugate-gradient close's pieces (Forces, Apply, Solve): degree
+    // systems' values, spheroidal then toroidal.
+    [[nodiscard]] std::vector<Complex> Forces(std::span<const Complex> load, std::span<const Complex> tide = {}) {
+      gpu::Check(sl3dgpu_v3d_step_forces(op_->h_.get(), gpu::Raw(load), gpu::Raw(tide), solutions_.doubles()));
+      return solutions_.Download();
+    }
+    [[nodiscard]] std::vector<Complex> Apply(std::span<const Complex> x) {
+      Expect(x.size(), solutions_.size(), "the degree systems' values");
+      gpu::DeviceVector<Complex> in(x);
+      gpu::Check(sl3dgpu_v3d_step_apply(op_->h_.get(), in.doubles(), solutions_.doubles()));
+      return solutions_.Download();
+    }
+    [[nodiscard]] std::pair<std::vector<Complex>, StepInfo> Solve(std::span<const Complex> forces) {
+      Expect(forces.size(), solutions_.size(), "the degree systems' values");
+      gpu::DeviceVector<Complex> in(forces);
+      sl3dgpu_step_info info{};
+      gpu::Check(sl3dgpu_v3d_step_solve(op_->h_.get(), in.doubles(), solutions_.doubles(), &info));
+      return {solutions_.Download(), Info(info)};
+    }
+
+   private:
+    friend class Viscoelastic3D;
+    OpenStep(Viscoelastic3D* op, State* state, double dt)
+        : op_(op), state_(state), dt_(dt), strain_(static_cast<std::size_t>(op->GetLayout().spectral)),
+          solutions_(static_cast<std::size_t>(op->GetLayout().spheroidal + op->GetLayout().toroidal)) {}
+    void Put(std::span<const Complex> strain) {
+      Expect(strain.size(), strain_.size(), "a spectral tensor");
+      strain_.Upload(strain);
+    }
+    Viscoelastic3D* op_;
+    State* state_;
+    double dt_;
+    gpu::DeviceVector<Complex> strain_, solutions_;
+  };
+  // StartStep: one stage of length dt (a one-stage family: backward Euler
+  // or the exponential trapezoid) opened from the state; load0 the load at
+  // the state's time where the state carries no strain (empty: none).
+  [[nodiscard]] OpenStep StartStep(State& state, double dt, Scheme family, std::span<const Complex> load0 = {}) {
+    if (family == Scheme::Sdirk2)
+      throw std::invalid_argument("StartStep opens one stage: backward Euler or the exponential trapezoid");
+    gpu::Check(sl3dgpu_v3d_start_step(h_.get(), state.Handle(), dt, static_cast<int>(family), gpu::Raw(load0)));
+    return OpenStep(this, &state, dt);
+  }
+
  private:
   std::map<int, std::vector<Complex>> SurfaceOf(int component) const {
     std::vector<Complex> flat(static_cast<std::size_t>(lmax_ + 1) * (lmax_ + 2) / 2);
     gpu::Check(sl3dgpu_v3d_surface(h_.get(), component, reinterpret_cast<double*>(flat.data())));
     return gpu::Columns(flat, lmax_);
+  }
+  static void Expect(std::size_t got, long long want, const char* what) {
+    if (static_cast<long long>(got) != want) throw std::invalid_argument(std::string(what) + " has the layout's size");
+  }
+  static StepInfo Info(const sl3dgpu_step_info& info) {
+    return StepInfo{info.iterations, info.residual, info.converged != 0, info.mixed_passes, info.solve_iterations,
+                    info.correction_passes};
   }
   int lmax_;
   std::unique_ptr<sl3dgpu_v3d, gpu::Deleter<sl3dgpu_v3d, sl3dgpu_v3d_destroy>> h_;
@@ -508,8 +718,37 @@ class ElasticPerturbation3D {
     gpu::Check(sl3dgpu_ep3d_surface(h_.get(), static_cast<int>(component), reinterpret_cast<double*>(flat.data())));
     return gpu::Columns(flat, lmax_);
   }
+  // The degree systems' complex values (spheroidal then toroidal), the
+  // layout of Force, Apply, LoadForces and Solution.
+  [[nodiscard]] std::size_t SolutionValues() const {
+    long long sph = 0, tor = 0;
+    gpu::Check(sl3dgpu_ep3d_layout(h_.get(), &sph, &tor));
+    return static_cast<std::size_t>(sph + tor);
+  }
+  // Force: (dK) x under the moduli last set (ElasticPerturbation3D.hpp:98-112).
+  [[nodiscard]] std::vector<Complex> Force(std::span<const Complex> x) { return Map(x, sl3dgpu_ep3d_force); }
+  // Apply: (K_ref + dK) x (:114-130).
+  [[nodiscard]] std::vector<Complex> Apply(std::span<const Complex> x) { return Map(x, sl3dgpu_ep3d_apply); }
+  // LoadForces: the unit load vectors times a load's coefficients.
+  [[nodiscard]] std::vector<Complex> LoadForces(std::span<const Complex> load) {
+    gpu::DeviceVector<Complex> out(SolutionValues());
+    gpu::Check(sl3dgpu_ep3d_load_forces(h_.get(), reinterpret_cast<const double*>(load.data()), out.doubles()));
+    return out.Download();
+  }
+  // The held solution (SolveLoad's, SolveLateral's or Respond's).
+  [[nodiscard]] std::vector<Complex> Solution() {
+    gpu::DeviceVector<Complex> out(SolutionValues());
+    gpu::Check(sl3dgpu_ep3d_solution(h_.get(), out.doubles()));
+    return out.Download();
+  }
 
  private:
+  std::vector<Complex> Map(std::span<const Complex> x, int (*fn)(sl3dgpu_ep3d*, const double*, double*)) {
+    if (x.size() != SolutionValues()) throw std::invalid_argument("x covers the degree systems' values");
+    gpu::DeviceVector<Complex> in(x), out(x.size());
+    gpu::Check(fn(h_.get(), in.doubles(), out.doubles()));
+    return out.Download();
+  }
   void SetModuli(std::span<const double> dMu, std::span<const double> dKappa) {
     for (auto s : {dMu, dKappa})
       if (!s.empty() && s.size() != FieldValues())

@@ -5,13 +5,18 @@
 //   test_api host   argument checks and error mapping, no GPU call
 //   test_api gpu    one degree's system, the band solvers, three Sdirk2
 //                   steps of the 3D operator and one lateral static solve,
-//                   each against the oracle on the same inputs
+//                   each against the oracle on the same inputs; a driver's
+//                   own iteration through OpenStep against the operator's
+//                   step, the GridCoupling maps' identities, and the static
+//                   problem's Force / Apply / LoadForces
 //
 // Prints one line per check and exits non-zero on the first failure.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <optional>
+#include <span>
 #include <random>
 #include <string>
 #include <vector>
@@ -318,6 +323,131 @@ void Static(const sl3dpp::Rheology& body) {
   oracle_v3d_destroy(ref);
 }
 
+// A driver's own within-step iteration through OpenStep -- StartStep,
+// then Respond / AddChannels / StrainOf / RelativeChange until the change is
+// under the tolerance, then Finish -- is the operator's own plain fixed
+// point step for step (the same passes in the same order); the
+// GridCoupling maps keep their identities.
+void OpenStepAndCoupling(const sl3dpp::Rheology& body) {
+  const int lmax = 10;
+  sl3dpp::Viscoelastic3D::Options options;
+  options.rtol = 1e-11;
+  options.max_iterations = 80;
+  options.anderson_memory = 0;
+  sl3dpp::Viscoelastic3D driver(body, lmax, Delta, options), plain(body, lmax, Delta, options);
+  const double year = 3.15576e7 / plain.TimeScale();
+  const double sigma = 1e3 / plain.SurfaceDensityScale();
+  auto load = [&](int l, double t) -> std::optional<std::vector<Complex>> {
+    if (l < 2 || l > 6) return std::nullopt;
+    std::vector<Complex> c(l + 1);
+    c[0] = sigma * (1.0 + t / (1500.0 * year)) / l;
+    c[1] = Complex(0.1, 0.3) * c[0];
+    return c;
+  };
+  const double h = 300.0 * year;
+  auto sd = driver.ZeroState(), sp = plain.ZeroState();
+  std::vector<Complex> converged;
+  for (int n = 0; n < 2; ++n) {
+    const auto l0 = sl3dpp::gpu::Flatten(load, lmax, sd.t), l1 = sl3dpp::gpu::Flatten(load, lmax, sd.t + h);
+    const auto info = plain.Step(sp, h, sl3dpp::Scheme::BackwardEuler, load);
+    auto step = driver.StartStep(sd, h, sl3dpp::Scheme::BackwardEuler, l0);
+    auto s = step.StartStrain();
+    int passes = 0;
+    for (bool first = true;; first = false) {
+      step.Respond(first ? std::span<const Complex>{} : std::span<const Complex>(s));
+      step.AddChannels(l1);
+      auto next = step.StrainOf();
+      const double change = step.RelativeChange(next, s);
+      ++passes;
+      s = std::move(next);
+      if (change <= options.rtol || passes >= options.max_iterations) break;
+    }
+    converged = s;
+    step.Finish(s);
+    Expect(info.converged && passes == info.iterations,
+           "open step " + std::to_string(n) + " takes the operator's passes (" + std::to_string(passes) + " / " +
+               std::to_string(info.iterations) + ")");
+    for (auto c : {sl3dpp::Component::U, sl3dpp::Component::Phi}) {
+      const auto a = driver.Surface(c), b = plain.Surface(c);
+      double diff = 0.0;
+      for (const auto& [l, col] : a)
+        for (std::size_t m = 0; m < col.size(); ++m) diff = std::max(diff, std::abs(col[m] - b.at(l)[m]));
+      Expect(diff == 0.0, "open step " + std::to_string(n) + " surface " + std::to_string(static_cast<int>(c)) +
+                              " is the operator's step bit for bit");
+    }
+  }
+  Expect(std::abs(sd.t - sp.t) == 0.0, "Finish advanced the state's time as Step did");
+  // GridCoupling: Analyse(Synthesise(s)) = s for band-limited s (the grid
+  // oversampled); the degree forces linear; the strain of zero solutions zero
+  const auto layout = driver.GetLayout();
+  Expect(static_cast<long long>(converged.size()) == layout.spectral, "a strain has the layout's spectral size");
+  const auto back = driver.Analyse(driver.Synthesise(converged));
+  double top = 0.0, err = 0.0;
+  for (std::size_t i = 0; i < converged.size(); ++i) {
+    top = std::max(top, std::abs(converged[i]));
+    err = std::max(err, std::abs(back[i] - converged[i]));
+  }
+  Expect(err < 1e-12 * top, "GridCoupling Analyse(Synthesise(s)) = s (" + std::to_string(err / top) + ")");
+  std::vector<Complex> scaled(converged);
+  for (auto& v : scaled) v *= 2.5;
+  const auto [f1s, f1t] = driver.DegreeForces(converged);
+  const auto [f2s, f2t] = driver.DegreeForces(scaled);
+  double ftop = 0.0, ferr = 0.0;
+  for (std::size_t i = 0; i < f1s.size(); ++i) {
+    ftop = std::max(ftop, std::abs(f2s[i]));
+    ferr = std::max(ferr, std::abs(f2s[i] - 2.5 * f1s[i]));
+  }
+  Expect(ferr <= 1e-14 * ftop && static_cast<long long>(f1t.size()) == layout.toroidal,
+         "GridCoupling degree forces are linear");
+  const auto zero = driver.StrainOfSolutions(std::vector<Complex>(layout.spheroidal),
+                                             std::vector<Complex>(layout.toroidal));
+  double zmax = 0.0;
+  for (const auto& v : zero) zmax = std::max(zmax, std::abs(v));
+  Expect(zmax == 0.0, "the strain of zero solutions is zero");
+  ExpectThrow<std::invalid_argument>([&] { (void)driver.Synthesise(std::vector<Complex>(3)); },
+                                     "a strain off the layout is refused");
+}
+
+// ElasticPerturbation3D's Force, Apply and LoadForces on the lateral
+// solution: Apply(y) = LoadForces(load) to the solve's tolerance, Force linear.
+void StaticForceApply(const sl3dpp::Rheology& body) {
+  const int lmax = 8;
+  sl3dpp::ElasticPerturbation3D op(body, lmax);
+  const auto radius = op.Radii();
+  const auto theta = op.CoLatitudes();
+  const int np = op.NumberOfLongitudes();
+  std::vector<double> dMu, dKappa;
+  for (double r : radius)
+    for (double t : theta)
+      for (int k = 0; k < np; ++k) {
+        const double p = 6.283185307179586476925286766559 * k / np;
+        dMu.push_back(0.03 * r * (std::sin(t) * std::cos(p) + 0.2));
+        dKappa.push_back(0.01 * (std::cos(t) + 0.5));
+      }
+  std::vector<Complex> load(static_cast<std::size_t>(lmax + 1) * (lmax + 2) / 2);
+  for (int l = 1; l <= lmax; ++l)
+    for (int m = 0; m <= l; ++m) load[l * (l + 1) / 2 + m] = 1e-4 * Complex(1.0 / (1.0 + l), m == 0 ? 0.0 : 0.2);
+  const auto info = op.SolveLateral(load, dMu, dKappa, {.rtol = 1e-12, .max_iterations = 300});
+  const auto y = op.Solution();
+  const auto applied = op.Apply(y), forces = op.LoadForces(load);
+  double top = 0.0, err = 0.0;
+  for (std::size_t i = 0; i < y.size(); ++i) {
+    top = std::max(top, std::abs(forces[i]));
+    err = std::max(err, std::abs(applied[i] - forces[i]));
+  }
+  Expect(info.converged && err < 1e-9 * top,
+         "ElasticPerturbation3D Apply(y) = LoadForces for SolveLateral's y (" + std::to_string(err / top) + ")");
+  std::vector<Complex> twice(y);
+  for (auto& v : twice) v *= 2.0;
+  const auto f1 = op.Force(y), f2 = op.Force(twice);
+  double ftop = 0.0, ferr = 0.0;
+  for (std::size_t i = 0; i < f1.size(); ++i) {
+    ftop = std::max(ftop, std::abs(f2[i]));
+    ferr = std::max(ferr, std::abs(f2[i] - 2.0 * f1[i]));
+  }
+  Expect(ftop > 0.0 && ferr <= 1e-14 * ftop, "ElasticPerturbation3D Force is linear");
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -330,6 +460,8 @@ int main(int argc, char** argv) {
       Degree(body);
       Step(body);
       Static(body);
+      OpenStepAndCoupling(body);
+      StaticForceApply(body);
     }
   } catch (const std::exception& e) {
     std::printf("FAIL uncaught %s\n", e.what());

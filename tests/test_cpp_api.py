@@ -7,7 +7,10 @@ std::runtime_error, the load callables' layout) runs without a GPU; the GPU
 half checks the band solvers, DegreeOperator / ToroidalOperator, three
 Sdirk2 steps of Viscoelastic3D (delta given as a callable, loads as
 LoadCallable3D) and one ElasticPerturbation3D::SolveLateral against the
-oracle on the same inputs (tests/cpp/test_api.cpp)."""
+oracle on the same inputs, a driver's own iteration through
+Viscoelastic3D::OpenStep against the operator's step (bit for bit), the
+GridCoupling maps' identities, and ElasticPerturbation3D's Force / Apply /
+LoadForces (tests/cpp/test_api.cpp)."""
 
 import pathlib
 import subprocess
@@ -54,3 +57,5 @@ def test_header_compiles_as_cxx23_and_maps_errors_without_a_gpu(binary):
 def test_cpp_api_matches_the_oracle_on_the_gpu(gpu, binary):
     out = _run(binary, "gpu", 900)
     assert "SolveLateral surface 2 matches the oracle" in out and "step 2 surface phi matches" in out
+    assert "open step 1 surface 2 is the operator's step bit for bit" in out
+    assert "ElasticPerturbation3D Force is linear" in out
