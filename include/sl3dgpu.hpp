@@ -9,9 +9,13 @@
 //   DegreeOperator, ToroidalOperator
 //                          include/sl3dpp/DegreeOperator.hpp:94-384
 //   SurfaceGrid            include/sl3dpp/SurfaceGrid.hpp:58-287
+//   GRDSolver              include/sl3dpp/SeaLevel.hpp:206-481 (SolveGeneralised,
+//                          SolveNonlinear, MakeState)
 //   Viscoelastic3D         include/sl3dpp/Viscoelastic3D.hpp:79-837, with
 //                          its OpenStep (:440-640) and the GridCoupling maps
 //                          (include/sl3dpp/GridCoupling.hpp:82-428)
+//   Evolution3D            include/sl3dpp/Evolution3D.hpp (Run, RunMigrating;
+//                          frozen and migrating shorelines)
 //   ElasticPerturbation3D  include/sl3dpp/ElasticPerturbation3D.hpp:77-225
 // Errors: a bad argument throws std::invalid_argument, anything else that
 // fails std::runtime_error, with the library's text (the reference's
@@ -35,6 +39,7 @@
 //    library's device arrays copied in and out by the classes.
 #pragma once
 
+#include <array>
 #include <complex>
 #include <cstddef>
 #include <functional>
@@ -303,6 +308,261 @@ class SurfaceGrid {
   int ntheta_ = 0, nphi_ = 0;
 };
 
+
+// -- the sea-level equation (include/sl3dpp/SeaLevel.hpp) ---------------------------------------------
+
+enum class RotationalFeedback { None = 0, Axial = 1, Full = 2 };
+
+// GRDSolver on its own grid (lmax, spin 0, oversampling 1), non-dimensional:
+// SolveGeneralised (SeaLevel.hpp:228-330) and SolveNonlinear (:418-481)
+// with MakeState (:206). Fields are host vectors over the grid
+// (colatitude-major), coefficients (l, m >= 0) complex; an empty vector is
+// an absent channel. Where the GPU build differs: the body's Love numbers
+// and constants are given as a Body (the reference converts its LoveNumbers
+// and SeaLevelParameters in the constructor), the ice density beside them.
+class GRDSolver {
+ public:
+  struct Body {
+    std::vector<double> h, k, l, ht, kt, lt;  // per degree 0 .. lmax (l, ht, kt, lt may be empty)
+    double g = 1.0, waterDensity = 1.0, radius = 1.0, iceDensity = 0.917;
+    RotationalFeedback rotation = RotationalFeedback::None;
+    double omega = 0.0, polarMoment = 0.0, equatorialMoment = 0.0, gravitationalConstant = 0.0;
+    double hc = 0.0, kc = 0.0, mU = 0.0, mPhi = 0.0, mC = 0.0;
+  };
+  struct Options {
+    double rtol = 1e-9;
+    int max_iterations = 1000;
+    int anderson_memory = 5;
+  };
+  struct State {
+    std::vector<double> iceThickness, seaLevel, oceanFunction;
+    double oceanArea = 0.0;
+    std::vector<char> forcedLand;
+  };
+  struct GeneralisedForcing {
+    std::vector<double> directLoad, directLoadOutsideWaterBudget, solidSurfaceChange;
+    std::vector<Complex> displacementResponse, potentialResponse, tangentialResponse, toroidalResponse, tide;
+    double inertiaMomentChange = 0.0;
+    std::array<double, 3> angularMomentumChange{0.0, 0.0, 0.0};
+  };
+  struct Response {
+    std::vector<double> relativeSeaLevelChange, displacement, potential, tangentialPotential, toroidalPotential;
+    std::array<double, 3> angularVelocity{0.0, 0.0, 0.0};
+    double uniformShift = 0.0;
+    int iterations = 0;
+    double error = 0.0;
+    bool converged = true;
+  };
+  struct NonlinearForcing {
+    std::vector<double> iceThicknessChange, directLoad, directLoadOutsideWaterBudget, solidSurfaceChange,
+        dynamicSeaLevelChange;
+    std::vector<Complex> displacementResponse, potentialResponse, tangentialResponse, toroidalResponse, tide;
+    double inertiaMomentChange = 0.0;
+    std::optional<std::vector<char>> forcedLand;  // absent: the state's
+  };
+  struct NonlinearResponse {
+    State finalState;
+    Response response;
+    std::vector<Complex> loadCoefficients;
+  };
+
+  GRDSolver(int lmax, Body body) : grid_(lmax, 0, 1.0), body_(std::move(body)), lmax_(lmax) {
+    for (const auto* v : {&body_.h, &body_.k})
+      if (static_cast<int>(v->size()) < lmax + 1) throw std::invalid_argument("h and k reach degree lmax");
+    size_ = static_cast<std::size_t>(grid_.NumberOfCoLatitudes()) * grid_.NumberOfLongitudes();
+    weights_.resize(grid_.NumberOfCoLatitudes());
+    std::vector<double> theta(weights_.size());
+    gpu::Check(sl3dgpu_grid_colatitudes(grid_.Handle(), theta.data(), weights_.data()));
+  }
+  [[nodiscard]] std::size_t FieldSize() const { return size_; }
+  [[nodiscard]] std::size_t CoefficientSize() const { return static_cast<std::size_t>(lmax_ + 1) * (lmax_ + 2) / 2; }
+  [[nodiscard]] const SurfaceGrid& Grid() const { return grid_; }
+
+  // int f dS over the sphere of the solver's radius
+  [[nodiscard]] double IntegrateSurface(std::span<const double> field) const {
+    const int nphi = grid_.NumberOfLongitudes();
+    double sum = 0.0;
+    for (std::size_t j = 0; j < weights_.size(); ++j) {
+      double ring = 0.0;
+      for (int k = 0; k < nphi; ++k) ring += field[j * nphi + k];
+      sum += weights_[j] * ring;
+    }
+    return body_.radius * body_.radius * sum * 6.283185307179586476925286766559 / nphi;
+  }
+
+  [[nodiscard]] State MakeState(std::vector<double> iceThickness, std::vector<double> seaLevel,
+                                std::span<const char> forcedLand = {}) const {
+    if (iceThickness.size() != size_ || seaLevel.size() != size_ || (!forcedLand.empty() && forcedLand.size() != size_))
+      throw std::invalid_argument("state fields must live on the grid");
+    gpu::DeviceVector<double> ice{std::span<const double>(iceThickness)}, sea{std::span<const double>(seaLevel)},
+        ocean(size_);
+    gpu::DeviceVector<unsigned char> land(forcedLand.size());
+    if (!forcedLand.empty()) land.Upload(std::span(reinterpret_cast<const unsigned char*>(forcedLand.data()), size_));
+    gpu::Check(sl3dgpu_sle_flotation(static_cast<long long>(size_), body_.waterDensity, body_.iceDensity, ice.data(),
+                                     sea.data(), forcedLand.empty() ? nullptr : land.data(), ocean.data(), nullptr));
+    State st;
+    st.oceanFunction = ocean.Download();
+    st.iceThickness = std::move(iceThickness);
+    st.seaLevel = std::move(seaLevel);
+    st.oceanArea = IntegrateSurface(st.oceanFunction);
+    st.forcedLand.assign(forcedLand.begin(), forcedLand.end());
+    return st;
+  }
+
+  [[nodiscard]] Response SolveGeneralised(const State& state, const GeneralisedForcing& forcing) const {
+    return SolveGeneralised(state, forcing, Options{});
+  }
+  [[nodiscard]] Response SolveGeneralised(const State& state, const GeneralisedForcing& forcing,
+                                          Options options) const {
+    Fields f(*this);
+    const double* ocean = f.Field(state.oceanFunction, "the ocean function", true);
+    sl3dgpu_sle_forcing c{};
+    c.direct_load = f.Field(forcing.directLoad, "the direct load");
+    c.direct_load_outside = f.Field(forcing.directLoadOutsideWaterBudget, "the direct load outside the budget");
+    c.solid_surface_change = f.Field(forcing.solidSurfaceChange, "the solid surface change");
+    c.displacement_response = f.Coeffs(forcing.displacementResponse);
+    c.potential_response = f.Coeffs(forcing.potentialResponse);
+    c.tangential_response = f.Coeffs(forcing.tangentialResponse);
+    c.toroidal_response = f.Coeffs(forcing.toroidalResponse);
+    c.tide = f.Coeffs(forcing.tide);
+    c.inertia_moment_change = forcing.inertiaMomentChange;
+    for (int i = 0; i < 3; ++i) c.angular_momentum_change[i] = forcing.angularMomentumChange[i];
+    Outputs out(size_);
+    const auto b = RawBody();
+    sl3dgpu_sle_result r{};
+    gpu::Check(sl3dgpu_sle_solve(grid_.Handle(), &b, ocean, &c, options.rtol, options.max_iterations,
+                                 options.anderson_memory, out.slc.data(), out.disp.data(), out.pot.data(),
+                                 out.tan.data(), out.tor.data(), &r, nullptr));
+    return out.Collect(r, !forcing.toroidalResponse.empty());
+  }
+
+  // the reference's default budget for the nonlinear solve: 50 iterations
+  [[nodiscard]] NonlinearResponse SolveNonlinear(const State& state, const NonlinearForcing& forcing) const {
+    Options options;
+    options.max_iterations = 50;
+    return SolveNonlinear(state, forcing, options);
+  }
+  [[nodiscard]] NonlinearResponse SolveNonlinear(const State& state, const NonlinearForcing& forcing,
+                                                 Options options) const {
+    Fields f(*this);
+    sl3dgpu_sle_state st{f.Field(state.iceThickness, "the ice thickness", true),
+                         f.Field(state.seaLevel, "the sea level", true),
+                         f.Field(state.oceanFunction, "the ocean function", true), f.Mask(state.forcedLand)};
+    sl3dgpu_sle_nonlinear_forcing c{};
+    c.ice_thickness_change = f.Field(forcing.iceThicknessChange, "the ice thickness change");
+    c.direct_load = f.Field(forcing.directLoad, "the direct load");
+    c.direct_load_outside = f.Field(forcing.directLoadOutsideWaterBudget, "the direct load outside the budget");
+    c.solid_surface_change = f.Field(forcing.solidSurfaceChange, "the solid surface change");
+    c.dynamic_sea_level_change = f.Field(forcing.dynamicSeaLevelChange, "the dynamic sea level change");
+    c.displacement_response = f.Coeffs(forcing.displacementResponse);
+    c.potential_response = f.Coeffs(forcing.potentialResponse);
+    c.tangential_response = f.Coeffs(forcing.tangentialResponse);
+    c.toroidal_response = f.Coeffs(forcing.toroidalResponse);
+    c.tide = f.Coeffs(forcing.tide);
+    c.inertia_moment_change = forcing.inertiaMomentChange;
+    if (forcing.forcedLand) {
+      c.hold_land = 1;
+      c.forced_land = f.Mask(*forcing.forcedLand);
+    }
+    Outputs out(size_);
+    gpu::DeviceVector<double> sea(size_), ocean(size_);
+    gpu::DeviceVector<Complex> load(CoefficientSize());
+    const auto b = RawBody();
+    sl3dgpu_sle_result r{};
+    gpu::Check(sl3dgpu_sle_solve_nonlinear(grid_.Handle(), &b, body_.iceDensity, &st, &c, options.rtol,
+                                           options.max_iterations, out.slc.data(), out.disp.data(), out.pot.data(),
+                                           out.tan.data(), out.tor.data(), sea.data(), ocean.data(), load.doubles(),
+                                           &r, nullptr));
+    NonlinearResponse nr;
+    nr.response = out.Collect(r, !forcing.toroidalResponse.empty());
+    nr.finalState.iceThickness = state.iceThickness;
+    if (!forcing.iceThicknessChange.empty())
+      for (std::size_t i = 0; i < size_; ++i) nr.finalState.iceThickness[i] += forcing.iceThicknessChange[i];
+    nr.finalState.seaLevel = sea.Download();
+    nr.finalState.oceanFunction = ocean.Download();
+    nr.finalState.oceanArea = IntegrateSurface(nr.finalState.oceanFunction);
+    nr.finalState.forcedLand = forcing.forcedLand ? *forcing.forcedLand : state.forcedLand;
+    nr.loadCoefficients = load.Download();
+    return nr;
+  }
+
+ private:
+  // the forcing's device copies, alive for one call
+  struct Fields {
+    explicit Fields(const GRDSolver& s) : solver(s) {}
+    const double* Field(const std::vector<double>& v, const char* what, bool required = false) {
+      if (v.empty()) {
+        if (required) throw std::invalid_argument(std::string(what) + " is required");
+        return nullptr;
+      }
+      if (v.size() != solver.size_) throw std::invalid_argument(std::string(what) + " is not a field on the grid");
+      return fields.emplace_back(std::span<const double>(v)).data();
+    }
+    const double* Coeffs(const std::vector<Complex>& v) {
+      if (v.empty()) return nullptr;
+      if (v.size() != solver.CoefficientSize())
+        throw std::invalid_argument("a response or tide is not a coefficient vector of the grid");
+      return coeffs.emplace_back(std::span<const Complex>(v)).doubles();
+    }
+    const unsigned char* Mask(const std::vector<char>& m) {
+      if (m.empty()) return nullptr;
+      if (m.size() != solver.size_) throw std::invalid_argument("the land held is not a mask on the grid");
+      return masks.emplace_back(std::span(reinterpret_cast<const unsigned char*>(m.data()), m.size())).data();
+    }
+    const GRDSolver& solver;
+    std::vector<gpu::DeviceVector<double>> fields;
+    std::vector<gpu::DeviceVector<Complex>> coeffs;
+    std::vector<gpu::DeviceVector<unsigned char>> masks;
+  };
+  struct Outputs {
+    explicit Outputs(std::size_t n) : slc(n), disp(n), pot(n), tan(n), tor(n) {}
+    GRDSolver::Response Collect(const sl3dgpu_sle_result& r, bool toroidal) const {
+      GRDSolver::Response out;
+      out.relativeSeaLevelChange = slc.Download();
+      out.displacement = disp.Download();
+      out.potential = pot.Download();
+      out.tangentialPotential = tan.Download();
+      if (toroidal) out.toroidalPotential = tor.Download();
+      for (int i = 0; i < 3; ++i) out.angularVelocity[i] = r.angular_velocity[i];
+      out.uniformShift = r.uniform_shift;
+      out.iterations = r.iterations;
+      out.error = r.error;
+      out.converged = r.converged != 0;
+      return out;
+    }
+    gpu::DeviceVector<double> slc, disp, pot, tan, tor;
+  };
+  [[nodiscard]] sl3dgpu_sle_body RawBody() const {
+    auto ptr = [](const std::vector<double>& v) { return v.empty() ? nullptr : v.data(); };
+    sl3dgpu_sle_body b{};
+    b.h = ptr(body_.h);
+    b.k = ptr(body_.k);
+    b.l = ptr(body_.l);
+    b.ht = ptr(body_.ht);
+    b.kt = ptr(body_.kt);
+    b.lt = ptr(body_.lt);
+    b.g = body_.g;
+    b.water_density = body_.waterDensity;
+    b.radius = body_.radius;
+    b.rotation = static_cast<int>(body_.rotation);
+    b.omega = body_.omega;
+    b.polar_moment = body_.polarMoment;
+    b.equatorial_moment = body_.equatorialMoment;
+    b.gravitational_constant = body_.gravitationalConstant;
+    b.hc = body_.hc;
+    b.kc = body_.kc;
+    b.m_u = body_.mU;
+    b.m_phi = body_.mPhi;
+    b.m_c = body_.mC;
+    return b;
+  }
+  SurfaceGrid grid_;
+  Body body_;
+  int lmax_;
+  std::size_t size_ = 0;
+  std::vector<double> weights_;
+};
+
 // -- the 3D step ----------------------------------------------------------------------------------------
 
 class Viscoelastic3D {
@@ -496,9 +756,9 @@ class Viscoelastic3D {
     Expect(field.c0.size(), l.gridValues, "a tensor field's spin -2 component");
     Expect(field.c1.size(), l.gridValues, "a tensor field's spin -1 component");
     Expect(field.r.size(), l.gridValues, "a tensor field's spin 0 component");
-    gpu::DeviceVector<Complex> c0(std::span<const Complex>(field.c0)), c1(std::span<const Complex>(field.c1)),
+    gpu::DeviceVector<Complex> c0{std::span<const Complex>(field.c0)}, c1{std::span<const Complex>(field.c1)},
         out(l.spectral);
-    gpu::DeviceVector<double> r(std::span<const double>(field.r));
+    gpu::DeviceVector<double> r{std::span<const double>(field.r)};
     gpu::Check(sl3dgpu_v3d_analyse_tensor(h_.get(), c0.doubles(), c1.doubles(), r.data(), out.doubles()));
     return out.Download();
   }
@@ -638,6 +898,178 @@ class Viscoelastic3D {
   int nodes_ = 0, ntheta_ = 0, nphi_ = 0;
   std::vector<double> radius_, theta_;
   double length_ = 1.0, time_ = 1.0, sigma_ = 1.0;
+};
+
+
+// -- the run through time (include/sl3dpp/Evolution3D.hpp) ---------------------------------------------
+
+// Evolution3D::Run and RunMigrating (src/Evolution3D.cpp:93-133, March
+// :540-821) on a Viscoelastic3D operator: without an ocean (NoOceanState, the
+// loads as coefficient callables), under an ocean with frozen shorelines
+// (SetOcean; the direct loads as fields on the sea-level grid), or with
+// migrating ones (SetMigrating; the ice thickness history as fields). Where
+// the GPU build differs: the ocean is set on the operator rather than given
+// as the GRDSolver and State of the reference's constructor, its constants
+// SI as SeaLevelParameters gives them; fields are in the model's units.
+class Evolution3D {
+ public:
+  using FieldCallable = std::function<std::vector<double>(double t)>;
+  struct Snapshot {
+    double t = 0.0;
+    std::vector<Complex> U, phi, seaLevel;  // (l, m >= 0) coefficients
+    std::array<double, 3> angularVelocity{0.0, 0.0, 0.0};
+    std::vector<double> oceanFunction;      // migrating shorelines: the node's
+    Viscoelastic3D::StepInfo info;
+  };
+  // The ocean's constants (SeaLevelParameters, include/sl3dpp/SeaLevel.hpp:54-68, SI).
+  struct Ocean {
+    RotationalFeedback rotation = RotationalFeedback::Axial;
+    double waterDensity = 1000.0, iceDensity = 917.0;
+    double rotationFrequency = 7.27220521664304e-05, polarMoment = 8.0359e37, equatorialMoment = 8.0096e37;
+    double rtol = 1e-10;
+    int max_iterations = 200, anderson_memory = 5, max_nonlinear_iterations = 50;
+  };
+
+  explicit Evolution3D(Viscoelastic3D& op, Scheme scheme = Scheme::Sdirk2) : op_(&op), scheme_(scheme) {}
+
+  // The sea-level grid (the operator's lmax, oversampling 1): fields on it are colatitude-major.
+  [[nodiscard]] std::size_t OceanFieldSize() const {
+    int nt = 0, np = 0;
+    gpu::Check(sl3dgpu_v3d_ocean_grid(op_->Handle(), &nt, &np, nullptr, nullptr));
+    return static_cast<std::size_t>(nt) * np;
+  }
+  // Frozen shorelines over an ocean function.
+  void SetOcean(std::span<const double> oceanFunction, const Ocean& c) {
+    if (oceanFunction.size() != OceanFieldSize()) throw std::invalid_argument("the ocean function lives on the sea-level grid");
+    sl3dgpu_v3d_ocean o = Raw(c);
+    o.ocean_function = oceanFunction.data();
+    gpu::Check(sl3dgpu_v3d_set_ocean(op_->Handle(), &o));
+    migrating_ = false;
+  }
+  // Migrating shorelines from a background state (model length; the land
+  // held, empty for none): its ocean function is flotation's.
+  void SetMigrating(std::span<const double> iceThickness, std::span<const double> seaLevel,
+                    std::span<const char> forcedLand, const Ocean& c) {
+    const std::size_t n = OceanFieldSize();
+    if (iceThickness.size() != n || seaLevel.size() != n || (!forcedLand.empty() && forcedLand.size() != n))
+      throw std::invalid_argument("the background's fields live on the sea-level grid");
+    sl3dgpu_v3d_ocean o = Raw(c);
+    o.migrating = 1;
+    o.ice_thickness = iceThickness.data();
+    o.sea_level = seaLevel.data();
+    o.forced_land = forcedLand.empty() ? nullptr : reinterpret_cast<const unsigned char*>(forcedLand.data());
+    gpu::Check(sl3dgpu_v3d_set_ocean(op_->Handle(), &o));
+    migrating_ = true;
+  }
+  void RemoveOcean() { gpu::Check(sl3dgpu_v3d_set_ocean(op_->Handle(), nullptr)); }
+
+  // Run without an ocean: node 0 the instantaneous response, a step a node.
+  [[nodiscard]] std::vector<Snapshot> Run(std::span<const double> times, const Viscoelastic3D::LoadCallable3D& load) {
+    const int n = static_cast<int>(times.size());
+    const std::size_t lm = Coefficients();
+    std::vector<Complex> loads(lm * n);
+    for (int k = 0; k < n; ++k) {
+      const auto flat = gpu::Flatten(load, op_->LMax(), times[k]);
+      std::copy(flat.begin(), flat.end(), loads.begin() + lm * k);
+    }
+    std::vector<Complex> U(lm * n), phi(lm * n);
+    std::vector<sl3dgpu_step_info> infos(std::max(n, 1));
+    auto state = op_->ZeroState();
+    gpu::Check(sl3dgpu_v3d_run(op_->Handle(), state.Handle(), times.data(), n, static_cast<int>(scheme_),
+                               reinterpret_cast<const double*>(loads.data()), reinterpret_cast<double*>(U.data()),
+                               reinterpret_cast<double*>(phi.data()), infos.data()));
+    return Snapshots(times, U, phi, {}, {}, {}, infos);
+  }
+  // Run under the frozen ocean: the direct (ice) load's fields per node.
+  [[nodiscard]] std::vector<Snapshot> RunOcean(std::span<const double> times, const FieldCallable& directLoad) {
+    const auto loads = Sample(times, directLoad, "a direct load");
+    const int n = static_cast<int>(times.size());
+    const std::size_t lm = Coefficients();
+    std::vector<Complex> U(lm * n), phi(lm * n), slc(lm * n);
+    std::vector<double> omega(3 * n);
+    std::vector<sl3dgpu_step_info> infos(std::max(n, 1));
+    auto state = op_->ZeroState();
+    gpu::Check(sl3dgpu_v3d_run_ocean(op_->Handle(), state.Handle(), times.data(), n, static_cast<int>(scheme_),
+                                     loads.data(), reinterpret_cast<double*>(U.data()),
+                                     reinterpret_cast<double*>(phi.data()), reinterpret_cast<double*>(slc.data()),
+                                     omega.data(), infos.data()));
+    return Snapshots(times, U, phi, slc, omega, {}, infos);
+  }
+  // RunMigrating: the ice thickness per node (the first the background's
+  // unless direct loads are given), the direct loads beside it (empty: none).
+  [[nodiscard]] std::vector<Snapshot> RunMigrating(std::span<const double> times, const FieldCallable& iceThickness,
+                                                   const FieldCallable& directLoad = {}) {
+    if (!migrating_) throw std::invalid_argument("RunMigrating needs SetMigrating");
+    const auto ice = Sample(times, iceThickness, "an ice thickness");
+    std::vector<double> loads;
+    if (directLoad) loads = Sample(times, directLoad, "a direct load");
+    const int n = static_cast<int>(times.size());
+    const std::size_t lm = Coefficients(), size = OceanFieldSize();
+    std::vector<Complex> U(lm * n), phi(lm * n), slc(lm * n);
+    std::vector<double> omega(3 * n), oceans(size * n);
+    std::vector<sl3dgpu_step_info> infos(std::max(n, 1));
+    auto state = op_->ZeroState();
+    gpu::Check(sl3dgpu_v3d_run_migrating(op_->Handle(), state.Handle(), times.data(), n, static_cast<int>(scheme_),
+                                         ice.data(), loads.empty() ? nullptr : loads.data(),
+                                         reinterpret_cast<double*>(U.data()), reinterpret_cast<double*>(phi.data()),
+                                         reinterpret_cast<double*>(slc.data()), omega.data(), oceans.data(),
+                                         infos.data()));
+    return Snapshots(times, U, phi, slc, omega, oceans, infos);
+  }
+
+ private:
+  [[nodiscard]] std::size_t Coefficients() const {
+    return static_cast<std::size_t>(op_->LMax() + 1) * (op_->LMax() + 2) / 2;
+  }
+  static sl3dgpu_v3d_ocean Raw(const Ocean& c) {
+    sl3dgpu_v3d_ocean o{};
+    o.rotation = static_cast<int>(c.rotation);
+    o.water_density = c.waterDensity;
+    o.rotation_frequency = c.rotationFrequency;
+    o.polar_moment = c.polarMoment;
+    o.equatorial_moment = c.equatorialMoment;
+    o.rtol = c.rtol;
+    o.max_iterations = c.max_iterations;
+    o.anderson_memory = c.anderson_memory;
+    o.ice_density = c.iceDensity;
+    o.max_nonlinear_iterations = c.max_nonlinear_iterations;
+    return o;
+  }
+  std::vector<double> Sample(std::span<const double> times, const FieldCallable& f, const char* what) const {
+    const std::size_t size = OceanFieldSize();
+    std::vector<double> out;
+    out.reserve(size * times.size());
+    for (double t : times) {
+      const auto v = f(t);
+      if (v.size() != size) throw std::invalid_argument(std::string(what) + " lives on the sea-level grid");
+      out.insert(out.end(), v.begin(), v.end());
+    }
+    return out;
+  }
+  std::vector<Snapshot> Snapshots(std::span<const double> times, const std::vector<Complex>& U,
+                                  const std::vector<Complex>& phi, const std::vector<Complex>& slc,
+                                  const std::vector<double>& omega, const std::vector<double>& oceans,
+                                  const std::vector<sl3dgpu_step_info>& infos) const {
+    const std::size_t lm = Coefficients(), size = OceanFieldSize();
+    std::vector<Snapshot> out(times.size());
+    for (std::size_t k = 0; k < times.size(); ++k) {
+      auto& s = out[k];
+      s.t = times[k];
+      s.U.assign(U.begin() + lm * k, U.begin() + lm * (k + 1));
+      s.phi.assign(phi.begin() + lm * k, phi.begin() + lm * (k + 1));
+      if (!slc.empty()) s.seaLevel.assign(slc.begin() + lm * k, slc.begin() + lm * (k + 1));
+      if (!omega.empty())
+        for (int i = 0; i < 3; ++i) s.angularVelocity[i] = omega[3 * k + i];
+      if (!oceans.empty()) s.oceanFunction.assign(oceans.begin() + size * k, oceans.begin() + size * (k + 1));
+      const auto& i = infos[k];
+      s.info = Viscoelastic3D::StepInfo{i.iterations, i.residual, i.converged != 0, i.mixed_passes,
+                                        i.solve_iterations, i.correction_passes};
+    }
+    return out;
+  }
+  Viscoelastic3D* op_;
+  Scheme scheme_;
+  bool migrating_ = false;
 };
 
 // -- the static 3D solve ----------------------------------------------------------------------------------

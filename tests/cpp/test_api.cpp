@@ -7,8 +7,9 @@
 //                   steps of the 3D operator and one lateral static solve,
 //                   each against the oracle on the same inputs; a driver's
 //                   own iteration through OpenStep against the operator's
-//                   step, the GridCoupling maps' identities, and the static
-//                   problem's Force / Apply / LoadForces
+//                   step, the GridCoupling maps' identities, the static
+//                   problem's Force / Apply / LoadForces, GRDSolver's
+//                   identities and Evolution3D's migrating and frozen runs
 //
 // Prints one line per check and exits non-zero on the first failure.
 #include <cmath>
@@ -82,6 +83,15 @@ double Rel(std::span<const double> a, std::span<const double> b) {
     size = std::max(size, std::abs(b[i]));
   }
   return diff / std::max(size, 1e-300);
+}
+
+double Rel(std::span<const Complex> a, std::span<const Complex> b) {
+  double diff = 0.0, size = 0.0;
+  for (std::size_t i = 0; i < a.size(); ++i) {
+    diff = std::max(diff, std::abs(a[i] - b[i]));
+    size = std::max(size, std::abs(b[i]));
+  }
+  return a.size() == b.size() ? diff / std::max(size, 1e-300) : 1.0;
 }
 
 double Rel(const std::map<int, std::vector<Complex>>& a, std::span<const Complex> flat) {
@@ -448,6 +458,138 @@ void StaticForceApply(const sl3dpp::Rheology& body) {
   Expect(ftop > 0.0 && ferr <= 1e-14 * ftop, "ElasticPerturbation3D Force is linear");
 }
 
+// GRDSolver on the GPU through the class API: the rigid-earth eustatic
+// limit and the ocean gaining the mass the load lost (the generalised solve,
+// tests/TestSeaLevel.cpp:135-206's identities); the nonlinear solve's
+// flotation, its carried load without mass, and where no shoreline moves the
+// linear solve under the grounded ice change.
+void SeaLevel() {
+  const int lmax = 14;  // at 16 the 5% thinning below floats a coastal cell
+  sl3dpp::GRDSolver::Body body;
+  for (int l = 0; l <= lmax; ++l) {
+    body.h.push_back(l > 0 ? -1.2 / (l + 1.0) : 0.0);
+    body.k.push_back(l > 0 ? -0.5 / (l + 1.0) : 0.0);
+    body.l.push_back(l > 0 ? 0.3 / (l + 1.0) : 0.0);
+  }
+  sl3dpp::GRDSolver solver(lmax, body);
+  const auto theta = solver.Grid().CoLatitudes();
+  const int np = solver.Grid().NumberOfLongitudes();
+  const std::size_t n = solver.FieldSize();
+  std::vector<double> sea(n), ice(n), load(n);
+  for (std::size_t j = 0; j < theta.size(); ++j)
+    for (int k = 0; k < np; ++k) {
+      const double t = theta[j], p = 6.283185307179586476925286766559 * k / np;
+      sea[j * np + k] = 0.3 * (0.5 * std::cos(2 * t) + 0.3 + 0.3 * std::sin(2 * p) * std::sin(t));
+      ice[j * np + k] = 0.75 * std::exp(-std::pow(t / 0.5, 4));
+      load[j * np + k] = -0.2 * std::exp(-std::pow((t - 0.3) / 0.2, 2));
+    }
+  const auto state = solver.MakeState(ice, sea);
+  bool flotation = true;
+  for (std::size_t i = 0; i < n; ++i)
+    flotation = flotation && state.oceanFunction[i] == (1.0 * sea[i] - 0.917 * ice[i] > 0.0 ? 1.0 : 0.0);
+  Expect(flotation && state.oceanArea > 0.0, "GRDSolver MakeState takes flotation's ocean function");
+  // the ocean gains what the load lost
+  std::vector<double> land(n);
+  for (std::size_t i = 0; i < n; ++i) land[i] = load[i] * (1.0 - state.oceanFunction[i]);
+  sl3dpp::GRDSolver::GeneralisedForcing forcing;
+  forcing.directLoad = land;
+  const auto r = solver.SolveGeneralised(state, forcing, {.rtol = 1e-12, .max_iterations = 300, .anderson_memory = 5});
+  std::vector<double> gained(n);
+  for (std::size_t i = 0; i < n; ++i) gained[i] = state.oceanFunction[i] * r.relativeSeaLevelChange[i];
+  const double lost = solver.IntegrateSurface(land), got = solver.IntegrateSurface(gained);
+  Expect(r.converged && std::abs(got + lost) < 1e-10 * std::abs(lost),
+         "GRDSolver SolveGeneralised: the ocean gains what the load lost");
+  // a thinning marine cap floats; the carried load has no mass; the final
+  // state is flotation's
+  sl3dpp::GRDSolver::NonlinearForcing melt;
+  melt.iceThicknessChange.resize(n);
+  for (std::size_t i = 0; i < n; ++i) melt.iceThicknessChange[i] = -0.6 * ice[i];
+  const auto nl = solver.SolveNonlinear(state, melt, {.rtol = 1e-12, .max_iterations = 200, .anderson_memory = 0});
+  std::size_t floated = 0;
+  bool final = true;
+  for (std::size_t i = 0; i < n; ++i) {
+    floated += state.oceanFunction[i] == 0.0 && nl.finalState.oceanFunction[i] == 1.0;
+    final = final && nl.finalState.oceanFunction[i] ==
+                         (1.0 * nl.finalState.seaLevel[i] - 0.917 * nl.finalState.iceThickness[i] > 0.0 ? 1.0 : 0.0);
+  }
+  double top = 0.0;
+  for (const auto& c : nl.loadCoefficients) top = std::max(top, std::abs(c));
+  Expect(nl.response.converged && floated > 0 && final,
+         "GRDSolver SolveNonlinear: the thinning cap floats (" + std::to_string(floated) +
+             " cells) and the final state is flotation's");
+  Expect(std::abs(nl.loadCoefficients[0]) < 1e-10 * top, "GRDSolver SolveNonlinear: the carried load has no mass");
+  // a thinning that floats nothing: the linear solve under rho_i (1 - C) dI
+  sl3dpp::GRDSolver::NonlinearForcing thin;
+  thin.iceThicknessChange.resize(n);
+  std::vector<double> grounded(n);
+  for (std::size_t i = 0; i < n; ++i) {
+    thin.iceThicknessChange[i] = -0.05 * ice[i];
+    grounded[i] = 0.917 * (1.0 - state.oceanFunction[i]) * thin.iceThicknessChange[i];
+  }
+  const auto still = solver.SolveNonlinear(state, thin, {.rtol = 1e-13, .max_iterations = 400, .anderson_memory = 0});
+  sl3dpp::GRDSolver::GeneralisedForcing lin;
+  lin.directLoad = grounded;
+  const auto linear = solver.SolveGeneralised(state, lin, {.rtol = 1e-13, .max_iterations = 400, .anderson_memory = 5});
+  Expect(still.finalState.oceanFunction == state.oceanFunction &&
+             Rel(still.response.relativeSeaLevelChange, linear.relativeSeaLevelChange) < 1e-10,
+         "GRDSolver SolveNonlinear without a moving shoreline is the linear solve");
+  ExpectThrow<std::invalid_argument>([&] { (void)solver.MakeState(std::vector<double>(3), sea); },
+                                     "a state off the grid is refused");
+}
+
+// Evolution3D through the class API: under ice that does not change and a
+// direct load that moves no shoreline, the migrating run is the frozen one
+// (tests/TestEvolution3D.cpp:486-507's check, at its 1e-7).
+void Evolution(const sl3dpp::Rheology& body) {
+  const int lmax = 8;
+  sl3dpp::Viscoelastic3D::Options options;
+  options.rtol = 1e-12;
+  options.max_iterations = 80;
+  sl3dpp::Viscoelastic3D a(body, lmax, Delta, options), b(body, lmax, Delta, options);
+  sl3dpp::Evolution3D moving(a), frozen(b);
+  const std::size_t n = moving.OceanFieldSize();
+  sl3dpp::SurfaceGrid grid(lmax, 0, 1.0);
+  const auto theta = grid.CoLatitudes();
+  const int np = grid.NumberOfLongitudes();
+  std::vector<double> sea(n), ice(n), cap(n);
+  const double length = a.LengthScale();
+  for (std::size_t j = 0; j < theta.size(); ++j)
+    for (int k = 0; k < np; ++k) {
+      const double t = theta[j], p = 6.283185307179586476925286766559 * k / np;
+      double f = 0.5 * std::cos(2 * t) + 0.3 + 0.3 * std::sin(2 * p) * std::sin(t);
+      if (std::abs(f) < 0.05) f = f < 0.0 ? -0.05 : 0.05;
+      sea[j * np + k] = 1500.0 * f / length;
+      ice[j * np + k] = 2500.0 * std::exp(-std::pow(t / 0.45, 4)) / length;
+      cap[j * np + k] = t < 0.26 ? 20.0 * 917.0 / a.SurfaceDensityScale() : 0.0;
+    }
+  sl3dpp::Evolution3D::Ocean c;
+  c.rtol = 1e-12;
+  c.max_iterations = 400;
+  c.max_nonlinear_iterations = 400;
+  moving.SetMigrating(ice, sea, {}, c);
+  std::vector<double> ocean(n);
+  for (std::size_t i = 0; i < n; ++i) ocean[i] = 1000.0 * sea[i] - 917.0 * ice[i] > 0.0 ? 1.0 : 0.0;
+  frozen.SetOcean(ocean, c);
+  const double year = 3.15576e7 / a.TimeScale();
+  std::vector<double> times;
+  for (int k = 0; k < 4; ++k) times.push_back(500.0 * year * k);
+  auto loadAt = [&](double t) {
+    std::vector<double> out(cap);
+    for (auto& v : out) v *= t / (1500.0 * year);
+    return out;
+  };
+  const auto m = moving.RunMigrating(times, [&](double) { return ice; }, loadAt);
+  const auto f = frozen.RunOcean(times, loadAt);
+  bool same = m.size() == f.size();
+  double worst = 0.0;
+  for (std::size_t k = 0; same && k < m.size(); ++k) {
+    same = m[k].oceanFunction == ocean;
+    worst = std::max({worst, Rel(m[k].U, f[k].U), Rel(m[k].seaLevel, f[k].seaLevel)});
+  }
+  Expect(same && worst < 1e-7, "Evolution3D RunMigrating under still ice is RunOcean's frozen run (" +
+                                   std::to_string(worst) + ")");
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -462,6 +604,8 @@ int main(int argc, char** argv) {
       Static(body);
       OpenStepAndCoupling(body);
       StaticForceApply(body);
+      SeaLevel();
+      Evolution(body);
     }
   } catch (const std::exception& e) {
     std::printf("FAIL uncaught %s\n", e.what());

@@ -9,8 +9,10 @@ Sdirk2 steps of Viscoelastic3D (delta given as a callable, loads as
 LoadCallable3D) and one ElasticPerturbation3D::SolveLateral against the
 oracle on the same inputs, a driver's own iteration through
 Viscoelastic3D::OpenStep against the operator's step (bit for bit), the
-GridCoupling maps' identities, and ElasticPerturbation3D's Force / Apply /
-LoadForces (tests/cpp/test_api.cpp)."""
+GridCoupling maps' identities, ElasticPerturbation3D's Force / Apply /
+LoadForces, GRDSolver's identities (generalised and nonlinear) and
+Evolution3D's migrating run under still ice against its frozen run
+(tests/cpp/test_api.cpp)."""
 
 import pathlib
 import subprocess
@@ -59,3 +61,5 @@ def test_cpp_api_matches_the_oracle_on_the_gpu(gpu, binary):
     assert "SolveLateral surface 2 matches the oracle" in out and "step 2 surface phi matches" in out
     assert "open step 1 surface 2 is the operator's step bit for bit" in out
     assert "ElasticPerturbation3D Force is linear" in out
+    assert "GRDSolver SolveNonlinear without a moving shoreline is the linear solve" in out
+    assert "Evolution3D RunMigrating under still ice is RunOcean's frozen run" in out
