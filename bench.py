@@ -539,17 +539,22 @@ def warmstart_case(args):
 # -- config 2: the coupled step under an ocean -----------------------------------------------------
 
 def ocean_case(args, device):
-    """Config 2: plain FP64 on the GPU, lmax 128, 80 elements of order 5,
-    Burgers (transient viscosity / 10, modulus ratio 0.5), delta to degree
-    32 at RMS 1.0, an ocean with frozen shorelines over a land mask at 30%
-    of the area (a seeded smooth field thresholded), axial rotational
-    feedback, 50 Sdirk2 steps of 250 yr under config 1's 15 degree cap
-    growing to 2 km over the first 10 steps and held; every pass closed by
-    the sea-level equation (rtol 1e-10). Node 0 is the instantaneous
-    response. Steps/s by CUDA events over the 50 steps (one synchronised
-    step at a time, as the run's host decides each step's loads); passes,
-    closure iterations and the final sea level's range. Parity with the
-    oracle at this shape is tests/test_ocean.py's."""
+    """Config 2 on the GPU, lmax 128, 80 elements of order 5, Burgers
+    (transient viscosity / 10, modulus ratio 0.5), delta to degree 32 at RMS
+    1.0, an ocean with frozen shorelines over a land mask at 30% of the area
+    (a seeded smooth field thresholded), axial rotational feedback, 50 Sdirk2
+    steps of 250 yr under config 1's 15 degree cap growing to 2 km over the
+    first 10 steps and held; every pass closed by the sea-level equation
+    (rtol 1e-10). Node 0 is the instantaneous response. Two forms: the plain
+    FP64 fixed point, and the mixed form (FP64 passes closed by the sea-level
+    equation, FP32 corrections without the ocean's feedback, refined away by
+    the FP64 passes; the Legendre contractions emulated on the tensor cores,
+    the extrapolated warm start). Steps/s by CUDA events over the 50 steps
+    (one synchronised step at a time, as the run's host decides each step's
+    loads); passes, closure iterations, the final sea level's range, and
+    the mixed form's largest relative difference from the FP64 form in the
+    surface U and the sea level over the steps. Parity with the oracle at
+    this shape is tests/test_ocean.py's."""
     import torch
 
     from sl3dpp_gb300 import configs
@@ -557,46 +562,63 @@ def ocean_case(args, device):
     from sl3dpp_gb300.viscoelastic3d import Options, Viscoelastic3D, standard_earth
 
     lmax, elements, ngll, steps, years = 128, 80, 6, 50, 250.0
-    op = Viscoelastic3D(standard_earth(elements, 0.5, 10.0),
-                        Options.defaults(lmax, ngll, rtol=1e-10, max_iterations=120))
-    grid = SurfaceGrid(lmax, 0, 1.5)
-    c = configs.delta_coefficients(lmax, 32, 1.0, 2)
-    pattern = grid.SynthesiseBatch(torch.tensor(c, device=device), 1)
-    ind = torch.tensor(configs.delta_indicator(op.radius), device=device)
-    delta = (ind[:, None] * pattern[None, :]).contiguous().view(-1)
-    op.set_delta(delta)
-    theta, w, nphi = op.ocean_grid()
-    sle_grid = SurfaceGrid(lmax, 0, 1.0)
-    land = sle_grid.SynthesiseBatch(torch.tensor(configs.land_field_coefficients(lmax, 11), device=device), 1)
-    ocean = configs.ocean_from_field(land.cpu().numpy(), w, nphi, 0.3)
-    op.set_ocean(ocean, rotation=1, rtol=1e-10, max_iterations=200, anderson_memory=5)
-    cap = configs.cap_field(theta, nphi, CAP_DEGREES, CAP_THICKNESS) / op.surface_density_scale
-    ice = lambda n: cap * min(n, 10) / 10.0
-    dt = years * configs.SECONDS_PER_YEAR / op.time_scale
-    state = op.ZeroState()
-    op.StepOcean(state, 0.0, 2, ice(0), ice(0))
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    passes, closure_iterations, ms = [], [], 0.0
-    for n in range(1, steps + 1):
-        torch.cuda.synchronize()
-        start.record()
-        info = op.StepOcean(state, dt, 2, ice(n - 1), ice(n))
-        stop.record()
-        stop.synchronize()
-        ms += start.elapsed_time(stop)
-        if not info.converged:
-            raise RuntimeError(f"config 2: step {n} did not converge ({info.iterations} passes)")
-        passes.append(info.iterations)
-        _, _, res = op.SeaLevel()
-        closure_iterations.append(res.iterations)
-    slc, omega, _ = op.SeaLevel()
-    field = sle_grid.SynthesiseBatch(torch.tensor(slc, device=device), 1).cpu().numpy() * op.length_scale
+
+    def run(mixed):
+        kw = dict(rtol=1e-10, max_iterations=120)
+        if mixed:
+            kw.update(precision=1, correction_rtol=CORRECTION_RTOL, correction_memory=CORRECTION_MEMORY,
+                      warm_start=1, fp64_emulation=1)
+        op = Viscoelastic3D(standard_earth(elements, 0.5, 10.0), Options.defaults(lmax, ngll, **kw))
+        grid = SurfaceGrid(lmax, 0, 1.5)
+        c = configs.delta_coefficients(lmax, 32, 1.0, 2)
+        pattern = grid.SynthesiseBatch(torch.tensor(c, device=device), 1)
+        ind = torch.tensor(configs.delta_indicator(op.radius), device=device)
+        op.set_delta((ind[:, None] * pattern[None, :]).contiguous().view(-1))
+        theta, w, nphi = op.ocean_grid()
+        sle_grid = SurfaceGrid(lmax, 0, 1.0)
+        land = sle_grid.SynthesiseBatch(torch.tensor(configs.land_field_coefficients(lmax, 11), device=device), 1)
+        ocean = configs.ocean_from_field(land.cpu().numpy(), w, nphi, 0.3)
+        op.set_ocean(ocean, rotation=1, rtol=1e-10, max_iterations=200, anderson_memory=5)
+        cap = configs.cap_field(theta, nphi, CAP_DEGREES, CAP_THICKNESS) / op.surface_density_scale
+        ice = lambda n: cap * min(n, 10) / 10.0
+        dt = years * configs.SECONDS_PER_YEAR / op.time_scale
+        state = op.ZeroState()
+        op.StepOcean(state, 0.0, 2, ice(0), ice(0))
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        passes, corrections, closure_iterations, surfaces, ms = [], [], [], [], 0.0
+        for n in range(1, steps + 1):
+            torch.cuda.synchronize()
+            start.record()
+            info = op.StepOcean(state, dt, 2, ice(n - 1), ice(n))
+            stop.record()
+            stop.synchronize()
+            ms += start.elapsed_time(stop)
+            if not info.converged:
+                raise RuntimeError(f"config 2: step {n} did not converge ({info.iterations} passes)")
+            passes.append(info.iterations)
+            corrections.append(info.correction_passes)
+            slc_n, _, res = op.SeaLevel()
+            closure_iterations.append(res.iterations)
+            surfaces.append((op.Surface(0), slc_n))
+        slc, omega, _ = op.SeaLevel()
+        field = sle_grid.SynthesiseBatch(torch.tensor(slc, device=device), 1).cpu().numpy() * op.length_scale
+        out = {"steps_per_s": steps / (ms / 1e3), "ms_per_step": ms / steps, "passes_per_step": float(np.mean(passes)),
+               "passes": passes, "last_closure_iterations": closure_iterations[-1],
+               "sea_level_range_m": [float(field.min()), float(field.max())],
+               "axial_angular_velocity": float(omega[2] / op.time_scale)}
+        if mixed:
+            out["correction_passes_per_step"] = float(np.mean(corrections))
+        return out, surfaces
+
+    fp64, s64 = run(False)
+    mixed, smx = run(True)
+    mixed["max_rel_diff_vs_fp64"] = {
+        "U": max(rel_err(a[0], b[0]) for a, b in zip(smx, s64)),
+        "sea_level": max(rel_err(a[1], b[1]) for a, b in zip(smx, s64))}
+    mixed["speedup_vs_fp64"] = mixed["steps_per_s"] / fp64["steps_per_s"]
     return {"case": "config 2: lmax 128, 80 elements of order 5, Burgers, delta degree 32 RMS 1.0, ocean with "
                     "frozen shorelines over 70% of the area, axial rotation, 50 Sdirk2 steps of 250 yr",
-            "steps_per_s": steps / (ms / 1e3), "ms_per_step": ms / steps, "passes_per_step": float(np.mean(passes)),
-            "passes": passes, "last_closure_iterations": closure_iterations[-1],
-            "sea_level_range_m": [float(field.min()), float(field.max())],
-            "axial_angular_velocity": float(omega[2] / op.time_scale)}
+            **fp64, "mixed": mixed}
 
 
 # -- config 4: the ensemble ----------------------------------------------------------------------

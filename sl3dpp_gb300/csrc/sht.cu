@@ -574,8 +574,7 @@ enum RingMode { kRingSynth = 0, kRingAnalyse = 1, kRingWeighted = 2 };
 // and the rings' buffers: two for the planned stages, one for the two-stage
 // form, which works in place) stays near 100 KB.
 template <class T2>
-int RingsPerCta(int n, int buffers) {
-  const long long budget = 100 * 1024;
+int RingsPerCta(int n, int buffers, long long budget = 100 * 1024) {
   const long long ring = static_cast<long long>(buffers) * n * sizeof(T2);
   const long long g = (budget - 2LL * n * sizeof(T2)) / ring;
   return static_cast<int>(std::max(1LL, std::min(8LL, g)));
@@ -1187,9 +1186,12 @@ int LaunchRing(const Grid& g, int mode, bool real, int count, const double* spec
   int buffers = 2;
   // double-float takes the planned stages: the two-stage form's unrolled
   // register transforms would outgrow the instruction cache in it
-  const RingFn<double2> kernel =
-      DoubleFloatRings(g) ? RingKernel<double2, Df2, 0, 0> : RingKernelFor<double2>(g.nphi, &buffers);
-  const int rings = RingsPerCta<double2>(g.nphi, buffers);
+  const bool df = DoubleFloatRings(g);
+  const RingFn<double2> kernel = df ? RingKernel<double2, Df2, 0, 0> : RingKernelFor<double2>(g.nphi, &buffers);
+  // the planned stages keep two rings of 16-byte values a warp: at long
+  // rings the double-float kernel takes one CTA an SM with up to eight
+  // rings rather than two CTAs of two
+  const int rings = RingsPerCta<double2>(g.nphi, buffers, df && g.nphi > 400 ? 210 * 1024 : 100 * 1024);
   const size_t smem = RingSmem<double2>(g.nphi, rings, buffers);
   SL3D_CUDA(AllowDynamicSmem(kernel));
   const int fields = real ? 2 * rings : rings;  // real fields go two to a ring

@@ -1398,8 +1398,8 @@ int Viscoelastic3DGpu::SetOcean(const sl3dgpu_v3d_ocean* o) {
     ocean.on = false;
     return SL3DGPU_OK;
   }
-  if (staticMode || options.solver != 0 || options.precision != 0) {
-    SetError("v3d: the ocean closure is built for the FP64 fixed point (precision 0, solver 0)");
+  if (staticMode || options.solver != 0) {
+    SetError("v3d: the ocean closure is built for the fixed point (solver 0), FP64 or mixed");
     return SL3DGPU_ERR_ARGUMENT;
   }
   if ((o->ocean_function == nullptr && !o->migrating) || o->rotation < 0 || o->rotation > 2 ||

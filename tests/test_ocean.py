@@ -13,7 +13,8 @@ GPU the library's coupled step (sl3dgpu_v3d_step_ocean) is compared with
 the oracle pass for pass at 1e-10 (the FP64 form's bar): a small Earth over
 several Sdirk2 and trapezoid steps, and config 2's shape (lmax 128, 80
 elements of order 5, Burgers, delta to degree 32 at RMS 1, an ocean over
-70% of a seeded mask, axial rotation) over the first passes of a stage."""
+70% of a seeded mask, axial rotation) over the first passes of a stage; the
+mixed form under the closure, frozen or migrating, against the FP64 form."""
 
 import numpy as np
 import pytest
@@ -183,3 +184,51 @@ def test_gpu_config2_coupled_stage_passes_match_the_oracle(gpu):
     slc_o, omega_o = o.sea_level()
     assert rel(slc_g, slc_o) < 1e-10
     assert abs(omega_g[2] - omega_o[2]) < 1e-10 * abs(omega_o[2])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("migrating", [False, True])
+def test_gpu_mixed_form_closes_the_ocean(gpu, migrating):
+    """The mixed form under the ocean closure: its FP64 passes close the
+    sea-level equation (frozen or migrating shorelines), its FP32
+    corrections leave the ocean's feedback out, and the FP64 passes refine
+    the difference away -- the same steps as the FP64 form to its bar's
+    neighbourhood (1e-8), in fewer FP64 passes."""
+    from sl3dpp_gb300.viscoelastic3d import Options, Viscoelastic3D, standard_earth
+    from tests.test_migrating import basin
+
+    lmax = 12
+    o = O.OracleStep(O.standard_earth(24, 0.5, 10.0), O.default_options(lmax, 5))
+    d = delta_for(o, lmax, 4, 0.8, 3)
+    forms = {}
+    for name, kw in (("fp64", {}), ("mixed", dict(precision=1, correction_rtol=3e-6, correction_memory=8,
+                                                   warm_start=1))):
+        g = Viscoelastic3D(standard_earth(24, 0.5, 10.0), Options.defaults(lmax, 5, rtol=1e-11, max_iterations=80,
+                                                                            **kw))
+        g.set_delta(d)
+        dt = 500 * configs.SECONDS_PER_YEAR / g.time_scale
+        state = g.ZeroState()
+        surfaces, passes = [], []
+        if migrating:
+            sea, ice = basin(o, lmax)
+            g.set_migrating_ocean(ice, sea, rotation=1, rtol=1e-11, max_nonlinear_iterations=300)
+            for n in range(1, 4):
+                info = g.StepMigrating(state, dt, "sdirk2", ice * (1 - 0.15 * (n - 1)), ice * (1 - 0.15 * n))
+                assert info.converged
+                surfaces.append((g.Surface(0), g.SeaLevel()[0], g.OceanFunction()))
+                passes.append(info.iterations)
+        else:
+            g.set_ocean(ocean_mask(lmax), rotation=1, rtol=1e-11)
+            load = cap_field(lmax, g.surface_density_scale, 2000.0)
+            g.StepOcean(state, 0.0, 2, 0.1 * load, 0.1 * load)
+            for n in range(1, 4):
+                info = g.StepOcean(state, dt, 2, 0.1 * n * load, 0.1 * (n + 1) * load)
+                assert info.converged
+                surfaces.append((g.Surface(0), g.SeaLevel()[0], None))
+                passes.append(info.iterations)
+        forms[name] = (surfaces, passes)
+    for (u64, s64, c64), (umx, smx, cmx) in zip(forms["fp64"][0], forms["mixed"][0]):
+        assert rel(umx, u64) < 1e-8 and rel(smx, s64) < 1e-8
+        if migrating:
+            np.testing.assert_array_equal(cmx, c64)
+    assert sum(forms["mixed"][1]) < sum(forms["fp64"][1])
