@@ -572,6 +572,32 @@ int sl3dgpu_v3d_state_coefficients_copy(const sl3dgpu_v3d* op, const sl3dgpu_v3d
  * node in the same layout; infos (nullable): each node's step info. */
 int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* times, int nodes, int scheme,
                     const double* loads, double* u, double* phi, sl3dgpu_step_info* infos);
+/* The discrete adjoint of that run (AdjointSolver3D::FirstOrderKernels under
+ * AdjointMethod::Discrete, include/sl3dpp/Adjoint3D.hpp:241-322,
+ * src/AdjointDiscrete3D.cpp): the run from a zero state, every node's state
+ * kept, then the exact transpose of its time-stepped map swept back node by
+ * node (Sdirk2's first stage repeated from the node below). The objective
+ * J = sum_n <u_dual_n, U_n> + <phi_dual_n, phi_n>, <a, b> = sum_{l, m >= 0}
+ * w_m Re(a b*) with w_m = 1 at m = 0 and 2 above (the surface integral of
+ * the two real fields over the unit sphere); u_dual, phi_dual: nodes x
+ * (l(l+1)/2 + m) complex host coefficients (nullable, m = 0 parts real).
+ * Out: load_kernels (required, the same layout), the load kernels
+ * (Kernels::directLoadKernels): dJ = sum_n <load_kernels_n, dL_n>;
+ * delta_gradient (nullable, one double per grid value, node-major as
+ * set_delta's samples): dJ/d delta at each sample, dJ = sum_x
+ * delta_gradient_x d delta_x -- divided by sl3dgpu_v3d_sample_volumes it
+ * is the reference's logViscosityKernel3D, a density per unit volume;
+ * objective (nullable): J of the forward run; infos (nullable): the forward
+ * steps' infos. Without an ocean and for the fixed-point step (solver 0,
+ * FP64 or mixed); the transposed solves take the operator's rtol. Every
+ * node's state is held on the device for the sweep. */
+int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* op, const double* times, int nodes, int scheme, const double* loads,
+                            const double* u_dual, const double* phi_dual, double* load_kernels,
+                            double* delta_gradient, double* objective, sl3dgpu_step_info* infos);
+/* The volume each grid sample stands for (GridCoupling's volume weight:
+ * the radial quadrature weight jac w_q r^2 of its memory node times its
+ * colatitude's weight 2 pi w_theta / nphi), one double per grid value. */
+int sl3dgpu_v3d_sample_volumes(const sl3dgpu_v3d* op, double* out);
 /* Many independent runs at once (an ensemble: the reference's calibration and
  * line-search workloads run Evolution3D per member): run i is
  * sl3dgpu_v3d_run(ops[i], states[i], times[i], nodes[i], scheme, loads[i],

@@ -33,6 +33,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "assemble.cuh"
@@ -263,6 +264,35 @@ class Viscoelastic3DGpu {
   int RunMigrating(V3dState& st, const double* times, int nodes, int scheme, const double* ice, const double* loads,
                    double* u, double* phi, double* slc, double* omega, double* oceans, sl3dgpu_step_info* infos);
   int OceanFunction(double* out);
+
+  // The discrete adjoint of Run without an ocean (AdjointSolver3D under
+  // AdjointMethod::Discrete, src/AdjointDiscrete3D.cpp): the forward run
+  // recorded at every node, then the transposed sweep node by node. With no
+  // ocean the step's system (K - F An W Syn Str) x = F phi + C sigma is
+  // symmetric, so each stage's transposed fixed point is the step's own
+  // iteration with a dual right-hand side. The sweep holds every node's
+  // memory on the grid (the lateral range widened to every node for its
+  // duration), so that the log-viscosity gradient is formed at every node.
+  Dev<double> nodeVolume, colWeight;  // rho_p r_p^2 per memory node; w_theta 2 pi / nphi per colatitude
+  const double2* passAddSph = nullptr;  // solutions a pass adds after its solve (the dual's K^-1 S^T g)
+  const double2* passAddTor = nullptr;
+  struct AdjointBuffers {
+    std::vector<GridTensor> m, hold;  // memory duals per branch; Sdirk2's held share
+    GridTensor d, bar;                // the strain dual; the end strain's total dual
+    Dev<double2> qSph, qTor, gU, gPhi, sigma;
+    Dev<double> grad;
+    V3dState scratch, stage;          // StartStage's output; Sdirk2's recomputed first stage
+    bool ready = false;
+  } adj;
+  int CopyState(const V3dState& from, V3dState& to);
+  int StageAdjoint(V3dState& in, const GridTensor& end, double dt, int scheme, bool measured,
+                   sl3dgpu_step_info& info);
+  int AdjointRun(const double* times, int nodes, int scheme, const double* loads, const double* uDual,
+                 const double* phiDual, double* loadKernels, double* deltaGradient, double* objective,
+                 sl3dgpu_step_info* infos);
+  int AdjointSweep(const double* times, int nodes, int scheme, const double* loads, const double* uDual,
+                   const double* phiDual, double* loadKernels, double* deltaGradient, double* objective,
+                   sl3dgpu_step_info* infos);
 
   ~Viscoelastic3DGpu() {
     for (auto& g : correctionGraphs)
@@ -645,6 +675,15 @@ int Viscoelastic3DGpu::Create(const sl3dgpu_layer* layers, int nlayers, const sl
     }
   }
 
+  {
+    std::vector<double> volume(P), colw(grid->ntheta);
+    for (int p = 0; p < P; ++p)
+      volume[p] = elemJac[nodeElement[p]] * pts.weight[nodeQ[p]] * nodeR[p] * nodeR[p];
+    for (int j = 0; j < grid->ntheta; ++j) colw[j] = grid->weights[j] * 2.0 * 3.14159265358979323846 / grid->nphi;
+    SL3D_CUDA(nodeVolume.Upload(volume));
+    SL3D_CUDA(colWeight.Upload(colw));
+  }
+
   // Branch moduli and reference inverse times at the nodes; exp(-delta) = 1.
   std::vector<double> mu(static_cast<size_t>(K) * P), itau(static_cast<size_t>(K) * P);
   for (int k = 0; k < K; ++k)
@@ -997,6 +1036,16 @@ int Viscoelastic3DGpu::Pass(const Flavour& f, const double2* strain, bool useSta
   if (sigma != nullptr || tide != nullptr) {
     LaunchAddLoad(geo, sigma, f.units.p, f.unitOffset.p, rhsSph.p, stream, tide, f.tideUnits.p);
     SL3D_CHECK_LAUNCH();
+  }
+  if (passAddSph != nullptr) {
+    LaunchAxpy(2 * rhsSphComplex, 1.0, reinterpret_cast<const double*>(passAddSph),
+               reinterpret_cast<double*>(rhsSph.p), stream);
+    SL3D_CHECK_LAUNCH();
+    if (rhsTorComplex > 0) {
+      LaunchAxpy(2 * rhsTorComplex, 1.0, reinterpret_cast<const double*>(passAddTor),
+                 reinterpret_cast<double*>(rhsTor.p), stream);
+      SL3D_CHECK_LAUNCH();
+    }
   }
   LaunchStrain(geo, rhsSph.p, rhsTor.p, next, stream);
   SL3D_CHECK_LAUNCH();
@@ -3029,6 +3078,343 @@ int Viscoelastic3DGpu::StrainReference(const V3dState& st, double* out) {
   return SL3DGPU_OK;
 }
 
+// -- the discrete adjoint -------------------------------------------------------------------------------
+
+int Viscoelastic3DGpu::CopyState(const V3dState& from, V3dState& to) {
+  for (int k = 0; k < K; ++k) {
+    SL3D_CUDA(cudaMemcpyAsync(to.m[k].c0.p, from.m[k].c0.p, values * sizeof(double2), cudaMemcpyDeviceToDevice,
+                              stream));
+    SL3D_CUDA(cudaMemcpyAsync(to.m[k].c1.p, from.m[k].c1.p, values * sizeof(double2), cudaMemcpyDeviceToDevice,
+                              stream));
+    SL3D_CUDA(cudaMemcpyAsync(to.m[k].r.p, from.m[k].r.p, values * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(to.mSpec[k].p, from.mSpec[k].p, spectralComplex * sizeof(double2),
+                              cudaMemcpyDeviceToDevice, stream));
+  }
+  SL3D_CUDA(cudaMemcpyAsync(to.strain.c0.p, from.strain.c0.p, values * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  SL3D_CUDA(cudaMemcpyAsync(to.strain.c1.p, from.strain.c1.p, values * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  SL3D_CUDA(cudaMemcpyAsync(to.strain.r.p, from.strain.r.p, values * sizeof(double), cudaMemcpyDeviceToDevice,
+                            stream));
+  SL3D_CUDA(cudaMemcpyAsync(to.coeffs.p, from.coeffs.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  to.hasStrain = from.hasStrain;
+  to.hasCoeffs = from.hasCoeffs;
+  to.hasPrev = false;
+  to.latFirst = from.latFirst;
+  to.latEnd = from.latEnd;
+  return SL3DGPU_OK;
+}
+
+// One stage transposed. Forward (StartStage, the converged fixed point,
+// FinishStage): m~_k = e_k m_k + alpha_k d_start; phi = An(sum_k mu_k m~_k);
+// (K - F An W Syn Str) x = F phi + K u sigma; d_end = Syn Str x; m'_k = m~_k +
+// beta_k d_end; the surface reads S x. Given the duals of m'_k and d_end (the
+// sweep's buffers) and of the surface reads (measured), the system's
+// symmetry makes its dual solve z = (K - F An W Syn Str)^-1 (F An d-bar +
+// S^T g), d-bar = dD + sum_k beta_k mD_k, the step's own iteration from a
+// zero strain with fixed force An(d-bar) and K^-1 S^T g added after every
+// solve; then zeta = Syn Str z gives the memory duals M_k = mD_k + mu_k zeta,
+// the start's duals e_k M_k and sum_k alpha_k M_k, the load's dual u^T K z
+// = u^T (F An(d-bar + W zeta) + S^T g) and the gradient in delta through
+// e, alpha, beta (W's share folded into M). The stage's weights are
+// StartStage's own, recomputed from the start state.
+int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const GridTensor& end, double dt, int scheme, bool measured,
+                                    sl3dgpu_step_info& info) {
+  Flavour* f = nullptr;
+  SL3D_TRY(StartStage(in, adj.scratch, dt, scheme, nullptr, &f));
+  AdjointStrainArgs sa{};
+  sa.values = values;
+  sa.branches = K;
+  for (int k = 0; k < K; ++k) {
+    sa.beta[k] = beta[k].p;
+    sa.m0[k] = adj.m[k].c0.p;
+    sa.m1[k] = adj.m[k].c1.p;
+    sa.mr[k] = adj.m[k].r.p;
+  }
+  sa.d0 = adj.d.c0.p;
+  sa.d1 = adj.d.c1.p;
+  sa.dr = adj.d.r.p;
+  sa.o0 = adj.bar.c0.p;
+  sa.o1 = adj.bar.c1.p;
+  sa.orr = adj.bar.r.p;
+  LaunchAdjointStrainDual(sa, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(AnalyseRange(adj.bar, fixedS.p, 0, P));
+  SL3D_CUDA(cudaMemcpyAsync(analysedStart.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  const double2* gU = measured ? adj.gU.p : nullptr;
+  const double2* gPhi = measured ? adj.gPhi.p : nullptr;
+  if (measured) {
+    SL3D_CUDA(cudaMemsetAsync(rhsSph.p, 0, rhsSphComplex * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(rhsTor.p, 0, std::max<long long>(rhsTorComplex, 1) * sizeof(double2), stream));
+    LaunchSurfaceDual(geo, gU, gPhi, rhsSph.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(SolveColumns(*f, rhsSph.p, rhsTor.p));
+    SL3D_CUDA(cudaMemcpyAsync(adj.qSph.p, rhsSph.p, rhsSphComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                              stream));
+    if (rhsTorComplex > 0)
+      SL3D_CUDA(cudaMemcpyAsync(adj.qTor.p, rhsTor.p, rhsTorComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                stream));
+    passAddSph = adj.qSph.p;
+    passAddTor = adj.qTor.p;
+  }
+  SL3D_CUDA(cudaMemsetAsync(s.p, 0, spectralComplex * sizeof(double2), stream));
+  stageGuess = nullptr;
+  info = sl3dgpu_step_info{};
+  int rc = SL3DGPU_OK;
+  if (options.precision == 1) {
+    LaunchCast(values, weight.p, weight32.p, stream);
+    SL3D_CHECK_LAUNCH();
+    rc = ConvergeMixed(*f, nullptr, info);
+  } else {
+    rc = Converge(*f, nullptr, info);
+  }
+  passAddSph = passAddTor = nullptr;
+  SL3D_TRY(rc);
+  if (grid->emulateFp64) SL3D_TRY(grid->TensorCoreStatus(stream));
+  if (!info.converged) {
+    SetError("v3d adjoint: a stage's transposed fixed point did not converge");
+    return SL3DGPU_ERR_UNCONVERGED;
+  }
+  // zeta = Syn Str z, the converged iterate's synthesis
+  SL3D_TRY(SynthesiseRange(s.p, dGrid, 0, P));
+  // the load's dual: u^T (F An(d-bar + W zeta) + S^T g)
+  SL3D_CUDA(cudaMemcpyAsync(analysed.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  SL3D_TRY(AnalyseWeighted(dGrid, weight.p, analysed.p));
+  SL3D_CUDA(cudaMemsetAsync(rhsSph.p, 0, rhsSphComplex * sizeof(double2), stream));
+  SL3D_CUDA(cudaMemsetAsync(rhsTor.p, 0, std::max<long long>(rhsTorComplex, 1) * sizeof(double2), stream));
+  LaunchForces(geo, analysed.p, rhsSph.p, rhsTor.p, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchSurfaceDual(geo, gU, gPhi, rhsSph.p, stream);
+  SL3D_CHECK_LAUNCH();
+  LaunchLoadDual(geo, f->units.p, f->unitOffset.p, rhsSph.p, adj.sigma.p, stream);
+  SL3D_CHECK_LAUNCH();
+  // the start's memory and strain duals, the gradient
+  AdjointMemoryArgs ma{};
+  ma.values = values;
+  ma.fieldSize = fieldSize;
+  ma.nphi = grid->nphi;
+  ma.branches = K;
+  ma.scheme = scheme == static_cast<int>(Scheme::BackwardEuler) ? 1 : 0;
+  ma.dt = dt;
+  ma.muBranch = muBranch.p;
+  ma.itauRef = itauRef.p;
+  ma.factor = factor.p;
+  ma.nodeVolume = nodeVolume.p;
+  ma.colWeight = colWeight.p;
+  for (int k = 0; k < K; ++k) {
+    ma.m0[k] = adj.m[k].c0.p;
+    ma.m1[k] = adj.m[k].c1.p;
+    ma.mr[k] = adj.m[k].r.p;
+    ma.s0[k] = in.m[k].c0.p;
+    ma.s1[k] = in.m[k].c1.p;
+    ma.sr[k] = in.m[k].r.p;
+  }
+  ma.d0 = adj.d.c0.p;
+  ma.d1 = adj.d.c1.p;
+  ma.dr = adj.d.r.p;
+  ma.z0 = dGrid.c0.p;
+  ma.z1 = dGrid.c1.p;
+  ma.zr = dGrid.r.p;
+  ma.a0 = in.strain.c0.p;
+  ma.a1 = in.strain.c1.p;
+  ma.ar = in.strain.r.p;
+  ma.b0 = end.c0.p;
+  ma.b1 = end.c1.p;
+  ma.br = end.r.p;
+  ma.grad = adj.grad.p;
+  LaunchAdjointMemory(ma, stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, const double* loads,
+                                  const double* uDual, const double* phiDual, double* loadKernels,
+                                  double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
+  if (staticMode || ocean.on || options.solver != 0) {
+    SetError("v3d adjoint: built for the fixed-point step (solver 0, FP64 or mixed) without an ocean");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (nodes < 1 || times == nullptr || loads == nullptr || loadKernels == nullptr || scheme < 0 || scheme > 2) {
+    SetError("v3d adjoint: at least one node, times, loads, the load kernels' buffer and a scheme of 0, 1 or 2");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (int k = 1; k < nodes; ++k)
+    if (!(times[k] >= times[k - 1])) {
+      SetError("v3d: node times must not decrease");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+  // every node on the grid for the sweep; the operator's own range back after
+  const int first = lateralFirst, end = lateralEnd;
+  lateralFirst = 0;
+  lateralEnd = P;
+  const int rc = AdjointSweep(times, nodes, scheme, loads, uDual, phiDual, loadKernels, deltaGradient, objective,
+                              infos);
+  passAddSph = passAddTor = nullptr;
+  lateralFirst = first;
+  lateralEnd = end;
+  return rc;
+}
+
+int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, const double* loads,
+                                    const double* uDual, const double* phiDual, double* loadKernels,
+                                    double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  if (!adj.ready) {
+    adj.m.resize(K);
+    adj.hold.resize(K);
+    for (int k = 0; k < K; ++k) {
+      SL3D_CUDA(adj.m[k].Alloc(values));
+      SL3D_CUDA(adj.hold[k].Alloc(values));
+    }
+    SL3D_CUDA(adj.d.Alloc(values));
+    SL3D_CUDA(adj.bar.Alloc(values));
+    SL3D_CUDA(adj.qSph.Alloc(rhsSphComplex));
+    SL3D_CUDA(adj.qTor.Alloc(std::max<long long>(rhsTorComplex, 1)));
+    SL3D_CUDA(adj.gU.Alloc(lm));
+    SL3D_CUDA(adj.gPhi.Alloc(lm));
+    SL3D_CUDA(adj.sigma.Alloc(lm));
+    SL3D_CUDA(adj.grad.Alloc(values));
+    SL3D_TRY(AllocState(adj.scratch));
+    SL3D_TRY(AllocState(adj.stage));
+    adj.ready = true;
+  }
+  auto zeroTensor = [&](GridTensor& t) -> int {
+    SL3D_CUDA(cudaMemsetAsync(t.c0.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(t.c1.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(t.r.p, 0, values * sizeof(double), stream));
+    return SL3DGPU_OK;
+  };
+  // the surface pairing of two coefficient arrays (l, m >= 0), m > 0 twice
+  auto pair = [&](const double* a, const double* b) {
+    double sum = 0.0;
+    for (int l = 0; l <= options.lmax; ++l)
+      for (int m = 0; m <= l; ++m) {
+        const size_t i = static_cast<size_t>(l) * (l + 1) / 2 + m;
+        sum += (m == 0 ? 1.0 : 2.0) * (a[2 * i] * b[2 * i] + a[2 * i + 1] * b[2 * i + 1]);
+      }
+    return sum;
+  };
+
+  // The forward run, every node's state kept (Evolution3D::Run: node 0 the
+  // instantaneous response, each later node one step under its two loads).
+  std::vector<V3dState> trajectory(nodes);
+  V3dState cur, zero;
+  SL3D_TRY(ZeroState(cur));
+  SL3D_TRY(ZeroState(zero));
+  SL3D_TRY(zeroTensor(zero.strain));
+  std::vector<double> surface(2 * lm);
+  double objectiveSum = 0.0;
+  for (int k = 0; k < nodes; ++k) {
+    const double* l1 = loads + 2 * lm * k;
+    const double* l0 = k > 0 ? loads + 2 * lm * (k - 1) : l1;
+    const double dt = k > 0 ? times[k] - times[k - 1] : 0.0;
+    sl3dgpu_step_info info{};
+    SL3D_TRY(Step(cur, dt, scheme, l0, l1, &info));
+    if (infos) infos[k] = info;
+    if (!info.converged) {
+      SetError("v3d adjoint: a step of the forward run did not converge");
+      return SL3DGPU_ERR_UNCONVERGED;
+    }
+    if (uDual) {
+      SL3D_TRY(Surface(0, surface.data()));
+      objectiveSum += pair(uDual + 2 * lm * k, surface.data());
+    }
+    if (phiDual) {
+      SL3D_TRY(Surface(2, surface.data()));
+      objectiveSum += pair(phiDual + 2 * lm * k, surface.data());
+    }
+    SL3D_TRY(AllocState(trajectory[k]));
+    SL3D_TRY(CopyState(cur, trajectory[k]));
+  }
+  if (objective) *objective = objectiveSum;
+
+  // The transposed sweep, node by node from the last.
+  for (int k = 0; k < K; ++k) SL3D_TRY(zeroTensor(adj.m[k]));
+  SL3D_TRY(zeroTensor(adj.d));
+  SL3D_CUDA(cudaMemsetAsync(adj.grad.p, 0, values * sizeof(double), stream));
+  std::vector<double> kernels(2 * lm * nodes, 0.0), sigma(2 * lm);
+  auto addSigma = [&](int node, double c) -> int {
+    SL3D_CUDA(cudaMemcpyAsync(sigma.data(), adj.sigma.p, lm * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    SL3D_CUDA(cudaStreamSynchronize(stream));
+    for (size_t i = 0; i < 2 * lm; ++i) kernels[2 * lm * node + i] += c * sigma[i];
+    return SL3DGPU_OK;
+  };
+  const bool measured = uDual != nullptr || phiDual != nullptr;
+  for (int n = nodes - 1; n >= 0; --n) {
+    V3dState& prev = n > 0 ? trajectory[n - 1] : zero;
+    const double dt = n > 0 ? times[n] - times[n - 1] : 0.0;
+    if (uDual)
+      SL3D_CUDA(cudaMemcpyAsync(adj.gU.p, uDual + 2 * lm * n, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    if (phiDual)
+      SL3D_CUDA(cudaMemcpyAsync(adj.gPhi.p, phiDual + 2 * lm * n, lm * sizeof(double2), cudaMemcpyHostToDevice,
+                                stream));
+    if (uDual == nullptr) SL3D_CUDA(cudaMemsetAsync(adj.gU.p, 0, lm * sizeof(double2), stream));
+    if (phiDual == nullptr) SL3D_CUDA(cudaMemsetAsync(adj.gPhi.p, 0, lm * sizeof(double2), stream));
+    sl3dgpu_step_info info{};
+    if (scheme != 2 || dt == 0.0) {
+      SL3D_TRY(StageAdjoint(prev, trajectory[n].strain, dt, scheme == 2 ? 1 : scheme, measured, info));
+      SL3D_TRY(addSigma(n, 1.0));
+      continue;
+    }
+    // Sdirk2: the first stage again from the node below, under the blend
+    // (1 - gamma) L_{n-1} + gamma L_n; the second stage's memory
+    // M2 = (1 - r) m_{n-1} + r Y1 formed in its place.
+    const double gamma = host::kSdirk2Gamma, h = gamma * dt, r = (1.0 - gamma) / gamma;
+    SL3D_CUDA(cudaMemcpyAsync(sigma0.p, loads + 2 * lm * (n - 1), lm * sizeof(double2), cudaMemcpyHostToDevice,
+                              stream));
+    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, loads + 2 * lm * n, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    LaunchBlend(static_cast<long long>(lm), gamma, sigma0.p, sigma1.p, sigmaMid.p, stream);
+    SL3D_CHECK_LAUNCH();
+    stageGuess = nullptr;
+    sl3dgpu_step_info first{};
+    SL3D_TRY(StepOnce(prev, adj.stage, h, 1, sigma0.p, sigmaMid.p, first));
+    if (!first.converged) {
+      SetError("v3d adjoint: the first stage of a forward step did not converge when repeated");
+      return SL3DGPU_ERR_UNCONVERGED;
+    }
+    for (int k = 0; k < K; ++k) {
+      LaunchStageCombine(values, r, prev.m[k].c0.p, prev.m[k].c1.p, prev.m[k].r.p, adj.stage.m[k].c0.p,
+                         adj.stage.m[k].c1.p, adj.stage.m[k].r.p, stream);
+      SL3D_CHECK_LAUNCH();
+    }
+    SL3D_TRY(StageAdjoint(adj.stage, trajectory[n].strain, h, 1, measured, info));
+    SL3D_TRY(addSigma(n, 1.0));
+    // the combination transposed: (1 - r) of M2's dual held for m_{n-1}, r of it Y1's
+    for (int k = 0; k < K; ++k) {
+      for (auto [from, to, count] : {std::tuple{reinterpret_cast<double*>(adj.m[k].c0.p),
+                                                reinterpret_cast<double*>(adj.hold[k].c0.p), 2 * values},
+                                     std::tuple{reinterpret_cast<double*>(adj.m[k].c1.p),
+                                                reinterpret_cast<double*>(adj.hold[k].c1.p), 2 * values},
+                                     std::tuple{adj.m[k].r.p, adj.hold[k].r.p, values}}) {
+        SL3D_CUDA(cudaMemcpyAsync(to, from, count * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        LaunchScale(count, 1.0 - r, to, stream);
+        SL3D_CHECK_LAUNCH();
+        LaunchScale(count, r, from, stream);
+        SL3D_CHECK_LAUNCH();
+      }
+    }
+    SL3D_TRY(StageAdjoint(prev, adj.stage.strain, h, 1, false, info));
+    SL3D_TRY(addSigma(n - 1, 1.0 - gamma));
+    SL3D_TRY(addSigma(n, gamma));
+    for (int k = 0; k < K; ++k) {
+      LaunchAxpy(2 * values, 1.0, reinterpret_cast<const double*>(adj.hold[k].c0.p),
+                 reinterpret_cast<double*>(adj.m[k].c0.p), stream);
+      LaunchAxpy(2 * values, 1.0, reinterpret_cast<const double*>(adj.hold[k].c1.p),
+                 reinterpret_cast<double*>(adj.m[k].c1.p), stream);
+      LaunchAxpy(values, 1.0, adj.hold[k].r.p, adj.m[k].r.p, stream);
+      SL3D_CHECK_LAUNCH();
+    }
+  }
+  std::copy(kernels.begin(), kernels.end(), loadKernels);
+  if (deltaGradient)
+    SL3D_CUDA(cudaMemcpyAsync(deltaGradient, adj.grad.p, values * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  SL3D_CUDA(cudaStreamSynchronize(stream));
+  return SL3DGPU_OK;
+}
+
 }  // namespace sl3dgpu
 
 // -- the C ABI -------------------------------------------------------------------------------------------
@@ -3536,6 +3922,34 @@ extern "C" int sl3dgpu_v3d_run(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const d
     return SL3DGPU_ERR_ARGUMENT;
   }
   return h->op.Run(state->st, times, nodes, scheme, loads, u, phi, infos);
+}
+
+extern "C" int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* h, const double* times, int nodes, int scheme,
+                                       const double* loads, const double* u_dual, const double* phi_dual,
+                                       double* load_kernels, double* delta_gradient, double* objective,
+                                       sl3dgpu_step_info* infos) {
+  if (h == nullptr) {
+    SetError("v3d adjoint: null operator");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.AdjointRun(times, nodes, scheme, loads, u_dual, phi_dual, load_kernels, delta_gradient, objective,
+                          infos);
+}
+
+extern "C" int sl3dgpu_v3d_sample_volumes(const sl3dgpu_v3d* h, double* out) {
+  if (h == nullptr || out == nullptr || h->op.staticMode) {
+    SetError("v3d: null argument");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  const auto& op = h->op;
+  std::vector<double> volume(op.P), colw(op.grid->ntheta);
+  SL3D_CUDA(cudaMemcpy(volume.data(), op.nodeVolume.p, op.P * sizeof(double), cudaMemcpyDeviceToHost));
+  SL3D_CUDA(cudaMemcpy(colw.data(), op.colWeight.p, colw.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int p = 0; p < op.P; ++p)
+    for (int j = 0; j < op.grid->ntheta; ++j)
+      for (int i = 0; i < op.grid->nphi; ++i)
+        out[(static_cast<long long>(p) * op.grid->ntheta + j) * op.grid->nphi + i] = volume[p] * colw[j];
+  return SL3DGPU_OK;
 }
 
 // Independent runs driven by a pool of host threads, one run at a time per

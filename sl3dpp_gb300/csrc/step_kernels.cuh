@@ -288,4 +288,72 @@ void LaunchGramResetIf(CorrectionControl* c, double* gram, int memory, cudaStrea
 // The mixer's count and slot moved on after an update.
 void LaunchMixerAdvanceIf(CorrectionControl* c, cudaStream_t stream);
 
+// -- the discrete adjoint of the step (adjoint_kernels.cu) ---------------------------------------
+//
+// Duals are carried in the pairings under which the force assembly of an
+// analysed tensor is the transpose of the strain synthesis of a solution:
+// grid tensors in the energy pairing sum_p rho_p r_p^2 sum_x w_x [4 Re(a0 b0*)
+// + 8 Re(a1 b1*) + 12 ar br] (rho_p the radial quadrature weight jac w_q of
+// memory node p, w_x the colatitude weight times 2 pi / nphi, spins -2, -1, 0),
+// solution columns in sum w_m Re(a b*) with w_m = 1 at m = 0 and 2 above,
+// surface coefficients likewise (the L2 pairing of real fields on the unit
+// sphere).
+
+// sol[surface U dof] += u_lm and sol[surface phi dof] += phi_lm (S^T of the
+// surface reads); either array may be null.
+void LaunchSurfaceDual(const Geometry& g, const double2* u, const double2* phi, double2* solSph,
+                       cudaStream_t stream);
+// out_lm = sum over the spheroidal dofs of units_l[dof] rhs[dof][m] (the
+// transpose of the load channel x += sigma_lm units_l).
+void LaunchLoadDual(const Geometry& g, const double* units, const long long* unitOffset, const double2* rhsSph,
+                    double2* out, cudaStream_t stream);
+// out = dD + sum_k beta_k mD_k over a grid tensor (the end strain's dual:
+// its own and the memory advance's).
+struct AdjointStrainArgs {
+  long long values;
+  int branches;
+  const double* beta[2];
+  const double2* m0[2];
+  const double2* m1[2];
+  const double* mr[2];
+  const double2 *d0, *d1;
+  const double* dr;
+  double2 *o0, *o1;
+  double* orr;
+};
+void LaunchAdjointStrainDual(const AdjointStrainArgs& a, cudaStream_t stream);
+// Per grid value, the stage's memory duals and the log-viscosity gradient:
+// M_k = mD_k + mu_k zeta; mD_k = e_k M_k (the start memory's dual); dD =
+// sum_k alpha_k M_k (the start strain's dual); grad += rho r^2 w_x sum_k
+// -h_k [e_k' <M_k, m_k> + alpha_k' <M_k, d_start> + beta_k' <M_k, d_end>]
+// (h_k = dt itau_ref exp(-delta), primes d/dh, <,> the energy metric).
+struct AdjointMemoryArgs {
+  long long values, fieldSize;
+  int nphi, branches, scheme;
+  double dt;
+  const double* muBranch;   // [k][P]
+  const double* itauRef;    // [k][P]
+  const double* factor;     // exp(-delta) per grid value
+  const double* nodeVolume; // rho_p r_p^2 per memory node
+  const double* colWeight;  // w_theta 2 pi / nphi per colatitude
+  double2* m0[2];           // memory duals per branch, updated in place
+  double2* m1[2];
+  double* mr[2];
+  double2 *d0, *d1;         // the strain dual, overwritten
+  double* dr;
+  const double2 *z0, *z1;   // zeta: the strain synthesis of the stage's dual solution
+  const double* zr;
+  const double2* s0[2];     // the stage's start memory per branch
+  const double2* s1[2];
+  const double* sr[2];
+  const double2 *a0, *a1;   // the start strain
+  const double* ar;
+  const double2 *b0, *b1;   // the end strain
+  const double* br;
+  double* grad;             // dJ / d delta per grid value, accumulated
+};
+void LaunchAdjointMemory(const AdjointMemoryArgs& a, cudaStream_t stream);
+// y *= a (n reals).
+void LaunchScale(long long n, double a, double* y, cudaStream_t stream);
+
 }  // namespace sl3dgpu

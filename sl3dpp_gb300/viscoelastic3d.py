@@ -113,6 +113,8 @@ def _signatures():
         "sl3dgpu_v3d_start_taken": (i, [v]),
         "sl3dgpu_v3d_state_coefficients": (i, [v, v, ctypes.POINTER(c_void_p), ctypes.POINTER(ctypes.c_longlong)]),
         "sl3dgpu_v3d_run": (i, [v, v, P_double, i, i, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_adjoint_run": (i, [v, P_double, i, i, v, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_sample_volumes": (i, [v, v]),
         "sl3dgpu_v3d_run_many": (i, [i, v, v, v, v, i, v, v, v, v, i, v]),
         "sl3dgpu_v3d_state_coefficients_host": (i, [v, v, v]),
         "sl3dgpu_v3d_assembled_band": (i, [v, i, d, i, i, P_double, ctypes.c_longlong, P_int, P_int]),
@@ -312,6 +314,13 @@ class Viscoelastic3D:
         out = np.zeros(max(n, 0))
         if n > 0:
             lib().sl3dgpu_v3d_correction_history(self._h, out.ctypes.data_as(P_double), n)
+        return out
+
+    def sample_volumes(self) -> np.ndarray:
+        """The volume each grid sample stands for (jac w_q r^2 of its memory
+        node times 2 pi w_theta / nphi of its colatitude), node-major."""
+        out = np.zeros(self.values)
+        check(lib().sl3dgpu_v3d_sample_volumes(self._h, out.ctypes.data))
         return out
 
     def Surface(self, component="U") -> np.ndarray:
@@ -620,6 +629,39 @@ class Evolution3D:
         check(lib().sl3dgpu_v3d_run(self.op._h, state._h, times.ctypes.data_as(P_double), n, self.scheme,
                                     loads.ctypes.data, U.ctypes.data, phi.ctypes.data, infos))
         return {"U": U, "phi": phi, "infos": [infos[k] for k in range(n)], "state": state}
+
+    def Adjoint(self, times, loads, u_dual=None, phi_dual=None, gradient=True):
+        """The discrete adjoint of Run from a zero state (AdjointSolver3D::
+        FirstOrderKernels under AdjointMethod::Discrete, include/sl3dpp/
+        Adjoint3D.hpp:241-322): for J = sum_n <u_dual_n, U_n> +
+        <phi_dual_n, phi_n> (the surface pairing of real fields, m > 0 twice),
+        the load kernels per node (dJ = sum_n <kernel_n, dL_n>), dJ/d delta at
+        every grid sample (node-major, as set_delta's samples) and J itself."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        loads = np.ascontiguousarray(loads, dtype=np.complex128)
+        n = times.size
+        lm = (self.op.lmax + 1) * (self.op.lmax + 2) // 2
+        if loads.shape != (n, lm):
+            raise ValueError("one load (l(l+1)/2 + m coefficients) per node")
+        duals = []
+        for g in (u_dual, phi_dual):
+            if g is None:
+                duals.append(None)
+                continue
+            g = np.ascontiguousarray(g, dtype=np.complex128)
+            if g.shape != (n, lm):
+                raise ValueError("one dual (l(l+1)/2 + m coefficients) per node")
+            duals.append(g)
+        kernels = np.zeros((n, lm), dtype=np.complex128)
+        grad = np.zeros(self.op.values) if gradient else None
+        objective = ctypes.c_double()
+        infos = (StepInfo * max(n, 1))()
+        check(lib().sl3dgpu_v3d_adjoint_run(
+            self.op._h, times.ctypes.data_as(P_double), n, self.scheme, loads.ctypes.data,
+            None if duals[0] is None else duals[0].ctypes.data, None if duals[1] is None else duals[1].ctypes.data,
+            kernels.ctypes.data, None if grad is None else grad.ctypes.data, ctypes.byref(objective), infos))
+        return {"objective": objective.value, "load_kernels": kernels, "delta_gradient": grad,
+                "infos": [infos[k] for k in range(n)]}
 
     def Instantaneous(self, load):
         out = self.Run(np.zeros(1), np.asarray(load)[None, :])

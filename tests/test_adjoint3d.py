@@ -1,0 +1,132 @@
+"""The discrete adjoint of the 3D run without an ocean (AdjointSolver3D::
+FirstOrderKernels under AdjointMethod::Discrete, include/sl3dpp/
+Adjoint3D.hpp:241-322, src/AdjointDiscrete3D.cpp), checked as the
+reference's own gates check it (tests/TestDiscreteAdjoint3D.cpp): the
+pairing identity and the gradient against differences of the forward run.
+
+With delta fixed the run is linear in its loads, so the load kernels must
+pair with any loads to the objective of the forward run under them:
+sum_n <kernel_n, L_n> = J(L) = sum_n <g_n, U_n(L)> + <h_n, phi_n(L)> -- against
+the library's forward run and against the oracle's march of the same nodes
+(1e-8: both runs and the transposed solves converge to rtol 1e-11). The
+log-viscosity gradient must give the derivative of J along a direction p
+over every node (the sweep forms it at nodes outside delta's range too):
+Richardson-extrapolated central differences of the forward run, 1e-6. Each
+for the three schemes, and the mixed form for Sdirk2."""
+
+import numpy as np
+import pytest
+
+from sl3dpp_gb300 import configs
+from tests import _oracle as O
+from tests.test_step import _pair, cap_load, rel
+
+
+def real_coefficients(lmax, rng, count):
+    """Random coefficients (l, m >= 0) of real fields: m = 0 parts real."""
+    lm = (lmax + 1) * (lmax + 2) // 2
+    c = rng.standard_normal((count, lm)) + 1j * rng.standard_normal((count, lm))
+    for l in range(lmax + 1):
+        c[:, l * (l + 1) // 2] = c[:, l * (l + 1) // 2].real
+    return c
+
+
+def pairing(lmax, a, b):
+    """sum over (l, m >= 0) of w_m Re(a conj b), w_m = 1 at m = 0 and 2 above."""
+    w = np.concatenate([[1.0] + [2.0] * l for l in range(lmax + 1)])
+    return float(np.sum(w * (a * np.conj(b)).real))
+
+
+def _run(lmax, scheme, nodes, precision=0, seed=3):
+    o, g = _pair(lmax, 20, 5, rms=0.8, rtol=1e-11, max_iterations=120, precision=precision)
+    rng = np.random.default_rng(seed)
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    times = dt * np.arange(nodes)
+    full = cap_load(lmax, o.sigma_scale, 2000.0)
+    loads = np.stack([full * (k + 1) / nodes for k in range(nodes)]) + 0.05 * np.max(np.abs(full)) * \
+        real_coefficients(lmax, rng, nodes)
+    gU = real_coefficients(lmax, rng, nodes)
+    gPhi = real_coefficients(lmax, rng, nodes)
+    return o, g, times, loads, gU, gPhi
+
+
+def _objective(lmax, out, gU, gPhi):
+    return sum(pairing(lmax, gU[k], out["U"][k]) + pairing(lmax, gPhi[k], out["phi"][k])
+               for k in range(len(gU)))
+
+
+CASES = [(2, 0), (0, 0), (1, 0), (2, 1)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme,precision", CASES)
+def test_gpu_load_kernels_pair_with_the_forward_run(gpu, scheme, precision):
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D
+
+    lmax, nodes = 8, 4
+    o, g, times, loads, gU, gPhi = _run(lmax, scheme, nodes, precision)
+    adj = Evolution3D(g, scheme).Adjoint(times, loads, gU, gPhi, gradient=False)
+    assert all(i.converged for i in adj["infos"])
+    paired = sum(pairing(lmax, adj["load_kernels"][k], loads[k]) for k in range(nodes))
+    forward = Evolution3D(g, scheme).Run(times, loads)
+    J = _objective(lmax, forward, gU, gPhi)
+    assert abs(adj["objective"] - J) < 1e-10 * abs(J)
+    assert abs(paired - J) < 1e-8 * abs(J), (paired, J)
+    # the oracle's march of the same nodes
+    U, phi = [], []
+    for k in range(nodes):
+        step_dt = 0.0 if k == 0 else times[k] - times[k - 1]
+        assert o.step(step_dt, scheme, loads[max(k - 1, 0)], loads[k]).converged
+        U.append(o.surface(0))
+        phi.append(o.surface(2))
+    Jo = _objective(lmax, {"U": U, "phi": phi}, gU, gPhi)
+    assert abs(paired - Jo) < 1e-8 * abs(Jo), (paired, Jo)
+    # one node's kernel alone: the response at the last node to a load at node 1
+    one = np.zeros_like(loads)
+    one[1] = loads[1]
+    single = Evolution3D(g, scheme).Run(times, one)
+    assert abs(pairing(lmax, adj["load_kernels"][1], loads[1]) - _objective(lmax, single, gU, gPhi)) < \
+        1e-8 * abs(J)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme,precision", CASES)
+def test_gpu_delta_gradient_matches_differences_of_the_run(gpu, scheme, precision):
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D
+
+    lmax, nodes = 8, 4
+    o, g, times, loads, gU, gPhi = _run(lmax, scheme, nodes, precision, seed=5)
+    delta = np.asarray(_delta(o, lmax))
+    adj = Evolution3D(g, scheme).Adjoint(times, loads, gU, gPhi)
+    grad = adj["delta_gradient"]
+    assert grad.shape == (g.values,)
+    # a smooth direction over every node, delta's range and beyond
+    rng = np.random.default_rng(17)
+    pattern = O.synthesise_real(lmax, o.theta, o.nphi, real_coefficients(lmax, rng, 1)[0] / (lmax + 1))
+    radial = 1.0 + 0.5 * np.sin(7.0 * np.asarray(o.radius))
+    p = (radial[:, None] * np.asarray(pattern).ravel()[None, :]).ravel()
+    predicted = float(grad @ p)
+
+    def J(h):
+        g.set_delta(delta + h * p)
+        return _objective(lmax, Evolution3D(g, scheme).Run(times, loads), gU, gPhi)
+
+    h = 1e-2
+    d1 = (J(h) - J(-h)) / (2 * h)
+    d2 = (J(h / 2) - J(-h / 2)) / h
+    richardson = (4 * d2 - d1) / 3
+    g.set_delta(delta)
+    assert abs(predicted - richardson) < 1e-6 * abs(richardson), (predicted, richardson, d1, d2)
+    # nodes outside delta's range carry gradient too
+    outside = np.ones(g.node_count, dtype=bool)
+    per_node = delta.reshape(g.node_count, -1)
+    outside[np.any(per_node != 0.0, axis=1)] = False
+    assert outside.any()
+    assert np.max(np.abs(grad.reshape(g.node_count, -1)[outside])) > 0.0
+
+
+def _delta(o, lmax):
+    from tests.test_step import delta_for
+
+    return delta_for(o, lmax, 4, 0.8, 11)
+
