@@ -621,6 +621,131 @@ def ocean_case(args, device):
             **fp64, "mixed": mixed}
 
 
+# -- the discrete adjoint ---------------------------------------------------------------------------
+
+def adjoint_case(args, device):
+    """The discrete 3D adjoint of the run without an ocean on the GPU, two
+    workloads: config 1's (lmax 32, 40 elements of order 4, Maxwell, delta to
+    degree 8 at RMS 0.5, FP64) and config 2's Earth without its ocean (lmax
+    128, 80 elements of order 5, Burgers, delta to degree 32 at RMS 1.0, the
+    mixed form); both under config 1's cap ramping to 2 km over 10 Sdirk2
+    steps of 500 yr (11 nodes), rtol 1e-10, the objective a seeded pattern of
+    U and one of phi read at every node with a weight growing in time. Per
+    workload: the forward run's seconds (Evolution3D::Run), the adjoint
+    call's (its own recorded forward run and the transposed sweep), the same
+    with the record stride 3 and its largest relative gap from the first, the
+    pairing identity's relative gap (the load kernels against the
+    objective), and the log-viscosity gradient against Richardson-
+    extrapolated central differences of the forward run along a seeded
+    smooth direction over every node."""
+    import torch
+
+    from sl3dpp_gb300 import configs
+    from sl3dpp_gb300.grid import SurfaceGrid
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D, Options, Viscoelastic3D, standard_earth
+
+    def pairing(lmax, a, b):
+        w = np.concatenate([[1.0] + [2.0] * l for l in range(lmax + 1)])
+        return float(np.sum(w * (a * np.conj(b)).real))
+
+    def real_coefficients(lmax, rng, count):
+        lm = (lmax + 1) * (lmax + 2) // 2
+        c = rng.standard_normal((count, lm)) + 1j * rng.standard_normal((count, lm))
+        for l in range(lmax + 1):
+            c[:, l * (l + 1) // 2] = c[:, l * (l + 1) // 2].real
+        return c
+
+    def workload(name, lmax, elements, ngll, kelvin, ldelta, rms, mixed):
+        kw = dict(rtol=1e-10, max_iterations=120)
+        if mixed:
+            kw.update(precision=1, correction_rtol=CORRECTION_RTOL, correction_memory=CORRECTION_MEMORY,
+                      fp64_emulation=1)
+        op = Viscoelastic3D(standard_earth(elements, kelvin, 10.0), Options.defaults(lmax, ngll, **kw))
+        grid = SurfaceGrid(lmax, 0, 1.5)
+        pattern = grid.SynthesiseBatch(torch.tensor(configs.delta_coefficients(lmax, ldelta, rms, DELTA_SEED),
+                                                    device=device), 1)
+        ind = torch.tensor(configs.delta_indicator(op.radius), device=device)
+        delta = (ind[:, None] * pattern[None, :]).contiguous().view(-1).cpu().numpy()
+        op.set_delta(delta)
+        sle = SurfaceGrid(lmax, 0, 1.0)
+        theta, w, nphi = op.ocean_grid()
+        cap = configs.cap_field(theta, nphi, CAP_DEGREES, CAP_THICKNESS) / op.surface_density_scale
+        full = sle.ExpandBatch(torch.tensor(cap, device=device).contiguous().view(-1), 1).cpu().numpy().ravel()
+        nodes = 11
+        dt = DT_YEARS * configs.SECONDS_PER_YEAR / op.time_scale
+        times = dt * np.arange(nodes)
+        loads = np.stack([full * min(k, RAMP_STEPS) / RAMP_STEPS for k in range(nodes)])
+        loads[0] = loads[1] * 0.5
+        # one seeded pattern of U and one of phi, read at every node with a
+        # weight growing in time (a time series of one field's observations)
+        rng = np.random.default_rng(7)
+        decay = 1.0 / (1.0 + np.repeat(np.arange(lmax + 1), np.arange(lmax + 1) + 1))
+        weight = (0.5 + np.arange(nodes) / nodes)[:, None]
+        gU = weight * (real_coefficients(lmax, rng, 1) * decay)
+        gPhi = weight * (real_coefficients(lmax, rng, 1) * decay)
+        ev = Evolution3D(op, "sdirk2")
+
+        def objective(out):
+            return sum(pairing(lmax, gU[k], out["U"][k]) + pairing(lmax, gPhi[k], out["phi"][k])
+                       for k in range(nodes))
+
+        ev.Run(times, loads)  # warm: flavours built, buffers allocated
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        forward = ev.Run(times, loads)
+        torch.cuda.synchronize()
+        forward_s = time.perf_counter() - t0
+        ev.Adjoint(times[:2], loads[:2], gU[:2], gPhi[:2])  # warm: the sweep's buffers
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        adj = ev.Adjoint(times, loads, gU, gPhi)
+        torch.cuda.synchronize()
+        adjoint_s = time.perf_counter() - t0
+        J = objective(forward)
+        paired = sum(pairing(lmax, adj["load_kernels"][k], loads[k]) for k in range(nodes))
+        # the record stride 3: 4 of the 11 states kept, the gaps rebuilt
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sparse = ev.Adjoint(times, loads, gU, gPhi, stride=3)
+        torch.cuda.synchronize()
+        stride_s = time.perf_counter() - t0
+        stride_gap = max(rel_err(sparse["load_kernels"], adj["load_kernels"]),
+                         rel_err(sparse["delta_gradient"], adj["delta_gradient"]))
+        # the gradient along a smooth direction over every node
+        prng = np.random.default_rng(17)
+        coeffs = real_coefficients(lmax, prng, 1)[0]
+        coeffs *= 1.0 / (1.0 + np.repeat(np.arange(lmax + 1), np.arange(lmax + 1) + 1)) ** 2
+        field = grid.SynthesiseBatch(torch.tensor(coeffs, device=device), 1).cpu().numpy().ravel()
+        radial = 1.0 + 0.5 * np.sin(7.0 * np.asarray(op.radius))
+        p = (radial[:, None] * field[None, :]).ravel()
+        p /= np.max(np.abs(p))
+        predicted = float(adj["delta_gradient"] @ p)
+
+        def J_at(h):
+            op.set_delta(delta + h * p)
+            return objective(ev.Run(times, loads))
+
+        h = 1e-2
+        d1 = (J_at(h) - J_at(-h)) / (2 * h)
+        d2 = (J_at(h / 2) - J_at(-h / 2)) / h
+        richardson = (4 * d2 - d1) / 3
+        op.set_delta(delta)
+        return {"workload": name, "nodes": nodes, "forward_s": forward_s, "adjoint_s": adjoint_s,
+                "sweep_over_forward": (adjoint_s - forward_s) / forward_s,
+                "stride3_adjoint_s": stride_s, "stride3_rel_gap": stride_gap,
+                "forward_passes_per_step": float(np.mean([i.iterations for i in forward["infos"][1:]])),
+                "pairing_identity_rel_gap": abs(paired - J) / abs(J),
+                "gradient_vs_differences_rel_gap": abs(predicted - richardson) / abs(richardson),
+                "directional_derivative": predicted}
+
+    out = [workload("config 1: lmax 32, 40 elements of order 4, Maxwell, delta degree 8 RMS 0.5, FP64",
+                    32, 40, 5, 0.0, 8, 0.5, False),
+           workload("config 2's Earth without its ocean: lmax 128, 80 elements of order 5, Burgers, delta degree "
+                    "32 RMS 1.0, mixed form", 128, 80, 6, 0.5, 32, 1.0, True)]
+    return {"case": "discrete 3D adjoint (load kernels and log-viscosity gradient), 10 Sdirk2 steps of 500 yr",
+            "workloads": out}
+
+
 # -- config 4: the ensemble ----------------------------------------------------------------------
 
 def ensemble_case(args):
@@ -690,6 +815,8 @@ def main():
                     help="instead: the FP32 tensor-core Legendre contraction alone at the workload's lmax")
     ap.add_argument("--ocean-case", action="store_true",
                     help="instead: config 2, the coupled step under an ocean at lmax 128, 50 steps")
+    ap.add_argument("--adjoint-case", action="store_true",
+                    help="instead: the discrete 3D adjoint at config 1's and config 2's Earth (no ocean)")
     ap.add_argument("--ensemble-case", action="store_true",
                     help="instead: config 4, the seeded ensemble (autotuned schedule, concurrent and one by one)")
     ap.add_argument("--ensemble-members", type=int, default=48)
@@ -756,6 +883,10 @@ def main():
     if args.ocean_case:
         if rank == 0:
             print(json.dumps(ocean_case(args, device)), flush=True)
+        return
+    if args.adjoint_case:
+        if rank == 0:
+            print(json.dumps(adjoint_case(args, device)), flush=True)
         return
     if args.ensemble_case:
         if rank == 0:

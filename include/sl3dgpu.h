@@ -576,7 +576,11 @@ int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* tim
  * AdjointMethod::Discrete, include/sl3dpp/Adjoint3D.hpp:241-322,
  * src/AdjointDiscrete3D.cpp): the run from a zero state, every node's state
  * kept, then the exact transpose of its time-stepped map swept back node by
- * node (Sdirk2's first stage repeated from the node below). The objective
+ * node (Sdirk2's first stage repeated from the node below). stride
+ * (ForwardTrajectory3D's record stride, at least 1): the states of every
+ * stride-th node are kept, a gap's rebuilt by the run's own steps when the
+ * sweep reaches it -- about nodes / stride + stride states held, fewest near
+ * sqrt(nodes). The objective
  * J = sum_n <u_dual_n, U_n> + <phi_dual_n, phi_n>, <a, b> = sum_{l, m >= 0}
  * w_m Re(a b*) with w_m = 1 at m = 0 and 2 above (the surface integral of
  * the two real fields over the unit sphere); u_dual, phi_dual: nodes x
@@ -589,10 +593,9 @@ int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* tim
  * is the reference's logViscosityKernel3D, a density per unit volume;
  * objective (nullable): J of the forward run; infos (nullable): the forward
  * steps' infos. Without an ocean and for the fixed-point step (solver 0,
- * FP64 or mixed); the transposed solves take the operator's rtol. Every
- * node's state is held on the device for the sweep. */
-int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* op, const double* times, int nodes, int scheme, const double* loads,
-                            const double* u_dual, const double* phi_dual, double* load_kernels,
+ * FP64 or mixed); the transposed solves take the operator's rtol. */
+int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* op, const double* times, int nodes, int scheme, int stride,
+                            const double* loads, const double* u_dual, const double* phi_dual, double* load_kernels,
                             double* delta_gradient, double* objective, sl3dgpu_step_info* infos);
 /* The volume each grid sample stands for (GridCoupling's volume weight:
  * the radial quadrature weight jac w_q r^2 of its memory node times its

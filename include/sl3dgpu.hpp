@@ -660,6 +660,8 @@ class Viscoelastic3D {
 
   [[nodiscard]] int LMax() const { return lmax_; }
   [[nodiscard]] int NodeCount() const { return nodes_; }
+  // grid values over every node: delta's samples, the kernels' layout
+  [[nodiscard]] std::size_t GridValues() const { return static_cast<std::size_t>(nodes_) * ntheta_ * nphi_; }
   [[nodiscard]] const std::vector<double>& Radii() const { return radius_; }
   // SI per model unit
   [[nodiscard]] double LengthScale() const { return length_; }
@@ -1070,6 +1072,83 @@ class Evolution3D {
   Viscoelastic3D* op_;
   Scheme scheme_;
   bool migrating_ = false;
+  friend class AdjointSolver3D;
+};
+
+// -- the discrete 3D adjoint -----------------------------------------------------------------------------
+
+// What an objective reads at one node (Adjoint.hpp's Measurement): the
+// duals of the surface U and phi coefficients (l, m >= 0, either empty),
+// paired by the surface integral of real fields (m > 0 twice).
+struct Measurement3D {
+  std::vector<Complex> displacementDual, potentialDual;
+};
+// The first-order kernels (Kernels3D, include/sl3dpp/Adjoint3D.hpp:104-140):
+// per node the direct-load kernel (dJ = sum_n <kernel_n, dL_n>); dJ/d delta
+// per grid sample and its density per unit volume (logViscosityKernel3D,
+// the gradient over the samples' volumes); the objective of the forward run.
+struct Kernels3D {
+  std::vector<std::vector<Complex>> directLoadKernels;
+  std::vector<double> deltaGradient, logViscosityKernel3D;
+  double objective = 0.0;
+};
+
+// AdjointSolver3D under AdjointMethod::Discrete (include/sl3dpp/Adjoint3D.hpp:
+// 241-322, src/AdjointDiscrete3D.cpp) for the evolution without an ocean:
+// the exact transpose of the time-stepped map, swept back over a forward
+// run the solver records itself from a zero state under the loads.
+class AdjointSolver3D {
+ public:
+  struct Options {
+    int record_stride = 1;  // the forward run's states kept every stride-th node (Evolution3D::Options::record_stride)
+  };
+  explicit AdjointSolver3D(const Evolution3D& evolution) : AdjointSolver3D(evolution, Options{}) {}
+  AdjointSolver3D(const Evolution3D& evolution, Options options) : evolution_(&evolution), options_(options) {}
+
+  [[nodiscard]] Kernels3D FirstOrderKernels(std::span<const double> times, const Viscoelastic3D::LoadCallable3D& load,
+                                            const std::map<std::size_t, Measurement3D>& measurements) const {
+    Viscoelastic3D& op = *evolution_->op_;
+    const int n = static_cast<int>(times.size());
+    const std::size_t lm = evolution_->Coefficients();
+    std::vector<Complex> loads(lm * n), u(lm * n), phi(lm * n);
+    for (int k = 0; k < n; ++k) {
+      const auto flat = gpu::Flatten(load, op.LMax(), times[k]);
+      std::copy(flat.begin(), flat.end(), loads.begin() + lm * k);
+    }
+    bool anyU = false, anyPhi = false;
+    for (const auto& [node, m] : measurements) {
+      if (node >= static_cast<std::size_t>(n)) throw std::invalid_argument("a measurement past the last node");
+      for (const auto* dual : {&m.displacementDual, &m.potentialDual}) {
+        if (dual->empty()) continue;
+        if (dual->size() != lm) throw std::invalid_argument("a dual has l(l+1)/2 + m coefficients");
+        auto& into = dual == &m.displacementDual ? u : phi;
+        std::copy(dual->begin(), dual->end(), into.begin() + lm * node);
+        (dual == &m.displacementDual ? anyU : anyPhi) = true;
+      }
+    }
+    Kernels3D out;
+    std::vector<Complex> kernels(lm * n);
+    const std::size_t values = op.GridValues();
+    out.deltaGradient.resize(values);
+    gpu::Check(sl3dgpu_v3d_adjoint_run(op.Handle(), times.data(), n, static_cast<int>(evolution_->scheme_),
+                                       options_.record_stride,
+                                       reinterpret_cast<const double*>(loads.data()),
+                                       anyU ? reinterpret_cast<const double*>(u.data()) : nullptr,
+                                       anyPhi ? reinterpret_cast<const double*>(phi.data()) : nullptr,
+                                       reinterpret_cast<double*>(kernels.data()), out.deltaGradient.data(),
+                                       &out.objective, nullptr));
+    out.directLoadKernels.resize(n);
+    for (int k = 0; k < n; ++k) out.directLoadKernels[k].assign(kernels.begin() + lm * k, kernels.begin() + lm * (k + 1));
+    std::vector<double> volume(values);
+    gpu::Check(sl3dgpu_v3d_sample_volumes(op.Handle(), volume.data()));
+    out.logViscosityKernel3D.resize(values);
+    for (std::size_t x = 0; x < values; ++x) out.logViscosityKernel3D[x] = out.deltaGradient[x] / volume[x];
+    return out;
+  }
+
+ private:
+  const Evolution3D* evolution_;
+  Options options_;
 };
 
 // -- the static 3D solve ----------------------------------------------------------------------------------

@@ -59,24 +59,6 @@ __global__ void LoadDualKernel(Geometry g, const double* units, const long long*
   if (lane == 0) out[lm] = make_double2(re, im);
 }
 
-__global__ void AdjointStrainKernel(AdjointStrainArgs a) {
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < a.values; x += stride) {
-    double2 o0 = a.d0[x], o1 = a.d1[x];
-    double orr = a.dr[x];
-    for (int k = 0; k < a.branches; ++k) {
-      const double b = a.beta[k][x];
-      const double2 m0 = a.m0[k][x], m1 = a.m1[k][x];
-      o0 = make_double2(o0.x + b * m0.x, o0.y + b * m0.y);
-      o1 = make_double2(o1.x + b * m1.x, o1.y + b * m1.y);
-      orr += b * a.mr[k][x];
-    }
-    a.o0[x] = o0;
-    a.o1[x] = o1;
-    a.orr[x] = orr;
-  }
-}
-
 // The stage weights of the step kernels (ExponentialTrapezoidWeights or
 // BackwardEulerWeight) and their derivatives in h.
 __device__ inline void WeightsAndSlopes(int scheme, double h, double& e, double& alpha, double& beta, double& de,
@@ -107,6 +89,28 @@ __device__ inline void WeightsAndSlopes(int scheme, double h, double& e, double&
   de = -ex;
   dalpha = dphi1 + ex;
   dbeta = -dphi1;
+}
+
+__global__ void AdjointStrainKernel(AdjointStrainArgs a) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const int P = static_cast<int>(a.values / a.fieldSize);
+  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < a.values; x += stride) {
+    const int node = static_cast<int>(x / a.fieldSize);
+    double2 o0 = a.d0[x], o1 = a.d1[x];
+    double orr = a.dr[x];
+    for (int k = 0; k < a.branches; ++k) {
+      const double h = a.dt * (a.itauRef[static_cast<long long>(k) * P + node] * a.factor[x]);
+      double e, alpha, b, de, dalpha, dbeta;
+      WeightsAndSlopes(a.scheme, h, e, alpha, b, de, dalpha, dbeta);
+      const double2 m0 = a.m0[k][x], m1 = a.m1[k][x];
+      o0 = make_double2(o0.x + b * m0.x, o0.y + b * m0.y);
+      o1 = make_double2(o1.x + b * m1.x, o1.y + b * m1.y);
+      orr += b * a.mr[k][x];
+    }
+    a.o0[x] = o0;
+    a.o1[x] = o1;
+    a.orr[x] = orr;
+  }
 }
 
 __device__ inline double Energy(double2 a0, double2 a1, double ar, double2 b0, double2 b1, double br) {

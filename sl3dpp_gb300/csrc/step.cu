@@ -267,30 +267,39 @@ class Viscoelastic3DGpu {
 
   // The discrete adjoint of Run without an ocean (AdjointSolver3D under
   // AdjointMethod::Discrete, src/AdjointDiscrete3D.cpp): the forward run
-  // recorded at every node, then the transposed sweep node by node. With no
-  // ocean the step's system (K - F An W Syn Str) x = F phi + C sigma is
-  // symmetric, so each stage's transposed fixed point is the step's own
-  // iteration with a dual right-hand side. The sweep holds every node's
-  // memory on the grid (the lateral range widened to every node for its
-  // duration), so that the log-viscosity gradient is formed at every node.
+  // recorded (every stride-th node kept), then the transposed sweep node by
+  // node. With no ocean the step's system (K - F An W Syn Str) x = F phi +
+  // C sigma is symmetric, so each stage's transposed fixed point is the
+  // step's own iteration, over the operator's lateral range, with a dual
+  // right-hand side. The memory and strain duals are grid tensors at every
+  // node (at the nodes where W is zero they stay band-limited, the exact
+  // image of the forward's coefficient memory there), so that the
+  // log-viscosity gradient is formed at every node.
   Dev<double> nodeVolume, colWeight;  // rho_p r_p^2 per memory node; w_theta 2 pi / nphi per colatitude
   const double2* passAddSph = nullptr;  // solutions a pass adds after its solve (the dual's K^-1 S^T g)
   const double2* passAddTor = nullptr;
   struct AdjointBuffers {
     std::vector<GridTensor> m, hold;  // memory duals per branch; Sdirk2's held share
     GridTensor d, bar;                // the strain dual; the end strain's total dual
+    std::vector<GridTensor> startM;   // the stage's start memory on the grid at every node
+    GridTensor startD, endD;          // its start and end strain on the grid at every node
     Dev<double2> qSph, qTor, gU, gPhi, sigma;
     Dev<double> grad;
     V3dState scratch, stage;          // StartStage's output; Sdirk2's recomputed first stage
+    // the last two converged dual strains per stage kind (one-stage, Sdirk2's
+    // first, its second): the next transposed solve's extrapolated start
+    Dev<double2> last[3], before[3];
+    int count[3] = {0, 0, 0};
     bool ready = false;
   } adj;
   int CopyState(const V3dState& from, V3dState& to);
-  int StageAdjoint(V3dState& in, const GridTensor& end, double dt, int scheme, bool measured,
+  int StageAdjoint(V3dState& in, const V3dState& end, double dt, int scheme, bool measured, int kind,
                    sl3dgpu_step_info& info);
-  int AdjointRun(const double* times, int nodes, int scheme, const double* loads, const double* uDual,
+  int ArmGuess(const double2* a, const double2* b, double c);
+  int AdjointRun(const double* times, int nodes, int scheme, int stride, const double* loads, const double* uDual,
                  const double* phiDual, double* loadKernels, double* deltaGradient, double* objective,
                  sl3dgpu_step_info* infos);
-  int AdjointSweep(const double* times, int nodes, int scheme, const double* loads, const double* uDual,
+  int AdjointSweep(const double* times, int nodes, int scheme, int stride, const double* loads, const double* uDual,
                    const double* phiDual, double* loadKernels, double* deltaGradient, double* objective,
                    sl3dgpu_step_info* infos);
 
@@ -3119,15 +3128,37 @@ int Viscoelastic3DGpu::CopyState(const V3dState& from, V3dState& to) {
 // = u^T (F An(d-bar + W zeta) + S^T g) and the gradient in delta through
 // e, alpha, beta (W's share folded into M). The stage's weights are
 // StartStage's own, recomputed from the start state.
-int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const GridTensor& end, double dt, int scheme, bool measured,
-                                    sl3dgpu_step_info& info) {
+// The next stage's start guess (1 - c) a + c b in the warm-start buffer
+// (b null: a itself), armed for the stage.
+int Viscoelastic3DGpu::ArmGuess(const double2* a, const double2* b, double c) {
+  if (guess.n != static_cast<size_t>(spectralComplex)) {
+    SL3D_CUDA(guess.Alloc(spectralComplex));
+    SL3D_CUDA(guessNext.Alloc(spectralComplex));
+  }
+  if (b == nullptr) {
+    SL3D_CUDA(cudaMemcpyAsync(guess.p, a, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  } else {
+    LaunchBlend(spectralComplex, c, a, b, guess.p, stream);
+    SL3D_CHECK_LAUNCH();
+  }
+  stageGuess = guess.p;
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const V3dState& end, double dt, int scheme, bool measured,
+                                    int kind, sl3dgpu_step_info& info) {
   Flavour* f = nullptr;
   SL3D_TRY(StartStage(in, adj.scratch, dt, scheme, nullptr, &f));
+  const int bw = scheme == static_cast<int>(Scheme::BackwardEuler) ? 1 : 0;
   AdjointStrainArgs sa{};
   sa.values = values;
+  sa.fieldSize = fieldSize;
   sa.branches = K;
+  sa.scheme = bw;
+  sa.dt = dt;
+  sa.itauRef = itauRef.p;
+  sa.factor = factor.p;
   for (int k = 0; k < K; ++k) {
-    sa.beta[k] = beta[k].p;
     sa.m0[k] = adj.m[k].c0.p;
     sa.m1[k] = adj.m[k].c1.p;
     sa.mr[k] = adj.m[k].r.p;
@@ -3160,7 +3191,11 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const GridTensor& end, double 
     passAddTor = adj.qTor.p;
   }
   SL3D_CUDA(cudaMemsetAsync(s.p, 0, spectralComplex * sizeof(double2), stream));
+  // the start: zero, and the extrapolation of this kind's last two dual
+  // strains when the sweep has them (kept only if its first pass is better)
   stageGuess = nullptr;
+  if (adj.count[kind] >= 2) SL3D_TRY(ArmGuess(adj.before[kind].p, adj.last[kind].p, 2.0));
+  else if (adj.count[kind] == 1) SL3D_TRY(ArmGuess(adj.last[kind].p, nullptr, 0.0));
   info = sl3dgpu_step_info{};
   int rc = SL3DGPU_OK;
   if (options.precision == 1) {
@@ -3177,6 +3212,10 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const GridTensor& end, double 
     SetError("v3d adjoint: a stage's transposed fixed point did not converge");
     return SL3DGPU_ERR_UNCONVERGED;
   }
+  std::swap(adj.before[kind], adj.last[kind]);
+  SL3D_CUDA(cudaMemcpyAsync(adj.last[kind].p, s.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  ++adj.count[kind];
   // zeta = Syn Str z, the converged iterate's synthesis
   SL3D_TRY(SynthesiseRange(s.p, dGrid, 0, P));
   // the load's dual: u^T (F An(d-bar + W zeta) + S^T g)
@@ -3191,13 +3230,38 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const GridTensor& end, double 
   SL3D_CHECK_LAUNCH();
   LaunchLoadDual(geo, f->units.p, f->unitOffset.p, rhsSph.p, adj.sigma.p, stream);
   SL3D_CHECK_LAUNCH();
+  // The stage's forward fields on the grid at every node: the memory as the
+  // state holds it at the lateral nodes and synthesised from its
+  // coefficients elsewhere, the strains from their coefficients.
+  const int p0 = lateralFirst, p1 = lateralEnd;
+  const long long begin = p0 * fieldSize, span = static_cast<long long>(p1 - p0) * fieldSize;
+  for (int k = 0; k < K; ++k) {
+    if (span > 0) {
+      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].c0.p + begin, in.m[k].c0.p + begin, span * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, stream));
+      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].c1.p + begin, in.m[k].c1.p + begin, span * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, stream));
+      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].r.p + begin, in.m[k].r.p + begin, span * sizeof(double),
+                                cudaMemcpyDeviceToDevice, stream));
+    }
+    if (p0 > 0) SL3D_TRY(SynthesiseRange(in.mSpec[k].p, adj.startM[k], 0, p0));
+    if (p1 < P) SL3D_TRY(SynthesiseRange(in.mSpec[k].p, adj.startM[k], p1, P - p1));
+  }
+  if (in.hasCoeffs) {
+    SL3D_TRY(SynthesiseRange(in.coeffs.p, adj.startD, 0, P));
+  } else {
+    SL3D_CUDA(cudaMemsetAsync(adj.startD.c0.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(adj.startD.c1.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(adj.startD.r.p, 0, values * sizeof(double), stream));
+  }
+  SL3D_TRY(SynthesiseRange(end.coeffs.p, adj.endD, 0, P));
   // the start's memory and strain duals, the gradient
   AdjointMemoryArgs ma{};
   ma.values = values;
   ma.fieldSize = fieldSize;
   ma.nphi = grid->nphi;
   ma.branches = K;
-  ma.scheme = scheme == static_cast<int>(Scheme::BackwardEuler) ? 1 : 0;
+  ma.scheme = bw;
   ma.dt = dt;
   ma.muBranch = muBranch.p;
   ma.itauRef = itauRef.p;
@@ -3208,9 +3272,9 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const GridTensor& end, double 
     ma.m0[k] = adj.m[k].c0.p;
     ma.m1[k] = adj.m[k].c1.p;
     ma.mr[k] = adj.m[k].r.p;
-    ma.s0[k] = in.m[k].c0.p;
-    ma.s1[k] = in.m[k].c1.p;
-    ma.sr[k] = in.m[k].r.p;
+    ma.s0[k] = adj.startM[k].c0.p;
+    ma.s1[k] = adj.startM[k].c1.p;
+    ma.sr[k] = adj.startM[k].r.p;
   }
   ma.d0 = adj.d.c0.p;
   ma.d1 = adj.d.c1.p;
@@ -3218,27 +3282,29 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const GridTensor& end, double 
   ma.z0 = dGrid.c0.p;
   ma.z1 = dGrid.c1.p;
   ma.zr = dGrid.r.p;
-  ma.a0 = in.strain.c0.p;
-  ma.a1 = in.strain.c1.p;
-  ma.ar = in.strain.r.p;
-  ma.b0 = end.c0.p;
-  ma.b1 = end.c1.p;
-  ma.br = end.r.p;
+  ma.a0 = adj.startD.c0.p;
+  ma.a1 = adj.startD.c1.p;
+  ma.ar = adj.startD.r.p;
+  ma.b0 = adj.endD.c0.p;
+  ma.b1 = adj.endD.c1.p;
+  ma.br = adj.endD.r.p;
   ma.grad = adj.grad.p;
   LaunchAdjointMemory(ma, stream);
   SL3D_CHECK_LAUNCH();
   return SL3DGPU_OK;
 }
 
-int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, const double* loads,
+int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, int stride, const double* loads,
                                   const double* uDual, const double* phiDual, double* loadKernels,
                                   double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
   if (staticMode || ocean.on || options.solver != 0) {
     SetError("v3d adjoint: built for the fixed-point step (solver 0, FP64 or mixed) without an ocean");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  if (nodes < 1 || times == nullptr || loads == nullptr || loadKernels == nullptr || scheme < 0 || scheme > 2) {
-    SetError("v3d adjoint: at least one node, times, loads, the load kernels' buffer and a scheme of 0, 1 or 2");
+  if (nodes < 1 || times == nullptr || loads == nullptr || loadKernels == nullptr || scheme < 0 || scheme > 2 ||
+      stride < 1) {
+    SetError("v3d adjoint: at least one node, times, loads, the load kernels' buffer, a scheme of 0, 1 or 2 and a "
+             "record stride of at least 1");
     return SL3DGPU_ERR_ARGUMENT;
   }
   for (int k = 1; k < nodes; ++k)
@@ -3246,29 +3312,28 @@ int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, co
       SetError("v3d: node times must not decrease");
       return SL3DGPU_ERR_ARGUMENT;
     }
-  // every node on the grid for the sweep; the operator's own range back after
-  const int first = lateralFirst, end = lateralEnd;
-  lateralFirst = 0;
-  lateralEnd = P;
-  const int rc = AdjointSweep(times, nodes, scheme, loads, uDual, phiDual, loadKernels, deltaGradient, objective,
-                              infos);
+  const int rc = AdjointSweep(times, nodes, scheme, stride, loads, uDual, phiDual, loadKernels, deltaGradient,
+                              objective, infos);
   passAddSph = passAddTor = nullptr;
-  lateralFirst = first;
-  lateralEnd = end;
+  stageGuess = nullptr;
   return rc;
 }
 
-int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, const double* loads,
+int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, int stride, const double* loads,
                                     const double* uDual, const double* phiDual, double* loadKernels,
                                     double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
   const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
   if (!adj.ready) {
     adj.m.resize(K);
     adj.hold.resize(K);
+    adj.startM.resize(K);
     for (int k = 0; k < K; ++k) {
       SL3D_CUDA(adj.m[k].Alloc(values));
       SL3D_CUDA(adj.hold[k].Alloc(values));
+      SL3D_CUDA(adj.startM[k].Alloc(values));
     }
+    SL3D_CUDA(adj.startD.Alloc(values));
+    SL3D_CUDA(adj.endD.Alloc(values));
     SL3D_CUDA(adj.d.Alloc(values));
     SL3D_CUDA(adj.bar.Alloc(values));
     SL3D_CUDA(adj.qSph.Alloc(rhsSphComplex));
@@ -3279,6 +3344,10 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
     SL3D_CUDA(adj.grad.Alloc(values));
     SL3D_TRY(AllocState(adj.scratch));
     SL3D_TRY(AllocState(adj.stage));
+    for (int i = 0; i < 3; ++i) {
+      SL3D_CUDA(adj.last[i].Alloc(spectralComplex));
+      SL3D_CUDA(adj.before[i].Alloc(spectralComplex));
+    }
     adj.ready = true;
   }
   auto zeroTensor = [&](GridTensor& t) -> int {
@@ -3326,12 +3395,46 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
       SL3D_TRY(Surface(2, surface.data()));
       objectiveSum += pair(phiDual + 2 * lm * k, surface.data());
     }
-    SL3D_TRY(AllocState(trajectory[k]));
-    SL3D_TRY(CopyState(cur, trajectory[k]));
+    if (k % stride == 0) {
+      SL3D_TRY(AllocState(trajectory[k]));
+      SL3D_TRY(CopyState(cur, trajectory[k]));
+    }
   }
   if (objective) *objective = objectiveSum;
 
+  // The states of a gap between two kept nodes, rebuilt by the run's own
+  // steps from the kept state below when the sweep first needs one of them
+  // (ForwardTrajectory3D's record stride): the kept states and one gap's
+  // are held, about nodes / stride + stride states.
+  std::vector<V3dState> gap(stride > 1 ? stride : 0);
+  int gapBase = -1;
+  auto stateAt = [&](int k, V3dState** out) -> int {
+    if (k % stride == 0) {
+      *out = &trajectory[k];
+      return SL3DGPU_OK;
+    }
+    const int base = k - k % stride;
+    if (base != gapBase) {
+      SL3D_TRY(CopyState(trajectory[base], cur));
+      for (int j = base + 1; j < std::min(base + stride, nodes); ++j) {
+        sl3dgpu_step_info info{};
+        SL3D_TRY(Step(cur, times[j] - times[j - 1], scheme, loads + 2 * lm * (j - 1), loads + 2 * lm * j, &info));
+        if (!info.converged) {
+          SetError("v3d adjoint: a step of the forward run did not converge when repeated");
+          return SL3DGPU_ERR_UNCONVERGED;
+        }
+        V3dState& slot = gap[j - base];
+        if (slot.m.empty()) SL3D_TRY(AllocState(slot));
+        SL3D_TRY(CopyState(cur, slot));
+      }
+      gapBase = base;
+    }
+    *out = &gap[k - base];
+    return SL3DGPU_OK;
+  };
+
   // The transposed sweep, node by node from the last.
+  for (int& c : adj.count) c = 0;
   for (int k = 0; k < K; ++k) SL3D_TRY(zeroTensor(adj.m[k]));
   SL3D_TRY(zeroTensor(adj.d));
   SL3D_CUDA(cudaMemsetAsync(adj.grad.p, 0, values * sizeof(double), stream));
@@ -3344,7 +3447,12 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
   };
   const bool measured = uDual != nullptr || phiDual != nullptr;
   for (int n = nodes - 1; n >= 0; --n) {
-    V3dState& prev = n > 0 ? trajectory[n - 1] : zero;
+    V3dState* prevState = &zero;
+    V3dState* endState = nullptr;
+    if (n > 0) SL3D_TRY(stateAt(n - 1, &prevState));
+    SL3D_TRY(stateAt(n, &endState));
+    V3dState& prev = *prevState;
+    V3dState& endAt = *endState;
     const double dt = n > 0 ? times[n] - times[n - 1] : 0.0;
     if (uDual)
       SL3D_CUDA(cudaMemcpyAsync(adj.gU.p, uDual + 2 * lm * n, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
@@ -3355,7 +3463,7 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
     if (phiDual == nullptr) SL3D_CUDA(cudaMemsetAsync(adj.gPhi.p, 0, lm * sizeof(double2), stream));
     sl3dgpu_step_info info{};
     if (scheme != 2 || dt == 0.0) {
-      SL3D_TRY(StageAdjoint(prev, trajectory[n].strain, dt, scheme == 2 ? 1 : scheme, measured, info));
+      SL3D_TRY(StageAdjoint(prev, endAt, dt, scheme == 2 ? 1 : scheme, measured, 0, info));
       SL3D_TRY(addSigma(n, 1.0));
       continue;
     }
@@ -3368,19 +3476,28 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
     SL3D_CUDA(cudaMemcpyAsync(sigma1.p, loads + 2 * lm * n, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
     LaunchBlend(static_cast<long long>(lm), gamma, sigma0.p, sigma1.p, sigmaMid.p, stream);
     SL3D_CHECK_LAUNCH();
-    stageGuess = nullptr;
+    // its start guess the forward's: (1 - gamma) s_{n-1} + gamma s_n
+    SL3D_TRY(ArmGuess(prev.coeffs.p, endAt.coeffs.p, gamma));
     sl3dgpu_step_info first{};
     SL3D_TRY(StepOnce(prev, adj.stage, h, 1, sigma0.p, sigmaMid.p, first));
+    stageGuess = nullptr;
     if (!first.converged) {
       SetError("v3d adjoint: the first stage of a forward step did not converge when repeated");
       return SL3DGPU_ERR_UNCONVERGED;
     }
+    const long long begin = lateralFirst * fieldSize, end = static_cast<long long>(lateralEnd) * fieldSize;
     for (int k = 0; k < K; ++k) {
-      LaunchStageCombine(values, r, prev.m[k].c0.p, prev.m[k].c1.p, prev.m[k].r.p, adj.stage.m[k].c0.p,
-                         adj.stage.m[k].c1.p, adj.stage.m[k].r.p, stream);
+      if (end > begin) {
+        LaunchStageCombine(end - begin, r, prev.m[k].c0.p + begin, prev.m[k].c1.p + begin, prev.m[k].r.p + begin,
+                           adj.stage.m[k].c0.p + begin, adj.stage.m[k].c1.p + begin, adj.stage.m[k].r.p + begin,
+                           stream);
+        SL3D_CHECK_LAUNCH();
+      }
+      LaunchSpectralCombine(rows0 + rows1 + rowsR, P, lateralFirst, lateralEnd, r, prev.mSpec[k].p,
+                            adj.stage.mSpec[k].p, stream);
       SL3D_CHECK_LAUNCH();
     }
-    SL3D_TRY(StageAdjoint(adj.stage, trajectory[n].strain, h, 1, measured, info));
+    SL3D_TRY(StageAdjoint(adj.stage, endAt, h, 1, measured, 2, info));
     SL3D_TRY(addSigma(n, 1.0));
     // the combination transposed: (1 - r) of M2's dual held for m_{n-1}, r of it Y1's
     for (int k = 0; k < K; ++k) {
@@ -3396,7 +3513,7 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
         SL3D_CHECK_LAUNCH();
       }
     }
-    SL3D_TRY(StageAdjoint(prev, adj.stage.strain, h, 1, false, info));
+    SL3D_TRY(StageAdjoint(prev, adj.stage, h, 1, false, 1, info));
     SL3D_TRY(addSigma(n - 1, 1.0 - gamma));
     SL3D_TRY(addSigma(n, gamma));
     for (int k = 0; k < K; ++k) {
@@ -3924,7 +4041,7 @@ extern "C" int sl3dgpu_v3d_run(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const d
   return h->op.Run(state->st, times, nodes, scheme, loads, u, phi, infos);
 }
 
-extern "C" int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* h, const double* times, int nodes, int scheme,
+extern "C" int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* h, const double* times, int nodes, int scheme, int stride,
                                        const double* loads, const double* u_dual, const double* phi_dual,
                                        double* load_kernels, double* delta_gradient, double* objective,
                                        sl3dgpu_step_info* infos) {
@@ -3932,8 +4049,8 @@ extern "C" int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* h, const double* times, int 
     SetError("v3d adjoint: null operator");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  return h->op.AdjointRun(times, nodes, scheme, loads, u_dual, phi_dual, load_kernels, delta_gradient, objective,
-                          infos);
+  return h->op.AdjointRun(times, nodes, scheme, stride, loads, u_dual, phi_dual, load_kernels, delta_gradient,
+                          objective, infos);
 }
 
 extern "C" int sl3dgpu_v3d_sample_volumes(const sl3dgpu_v3d* h, double* out) {

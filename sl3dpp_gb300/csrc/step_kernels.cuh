@@ -308,11 +308,14 @@ void LaunchSurfaceDual(const Geometry& g, const double2* u, const double2* phi, 
 void LaunchLoadDual(const Geometry& g, const double* units, const long long* unitOffset, const double2* rhsSph,
                     double2* out, cudaStream_t stream);
 // out = dD + sum_k beta_k mD_k over a grid tensor (the end strain's dual:
-// its own and the memory advance's).
+// its own and the memory advance's), beta_k the stage's weight at every
+// grid value.
 struct AdjointStrainArgs {
-  long long values;
-  int branches;
-  const double* beta[2];
+  long long values, fieldSize;
+  int branches, scheme;
+  double dt;
+  const double* itauRef;    // [k][P]
+  const double* factor;     // exp(-delta) per grid value
   const double2* m0[2];
   const double2* m1[2];
   const double* mr[2];

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <optional>
 #include <span>
 #include <random>
@@ -590,6 +591,67 @@ void Evolution(const sl3dpp::Rheology& body) {
                                    std::to_string(worst) + ")");
 }
 
+// AdjointSolver3D: the load kernels pair with the loads to the objective of
+// the forward run (Evolution3D::Run) under them; the kernel in delta is a
+// finite density wherever the gradient is.
+void Adjoint(const sl3dpp::Rheology& body) {
+  const int lmax = 8;
+  sl3dpp::Viscoelastic3D::Options options;
+  options.rtol = 1e-12;
+  options.max_iterations = 80;
+  sl3dpp::Viscoelastic3D op(body, lmax, Delta, options);
+  sl3dpp::Evolution3D evolution(op);
+  const double year = 3.15576e7 / op.TimeScale();
+  std::vector<double> times;
+  for (int k = 0; k < 4; ++k) times.push_back(500.0 * year * k);
+  auto load = [&](int l, double t) -> std::optional<std::vector<Complex>> {
+    std::vector<Complex> c(l + 1);
+    for (int m = 0; m <= l; ++m)
+      c[m] = Complex(std::cos(1.0 + l + 0.3 * m + t / year), m == 0 ? 0.0 : std::sin(2.0 * l - m)) / (1.0 + l * l);
+    return c;
+  };
+  const std::size_t lm = static_cast<std::size_t>(lmax + 1) * (lmax + 2) / 2;
+  std::map<std::size_t, sl3dpp::Measurement3D> measurements;
+  for (std::size_t node : {std::size_t{1}, std::size_t{3}}) {
+    auto& m = measurements[node];
+    m.displacementDual.resize(lm);
+    m.potentialDual.resize(lm);
+    for (std::size_t i = 0; i < lm; ++i) {
+      m.displacementDual[i] = Complex(std::sin(0.7 * static_cast<double>(i + node)), 0.0);
+      m.potentialDual[i] = Complex(std::cos(0.3 * static_cast<double>(i) - static_cast<double>(node)), 0.0);
+    }
+  }
+  const auto kernels = sl3dpp::AdjointSolver3D(evolution).FirstOrderKernels(times, load, measurements);
+  const auto run = evolution.Run(times, load);
+  auto pair = [&](const std::vector<Complex>& a, const std::vector<Complex>& b) {
+    double sum = 0.0;
+    for (int l = 0, i = 0; l <= lmax; ++l)
+      for (int m = 0; m <= l; ++m, ++i) sum += (m == 0 ? 1.0 : 2.0) * (a[i] * std::conj(b[i])).real();
+    return sum;
+  };
+  double objective = 0.0, paired = 0.0;
+  for (const auto& [node, m] : measurements)
+    objective += pair(m.displacementDual, run[node].U) + pair(m.potentialDual, run[node].phi);
+  for (std::size_t k = 0; k < times.size(); ++k) {
+    std::vector<Complex> flat;
+    for (int l = 0; l <= lmax; ++l) {
+      const auto c = *load(l, times[k]);
+      flat.insert(flat.end(), c.begin(), c.end());
+    }
+    paired += pair(kernels.directLoadKernels[k], flat);
+  }
+  bool finite = kernels.logViscosityKernel3D.size() == op.GridValues();
+  double largest = 0.0;
+  for (double v : kernels.logViscosityKernel3D) {
+    finite = finite && std::isfinite(v);
+    largest = std::max(largest, std::abs(v));
+  }
+  Expect(std::abs(kernels.objective - objective) < 1e-10 * std::abs(objective) &&
+             std::abs(paired - objective) < 1e-8 * std::abs(objective) && finite && largest > 0.0,
+         "AdjointSolver3D load kernels pair with the loads to the forward run's objective (" +
+             std::to_string(std::abs(paired - objective) / std::abs(objective)) + ")");
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -606,6 +668,7 @@ int main(int argc, char** argv) {
       StaticForceApply(body);
       SeaLevel();
       Evolution(body);
+      Adjoint(body);
     }
   } catch (const std::exception& e) {
     std::printf("FAIL uncaught %s\n", e.what());

@@ -12,7 +12,9 @@ the library's forward run and against the oracle's march of the same nodes
 log-viscosity gradient must give the derivative of J along a direction p
 over every node (the sweep forms it at nodes outside delta's range too):
 Richardson-extrapolated central differences of the forward run, 1e-6. Each
-for the three schemes, and the mixed form for Sdirk2."""
+for the three schemes, and the mixed form for Sdirk2. A record stride (the
+forward states kept every stride-th node, the gaps rebuilt) changes nothing
+but the memory held."""
 
 import numpy as np
 import pytest
@@ -130,3 +132,20 @@ def _delta(o, lmax):
 
     return delta_for(o, lmax, 4, 0.8, 11)
 
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("stride", [2, 3])
+def test_gpu_record_stride_gives_the_kernels_of_every_node_kept(gpu, stride):
+    """ForwardTrajectory3D's stride: the sweep rebuilds a gap's states by the
+    run's own steps from the kept state below; the kernels are those of the
+    run with every node kept (1e-9: the rebuilt steps converge afresh)."""
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D
+
+    lmax, nodes = 8, 7
+    o, g, times, loads, gU, gPhi = _run(lmax, 2, nodes, 0, seed=9)
+    every = Evolution3D(g, 2).Adjoint(times, loads, gU, gPhi)
+    sparse = Evolution3D(g, 2).Adjoint(times, loads, gU, gPhi, stride=stride)
+    assert abs(sparse["objective"] - every["objective"]) < 1e-12 * abs(every["objective"])
+    assert rel(sparse["load_kernels"], every["load_kernels"]) < 1e-9
+    assert rel(sparse["delta_gradient"], every["delta_gradient"]) < 1e-9
