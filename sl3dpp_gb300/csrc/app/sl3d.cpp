@@ -8,6 +8,10 @@
 //   sl3d solve CONFIG.json   the run: node 0 the instantaneous response,
 //                            then a step per node; a checkpoint every
 //                            `stride` nodes; the surface table at the end
+//   sl3d kernel CONFIG.json  the kernels of the config's measurements (the
+//                            reference's `sl3d kernel` under the discrete
+//                            method, for a run without an ocean): per
+//                            measurement one transposed sweep of the run
 //
 // The config (JSON; members other than these are refused):
 //   model       {"earth": "standard", "elements": N, "kelvin_fraction": f,
@@ -49,6 +53,19 @@
 //   output      {"file"}: the surface table, a row per node and (l, m >= 0):
 //               node, time (yr), l, m, U (m, re im), phi (m^2 s^-2, re im)
 //               and, with an ocean, the relative sea level change (m, re im)
+////   kernels     (the kernel command) {"method": "discrete", "parameters":
+//               ["load", "viscosity"], "measurements": [{"type":
+//               "displacement_point" | "displacement_cap" | "potential_point"
+//               | "potential_cap", "name", "latitude", "longitude",
+//               "width_deg" (a cap's Gaussian width), "time" (a node's, on the
+//               run's clock; the last node by default)}], "output": DIR,
+//               "record_stride" (1)}; per measurement NAME_summary.txt (its
+//               value in SI), NAME_load_kernels.txt (the load kernel's (l, m
+//               >= 0) coefficients per node, per kg m^-2 per m^2 of the
+//               run's sphere) and NAME_viscosity_kernels.bin with
+//               NAME_viscosity_grid.txt (dJ/d delta per m^3 on every memory
+//               node's grid). Kernels under an ocean, the continuous method
+//               and the other parameters are refused as not built.
 //
 // Checkpoints (the reference's scheme: a whole file written as
 // `.node_NNNNNN.partial` and renamed to `node_NNNNNN.ckpt`, the newest two
@@ -61,6 +78,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -132,6 +150,16 @@ struct Config {
   long long stopAfter = -1;
   std::string output;
   uint64_t hash = 0;
+  // kernels (the `kernel` command)
+  struct Measurement {
+    std::string name, type;  // displacement_point | displacement_cap | potential_point | potential_cap
+    double latitude = 0.0, longitude = 0.0, widthDeg = 0.0;
+    size_t node = 0;
+  };
+  bool kernels = false, loadKernels = false, viscosityKernels = false;
+  std::vector<Measurement> measurements;
+  std::string kernelDir;
+  int recordStride = 1;
 };
 
 uint64_t Fnv1a(const std::string& text) {
@@ -151,7 +179,7 @@ Config ReadConfig(const std::string& path) {
   const Value doc = sl3d::json::Parse(text.str());
   const Object& root = doc.Members("the config");
   OnlyKeys(root, {"model", "mesh", "lateral", "forcing", "ocean", "time", "solve", "checkpoint", "restart",
-                  "stop_after_node", "output"},
+                  "stop_after_node", "output", "kernels"},
            "config");
   Config c;
   // the members that decide the computation, for the run hash
@@ -340,6 +368,89 @@ Config ReadConfig(const std::string& path) {
   OnlyKeys(o, {"file"}, "output");
   c.output = Find(o, "file") ? Find(o, "file")->String("output.file") : "";
   if (c.output.empty()) throw std::invalid_argument("output: a file is required");
+
+  // kernels
+  if (const Value* kv = Find(root, "kernels")) {
+    const Object& k = kv->Members("kernels");
+    OnlyKeys(k, {"method", "parameters", "measurements", "output", "record_stride"}, "kernels");
+    c.kernels = true;
+    if (c.ocean)
+      throw std::invalid_argument("kernels: the kernels of a run under an ocean are not built (the sweep is the run "
+                                  "without an ocean's)");
+    if (const Value* m = Find(k, "method")) {
+      const std::string& name = m->String("kernels.method");
+      if (name == "continuous") throw std::invalid_argument("kernels.method: \"continuous\" is not built; \"discrete\"");
+      if (name != "discrete") throw std::invalid_argument("kernels.method: \"discrete\"");
+    }
+    const Value* params = Find(k, "parameters");
+    if (!params) throw std::invalid_argument("kernels.parameters is required: \"load\", \"viscosity\"");
+    for (const Value& v : params->Items("kernels.parameters")) {
+      const std::string& word = v.String("kernels.parameters");
+      bool& flag = word == "load" ? c.loadKernels : c.viscosityKernels;
+      if (word != "load" && word != "viscosity") {
+        if (word == "ice") throw std::invalid_argument("kernels.parameters: \"ice\" needs an ocean");
+        throw std::invalid_argument("kernels.parameters: \"" + word + "\" is not built; \"load\", \"viscosity\"");
+      }
+      if (flag) throw std::invalid_argument("kernels.parameters: \"" + word + "\" named twice");
+      flag = true;
+    }
+    if (!c.loadKernels && !c.viscosityKernels) throw std::invalid_argument("kernels.parameters: at least one");
+    const Value* dir = Find(k, "output");
+    c.kernelDir = dir ? dir->String("kernels.output") : "";
+    if (c.kernelDir.empty()) throw std::invalid_argument("kernels.output: a directory is required");
+    c.recordStride = static_cast<int>(NumberOr(k, "record_stride", 1));
+    if (c.recordStride < 1) throw std::invalid_argument("kernels.record_stride: at least 1");
+    const Value* ms = Find(k, "measurements");
+    if (!ms) throw std::invalid_argument("kernels.measurements is required");
+    const double span = c.timesYr.back() - c.timesYr.front();
+    for (const Value& mv : ms->Items("kernels.measurements")) {
+      const Object& mo = mv.Members("a measurement");
+      OnlyKeys(mo, {"type", "name", "latitude", "longitude", "width_deg", "time"}, "a measurement");
+      Config::Measurement m;
+      m.name = Find(mo, "name") ? Find(mo, "name")->String("measurement.name")
+                                : "measurement_" + std::to_string(c.measurements.size());
+      const bool plain = !m.name.empty() && m.name[0] != '.' &&
+                         std::all_of(m.name.begin(), m.name.end(), [](char ch) {
+                           return std::isalnum(static_cast<unsigned char>(ch)) || ch == '_' || ch == '-' || ch == '.';
+                         });
+      if (!plain) throw std::invalid_argument("measurement.name: letters, digits, _, - and ., not starting with .");
+      for (const auto& other : c.measurements)
+        if (other.name == m.name) throw std::invalid_argument("measurement.name: \"" + m.name + "\" named twice");
+      m.type = Find(mo, "type") ? Find(mo, "type")->String("measurement.type") : "";
+      const bool cap = m.type == "displacement_cap" || m.type == "potential_cap";
+      const bool point = m.type == "displacement_point" || m.type == "potential_point";
+      if (m.type.rfind("relative_sea_level", 0) == 0 || m.type == "decay_time")
+        throw std::invalid_argument("measurement.type: \"" + m.type + "\" needs an ocean");
+      if (!cap && !point)
+        throw std::invalid_argument("measurement.type: displacement_point, displacement_cap, potential_point or "
+                                    "potential_cap");
+      if (!Find(mo, "latitude") || !Find(mo, "longitude"))
+        throw std::invalid_argument("measurement " + m.name + ": latitude and longitude are required");
+      m.latitude = Find(mo, "latitude")->Number("measurement.latitude");
+      m.longitude = Find(mo, "longitude")->Number("measurement.longitude");
+      if (!(m.latitude >= -90.0 && m.latitude <= 90.0))
+        throw std::invalid_argument("measurement " + m.name + ": latitude in [-90, 90]");
+      if (cap) {
+        m.widthDeg = NumberOr(mo, "width_deg", -1.0);
+        if (!(m.widthDeg > 0.0)) throw std::invalid_argument("measurement " + m.name + ": width_deg > 0");
+      } else if (Find(mo, "width_deg")) {
+        throw std::invalid_argument("measurement " + m.name + ": width_deg is a cap's");
+      }
+      m.node = c.timesYr.size() - 1;
+      if (const Value* tv = Find(mo, "time")) {
+        const double t = tv->Number("measurement.time");
+        bool found = false;
+        for (size_t n = 0; n < c.timesYr.size() && !found; ++n)
+          if (std::abs(c.timesYr[n] - t) <= 1e-9 * std::max(span, 1.0)) {
+            m.node = n;
+            found = true;
+          }
+        if (!found) throw std::invalid_argument("measurement " + m.name + ": time is not a node of the run");
+      }
+      c.measurements.push_back(m);
+    }
+    if (c.measurements.empty()) throw std::invalid_argument("kernels.measurements: at least one");
+  }
   return c;
 }
 
@@ -533,27 +644,17 @@ long long ReadCheckpoint(const Config& c, sl3dgpu_v3d* op, sl3dgpu_v3d_state* st
   return static_cast<long long>(node);
 }
 
-int Solve(const Config& c) {
+// The lateral viscosity on every node's grid: the seeded (or read) pattern
+// between the two depths.
+void SetLateral(const Config& c, sl3dgpu_v3d* op) {
   const int lmax = c.options.lmax;
   const size_t lm = Index(lmax, lmax) + 1;
-  sl3dgpu_v3d* op = nullptr;
-  Check(sl3dgpu_v3d_create(c.layers.data(), static_cast<int>(c.layers.size()), &c.options, &op), "operator");
-  struct Guard {
-    sl3dgpu_v3d* op;
-    sl3dgpu_v3d_state* state = nullptr;
-    ~Guard() {
-      if (state) sl3dgpu_v3d_free_state(state);
-      sl3dgpu_v3d_destroy(op);
-    }
-  } guard{op};
   int P = 0, nt = 0, np = 0;
   Check(sl3dgpu_v3d_shape(op, &P, &nt, &np), "shape");
   std::vector<double> radius(P);
   Check(sl3dgpu_v3d_nodes(op, radius.data(), nullptr), "nodes");
   double length = 1.0, time = 1.0, sigma = 1.0;
   Check(sl3dgpu_v3d_scales(op, &length, &time, &sigma), "scales");
-
-  // the lateral viscosity on every node's grid
   if (c.deltaRms > 0.0 || !c.coefficientsFile.empty()) {
     std::vector<Complex> coeffs;
     if (c.seeded) {
@@ -577,6 +678,24 @@ int Solve(const Config& c) {
     }
     Check(sl3dgpu_v3d_set_delta(op, samples.data(), 0), "delta");
   }
+}
+
+int Solve(const Config& c) {
+  const int lmax = c.options.lmax;
+  const size_t lm = Index(lmax, lmax) + 1;
+  sl3dgpu_v3d* op = nullptr;
+  Check(sl3dgpu_v3d_create(c.layers.data(), static_cast<int>(c.layers.size()), &c.options, &op), "operator");
+  struct Guard {
+    sl3dgpu_v3d* op;
+    sl3dgpu_v3d_state* state = nullptr;
+    ~Guard() {
+      if (state) sl3dgpu_v3d_free_state(state);
+      sl3dgpu_v3d_destroy(op);
+    }
+  } guard{op};
+  double length = 1.0, time = 1.0, sigma = 1.0;
+  Check(sl3dgpu_v3d_scales(op, &length, &time, &sigma), "scales");
+  SetLateral(c, op);
 
   // the ice cap, on the sea-level grid (the ocean closure's) or as coefficients
   std::vector<double> seaLevel, backgroundIce, oceanWeights;
@@ -752,11 +871,192 @@ int Solve(const Config& c) {
   return 0;
 }
 
+
+// -- kernel: the discrete adjoint of the run -----------------------------------------------------------
+
+// Orthonormal spherical harmonics Y_lm(theta, phi), m >= 0, with the
+// Condon-Shortley phase (the library's basis), by the standard recurrences
+// of the normalised associated Legendre functions; (l, m) at l(l+1)/2 + m.
+std::vector<Complex> Harmonics(int lmax, double theta, double phi) {
+  const double x = std::cos(theta), s = std::sin(theta);
+  std::vector<double> P(Index(lmax, lmax) + 1, 0.0);
+  P[0] = std::sqrt(1.0 / (4.0 * kPi));
+  for (int m = 1; m <= lmax; ++m) P[Index(m, m)] = -std::sqrt((2.0 * m + 1.0) / (2.0 * m)) * s * P[Index(m - 1, m - 1)];
+  for (int m = 0; m < lmax; ++m) P[Index(m + 1, m)] = std::sqrt(2.0 * m + 3.0) * x * P[Index(m, m)];
+  for (int m = 0; m <= lmax; ++m)
+    for (int l = m + 2; l <= lmax; ++l) {
+      const double a = std::sqrt((4.0 * l * l - 1.0) / (static_cast<double>(l) * l - static_cast<double>(m) * m));
+      const double b = std::sqrt(((l - 1.0) * (l - 1.0) - static_cast<double>(m) * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+      P[Index(l, m)] = a * (x * P[Index(l - 1, m)] - b * P[Index(l - 2, m)]);
+    }
+  std::vector<Complex> Y(P.size());
+  for (int l = 0; l <= lmax; ++l)
+    for (int m = 0; m <= l; ++m) Y[Index(l, m)] = P[Index(l, m)] * std::polar(1.0, m * phi);
+  return Y;
+}
+
+// A Gaussian cap's degree weights: b_l = 2 pi int cap(d) P_l(cos d) sin d dd
+// for the cap exp(-d^2 / (2 w^2)) normalised to a unit integral over the
+// sphere (composite Simpson in d).
+std::vector<double> CapWeights(int lmax, double widthDeg) {
+  const double w = widthDeg * kPi / 180.0;
+  const int n = 20000;
+  const double h = kPi / n;
+  std::vector<double> b(lmax + 1, 0.0);
+  double area = 0.0;
+  std::vector<double> Pl(lmax + 1);
+  for (int i = 0; i <= n; ++i) {
+    const double d = i * h, x = std::cos(d);
+    const double weight = (i == 0 || i == n) ? 1.0 : (i % 2 ? 4.0 : 2.0);
+    const double f = std::exp(-d * d / (2.0 * w * w)) * std::sin(d) * weight;
+    Pl[0] = 1.0;
+    if (lmax > 0) Pl[1] = x;
+    for (int l = 2; l <= lmax; ++l) Pl[l] = ((2.0 * l - 1.0) * x * Pl[l - 1] - (l - 1.0) * Pl[l - 2]) / l;
+    area += f;
+    for (int l = 0; l <= lmax; ++l) b[l] += f * Pl[l];
+  }
+  for (double& v : b) v /= area;  // 2 pi and h / 3 cancel in the normalisation
+  return b;
+}
+
+// `sl3d kernel CONFIG`: the run of `solve` (without an ocean) and, for each
+// measurement, one transposed sweep (sl3dgpu_v3d_adjoint_run) giving the
+// load kernels and the log-viscosity kernel, written in SI.
+int Kernel(const Config& c) {
+  const int lmax = c.options.lmax;
+  const size_t lm = Index(lmax, lmax) + 1;
+  sl3dgpu_v3d* op = nullptr;
+  Check(sl3dgpu_v3d_create(c.layers.data(), static_cast<int>(c.layers.size()), &c.options, &op), "operator");
+  struct Guard {
+    sl3dgpu_v3d* op;
+    ~Guard() { sl3dgpu_v3d_destroy(op); }
+  } guard{op};
+  int P = 0, nt = 0, np = 0;
+  Check(sl3dgpu_v3d_shape(op, &P, &nt, &np), "shape");
+  std::vector<double> radius(P), theta(nt), thetaWeights(nt);
+  Check(sl3dgpu_v3d_nodes(op, radius.data(), nullptr), "nodes");
+  Check(sl3dgpu_v3d_colatitudes(op, theta.data(), thetaWeights.data()), "colatitudes");
+  double length = 1.0, time = 1.0, sigma = 1.0;
+  Check(sl3dgpu_v3d_scales(op, &length, &time, &sigma), "scales");
+  SetLateral(c, op);
+  double surface = 0.0;  // the run's sphere (m)
+  for (const auto& layer : c.layers) surface = std::max(surface, layer.r1);
+
+  // the node loads: the cap's coefficients ramped
+  sl3dgpu_grid* exact = nullptr;
+  Check(sl3dgpu_grid_create(lmax, 0, 1.0, &exact), "grid");
+  int et = 0, ep = 0;
+  Check(sl3dgpu_grid_shape(exact, &et, &ep), "grid");
+  std::vector<double> capTheta(et), capWeights(et);
+  Check(sl3dgpu_grid_colatitudes(exact, capTheta.data(), capWeights.data()), "grid");
+  std::vector<double> cap(static_cast<size_t>(et) * ep, 0.0);
+  for (int j = 0; j < et; ++j)
+    if (capTheta[j] < c.capDegrees * kPi / 180.0)
+      for (int k = 0; k < ep; ++k) cap[static_cast<size_t>(j) * ep + k] = kIceDensity * c.thicknessM / sigma;
+  const std::vector<Complex> capCoeffs = Expand(exact, cap, lm);
+  sl3dgpu_grid_destroy(exact);
+  const size_t nodes = c.timesYr.size();
+  std::vector<Complex> loads(lm * nodes);
+  std::vector<double> times(nodes);
+  for (size_t n = 0; n < nodes; ++n) {
+    const double ramp = std::min<double>(static_cast<double>(n), c.rampNodes) / c.rampNodes;
+    for (size_t i = 0; i < lm; ++i) loads[lm * n + i] = ramp * capCoeffs[i];
+    times[n] = c.timesYr[n] * kYear / time;
+  }
+  const size_t values = static_cast<size_t>(P) * nt * np;
+  std::vector<double> volume(values);
+  Check(sl3dgpu_v3d_sample_volumes(op, volume.data()), "volumes");
+  fs::create_directories(c.kernelDir);
+
+  for (const auto& m : c.measurements) {
+    const bool displacement = m.type.rfind("displacement", 0) == 0;
+    const bool isCap = m.type.size() > 4 && m.type.substr(m.type.size() - 4) == "_cap";
+    const double scale = displacement ? length : length * length / (time * time);  // SI per model unit of J
+    const char* unit = displacement ? "m" : "m^2 s^-2";
+    // J = sum_{m >= 0} w_m Re(g* X) at the node: g = b_l conj(Y_lm(x0)), b_l = 1 at a point
+    const auto Y = Harmonics(lmax, (90.0 - m.latitude) * kPi / 180.0, m.longitude * kPi / 180.0);
+    const std::vector<double> b = isCap ? CapWeights(lmax, m.widthDeg) : std::vector<double>(lmax + 1, 1.0);
+    std::vector<Complex> dual(lm * nodes);
+    for (int l = 0; l <= lmax; ++l)
+      for (int k = 0; k <= l; ++k) dual[lm * m.node + Index(l, k)] = b[l] * std::conj(Y[Index(l, k)]);
+    std::vector<Complex> kernels(lm * nodes);
+    std::vector<double> gradient(c.viscosityKernels ? values : 0);
+    double objective = 0.0;
+    Check(sl3dgpu_v3d_adjoint_run(op, times.data(), static_cast<int>(nodes), c.scheme, c.recordStride,
+                                  reinterpret_cast<const double*>(loads.data()),
+                                  displacement ? reinterpret_cast<const double*>(dual.data()) : nullptr,
+                                  displacement ? nullptr : reinterpret_cast<const double*>(dual.data()),
+                                  reinterpret_cast<double*>(kernels.data()),
+                                  c.viscosityKernels ? gradient.data() : nullptr, &objective, nullptr),
+          "adjoint");
+    const double value = scale * objective;
+    const fs::path dir(c.kernelDir);
+    {
+      std::ofstream out(dir / (m.name + "_summary.txt"));
+      char line[512];
+      std::snprintf(line, sizeof(line),
+                    "measurement %s\ntype %s\nlatitude %.17g\nlongitude %.17g\nwidth_deg %.17g\nnode %zu\nt_yr "
+                    "%.17g\nvalue %.17g %s\nmethod discrete\nrun_hash %016llx\n",
+                    m.name.c_str(), m.type.c_str(), m.latitude, m.longitude, m.widthDeg, m.node, c.timesYr[m.node],
+                    value, unit, static_cast<unsigned long long>(c.hash));
+      out << line;
+      if (!out) throw std::runtime_error("cannot write the summary of " + m.name);
+    }
+    if (c.loadKernels) {
+      // K_n(x) = sum_{m >= 0} w_m Re(K_lm Y_lm(x)) per kg m^-2 per m^2 of the run's sphere
+      const double toSi = scale / (sigma * surface * surface);
+      std::ofstream out(dir / (m.name + "_load_kernels.txt"));
+      out << "# sl3d load kernels of " << m.name << " (" << m.type << ", " << unit
+          << "): node t_yr l m K_re K_im, the coefficients of K_n(x) = sum_{m >= 0} w_m Re(K_lm Y_lm(x)) "
+             "(w_m = 1 at m = 0, 2 above; Y orthonormal, Condon-Shortley phase), dJ = sum_n int K_n dsigma_n dS "
+             "over the sphere of radius "
+          << surface << " m, per kg m^-2 per m^2\n";
+      char row[256];
+      for (size_t n = 0; n < nodes; ++n)
+        for (int l = 0; l <= lmax; ++l)
+          for (int k = 0; k <= l; ++k) {
+            const Complex v = toSi * kernels[lm * n + Index(l, k)];
+            std::snprintf(row, sizeof(row), "%zu %.17g %d %d %.17g %.17g\n", n, c.timesYr[n], l, k, v.real(),
+                          v.imag());
+            out << row;
+          }
+      if (!out) throw std::runtime_error("cannot write the load kernels of " + m.name);
+    }
+    if (c.viscosityKernels) {
+      // dJ / d delta per unit volume (SI): the gradient over the samples' volumes
+      const double toSi = scale / (length * length * length);
+      std::vector<double> density(values);
+      for (size_t x = 0; x < values; ++x) density[x] = toSi * gradient[x] / volume[x];
+      std::ofstream bin(dir / (m.name + "_viscosity_kernels.bin"), std::ios::binary);
+      bin.write(reinterpret_cast<const char*>(density.data()), static_cast<std::streamsize>(values * sizeof(double)));
+      std::ofstream grid(dir / (m.name + "_viscosity_grid.txt"));
+      grid << "# " << m.name << "_viscosity_kernels.bin: the log-viscosity kernel dJ / d delta (" << unit
+           << " per m^3; eta = eta_ref exp(delta)), float64 little-endian, node-major [node][colatitude][longitude], "
+           << P << " x " << nt << " x " << np << "; dJ = sum K d delta dV\n# nodes (radius m)\n";
+      char row[64];
+      for (int p = 0; p < P; ++p) {
+        std::snprintf(row, sizeof(row), "%.17g\n", radius[p] * length);
+        grid << row;
+      }
+      grid << "# colatitudes (rad)\n";
+      for (int j = 0; j < nt; ++j) {
+        std::snprintf(row, sizeof(row), "%.17g\n", theta[j]);
+        grid << row;
+      }
+      grid << "# longitudes: " << np << ", 2 pi k / " << np << "\n";
+      if (!bin || !grid) throw std::runtime_error("cannot write the viscosity kernels of " + m.name);
+    }
+    std::printf("sl3d: measurement %s (node %zu) = %.17g %s; kernels in %s\n", m.name.c_str(), m.node, value, unit,
+                c.kernelDir.c_str());
+  }
+  return 0;
+}
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc != 3 || (std::strcmp(argv[1], "check") != 0 && std::strcmp(argv[1], "solve") != 0)) {
-    std::fprintf(stderr, "usage: sl3d check|solve CONFIG.json\n");
+  if (argc != 3 || (std::strcmp(argv[1], "check") != 0 && std::strcmp(argv[1], "solve") != 0 &&
+                    std::strcmp(argv[1], "kernel") != 0)) {
+    std::fprintf(stderr, "usage: sl3d check|solve|kernel CONFIG.json\n");
     return 2;
   }
   try {
@@ -766,6 +1066,10 @@ int main(int argc, char** argv) {
                   static_cast<unsigned long long>(c.hash), c.options.lmax, c.layers.size(), c.timesYr.size(),
                   c.ocean ? ", ocean" : "");
       return 0;
+    }
+    if (std::strcmp(argv[1], "kernel") == 0) {
+      if (!c.kernels) throw std::invalid_argument("kernel: the config needs a kernels block");
+      return Kernel(c);
     }
     return Solve(c);
   } catch (const std::invalid_argument& e) {

@@ -1,6 +1,8 @@
 """The sl3d front end (sl3dpp_gb300/csrc/app/sl3d.cpp): the reference's
 `sl3d solve` for a 3D run through time (apps/SolveCommand.cpp:1747-1795) with
-its disk checkpoints (:239-290) and restart.
+its disk checkpoints (:239-290) and restart, and `sl3d kernel` (the
+discrete adjoint's kernels of point and cap measurements, the run without an
+ocean).
 
 Without a GPU: configs are read and checked (`sl3d check`): unknown members,
 bad values and missing blocks are refused; the run hash depends on the
@@ -12,7 +14,9 @@ checkpoint writes the uninterrupted run's table bit for bit; another run's
 checkpoint is refused; an ocean run, frozen or migrating, writes the sea
 level beside U and phi and restarts alike; the migrating run's growing cap
 moves the shorelines (the ocean's share of the area changes from node to
-node)."""
+node). `sl3d kernel`: its kernels block is checked and refused where a
+kernel is not built; on the GPU each measurement's value is the solve's
+field read there and the load kernels pair with the run's loads to it."""
 
 import json
 import pathlib
@@ -189,3 +193,111 @@ def test_gpu_migrating_run_moves_the_shorelines(gpu, sl3d, tmp_path):
     got = table(tmp_path / "surface.txt")
     assert np.all(got[got[:, 0] == 0][:, 4:] == 0.0)
     assert np.max(np.abs(got[got[:, 0] == 4][:, 8:10])) > 0.0
+
+
+# -- sl3d kernel ---------------------------------------------------------------------------------------
+
+def kernel_config(tmp_path, **kernels):
+    cfg = base(tmp_path, nodes=5)
+    block = {"method": "discrete", "parameters": ["load", "viscosity"], "output": str(tmp_path / "kernels"),
+             "measurements": [{"type": "displacement_point", "name": "uplift", "latitude": 63.2, "longitude": -20.5},
+                              {"type": "potential_cap", "name": "geoid", "latitude": 70.0, "longitude": 10.0,
+                               "width_deg": 8.0, "time": 1500.0}]}
+    block.update(kernels)
+    cfg["kernels"] = block
+    return cfg
+
+
+def test_check_reads_a_kernel_config(sl3d, tmp_path):
+    result = run(sl3d, "check", kernel_config(tmp_path), tmp_path)
+    assert result.returncode == 0, result.stderr
+    # the kernels block steers the run, it does not decide it
+    assert run_hash(result) == run_hash(run(sl3d, "check", base(tmp_path, nodes=5), tmp_path))
+
+
+@pytest.mark.parametrize("change,text", [
+    (lambda c: c.update(ocean={}), "under an ocean are not built"),
+    (lambda c: c["kernels"].update(method="continuous"), "\"continuous\" is not built"),
+    (lambda c: c["kernels"].update(parameters=["ice"]), "\"ice\" needs an ocean"),
+    (lambda c: c["kernels"].update(parameters=["moduli"]), "\"moduli\" is not built"),
+    (lambda c: c["kernels"].update(parameters=["load", "load"]), "named twice"),
+    (lambda c: c["kernels"].update(parameters=[]), "at least one"),
+    (lambda c: c["kernels"].pop("output"), "kernels.output"),
+    (lambda c: c["kernels"]["measurements"][0].update(type="relative_sea_level_point"), "needs an ocean"),
+    (lambda c: c["kernels"]["measurements"][0].update(time=250.0), "not a node"),
+    (lambda c: c["kernels"]["measurements"][1].pop("width_deg"), "width_deg > 0"),
+    (lambda c: c["kernels"]["measurements"][1].update(name="uplift"), "named twice"),
+    (lambda c: c["kernels"]["measurements"][0].update(name="../up"), "measurement.name"),
+])
+def test_check_refuses_bad_kernel_configs(sl3d, tmp_path, change, text):
+    cfg = kernel_config(tmp_path)
+    change(cfg)
+    result = run(sl3d, "check", cfg, tmp_path)
+    assert result.returncode == 2 and text in result.stderr, result.stderr
+
+
+@pytest.mark.gpu
+def test_gpu_kernel_values_and_kernels_are_the_runs(gpu, sl3d, tmp_path):
+    """`sl3d kernel`: each measurement's value is the solve's surface field
+    read there (a point by the orthonormal harmonics, a Gaussian cap by its
+    degree weights); the load kernels pair with the run's loads to that
+    value (dJ = sum_n int K_n sigma_n dS); the viscosity kernel is the
+    library adjoint's gradient over the samples' volumes, in SI."""
+    import torch
+    from scipy.special import sph_harm_y
+
+    from sl3dpp_gb300 import configs
+    from sl3dpp_gb300.grid import SurfaceGrid
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D, Options, Viscoelastic3D, standard_earth
+
+    lmax, nodes = 8, 5
+    cfg = kernel_config(tmp_path)
+    solved = run(sl3d, "solve", cfg, tmp_path)
+    assert solved.returncode == 0, solved.stdout + solved.stderr
+    result = run(sl3d, "kernel", cfg, tmp_path)
+    assert result.returncode == 0, result.stdout + result.stderr
+    got = table(tmp_path / "surface.txt")
+    lm = (lmax + 1) * (lmax + 2) // 2
+    U = (got[:, 4] + 1j * got[:, 5]).reshape(nodes, lm)
+    phi = (got[:, 6] + 1j * got[:, 7]).reshape(nodes, lm)
+    ls = np.concatenate([[l] * (l + 1) for l in range(lmax + 1)])
+    ms = np.concatenate([list(range(l + 1)) for l in range(lmax + 1)])
+    w = np.where(ms == 0, 1.0, 2.0)
+
+    def at(coeffs, lat, lon, b=None):
+        Y = sph_harm_y(ls, ms, np.radians(90.0 - lat), np.radians(lon))
+        b = np.ones(lmax + 1) if b is None else b
+        return float(np.sum(w * b[ls] * (coeffs * Y).real))
+
+    def value(name):
+        for line in (tmp_path / "kernels" / f"{name}_summary.txt").read_text().splitlines():
+            if line.startswith("value "):
+                return float(line.split()[1])
+
+    uplift = at(U[nodes - 1], 63.2, -20.5)
+    assert abs(value("uplift") - uplift) < 1e-9 * abs(uplift)
+    d = np.linspace(0.0, np.pi, 40001)
+    wcap = np.radians(8.0)
+    f = np.exp(-d ** 2 / (2 * wcap ** 2)) * np.sin(d)
+    Pl = [np.ones_like(d), np.cos(d)]
+    for l in range(2, lmax + 1):
+        Pl.append(((2 * l - 1) * np.cos(d) * Pl[-1] - (l - 1) * Pl[-2]) / l)
+    trapezoid = getattr(np, "trapezoid", None) or np.trapz
+    b = np.array([trapezoid(f * P, d) for P in Pl]) / trapezoid(f, d)
+    geoid = at(phi[3], 70.0, 10.0, b)
+    assert abs(value("geoid") - geoid) < 1e-7 * abs(geoid)
+
+    # the load kernels pair with the run's loads (SI) to the value
+    op = Viscoelastic3D(standard_earth(20), Options.defaults(lmax, 5, rtol=1e-10, max_iterations=60))
+    exact = SurfaceGrid(lmax, 0, 1.0)
+    cap = configs.cap_field(exact.theta, exact.nphi, 15.0, 2000.0)
+    sigma = exact.ExpandBatch(torch.tensor(cap, device=gpu), 1).cpu().numpy()
+    radius = max(layer.r1 for layer in standard_earth(20))
+    for name, v in (("uplift", uplift), ("geoid", geoid)):
+        k = table(tmp_path / "kernels" / f"{name}_load_kernels.txt")
+        K = (k[:, 4] + 1j * k[:, 5]).reshape(nodes, lm)
+        paired = sum(min(n, 4) / 4 * radius ** 2 * float(np.sum(w * (np.conj(K[n]) * sigma).real))
+                     for n in range(nodes))
+        assert abs(paired - v) < 1e-8 * abs(v), (name, paired, v)
+        density = np.fromfile(tmp_path / "kernels" / f"{name}_viscosity_kernels.bin")
+        assert density.size == op.values and np.all(np.isfinite(density)) and np.max(np.abs(density)) > 0
