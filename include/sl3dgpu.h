@@ -597,6 +597,20 @@ int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* tim
 int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* op, const double* times, int nodes, int scheme, int stride,
                             const double* loads, const double* u_dual, const double* phi_dual, double* load_kernels,
                             double* delta_gradient, double* objective, sl3dgpu_step_info* infos);
+/* The discrete tangent-linear run beside the same run
+ * (TangentLinearSolver3D, src/TangentLinear3D.cpp, its discrete method): the
+ * derivative of the surface U and phi at every node along a log-viscosity
+ * direction (delta_direction: one double per grid value, node-major as
+ * set_delta's samples, nullable) and along load directions (nodes x
+ * (l(l+1)/2 + m) complex host coefficients, nullable), each stage's tangent
+ * solve the step's own iteration. u, phi (nullable): the derivatives per
+ * node, the run's layout; infos: the forward steps'. Without an ocean, the
+ * fixed-point step (FP64 or mixed). With the adjoint:
+ * sum_n <u_dual_n, u_n> + <phi_dual_n, phi_n> = delta_gradient . direction
+ * + sum_n <load_kernels_n, load_direction_n>. */
+int sl3dgpu_v3d_tangent_run(sl3dgpu_v3d* op, const double* times, int nodes, int scheme, const double* loads,
+                            const double* delta_direction, const double* load_directions, double* u, double* phi,
+                            sl3dgpu_step_info* infos);
 /* The volume each grid sample stands for (GridCoupling's volume weight:
  * the radial quadrature weight jac w_q r^2 of its memory node times its
  * colatitude's weight 2 pi w_theta / nphi), one double per grid value. */

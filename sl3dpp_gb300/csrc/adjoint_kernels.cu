@@ -155,6 +155,53 @@ __global__ void AdjointMemoryKernel(AdjointMemoryArgs a) {
   }
 }
 
+__global__ void TangentKernel(TangentArgs a) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  const int P = static_cast<int>(a.values / a.fieldSize);
+  for (long long x = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; x < a.values; x += stride) {
+    const int node = static_cast<int>(x / a.fieldSize);
+    const double p = a.direction != nullptr ? a.direction[x] : 0.0;
+    const double2 t0 = a.t0[x], t1 = a.t1[x], b0 = a.b0[x], b1 = a.b1[x];
+    const double tr = a.tr[x], br = a.br[x];
+    double2 f0 = make_double2(0.0, 0.0), f1 = make_double2(0.0, 0.0);
+    double fr = 0.0, wdot = 0.0;
+    for (int k = 0; k < a.branches; ++k) {
+      const double mu = a.muBranch[static_cast<long long>(k) * P + node];
+      const double h = a.dt * (a.itauRef[static_cast<long long>(k) * P + node] * a.factor[x]);
+      double e, alpha, beta, de, dalpha, dbeta;
+      WeightsAndSlopes(a.scheme, h, e, alpha, beta, de, dalpha, dbeta);
+      const double hdot = -h * p;
+      if (a.finish) {
+        const double bd = dbeta * hdot;
+        a.m0[k][x] = make_double2(a.m0[k][x].x + beta * t0.x + bd * b0.x, a.m0[k][x].y + beta * t0.y + bd * b0.y);
+        a.m1[k][x] = make_double2(a.m1[k][x].x + beta * t1.x + bd * b1.x, a.m1[k][x].y + beta * t1.y + bd * b1.y);
+        a.mr[k][x] += beta * tr + bd * br;
+        continue;
+      }
+      const double ed = de * hdot, ad = dalpha * hdot;
+      const double2 s0 = a.s0[k][x], s1 = a.s1[k][x], a0 = a.a0[x], a1 = a.a1[x];
+      const double sr = a.sr[k][x], ar = a.ar[x];
+      const double2 m0 = make_double2(e * a.m0[k][x].x + alpha * t0.x + ed * s0.x + ad * a0.x,
+                                      e * a.m0[k][x].y + alpha * t0.y + ed * s0.y + ad * a0.y);
+      const double2 m1 = make_double2(e * a.m1[k][x].x + alpha * t1.x + ed * s1.x + ad * a1.x,
+                                      e * a.m1[k][x].y + alpha * t1.y + ed * s1.y + ad * a1.y);
+      const double mr = e * a.mr[k][x] + alpha * tr + ed * sr + ad * ar;
+      a.m0[k][x] = m0;
+      a.m1[k][x] = m1;
+      a.mr[k][x] = mr;
+      f0 = make_double2(f0.x + mu * m0.x, f0.y + mu * m0.y);
+      f1 = make_double2(f1.x + mu * m1.x, f1.y + mu * m1.y);
+      fr += mu * mr;
+      wdot += mu * dbeta * hdot;
+    }
+    if (!a.finish) {
+      a.f0[x] = make_double2(f0.x + wdot * b0.x, f0.y + wdot * b0.y);
+      a.f1[x] = make_double2(f1.x + wdot * b1.x, f1.y + wdot * b1.y);
+      a.fr[x] = fr + wdot * br;
+    }
+  }
+}
+
 __global__ void ScaleKernel(long long n, double s, double* y) {
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n; i += stride) y[i] *= s;
@@ -190,6 +237,11 @@ void LaunchAdjointStrainDual(const AdjointStrainArgs& a, cudaStream_t stream) {
 void LaunchAdjointMemory(const AdjointMemoryArgs& a, cudaStream_t stream) {
   prof::Scope scope(prof::kStream, stream, 0.0, a.values * (a.branches * 120.0 + 136.0));
   AdjointMemoryKernel<<<Blocks(a.values), 256, 0, stream>>>(a);
+}
+
+void LaunchTangent(const TangentArgs& a, cudaStream_t stream) {
+  prof::Scope scope(prof::kStream, stream, 0.0, a.values * (a.branches * (a.finish ? 80.0 : 120.0) + 120.0));
+  TangentKernel<<<Blocks(a.values), 256, 0, stream>>>(a);
 }
 
 void LaunchScale(long long n, double a, double* y, cudaStream_t stream) {

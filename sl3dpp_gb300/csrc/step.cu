@@ -292,6 +292,24 @@ class Viscoelastic3DGpu {
     int count[3] = {0, 0, 0};
     bool ready = false;
   } adj;
+  // The tangent-linear run (TangentLinearSolver3D's discrete run) beside
+  // its forward run, stage by stage: the tangent memory and strain on the
+  // grid at every node, each stage's tangent solve the step's own iteration
+  // with the tangent's fixed force and load channel.
+  struct TangentBuffers {
+    std::vector<GridTensor> m, hold;  // tangent memory per branch; Sdirk2's held start
+    GridTensor d, fixed;              // the tangent strain; a stage's fixed force
+    Dev<double> direction;            // p per grid value
+    Dev<double2> load0, load1, loadMid;
+    V3dState prev, first, end;        // the forward's start, first stage and end states
+    bool ready = false;
+  } tan;
+  int AllocAdjoint();
+  int ForwardFields(const V3dState& in, const V3dState& end);
+  int TangentStage(V3dState& in, const V3dState& end, double dt, int scheme, const double2* loadDot,
+                   sl3dgpu_step_info& info);
+  int TangentRun(const double* times, int nodes, int scheme, const double* loads, const double* direction,
+                 const double* loadDirections, double* u, double* phi, sl3dgpu_step_info* infos);
   int CopyState(const V3dState& from, V3dState& to);
   int StageAdjoint(V3dState& in, const V3dState& end, double dt, int scheme, bool measured, int kind,
                    sl3dgpu_step_info& info);
@@ -3128,6 +3146,36 @@ int Viscoelastic3DGpu::CopyState(const V3dState& from, V3dState& to) {
 // = u^T (F An(d-bar + W zeta) + S^T g) and the gradient in delta through
 // e, alpha, beta (W's share folded into M). The stage's weights are
 // StartStage's own, recomputed from the start state.
+// The stage's forward fields on the grid at every node (adj.startM,
+// startD, endD): the memory as the state holds it at the lateral nodes and
+// synthesised from its coefficients elsewhere, the strains from their
+// coefficients.
+int Viscoelastic3DGpu::ForwardFields(const V3dState& in, const V3dState& end) {
+  const int p0 = lateralFirst, p1 = lateralEnd;
+  const long long begin = p0 * fieldSize, span = static_cast<long long>(p1 - p0) * fieldSize;
+  for (int k = 0; k < K; ++k) {
+    if (span > 0) {
+      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].c0.p + begin, in.m[k].c0.p + begin, span * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, stream));
+      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].c1.p + begin, in.m[k].c1.p + begin, span * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, stream));
+      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].r.p + begin, in.m[k].r.p + begin, span * sizeof(double),
+                                cudaMemcpyDeviceToDevice, stream));
+    }
+    if (p0 > 0) SL3D_TRY(SynthesiseRange(in.mSpec[k].p, adj.startM[k], 0, p0));
+    if (p1 < P) SL3D_TRY(SynthesiseRange(in.mSpec[k].p, adj.startM[k], p1, P - p1));
+  }
+  if (in.hasCoeffs) {
+    SL3D_TRY(SynthesiseRange(in.coeffs.p, adj.startD, 0, P));
+  } else {
+    SL3D_CUDA(cudaMemsetAsync(adj.startD.c0.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(adj.startD.c1.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(adj.startD.r.p, 0, values * sizeof(double), stream));
+  }
+  SL3D_TRY(SynthesiseRange(end.coeffs.p, adj.endD, 0, P));
+  return SL3DGPU_OK;
+}
+
 // The next stage's start guess (1 - c) a + c b in the warm-start buffer
 // (b null: a itself), armed for the stage.
 int Viscoelastic3DGpu::ArmGuess(const double2* a, const double2* b, double c) {
@@ -3230,31 +3278,7 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const V3dState& end, double dt
   SL3D_CHECK_LAUNCH();
   LaunchLoadDual(geo, f->units.p, f->unitOffset.p, rhsSph.p, adj.sigma.p, stream);
   SL3D_CHECK_LAUNCH();
-  // The stage's forward fields on the grid at every node: the memory as the
-  // state holds it at the lateral nodes and synthesised from its
-  // coefficients elsewhere, the strains from their coefficients.
-  const int p0 = lateralFirst, p1 = lateralEnd;
-  const long long begin = p0 * fieldSize, span = static_cast<long long>(p1 - p0) * fieldSize;
-  for (int k = 0; k < K; ++k) {
-    if (span > 0) {
-      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].c0.p + begin, in.m[k].c0.p + begin, span * sizeof(double2),
-                                cudaMemcpyDeviceToDevice, stream));
-      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].c1.p + begin, in.m[k].c1.p + begin, span * sizeof(double2),
-                                cudaMemcpyDeviceToDevice, stream));
-      SL3D_CUDA(cudaMemcpyAsync(adj.startM[k].r.p + begin, in.m[k].r.p + begin, span * sizeof(double),
-                                cudaMemcpyDeviceToDevice, stream));
-    }
-    if (p0 > 0) SL3D_TRY(SynthesiseRange(in.mSpec[k].p, adj.startM[k], 0, p0));
-    if (p1 < P) SL3D_TRY(SynthesiseRange(in.mSpec[k].p, adj.startM[k], p1, P - p1));
-  }
-  if (in.hasCoeffs) {
-    SL3D_TRY(SynthesiseRange(in.coeffs.p, adj.startD, 0, P));
-  } else {
-    SL3D_CUDA(cudaMemsetAsync(adj.startD.c0.p, 0, values * sizeof(double2), stream));
-    SL3D_CUDA(cudaMemsetAsync(adj.startD.c1.p, 0, values * sizeof(double2), stream));
-    SL3D_CUDA(cudaMemsetAsync(adj.startD.r.p, 0, values * sizeof(double), stream));
-  }
-  SL3D_TRY(SynthesiseRange(end.coeffs.p, adj.endD, 0, P));
+  SL3D_TRY(ForwardFields(in, end));
   // the start's memory and strain duals, the gradient
   AdjointMemoryArgs ma{};
   ma.values = values;
@@ -3294,6 +3318,230 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const V3dState& end, double dt
   return SL3DGPU_OK;
 }
 
+// One tangent-linear stage beside its forward stage (in -> end, already
+// stepped): the tangent memory's decay and the fixed force of it and of W'
+// d_end, the tangent solve (the step's own iteration from a zero strain,
+// the tangent load in the load channel), the tangent end strain and the
+// memory's advance.
+int Viscoelastic3DGpu::TangentStage(V3dState& in, const V3dState& end, double dt, int scheme,
+                                    const double2* loadDot, sl3dgpu_step_info& info) {
+  Flavour* f = nullptr;
+  SL3D_TRY(StartStage(in, adj.scratch, dt, scheme, nullptr, &f));
+  SL3D_TRY(ForwardFields(in, end));
+  TangentArgs ta{};
+  ta.values = values;
+  ta.fieldSize = fieldSize;
+  ta.branches = K;
+  ta.scheme = scheme == static_cast<int>(Scheme::BackwardEuler) ? 1 : 0;
+  ta.dt = dt;
+  ta.muBranch = muBranch.p;
+  ta.itauRef = itauRef.p;
+  ta.factor = factor.p;
+  ta.direction = tan.direction.p;
+  for (int k = 0; k < K; ++k) {
+    ta.m0[k] = tan.m[k].c0.p;
+    ta.m1[k] = tan.m[k].c1.p;
+    ta.mr[k] = tan.m[k].r.p;
+    ta.s0[k] = adj.startM[k].c0.p;
+    ta.s1[k] = adj.startM[k].c1.p;
+    ta.sr[k] = adj.startM[k].r.p;
+  }
+  ta.t0 = tan.d.c0.p;
+  ta.t1 = tan.d.c1.p;
+  ta.tr = tan.d.r.p;
+  ta.a0 = adj.startD.c0.p;
+  ta.a1 = adj.startD.c1.p;
+  ta.ar = adj.startD.r.p;
+  ta.b0 = adj.endD.c0.p;
+  ta.b1 = adj.endD.c1.p;
+  ta.br = adj.endD.r.p;
+  ta.f0 = tan.fixed.c0.p;
+  ta.f1 = tan.fixed.c1.p;
+  ta.fr = tan.fixed.r.p;
+  LaunchTangent(ta, stream);
+  SL3D_CHECK_LAUNCH();
+  SL3D_TRY(AnalyseRange(tan.fixed, fixedS.p, 0, P));
+  SL3D_CUDA(cudaMemcpyAsync(analysedStart.p, fixedS.p, spectralComplex * sizeof(double2), cudaMemcpyDeviceToDevice,
+                            stream));
+  SL3D_CUDA(cudaMemsetAsync(s.p, 0, spectralComplex * sizeof(double2), stream));
+  stageGuess = nullptr;
+  info = sl3dgpu_step_info{};
+  if (options.precision == 1) {
+    LaunchCast(values, weight.p, weight32.p, stream);
+    SL3D_CHECK_LAUNCH();
+    SL3D_TRY(ConvergeMixed(*f, loadDot, info));
+  } else {
+    SL3D_TRY(Converge(*f, loadDot, info));
+  }
+  if (grid->emulateFp64) SL3D_TRY(grid->TensorCoreStatus(stream));
+  if (!info.converged) {
+    SetError("v3d tangent: a stage's tangent solve did not converge");
+    return SL3DGPU_ERR_UNCONVERGED;
+  }
+  SL3D_TRY(SynthesiseRange(s.p, tan.d, 0, P));
+  ta.finish = true;
+  LaunchTangent(ta, stream);
+  SL3D_CHECK_LAUNCH();
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::TangentRun(const double* times, int nodes, int scheme, const double* loads,
+                                  const double* direction, const double* loadDirections, double* u, double* phi,
+                                  sl3dgpu_step_info* infos) {
+  if (staticMode || ocean.on || options.solver != 0) {
+    SetError("v3d tangent: built for the fixed-point step (solver 0, FP64 or mixed) without an ocean");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  if (nodes < 1 || times == nullptr || loads == nullptr || scheme < 0 || scheme > 2) {
+    SetError("v3d tangent: at least one node, times, loads and a scheme of 0, 1 or 2");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  for (int k = 1; k < nodes; ++k)
+    if (!(times[k] >= times[k - 1])) {
+      SetError("v3d: node times must not decrease");
+      return SL3DGPU_ERR_ARGUMENT;
+    }
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  SL3D_TRY(AllocAdjoint());
+  if (!tan.ready) {
+    tan.m.resize(K);
+    tan.hold.resize(K);
+    for (int k = 0; k < K; ++k) {
+      SL3D_CUDA(tan.m[k].Alloc(values));
+      SL3D_CUDA(tan.hold[k].Alloc(values));
+    }
+    SL3D_CUDA(tan.d.Alloc(values));
+    SL3D_CUDA(tan.fixed.Alloc(values));
+    SL3D_CUDA(tan.direction.Alloc(values));
+    SL3D_CUDA(tan.load0.Alloc(lm));
+    SL3D_CUDA(tan.load1.Alloc(lm));
+    SL3D_CUDA(tan.loadMid.Alloc(lm));
+    SL3D_TRY(AllocState(tan.first));
+    SL3D_TRY(AllocState(tan.end));
+    tan.ready = true;
+  }
+  if (direction)
+    SL3D_CUDA(cudaMemcpyAsync(tan.direction.p, direction, values * sizeof(double), cudaMemcpyHostToDevice, stream));
+  else
+    SL3D_CUDA(cudaMemsetAsync(tan.direction.p, 0, values * sizeof(double), stream));
+  auto zeroTensor = [&](GridTensor& t) -> int {
+    SL3D_CUDA(cudaMemsetAsync(t.c0.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(t.c1.p, 0, values * sizeof(double2), stream));
+    SL3D_CUDA(cudaMemsetAsync(t.r.p, 0, values * sizeof(double), stream));
+    return SL3DGPU_OK;
+  };
+  for (int k = 0; k < K; ++k) SL3D_TRY(zeroTensor(tan.m[k]));
+  SL3D_TRY(zeroTensor(tan.d));
+  SL3D_TRY(ZeroState(tan.prev));
+  SL3D_TRY(zeroTensor(tan.prev.strain));
+  for (int k = 0; k < nodes; ++k) {
+    const double* l1 = loads + 2 * lm * k;
+    const double* l0 = k > 0 ? loads + 2 * lm * (k - 1) : l1;
+    const double dt = k > 0 ? times[k] - times[k - 1] : 0.0;
+    SL3D_CUDA(cudaMemcpyAsync(sigma0.p, l0, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    SL3D_CUDA(cudaMemcpyAsync(sigma1.p, l1, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+    const double2* dot0 = nullptr;
+    const double2* dot1 = nullptr;
+    if (loadDirections) {
+      const double* t1 = loadDirections + 2 * lm * k;
+      const double* t0 = k > 0 ? loadDirections + 2 * lm * (k - 1) : t1;
+      SL3D_CUDA(cudaMemcpyAsync(tan.load0.p, t0, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+      SL3D_CUDA(cudaMemcpyAsync(tan.load1.p, t1, lm * sizeof(double2), cudaMemcpyHostToDevice, stream));
+      dot0 = tan.load0.p;
+      dot1 = tan.load1.p;
+    }
+    sl3dgpu_step_info info{}, tangent{};
+    stageGuess = nullptr;
+    if (scheme != 2 || dt == 0.0) {
+      const int one = scheme == 2 ? 1 : scheme;
+      SL3D_TRY(StepOnce(tan.prev, tan.end, dt, one, sigma0.p, sigma1.p, info));
+      SL3D_TRY(TangentStage(tan.prev, tan.end, dt, one, dot1, tangent));
+    } else {
+      const double gamma = host::kSdirk2Gamma, h = gamma * dt, r = (1.0 - gamma) / gamma;
+      LaunchBlend(static_cast<long long>(lm), gamma, sigma0.p, sigma1.p, sigmaMid.p, stream);
+      SL3D_CHECK_LAUNCH();
+      const double2* dotMid = nullptr;
+      if (dot0) {
+        LaunchBlend(static_cast<long long>(lm), gamma, dot0, dot1, tan.loadMid.p, stream);
+        SL3D_CHECK_LAUNCH();
+        dotMid = tan.loadMid.p;
+      }
+      sl3dgpu_step_info i1{};
+      SL3D_TRY(StepOnce(tan.prev, tan.first, h, 1, sigma0.p, sigmaMid.p, i1));
+      for (int b = 0; b < K; ++b) {
+        SL3D_CUDA(cudaMemcpyAsync(tan.hold[b].c0.p, tan.m[b].c0.p, values * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                  stream));
+        SL3D_CUDA(cudaMemcpyAsync(tan.hold[b].c1.p, tan.m[b].c1.p, values * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                  stream));
+        SL3D_CUDA(cudaMemcpyAsync(tan.hold[b].r.p, tan.m[b].r.p, values * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  stream));
+      }
+      SL3D_TRY(TangentStage(tan.prev, tan.first, h, 1, dotMid, tangent));
+      // the second stage's memory (1 - r) m_n + r Y1, forward and tangent
+      const long long begin = lateralFirst * fieldSize, stop = static_cast<long long>(lateralEnd) * fieldSize;
+      for (int b = 0; b < K; ++b) {
+        if (stop > begin) {
+          LaunchStageCombine(stop - begin, r, tan.prev.m[b].c0.p + begin, tan.prev.m[b].c1.p + begin,
+                             tan.prev.m[b].r.p + begin, tan.first.m[b].c0.p + begin, tan.first.m[b].c1.p + begin,
+                             tan.first.m[b].r.p + begin, stream);
+          SL3D_CHECK_LAUNCH();
+        }
+        LaunchSpectralCombine(rows0 + rows1 + rowsR, P, lateralFirst, lateralEnd, r, tan.prev.mSpec[b].p,
+                              tan.first.mSpec[b].p, stream);
+        SL3D_CHECK_LAUNCH();
+        LaunchStageCombine(values, r, tan.hold[b].c0.p, tan.hold[b].c1.p, tan.hold[b].r.p, tan.m[b].c0.p,
+                           tan.m[b].c1.p, tan.m[b].r.p, stream);
+        SL3D_CHECK_LAUNCH();
+      }
+      sl3dgpu_step_info t1{};
+      SL3D_TRY(StepOnce(tan.first, tan.end, h, 1, sigmaMid.p, sigma1.p, info));
+      SL3D_TRY(TangentStage(tan.first, tan.end, h, 1, dot1, t1));
+      info.converged = info.converged && i1.converged;
+    }
+    if (infos) infos[k] = info;
+    if (!info.converged) {
+      SetError("v3d tangent: a step of the forward run did not converge");
+      return SL3DGPU_ERR_UNCONVERGED;
+    }
+    if (u) SL3D_TRY(Surface(0, u + 2 * lm * k));
+    if (phi) SL3D_TRY(Surface(2, phi + 2 * lm * k));
+    std::swap(tan.prev, tan.end);
+  }
+  return SL3DGPU_OK;
+}
+
+int Viscoelastic3DGpu::AllocAdjoint() {
+  const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
+  if (!adj.ready) {
+    adj.m.resize(K);
+    adj.hold.resize(K);
+    adj.startM.resize(K);
+    for (int k = 0; k < K; ++k) {
+      SL3D_CUDA(adj.m[k].Alloc(values));
+      SL3D_CUDA(adj.hold[k].Alloc(values));
+      SL3D_CUDA(adj.startM[k].Alloc(values));
+    }
+    SL3D_CUDA(adj.startD.Alloc(values));
+    SL3D_CUDA(adj.endD.Alloc(values));
+    SL3D_CUDA(adj.d.Alloc(values));
+    SL3D_CUDA(adj.bar.Alloc(values));
+    SL3D_CUDA(adj.qSph.Alloc(rhsSphComplex));
+    SL3D_CUDA(adj.qTor.Alloc(std::max<long long>(rhsTorComplex, 1)));
+    SL3D_CUDA(adj.gU.Alloc(lm));
+    SL3D_CUDA(adj.gPhi.Alloc(lm));
+    SL3D_CUDA(adj.sigma.Alloc(lm));
+    SL3D_CUDA(adj.grad.Alloc(values));
+    SL3D_TRY(AllocState(adj.scratch));
+    SL3D_TRY(AllocState(adj.stage));
+    for (int i = 0; i < 3; ++i) {
+      SL3D_CUDA(adj.last[i].Alloc(spectralComplex));
+      SL3D_CUDA(adj.before[i].Alloc(spectralComplex));
+    }
+    adj.ready = true;
+  }
+  return SL3DGPU_OK;
+}
+
 int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, int stride, const double* loads,
                                   const double* uDual, const double* phiDual, double* loadKernels,
                                   double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
@@ -3323,33 +3571,7 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
                                     const double* uDual, const double* phiDual, double* loadKernels,
                                     double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
   const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
-  if (!adj.ready) {
-    adj.m.resize(K);
-    adj.hold.resize(K);
-    adj.startM.resize(K);
-    for (int k = 0; k < K; ++k) {
-      SL3D_CUDA(adj.m[k].Alloc(values));
-      SL3D_CUDA(adj.hold[k].Alloc(values));
-      SL3D_CUDA(adj.startM[k].Alloc(values));
-    }
-    SL3D_CUDA(adj.startD.Alloc(values));
-    SL3D_CUDA(adj.endD.Alloc(values));
-    SL3D_CUDA(adj.d.Alloc(values));
-    SL3D_CUDA(adj.bar.Alloc(values));
-    SL3D_CUDA(adj.qSph.Alloc(rhsSphComplex));
-    SL3D_CUDA(adj.qTor.Alloc(std::max<long long>(rhsTorComplex, 1)));
-    SL3D_CUDA(adj.gU.Alloc(lm));
-    SL3D_CUDA(adj.gPhi.Alloc(lm));
-    SL3D_CUDA(adj.sigma.Alloc(lm));
-    SL3D_CUDA(adj.grad.Alloc(values));
-    SL3D_TRY(AllocState(adj.scratch));
-    SL3D_TRY(AllocState(adj.stage));
-    for (int i = 0; i < 3; ++i) {
-      SL3D_CUDA(adj.last[i].Alloc(spectralComplex));
-      SL3D_CUDA(adj.before[i].Alloc(spectralComplex));
-    }
-    adj.ready = true;
-  }
+  SL3D_TRY(AllocAdjoint());
   auto zeroTensor = [&](GridTensor& t) -> int {
     SL3D_CUDA(cudaMemsetAsync(t.c0.p, 0, values * sizeof(double2), stream));
     SL3D_CUDA(cudaMemsetAsync(t.c1.p, 0, values * sizeof(double2), stream));
@@ -4051,6 +4273,17 @@ extern "C" int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* h, const double* times, int 
   }
   return h->op.AdjointRun(times, nodes, scheme, stride, loads, u_dual, phi_dual, load_kernels, delta_gradient,
                           objective, infos);
+}
+
+extern "C" int sl3dgpu_v3d_tangent_run(sl3dgpu_v3d* h, const double* times, int nodes, int scheme,
+                                       const double* loads, const double* delta_direction,
+                                       const double* load_directions, double* u, double* phi,
+                                       sl3dgpu_step_info* infos) {
+  if (h == nullptr) {
+    SetError("v3d tangent: null operator");
+    return SL3DGPU_ERR_ARGUMENT;
+  }
+  return h->op.TangentRun(times, nodes, scheme, loads, delta_direction, load_directions, u, phi, infos);
 }
 
 extern "C" int sl3dgpu_v3d_sample_volumes(const sl3dgpu_v3d* h, double* out) {

@@ -359,4 +359,36 @@ void LaunchAdjointMemory(const AdjointMemoryArgs& a, cudaStream_t stream);
 // y *= a (n reals).
 void LaunchScale(long long n, double a, double* y, cudaStream_t stream);
 
+// The tangent-linear stage (TangentLinearSolver3D's discrete run) along a
+// log-viscosity direction p: h' = -h p, e.g. e' = (de/dh) h'. Start: the
+// tangent memory's decay tm~_k = e_k tm_k + alpha_k td_start + e'_k m_k +
+// alpha'_k d_start, in place, and its fixed force sum_k mu_k tm~_k + W' d_end
+// (W' = sum_k mu_k beta'_k) into `fixed`. Finish (finish = true): tm_k =
+// tm~_k + beta_k td_end + beta'_k d_end, in place.
+struct TangentArgs {
+  long long values, fieldSize;
+  int branches, scheme;
+  double dt;
+  bool finish;
+  const double* muBranch;   // [k][P]
+  const double* itauRef;    // [k][P]
+  const double* factor;     // exp(-delta)
+  const double* direction;  // p per grid value
+  double2* m0[2];           // tangent memory per branch, in place
+  double2* m1[2];
+  double* mr[2];
+  const double2 *t0, *t1;   // the tangent strain: the start's (start) or the end's (finish)
+  const double* tr;
+  const double2* s0[2];     // the stage's start memory
+  const double2* s1[2];
+  const double* sr[2];
+  const double2 *a0, *a1;   // the start strain
+  const double* ar;
+  const double2 *b0, *b1;   // the end strain
+  const double* br;
+  double2 *f0, *f1;         // the fixed force (start)
+  double* fr;
+};
+void LaunchTangent(const TangentArgs& a, cudaStream_t stream);
+
 }  // namespace sl3dgpu

@@ -115,6 +115,7 @@ def _signatures():
         "sl3dgpu_v3d_run": (i, [v, v, P_double, i, i, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_adjoint_run": (i, [v, P_double, i, i, i, v, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_sample_volumes": (i, [v, v]),
+        "sl3dgpu_v3d_tangent_run": (i, [v, P_double, i, i, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_run_many": (i, [i, v, v, v, v, i, v, v, v, v, i, v]),
         "sl3dgpu_v3d_state_coefficients_host": (i, [v, v, v]),
         "sl3dgpu_v3d_assembled_band": (i, [v, i, d, i, i, P_double, ctypes.c_longlong, P_int, P_int]),
@@ -664,6 +665,32 @@ class Evolution3D:
             kernels.ctypes.data, None if grad is None else grad.ctypes.data, ctypes.byref(objective), infos))
         return {"objective": objective.value, "load_kernels": kernels, "delta_gradient": grad,
                 "infos": [infos[k] for k in range(n)]}
+
+    def Tangent(self, times, loads, delta_direction=None, load_directions=None):
+        """The discrete tangent-linear run beside Run from a zero state
+        (TangentLinearSolver3D's discrete method): the derivative of U and
+        phi at every node along a log-viscosity direction over every grid
+        sample and along per-node load directions (either None)."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        loads = np.ascontiguousarray(loads, dtype=np.complex128)
+        n = times.size
+        lm = (self.op.lmax + 1) * (self.op.lmax + 2) // 2
+        if loads.shape != (n, lm):
+            raise ValueError("one load (l(l+1)/2 + m coefficients) per node")
+        p = None if delta_direction is None else np.ascontiguousarray(delta_direction, dtype=np.float64).ravel()
+        if p is not None and p.size != self.op.values:
+            raise ValueError("one direction value per grid sample")
+        dl = None if load_directions is None else np.ascontiguousarray(load_directions, dtype=np.complex128)
+        if dl is not None and dl.shape != (n, lm):
+            raise ValueError("one load direction per node")
+        U = np.zeros((n, lm), dtype=np.complex128)
+        phi = np.zeros((n, lm), dtype=np.complex128)
+        infos = (StepInfo * max(n, 1))()
+        check(lib().sl3dgpu_v3d_tangent_run(self.op._h, times.ctypes.data_as(P_double), n, self.scheme,
+                                            loads.ctypes.data, None if p is None else p.ctypes.data,
+                                            None if dl is None else dl.ctypes.data, U.ctypes.data, phi.ctypes.data,
+                                            infos))
+        return {"U": U, "phi": phi, "infos": [infos[k] for k in range(n)]}
 
     def Instantaneous(self, load):
         out = self.Run(np.zeros(1), np.asarray(load)[None, :])

@@ -14,7 +14,9 @@ over every node (the sweep forms it at nodes outside delta's range too):
 Richardson-extrapolated central differences of the forward run, 1e-6. Each
 for the three schemes, and the mixed form for Sdirk2. A record stride (the
 forward states kept every stride-th node, the gaps rebuilt) changes nothing
-but the memory held."""
+but the memory held. The tangent-linear run (TangentLinearSolver3D's
+discrete method) pairs with the adjoint to 1e-8 along a direction in the
+log-viscosity and the loads together."""
 
 import numpy as np
 import pytest
@@ -149,3 +151,33 @@ def test_gpu_record_stride_gives_the_kernels_of_every_node_kept(gpu, stride):
     assert abs(sparse["objective"] - every["objective"]) < 1e-12 * abs(every["objective"])
     assert rel(sparse["load_kernels"], every["load_kernels"]) < 1e-9
     assert rel(sparse["delta_gradient"], every["delta_gradient"]) < 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme,precision", CASES)
+def test_gpu_adjoint_pairs_with_the_tangent_linear_run(gpu, scheme, precision):
+    """The reference's tight gate (TestDiscreteAdjoint3D): the adjoint's
+    gradient and load kernels paired with a direction -- in the log-viscosity
+    over every node and in the loads, together -- equal the objective's
+    derivative from the tangent-linear run along it (1e-8); along loads
+    alone the tangent run is the forward run under them."""
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D
+
+    lmax, nodes = 8, 4
+    o, g, times, loads, gU, gPhi = _run(lmax, scheme, nodes, precision, seed=21)
+    ev = Evolution3D(g, scheme)
+    adj = ev.Adjoint(times, loads, gU, gPhi)
+    rng = np.random.default_rng(23)
+    pattern = O.synthesise_real(lmax, o.theta, o.nphi, real_coefficients(lmax, rng, 1)[0] / (lmax + 1))
+    radial = 1.0 + 0.5 * np.cos(5.0 * np.asarray(o.radius))
+    p = (radial[:, None] * np.asarray(pattern).ravel()[None, :]).ravel()
+    dL = 0.1 * np.max(np.abs(loads)) * real_coefficients(lmax, rng, nodes)
+    tl = ev.Tangent(times, loads, p, dL)
+    assert all(i.converged for i in tl["infos"])
+    lhs = _objective(lmax, tl, gU, gPhi)
+    rhs = float(adj["delta_gradient"] @ p) + sum(pairing(lmax, adj["load_kernels"][k], dL[k]) for k in range(nodes))
+    assert abs(lhs - rhs) < 1e-8 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    # along loads alone: the forward run under them
+    alone = ev.Tangent(times, loads, None, dL)
+    run = ev.Run(times, dL)
+    assert rel(alone["U"], run["U"]) < 1e-9 and rel(alone["phi"], run["phi"]) < 1e-9
