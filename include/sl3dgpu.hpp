@@ -1073,6 +1073,7 @@ class Evolution3D {
   Scheme scheme_;
   bool migrating_ = false;
   friend class AdjointSolver3D;
+  friend class TangentLinearSolver3D;
 };
 
 // -- the discrete 3D adjoint -----------------------------------------------------------------------------
@@ -1149,6 +1150,55 @@ class AdjointSolver3D {
  private:
   const Evolution3D* evolution_;
   Options options_;
+};
+
+// TangentLinearSolver3D's discrete run (src/TangentLinear3D.cpp) for the
+// evolution without an ocean: the derivative of the surface U and phi at
+// every node along a log-viscosity direction over every grid sample
+// (empty: none) and along a load direction (empty callable: none), beside
+// the forward run from a zero state under the loads.
+class TangentLinearSolver3D {
+ public:
+  struct Derivative {
+    std::vector<std::vector<Complex>> U, phi;  // per node, (l, m >= 0)
+  };
+  explicit TangentLinearSolver3D(const Evolution3D& evolution) : evolution_(&evolution) {}
+
+  [[nodiscard]] Derivative Run(std::span<const double> times, const Viscoelastic3D::LoadCallable3D& load,
+                               std::span<const double> deltaDirection,
+                               const Viscoelastic3D::LoadCallable3D& loadDirection = {}) const {
+    Viscoelastic3D& op = *evolution_->op_;
+    const int n = static_cast<int>(times.size());
+    const std::size_t lm = evolution_->Coefficients();
+    if (!deltaDirection.empty() && deltaDirection.size() != op.GridValues())
+      throw std::invalid_argument("the direction has one value per grid sample");
+    std::vector<Complex> loads(lm * n), directions(loadDirection ? lm * n : 0), U(lm * n), phi(lm * n);
+    for (int k = 0; k < n; ++k) {
+      const auto flat = gpu::Flatten(load, op.LMax(), times[k]);
+      std::copy(flat.begin(), flat.end(), loads.begin() + lm * k);
+      if (loadDirection) {
+        const auto d = gpu::Flatten(loadDirection, op.LMax(), times[k]);
+        std::copy(d.begin(), d.end(), directions.begin() + lm * k);
+      }
+    }
+    gpu::Check(sl3dgpu_v3d_tangent_run(op.Handle(), times.data(), n, static_cast<int>(evolution_->scheme_),
+                                       reinterpret_cast<const double*>(loads.data()),
+                                       deltaDirection.empty() ? nullptr : deltaDirection.data(),
+                                       loadDirection ? reinterpret_cast<const double*>(directions.data()) : nullptr,
+                                       reinterpret_cast<double*>(U.data()), reinterpret_cast<double*>(phi.data()),
+                                       nullptr));
+    Derivative out;
+    out.U.resize(n);
+    out.phi.resize(n);
+    for (int k = 0; k < n; ++k) {
+      out.U[k].assign(U.begin() + lm * k, U.begin() + lm * (k + 1));
+      out.phi[k].assign(phi.begin() + lm * k, phi.begin() + lm * (k + 1));
+    }
+    return out;
+  }
+
+ private:
+  const Evolution3D* evolution_;
 };
 
 // -- the static 3D solve ----------------------------------------------------------------------------------

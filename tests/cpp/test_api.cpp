@@ -650,6 +650,18 @@ void Adjoint(const sl3dpp::Rheology& body) {
              std::abs(paired - objective) < 1e-8 * std::abs(objective) && finite && largest > 0.0,
          "AdjointSolver3D load kernels pair with the loads to the forward run's objective (" +
              std::to_string(std::abs(paired - objective) / std::abs(objective)) + ")");
+  // TangentLinearSolver3D along a log-viscosity direction: the objective's
+  // derivative is the gradient paired with it
+  std::vector<double> direction(op.GridValues());
+  for (std::size_t x = 0; x < direction.size(); ++x) direction[x] = std::sin(0.37 * static_cast<double>(x % 977));
+  const auto tangent = sl3dpp::TangentLinearSolver3D(evolution).Run(times, load, direction);
+  double derivative = 0.0, predicted = 0.0;
+  for (const auto& [node, m] : measurements)
+    derivative += pair(m.displacementDual, tangent.U[node]) + pair(m.potentialDual, tangent.phi[node]);
+  for (std::size_t x = 0; x < direction.size(); ++x) predicted += kernels.deltaGradient[x] * direction[x];
+  Expect(std::abs(derivative - predicted) < 1e-8 * std::max(std::abs(derivative), std::abs(predicted)),
+         "TangentLinearSolver3D pairs with AdjointSolver3D's gradient (" +
+             std::to_string(std::abs(derivative - predicted) / std::abs(predicted)) + ")");
 }
 
 }  // namespace
