@@ -587,6 +587,9 @@ int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* tim
  * (l(l+1)/2 + m) complex host coefficients (nullable, m = 0 parts real).
  * Out: load_kernels (required, the same layout), the load kernels
  * (Kernels::directLoadKernels): dJ = sum_n <load_kernels_n, dL_n>;
+ * tide_kernels (nullable, the same layout; Kernels::tideKernels): dJ =
+ * sum_n <tide_kernels_n, dpsi_n> for a tidal potential added to the run's
+ * tide channel (degree 1 none);
  * delta_gradient (nullable, one double per grid value, node-major as
  * set_delta's samples): dJ/d delta at each sample, dJ = sum_x
  * delta_gradient_x d delta_x -- divided by sl3dgpu_v3d_sample_volumes it
@@ -596,7 +599,8 @@ int sl3dgpu_v3d_run(sl3dgpu_v3d* op, sl3dgpu_v3d_state* state, const double* tim
  * FP64 or mixed); the transposed solves take the operator's rtol. */
 int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* op, const double* times, int nodes, int scheme, int stride,
                             const double* loads, const double* u_dual, const double* phi_dual, double* load_kernels,
-                            double* delta_gradient, double* objective, sl3dgpu_step_info* infos);
+                            double* tide_kernels, double* delta_gradient, double* objective,
+                            sl3dgpu_step_info* infos);
 /* The discrete tangent-linear run beside the same run
  * (TangentLinearSolver3D, src/TangentLinear3D.cpp, its discrete method): the
  * derivative of the surface U and phi at every node along a log-viscosity

@@ -1085,11 +1085,11 @@ struct Measurement3D {
   std::vector<Complex> displacementDual, potentialDual;
 };
 // The first-order kernels (Kernels3D, include/sl3dpp/Adjoint3D.hpp:104-140):
-// per node the direct-load kernel (dJ = sum_n <kernel_n, dL_n>); dJ/d delta
+// per node the direct-load and tide kernels (dJ = sum_n <kernel_n, dL_n>); dJ/d delta
 // per grid sample and its density per unit volume (logViscosityKernel3D,
 // the gradient over the samples' volumes); the objective of the forward run.
 struct Kernels3D {
-  std::vector<std::vector<Complex>> directLoadKernels;
+  std::vector<std::vector<Complex>> directLoadKernels, tideKernels;
   std::vector<double> deltaGradient, logViscosityKernel3D;
   double objective = 0.0;
 };
@@ -1128,7 +1128,7 @@ class AdjointSolver3D {
       }
     }
     Kernels3D out;
-    std::vector<Complex> kernels(lm * n);
+    std::vector<Complex> kernels(lm * n), tides(lm * n);
     const std::size_t values = op.GridValues();
     out.deltaGradient.resize(values);
     gpu::Check(sl3dgpu_v3d_adjoint_run(op.Handle(), times.data(), n, static_cast<int>(evolution_->scheme_),
@@ -1136,10 +1136,15 @@ class AdjointSolver3D {
                                        reinterpret_cast<const double*>(loads.data()),
                                        anyU ? reinterpret_cast<const double*>(u.data()) : nullptr,
                                        anyPhi ? reinterpret_cast<const double*>(phi.data()) : nullptr,
-                                       reinterpret_cast<double*>(kernels.data()), out.deltaGradient.data(),
+                                       reinterpret_cast<double*>(kernels.data()),
+                                       reinterpret_cast<double*>(tides.data()), out.deltaGradient.data(),
                                        &out.objective, nullptr));
     out.directLoadKernels.resize(n);
-    for (int k = 0; k < n; ++k) out.directLoadKernels[k].assign(kernels.begin() + lm * k, kernels.begin() + lm * (k + 1));
+    out.tideKernels.resize(n);
+    for (int k = 0; k < n; ++k) {
+      out.directLoadKernels[k].assign(kernels.begin() + lm * k, kernels.begin() + lm * (k + 1));
+      out.tideKernels[k].assign(tides.begin() + lm * k, tides.begin() + lm * (k + 1));
+    }
     std::vector<double> volume(values);
     gpu::Check(sl3dgpu_v3d_sample_volumes(op.Handle(), volume.data()));
     out.logViscosityKernel3D.resize(values);

@@ -986,7 +986,7 @@ int Kernel(const Config& c) {
                                   reinterpret_cast<const double*>(loads.data()),
                                   displacement ? reinterpret_cast<const double*>(dual.data()) : nullptr,
                                   displacement ? nullptr : reinterpret_cast<const double*>(dual.data()),
-                                  reinterpret_cast<double*>(kernels.data()),
+                                  reinterpret_cast<double*>(kernels.data()), nullptr,
                                   c.viscosityKernels ? gradient.data() : nullptr, &objective, nullptr),
           "adjoint");
     const double value = scale * objective;

@@ -283,7 +283,7 @@ class Viscoelastic3DGpu {
     GridTensor d, bar;                // the strain dual; the end strain's total dual
     std::vector<GridTensor> startM;   // the stage's start memory on the grid at every node
     GridTensor startD, endD;          // its start and end strain on the grid at every node
-    Dev<double2> qSph, qTor, gU, gPhi, sigma;
+    Dev<double2> qSph, qTor, gU, gPhi, sigma, tide;
     Dev<double> grad;
     V3dState scratch, stage;          // StartStage's output; Sdirk2's recomputed first stage
     // the last two converged dual strains per stage kind (one-stage, Sdirk2's
@@ -315,11 +315,11 @@ class Viscoelastic3DGpu {
                    sl3dgpu_step_info& info);
   int ArmGuess(const double2* a, const double2* b, double c);
   int AdjointRun(const double* times, int nodes, int scheme, int stride, const double* loads, const double* uDual,
-                 const double* phiDual, double* loadKernels, double* deltaGradient, double* objective,
-                 sl3dgpu_step_info* infos);
+                 const double* phiDual, double* loadKernels, double* tideKernels, double* deltaGradient,
+                 double* objective, sl3dgpu_step_info* infos);
   int AdjointSweep(const double* times, int nodes, int scheme, int stride, const double* loads, const double* uDual,
-                   const double* phiDual, double* loadKernels, double* deltaGradient, double* objective,
-                   sl3dgpu_step_info* infos);
+                   const double* phiDual, double* loadKernels, double* tideKernels, double* deltaGradient,
+                   double* objective, sl3dgpu_step_info* infos);
 
   ~Viscoelastic3DGpu() {
     for (auto& g : correctionGraphs)
@@ -3278,6 +3278,8 @@ int Viscoelastic3DGpu::StageAdjoint(V3dState& in, const V3dState& end, double dt
   SL3D_CHECK_LAUNCH();
   LaunchLoadDual(geo, f->units.p, f->unitOffset.p, rhsSph.p, adj.sigma.p, stream);
   SL3D_CHECK_LAUNCH();
+  LaunchLoadDual(geo, f->tideUnits.p, f->unitOffset.p, rhsSph.p, adj.tide.p, stream);  // the tide channel's
+  SL3D_CHECK_LAUNCH();
   SL3D_TRY(ForwardFields(in, end));
   // the start's memory and strain duals, the gradient
   AdjointMemoryArgs ma{};
@@ -3530,6 +3532,7 @@ int Viscoelastic3DGpu::AllocAdjoint() {
     SL3D_CUDA(adj.gU.Alloc(lm));
     SL3D_CUDA(adj.gPhi.Alloc(lm));
     SL3D_CUDA(adj.sigma.Alloc(lm));
+    SL3D_CUDA(adj.tide.Alloc(lm));
     SL3D_CUDA(adj.grad.Alloc(values));
     SL3D_TRY(AllocState(adj.scratch));
     SL3D_TRY(AllocState(adj.stage));
@@ -3544,7 +3547,8 @@ int Viscoelastic3DGpu::AllocAdjoint() {
 
 int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, int stride, const double* loads,
                                   const double* uDual, const double* phiDual, double* loadKernels,
-                                  double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
+                                  double* tideKernels, double* deltaGradient, double* objective,
+                                  sl3dgpu_step_info* infos) {
   if (staticMode || ocean.on || options.solver != 0) {
     SetError("v3d adjoint: built for the fixed-point step (solver 0, FP64 or mixed) without an ocean");
     return SL3DGPU_ERR_ARGUMENT;
@@ -3560,8 +3564,8 @@ int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, in
       SetError("v3d: node times must not decrease");
       return SL3DGPU_ERR_ARGUMENT;
     }
-  const int rc = AdjointSweep(times, nodes, scheme, stride, loads, uDual, phiDual, loadKernels, deltaGradient,
-                              objective, infos);
+  const int rc = AdjointSweep(times, nodes, scheme, stride, loads, uDual, phiDual, loadKernels, tideKernels,
+                              deltaGradient, objective, infos);
   passAddSph = passAddTor = nullptr;
   stageGuess = nullptr;
   return rc;
@@ -3569,7 +3573,8 @@ int Viscoelastic3DGpu::AdjointRun(const double* times, int nodes, int scheme, in
 
 int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, int stride, const double* loads,
                                     const double* uDual, const double* phiDual, double* loadKernels,
-                                    double* deltaGradient, double* objective, sl3dgpu_step_info* infos) {
+                                    double* tideKernels, double* deltaGradient, double* objective,
+                                    sl3dgpu_step_info* infos) {
   const size_t lm = static_cast<size_t>(options.lmax + 1) * (options.lmax + 2) / 2;
   SL3D_TRY(AllocAdjoint());
   auto zeroTensor = [&](GridTensor& t) -> int {
@@ -3660,11 +3665,18 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
   for (int k = 0; k < K; ++k) SL3D_TRY(zeroTensor(adj.m[k]));
   SL3D_TRY(zeroTensor(adj.d));
   SL3D_CUDA(cudaMemsetAsync(adj.grad.p, 0, values * sizeof(double), stream));
-  std::vector<double> kernels(2 * lm * nodes, 0.0), sigma(2 * lm);
+  std::vector<double> kernels(2 * lm * nodes, 0.0), tides(tideKernels ? 2 * lm * nodes : 0, 0.0), sigma(2 * lm),
+      tide(2 * lm);
+  // a stage's load and tide duals, c of them to the node (its end load's
+  // share of the stage's)
   auto addSigma = [&](int node, double c) -> int {
     SL3D_CUDA(cudaMemcpyAsync(sigma.data(), adj.sigma.p, lm * sizeof(double2), cudaMemcpyDeviceToHost, stream));
+    if (tideKernels)
+      SL3D_CUDA(cudaMemcpyAsync(tide.data(), adj.tide.p, lm * sizeof(double2), cudaMemcpyDeviceToHost, stream));
     SL3D_CUDA(cudaStreamSynchronize(stream));
     for (size_t i = 0; i < 2 * lm; ++i) kernels[2 * lm * node + i] += c * sigma[i];
+    if (tideKernels)
+      for (size_t i = 0; i < 2 * lm; ++i) tides[2 * lm * node + i] += c * tide[i];
     return SL3DGPU_OK;
   };
   const bool measured = uDual != nullptr || phiDual != nullptr;
@@ -3748,6 +3760,13 @@ int Viscoelastic3DGpu::AdjointSweep(const double* times, int nodes, int scheme, 
     }
   }
   std::copy(kernels.begin(), kernels.end(), loadKernels);
+  if (tideKernels) {
+    // a tide has no degree-1 part (the channel refuses one): its kernel there is none
+    if (options.lmax >= 1)
+      for (int n = 0; n < nodes; ++n)
+        for (size_t i = 2; i < 6; ++i) tides[2 * lm * n + i] = 0.0;
+    std::copy(tides.begin(), tides.end(), tideKernels);
+  }
   if (deltaGradient)
     SL3D_CUDA(cudaMemcpyAsync(deltaGradient, adj.grad.p, values * sizeof(double), cudaMemcpyDeviceToHost, stream));
   SL3D_CUDA(cudaStreamSynchronize(stream));
@@ -4265,14 +4284,14 @@ extern "C" int sl3dgpu_v3d_run(sl3dgpu_v3d* h, sl3dgpu_v3d_state* state, const d
 
 extern "C" int sl3dgpu_v3d_adjoint_run(sl3dgpu_v3d* h, const double* times, int nodes, int scheme, int stride,
                                        const double* loads, const double* u_dual, const double* phi_dual,
-                                       double* load_kernels, double* delta_gradient, double* objective,
-                                       sl3dgpu_step_info* infos) {
+                                       double* load_kernels, double* tide_kernels, double* delta_gradient,
+                                       double* objective, sl3dgpu_step_info* infos) {
   if (h == nullptr) {
     SetError("v3d adjoint: null operator");
     return SL3DGPU_ERR_ARGUMENT;
   }
-  return h->op.AdjointRun(times, nodes, scheme, stride, loads, u_dual, phi_dual, load_kernels, delta_gradient,
-                          objective, infos);
+  return h->op.AdjointRun(times, nodes, scheme, stride, loads, u_dual, phi_dual, load_kernels, tide_kernels,
+                          delta_gradient, objective, infos);
 }
 
 extern "C" int sl3dgpu_v3d_tangent_run(sl3dgpu_v3d* h, const double* times, int nodes, int scheme,

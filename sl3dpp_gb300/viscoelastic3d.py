@@ -113,7 +113,7 @@ def _signatures():
         "sl3dgpu_v3d_start_taken": (i, [v]),
         "sl3dgpu_v3d_state_coefficients": (i, [v, v, ctypes.POINTER(c_void_p), ctypes.POINTER(ctypes.c_longlong)]),
         "sl3dgpu_v3d_run": (i, [v, v, P_double, i, i, v, v, v, ctypes.POINTER(StepInfo)]),
-        "sl3dgpu_v3d_adjoint_run": (i, [v, P_double, i, i, i, v, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
+        "sl3dgpu_v3d_adjoint_run": (i, [v, P_double, i, i, i, v, v, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_sample_volumes": (i, [v, v]),
         "sl3dgpu_v3d_tangent_run": (i, [v, P_double, i, i, v, v, v, v, v, ctypes.POINTER(StepInfo)]),
         "sl3dgpu_v3d_run_many": (i, [i, v, v, v, v, i, v, v, v, v, i, v]),
@@ -636,7 +636,7 @@ class Evolution3D:
         FirstOrderKernels under AdjointMethod::Discrete, include/sl3dpp/
         Adjoint3D.hpp:241-322): for J = sum_n <u_dual_n, U_n> +
         <phi_dual_n, phi_n> (the surface pairing of real fields, m > 0 twice),
-        the load kernels per node (dJ = sum_n <kernel_n, dL_n>), dJ/d delta at
+        the load and tide kernels per node (dJ = sum_n <kernel_n, dL_n>), dJ/d delta at
         every grid sample (node-major, as set_delta's samples) and J itself.
         stride: the forward run's states kept every stride-th node, the gaps
         rebuilt by its own steps during the sweep."""
@@ -656,14 +656,16 @@ class Evolution3D:
                 raise ValueError("one dual (l(l+1)/2 + m coefficients) per node")
             duals.append(g)
         kernels = np.zeros((n, lm), dtype=np.complex128)
+        tides = np.zeros((n, lm), dtype=np.complex128)
         grad = np.zeros(self.op.values) if gradient else None
         objective = ctypes.c_double()
         infos = (StepInfo * max(n, 1))()
         check(lib().sl3dgpu_v3d_adjoint_run(
             self.op._h, times.ctypes.data_as(P_double), n, self.scheme, int(stride), loads.ctypes.data,
             None if duals[0] is None else duals[0].ctypes.data, None if duals[1] is None else duals[1].ctypes.data,
-            kernels.ctypes.data, None if grad is None else grad.ctypes.data, ctypes.byref(objective), infos))
-        return {"objective": objective.value, "load_kernels": kernels, "delta_gradient": grad,
+            kernels.ctypes.data, tides.ctypes.data, None if grad is None else grad.ctypes.data,
+            ctypes.byref(objective), infos))
+        return {"objective": objective.value, "load_kernels": kernels, "tide_kernels": tides, "delta_gradient": grad,
                 "infos": [infos[k] for k in range(n)]}
 
     def Tangent(self, times, loads, delta_direction=None, load_directions=None):

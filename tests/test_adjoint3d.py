@@ -181,3 +181,30 @@ def test_gpu_adjoint_pairs_with_the_tangent_linear_run(gpu, scheme, precision):
     alone = ev.Tangent(times, loads, None, dL)
     run = ev.Run(times, dL)
     assert rel(alone["U"], run["U"]) < 1e-9 and rel(alone["phi"], run["phi"]) < 1e-9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", [2, 0])
+def test_gpu_tide_kernels_pair_with_a_tide_run(gpu, scheme):
+    """Kernels::tideKernels: the run is linear in a tide added to its tide
+    channel, so the tide kernels pair with any tides (no degree-1 part) to
+    the objective of the run under those tides alone (1e-8)."""
+    from sl3dpp_gb300.viscoelastic3d import Evolution3D
+
+    lmax, nodes = 8, 4
+    o, g, times, loads, gU, gPhi = _run(lmax, scheme, nodes, 0, seed=31)
+    adj = Evolution3D(g, scheme).Adjoint(times, loads, gU, gPhi, gradient=False)
+    tides = 1e-3 * real_coefficients(lmax, np.random.default_rng(33), nodes)
+    tides[:, 1:3] = 0.0  # no degree-1 tide
+    zero = np.zeros_like(tides[0])
+    state = g.ZeroState()
+    U, phi = [], []
+    for k in range(nodes):
+        dt = 0.0 if k == 0 else times[k] - times[k - 1]
+        assert g.Step(state, dt, scheme, zero, zero, tides[max(k - 1, 0)], tides[k]).converged
+        U.append(g.Surface("U"))
+        phi.append(g.Surface("phi"))
+    J = _objective(lmax, {"U": U, "phi": phi}, gU, gPhi)
+    paired = sum(pairing(lmax, adj["tide_kernels"][k], tides[k]) for k in range(nodes))
+    assert abs(paired - J) < 1e-8 * abs(J), (paired, J)
+    assert np.all(adj["tide_kernels"][:, 1:3] == 0.0)
