@@ -54,7 +54,7 @@
 //               node, time (yr), l, m, U (m, re im), phi (m^2 s^-2, re im)
 //               and, with an ocean, the relative sea level change (m, re im)
 ////   kernels     (the kernel command) {"method": "discrete", "parameters":
-//               ["load", "viscosity"], "measurements": [{"type":
+//               ["load", "tide", "viscosity"], "measurements": [{"type":
 //               "displacement_point" | "displacement_cap" | "potential_point"
 //               | "potential_cap", "name", "latitude", "longitude",
 //               "width_deg" (a cap's Gaussian width), "time" (a node's, on the
@@ -62,7 +62,8 @@
 //               "record_stride" (1)}; per measurement NAME_summary.txt (its
 //               value in SI), NAME_load_kernels.txt (the load kernel's (l, m
 //               >= 0) coefficients per node, per kg m^-2 per m^2 of the
-//               run's sphere) and NAME_viscosity_kernels.bin with
+//               run's sphere), NAME_tide_kernels.txt ("tide": per tidal
+//               potential coefficient, m^2 s^-2) and NAME_viscosity_kernels.bin with
 //               NAME_viscosity_grid.txt (dJ/d delta per m^3 on every memory
 //               node's grid). Kernels under an ocean, the continuous method
 //               and the other parameters are refused as not built.
@@ -156,7 +157,7 @@ struct Config {
     double latitude = 0.0, longitude = 0.0, widthDeg = 0.0;
     size_t node = 0;
   };
-  bool kernels = false, loadKernels = false, viscosityKernels = false;
+  bool kernels = false, loadKernels = false, tideKernels = false, viscosityKernels = false;
   std::vector<Measurement> measurements;
   std::string kernelDir;
   int recordStride = 1;
@@ -383,18 +384,20 @@ Config ReadConfig(const std::string& path) {
       if (name != "discrete") throw std::invalid_argument("kernels.method: \"discrete\"");
     }
     const Value* params = Find(k, "parameters");
-    if (!params) throw std::invalid_argument("kernels.parameters is required: \"load\", \"viscosity\"");
+    if (!params) throw std::invalid_argument("kernels.parameters is required: \"load\", \"tide\", \"viscosity\"");
     for (const Value& v : params->Items("kernels.parameters")) {
       const std::string& word = v.String("kernels.parameters");
-      bool& flag = word == "load" ? c.loadKernels : c.viscosityKernels;
-      if (word != "load" && word != "viscosity") {
+      bool& flag = word == "load" ? c.loadKernels : word == "tide" ? c.tideKernels : c.viscosityKernels;
+      if (word != "load" && word != "tide" && word != "viscosity") {
         if (word == "ice") throw std::invalid_argument("kernels.parameters: \"ice\" needs an ocean");
-        throw std::invalid_argument("kernels.parameters: \"" + word + "\" is not built; \"load\", \"viscosity\"");
+        throw std::invalid_argument("kernels.parameters: \"" + word +
+                                    "\" is not built; \"load\", \"tide\", \"viscosity\"");
       }
       if (flag) throw std::invalid_argument("kernels.parameters: \"" + word + "\" named twice");
       flag = true;
     }
-    if (!c.loadKernels && !c.viscosityKernels) throw std::invalid_argument("kernels.parameters: at least one");
+    if (!c.loadKernels && !c.tideKernels && !c.viscosityKernels)
+      throw std::invalid_argument("kernels.parameters: at least one");
     const Value* dir = Find(k, "output");
     c.kernelDir = dir ? dir->String("kernels.output") : "";
     if (c.kernelDir.empty()) throw std::invalid_argument("kernels.output: a directory is required");
@@ -979,14 +982,15 @@ int Kernel(const Config& c) {
     std::vector<Complex> dual(lm * nodes);
     for (int l = 0; l <= lmax; ++l)
       for (int k = 0; k <= l; ++k) dual[lm * m.node + Index(l, k)] = b[l] * std::conj(Y[Index(l, k)]);
-    std::vector<Complex> kernels(lm * nodes);
+    std::vector<Complex> kernels(lm * nodes), tides(c.tideKernels ? lm * nodes : 0);
     std::vector<double> gradient(c.viscosityKernels ? values : 0);
     double objective = 0.0;
     Check(sl3dgpu_v3d_adjoint_run(op, times.data(), static_cast<int>(nodes), c.scheme, c.recordStride,
                                   reinterpret_cast<const double*>(loads.data()),
                                   displacement ? reinterpret_cast<const double*>(dual.data()) : nullptr,
                                   displacement ? nullptr : reinterpret_cast<const double*>(dual.data()),
-                                  reinterpret_cast<double*>(kernels.data()), nullptr,
+                                  reinterpret_cast<double*>(kernels.data()),
+                                  c.tideKernels ? reinterpret_cast<double*>(tides.data()) : nullptr,
                                   c.viscosityKernels ? gradient.data() : nullptr, &objective, nullptr),
           "adjoint");
     const double value = scale * objective;
@@ -1021,6 +1025,25 @@ int Kernel(const Config& c) {
             out << row;
           }
       if (!out) throw std::runtime_error("cannot write the load kernels of " + m.name);
+    }
+    if (c.tideKernels) {
+      // per (l, m >= 0) coefficient of a tidal potential (m^2 s^-2), the
+      // coefficient pairing of real fields (m > 0 twice); degree 1 none
+      const double toSi = scale * time * time / (length * length);
+      std::ofstream out(dir / (m.name + "_tide_kernels.txt"));
+      out << "# sl3d tide kernels of " << m.name << " (" << m.type << ", " << unit
+          << "): node t_yr l m K_re K_im, dJ = sum_n sum_{l, m >= 0} w_m Re(K_lm* dpsi_lm) for a tidal potential's "
+             "coefficients dpsi (m^2 s^-2; w_m = 1 at m = 0, 2 above; no degree-1 tide)\n";
+      char row[256];
+      for (size_t n = 0; n < nodes; ++n)
+        for (int l = 0; l <= lmax; ++l)
+          for (int k = 0; k <= l; ++k) {
+            const Complex v = toSi * tides[lm * n + Index(l, k)];
+            std::snprintf(row, sizeof(row), "%zu %.17g %d %d %.17g %.17g\n", n, c.timesYr[n], l, k, v.real(),
+                          v.imag());
+            out << row;
+          }
+      if (!out) throw std::runtime_error("cannot write the tide kernels of " + m.name);
     }
     if (c.viscosityKernels) {
       // dJ / d delta per unit volume (SI): the gradient over the samples' volumes

@@ -199,7 +199,7 @@ def test_gpu_migrating_run_moves_the_shorelines(gpu, sl3d, tmp_path):
 
 def kernel_config(tmp_path, **kernels):
     cfg = base(tmp_path, nodes=5)
-    block = {"method": "discrete", "parameters": ["load", "viscosity"], "output": str(tmp_path / "kernels"),
+    block = {"method": "discrete", "parameters": ["load", "tide", "viscosity"], "output": str(tmp_path / "kernels"),
              "measurements": [{"type": "displacement_point", "name": "uplift", "latitude": 63.2, "longitude": -20.5},
                               {"type": "potential_cap", "name": "geoid", "latitude": 70.0, "longitude": 10.0,
                                "width_deg": 8.0, "time": 1500.0}]}
@@ -301,3 +301,7 @@ def test_gpu_kernel_values_and_kernels_are_the_runs(gpu, sl3d, tmp_path):
         assert abs(paired - v) < 1e-8 * abs(v), (name, paired, v)
         density = np.fromfile(tmp_path / "kernels" / f"{name}_viscosity_kernels.bin")
         assert density.size == op.values and np.all(np.isfinite(density)) and np.max(np.abs(density)) > 0
+    # the tide kernels: written per node, none at degree 1
+    tide = table(tmp_path / "kernels" / "uplift_tide_kernels.txt")
+    T = (tide[:, 4] + 1j * tide[:, 5]).reshape(nodes, lm)
+    assert np.all(np.isfinite(T)) and np.max(np.abs(T)) > 0 and np.all(T[:, 1:3] == 0)
