@@ -1433,6 +1433,290 @@ class Viscoelastic3D {
     return out;
   }
 
+  // The discrete adjoint of the run from a zero state (AdjointSolver3D
+  // under AdjointMethod::Discrete, src/AdjointDiscrete3D.cpp; the transpose
+  // of this restatement's own step): J = sum_n <u_n, U_n> + <phi_n, phi_n>
+  // (surface pairing, m > 0 twice); out: the load kernels per node and
+  // dJ/d delta per grid sample; returns J. Every state is kept and the
+  // memory is on the grid at every node; each stage's transposed fixed
+  // point is solved with this step's plain and Anderson iteration.
+  double AdjointRun(const double* times, int nodes, Scheme scheme, const C* loads, const C* uDual, const C* phiDual,
+                    C* loadKernels, double* grad) {
+    const std::size_t lm = grid_.RealSize(), fs = grid_.FieldSize();
+    const std::size_t K = ZeroState().m.size();
+    const int L = options_.lmax;
+    auto pairSurface = [&](const C* a, const C* b) {
+      double sum = 0.0;
+      for (int l = 0; l <= L; ++l)
+        for (int m = 0; m <= l; ++m) {
+          const std::size_t i = OGrid::Index(l, m);
+          sum += (m == 0 ? 1.0 : 2.0) * (std::conj(a[i]) * b[i]).real();
+        }
+      return sum;
+    };
+    // the forward run, every node (and Sdirk2's first stage) kept
+    std::vector<State> states(nodes), firsts(nodes);
+    State cur = ZeroState();
+    double J = 0.0;
+    std::vector<C> surface(lm), mid(lm);
+    const double gamma = kSdirk2Gamma, r = (1.0 - gamma) / gamma;
+    auto combine = [&](const State& a, const State& y1) {
+      State from;
+      for (std::size_t k = 0; k < K; ++k) {
+        Tensor t = ZeroTensor();
+        for (std::size_t i = 0; i < t.r.size(); ++i) {
+          t.c0[i] = (1.0 - r) * a.m[k].c0[i] + r * y1.m[k].c0[i];
+          t.c1[i] = (1.0 - r) * a.m[k].c1[i] + r * y1.m[k].c1[i];
+          t.r[i] = (1.0 - r) * a.m[k].r[i] + r * y1.m[k].r[i];
+        }
+        from.m.push_back(std::move(t));
+      }
+      from.strain = y1.strain;
+      from.strainCoefficients = y1.strainCoefficients;
+      return from;
+    };
+    for (int k = 0; k < nodes; ++k) {
+      const C* l1 = loads + lm * k;
+      const C* l0 = k > 0 ? loads + lm * (k - 1) : l1;
+      const double dt = k > 0 ? times[k] - times[k - 1] : 0.0;
+      Info info;
+      Solutions sol;
+      if (scheme != Scheme::Sdirk2 || dt == 0.0) {
+        cur = StepOnce(cur, dt, scheme == Scheme::Sdirk2 ? Scheme::BackwardEuler : scheme, l0, l1, info, sol);
+      } else {
+        for (std::size_t i = 0; i < lm; ++i) mid[i] = (1.0 - gamma) * l0[i] + gamma * l1[i];
+        firsts[k] = StepOnce(cur, gamma * dt, Scheme::BackwardEuler, l0, mid.data(), info, sol);
+        cur = StepOnce(combine(cur, firsts[k]), gamma * dt, Scheme::BackwardEuler, mid.data(), l1, info, sol);
+      }
+      if (uDual) {
+        SurfaceOf(sol, 0, surface.data());
+        J += pairSurface(uDual + lm * k, surface.data());
+      }
+      if (phiDual) {
+        SurfaceOf(sol, 2, surface.data());
+        J += pairSurface(phiDual + lm * k, surface.data());
+      }
+      states[k] = cur;
+    }
+    // the transposed sweep
+    std::vector<Tensor> mD(K, ZeroTensor());
+    Tensor dD = ZeroTensor();
+    std::vector<double> gradient(static_cast<std::size_t>(NodeCount()) * fs, 0.0);
+    std::fill(loadKernels, loadKernels + lm * nodes, C{});
+    const State zero = [&] {
+      State z = ZeroState();
+      z.strain = ZeroTensor();
+      return z;
+    }();
+    const auto& mesh = nodal_->mesh;
+    const auto& pts = *points_;
+    auto energy = [](C a0, C a1, double ar, C b0, C b1, double br) {
+      return 4.0 * (std::conj(a0) * b0).real() + 8.0 * (std::conj(a1) * b1).real() + 12.0 * ar * br;
+    };
+    // one stage (in -> its end strain) transposed; the load's dual into sigma
+    auto stage = [&](const State& in, const Tensor& dEnd, double dt, Scheme sch, const C* gU, const C* gPhi,
+                     std::vector<C>& sigma) {
+      const auto& f = FlavourOf(sch, dt);
+      const bool be = sch == Scheme::BackwardEuler;
+      auto weights = [&](double h, double& e, double& a, double& b, double& de, double& da, double& db) {
+        if (be) {
+          e = BackwardEulerWeight(h);
+          a = 0.0;
+          b = 1.0 - e;
+          de = -e * e;
+          da = 0.0;
+          db = e * e;
+          return;
+        }
+        const auto tw = ExponentialTrapezoidWeights(h);
+        const double phi1 = tw.alpha + tw.e;
+        const double dphi1 = std::abs(h) < 1e-3 ? -0.5 + h / 3.0 - h * h / 8.0 + h * h * h / 30.0 : (tw.e - phi1) / h;
+        e = tw.e;
+        a = tw.alpha;
+        b = tw.beta;
+        de = -tw.e;
+        da = dphi1 + tw.e;
+        db = -dphi1;
+      };
+      // the lateral weight and the end strain's dual d-bar
+      std::vector<double> W(gradient.size(), 0.0);
+      Tensor bar = dD;
+      for (std::size_t k = 0; k < K; ++k)
+        for (int node = 0; node < NodeCount(); ++node) {
+          const double itau = ItauRef(k, node), mu = MuBranch(k, node);
+          double e0, a0, b0, de0, da0, db0;
+          weights(dt * itau, e0, a0, b0, de0, da0, db0);
+          for (std::size_t at = node * fs; at < (node + 1) * fs; ++at) {
+            double e, a, b, de, da, db;
+            weights(dt * (itau * factor_[at]), e, a, b, de, da, db);
+            W[at] += mu * (b - b0);
+            bar.c0[at] += b * mD[k].c0[at];
+            bar.c1[at] += b * mD[k].c1[at];
+            bar.r[at] += b * mD[k].r[at];
+          }
+        }
+      Spectral fixedS = ZeroSpectral();
+      Analyse(bar, fixedS);
+      // S^T g at the surface dofs, and K^-1 of it
+      auto surfaceForces = [&](std::vector<std::vector<C>>& sph) {
+        for (int l = 0; l <= L; ++l) {
+          const auto& op = *f.sph[l];
+          const int iU = op.SurfaceDof(kU), iP = op.SurfaceDof(kPhi);
+          for (int m = 0; m <= l; ++m) {
+            const std::size_t i = OGrid::Index(l, m);
+            if (gU && iU >= 0) sph[l][static_cast<std::size_t>(m) * op.DofCount() + iU] += gU[i];
+            if (gPhi && iP >= 0) sph[l][static_cast<std::size_t>(m) * op.DofCount() + iP] += gPhi[i];
+          }
+        }
+      };
+      std::vector<std::vector<C>> gs(L + 1), gt(L + 1);
+      for (int l = 0; l <= L; ++l) {
+        gs[l].assign(static_cast<std::size_t>(f.sph[l]->DofCount()) * (l + 1), C{});
+        if (l >= 1) gt[l].assign(static_cast<std::size_t>(f.tor[l]->DofCount()) * (l + 1), C{});
+      }
+      surfaceForces(gs);
+      const Solutions q = SolveForces(gs, gt, f);
+      // the fixed point t = Str(K^-1 F(An(W Syn t) + An(d-bar)) + q)
+      Tensor g = ZeroTensor();
+      Spectral analysed = ZeroSpectral();
+      Solutions z;
+      auto pass = [&](const Spectral& t) {
+        Synthesise(t, g);
+        for (std::size_t i = 0; i < W.size(); ++i) {
+          g.c0[i] *= W[i];
+          g.c1[i] *= W[i];
+          g.r[i] *= W[i];
+        }
+        Analyse(g, analysed);
+        for (std::size_t i = 0; i < analysed.c0.size(); ++i) analysed.c0[i] += fixedS.c0[i];
+        for (std::size_t i = 0; i < analysed.c1.size(); ++i) analysed.c1[i] += fixedS.c1[i];
+        for (std::size_t i = 0; i < analysed.r.size(); ++i) analysed.r[i] += fixedS.r[i];
+        z = SolveAll(analysed, f);
+        Axpy(z, 1.0, q);
+        return StrainOf(z, f);
+      };
+      Spectral t = ZeroSpectral();
+      std::optional<Mixer> mixer;
+      double previous = 0.0;
+      bool converged = false;
+      for (int iteration = 0; iteration < options_.max_iterations; ++iteration) {
+        Spectral next = pass(t);
+        const double residual = RelativeChange(next, t);
+        if (!std::isfinite(residual)) break;
+        if (residual <= options_.rtol) {  // a zero dual converges at once (zero change of zero)
+          t = std::move(next);
+          converged = true;
+          break;
+        }
+        if (!mixer && options_.anderson_memory > 0 && iteration > 0 && residual > options_.anderson_rate * previous)
+          mixer.emplace(options_.anderson_memory);
+        previous = residual;
+        if (mixer) {
+          mixer->Update({reinterpret_cast<double*>(t.c0.data()), reinterpret_cast<double*>(t.c1.data()),
+                         reinterpret_cast<double*>(t.r.data())},
+                        {reinterpret_cast<const double*>(next.c0.data()),
+                         reinterpret_cast<const double*>(next.c1.data()), reinterpret_cast<const double*>(next.r.data())},
+                        {2 * t.c0.size(), 2 * t.c1.size(), 2 * t.r.size()});
+        } else {
+          t = std::move(next);
+        }
+      }
+      if (!converged) throw std::runtime_error("oracle adjoint: a transposed stage did not converge");
+      Tensor zeta = ZeroTensor();
+      Synthesise(t, zeta);
+      // the load's dual u^T (F An(d-bar + W zeta) + S^T g)
+      Tensor y = bar;
+      for (std::size_t i = 0; i < W.size(); ++i) {
+        y.c0[i] += W[i] * zeta.c0[i];
+        y.c1[i] += W[i] * zeta.c1[i];
+        y.r[i] += W[i] * zeta.r[i];
+      }
+      Spectral ys = ZeroSpectral();
+      Analyse(y, ys);
+      std::vector<std::vector<C>> fsph, ftor;
+      Forces(ys, f, fsph, ftor);
+      surfaceForces(fsph);
+      sigma.assign(lm, C{});
+      for (int l = 0; l <= L; ++l) {
+        const int ndof = f.sph[l]->DofCount();
+        for (int m = 0; m <= l; ++m) {
+          C sum{};
+          for (int d = 0; d < ndof; ++d) sum += f.units[l][d] * fsph[l][static_cast<std::size_t>(m) * ndof + d];
+          sigma[OGrid::Index(l, m)] = sum;
+        }
+      }
+      // the start's duals and the gradient
+      Tensor start = in.strain.has_value() ? *in.strain : ZeroTensor();
+      Tensor nextD = ZeroTensor();
+      for (int node = 0; node < NodeCount(); ++node) {
+        const auto& nd = nodes_[node];
+        const double volume = mesh.Jacobian(nd.element) * pts.weight[nd.q] * nd.r * nd.r;
+        for (std::size_t at = node * fs; at < (node + 1) * fs; ++at) {
+          const double omega = volume * grid_.w[(at % fs) / grid_.nphi] * 2.0 * kPi / grid_.nphi;
+          double sum = 0.0;
+          for (std::size_t k = 0; k < K; ++k) {
+            const double mu = MuBranch(k, node), h = dt * (ItauRef(k, node) * factor_[at]);
+            double e, a, b, de, da, db;
+            weights(h, e, a, b, de, da, db);
+            const C M0 = mD[k].c0[at] + mu * zeta.c0[at], M1 = mD[k].c1[at] + mu * zeta.c1[at];
+            const double Mr = mD[k].r[at] + mu * zeta.r[at];
+            sum -= h * (de * energy(M0, M1, Mr, in.m[k].c0[at], in.m[k].c1[at], in.m[k].r[at]) +
+                        da * energy(M0, M1, Mr, start.c0[at], start.c1[at], start.r[at]) +
+                        db * energy(M0, M1, Mr, dEnd.c0[at], dEnd.c1[at], dEnd.r[at]));
+            mD[k].c0[at] = e * M0;
+            mD[k].c1[at] = e * M1;
+            mD[k].r[at] = e * Mr;
+            nextD.c0[at] += a * M0;
+            nextD.c1[at] += a * M1;
+            nextD.r[at] += a * Mr;
+          }
+          gradient[at] += omega * sum;
+        }
+      }
+      dD = std::move(nextD);
+    };
+    std::vector<C> sigma;
+    for (int n = nodes - 1; n >= 0; --n) {
+      const State& prev = n > 0 ? states[n - 1] : zero;
+      const double dt = n > 0 ? times[n] - times[n - 1] : 0.0;
+      const C* gU = uDual ? uDual + lm * n : nullptr;
+      const C* gPhi = phiDual ? phiDual + lm * n : nullptr;
+      auto add = [&](int node, double c) {
+        for (std::size_t i = 0; i < lm; ++i) loadKernels[lm * node + i] += c * sigma[i];
+      };
+      if (scheme != Scheme::Sdirk2 || dt == 0.0) {
+        stage(prev, *states[n].strain, dt, scheme == Scheme::Sdirk2 ? Scheme::BackwardEuler : scheme, gU, gPhi,
+              sigma);
+        add(n, 1.0);
+        continue;
+      }
+      const State from = combine(prev, firsts[n]);
+      stage(from, *states[n].strain, gamma * dt, Scheme::BackwardEuler, gU, gPhi, sigma);
+      add(n, 1.0);
+      std::vector<Tensor> held(K, ZeroTensor());
+      for (std::size_t k = 0; k < K; ++k)
+        for (std::size_t i = 0; i < mD[k].r.size(); ++i) {
+          held[k].c0[i] = (1.0 - r) * mD[k].c0[i];
+          held[k].c1[i] = (1.0 - r) * mD[k].c1[i];
+          held[k].r[i] = (1.0 - r) * mD[k].r[i];
+          mD[k].c0[i] *= r;
+          mD[k].c1[i] *= r;
+          mD[k].r[i] *= r;
+        }
+      stage(prev, *firsts[n].strain, gamma * dt, Scheme::BackwardEuler, nullptr, nullptr, sigma);
+      add(n - 1, 1.0 - gamma);
+      add(n, gamma);
+      for (std::size_t k = 0; k < K; ++k)
+        for (std::size_t i = 0; i < mD[k].r.size(); ++i) {
+          mD[k].c0[i] += held[k].c0[i];
+          mD[k].c1[i] += held[k].c1[i];
+          mD[k].r[i] += held[k].r[i];
+        }
+    }
+    if (grad) std::copy(gradient.begin(), gradient.end(), grad);
+    return J;
+  }
+
   // Surface (Viscoelastic3D.cpp:2032-2051): U, V or phi at the surface node.
   // InertiaMoment (Viscoelastic3D.cpp:2032-2048 with the degree-0 moment row
   // of detail/ViscoelasticDegree.hpp:142-161): sqrt(4 pi) sum over the
@@ -1626,6 +1910,23 @@ int oracle_v3d_sample(oracle_v3d* h, oracle_state* state, double dt, const doubl
 }
 
 int oracle_threads(void) { return omp_get_max_threads(); }
+
+// The discrete adjoint of the run from a zero state (the restatement's own
+// transpose): the load kernels per node ((l, m >= 0) complex), dJ/d delta per
+// grid sample (nullable) and J; status -1 when a transposed stage did not
+// converge.
+int oracle_v3d_adjoint_run(oracle_v3d* h, const double* times, int nodes, int scheme, const double* loads,
+                           const double* u_dual, const double* phi_dual, double* load_kernels, double* grad,
+                           double* objective) {
+  try {
+    *objective = h->op->AdjointRun(times, nodes, static_cast<orc::Scheme>(scheme), reinterpret_cast<const C*>(loads),
+                                   reinterpret_cast<const C*>(u_dual), reinterpret_cast<const C*>(phi_dual),
+                                   reinterpret_cast<C*>(load_kernels), grad);
+  } catch (const std::exception&) {
+    return -1;
+  }
+  return 0;
+}
 
 // The ocean closure: each pass's load and tide channels from the callback
 // (NULL: the plain load channel again).

@@ -16,7 +16,10 @@ for the three schemes, and the mixed form for Sdirk2. A record stride (the
 forward states kept every stride-th node, the gaps rebuilt) changes nothing
 but the memory held. The tangent-linear run (TangentLinearSolver3D's
 discrete method) pairs with the adjoint to 1e-8 along a direction in the
-log-viscosity and the loads together."""
+log-viscosity and the loads together. On the CPU, the oracle's own
+restatement of the transposed sweep (oracle_step.cpp, AdjointRun) meets the
+pairing identity with the oracle's run (1e-12) and its gradient the
+differences of that run (1e-6)."""
 
 import numpy as np
 import pytest
@@ -208,3 +211,75 @@ def test_gpu_tide_kernels_pair_with_a_tide_run(gpu, scheme):
     paired = sum(pairing(lmax, adj["tide_kernels"][k], tides[k]) for k in range(nodes))
     assert abs(paired - J) < 1e-8 * abs(J), (paired, J)
     assert np.all(adj["tide_kernels"][:, 1:3] == 0.0)
+
+
+# -- the oracle's restatement (CPU) ---------------------------------------------------------------
+
+def _oracle_case(lmax=6, nodes=4, seed=3):
+    def make():
+        o = O.OracleStep(O.standard_earth(20, 0.0, 10.0), O.default_options(lmax, 5, rtol=1e-11, max_iterations=80))
+        o.set_delta(_delta_of(o, lmax))
+        return o
+
+    o = make()
+    rng = np.random.default_rng(seed)
+    dt = 500 * configs.SECONDS_PER_YEAR / o.time_scale
+    times = dt * np.arange(nodes)
+    full = cap_load(lmax, o.sigma_scale, 2000.0, alpha=40.0)
+    loads = np.stack([full * (k + 1) / nodes for k in range(nodes)]) + 0.05 * np.max(np.abs(full)) * \
+        real_coefficients(lmax, rng, nodes)
+    return make, times, loads, real_coefficients(lmax, rng, nodes), real_coefficients(lmax, rng, nodes)
+
+
+def _delta_of(o, lmax):
+    from tests.test_step import delta_for
+
+    return delta_for(o, lmax, 3, 0.8, 11)
+
+
+def _oracle_objective(make, lmax, scheme, times, loads, gU, gPhi, delta=None):
+    o = make()
+    if delta is not None:
+        o.set_delta(delta)
+    J = 0.0
+    for k in range(len(times)):
+        dt = 0.0 if k == 0 else times[k] - times[k - 1]
+        assert o.step(dt, scheme, loads[max(k - 1, 0)], loads[k]).converged
+        J += pairing(o.options.lmax, gU[k], o.surface(0)) + pairing(o.options.lmax, gPhi[k], o.surface(2))
+    return J
+
+
+@pytest.mark.parametrize("scheme", [2, 0, 1])
+def test_oracle_adjoint_pairs_with_the_oracle_run(scheme):
+    """The oracle's own transpose of its step (the restatement the GPU sweep
+    is compared with): its load kernels pair with the loads to its forward
+    run's objective (1e-12)."""
+    lmax = 6
+    make, times, loads, gU, gPhi = _oracle_case(lmax)
+    adj = make().adjoint(times, scheme, loads, gU, gPhi)
+    J = _oracle_objective(make, lmax, scheme, times, loads, gU, gPhi)
+    paired = sum(pairing(lmax, adj["load_kernels"][k], loads[k]) for k in range(len(times)))
+    assert abs(adj["objective"] - J) < 1e-13 * abs(J)
+    assert abs(paired - J) < 1e-12 * abs(J), (paired, J)
+
+
+def test_oracle_delta_gradient_matches_differences():
+    """The oracle's gradient in delta along a direction over every node
+    against Richardson-extrapolated central differences of its run (1e-6)."""
+    lmax, scheme = 6, 2
+    make, times, loads, gU, gPhi = _oracle_case(lmax, seed=5)
+    o = make()
+    delta = np.asarray(_delta_of(o, lmax))
+    adj = o.adjoint(times, scheme, loads, gU, gPhi)
+    rng = np.random.default_rng(17)
+    pattern = O.synthesise_real(lmax, o.theta, o.nphi, real_coefficients(lmax, rng, 1)[0] / (lmax + 1))
+    radial = 1.0 + 0.5 * np.sin(7.0 * np.asarray(o.radius))
+    p = (radial[:, None] * np.asarray(pattern).ravel()[None, :]).ravel()
+    J = lambda h: _oracle_objective(make, lmax, scheme, times, loads, gU, gPhi, delta + h * p)
+    h = 1e-2
+    d1 = (J(h) - J(-h)) / (2 * h)
+    d2 = (J(h / 2) - J(-h / 2)) / h
+    richardson = (4 * d2 - d1) / 3
+    predicted = float(adj["delta_gradient"] @ p)
+    assert abs(predicted - richardson) < 1e-6 * abs(richardson), (predicted, richardson)
+
