@@ -1433,6 +1433,176 @@ class Viscoelastic3D {
     return out;
   }
 
+  // A stage's weights at h (ExponentialTrapezoidWeights or
+  // BackwardEulerWeight) and their derivatives in h.
+  static void StageWeightSlopes(Scheme sch, double h, double& e, double& a, double& b, double& de, double& da,
+                                double& db) {
+    if (sch == Scheme::BackwardEuler) {
+      e = BackwardEulerWeight(h);
+      a = 0.0;
+      b = 1.0 - e;
+      de = -e * e;
+      da = 0.0;
+      db = e * e;
+      return;
+    }
+    const auto tw = ExponentialTrapezoidWeights(h);
+    const double phi1 = tw.alpha + tw.e;
+    const double dphi1 = std::abs(h) < 1e-3 ? -0.5 + h / 3.0 - h * h / 8.0 + h * h * h / 30.0 : (tw.e - phi1) / h;
+    e = tw.e;
+    a = tw.alpha;
+    b = tw.beta;
+    de = -tw.e;
+    da = dphi1 + tw.e;
+    db = -dphi1;
+  }
+
+  // The tangent-linear run beside the run from a zero state
+  // (TangentLinearSolver3D's discrete run, src/TangentLinear3D.cpp): the
+  // derivative of U and phi at every node along a log-viscosity direction p
+  // (per grid sample, nullable) and load directions (nullable), stage by
+  // stage beside the forward stage; each tangent solve is this step's own
+  // iteration with the tangent's fixed force and load channel.
+  void TangentRun(const double* times, int nodes, Scheme scheme, const C* loads, const double* p,
+                  const C* loadDirections, C* uOut, C* phiOut) {
+    const std::size_t lm = grid_.RealSize(), fs = grid_.FieldSize();
+    State cur = ZeroState();
+    cur.strain = ZeroTensor();
+    const std::size_t K = cur.m.size();
+    std::vector<Tensor> tm(K, ZeroTensor());
+    Tensor td = ZeroTensor();
+    const double gamma = kSdirk2Gamma, r = (1.0 - gamma) / gamma;
+    // one tangent stage beside the forward stage in -> out
+    auto stage = [&](const State& in, const State& out, double dt, Scheme sch, const C* loadDot) {
+      const auto& f = FlavourOf(sch, dt);
+      const Tensor start = in.strain.has_value() ? *in.strain : ZeroTensor();
+      const Tensor& dEnd = *out.strain;
+      std::vector<double> W(tm[0].r.size(), 0.0), hdot(W.size(), 0.0);
+      Tensor fixed = ZeroTensor();
+      std::vector<std::vector<double>> bdot(K, std::vector<double>(W.size())), beta(K, std::vector<double>(W.size()));
+      for (std::size_t k = 0; k < K; ++k)
+        for (int node = 0; node < NodeCount(); ++node) {
+          const double itau = ItauRef(k, node), mu = MuBranch(k, node);
+          double e0, a0, b0, de0, da0, db0;
+          StageWeightSlopes(sch, dt * itau, e0, a0, b0, de0, da0, db0);
+          for (std::size_t at = node * fs; at < (node + 1) * fs; ++at) {
+            const double h = dt * (itau * factor_[at]), hd = -h * (p ? p[at] : 0.0);
+            double e, a, b, de, da, db;
+            StageWeightSlopes(sch, h, e, a, b, de, da, db);
+            W[at] += mu * (b - b0);
+            beta[k][at] = b;
+            bdot[k][at] = db * hd;
+            tm[k].c0[at] = e * tm[k].c0[at] + a * td.c0[at] + de * hd * in.m[k].c0[at] + da * hd * start.c0[at];
+            tm[k].c1[at] = e * tm[k].c1[at] + a * td.c1[at] + de * hd * in.m[k].c1[at] + da * hd * start.c1[at];
+            tm[k].r[at] = e * tm[k].r[at] + a * td.r[at] + de * hd * in.m[k].r[at] + da * hd * start.r[at];
+            fixed.c0[at] += mu * tm[k].c0[at] + mu * db * hd * dEnd.c0[at];
+            fixed.c1[at] += mu * tm[k].c1[at] + mu * db * hd * dEnd.c1[at];
+            fixed.r[at] += mu * tm[k].r[at] + mu * db * hd * dEnd.r[at];
+          }
+        }
+      Spectral fixedS = ZeroSpectral();
+      Analyse(fixed, fixedS);
+      Tensor g = ZeroTensor();
+      Spectral analysed = ZeroSpectral();
+      Solutions x;
+      auto pass = [&](const Spectral& t) {
+        Synthesise(t, g);
+        for (std::size_t i = 0; i < W.size(); ++i) {
+          g.c0[i] *= W[i];
+          g.c1[i] *= W[i];
+          g.r[i] *= W[i];
+        }
+        Analyse(g, analysed);
+        for (std::size_t i = 0; i < analysed.c0.size(); ++i) analysed.c0[i] += fixedS.c0[i];
+        for (std::size_t i = 0; i < analysed.c1.size(); ++i) analysed.c1[i] += fixedS.c1[i];
+        for (std::size_t i = 0; i < analysed.r.size(); ++i) analysed.r[i] += fixedS.r[i];
+        x = SolveAll(analysed, f);
+        AddLoad(x, f, loadDot);
+        return StrainOf(x, f);
+      };
+      Spectral t = ZeroSpectral();
+      std::optional<Mixer> mixer;
+      double previous = 0.0;
+      bool converged = false;
+      for (int iteration = 0; iteration < options_.max_iterations; ++iteration) {
+        Spectral next = pass(t);
+        const double residual = RelativeChange(next, t);
+        if (!std::isfinite(residual)) break;
+        if (residual <= options_.rtol) {
+          t = std::move(next);
+          converged = true;
+          break;
+        }
+        if (!mixer && options_.anderson_memory > 0 && iteration > 0 && residual > options_.anderson_rate * previous)
+          mixer.emplace(options_.anderson_memory);
+        previous = residual;
+        if (mixer) {
+          mixer->Update({reinterpret_cast<double*>(t.c0.data()), reinterpret_cast<double*>(t.c1.data()),
+                         reinterpret_cast<double*>(t.r.data())},
+                        {reinterpret_cast<const double*>(next.c0.data()),
+                         reinterpret_cast<const double*>(next.c1.data()), reinterpret_cast<const double*>(next.r.data())},
+                        {2 * t.c0.size(), 2 * t.c1.size(), 2 * t.r.size()});
+        } else {
+          t = std::move(next);
+        }
+      }
+      if (!converged) throw std::runtime_error("oracle tangent: a tangent stage did not converge");
+      Synthesise(t, td);
+      for (std::size_t k = 0; k < K; ++k)
+        for (std::size_t i = 0; i < W.size(); ++i) {
+          tm[k].c0[i] += beta[k][i] * td.c0[i] + bdot[k][i] * dEnd.c0[i];
+          tm[k].c1[i] += beta[k][i] * td.c1[i] + bdot[k][i] * dEnd.c1[i];
+          tm[k].r[i] += beta[k][i] * td.r[i] + bdot[k][i] * dEnd.r[i];
+        }
+      return x;
+    };
+    std::vector<C> mid(lm), dmid(lm);
+    for (int k = 0; k < nodes; ++k) {
+      const C* l1 = loads + lm * k;
+      const C* l0 = k > 0 ? loads + lm * (k - 1) : l1;
+      const C* t1 = loadDirections ? loadDirections + lm * k : nullptr;
+      const C* t0 = loadDirections ? (k > 0 ? loadDirections + lm * (k - 1) : t1) : nullptr;
+      const double dt = k > 0 ? times[k] - times[k - 1] : 0.0;
+      Info info;
+      Solutions sol, x;
+      if (scheme != Scheme::Sdirk2 || dt == 0.0) {
+        const Scheme one = scheme == Scheme::Sdirk2 ? Scheme::BackwardEuler : scheme;
+        const State out = StepOnce(cur, dt, one, l0, l1, info, sol);
+        x = stage(cur, out, dt, one, t1);
+        cur = out;
+      } else {
+        for (std::size_t i = 0; i < lm; ++i) {
+          mid[i] = (1.0 - gamma) * l0[i] + gamma * l1[i];
+          if (t0) dmid[i] = (1.0 - gamma) * t0[i] + gamma * t1[i];
+        }
+        const State y1 = StepOnce(cur, gamma * dt, Scheme::BackwardEuler, l0, mid.data(), info, sol);
+        const std::vector<Tensor> held = tm;
+        stage(cur, y1, gamma * dt, Scheme::BackwardEuler, t0 ? dmid.data() : nullptr);
+        State from;
+        for (std::size_t b = 0; b < K; ++b) {
+          Tensor c = ZeroTensor();
+          for (std::size_t i = 0; i < c.r.size(); ++i) {
+            c.c0[i] = (1.0 - r) * cur.m[b].c0[i] + r * y1.m[b].c0[i];
+            c.c1[i] = (1.0 - r) * cur.m[b].c1[i] + r * y1.m[b].c1[i];
+            c.r[i] = (1.0 - r) * cur.m[b].r[i] + r * y1.m[b].r[i];
+            tm[b].c0[i] = (1.0 - r) * held[b].c0[i] + r * tm[b].c0[i];
+            tm[b].c1[i] = (1.0 - r) * held[b].c1[i] + r * tm[b].c1[i];
+            tm[b].r[i] = (1.0 - r) * held[b].r[i] + r * tm[b].r[i];
+          }
+          from.m.push_back(std::move(c));
+        }
+        from.strain = y1.strain;
+        from.strainCoefficients = y1.strainCoefficients;
+        const State out = StepOnce(from, gamma * dt, Scheme::BackwardEuler, mid.data(), l1, info, sol);
+        x = stage(from, out, gamma * dt, Scheme::BackwardEuler, t1);
+        cur = out;
+      }
+      if (!info.converged) throw std::runtime_error("oracle tangent: a forward stage did not converge");
+      if (uOut) SurfaceOf(x, 0, uOut + lm * k);
+      if (phiOut) SurfaceOf(x, 2, phiOut + lm * k);
+    }
+  }
+
   // The discrete adjoint of the run from a zero state (AdjointSolver3D
   // under AdjointMethod::Discrete, src/AdjointDiscrete3D.cpp; the transpose
   // of this restatement's own step): J = sum_n <u_n, U_n> + <phi_n, phi_n>
@@ -1441,7 +1611,7 @@ class Viscoelastic3D {
   // memory is on the grid at every node; each stage's transposed fixed
   // point is solved with this step's plain and Anderson iteration.
   double AdjointRun(const double* times, int nodes, Scheme scheme, const C* loads, const C* uDual, const C* phiDual,
-                    C* loadKernels, double* grad) {
+                    C* loadKernels, double* grad, C* tideKernels = nullptr) {
     const std::size_t lm = grid_.RealSize(), fs = grid_.FieldSize();
     const std::size_t K = ZeroState().m.size();
     const int L = options_.lmax;
@@ -1515,28 +1685,10 @@ class Viscoelastic3D {
     };
     // one stage (in -> its end strain) transposed; the load's dual into sigma
     auto stage = [&](const State& in, const Tensor& dEnd, double dt, Scheme sch, const C* gU, const C* gPhi,
-                     std::vector<C>& sigma) {
+                     std::vector<C>& sigma, std::vector<C>& tide) {
       const auto& f = FlavourOf(sch, dt);
-      const bool be = sch == Scheme::BackwardEuler;
       auto weights = [&](double h, double& e, double& a, double& b, double& de, double& da, double& db) {
-        if (be) {
-          e = BackwardEulerWeight(h);
-          a = 0.0;
-          b = 1.0 - e;
-          de = -e * e;
-          da = 0.0;
-          db = e * e;
-          return;
-        }
-        const auto tw = ExponentialTrapezoidWeights(h);
-        const double phi1 = tw.alpha + tw.e;
-        const double dphi1 = std::abs(h) < 1e-3 ? -0.5 + h / 3.0 - h * h / 8.0 + h * h * h / 30.0 : (tw.e - phi1) / h;
-        e = tw.e;
-        a = tw.alpha;
-        b = tw.beta;
-        de = -tw.e;
-        da = dphi1 + tw.e;
-        db = -dphi1;
+        StageWeightSlopes(sch, h, e, a, b, de, da, db);
       };
       // the lateral weight and the end strain's dual d-bar
       std::vector<double> W(gradient.size(), 0.0);
@@ -1637,12 +1789,17 @@ class Viscoelastic3D {
       Forces(ys, f, fsph, ftor);
       surfaceForces(fsph);
       sigma.assign(lm, C{});
+      tide.assign(lm, C{});
       for (int l = 0; l <= L; ++l) {
         const int ndof = f.sph[l]->DofCount();
         for (int m = 0; m <= l; ++m) {
-          C sum{};
-          for (int d = 0; d < ndof; ++d) sum += f.units[l][d] * fsph[l][static_cast<std::size_t>(m) * ndof + d];
+          C sum{}, tsum{};
+          for (int d = 0; d < ndof; ++d) {
+            sum += f.units[l][d] * fsph[l][static_cast<std::size_t>(m) * ndof + d];
+            tsum += f.tideUnits[l][d] * fsph[l][static_cast<std::size_t>(m) * ndof + d];
+          }
           sigma[OGrid::Index(l, m)] = sum;
+          if (l != 1) tide[OGrid::Index(l, m)] = tsum;  // no degree-1 tide
         }
       }
       // the start's duals and the gradient
@@ -1675,7 +1832,8 @@ class Viscoelastic3D {
       }
       dD = std::move(nextD);
     };
-    std::vector<C> sigma;
+    std::vector<C> sigma, tide;
+    if (tideKernels) std::fill(tideKernels, tideKernels + lm * nodes, C{});
     for (int n = nodes - 1; n >= 0; --n) {
       const State& prev = n > 0 ? states[n - 1] : zero;
       const double dt = n > 0 ? times[n] - times[n - 1] : 0.0;
@@ -1683,15 +1841,17 @@ class Viscoelastic3D {
       const C* gPhi = phiDual ? phiDual + lm * n : nullptr;
       auto add = [&](int node, double c) {
         for (std::size_t i = 0; i < lm; ++i) loadKernels[lm * node + i] += c * sigma[i];
+        if (tideKernels)
+          for (std::size_t i = 0; i < lm; ++i) tideKernels[lm * node + i] += c * tide[i];
       };
       if (scheme != Scheme::Sdirk2 || dt == 0.0) {
         stage(prev, *states[n].strain, dt, scheme == Scheme::Sdirk2 ? Scheme::BackwardEuler : scheme, gU, gPhi,
-              sigma);
+              sigma, tide);
         add(n, 1.0);
         continue;
       }
       const State from = combine(prev, firsts[n]);
-      stage(from, *states[n].strain, gamma * dt, Scheme::BackwardEuler, gU, gPhi, sigma);
+      stage(from, *states[n].strain, gamma * dt, Scheme::BackwardEuler, gU, gPhi, sigma, tide);
       add(n, 1.0);
       std::vector<Tensor> held(K, ZeroTensor());
       for (std::size_t k = 0; k < K; ++k)
@@ -1703,7 +1863,7 @@ class Viscoelastic3D {
           mD[k].c1[i] *= r;
           mD[k].r[i] *= r;
         }
-      stage(prev, *firsts[n].strain, gamma * dt, Scheme::BackwardEuler, nullptr, nullptr, sigma);
+      stage(prev, *firsts[n].strain, gamma * dt, Scheme::BackwardEuler, nullptr, nullptr, sigma, tide);
       add(n - 1, 1.0 - gamma);
       add(n, gamma);
       for (std::size_t k = 0; k < K; ++k)
@@ -1911,17 +2071,32 @@ int oracle_v3d_sample(oracle_v3d* h, oracle_state* state, double dt, const doubl
 
 int oracle_threads(void) { return omp_get_max_threads(); }
 
+// The tangent-linear run beside the run from a zero state (the
+// restatement's own derivative): U and phi derivatives per node along a
+// log-viscosity direction (per grid sample, nullable) and load directions
+// (nullable); status -1 when a stage did not converge.
+int oracle_v3d_tangent_run(oracle_v3d* h, const double* times, int nodes, int scheme, const double* loads,
+                           const double* direction, const double* load_directions, double* u, double* phi) {
+  try {
+    h->op->TangentRun(times, nodes, static_cast<orc::Scheme>(scheme), reinterpret_cast<const C*>(loads), direction,
+                      reinterpret_cast<const C*>(load_directions), reinterpret_cast<C*>(u), reinterpret_cast<C*>(phi));
+  } catch (const std::exception&) {
+    return -1;
+  }
+  return 0;
+}
+
 // The discrete adjoint of the run from a zero state (the restatement's own
 // transpose): the load kernels per node ((l, m >= 0) complex), dJ/d delta per
-// grid sample (nullable) and J; status -1 when a transposed stage did not
-// converge.
+// grid sample (nullable), J and the tide kernels (nullable, none at degree
+// 1); status -1 when a transposed stage did not converge.
 int oracle_v3d_adjoint_run(oracle_v3d* h, const double* times, int nodes, int scheme, const double* loads,
                            const double* u_dual, const double* phi_dual, double* load_kernels, double* grad,
-                           double* objective) {
+                           double* objective, double* tide_kernels) {
   try {
     *objective = h->op->AdjointRun(times, nodes, static_cast<orc::Scheme>(scheme), reinterpret_cast<const C*>(loads),
                                    reinterpret_cast<const C*>(u_dual), reinterpret_cast<const C*>(phi_dual),
-                                   reinterpret_cast<C*>(load_kernels), grad);
+                                   reinterpret_cast<C*>(load_kernels), grad, reinterpret_cast<C*>(tide_kernels));
   } catch (const std::exception&) {
     return -1;
   }

@@ -220,7 +220,8 @@ def _v3d_sigs(L):
         "oracle_v3d_set_closure": (None, [v, _CLOSURE, v]),
         "oracle_v3d_effective_love": (None, [v, i, d, P_double]),
         "oracle_v3d_body": (None, [v, P_double]),
-        "oracle_v3d_adjoint_run": (i, [v, P_double, i, i, v, v, v, v, v, P_double]),
+        "oracle_v3d_adjoint_run": (i, [v, P_double, i, i, v, v, v, v, v, P_double, v]),
+        "oracle_v3d_tangent_run": (i, [v, P_double, i, i, v, v, v, v, v]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -284,20 +285,36 @@ class OracleStep:
 
     def adjoint(self, times, scheme, loads, u_dual=None, phi_dual=None):
         """The oracle's discrete adjoint of the run from a zero state: the
-        objective, the load kernels per node and dJ/d delta per sample."""
+        objective, the load and tide kernels per node and dJ/d delta per
+        sample."""
         times = np.ascontiguousarray(times, dtype=np.float64)
         loads = np.ascontiguousarray(loads, dtype=np.complex128)
         n = times.size
         duals = [None if g is None else np.ascontiguousarray(g, dtype=np.complex128) for g in (u_dual, phi_dual)]
         kernels = np.zeros_like(loads)
+        tides = np.zeros_like(loads)
         grad = np.zeros(self.P * self.ntheta * self.nphi)
         J = _ct.c_double()
         st = self.L.oracle_v3d_adjoint_run(self.h, ptr(times), n, scheme, loads.ctypes.data,
                                            None if duals[0] is None else duals[0].ctypes.data,
                                            None if duals[1] is None else duals[1].ctypes.data,
-                                           kernels.ctypes.data, ptr(grad), _ct.byref(J))
+                                           kernels.ctypes.data, ptr(grad), _ct.byref(J), tides.ctypes.data)
         assert st == 0
-        return {"objective": J.value, "load_kernels": kernels, "delta_gradient": grad}
+        return {"objective": J.value, "load_kernels": kernels, "tide_kernels": tides, "delta_gradient": grad}
+
+    def tangent(self, times, scheme, loads, direction=None, load_directions=None):
+        """The oracle's tangent-linear run beside the run from a zero state:
+        the derivatives of U and phi per node."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        loads = np.ascontiguousarray(loads, dtype=np.complex128)
+        p = None if direction is None else np.ascontiguousarray(direction, dtype=np.float64)
+        d = None if load_directions is None else np.ascontiguousarray(load_directions, dtype=np.complex128)
+        U, phi = np.zeros_like(loads), np.zeros_like(loads)
+        st = self.L.oracle_v3d_tangent_run(self.h, ptr(times), times.size, scheme, loads.ctypes.data,
+                                           None if p is None else p.ctypes.data, None if d is None else d.ctypes.data,
+                                           U.ctypes.data, phi.ctypes.data)
+        assert st == 0
+        return {"U": U, "phi": phi}
 
     def sample(self, dt, passes, load0=None, load1=None):
         """Seconds of a backward Euler stage's start, and of each of `passes`

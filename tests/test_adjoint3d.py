@@ -18,8 +18,9 @@ but the memory held. The tangent-linear run (TangentLinearSolver3D's
 discrete method) pairs with the adjoint to 1e-8 along a direction in the
 log-viscosity and the loads together. On the CPU, the oracle's own
 restatement of the transposed sweep (oracle_step.cpp, AdjointRun) meets the
-pairing identity with the oracle's run (1e-12) and its gradient the
-differences of that run (1e-6)."""
+pairing identity with the oracle's run (1e-12), its tide kernels a run under
+tides (1e-12), its gradient the differences of that run (1e-6) and the
+oracle's tangent-linear run (1e-10)."""
 
 import numpy as np
 import pytest
@@ -283,3 +284,42 @@ def test_oracle_delta_gradient_matches_differences():
     predicted = float(adj["delta_gradient"] @ p)
     assert abs(predicted - richardson) < 1e-6 * abs(richardson), (predicted, richardson)
 
+
+
+@pytest.mark.parametrize("scheme", [2, 0])
+def test_oracle_tangent_pairs_with_the_oracle_adjoint(scheme):
+    """The oracle's tangent-linear run against its adjoint along a direction
+    in the log-viscosity over every node and in the loads (1e-10)."""
+    lmax = 6
+    make, times, loads, gU, gPhi = _oracle_case(lmax, seed=7)
+    adj = make().adjoint(times, scheme, loads, gU, gPhi)
+    o = make()
+    rng = np.random.default_rng(29)
+    pattern = O.synthesise_real(lmax, o.theta, o.nphi, real_coefficients(lmax, rng, 1)[0] / (lmax + 1))
+    radial = 1.0 + 0.5 * np.cos(5.0 * np.asarray(o.radius))
+    p = (radial[:, None] * np.asarray(pattern).ravel()[None, :]).ravel()
+    dL = 0.1 * np.max(np.abs(loads)) * real_coefficients(lmax, rng, len(times))
+    tl = o.tangent(times, scheme, loads, p, dL)
+    lhs = _objective(lmax, tl, gU, gPhi)
+    rhs = float(adj["delta_gradient"] @ p) + sum(pairing(lmax, adj["load_kernels"][k], dL[k])
+                                                 for k in range(len(times)))
+    assert abs(lhs - rhs) < 1e-10 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_oracle_tide_kernels_pair_with_a_tide_run():
+    """The oracle's tide kernels pair with tides (no degree-1 part) to its
+    run under those tides alone (1e-12)."""
+    lmax, scheme = 6, 2
+    make, times, loads, gU, gPhi = _oracle_case(lmax, seed=9)
+    adj = make().adjoint(times, scheme, loads, gU, gPhi)
+    tides = 1e-3 * real_coefficients(lmax, np.random.default_rng(33), len(times))
+    tides[:, 1:3] = 0.0
+    zero = np.zeros_like(tides[0])
+    o = make()
+    J = 0.0
+    for k in range(len(times)):
+        dt = 0.0 if k == 0 else times[k] - times[k - 1]
+        assert o.step(dt, scheme, zero, zero, tides[max(k - 1, 0)], tides[k]).converged
+        J += pairing(lmax, gU[k], o.surface(0)) + pairing(lmax, gPhi[k], o.surface(2))
+    paired = sum(pairing(lmax, adj["tide_kernels"][k], tides[k]) for k in range(len(times)))
+    assert abs(paired - J) < 1e-12 * abs(J), (paired, J)
