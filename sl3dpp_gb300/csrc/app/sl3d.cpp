@@ -1085,9 +1085,11 @@ int main(int argc, char** argv) {
   try {
     const Config c = ReadConfig(argv[2]);
     if (std::strcmp(argv[1], "check") == 0) {
-      std::printf("sl3d: config ok: run hash %016llx, lmax %d, %zu layers, %zu nodes%s\n",
+      std::printf("sl3d: config ok: run hash %016llx, lmax %d, %zu layers, %zu nodes%s%s\n",
                   static_cast<unsigned long long>(c.hash), c.options.lmax, c.layers.size(), c.timesYr.size(),
-                  c.ocean ? ", ocean" : "");
+                  c.ocean ? ", ocean" : "",
+                  c.kernels ? (", kernels of " + std::to_string(c.measurements.size()) + " measurement(s)").c_str()
+                            : "");
       return 0;
     }
     if (std::strcmp(argv[1], "kernel") == 0) {

@@ -211,6 +211,7 @@ def kernel_config(tmp_path, **kernels):
 def test_check_reads_a_kernel_config(sl3d, tmp_path):
     result = run(sl3d, "check", kernel_config(tmp_path), tmp_path)
     assert result.returncode == 0, result.stderr
+    assert "kernels of 2 measurement(s)" in result.stdout
     # the kernels block steers the run, it does not decide it
     assert run_hash(result) == run_hash(run(sl3d, "check", base(tmp_path, nodes=5), tmp_path))
 
